@@ -1,0 +1,259 @@
+/*
+ * ref_harness.cpp -- TEST INFRASTRUCTURE.  extern "C" entry points over the
+ * reference's own compiled sources (Makefile in this folder), used only to
+ * pin the oracle restatement (oracle/tg3_oracle.c) and to make the golden
+ * fixtures in tests/golden/.  Each entry point calls the reference routine
+ * named in its comment; the loops around them follow the reference caller
+ * cited beside them.  All arithmetic is the reference's, in double precision.
+ */
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include <boost/bind.hpp>
+
+#include "Logging.h"
+#include "Precision.h"
+#include "Functions.h"
+#include "TabFunction.h"
+#include "CTF.h"
+#include "Euler.h"
+#include "ImageFunctions.h"
+#include "Volume.h"
+#include "Projector.h"
+#include "Particle.h"
+
+INITIALIZE_EASYLOGGINGPP
+
+/* Defined in src/Optimiser.cpp (non-static, no header declaration). */
+RFLOAT logDataVSPrior_m_huabin(const Complex* dat, const Complex* pri,
+                               const RFLOAT* ctf, const RFLOAT* sigRcp,
+                               const int m);
+RFLOAT* logDataVSPrior_m_n_huabin(const Complex* dat, const Complex* pri,
+                                  const RFLOAT* ctf, const RFLOAT* sigRcp,
+                                  const int n, const int m, RFLOAT* result);
+
+/* ---- stand-ins for the external calls the compared routines make -------- */
+
+/* FFTW's allocator, used by ImageBase through TSFFTW_malloc. */
+extern "C" void* fftw_malloc(size_t n)
+{
+    void* p = NULL;
+    if (posix_memalign(&p, 64, n ? n : 64) != 0) return NULL;
+    return p;
+}
+extern "C" void fftw_free(void* p) { free(p); }
+
+/* Particle::resample / Particle::shuffle draw their randomness through these
+ * two GSL calls; the harness injects the permutation and u0 instead. */
+static std::vector<size_t> g_perm;
+static double g_u0 = 0;
+static double g_flat_b = -1;
+
+static char g_engine_dummy[64];
+gsl_rng* get_random_engine() { return (gsl_rng*)g_engine_dummy; }
+
+extern "C" void gsl_ran_shuffle(const gsl_rng*, void* base, size_t n, size_t size)
+{
+    if (size != sizeof(size_t) || n != g_perm.size()) abort();
+    memcpy(base, g_perm.data(), n * sizeof(size_t));
+}
+
+extern "C" double gsl_ran_flat(const gsl_rng*, const double a, const double b)
+{
+    g_flat_b = b;
+    return a + g_u0;
+}
+
+/* ---- entry points ------------------------------------------------------- */
+
+extern "C" {
+
+/* rotate3D(dmat33&, const dvec4&), src/Geometry/Euler.cpp:181-189 */
+void ref_rotmat(const double* quat, int n, double* mat)
+{
+    for (int r = 0; r < n; r++) {
+        dmat33 R;
+        dvec4 q(quat[4 * r], quat[4 * r + 1], quat[4 * r + 2], quat[4 * r + 3]);
+        rotate3D(R, q);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) mat[9 * r + 3 * i + j] = R(i, j);
+    }
+}
+
+/* Projector::project(Complex*, const dmat33&, iCol, iRow, nPxl, nThread),
+ * src/Projector.cpp:356-374, on a projectee volume set directly in Fourier
+ * space (vdim^3 padded grid, half-FT storage). */
+void ref_project(const double* vol, int vdim, const double* mat, int nR,
+                 const int* iCol, const int* iRow, int K, int pf, double* out)
+{
+    Projector proj;
+    proj.setMode(MODE_3D);
+    proj.setPf(pf);
+    proj.setInterp(LINEAR_INTERP);
+    Volume v(vdim, vdim, vdim, FT_SPACE);
+    memcpy(&v[0], vol, sizeof(Complex) * v.sizeFT());
+    const_cast<Volume&>(proj.projectee3D()).swap(v);
+    for (int r = 0; r < nR; r++) {
+        dmat33 R;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) R(i, j) = mat[9 * r + 3 * i + j];
+        proj.project((Complex*)(out + 2 * (size_t)r * K), R, iCol, iRow, K, 1);
+    }
+}
+
+/* translate(Complex*, nTransCol, nTransRow, nCol, nRow, iCol, iRow, nPxl,
+ * nThread), src/Image/ImageFunctions.cpp:233-252 */
+void ref_translate(const double* trans, int nT, int N, const int* iCol,
+                   const int* iRow, int K, double* out)
+{
+    for (int t = 0; t < nT; t++)
+        translate((Complex*)(out + 2 * (size_t)t * K), trans[2 * t],
+                  trans[2 * t + 1], N, N, iCol, iRow, K, 1);
+}
+
+/* translate(Complex* dst, const Complex* src, ...),
+ * src/Image/ImageFunctions.cpp:471-492 */
+void ref_translate_image(const double* src, double tx, double ty, int N,
+                         const int* iCol, const int* iRow, int K, double* dst)
+{
+    translate((Complex*)dst, (const Complex*)src, tx, ty, N, N, iCol, iRow, K, 1);
+}
+
+/* CTF(RFLOAT*, ...), src/CTF.cpp:98-145; attr in CTFAttr field order */
+void ref_ctf(const double* attr, double pixelSize, int N, const int* iCol,
+             const int* iRow, int K, double* out)
+{
+    CTF(out, pixelSize, attr[0], attr[1], attr[2], attr[3], attr[4], attr[5],
+        attr[6], N, N, iCol, iRow, K);
+}
+
+/* logDataVSPrior_m_huabin, src/Optimiser.cpp:8922-8946 */
+double ref_logdvp(const double* dat, const double* pri, const double* ctf,
+                  const double* sigRcp, int K)
+{
+    return logDataVSPrior_m_huabin((const Complex*)dat, (const Complex*)pri,
+                                   ctf, sigRcp, K);
+}
+
+/* logDataVSPrior_m_n_huabin (pixel-major, n images),
+ * src/Optimiser.cpp:9666-9707 */
+void ref_logdvp_mn(const double* dat, const double* pri, const double* ctf,
+                   const double* sigRcp, int nImg, int K, double* result)
+{
+    memset(result, 0, sizeof(double) * nImg);
+    logDataVSPrior_m_n_huabin((const Complex*)dat, (const Complex*)pri, ctf,
+                              sigRcp, nImg, K, result);
+}
+
+/* TabFunction::init(MKB_FT_R2(., a, alpha), 0, b, n), src/TabFunction.cpp:25-39
+ * with MKB_FT_R2, src/Functions/Functions.cpp:108-126; read back through
+ * TabFunction::operator() at the grid points. */
+void ref_mkb_table(double a, double alpha, double b, int n, double* tab)
+{
+    TabFunction tf;
+    tf.init(boost::bind(MKB_FT_R2, boost::placeholders::_1, a, alpha), 0, b, n);
+    double s = b / n;
+    for (int i = 0; i <= n; i++) tab[i] = tf(i * s);
+}
+
+/* Reconstructor::insertP's per-pixel loop, src/Reconstructor.cpp:807-862,
+ * calling the reference's Volume::addFT:
+ *   kernel 1: addFT(value, x, y, z, a, TabFunction), src/Image/Volume.cpp:399-431
+ *   kernel 0: addFT(value, x, y, z) (trilinear), src/Image/Volume.cpp:334-369
+ * F is complex [vdim][vdim][vdim/2+1]; T real of the same shape (stored in the
+ * real part of a complex Volume in the reference). */
+void ref_insert(double* F, double* T, int vdim, const double* img,
+                const double* ctf, const double* mat, double w,
+                const int* iColPad, const int* iRowPad, int K, int kernel,
+                double a, double alpha, double tabB, int tabN)
+{
+    Volume vF(vdim, vdim, vdim, FT_SPACE), vT(vdim, vdim, vdim, FT_SPACE);
+    const size_t n = vF.sizeFT();
+    for (size_t i = 0; i < n; i++) {
+        vF[i].dat[0] = F[2 * i];
+        vF[i].dat[1] = F[2 * i + 1];
+        vT[i].dat[0] = T[i];
+        vT[i].dat[1] = 0;
+    }
+    TabFunction tf;
+    tf.init(boost::bind(MKB_FT_R2, boost::placeholders::_1, a, alpha), 0, tabB, tabN);
+    const double pfa = sqrt(tabB);
+    for (int i = 0; i < K; i++) {
+        double oldCor[3];
+        double c = iColPad[i], r = iRowPad[i];
+        /* rotation as applied by insertP: oldCor = R (iCol, iRow, 0) */
+        oldCor[0] = mat[0] * c + mat[1] * r;
+        oldCor[1] = mat[3] * c + mat[4] * r;
+        oldCor[2] = mat[6] * c + mat[7] * r;
+        Complex src;
+        src.dat[0] = img[2 * i];
+        src.dat[1] = img[2 * i + 1];
+        Complex val = src * ctf[i] * w;
+        double tval = ctf[i] * ctf[i] * w;
+        if (kernel == 1) {
+            vF.addFT(val, oldCor[0], oldCor[1], oldCor[2], pfa, tf);
+            vT.addFT(tval, oldCor[0], oldCor[1], oldCor[2], pfa, tf);
+        } else {
+            vF.addFT(val, oldCor[0], oldCor[1], oldCor[2]);
+            vT.addFT(tval, oldCor[0], oldCor[1], oldCor[2]);
+        }
+    }
+    for (size_t i = 0; i < n; i++) {
+        F[2 * i] = vF[i].dat[0];
+        F[2 * i + 1] = vF[i].dat[1];
+        T[i] = vT[i].dat[0];
+    }
+}
+
+/* Particle rotation-axis narrowing + resampling, as Optimiser::updateSP runs
+ * them (src/Optimiser.cpp:1357-1396): setUR, [setPeakFactor(PAR_R),]
+ * keepHalfHeightPeak(PAR_R), resample(nOut, PAR_R)
+ * (src/Particle.cpp:1864-1973, 1275-1463).  The shuffle permutation and u0
+ * are injected.  Row i of the particle's quaternion matrix carries i in its
+ * first component so that the source of every resampled row can be read
+ * back.  mode: 0 = no narrowing, 1 = setPeakFactor + keepHalfHeightPeak.
+ * Returns the b bound that resample passed to gsl_ran_flat. */
+double ref_resample(int n, const double* u, const double* w, const size_t* perm,
+                    double u0, int nOut, int mode, int* src, double* wOut)
+{
+    Particle par;
+    par.setMode(MODE_3D);
+    par.setNR(n);
+    dmat4 r = dmat4::Zero(n, 4);
+    dvec wR(n), uR(n);
+    for (int i = 0; i < n; i++) {
+        r(i, 0) = i;
+        wR(i) = w[i];
+        uR(i) = u[i];
+    }
+    par.setR(r);
+    par.setWR(wR);
+    par.setUR(uR);
+    if (mode == 1) {
+        par.setPeakFactor(PAR_R);
+        par.keepHalfHeightPeak(PAR_R);
+    }
+    g_perm.assign(perm, perm + n);
+    g_u0 = u0;
+    par.resample(nOut, PAR_R);
+    dmat4 ro = par.r();
+    dvec wo = par.wR();
+    for (int j = 0; j < nOut; j++) {
+        src[j] = (int)ro(j, 0);
+        wOut[j] = wo(j);
+    }
+    return g_flat_b;
+}
+
+/* d_index_sort_descend (gsl_sort_largest_index),
+ * src/Functions/Functions.cpp:72-79 */
+void ref_sort_descend(const double* v, int n, size_t* idx)
+{
+    dvec d(n);
+    for (int i = 0; i < n; i++) d(i) = v[i];
+    uvec o = d_index_sort_descend(d);
+    for (int i = 0; i < n; i++) idx[i] = o(i);
+}
+
+} /* extern "C" */

@@ -1,0 +1,128 @@
+"""Write tests/golden/ref_golden.npz: inputs and outputs of the reference's
+own compiled routines (oracle/_ref/libthunder_ref.so, built by
+oracle/ref/Makefile from the THUNDER sources) on small seeded cases.
+
+Run in a checkout that has the THUNDER tree:
+    python tests/golden/make_golden.py
+The fixture pins the oracle (tests/test_oracle_golden.py) on machines that
+do not have the reference sources."""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "thunder-refactor-expectation_gb300"))
+
+from oracle import oracle as O  # noqa: E402
+from tg3 import synth  # noqa: E402
+
+
+def main():
+    R = O.ref()
+    if R is None:
+        raise SystemExit("reference cross-check library unavailable")
+    rng = np.random.default_rng(20261203)
+    g = {}
+    box, pf = 16, 2
+    iCol, iRow, iSig, iPxl = synth.pixel_index(box, 6, 1)
+    K = len(iCol)
+    g["iCol"], g["iRow"] = iCol, iRow
+    g["box"], g["pf"] = box, pf
+
+    # rotations
+    q = synth.haar_quaternions(rng, 8)
+    q[0] = (1, 0, 0, 0)
+    mat = np.zeros((8, 9))
+    R.ref_rotmat(q, 8, mat)
+    g["rot_quat"], g["rot_mat"] = q, mat
+
+    # projection: a blob map on the padded grid, rotations incl. identity
+    bm = synth.blob_map(rng, 6, (2.0, 4.0), 1.5, 4.0)
+    vol = np.ascontiguousarray(synth.padded_volume(bm, box, pf).numpy())
+    proj = np.zeros((8, K), np.complex128)
+    R.ref_project(vol, vol.shape[0], mat, 8, iCol, iRow, K, pf, proj)
+    g["vol"], g["proj"] = vol, proj
+
+    # phase shifts and an image shift
+    t = np.array([[0.0, 0.0], [1.0, -2.0], [-2.5, 0.75], [3.0, 3.0]])
+    tra = np.zeros((4, K), np.complex128)
+    R.ref_translate(t, 4, box, iCol, iRow, K, tra)
+    g["trans"], g["tra"] = t, tra
+
+    # CTF
+    attr = synth.ctf_attrs(rng, 3)
+    ctf = np.zeros((3, K))
+    for i in range(3):
+        row = np.zeros(K)
+        R.ref_ctf(np.ascontiguousarray(attr[i]), 1.5, box, iCol, iRow, K, row)
+        ctf[i] = row
+    g["ctf_attr"], g["ctf"] = attr, ctf
+
+    # likelihood: image-major single and pixel-major batch
+    dat = rng.standard_normal((4, K)) + 1j * rng.standard_normal((4, K))
+    sig = -0.5 / (1 + rng.random((4, K)))
+    cc = np.concatenate([ctf, ctf[:1]], 0)
+    pri = proj[1] * tra[1]
+    g["dvp_dat"], g["dvp_sig"], g["dvp_ctf"], g["dvp_pri"] = dat, sig, cc, pri
+    g["dvp_one"] = np.array([R.ref_logdvp(np.ascontiguousarray(dat[0]), pri,
+                                          np.ascontiguousarray(cc[0]),
+                                          np.ascontiguousarray(sig[0]), K)])
+    mn = np.zeros(4)
+    R.ref_logdvp_mn(np.ascontiguousarray(dat.T), pri, np.ascontiguousarray(cc.T),
+                    np.ascontiguousarray(sig.T), 4, K, mn)
+    g["dvp_mn"] = mn
+
+    # MKB table (a = 1.9, alpha = 15, b = (pf a)^2, n = 1e5): keep a sample
+    tab = np.zeros(100001)
+    R.ref_mkb_table(1.9, 15.0, (2 * 1.9) ** 2, 100000, tab)
+    sel = np.unique(np.concatenate([np.arange(0, 25100, 97), [24999, 25000, 25001, 100000]]))
+    g["mkb_idx"], g["mkb_val"] = sel, tab[sel]
+
+    # insertion, both kernels, two slices each
+    img = rng.standard_normal((2, K)) + 1j * rng.standard_normal((2, K))
+    g["ins_img"], g["ins_w"] = img, np.array([0.3, 1.7])
+    for kern in (0, 1):
+        F = np.zeros(vol.shape, np.complex128)
+        T = np.zeros(vol.shape)
+        for s in range(2):
+            R.ref_insert(F, T, vol.shape[0], np.ascontiguousarray(img[s]),
+                         np.ascontiguousarray(ctf[s]), np.ascontiguousarray(mat[s + 1]),
+                         float(g["ins_w"][s]), (iCol * pf).astype(np.int32),
+                         (iRow * pf).astype(np.int32), K, kern, 1.9, 15.0,
+                         (2 * 1.9) ** 2, 100000)
+        nz = np.nonzero((np.abs(F) + np.abs(T)).ravel())[0]
+        g[f"ins{kern}_idx"], g[f"ins{kern}_F"], g[f"ins{kern}_T"] = nz, F.ravel()[nz], T.ravel()[nz]
+
+    # resampling: (n, nOut, narrowing)
+    for c, (n, n_out, mode) in enumerate([(50, 40, 0), (100, 100, 1), (1000, 1000, 1)]):
+        u = np.exp(3 * rng.standard_normal(n))
+        if c == 1:
+            u[rng.integers(0, n, 10)] = 0.0
+        w = rng.random(n)
+        w /= w.sum()
+        perm = rng.permutation(n)
+        u0 = rng.random() / n_out
+        src = np.zeros(n_out, np.int32)
+        wo = np.zeros(n_out)
+        R.ref_resample(n, u, w, perm.astype(np.uint64), u0, n_out, mode, src, wo)
+        g[f"rs{c}_u"], g[f"rs{c}_w"], g[f"rs{c}_perm"] = u, w, perm.astype(np.int32)
+        g[f"rs{c}_u0"], g[f"rs{c}_mode"] = np.array([u0]), np.array([mode])
+        g[f"rs{c}_src"], g[f"rs{c}_wout"] = src, wo
+
+    # descending index sort with ties
+    v = rng.integers(0, 6, 40).astype(np.float64)
+    o = np.zeros(40, np.uint64)
+    R.ref_sort_descend(v, 40, o)
+    g["sort_v"], g["sort_idx"] = v, o.astype(np.int64)
+
+    out = Path(__file__).resolve().parent / "ref_golden.npz"
+    np.savez_compressed(out, **g)
+    print(f"wrote {out} ({out.stat().st_size} bytes)")
+
+
+if __name__ == "__main__":
+    main()

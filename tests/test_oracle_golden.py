@@ -1,0 +1,93 @@
+"""The oracle restatement against the reference's own outputs, stored in
+tests/golden/ref_golden.npz by tests/golden/make_golden.py (which ran the
+reference's compiled sources).  CPU only."""
+import numpy as np
+
+from oracle import oracle as O
+
+
+def test_rotmat(golden):
+    m = O.rotmat(golden["rot_quat"]).reshape(-1, 9)
+    assert np.array_equal(m, golden["rot_mat"])
+
+
+def test_project_bit_exact(golden):
+    m = golden["rot_mat"]
+    P = O.project(golden["vol"], m, golden["iCol"], golden["iRow"], int(golden["pf"]))
+    assert np.array_equal(P, golden["proj"])
+
+
+def test_translate(golden):
+    S = O.translate(golden["trans"], int(golden["box"]), golden["iCol"], golden["iRow"])
+    np.testing.assert_allclose(S, golden["tra"], rtol=0, atol=1e-13)
+
+
+def test_ctf(golden):
+    c = O.ctf(golden["ctf_attr"], 1.5, int(golden["box"]), golden["iCol"], golden["iRow"])
+    np.testing.assert_allclose(c, golden["ctf"], rtol=0, atol=1e-12)
+
+
+def test_logdvp(golden):
+    d, s, c, p = golden["dvp_dat"], golden["dvp_sig"], golden["dvp_ctf"], golden["dvp_pri"]
+    assert O.logdvp(d[0], p, c[0], s[0]) == golden["dvp_one"][0]
+    mn = np.array([O.logdvp(d[i], p, c[i], s[i]) for i in range(4)])
+    np.testing.assert_allclose(mn, golden["dvp_mn"], rtol=1e-14)
+
+
+def test_mkb_table(golden):
+    tab = O.mkb_table(1.9, 15.0, (2 * 1.9) ** 2, 100000)
+    idx = golden["mkb_idx"]
+    np.testing.assert_allclose(tab[idx], golden["mkb_val"], rtol=1e-13, atol=1e-300)
+    # support ends at r^2 = a^2 = 3.61 (index 25000 of 1e5 over 14.44)
+    assert tab[25000] > 0 and tab[25001] == 0
+
+
+def _insert(golden, kern):
+    box, pf = int(golden["box"]), int(golden["pf"])
+    vol = golden["vol"]
+    F = np.zeros(vol.shape, np.complex128)
+    T = np.zeros(vol.shape)
+    tab = O.mkb_table(1.9, 15.0, (2 * 1.9) ** 2, 100000)
+    for s in range(2):
+        O.insert(F, T, golden["ins_img"][s], golden["ctf"][s],
+                 golden["rot_mat"][s + 1], golden["ins_w"][s],
+                 golden["iCol"] * pf, golden["iRow"] * pf, kern, 2 * 1.9, tab,
+                 (2 * 1.9) ** 2)
+    return F.ravel(), T.ravel()
+
+
+def test_insert_trilinear_bit_exact(golden):
+    F, T = _insert(golden, 0)
+    idx = golden["ins0_idx"]
+    assert np.count_nonzero(np.abs(F) + np.abs(T)) == len(idx)
+    assert np.array_equal(F[idx], golden["ins0_F"])
+    assert np.array_equal(T[idx], golden["ins0_T"])
+
+
+def test_insert_mkb(golden):
+    F, T = _insert(golden, 1)
+    idx = golden["ins1_idx"]
+    assert np.count_nonzero(np.abs(F) + np.abs(T)) == len(idx)
+    np.testing.assert_allclose(F[idx], golden["ins1_F"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(T[idx], golden["ins1_T"], rtol=1e-12, atol=1e-14)
+
+
+def test_resample_bit_exact(golden):
+    for c in range(3):
+        u, w, perm = golden[f"rs{c}_u"], golden[f"rs{c}_w"], golden[f"rs{c}_perm"]
+        mode = int(golden[f"rs{c}_mode"][0])
+        pfac = O.peak_factor_r(u) if mode else 0.0
+        n_out = len(golden[f"rs{c}_src"])
+        src, wout, _ = O.resample(u, w, perm, golden[f"rs{c}_u0"][0], pfac, n_out)
+        assert np.array_equal(src, golden[f"rs{c}_src"]), c
+        assert np.array_equal(wout, golden[f"rs{c}_wout"]), c
+
+
+def test_descend_order_ties(golden):
+    assert np.array_equal(O.descend_order(golden["sort_v"]), golden["sort_idx"])
+
+
+def test_bessel_i0_series():
+    scipy = __import__("pytest").importorskip("scipy.special")
+    for x in (0.0, 0.5, 3.0, 7.5, 15.0):
+        np.testing.assert_allclose(O.bessel_i0(x), scipy.i0(x), rtol=1e-14)

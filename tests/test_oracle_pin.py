@@ -1,0 +1,71 @@
+"""Live pin: the oracle restatement against the reference's own compiled
+sources (oracle/_ref, built from the THUNDER tree by oracle/ref/Makefile) on
+fresh seeded cases.  Skipped where the THUNDER tree is absent; the golden
+fixtures cover those machines."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tg3 import synth
+
+R = O.ref()
+pytestmark = pytest.mark.skipif(R is None, reason="reference sources unavailable")
+
+
+@pytest.fixture(scope="module")
+def case():
+    rng = np.random.default_rng(7)
+    box, pf = 24, 2
+    iCol, iRow, _, _ = synth.pixel_index(box, 10, 1)
+    bm = synth.blob_map(rng, 12, (2.0, 4.0), 1.5, 7.0)
+    vol = np.ascontiguousarray(synth.padded_volume(bm, box, pf).numpy())
+    return dict(rng=rng, box=box, pf=pf, iCol=iCol, iRow=iRow, vol=vol, K=len(iCol))
+
+
+def test_project(case):
+    rng = case["rng"]
+    q = synth.haar_quaternions(rng, 64)
+    m = np.zeros((64, 9))
+    R.ref_rotmat(q, 64, m)
+    P2 = np.zeros((64, case["K"]), np.complex128)
+    R.ref_project(case["vol"], case["vol"].shape[0], m, 64, case["iCol"], case["iRow"],
+                  case["K"], case["pf"], P2)
+    P1 = O.project(case["vol"], O.rotmat(q), case["iCol"], case["iRow"], case["pf"])
+    assert np.array_equal(P1, P2)
+
+
+def test_insert_mkb(case):
+    rng = case["rng"]
+    K, pf = case["K"], case["pf"]
+    q = synth.haar_quaternions(rng, 3)
+    tab = O.mkb_table(1.9, 15.0, (pf * 1.9) ** 2, 100000)
+    F1 = np.zeros(case["vol"].shape, np.complex128)
+    T1 = np.zeros(case["vol"].shape)
+    F2, T2 = F1.copy(), T1.copy()
+    m = O.rotmat(q)
+    for s in range(3):
+        img = rng.standard_normal(K) + 1j * rng.standard_normal(K)
+        c = rng.standard_normal(K)
+        O.insert(F1, T1, img, c, m[s], 0.5, case["iCol"] * pf, case["iRow"] * pf, 1,
+                 pf * 1.9, tab, (pf * 1.9) ** 2)
+        R.ref_insert(F2, T2, F2.shape[0], img, c, np.ascontiguousarray(m[s].ravel()), 0.5,
+                     (case["iCol"] * pf).astype(np.int32), (case["iRow"] * pf).astype(np.int32),
+                     K, 1, 1.9, 15.0, (pf * 1.9) ** 2, 100000)
+    np.testing.assert_allclose(F1, F2, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(T1, T2, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("n,n_out,mode", [(7, 7, 0), (300, 250, 1), (2000, 2000, 1)])
+def test_resample(n, n_out, mode):
+    rng = np.random.default_rng(n)
+    u = np.exp(2 * rng.standard_normal(n))
+    w = rng.random(n)
+    perm = rng.permutation(n)
+    u0 = rng.random() / n_out
+    src2 = np.zeros(n_out, np.int32)
+    w2 = np.zeros(n_out)
+    R.ref_resample(n, u, w, perm.astype(np.uint64), u0, n_out, mode, src2, w2)
+    pfac = O.peak_factor_r(u) if mode else 0.0
+    src1, w1, _ = O.resample(u, w, perm.astype(np.int32), u0, pfac, n_out)
+    assert np.array_equal(src1, src2)
+    assert np.array_equal(w1, w2)

@@ -1,0 +1,406 @@
+"""Seeded synthetic E-step workloads (host-side input generation).
+
+The reference refines real cryo-EM particle stacks; here every input is made
+from a fixed seed so that the CUDA path, the oracle and the benchmark all see
+the same numbers:
+
+* a reference map made of isotropic Gaussian blobs, generated directly in
+  Fourier space on the padded grid.  The transform of a blob of amplitude A,
+  width s (pixels) and centre c is A (2 pi s^2)^(3/2) exp(-2 pi^2 s^2 |f|^2)
+  exp(-2 pi i f.c), sampled at f = (x, y, z) / (pf N) cycles per pixel.  This
+  stands in for Projector::setProjectee (padding, gridding correction and FFT
+  of a real-space map, src/Projector.cpp:123-200), which runs once per
+  iteration and is outside the hot path;
+* particle images in the selected Fourier pixels: CTF x phase shift x the
+  exact central slice of the same analytic transform at the true pose, plus
+  white complex Gaussian noise at a stated SNR (signal power over noise power
+  over the in-cutoff pixels);
+* pixel selection restating Optimiser::allocPreCalIdx
+  (src/Optimiser.cpp:7942-7992);
+* pose hypotheses: HEALPix (ring scheme, Gorski et al. 2005) directions x
+  in-plane angles for the global scan, von Mises-Fisher samples on the
+  quaternion sphere (Wood 1994) for local rounds, Gaussian translations.
+
+Volumes are returned as complex tensors of shape (vdim, vdim, vdim//2 + 1)
+indexed [z, y, x] -- the half-FT storage of Volume::iFTHalf
+(include/Image/Volume.h:566-573).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+
+# --------------------------------------------------------------------------
+# pixel selection
+# --------------------------------------------------------------------------
+def pixel_index(size: int, rU: float, rL: float):
+    """Half-plane Fourier pixels with rL <= rint(|k|) < rU and
+    rL^2 <= |k|^2 < rU^2, j-outer / i-inner, skipping i == 0 and j < 0
+    (Optimiser::allocPreCalIdx, src/Optimiser.cpp:7942-7992).
+
+    Returns int32 arrays iCol, iRow, iSig, iPxl."""
+    r = rU + 1
+    j = np.arange(int(-r), math.ceil(r) + 1)
+    j = j[j < r]
+    i = np.arange(0, int(math.floor(r)) + 1)
+    jj, ii = np.meshgrid(j, i, indexing="ij")
+    jj = jj.ravel()
+    ii = ii.ravel()
+    keep = ~((ii == 0) & (jj < 0))
+    u = ii.astype(np.float64) ** 2 + jj.astype(np.float64) ** 2
+    keep &= (u < rU * rU) & (u >= rL * rL)
+    v = np.rint(np.hypot(ii, jj)).astype(np.int64)
+    keep &= (v < rU) & (v >= rL)
+    ii, jj, v = ii[keep], jj[keep], v[keep]
+    iPxl = np.where(jj >= 0, jj, jj + size) * (size // 2 + 1) + ii
+    return (ii.astype(np.int32), jj.astype(np.int32), v.astype(np.int32),
+            iPxl.astype(np.int32))
+
+
+# --------------------------------------------------------------------------
+# rotations
+# --------------------------------------------------------------------------
+def quat_to_mat(q: np.ndarray) -> np.ndarray:
+    """Row-major rotation matrices of unit quaternions (w, x, y, z):
+    R = I + 2 w A + 2 A^2 (rotate3D, src/Geometry/Euler.cpp:181-189)."""
+    q = np.asarray(q, dtype=np.float64).reshape(-1, 4)
+    w, x, y, z = q.T
+    A = np.zeros((len(q), 3, 3))
+    A[:, 0, 1], A[:, 0, 2] = -z, y
+    A[:, 1, 0], A[:, 1, 2] = z, -x
+    A[:, 2, 0], A[:, 2, 1] = -y, x
+    eye = np.broadcast_to(np.eye(3), A.shape)
+    return eye + 2 * w[:, None, None] * A + 2 * A @ A
+
+
+def quat_mul(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Hamilton product of quaternion arrays (..., 4)."""
+    aw, ax, ay, az = np.moveaxis(a, -1, 0)
+    bw, bx, by, bz = np.moveaxis(b, -1, 0)
+    return np.stack([aw * bw - ax * bx - ay * by - az * bz,
+                     aw * bx + ax * bw + ay * bz - az * by,
+                     aw * by - ax * bz + ay * bw + az * bx,
+                     aw * bz + ax * by - ay * bx + az * bw], axis=-1)
+
+
+def haar_quaternions(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Haar-uniform rotations: normalised 4-D Gaussian vectors, w >= 0."""
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    q[q[:, 0] < 0] *= -1
+    return q
+
+
+def euler_zyz_to_quat(phi, theta, psi) -> np.ndarray:
+    """Quaternion of R = Rz(phi) Ry(theta) Rz(psi)."""
+    def qz(a):
+        return np.stack([np.cos(a / 2), 0 * a, 0 * a, np.sin(a / 2)], -1)
+
+    def qy(a):
+        return np.stack([np.cos(a / 2), 0 * a, np.sin(a / 2), 0 * a], -1)
+    q = quat_mul(quat_mul(qz(phi), qy(theta)), qz(psi))
+    q[q[..., 0] < 0] *= -1
+    return q
+
+
+def healpix_ring_centres(nside: int):
+    """(theta, phi) of the 12 nside^2 HEALPix pixel centres, ring scheme
+    (Gorski et al. 2005, ApJ 622:759, eqs. 4-9)."""
+    npix = 12 * nside * nside
+    ncap = 2 * nside * (nside - 1)
+    out = np.zeros((npix, 2))
+    for p in range(npix):
+        if p < ncap:                                   # north polar cap
+            i = int((1 + math.isqrt(1 + 2 * p)) // 2)
+            while 2 * i * (i + 1) <= p:
+                i += 1
+            while 2 * i * (i - 1) > p:
+                i -= 1
+            j = p - 2 * i * (i - 1) + 1
+            z = 1 - i * i / (3.0 * nside * nside)
+            ph = (j - 0.5) * math.pi / (2 * i)
+        elif p < npix - ncap:                          # equatorial belt
+            pp = p - ncap
+            i = pp // (4 * nside) + nside
+            j = pp % (4 * nside) + 1
+            s = (i - nside + 1) % 2
+            z = (2 * nside - i) * 2.0 / (3 * nside)
+            ph = (j - s / 2.0) * math.pi / (2 * nside)
+        else:                                          # south polar cap
+            pp = npix - p - 1
+            i = int((1 + math.isqrt(1 + 2 * pp)) // 2)
+            while 2 * i * (i + 1) <= pp:
+                i += 1
+            while 2 * i * (i - 1) > pp:
+                i -= 1
+            j = 4 * i - (pp - 2 * i * (i - 1))
+            z = -(1 - i * i / (3.0 * nside * nside))
+            ph = (j - 0.5) * math.pi / (2 * i)
+        out[p] = (math.acos(max(-1.0, min(1.0, z))), ph)
+    return out
+
+
+def global_rotations(nside: int = 4, n_psi: int = 36) -> np.ndarray:
+    """HEALPix directions x uniform in-plane angles as quaternions
+    (192 x 36 = 6,912 for nside 4)."""
+    tp = healpix_ring_centres(nside)
+    psi = np.arange(n_psi) * (2 * math.pi / n_psi)
+    th = np.repeat(tp[:, 0], n_psi)
+    ph = np.repeat(tp[:, 1], n_psi)
+    ps = np.tile(psi, len(tp))
+    return euler_zyz_to_quat(ph, th, ps)
+
+
+def vmf_quaternions(rng: np.random.Generator, mean: np.ndarray, kappa: float,
+                    n: int) -> np.ndarray:
+    """n samples of the von Mises-Fisher distribution on S^3 with mean
+    direction `mean` and concentration kappa (Wood 1994, Commun. Stat.
+    Simul. Comput. 23:157)."""
+    p = 4
+    b = (-2 * kappa + math.sqrt(4 * kappa * kappa + (p - 1) ** 2)) / (p - 1)
+    x0 = (1 - b) / (1 + b)
+    c = kappa * x0 + (p - 1) * math.log(1 - x0 * x0)
+    w = np.empty(n)
+    filled = 0
+    while filled < n:
+        m = (n - filled) * 2 + 8
+        z = rng.beta((p - 1) / 2, (p - 1) / 2, m)
+        u = rng.random(m)
+        ww = (1 - (1 + b) * z) / (1 - (1 - b) * z)
+        ok = kappa * ww + (p - 1) * np.log(1 - x0 * ww) - c >= np.log(u)
+        take = ww[ok][: n - filled]
+        w[filled:filled + len(take)] = take
+        filled += len(take)
+    v = rng.standard_normal((n, p - 1))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    samp = np.concatenate([w[:, None], np.sqrt(1 - w * w)[:, None] * v], 1)
+    # rotate e0 = (1, 0, 0, 0) onto the mean: left-multiply by the mean
+    out = quat_mul(np.broadcast_to(mean, samp.shape), samp)
+    out /= np.linalg.norm(out, axis=1, keepdims=True)
+    return out
+
+
+# --------------------------------------------------------------------------
+# maps
+# --------------------------------------------------------------------------
+@dataclass
+class BlobMap:
+    amp: np.ndarray       # (nb,)
+    sigma: np.ndarray     # (nb,) pixels
+    centre: np.ndarray    # (nb, 3) pixels, relative to the box centre
+
+
+def blob_map(rng: np.random.Generator, n_blobs: int, sigma_a: tuple,
+             pixel_size: float, radius_px: float) -> BlobMap:
+    """n_blobs isotropic Gaussians: widths U(sigma_a) in Angstrom, centres
+    uniform in a ball of radius_px pixels, amplitudes U(0.5, 1)."""
+    d = rng.standard_normal((n_blobs, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rad = radius_px * rng.random(n_blobs) ** (1.0 / 3.0)
+    return BlobMap(amp=rng.uniform(0.5, 1.0, n_blobs),
+                   sigma=rng.uniform(*sigma_a, n_blobs) / pixel_size,
+                   centre=d * rad[:, None])
+
+
+def blob_ft(bm: BlobMap, f: torch.Tensor) -> torch.Tensor:
+    """Analytic Fourier transform of the blob map at frequencies f (..., 3)
+    in cycles per pixel."""
+    dt = f.dtype
+    amp = torch.as_tensor(bm.amp, dtype=dt, device=f.device)
+    s2 = torch.as_tensor(bm.sigma ** 2, dtype=dt, device=f.device)
+    c = torch.as_tensor(bm.centre, dtype=dt, device=f.device)
+    f2 = (f * f).sum(-1, keepdim=True)                       # (..., 1)
+    env = amp * (2 * math.pi * s2) ** 1.5 * torch.exp(-2 * math.pi ** 2 * s2 * f2)
+    ph = -2 * math.pi * (f @ c.T)                             # (..., nb)
+    re = (env * torch.cos(ph)).sum(-1)
+    im = (env * torch.sin(ph)).sum(-1)
+    return torch.complex(re, im)
+
+
+def padded_volume(bm: BlobMap, box: int, pf: int, device="cpu",
+                  dtype=torch.float64, chunk: int = 1 << 21) -> torch.Tensor:
+    """The map's transform on the padded half-FT grid: complex tensor
+    (vdim, vdim, vdim//2 + 1), vdim = pf * box, indexed [z, y, x]."""
+    vdim = pf * box
+    nx = vdim // 2 + 1
+    cdt = torch.complex128 if dtype == torch.float64 else torch.complex64
+    out = torch.empty((vdim, vdim, nx), dtype=cdt, device=device)
+    flat = out.view(-1)
+    n = flat.numel()
+    idx_all = torch.arange(n, device=device)
+    for s in range(0, n, chunk):
+        idx = idx_all[s:s + chunk]
+        x = idx % nx
+        y = (idx // nx) % vdim
+        z = idx // (nx * vdim)
+        y = torch.where(y < vdim // 2, y, y - vdim)
+        z = torch.where(z < vdim // 2, z, z - vdim)
+        f = torch.stack([x, y, z], -1).to(dtype) / vdim
+        flat[s:s + chunk] = blob_ft(bm, f)
+    return out
+
+
+# --------------------------------------------------------------------------
+# CTF
+# --------------------------------------------------------------------------
+CTF_FIELDS = ("voltage", "defocusU", "defocusV", "defocusTheta", "Cs",
+              "amplitudeContrast", "phaseShift")
+
+
+def ctf_attrs(rng: np.random.Generator, n: int, voltage_kv=300.0, cs_mm=2.7,
+              amp=0.1, defocus_um=(1.0, 3.0)) -> np.ndarray:
+    """(n, 7) float64 rows in CTFAttr field order (include/Database.h:108-122),
+    in the units CTF() expects: volts, Angstrom, radians."""
+    a = np.zeros((n, 7))
+    a[:, 0] = voltage_kv * 1e3
+    a[:, 1] = rng.uniform(*defocus_um, n) * 1e4
+    a[:, 2] = rng.uniform(*defocus_um, n) * 1e4
+    a[:, 3] = rng.uniform(0, math.pi, n)
+    a[:, 4] = cs_mm * 1e7
+    a[:, 5] = amp
+    a[:, 6] = 0.0
+    return a
+
+
+def ctf_values(attr: np.ndarray, pixel_size: float, N: int, iCol, iRow):
+    """CTF at the selected pixels for every row of attr (vectorised form of
+    CTF(RFLOAT*, ...), src/CTF.cpp:98-145); (n, K) float64."""
+    attr = np.atleast_2d(attr)
+    V, dU, dV, th, Cs, A, ps = [attr[:, k:k + 1] for k in range(7)]
+    lam = 12.2643247 / np.sqrt(V * (1 + V * 0.978466e-6))
+    K1 = math.pi * lam
+    K2 = (math.pi / 2) * Cs * lam ** 3
+    u = np.hypot(iCol / (pixel_size * N), iRow / (pixel_size * N))[None, :]
+    ang = np.arctan2(iRow, iCol)[None, :] - th
+    dfc = -(dU + dV + (dU - dV) * np.cos(2 * ang)) / 2
+    ki = K1 * dfc * u ** 2 + K2 * u ** 4 - ps
+    return -np.sqrt(1 - A * A) * np.sin(ki) + A * np.cos(ki)
+
+
+def phase_shift(trans: np.ndarray, N: int, iCol, iRow) -> np.ndarray:
+    """exp(-2 pi i (iCol tx + iRow ty) / N) for each translation: (nT, K)."""
+    trans = np.atleast_2d(trans)
+    ph = 2 * math.pi * (np.outer(trans[:, 0] / N, iCol) + np.outer(trans[:, 1] / N, iRow))
+    return np.exp(-1j * ph)
+
+
+# --------------------------------------------------------------------------
+# a particle stack
+# --------------------------------------------------------------------------
+@dataclass
+class Stack:
+    box: int
+    pixel_size: float
+    pf: int
+    rU: float
+    rL: float
+    iCol: np.ndarray
+    iRow: np.ndarray
+    iSig: np.ndarray
+    quat_true: np.ndarray       # (n, 4)
+    trans_true: np.ndarray      # (n, 2) pixels
+    ctf_attr: np.ndarray        # (n, 7)
+    ctf: np.ndarray             # (n, K) float64
+    dat: np.ndarray             # (n, K) complex128
+    sigRcp: np.ndarray          # (n, K) float64, -1 / (2 s^2)
+    noise_s2: float
+    maps: list = field(default_factory=list)
+    cls_true: np.ndarray = None
+
+    @property
+    def K(self):
+        return len(self.iCol)
+
+
+def make_stack(seed: int, maps, box: int, pixel_size: float, pf: int,
+               rU: float, rL: float, n: int, shift_range: float, snr: float,
+               device="cpu") -> Stack:
+    """n particles from `maps` (assigned round-robin, 1:1:...) at Haar-uniform
+    poses and U(-shift_range, shift_range) shifts, with white noise at `snr`."""
+    rng = np.random.default_rng(seed)
+    iCol, iRow, iSig, _ = pixel_index(box, rU, rL)
+    K = len(iCol)
+    q = haar_quaternions(rng, n)
+    t = rng.uniform(-shift_range, shift_range, (n, 2))
+    attr = ctf_attrs(rng, n)
+    ctf = ctf_values(attr, pixel_size, box, iCol, iRow)
+    cls = np.arange(n) % len(maps)
+    R = quat_to_mat(q)
+    k2 = np.stack([iCol, iRow, np.zeros(K)], 0).astype(np.float64) / box  # (3, K)
+    sig = np.zeros((n, K), dtype=np.complex128)
+    for c, bm in enumerate(maps):
+        sel = np.nonzero(cls == c)[0]
+        for s in range(0, len(sel), 4096):
+            ids = sel[s:s + 4096]
+            f = torch.as_tensor(np.einsum("nij,jk->nki", R[ids], k2), device=device)
+            sig[ids] = blob_ft(bm, f).cpu().numpy()
+    sig = sig * ctf * np.exp(-2j * math.pi * (np.outer(t[:, 0] / box, iCol)
+                                              + np.outer(t[:, 1] / box, iRow)))
+    p_sig = float(np.mean(np.abs(sig) ** 2))
+    s2 = p_sig / snr / 2.0
+    noise = rng.standard_normal((n, K)) + 1j * rng.standard_normal((n, K))
+    dat = sig + math.sqrt(s2) * noise
+    sigRcp = np.full((n, K), -1.0 / (2.0 * s2))
+    return Stack(box=box, pixel_size=pixel_size, pf=pf, rU=rU, rL=rL,
+                 iCol=iCol, iRow=iRow, iSig=iSig, quat_true=q, trans_true=t,
+                 ctf_attr=attr, ctf=ctf, dat=dat, sigRcp=sigRcp, noise_s2=s2,
+                 maps=list(maps), cls_true=cls)
+
+
+# --------------------------------------------------------------------------
+# named workloads
+# --------------------------------------------------------------------------
+def global_translations(half: int = 3, step: float = 1.0) -> np.ndarray:
+    """(2 half + 1)^2 grid of shifts, `step` pixels apart (7 x 7 = 49)."""
+    g = np.arange(-half, half + 1) * step
+    tx, ty = np.meshgrid(g, g, indexing="ij")
+    return np.stack([tx.ravel(), ty.ravel()], 1)
+
+
+def local_hypotheses(rng: np.random.Generator, q_centre: np.ndarray,
+                     t_centre: np.ndarray, nR: int, nT: int, kappa: float,
+                     trans_sd: float):
+    """Per-particle local hypothesis sets: nR vMF rotations about q_centre
+    and nT Gaussian translations about t_centre.  Returns (n, nR, 4) and
+    (n, nT, 2) float64."""
+    n = len(q_centre)
+    qs = np.empty((n, nR, 4))
+    for i in range(n):
+        qs[i] = vmf_quaternions(rng, q_centre[i], kappa, nR)
+    ts = t_centre[:, None, :] + trans_sd * rng.standard_normal((n, nT, 2))
+    return qs, ts
+
+
+def perturb_poses(rng: np.random.Generator, q: np.ndarray, t: np.ndarray,
+                  rot_deg: float, trans_px: float):
+    """Current poses a small random step away from the true ones."""
+    axis = rng.standard_normal((len(q), 3))
+    axis /= np.linalg.norm(axis, axis=1, keepdims=True)
+    ang = np.deg2rad(rot_deg) * rng.random(len(q))
+    dq = np.concatenate([np.cos(ang / 2)[:, None], np.sin(ang / 2)[:, None] * axis], 1)
+    qn = quat_mul(q, dq)
+    qn /= np.linalg.norm(qn, axis=1, keepdims=True)
+    return qn, t + trans_px * rng.standard_normal(t.shape)
+
+
+CONFIGS = {
+    # configuration 0: 64^3, global scan, CPU-runnable
+    "box64_global": dict(box=64, pixel_size=1.5, n_blobs=40, sigma_a=(2.0, 4.0),
+                         radius_px=20.0, n=2000, shift=3.0, snr=0.05, rU=16,
+                         pf=2, n_classes=1),
+    # configuration 1: 256^3, local rounds 1,000 rotations x 100 translations
+    "box256_local": dict(box=256, pixel_size=1.1, n_blobs=200, sigma_a=(1.5, 3.0),
+                         radius_px=80.0, n=50000, shift=8.0, snr=0.03, rU=80,
+                         pf=2, n_classes=1, nR=1000, nT=100, kappa=200.0),
+}
+
+
+def config_rL(box: int, pixel_size: float, ignore_res: float = 200.0) -> float:
+    """Lower pixel radius of the likelihood,
+    rL = floor(resA2P(1 / ignoreRes, size, pixelSize)) (src/Optimiser.cpp:243,
+    resA2P src/Functions/Spectrum.cpp:26-31); ignoreRes 200 Angstrom."""
+    return float(math.floor(box * pixel_size / ignore_res))
