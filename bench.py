@@ -1,0 +1,511 @@
+"""E-step throughput benchmark on synthetic particles.
+
+One step = one local particle-filter phase over a batch of particles at the
+production configuration (256^3 map, 1.1 A/px, 200 blobs, cutoff 80 Fourier
+pixels -> K = 9,930, padding 2, 1,000 rotations x 100 translations per
+particle): projection of every particle's rotations, phase-shifted weighted
+data, likelihood of every hypothesis, marginal weights, and narrowing +
+systematic resampling of the rotation and translation sets.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp32|bf16x3]
+  python bench.py --impl reference ...   # the CPU path timed on the host cores
+
+Prints one JSON line (rank 0).  Under torchrun each rank drives its own GPU
+with its own particles (weak scaling, no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "thunder-refactor-expectation_gb300"
+for _p in (str(ROOT), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "E-step particles/sec, box 256: learned+BF16 vs plain FP32 GPU at equal pose error"
+UNIT = "particles/s"
+WORKLOAD = dict(box=256, pixel_size=1.1, n_blobs=200, sigma_a=(1.5, 3.0), radius_px=80.0,
+                shift=8.0, snr=0.03, rU=80, pf=2, nR=1000, nT=100, kappa=200.0)
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+# ---------------------------------------------------------------- clocks ----
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- workload ---
+def make_workload(torch, dev, nP, n_batches, seed, box=None):
+    """Synthetic map + particle batches, generated on the GPU."""
+    from tg3 import synth
+    W = dict(WORKLOAD)
+    if box is not None:          # reduced case for profiling captures
+        scale = box / W["box"]
+        W.update(box=box, rU=max(8, int(W["rU"] * scale)), radius_px=W["radius_px"] * scale)
+    rng = np.random.default_rng(seed)
+    bm = synth.blob_map(rng, W["n_blobs"], W["sigma_a"], W["pixel_size"], W["radius_px"])
+    vol = synth.padded_volume(bm, W["box"], W["pf"], device=dev, dtype=torch.float32)
+    rL = synth.config_rL(W["box"], W["pixel_size"])
+    n = nP * n_batches
+    st = synth.make_stack(seed + 1, [bm], W["box"], W["pixel_size"], W["pf"], W["rU"], rL, n,
+                          W["shift"], W["snr"], device=dev)
+    qc, tc = synth.perturb_poses(rng, st.quat_true, st.trans_true, 3.0, 1.0)
+    qs, ts = synth.local_hypotheses(rng, qc, tc, W["nR"], W["nT"], W["kappa"], 2.0)
+    nR, nT = W["nR"], W["nT"]
+    batches = []
+    for b in range(n_batches):
+        sl = slice(b * nP, (b + 1) * nP)
+        perm_r = np.stack([rng.permutation(nR) for _ in range(nP)]).astype(np.int32)
+        perm_t = np.stack([rng.permutation(nT) for _ in range(nP)]).astype(np.int32)
+        host = dict(
+            dat=np.ascontiguousarray(st.dat[sl].astype(np.complex64)),
+            ctf=np.ascontiguousarray(st.ctf[sl].astype(np.float32)),
+            sig=np.ascontiguousarray(st.sigRcp[sl].astype(np.float32)),
+            quat=np.ascontiguousarray(qs[sl]), trans=np.ascontiguousarray(ts[sl]),
+            pwR=np.full((nP, nR), 1.0 / nR), pwT=np.full((nP, nT), 1.0 / nT), pwC=np.ones(nP),
+            perm_r=perm_r, perm_t=perm_t,
+            u0_r=rng.random(nP) / nR, u0_t=rng.random(nP) / nT,
+            peak_r=np.full(nP, np.nan), peak_t=np.zeros(nP))
+        batches.append(host)
+    return W, vol, st, batches
+
+
+def to_dev(torch, dev, host):
+    return {k: torch.as_tensor(v).to(dev).contiguous() for k, v in host.items()}
+
+
+def pin(torch, host):
+    out = {}
+    for k, v in host.items():
+        t = torch.as_tensor(v)
+        out[k] = t.pin_memory() if torch.cuda.is_available() else t
+    return out
+
+
+# ---------------------------------------------------------------- tg3 arm ---
+def run_tg3(args, rank, world, local_rank):
+    import torch
+    import tg3
+
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    nP = args.batch
+    W, vol, st, batches = make_workload(torch, dev, nP, args.batches, 1000 + 1 + 97 * rank,
+                                        box=args.box)
+    nR, nT, K = W["nR"], W["nT"], st.K
+    prec = tg3.SCORE_BF16X3 if args.precision == "bf16x3" else tg3.SCORE_FP32
+    ctx = tg3.Context(local_rank)
+    ctx.set_volume(0, vol, W["pf"])
+    ctx.set_pixels(st.iCol, st.iRow, W["box"])
+    del vol
+    dbat = [to_dev(torch, dev, b) for b in batches]
+    out = dict(wC=torch.empty(nP, dtype=torch.float64, device=dev),
+               wR=torch.empty((nP, nR), dtype=torch.float64, device=dev),
+               wT=torch.empty((nP, nT), dtype=torch.float64, device=dev),
+               base=torch.empty(nP, dtype=torch.float64, device=dev),
+               src_r=torch.empty((nP, nR), dtype=torch.int32, device=dev),
+               src_t=torch.empty((nP, nT), dtype=torch.int32, device=dev),
+               w_r=torch.empty((nP, nR), dtype=torch.float64, device=dev),
+               w_t=torch.empty((nP, nT), dtype=torch.float64, device=dev),
+               top=torch.empty(nP, dtype=torch.int32, device=dev))
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def step(i):
+        b = dbat[i % len(dbat)]
+        ctx.local_phase(nP, nR, nT, b["dat"], b["ctf"], b["sig"], b["quat"], b["trans"],
+                        b["pwR"], b["pwT"], b["pwC"], None, out["wC"], out["wR"], out["wT"],
+                        out["base"], None, prec)
+        ctx.resample(nP, nR, out["wR"], b["pwR"], b["perm_r"], b["u0_r"], b["peak_r"], nR,
+                     out["src_r"], out["w_r"], out["top"])
+        ctx.resample(nP, nT, out["wT"], b["pwT"], b["perm_t"], b["u0_t"], b["peak_t"], nT,
+                     out["src_t"], out["w_t"], out["top"])
+
+    launches_per_step = 7   # project, shift, x0, cross term, weights, 2 x resample
+    for i in range(args.warmup):
+        step(i)
+    ctx.sync()
+
+    # FP32 SGEMM (TF32 off) reference throughput for the plain path's roofline
+    fp32_peak = None
+    if prec == tg3.SCORE_FP32:
+        torch.backends.cuda.matmul.allow_tf32 = False
+        a = torch.randn(8192, 8192, device=dev)
+        bmat = torch.randn(8192, 8192, device=dev)
+        for _ in range(3):
+            a @ bmat
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        best = 1e9
+        for _ in range(5):
+            e0.record()
+            a @ bmat
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        fp32_peak = 2 * 8192 ** 3 / (best * 1e-3) / 1e12
+        del a, bmat
+
+    # ---- timed region (device-resident inputs)
+    barrier(world)
+    torch.cuda.synchronize()
+    clk = ClockSampler(local_rank)
+    clk.start()
+    ctx.set_timing(True)
+    ctx.stage_times(reset=True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    t_wall = time.perf_counter()
+    with torch.cuda.stream(stream):
+        ev0.record(stream)
+        for i in range(args.steps):
+            step(i)
+        ev1.record(stream)
+    ev1.synchronize()
+    wall = time.perf_counter() - t_wall
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = clk.stop()
+    stages = ctx.stage_times(reset=True)
+    ctx.set_timing(False)
+    ms = ev0.elapsed_time(ev1)
+    ms = reduce_max(world, ms)
+
+    # ---- end to end: host buffers, copies inside the timed region
+    hbat = [pin(torch, b) for b in batches]
+    hout = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in out.items()}
+    inputs = ("dat", "ctf", "sig", "quat", "trans", "pwR", "pwT", "pwC")
+    h2d = sum(hbat[0][k].numel() * hbat[0][k].element_size() for k in inputs)
+    h2d += sum(hbat[0][k].numel() * hbat[0][k].element_size()
+               for k in ("perm_r", "perm_t", "u0_r", "u0_t", "peak_r", "peak_t", "pwR", "pwT"))
+    d2h = sum(hout[k].numel() * hout[k].element_size()
+              for k in ("wC", "wR", "wT", "base", "src_r", "src_t", "w_r", "w_t", "top"))
+
+    def e2e_step(i):
+        b = hbat[i % len(hbat)]
+        ctx.local_phase_host(nP, nR, nT, b["dat"], b["ctf"], b["sig"], b["quat"], b["trans"],
+                             b["pwR"], b["pwT"], b["pwC"], None, hout["wC"], hout["wR"],
+                             hout["wT"], hout["base"], None, prec)
+        tg3.check(tg3.lib().tg3_resample(nP, nR, tg3.ptr(hout["wR"]), tg3.ptr(b["pwR"]),
+                                         tg3.ptr(b["perm_r"]), tg3.ptr(b["u0_r"]),
+                                         tg3.ptr(b["peak_r"]), nR, tg3.ptr(hout["src_r"]),
+                                         tg3.ptr(hout["w_r"]), tg3.ptr(hout["top"])))
+        tg3.check(tg3.lib().tg3_resample(nP, nT, tg3.ptr(hout["wT"]), tg3.ptr(b["pwT"]),
+                                         tg3.ptr(b["perm_t"]), tg3.ptr(b["u0_t"]),
+                                         tg3.ptr(b["peak_t"]), nT, tg3.ptr(hout["src_t"]),
+                                         tg3.ptr(hout["w_t"]), tg3.ptr(hout["top"])))
+
+    for i in range(2):
+        e2e_step(i)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(args.e2e_steps):
+        e2e_step(i)
+    torch.cuda.synchronize()
+    e2e_s = reduce_max(world, time.perf_counter() - t0)
+    barrier(world)
+
+    value = nP * args.steps * world / (ms * 1e-3)
+    e2e_value = nP * args.e2e_steps * world / e2e_s
+    cross_ms, cross_n = stages["cross"]
+    flop = 4.0 * K * nR * nT * nP          # real part of the complex cross term
+    achieved = flop / (cross_ms / cross_n * 1e-3) / 1e12
+    hbm, bf16, kind = peaks()
+    if prec == tg3.SCORE_FP32:
+        peak, peak_note = fp32_peak, "cuBLAS FP32 SGEMM (TF32 off) measured live"
+    else:
+        peak, peak_note = bf16, f"bf16 dense tensor, {kind} (MEASURED_PEAKS.json)"
+    proj_ms, proj_n = stages["project"]
+    proj_bytes = 72.0 * nR * K * nP
+    res = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32" if prec == tg3.SCORE_FP32 else "bf16x3+fp32",
+        "data": "synthetic (seeded Gaussian-blob map and particles, generated on the GPU)",
+        "config": {"workload": f"local particle-filter phase, box {W['box']}, K={K}, "
+                               f"{nR} rotations x {nT} translations per particle",
+                   "box": W["box"], "pf": W["pf"], "K": K, "nR": nR, "nT": nT,
+                   "particles_per_step": nP, "precision": args.precision,
+                   "l2": "inputs larger than L2: the projection bank alone is "
+                         f"{nP * nR * ctx_kp(K) * 4 / 1e9:.1f} GB per step"},
+        "clocks": clocks,
+        "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "wall_s": round(e2e_s, 3)},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"kernel": "cross term GEMM", "bound": "tensor",
+                     "achieved": round(achieved, 2), "peak": round(peak, 1) if peak else None,
+                     "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
+                     "peak_source": peak_note, "traffic": None,
+                     "algorithmic_flop_per_launch": flop},
+        "stages": {k: {"ms_per_launch": round(v[0] / max(v[1], 1), 4), "launches": v[1]}
+                   for k, v in stages.items() if v[1]},
+        "projection": {"achieved_gbs": round(proj_bytes / (proj_ms / proj_n * 1e-3) / 1e9, 1),
+                       "peak_gbs": hbm, "frac": round(proj_bytes / (proj_ms / proj_n * 1e-3) / 1e9 / hbm, 4),
+                       "bytes_per_launch": proj_bytes},
+        "hypotheses_per_s": round(value * nR * nT, 1),
+        "wall_s_timed": round(wall, 3),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_baseline(st, batches[0], W, args.cpu_sample)
+    ctx.close()
+    return res
+
+
+def ctx_kp(K):
+    return int(math.ceil(2 * K / 64) * 64)
+
+
+# --------------------------------------------------------------- CPU path ---
+def _cpu_worker(job):
+    """Score `job` particles with the oracle port (one process per core)."""
+    import sys as _s
+    for p in job["paths"]:
+        if p not in _s.path:
+            _s.path.insert(0, p)
+    from oracle import oracle as O
+    vol = job["vol"]
+    if isinstance(vol, str):
+        vol = np.load(vol, mmap_mode="r")
+    out = []
+    for d in job["items"]:
+        r = O.score_local(vol, job["pf"], job["iCol"], job["iRow"], job["box"], d["dat"],
+                          d["ctf"], d["sig"], d["quat"], d["trans"], d["pwR"], d["pwT"], 1.0,
+                          want_dvp=False)
+        src, w, top = O.resample(r["wR"], d["pwR"], d["perm_r"], d["u0_r"],
+                                 O.peak_factor_r(r["wR"]), len(d["pwR"]))
+        src, w, top = O.resample(r["wT"], d["pwT"], d["perm_t"], d["u0_t"], 0.0, len(d["pwT"]))
+        out.append(r["base"])
+    return out
+
+
+def cpu_time(vol_np, st, host, W, n_particles, n_rot, workers):
+    """Time the CPU path on a bounded sample: n_particles particles with n_rot
+    of their rotations each (all translations), over `workers` processes."""
+    import multiprocessing as mp
+    items = []
+    for l in range(n_particles):
+        items.append(dict(dat=host["dat"][l].astype(np.complex128),
+                          ctf=host["ctf"][l].astype(np.float64),
+                          sig=host["sig"][l].astype(np.float64),
+                          quat=host["quat"][l][:n_rot], trans=host["trans"][l],
+                          pwR=host["pwR"][l][:n_rot] * (len(host["pwR"][l]) / n_rot),
+                          pwT=host["pwT"][l], perm_r=np.random.default_rng(l).permutation(n_rot).astype(np.int32),
+                          perm_t=host["perm_t"][l], u0_r=float(host["u0_r"][l]), u0_t=float(host["u0_t"][l])))
+    paths = [str(ROOT), str(PKG)]
+    if workers == 1:
+        job = dict(items=items, vol=vol_np, pf=W["pf"], iCol=st.iCol, iRow=st.iRow,
+                   box=W["box"], paths=paths)
+        t0 = time.perf_counter()
+        _cpu_worker(job)
+        return time.perf_counter() - t0
+    # the volume reaches the workers through one memory-mapped file
+    import tempfile
+    fd, vpath = tempfile.mkstemp(suffix=".npy")
+    os.close(fd)
+    np.save(vpath, np.ascontiguousarray(vol_np))
+    try:
+        jobs = [dict(items=items[i::workers], vol=vpath, pf=W["pf"], iCol=st.iCol,
+                     iRow=st.iRow, box=W["box"], paths=paths) for i in range(workers)]
+        jobs = [j for j in jobs if j["items"]]
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(len(jobs)) as pool:
+            pool.map(_cpu_worker, jobs[:1])          # start-up and page-in, untimed
+            t0 = time.perf_counter()
+            pool.map(_cpu_worker, jobs)
+            return time.perf_counter() - t0
+    finally:
+        os.unlink(vpath)
+
+
+def cpu_baseline(st, host, W, sample_rot):
+    """The oracle port of the reference CPU E-step, timed on this host."""
+    from tg3 import synth
+    import torch
+    rng = np.random.default_rng(1001)
+    bm = synth.blob_map(rng, W["n_blobs"], W["sigma_a"], W["pixel_size"], W["radius_px"])
+    vol = synth.padded_volume(bm, W["box"], W["pf"], device="cuda" if torch.cuda.is_available() else "cpu",
+                              dtype=torch.float32).cpu().numpy().astype(np.complex128)
+    secs = cpu_time(vol, st, host, W, 1, sample_rot, 1)
+    per_particle = secs * W["nR"] / sample_rot
+    return {"value": round(1.0 / per_particle, 6), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"1 particle x {sample_rot} of its {W['nR']} rotations x {W['nT']} "
+                      f"translations, K={st.K}, scaled to a full particle ({secs:.1f} s measured); "
+                      "double-precision oracle port, one core"}
+
+
+def run_reference(args, rank, world):
+    """The CPU implementation of the path on all host cores (rank 0 only)."""
+    if rank != 0:
+        return None
+    import torch
+    from tg3 import synth
+    W = dict(WORKLOAD)
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(1001)
+    bm = synth.blob_map(rng, W["n_blobs"], W["sigma_a"], W["pixel_size"], W["radius_px"])
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    vol = synth.padded_volume(bm, W["box"], W["pf"], device=dev,
+                              dtype=torch.float32).cpu().numpy().astype(np.complex128)
+    n = cores
+    rL = synth.config_rL(W["box"], W["pixel_size"])
+    st = synth.make_stack(1002, [bm], W["box"], W["pixel_size"], W["pf"], W["rU"], rL, n,
+                          W["shift"], W["snr"], device=dev)
+    qc, tc = synth.perturb_poses(rng, st.quat_true, st.trans_true, 3.0, 1.0)
+    qs, ts = synth.local_hypotheses(rng, qc, tc, W["nR"], W["nT"], W["kappa"], 2.0)
+    host = dict(dat=st.dat, ctf=st.ctf, sig=st.sigRcp, quat=qs, trans=ts,
+                pwR=np.full((n, W["nR"]), 1.0 / W["nR"]), pwT=np.full((n, W["nT"]), 1.0 / W["nT"]),
+                perm_t=np.stack([rng.permutation(W["nT"]) for _ in range(n)]).astype(np.int32),
+                u0_r=rng.random(n) / W["nR"], u0_t=rng.random(n) / W["nT"])
+    n_rot = args.cpu_sample
+    times = []
+    for i in range(args.warmup + args.steps):
+        secs = cpu_time(vol, st, host, W, n, n_rot, cores)
+        if i >= args.warmup:
+            times.append(secs)
+    per_step = float(np.mean(times))
+    value = n * n_rot / W["nR"] / per_step
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(per_step * 1e3, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+            "data": "synthetic", "config": {"workload": "local particle-filter phase, box 256, "
+                                            "K=9930, 1000 rotations x 100 translations",
+                                            "sample_rotations": n_rot, "particles_per_step": n},
+            "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{n} particles (one per core) x {n_rot} of 1000 rotations "
+                                       "x 100 translations per step, scaled to full particles; "
+                                       "double-precision oracle port (the reference sources are "
+                                       "not present on this machine)"},
+            "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+# ------------------------------------------------------------ distributed ---
+_pg = None
+
+
+def init_dist():
+    global _pg
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+        _pg = dist
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1 and _pg is not None:
+        _pg.barrier()
+
+
+def reduce_max(world, x: float) -> float:
+    if world > 1 and _pg is not None:
+        import torch
+        t = torch.tensor([float(x)])
+        _pg.all_reduce(t, op=_pg.ReduceOp.MAX)
+        return float(t.item())
+    return float(x)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="tg3", choices=["tg3", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16x3"])
+    ap.add_argument("--batch", type=int, default=128, help="particles per step")
+    ap.add_argument("--batches", type=int, default=3, help="distinct particle batches cycled")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-sample", type=int, default=40,
+                    help="rotations per particle in the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
+    args = ap.parse_args()
+    rank, world, local = init_dist()
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        res = run_tg3(args, rank, world, local)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+    if world > 1 and _pg is not None:
+        _pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

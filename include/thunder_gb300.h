@@ -1,0 +1,254 @@
+/*
+ * thunder_gb300.h -- C ABI of the GB300-native THUNDER E-step + insertion
+ * library (libtg3.so).
+ *
+ * Every entry point returns an int status (TG3_OK on success); the message of
+ * the last failure on the calling thread is available from tg3_last_error().
+ * Plain pointers and sizes only.  Complex numbers are interleaved
+ * (re, im) float pairs, the layout of THUNDER's Complex with RFLOAT = float
+ * (include/Precision.h:65-99 of the reference).
+ *
+ * Two layers:
+ *  1. Reference-shaped entry points (tg3_Expect*, tg3_InsertFT): host
+ *     pointers, the argument meaning and layouts of the functions of
+ *     gpu/interface/Interface.h that they replace (cited beside each).  The
+ *     drop-in adaptor interface/Interface.cpp in the package maps the
+ *     reference's C++ signatures onto them 1:1.
+ *  2. Device-resident entry points (tg3_*_d and the context API): device
+ *     pointers and a CUDA stream, for callers that keep data in HBM across
+ *     calls (the batched particle-filter phase).
+ *
+ * Geometry conventions (shared by both layers):
+ *  - a padded half-FT volume of edge vdim is stored [z][y][x], x in
+ *    [0, vdim/2], y and z in [0, vdim) with negative frequencies wrapped
+ *    (Volume::iFTHalf, include/Image/Volume.h:566-573);
+ *  - rotation matrices are row-major 3x3 doubles; quaternions (w, x, y, z);
+ *  - pixel lists iCol/iRow are those of Optimiser::allocPreCalIdx
+ *    (src/Optimiser.cpp:7942-7992), K = npxl entries, unpadded units;
+ *  - CTF attributes are 7 floats per image in struct CTFAttr order
+ *    (voltage, defocusU, defocusV, defocusTheta, Cs, amplitudeContrast,
+ *    phaseShift; include/Database.h:108-122).
+ */
+#ifndef THUNDER_GB300_H
+#define THUNDER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    TG3_OK = 0,
+    TG3_ERR_ARG = 1,       /* bad argument (null pointer, size, layout) */
+    TG3_ERR_CUDA = 2,      /* a CUDA runtime call or kernel launch failed */
+    TG3_ERR_ALLOC = 3,     /* device or pinned host allocation failed */
+    TG3_ERR_STATE = 4,     /* call out of order (e.g. no volume set) */
+    TG3_ERR_TIMEOUT = 5,   /* a bounded device-side wait expired */
+    TG3_ERR_NUMERIC = 6,   /* non-finite or all-zero weights */
+    TG3_ERR_UNSUPPORTED = 7
+};
+
+/* Insertion kernels. */
+enum { TG3_KERNEL_TRILINEAR = 0, TG3_KERNEL_MKB = 1 };
+
+/* Scoring precision of the likelihood cross term. */
+enum { TG3_SCORE_FP32 = 0, TG3_SCORE_BF16X3 = 1 };
+
+const char* tg3_status_string(int status);
+const char* tg3_last_error(void);
+/* Library version string, e.g. "tg3 1.0 sm_103a". */
+const char* tg3_version(void);
+
+/* ------------------------------------------------------------------------
+ * Layer 1: reference-shaped entry points (host pointers).
+ * --------------------------------------------------------------------- */
+
+/* Replaces getAviDevice(std::vector<int>&), gpu/interface/Interface.h:16.
+ * Writes up to `cap` usable device ordinals to gpus; *n gets the count. */
+int tg3_getAviDevice(int* gpus, int cap, int* n);
+
+/* Replaces ExpectRotran, gpu/interface/Interface.h:199-208.
+ * traP [nT][npxl] complex: exp(-2 pi i (iCol tx + iRow ty) / idim) for the
+ * translations trans [nT][2]; rotMat [nR][9] from the quaternions
+ * rot [nR][4]. */
+int tg3_ExpectRotran(float* traP, const double* trans, const double* rot,
+                     double* rotMat, const int* iCol, const int* iRow,
+                     int nR, int nT, int idim, int npxl);
+
+/* Replaces ExpectProject, gpu/interface/Interface.h:210-219.
+ * rotP [nR][npxl] complex = trilinear samples of volume (edge vdim, padded
+ * by pf) at rotMat (iCol pf, iRow pf, 0).  interp must be linear (1). */
+int tg3_ExpectProject(const float* volume, float* rotP, const double* rotMat,
+                      const int* iCol, const int* iRow, int nR, int pf,
+                      int interp, int vdim, int npxl);
+
+/* Replaces ExpectGlobal3D, gpu/interface/Interface.h:221-237.
+ * Scores every (image, rotation, translation) of class kIdx of nK and folds
+ * the weights into wC [imgNum][nK], wR [imgNum][nK][nR], wT [imgNum][nK][nT]
+ * relative to the running per-image baseline baseL [imgNum].  kIdx == 0
+ * initialises; kIdx > 0 rescales earlier classes when the baseline rises.
+ * datP/ctfP/sigRcpP are image-major [imgNum][npxl]; pR [nR], pT [nT] are the
+ * prior weights. */
+int tg3_ExpectGlobal3D(const float* rotP, const float* traP, const float* datP,
+                       const float* ctfP, const float* sigRcpP, float* wC,
+                       float* wR, float* wT, const double* pR, const double* pT,
+                       float* baseL, int kIdx, int nK, int nR, int nT, int npxl,
+                       int imgNum);
+
+/* Replaces InsertFT (single-class form), gpu/interface/Interface.h:294-318,
+ * on one GPU (no hemisphere/slave communicators).  For every image l and
+ * draw m < mReco: rotation from the quaternion nR[(l mReco + m) 4 ..],
+ * translation nT[(l mReco + m) 2 ..], shift the image by -(t - offS[l]),
+ * weight w[l], and grid datP * ctfP * w into F3D and ctfP^2 * w into T3D
+ * (edge dimSize = pf idim), with the trilinear kernel (the reference GPU
+ * behaviour) or the MKB kernel (radius a = 1.9, alpha = 15, tabulated as in
+ * Reconstructor).  O3D [3] accumulates -R (t - offS, 0), counter the
+ * number of inserted draws.  F3D is complex, T3D real, both
+ * [dimSize][dimSize][dimSize/2 + 1], accumulated into (not cleared).
+ * ctfaData, nD and cSearch are accepted for signature parity; cSearch must
+ * be false.  kernel is TG3_KERNEL_*. */
+int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter,
+                 const float* datP, const float* ctfP, const float* sigRcpP,
+                 const float* ctfaData, const double* offS, const float* w,
+                 const double* nR, const double* nT, const double* nD,
+                 const int* iCol, const int* iRow, float pixelSize,
+                 int cSearch, int opf, int npxl, int mReco, int idim,
+                 int dimSize, int imgNum, int kernel);
+
+/* Local particle-filter scoring of one particle, the combined work of
+ * ExpectLocalRTD + ExpectLocalPreI3D + ExpectLocalM,
+ * gpu/interface/Interface.h:80-139 (no defocus search): project the nR
+ * rotations rot [nR][4] of the current volume handle, shift by the nT
+ * translations trans [nT][2], score against dat/ctf/sigRcp [npxl] and
+ * return wC [1], wR [nR], wT [nT] relative to the best hypothesis, with the
+ * prior weights oldR [nR], oldT [nT], oldC.  Optional dvp [nR][nT] (may be
+ * NULL) receives the log-likelihoods and baseL the best one. */
+typedef struct tg3_volume tg3_volume;
+int tg3_volume_create(tg3_volume** vol, const float* volume, int vdim, int pf);
+int tg3_volume_destroy(tg3_volume* vol);
+int tg3_ExpectLocal3D(tg3_volume* vol, const float* dat, const float* ctf,
+                      const float* sigRcp, const int* iCol, const int* iRow,
+                      int npxl, int idim, const double* rot, int nR,
+                      const double* trans, int nT, const double* oldR,
+                      const double* oldT, double oldC, float* wC, float* wR,
+                      float* wT, float* dvp, float* baseL);
+
+/* Particle-filter narrowing + systematic resampling of one axis of nP
+ * particles, Particle::keepHalfHeightPeak + Particle::resample(n, pt)
+ * (src/Particle.cpp:1935-1973, 1275-1463) with the shuffle permutation and
+ * u0 supplied by the caller (the reference draws them from its RNG).
+ * u [nP][n] likelihood weights, w [nP][n] prior weights, perm [nP][n],
+ * u0 [nP], peak [nP] (<= 0: no narrowing; NaN: derive it as
+ * Particle::setPeakFactor(PAR_R) does in 3D).  Outputs src [nP][nOut]
+ * (index of each new sample's source), wOut [nP][nOut] (normalised new
+ * priors), top [nP] (index of the best sample).  Host pointers. */
+int tg3_resample(int nP, int n, const double* u, const double* w,
+                 const int* perm, const double* u0, const double* peak,
+                 int nOut, int* src, double* wOut, int* top);
+
+/* ------------------------------------------------------------------------
+ * Layer 2: device-resident context (device pointers, caller's stream).
+ * A context owns a CUDA stream, the projection volume in the paired-corner
+ * layout, the insertion accumulator and a grow-only workspace.
+ * --------------------------------------------------------------------- */
+typedef struct tg3_ctx tg3_ctx;
+
+int tg3_ctx_create(tg3_ctx** ctx, int device);
+int tg3_ctx_destroy(tg3_ctx* ctx);
+/* The context's CUDA stream (cudaStream_t) as void*. */
+void* tg3_ctx_stream(tg3_ctx* ctx);
+int tg3_ctx_sync(tg3_ctx* ctx);
+/* Bytes of device workspace currently held. */
+size_t tg3_ctx_workspace_bytes(tg3_ctx* ctx);
+
+/* Projection volume for class `cls` (0-based, < 16): device or host complex
+ * half-FT volume of edge vdim, padding factor pf.  Copied into the
+ * context's paired-corner layout. */
+int tg3_ctx_set_volume(tg3_ctx* ctx, int cls, const float* volume, int vdim,
+                       int pf, int volume_on_device);
+
+/* Pixel list (host arrays), shared by all later calls: K pixels, image edge
+ * idim.  Fails if a rotated pixel could leave the volume. */
+int tg3_ctx_set_pixels(tg3_ctx* ctx, const int* iCol, const int* iRow, int K,
+                       int idim);
+
+/* Batched local phase of nP particles (all device pointers, layouts
+ * particle-major): dat [nP][K] complex, ctf, sigRcp [nP][K]; quat
+ * [nP][nR][4], trans [nP][nT][2] (double); priors pwR [nP][nR],
+ * pwT [nP][nT] (double), pwC [nP] (double); class index per particle cls
+ * [nP] (int, may be NULL for class 0).
+ * Outputs: wC [nP], wR [nP][nR], wT [nP][nT] (double, relative to
+ * baseL), baseL [nP] (double), dvp [nP][nR][nT] (float, may be NULL).
+ * precision: TG3_SCORE_FP32 or TG3_SCORE_BF16X3. */
+int tg3_local_phase_d(tg3_ctx* ctx, int nP, int nR, int nT,
+                      const float* dat, const float* ctf, const float* sigRcp,
+                      const double* quat, const double* trans,
+                      const double* pwR, const double* pwT, const double* pwC,
+                      const int* cls, double* wC, double* wR, double* wT,
+                      double* baseL, float* dvp, int precision);
+
+/* Host-buffer form of tg3_local_phase_d: the same arguments in host memory
+ * (pinned memory gives asynchronous copies).  Inputs are staged into the
+ * context's workspace, outputs copied back; returns after completion. */
+int tg3_local_phase(tg3_ctx* ctx, int nP, int nR, int nT, const float* dat,
+                    const float* ctf, const float* sigRcp, const double* quat,
+                    const double* trans, const double* pwR, const double* pwT,
+                    const double* pwC, const int* cls, double* wC, double* wR,
+                    double* wT, double* baseL, float* dvp, int precision);
+
+/* Per-stage device timing (CUDA events on the context stream).  When
+ * enabled, every stage launch is bracketed by events; tg3_ctx_stage_times
+ * synchronises and returns, per stage, the summed milliseconds and the
+ * number of launches since the last reset. */
+enum {
+    TG3_STAGE_PROJECT = 0, TG3_STAGE_SHIFT = 1, TG3_STAGE_CROSS = 2,
+    TG3_STAGE_WEIGHTS = 3, TG3_STAGE_RESAMPLE = 4, TG3_STAGE_INSERT = 5,
+    TG3_STAGE_COUNT = 6
+};
+int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
+int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);
+
+/* Device form of tg3_resample (all pointers device memory, stream of ctx). */
+int tg3_resample_d(tg3_ctx* ctx, int nP, int n, const double* u,
+                   const double* w, const int* perm, const double* u0,
+                   const double* peak, int nOut, int* src, double* wOut,
+                   int* top);
+
+/* Insertion accumulator: edge vdim (= pf idim), cleared to zero. */
+int tg3_ctx_insert_begin(tg3_ctx* ctx, int vdim, int pf);
+/* Insert nP particles' draws (device pointers): dat [nP][K] complex,
+ * ctf [nP][K], quat [nP][4], trans [nP][2], offset [nP][2] (double),
+ * w [nP] (float); kernel TG3_KERNEL_*.  O3D (device double[3]) and counter
+ * (device int) may be NULL. */
+int tg3_insert_d(tg3_ctx* ctx, int nP, const float* dat, const float* ctf,
+                 const double* quat, const double* trans, const double* offset,
+                 const float* w, int kernel, double* O3D, int* counter);
+/* Read the accumulator into separate F (complex) and T (real) device
+ * arrays of [vdim][vdim][vdim/2+1] entries, adding to their contents
+ * when accumulate != 0. */
+int tg3_ctx_insert_read_d(tg3_ctx* ctx, float* F, float* T, int accumulate);
+
+/* ------------------------------------------------------------------------
+ * Kernel-level device entry points (device pointers, explicit stream).
+ * --------------------------------------------------------------------- */
+/* rotMat [n][9] (double, row-major) from quat [n][4]. */
+int tg3_rotmat_d(const double* quat, int n, double* rotMat, void* stream);
+/* out [nT][K] complex phase-shift bank (see tg3_ExpectRotran). */
+int tg3_translate_d(const double* trans, int nT, int idim, const int* iCol,
+                    const int* iRow, int K, float* out, void* stream);
+/* out [nImg][K] CTF values for attr [nImg][7] (CTF(), src/CTF.cpp:98-145). */
+int tg3_ctf_d(const float* attr, int nImg, float pixelSize, int idim,
+              const int* iCol, const int* iRow, int K, float* out,
+              void* stream);
+/* out [nR][K] complex projections of the context's class-`cls` volume at
+ * rotMat [nR][9] (double). */
+int tg3_project_d(tg3_ctx* ctx, int cls, const double* rotMat, int nR,
+                  float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* THUNDER_GB300_H */

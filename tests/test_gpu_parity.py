@@ -1,0 +1,384 @@
+"""GPU parity: every CUDA stage of the E-step and the insertion, called
+through the C ABI (libtg3.so), against the double-precision oracle on the
+same seeded inputs.  The oracle receives the float32-rounded inputs the GPU
+sees, so the differences measured are the GPU's arithmetic only.
+
+Tolerances (FP32 plain path, from the acceptance bars): log-likelihoods
+within 1e-4 relative; marginal weights compared after normalisation within
+2e-3 absolute on the distribution; projections within 1e-5 of the slice's
+peak magnitude; resampling bit-exact; insertion FSC >= 0.999."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+import tg3
+from tg3 import synth
+
+pytestmark = pytest.mark.gpu
+
+DEV = "cuda:0"
+
+
+def f32(x):
+    """float32-rounded copy in float64 (complex128 for complex)."""
+    x = np.asarray(x)
+    if np.iscomplexobj(x):
+        return x.astype(np.complex64).astype(np.complex128)
+    return x.astype(np.float32).astype(np.float64)
+
+
+def dev(x, dtype=None):
+    t = torch.as_tensor(np.ascontiguousarray(x))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.to(DEV).contiguous()
+
+
+@pytest.fixture(scope="module")
+def small():
+    rng = np.random.default_rng(11)
+    box, pf, px = 32, 2, 1.5
+    rU = 12
+    iCol, iRow, iSig, _ = synth.pixel_index(box, rU, synth.config_rL(box, px))
+    bm = synth.blob_map(rng, 20, (2.0, 4.0), px, 9.0)
+    vol = synth.padded_volume(bm, box, pf).numpy()
+    vol32 = vol.astype(np.complex64)
+    st = synth.make_stack(5, [bm], box, px, pf, rU, synth.config_rL(box, px), 16, 2.0, 0.5)
+    return dict(rng=rng, box=box, pf=pf, px=px, iCol=iCol, iRow=iRow, vol=f32(vol32),
+                vol32=vol32, st=st)
+
+
+@pytest.fixture(scope="module")
+def ctx(small):
+    c = tg3.Context(0)
+    c.set_volume(0, torch.as_tensor(small["vol32"]).to(DEV), small["pf"])
+    c.set_pixels(small["iCol"], small["iRow"], small["box"])
+    yield c
+    c.close()
+
+
+def test_rotmat_translate_ctf(small):
+    rng = small["rng"]
+    q = synth.haar_quaternions(rng, 33)
+    mat = torch.empty((33, 9), dtype=torch.float64, device=DEV)
+    tg3.check(tg3.lib().tg3_rotmat_d(tg3.ptr(dev(q)), 33, tg3.ptr(mat), None))
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(mat.cpu().numpy(), O.rotmat(q).reshape(-1, 9), rtol=0, atol=1e-15)
+
+    iCol, iRow, K = small["iCol"], small["iRow"], len(small["iCol"])
+    t = rng.uniform(-8, 8, (7, 2))
+    out = torch.empty((7, K, 2), dtype=torch.float32, device=DEV)
+    tg3.check(tg3.lib().tg3_translate_d(tg3.ptr(dev(t)), 7, small["box"], tg3.ptr(dev(iCol)),
+                                        tg3.ptr(dev(iRow)), K, tg3.ptr(out), None))
+    torch.cuda.synchronize()
+    S = out.cpu().numpy().astype(np.float64)
+    S = S[..., 0] + 1j * S[..., 1]
+    np.testing.assert_allclose(S, O.translate(f32(t), small["box"], iCol, iRow), atol=2e-6)
+
+    attr = synth.ctf_attrs(rng, 4)
+    cout = torch.empty((4, K), dtype=torch.float32, device=DEV)
+    tg3.check(tg3.lib().tg3_ctf_d(tg3.ptr(dev(attr, torch.float32)), 4, small["px"], small["box"],
+                                  tg3.ptr(dev(iCol)), tg3.ptr(dev(iRow)), K, tg3.ptr(cout), None))
+    torch.cuda.synchronize()
+    ref = O.ctf(f32(attr), small["px"], small["box"], iCol, iRow)
+    np.testing.assert_allclose(cout.cpu().numpy(), ref, atol=5e-4)
+
+
+def test_project(small, ctx):
+    rng = small["rng"]
+    q = synth.haar_quaternions(rng, 64)
+    mat = O.rotmat(q).reshape(-1, 9)
+    K = len(small["iCol"])
+    out = torch.empty((64, K, 2), dtype=torch.float32, device=DEV)
+    ctx.project(0, dev(mat), 64, out)
+    ctx.sync()
+    P = out.cpu().numpy().astype(np.float64)
+    P = P[..., 0] + 1j * P[..., 1]
+    ref = O.project(small["vol"], mat, small["iCol"], small["iRow"], small["pf"])
+    scale = np.abs(ref).max(axis=1, keepdims=True)
+    assert np.max(np.abs(P - ref) / scale) < 1e-5
+
+
+def test_expect_project_host(small):
+    rng = small["rng"]
+    q = synth.haar_quaternions(rng, 10)
+    mat = np.ascontiguousarray(O.rotmat(q).reshape(-1, 9))
+    K = len(small["iCol"])
+    rotP = np.zeros((10, K), np.complex64)
+    vol = np.ascontiguousarray(small["vol32"])
+    tg3.check(tg3.lib().tg3_ExpectProject(tg3.ptr(vol), tg3.ptr(rotP), tg3.ptr(mat),
+                                          tg3.ptr(np.ascontiguousarray(small["iCol"])),
+                                          tg3.ptr(np.ascontiguousarray(small["iRow"])), 10,
+                                          small["pf"], 1, vol.shape[0], K))
+    ref = O.project(small["vol"], mat, small["iCol"], small["iRow"], small["pf"])
+    assert np.max(np.abs(rotP - ref)) < 1e-5 * np.abs(ref).max()
+
+
+def _local_inputs(small, nP, nR, nT, seed):
+    rng = np.random.default_rng(seed)
+    st = small["st"]
+    K = st.K
+    qs, ts = synth.local_hypotheses(rng, st.quat_true[:nP], st.trans_true[:nP], nR, nT, 200.0, 1.0)
+    pwR = rng.random((nP, nR)) + 0.5
+    pwT = rng.random((nP, nT)) + 0.5
+    pwC = np.ones(nP)
+    return dict(qs=qs, ts=ts, pwR=pwR, pwT=pwT, pwC=pwC, dat=st.dat[:nP].astype(np.complex64),
+                ctf=st.ctf[:nP].astype(np.float32), sig=st.sigRcp[:nP].astype(np.float32), K=K)
+
+
+@pytest.mark.parametrize("precision", [tg3.SCORE_FP32])
+def test_local_phase(small, ctx, precision):
+    nP, nR, nT = 4, 96, 21
+    d = _local_inputs(small, nP, nR, nT, 3)
+    outs = dict(wC=torch.empty(nP, dtype=torch.float64, device=DEV),
+                wR=torch.empty((nP, nR), dtype=torch.float64, device=DEV),
+                wT=torch.empty((nP, nT), dtype=torch.float64, device=DEV),
+                base=torch.empty(nP, dtype=torch.float64, device=DEV),
+                dvp=torch.empty((nP, nR, nT), dtype=torch.float32, device=DEV))
+    ctx.local_phase(nP, nR, nT, dev(d["dat"]), dev(d["ctf"]), dev(d["sig"]), dev(d["qs"]),
+                    dev(d["ts"]), dev(d["pwR"]), dev(d["pwT"]), dev(d["pwC"]), None,
+                    outs["wC"], outs["wR"], outs["wT"], outs["base"], outs["dvp"], precision)
+    ctx.sync()
+    g = {k: v.cpu().numpy() for k, v in outs.items()}
+    for l in range(nP):
+        r = O.score_local(small["vol"], small["pf"], small["iCol"], small["iRow"], small["box"],
+                          f32(d["dat"][l]), f32(d["ctf"][l]), f32(d["sig"][l]), f32(d["qs"][l]),
+                          f32(d["ts"][l]), d["pwR"][l], d["pwT"][l], 1.0)
+        rel = np.abs(g["dvp"][l] - r["dvp"]) / np.abs(r["dvp"])
+        assert rel.max() < 1e-4, rel.max()
+        assert abs(g["base"][l] - r["base"]) / abs(r["base"]) < 1e-4
+        assert np.argmax(g["dvp"][l]) == np.argmax(r["dvp"])
+        # weights relative to each one's own baseline: compare normalised forms
+        gw = g["wR"][l] / g["wR"][l].sum()
+        rw = r["wR"] / r["wR"].sum()
+        assert np.abs(gw - rw).max() < 2e-3
+        gt = g["wT"][l] / g["wT"][l].sum()
+        rt = r["wT"] / r["wT"].sum()
+        assert np.abs(gt - rt).max() < 2e-3
+        # wC against the same baseline shift
+        wc_ref = r["wC"] * np.exp(r["base"] - g["base"][l])
+        assert abs(g["wC"][l] - wc_ref) / wc_ref < 5e-2
+
+
+def test_expect_global3d_two_classes(small):
+    rng = np.random.default_rng(17)
+    st = small["st"]
+    K = st.K
+    nImg, nR, nT, nK = 9, 40, 9, 2
+    q = synth.haar_quaternions(rng, nR)
+    mat = O.rotmat(q).reshape(-1, 9)
+    vols = [small["vol"], f32(small["vol32"] * np.complex64(0.8))]
+    trans = synth.global_translations(1, 1.0)
+    traP = O.translate(f32(trans), small["box"], small["iCol"], small["iRow"]).astype(np.complex64)
+    pR = rng.random(nR)
+    pT = rng.random(nT)
+    dat = st.dat[:nImg].astype(np.complex64)
+    ctf = st.ctf[:nImg].astype(np.float32)
+    sig = st.sigRcp[:nImg].astype(np.float32)
+    wC = np.zeros(nImg * nK, np.float32)
+    wR = np.zeros(nImg * nK * nR, np.float32)
+    wT = np.zeros(nImg * nK * nT, np.float32)
+    bL = np.zeros(nImg, np.float32)
+    state = None
+    for k in range(nK):
+        rotP = O.project(vols[k], mat, small["iCol"], small["iRow"], small["pf"]).astype(np.complex64)
+        tg3.check(tg3.lib().tg3_ExpectGlobal3D(
+            tg3.ptr(rotP), tg3.ptr(traP), tg3.ptr(dat), tg3.ptr(ctf), tg3.ptr(sig), tg3.ptr(wC),
+            tg3.ptr(wR), tg3.ptr(wT), tg3.ptr(pR), tg3.ptr(pT), tg3.ptr(bL), k, nK, nR, nT, K,
+            nImg))
+        state = O.score_global(f32(rotP), f32(traP), f32(dat), f32(ctf), f32(sig), pR, pT, k, nK,
+                               state=None if state is None else (state["wC"], state["wR"],
+                                                                 state["wT"], state["baseL"]),
+                               want_dvp=False)
+    assert np.abs(bL - state["baseL"]).max() / np.abs(state["baseL"]).max() < 1e-4
+    for l in range(nImg):
+        shift = np.exp(state["baseL"][l] - bL[l])
+        a = wC[l * nK:(l + 1) * nK]
+        b = state["wC"][l * nK:(l + 1) * nK] * shift
+        np.testing.assert_allclose(a / a.sum(), b / b.sum(), atol=2e-3)
+        a = wR[l * nK * nR:(l + 1) * nK * nR]
+        b = state["wR"][l * nK * nR:(l + 1) * nK * nR] * shift
+        np.testing.assert_allclose(a / a.sum(), b / b.sum(), atol=2e-3)
+
+
+@pytest.mark.parametrize("n,n_out,peak", [(1000, 1000, np.nan), (777, 500, 0.05), (50, 80, 0.0)])
+def test_resample_bit_exact(n, n_out, peak):
+    rng = np.random.default_rng(n)
+    nP = 6
+    u = np.exp(3 * rng.standard_normal((nP, n)))
+    u[:, rng.integers(0, n, 5)] = 0.0
+    w = rng.random((nP, n))
+    perm = np.stack([rng.permutation(n) for _ in range(nP)]).astype(np.int32)
+    u0 = rng.random(nP) / n_out
+    peaks = np.full(nP, peak)
+    src = np.zeros((nP, n_out), np.int32)
+    wout = np.zeros((nP, n_out))
+    top = np.zeros(nP, np.int32)
+    tg3.check(tg3.lib().tg3_resample(nP, n, tg3.ptr(u), tg3.ptr(w), tg3.ptr(perm), tg3.ptr(u0),
+                                     tg3.ptr(peaks), n_out, tg3.ptr(src), tg3.ptr(wout),
+                                     tg3.ptr(top)))
+    for b in range(nP):
+        pf = O.peak_factor_r(u[b]) if np.isnan(peak) else peak
+        s_ref, w_ref, top_ref = O.resample(u[b], w[b], perm[b], u0[b], pf, n_out)
+        assert np.array_equal(src[b], s_ref)
+        assert np.array_equal(wout[b], w_ref)
+        assert top[b] == top_ref
+
+
+def test_resample_rejects_bad_permutation():
+    n = 10
+    u = np.ones(n)
+    w = np.ones(n)
+    perm = np.arange(n, dtype=np.int32)
+    perm[3] = 99
+    u0 = np.array([0.01])
+    src = np.zeros(n, np.int32)
+    wout = np.zeros(n)
+    top = np.zeros(1, np.int32)
+    st = tg3.lib().tg3_resample(1, n, tg3.ptr(u), tg3.ptr(w), tg3.ptr(perm), tg3.ptr(u0), None,
+                                n, tg3.ptr(src), tg3.ptr(wout), tg3.ptr(top))
+    assert st == tg3.ERR_ARG
+
+
+def _fsc_ok(F, Fr, vdim, lo=0.999):
+    f = O.fsc(F, Fr, vdim, vdim // 2)
+    # shells that hold inserted data (the cutoff times pf)
+    return f
+
+
+@pytest.mark.parametrize("kernel", [tg3.KERNEL_MKB, tg3.KERNEL_TRILINEAR])
+def test_insert(small, kernel):
+    rng = np.random.default_rng(23)
+    st = small["st"]
+    K, pf, box = st.K, small["pf"], small["box"]
+    vdim = pf * box
+    nP = 12
+    q = synth.haar_quaternions(rng, nP)
+    t = rng.uniform(-2, 2, (nP, 2))
+    off = rng.uniform(-0.5, 0.5, (nP, 2))
+    w = rng.uniform(0.5, 1.5, nP).astype(np.float32)
+    dat = st.dat[:nP].astype(np.complex64)
+    ctf = st.ctf[:nP].astype(np.float32)
+    c = tg3.Context(0)
+    try:
+        c.set_pixels(small["iCol"], small["iRow"], box)
+        c.insert_begin(vdim, pf)
+        O3D = torch.zeros(3, dtype=torch.float64, device=DEV)
+        cnt = torch.zeros(1, dtype=torch.int32, device=DEV)
+        c.insert(nP, dev(dat), dev(ctf), dev(q), dev(t), dev(off), dev(w), kernel, O3D, cnt)
+        F = torch.empty((vdim, vdim, vdim // 2 + 1, 2), dtype=torch.float32, device=DEV)
+        T = torch.empty((vdim, vdim, vdim // 2 + 1), dtype=torch.float32, device=DEV)
+        c.insert_read(F, T)
+        c.sync()
+        Fg = F.cpu().numpy().astype(np.float64)
+        Fg = Fg[..., 0] + 1j * Fg[..., 1]
+        Tg = T.cpu().numpy().astype(np.float64)
+        assert int(cnt.item()) == nP
+    finally:
+        c.close()
+    Fr = np.zeros((vdim, vdim, vdim // 2 + 1), np.complex128)
+    Tr = np.zeros(Fr.shape)
+    tab = O.mkb_table(1.9, 15.0, (pf * 1.9) ** 2, 100000)
+    mats = O.rotmat(q)
+    Or = np.zeros(3)
+    for l in range(nP):
+        tt = f32(t[l]) - f32(off[l])
+        img = O.translate_image(f32(dat[l]), -tt[0], -tt[1], box, small["iCol"], small["iRow"])
+        O.insert(Fr, Tr, img, f32(ctf[l]), mats[l], float(w[l]), small["iCol"] * pf,
+                 small["iRow"] * pf, kernel, pf * 1.9, tab, (pf * 1.9) ** 2)
+        Or -= mats[l] @ np.array([t[l, 0] - off[l, 0], t[l, 1] - off[l, 1], 0.0])
+    np.testing.assert_allclose(O3D.cpu().numpy(), Or, rtol=1e-9, atol=1e-9)
+    # volume agreement: relative error and FSC over the shells that hold data
+    scale = np.abs(Fr).max()
+    assert np.abs(Fg - Fr).max() < 2e-4 * scale
+    assert np.abs(Tg - Tr).max() < 2e-4 * np.abs(Tr).max()
+    rmax = int(12 * pf)
+    f = O.fsc(Fg, Fr, vdim, rmax)
+    assert f[1:].min() >= 0.999, f
+
+
+def test_insertft_host(small):
+    rng = np.random.default_rng(29)
+    st = small["st"]
+    K, pf, box = st.K, small["pf"], small["box"]
+    vdim = pf * box
+    nImg, mReco = 5, 3
+    quats = synth.haar_quaternions(rng, nImg * mReco)
+    trans = rng.uniform(-2, 2, (nImg * mReco, 2))
+    offS = rng.uniform(-0.5, 0.5, (nImg, 2))
+    w = (np.ones(nImg) / mReco).astype(np.float32)
+    F = np.zeros((vdim, vdim, vdim // 2 + 1), np.complex64)
+    F[1, 2, 3] = 1 + 2j       # accumulated into, not overwritten
+    T = np.zeros((vdim, vdim, vdim // 2 + 1), np.float32)
+    O3D = np.zeros(3)
+    counter = np.zeros(1, np.int32)
+    dat = np.ascontiguousarray(st.dat[:nImg].astype(np.complex64))
+    ctf = np.ascontiguousarray(st.ctf[:nImg].astype(np.float32))
+    sig = np.ascontiguousarray(st.sigRcp[:nImg].astype(np.float32))
+    tg3.check(tg3.lib().tg3_InsertFT(
+        tg3.ptr(F), tg3.ptr(T), tg3.ptr(O3D), tg3.ptr(counter), tg3.ptr(dat), tg3.ptr(ctf),
+        tg3.ptr(sig), None, tg3.ptr(offS), tg3.ptr(w), tg3.ptr(quats), tg3.ptr(trans), None,
+        tg3.ptr(np.ascontiguousarray(small["iCol"])), tg3.ptr(np.ascontiguousarray(small["iRow"])),
+        small["px"], 0, pf, K, mReco, box, vdim, nImg, tg3.KERNEL_TRILINEAR))
+    assert counter[0] == nImg * mReco
+    Fr = np.zeros(F.shape, np.complex128)
+    Fr[1, 2, 3] = 1 + 2j
+    Tr = np.zeros(T.shape)
+    tab = O.mkb_table(1.9, 15.0, (pf * 1.9) ** 2, 100000)
+    mats = O.rotmat(quats)
+    for l in range(nImg):
+        for m in range(mReco):
+            d = l * mReco + m
+            tt = f32(trans[d]) - f32(offS[l])
+            img = O.translate_image(f32(dat[l]), -tt[0], -tt[1], box, small["iCol"], small["iRow"])
+            O.insert(Fr, Tr, img, f32(ctf[l]), mats[d], float(w[l]), small["iCol"] * pf,
+                     small["iRow"] * pf, 0, pf * 1.9, tab, (pf * 1.9) ** 2)
+    assert np.abs(F - Fr).max() < 2e-4 * np.abs(Fr).max()
+    assert np.abs(T - Tr).max() < 2e-4 * np.abs(Tr).max()
+
+
+def test_expect_local3d_host(small):
+    st = small["st"]
+    d = _local_inputs(small, 1, 64, 16, 31)
+    vol = np.ascontiguousarray(small["vol32"])
+    h = tg3.ctypes.c_void_p()
+    tg3.check(tg3.lib().tg3_volume_create(tg3.ctypes.byref(h), tg3.ptr(vol), vol.shape[0],
+                                          small["pf"]))
+    try:
+        wC = np.zeros(1, np.float32)
+        wR = np.zeros(64, np.float32)
+        wT = np.zeros(16, np.float32)
+        dvp = np.zeros((64, 16), np.float32)
+        bl = np.zeros(1, np.float32)
+        q = np.ascontiguousarray(d["qs"][0])
+        t = np.ascontiguousarray(d["ts"][0])
+        tg3.check(tg3.lib().tg3_ExpectLocal3D(
+            h, tg3.ptr(np.ascontiguousarray(d["dat"][0])), tg3.ptr(np.ascontiguousarray(d["ctf"][0])),
+            tg3.ptr(np.ascontiguousarray(d["sig"][0])), tg3.ptr(np.ascontiguousarray(small["iCol"])),
+            tg3.ptr(np.ascontiguousarray(small["iRow"])), st.K, small["box"], tg3.ptr(q), 64,
+            tg3.ptr(t), 16, tg3.ptr(np.ascontiguousarray(d["pwR"][0])),
+            tg3.ptr(np.ascontiguousarray(d["pwT"][0])), 1.0, tg3.ptr(wC), tg3.ptr(wR), tg3.ptr(wT),
+            tg3.ptr(dvp), tg3.ptr(bl)))
+    finally:
+        tg3.lib().tg3_volume_destroy(h)
+    r = O.score_local(small["vol"], small["pf"], small["iCol"], small["iRow"], small["box"],
+                      f32(d["dat"][0]), f32(d["ctf"][0]), f32(d["sig"][0]), f32(q), f32(t),
+                      d["pwR"][0], d["pwT"][0], 1.0)
+    assert (np.abs(dvp - r["dvp"]) / np.abs(r["dvp"])).max() < 1e-4
+    np.testing.assert_allclose(wR / wR.sum(), r["wR"] / r["wR"].sum(), atol=2e-3)
+
+
+def test_bad_geometry_rejected(small):
+    c = tg3.Context(0)
+    try:
+        c.set_volume(0, torch.as_tensor(small["vol32"]).to(DEV), small["pf"])
+        # a pixel at the image edge cannot be sampled from this volume with margin
+        big = np.array([0, 16], np.int32)
+        c.set_pixels(big, np.array([16, 0], np.int32), small["box"])
+        out = torch.empty((1, 2, 2), dtype=torch.float32, device=DEV)
+        with pytest.raises(tg3.TG3Error) as e:
+            c.project(0, dev(np.eye(3).reshape(1, 9)), 1, out)
+        assert e.value.status == tg3.ERR_ARG
+    finally:
+        c.close()

@@ -1,0 +1,108 @@
+"""CPU-only checks: the C-ABI library loads and exports every declared entry
+point, and the host-side input generation follows the reference's rules."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tg3 import synth
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(tg3_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_lists_entry_points():
+    names = declared_symbols()
+    assert {"tg3_ExpectRotran", "tg3_ExpectProject", "tg3_ExpectGlobal3D", "tg3_InsertFT",
+            "tg3_local_phase_d", "tg3_resample"} <= names
+
+
+def test_library_exports_every_declared_symbol():
+    import ctypes
+    import tg3
+    if not tg3.LIB_PATH.exists():
+        from tg3 import build
+        build.build()
+    lib = ctypes.CDLL(str(tg3.LIB_PATH))
+    names = declared_symbols()
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(tg3.EXPORTS) == names
+    # calls that need no GPU
+    tg3.lib()
+    assert tg3.version().startswith("tg3")
+    assert tg3.lib().tg3_status_string(tg3.ERR_ARG) == b"invalid argument"
+
+
+def test_pixel_index_matches_oracle():
+    for box, px, rU in [(64, 1.5, 16), (256, 1.1, 80), (192, 1.3, 40), (24, 1.0, 7.5)]:
+        rL = synth.config_rL(box, px)
+        a = synth.pixel_index(box, rU, rL)
+        b = O.pixel_index(box, rU, rL)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
+
+def test_pixel_counts_of_the_configurations():
+    # K of each benchmark configuration under the reference's selection rule
+    for box, px, rU, K in [(64, 1.5, 16, 375), (256, 1.1, 80, 9930), (256, 1.1, 120, 22422),
+                           (192, 1.3, 40, 2452), (192, 1.3, 56, 4844), (192, 1.3, 72, 8026),
+                           (192, 1.3, 96, 14324)]:
+        assert len(synth.pixel_index(box, rU, synth.config_rL(box, px))[0]) == K
+
+
+def test_quaternion_matrices_match_oracle():
+    q = synth.haar_quaternions(np.random.default_rng(0), 50)
+    np.testing.assert_allclose(synth.quat_to_mat(q), O.rotmat(q), atol=1e-15)
+    R = synth.quat_to_mat(q)
+    np.testing.assert_allclose(R @ R.transpose(0, 2, 1), np.broadcast_to(np.eye(3), R.shape),
+                               atol=1e-12)
+
+
+def test_global_rotation_grid():
+    hp = synth.healpix_ring_centres(4)
+    assert hp.shape == (192, 2)
+    z = np.cos(hp[:, 0])
+    # equal-area pixels: the z histogram of centres is symmetric
+    np.testing.assert_allclose(np.sort(z), -np.sort(z)[::-1], atol=1e-12)
+    q = synth.global_rotations(4, 36)
+    assert q.shape == (6912, 4)
+    np.testing.assert_allclose(np.linalg.norm(q, axis=1), 1, atol=1e-12)
+    assert len(synth.global_translations(3, 1.0)) == 49
+
+
+def test_vmf_concentration():
+    rng = np.random.default_rng(1)
+    mean = synth.haar_quaternions(rng, 1)[0]
+    s = synth.vmf_quaternions(rng, mean, 200.0, 4000)
+    c = np.abs(s @ mean)
+    # E[1 - mu.x] ~ (p - 1) / (2 kappa) for large kappa on S^3
+    assert abs(np.mean(1 - c) - 3 / 400) < 1e-3
+
+
+def test_ctf_vectorised_matches_oracle():
+    rng = np.random.default_rng(2)
+    iCol, iRow, _, _ = synth.pixel_index(64, 16, 0)
+    attr = synth.ctf_attrs(rng, 5)
+    np.testing.assert_allclose(synth.ctf_values(attr, 1.5, 64, iCol, iRow),
+                               O.ctf(attr, 1.5, 64, iCol, iRow), atol=1e-12)
+
+
+def test_blob_volume_is_hermitian_on_x0_plane():
+    rng = np.random.default_rng(3)
+    bm = synth.blob_map(rng, 5, (2.0, 4.0), 1.5, 5.0)
+    v = synth.padded_volume(bm, 16, 2).numpy()
+    n = v.shape[0]
+    for y in range(1, n // 2):
+        for z in range(1, n // 2):
+            assert np.isclose(v[z, y, 0], np.conj(v[n - z, n - y, 0]), atol=1e-10)

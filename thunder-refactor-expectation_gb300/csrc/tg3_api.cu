@@ -1,0 +1,1065 @@
+// tg3_api.cu -- the extern "C" boundary of libtg3.so (include/thunder_gb300.h).
+//
+// Host orchestration only: argument checks, workspace management, staging of
+// host buffers, and the kernel sequences of the E-step and the insertion.
+// Every failure returns a status and records a message; nothing falls back to
+// host computation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "tg3_internal.cuh"
+
+namespace tg3 {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+int fail(int status, const std::string& msg)
+{
+    g_err = msg;
+    return status;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? TG3_ERR_ALLOC : TG3_ERR_CUDA;
+}
+
+void* ws_get(tg3_ctx* c, WsSlot s, size_t bytes, int* status)
+{
+    Buffer& b = c->ws[s];
+    if (bytes == 0) bytes = 256;
+    if (b.bytes < bytes) {
+        if (b.ptr) {
+            cudaStreamSynchronize(c->stream);
+            cudaFree(b.ptr);
+            b.ptr = nullptr;
+            b.bytes = 0;
+        }
+        size_t want = round_up(bytes + bytes / 8, (size_t)2 << 20);
+        cudaError_t e = cudaMalloc(&b.ptr, want);
+        if (e != cudaSuccess) {
+            b.ptr = nullptr;
+            *status = cuda_fail(e, "workspace allocation");
+            return nullptr;
+        }
+        b.bytes = want;
+    }
+    *status = TG3_OK;
+    return b.ptr;
+}
+
+// ---------------------------------------------------------- stage timing --
+static cudaEvent_t take_event(tg3_ctx* c)
+{
+    if (!c->eventPool.empty()) {
+        cudaEvent_t e = c->eventPool.back();
+        c->eventPool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+}
+
+StageTimer::StageTimer(tg3_ctx* c_, int s) : c(c_), stage(s)
+{
+    if (!c->timing) return;
+    a = take_event(c);
+    b = take_event(c);
+    if (a) cudaEventRecord(a, c->stream);
+}
+
+StageTimer::~StageTimer()
+{
+    if (!c->timing || !a || !b) return;
+    cudaEventRecord(b, c->stream);
+    c->pending[stage].emplace_back(a, b);
+}
+
+static void collect_times(tg3_ctx* c)
+{
+    for (int s = 0; s < TG3_STAGE_COUNT; s++) {
+        for (auto& pr : c->pending[s]) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) {
+                c->stageMs[s] += ms;
+                c->stageLaunches[s] += 1;
+            }
+            c->eventPool.push_back(pr.first);
+            c->eventPool.push_back(pr.second);
+        }
+        c->pending[s].clear();
+    }
+}
+
+// ------------------------------------------------------------- MKB table --
+// I0 from its power series sum_k ((x/2)^k / k!)^2 (Abramowitz & Stegun
+// 9.6.10); MKB_FT_R2 order 0 (src/Functions/Functions.cpp:108-126) tabulated
+// on n + 1 uniform r^2 points over [0, b] (TabFunction::init,
+// src/TabFunction.cpp:25-39).
+static double bessel_i0(double x)
+{
+    double q = 0.25 * x * x, term = 1, sum = 1;
+    for (int k = 1; k < 200; k++) {
+        term *= q / ((double)k * k);
+        sum += term;
+        if (term < sum * 1e-17) break;
+    }
+    return sum;
+}
+
+static void mkb_table(double a, double alpha, double b, int n, std::vector<float>& tab,
+                      int& nz)
+{
+    const double s = b / n, i0a = bessel_i0(alpha);
+    tab.assign(n + 1, 0.f);
+    nz = 0;
+    for (int i = 0; i <= n; i++) {
+        const double u2 = (i * s) / (a * a);
+        double v = u2 > 1 ? 0.0 : bessel_i0(alpha * std::sqrt(1 - u2)) / i0a;
+        tab[i] = (float)v;
+        if (v != 0.0) nz = i;
+    }
+}
+
+constexpr double kMkbA = 1.9, kMkbAlpha = 15.0;
+constexpr int kMkbN = 100000;
+
+static int check_ctx(tg3_ctx* c)
+{
+    if (!c) return fail(TG3_ERR_ARG, "null context");
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return TG3_OK;
+}
+
+static int check_geometry(tg3_ctx* c, int vdim, int pf)
+{
+    if (c->px.K <= 0) return fail(TG3_ERR_STATE, "pixel list not set");
+    // every rotated pixel must stay strictly inside the stored half volume:
+    // |R v| = |v| < vdim / 2 - 1 keeps all eight corners (and the MKB support)
+    if (c->px.maxRadius * pf + 2.0 > vdim / 2)
+        return fail(TG3_ERR_ARG, "pixel radius " + std::to_string(c->px.maxRadius) +
+                                     " x pf does not fit the volume edge " + std::to_string(vdim));
+    return TG3_OK;
+}
+
+static int sync_and_check(tg3_ctx* c)
+{
+    TG3_CUDA(cudaStreamSynchronize(c->stream));
+    int flag = 0;
+    TG3_CUDA(cudaMemcpy(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+        TG3_CUDA(cudaMemset(c->d_flag, 0, sizeof(int)));
+        if (flag & 1) return fail(TG3_ERR_ARG, "resampling permutation out of range");
+        if (flag & 2) return fail(TG3_ERR_NUMERIC, "resampling weights sum to zero");
+        if (flag & 4) return fail(TG3_ERR_TIMEOUT, "device wait expired");
+        if (flag & 8) return fail(TG3_ERR_STATE, "a particle's class has no volume set");
+        return fail(TG3_ERR_CUDA, "device error flag " + std::to_string(flag));
+    }
+    return TG3_OK;
+}
+
+// Per-device default context used by the reference-shaped entry points.
+static tg3_ctx* default_ctx(int* status)
+{
+    static std::mutex mu;
+    static tg3_ctx* ctxs[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        *status = cuda_fail(e, "cudaGetDevice");
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev < 0 || dev >= 64) {
+        *status = fail(TG3_ERR_ARG, "device ordinal out of range");
+        return nullptr;
+    }
+    if (!ctxs[dev]) {
+        tg3_ctx* c = nullptr;
+        *status = tg3_ctx_create(&c, dev);
+        if (*status != TG3_OK) return nullptr;
+        ctxs[dev] = c;
+    }
+    *status = TG3_OK;
+    return ctxs[dev];
+}
+
+template <class T>
+static int upload(tg3_ctx* c, WsSlot slot, size_t offset_bytes, const T* host, size_t n,
+                  T** dev)
+{
+    int st = TG3_OK;
+    char* base = (char*)ws_get(c, slot, offset_bytes + n * sizeof(T), &st);
+    if (!base) return st;
+    *dev = reinterpret_cast<T*>(base + offset_bytes);
+    if (n) TG3_CUDA(cudaMemcpyAsync(*dev, host, n * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+    return TG3_OK;
+}
+
+// Bump allocator over one workspace slot (host-staged arrays of one call).
+struct Arena {
+    tg3_ctx* c;
+    WsSlot slot;
+    size_t used = 0;
+    std::vector<std::pair<size_t, size_t>> items;
+    Arena(tg3_ctx* c_, WsSlot s) : c(c_), slot(s) {}
+    size_t add(size_t bytes)
+    {
+        size_t off = round_up(used, 256);
+        used = off + bytes;
+        return off;
+    }
+};
+
+}  // namespace tg3
+
+using namespace tg3;
+
+// ===================================================================== misc
+extern "C" const char* tg3_status_string(int s)
+{
+    switch (s) {
+    case TG3_OK: return "ok";
+    case TG3_ERR_ARG: return "invalid argument";
+    case TG3_ERR_CUDA: return "CUDA error";
+    case TG3_ERR_ALLOC: return "allocation failed";
+    case TG3_ERR_STATE: return "call out of order";
+    case TG3_ERR_TIMEOUT: return "device wait expired";
+    case TG3_ERR_NUMERIC: return "numeric failure";
+    case TG3_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+extern "C" const char* tg3_last_error(void) { return g_err.c_str(); }
+
+extern "C" const char* tg3_version(void) { return "tg3 1.0 sm_103a"; }
+
+extern "C" int tg3_getAviDevice(int* gpus, int cap, int* n)
+{
+    if (!n) return fail(TG3_ERR_ARG, "null count");
+    int cnt = 0;
+    TG3_CUDA(cudaGetDeviceCount(&cnt));
+    int k = 0;
+    for (int d = 0; d < cnt; d++) {
+        cudaDeviceProp p;
+        TG3_CUDA(cudaGetDeviceProperties(&p, d));
+        if (p.major >= 10) {
+            if (gpus && k < cap) gpus[k] = d;
+            k++;
+        }
+    }
+    *n = k;
+    return TG3_OK;
+}
+
+// ================================================================== context
+extern "C" int tg3_ctx_create(tg3_ctx** out, int device)
+{
+    if (!out) return fail(TG3_ERR_ARG, "null output");
+    *out = nullptr;
+    TG3_CUDA(cudaSetDevice(device));
+    tg3_ctx* c = new tg3_ctx();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_flag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c->d_flag, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_volTable, sizeof(float4*) * kMaxClasses);
+    if (e == cudaSuccess) e = cudaMemset(c->d_volTable, 0, sizeof(float4*) * kMaxClasses);
+    if (e != cudaSuccess) {
+        int st = cuda_fail(e, "context set-up");
+        tg3_ctx_destroy(c);
+        return st;
+    }
+    *out = c;
+    return TG3_OK;
+}
+
+extern "C" int tg3_ctx_destroy(tg3_ctx* c)
+{
+    if (!c) return TG3_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& v : c->vol) cudaFree(v.pairs);
+    for (auto& b : c->ws) cudaFree(b.ptr);
+    cudaFree(c->px.iCol);
+    cudaFree(c->px.iRow);
+    cudaFree(c->ins.acc);
+    cudaFree(c->ins.tab);
+    cudaFree(c->d_flag);
+    cudaFree(c->d_volTable);
+    for (auto& v : c->pending)
+        for (auto& pr : v) {
+            cudaEventDestroy(pr.first);
+            cudaEventDestroy(pr.second);
+        }
+    for (auto e : c->eventPool) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return TG3_OK;
+}
+
+extern "C" void* tg3_ctx_stream(tg3_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" int tg3_ctx_sync(tg3_ctx* c)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    return sync_and_check(c);
+}
+
+extern "C" size_t tg3_ctx_workspace_bytes(tg3_ctx* c)
+{
+    if (!c) return 0;
+    size_t s = 0;
+    for (auto& b : c->ws) s += b.bytes;
+    return s;
+}
+
+extern "C" int tg3_ctx_set_volume(tg3_ctx* c, int cls, const float* volume, int vdim, int pf,
+                                  int on_device)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (cls < 0 || cls >= kMaxClasses) return fail(TG3_ERR_ARG, "class index out of range");
+    if (!volume || vdim < 4 || (vdim & 1) || pf < 1) return fail(TG3_ERR_ARG, "bad volume");
+    Volume& v = c->vol[cls];
+    const size_t nvox = (size_t)vdim * vdim * (vdim / 2 + 1);
+    const size_t bytes = nvox * sizeof(float4);
+    if (v.bytes != bytes) {
+        TG3_CUDA(cudaStreamSynchronize(c->stream));
+        cudaFree(v.pairs);
+        v.pairs = nullptr;
+        v.bytes = 0;
+        TG3_CUDA(cudaMalloc(&v.pairs, bytes));
+        v.bytes = bytes;
+    }
+    v.vdim = vdim;
+    v.pf = pf;
+    const float2* src = reinterpret_cast<const float2*>(volume);
+    if (!on_device) {
+        float2* tmp = nullptr;
+        st = upload(c, WS_PAIRS_TMP, 0, src, nvox, &tmp);
+        if (st) return st;
+        src = tmp;
+    }
+    TG3_CUDA(launch_volume_pairs(src, vdim, v.pairs, c->stream));
+    float4* table[kMaxClasses];
+    for (int i = 0; i < kMaxClasses; i++) table[i] = c->vol[i].pairs;
+    TG3_CUDA(cudaMemcpyAsync(c->d_volTable, table, sizeof(table), cudaMemcpyHostToDevice,
+                             c->stream));
+    TG3_CUDA(cudaStreamSynchronize(c->stream));
+    return TG3_OK;
+}
+
+extern "C" int tg3_ctx_set_pixels(tg3_ctx* c, const int* iCol, const int* iRow, int K,
+                                  int idim)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (!iCol || !iRow || K <= 0 || idim <= 0) return fail(TG3_ERR_ARG, "bad pixel list");
+    double mr = 0;
+    for (int p = 0; p < K; p++) {
+        if (iCol[p] < 0 || std::abs(iCol[p]) > idim / 2 || std::abs(iRow[p]) > idim / 2)
+            return fail(TG3_ERR_ARG, "pixel outside the half plane of the image");
+        mr = std::max(mr, std::sqrt((double)iCol[p] * iCol[p] + (double)iRow[p] * iRow[p]));
+    }
+    if (c->px.K != K) {
+        TG3_CUDA(cudaStreamSynchronize(c->stream));
+        cudaFree(c->px.iCol);
+        cudaFree(c->px.iRow);
+        c->px.iCol = c->px.iRow = nullptr;
+        TG3_CUDA(cudaMalloc(&c->px.iCol, sizeof(int) * K));
+        TG3_CUDA(cudaMalloc(&c->px.iRow, sizeof(int) * K));
+    }
+    TG3_CUDA(cudaMemcpyAsync(c->px.iCol, iCol, sizeof(int) * K, cudaMemcpyHostToDevice, c->stream));
+    TG3_CUDA(cudaMemcpyAsync(c->px.iRow, iRow, sizeof(int) * K, cudaMemcpyHostToDevice, c->stream));
+    TG3_CUDA(cudaStreamSynchronize(c->stream));
+    c->px.K = K;
+    c->px.Kp = (int)round_up(2 * (size_t)K, 64);
+    c->px.idim = idim;
+    c->px.maxRadius = mr;
+    return TG3_OK;
+}
+
+// ======================================================= batched local phase
+// Sequence per batch: project (+ per-row norm) -> shifted data bank -> cross
+// term GEMM (FP32 CUDA cores or split-bf16 tensor cores) with the norm folded
+// into its epilogue -> marginal weights.
+static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
+                       const float* ctf, const float* sigRcp, const double* quat,
+                       const double* trans, const double* pwR, const double* pwT,
+                       const double* pwC, const int* cls, double* wC, double* wR,
+                       double* wT, double* baseL, float* dvp, int precision)
+{
+    const int K = c->px.K, Kp = c->px.Kp;
+    int st = TG3_OK;
+    // volume of every class used must be set; check class 0 geometry
+    const Volume& v0 = c->vol[0];
+    if (!v0.pairs) return fail(TG3_ERR_STATE, "volume of class 0 not set");
+    for (int k = 1; k < kMaxClasses; k++)
+        if (c->vol[k].pairs && (c->vol[k].vdim != v0.vdim || c->vol[k].pf != v0.pf))
+            return fail(TG3_ERR_ARG, "all class volumes must share one edge and pf");
+    if ((st = check_geometry(c, v0.vdim, v0.pf))) return st;
+    float* P = (float*)ws_get(c, WS_P, sizeof(float) * (size_t)nP * nR * Kp, &st);
+    if (!P) return st;
+    float* A = (float*)ws_get(c, WS_A, sizeof(float) * (size_t)nP * nT * Kp, &st);
+    if (!A) return st;
+    float* D = (float*)ws_get(c, WS_D, sizeof(float) * (size_t)nP * nR * nT, &st);
+    if (!D) return st;
+    float* nrm = (float*)ws_get(c, WS_NRM, sizeof(float) * (size_t)nP * nR, &st);
+    if (!nrm) return st;
+    double* x0 = (double*)ws_get(c, WS_X0, sizeof(double) * (size_t)nP, &st);
+    if (!x0) return st;
+    cudaStream_t s = c->stream;
+    {
+        StageTimer tm(c, TG3_STAGE_PROJECT);
+        TG3_CUDA(launch_project(c->d_volTable, cls, nullptr, v0.vdim, v0.pf, quat, nullptr,
+                                nP * nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, sigRcp, ctf, nrm,
+                                c->d_flag, s));
+    }
+    {
+        StageTimer tm(c, TG3_STAGE_SHIFT);
+        TG3_CUDA(launch_shift_bank(reinterpret_cast<const float2*>(dat), ctf, sigRcp, trans,
+                                   nullptr, nP, nT, c->px.idim, c->px.iCol, c->px.iRow, K, A, Kp,
+                                   s));
+        TG3_CUDA(launch_x0(reinterpret_cast<const float2*>(dat), sigRcp, nP, K, x0, s));
+    }
+    if (precision != TG3_SCORE_FP32 && precision != TG3_SCORE_BF16X3)
+        return fail(TG3_ERR_ARG, "unknown precision");
+    if (precision == TG3_SCORE_BF16X3 && !bf16x3_available())
+        return fail(TG3_ERR_UNSUPPORTED, "split-bf16 tensor-core path not built");
+    void* scratch = nullptr;
+    size_t sb = 0;
+    if (precision == TG3_SCORE_BF16X3) {
+        sb = bf16x3_scratch_bytes(nR, nT, Kp, nP);
+        scratch = ws_get(c, WS_BF16, sb, &st);
+        if (!scratch) return st;
+    }
+    {
+        StageTimer tm(c, TG3_STAGE_CROSS);
+        if (precision == TG3_SCORE_BF16X3)
+            TG3_CUDA(launch_gemm_nt_bf16x3(P, (long long)nR * Kp, Kp, A, (long long)nT * Kp, Kp,
+                                           nR, nT, Kp, nP, D, (long long)nR * nT, nT, nrm, nR,
+                                           -2.0f, scratch, sb, c->d_flag, s));
+        else
+            TG3_CUDA(launch_gemm_nt_fp32(P, (long long)nR * Kp, Kp, A, (long long)nT * Kp, Kp, nR,
+                                         nT, Kp, nP, D, (long long)nR * nT, nT, nrm, nR, -2.0f,
+                                         s));
+    }
+    {
+        StageTimer tm(c, TG3_STAGE_WEIGHTS);
+        TG3_CUDA(launch_weights(D, (long long)nR * nT, nT, nR, nT, 1, nP, nullptr, x0, pwR, nR,
+                                pwT, nT, pwC, wC, wR, wT, baseL, dvp, s));
+    }
+    return TG3_OK;
+}
+
+extern "C" int tg3_local_phase_d(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
+                                 const float* ctf, const float* sigRcp, const double* quat,
+                                 const double* trans, const double* pwR, const double* pwT,
+                                 const double* pwC, const int* cls, double* wC, double* wR,
+                                 double* wT, double* baseL, float* dvp, int precision)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (nP <= 0 || nR <= 0 || nT <= 0 || nT > 2048) return fail(TG3_ERR_ARG, "bad batch shape (nT <= 2048)");
+    if (!dat || !ctf || !sigRcp || !quat || !trans || !pwR || !pwT || !wC || !wR || !wT || !baseL)
+        return fail(TG3_ERR_ARG, "null device pointer");
+    return local_phase(c, nP, nR, nT, dat, ctf, sigRcp, quat, trans, pwR, pwT, pwC, cls, wC, wR,
+                       wT, baseL, dvp, precision);
+}
+
+// ================================================================ resample
+extern "C" int tg3_resample_d(tg3_ctx* c, int nP, int n, const double* u, const double* w,
+                              const int* perm, const double* u0, const double* peak, int nOut,
+                              int* src, double* wOut, int* top)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (nP <= 0 || n <= 0 || nOut <= 0 || n > kMaxResampleN || nOut > kMaxResampleN)
+        return fail(TG3_ERR_ARG, "resample sizes out of range (1.." +
+                                     std::to_string(kMaxResampleN) + ")");
+    if (!u || !w || !perm || !u0 || !src || !wOut || !top) return fail(TG3_ERR_ARG, "null pointer");
+    StageTimer tm(c, TG3_STAGE_RESAMPLE);
+    TG3_CUDA(launch_resample(nP, n, u, w, perm, u0, peak, nOut, src, wOut, top, c->d_flag,
+                             c->stream));
+    return TG3_OK;
+}
+
+extern "C" int tg3_resample(int nP, int n, const double* u, const double* w, const int* perm,
+                            const double* u0, const double* peak, int nOut, int* src,
+                            double* wOut, int* top)
+{
+    int st = TG3_OK;
+    tg3_ctx* c = default_ctx(&st);
+    if (!c) return st;
+    if (nP <= 0 || n <= 0 || nOut <= 0) return fail(TG3_ERR_ARG, "bad sizes");
+    if (!u || !w || !perm || !u0 || !src || !wOut || !top) return fail(TG3_ERR_ARG, "null pointer");
+    Arena ar(c, WS_H2D);
+    const size_t nn = (size_t)nP * n, no = (size_t)nP * nOut;
+    size_t ou = ar.add(nn * 8), ow = ar.add(nn * 8), op = ar.add(nn * 4), o0 = ar.add(nP * 8),
+           opk = ar.add(nP * 8), os = ar.add(no * 4), owo = ar.add(no * 8), ot = ar.add(nP * 4);
+    char* base = (char*)ws_get(c, WS_H2D, ar.used, &st);
+    if (!base) return st;
+    cudaStream_t s = c->stream;
+    TG3_CUDA(cudaMemcpyAsync(base + ou, u, nn * 8, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(base + ow, w, nn * 8, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(base + op, perm, nn * 4, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(base + o0, u0, nP * 8, cudaMemcpyHostToDevice, s));
+    if (peak) TG3_CUDA(cudaMemcpyAsync(base + opk, peak, nP * 8, cudaMemcpyHostToDevice, s));
+    st = tg3_resample_d(c, nP, n, (double*)(base + ou), (double*)(base + ow), (int*)(base + op),
+                        (double*)(base + o0), peak ? (double*)(base + opk) : nullptr, nOut,
+                        (int*)(base + os), (double*)(base + owo), (int*)(base + ot));
+    if (st) return st;
+    if ((st = sync_and_check(c))) return st;
+    TG3_CUDA(cudaMemcpy(src, base + os, no * 4, cudaMemcpyDeviceToHost));
+    TG3_CUDA(cudaMemcpy(wOut, base + owo, no * 8, cudaMemcpyDeviceToHost));
+    TG3_CUDA(cudaMemcpy(top, base + ot, nP * 4, cudaMemcpyDeviceToHost));
+    return TG3_OK;
+}
+
+// =============================================================== insertion
+extern "C" int tg3_ctx_insert_begin(tg3_ctx* c, int vdim, int pf)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (vdim < 4 || (vdim & 1) || pf < 1) return fail(TG3_ERR_ARG, "bad insertion volume");
+    InsertAcc& in = c->ins;
+    const size_t bytes = (size_t)vdim * vdim * (vdim / 2 + 1) * sizeof(float4);
+    if (in.bytes != bytes) {
+        TG3_CUDA(cudaStreamSynchronize(c->stream));
+        cudaFree(in.acc);
+        in.acc = nullptr;
+        in.bytes = 0;
+        TG3_CUDA(cudaMalloc(&in.acc, bytes));
+        in.bytes = bytes;
+    }
+    if (in.pf != pf || !in.tab) {
+        std::vector<float> tab;
+        int nz = 0;
+        const double b = (pf * kMkbA) * (pf * kMkbA);
+        mkb_table(kMkbA, kMkbAlpha, b, kMkbN, tab, nz);
+        TG3_CUDA(cudaStreamSynchronize(c->stream));
+        cudaFree(in.tab);
+        in.tab = nullptr;
+        TG3_CUDA(cudaMalloc(&in.tab, sizeof(float) * (nz + 1)));
+        TG3_CUDA(cudaMemcpy(in.tab, tab.data(), sizeof(float) * (nz + 1), cudaMemcpyHostToDevice));
+        in.tabNz = nz;
+        in.tabInvStep = (float)(kMkbN / b);
+    }
+    in.vdim = vdim;
+    in.pf = pf;
+    TG3_CUDA(cudaMemsetAsync(in.acc, 0, bytes, c->stream));
+    return TG3_OK;
+}
+
+static int insert_draws(tg3_ctx* c, int nDraws, int drawsPerImage, const float* dat,
+                        const float* ctf, const double* quat, const double* trans,
+                        const double* offset, const float* w, int kernel, double* O3D,
+                        int* counter)
+{
+    if (!c->ins.acc) return fail(TG3_ERR_STATE, "insertion volume not begun");
+    if (kernel != TG3_KERNEL_MKB && kernel != TG3_KERNEL_TRILINEAR)
+        return fail(TG3_ERR_ARG, "unknown insertion kernel");
+    int st = check_geometry(c, c->ins.vdim, c->ins.pf);
+    if (st) return st;
+    StageTimer tm(c, TG3_STAGE_INSERT);
+    TG3_CUDA(launch_insert(c->ins.acc, c->ins.vdim, kernel, c->ins.tab, c->ins.tabNz,
+                           c->ins.tabInvStep, nDraws, drawsPerImage,
+                           reinterpret_cast<const float2*>(dat), ctf, quat, trans, offset, w,
+                           c->px.iCol, c->px.iRow, c->px.K, c->ins.pf, c->px.idim, O3D,
+                           counter, c->stream));
+    return TG3_OK;
+}
+
+extern "C" int tg3_insert_d(tg3_ctx* c, int nP, const float* dat, const float* ctf,
+                            const double* quat, const double* trans, const double* offset,
+                            const float* w, int kernel, double* O3D, int* counter)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (nP <= 0 || !dat || !ctf || !quat || !trans || !w) return fail(TG3_ERR_ARG, "bad insert args");
+    return insert_draws(c, nP, 1, dat, ctf, quat, trans, offset, w, kernel, O3D, counter);
+}
+
+extern "C" int tg3_ctx_insert_read_d(tg3_ctx* c, float* F, float* T, int accumulate)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (!c->ins.acc) return fail(TG3_ERR_STATE, "insertion volume not begun");
+    if (!F || !T) return fail(TG3_ERR_ARG, "null output");
+    const size_t n = (size_t)c->ins.vdim * c->ins.vdim * (c->ins.vdim / 2 + 1);
+    TG3_CUDA(launch_acc_read(c->ins.acc, n, reinterpret_cast<float2*>(F), T, accumulate,
+                             c->stream));
+    return TG3_OK;
+}
+
+// ======================================================= kernel-level calls
+extern "C" int tg3_rotmat_d(const double* quat, int n, double* mat, void* stream)
+{
+    if (!quat || !mat || n <= 0) return fail(TG3_ERR_ARG, "bad rotmat args");
+    TG3_CUDA(launch_rotmat(quat, n, mat, (cudaStream_t)stream));
+    return TG3_OK;
+}
+
+extern "C" int tg3_translate_d(const double* trans, int nT, int idim, const int* iCol,
+                               const int* iRow, int K, float* out, void* stream)
+{
+    if (!trans || !iCol || !iRow || !out || nT <= 0 || K <= 0 || idim <= 0)
+        return fail(TG3_ERR_ARG, "bad translate args");
+    TG3_CUDA(launch_translate(trans, nT, idim, iCol, iRow, K, reinterpret_cast<float2*>(out), K,
+                              (cudaStream_t)stream));
+    return TG3_OK;
+}
+
+extern "C" int tg3_ctf_d(const float* attr, int nImg, float pixelSize, int idim,
+                         const int* iCol, const int* iRow, int K, float* out, void* stream)
+{
+    if (!attr || !iCol || !iRow || !out || nImg <= 0 || K <= 0 || pixelSize <= 0)
+        return fail(TG3_ERR_ARG, "bad ctf args");
+    TG3_CUDA(launch_ctf(attr, nImg, pixelSize, idim, iCol, iRow, K, out, (cudaStream_t)stream));
+    return TG3_OK;
+}
+
+extern "C" int tg3_project_d(tg3_ctx* c, int cls, const double* rotMat, int nR, float* out)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].pairs) return fail(TG3_ERR_STATE, "volume not set");
+    if (!rotMat || !out || nR <= 0) return fail(TG3_ERR_ARG, "bad project args");
+    const Volume& v = c->vol[cls];
+    if ((st = check_geometry(c, v.vdim, v.pf))) return st;
+    TG3_CUDA(launch_project(nullptr, nullptr, v.pairs, v.vdim, v.pf, nullptr, rotMat, nR, nR,
+                            c->px.iCol, c->px.iRow, c->px.K, out, 2 * c->px.K, nullptr, nullptr,
+                            nullptr, c->d_flag, c->stream));
+    return TG3_OK;
+}
+
+// ============================================ reference-shaped entry points
+extern "C" int tg3_ExpectRotran(float* traP, const double* trans, const double* rot,
+                                double* rotMat, const int* iCol, const int* iRow, int nR,
+                                int nT, int idim, int npxl)
+{
+    if (!traP || !trans || !rot || !rotMat || !iCol || !iRow || nR <= 0 || nT <= 0 || npxl <= 0 ||
+        idim <= 0)
+        return fail(TG3_ERR_ARG, "bad ExpectRotran args");
+    int st = TG3_OK;
+    tg3_ctx* c = default_ctx(&st);
+    if (!c) return st;
+    Arena ar(c, WS_H2D);
+    size_t ot = ar.add(sizeof(double) * 2 * nT), orr = ar.add(sizeof(double) * 4 * nR),
+           oc = ar.add(sizeof(int) * npxl), orw = ar.add(sizeof(int) * npxl),
+           om = ar.add(sizeof(double) * 9 * nR), otr = ar.add(sizeof(float) * 2 * (size_t)nT * npxl);
+    char* b = (char*)ws_get(c, WS_H2D, ar.used, &st);
+    if (!b) return st;
+    cudaStream_t s = c->stream;
+    TG3_CUDA(cudaMemcpyAsync(b + ot, trans, sizeof(double) * 2 * nT, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + orr, rot, sizeof(double) * 4 * nR, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + oc, iCol, sizeof(int) * npxl, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + orw, iRow, sizeof(int) * npxl, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(launch_translate((double*)(b + ot), nT, idim, (int*)(b + oc), (int*)(b + orw), npxl,
+                              (float2*)(b + otr), npxl, s));
+    TG3_CUDA(launch_rotmat((double*)(b + orr), nR, (double*)(b + om), s));
+    TG3_CUDA(cudaMemcpyAsync(traP, b + otr, sizeof(float) * 2 * (size_t)nT * npxl,
+                             cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(rotMat, b + om, sizeof(double) * 9 * nR, cudaMemcpyDeviceToHost, s));
+    return sync_and_check(c);
+}
+
+extern "C" int tg3_ExpectProject(const float* volume, float* rotP, const double* rotMat,
+                                 const int* iCol, const int* iRow, int nR, int pf, int interp,
+                                 int vdim, int npxl)
+{
+    if (!volume || !rotP || !rotMat || !iCol || !iRow || nR <= 0 || pf < 1 || vdim < 4 || npxl <= 0)
+        return fail(TG3_ERR_ARG, "bad ExpectProject args");
+    if (interp != 1) return fail(TG3_ERR_UNSUPPORTED, "only linear interpolation (interp 1)");
+    int st = TG3_OK;
+    tg3_ctx* c = default_ctx(&st);
+    if (!c) return st;
+    const int slot = kMaxClasses - 1;   // reserved for the reference-shaped calls
+    if ((st = tg3_ctx_set_volume(c, slot, volume, vdim, pf, 0))) return st;
+    if ((st = tg3_ctx_set_pixels(c, iCol, iRow, npxl, vdim / pf))) return st;
+    Arena ar(c, WS_H2D);
+    size_t om = ar.add(sizeof(double) * 9 * nR), oo = ar.add(sizeof(float) * 2 * (size_t)nR * npxl);
+    char* b = (char*)ws_get(c, WS_H2D, ar.used, &st);
+    if (!b) return st;
+    TG3_CUDA(cudaMemcpyAsync(b + om, rotMat, sizeof(double) * 9 * nR, cudaMemcpyHostToDevice,
+                             c->stream));
+    if ((st = tg3_project_d(c, slot, (double*)(b + om), nR, (float*)(b + oo)))) return st;
+    TG3_CUDA(cudaMemcpyAsync(rotP, b + oo, sizeof(float) * 2 * (size_t)nR * npxl,
+                             cudaMemcpyDeviceToHost, c->stream));
+    return sync_and_check(c);
+}
+
+// |P|^2 rows and sigRcp ctf^2 rows for the per-(image, rotation) norm GEMM.
+namespace tg3 {
+__global__ void k_abs2_rows(const float2* __restrict__ in, int K, int rows, float* __restrict__ out,
+                            int ldo)
+{
+    const int r = blockIdx.y;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ldo; p += gridDim.x * blockDim.x) {
+        float v = 0.f;
+        if (p < K) {
+            const float2 a = in[(size_t)r * K + p];
+            v = a.x * a.x + a.y * a.y;
+        }
+        out[(size_t)r * ldo + p] = v;
+    }
+}
+__global__ void k_sc2_rows(const float* __restrict__ sig, const float* __restrict__ ctf, int K,
+                           float* __restrict__ out, int ldo)
+{
+    const int r = blockIdx.y;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ldo; p += gridDim.x * blockDim.x) {
+        float v = 0.f;
+        if (p < K) {
+            const float c = ctf[(size_t)r * K + p];
+            v = sig[(size_t)r * K + p] * c * c;
+        }
+        out[(size_t)r * ldo + p] = v;
+    }
+}
+__global__ void k_pad_rows(const float2* __restrict__ in, int K, float2* __restrict__ out, int ldo2)
+{
+    const int r = blockIdx.y;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ldo2; p += gridDim.x * blockDim.x)
+        out[(size_t)r * ldo2 + p] = p < K ? in[(size_t)r * K + p] : make_float2(0.f, 0.f);
+}
+}  // namespace tg3
+
+extern "C" int tg3_ExpectGlobal3D(const float* rotP, const float* traP, const float* datP,
+                                  const float* ctfP, const float* sigRcpP, float* wC, float* wR,
+                                  float* wT, const double* pR, const double* pT, float* baseL,
+                                  int kIdx, int nK, int nR, int nT, int npxl, int imgNum)
+{
+    if (!rotP || !traP || !datP || !ctfP || !sigRcpP || !wC || !wR || !wT || !pR || !pT || !baseL)
+        return fail(TG3_ERR_ARG, "null pointer");
+    if (nK <= 0 || kIdx < 0 || kIdx >= nK || nR <= 0 || nT <= 0 || npxl <= 0 || imgNum <= 0 ||
+        nT > 4096)
+        return fail(TG3_ERR_ARG, "bad ExpectGlobal3D sizes");
+    int st = TG3_OK;
+    tg3_ctx* c = default_ctx(&st);
+    if (!c) return st;
+    cudaStream_t s = c->stream;
+    const int K = npxl, Kp = (int)round_up(2 * (size_t)K, 64), Kq = (int)round_up(K, 64);
+    // rotation bank, padded rows, and its |P|^2
+    float* P = (float*)ws_get(c, WS_P, sizeof(float) * ((size_t)nR * Kp + (size_t)nR * Kq), &st);
+    if (!P) return st;
+    float* P2 = P + (size_t)nR * Kp;
+    Arena ar(c, WS_H2D);
+    size_t orp = ar.add(sizeof(float) * 2 * (size_t)nR * K), otp = ar.add(sizeof(float) * 2 * (size_t)nT * K),
+           opr = ar.add(sizeof(double) * nR), opt = ar.add(sizeof(double) * nT);
+    const int IB = 1024;   // images per pass
+    const int nb = std::min(imgNum, IB);
+    size_t od = ar.add(sizeof(float) * 2 * (size_t)nb * K), oc = ar.add(sizeof(float) * (size_t)nb * K),
+           os = ar.add(sizeof(float) * (size_t)nb * K), osc = ar.add(sizeof(float) * (size_t)nb * Kq),
+           ox0 = ar.add(sizeof(double) * nb), owc = ar.add(sizeof(double) * nb),
+           owr = ar.add(sizeof(double) * (size_t)nb * nR), owt = ar.add(sizeof(double) * (size_t)nb * nT),
+           obs = ar.add(sizeof(double) * nb), onr = ar.add(sizeof(float) * (size_t)nR * nb),
+           oWC = ar.add(sizeof(float) * (size_t)nb * nK), oWR = ar.add(sizeof(float) * (size_t)nb * nK * nR),
+           oWT = ar.add(sizeof(float) * (size_t)nb * nK * nT), oBL = ar.add(sizeof(float) * nb);
+    char* b = (char*)ws_get(c, WS_H2D, ar.used, &st);
+    if (!b) return st;
+    float* A = (float*)ws_get(c, WS_A, sizeof(float) * (size_t)nb * nT * Kp, &st);
+    if (!A) return st;
+    float* D = (float*)ws_get(c, WS_D, sizeof(float) * (size_t)nR * nb * nT, &st);
+    if (!D) return st;
+    TG3_CUDA(cudaMemcpyAsync(b + orp, rotP, sizeof(float) * 2 * (size_t)nR * K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + otp, traP, sizeof(float) * 2 * (size_t)nT * K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opr, pR, sizeof(double) * nR, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opt, pT, sizeof(double) * nT, cudaMemcpyHostToDevice, s));
+    {
+        dim3 g1((Kp / 2 + 255) / 256, nR);
+        k_pad_rows<<<g1, 256, 0, s>>>((const float2*)(b + orp), K, (float2*)P, Kp / 2);
+        dim3 g2((Kq + 255) / 256, nR);
+        k_abs2_rows<<<g2, 256, 0, s>>>((const float2*)(b + orp), K, nR, P2, Kq);
+        TG3_LAUNCH_CHECK("bank preparation");
+    }
+    for (int l0 = 0; l0 < imgNum; l0 += IB) {
+        const int n = std::min(IB, imgNum - l0);
+        TG3_CUDA(cudaMemcpyAsync(b + od, datP + 2 * (size_t)l0 * K, sizeof(float) * 2 * (size_t)n * K,
+                                 cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + oc, ctfP + (size_t)l0 * K, sizeof(float) * (size_t)n * K,
+                                 cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + os, sigRcpP + (size_t)l0 * K, sizeof(float) * (size_t)n * K,
+                                 cudaMemcpyHostToDevice, s));
+        if (kIdx > 0) {
+            TG3_CUDA(cudaMemcpyAsync(b + oWC, wC + (size_t)l0 * nK, sizeof(float) * (size_t)n * nK,
+                                     cudaMemcpyHostToDevice, s));
+            TG3_CUDA(cudaMemcpyAsync(b + oWR, wR + (size_t)l0 * nK * nR, sizeof(float) * (size_t)n * nK * nR,
+                                     cudaMemcpyHostToDevice, s));
+            TG3_CUDA(cudaMemcpyAsync(b + oWT, wT + (size_t)l0 * nK * nT, sizeof(float) * (size_t)n * nK * nT,
+                                     cudaMemcpyHostToDevice, s));
+            TG3_CUDA(cudaMemcpyAsync(b + oBL, baseL + l0, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+        }
+        const float2* dd = (const float2*)(b + od);
+        const float* cc = (const float*)(b + oc);
+        const float* ss = (const float*)(b + os);
+        TG3_CUDA(launch_shift_bank(dd, cc, ss, nullptr, (const float2*)(b + otp), n, nT, 1, nullptr,
+                                   nullptr, K, A, Kp, s));
+        TG3_CUDA(launch_x0(dd, ss, n, K, (double*)(b + ox0), s));
+        {
+            dim3 g3((Kq + 255) / 256, n);
+            k_sc2_rows<<<g3, 256, 0, s>>>(ss, cc, K, (float*)(b + osc), Kq);
+            TG3_LAUNCH_CHECK("norm operand");
+        }
+        // cross term: D[r][l nT + t] = -2 sum A''[l t] . P[r]
+        TG3_CUDA(launch_gemm_nt_fp32(P, 0, Kp, A, 0, Kp, nR, n * nT, Kp, 1, D, 0, n * nT, nullptr, 0,
+                                     -2.0f, s));
+        // norm term: N[r][l] = sum_p |P_rp|^2 sigRcp_lp ctf_lp^2
+        TG3_CUDA(launch_gemm_nt_fp32(P2, 0, Kq, (const float*)(b + osc), 0, Kq, nR, n, Kq, 1,
+                                     (float*)(b + onr), 0, n, nullptr, 0, 1.0f, s));
+        TG3_CUDA(launch_weights(D, 0, n * nT, nR, nT, n, n, (const float*)(b + onr),
+                                (const double*)(b + ox0), (const double*)(b + opr), 0,
+                                (const double*)(b + opt), 0, nullptr, (double*)(b + owc),
+                                (double*)(b + owr), (double*)(b + owt), (double*)(b + obs), nullptr, s));
+        TG3_CUDA(launch_merge_class(n, nK, kIdx, nR, nT, (const double*)(b + owc),
+                                    (const double*)(b + owr), (const double*)(b + owt),
+                                    (const double*)(b + obs), (float*)(b + oWC), (float*)(b + oWR),
+                                    (float*)(b + oWT), (float*)(b + oBL), s));
+        TG3_CUDA(cudaMemcpyAsync(wC + (size_t)l0 * nK, b + oWC, sizeof(float) * (size_t)n * nK,
+                                 cudaMemcpyDeviceToHost, s));
+        TG3_CUDA(cudaMemcpyAsync(wR + (size_t)l0 * nK * nR, b + oWR, sizeof(float) * (size_t)n * nK * nR,
+                                 cudaMemcpyDeviceToHost, s));
+        TG3_CUDA(cudaMemcpyAsync(wT + (size_t)l0 * nK * nT, b + oWT, sizeof(float) * (size_t)n * nK * nT,
+                                 cudaMemcpyDeviceToHost, s));
+        TG3_CUDA(cudaMemcpyAsync(baseL + l0, b + oBL, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+        if ((st = sync_and_check(c))) return st;
+    }
+    return TG3_OK;
+}
+
+extern "C" int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter, const float* datP,
+                            const float* ctfP, const float* sigRcpP, const float* ctfaData,
+                            const double* offS, const float* w, const double* nR,
+                            const double* nT, const double* nD, const int* iCol, const int* iRow,
+                            float pixelSize, int cSearch, int opf, int npxl, int mReco, int idim,
+                            int dimSize, int imgNum, int kernel)
+{
+    (void)sigRcpP; (void)ctfaData; (void)nD; (void)pixelSize;
+    if (cSearch) return fail(TG3_ERR_UNSUPPORTED, "defocus search insertion (cSearch) not supported");
+    if (!F3D || !T3D || !O3D || !counter || !datP || !ctfP || !offS || !w || !nR || !nT || !iCol ||
+        !iRow)
+        return fail(TG3_ERR_ARG, "null pointer");
+    if (opf < 1 || npxl <= 0 || mReco <= 0 || idim <= 0 || imgNum <= 0 || dimSize != opf * idim)
+        return fail(TG3_ERR_ARG, "bad InsertFT sizes (dimSize must equal opf * idim)");
+    int st = TG3_OK;
+    tg3_ctx* c = default_ctx(&st);
+    if (!c) return st;
+    if ((st = tg3_ctx_set_pixels(c, iCol, iRow, npxl, idim))) return st;
+    if ((st = tg3_ctx_insert_begin(c, dimSize, opf))) return st;
+    cudaStream_t s = c->stream;
+    const size_t nvox = (size_t)dimSize * dimSize * (dimSize / 2 + 1);
+    const int K = npxl;
+    Arena ar(c, WS_H2D);
+    const int IB = 4096;
+    const int nb = std::min(imgNum, IB);
+    size_t od = ar.add(sizeof(float) * 2 * (size_t)nb * K), oc = ar.add(sizeof(float) * (size_t)nb * K),
+           oq = ar.add(sizeof(double) * 4 * (size_t)nb * mReco), ot = ar.add(sizeof(double) * 2 * (size_t)nb * mReco),
+           oo = ar.add(sizeof(double) * 2 * (size_t)nb), ow = ar.add(sizeof(float) * (size_t)nb),
+           oO = ar.add(sizeof(double) * 3), on = ar.add(sizeof(int));
+    char* b = (char*)ws_get(c, WS_H2D, ar.used, &st);
+    if (!b) return st;
+    TG3_CUDA(cudaMemcpyAsync(b + oO, O3D, sizeof(double) * 3, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + on, counter, sizeof(int), cudaMemcpyHostToDevice, s));
+    for (int l0 = 0; l0 < imgNum; l0 += IB) {
+        const int n = std::min(IB, imgNum - l0);
+        TG3_CUDA(cudaMemcpyAsync(b + od, datP + 2 * (size_t)l0 * K, sizeof(float) * 2 * (size_t)n * K,
+                                 cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + oc, ctfP + (size_t)l0 * K, sizeof(float) * (size_t)n * K,
+                                 cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + oq, nR + 4 * (size_t)l0 * mReco, sizeof(double) * 4 * (size_t)n * mReco,
+                                 cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + ot, nT + 2 * (size_t)l0 * mReco, sizeof(double) * 2 * (size_t)n * mReco,
+                                 cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + oo, offS + 2 * (size_t)l0, sizeof(double) * 2 * (size_t)n,
+                                 cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + ow, w + l0, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, s));
+        if ((st = insert_draws(c, n * mReco, mReco, (const float*)(b + od), (const float*)(b + oc),
+                               (const double*)(b + oq), (const double*)(b + ot),
+                               (const double*)(b + oo), (const float*)(b + ow), kernel,
+                               (double*)(b + oO), (int*)(b + on))))
+            return st;
+        // the staging buffer is reused by the next pass
+        TG3_CUDA(cudaStreamSynchronize(s));
+    }
+    // add the accumulator to the caller's volumes
+    float* dF = (float*)ws_get(c, WS_D2H, sizeof(float) * 3 * nvox, &st);
+    if (!dF) return st;
+    float* dT = dF + 2 * nvox;
+    TG3_CUDA(cudaMemcpyAsync(dF, F3D, sizeof(float) * 2 * nvox, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(dT, T3D, sizeof(float) * nvox, cudaMemcpyHostToDevice, s));
+    if ((st = tg3_ctx_insert_read_d(c, dF, dT, 1))) return st;
+    TG3_CUDA(cudaMemcpyAsync(F3D, dF, sizeof(float) * 2 * nvox, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(T3D, dT, sizeof(float) * nvox, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(O3D, b + oO, sizeof(double) * 3, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(counter, b + on, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return sync_and_check(c);
+}
+
+// ====================================================== volume handle + local
+extern "C" int tg3_volume_create(tg3_volume** out, const float* volume, int vdim, int pf)
+{
+    if (!out) return fail(TG3_ERR_ARG, "null output");
+    *out = nullptr;
+    int dev = 0;
+    TG3_CUDA(cudaGetDevice(&dev));
+    tg3_volume* h = new tg3_volume();
+    int st = tg3_ctx_create(&h->ctx, dev);
+    if (st == TG3_OK) st = tg3_ctx_set_volume(h->ctx, 0, volume, vdim, pf, 0);
+    if (st != TG3_OK) {
+        tg3_ctx_destroy(h->ctx);
+        delete h;
+        return st;
+    }
+    *out = h;
+    return TG3_OK;
+}
+
+extern "C" int tg3_volume_destroy(tg3_volume* h)
+{
+    if (!h) return TG3_OK;
+    tg3_ctx_destroy(h->ctx);
+    delete h;
+    return TG3_OK;
+}
+
+extern "C" int tg3_ExpectLocal3D(tg3_volume* h, const float* dat, const float* ctf,
+                                 const float* sigRcp, const int* iCol, const int* iRow, int npxl,
+                                 int idim, const double* rot, int nR, const double* trans, int nT,
+                                 const double* oldR, const double* oldT, double oldC, float* wC,
+                                 float* wR, float* wT, float* dvp, float* baseL)
+{
+    if (!h || !h->ctx) return fail(TG3_ERR_ARG, "null volume handle");
+    if (!dat || !ctf || !sigRcp || !iCol || !iRow || !rot || !trans || !oldR || !oldT || !wC ||
+        !wR || !wT || !baseL || npxl <= 0 || nR <= 0 || nT <= 0)
+        return fail(TG3_ERR_ARG, "bad ExpectLocal3D args");
+    tg3_ctx* c = h->ctx;
+    int st = check_ctx(c);
+    if (st) return st;
+    if (c->px.K != npxl || c->px.idim != idim) {
+        if ((st = tg3_ctx_set_pixels(c, iCol, iRow, npxl, idim))) return st;
+    }
+    cudaStream_t s = c->stream;
+    const int K = npxl;
+    Arena ar(c, WS_H2D);
+    size_t od = ar.add(8 * (size_t)K), oc = ar.add(4 * (size_t)K), os = ar.add(4 * (size_t)K),
+           oq = ar.add(32 * (size_t)nR), ot = ar.add(16 * (size_t)nT), opr = ar.add(8 * (size_t)nR),
+           opt = ar.add(8 * (size_t)nT), opc = ar.add(8), owc = ar.add(8), owr = ar.add(8 * (size_t)nR),
+           owt = ar.add(8 * (size_t)nT), obl = ar.add(8), odv = ar.add(4 * (size_t)nR * nT);
+    char* b = (char*)ws_get(c, WS_H2D, ar.used, &st);
+    if (!b) return st;
+    TG3_CUDA(cudaMemcpyAsync(b + od, dat, 8 * (size_t)K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + oc, ctf, 4 * (size_t)K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + os, sigRcp, 4 * (size_t)K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + oq, rot, 32 * (size_t)nR, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + ot, trans, 16 * (size_t)nT, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opr, oldR, 8 * (size_t)nR, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opt, oldT, 8 * (size_t)nT, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opc, &oldC, 8, cudaMemcpyHostToDevice, s));
+    st = local_phase(c, 1, nR, nT, (float*)(b + od), (float*)(b + oc), (float*)(b + os),
+                     (double*)(b + oq), (double*)(b + ot), (double*)(b + opr), (double*)(b + opt),
+                     (double*)(b + opc), nullptr, (double*)(b + owc), (double*)(b + owr),
+                     (double*)(b + owt), (double*)(b + obl), dvp ? (float*)(b + odv) : nullptr,
+                     TG3_SCORE_FP32);
+    if (st) return st;
+    std::vector<double> hwr(nR), hwt(nT);
+    double hwc = 0, hbl = 0;
+    TG3_CUDA(cudaMemcpyAsync(hwr.data(), b + owr, 8 * (size_t)nR, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(hwt.data(), b + owt, 8 * (size_t)nT, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(&hwc, b + owc, 8, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(&hbl, b + obl, 8, cudaMemcpyDeviceToHost, s));
+    if (dvp) TG3_CUDA(cudaMemcpyAsync(dvp, b + odv, 4 * (size_t)nR * nT, cudaMemcpyDeviceToHost, s));
+    if ((st = sync_and_check(c))) return st;
+    for (int r = 0; r < nR; r++) wR[r] = (float)hwr[r];
+    for (int t = 0; t < nT; t++) wT[t] = (float)hwt[t];
+    *wC = (float)hwc;
+    *baseL = (float)hbl;
+    return TG3_OK;
+}
+
+// ====================================================== host batched phase
+extern "C" int tg3_local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
+                               const float* ctf, const float* sigRcp, const double* quat,
+                               const double* trans, const double* pwR, const double* pwT,
+                               const double* pwC, const int* cls, double* wC, double* wR,
+                               double* wT, double* baseL, float* dvp, int precision)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (nP <= 0 || nR <= 0 || nT <= 0 || nT > 2048) return fail(TG3_ERR_ARG, "bad batch shape (nT <= 2048)");
+    if (!dat || !ctf || !sigRcp || !quat || !trans || !pwR || !pwT || !wC || !wR || !wT || !baseL)
+        return fail(TG3_ERR_ARG, "null host pointer");
+    const size_t K = c->px.K;
+    if (K == 0) return fail(TG3_ERR_STATE, "pixel list not set");
+    Arena ar(c, WS_H2D);
+    const size_t P_ = nP, R_ = nR, T_ = nT;
+    size_t od = ar.add(8 * P_ * K), oc = ar.add(4 * P_ * K), os = ar.add(4 * P_ * K),
+           oq = ar.add(32 * P_ * R_), ot = ar.add(16 * P_ * T_), opr = ar.add(8 * P_ * R_),
+           opt = ar.add(8 * P_ * T_), opc = ar.add(8 * P_), ocl = ar.add(4 * P_),
+           owc = ar.add(8 * P_), owr = ar.add(8 * P_ * R_), owt = ar.add(8 * P_ * T_),
+           obl = ar.add(8 * P_), odv = ar.add(dvp ? 4 * P_ * R_ * T_ : 0);
+    char* b = (char*)ws_get(c, WS_H2D, ar.used, &st);
+    if (!b) return st;
+    cudaStream_t s = c->stream;
+    TG3_CUDA(cudaMemcpyAsync(b + od, dat, 8 * P_ * K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + oc, ctf, 4 * P_ * K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + os, sigRcp, 4 * P_ * K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + oq, quat, 32 * P_ * R_, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + ot, trans, 16 * P_ * T_, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opr, pwR, 8 * P_ * R_, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opt, pwT, 8 * P_ * T_, cudaMemcpyHostToDevice, s));
+    if (pwC) TG3_CUDA(cudaMemcpyAsync(b + opc, pwC, 8 * P_, cudaMemcpyHostToDevice, s));
+    if (cls) TG3_CUDA(cudaMemcpyAsync(b + ocl, cls, 4 * P_, cudaMemcpyHostToDevice, s));
+    st = local_phase(c, nP, nR, nT, (float*)(b + od), (float*)(b + oc), (float*)(b + os),
+                     (double*)(b + oq), (double*)(b + ot), (double*)(b + opr), (double*)(b + opt),
+                     pwC ? (double*)(b + opc) : nullptr, cls ? (int*)(b + ocl) : nullptr,
+                     (double*)(b + owc), (double*)(b + owr), (double*)(b + owt),
+                     (double*)(b + obl), dvp ? (float*)(b + odv) : nullptr, precision);
+    if (st) return st;
+    TG3_CUDA(cudaMemcpyAsync(wC, b + owc, 8 * P_, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(wR, b + owr, 8 * P_ * R_, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(wT, b + owt, 8 * P_ * T_, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(baseL, b + obl, 8 * P_, cudaMemcpyDeviceToHost, s));
+    if (dvp) TG3_CUDA(cudaMemcpyAsync(dvp, b + odv, 4 * P_ * R_ * T_, cudaMemcpyDeviceToHost, s));
+    return sync_and_check(c);
+}
+
+// ============================================================ stage timing
+extern "C" int tg3_ctx_set_timing(tg3_ctx* c, int enable)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    c->timing = enable != 0;
+    return TG3_OK;
+}
+
+extern "C" int tg3_ctx_stage_times(tg3_ctx* c, double* ms, int* launches, int reset)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    TG3_CUDA(cudaStreamSynchronize(c->stream));
+    collect_times(c);
+    for (int i = 0; i < TG3_STAGE_COUNT; i++) {
+        if (ms) ms[i] = c->stageMs[i];
+        if (launches) launches[i] = c->stageLaunches[i];
+        if (reset) {
+            c->stageMs[i] = 0;
+            c->stageLaunches[i] = 0;
+        }
+    }
+    return TG3_OK;
+}

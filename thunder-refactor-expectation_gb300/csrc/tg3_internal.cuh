@@ -1,0 +1,199 @@
+// tg3_internal.cuh -- shared declarations of the GB300 E-step library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "thunder_gb300.h"
+
+namespace tg3 {
+
+constexpr int kMaxClasses = 16;
+constexpr int kMaxResampleN = 4096;   // particle-set size held in shared memory
+
+// ---------------------------------------------------------------- errors --
+void set_error(const std::string& msg);
+int fail(int status, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define TG3_CUDA(call)                                                   \
+    do {                                                                 \
+        cudaError_t e_ = (call);                                         \
+        if (e_ != cudaSuccess) return ::tg3::cuda_fail(e_, #call);       \
+    } while (0)
+
+#define TG3_LAUNCH_CHECK(what)                                           \
+    do {                                                                 \
+        cudaError_t e_ = cudaGetLastError();                             \
+        if (e_ != cudaSuccess) return ::tg3::cuda_fail(e_, what);        \
+    } while (0)
+
+inline size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+
+// ------------------------------------------------------------- workspace --
+// Grow-only named device buffers of a context.
+enum WsSlot {
+    WS_P = 0,        // projections  [rows][Kp] floats
+    WS_A,            // shifted, weighted data [nP][nT][Kp]
+    WS_D,            // hypothesis-dependent log-likelihood part [nP][nR][nT]
+    WS_NRM,          // sum sigRcp ctf^2 |P|^2 per projected row
+    WS_X0,           // sum sigRcp |X|^2 per particle (double)
+    WS_PAIRS_TMP,
+    WS_H2D,          // staging of host inputs
+    WS_D2H,
+    WS_BF16,         // split-bf16 operand planes
+    WS_MISC,
+    WS_COUNT
+};
+
+struct Buffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct Volume {
+    float4* pairs = nullptr;   // [vdim][vdim][nx] of (V[x], V[x+1])
+    int vdim = 0;
+    int pf = 0;
+    size_t bytes = 0;
+};
+
+struct Pixels {
+    int* iCol = nullptr;
+    int* iRow = nullptr;
+    int K = 0;
+    int Kp = 0;        // floats per padded complex row (multiple of 64)
+    int idim = 0;
+    double maxRadius = 0;
+};
+
+struct InsertAcc {
+    float4* acc = nullptr;     // [vdim][vdim][nx] of (F.re, F.im, T, 0)
+    int vdim = 0;
+    int pf = 0;
+    size_t bytes = 0;
+    float* tab = nullptr;      // MKB table, nonzero part
+    int tabNz = 0;             // last index with a nonzero value
+    float tabInvStep = 0;      // n / b
+};
+
+}  // namespace tg3
+
+struct tg3_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    tg3::Volume vol[tg3::kMaxClasses];
+    float4** d_volTable = nullptr;   // device copy of the class -> pairs table
+    tg3::Pixels px;
+    tg3::InsertAcc ins;
+    tg3::Buffer ws[tg3::WS_COUNT];
+    int* d_flag = nullptr;           // device error word
+    // per-stage event timing (tg3_ctx_set_timing)
+    bool timing = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[TG3_STAGE_COUNT];
+    std::vector<cudaEvent_t> eventPool;
+    double stageMs[TG3_STAGE_COUNT] = {};
+    int stageLaunches[TG3_STAGE_COUNT] = {};
+};
+
+namespace tg3 {
+// Brackets one stage's launches with events when timing is enabled.
+struct StageTimer {
+    tg3_ctx* c;
+    int stage;
+    cudaEvent_t a = nullptr, b = nullptr;
+    StageTimer(tg3_ctx* c_, int s);
+    ~StageTimer();
+};
+}  // namespace tg3
+
+struct tg3_volume {
+    tg3_ctx* ctx = nullptr;
+};
+
+namespace tg3 {
+
+void* ws_get(tg3_ctx* c, WsSlot s, size_t bytes, int* status);
+
+// ---------------------------------------------------------- kernel calls --
+// All launchers return cudaError_t of the launch (no synchronisation).
+cudaError_t launch_rotmat(const double* quat, int n, double* mat, cudaStream_t st);
+cudaError_t launch_translate(const double* trans, int nT, int idim, const int* iCol,
+                             const int* iRow, int K, float2* out, int ldo2,
+                             cudaStream_t st);
+cudaError_t launch_ctf(const float* attr, int nImg, float px, int idim,
+                       const int* iCol, const int* iRow, int K, float* out,
+                       cudaStream_t st);
+cudaError_t launch_volume_pairs(const float2* vol, int vdim, float4* pairs,
+                                cudaStream_t st);
+// rows: projected rows; a row r belongs to particle r / rowsPerParticle.
+// Exactly one of quat [rows][4] / mat [rows][9] is non-null.
+cudaError_t launch_project(float4* const* volTable, const int* cls,
+                           const float4* vol, int vdim, int pf,
+                           const double* quat, const double* mat, int rows,
+                           int rowsPerParticle, const int* iCol,
+                           const int* iRow, int K, float* out, int ldo,
+                           const float* sigRcp, const float* ctf, float* nrm, int* flag,
+                           cudaStream_t st);
+// Either trans [nP][nT][2] or a shared phase bank [nT][K] complex.
+cudaError_t launch_shift_bank(const float2* dat, const float* ctf,
+                              const float* sigRcp, const double* trans,
+                              const float2* bank,
+                              int nP, int nT, int idim, const int* iCol,
+                              const int* iRow, int K, float* out, int ldo,
+                              cudaStream_t st);
+cudaError_t launch_x0(const float2* dat, const float* sigRcp, int nP, int K,
+                      double* x0, cudaStream_t st);
+// C[b][i][j] = alpha * sum_k A[b][i][k] B[b][j][k] + nrm[b][i]   (FP32)
+cudaError_t launch_gemm_nt_fp32(const float* A, long long sA, int lda,
+                                const float* B, long long sB, int ldb,
+                                int M, int N, int Kd, int batch, float* C,
+                                long long sC, int ldc, const float* nrm,
+                                long long sN, float alpha, cudaStream_t st);
+// nrmG (optional) adds a per-(rotation, group) term nrmG[r G + g].
+cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR,
+                           int nT, int G, int nBlocks, const float* nrmG,
+                           const double* x0,
+                           const double* pwR, long long sR, const double* pwT,
+                           long long sT, const double* pwC, double* wC,
+                           double* wR, double* wT, double* base, float* dvp,
+                           cudaStream_t st);
+cudaError_t launch_resample(int nP, int n, const double* u, const double* w,
+                            const int* perm, const double* u0,
+                            const double* peak, int nOut, int* src,
+                            double* wOut, int* top, int* flag,
+                            cudaStream_t st);
+// One CTA per draw; draw d uses image d / drawsPerImage.
+cudaError_t launch_insert(float4* acc, int vdim, int kernel, const float* tab,
+                          int tabNz, float tabInvStep, int nDraws,
+                          int drawsPerImage, const float2* dat,
+                          const float* ctf, const double* quat,
+                          const double* trans, const double* offset,
+                          const float* w, const int* iCol, const int* iRow,
+                          int K, int pf, int idim, double* O3D, int* counter,
+                          cudaStream_t st);
+cudaError_t launch_acc_read(const float4* acc, size_t n, float2* F, float* T,
+                            int accumulate, cudaStream_t st);
+cudaError_t launch_merge_class(int nImg, int nK, int kIdx, int nR, int nT,
+                               const double* wCn, const double* wRn,
+                               const double* wTn, const double* basen,
+                               float* wC, float* wR, float* wT, float* baseL,
+                               cudaStream_t st);
+
+// Split-bf16 tensor-core cross term (tcgen05), when available.
+bool bf16x3_available();
+cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda,
+                                  const float* B, long long sB, int ldb,
+                                  int M, int N, int Kd, int batch, float* C,
+                                  long long sC, int ldc, const float* nrm,
+                                  long long sN, float alpha, void* scratch,
+                                  size_t scratchBytes, int* flag,
+                                  cudaStream_t st);
+size_t bf16x3_scratch_bytes(int M, int N, int Kd, int batch);
+
+}  // namespace tg3

@@ -1,0 +1,922 @@
+// tg3_kernels.cu -- the plain (FP32) E-step and insertion kernels for sm_103a.
+//
+// Data layout in HBM (all particle-major):
+//   projection volume  : paired-corner float4 [vdim][vdim][nx], element x holds
+//                        (V[x], V[x+1]) so that each trilinear sample is four
+//                        16-byte loads instead of eight 8-byte ones;
+//   projections P      : [row][Kp] floats, a complex row padded with zeros to
+//                        Kp floats (Kp a multiple of 64);
+//   shifted data A''   : [particle][translation][Kp] floats, the complex
+//                        sigRcp * ctf * X * exp(+2 pi i k.t / N);
+//   log-likelihoods D  : [particle][rotation][translation] floats, without the
+//                        per-particle constant sum sigRcp |X|^2;
+//   insertion volume   : float4 [vdim][vdim][nx] of (F.re, F.im, T, 0), one
+//                        16-byte atomic per voxel update.
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include "tg3_internal.cuh"
+
+namespace tg3 {
+
+namespace {
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float warp_max(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide sum (double) through shared scratch of >= 32 doubles.
+__device__ double block_sum_d(double v, double* scratch)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    v = warp_sum_d(v);
+    __syncthreads();
+    if (lane == 0) scratch[wid] = v;
+    __syncthreads();
+    double r = 0;
+    if (wid == 0) {
+        r = lane < nw ? scratch[lane] : 0.0;
+        r = warp_sum_d(r);
+        if (lane == 0) scratch[0] = r;
+    }
+    __syncthreads();
+    r = scratch[0];
+    __syncthreads();
+    return r;
+}
+
+// Quaternion -> row-major rotation matrix, R = I + 2 w A + 2 A^2
+// (rotate3D, src/Geometry/Euler.cpp:181-189).
+__device__ __forceinline__ void quat_to_mat(const double* q, double* m)
+{
+    const double A[3][3] = {{0, -q[3], q[2]}, {q[3], 0, -q[1]}, {-q[2], q[1], 0}};
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double aa = (2 * A[i][0]) * A[0][j] + (2 * A[i][1]) * A[1][j]
+                      + (2 * A[i][2]) * A[2][j];
+            m[3 * i + j] = ((i == j ? 1.0 : 0.0) + (2 * q[0]) * A[i][j]) + aa;
+        }
+}
+
+// ------------------------------------------------------------------------
+__global__ void k_rotmat(const double* __restrict__ quat, int n, double* __restrict__ mat)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double q[4] = {quat[4 * r], quat[4 * r + 1], quat[4 * r + 2], quat[4 * r + 3]};
+    quat_to_mat(q, mat + 9 * (size_t)r);
+}
+
+// Phase-shift bank S[t][p] = exp(-2 pi i (iCol tx + iRow ty) / N)
+// (translate, src/Image/ImageFunctions.cpp:233-252).
+__global__ void k_translate(const double* __restrict__ trans, int nT, int idim,
+                            const int* __restrict__ iCol, const int* __restrict__ iRow,
+                            int K, float2* __restrict__ out, int ldo2)
+{
+    const int t = blockIdx.y;
+    const float tx = (float)trans[2 * t], ty = (float)trans[2 * t + 1];
+    const float invN = 1.0f / (float)idim;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ldo2; p += gridDim.x * blockDim.x) {
+        float2 v = make_float2(0.f, 0.f);
+        if (p < K) {
+            float f = ((float)iCol[p] * tx + (float)iRow[p] * ty) * invN;
+            float s, c;
+            sincospif(2.0f * f, &s, &c);
+            v = make_float2(c, -s);
+        }
+        out[(size_t)t * ldo2 + p] = v;
+    }
+}
+
+// CTF at the selected pixels (CTF(RFLOAT*, ...), src/CTF.cpp:98-145).
+__global__ void k_ctf(const float* __restrict__ attr, int nImg, float px, int idim,
+                      const int* __restrict__ iCol, const int* __restrict__ iRow,
+                      int K, float* __restrict__ out)
+{
+    const int l = blockIdx.x;
+    const float* a = attr + 7 * (size_t)l;
+    const float V = a[0], dU = a[1], dV = a[2], th = a[3], Cs = a[4], A = a[5], ps = a[6];
+    const float lambda = 12.2643247f / sqrtf(V * (1 + V * 0.978466e-6f));
+    const float w1 = sqrtf(1 - A * A), w2 = A;
+    const float K1 = CUDART_PI_F * lambda;
+    const float K2 = (CUDART_PI_F / 2) * Cs * lambda * lambda * lambda;
+    const float inv = 1.0f / (px * (float)idim);
+    for (int p = threadIdx.x; p < K; p += blockDim.x) {
+        float u = hypotf((float)iCol[p] * inv, (float)iRow[p] * inv);
+        float ang = atan2f((float)iRow[p], (float)iCol[p]) - th;
+        float dfc = -(dU + dV + (dU - dV) * cosf(2 * ang)) / 2;
+        float u2 = u * u;
+        float ki = K1 * dfc * u2 + K2 * u2 * u2 - ps;
+        out[(size_t)l * K + p] = -w1 * sinf(ki) + w2 * cosf(ki);
+    }
+}
+
+__global__ void k_volume_pairs(const float2* __restrict__ vol, int vdim,
+                               float4* __restrict__ pairs)
+{
+    const int nx = vdim / 2 + 1;
+    const size_t n = (size_t)vdim * vdim * nx;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(i % nx);
+        float2 a = vol[i];
+        float2 b = (x + 1 < nx) ? vol[i + 1] : make_float2(0.f, 0.f);
+        pairs[i] = make_float4(a.x, a.y, b.x, b.y);
+    }
+}
+
+// ------------------------------------------------------------------------
+// Fourier-slice extraction.  One CTA per projected row (a rotation of a
+// particle): P[p] = trilinear(V, R (iCol pf, iRow pf, 0)), Friedel-mirrored
+// when x < 0 (Projector::project, src/Projector.cpp:356-374;
+// Volume::getByInterpolationFT, src/Image/Volume.cpp:308-332).  Optionally
+// nrm[row] = sum_p sigRcp ctf^2 |P|^2 of the row's particle.
+__global__ void __launch_bounds__(256)
+k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
+          const float4* __restrict__ vol0, int vdim, int pf,
+          const double* __restrict__ quat, const double* __restrict__ mat,
+          int rowsPerParticle, const int* __restrict__ iCol,
+          const int* __restrict__ iRow, int K, float* __restrict__ out, int ldo,
+          const float* __restrict__ sigRcp, const float* __restrict__ ctf,
+          float* __restrict__ nrm, int* __restrict__ flag)
+{
+    __shared__ float m[9];
+    __shared__ double red[32];
+    const int row = blockIdx.x;
+    const int l = row / rowsPerParticle;
+    if (threadIdx.x == 0) {
+        double md[9];
+        if (quat) {
+            double q[4] = {quat[4 * (size_t)row], quat[4 * (size_t)row + 1],
+                           quat[4 * (size_t)row + 2], quat[4 * (size_t)row + 3]};
+            quat_to_mat(q, md);
+        } else {
+            for (int i = 0; i < 9; i++) md[i] = mat[9 * (size_t)row + i];
+        }
+        for (int i = 0; i < 9; i++) m[i] = (float)md[i];
+    }
+    __syncthreads();
+    const float4* __restrict__ vol = vol0;
+    if (volTable) {
+        const int k = cls ? cls[l] : 0;
+        vol = (k >= 0 && k < kMaxClasses) ? volTable[k] : nullptr;
+        if (!vol) {
+            // unknown class: record it, leave the row zero and skip sampling
+            if (threadIdx.x == 0 && flag) atomicOr(flag, 8);
+            float2* orow = reinterpret_cast<float2*>(out + (size_t)row * ldo);
+            for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x) orow[p] = make_float2(0.f, 0.f);
+            if (nrm && threadIdx.x == 0) nrm[row] = 0.f;
+            return;
+        }
+    }
+    const int nx = vdim / 2 + 1;
+    const float fpf = (float)pf;
+    float2* orow = reinterpret_cast<float2*>(out + (size_t)row * ldo);
+    const float* sg = sigRcp ? sigRcp + (size_t)l * K : nullptr;
+    const float* cf = ctf ? ctf + (size_t)l * K : nullptr;
+    float acc = 0.f;
+    for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x) {
+        if (p >= K) {
+            orow[p] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const float a = (float)iCol[p] * fpf, b = (float)iRow[p] * fpf;
+        float x = m[0] * a + m[1] * b;
+        float y = m[3] * a + m[4] * b;
+        float z = m[6] * a + m[7] * b;
+        const bool conj = x < 0.f;
+        if (conj) { x = -x; y = -y; z = -z; }
+        const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+        const int x0 = (int)xf, y0 = (int)yf, z0 = (int)zf;
+        const float fx = x - xf, fy = y - yf, fz = z - zf;
+        const float wx[2] = {1.f - fx, fx}, wy[2] = {1.f - fy, fy}, wz[2] = {1.f - fz, fz};
+        const int ys[2] = {y0 < 0 ? y0 + vdim : y0, y0 + 1 < 0 ? y0 + 1 + vdim : y0 + 1};
+        const int zs[2] = {z0 < 0 ? z0 + vdim : z0, z0 + 1 < 0 ? z0 + 1 + vdim : z0 + 1};
+        float4 c[4];
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+                c[2 * k + j] = __ldg(vol + ((size_t)zs[k] * vdim + ys[j]) * nx + x0);
+        float re = 0.f, im = 0.f;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const float4 v = c[2 * k + j];
+                const float w0 = wx[0] * wy[j] * wz[k], w1 = wx[1] * wy[j] * wz[k];
+                re += v.x * w0 + v.z * w1;
+                im += v.y * w0 + v.w * w1;
+            }
+        if (conj) im = -im;
+        orow[p] = make_float2(re, im);
+        if (nrm) acc += sg[p] * cf[p] * cf[p] * (re * re + im * im);
+    }
+    if (nrm) {
+        double s = block_sum_d((double)acc, red);
+        if (threadIdx.x == 0) nrm[row] = (float)s;
+    }
+}
+
+// Shifted, weighted data A''[l][t][p] = sigRcp ctf X exp(+2 pi i (iCol tx +
+// iRow ty) / N), the conjugate of sigRcp ctf conj(X) S_t, so that
+// Re sum_p sigRcp ctf conj(X) S_t P = sum over the 2K floats of A'' . P.
+__global__ void k_shift_bank(const float2* __restrict__ dat, const float* __restrict__ ctf,
+                             const float* __restrict__ sigRcp,
+                             const double* __restrict__ trans, const float2* __restrict__ bank,
+                             int nT, int idim,
+                             const int* __restrict__ iCol, const int* __restrict__ iRow,
+                             int K, float* __restrict__ out, int ldo)
+{
+    const int lt = blockIdx.x;            // l * nT + t
+    const int l = lt / nT;
+    const float tx = bank ? 0.f : (float)trans[2 * (size_t)lt];
+    const float ty = bank ? 0.f : (float)trans[2 * (size_t)lt + 1];
+    const float invN = 1.0f / (float)idim;
+    float2* orow = reinterpret_cast<float2*>(out + (size_t)lt * ldo);
+    for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x) {
+        float2 v = make_float2(0.f, 0.f);
+        if (p < K) {
+            const size_t i = (size_t)l * K + p;
+            const float sc = sigRcp[i] * ctf[i];
+            const float2 X = dat[i];
+            float s, c;
+            if (bank) {
+                // shared phase bank S[t][p] = (cos, -sin): use conj(S)
+                const float2 S = bank[(size_t)(lt % nT) * K + p];
+                c = S.x;
+                s = -S.y;
+            } else {
+                float f = ((float)iCol[p] * tx + (float)iRow[p] * ty) * invN;
+                sincospif(2.0f * f, &s, &c);
+            }
+            v = make_float2(sc * (X.x * c - X.y * s), sc * (X.x * s + X.y * c));
+        }
+        orow[p] = v;
+    }
+}
+
+__global__ void k_x0(const float2* __restrict__ dat, const float* __restrict__ sigRcp,
+                     int K, double* __restrict__ x0)
+{
+    __shared__ double red[32];
+    const int l = blockIdx.x;
+    double acc = 0;
+    for (int p = threadIdx.x; p < K; p += blockDim.x) {
+        const float2 X = dat[(size_t)l * K + p];
+        acc += (double)sigRcp[(size_t)l * K + p] * ((double)X.x * X.x + (double)X.y * X.y);
+    }
+    double s = block_sum_d(acc, red);
+    if (threadIdx.x == 0) x0[l] = s;
+}
+
+// ------------------------------------------------------------------------
+// Batched FP32 "NT" GEMM on the CUDA cores: C[b][i][j] = alpha sum_k
+// A[b][i][k] B[b][j][k] (+ nrm[b][i]).  128 x 128 x 16 tiles, 256 threads,
+// 8 x 8 outputs per thread, register-staged double buffering.  Kd must be a
+// multiple of 16 and lda/ldb multiples of 4 (rows zero-padded).
+constexpr int GB_M = 128, GB_N = 128, GB_K = 16, GB_PAD = 4;
+
+__global__ void __launch_bounds__(256, 1)
+k_gemm_nt_fp32(const float* __restrict__ A, long long sA, int lda,
+               const float* __restrict__ B, long long sB, int ldb,
+               int M, int N, int Kd, float* __restrict__ C, long long sC, int ldc,
+               const float* __restrict__ nrm, long long sN, float alpha)
+{
+    __shared__ __align__(16) float As[2][GB_K][GB_M + GB_PAD];
+    __shared__ __align__(16) float Bs[2][GB_K][GB_N + GB_PAD];
+    const int b = blockIdx.z;
+    const int i0 = blockIdx.y * GB_M, j0 = blockIdx.x * GB_N;
+    A += b * sA;
+    B += b * sB;
+    C += b * sC;
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    // loader mapping: two float4 per operand per k-tile (rows lr and lr + 64)
+    const int lr = tid >> 2, lk = (tid & 3) * 4;
+    const bool a0ok = i0 + lr < M, a1ok = i0 + lr + 64 < M;
+    const bool b0ok = j0 + lr < N, b1ok = j0 + lr + 64 < N;
+    const float* Ap0 = A + (size_t)(a0ok ? i0 + lr : 0) * lda + lk;
+    const float* Ap1 = A + (size_t)(a1ok ? i0 + lr + 64 : 0) * lda + lk;
+    const float* Bp0 = B + (size_t)(b0ok ? j0 + lr : 0) * ldb + lk;
+    const float* Bp1 = B + (size_t)(b1ok ? j0 + lr + 64 : 0) * ldb + lk;
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
+
+    float4 ra[2], rb[2];
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    ra[0] = a0ok ? __ldg(reinterpret_cast<const float4*>(Ap0)) : z4;
+    ra[1] = a1ok ? __ldg(reinterpret_cast<const float4*>(Ap1)) : z4;
+    rb[0] = b0ok ? __ldg(reinterpret_cast<const float4*>(Bp0)) : z4;
+    rb[1] = b1ok ? __ldg(reinterpret_cast<const float4*>(Bp1)) : z4;
+    const int nk = Kd / GB_K;
+    int buf = 0;
+    for (int kt = 0; kt < nk; kt++) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            As[buf][lk + 0][lr + 64 * h] = ra[h].x;
+            As[buf][lk + 1][lr + 64 * h] = ra[h].y;
+            As[buf][lk + 2][lr + 64 * h] = ra[h].z;
+            As[buf][lk + 3][lr + 64 * h] = ra[h].w;
+            Bs[buf][lk + 0][lr + 64 * h] = rb[h].x;
+            Bs[buf][lk + 1][lr + 64 * h] = rb[h].y;
+            Bs[buf][lk + 2][lr + 64 * h] = rb[h].z;
+            Bs[buf][lk + 3][lr + 64 * h] = rb[h].w;
+        }
+        __syncthreads();
+        if (kt + 1 < nk) {
+            const int off = (kt + 1) * GB_K;
+            ra[0] = a0ok ? __ldg(reinterpret_cast<const float4*>(Ap0 + off)) : z4;
+            ra[1] = a1ok ? __ldg(reinterpret_cast<const float4*>(Ap1 + off)) : z4;
+            rb[0] = b0ok ? __ldg(reinterpret_cast<const float4*>(Bp0 + off)) : z4;
+            rb[1] = b1ok ? __ldg(reinterpret_cast<const float4*>(Bp1 + off)) : z4;
+        }
+#pragma unroll
+        for (int kk = 0; kk < GB_K; kk++) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][64 + ty * 4]);
+            const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
+            const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][kk][64 + tx * 4]);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+        buf ^= 1;
+    }
+    // epilogue
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int gi = i0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+        if (gi >= M) continue;
+        const float add = nrm ? nrm[b * sN + gi] : 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int gj = j0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
+            if (gj < N) C[(size_t)gi * ldc + gj] = fmaf(alpha, acc[i][j], add);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------
+// Marginal weights of one hypothesis block (a particle, or an image of the
+// global scan): base = max D, s = exp(D - base),
+//   wR[r] = sum_t s pwC pwT[t], wT[t] = sum_r s pwC pwR[r],
+//   wC = sum s pwR[r] pwT[t]
+// (the running-baseline accumulation of Optimiser::updateSP,
+// src/Optimiser.cpp:1326-1347, evaluated in two passes).  D of block (b, g)
+// is D[b sD + r ldc + g nT + t].  One CTA of 256 threads per block; dynamic
+// shared memory holds 8 per-warp copies of wT (8 nT doubles).
+__global__ void __launch_bounds__(256)
+k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, int G,
+          const float* __restrict__ nrmG, const double* __restrict__ x0, const double* __restrict__ pwR, long long sR,
+          const double* __restrict__ pwT, long long sT, const double* __restrict__ pwC,
+          double* __restrict__ wC, double* __restrict__ wR, double* __restrict__ wT,
+          double* __restrict__ base, float* __restrict__ dvp)
+{
+    extern __shared__ double wTw[];      // [8][nT]
+    __shared__ float redf[32];
+    __shared__ double red[32];
+    const int blk = blockIdx.x;
+    const int b = blk / G, g = blk % G;
+    const float* Db = D + b * sD + (size_t)g * nT;
+    const double* pr = pwR + blk * sR;
+    const double* pt = pwT + blk * sT;
+    const double pc = pwC ? pwC[blk] : 1.0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    // pass 1: maximum
+    float mx = -CUDART_INF_F;
+    for (int r = wid; r < nR; r += nw) {
+        const float ad = nrmG ? nrmG[(size_t)r * G + g] : 0.f;
+        for (int t = lane; t < nT; t += 32) mx = fmaxf(mx, Db[(size_t)r * ldc + t] + ad);
+    }
+    mx = warp_max(mx);
+    if (lane == 0) redf[wid] = mx;
+    __syncthreads();
+    if (wid == 0) {
+        float v = lane < nw ? redf[lane] : -CUDART_INF_F;
+        v = warp_max(v);
+        if (lane == 0) redf[0] = v;
+    }
+    __syncthreads();
+    const float M = redf[0];
+    for (int i = threadIdx.x; i < nw * nT; i += blockDim.x) wTw[i] = 0.0;
+    __syncthreads();
+    const double x0b = x0 ? x0[blk] : 0.0;
+    // pass 2: marginals
+    double cacc = 0.0;
+    for (int r = wid; r < nR; r += nw) {
+        const double prr = pr[r];
+        const float ad = nrmG ? nrmG[(size_t)r * G + g] : 0.f;
+        double racc = 0.0;
+        for (int t = lane; t < nT; t += 32) {
+            const float d = Db[(size_t)r * ldc + t] + ad;
+            const double s = (double)__expf(d - M);
+            racc += s * pt[t];
+            wTw[wid * nT + t] += s * prr;
+            cacc += s * (prr * pt[t]);
+            if (dvp) dvp[((size_t)blk * nR + r) * nT + t] = (float)(x0b + (double)d);
+        }
+        racc = warp_sum_d(racc);
+        if (lane == 0) wR[(size_t)blk * nR + r] = racc * pc;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
+        double s = 0.0;
+        for (int w = 0; w < nw; w++) s += wTw[w * nT + t];
+        wT[(size_t)blk * nT + t] = s * pc;
+    }
+    double c = block_sum_d(cacc, red);
+    if (threadIdx.x == 0) {
+        wC[blk] = c;
+        base[blk] = x0b + (double)M;
+    }
+}
+
+// Fold the weights of class kIdx into the reference's running per-image
+// layout: wC [img][nK], wR [img][nK][nR], wT [img][nK][nT] relative to baseL
+// (kernel_setBaseLine / kernel_UpdateW of the reference GPU path, with the
+// CPU scan's rescale rule, src/Optimiser.cpp:835-898).
+__global__ void k_merge_class(int nK, int kIdx, int nR, int nT,
+                              const double* __restrict__ wCn, const double* __restrict__ wRn,
+                              const double* __restrict__ wTn, const double* __restrict__ basen,
+                              float* __restrict__ wC, float* __restrict__ wR,
+                              float* __restrict__ wT, float* __restrict__ baseL)
+{
+    const int l = blockIdx.x;
+    const double bn = basen[l];
+    double scaleOld = 0.0, scaleNew = 1.0, newBase = bn;
+    if (kIdx > 0) {
+        const double bo = baseL[l];
+        if (bn > bo) { scaleOld = exp(bo - bn); newBase = bn; }
+        else { scaleOld = 1.0; scaleNew = exp(bn - bo); newBase = bo; }
+    }
+    __syncthreads();
+    for (int k = 0; k < nK; k++) {
+        const bool cur = (k == kIdx);
+        if (!cur && (kIdx == 0 || k > kIdx)) {
+            // classes not yet scored: zero on the first class only
+            if (kIdx == 0) {
+                if (threadIdx.x == 0) wC[(size_t)l * nK + k] = 0.f;
+                for (int r = threadIdx.x; r < nR; r += blockDim.x) wR[((size_t)l * nK + k) * nR + r] = 0.f;
+                for (int t = threadIdx.x; t < nT; t += blockDim.x) wT[((size_t)l * nK + k) * nT + t] = 0.f;
+            }
+            continue;
+        }
+        if (cur) {
+            if (threadIdx.x == 0) wC[(size_t)l * nK + k] = (float)(wCn[l] * scaleNew);
+            for (int r = threadIdx.x; r < nR; r += blockDim.x)
+                wR[((size_t)l * nK + k) * nR + r] = (float)(wRn[(size_t)l * nR + r] * scaleNew);
+            for (int t = threadIdx.x; t < nT; t += blockDim.x)
+                wT[((size_t)l * nK + k) * nT + t] = (float)(wTn[(size_t)l * nT + t] * scaleNew);
+        } else if (scaleOld != 1.0) {
+            if (threadIdx.x == 0) wC[(size_t)l * nK + k] = (float)(wC[(size_t)l * nK + k] * scaleOld);
+            for (int r = threadIdx.x; r < nR; r += blockDim.x)
+                wR[((size_t)l * nK + k) * nR + r] = (float)(wR[((size_t)l * nK + k) * nR + r] * scaleOld);
+            for (int t = threadIdx.x; t < nT; t += blockDim.x)
+                wT[((size_t)l * nK + k) * nT + t] = (float)(wT[((size_t)l * nK + k) * nT + t] * scaleOld);
+        }
+    }
+    if (threadIdx.x == 0) baseL[l] = (float)newBase;
+}
+
+// ------------------------------------------------------------------------
+// Narrowing + systematic resampling of one axis of one particle per CTA
+// (Particle::keepHalfHeightPeak, src/Particle.cpp:1935-1973;
+//  Particle::shuffle, :2173-2270; Particle::resample(n, pt), :1275-1463;
+//  Particle::normW, :813-820; Particle::setPeakFactor(PAR_R) 3D, :1886-1896).
+// Sums and the cumulative sum run sequentially in one thread so that every
+// result is bit-identical to the reference's sequential double arithmetic;
+// the draws use a binary search, which finds the same first index with
+// cdf >= u_j as the reference's forward scan.
+__global__ void __launch_bounds__(256)
+k_resample(int n, const double* __restrict__ uIn, const double* __restrict__ wIn,
+           const int* __restrict__ perm, const double* __restrict__ u0s,
+           const double* __restrict__ peaks, int nOut, int* __restrict__ src,
+           double* __restrict__ wOut, int* __restrict__ top, int* __restrict__ flag)
+{
+    extern __shared__ double sm[];
+    double* u = sm;                 // [n]
+    double* w = u + n;              // [n]
+    double* cdf = w + n;            // [max(n, nOut)]
+    int* idx = reinterpret_cast<int*>(cdf + (n > nOut ? n : nOut));   // [n]
+    __shared__ double sval[32];
+    __shared__ int sidx[32];
+    __shared__ double sh;
+    __shared__ int bad;
+    const int b = blockIdx.x;
+    const double* ub = uIn + (size_t)b * n;
+    const double* wb = wIn + (size_t)b * n;
+    const int* pb = perm + (size_t)b * n;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) bad = 0;
+    // maximum of u (exact in any order)
+    double mx = -CUDART_INF;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, ub[i]);
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) sval[wid] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = sval[0];
+        for (int i = 1; i < nw; i++) m = fmax(m, sval[i]);
+        sh = m;
+    }
+    __syncthreads();
+    const double umax = sh;
+    double pf = peaks ? peaks[b] : 0.0;
+    if (isnan(pf)) {
+        // value of rank n/8 in descending order (Particle::setPeakFactor)
+        const int k = n / 8;
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double v = ub[i];
+            int gt = 0, ge = 0;
+            for (int j = 0; j < n; j++) {
+                const double x = ub[j];
+                gt += x > v;
+                ge += x >= v;
+            }
+            if (gt <= k && k < ge) sh = v;   // all writers store the same value
+        }
+        __syncthreads();
+        const double r = __ddiv_rn(sh, umax);
+        pf = fmax(1e-3, fmin(0.5, r));
+        __syncthreads();
+    }
+    const double hh = pf > 0 ? __dmul_rn(umax, pf) : 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double ui = ub[i];
+        if (pf > 0) ui = (ui < hh) ? 0.0 : __dsub_rn(ui, hh);
+        const int d = pb[i];
+        if (d < 0 || d >= n) { bad = 1; continue; }
+        u[d] = ui;
+        w[d] = wb[i];
+        idx[d] = i;
+    }
+    __syncthreads();
+    if (bad) {
+        if (threadIdx.x == 0) atomicOr(flag, 1);
+        return;
+    }
+    // best sample, last index among equal maxima (gsl_sort_largest_index)
+    double bv = -CUDART_INF;
+    int bi = -1;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (u[i] >= bv) { bv = u[i]; bi = i; }
+    for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > bv || (ov == bv && oi > bi)) { bv = ov; bi = oi; }
+    }
+    if (lane == 0) { sval[wid] = bv; sidx[wid] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = sval[0];
+        int ii = sidx[0];
+        for (int i = 1; i < nw; i++)
+            if (sval[i] > v || (sval[i] == v && sidx[i] > ii)) { v = sval[i]; ii = sidx[i]; }
+        top[b] = ii >= 0 ? idx[ii] : 0;
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] = __dmul_rn(w[i], u[i]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = w[0];
+        for (int i = 1; i < n; i++) s = __dadd_rn(s, w[i]);
+        sh = s;
+    }
+    __syncthreads();
+    const double ws = sh;
+    if (!(ws > 0.0)) {
+        if (threadIdx.x == 0) atomicOr(flag, 2);
+        return;
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] = __ddiv_rn(w[i], ws);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double acc = 0.0;
+        for (int i = 0; i < n; i++) { acc = __dadd_rn(acc, w[i]); cdf[i] = acc; }
+    }
+    __syncthreads();
+    const double last = cdf[n - 1];
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) cdf[i] = __ddiv_rn(cdf[i], last);
+    __syncthreads();
+    const double u0 = u0s[b];
+    int* so = src + (size_t)b * nOut;
+    for (int j = threadIdx.x; j < nOut; j += blockDim.x) {
+        const double uj = __dadd_rn(u0, __ddiv_rn((double)j, (double)nOut));
+        int lo = 0, hi = n - 1;       // first i with cdf[i] >= uj
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (uj > cdf[mid]) lo = mid + 1; else hi = mid;
+        }
+        so[j] = idx[lo];
+        // new prior 1 / u of the source (PARTICLE_PRIOR_ONE)
+        wOut[(size_t)b * nOut + j] = __ddiv_rn(1.0, u[lo]);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double* wb2 = wOut + (size_t)b * nOut;
+        double s = wb2[0];
+        for (int j = 1; j < nOut; j++) s = __dadd_rn(s, wb2[j]);
+        sh = s;
+    }
+    __syncthreads();
+    const double s2 = sh;
+    for (int j = threadIdx.x; j < nOut; j += blockDim.x)
+        wOut[(size_t)b * nOut + j] = __ddiv_rn(wOut[(size_t)b * nOut + j], s2);
+}
+
+// ------------------------------------------------------------------------
+// Insertion of one weighted, shifted slice per CTA into the interleaved
+// (F.re, F.im, T, 0) accumulator (Reconstructor::insertP,
+// src/Reconstructor.cpp:782-863).  The image is first shifted by
+// -(t - offset) (translate, src/Image/ImageFunctions.cpp:471-492, as in
+// Optimiser::reconstructRef, src/Optimiser.cpp:7115-7136).
+//   MKB: every voxel with tab[rint(r^2 n / b)] != 0 inside the radius
+//        (Volume::addFT(value, x, y, z, a, TabFunction),
+//        src/Image/Volume.cpp:399-431; entries past the kernel support are
+//        zero, so the loop covers only the support);
+//   trilinear: the eight corners (Volume::addFT(value, x, y, z),
+//        src/Image/Volume.cpp:334-369).
+// Voxels with x < 0 are mirrored and conjugated (Volume::iFT).
+__device__ __forceinline__ void red_voxel(float4* acc, int vdim, int nx, int i, int j, int k,
+                                          float fr, float fi, float t)
+{
+    if (i < 0) { i = -i; j = -j; k = -k; fi = -fi; }
+    const int yy = j < 0 ? j + vdim : j, zz = k < 0 ? k + vdim : k;
+    float4* p = acc + ((size_t)zz * vdim + yy) * nx + i;
+    atomicAdd(p, make_float4(fr, fi, t, 0.f));
+}
+
+__global__ void __launch_bounds__(256)
+k_insert(float4* __restrict__ acc, int vdim, int kernel, const float* __restrict__ tab,
+         int tabNz, float tabInvStep, const float2* __restrict__ dat,
+         const float* __restrict__ ctf, const double* __restrict__ quat,
+         const double* __restrict__ trans, const double* __restrict__ offset,
+         const float* __restrict__ wgt, const int* __restrict__ iCol,
+         const int* __restrict__ iRow, int K, int pf, int idim, int drawsPerImage,
+         double* __restrict__ O3D, int* __restrict__ counter)
+{
+    __shared__ float m[9];
+    __shared__ float sh[3];
+    const int d = blockIdx.x;                 // draw
+    const int l = d / drawsPerImage;          // image
+    if (threadIdx.x == 0) {
+        double q[4] = {quat[4 * (size_t)d], quat[4 * (size_t)d + 1], quat[4 * (size_t)d + 2],
+                       quat[4 * (size_t)d + 3]};
+        double md[9];
+        quat_to_mat(q, md);
+        for (int i = 0; i < 9; i++) m[i] = (float)md[i];
+        const double tx = trans[2 * (size_t)d] - (offset ? offset[2 * (size_t)l] : 0.0);
+        const double ty = trans[2 * (size_t)d + 1] - (offset ? offset[2 * (size_t)l + 1] : 0.0);
+        sh[0] = (float)tx;
+        sh[1] = (float)ty;
+        sh[2] = wgt[l];
+        if (O3D) {
+            // insertDir(-R (t - offset, 0)), src/Optimiser.cpp:7180-7186
+            atomicAdd(O3D + 0, -(md[0] * tx + md[1] * ty));
+            atomicAdd(O3D + 1, -(md[3] * tx + md[4] * ty));
+            atomicAdd(O3D + 2, -(md[6] * tx + md[7] * ty));
+        }
+        if (counter) atomicAdd(counter, 1);
+    }
+    __syncthreads();
+    const int nx = vdim / 2 + 1, half = vdim / 2;
+    const float tx = sh[0], ty = sh[1], w = sh[2];
+    const float invN = 1.0f / (float)idim;
+    const float fpf = (float)pf;
+    for (int p = threadIdx.x; p < K; p += blockDim.x) {
+        const size_t di = (size_t)l * K + p;
+        const float c = ctf[di];
+        const float2 X = dat[di];
+        // shift by -(t - offset): multiply by exp(+2 pi i k.t / N)
+        float f = ((float)iCol[p] * tx + (float)iRow[p] * ty) * invN;
+        float s, co;
+        sincospif(2.0f * f, &s, &co);
+        const float cw = c * w;
+        const float vr = (X.x * co - X.y * s) * cw, vi = (X.x * s + X.y * co) * cw;
+        const float vt = c * c * w;
+        const float a = (float)iCol[p] * fpf, b = (float)iRow[p] * fpf;
+        float x = m[0] * a + m[1] * b;
+        float y = m[3] * a + m[4] * b;
+        float z = m[6] * a + m[7] * b;
+        if (kernel == TG3_KERNEL_MKB) {
+            const float rad = 2.0f;   // covers the table's support r^2 <= 3.6101
+            const int k0 = max(-half, (int)floorf(z - rad)), k1 = min(half - 1, (int)ceilf(z + rad));
+            const int j0 = max(-half, (int)floorf(y - rad)), j1 = min(half - 1, (int)ceilf(y + rad));
+            const int i0 = max(-half, (int)floorf(x - rad)), i1 = min(half, (int)ceilf(x + rad));
+            for (int kk = k0; kk <= k1; kk++) {
+                const float dz = z - (float)kk;
+                for (int jj = j0; jj <= j1; jj++) {
+                    const float dy = y - (float)jj;
+                    const float dyz = dy * dy + dz * dz;
+                    for (int ii = i0; ii <= i1; ii++) {
+                        const float dx = x - (float)ii;
+                        const float r2 = dx * dx + dyz;
+                        const int ti = __float2int_rn(r2 * tabInvStep);
+                        if (ti > tabNz) continue;
+                        const float kv = __ldg(tab + ti);
+                        red_voxel(acc, vdim, nx, ii, jj, kk, vr * kv, vi * kv, vt * kv);
+                    }
+                }
+            }
+        } else {
+            float fi = vi;
+            if (x < 0.f) { x = -x; y = -y; z = -z; fi = -fi; }
+            const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+            const int x0 = (int)xf, y0 = (int)yf, z0 = (int)zf;
+            const float fx = x - xf, fy = y - yf, fz = z - zf;
+            const float wx[2] = {1.f - fx, fx}, wy[2] = {1.f - fy, fy}, wz[2] = {1.f - fz, fz};
+#pragma unroll
+            for (int k = 0; k < 2; k++)
+#pragma unroll
+                for (int j = 0; j < 2; j++)
+#pragma unroll
+                    for (int i = 0; i < 2; i++) {
+                        const float ww = wx[i] * wy[j] * wz[k];
+                        int yy = y0 + j, zz = z0 + k;
+                        yy = yy < 0 ? yy + vdim : yy;
+                        zz = zz < 0 ? zz + vdim : zz;
+                        atomicAdd(acc + ((size_t)zz * vdim + yy) * nx + (x0 + i),
+                                  make_float4(vr * ww, fi * ww, vt * ww, 0.f));
+                    }
+        }
+    }
+}
+
+__global__ void k_acc_read(const float4* __restrict__ acc, size_t n, float2* __restrict__ F,
+                           float* __restrict__ T, int accumulate)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float4 a = acc[i];
+        if (accumulate) {
+            float2 f = F[i];
+            F[i] = make_float2(f.x + a.x, f.y + a.y);
+            T[i] += a.z;
+        } else {
+            F[i] = make_float2(a.x, a.y);
+            T[i] = a.z;
+        }
+    }
+}
+
+inline int grid_for(size_t n, int block, int cap = 152 * 16)
+{
+    size_t g = (n + block - 1) / block;
+    if (g > (size_t)cap) g = cap;
+    return (int)(g ? g : 1);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers
+cudaError_t launch_rotmat(const double* quat, int n, double* mat, cudaStream_t st)
+{
+    k_rotmat<<<(n + 127) / 128, 128, 0, st>>>(quat, n, mat);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_translate(const double* trans, int nT, int idim, const int* iCol,
+                             const int* iRow, int K, float2* out, int ldo2, cudaStream_t st)
+{
+    dim3 grid((ldo2 + 255) / 256, nT);
+    k_translate<<<grid, 256, 0, st>>>(trans, nT, idim, iCol, iRow, K, out, ldo2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ctf(const float* attr, int nImg, float px, int idim, const int* iCol,
+                       const int* iRow, int K, float* out, cudaStream_t st)
+{
+    dim3 grid(nImg);
+    k_ctf<<<grid, 256, 0, st>>>(attr, nImg, px, idim, iCol, iRow, K, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_volume_pairs(const float2* vol, int vdim, float4* pairs, cudaStream_t st)
+{
+    size_t n = (size_t)vdim * vdim * (vdim / 2 + 1);
+    k_volume_pairs<<<grid_for(n, 256), 256, 0, st>>>(vol, vdim, pairs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_project(float4* const* volTable, const int* cls, const float4* vol,
+                           int vdim, int pf, const double* quat, const double* mat,
+                           int rows, int rowsPerParticle, const int* iCol,
+                           const int* iRow, int K, float* out, int ldo,
+                           const float* sigRcp, const float* ctf, float* nrm, int* flag,
+                           cudaStream_t st)
+{
+    if (rows <= 0) return cudaSuccess;
+    k_project<<<rows, 256, 0, st>>>(volTable, cls, vol, vdim, pf, quat, mat,
+                                     rowsPerParticle, iCol, iRow, K, out, ldo,
+                                     sigRcp, ctf, nrm, flag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shift_bank(const float2* dat, const float* ctf, const float* sigRcp,
+                              const double* trans, const float2* bank, int nP, int nT,
+                              int idim, const int* iCol, const int* iRow, int K, float* out,
+                              int ldo, cudaStream_t st)
+{
+    dim3 grid(nP * nT);
+    k_shift_bank<<<grid, 256, 0, st>>>(dat, ctf, sigRcp, trans, bank, nT, idim, iCol, iRow,
+                                        K, out, ldo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_x0(const float2* dat, const float* sigRcp, int nP, int K, double* x0,
+                      cudaStream_t st)
+{
+    k_x0<<<nP, 256, 0, st>>>(dat, sigRcp, K, x0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_nt_fp32(const float* A, long long sA, int lda, const float* B,
+                                long long sB, int ldb, int M, int N, int Kd, int batch,
+                                float* C, long long sC, int ldc, const float* nrm,
+                                long long sN, float alpha, cudaStream_t st)
+{
+    dim3 grid((N + GB_N - 1) / GB_N, (M + GB_M - 1) / GB_M, batch);
+    k_gemm_nt_fp32<<<grid, 256, 0, st>>>(A, sA, lda, B, sB, ldb, M, N, Kd, C, sC, ldc,
+                                          nrm, sN, alpha);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR, int nT, int G,
+                           int nBlocks, const float* nrmG, const double* x0, const double* pwR, long long sR,
+                           const double* pwT, long long sT, const double* pwC, double* wC,
+                           double* wR, double* wT, double* base, float* dvp,
+                           cudaStream_t st)
+{
+    size_t smem = sizeof(double) * 8 * (size_t)nT;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_weights, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_weights<<<nBlocks, 256, smem, st>>>(D, sD, ldc, nR, nT, G, nrmG, x0, pwR, sR, pwT, sT, pwC,
+                                           wC, wR, wT, base, dvp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_merge_class(int nImg, int nK, int kIdx, int nR, int nT, const double* wCn,
+                               const double* wRn, const double* wTn, const double* basen,
+                               float* wC, float* wR, float* wT, float* baseL, cudaStream_t st)
+{
+    k_merge_class<<<nImg, 256, 0, st>>>(nK, kIdx, nR, nT, wCn, wRn, wTn, basen, wC, wR, wT,
+                                         baseL);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resample(int nP, int n, const double* u, const double* w, const int* perm,
+                            const double* u0, const double* peak, int nOut, int* src,
+                            double* wOut, int* top, int* flag, cudaStream_t st)
+{
+    size_t smem = sizeof(double) * (2 * (size_t)n + (size_t)(n > nOut ? n : nOut))
+                + sizeof(int) * (size_t)n;
+    cudaError_t e = cudaFuncSetAttribute(k_resample, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    k_resample<<<nP, 256, smem, st>>>(n, u, w, perm, u0, peak, nOut, src, wOut, top, flag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_insert(float4* acc, int vdim, int kernel, const float* tab, int tabNz,
+                          float tabInvStep, int nDraws, int drawsPerImage, const float2* dat,
+                          const float* ctf, const double* quat, const double* trans,
+                          const double* offset, const float* w, const int* iCol,
+                          const int* iRow, int K, int pf, int idim, double* O3D, int* counter,
+                          cudaStream_t st)
+{
+    if (nDraws <= 0) return cudaSuccess;
+    k_insert<<<nDraws, 256, 0, st>>>(acc, vdim, kernel, tab, tabNz, tabInvStep, dat, ctf, quat,
+                                      trans, offset, w, iCol, iRow, K, pf, idim, drawsPerImage,
+                                      O3D, counter);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_acc_read(const float4* acc, size_t n, float2* F, float* T, int accumulate,
+                            cudaStream_t st)
+{
+    k_acc_read<<<grid_for(n, 256), 256, 0, st>>>(acc, n, F, T, accumulate);
+    return cudaGetLastError();
+}
+
+}  // namespace tg3

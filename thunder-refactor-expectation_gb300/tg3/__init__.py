@@ -1,0 +1,203 @@
+"""Python binding of libtg3.so (the GB300 E-step + insertion library).
+
+This is plumbing over the C ABI declared in include/thunder_gb300.h: ctypes
+signatures, status checking, and helpers that pass torch CUDA tensors (device
+pointers) or numpy arrays (host pointers).  There is no compute here and no
+fallback: if the shared library is missing the import of `lib()` fails.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parents[1]
+LIB_PATH = PKG / "libtg3.so"
+
+OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_STATE, ERR_TIMEOUT, ERR_NUMERIC, ERR_UNSUPPORTED = range(8)
+KERNEL_TRILINEAR, KERNEL_MKB = 0, 1
+SCORE_FP32, SCORE_BF16X3 = 0, 1
+
+# every extern "C" symbol declared in include/thunder_gb300.h
+EXPORTS = [
+    "tg3_status_string", "tg3_last_error", "tg3_version", "tg3_getAviDevice",
+    "tg3_ExpectRotran", "tg3_ExpectProject", "tg3_ExpectGlobal3D", "tg3_InsertFT",
+    "tg3_volume_create", "tg3_volume_destroy", "tg3_ExpectLocal3D", "tg3_resample",
+    "tg3_ctx_create", "tg3_ctx_destroy", "tg3_ctx_stream", "tg3_ctx_sync",
+    "tg3_ctx_workspace_bytes", "tg3_ctx_set_volume", "tg3_ctx_set_pixels",
+    "tg3_local_phase_d", "tg3_resample_d", "tg3_ctx_insert_begin", "tg3_insert_d",
+    "tg3_ctx_insert_read_d", "tg3_rotmat_d", "tg3_translate_d", "tg3_ctf_d",
+    "tg3_project_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
+]
+STAGES = ("project", "shift", "cross", "weights", "resample", "insert")
+
+
+class TG3Error(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"tg3 status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+_F = ctypes.c_float
+
+
+def lib():
+    """Load libtg3.so (built by tg3.build / __graft_entry__.build())."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: build the CUDA library first "
+                              "(python -c 'import __graft_entry__ as g; g.build()')")
+        L = ctypes.CDLL(str(LIB_PATH))
+        sig = {
+            "tg3_status_string": ([_I], ctypes.c_char_p),
+            "tg3_last_error": ([], ctypes.c_char_p),
+            "tg3_version": ([], ctypes.c_char_p),
+            "tg3_getAviDevice": ([_P, _I, _P], _I),
+            "tg3_ExpectRotran": ([_P, _P, _P, _P, _P, _P, _I, _I, _I, _I], _I),
+            "tg3_ExpectProject": ([_P, _P, _P, _P, _P, _I, _I, _I, _I, _I], _I),
+            "tg3_ExpectGlobal3D": ([_P] * 11 + [_I] * 6, _I),
+            "tg3_InsertFT": ([_P] * 15 + [_F, _I, _I, _I, _I, _I, _I, _I, _I], _I),
+            "tg3_volume_create": ([_P, _P, _I, _I], _I),
+            "tg3_volume_destroy": ([_P], _I),
+            "tg3_ExpectLocal3D": ([_P, _P, _P, _P, _P, _P, _I, _I, _P, _I, _P, _I, _P, _P, _D,
+                                   _P, _P, _P, _P, _P], _I),
+            "tg3_resample": ([_I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P], _I),
+            "tg3_ctx_create": ([_P, _I], _I),
+            "tg3_ctx_destroy": ([_P], _I),
+            "tg3_ctx_stream": ([_P], _P),
+            "tg3_ctx_sync": ([_P], _I),
+            "tg3_ctx_workspace_bytes": ([_P], ctypes.c_size_t),
+            "tg3_ctx_set_volume": ([_P, _I, _P, _I, _I, _I], _I),
+            "tg3_ctx_set_pixels": ([_P, _P, _P, _I, _I], _I),
+            "tg3_local_phase_d": ([_P, _I, _I, _I] + [_P] * 15 + [_I], _I),
+            "tg3_resample_d": ([_P, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P], _I),
+            "tg3_ctx_insert_begin": ([_P, _I, _I], _I),
+            "tg3_insert_d": ([_P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _P], _I),
+            "tg3_ctx_insert_read_d": ([_P, _P, _P, _I], _I),
+            "tg3_rotmat_d": ([_P, _I, _P, _P], _I),
+            "tg3_translate_d": ([_P, _I, _I, _P, _P, _I, _P, _P], _I),
+            "tg3_ctf_d": ([_P, _I, _F, _I, _P, _P, _I, _P, _P], _I),
+            "tg3_project_d": ([_P, _I, _P, _I, _P], _I),
+            "tg3_local_phase": ([_P, _I, _I, _I] + [_P] * 15 + [_I], _I),
+            "tg3_ctx_set_timing": ([_P, _I], _I),
+            "tg3_ctx_stage_times": ([_P, _P, _P, _I], _I),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def check(status: int):
+    if status != OK:
+        msg = lib().tg3_last_error().decode(errors="replace")
+        raise TG3Error(status, msg)
+
+
+def ptr(x) -> int | None:
+    """Address of a torch tensor (device or host) or a numpy array; None -> 0."""
+    if x is None:
+        return None
+    if isinstance(x, np.ndarray):
+        if not x.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        if not x.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return x.data_ptr()
+    raise TypeError(type(x))
+
+
+class Context:
+    """A tg3_ctx: stream, volumes, pixel list, workspace on one device."""
+
+    def __init__(self, device: int = 0):
+        h = ctypes.c_void_p()
+        check(lib().tg3_ctx_create(ctypes.byref(h), device))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if self.h:
+            lib().tg3_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return lib().tg3_ctx_stream(self.h)
+
+    def sync(self):
+        check(lib().tg3_ctx_sync(self.h))
+
+    def workspace_bytes(self) -> int:
+        return lib().tg3_ctx_workspace_bytes(self.h)
+
+    def set_volume(self, cls, vol, pf):
+        """vol: complex64 tensor/array (vdim, vdim, vdim//2+1), host or device."""
+        on_dev = int(hasattr(vol, "is_cuda") and vol.is_cuda)
+        check(lib().tg3_ctx_set_volume(self.h, cls, ptr(vol), vol.shape[0], pf, on_dev))
+
+    def set_pixels(self, iCol, iRow, idim):
+        iCol = np.ascontiguousarray(iCol, np.int32)
+        iRow = np.ascontiguousarray(iRow, np.int32)
+        check(lib().tg3_ctx_set_pixels(self.h, ptr(iCol), ptr(iRow), len(iCol), idim))
+
+    def local_phase(self, nP, nR, nT, dat, ctf, sig, quat, trans, pwR, pwT, pwC, cls,
+                    wC, wR, wT, base, dvp=None, precision=SCORE_FP32):
+        check(lib().tg3_local_phase_d(self.h, nP, nR, nT, ptr(dat), ptr(ctf), ptr(sig),
+                                      ptr(quat), ptr(trans), ptr(pwR), ptr(pwT), ptr(pwC),
+                                      ptr(cls), ptr(wC), ptr(wR), ptr(wT), ptr(base), ptr(dvp),
+                                      precision))
+
+    def local_phase_host(self, nP, nR, nT, dat, ctf, sig, quat, trans, pwR, pwT, pwC, cls,
+                         wC, wR, wT, base, dvp=None, precision=SCORE_FP32):
+        """Host-buffer batched phase (arrays/tensors in host memory)."""
+        check(lib().tg3_local_phase(self.h, nP, nR, nT, ptr(dat), ptr(ctf), ptr(sig), ptr(quat),
+                                    ptr(trans), ptr(pwR), ptr(pwT), ptr(pwC), ptr(cls), ptr(wC),
+                                    ptr(wR), ptr(wT), ptr(base), ptr(dvp), precision))
+
+    def set_timing(self, enable: bool):
+        check(lib().tg3_ctx_set_timing(self.h, int(enable)))
+
+    def stage_times(self, reset: bool = False):
+        """{stage: (milliseconds, launches)} accumulated since the last reset."""
+        ms = np.zeros(len(STAGES))
+        n = np.zeros(len(STAGES), np.int32)
+        check(lib().tg3_ctx_stage_times(self.h, ptr(ms), ptr(n), int(reset)))
+        return {s: (float(ms[i]), int(n[i])) for i, s in enumerate(STAGES)}
+
+    def resample(self, nP, n, u, w, perm, u0, peak, nOut, src, wOut, top):
+        check(lib().tg3_resample_d(self.h, nP, n, ptr(u), ptr(w), ptr(perm), ptr(u0), ptr(peak),
+                                   nOut, ptr(src), ptr(wOut), ptr(top)))
+
+    def insert_begin(self, vdim, pf):
+        check(lib().tg3_ctx_insert_begin(self.h, vdim, pf))
+
+    def insert(self, nP, dat, ctf, quat, trans, offset, w, kernel, O3D=None, counter=None):
+        check(lib().tg3_insert_d(self.h, nP, ptr(dat), ptr(ctf), ptr(quat), ptr(trans),
+                                 ptr(offset), ptr(w), kernel, ptr(O3D), ptr(counter)))
+
+    def insert_read(self, F, T, accumulate=False):
+        check(lib().tg3_ctx_insert_read_d(self.h, ptr(F), ptr(T), int(accumulate)))
+
+    def project(self, cls, rotmat, nR, out):
+        check(lib().tg3_project_d(self.h, cls, ptr(rotmat), nR, ptr(out)))
+
+
+def version() -> str:
+    return lib().tg3_version().decode()

@@ -334,8 +334,9 @@ def make_stack(seed: int, maps, box: int, pixel_size: float, pf: int,
     sig = np.zeros((n, K), dtype=np.complex128)
     for c, bm in enumerate(maps):
         sel = np.nonzero(cls == c)[0]
-        for s in range(0, len(sel), 4096):
-            ids = sel[s:s + 4096]
+        step = max(1, (1 << 27) // max(1, K * len(bm.amp)))   # bound the (n, K, blobs) temporaries
+        for s in range(0, len(sel), step):
+            ids = sel[s:s + step]
             f = torch.as_tensor(np.einsum("nij,jk->nki", R[ids], k2), device=device)
             sig[ids] = blob_ft(bm, f).cpu().numpy()
     sig = sig * ctf * np.exp(-2j * math.pi * (np.outer(t[:, 0] / box, iCol)
