@@ -62,15 +62,17 @@ def test_rotmat_translate_ctf(small):
     rng = small["rng"]
     q = synth.haar_quaternions(rng, 33)
     mat = torch.empty((33, 9), dtype=torch.float64, device=DEV)
-    tg3.check(tg3.lib().tg3_rotmat_d(tg3.ptr(dev(q)), 33, tg3.ptr(mat), None))
+    dq = dev(q)
+    tg3.check(tg3.lib().tg3_rotmat_d(tg3.ptr(dq), 33, tg3.ptr(mat), None))
     torch.cuda.synchronize()
     np.testing.assert_allclose(mat.cpu().numpy(), O.rotmat(q).reshape(-1, 9), rtol=0, atol=1e-15)
 
     iCol, iRow, K = small["iCol"], small["iRow"], len(small["iCol"])
     t = rng.uniform(-8, 8, (7, 2))
     out = torch.empty((7, K, 2), dtype=torch.float32, device=DEV)
-    tg3.check(tg3.lib().tg3_translate_d(tg3.ptr(dev(t)), 7, small["box"], tg3.ptr(dev(iCol)),
-                                        tg3.ptr(dev(iRow)), K, tg3.ptr(out), None))
+    dt, dc, dr = dev(t), dev(iCol), dev(iRow)
+    tg3.check(tg3.lib().tg3_translate_d(tg3.ptr(dt), 7, small["box"], tg3.ptr(dc),
+                                        tg3.ptr(dr), K, tg3.ptr(out), None))
     torch.cuda.synchronize()
     S = out.cpu().numpy().astype(np.float64)
     S = S[..., 0] + 1j * S[..., 1]
@@ -78,8 +80,9 @@ def test_rotmat_translate_ctf(small):
 
     attr = synth.ctf_attrs(rng, 4)
     cout = torch.empty((4, K), dtype=torch.float32, device=DEV)
-    tg3.check(tg3.lib().tg3_ctf_d(tg3.ptr(dev(attr, torch.float32)), 4, small["px"], small["box"],
-                                  tg3.ptr(dev(iCol)), tg3.ptr(dev(iRow)), K, tg3.ptr(cout), None))
+    da = dev(attr, torch.float32)
+    tg3.check(tg3.lib().tg3_ctf_d(tg3.ptr(da), 4, small["px"], small["box"],
+                                  tg3.ptr(dc), tg3.ptr(dr), K, tg3.ptr(cout), None))
     torch.cuda.synchronize()
     ref = O.ctf(f32(attr), small["px"], small["box"], iCol, iRow)
     np.testing.assert_allclose(cout.cpu().numpy(), ref, atol=5e-4)
@@ -127,9 +130,11 @@ def _local_inputs(small, nP, nR, nT, seed):
                 ctf=st.ctf[:nP].astype(np.float32), sig=st.sigRcp[:nP].astype(np.float32), K=K)
 
 
-@pytest.mark.parametrize("precision", [tg3.SCORE_FP32])
-def test_local_phase(small, ctx, precision):
-    nP, nR, nT = 4, 96, 21
+@pytest.mark.parametrize("precision,shape", [
+    (tg3.SCORE_FP32, (4, 96, 21)), (tg3.SCORE_BF16X3, (4, 96, 21)),
+    (tg3.SCORE_FP32, (3, 300, 100)), (tg3.SCORE_BF16X3, (3, 300, 100))])
+def test_local_phase(small, ctx, precision, shape):
+    nP, nR, nT = shape
     d = _local_inputs(small, nP, nR, nT, 3)
     outs = dict(wC=torch.empty(nP, dtype=torch.float64, device=DEV),
                 wR=torch.empty((nP, nR), dtype=torch.float64, device=DEV),

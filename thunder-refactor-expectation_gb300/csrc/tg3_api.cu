@@ -273,7 +273,9 @@ extern "C" int tg3_ctx_create(tg3_ctx** out, int device)
     TG3_CUDA(cudaSetDevice(device));
     tg3_ctx* c = new tg3_ctx();
     c->device = device;
-    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    // a blocking stream: ordered with work the caller queued on the legacy
+    // default stream (e.g. copies that produced our inputs)
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamDefault);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(c->d_flag, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&c->d_volTable, sizeof(float4*) * kMaxClasses);
@@ -424,36 +426,34 @@ static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
     double* x0 = (double*)ws_get(c, WS_X0, sizeof(double) * (size_t)nP, &st);
     if (!x0) return st;
     cudaStream_t s = c->stream;
+    if (precision != TG3_SCORE_FP32 && precision != TG3_SCORE_BF16X3)
+        return fail(TG3_ERR_ARG, "unknown precision");
+    const bool split = precision == TG3_SCORE_BF16X3;
+    if (split && !bf16x3_available())
+        return fail(TG3_ERR_UNSUPPORTED, "split-bf16 tensor-core path unavailable (no TMA encoder)");
+    if (split && nT > 256) return fail(TG3_ERR_UNSUPPORTED, "split-bf16 path needs nT <= 256");
+    // split-bf16: the same buffers hold a hi plane followed by a lo plane
+    const long long splitP = split ? (long long)nP * nR * Kp : 0;
+    const long long splitA = split ? (long long)nP * nT * Kp : 0;
     {
         StageTimer tm(c, TG3_STAGE_PROJECT);
         TG3_CUDA(launch_project(c->d_volTable, cls, nullptr, v0.vdim, v0.pf, quat, nullptr,
                                 nP * nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, sigRcp, ctf, nrm,
-                                c->d_flag, s));
+                                c->d_flag, splitP, s));
     }
     {
         StageTimer tm(c, TG3_STAGE_SHIFT);
         TG3_CUDA(launch_shift_bank(reinterpret_cast<const float2*>(dat), ctf, sigRcp, trans,
                                    nullptr, nP, nT, c->px.idim, c->px.iCol, c->px.iRow, K, A, Kp,
-                                   s));
+                                   splitA, s));
         TG3_CUDA(launch_x0(reinterpret_cast<const float2*>(dat), sigRcp, nP, K, x0, s));
-    }
-    if (precision != TG3_SCORE_FP32 && precision != TG3_SCORE_BF16X3)
-        return fail(TG3_ERR_ARG, "unknown precision");
-    if (precision == TG3_SCORE_BF16X3 && !bf16x3_available())
-        return fail(TG3_ERR_UNSUPPORTED, "split-bf16 tensor-core path not built");
-    void* scratch = nullptr;
-    size_t sb = 0;
-    if (precision == TG3_SCORE_BF16X3) {
-        sb = bf16x3_scratch_bytes(nR, nT, Kp, nP);
-        scratch = ws_get(c, WS_BF16, sb, &st);
-        if (!scratch) return st;
     }
     {
         StageTimer tm(c, TG3_STAGE_CROSS);
-        if (precision == TG3_SCORE_BF16X3)
+        if (split)
             TG3_CUDA(launch_gemm_nt_bf16x3(P, (long long)nR * Kp, Kp, A, (long long)nT * Kp, Kp,
                                            nR, nT, Kp, nP, D, (long long)nR * nT, nT, nrm, nR,
-                                           -2.0f, scratch, sb, c->d_flag, s));
+                                           -2.0f, nullptr, 0, c->d_flag, s));
         else
             TG3_CUDA(launch_gemm_nt_fp32(P, (long long)nR * Kp, Kp, A, (long long)nT * Kp, Kp, nR,
                                          nT, Kp, nP, D, (long long)nR * nT, nT, nrm, nR, -2.0f,
@@ -644,7 +644,7 @@ extern "C" int tg3_project_d(tg3_ctx* c, int cls, const double* rotMat, int nR, 
     if ((st = check_geometry(c, v.vdim, v.pf))) return st;
     TG3_CUDA(launch_project(nullptr, nullptr, v.pairs, v.vdim, v.pf, nullptr, rotMat, nR, nR,
                             c->px.iCol, c->px.iRow, c->px.K, out, 2 * c->px.K, nullptr, nullptr,
-                            nullptr, c->d_flag, c->stream));
+                            nullptr, c->d_flag, 0, c->stream));
     return TG3_OK;
 }
 
@@ -809,7 +809,7 @@ extern "C" int tg3_ExpectGlobal3D(const float* rotP, const float* traP, const fl
         const float* cc = (const float*)(b + oc);
         const float* ss = (const float*)(b + os);
         TG3_CUDA(launch_shift_bank(dd, cc, ss, nullptr, (const float2*)(b + otp), n, nT, 1, nullptr,
-                                   nullptr, K, A, Kp, s));
+                                   nullptr, K, A, Kp, 0, s));
         TG3_CUDA(launch_x0(dd, ss, n, K, (double*)(b + ox0), s));
         {
             dim3 g3((Kq + 255) / 256, n);

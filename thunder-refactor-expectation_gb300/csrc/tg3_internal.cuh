@@ -139,14 +139,16 @@ cudaError_t launch_project(float4* const* volTable, const int* cls,
                            int rowsPerParticle, const int* iCol,
                            const int* iRow, int K, float* out, int ldo,
                            const float* sigRcp, const float* ctf, float* nrm, int* flag,
-                           cudaStream_t st);
+                           long long splitLo, cudaStream_t st);
 // Either trans [nP][nT][2] or a shared phase bank [nT][K] complex.
+// splitLo != 0: write bf16 hi/lo planes (lo plane splitLo elements after
+// the hi plane at `out`) instead of floats; the same for launch_project.
 cudaError_t launch_shift_bank(const float2* dat, const float* ctf,
                               const float* sigRcp, const double* trans,
                               const float2* bank,
                               int nP, int nT, int idim, const int* iCol,
                               const int* iRow, int K, float* out, int ldo,
-                              cudaStream_t st);
+                              long long splitLo, cudaStream_t st);
 cudaError_t launch_x0(const float2* dat, const float* sigRcp, int nP, int K,
                       double* x0, cudaStream_t st);
 // C[b][i][j] = alpha * sum_k A[b][i][k] B[b][j][k] + nrm[b][i]   (FP32)

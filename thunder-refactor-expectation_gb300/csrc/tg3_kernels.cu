@@ -12,6 +12,7 @@
 //                        per-particle constant sum sigRcp |X|^2;
 //   insertion volume   : float4 [vdim][vdim][nx] of (F.re, F.im, T, 0), one
 //                        16-byte atomic per voxel update.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <stdint.h>
@@ -21,6 +22,25 @@
 namespace tg3 {
 
 namespace {
+
+// Store one complex value at element pair p of row `row` (pitch ldo
+// elements): as two floats, or -- when splitLo != 0 -- as the bf16 pair
+// hi = bf16(v) in the plane at `out` and lo = bf16(v - hi) in the plane
+// splitLo elements further on.
+__device__ __forceinline__ void store_pair(float* out, long long splitLo, size_t row, int ldo,
+                                           int p, float a, float b)
+{
+    if (splitLo == 0) {
+        reinterpret_cast<float2*>(out + row * ldo)[p] = make_float2(a, b);
+        return;
+    }
+    __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(out);
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+    reinterpret_cast<__nv_bfloat162*>(hi + row * ldo)[p] = h;
+    reinterpret_cast<__nv_bfloat162*>(hi + splitLo + row * ldo)[p] = l;
+}
 
 __device__ __forceinline__ double warp_sum_d(double v)
 {
@@ -148,7 +168,7 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
           int rowsPerParticle, const int* __restrict__ iCol,
           const int* __restrict__ iRow, int K, float* __restrict__ out, int ldo,
           const float* __restrict__ sigRcp, const float* __restrict__ ctf,
-          float* __restrict__ nrm, int* __restrict__ flag)
+          float* __restrict__ nrm, int* __restrict__ flag, long long splitLo)
 {
     __shared__ float m[9];
     __shared__ double red[32];
@@ -173,21 +193,20 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
         if (!vol) {
             // unknown class: record it, leave the row zero and skip sampling
             if (threadIdx.x == 0 && flag) atomicOr(flag, 8);
-            float2* orow = reinterpret_cast<float2*>(out + (size_t)row * ldo);
-            for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x) orow[p] = make_float2(0.f, 0.f);
+            for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x)
+                store_pair(out, splitLo, row, ldo, p, 0.f, 0.f);
             if (nrm && threadIdx.x == 0) nrm[row] = 0.f;
             return;
         }
     }
     const int nx = vdim / 2 + 1;
     const float fpf = (float)pf;
-    float2* orow = reinterpret_cast<float2*>(out + (size_t)row * ldo);
     const float* sg = sigRcp ? sigRcp + (size_t)l * K : nullptr;
     const float* cf = ctf ? ctf + (size_t)l * K : nullptr;
     float acc = 0.f;
     for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x) {
         if (p >= K) {
-            orow[p] = make_float2(0.f, 0.f);
+            store_pair(out, splitLo, row, ldo, p, 0.f, 0.f);
             continue;
         }
         const float a = (float)iCol[p] * fpf, b = (float)iRow[p] * fpf;
@@ -219,7 +238,7 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
                 im += v.y * w0 + v.w * w1;
             }
         if (conj) im = -im;
-        orow[p] = make_float2(re, im);
+        store_pair(out, splitLo, row, ldo, p, re, im);
         if (nrm) acc += sg[p] * cf[p] * cf[p] * (re * re + im * im);
     }
     if (nrm) {
@@ -236,14 +255,13 @@ __global__ void k_shift_bank(const float2* __restrict__ dat, const float* __rest
                              const double* __restrict__ trans, const float2* __restrict__ bank,
                              int nT, int idim,
                              const int* __restrict__ iCol, const int* __restrict__ iRow,
-                             int K, float* __restrict__ out, int ldo)
+                             int K, float* __restrict__ out, int ldo, long long splitLo)
 {
     const int lt = blockIdx.x;            // l * nT + t
     const int l = lt / nT;
     const float tx = bank ? 0.f : (float)trans[2 * (size_t)lt];
     const float ty = bank ? 0.f : (float)trans[2 * (size_t)lt + 1];
     const float invN = 1.0f / (float)idim;
-    float2* orow = reinterpret_cast<float2*>(out + (size_t)lt * ldo);
     for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x) {
         float2 v = make_float2(0.f, 0.f);
         if (p < K) {
@@ -262,7 +280,7 @@ __global__ void k_shift_bank(const float2* __restrict__ dat, const float* __rest
             }
             v = make_float2(sc * (X.x * c - X.y * s), sc * (X.x * s + X.y * c));
         }
-        orow[p] = v;
+        store_pair(out, splitLo, lt, ldo, p, v.x, v.y);
     }
 }
 
@@ -820,24 +838,24 @@ cudaError_t launch_project(float4* const* volTable, const int* cls, const float4
                            int vdim, int pf, const double* quat, const double* mat,
                            int rows, int rowsPerParticle, const int* iCol,
                            const int* iRow, int K, float* out, int ldo,
-                           const float* sigRcp, const float* ctf, float* nrm, int* flag,
+                           const float* sigRcp, const float* ctf, float* nrm, int* flag, long long splitLo,
                            cudaStream_t st)
 {
     if (rows <= 0) return cudaSuccess;
     k_project<<<rows, 256, 0, st>>>(volTable, cls, vol, vdim, pf, quat, mat,
                                      rowsPerParticle, iCol, iRow, K, out, ldo,
-                                     sigRcp, ctf, nrm, flag);
+                                     sigRcp, ctf, nrm, flag, splitLo);
     return cudaGetLastError();
 }
 
 cudaError_t launch_shift_bank(const float2* dat, const float* ctf, const float* sigRcp,
                               const double* trans, const float2* bank, int nP, int nT,
                               int idim, const int* iCol, const int* iRow, int K, float* out,
-                              int ldo, cudaStream_t st)
+                              int ldo, long long splitLo, cudaStream_t st)
 {
     dim3 grid(nP * nT);
     k_shift_bank<<<grid, 256, 0, st>>>(dat, ctf, sigRcp, trans, bank, nT, idim, iCol, iRow,
-                                        K, out, ldo);
+                                        K, out, ldo, splitLo);
     return cudaGetLastError();
 }
 

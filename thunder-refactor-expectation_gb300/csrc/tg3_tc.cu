@@ -1,17 +1,416 @@
-// tg3_tc.cu -- split-bf16 tensor-core cross term (tcgen05 / TMEM / TMA).
+// tg3_tc.cu -- the likelihood cross term on the 5th-generation tensor cores.
+//
+// C[b][i][j] = alpha * sum_k A[b][i][k] B[b][j][k] + nrm[b][i], with each FP32
+// operand stored as two bf16 planes, hi = bf16(x) and lo = bf16(x - hi), and
+// the product formed as Ah Bh + Ah Bl + Al Bh (the lo x lo term, ~2^-16 of
+// the product, is dropped), accumulated in FP32 in tensor memory.
+//
+// One CTA per (128-row tile of A, batch item); N (<= 256) columns in one
+// UMMA of shape 128 x N x 16.  128 threads:
+//   warp 0 lane 0 : TMA producer (cp.async.bulk.tensor, 128B swizzle),
+//   warp 1 lane 0 : tcgen05.mma issuer, commits to the stage's empty barrier,
+//   warps 0-3     : epilogue (tcgen05.ld 32x32b, + nrm, store).
+// Every mbarrier wait is bounded (clock64 budget); on expiry the CTA records
+// TG3 flag bit 4, stops issuing, waits (bounded) for its own copies and MMAs,
+// frees its tensor memory and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
 #include "tg3_internal.cuh"
 
 namespace tg3 {
 
-bool bf16x3_available() { return false; }
+namespace {
+
+constexpr int TC_M = 128;          // rows of A per CTA (UMMA M)
+constexpr int TC_BK = 64;          // bf16 elements per K block (one 128-byte row)
+constexpr int TC_THREADS = 128;
+constexpr long long kWaitBudget = 4000000000LL;   // ~2 s of SM clocks
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        " .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait; false when the budget ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long budget)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > budget) return false;
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// UMMA shared-memory descriptor: K-major operand, 128-byte swizzle, rows of
+// 128 bytes, 8-row groups 1024 bytes apart (SBO); LBO unused for this layout.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;                 // LBO (16 B; ignored for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;       // SBO
+    d |= (uint64_t)1 << 46;                 // descriptor version for tcgen05
+    d |= (uint64_t)2 << 61;                 // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulate, bf16 A and B, both
+// K-major, shape M x N.
+__host__ __device__ constexpr uint32_t umma_idesc(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n"
+        " .reg .pred p;\n"
+        " setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar)
+{
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32"
+        " {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+struct TcParams {
+    int M, N, Kd;            // rows of A per item, columns (rows of B) per item, K
+    int ntile;               // N rounded up to 16 (the UMMA N)
+    int tmemCols;            // power of two >= ntile
+    int stages;
+    float* C;
+    long long sC;
+    int ldc;
+    const float* nrm;
+    long long sN;
+    float alpha;
+    int* flag;
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+k_gemm_bf16x3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+              const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
+              const TcParams p)
+{
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    // 1024-byte aligned stage buffers
+    uint8_t* smem = reinterpret_cast<uint8_t*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const int aBytes = TC_M * TC_BK * 2;                  // 16 KB
+    const int bBytes = p.ntile * TC_BK * 2;               // ntile * 128 B
+    const int stageBytes = 2 * aBytes + 2 * bBytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + p.stages * stageBytes);
+    uint64_t* empty = full + p.stages;
+    uint64_t* accum = empty + p.stages;
+    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(accum + 1);
+    int* abortFlag = reinterpret_cast<int*>(tmemSlot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mtile = blockIdx.x, item = blockIdx.y;
+    const int aRow0 = item * p.M + mtile * TC_M;
+    const int bRow0 = item * p.N;
+    const int nkb = p.Kd / TC_BK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < p.stages; s++) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        mbar_init(accum, 1);
+        *abortFlag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmemSlot)),
+                     "r"(p.tmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmemSlot;
+
+    int issuedTma = 0;      // K blocks whose copies were issued (producer)
+    int issuedMma = 0;      // K blocks whose MMAs were issued (issuer)
+    if (warp == 0 && lane == 0) {
+        // ---------------- TMA producer
+        for (int kb = 0; kb < nkb; kb++) {
+            const int s = kb % p.stages;
+            const int round = kb / p.stages;
+            if (round > 0 && !mbar_wait(empty + s, (round - 1) & 1, kWaitBudget)) {
+                atomicOr(p.flag, 4);
+                *(volatile int*)abortFlag = 1;
+                break;
+            }
+            if (*(volatile int*)abortFlag) break;
+            uint8_t* st = smem + s * stageBytes;
+            mbar_expect_tx(full + s, stageBytes);
+            tma_load_2d(st, &tmAh, full + s, kb * TC_BK, aRow0);
+            tma_load_2d(st + aBytes, &tmAl, full + s, kb * TC_BK, aRow0);
+            tma_load_2d(st + 2 * aBytes, &tmBh, full + s, kb * TC_BK, bRow0);
+            tma_load_2d(st + 2 * aBytes + bBytes, &tmBl, full + s, kb * TC_BK, bRow0);
+            issuedTma = kb + 1;
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ---------------- MMA issuer
+        const uint32_t idesc = umma_idesc(TC_M, p.ntile);
+        for (int kb = 0; kb < nkb; kb++) {
+            const int s = kb % p.stages;
+            const int round = kb / p.stages;
+            if (!mbar_wait(full + s, round & 1, kWaitBudget)) {
+                atomicOr(p.flag, 4);
+                *(volatile int*)abortFlag = 1;
+                break;
+            }
+            if (*(volatile int*)abortFlag) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            uint8_t* st = smem + s * stageBytes;
+            const uint32_t ah = smem_u32(st), al = smem_u32(st + aBytes);
+            const uint32_t bh = smem_u32(st + 2 * aBytes), bl = smem_u32(st + 2 * aBytes + bBytes);
+#pragma unroll
+            for (int kk = 0; kk < TC_BK / 16; kk++) {
+                const uint32_t off = kk * 32;      // 16 bf16 = 32 bytes along K
+                umma_bf16(tmem, umma_desc(ah + off), umma_desc(bh + off), idesc,
+                          (kb | kk) != 0);
+                umma_bf16(tmem, umma_desc(ah + off), umma_desc(bl + off), idesc, 1);
+                umma_bf16(tmem, umma_desc(al + off), umma_desc(bh + off), idesc, 1);
+            }
+            umma_commit(empty + s);        // stage free once these MMAs have read it
+            issuedMma = kb + 1;
+        }
+        umma_commit(accum);                // all issued MMAs complete -> epilogue
+    }
+    __syncthreads();
+    // ---------------- epilogue (all four warps)
+    bool ok = *(volatile int*)abortFlag == 0 && mbar_wait(accum, 0, kWaitBudget);
+    // block-uniform decision (the tcgen05.ld below is warp-collective)
+    ok = __syncthreads_and(ok) != 0;
+    if (!ok && threadIdx.x == 0) {
+        atomicOr(p.flag, 4);
+        *(volatile int*)abortFlag = 1;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool aborted = !ok;
+    const int rowInTile = warp * 32 + lane;
+    const int row = mtile * TC_M + rowInTile;            // row within the item
+    if (!aborted) {
+        const bool rowOk = row < p.M;
+        const float add = (rowOk && p.nrm) ? p.nrm[item * p.sN + row] : 0.f;
+        float* crow = p.C + item * p.sC + (size_t)(rowOk ? row : 0) * p.ldc;
+        for (int c0 = 0; c0 < p.ntile; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            if (rowOk) {
+#pragma unroll
+                for (int i = 0; i < 16; i++)
+                    if (c0 + i < p.N) crow[c0 + i] = fmaf(p.alpha, v[i], add);
+            }
+        }
+    }
+    // on an abort, let the copies this CTA issued land before leaving
+    if (aborted && warp == 0 && lane == 0) {
+        for (int kb = 0; kb < issuedTma; kb++) {
+            const int s = kb % p.stages;
+            mbar_wait(full + s, (kb / p.stages) & 1, kWaitBudget / 4);
+        }
+    }
+    // on an abort, the MMA issuer waits (bounded) for the MMAs it issued
+    if (aborted && warp == 1 && lane == 0 && issuedMma > 0)
+        mbar_wait(accum, 0, kWaitBudget / 4);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(p.tmemCols)
+                     : "memory");
+    }
+}
+
+// ------------------------------------------------------- host: tensor maps
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(f);
+    }
+    return fn;
+}
+
+// 2-D bf16 plane [rows][Kd], box [64 x boxRows], 128-byte swizzle.
+bool make_map(CUtensorMap* m, const void* base, long long rows, int Kd, int boxRows)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)Kd, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)Kd * 2};
+    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)boxRows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+                    box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+bool bf16x3_available() { return encode_fn() != nullptr; }
 
 size_t bf16x3_scratch_bytes(int, int, int, int) { return 256; }
 
-cudaError_t launch_gemm_nt_bf16x3(const float*, long long, int, const float*, long long, int,
-                                  int, int, int, int, float*, long long, int, const float*,
-                                  long long, float, void*, size_t, int*, cudaStream_t)
+// A and B point at the hi planes; the lo plane of each follows its hi plane
+// (rows * Kd bf16 elements later).  lda / ldb must equal Kd.
+cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda, const float* B,
+                                  long long sB, int ldb, int M, int N, int Kd, int batch,
+                                  float* C, long long sC, int ldc, const float* nrm,
+                                  long long sN, float alpha, void*, size_t, int* flag,
+                                  cudaStream_t st)
 {
-    return cudaErrorNotSupported;
+    if (N <= 0 || N > 256 || M <= 0 || Kd % TC_BK || lda != Kd || ldb != Kd ||
+        sA != (long long)M * Kd || sB != (long long)N * Kd)
+        return cudaErrorInvalidValue;
+    const long long rowsA = (long long)batch * M, rowsB = (long long)batch * N;
+    const __nv_bfloat16* Ah = reinterpret_cast<const __nv_bfloat16*>(A);
+    const __nv_bfloat16* Al = Ah + rowsA * Kd;
+    const __nv_bfloat16* Bh = reinterpret_cast<const __nv_bfloat16*>(B);
+    const __nv_bfloat16* Bl = Bh + rowsB * Kd;
+    TcParams p;
+    p.M = M;
+    p.N = N;
+    p.Kd = Kd;
+    p.ntile = (N + 15) / 16 * 16;
+    p.tmemCols = 32;
+    while (p.tmemCols < p.ntile) p.tmemCols <<= 1;
+    const int stageBytes = 2 * TC_M * TC_BK * 2 + 2 * p.ntile * TC_BK * 2;
+    p.stages = (200 * 1024) / stageBytes;
+    if (p.stages > 4) p.stages = 4;
+    if (p.stages < 2) return cudaErrorInvalidValue;
+    p.C = C;
+    p.sC = sC;
+    p.ldc = ldc;
+    p.nrm = nrm;
+    p.sN = sN;
+    p.alpha = alpha;
+    p.flag = flag;
+    CUtensorMap mAh, mAl, mBh, mBl;
+    if (!make_map(&mAh, Ah, rowsA, Kd, TC_M) || !make_map(&mAl, Al, rowsA, Kd, TC_M) ||
+        !make_map(&mBh, Bh, rowsB, Kd, p.ntile) || !make_map(&mBl, Bl, rowsB, Kd, p.ntile))
+        return cudaErrorInvalidValue;
+    const size_t smem = 1024 + (size_t)p.stages * stageBytes + 256;
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((M + TC_M - 1) / TC_M, batch);
+    k_gemm_bf16x3<<<grid, TC_THREADS, smem, st>>>(mAh, mAl, mBh, mBl, p);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// Split planes: hi = bf16(x), lo = bf16(x - hi) of an FP32 array of `rows`
+// rows of Kd floats (zero-padded), written as two [rows][Kd] bf16 planes.
+namespace {
+__global__ void k_split_planes(const float* __restrict__ in, long long n, __nv_bfloat16* __restrict__ hi,
+                               __nv_bfloat16* __restrict__ lo)
+{
+    for (long long i = (blockIdx.x * (long long)blockDim.x + threadIdx.x) * 2; i < n;
+         i += (long long)gridDim.x * blockDim.x * 2) {
+        const float2 v = *reinterpret_cast<const float2*>(in + i);
+        const __nv_bfloat162 h = __floats2bfloat162_rn(v.x, v.y);
+        const float2 hf = __bfloat1622float2(h);
+        const __nv_bfloat162 l = __floats2bfloat162_rn(v.x - hf.x, v.y - hf.y);
+        *reinterpret_cast<__nv_bfloat162*>(hi + i) = h;
+        *reinterpret_cast<__nv_bfloat162*>(lo + i) = l;
+    }
+}
+}  // namespace
+
+cudaError_t launch_split_planes(const float* in, long long n, void* hi, void* lo, cudaStream_t st)
+{
+    long long g = (n / 2 + 255) / 256;
+    if (g > 152 * 32) g = 152 * 32;
+    k_split_planes<<<(int)g, 256, 0, st>>>(in, n, reinterpret_cast<__nv_bfloat16*>(hi),
+                                            reinterpret_cast<__nv_bfloat16*>(lo));
+    return cudaGetLastError();
 }
 
 }  // namespace tg3

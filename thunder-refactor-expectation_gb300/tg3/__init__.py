@@ -118,18 +118,26 @@ def ptr(x) -> int | None:
 
 
 class Context:
-    """A tg3_ctx: stream, volumes, pixel list, workspace on one device."""
+    """A tg3_ctx: stream, volumes, pixel list, workspace on one device.
+
+    Device work is asynchronous on the context's stream, so every tensor
+    passed to a method is kept alive until the next sync()."""
 
     def __init__(self, device: int = 0):
         h = ctypes.c_void_p()
         check(lib().tg3_ctx_create(ctypes.byref(h), device))
         self.h = h
         self.device = device
+        self._keep = []
+
+    def _hold(self, *xs):
+        self._keep.extend(x for x in xs if x is not None and not isinstance(x, (int, float)))
 
     def close(self):
         if self.h:
             lib().tg3_ctx_destroy(self.h)
             self.h = None
+        self._keep = []
 
     def __del__(self):
         try:
@@ -143,6 +151,7 @@ class Context:
 
     def sync(self):
         check(lib().tg3_ctx_sync(self.h))
+        self._keep = []
 
     def workspace_bytes(self) -> int:
         return lib().tg3_ctx_workspace_bytes(self.h)
@@ -159,6 +168,7 @@ class Context:
 
     def local_phase(self, nP, nR, nT, dat, ctf, sig, quat, trans, pwR, pwT, pwC, cls,
                     wC, wR, wT, base, dvp=None, precision=SCORE_FP32):
+        self._hold(dat, ctf, sig, quat, trans, pwR, pwT, pwC, cls, wC, wR, wT, base, dvp)
         check(lib().tg3_local_phase_d(self.h, nP, nR, nT, ptr(dat), ptr(ctf), ptr(sig),
                                       ptr(quat), ptr(trans), ptr(pwR), ptr(pwT), ptr(pwC),
                                       ptr(cls), ptr(wC), ptr(wR), ptr(wT), ptr(base), ptr(dvp),
@@ -166,7 +176,8 @@ class Context:
 
     def local_phase_host(self, nP, nR, nT, dat, ctf, sig, quat, trans, pwR, pwT, pwC, cls,
                          wC, wR, wT, base, dvp=None, precision=SCORE_FP32):
-        """Host-buffer batched phase (arrays/tensors in host memory)."""
+        """Host-buffer batched phase (arrays/tensors in host memory); returns
+        after the outputs are in host memory."""
         check(lib().tg3_local_phase(self.h, nP, nR, nT, ptr(dat), ptr(ctf), ptr(sig), ptr(quat),
                                     ptr(trans), ptr(pwR), ptr(pwT), ptr(pwC), ptr(cls), ptr(wC),
                                     ptr(wR), ptr(wT), ptr(base), ptr(dvp), precision))
@@ -182,6 +193,7 @@ class Context:
         return {s: (float(ms[i]), int(n[i])) for i, s in enumerate(STAGES)}
 
     def resample(self, nP, n, u, w, perm, u0, peak, nOut, src, wOut, top):
+        self._hold(u, w, perm, u0, peak, src, wOut, top)
         check(lib().tg3_resample_d(self.h, nP, n, ptr(u), ptr(w), ptr(perm), ptr(u0), ptr(peak),
                                    nOut, ptr(src), ptr(wOut), ptr(top)))
 
@@ -189,13 +201,16 @@ class Context:
         check(lib().tg3_ctx_insert_begin(self.h, vdim, pf))
 
     def insert(self, nP, dat, ctf, quat, trans, offset, w, kernel, O3D=None, counter=None):
+        self._hold(dat, ctf, quat, trans, offset, w, O3D, counter)
         check(lib().tg3_insert_d(self.h, nP, ptr(dat), ptr(ctf), ptr(quat), ptr(trans),
                                  ptr(offset), ptr(w), kernel, ptr(O3D), ptr(counter)))
 
     def insert_read(self, F, T, accumulate=False):
+        self._hold(F, T)
         check(lib().tg3_ctx_insert_read_d(self.h, ptr(F), ptr(T), int(accumulate)))
 
     def project(self, cls, rotmat, nR, out):
+        self._hold(rotmat, out)
         check(lib().tg3_project_d(self.h, cls, ptr(rotmat), nR, ptr(out)))
 
 
