@@ -102,11 +102,15 @@ int tg3_ExpectGlobal3D(const float* rotP, const float* traP, const float* datP,
  * draw m < mReco: rotation from the quaternion nR[(l mReco + m) 4 ..],
  * translation nT[(l mReco + m) 2 ..], shift the image by -(t - offS[l]),
  * weight w[l], and grid datP * ctfP * w into F3D and ctfP^2 * w into T3D
- * (edge dimSize = pf idim), with the trilinear kernel (the reference GPU
+ * (edge dimSize = opf idim), with the trilinear kernel (the reference GPU
  * behaviour) or the MKB kernel (radius a = 1.9, alpha = 15, tabulated as in
- * Reconstructor).  O3D [3] accumulates -R (t - offS, 0), counter the
- * number of inserted draws.  F3D is complex, T3D real, both
- * [dimSize][dimSize][dimSize/2 + 1], accumulated into (not cleared).
+ * Reconstructor).  iCol/iRow are the reconstructor's padded pixel indices
+ * (i opf, Optimiser.cpp:7984-7986), as the reference passes them.  O3D [3]
+ * accumulates -R (t - offS, 0), counter the number of inserted draws.  F3D
+ * is complex, T3D real, both [dimSize][dimSize][dimSize/2 + 1],
+ * accumulated into (not cleared).  Note: dimSize here is the volume edge;
+ * the reference's InsertFT passes the voxel count in its dimSize and the
+ * edge (F3D.nSlcFT()) to its back end.
  * ctfaData, nD and cSearch are accepted for signature parity; cSearch must
  * be false.  kernel is TG3_KERNEL_*. */
 int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter,

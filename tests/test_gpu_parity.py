@@ -321,10 +321,13 @@ def test_insertft_host(small):
     dat = np.ascontiguousarray(st.dat[:nImg].astype(np.complex64))
     ctf = np.ascontiguousarray(st.ctf[:nImg].astype(np.float32))
     sig = np.ascontiguousarray(st.sigRcp[:nImg].astype(np.float32))
+    # the reconstructor's padded pixel indices, as the reference passes them
+    iColPad = np.ascontiguousarray(small["iCol"] * pf, np.int32)
+    iRowPad = np.ascontiguousarray(small["iRow"] * pf, np.int32)
     tg3.check(tg3.lib().tg3_InsertFT(
         tg3.ptr(F), tg3.ptr(T), tg3.ptr(O3D), tg3.ptr(counter), tg3.ptr(dat), tg3.ptr(ctf),
         tg3.ptr(sig), None, tg3.ptr(offS), tg3.ptr(w), tg3.ptr(quats), tg3.ptr(trans), None,
-        tg3.ptr(np.ascontiguousarray(small["iCol"])), tg3.ptr(np.ascontiguousarray(small["iRow"])),
+        tg3.ptr(iColPad), tg3.ptr(iRowPad),
         small["px"], 0, pf, K, mReco, box, vdim, nImg, tg3.KERNEL_TRILINEAR))
     assert counter[0] == nImg * mReco
     Fr = np.zeros(F.shape, np.complex128)

@@ -106,3 +106,46 @@ def test_blob_volume_is_hermitian_on_x0_plane():
     for y in range(1, n // 2):
         for z in range(1, n // 2):
             assert np.isclose(v[z, y, 0], np.conj(v[n - z, n - y, 0]), atol=1e-10)
+
+
+REF = O.REF_TREE
+
+
+@pytest.mark.skipif(not (REF / "gpu" / "interface" / "Interface.h").exists(),
+                    reason="reference sources unavailable")
+def test_dropin_adaptor_compiles_against_reference_interface(tmp_path):
+    """interface/Interface.cpp defines the E-step and insertion entry points
+    with the exact signatures of the reference's gpu/interface/Interface.h."""
+    import subprocess
+    from oracle import oracle as Oo
+    Oo.build_ref()   # provides the GSL/FFTW header links and the MPI stand-in
+    incs = ["-I" + str(ROOT / "oracle" / "_ref" / "inc"), "-I" + str(ROOT / "oracle" / "ref")]
+    incs += ["-I" + str(p) for p in (REF / "include").rglob("*") if p.is_dir()]
+    incs += ["-I" + str(REF / "include"), "-I" + str(REF / "gpu" / "interface"),
+             "-I" + str(REF / "gpu" / "include"), "-I" + str(REF / "external" / "Eigen3"),
+             "-I" + str(REF / "external" / "boost"), "-I" + str(REF / "external" / "easylogging"),
+             "-I" + str(ROOT / "include"), "-I/usr/local/cuda/include"]
+    obj = tmp_path / "iface.o"
+    r = subprocess.run(["g++", "-std=c++11", "-c", "-w", "-DSINGLE_PRECISION", "-DGPU_VERSION",
+                        *incs, str(ROOT / "thunder-refactor-expectation_gb300" / "interface" /
+                                   "Interface.cpp"), "-o", str(obj)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    syms = subprocess.run(["nm", "-C", str(obj)], capture_output=True, text=True).stdout
+    for name in ("ExpectRotran(", "ExpectProject(", "ExpectGlobal3D(", "ExpectLocalM(",
+                 "ExpectLocalPreI3D(", "InsertFT(Volume&", "getAviDevice("):
+        assert any(" T " in ln and name in ln for ln in syms.splitlines()), name
+
+
+def test_binding_signatures_match_header():
+    """The ctypes argument lists agree with the header's parameter counts."""
+    import tg3
+    if not tg3.LIB_PATH.exists():
+        from tg3 import build
+        build.build()
+    L = tg3.lib()
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "thunder_gb300.h").read_text(), flags=re.S)
+    for m in re.finditer(r"\b(tg3_\w+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        name, params = m.group(1), m.group(2).strip()
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        assert len(getattr(L, name).argtypes) == n, (name, n, len(getattr(L, name).argtypes))

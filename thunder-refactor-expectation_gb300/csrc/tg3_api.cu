@@ -859,7 +859,15 @@ extern "C" int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter, c
     int st = TG3_OK;
     tg3_ctx* c = default_ctx(&st);
     if (!c) return st;
-    if ((st = tg3_ctx_set_pixels(c, iCol, iRow, npxl, idim))) return st;
+    // the reference hands the reconstructor's padded pixel indices (i * opf)
+    std::vector<int> ic(npxl), ir(npxl);
+    for (int p = 0; p < npxl; p++) {
+        if (iCol[p] % opf || iRow[p] % opf)
+            return fail(TG3_ERR_ARG, "InsertFT pixel indices must be multiples of opf");
+        ic[p] = iCol[p] / opf;
+        ir[p] = iRow[p] / opf;
+    }
+    if ((st = tg3_ctx_set_pixels(c, ic.data(), ir.data(), npxl, idim))) return st;
     if ((st = tg3_ctx_insert_begin(c, dimSize, opf))) return st;
     cudaStream_t s = c->stream;
     const size_t nvox = (size_t)dimSize * dimSize * (dimSize / 2 + 1);

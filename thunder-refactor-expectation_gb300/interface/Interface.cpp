@@ -1,0 +1,396 @@
+/*
+ * Interface.cpp -- drop-in definitions of the E-step and insertion entry
+ * points of THUNDER's gpu/interface/Interface.h over libtg3.so.
+ *
+ * The signatures are those of gpu/interface/Interface.h (cited per function);
+ * this file replaces the corresponding definitions of the reference's
+ * gpu/interface/Interface.cpp.  Entry points outside this path (2-D
+ * classification, PrepareTF and the reconstruction Expose* family, the
+ * multi-class InsertFT) keep their reference definitions.
+ *
+ * Behaviour kept from the reference: functions return void and a failure
+ * prints the library's message and exits the process (the reference's
+ * cudaCheckErrors does the same); "device pointers" handed back to the
+ * caller are opaque handles the caller only passes back in.
+ *
+ * Thread safety: the Optimiser calls these from OpenMP threads, holding a
+ * per-GPU lock around ExpectLocalRTD / PreI3D / M; the side tables below are
+ * guarded by one mutex.
+ */
+#include "Interface.h"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "thunder_gb300.h"
+
+static_assert(sizeof(RFLOAT) == sizeof(float),
+              "the GB300 library implements the single-precision (RFLOAT = float) interface");
+
+namespace {
+
+std::mutex g_mu;
+
+[[noreturn]] void die(const char* where, int status)
+{
+    std::fprintf(stderr, "%s: %s (%s)\n", where, tg3_status_string(status), tg3_last_error());
+    std::exit(1);
+}
+
+inline void ok(const char* where, int status)
+{
+    if (status != TG3_OK) die(where, status);
+}
+
+// ExpectPreidx: the pixel list, returned to the caller as opaque handles.
+struct PixelList {
+    std::vector<int> iCol, iRow;
+};
+std::map<int*, PixelList*> g_pixels;
+
+// ExpectLocalIn: per-GPU image slots (cpyNumL images of npxl pixels).
+struct Slots {
+    int npxl = 0, n = 0;
+    std::vector<Complex> dat;
+    std::vector<RFLOAT> ctf, sig, def;
+};
+std::map<Complex*, Slots*> g_slots;
+
+// ExpectLocalV3D: the volume behind a ManagedArrayTexture.
+struct VolState {
+    const Complex* host = nullptr;
+    int vdim = 0;
+    int pf = 0;
+    tg3_volume* h = nullptr;
+};
+std::map<ManagedArrayTexture*, VolState> g_vols;
+
+// ExpectLocalRTD / PreI3D: the hypothesis set behind a ManagedCalPoint.
+struct CalState {
+    std::vector<double> rot, trans, oldR, oldT;
+    int nR = 0, nT = 0;
+    ManagedArrayTexture* mgr = nullptr;
+    int idim = 0, npxl = 0;
+    const int* iCol = nullptr;
+    const int* iRow = nullptr;
+};
+std::map<ManagedCalPoint*, CalState> g_cal;
+
+Slots* slots_of(Complex* devdatP)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_slots.find(devdatP);
+    if (it == g_slots.end()) die("tg3 Interface: unknown image slots", TG3_ERR_STATE);
+    return it->second;
+}
+
+const PixelList* pixels_of(int* deviCol)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_pixels.find(deviCol);
+    if (it == g_pixels.end()) die("tg3 Interface: unknown pixel list", TG3_ERR_STATE);
+    return it->second;
+}
+
+}  // namespace
+
+// gpu/interface/Interface.h:16
+void getAviDevice(std::vector<int>& gpus)
+{
+    int ids[64], n = 0;
+    ok("getAviDevice", tg3_getAviDevice(ids, 64, &n));
+    gpus.assign(ids, ids + (n < 64 ? n : 64));
+}
+
+// gpu/interface/Interface.h:18-23
+void ExpectPreidx(int gpuIdx, int** deviCol, int** deviRow, int* iCol, int* iRow, int npxl)
+{
+    (void)gpuIdx;
+    PixelList* p = new PixelList();
+    p->iCol.assign(iCol, iCol + npxl);
+    p->iRow.assign(iRow, iRow + npxl);
+    std::lock_guard<std::mutex> lk(g_mu);
+    *deviCol = p->iCol.data();
+    *deviRow = p->iRow.data();
+    g_pixels[*deviCol] = p;
+}
+
+// gpu/interface/Interface.h:26-29 (frequencies are used by the defocus
+// search only, which this path does not take)
+void ExpectPrefre(int gpuIdx, RFLOAT** devfreQ, RFLOAT* freQ, int npxl)
+{
+    (void)gpuIdx;
+    RFLOAT* f = new RFLOAT[npxl];
+    std::memcpy(f, freQ, sizeof(RFLOAT) * npxl);
+    *devfreQ = f;
+}
+
+// gpu/interface/Interface.h:31-38
+void ExpectLocalIn(int gpuIdx, Complex** devdatP, RFLOAT** devctfP, RFLOAT** devdefO,
+                   RFLOAT** devsigP, int nPxl, int cpyNumL, int searchType)
+{
+    (void)gpuIdx;
+    (void)searchType;
+    Slots* s = new Slots();
+    s->npxl = nPxl;
+    s->n = cpyNumL;
+    s->dat.resize((size_t)nPxl * cpyNumL);
+    s->ctf.resize((size_t)nPxl * cpyNumL);
+    s->sig.resize((size_t)nPxl * cpyNumL);
+    s->def.resize((size_t)nPxl * cpyNumL);
+    std::lock_guard<std::mutex> lk(g_mu);
+    *devdatP = s->dat.data();
+    *devctfP = s->ctf.data();
+    *devsigP = s->sig.data();
+    *devdefO = s->def.data();
+    g_slots[*devdatP] = s;
+}
+
+// gpu/interface/Interface.h:45-48
+void ExpectLocalV3D(int gpuIdx, ManagedArrayTexture* mgr, Complex* volume, int vdim)
+{
+    (void)gpuIdx;
+    std::lock_guard<std::mutex> lk(g_mu);
+    VolState& v = g_vols[mgr];
+    if (v.h) tg3_volume_destroy(v.h);
+    v.h = nullptr;
+    v.host = volume;
+    v.vdim = vdim;
+    v.pf = 0;
+}
+
+// gpu/interface/Interface.h:50-62: copy image imgId into slot threadId
+void ExpectLocalP(int gpuIdx, Complex* devdatP, RFLOAT* devctfP, RFLOAT* devdefO,
+                  RFLOAT* devsigP, Complex* datP, RFLOAT* ctfP, RFLOAT* defO, RFLOAT* sigP,
+                  int threadId, int imgId, int npxl, int cSearch)
+{
+    (void)gpuIdx;
+    (void)devctfP;
+    (void)devsigP;
+    (void)devdefO;
+    Slots* s = slots_of(devdatP);
+    if (threadId < 0 || threadId >= s->n || npxl != s->npxl) die("ExpectLocalP", TG3_ERR_ARG);
+    const size_t src = (size_t)imgId * npxl, dst = (size_t)threadId * npxl;
+    std::memcpy(&s->dat[dst], datP + src, sizeof(Complex) * npxl);
+    std::memcpy(&s->sig[dst], sigP + src, sizeof(RFLOAT) * npxl);
+    if (cSearch) std::memcpy(&s->def[dst], defO + src, sizeof(RFLOAT) * npxl);
+    else std::memcpy(&s->ctf[dst], ctfP + src, sizeof(RFLOAT) * npxl);
+}
+
+// gpu/interface/Interface.h:64-78
+void ExpectLocalHostA(int gpuIdx, RFLOAT** wC, RFLOAT** wR, RFLOAT** wT, RFLOAT** wD,
+                      double** oldR, double** oldT, double** oldD, double** trans,
+                      double** rot, double** dpara, int mR, int mT, int mD, int cSearch)
+{
+    (void)gpuIdx;
+    (void)cSearch;
+    *wC = new RFLOAT[1];
+    *wR = new RFLOAT[mR];
+    *wT = new RFLOAT[mT];
+    *wD = new RFLOAT[mD];
+    *oldR = new double[mR];
+    *oldT = new double[mT];
+    *oldD = new double[mD];
+    *trans = new double[mT * 2];
+    *rot = new double[mR * 4];
+    *dpara = new double[mD];
+}
+
+// gpu/interface/Interface.h:80-87: take a copy of the particle's hypotheses
+void ExpectLocalRTD(int gpuIdx, ManagedCalPoint* mcp, double* oldR, double* oldT, double* oldD,
+                    double* trans, double* rot, double* dpara)
+{
+    (void)gpuIdx;
+    (void)oldD;
+    (void)dpara;
+    std::lock_guard<std::mutex> lk(g_mu);
+    CalState& c = g_cal[mcp];
+    // the hypothesis counts are those of ManagedCalPoint::Init (getNR/getNT)
+    c.nR = mcp->getNR();
+    c.nT = mcp->getNT();
+    c.rot.assign(rot, rot + 4 * c.nR);
+    c.trans.assign(trans, trans + 2 * c.nT);
+    c.oldR.assign(oldR, oldR + c.nR);
+    c.oldT.assign(oldT, oldT + c.nT);
+}
+
+// gpu/interface/Interface.h:107-123: bind the volume and geometry; the
+// projection itself runs inside ExpectLocalM, fused with the scoring
+void ExpectLocalPreI3D(int gpuIdx, int datShift, ManagedArrayTexture* mgr, ManagedCalPoint* mcp,
+                       RFLOAT* devdefO, RFLOAT* devfreQ, int* deviCol, int* deviRow,
+                       RFLOAT phaseShift, RFLOAT conT, RFLOAT k1, RFLOAT k2, int pf, int idim,
+                       int vdim, int npxl, int interp)
+{
+    (void)gpuIdx;
+    (void)datShift;
+    (void)devdefO;
+    (void)devfreQ;
+    (void)phaseShift;
+    (void)conT;
+    if (k1 != 0 || k2 != 0) die("ExpectLocalPreI3D: defocus search", TG3_ERR_UNSUPPORTED);
+    if (interp != 1) die("ExpectLocalPreI3D: interpolation", TG3_ERR_UNSUPPORTED);
+    const PixelList* px = pixels_of(deviCol);
+    (void)deviRow;
+    std::lock_guard<std::mutex> lk(g_mu);
+    VolState& v = g_vols[mgr];
+    if (!v.host || v.vdim != vdim) die("ExpectLocalPreI3D: volume not set", TG3_ERR_STATE);
+    if (!v.h || v.pf != pf) {
+        if (v.h) tg3_volume_destroy(v.h);
+        v.h = nullptr;
+        ok("ExpectLocalPreI3D", tg3_volume_create(&v.h, reinterpret_cast<const float*>(v.host),
+                                                  vdim, pf));
+        v.pf = pf;
+    }
+    CalState& c = g_cal[mcp];
+    c.mgr = mgr;
+    c.idim = idim;
+    c.npxl = npxl;
+    c.iCol = px->iCol.data();
+    c.iRow = px->iRow.data();
+}
+
+// gpu/interface/Interface.h:125-139: project, shift, score and return the
+// marginal weights of the particle in slot datShift
+void ExpectLocalM(int gpuIdx, int datShift, ManagedCalPoint* mcp, Complex* devdatP,
+                  RFLOAT* devctfP, RFLOAT* devsigP, RFLOAT* wC, RFLOAT* wR, RFLOAT* wT,
+                  RFLOAT* wD, double oldC, int npxl)
+{
+    (void)gpuIdx;
+    (void)devctfP;
+    (void)devsigP;
+    Slots* s = slots_of(devdatP);
+    CalState c;
+    tg3_volume* h = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        c = g_cal[mcp];
+        h = g_vols[c.mgr].h;
+    }
+    if (!h || c.npxl != npxl) die("ExpectLocalM: call order", TG3_ERR_STATE);
+    const size_t off = (size_t)datShift * npxl;
+    float baseL = 0;
+    ok("ExpectLocalM",
+       tg3_ExpectLocal3D(h, reinterpret_cast<const float*>(&s->dat[off]), &s->ctf[off],
+                         &s->sig[off], c.iCol, c.iRow, npxl, c.idim, c.rot.data(), c.nR,
+                         c.trans.data(), c.nT, c.oldR.data(), c.oldT.data(), oldC, wC, wR, wT,
+                         nullptr, &baseL));
+    wD[0] = 1;   // one defocus hypothesis
+}
+
+// gpu/interface/Interface.h:141-152
+void ExpectLocalHostF(int gpuIdx, RFLOAT** wC, RFLOAT** wR, RFLOAT** wT, RFLOAT** wD,
+                      double** oldR, double** oldT, double** oldD, double** trans,
+                      double** rot, double** dpara, int cSearch)
+{
+    (void)gpuIdx;
+    (void)cSearch;
+    delete[] *wC;
+    delete[] *wR;
+    delete[] *wT;
+    delete[] *wD;
+    delete[] *oldR;
+    delete[] *oldT;
+    delete[] *oldD;
+    delete[] *trans;
+    delete[] *rot;
+    delete[] *dpara;
+}
+
+// gpu/interface/Interface.h:154-160
+void ExpectLocalFin(int gpuIdx, Complex** devdatP, RFLOAT** devctfP, RFLOAT** devdefO,
+                    RFLOAT** devfreQ, RFLOAT** devsigP, int cSearch)
+{
+    (void)gpuIdx;
+    (void)devctfP;
+    (void)devdefO;
+    (void)devsigP;
+    (void)cSearch;
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_slots.find(*devdatP);
+    if (it != g_slots.end()) {
+        delete it->second;
+        g_slots.erase(it);
+    }
+    if (devfreQ && *devfreQ) {
+        delete[] *devfreQ;
+        *devfreQ = nullptr;
+    }
+    for (auto& kv : g_vols)
+        if (kv.second.h) {
+            tg3_volume_destroy(kv.second.h);
+            kv.second.h = nullptr;
+        }
+    g_vols.clear();
+    g_cal.clear();
+}
+
+// gpu/interface/Interface.h:162-164
+void ExpectFreeIdx(int gpuIdx, int** deviCol, int** deviRow)
+{
+    (void)gpuIdx;
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_pixels.find(*deviCol);
+    if (it != g_pixels.end()) {
+        delete it->second;
+        g_pixels.erase(it);
+    }
+    *deviCol = nullptr;
+    *deviRow = nullptr;
+}
+
+// gpu/interface/Interface.h:199-208
+void ExpectRotran(Complex* traP, double* trans, double* rot, double* rotMat, const int* iCol,
+                  const int* iRow, int nR, int nT, int idim, int npxl)
+{
+    ok("ExpectRotran", tg3_ExpectRotran(reinterpret_cast<float*>(traP), trans, rot, rotMat, iCol,
+                                        iRow, nR, nT, idim, npxl));
+}
+
+// gpu/interface/Interface.h:210-219
+void ExpectProject(Complex* volume, Complex* rotP, double* rotMat, const int* iCol,
+                   const int* iRow, int nR, int pf, int interp, int vdim, int npxl)
+{
+    ok("ExpectProject",
+       tg3_ExpectProject(reinterpret_cast<const float*>(volume), reinterpret_cast<float*>(rotP),
+                         rotMat, iCol, iRow, nR, pf, interp, vdim, npxl));
+}
+
+// gpu/interface/Interface.h:221-237
+void ExpectGlobal3D(Complex* rotP, Complex* traP, Complex* datP, RFLOAT* ctfP, RFLOAT* sigRcpP,
+                    RFLOAT* wC, RFLOAT* wR, RFLOAT* wT, double* pR, double* pT, RFLOAT* baseL,
+                    int kIdx, int nK, int nR, int nT, int npxl, int imgNum)
+{
+    ok("ExpectGlobal3D",
+       tg3_ExpectGlobal3D(reinterpret_cast<const float*>(rotP), reinterpret_cast<const float*>(traP),
+                          reinterpret_cast<const float*>(datP), ctfP, sigRcpP, wC, wR, wT, pR, pT,
+                          baseL, kIdx, nK, nR, nT, npxl, imgNum));
+}
+
+// gpu/interface/Interface.h:294-318 (single-class form).  F3D is complex and
+// T3D is a complex Volume whose real parts hold T (Interface.cpp of the
+// reference converts it the same way around the call).
+void InsertFT(Volume& F3D, Volume& T3D, double* O3D, int* counter, MPI_Comm& hemi,
+              MPI_Comm& slav, Complex* datP, RFLOAT* ctfP, RFLOAT* sigRcpP,
+              CTFAttr* ctfaData, double* offS, RFLOAT* w, double* nR, double* nT, double* nD,
+              const int* iCol, const int* iRow, RFLOAT pixelSize, bool cSearch, int opf,
+              int npxl, int mReco, int idim, int dimSize, int imgNum)
+{
+    (void)hemi;
+    (void)slav;
+    const size_t n = F3D.sizeFT();
+    std::vector<RFLOAT> T(n);
+    for (size_t i = 0; i < n; i++) T[i] = REAL(T3D[i]);
+    const int vdim = F3D.nSlcFT();
+    (void)dimSize;
+    ok("InsertFT",
+       tg3_InsertFT(reinterpret_cast<float*>(&F3D[0]), T.data(), O3D, counter,
+                    reinterpret_cast<const float*>(datP), ctfP, sigRcpP,
+                    reinterpret_cast<const float*>(ctfaData), offS, w, nR, nT, nD, iCol, iRow,
+                    pixelSize, cSearch ? 1 : 0, opf, npxl, mReco, idim, vdim, imgNum,
+                    TG3_KERNEL_TRILINEAR));
+    for (size_t i = 0; i < n; i++) T3D[i] = COMPLEX(T[i], 0);
+}

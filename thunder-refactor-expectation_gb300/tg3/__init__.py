@@ -75,7 +75,7 @@ def lib():
             "tg3_ctx_workspace_bytes": ([_P], ctypes.c_size_t),
             "tg3_ctx_set_volume": ([_P, _I, _P, _I, _I, _I], _I),
             "tg3_ctx_set_pixels": ([_P, _P, _P, _I, _I], _I),
-            "tg3_local_phase_d": ([_P, _I, _I, _I] + [_P] * 15 + [_I], _I),
+            "tg3_local_phase_d": ([_P, _I, _I, _I] + [_P] * 14 + [_I], _I),
             "tg3_resample_d": ([_P, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _P], _I),
             "tg3_ctx_insert_begin": ([_P, _I, _I], _I),
             "tg3_insert_d": ([_P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _P], _I),
@@ -84,7 +84,7 @@ def lib():
             "tg3_translate_d": ([_P, _I, _I, _P, _P, _I, _P, _P], _I),
             "tg3_ctf_d": ([_P, _I, _F, _I, _P, _P, _I, _P, _P], _I),
             "tg3_project_d": ([_P, _I, _P, _I, _P], _I),
-            "tg3_local_phase": ([_P, _I, _I, _I] + [_P] * 15 + [_I], _I),
+            "tg3_local_phase": ([_P, _I, _I, _I] + [_P] * 14 + [_I], _I),
             "tg3_ctx_set_timing": ([_P, _I], _I),
             "tg3_ctx_stage_times": ([_P, _P, _P, _I], _I),
         }
