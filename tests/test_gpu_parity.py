@@ -246,12 +246,6 @@ def test_resample_rejects_bad_permutation():
     assert st == tg3.ERR_ARG
 
 
-def _fsc_ok(F, Fr, vdim, lo=0.999):
-    f = O.fsc(F, Fr, vdim, vdim // 2)
-    # shells that hold inserted data (the cutoff times pf)
-    return f
-
-
 @pytest.mark.parametrize("kernel", [tg3.KERNEL_MKB, tg3.KERNEL_TRILINEAR])
 def test_insert(small, kernel):
     rng = np.random.default_rng(23)
@@ -299,7 +293,7 @@ def test_insert(small, kernel):
     assert np.abs(Fg - Fr).max() < 2e-4 * scale
     assert np.abs(Tg - Tr).max() < 2e-4 * np.abs(Tr).max()
     rmax = int(12 * pf)
-    f = O.fsc(Fg, Fr, vdim, rmax)
+    f = O.fsc(Fg, Fr, rmax)
     assert f[1:].min() >= 0.999, f
 
 
