@@ -57,7 +57,7 @@ struct Buffer {
 };
 
 struct Volume {
-    float4* pairs = nullptr;   // [vdim][vdim][nx] of (V[x], V[x+1])
+    float4* pairs = nullptr;   // [vdim][vdim][nx] corner blocks, 2 float4 each
     int vdim = 0;
     int pf = 0;
     size_t bytes = 0;

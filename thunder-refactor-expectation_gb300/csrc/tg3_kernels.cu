@@ -141,17 +141,26 @@ __global__ void k_ctf(const float* __restrict__ attr, int nImg, float px, int id
     }
 }
 
+// Corner-block layout of the projection volume: the 32-byte element of voxel
+// (z, y, x) holds V[z][y][x], V[z][y][x+1], V[z][y+1][x], V[z][y+1][x+1]
+// (row y+1 taken modulo vdim, the wrap of Volume::iFTHalf), so a trilinear
+// sample reads one aligned 32-byte sector in each of its two z slabs.
 __global__ void k_volume_pairs(const float2* __restrict__ vol, int vdim,
-                               float4* __restrict__ pairs)
+                               float4* __restrict__ blocks)
 {
     const int nx = vdim / 2 + 1;
     const size_t n = (size_t)vdim * vdim * nx;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(i % nx);
-        float2 a = vol[i];
-        float2 b = (x + 1 < nx) ? vol[i + 1] : make_float2(0.f, 0.f);
-        pairs[i] = make_float4(a.x, a.y, b.x, b.y);
+        const int y = (int)((i / nx) % vdim);
+        const size_t z = i / ((size_t)nx * vdim);
+        const size_t i1 = (z * vdim + (y + 1 == vdim ? 0 : y + 1)) * nx + x;
+        const float2 zero = make_float2(0.f, 0.f);
+        const float2 a = vol[i], b = (x + 1 < nx) ? vol[i + 1] : zero;
+        const float2 c = vol[i1], d = (x + 1 < nx) ? vol[i1 + 1] : zero;
+        blocks[2 * i] = make_float4(a.x, a.y, b.x, b.y);
+        blocks[2 * i + 1] = make_float4(c.x, c.y, d.x, d.y);
     }
 }
 
@@ -219,14 +228,20 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
         const int x0 = (int)xf, y0 = (int)yf, z0 = (int)zf;
         const float fx = x - xf, fy = y - yf, fz = z - zf;
         const float wx[2] = {1.f - fx, fx}, wy[2] = {1.f - fy, fy}, wz[2] = {1.f - fz, fz};
-        const int ys[2] = {y0 < 0 ? y0 + vdim : y0, y0 + 1 < 0 ? y0 + 1 + vdim : y0 + 1};
+        // corner block at row y0 carries rows y0 and y0 + 1 (wrapped)
+        const int ys = y0 < 0 ? y0 + vdim : y0;
         const int zs[2] = {z0 < 0 ? z0 + vdim : z0, z0 + 1 < 0 ? z0 + 1 + vdim : z0 + 1};
         float4 c[4];
 #pragma unroll
-        for (int k = 0; k < 2; k++)
-#pragma unroll
-            for (int j = 0; j < 2; j++)
-                c[2 * k + j] = __ldg(vol + ((size_t)zs[k] * vdim + ys[j]) * nx + x0);
+        for (int k = 0; k < 2; k++) {
+            // one 256-bit read-only load of the 32-byte corner block
+            const float4* e = vol + 2 * (((size_t)zs[k] * vdim + ys) * nx + x0);
+            asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                : "=f"(c[2 * k].x), "=f"(c[2 * k].y), "=f"(c[2 * k].z), "=f"(c[2 * k].w),
+                  "=f"(c[2 * k + 1].x), "=f"(c[2 * k + 1].y), "=f"(c[2 * k + 1].z),
+                  "=f"(c[2 * k + 1].w)
+                : "l"(e));
+        }
         float re = 0.f, im = 0.f;
 #pragma unroll
         for (int k = 0; k < 2; k++)
