@@ -235,6 +235,44 @@ int tg3_insert_d(tg3_ctx* ctx, int nP, const float* dat, const float* ctf,
 int tg3_ctx_insert_read_d(tg3_ctx* ctx, float* F, float* T, int accumulate);
 
 /* ------------------------------------------------------------------------
+ * Allocation-free local scoring.  No counterpart in the reference.
+ *
+ * For callers that cannot let a library allocate device memory: an
+ * application that has given the GPU's memory to its own pool allocator, or
+ * one that scores particles from many host threads at once, where every
+ * cudaMalloc / cudaFree would synchronise the device and stall the other
+ * threads.  It computes what tg3_local_phase_d computes for one particle on
+ * the FP32 path, with its scratch in a fixed device array that belongs to the
+ * library image (tg3_noalloc_scratch_bytes() bytes, 64 MiB, held by every GPU
+ * that loads the library until the process exits).  It calls no allocator.
+ *
+ * All pointers are device memory: volume is the plain complex half-FT volume
+ * [vdim][vdim][vdim/2 + 1] (padding factor pf); iCol/iRow the K unpadded
+ * pixel indices of an image of edge idim; dat [K] complex, ctf, sigRcp [K];
+ * quat [nR][4], trans [nT][2]; priors pwR [nR], pwT [nT], pwC [1] (NULL for
+ * 1).  Outputs as tg3_local_phase_d with nP = 1; dvp may be NULL.
+ *
+ * Limit: 256 + 4 ((nR + nT) Kp + nR nT + nR) + 512 bytes (rounded up to
+ * 256-byte pieces) must fit the scratch, Kp = 2K rounded up to 64; larger
+ * sets are rejected with TG3_ERR_ARG.  The call returns after the work has
+ * finished on `stream` (cudaStream_t, NULL for the legacy stream).
+ * The first call on a device looks up the scratch array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  Every call shares the one array: calls that
+ * may overlap on the GPU (other streams, unsynchronised host threads) race
+ * and must not be issued.  Each call writes all the scratch it reads, so no
+ * clearing is needed between calls. */
+size_t tg3_noalloc_scratch_bytes(void);
+int tg3_local_phase_noalloc(const float* volume, int vdim, int pf,
+                            const int* iCol, const int* iRow, int K, int idim,
+                            const float* dat, const float* ctf,
+                            const float* sigRcp, const double* quat, int nR,
+                            const double* trans, int nT, const double* pwR,
+                            const double* pwT, const double* pwC, double* wC,
+                            double* wR, double* wT, double* baseL, float* dvp,
+                            void* stream);
+
+/* ------------------------------------------------------------------------
  * Kernel-level device entry points (device pointers, explicit stream).
  * --------------------------------------------------------------------- */
 /* rotMat [n][9] (double, row-major) from quat [n][4]. */

@@ -29,6 +29,7 @@ EXPORTS = [
     "tg3_local_phase_d", "tg3_resample_d", "tg3_ctx_insert_begin", "tg3_insert_d",
     "tg3_ctx_insert_read_d", "tg3_rotmat_d", "tg3_translate_d", "tg3_ctf_d",
     "tg3_project_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
+    "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert")
 
@@ -87,6 +88,9 @@ def lib():
             "tg3_local_phase": ([_P, _I, _I, _I] + [_P] * 14 + [_I], _I),
             "tg3_ctx_set_timing": ([_P, _I], _I),
             "tg3_ctx_stage_times": ([_P, _P, _P, _I], _I),
+            "tg3_noalloc_scratch_bytes": ([], ctypes.c_size_t),
+            "tg3_local_phase_noalloc": ([_P, _I, _I, _P, _P, _I, _I, _P, _P, _P, _P, _I, _P, _I,
+                                         _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
