@@ -152,6 +152,27 @@ def pin(torch, host):
 
 
 # ---------------------------------------------------------------- tg3 arm ---
+def fp32_sgemm_peak(torch, dev):
+    """cuBLAS FP32 SGEMM (TF32 off) throughput, the CUDA-core denominator."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.randn(8192, 8192, device=dev)
+    b = torch.randn(8192, 8192, device=dev)
+    for _ in range(3):
+        a @ b
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 1e9
+    for _ in range(5):
+        e0.record()
+        a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    return 2 * 8192 ** 3 / (best * 1e-3) / 1e12
+
+
 def run_tg3(args, rank, world, local_rank):
     import torch
     import tg3
@@ -162,7 +183,6 @@ def run_tg3(args, rank, world, local_rank):
     W, vol, st, batches = make_workload(torch, dev, nP, args.batches, 1000 + 1 + 97 * rank,
                                         box=args.box)
     nR, nT, K = W["nR"], W["nT"], st.K
-    prec = tg3.SCORE_BF16X3 if args.precision == "bf16x3" else tg3.SCORE_FP32
     ctx = tg3.Context(local_rank)
     ctx.set_volume(0, vol, W["pf"])
     ctx.set_pixels(st.iCol, st.iRow, W["box"])
@@ -178,8 +198,9 @@ def run_tg3(args, rank, world, local_rank):
                w_t=torch.empty((nP, nT), dtype=torch.float64, device=dev),
                top=torch.empty(nP, dtype=torch.int32, device=dev))
     stream = torch.cuda.ExternalStream(ctx.stream)
+    launches_per_step = 7   # project, shift, x0, cross term, weights, 2 x resample
 
-    def step(i):
+    def step(i, prec):
         b = dbat[i % len(dbat)]
         ctx.local_phase(nP, nR, nT, b["dat"], b["ctf"], b["sig"], b["quat"], b["trans"],
                         b["pwR"], b["pwT"], b["pwC"], None, out["wC"], out["wR"], out["wT"],
@@ -189,55 +210,59 @@ def run_tg3(args, rank, world, local_rank):
         ctx.resample(nP, nT, out["wT"], b["pwT"], b["perm_t"], b["u0_t"], b["peak_t"], nT,
                      out["src_t"], out["w_t"], out["top"])
 
-    launches_per_step = 7   # project, shift, x0, cross term, weights, 2 x resample
-    for i in range(args.warmup):
-        step(i)
-    ctx.sync()
-
-    # FP32 SGEMM (TF32 off) reference throughput for the plain path's roofline
-    fp32_peak = None
-    if prec == tg3.SCORE_FP32:
-        torch.backends.cuda.matmul.allow_tf32 = False
-        a = torch.randn(8192, 8192, device=dev)
-        bmat = torch.randn(8192, 8192, device=dev)
-        for _ in range(3):
-            a @ bmat
+    def timed(prec):
+        """W warm-up steps, then exactly K timed steps between barriers and
+        device synchronisations, CUDA events on the library's stream."""
+        for i in range(args.warmup):
+            step(i, prec)
+        ctx.sync()
+        barrier(world)
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        best = 1e9
-        for _ in range(5):
-            e0.record()
-            a @ bmat
-            e1.record()
-            torch.cuda.synchronize()
-            best = min(best, e0.elapsed_time(e1))
-        fp32_peak = 2 * 8192 ** 3 / (best * 1e-3) / 1e12
-        del a, bmat
+        clk = ClockSampler(local_rank)
+        clk.start()
+        ctx.set_timing(True)
+        ctx.stage_times(reset=True)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for i in range(args.steps):
+                step(i, prec)
+            ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+        barrier(world)
+        clocks = clk.stop()
+        stages = ctx.stage_times(reset=True)
+        ctx.set_timing(False)
+        ctx.sync()
+        return reduce_max(world, ev0.elapsed_time(ev1)), stages, clocks
 
-    # ---- timed region (device-resident inputs)
-    barrier(world)
-    torch.cuda.synchronize()
-    clk = ClockSampler(local_rank)
-    clk.start()
+    prec = tg3.SCORE_BF16X3 if args.precision == "bf16x3" else tg3.SCORE_FP32
+    ms, stages, clocks = timed(prec)
+    plain = None
+    if prec != tg3.SCORE_FP32 and not args.no_compare:
+        ms_p, stages_p, clocks_p = timed(tg3.SCORE_FP32)
+        plain = (ms_p, stages_p, clocks_p)
+
+    # ---- insertion of every particle's best pose (MKB kernel), timed alone
+    ctx.insert_begin(W["pf"] * W["box"], W["pf"])
+    ins_w = torch.ones(nP, dtype=torch.float32, device=dev)
+    zero2 = torch.zeros((nP, 2), dtype=torch.float64, device=dev)
+    ins_q = [b["quat"][:, 0, :].contiguous() for b in dbat]
+    ins_t = [b["trans"][:, 0, :].contiguous() for b in dbat]
+    for i in range(2):
+        ctx.insert(nP, dbat[i % len(dbat)]["dat"], dbat[i % len(dbat)]["ctf"],
+                   ins_q[i % len(dbat)], ins_t[i % len(dbat)], zero2, ins_w, tg3.KERNEL_MKB)
+    ctx.sync()
     ctx.set_timing(True)
     ctx.stage_times(reset=True)
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    t_wall = time.perf_counter()
-    with torch.cuda.stream(stream):
-        ev0.record(stream)
-        for i in range(args.steps):
-            step(i)
-        ev1.record(stream)
-    ev1.synchronize()
-    wall = time.perf_counter() - t_wall
-    torch.cuda.synchronize()
-    barrier(world)
-    clocks = clk.stop()
-    stages = ctx.stage_times(reset=True)
+    for i in range(args.steps):
+        ctx.insert(nP, dbat[i % len(dbat)]["dat"], dbat[i % len(dbat)]["ctf"],
+                   ins_q[i % len(dbat)], ins_t[i % len(dbat)], zero2, ins_w, tg3.KERNEL_MKB)
+    ins_stage = ctx.stage_times(reset=True)["insert"]
     ctx.set_timing(False)
-    ms = ev0.elapsed_time(ev1)
-    ms = reduce_max(world, ms)
+    ctx.sync()
 
     # ---- end to end: host buffers, copies inside the timed region
     hbat = [pin(torch, b) for b in batches]
@@ -274,23 +299,47 @@ def run_tg3(args, rank, world, local_rank):
     e2e_s = reduce_max(world, time.perf_counter() - t0)
     barrier(world)
 
-    value = nP * args.steps * world / (ms * 1e-3)
-    e2e_value = nP * args.e2e_steps * world / e2e_s
-    cross_ms, cross_n = stages["cross"]
-    flop = 4.0 * K * nR * nT * nP          # real part of the complex cross term
-    achieved = flop / (cross_ms / cross_n * 1e-3) / 1e12
     hbm, bf16, kind = peaks()
-    if prec == tg3.SCORE_FP32:
-        peak, peak_note = fp32_peak, "cuBLAS FP32 SGEMM (TF32 off) measured live"
-    else:
-        peak, peak_note = bf16, f"bf16 dense tensor, {kind} (MEASURED_PEAKS.json)"
-    proj_ms, proj_n = stages["project"]
-    proj_bytes = 72.0 * nR * K * nP
+    fp32_peak = fp32_sgemm_peak(torch, dev)
+
+    def per_launch(st_, name):
+        t, n = st_[name]
+        return t / max(n, 1)
+
+    flop = 4.0 * K * nR * nT * nP          # real part of the complex cross term
+    proj_bytes = 72.0 * nR * K * nP        # 8 corners x 8 B read + 8 B written per sample
+
+    def cross_roof(st_, p_):
+        ach = flop / (per_launch(st_, "cross") * 1e-3) / 1e12
+        if p_ == tg3.SCORE_FP32:
+            pk, note = fp32_peak, "cuBLAS FP32 SGEMM (TF32 off) measured live in this run"
+        else:
+            pk, note = bf16, f"bf16 dense tensor burst, {kind} (MEASURED_PEAKS.json)"
+        return {"kernel": "k_gemm_nt_fp32" if p_ == tg3.SCORE_FP32 else "k_gemm_bf16x3 (tcgen05)",
+                "bound": "tensor", "achieved": round(ach, 2), "peak": round(pk, 1),
+                "unit": "TFLOP/s", "frac": round(ach / pk, 4), "peak_source": note,
+                "traffic": TRAFFIC.get("cross_bf16x3" if p_ != tg3.SCORE_FP32 else "cross_fp32"),
+                "algorithmic_flop_per_launch": flop,
+                "executed_bf16_flop_per_launch": 3 * flop if p_ != tg3.SCORE_FP32 else None}
+
+    def proj_roof(st_):
+        ach = proj_bytes / (per_launch(st_, "project") * 1e-3) / 1e9
+        return {"kernel": "k_project", "bound": "hbm", "achieved": round(ach, 1),
+                "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4),
+                "peak_source": f"hbm_gbs, {kind} (MEASURED_PEAKS.json)",
+                "traffic": TRAFFIC.get("project"),
+                "algorithmic_bytes_per_launch": proj_bytes}
+
+    dominant = max(("project", "cross"), key=lambda k: per_launch(stages, k))
+    roof = proj_roof(stages) if dominant == "project" else cross_roof(stages, prec)
+    ins_ms = ins_stage[0] / max(ins_stage[1], 1)
+    ins_bytes = 705.5 * K * nP             # 16 B in + 28.7 voxel updates x 24 B per pixel
+    value = nP * args.steps * world / (ms * 1e-3)
     res = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32" if prec == tg3.SCORE_FP32 else "bf16x3+fp32",
+        "dtype": "fp32" if prec == tg3.SCORE_FP32 else "bf16x3 cross term, fp32 elsewhere",
         "data": "synthetic (seeded Gaussian-blob map and particles, generated on the GPU)",
         "config": {"workload": f"local particle-filter phase, box {W['box']}, K={K}, "
                                f"{nR} rotations x {nT} translations per particle",
@@ -299,26 +348,40 @@ def run_tg3(args, rank, world, local_rank):
                    "l2": "inputs larger than L2: the projection bank alone is "
                          f"{nP * nR * ctx_kp(K) * 4 / 1e9:.1f} GB per step"},
         "clocks": clocks,
-        "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "wall_s": round(e2e_s, 3)},
+        "e2e": {"value": round(nP * args.e2e_steps * world / e2e_s, 2), "unit": UNIT,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "wall_s": round(e2e_s, 3)},
         "gpu_launches": launches_per_step * args.steps,
-        "roofline": {"kernel": "cross term GEMM", "bound": "tensor",
-                     "achieved": round(achieved, 2), "peak": round(peak, 1) if peak else None,
-                     "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
-                     "peak_source": peak_note, "traffic": None,
-                     "algorithmic_flop_per_launch": flop},
+        "roofline": roof,
+        "roofline_cross_term": cross_roof(stages, prec),
+        "roofline_projection": proj_roof(stages),
         "stages": {k: {"ms_per_launch": round(v[0] / max(v[1], 1), 4), "launches": v[1]}
                    for k, v in stages.items() if v[1]},
-        "projection": {"achieved_gbs": round(proj_bytes / (proj_ms / proj_n * 1e-3) / 1e9, 1),
-                       "peak_gbs": hbm, "frac": round(proj_bytes / (proj_ms / proj_n * 1e-3) / 1e9 / hbm, 4),
-                       "bytes_per_launch": proj_bytes},
+        "insertion": {"kernel": "k_insert (MKB, a = 1.9, alpha = 15)", "particles": nP,
+                      "ms_per_launch": round(ins_ms, 4),
+                      "particles_per_s": round(nP / (ins_ms * 1e-3), 1),
+                      "achieved_gbs": round(ins_bytes / (ins_ms * 1e-3) / 1e9, 1),
+                      "peak_gbs": hbm, "frac": round(ins_bytes / (ins_ms * 1e-3) / 1e9 / hbm, 4)},
         "hypotheses_per_s": round(value * nR * nT, 1),
-        "wall_s_timed": round(wall, 3),
     }
+    if plain is not None:
+        ms_p, stages_p, clocks_p = plain
+        v_p = nP * args.steps * world / (ms_p * 1e-3)
+        res["plain_fp32"] = {"value": round(v_p, 2), "ms_per_step": round(ms_p / args.steps, 4),
+                             "stages": {k: round(v[0] / max(v[1], 1), 4)
+                                        for k, v in stages_p.items() if v[1]},
+                             "roofline_cross_term": cross_roof(stages_p, tg3.SCORE_FP32),
+                             "clocks": clocks_p}
+        res["speedup_vs_plain_fp32"] = round(value / v_p, 3)
     if rank == 0 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(st, batches[0], W, args.cpu_sample)
     ctx.close()
     return res
+
+
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+# the ncu captures summarised in profiles/ (box 256, 64 particles per launch).
+TRAFFIC = {}
 
 
 def ctx_kp(K):
@@ -487,7 +550,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="tg3", choices=["tg3", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16x3"])
+    ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16x3"])
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the plain FP32 measurement beside a bf16x3 run")
     ap.add_argument("--batch", type=int, default=128, help="particles per step")
     ap.add_argument("--batches", type=int, default=3, help="distinct particle batches cycled")
     ap.add_argument("--e2e-steps", type=int, default=10)
