@@ -214,6 +214,21 @@ enum {
 int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);
 
+/* Global scan of nImg images over one shared set of nR rotations and nT
+ * translations, for the context's class-`cls` volume: the scan of
+ * Optimiser::doGlobalSearch (src/Optimiser.cpp:759-899), the work of
+ * ExpectProject + ExpectGlobal3D kept on the device.  rotMat [nR][9] and
+ * trans [nT][2] (double), dat [nImg][K] complex, ctf/sigRcp [nImg][K],
+ * priors pR [nR], pT [nT].  Outputs per image, relative to its best
+ * hypothesis: wC [nImg], wR [nImg][nR], wT [nImg][nT], baseL [nImg]
+ * (double); dvp [nImg][nR][nT] (float, may be NULL). */
+int tg3_global_scan_d(tg3_ctx* ctx, int cls, int nImg, int nR, int nT,
+                      const float* dat, const float* ctf, const float* sigRcp,
+                      const double* rotMat, const double* trans,
+                      const double* pR, const double* pT, double* wC,
+                      double* wR, double* wT, double* baseL, float* dvp,
+                      int precision);
+
 /* Device form of tg3_resample (all pointers device memory, stream of ctx). */
 int tg3_resample_d(tg3_ctx* ctx, int nP, int n, const double* u,
                    const double* w, const int* perm, const double* u0,

@@ -44,7 +44,7 @@ def small():
     bm = synth.blob_map(rng, 20, (2.0, 4.0), px, 9.0)
     vol = synth.padded_volume(bm, box, pf).numpy()
     vol32 = vol.astype(np.complex64)
-    st = synth.make_stack(5, [bm], box, px, pf, rU, synth.config_rL(box, px), 16, 2.0, 0.5)
+    st = synth.make_stack(5, [bm], box, px, pf, rU, synth.config_rL(box, px), 48, 2.0, 0.5)
     return dict(rng=rng, box=box, pf=pf, px=px, iCol=iCol, iRow=iRow, vol=f32(vol32),
                 vol32=vol32, st=st)
 
@@ -384,3 +384,42 @@ def test_bad_geometry_rejected(small):
         assert e.value.status == tg3.ERR_ARG
     finally:
         c.close()
+
+
+@pytest.mark.parametrize("precision", [tg3.SCORE_FP32, tg3.SCORE_BF16X3])
+def test_global_scan(small, ctx, precision):
+    """Device global scan (shared rotations x translations for many images)
+    against the oracle's doGlobalSearch restatement."""
+    rng = np.random.default_rng(41)
+    st = small["st"]
+    nImg, nR, nT = 40, 70, 9     # 360 columns: two split-bf16 column tiles
+    q = synth.haar_quaternions(rng, nR)
+    mat = np.ascontiguousarray(O.rotmat(q).reshape(-1, 9))
+    trans = synth.global_translations(1, 1.0)
+    pR = rng.random(nR) + 0.5
+    pT = rng.random(nT) + 0.5
+    dat = st.dat[:nImg].astype(np.complex64)
+    ctf = st.ctf[:nImg].astype(np.float32)
+    sig = st.sigRcp[:nImg].astype(np.float32)
+    o = dict(wC=torch.empty(nImg, dtype=torch.float64, device=DEV),
+             wR=torch.empty((nImg, nR), dtype=torch.float64, device=DEV),
+             wT=torch.empty((nImg, nT), dtype=torch.float64, device=DEV),
+             base=torch.empty(nImg, dtype=torch.float64, device=DEV),
+             dvp=torch.empty((nImg, nR, nT), dtype=torch.float32, device=DEV))
+    ctx.global_scan(0, nImg, nR, nT, dev(dat), dev(ctf), dev(sig), dev(mat), dev(trans),
+                    dev(pR), dev(pT), o["wC"], o["wR"], o["wT"], o["base"], o["dvp"], precision)
+    ctx.sync()
+    g = {k: v.cpu().numpy() for k, v in o.items()}
+    rotP = O.project(small["vol"], mat, small["iCol"], small["iRow"], small["pf"])
+    traP = O.translate(f32(trans), small["box"], small["iCol"], small["iRow"])
+    r = O.score_global(rotP, traP, f32(dat), f32(ctf), f32(sig), pR, pT)
+    rel = np.abs(g["dvp"] - r["dvp"]) / np.abs(r["dvp"])
+    assert rel.max() < 1e-4, rel.max()
+    for l in range(nImg):
+        assert np.argmax(g["dvp"][l]) == np.argmax(r["dvp"][l])
+        a = g["wR"][l] / g["wR"][l].sum()
+        b = r["wR"][l * nR:(l + 1) * nR]
+        np.testing.assert_allclose(a, b / b.sum(), atol=2e-3)
+        a = g["wT"][l] / g["wT"][l].sum()
+        b = r["wT"][l * nT:(l + 1) * nT]
+        np.testing.assert_allclose(a, b / b.sum(), atol=2e-3)

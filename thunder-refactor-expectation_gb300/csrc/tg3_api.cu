@@ -4,6 +4,7 @@
 // host buffers, and the kernel sequences of the E-step and the insertion.
 // Every failure returns a status and records a message; nothing falls back to
 // host computation.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -151,6 +152,14 @@ static int check_geometry(tg3_ctx* c, int vdim, int pf)
     if (c->px.maxRadius * pf + 2.0 > vdim / 2)
         return fail(TG3_ERR_ARG, "pixel radius " + std::to_string(c->px.maxRadius) +
                                      " x pf does not fit the volume edge " + std::to_string(vdim));
+    return TG3_OK;
+}
+
+// The weights kernel keeps 2 nT floats in shared memory.
+static int check_weights_shape(int nR, int nT)
+{
+    if (nR <= 0 || (size_t)2 * nT * sizeof(float) > 48 * 1024)
+        return fail(TG3_ERR_UNSUPPORTED, "nT must not exceed 6144");
     return TG3_OK;
 }
 
@@ -415,6 +424,7 @@ static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
         if (c->vol[k].pairs && (c->vol[k].vdim != v0.vdim || c->vol[k].pf != v0.pf))
             return fail(TG3_ERR_ARG, "all class volumes must share one edge and pf");
     if ((st = check_geometry(c, v0.vdim, v0.pf))) return st;
+    if ((st = check_weights_shape(nR, nT))) return st;
     float* P = (float*)ws_get(c, WS_P, sizeof(float) * (size_t)nP * nR * Kp, &st);
     if (!P) return st;
     float* A = (float*)ws_get(c, WS_A, sizeof(float) * (size_t)nP * nT * Kp, &st);
@@ -461,7 +471,7 @@ static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
     }
     {
         StageTimer tm(c, TG3_STAGE_WEIGHTS);
-        TG3_CUDA(launch_weights(D, (long long)nR * nT, nT, nR, nT, 1, nP, nullptr, x0, pwR, nR,
+        TG3_CUDA(launch_weights(D, (long long)nR * nT, nT, nR, nT, 1, nP, nullptr, 0, x0, pwR, nR,
                                 pwT, nT, pwC, wC, wR, wT, baseL, dvp, s));
     }
     return TG3_OK;
@@ -750,7 +760,8 @@ extern "C" int tg3_ExpectGlobal3D(const float* rotP, const float* traP, const fl
     if (nK <= 0 || kIdx < 0 || kIdx >= nK || nR <= 0 || nT <= 0 || npxl <= 0 || imgNum <= 0 ||
         nT > 4096)
         return fail(TG3_ERR_ARG, "bad ExpectGlobal3D sizes");
-    int st = TG3_OK;
+    int st = check_weights_shape(nR, nT);
+    if (st) return st;
     tg3_ctx* c = default_ctx(&st);
     if (!c) return st;
     cudaStream_t s = c->stream;
@@ -816,13 +827,13 @@ extern "C" int tg3_ExpectGlobal3D(const float* rotP, const float* traP, const fl
             k_sc2_rows<<<g3, 256, 0, s>>>(ss, cc, K, (float*)(b + osc), Kq);
             TG3_LAUNCH_CHECK("norm operand");
         }
-        // cross term: D[r][l nT + t] = -2 sum A''[l t] . P[r]
-        TG3_CUDA(launch_gemm_nt_fp32(P, 0, Kp, A, 0, Kp, nR, n * nT, Kp, 1, D, 0, n * nT, nullptr, 0,
-                                     -2.0f, s));
+        // cross term, written image-major: D[l][r][t] = -2 sum A''[l t] . P[r]
+        TG3_CUDA(launch_gemm_nt_fp32(P, 0, Kp, A, 0, Kp, nR, n * nT, Kp, 1, D, 0, nT, nullptr, 0,
+                                     -2.0f, s, nT, (long long)nR * nT));
         // norm term: N[r][l] = sum_p |P_rp|^2 sigRcp_lp ctf_lp^2
         TG3_CUDA(launch_gemm_nt_fp32(P2, 0, Kq, (const float*)(b + osc), 0, Kq, nR, n, Kq, 1,
                                      (float*)(b + onr), 0, n, nullptr, 0, 1.0f, s));
-        TG3_CUDA(launch_weights(D, 0, n * nT, nR, nT, n, n, (const float*)(b + onr),
+        TG3_CUDA(launch_weights(D, (long long)nR * nT, nT, nR, nT, 1, n, (const float*)(b + onr), n,
                                 (const double*)(b + ox0), (const double*)(b + opr), 0,
                                 (const double*)(b + opt), 0, nullptr, (double*)(b + owc),
                                 (double*)(b + owr), (double*)(b + owt), (double*)(b + obs), nullptr, s));
@@ -1067,6 +1078,134 @@ extern "C" int tg3_ctx_stage_times(tg3_ctx* c, double* ms, int* launches, int re
         if (reset) {
             c->stageMs[i] = 0;
             c->stageLaunches[i] = 0;
+        }
+    }
+    return TG3_OK;
+}
+
+// ======================================================= global scan (device)
+namespace tg3 {
+// |P|^2 of padded projection rows (floats, or split bf16 planes with the lo
+// plane loOff elements after the hi plane) into rows of ldq floats.
+__global__ void k_abs2_from(const float* __restrict__ P, long long loOff, int K, int Kp,
+                            float* __restrict__ out, int ldq)
+{
+    const int r = blockIdx.x;
+    for (int p = threadIdx.x; p < ldq; p += blockDim.x) {
+        float v = 0.f;
+        if (p < K) {
+            float re, im;
+            if (loOff == 0) {
+                const float2 a = reinterpret_cast<const float2*>(P + (size_t)r * Kp)[p];
+                re = a.x;
+                im = a.y;
+            } else {
+                const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(
+                    reinterpret_cast<const __nv_bfloat16*>(P) + (size_t)r * Kp);
+                const __nv_bfloat162* l = reinterpret_cast<const __nv_bfloat162*>(
+                    reinterpret_cast<const __nv_bfloat16*>(P) + loOff + (size_t)r * Kp);
+                const float2 hf = __bfloat1622float2(h[p]), lf = __bfloat1622float2(l[p]);
+                re = hf.x + lf.x;
+                im = hf.y + lf.y;
+            }
+            v = re * re + im * im;
+        }
+        out[(size_t)r * ldq + p] = v;
+    }
+}
+}  // namespace tg3
+
+extern "C" int tg3_global_scan_d(tg3_ctx* c, int cls, int nImg, int nR, int nT, const float* dat,
+                                 const float* ctf, const float* sigRcp, const double* rotMat,
+                                 const double* trans, const double* pR, const double* pT,
+                                 double* wC, double* wR, double* wT, double* baseL, float* dvp,
+                                 int precision)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].pairs)
+        return fail(TG3_ERR_STATE, "volume of the class not set");
+    if (nImg <= 0 || nR <= 0 || nT <= 0 || nT > 2048) return fail(TG3_ERR_ARG, "bad scan shape");
+    if (!dat || !ctf || !sigRcp || !rotMat || !trans || !pR || !pT || !wC || !wR || !wT || !baseL)
+        return fail(TG3_ERR_ARG, "null device pointer");
+    if (precision != TG3_SCORE_FP32 && precision != TG3_SCORE_BF16X3)
+        return fail(TG3_ERR_ARG, "unknown precision");
+    const bool split = precision == TG3_SCORE_BF16X3;
+    if (split && !bf16x3_available()) return fail(TG3_ERR_UNSUPPORTED, "no TMA encoder");
+    const Volume& v = c->vol[cls];
+    if ((st = check_geometry(c, v.vdim, v.pf))) return st;
+    if ((st = check_weights_shape(nR, nT))) return st;
+    const int K = c->px.K, Kp = c->px.Kp, Kq = (int)round_up(K, 64);
+    // images per pass: keep the likelihood block within 4 GiB
+    long long ib = (4LL << 30) / (4LL * nR * nT);
+    const int IB = (int)std::max(1LL, std::min(std::min((long long)nImg, ib), 65535LL));
+    // workspace
+    float* P = (float*)ws_get(c, WS_P, 4 * (size_t)nR * Kp, &st);
+    if (!P) return st;
+    float* A = (float*)ws_get(c, WS_A, 4 * (size_t)IB * nT * Kp, &st);
+    if (!A) return st;
+    float* D = (float*)ws_get(c, WS_D, 4 * (size_t)IB * nR * nT, &st);
+    if (!D) return st;
+    float* nrmG = (float*)ws_get(c, WS_NRM, 4 * (size_t)nR * IB, &st);
+    if (!nrmG) return st;
+    double* x0 = (double*)ws_get(c, WS_X0, 8 * (size_t)nImg, &st);
+    if (!x0) return st;
+    Arena ar(c, WS_MISC);
+    const size_t oAbs = ar.add(4 * (size_t)nR * Kq), oBank = ar.add(8 * (size_t)nT * K),
+                 oSc = ar.add(4 * (size_t)IB * Kq);
+    char* m = (char*)ws_get(c, WS_MISC, ar.used, &st);
+    if (!m) return st;
+    float* abs2 = (float*)(m + oAbs);
+    float2* bank = (float2*)(m + oBank);
+    float* sc2 = (float*)(m + oSc);
+    cudaStream_t s = c->stream;
+    const long long splitP = split ? (long long)nR * Kp : 0;
+    {
+        StageTimer tm(c, TG3_STAGE_PROJECT);
+        TG3_CUDA(launch_project(nullptr, nullptr, v.pairs, v.vdim, v.pf, nullptr, rotMat, nR, nR,
+                                c->px.iCol, c->px.iRow, K, P, Kp, nullptr, nullptr, nullptr,
+                                c->d_flag, splitP, s));
+        k_abs2_from<<<nR, 256, 0, s>>>(P, splitP, K, Kp, abs2, Kq);
+        TG3_LAUNCH_CHECK("projection norms");
+    }
+    TG3_CUDA(launch_translate(trans, nT, c->px.idim, c->px.iCol, c->px.iRow, K, bank, K, s));
+    for (int l0 = 0; l0 < nImg; l0 += IB) {
+        const int n = std::min(IB, nImg - l0);
+        const float2* dd = reinterpret_cast<const float2*>(dat) + (size_t)l0 * K;
+        const float* cc = ctf + (size_t)l0 * K;
+        const float* ss = sigRcp + (size_t)l0 * K;
+        const long long splitA = split ? (long long)n * nT * Kp : 0;
+        {
+            StageTimer tm(c, TG3_STAGE_SHIFT);
+            TG3_CUDA(launch_shift_bank(dd, cc, ss, nullptr, bank, n, nT, 1, nullptr, nullptr, K, A,
+                                       Kp, splitA, s));
+            TG3_CUDA(launch_x0(dd, ss, n, K, x0 + l0, s));
+            k_sc2_rows<<<dim3((Kq + 255) / 256, n), 256, 0, s>>>(ss, cc, K, sc2, Kq);
+            TG3_LAUNCH_CHECK("norm operand");
+        }
+        {
+            StageTimer tm(c, TG3_STAGE_CROSS);
+            // per-(rotation, image) norm, then the cross term
+            TG3_CUDA(launch_gemm_nt_fp32(abs2, 0, Kq, sc2, 0, Kq, nR, n, Kq, 1, nrmG, 0, n, nullptr,
+                                         0, 1.0f, s));
+            // the cross term is written image-major: D[l][r][t]
+            const int cols = n * nT;
+            if (split) {
+                const int Nt = std::min(256, (cols + 15) / 16 * 16);
+                const int items = (cols + Nt - 1) / Nt;
+                TG3_CUDA(launch_gemm_bf16x3(P, nR, A, (long long)cols, nR, Nt, Kp, items, 0, Nt,
+                                            cols, D, 0, nT, nullptr, 0, -2.0f, c->d_flag, s, nT,
+                                            (long long)nR * nT));
+            } else {
+                TG3_CUDA(launch_gemm_nt_fp32(P, 0, Kp, A, 0, Kp, nR, cols, Kp, 1, D, 0, nT, nullptr,
+                                             0, -2.0f, s, nT, (long long)nR * nT));
+            }
+        }
+        {
+            StageTimer tm(c, TG3_STAGE_WEIGHTS);
+            TG3_CUDA(launch_weights(D, (long long)nR * nT, nT, nR, nT, 1, n, nrmG, n, x0 + l0, pR, 0, pT, 0,
+                                    nullptr, wC + l0, wR + (size_t)l0 * nR, wT + (size_t)l0 * nT,
+                                    baseL + l0, dvp ? dvp + (size_t)l0 * nR * nT : nullptr, s));
         }
     }
     return TG3_OK;

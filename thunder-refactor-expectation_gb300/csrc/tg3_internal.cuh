@@ -151,16 +151,19 @@ cudaError_t launch_shift_bank(const float2* dat, const float* ctf,
                               long long splitLo, cudaStream_t st);
 cudaError_t launch_x0(const float2* dat, const float* sigRcp, int nP, int K,
                       double* x0, cudaStream_t st);
-// C[b][i][j] = alpha * sum_k A[b][i][k] B[b][j][k] + nrm[b][i]   (FP32)
+// C[b][i][j] = alpha * sum_k A[b][i][k] B[b][j][k] + nrm[b][i]   (FP32).
+// cGroup > 0: column j is written to group j / cGroup (cGroupStride
+// elements apart) at column j % cGroup.
 cudaError_t launch_gemm_nt_fp32(const float* A, long long sA, int lda,
                                 const float* B, long long sB, int ldb,
                                 int M, int N, int Kd, int batch, float* C,
                                 long long sC, int ldc, const float* nrm,
-                                long long sN, float alpha, cudaStream_t st);
-// nrmG (optional) adds a per-(rotation, group) term nrmG[r G + g].
+                                long long sN, float alpha, cudaStream_t st,
+                                int cGroup = 0, long long cGroupStride = 0);
+// nrmG (optional) adds a per-(rotation, block) term nrmG[r nrmRS + blk].
 cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR,
                            int nT, int G, int nBlocks, const float* nrmG,
-                           const double* x0,
+                           int nrmRS, const double* x0,
                            const double* pwR, long long sR, const double* pwT,
                            long long sT, const double* pwC, double* wC,
                            double* wR, double* wT, double* base, float* dvp,
@@ -197,5 +200,12 @@ cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda,
                                   size_t scratchBytes, int* flag,
                                   cudaStream_t st);
 size_t bf16x3_scratch_bytes(int M, int N, int Kd, int batch);
+// General split-bf16 GEMM over `items` (see tg3_tc.cu): A/B point at hi
+// planes followed by lo planes of rowsA / rowsB rows of Kd bf16 elements.
+cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, long long rowsB,
+                               int M, int N, int Kd, int items, int aRowsPerItem,
+                               int bRowsPerItem, int nTotal, float* C, long long sC, int ldc,
+                               const float* nrm, long long sN, float alpha, int* flag,
+                               cudaStream_t st, int cGroup = 0, long long cGroupStride = 0);
 
 }  // namespace tg3

@@ -1,9 +1,9 @@
 // tg3_kernels.cu -- the plain (FP32) E-step and insertion kernels for sm_103a.
 //
 // Data layout in HBM (all particle-major):
-//   projection volume  : paired-corner float4 [vdim][vdim][nx], element x holds
-//                        (V[x], V[x+1]) so that each trilinear sample is four
-//                        16-byte loads instead of eight 8-byte ones;
+//   projection volume  : 32-byte corner blocks [vdim][vdim][nx] (see
+//                        k_volume_pairs), one 256-bit load per z slab of a
+//                        trilinear sample instead of eight 8-byte loads;
 //   projections P      : [row][Kp] floats, a complex row padded with zeros to
 //                        Kp floats (Kp a multiple of 64);
 //   shifted data A''   : [particle][translation][Kp] floats, the complex
@@ -40,6 +40,12 @@ __device__ __forceinline__ void store_pair(float* out, long long splitLo, size_t
     const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
     reinterpret_cast<__nv_bfloat162*>(hi + row * ldo)[p] = h;
     reinterpret_cast<__nv_bfloat162*>(hi + splitLo + row * ldo)[p] = l;
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 
 __device__ __forceinline__ double warp_sum_d(double v)
@@ -213,48 +219,74 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
     const float* sg = sigRcp ? sigRcp + (size_t)l * K : nullptr;
     const float* cf = ctf ? ctf + (size_t)l * K : nullptr;
     float acc = 0.f;
-    for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x) {
-        if (p >= K) {
-            store_pair(out, splitLo, row, ldo, p, 0.f, 0.f);
-            continue;
+    // Two pixels per thread per iteration: both pairs of 256-bit corner loads
+    // are issued before either sample is interpolated, so each thread keeps
+    // four loads in flight.  Pixels past K (the zero padding) read the first
+    // block harmlessly and store zeros.
+    const int nOut = ldo / 2;
+    for (int base = threadIdx.x; base < nOut; base += 2 * blockDim.x) {
+        int pp[2] = {base, base + (int)blockDim.x};
+        float fw[2][3];
+        bool cj[2], ok[2];
+        const float4* e[2][2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int p = pp[u];
+            ok[u] = p < K;
+            const int q = ok[u] ? p : 0;
+            const float a = (float)iCol[q] * fpf, b = (float)iRow[q] * fpf;
+            float x = m[0] * a + m[1] * b;
+            float y = m[3] * a + m[4] * b;
+            float z = m[6] * a + m[7] * b;
+            cj[u] = x < 0.f;
+            if (cj[u]) { x = -x; y = -y; z = -z; }
+            const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+            const int x0 = (int)xf, y0 = (int)yf, z0 = (int)zf;
+            fw[u][0] = x - xf;
+            fw[u][1] = y - yf;
+            fw[u][2] = z - zf;
+            // corner block at row y0 carries rows y0 and y0 + 1 (wrapped)
+            const int ys = y0 < 0 ? y0 + vdim : y0;
+            const int z1 = z0 + 1;
+            const int zs0 = z0 < 0 ? z0 + vdim : z0, zs1 = z1 < 0 ? z1 + vdim : z1;
+            e[u][0] = vol + 2 * (((size_t)zs0 * vdim + ys) * nx + x0);
+            e[u][1] = vol + 2 * (((size_t)zs1 * vdim + ys) * nx + x0);
         }
-        const float a = (float)iCol[p] * fpf, b = (float)iRow[p] * fpf;
-        float x = m[0] * a + m[1] * b;
-        float y = m[3] * a + m[4] * b;
-        float z = m[6] * a + m[7] * b;
-        const bool conj = x < 0.f;
-        if (conj) { x = -x; y = -y; z = -z; }
-        const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
-        const int x0 = (int)xf, y0 = (int)yf, z0 = (int)zf;
-        const float fx = x - xf, fy = y - yf, fz = z - zf;
-        const float wx[2] = {1.f - fx, fx}, wy[2] = {1.f - fy, fy}, wz[2] = {1.f - fz, fz};
-        // corner block at row y0 carries rows y0 and y0 + 1 (wrapped)
-        const int ys = y0 < 0 ? y0 + vdim : y0;
-        const int zs[2] = {z0 < 0 ? z0 + vdim : z0, z0 + 1 < 0 ? z0 + 1 + vdim : z0 + 1};
-        float4 c[4];
+        float4 c[2][4];
 #pragma unroll
-        for (int k = 0; k < 2; k++) {
-            // one 256-bit read-only load of the 32-byte corner block
-            const float4* e = vol + 2 * (((size_t)zs[k] * vdim + ys) * nx + x0);
-            asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                : "=f"(c[2 * k].x), "=f"(c[2 * k].y), "=f"(c[2 * k].z), "=f"(c[2 * k].w),
-                  "=f"(c[2 * k + 1].x), "=f"(c[2 * k + 1].y), "=f"(c[2 * k + 1].z),
-                  "=f"(c[2 * k + 1].w)
-                : "l"(e));
-        }
-        float re = 0.f, im = 0.f;
+        for (int u = 0; u < 2; u++)
 #pragma unroll
-        for (int k = 0; k < 2; k++)
+            for (int k = 0; k < 2; k++)
+                // one 256-bit read-only load of the 32-byte corner block
+                asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                    : "=f"(c[u][2 * k].x), "=f"(c[u][2 * k].y), "=f"(c[u][2 * k].z),
+                      "=f"(c[u][2 * k].w), "=f"(c[u][2 * k + 1].x), "=f"(c[u][2 * k + 1].y),
+                      "=f"(c[u][2 * k + 1].z), "=f"(c[u][2 * k + 1].w)
+                    : "l"(e[u][k]));
 #pragma unroll
-            for (int j = 0; j < 2; j++) {
-                const float4 v = c[2 * k + j];
-                const float w0 = wx[0] * wy[j] * wz[k], w1 = wx[1] * wy[j] * wz[k];
-                re += v.x * w0 + v.z * w1;
-                im += v.y * w0 + v.w * w1;
+        for (int u = 0; u < 2; u++) {
+            const int p = pp[u];
+            if (p >= nOut) continue;
+            if (!ok[u]) {
+                store_pair(out, splitLo, row, ldo, p, 0.f, 0.f);
+                continue;
             }
-        if (conj) im = -im;
-        store_pair(out, splitLo, row, ldo, p, re, im);
-        if (nrm) acc += sg[p] * cf[p] * cf[p] * (re * re + im * im);
+            const float fx = fw[u][0], fy = fw[u][1], fz = fw[u][2];
+            const float wx[2] = {1.f - fx, fx}, wy[2] = {1.f - fy, fy}, wz[2] = {1.f - fz, fz};
+            float re = 0.f, im = 0.f;
+#pragma unroll
+            for (int k = 0; k < 2; k++)
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    const float4 v = c[u][2 * k + j];
+                    const float w0 = wx[0] * wy[j] * wz[k], w1 = wx[1] * wy[j] * wz[k];
+                    re += v.x * w0 + v.z * w1;
+                    im += v.y * w0 + v.w * w1;
+                }
+            if (cj[u]) im = -im;
+            store_pair(out, splitLo, row, ldo, p, re, im);
+            if (nrm) acc += sg[p] * cf[p] * cf[p] * (re * re + im * im);
+        }
     }
     if (nrm) {
         double s = block_sum_d((double)acc, red);
@@ -324,7 +356,8 @@ __global__ void __launch_bounds__(256, 1)
 k_gemm_nt_fp32(const float* __restrict__ A, long long sA, int lda,
                const float* __restrict__ B, long long sB, int ldb,
                int M, int N, int Kd, float* __restrict__ C, long long sC, int ldc,
-               const float* __restrict__ nrm, long long sN, float alpha)
+               const float* __restrict__ nrm, long long sN, float alpha, int cGroup,
+               long long cGroupStride)
 {
     __shared__ __align__(16) float As[2][GB_K][GB_M + GB_PAD];
     __shared__ __align__(16) float Bs[2][GB_K][GB_N + GB_PAD];
@@ -401,7 +434,14 @@ k_gemm_nt_fp32(const float* __restrict__ A, long long sA, int lda,
 #pragma unroll
         for (int j = 0; j < 8; j++) {
             const int gj = j0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
-            if (gj < N) C[(size_t)gi * ldc + gj] = fmaf(alpha, acc[i][j], add);
+            if (gj < N) {
+                size_t off = (size_t)gi * ldc + gj;
+                if (cGroup > 0) {
+                    const int l = gj / cGroup;
+                    off = (size_t)l * cGroupStride + (size_t)gi * ldc + (gj - l * cGroup);
+                }
+                C[off] = fmaf(alpha, acc[i][j], add);
+            }
         }
     }
 }
@@ -413,16 +453,25 @@ k_gemm_nt_fp32(const float* __restrict__ A, long long sA, int lda,
 //   wC = sum s pwR[r] pwT[t]
 // (the running-baseline accumulation of Optimiser::updateSP,
 // src/Optimiser.cpp:1326-1347, evaluated in two passes).  D of block (b, g)
-// is D[b sD + r ldc + g nT + t].  One CTA of 256 threads per block; dynamic
-// shared memory holds 8 per-warp copies of wT (8 nT doubles).
-__global__ void __launch_bounds__(256)
+// is D[b sD + r ldc + g nT + t].  One CTA of 512 threads per block; a warp
+// takes whole rotation rows (lanes over translations, coalesced), sums wR[r]
+// with shuffles, and keeps its share of wT in registers (TS slots of 32
+// translations; TS == 0: shared-memory atomics for long rows).  FP32
+// accumulation, as in the reference GPU path; totals are combined in FP64.
+constexpr int WEIGHTS_THREADS = 512;
+
+template <int TS>
+__global__ void __launch_bounds__(WEIGHTS_THREADS)
 k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, int G,
-          const float* __restrict__ nrmG, const double* __restrict__ x0, const double* __restrict__ pwR, long long sR,
+          const float* __restrict__ nrmG, int nrmRS, const double* __restrict__ x0,
+          const double* __restrict__ pwR, long long sR,
           const double* __restrict__ pwT, long long sT, const double* __restrict__ pwC,
           double* __restrict__ wC, double* __restrict__ wR, double* __restrict__ wT,
           double* __restrict__ base, float* __restrict__ dvp)
 {
-    extern __shared__ double wTw[];      // [8][nT]
+    extern __shared__ float wsm[];
+    float* wTs = wsm;                // [nT]
+    float* pTs = wTs + nT;           // [nT]
     __shared__ float redf[32];
     __shared__ double red[32];
     const int blk = blockIdx.x;
@@ -432,11 +481,31 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
     const double* pt = pwT + blk * sT;
     const double pc = pwC ? pwC[blk] : 1.0;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    // pass 1: maximum
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
+        wTs[t] = 0.f;
+        pTs[t] = (float)pt[t];
+    }
+    // pass 1: maximum (four rows per warp in flight)
     float mx = -CUDART_INF_F;
-    for (int r = wid; r < nR; r += nw) {
-        const float ad = nrmG ? nrmG[(size_t)r * G + g] : 0.f;
-        for (int t = lane; t < nT; t += 32) mx = fmaxf(mx, Db[(size_t)r * ldc + t] + ad);
+    for (int r0 = wid; r0 < nR; r0 += 4 * nw) {
+        float v[4][TS > 0 ? TS : 1];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int r = r0 + q * nw;
+            const float ad = (r < nR && nrmG) ? nrmG[(size_t)r * nrmRS + blk] : 0.f;
+            const float* row = Db + (size_t)(r < nR ? r : 0) * ldc;
+#pragma unroll
+            for (int j = 0; j < (TS > 0 ? TS : 1); j++) {
+                const int t = lane + 32 * j;
+                v[q][j] = (r < nR && t < nT && TS > 0) ? row[t] + ad : -CUDART_INF_F;
+            }
+            if (TS == 0 && r < nR)
+                for (int t = lane; t < nT; t += 32) mx = fmaxf(mx, row[t] + ad);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int j = 0; j < (TS > 0 ? TS : 1); j++) mx = fmaxf(mx, v[q][j]);
     }
     mx = warp_max(mx);
     if (lane == 0) redf[wid] = mx;
@@ -448,33 +517,75 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
     }
     __syncthreads();
     const float M = redf[0];
-    for (int i = threadIdx.x; i < nw * nT; i += blockDim.x) wTw[i] = 0.0;
-    __syncthreads();
     const double x0b = x0 ? x0[blk] : 0.0;
     // pass 2: marginals
-    double cacc = 0.0;
-    for (int r = wid; r < nR; r += nw) {
-        const double prr = pr[r];
-        const float ad = nrmG ? nrmG[(size_t)r * G + g] : 0.f;
-        double racc = 0.0;
-        for (int t = lane; t < nT; t += 32) {
-            const float d = Db[(size_t)r * ldc + t] + ad;
-            const double s = (double)__expf(d - M);
-            racc += s * pt[t];
-            wTw[wid * nT + t] += s * prr;
-            cacc += s * (prr * pt[t]);
-            if (dvp) dvp[((size_t)blk * nR + r) * nT + t] = (float)(x0b + (double)d);
+    float tacc[TS > 0 ? TS : 1], ptv[TS > 0 ? TS : 1];
+#pragma unroll
+    for (int j = 0; j < (TS > 0 ? TS : 1); j++) {
+        tacc[j] = 0.f;
+        const int t = lane + 32 * j;
+        ptv[j] = (TS > 0 && t < nT) ? pTs[t] : 0.f;
+    }
+    float cacc = 0.f;
+    // two rows per warp in flight: both rows' loads precede their arithmetic
+    for (int r0 = wid; r0 < nR; r0 += 2 * nw) {
+        float dv[2][TS > 0 ? TS : 1], prr[2], ad[2];
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const int r = r0 + q * nw;
+            const bool rok = r < nR;
+            prr[q] = rok ? (float)pr[r] : 0.f;
+            ad[q] = (rok && nrmG) ? nrmG[(size_t)r * nrmRS + blk] : 0.f;
+            const float* row = Db + (size_t)(rok ? r : 0) * ldc;
+#pragma unroll
+            for (int j = 0; j < (TS > 0 ? TS : 1); j++) {
+                const int t = lane + 32 * j;
+                dv[q][j] = (TS > 0 && rok && t < nT) ? row[t] : 0.f;
+            }
         }
-        racc = warp_sum_d(racc);
-        if (lane == 0) wR[(size_t)blk * nR + r] = racc * pc;
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const int r = r0 + q * nw;
+            if (r >= nR) break;
+            const float* row = Db + (size_t)r * ldc;
+            float racc = 0.f;
+            if (TS > 0) {
+#pragma unroll
+                for (int j = 0; j < (TS > 0 ? TS : 1); j++) {
+                    const int t = lane + 32 * j;
+                    if (t < nT) {
+                        const float d = dv[q][j] + ad[q];
+                        const float sv = __expf(d - M);
+                        racc = fmaf(sv, ptv[j], racc);
+                        tacc[j] = fmaf(sv, prr[q], tacc[j]);
+                        if (dvp) dvp[((size_t)blk * nR + r) * nT + t] = (float)(x0b + (double)d);
+                    }
+                }
+            } else {
+                for (int t = lane; t < nT; t += 32) {
+                    const float d = row[t] + ad[q];
+                    const float sv = __expf(d - M);
+                    racc = fmaf(sv, pTs[t], racc);
+                    atomicAdd(wTs + t, sv * prr[q]);
+                    if (dvp) dvp[((size_t)blk * nR + r) * nT + t] = (float)(x0b + (double)d);
+                }
+            }
+            racc = warp_sum(racc);
+            cacc = fmaf(racc, prr[q], cacc);   // sum_t s pT[t] pR[r], once per row
+            if (lane == 0) wR[(size_t)blk * nR + r] = (double)racc * pc;
+        }
+    }
+    if (TS > 0) {
+#pragma unroll
+        for (int j = 0; j < (TS > 0 ? TS : 1); j++) {
+            const int t = lane + 32 * j;
+            if (t < nT) atomicAdd(wTs + t, tacc[j]);
+        }
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
-        double s = 0.0;
-        for (int w = 0; w < nw; w++) s += wTw[w * nT + t];
-        wT[(size_t)blk * nT + t] = s * pc;
-    }
-    double c = block_sum_d(cacc, red);
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) wT[(size_t)blk * nT + t] = (double)wTs[t] * pc;
+    // every lane holds the same cacc per warp: count lane 0's only
+    const double c = block_sum_d(lane == 0 ? (double)cacc : 0.0, red);
     if (threadIdx.x == 0) {
         wC[blk] = c;
         base[blk] = x0b + (double)M;
@@ -574,17 +685,26 @@ k_resample(int n, const double* __restrict__ uIn, const double* __restrict__ wIn
     double pf = peaks ? peaks[b] : 0.0;
     if (isnan(pf)) {
         // value of rank n/8 in descending order (Particle::setPeakFactor)
+        // The rank count compares monotone integer keys of the doubles (the
+        // IEEE bit pattern, negatives reflected): exact, and integer compares
+        // run at full rate where FP64 compares would not.
         const int k = n / 8;
+        long long* key = reinterpret_cast<long long*>(cdf);   // cdf is unused yet
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double x = ub[i];
+            const long long bits = __double_as_longlong(x == 0.0 ? 0.0 : x);
+            key[i] = bits ^ ((bits >> 63) & 0x7fffffffffffffffLL);
+        }
         __syncthreads();
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const double v = ub[i];
+            const long long v = key[i];
             int gt = 0, ge = 0;
             for (int j = 0; j < n; j++) {
-                const double x = ub[j];
+                const long long x = key[j];
                 gt += x > v;
                 ge += x >= v;
             }
-            if (gt <= k && k < ge) sh = v;   // all writers store the same value
+            if (gt <= k && k < ge) sh = ub[i];   // all writers store the same value
         }
         __syncthreads();
         const double r = __ddiv_rn(sh, umax);
@@ -884,28 +1004,33 @@ cudaError_t launch_x0(const float2* dat, const float* sigRcp, int nP, int K, dou
 cudaError_t launch_gemm_nt_fp32(const float* A, long long sA, int lda, const float* B,
                                 long long sB, int ldb, int M, int N, int Kd, int batch,
                                 float* C, long long sC, int ldc, const float* nrm,
-                                long long sN, float alpha, cudaStream_t st)
+                                long long sN, float alpha, cudaStream_t st, int cGroup,
+                                long long cGroupStride)
 {
     dim3 grid((N + GB_N - 1) / GB_N, (M + GB_M - 1) / GB_M, batch);
     k_gemm_nt_fp32<<<grid, 256, 0, st>>>(A, sA, lda, B, sB, ldb, M, N, Kd, C, sC, ldc,
-                                          nrm, sN, alpha);
+                                          nrm, sN, alpha, cGroup, cGroupStride);
     return cudaGetLastError();
 }
 
 cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR, int nT, int G,
-                           int nBlocks, const float* nrmG, const double* x0, const double* pwR, long long sR,
-                           const double* pwT, long long sT, const double* pwC, double* wC,
-                           double* wR, double* wT, double* base, float* dvp,
+                           int nBlocks, const float* nrmG, int nrmRS, const double* x0,
+                           const double* pwR,
+                           long long sR, const double* pwT, long long sT, const double* pwC,
+                           double* wC, double* wR, double* wT, double* base, float* dvp,
                            cudaStream_t st)
 {
-    size_t smem = sizeof(double) * 8 * (size_t)nT;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_weights, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-    }
-    k_weights<<<nBlocks, 256, smem, st>>>(D, sD, ldc, nR, nT, G, nrmG, x0, pwR, sR, pwT, sT, pwC,
-                                           wC, wR, wT, base, dvp);
+    const size_t smem = sizeof(float) * 2 * (size_t)nT;
+    if (smem > 48 * 1024) return cudaErrorInvalidValue;
+#define TG3_WEIGHTS(TS)                                                                        \
+    k_weights<TS><<<nBlocks, WEIGHTS_THREADS, smem, st>>>(D, sD, ldc, nR, nT, G, nrmG, nrmRS, x0, pwR, \
+                                                          sR, pwT, sT, pwC, wC, wR, wT, base, dvp)
+    if (nT <= 32) TG3_WEIGHTS(1);
+    else if (nT <= 64) TG3_WEIGHTS(2);
+    else if (nT <= 128) TG3_WEIGHTS(4);
+    else if (nT <= 256) TG3_WEIGHTS(8);
+    else TG3_WEIGHTS(0);
+#undef TG3_WEIGHTS
     return cudaGetLastError();
 }
 

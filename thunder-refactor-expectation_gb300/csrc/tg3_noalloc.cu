@@ -187,7 +187,7 @@ extern "C" int tg3_local_phase_noalloc(const float* volume, int vdim, int pf, co
     TG3_CUDA(launch_x0(reinterpret_cast<const float2*>(dat), sigRcp, 1, K, x0, cs));
     TG3_CUDA(launch_gemm_nt_fp32(P, 0, (int)Kp, A, 0, (int)Kp, nR, nT, (int)Kp, 1, D, 0, nT, nrm, 0,
                                  -2.0f, cs));
-    TG3_CUDA(launch_weights(D, 0, nT, nR, nT, 1, 1, nullptr, x0, pwR, 0, pwT, 0, pwC, wC, wR, wT,
+    TG3_CUDA(launch_weights(D, 0, nT, nR, nT, 1, 1, nullptr, 0, x0, pwR, 0, pwT, 0, pwC, wC, wR, wT,
                             baseL, dvp, cs));
     TG3_CUDA(cudaStreamSynchronize(cs));
     int h = 0;

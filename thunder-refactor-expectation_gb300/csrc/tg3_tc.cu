@@ -141,6 +141,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
 
 struct TcParams {
     int M, N, Kd;            // rows of A per item, columns (rows of B) per item, K
+    int aRowsPerItem;        // A row offset between items (0: A shared by all items)
+    int bRowsPerItem;        // B row offset between items
+    int nTotal;              // > 0: columns of the whole problem (the last item is partial)
+    int colPerItem;          // column offset between items (column-group remap)
+    int cGroup;              // > 0: column j goes to group j / cGroup, position j % cGroup
+    long long cGroupStride;  // element stride between column groups
     int ntile;               // N rounded up to 16 (the UMMA N)
     int tmemCols;            // power of two >= ntile
     int stages;
@@ -173,8 +179,9 @@ k_gemm_bf16x3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ 
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int mtile = blockIdx.x, item = blockIdx.y;
-    const int aRow0 = item * p.M + mtile * TC_M;
-    const int bRow0 = item * p.N;
+    const int aRow0 = item * p.aRowsPerItem + mtile * TC_M;
+    const int bRow0 = item * p.bRowsPerItem;
+    const int nValid = p.nTotal > 0 ? min(p.N, p.nTotal - item * p.N) : p.N;
     const int nkb = p.Kd / TC_BK;
 
     if (threadIdx.x == 0) {
@@ -259,19 +266,37 @@ k_gemm_bf16x3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ 
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const bool aborted = !ok;
-    const int rowInTile = warp * 32 + lane;
-    const int row = mtile * TC_M + rowInTile;            // row within the item
     if (!aborted) {
-        const bool rowOk = row < p.M;
-        const float add = (rowOk && p.nrm) ? p.nrm[item * p.sN + row] : 0.f;
-        float* crow = p.C + item * p.sC + (size_t)(rowOk ? row : 0) * p.ldc;
+        // The pipeline stages are free once the accumulator is complete: stage
+        // the warp's 32 rows there, then write every row with lanes over
+        // columns (coalesced).  Rows are padded by one float so both the
+        // column-wise fill and the row-wise drain are free of bank conflicts.
+        const int pitch = p.ntile + 1;
+        float* stage = reinterpret_cast<float*>(smem) + (size_t)warp * 32 * pitch;
+        const int rowBase = mtile * TC_M + warp * 32;
+        const bool rowOk = rowBase + lane < p.M;
+        const float add = (rowOk && p.nrm) ? p.nrm[item * p.sN + rowBase + lane] : 0.f;
         for (int c0 = 0; c0 < p.ntile; c0 += 16) {
             float v[16];
             tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            if (rowOk) {
 #pragma unroll
-                for (int i = 0; i < 16; i++)
-                    if (c0 + i < p.N) crow[c0 + i] = fmaf(p.alpha, v[i], add);
+            for (int i = 0; i < 16; i++) stage[lane * pitch + c0 + i] = fmaf(p.alpha, v[i], add);
+        }
+        __syncwarp();
+        float* cbase = p.C + item * p.sC;
+        for (int rr = 0; rr < 32; rr++) {
+            const int r = rowBase + rr;
+            if (r >= p.M) break;
+            for (int j = lane; j < nValid; j += 32) {
+                size_t off;
+                if (p.cGroup > 0) {
+                    const int jj = item * p.colPerItem + j;
+                    const int l = jj / p.cGroup;
+                    off = (size_t)l * p.cGroupStride + (size_t)r * p.ldc + (jj - l * p.cGroup);
+                } else {
+                    off = (size_t)r * p.ldc + j;
+                }
+                cbase[off] = stage[rr * pitch + j];
             }
         }
     }
@@ -340,16 +365,18 @@ size_t bf16x3_scratch_bytes(int, int, int, int) { return 256; }
 
 // A and B point at the hi planes; the lo plane of each follows its hi plane
 // (rows * Kd bf16 elements later).  lda / ldb must equal Kd.
-cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda, const float* B,
-                                  long long sB, int ldb, int M, int N, int Kd, int batch,
-                                  float* C, long long sC, int ldc, const float* nrm,
-                                  long long sN, float alpha, void*, size_t, int* flag,
-                                  cudaStream_t st)
+// General form.  A: hi plane at A, lo plane rowsA x Kd elements later; B the
+// same with rowsB.  Item i uses A rows i * aRowsPerItem + (0 .. M) and B rows
+// i * bRowsPerItem + (0 .. N); it writes C + i * sC (+ row * ldc + col) for
+// row < M and col < N (col < nTotal - i * N when nTotal > 0).
+cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, long long rowsB,
+                               int M, int N, int Kd, int items, int aRowsPerItem,
+                               int bRowsPerItem, int nTotal, float* C, long long sC, int ldc,
+                               const float* nrm, long long sN, float alpha, int* flag,
+                               cudaStream_t st, int cGroup, long long cGroupStride)
 {
-    if (N <= 0 || N > 256 || M <= 0 || Kd % TC_BK || lda != Kd || ldb != Kd ||
-        sA != (long long)M * Kd || sB != (long long)N * Kd)
+    if (N <= 0 || N > 256 || M <= 0 || items <= 0 || Kd <= 0 || Kd % TC_BK)
         return cudaErrorInvalidValue;
-    const long long rowsA = (long long)batch * M, rowsB = (long long)batch * N;
     const __nv_bfloat16* Ah = reinterpret_cast<const __nv_bfloat16*>(A);
     const __nv_bfloat16* Al = Ah + rowsA * Kd;
     const __nv_bfloat16* Bh = reinterpret_cast<const __nv_bfloat16*>(B);
@@ -358,6 +385,12 @@ cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda, const f
     p.M = M;
     p.N = N;
     p.Kd = Kd;
+    p.aRowsPerItem = aRowsPerItem;
+    p.bRowsPerItem = bRowsPerItem;
+    p.nTotal = nTotal;
+    p.colPerItem = N;
+    p.cGroup = cGroup;
+    p.cGroupStride = cGroupStride;
     p.ntile = (N + 15) / 16 * 16;
     p.tmemCols = 32;
     while (p.tmemCols < p.ntile) p.tmemCols <<= 1;
@@ -365,6 +398,8 @@ cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda, const f
     p.stages = (200 * 1024) / stageBytes;
     if (p.stages > 4) p.stages = 4;
     if (p.stages < 2) return cudaErrorInvalidValue;
+    // the epilogue stages 128 rows of ntile + 1 floats in the pipeline buffers
+    if ((size_t)TC_M * (p.ntile + 1) * 4 > (size_t)p.stages * stageBytes) return cudaErrorInvalidValue;
     p.C = C;
     p.sC = sC;
     p.ldc = ldc;
@@ -380,37 +415,23 @@ cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda, const f
     cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    dim3 grid((M + TC_M - 1) / TC_M, batch);
+    dim3 grid((M + TC_M - 1) / TC_M, items);
     k_gemm_bf16x3<<<grid, TC_THREADS, smem, st>>>(mAh, mAl, mBh, mBl, p);
     return cudaGetLastError();
 }
 
-// ------------------------------------------------------------------------
-// Split planes: hi = bf16(x), lo = bf16(x - hi) of an FP32 array of `rows`
-// rows of Kd floats (zero-padded), written as two [rows][Kd] bf16 planes.
-namespace {
-__global__ void k_split_planes(const float* __restrict__ in, long long n, __nv_bfloat16* __restrict__ hi,
-                               __nv_bfloat16* __restrict__ lo)
+// Batched form: item b multiplies A rows [b M, (b + 1) M) with B rows
+// [b N, (b + 1) N).  lda / ldb must equal Kd and the batch strides M Kd / N Kd.
+cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda, const float* B,
+                                  long long sB, int ldb, int M, int N, int Kd, int batch,
+                                  float* C, long long sC, int ldc, const float* nrm,
+                                  long long sN, float alpha, void*, size_t, int* flag,
+                                  cudaStream_t st)
 {
-    for (long long i = (blockIdx.x * (long long)blockDim.x + threadIdx.x) * 2; i < n;
-         i += (long long)gridDim.x * blockDim.x * 2) {
-        const float2 v = *reinterpret_cast<const float2*>(in + i);
-        const __nv_bfloat162 h = __floats2bfloat162_rn(v.x, v.y);
-        const float2 hf = __bfloat1622float2(h);
-        const __nv_bfloat162 l = __floats2bfloat162_rn(v.x - hf.x, v.y - hf.y);
-        *reinterpret_cast<__nv_bfloat162*>(hi + i) = h;
-        *reinterpret_cast<__nv_bfloat162*>(lo + i) = l;
-    }
-}
-}  // namespace
-
-cudaError_t launch_split_planes(const float* in, long long n, void* hi, void* lo, cudaStream_t st)
-{
-    long long g = (n / 2 + 255) / 256;
-    if (g > 152 * 32) g = 152 * 32;
-    k_split_planes<<<(int)g, 256, 0, st>>>(in, n, reinterpret_cast<__nv_bfloat16*>(hi),
-                                            reinterpret_cast<__nv_bfloat16*>(lo));
-    return cudaGetLastError();
+    if (lda != Kd || ldb != Kd || sA != (long long)M * Kd || sB != (long long)N * Kd)
+        return cudaErrorInvalidValue;
+    return launch_gemm_bf16x3(A, (long long)batch * M, B, (long long)batch * N, M, N, Kd, batch, M,
+                              N, 0, C, sC, ldc, nrm, sN, alpha, flag, st, 0, 0);
 }
 
 }  // namespace tg3

@@ -29,7 +29,7 @@ EXPORTS = [
     "tg3_local_phase_d", "tg3_resample_d", "tg3_ctx_insert_begin", "tg3_insert_d",
     "tg3_ctx_insert_read_d", "tg3_rotmat_d", "tg3_translate_d", "tg3_ctf_d",
     "tg3_project_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
-    "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc",
+    "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert")
 
@@ -89,6 +89,7 @@ def lib():
             "tg3_ctx_set_timing": ([_P, _I], _I),
             "tg3_ctx_stage_times": ([_P, _P, _P, _I], _I),
             "tg3_noalloc_scratch_bytes": ([], ctypes.c_size_t),
+            "tg3_global_scan_d": ([_P, _I, _I, _I, _I] + [_P] * 12 + [_I], _I),
             "tg3_local_phase_noalloc": ([_P, _I, _I, _P, _P, _I, _I, _P, _P, _P, _P, _I, _P, _I,
                                          _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
         }
@@ -195,6 +196,13 @@ class Context:
         n = np.zeros(len(STAGES), np.int32)
         check(lib().tg3_ctx_stage_times(self.h, ptr(ms), ptr(n), int(reset)))
         return {s: (float(ms[i]), int(n[i])) for i, s in enumerate(STAGES)}
+
+    def global_scan(self, cls, nImg, nR, nT, dat, ctf, sig, rotmat, trans, pR, pT,
+                    wC, wR, wT, base, dvp=None, precision=SCORE_FP32):
+        self._hold(dat, ctf, sig, rotmat, trans, pR, pT, wC, wR, wT, base, dvp)
+        check(lib().tg3_global_scan_d(self.h, cls, nImg, nR, nT, ptr(dat), ptr(ctf), ptr(sig),
+                                      ptr(rotmat), ptr(trans), ptr(pR), ptr(pT), ptr(wC),
+                                      ptr(wR), ptr(wT), ptr(base), ptr(dvp), precision))
 
     def resample(self, nP, n, u, w, perm, u0, peak, nOut, src, wOut, top):
         self._hold(u, w, perm, u0, peak, src, wOut, top)
