@@ -303,7 +303,7 @@ extern "C" int tg3_ctx_destroy(tg3_ctx* c)
     if (!c) return TG3_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    for (auto& v : c->vol) cudaFree(v.pairs);
+    for (auto& v : c->vol) cudaFree(v.blocks);
     for (auto& b : c->ws) cudaFree(b.ptr);
     cudaFree(c->px.iCol);
     cudaFree(c->px.iRow);
@@ -348,13 +348,13 @@ extern "C" int tg3_ctx_set_volume(tg3_ctx* c, int cls, const float* volume, int 
     if (!volume || vdim < 4 || (vdim & 1) || pf < 1) return fail(TG3_ERR_ARG, "bad volume");
     Volume& v = c->vol[cls];
     const size_t nvox = (size_t)vdim * vdim * (vdim / 2 + 1);
-    const size_t bytes = nvox * 2 * sizeof(float4);   // 32-byte corner blocks
+    const size_t bytes = nvox * 4 * sizeof(float4);   // 64-byte corner blocks
     if (v.bytes != bytes) {
         TG3_CUDA(cudaStreamSynchronize(c->stream));
-        cudaFree(v.pairs);
-        v.pairs = nullptr;
+        cudaFree(v.blocks);
+        v.blocks = nullptr;
         v.bytes = 0;
-        TG3_CUDA(cudaMalloc(&v.pairs, bytes));
+        TG3_CUDA(cudaMalloc(&v.blocks, bytes));
         v.bytes = bytes;
     }
     v.vdim = vdim;
@@ -366,9 +366,9 @@ extern "C" int tg3_ctx_set_volume(tg3_ctx* c, int cls, const float* volume, int 
         if (st) return st;
         src = tmp;
     }
-    TG3_CUDA(launch_volume_pairs(src, vdim, v.pairs, c->stream));
+    TG3_CUDA(launch_volume_blocks(src, vdim, v.blocks, c->stream));
     float4* table[kMaxClasses];
-    for (int i = 0; i < kMaxClasses; i++) table[i] = c->vol[i].pairs;
+    for (int i = 0; i < kMaxClasses; i++) table[i] = c->vol[i].blocks;
     TG3_CUDA(cudaMemcpyAsync(c->d_volTable, table, sizeof(table), cudaMemcpyHostToDevice,
                              c->stream));
     TG3_CUDA(cudaStreamSynchronize(c->stream));
@@ -419,9 +419,9 @@ static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
     int st = TG3_OK;
     // volume of every class used must be set; check class 0 geometry
     const Volume& v0 = c->vol[0];
-    if (!v0.pairs) return fail(TG3_ERR_STATE, "volume of class 0 not set");
+    if (!v0.blocks) return fail(TG3_ERR_STATE, "volume of class 0 not set");
     for (int k = 1; k < kMaxClasses; k++)
-        if (c->vol[k].pairs && (c->vol[k].vdim != v0.vdim || c->vol[k].pf != v0.pf))
+        if (c->vol[k].blocks && (c->vol[k].vdim != v0.vdim || c->vol[k].pf != v0.pf))
             return fail(TG3_ERR_ARG, "all class volumes must share one edge and pf");
     if ((st = check_geometry(c, v0.vdim, v0.pf))) return st;
     if ((st = check_weights_shape(nR, nT))) return st;
@@ -648,11 +648,11 @@ extern "C" int tg3_project_d(tg3_ctx* c, int cls, const double* rotMat, int nR, 
 {
     int st = check_ctx(c);
     if (st) return st;
-    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].pairs) return fail(TG3_ERR_STATE, "volume not set");
+    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].blocks) return fail(TG3_ERR_STATE, "volume not set");
     if (!rotMat || !out || nR <= 0) return fail(TG3_ERR_ARG, "bad project args");
     const Volume& v = c->vol[cls];
     if ((st = check_geometry(c, v.vdim, v.pf))) return st;
-    TG3_CUDA(launch_project(nullptr, nullptr, v.pairs, v.vdim, v.pf, nullptr, rotMat, nR, nR,
+    TG3_CUDA(launch_project(nullptr, nullptr, v.blocks, v.vdim, v.pf, nullptr, rotMat, nR, nR,
                             c->px.iCol, c->px.iRow, c->px.K, out, 2 * c->px.K, nullptr, nullptr,
                             nullptr, c->d_flag, 0, c->stream));
     return TG3_OK;
@@ -1123,7 +1123,7 @@ extern "C" int tg3_global_scan_d(tg3_ctx* c, int cls, int nImg, int nR, int nT, 
 {
     int st = check_ctx(c);
     if (st) return st;
-    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].pairs)
+    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].blocks)
         return fail(TG3_ERR_STATE, "volume of the class not set");
     if (nImg <= 0 || nR <= 0 || nT <= 0 || nT > 2048) return fail(TG3_ERR_ARG, "bad scan shape");
     if (!dat || !ctf || !sigRcp || !rotMat || !trans || !pR || !pT || !wC || !wR || !wT || !baseL)
@@ -1162,7 +1162,7 @@ extern "C" int tg3_global_scan_d(tg3_ctx* c, int cls, int nImg, int nR, int nT, 
     const long long splitP = split ? (long long)nR * Kp : 0;
     {
         StageTimer tm(c, TG3_STAGE_PROJECT);
-        TG3_CUDA(launch_project(nullptr, nullptr, v.pairs, v.vdim, v.pf, nullptr, rotMat, nR, nR,
+        TG3_CUDA(launch_project(nullptr, nullptr, v.blocks, v.vdim, v.pf, nullptr, rotMat, nR, nR,
                                 c->px.iCol, c->px.iRow, K, P, Kp, nullptr, nullptr, nullptr,
                                 c->d_flag, splitP, s));
         k_abs2_from<<<nR, 256, 0, s>>>(P, splitP, K, Kp, abs2, Kq);

@@ -14,6 +14,8 @@
 namespace tg3 {
 
 constexpr int kMaxClasses = 16;
+// pixels a lane pair of the projection carries per iteration
+constexpr int kProjU = 4;
 constexpr int kMaxResampleN = 4096;   // particle-set size held in shared memory
 
 // ---------------------------------------------------------------- errors --
@@ -57,7 +59,7 @@ struct Buffer {
 };
 
 struct Volume {
-    float4* pairs = nullptr;   // [vdim][vdim][nx] corner blocks, 2 float4 each
+    float4* blocks = nullptr;   // [vdim][vdim][nx] corner blocks, 4 float4 each
     int vdim = 0;
     int pf = 0;
     size_t bytes = 0;
@@ -88,7 +90,7 @@ struct tg3_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     tg3::Volume vol[tg3::kMaxClasses];
-    float4** d_volTable = nullptr;   // device copy of the class -> pairs table
+    float4** d_volTable = nullptr;   // device copy of the class -> blocks table
     tg3::Pixels px;
     tg3::InsertAcc ins;
     tg3::Buffer ws[tg3::WS_COUNT];
@@ -129,7 +131,7 @@ cudaError_t launch_translate(const double* trans, int nT, int idim, const int* i
 cudaError_t launch_ctf(const float* attr, int nImg, float px, int idim,
                        const int* iCol, const int* iRow, int K, float* out,
                        cudaStream_t st);
-cudaError_t launch_volume_pairs(const float2* vol, int vdim, float4* pairs,
+cudaError_t launch_volume_blocks(const float2* vol, int vdim, float4* blocks,
                                 cudaStream_t st);
 // rows: projected rows; a row r belongs to particle r / rowsPerParticle.
 // Exactly one of quat [rows][4] / mat [rows][9] is non-null.

@@ -1,9 +1,10 @@
 // tg3_kernels.cu -- the plain (FP32) E-step and insertion kernels for sm_103a.
 //
 // Data layout in HBM (all particle-major):
-//   projection volume  : 32-byte corner blocks [vdim][vdim][nx] (see
-//                        k_volume_pairs), one 256-bit load per z slab of a
-//                        trilinear sample instead of eight 8-byte loads;
+//   projection volume  : 64-byte corner blocks [vdim][vdim][nx] (see
+//                        k_volume_blocks), all eight corners of a trilinear
+//                        sample in one half cache line, read by two lanes
+//                        with one 256-bit load each;
 //   projections P      : [row][Kp] floats, a complex row padded with zeros to
 //                        Kp floats (Kp a multiple of 64);
 //   shifted data A''   : [particle][translation][Kp] floats, the complex
@@ -40,6 +41,25 @@ __device__ __forceinline__ void store_pair(float* out, long long splitLo, size_t
     const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
     reinterpret_cast<__nv_bfloat162*>(hi + row * ldo)[p] = h;
     reinterpret_cast<__nv_bfloat162*>(hi + splitLo + row * ldo)[p] = l;
+}
+
+// Lane-pair form of store_pair: both lanes of a pair hold (a, b); lane half
+// h stores its share -- the real (h = 0) or imaginary (h = 1) float, or the
+// hi (h = 0) or lo (h = 1) bf16 pair -- so a warp's stores are contiguous.
+__device__ __forceinline__ void store_pair_half(float* out, long long splitLo, size_t row, int ldo,
+                                                int p, int h, float a, float b)
+{
+    if (splitLo == 0) {
+        out[row * ldo + 2 * (size_t)p + h] = h ? b : a;
+        return;
+    }
+    __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(out);
+    __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    if (h) {
+        const float2 hf = __bfloat1622float2(v);
+        v = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+    }
+    reinterpret_cast<__nv_bfloat162*>(hi + (h ? splitLo : 0) + row * ldo)[p] = v;
 }
 
 __device__ __forceinline__ float warp_sum(float v)
@@ -147,26 +167,33 @@ __global__ void k_ctf(const float* __restrict__ attr, int nImg, float px, int id
     }
 }
 
-// Corner-block layout of the projection volume: the 32-byte element of voxel
-// (z, y, x) holds V[z][y][x], V[z][y][x+1], V[z][y+1][x], V[z][y+1][x+1]
-// (row y+1 taken modulo vdim, the wrap of Volume::iFTHalf), so a trilinear
-// sample reads one aligned 32-byte sector in each of its two z slabs.
-__global__ void k_volume_pairs(const float2* __restrict__ vol, int vdim,
-                               float4* __restrict__ blocks)
+// Corner-block layout of the projection volume: the 64-byte element of voxel
+// (z, y, x) holds, for slab z then slab z + 1, V[.][y][x], V[.][y][x+1],
+// V[.][y+1][x], V[.][y+1][x+1] (rows and slabs taken modulo vdim, the wrap of
+// Volume::iFTHalf; x + 1 past the stored half reads zero).  A trilinear
+// sample then reads one aligned half cache line: one L1 wavefront per sample.
+__global__ void k_volume_blocks(const float2* __restrict__ vol, int vdim,
+                                float4* __restrict__ blocks)
 {
     const int nx = vdim / 2 + 1;
     const size_t n = (size_t)vdim * vdim * nx;
+    const float2 zero = make_float2(0.f, 0.f);
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(i % nx);
         const int y = (int)((i / nx) % vdim);
-        const size_t z = i / ((size_t)nx * vdim);
-        const size_t i1 = (z * vdim + (y + 1 == vdim ? 0 : y + 1)) * nx + x;
-        const float2 zero = make_float2(0.f, 0.f);
-        const float2 a = vol[i], b = (x + 1 < nx) ? vol[i + 1] : zero;
-        const float2 c = vol[i1], d = (x + 1 < nx) ? vol[i1 + 1] : zero;
-        blocks[2 * i] = make_float4(a.x, a.y, b.x, b.y);
-        blocks[2 * i + 1] = make_float4(c.x, c.y, d.x, d.y);
+        const int z = (int)(i / ((size_t)nx * vdim));
+        const int y1 = y + 1 == vdim ? 0 : y + 1;
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            const int zz = k == 0 ? z : (z + 1 == vdim ? 0 : z + 1);
+            const size_t i0 = ((size_t)zz * vdim + y) * nx + x;
+            const size_t i1 = ((size_t)zz * vdim + y1) * nx + x;
+            const float2 a = vol[i0], b = (x + 1 < nx) ? vol[i0 + 1] : zero;
+            const float2 c = vol[i1], d = (x + 1 < nx) ? vol[i1 + 1] : zero;
+            blocks[4 * i + 2 * k] = make_float4(a.x, a.y, b.x, b.y);
+            blocks[4 * i + 2 * k + 1] = make_float4(c.x, c.y, d.x, d.y);
+        }
     }
 }
 
@@ -219,22 +246,28 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
     const float* sg = sigRcp ? sigRcp + (size_t)l * K : nullptr;
     const float* cf = ctf ? ctf + (size_t)l * K : nullptr;
     float acc = 0.f;
-    // Two pixels per thread per iteration: both pairs of 256-bit corner loads
-    // are issued before either sample is interpolated, so each thread keeps
-    // four loads in flight.  Pixels past K (the zero padding) read the first
-    // block harmlessly and store zeros.
+    // A lane pair serves one pixel: lane half h reads slab z0 + h of the
+    // pixel's 64-byte corner block (one 256-bit load) and the two partial sums
+    // meet through one shuffle.  Each pair carries kProjU pixels per
+    // iteration, all loads issued before any interpolation.  The trip count is
+    // uniform across a warp (the shuffle needs every lane); pixels past K
+    // read pixel 0's block harmlessly and store zeros.
     const int nOut = ldo / 2;
-    for (int base = threadIdx.x; base < nOut; base += 2 * blockDim.x) {
-        int pp[2] = {base, base + (int)blockDim.x};
-        float fw[2][3];
-        bool cj[2], ok[2];
-        const float4* e[2][2];
+    const int h = threadIdx.x & 1;
+    const int npairs = blockDim.x >> 1;
+    const int warpBase = (threadIdx.x >> 5) * 16;
+    const int inWarp = (threadIdx.x & 31) >> 1;
+    for (int it = warpBase; it < nOut; it += kProjU * npairs) {
+        float fw[kProjU][3];
+        float w2[kProjU];   // sigRcp ctf^2 of the pixel, loaded with its indices
+        bool cj[kProjU];
+        const float4* e[kProjU];
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
-            const int p = pp[u];
-            ok[u] = p < K;
-            const int q = ok[u] ? p : 0;
+        for (int u = 0; u < kProjU; u++) {
+            const int p = it + inWarp + u * npairs;
+            const int q = p < K ? p : 0;
             const float a = (float)iCol[q] * fpf, b = (float)iRow[q] * fpf;
+            w2[u] = nrm ? sg[q] * cf[q] * cf[q] : 0.f;
             float x = m[0] * a + m[1] * b;
             float y = m[3] * a + m[4] * b;
             float z = m[6] * a + m[7] * b;
@@ -245,47 +278,39 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
             fw[u][0] = x - xf;
             fw[u][1] = y - yf;
             fw[u][2] = z - zf;
-            // corner block at row y0 carries rows y0 and y0 + 1 (wrapped)
             const int ys = y0 < 0 ? y0 + vdim : y0;
-            const int z1 = z0 + 1;
-            const int zs0 = z0 < 0 ? z0 + vdim : z0, zs1 = z1 < 0 ? z1 + vdim : z1;
-            e[u][0] = vol + 2 * (((size_t)zs0 * vdim + ys) * nx + x0);
-            e[u][1] = vol + 2 * (((size_t)zs1 * vdim + ys) * nx + x0);
+            const int zs = z0 < 0 ? z0 + vdim : z0;
+            e[u] = vol + 4 * (((size_t)zs * vdim + ys) * nx + x0) + 2 * h;
         }
-        float4 c[2][4];
+        float4 c[kProjU][2];
 #pragma unroll
-        for (int u = 0; u < 2; u++)
+        for (int u = 0; u < kProjU; u++)
+            asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                : "=f"(c[u][0].x), "=f"(c[u][0].y), "=f"(c[u][0].z), "=f"(c[u][0].w),
+                  "=f"(c[u][1].x), "=f"(c[u][1].y), "=f"(c[u][1].z), "=f"(c[u][1].w)
+                : "l"(e[u]));
 #pragma unroll
-            for (int k = 0; k < 2; k++)
-                // one 256-bit read-only load of the 32-byte corner block
-                asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                    : "=f"(c[u][2 * k].x), "=f"(c[u][2 * k].y), "=f"(c[u][2 * k].z),
-                      "=f"(c[u][2 * k].w), "=f"(c[u][2 * k + 1].x), "=f"(c[u][2 * k + 1].y),
-                      "=f"(c[u][2 * k + 1].z), "=f"(c[u][2 * k + 1].w)
-                    : "l"(e[u][k]));
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-            const int p = pp[u];
-            if (p >= nOut) continue;
-            if (!ok[u]) {
-                store_pair(out, splitLo, row, ldo, p, 0.f, 0.f);
-                continue;
-            }
+        for (int u = 0; u < kProjU; u++) {
             const float fx = fw[u][0], fy = fw[u][1], fz = fw[u][2];
-            const float wx[2] = {1.f - fx, fx}, wy[2] = {1.f - fy, fy}, wz[2] = {1.f - fz, fz};
-            float re = 0.f, im = 0.f;
-#pragma unroll
-            for (int k = 0; k < 2; k++)
-#pragma unroll
-                for (int j = 0; j < 2; j++) {
-                    const float4 v = c[u][2 * k + j];
-                    const float w0 = wx[0] * wy[j] * wz[k], w1 = wx[1] * wy[j] * wz[k];
-                    re += v.x * w0 + v.z * w1;
-                    im += v.y * w0 + v.w * w1;
+            const float wz = h ? fz : 1.f - fz;
+            const float wx0 = 1.f - fx, wx1 = fx;
+            const float wy0 = (1.f - fy) * wz, wy1 = fy * wz;
+            float re = c[u][0].x * (wx0 * wy0) + c[u][0].z * (wx1 * wy0);
+            float im = c[u][0].y * (wx0 * wy0) + c[u][0].w * (wx1 * wy0);
+            re += c[u][1].x * (wx0 * wy1) + c[u][1].z * (wx1 * wy1);
+            im += c[u][1].y * (wx0 * wy1) + c[u][1].w * (wx1 * wy1);
+            re += __shfl_xor_sync(0xffffffffu, re, 1);
+            im += __shfl_xor_sync(0xffffffffu, im, 1);
+            const int p = it + inWarp + u * npairs;
+            if (p < nOut) {
+                if (p < K) {
+                    if (cj[u]) im = -im;
+                    store_pair_half(out, splitLo, row, ldo, p, h, re, im);
+                    if (h == 0) acc = fmaf(w2[u], re * re + im * im, acc);
+                } else {
+                    store_pair_half(out, splitLo, row, ldo, p, h, 0.f, 0.f);
                 }
-            if (cj[u]) im = -im;
-            store_pair(out, splitLo, row, ldo, p, re, im);
-            if (nrm) acc += sg[p] * cf[p] * cf[p] * (re * re + im * im);
+            }
         }
     }
     if (nrm) {
@@ -962,10 +987,10 @@ cudaError_t launch_ctf(const float* attr, int nImg, float px, int idim, const in
     return cudaGetLastError();
 }
 
-cudaError_t launch_volume_pairs(const float2* vol, int vdim, float4* pairs, cudaStream_t st)
+cudaError_t launch_volume_blocks(const float2* vol, int vdim, float4* blocks, cudaStream_t st)
 {
     size_t n = (size_t)vdim * vdim * (vdim / 2 + 1);
-    k_volume_pairs<<<grid_for(n, 256), 256, 0, st>>>(vol, vdim, pairs);
+    k_volume_blocks<<<grid_for(n, 256), 256, 0, st>>>(vol, vdim, blocks);
     return cudaGetLastError();
 }
 
