@@ -14,8 +14,11 @@
 namespace tg3 {
 
 constexpr int kMaxClasses = 16;
-// pixels a lane pair of the projection carries per iteration
+// projection work unit: a lane pair carries kProjU pixels of a chunk of
+// kProjChunk (= 128 pairs x kProjU) pixels, for kProjG rotations per CTA
 constexpr int kProjU = 4;
+constexpr int kProjChunk = 128 * kProjU;
+constexpr int kProjG = 8;
 constexpr int kMaxResampleN = 4096;   // particle-set size held in shared memory
 
 // ---------------------------------------------------------------- errors --
@@ -44,6 +47,7 @@ enum WsSlot {
     WS_A,            // shifted, weighted data [nP][nT][Kp]
     WS_D,            // hypothesis-dependent log-likelihood part [nP][nR][nT]
     WS_NRM,          // sum sigRcp ctf^2 |P|^2 per projected row
+    WS_NRM_PART,     // its per-pixel-chunk shares [rows][project_chunks(ldo)]
     WS_X0,           // sum sigRcp |X|^2 per particle (double)
     WS_PAIRS_TMP,
     WS_H2D,          // staging of host inputs
@@ -133,15 +137,18 @@ cudaError_t launch_ctf(const float* attr, int nImg, float px, int idim,
                        cudaStream_t st);
 cudaError_t launch_volume_blocks(const float2* vol, int vdim, float4* blocks,
                                 cudaStream_t st);
-// rows: projected rows; a row r belongs to particle r / rowsPerParticle.
-// Exactly one of quat [rows][4] / mat [rows][9] is non-null.
+// rows: projected rows; a row r belongs to particle r / rowsPerParticle
+// (rows a multiple of rowsPerParticle).  Exactly one of quat [rows][4] /
+// mat [rows][9] is non-null.  nrm (optional) needs the workspace nrmPart of
+// rows x project_chunks(ldo) floats.
+int project_chunks(int ldo);
 cudaError_t launch_project(float4* const* volTable, const int* cls,
                            const float4* vol, int vdim, int pf,
                            const double* quat, const double* mat, int rows,
                            int rowsPerParticle, const int* iCol,
                            const int* iRow, int K, float* out, int ldo,
-                           const float* sigRcp, const float* ctf, float* nrm, int* flag,
-                           long long splitLo, cudaStream_t st);
+                           const float* sigRcp, const float* ctf, float* nrm, float* nrmPart,
+                           int* flag, long long splitLo, cudaStream_t st);
 // Either trans [nP][nT][2] or a shared phase bank [nT][K] complex.
 // splitLo != 0: write bf16 hi/lo planes (lo plane splitLo elements after
 // the hi plane at `out`) instead of floats; the same for launch_project.

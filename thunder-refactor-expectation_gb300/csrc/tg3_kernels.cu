@@ -198,46 +198,73 @@ __global__ void k_volume_blocks(const float2* __restrict__ vol, int vdim,
 }
 
 // ------------------------------------------------------------------------
-// Fourier-slice extraction.  One CTA per projected row (a rotation of a
-// particle): P[p] = trilinear(V, R (iCol pf, iRow pf, 0)), Friedel-mirrored
-// when x < 0 (Projector::project, src/Projector.cpp:356-374;
-// Volume::getByInterpolationFT, src/Image/Volume.cpp:308-332).  Optionally
-// nrm[row] = sum_p sigRcp ctf^2 |P|^2 of the row's particle.
+// Fourier-slice extraction: P[row][p] = trilinear(V, R_row (iCol pf, iRow pf,
+// 0)), Friedel-mirrored when x < 0 (Projector::project,
+// src/Projector.cpp:356-374; Volume::getByInterpolationFT,
+// src/Image/Volume.cpp:308-332).
+//
+// Work order.  A CTA takes one pixel chunk (kProjChunk consecutive pixels) of
+// one particle for a group of kProjG of its rotations, and consecutive CTAs
+// take the rotation groups of the same chunk.  The CTAs resident at any time
+// therefore sweep one narrow band of pixels through all of a particle's
+// rotations: the volume blocks that band touches (a few MB) stay in L2 while
+// every rotation that reuses them runs, instead of the particle's whole
+// footprint (about 160 MB at box 256) streaming from HBM once per reuse.
+//
+// A lane pair serves one pixel: lane half h reads slab z0 + h of the pixel's
+// 64-byte corner block (one 256-bit load) and the two partial sums meet
+// through one shuffle.  Each pair carries kProjU pixels of the chunk, whose
+// indices and norm weights are loaded once for all the CTA's rotations.
+//
+// With nrmPart != null, nrmPart[row * nChunks + chunk] receives the chunk's
+// share of sum_p sigRcp ctf^2 |P|^2 (k_norm_reduce sums the chunks).
 __global__ void __launch_bounds__(256)
 k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
           const float4* __restrict__ vol0, int vdim, int pf,
           const double* __restrict__ quat, const double* __restrict__ mat,
-          int rowsPerParticle, const int* __restrict__ iCol,
+          int rowsPerParticle, int nGroups, int nChunks, const int* __restrict__ iCol,
           const int* __restrict__ iRow, int K, float* __restrict__ out, int ldo,
           const float* __restrict__ sigRcp, const float* __restrict__ ctf,
-          float* __restrict__ nrm, int* __restrict__ flag, long long splitLo)
+          float* __restrict__ nrmPart, int* __restrict__ flag, long long splitLo)
 {
-    __shared__ float m[9];
-    __shared__ double red[32];
-    const int row = blockIdx.x;
-    const int l = row / rowsPerParticle;
-    if (threadIdx.x == 0) {
+    __shared__ float m[kProjG][9];
+    __shared__ float red[kProjG][8];
+    const int g = blockIdx.x % nGroups;
+    const int chunk = (blockIdx.x / nGroups) % nChunks;
+    const int l = blockIdx.x / (nGroups * nChunks);
+    const int r0 = g * kProjG;
+    const int nRot = min(kProjG, rowsPerParticle - r0);
+    const size_t row0 = (size_t)l * rowsPerParticle + r0;
+    if (threadIdx.x < nRot) {
+        const size_t row = row0 + threadIdx.x;
         double md[9];
         if (quat) {
-            double q[4] = {quat[4 * (size_t)row], quat[4 * (size_t)row + 1],
-                           quat[4 * (size_t)row + 2], quat[4 * (size_t)row + 3]};
+            double q[4] = {quat[4 * row], quat[4 * row + 1], quat[4 * row + 2], quat[4 * row + 3]};
             quat_to_mat(q, md);
         } else {
-            for (int i = 0; i < 9; i++) md[i] = mat[9 * (size_t)row + i];
+            for (int i = 0; i < 9; i++) md[i] = mat[9 * row + i];
         }
-        for (int i = 0; i < 9; i++) m[i] = (float)md[i];
+        for (int i = 0; i < 9; i++) m[threadIdx.x][i] = (float)md[i];
     }
     __syncthreads();
+    const int nOut = ldo / 2;
+    const int h = threadIdx.x & 1;
+    const int npairs = blockDim.x >> 1;
+    const int pBase = chunk * kProjChunk + (threadIdx.x >> 5) * 16 + ((threadIdx.x & 31) >> 1);
     const float4* __restrict__ vol = vol0;
     if (volTable) {
         const int k = cls ? cls[l] : 0;
         vol = (k >= 0 && k < kMaxClasses) ? volTable[k] : nullptr;
         if (!vol) {
-            // unknown class: record it, leave the row zero and skip sampling
+            // unknown class: record it, leave the rows' chunk zero and skip sampling
             if (threadIdx.x == 0 && flag) atomicOr(flag, 8);
-            for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x)
-                store_pair(out, splitLo, row, ldo, p, 0.f, 0.f);
-            if (nrm && threadIdx.x == 0) nrm[row] = 0.f;
+            for (int i = 0; i < nRot; i++)
+#pragma unroll
+                for (int u = 0; u < kProjU; u++) {
+                    const int p = pBase + u * npairs;
+                    if (p < nOut) store_pair_half(out, splitLo, row0 + i, ldo, p, h, 0.f, 0.f);
+                }
+            if (nrmPart && threadIdx.x < nRot) nrmPart[(row0 + threadIdx.x) * nChunks + chunk] = 0.f;
             return;
         }
     }
@@ -245,32 +272,31 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
     const float fpf = (float)pf;
     const float* sg = sigRcp ? sigRcp + (size_t)l * K : nullptr;
     const float* cf = ctf ? ctf + (size_t)l * K : nullptr;
-    float acc = 0.f;
-    // A lane pair serves one pixel: lane half h reads slab z0 + h of the
-    // pixel's 64-byte corner block (one 256-bit load) and the two partial sums
-    // meet through one shuffle.  Each pair carries kProjU pixels per
-    // iteration, all loads issued before any interpolation.  The trip count is
-    // uniform across a warp (the shuffle needs every lane); pixels past K
-    // read pixel 0's block harmlessly and store zeros.
-    const int nOut = ldo / 2;
-    const int h = threadIdx.x & 1;
-    const int npairs = blockDim.x >> 1;
-    const int warpBase = (threadIdx.x >> 5) * 16;
-    const int inWarp = (threadIdx.x & 31) >> 1;
-    for (int it = warpBase; it < nOut; it += kProjU * npairs) {
+    // the chunk's pixels: coordinates and norm weights, shared by all rotations
+    float pa[kProjU], pb[kProjU], w2[kProjU];
+#pragma unroll
+    for (int u = 0; u < kProjU; u++) {
+        const int p = pBase + u * npairs;
+        const int q = p < K ? p : 0;
+        pa[u] = (float)iCol[q] * fpf;
+        pb[u] = (float)iRow[q] * fpf;
+        w2[u] = (nrmPart && p < K) ? sg[q] * cf[q] * cf[q] : 0.f;
+    }
+    float acc[kProjG];
+#pragma unroll
+    for (int i = 0; i < kProjG; i++) acc[i] = 0.f;
+#pragma unroll
+    for (int i = 0; i < kProjG; i++) {
+        if (i >= nRot) break;   // uniform across the CTA
+        const float* mm = m[i];
         float fw[kProjU][3];
-        float w2[kProjU];   // sigRcp ctf^2 of the pixel, loaded with its indices
         bool cj[kProjU];
         const float4* e[kProjU];
 #pragma unroll
         for (int u = 0; u < kProjU; u++) {
-            const int p = it + inWarp + u * npairs;
-            const int q = p < K ? p : 0;
-            const float a = (float)iCol[q] * fpf, b = (float)iRow[q] * fpf;
-            w2[u] = nrm ? sg[q] * cf[q] * cf[q] : 0.f;
-            float x = m[0] * a + m[1] * b;
-            float y = m[3] * a + m[4] * b;
-            float z = m[6] * a + m[7] * b;
+            float x = mm[0] * pa[u] + mm[1] * pb[u];
+            float y = mm[3] * pa[u] + mm[4] * pb[u];
+            float z = mm[6] * pa[u] + mm[7] * pb[u];
             cj[u] = x < 0.f;
             if (cj[u]) { x = -x; y = -y; z = -z; }
             const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
@@ -301,21 +327,42 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
             im += c[u][1].y * (wx0 * wy1) + c[u][1].w * (wx1 * wy1);
             re += __shfl_xor_sync(0xffffffffu, re, 1);
             im += __shfl_xor_sync(0xffffffffu, im, 1);
-            const int p = it + inWarp + u * npairs;
+            const int p = pBase + u * npairs;
             if (p < nOut) {
                 if (p < K) {
                     if (cj[u]) im = -im;
-                    store_pair_half(out, splitLo, row, ldo, p, h, re, im);
-                    if (h == 0) acc = fmaf(w2[u], re * re + im * im, acc);
+                    store_pair_half(out, splitLo, row0 + i, ldo, p, h, re, im);
+                    if (h == 0) acc[i] = fmaf(w2[u], re * re + im * im, acc[i]);
                 } else {
-                    store_pair_half(out, splitLo, row, ldo, p, h, 0.f, 0.f);
+                    store_pair_half(out, splitLo, row0 + i, ldo, p, h, 0.f, 0.f);
                 }
             }
         }
     }
-    if (nrm) {
-        double s = block_sum_d((double)acc, red);
-        if (threadIdx.x == 0) nrm[row] = (float)s;
+    if (nrmPart) {
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+        for (int i = 0; i < kProjG; i++) {
+            const float v = warp_sum(acc[i]);
+            if (lane == 0) red[i][wid] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < nRot) {
+            float s = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[threadIdx.x][w];
+            nrmPart[(row0 + threadIdx.x) * nChunks + chunk] = s;
+        }
+    }
+}
+
+// nrm[row] = sum over the row's pixel chunks of nrmPart, in chunk order.
+__global__ void k_norm_reduce(const float* __restrict__ nrmPart, int rows, int nChunks,
+                              float* __restrict__ nrm)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < nChunks; c++) s += (double)nrmPart[(size_t)r * nChunks + c];
+        nrm[r] = (float)s;
     }
 }
 
@@ -994,17 +1041,29 @@ cudaError_t launch_volume_blocks(const float2* vol, int vdim, float4* blocks, cu
     return cudaGetLastError();
 }
 
+int project_chunks(int ldo) { return (ldo / 2 + kProjChunk - 1) / kProjChunk; }
+
 cudaError_t launch_project(float4* const* volTable, const int* cls, const float4* vol,
                            int vdim, int pf, const double* quat, const double* mat,
                            int rows, int rowsPerParticle, const int* iCol,
                            const int* iRow, int K, float* out, int ldo,
-                           const float* sigRcp, const float* ctf, float* nrm, int* flag, long long splitLo,
-                           cudaStream_t st)
+                           const float* sigRcp, const float* ctf, float* nrm, float* nrmPart,
+                           int* flag, long long splitLo, cudaStream_t st)
 {
     if (rows <= 0) return cudaSuccess;
-    k_project<<<rows, 256, 0, st>>>(volTable, cls, vol, vdim, pf, quat, mat,
-                                     rowsPerParticle, iCol, iRow, K, out, ldo,
-                                     sigRcp, ctf, nrm, flag, splitLo);
+    if (nrm && !nrmPart) return cudaErrorInvalidValue;
+    const int nP = rows / rowsPerParticle;
+    const int nGroups = (rowsPerParticle + kProjG - 1) / kProjG;
+    const int nChunks = project_chunks(ldo);
+    const long long grid = (long long)nP * nChunks * nGroups;
+    if (grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    k_project<<<(unsigned)grid, 256, 0, st>>>(volTable, cls, vol, vdim, pf, quat, mat,
+                                               rowsPerParticle, nGroups, nChunks, iCol, iRow, K,
+                                               out, ldo, sigRcp, ctf, nrm ? nrmPart : nullptr,
+                                               flag, splitLo);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !nrm) return e;
+    k_norm_reduce<<<grid_for((size_t)rows, 256), 256, 0, st>>>(nrmPart, rows, nChunks, nrm);
     return cudaGetLastError();
 }
 
