@@ -348,7 +348,7 @@ extern "C" int tg3_ctx_set_volume(tg3_ctx* c, int cls, const float* volume, int 
     if (!volume || vdim < 4 || (vdim & 1) || pf < 1) return fail(TG3_ERR_ARG, "bad volume");
     Volume& v = c->vol[cls];
     const size_t nvox = (size_t)vdim * vdim * (vdim / 2 + 1);
-    const size_t bytes = nvox * 4 * sizeof(float4);   // 64-byte corner blocks
+    const size_t bytes = volume_block_count(vdim) * 4 * sizeof(float4);   // 64-byte blocks
     if (v.bytes != bytes) {
         TG3_CUDA(cudaStreamSynchronize(c->stream));
         cudaFree(v.blocks);

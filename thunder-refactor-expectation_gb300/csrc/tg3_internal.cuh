@@ -63,7 +63,7 @@ struct Buffer {
 };
 
 struct Volume {
-    float4* blocks = nullptr;   // [vdim][vdim][nx] corner blocks, 4 float4 each
+    float4* blocks = nullptr;   // volume_block_count(vdim) corner blocks, 4 float4 each
     int vdim = 0;
     int pf = 0;
     size_t bytes = 0;
@@ -135,6 +135,8 @@ cudaError_t launch_translate(const double* trans, int nT, int idim, const int* i
 cudaError_t launch_ctf(const float* attr, int nImg, float px, int idim,
                        const int* iCol, const int* iRow, int K, float* out,
                        cudaStream_t st);
+// corner blocks the projection volume of edge vdim occupies (64 bytes each)
+size_t volume_block_count(int vdim);
 cudaError_t launch_volume_blocks(const float2* vol, int vdim, float4* blocks,
                                 cudaStream_t st);
 // rows: projected rows; a row r belongs to particle r / rowsPerParticle

@@ -1,10 +1,10 @@
 // tg3_kernels.cu -- the plain (FP32) E-step and insertion kernels for sm_103a.
 //
 // Data layout in HBM (all particle-major):
-//   projection volume  : 64-byte corner blocks [vdim][vdim][nx] (see
-//                        k_volume_blocks), all eight corners of a trilinear
-//                        sample in one half cache line, read by two lanes
-//                        with one 256-bit load each;
+//   projection volume  : 64-byte corner blocks (see k_volume_blocks), all
+//                        eight corners of a trilinear sample in one half
+//                        cache line, read by two lanes with one 256-bit load
+//                        each, placed in 32^3-voxel cubes (brick_index);
 //   projections P      : [row][Kp] floats, a complex row padded with zeros to
 //                        Kp floats (Kp a multiple of 64);
 //   shifted data A''   : [particle][translation][Kp] floats, the complex
@@ -167,15 +167,34 @@ __global__ void k_ctf(const float* __restrict__ attr, int nImg, float px, int id
     }
 }
 
-// Corner-block layout of the projection volume: the 64-byte element of voxel
-// (z, y, x) holds, for slab z then slab z + 1, V[.][y][x], V[.][y][x+1],
-// V[.][y+1][x], V[.][y+1][x+1] (rows and slabs taken modulo vdim, the wrap of
+// Placement of voxel (z, y, x)'s corner block: the volume is cut into
+// cubes of 32^3 voxels (32768 blocks = 2 MB, one large page each, cubes in
+// z, y, x order), each cube into 4^3 bricks of 8^3 voxels, voxels x-fastest
+// within a brick.  A projection's samples within one pixel band then touch a
+// few hundred pages instead of one page per z plane of the band, which in
+// the plain [z][y][x] order left the gather translation-bound.
+__device__ __forceinline__ size_t brick_index(int x, int y, int z, int nxc, int nyc)
+{
+    const size_t cube = ((size_t)(z >> 5) * nyc + (y >> 5)) * nxc + (x >> 5);
+    const int brick = (((z >> 3) & 3) * 4 + ((y >> 3) & 3)) * 4 + ((x >> 3) & 3);
+    const int v = ((z & 7) * 8 + (y & 7)) * 8 + (x & 7);
+    return (cube * 64 + brick) * 512 + v;
+}
+
+// Cube counts along x (nx = vdim / 2 + 1 stored columns) and along y and z.
+__host__ __device__ __forceinline__ int cubes_x(int vdim) { return (vdim / 2 + 1 + 31) / 32; }
+__host__ __device__ __forceinline__ int cubes_yz(int vdim) { return (vdim + 31) / 32; }
+
+// Corner-block content: the 64-byte element of voxel (z, y, x) holds, for
+// slab z then slab z + 1, V[.][y][x], V[.][y][x+1], V[.][y+1][x],
+// V[.][y+1][x+1] (rows and slabs taken modulo vdim, the wrap of
 // Volume::iFTHalf; x + 1 past the stored half reads zero).  A trilinear
-// sample then reads one aligned half cache line: one L1 wavefront per sample.
+// sample then reads one aligned half cache line.
 __global__ void k_volume_blocks(const float2* __restrict__ vol, int vdim,
                                 float4* __restrict__ blocks)
 {
     const int nx = vdim / 2 + 1;
+    const int nxc = cubes_x(vdim), nyc = cubes_yz(vdim);
     const size_t n = (size_t)vdim * vdim * nx;
     const float2 zero = make_float2(0.f, 0.f);
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
@@ -183,6 +202,7 @@ __global__ void k_volume_blocks(const float2* __restrict__ vol, int vdim,
         const int x = (int)(i % nx);
         const int y = (int)((i / nx) % vdim);
         const int z = (int)(i / ((size_t)nx * vdim));
+        const size_t d = brick_index(x, y, z, nxc, nyc);
         const int y1 = y + 1 == vdim ? 0 : y + 1;
 #pragma unroll
         for (int k = 0; k < 2; k++) {
@@ -190,9 +210,9 @@ __global__ void k_volume_blocks(const float2* __restrict__ vol, int vdim,
             const size_t i0 = ((size_t)zz * vdim + y) * nx + x;
             const size_t i1 = ((size_t)zz * vdim + y1) * nx + x;
             const float2 a = vol[i0], b = (x + 1 < nx) ? vol[i0 + 1] : zero;
-            const float2 c = vol[i1], d = (x + 1 < nx) ? vol[i1 + 1] : zero;
-            blocks[4 * i + 2 * k] = make_float4(a.x, a.y, b.x, b.y);
-            blocks[4 * i + 2 * k + 1] = make_float4(c.x, c.y, d.x, d.y);
+            const float2 c = vol[i1], dd = (x + 1 < nx) ? vol[i1 + 1] : zero;
+            blocks[4 * d + 2 * k] = make_float4(a.x, a.y, b.x, b.y);
+            blocks[4 * d + 2 * k + 1] = make_float4(c.x, c.y, dd.x, dd.y);
         }
     }
 }
@@ -218,7 +238,7 @@ __global__ void k_volume_blocks(const float2* __restrict__ vol, int vdim,
 //
 // With nrmPart != null, nrmPart[row * nChunks + chunk] receives the chunk's
 // share of sum_p sigRcp ctf^2 |P|^2 (k_norm_reduce sums the chunks).
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
           const float4* __restrict__ vol0, int vdim, int pf,
           const double* __restrict__ quat, const double* __restrict__ mat,
@@ -268,7 +288,7 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
             return;
         }
     }
-    const int nx = vdim / 2 + 1;
+    const int nxc = cubes_x(vdim), nyc = cubes_yz(vdim);
     const float fpf = (float)pf;
     const float* sg = sigRcp ? sigRcp + (size_t)l * K : nullptr;
     const float* cf = ctf ? ctf + (size_t)l * K : nullptr;
@@ -306,7 +326,7 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
             fw[u][2] = z - zf;
             const int ys = y0 < 0 ? y0 + vdim : y0;
             const int zs = z0 < 0 ? z0 + vdim : z0;
-            e[u] = vol + 4 * (((size_t)zs * vdim + ys) * nx + x0) + 2 * h;
+            e[u] = vol + 4 * brick_index(x0, ys, zs, nxc, nyc) + 2 * h;
         }
         float4 c[kProjU][2];
 #pragma unroll
@@ -1032,6 +1052,11 @@ cudaError_t launch_ctf(const float* attr, int nImg, float px, int idim, const in
     dim3 grid(nImg);
     k_ctf<<<grid, 256, 0, st>>>(attr, nImg, px, idim, iCol, iRow, K, out);
     return cudaGetLastError();
+}
+
+size_t volume_block_count(int vdim)
+{
+    return (size_t)cubes_x(vdim) * cubes_yz(vdim) * cubes_yz(vdim) * 32768;
 }
 
 cudaError_t launch_volume_blocks(const float2* vol, int vdim, float4* blocks, cudaStream_t st)
