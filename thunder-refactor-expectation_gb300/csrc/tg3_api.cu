@@ -433,9 +433,9 @@ static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
     if (!D) return st;
     float* nrm = (float*)ws_get(c, WS_NRM, sizeof(float) * (size_t)nP * nR, &st);
     if (!nrm) return st;
-    float* nrmPart = (float*)ws_get(
-        c, WS_NRM_PART, sizeof(float) * (size_t)nP * nR * project_chunks((int)Kp), &st);
-    if (!nrmPart) return st;
+    float* pscr = (float*)ws_get(
+        c, WS_PROJ, sizeof(float) * project_scratch_floats(nP * nR, (int)Kp), &st);
+    if (!pscr) return st;
     double* x0 = (double*)ws_get(c, WS_X0, sizeof(double) * (size_t)nP, &st);
     if (!x0) return st;
     cudaStream_t s = c->stream;
@@ -452,7 +452,7 @@ static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
         StageTimer tm(c, TG3_STAGE_PROJECT);
         TG3_CUDA(launch_project(c->d_volTable, cls, nullptr, v0.vdim, v0.pf, quat, nullptr,
                                 nP * nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, sigRcp, ctf, nrm,
-                                nrmPart, c->d_flag, splitP, s));
+                                pscr, c->d_flag, splitP, s));
     }
     {
         StageTimer tm(c, TG3_STAGE_SHIFT);
@@ -655,9 +655,12 @@ extern "C" int tg3_project_d(tg3_ctx* c, int cls, const double* rotMat, int nR, 
     if (!rotMat || !out || nR <= 0) return fail(TG3_ERR_ARG, "bad project args");
     const Volume& v = c->vol[cls];
     if ((st = check_geometry(c, v.vdim, v.pf))) return st;
+    float* pscr = (float*)ws_get(
+        c, WS_PROJ, sizeof(float) * project_scratch_floats(nR, 2 * c->px.K), &st);
+    if (!pscr) return st;
     TG3_CUDA(launch_project(nullptr, nullptr, v.blocks, v.vdim, v.pf, nullptr, rotMat, nR, nR,
                             c->px.iCol, c->px.iRow, c->px.K, out, 2 * c->px.K, nullptr, nullptr,
-                            nullptr, nullptr, c->d_flag, 0, c->stream));
+                            nullptr, pscr, c->d_flag, 0, c->stream));
     return TG3_OK;
 }
 
@@ -1161,13 +1164,15 @@ extern "C" int tg3_global_scan_d(tg3_ctx* c, int cls, int nImg, int nR, int nT, 
     float* abs2 = (float*)(m + oAbs);
     float2* bank = (float2*)(m + oBank);
     float* sc2 = (float*)(m + oSc);
+    float* pscr = (float*)ws_get(c, WS_PROJ, sizeof(float) * project_scratch_floats(nR, Kp), &st);
+    if (!pscr) return st;
     cudaStream_t s = c->stream;
     const long long splitP = split ? (long long)nR * Kp : 0;
     {
         StageTimer tm(c, TG3_STAGE_PROJECT);
         TG3_CUDA(launch_project(nullptr, nullptr, v.blocks, v.vdim, v.pf, nullptr, rotMat, nR, nR,
                                 c->px.iCol, c->px.iRow, K, P, Kp, nullptr, nullptr, nullptr,
-                                nullptr, c->d_flag, splitP, s));
+                                pscr, c->d_flag, splitP, s));
         k_abs2_from<<<nR, 256, 0, s>>>(P, splitP, K, Kp, abs2, Kq);
         TG3_LAUNCH_CHECK("projection norms");
     }

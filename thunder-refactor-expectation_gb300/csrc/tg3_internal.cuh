@@ -47,7 +47,7 @@ enum WsSlot {
     WS_A,            // shifted, weighted data [nP][nT][Kp]
     WS_D,            // hypothesis-dependent log-likelihood part [nP][nR][nT]
     WS_NRM,          // sum sigRcp ctf^2 |P|^2 per projected row
-    WS_NRM_PART,     // its per-pixel-chunk shares [rows][project_chunks(ldo)]
+    WS_PROJ,         // projection scratch: FP32 matrices and norm shares
     WS_X0,           // sum sigRcp |X|^2 per particle (double)
     WS_PAIRS_TMP,
     WS_H2D,          // staging of host inputs
@@ -141,15 +141,16 @@ cudaError_t launch_volume_blocks(const float2* vol, int vdim, float4* blocks,
                                 cudaStream_t st);
 // rows: projected rows; a row r belongs to particle r / rowsPerParticle
 // (rows a multiple of rowsPerParticle).  Exactly one of quat [rows][4] /
-// mat [rows][9] is non-null.  nrm (optional) needs the workspace nrmPart of
-// rows x project_chunks(ldo) floats.
+// mat [rows][9] is non-null; nrm is optional.  scratch: device workspace of
+// project_scratch_floats(rows, ldo) floats (FP32 matrices, norm shares).
 int project_chunks(int ldo);
+size_t project_scratch_floats(int rows, int ldo);
 cudaError_t launch_project(float4* const* volTable, const int* cls,
                            const float4* vol, int vdim, int pf,
                            const double* quat, const double* mat, int rows,
                            int rowsPerParticle, const int* iCol,
                            const int* iRow, int K, float* out, int ldo,
-                           const float* sigRcp, const float* ctf, float* nrm, float* nrmPart,
+                           const float* sigRcp, const float* ctf, float* nrm, float* scratch,
                            int* flag, long long splitLo, cudaStream_t st);
 // Either trans [nP][nT][2] or a shared phase bank [nT][K] complex.
 // splitLo != 0: write bf16 hi/lo planes (lo plane splitLo elements after

@@ -238,10 +238,9 @@ __global__ void k_volume_blocks(const float2* __restrict__ vol, int vdim,
 //
 // With nrmPart != null, nrmPart[row * nChunks + chunk] receives the chunk's
 // share of sum_p sigRcp ctf^2 |P|^2 (k_norm_reduce sums the chunks).
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, 4)
 k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
-          const float4* __restrict__ vol0, int vdim, int pf,
-          const double* __restrict__ quat, const double* __restrict__ mat,
+          const float4* __restrict__ vol0, int vdim, int pf, const float* __restrict__ mf,
           int rowsPerParticle, int nGroups, int nChunks, const int* __restrict__ iCol,
           const int* __restrict__ iRow, int K, float* __restrict__ out, int ldo,
           const float* __restrict__ sigRcp, const float* __restrict__ ctf,
@@ -255,17 +254,7 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
     const int r0 = g * kProjG;
     const int nRot = min(kProjG, rowsPerParticle - r0);
     const size_t row0 = (size_t)l * rowsPerParticle + r0;
-    if (threadIdx.x < nRot) {
-        const size_t row = row0 + threadIdx.x;
-        double md[9];
-        if (quat) {
-            double q[4] = {quat[4 * row], quat[4 * row + 1], quat[4 * row + 2], quat[4 * row + 3]};
-            quat_to_mat(q, md);
-        } else {
-            for (int i = 0; i < 9; i++) md[i] = mat[9 * row + i];
-        }
-        for (int i = 0; i < 9; i++) m[threadIdx.x][i] = (float)md[i];
-    }
+    if (threadIdx.x < 9 * nRot) m[threadIdx.x / 9][threadIdx.x % 9] = mf[9 * row0 + threadIdx.x];
     __syncthreads();
     const int nOut = ldo / 2;
     const int h = threadIdx.x & 1;
@@ -302,13 +291,11 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
         pb[u] = (float)iRow[q] * fpf;
         w2[u] = (nrmPart && p < K) ? sg[q] * cf[q] * cf[q] : 0.f;
     }
-    float acc[kProjG];
-#pragma unroll
-    for (int i = 0; i < kProjG; i++) acc[i] = 0.f;
-#pragma unroll
-    for (int i = 0; i < kProjG; i++) {
-        if (i >= nRot) break;   // uniform across the CTA
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll 1
+    for (int i = 0; i < nRot; i++) {   // nRot is uniform across the CTA
         const float* mm = m[i];
+        float acc = 0.f;
         float fw[kProjU][3];
         bool cj[kProjU];
         const float4* e[kProjU];
@@ -352,26 +339,43 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
                 if (p < K) {
                     if (cj[u]) im = -im;
                     store_pair_half(out, splitLo, row0 + i, ldo, p, h, re, im);
-                    if (h == 0) acc[i] = fmaf(w2[u], re * re + im * im, acc[i]);
+                    if (h == 0) acc = fmaf(w2[u], re * re + im * im, acc);
                 } else {
                     store_pair_half(out, splitLo, row0 + i, ldo, p, h, 0.f, 0.f);
                 }
             }
         }
+        // the warp's share of this rotation's norm, in a fixed order
+        if (nrmPart) {
+            acc = warp_sum(acc);
+            if (lane == 0) red[i][wid] = acc;
+        }
     }
     if (nrmPart) {
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-        for (int i = 0; i < kProjG; i++) {
-            const float v = warp_sum(acc[i]);
-            if (lane == 0) red[i][wid] = v;
-        }
         __syncthreads();
         if (threadIdx.x < nRot) {
             float s = 0.f;
             for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[threadIdx.x][w];
             nrmPart[(row0 + threadIdx.x) * nChunks + chunk] = s;
         }
+    }
+}
+
+// FP32 rotation matrix of each projected row, from its quaternion
+// (quat_to_mat in FP64, then rounded) or from an FP64 matrix.
+__global__ void k_rot_f32(const double* __restrict__ quat, const double* __restrict__ mat,
+                          int rows, float* __restrict__ mf)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        double md[9];
+        if (quat) {
+            double q[4] = {quat[4 * (size_t)r], quat[4 * (size_t)r + 1], quat[4 * (size_t)r + 2],
+                           quat[4 * (size_t)r + 3]};
+            quat_to_mat(q, md);
+        } else {
+            for (int i = 0; i < 9; i++) md[i] = mat[9 * (size_t)r + i];
+        }
+        for (int i = 0; i < 9; i++) mf[9 * (size_t)r + i] = (float)md[i];
     }
 }
 
@@ -1068,25 +1072,34 @@ cudaError_t launch_volume_blocks(const float2* vol, int vdim, float4* blocks, cu
 
 int project_chunks(int ldo) { return (ldo / 2 + kProjChunk - 1) / kProjChunk; }
 
+size_t project_scratch_floats(int rows, int ldo)
+{
+    return (size_t)rows * (9 + project_chunks(ldo));
+}
+
 cudaError_t launch_project(float4* const* volTable, const int* cls, const float4* vol,
                            int vdim, int pf, const double* quat, const double* mat,
                            int rows, int rowsPerParticle, const int* iCol,
                            const int* iRow, int K, float* out, int ldo,
-                           const float* sigRcp, const float* ctf, float* nrm, float* nrmPart,
+                           const float* sigRcp, const float* ctf, float* nrm, float* scratch,
                            int* flag, long long splitLo, cudaStream_t st)
 {
     if (rows <= 0) return cudaSuccess;
-    if (nrm && !nrmPart) return cudaErrorInvalidValue;
+    if (!scratch || rows % rowsPerParticle) return cudaErrorInvalidValue;
     const int nP = rows / rowsPerParticle;
     const int nGroups = (rowsPerParticle + kProjG - 1) / kProjG;
     const int nChunks = project_chunks(ldo);
     const long long grid = (long long)nP * nChunks * nGroups;
     if (grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    k_project<<<(unsigned)grid, 256, 0, st>>>(volTable, cls, vol, vdim, pf, quat, mat,
-                                               rowsPerParticle, nGroups, nChunks, iCol, iRow, K,
-                                               out, ldo, sigRcp, ctf, nrm ? nrmPart : nullptr,
-                                               flag, splitLo);
+    float* mf = scratch;
+    float* nrmPart = scratch + (size_t)rows * 9;
+    k_rot_f32<<<grid_for((size_t)rows, 256), 256, 0, st>>>(quat, mat, rows, mf);
     cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_project<<<(unsigned)grid, 256, 0, st>>>(volTable, cls, vol, vdim, pf, mf, rowsPerParticle,
+                                               nGroups, nChunks, iCol, iRow, K, out, ldo, sigRcp,
+                                               ctf, nrm ? nrmPart : nullptr, flag, splitLo);
+    e = cudaGetLastError();
     if (e != cudaSuccess || !nrm) return e;
     k_norm_reduce<<<grid_for((size_t)rows, 256), 256, 0, st>>>(nrmPart, rows, nChunks, nrm);
     return cudaGetLastError();
