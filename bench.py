@@ -318,7 +318,8 @@ def run_tg3(args, rank, world, local_rank):
         return {"kernel": "k_gemm_nt_fp32" if p_ == tg3.SCORE_FP32 else "k_gemm_bf16x3 (tcgen05)",
                 "bound": "tensor", "achieved": round(ach, 2), "peak": round(pk, 1),
                 "unit": "TFLOP/s", "frac": round(ach / pk, 4), "peak_source": note,
-                "traffic": TRAFFIC.get("cross_bf16x3" if p_ != tg3.SCORE_FP32 else "cross_fp32"),
+                "traffic": traffic("cross_bf16x3" if p_ != tg3.SCORE_FP32 else "cross_fp32",
+                                   W["box"], nP),
                 "algorithmic_flop_per_launch": flop,
                 "executed_bf16_flop_per_launch": 3 * flop if p_ != tg3.SCORE_FP32 else None}
 
@@ -327,7 +328,9 @@ def run_tg3(args, rank, world, local_rank):
         return {"kernel": "k_project", "bound": "hbm", "achieved": round(ach, 1),
                 "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4),
                 "peak_source": f"hbm_gbs, {kind} (MEASURED_PEAKS.json)",
-                "traffic": TRAFFIC.get("project"),
+                "traffic": traffic("project", W["box"], nP),
+                "traffic_note": "DRAM bytes per launch (ncu); below the algorithmic bytes "
+                                "because L2 serves the volume blocks a pixel band reuses",
                 "algorithmic_bytes_per_launch": proj_bytes}
 
     dominant = max(("project", "cross"), key=lambda k: per_launch(stages, k))
@@ -448,9 +451,17 @@ def run_global(args, rank, world, local_rank):
     return res
 
 
-# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# the ncu captures summarised in profiles/ (box 256, 64 particles per launch).
-TRAFFIC = {}
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per particle of a
+# launch, box 256 local workload: one 1-pass ncu capture of a 64-particle
+# launch (k_project 13.36 GB read + 5.09 GB written; k_gemm_bf16x3 5.62 GB +
+# 0.02 GB), divided by 64.  Both grow in proportion to the particles of a
+# launch (every particle's volume footprint and operand planes are its own).
+TRAFFIC_PER_PARTICLE_BOX256 = {"project": 18.45e9 / 64, "cross_bf16x3": 5.643e9 / 64}
+
+
+def traffic(key, box, nP):
+    per = TRAFFIC_PER_PARTICLE_BOX256.get(key) if box == 256 else None
+    return None if per is None else round(per * nP)
 
 
 def ctx_kp(K):
@@ -616,7 +627,8 @@ def reduce_max(world, x: float) -> float:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    # about 2 s of timed work at the default batch: enough clock samples
+    ap.add_argument("--steps", type=int, default=150)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="tg3", choices=["tg3", "reference"])
     ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16x3"])

@@ -348,6 +348,8 @@ extern "C" int tg3_ctx_set_volume(tg3_ctx* c, int cls, const float* volume, int 
     if (!volume || vdim < 4 || (vdim & 1) || pf < 1) return fail(TG3_ERR_ARG, "bad volume");
     Volume& v = c->vol[cls];
     const size_t nvox = (size_t)vdim * vdim * (vdim / 2 + 1);
+    if (volume_block_count(vdim) > (size_t)0x7fffffff)
+        return fail(TG3_ERR_ARG, "volume edge too large for 32-bit block indices");
     const size_t bytes = volume_block_count(vdim) * 4 * sizeof(float4);   // 64-byte blocks
     if (v.bytes != bytes) {
         TG3_CUDA(cudaStreamSynchronize(c->stream));

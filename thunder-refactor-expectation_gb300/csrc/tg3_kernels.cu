@@ -254,6 +254,23 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
     const int r0 = g * kProjG;
     const int nRot = min(kProjG, rowsPerParticle - r0);
     const size_t row0 = (size_t)l * rowsPerParticle + r0;
+    // brick_index split into per-axis terms: tx[x] + ty[y + vdim/2] +
+    // tz[z + vdim/2], the y and z tables absorbing the wrap of negative rows
+    extern __shared__ int tab[];
+    const int nx = vdim / 2 + 1, half = vdim / 2;
+    int* tx = tab;
+    int* ty = tab + nx;
+    int* tz = ty + vdim;
+    {
+        const int nxc = cubes_x(vdim), nyc = cubes_yz(vdim);
+        for (int j = threadIdx.x; j < nx; j += blockDim.x)
+            tx[j] = (j >> 5) * 32768 + ((j >> 3) & 3) * 512 + (j & 7);
+        for (int j = threadIdx.x; j < vdim; j += blockDim.x) {
+            const int w = j - half < 0 ? j + half : j - half;
+            ty[j] = (w >> 5) * nxc * 32768 + ((w >> 3) & 3) * 2048 + (w & 7) * 8;
+            tz[j] = (w >> 5) * nyc * nxc * 32768 + ((w >> 3) & 3) * 8192 + (w & 7) * 64;
+        }
+    }
     if (threadIdx.x < 9 * nRot) m[threadIdx.x / 9][threadIdx.x % 9] = mf[9 * row0 + threadIdx.x];
     __syncthreads();
     const int nOut = ldo / 2;
@@ -277,7 +294,6 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
             return;
         }
     }
-    const int nxc = cubes_x(vdim), nyc = cubes_yz(vdim);
     const float fpf = (float)pf;
     const float* sg = sigRcp ? sigRcp + (size_t)l * K : nullptr;
     const float* cf = ctf ? ctf + (size_t)l * K : nullptr;
@@ -311,9 +327,8 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
             fw[u][0] = x - xf;
             fw[u][1] = y - yf;
             fw[u][2] = z - zf;
-            const int ys = y0 < 0 ? y0 + vdim : y0;
-            const int zs = z0 < 0 ? z0 + vdim : z0;
-            e[u] = vol + 4 * brick_index(x0, ys, zs, nxc, nyc) + 2 * h;
+            const unsigned blk = (unsigned)(tx[x0] + ty[y0 + half] + tz[z0 + half]);
+            e[u] = vol + 4 * (size_t)blk + 2 * h;
         }
         float4 c[kProjU][2];
 #pragma unroll
@@ -1096,7 +1111,13 @@ cudaError_t launch_project(float4* const* volTable, const int* cls, const float4
     k_rot_f32<<<grid_for((size_t)rows, 256), 256, 0, st>>>(quat, mat, rows, mf);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_project<<<(unsigned)grid, 256, 0, st>>>(volTable, cls, vol, vdim, pf, mf, rowsPerParticle,
+    const size_t tabBytes = sizeof(int) * ((size_t)vdim / 2 + 1 + 2 * (size_t)vdim);
+    if (tabBytes > 48 * 1024) {
+        e = cudaFuncSetAttribute(k_project, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tabBytes);
+        if (e != cudaSuccess) return e;
+    }
+    k_project<<<(unsigned)grid, 256, tabBytes, st>>>(volTable, cls, vol, vdim, pf, mf, rowsPerParticle,
                                                nGroups, nChunks, iCol, iRow, K, out, ldo, sigRcp,
                                                ctf, nrm ? nrmPart : nullptr, flag, splitLo);
     e = cudaGetLastError();
