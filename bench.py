@@ -36,7 +36,11 @@ for _p in (str(ROOT), str(PKG)):
 METRIC = "E-step particles/sec, box 256: learned+BF16 vs plain FP32 GPU at equal pose error"
 UNIT = "particles/s"
 WORKLOAD = dict(box=256, pixel_size=1.1, n_blobs=200, sigma_a=(1.5, 3.0), radius_px=80.0,
-                shift=8.0, snr=0.03, rU=80, pf=2, nR=1000, nT=100, kappa=200.0)
+                shift=8.0, snr=0.03, rU=80, pf=2, nR=1000, nT=100, kappa=200.0,
+                n_classes=1, shared=1.0)
+# the same local phase with 3 classes whose maps share 70 % of their blobs
+# (the other 30 % re-drawn per class, particles split 1:1:1) at cutoff 120
+WORKLOAD_C3 = dict(WORKLOAD, rU=120, n_classes=3, shared=0.7)
 
 
 def peaks():
@@ -104,19 +108,21 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------- workload ---
-def make_workload(torch, dev, nP, n_batches, seed, box=None):
-    """Synthetic map + particle batches, generated on the GPU."""
+def make_workload(torch, dev, nP, n_batches, seed, box=None, W0=None):
+    """Synthetic class maps + particle batches, generated on the GPU."""
     from tg3 import synth
-    W = dict(WORKLOAD)
+    W = dict(WORKLOAD if W0 is None else W0)
     if box is not None:          # reduced case for profiling captures
         scale = box / W["box"]
         W.update(box=box, rU=max(8, int(W["rU"] * scale)), radius_px=W["radius_px"] * scale)
     rng = np.random.default_rng(seed)
-    bm = synth.blob_map(rng, W["n_blobs"], W["sigma_a"], W["pixel_size"], W["radius_px"])
-    vol = synth.padded_volume(bm, W["box"], W["pf"], device=dev, dtype=torch.float32)
+    maps = synth.class_maps(rng, W["n_classes"], W["shared"], W["n_blobs"], W["sigma_a"],
+                            W["pixel_size"], W["radius_px"])
+    vols = [synth.padded_volume(bm, W["box"], W["pf"], device=dev, dtype=torch.float32)
+            for bm in maps]
     rL = synth.config_rL(W["box"], W["pixel_size"])
     n = nP * n_batches
-    st = synth.make_stack(seed + 1, [bm], W["box"], W["pixel_size"], W["pf"], W["rU"], rL, n,
+    st = synth.make_stack(seed + 1, maps, W["box"], W["pixel_size"], W["pf"], W["rU"], rL, n,
                           W["shift"], W["snr"], device=dev)
     qc, tc = synth.perturb_poses(rng, st.quat_true, st.trans_true, 3.0, 1.0)
     qs, ts = synth.local_hypotheses(rng, qc, tc, W["nR"], W["nT"], W["kappa"], 2.0)
@@ -132,11 +138,13 @@ def make_workload(torch, dev, nP, n_batches, seed, box=None):
             sig=np.ascontiguousarray(st.sigRcp[sl].astype(np.float32)),
             quat=np.ascontiguousarray(qs[sl]), trans=np.ascontiguousarray(ts[sl]),
             pwR=np.full((nP, nR), 1.0 / nR), pwT=np.full((nP, nT), 1.0 / nT), pwC=np.ones(nP),
+            cls=np.ascontiguousarray(st.cls_true[sl].astype(np.int32)),
+            q_true=np.ascontiguousarray(st.quat_true[sl]),
             perm_r=perm_r, perm_t=perm_t,
             u0_r=rng.random(nP) / nR, u0_t=rng.random(nP) / nT,
             peak_r=np.full(nP, np.nan), peak_t=np.zeros(nP))
         batches.append(host)
-    return W, vol, st, batches
+    return W, vols, st, batches
 
 
 def to_dev(torch, dev, host):
@@ -180,13 +188,15 @@ def run_tg3(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = f"cuda:{local_rank}"
     nP = args.batch
-    W, vol, st, batches = make_workload(torch, dev, nP, args.batches, 1000 + 1 + 97 * rank,
-                                        box=args.box)
+    W0 = WORKLOAD_C3 if args.workload == "local256c3" else WORKLOAD
+    W, vols, st, batches = make_workload(torch, dev, nP, args.batches, 1000 + 1 + 97 * rank,
+                                         box=args.box, W0=W0)
     nR, nT, K = W["nR"], W["nT"], st.K
     ctx = tg3.Context(local_rank)
-    ctx.set_volume(0, vol, W["pf"])
+    for c, v in enumerate(vols):
+        ctx.set_volume(c, v, W["pf"])
     ctx.set_pixels(st.iCol, st.iRow, W["box"])
-    del vol
+    del vols
     dbat = [to_dev(torch, dev, b) for b in batches]
     out = dict(wC=torch.empty(nP, dtype=torch.float64, device=dev),
                wR=torch.empty((nP, nR), dtype=torch.float64, device=dev),
@@ -203,7 +213,7 @@ def run_tg3(args, rank, world, local_rank):
     def step(i, prec):
         b = dbat[i % len(dbat)]
         ctx.local_phase(nP, nR, nT, b["dat"], b["ctf"], b["sig"], b["quat"], b["trans"],
-                        b["pwR"], b["pwT"], b["pwC"], None, out["wC"], out["wR"], out["wT"],
+                        b["pwR"], b["pwT"], b["pwC"], b["cls"], out["wC"], out["wR"], out["wT"],
                         out["base"], None, prec)
         ctx.resample(nP, nR, out["wR"], b["pwR"], b["perm_r"], b["u0_r"], b["peak_r"], nR,
                      out["src_r"], out["w_r"], out["top"])
@@ -238,12 +248,30 @@ def run_tg3(args, rank, world, local_rank):
         ctx.sync()
         return reduce_max(world, ev0.elapsed_time(ev1)), stages, clocks
 
+    def best_rotations(prec_):
+        """Best rotation (argmax of the marginal wR) of every particle of
+        batch 0, and its angle to the particle's true pose in degrees."""
+        step(0, prec_)
+        ctx.sync()
+        best = out["wR"].argmax(1).cpu().numpy()
+        q = batches[0]["quat"][np.arange(nP), best]
+        dot = np.abs((q * batches[0]["q_true"]).sum(1)).clip(0.0, 1.0)
+        return best, np.degrees(2.0 * np.arccos(dot))
+
     prec = tg3.SCORE_BF16X3 if args.precision == "bf16x3" else tg3.SCORE_FP32
     ms, stages, clocks = timed(prec)
     plain = None
     if prec != tg3.SCORE_FP32 and not args.no_compare:
         ms_p, stages_p, clocks_p = timed(tg3.SCORE_FP32)
         plain = (ms_p, stages_p, clocks_p)
+    best_m, ang_m = best_rotations(prec)
+    pose = {"particles": nP, f"median_deg_{args.precision}": round(float(np.median(ang_m)), 4)}
+    if prec != tg3.SCORE_FP32:
+        best_p, ang_p = best_rotations(tg3.SCORE_FP32)
+        pose.update(median_deg_fp32=round(float(np.median(ang_p)), 4),
+                    same_best_rotation=round(float(np.mean(best_m == best_p)), 4))
+    pose["note"] = ("best local rotation (argmax of the marginal weights) against the true pose "
+                    "of the synthetic particle")
 
     # ---- insertion of every particle's best pose (MKB kernel), timed alone
     ctx.insert_begin(W["pf"] * W["box"], W["pf"])
@@ -267,7 +295,7 @@ def run_tg3(args, rank, world, local_rank):
     # ---- end to end: host buffers, copies inside the timed region
     hbat = [pin(torch, b) for b in batches]
     hout = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in out.items()}
-    inputs = ("dat", "ctf", "sig", "quat", "trans", "pwR", "pwT", "pwC")
+    inputs = ("dat", "ctf", "sig", "quat", "trans", "pwR", "pwT", "pwC", "cls")
     h2d = sum(hbat[0][k].numel() * hbat[0][k].element_size() for k in inputs)
     h2d += sum(hbat[0][k].numel() * hbat[0][k].element_size()
                for k in ("perm_r", "perm_t", "u0_r", "u0_t", "peak_r", "peak_t", "pwR", "pwT"))
@@ -277,7 +305,7 @@ def run_tg3(args, rank, world, local_rank):
     def e2e_step(i):
         b = hbat[i % len(hbat)]
         ctx.local_phase_host(nP, nR, nT, b["dat"], b["ctf"], b["sig"], b["quat"], b["trans"],
-                             b["pwR"], b["pwT"], b["pwC"], None, hout["wC"], hout["wR"],
+                             b["pwR"], b["pwT"], b["pwC"], b["cls"], hout["wC"], hout["wR"],
                              hout["wT"], hout["base"], None, prec)
         tg3.check(tg3.lib().tg3_resample(nP, nR, tg3.ptr(hout["wR"]), tg3.ptr(b["pwR"]),
                                          tg3.ptr(b["perm_r"]), tg3.ptr(b["u0_r"]),
@@ -345,9 +373,13 @@ def run_tg3(args, rank, world, local_rank):
         "dtype": "fp32" if prec == tg3.SCORE_FP32 else "bf16x3 cross term, fp32 elsewhere",
         "data": "synthetic (seeded Gaussian-blob map and particles, generated on the GPU)",
         "config": {"workload": f"local particle-filter phase, box {W['box']}, K={K}, "
-                               f"{nR} rotations x {nT} translations per particle",
+                               f"{nR} rotations x {nT} translations per particle"
+                               + (f", {W['n_classes']} classes sharing "
+                                  f"{round(100 * W['shared'])} % of their blobs, particles "
+                                  "split evenly" if W["n_classes"] > 1 else ""),
                    "box": W["box"], "pf": W["pf"], "K": K, "nR": nR, "nT": nT,
-                   "particles_per_step": nP, "precision": args.precision,
+                   "classes": W["n_classes"], "particles_per_step": nP,
+                   "precision": args.precision,
                    "l2": "inputs larger than L2: the projection bank alone is "
                          f"{nP * nR * ctx_kp(K) * 4 / 1e9:.1f} GB per step"},
         "clocks": clocks,
@@ -366,6 +398,7 @@ def run_tg3(args, rank, world, local_rank):
                       "achieved_gbs": round(ins_bytes / (ins_ms * 1e-3) / 1e9, 1),
                       "peak_gbs": hbm, "frac": round(ins_bytes / (ins_ms * 1e-3) / 1e9 / hbm, 4)},
         "hypotheses_per_s": round(value * nR * nT, 1),
+        "pose": pose,
     }
     if plain is not None:
         ms_p, stages_p, clocks_p = plain
@@ -641,7 +674,8 @@ def main():
                     help="rotations per particle in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
-    ap.add_argument("--workload", default="local256", choices=["local256", "global64"])
+    ap.add_argument("--workload", default="local256",
+                    choices=["local256", "local256c3", "global64"])
     ap.add_argument("--global-particles", type=int, default=2000)
     args = ap.parse_args()
     rank, world, local = init_dist()

@@ -206,6 +206,25 @@ def blob_map(rng: np.random.Generator, n_blobs: int, sigma_a: tuple,
                    centre=d * rad[:, None])
 
 
+def class_maps(rng: np.random.Generator, n_classes: int, shared: float, n_blobs: int,
+               sigma_a: tuple, pixel_size: float, radius_px: float) -> list:
+    """n_classes blob maps sharing a fraction `shared` of their n_blobs
+    blobs: one base map whose remaining blobs (one fixed index set) are
+    re-drawn for every class.  One class returns the base map itself."""
+    base = blob_map(rng, n_blobs, sigma_a, pixel_size, radius_px)
+    if n_classes == 1:
+        return [base]
+    n_new = int(round(n_blobs * (1.0 - shared)))
+    idx = rng.choice(n_blobs, n_new, replace=False)
+    maps = []
+    for _ in range(n_classes):
+        fresh = blob_map(rng, n_new, sigma_a, pixel_size, radius_px)
+        amp, sig, cen = base.amp.copy(), base.sigma.copy(), base.centre.copy()
+        amp[idx], sig[idx], cen[idx] = fresh.amp, fresh.sigma, fresh.centre
+        maps.append(BlobMap(amp=amp, sigma=sig, centre=cen))
+    return maps
+
+
 def blob_ft(bm: BlobMap, f: torch.Tensor) -> torch.Tensor:
     """Analytic Fourier transform of the blob map at frequencies f (..., 3)
     in cycles per pixel."""
