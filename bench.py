@@ -193,6 +193,8 @@ def run_tg3(args, rank, world, local_rank):
                                          box=args.box, W0=W0)
     nR, nT, K = W["nR"], W["nT"], st.K
     ctx = tg3.Context(local_rank)
+    if args.fused:
+        ctx.set_option(tg3.OPT_FUSED, 1)
     for c, v in enumerate(vols):
         ctx.set_volume(c, v, W["pf"])
     ctx.set_pixels(st.iCol, st.iRow, W["box"])
@@ -208,7 +210,6 @@ def run_tg3(args, rank, world, local_rank):
                w_t=torch.empty((nP, nT), dtype=torch.float64, device=dev),
                top=torch.empty(nP, dtype=torch.int32, device=dev))
     stream = torch.cuda.ExternalStream(ctx.stream)
-    launches_per_step = 7   # project, shift, x0, cross term, weights, 2 x resample
 
     def step(i, prec):
         b = dbat[i % len(dbat)]
@@ -361,8 +362,32 @@ def run_tg3(args, rank, world, local_rank):
                                 "because L2 serves the volume blocks a pixel band reuses",
                 "algorithmic_bytes_per_launch": proj_bytes}
 
-    dominant = max(("project", "cross"), key=lambda k: per_launch(stages, k))
-    roof = proj_roof(stages) if dominant == "project" else cross_roof(stages, prec)
+    def fused_roof(st_):
+        """k_fused_bf16x3: the gather bound (64 B of corners per sample, no
+        slice written), with the tensor rate of the same launch beside it."""
+        t = per_launch(st_, "fused") * 1e-3
+        fb = 64.0 * nR * K * nP
+        ach = fb / t / 1e9
+        return {"kernel": "k_fused_bf16x3 (gather + tcgen05)", "bound": "hbm",
+                "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(ach / hbm, 4),
+                "peak_source": f"hbm_gbs, {kind} (MEASURED_PEAKS.json)",
+                "traffic": traffic("fused", W["box"], nP),
+                "algorithmic_bytes_per_launch": fb,
+                "tensor": {"achieved_tflops": round(flop / t / 1e12, 2), "peak": round(bf16, 1),
+                           "frac": round(flop / t / 1e12 / bf16, 4),
+                           "algorithmic_flop_per_launch": flop,
+                           "executed_bf16_flop_per_launch": 3 * flop}}
+
+    fused = stages.get("fused", (0.0, 0))[1] > 0
+    if fused:
+        roof = fused_roof(stages)
+    else:
+        dominant = max(("project", "cross"), key=lambda k: per_launch(stages, k))
+        roof = proj_roof(stages) if dominant == "project" else cross_roof(stages, prec)
+    # kernels of one step: shift, x0, rotation matrices, 2 x resample, weights, plus
+    # fused: descriptors + the fused kernel; else: projection, norm sum, cross term
+    launches_per_step = 8 if fused else 9
     ins_ms = ins_stage[0] / max(ins_stage[1], 1)
     ins_bytes = 705.5 * K * nP             # 16 B in + 28.7 voxel updates x 24 B per pixel
     value = nP * args.steps * world / (ms * 1e-3)
@@ -388,8 +413,8 @@ def run_tg3(args, rank, world, local_rank):
                 "wall_s": round(e2e_s, 3)},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": roof,
-        "roofline_cross_term": cross_roof(stages, prec),
-        "roofline_projection": proj_roof(stages),
+        "roofline_cross_term": None if fused else cross_roof(stages, prec),
+        "roofline_projection": None if fused else proj_roof(stages),
         "stages": {k: {"ms_per_launch": round(v[0] / max(v[1], 1), 4), "launches": v[1]}
                    for k, v in stages.items() if v[1]},
         "insertion": {"kernel": "k_insert (MKB, a = 1.9, alpha = 15)", "particles": nP,
@@ -673,6 +698,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=40,
                     help="rotations per particle in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fused", action="store_true",
+                    help="split-bf16 path through the fused projection + tcgen05 kernel")
     ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
     ap.add_argument("--workload", default="local256",
                     choices=["local256", "local256c3", "global64"])

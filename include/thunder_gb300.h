@@ -209,9 +209,19 @@ int tg3_local_phase(tg3_ctx* ctx, int nP, int nR, int nT, const float* dat,
 enum {
     TG3_STAGE_PROJECT = 0, TG3_STAGE_SHIFT = 1, TG3_STAGE_CROSS = 2,
     TG3_STAGE_WEIGHTS = 3, TG3_STAGE_RESAMPLE = 4, TG3_STAGE_INSERT = 5,
-    TG3_STAGE_COUNT = 6
+    TG3_STAGE_FUSED = 6,   /* projection + split-bf16 cross term in one kernel */
+    TG3_STAGE_COUNT = 7
 };
 int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
+
+/* Context options (no counterpart in the reference).
+ * TG3_OPT_FUSED (default 0): 1 makes the split-bf16 local phase gather every
+ *   slice straight into the tensor-core operand of one persistent kernel
+ *   (projection + cross term fused, no slice bank in HBM); 0 keeps the
+ *   two-kernel form (k_project writing the slice bank, then the GEMM), which
+ *   is the faster of the two on GB300. */
+enum { TG3_OPT_FUSED = 0 };
+int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);
 
 /* Global scan of nImg images over one shared set of nR rotations and nT

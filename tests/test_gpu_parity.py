@@ -423,3 +423,31 @@ def test_global_scan(small, ctx, precision):
         a = g["wT"][l] / g["wT"][l].sum()
         b = r["wT"][l * nT:(l + 1) * nT]
         np.testing.assert_allclose(a, b / b.sum(), atol=2e-3)
+
+
+@pytest.mark.parametrize("shape", [(4, 96, 21), (3, 300, 100), (2, 129, 7)])
+def test_fused_matches_two_kernel_form(small, ctx, shape):
+    """The fused projection + split-bf16 kernel (slices gathered straight into
+    the tensor-core operand) against the two-kernel form (slice bank in HBM,
+    then the GEMM) on the same inputs: likelihoods within 1e-5 relative."""
+    nP, nR, nT = shape
+    d = _local_inputs(small, nP, nR, nT, 5)
+    res = {}
+    for fused in (1, 0):
+        ctx.set_option(tg3.OPT_FUSED, fused)
+        o = dict(wC=torch.empty(nP, dtype=torch.float64, device=DEV),
+                 wR=torch.empty((nP, nR), dtype=torch.float64, device=DEV),
+                 wT=torch.empty((nP, nT), dtype=torch.float64, device=DEV),
+                 base=torch.empty(nP, dtype=torch.float64, device=DEV),
+                 dvp=torch.empty((nP, nR, nT), dtype=torch.float32, device=DEV))
+        ctx.local_phase(nP, nR, nT, dev(d["dat"]), dev(d["ctf"]), dev(d["sig"]), dev(d["qs"]),
+                        dev(d["ts"]), dev(d["pwR"]), dev(d["pwT"]), dev(d["pwC"]), None,
+                        o["wC"], o["wR"], o["wT"], o["base"], o["dvp"], tg3.SCORE_BF16X3)
+        ctx.sync()
+        res[fused] = {k: v.cpu().numpy() for k, v in o.items()}
+    ctx.set_option(tg3.OPT_FUSED, 0)
+    f, u = res[1], res[0]
+    rel = np.abs(f["dvp"] - u["dvp"]) / np.abs(u["dvp"])
+    assert rel.max() < 1e-5, rel.max()
+    assert np.all(np.argmax(f["dvp"].reshape(nP, -1), 1) == np.argmax(u["dvp"].reshape(nP, -1), 1))
+    assert np.allclose(f["base"], u["base"], rtol=1e-6)

@@ -427,8 +427,10 @@ static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
             return fail(TG3_ERR_ARG, "all class volumes must share one edge and pf");
     if ((st = check_geometry(c, v0.vdim, v0.pf))) return st;
     if ((st = check_weights_shape(nR, nT))) return st;
-    float* P = (float*)ws_get(c, WS_P, sizeof(float) * (size_t)nP * nR * Kp, &st);
-    if (!P) return st;
+    const bool fusedPath = precision == TG3_SCORE_BF16X3 && c->fused;
+    float* P = fusedPath ? nullptr
+                         : (float*)ws_get(c, WS_P, sizeof(float) * (size_t)nP * nR * Kp, &st);
+    if (!fusedPath && !P) return st;
     float* A = (float*)ws_get(c, WS_A, sizeof(float) * (size_t)nP * nT * Kp, &st);
     if (!A) return st;
     float* D = (float*)ws_get(c, WS_D, sizeof(float) * (size_t)nP * nR * nT, &st);
@@ -450,6 +452,40 @@ static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
     // split-bf16: the same buffers hold a hi plane followed by a lo plane
     const long long splitP = split ? (long long)nP * nR * Kp : 0;
     const long long splitA = split ? (long long)nP * nT * Kp : 0;
+    if (split && c->fused) {
+        // projection + cross term in one kernel; the slices stay on chip
+        const size_t partBytes = round_up(sizeof(FusedParticle) * (size_t)nP, 256);
+        const size_t offBytes = round_up(sizeof(int) * ((size_t)nP + 1), 256);
+        char* fw = (char*)ws_get(c, WS_FUSED, partBytes + offBytes + 256, &st);
+        if (!fw) return st;
+        FusedParticle* part = reinterpret_cast<FusedParticle*>(fw);
+        int* itemOff = reinterpret_cast<int*>(fw + partBytes);
+        int* counter = reinterpret_cast<int*>(fw + partBytes + offBytes);
+        {
+            StageTimer tm(c, TG3_STAGE_SHIFT);
+            TG3_CUDA(launch_shift_bank(reinterpret_cast<const float2*>(dat), ctf, sigRcp, trans,
+                                       nullptr, nP, nT, c->px.idim, c->px.iCol, c->px.iRow, K, A,
+                                       Kp, splitA, s));
+            TG3_CUDA(launch_x0(reinterpret_cast<const float2*>(dat), sigRcp, nP, K, x0, s));
+            TG3_CUDA(launch_rot_f32(quat, nullptr, nP * nR, pscr, s));
+            TG3_CUDA(launch_fused_uniform_setup(nP, nR, nT, K, cls, part, itemOff, s));
+        }
+        {
+            StageTimer tm(c, TG3_STAGE_FUSED);
+            FusedPixels pix[kMaxClasses];
+            for (int k = 0; k < kMaxClasses; k++) pix[k] = {c->px.iCol, c->px.iRow, K, Kp};
+            TG3_CUDA(launch_fused_bf16x3(c->d_volTable, v0.vdim, v0.pf, pscr, part, itemOff, nP,
+                                         nP * fused_items(nR), pix, sigRcp, ctf, A,
+                                         (long long)nP * nT, Kp, nT, D, -2.0f, c->d_flag,
+                                         counter, s));
+        }
+        {
+            StageTimer tm(c, TG3_STAGE_WEIGHTS);
+            TG3_CUDA(launch_weights(D, (long long)nR * nT, nT, nR, nT, 1, nP, nullptr, 0, x0, pwR,
+                                    nR, pwT, nT, pwC, wC, wR, wT, baseL, dvp, s));
+        }
+        return TG3_OK;
+    }
     {
         StageTimer tm(c, TG3_STAGE_PROJECT);
         TG3_CUDA(launch_project(c->d_volTable, cls, nullptr, v0.vdim, v0.pf, quat, nullptr,
@@ -1066,6 +1102,15 @@ extern "C" int tg3_local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* 
 }
 
 // ============================================================ stage timing
+extern "C" int tg3_ctx_set_option(tg3_ctx* c, int option, int value)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (option != TG3_OPT_FUSED) return fail(TG3_ERR_ARG, "unknown option");
+    c->fused = value != 0;
+    return TG3_OK;
+}
+
 extern "C" int tg3_ctx_set_timing(tg3_ctx* c, int enable)
 {
     int st = check_ctx(c);

@@ -40,6 +40,30 @@ int cuda_fail(cudaError_t e, const char* what);
 
 inline size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 
+// ------------------------------------------------- projection volume layout --
+// The corner blocks of a volume of edge vdim sit in cubes of 32^3 voxels
+// (brick_index in tg3_kernels.cu); cube counts along x (vdim / 2 + 1 stored
+// columns) and along y and z.
+__host__ __device__ __forceinline__ int cubes_x(int vdim) { return (vdim / 2 + 1 + 31) / 32; }
+__host__ __device__ __forceinline__ int cubes_yz(int vdim) { return (vdim + 31) / 32; }
+
+// Per-axis terms of a block's index: block(x, y, z) = tx[x] + ty[y + vdim/2]
+// + tz[z + vdim/2] for x in [0, vdim/2], y, z in [-vdim/2, vdim/2), the y and
+// z tables absorbing the wrap of negative rows.  tx has vdim/2 + 1 entries,
+// ty and tz vdim each; filled by the threads of a CTA (x-stride blockDim.x).
+__device__ __forceinline__ void fill_brick_tables(int vdim, int* tx, int* ty, int* tz)
+{
+    const int nx = vdim / 2 + 1, half = vdim / 2;
+    const int nxc = cubes_x(vdim), nyc = cubes_yz(vdim);
+    for (int j = threadIdx.x; j < nx; j += blockDim.x)
+        tx[j] = (j >> 5) * 32768 + ((j >> 3) & 3) * 512 + (j & 7);
+    for (int j = threadIdx.x; j < vdim; j += blockDim.x) {
+        const int w = j - half < 0 ? j + half : j - half;
+        ty[j] = (w >> 5) * nxc * 32768 + ((w >> 3) & 3) * 2048 + (w & 7) * 8;
+        tz[j] = (w >> 5) * nyc * nxc * 32768 + ((w >> 3) & 3) * 8192 + (w & 7) * 64;
+    }
+}
+
 // ------------------------------------------------------------- workspace --
 // Grow-only named device buffers of a context.
 enum WsSlot {
@@ -48,6 +72,7 @@ enum WsSlot {
     WS_D,            // hypothesis-dependent log-likelihood part [nP][nR][nT]
     WS_NRM,          // sum sigRcp ctf^2 |P|^2 per projected row
     WS_PROJ,         // projection scratch: FP32 matrices and norm shares
+    WS_FUSED,        // fused launch: particle descriptors, item offsets, counter
     WS_X0,           // sum sigRcp |X|^2 per particle (double)
     WS_PAIRS_TMP,
     WS_H2D,          // staging of host inputs
@@ -99,6 +124,8 @@ struct tg3_ctx {
     tg3::InsertAcc ins;
     tg3::Buffer ws[tg3::WS_COUNT];
     int* d_flag = nullptr;           // device error word
+    // tg3_ctx_set_option
+    bool fused = false;
     // per-stage event timing (tg3_ctx_set_timing)
     bool timing = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[TG3_STAGE_COUNT];
@@ -203,6 +230,42 @@ cudaError_t launch_merge_class(int nImg, int nK, int kIdx, int nR, int nT,
                                cudaStream_t st);
 
 // Split-bf16 tensor-core cross term (tcgen05), when available.
+// ------------------------------------------- fused projection + scoring --
+// One particle of a fused launch: its class, hypothesis counts, first row of
+// its rotation matrices and of its shifted-data planes, the offset of its
+// sigRcp / ctf values, and the first element of its [nR][nT] likelihoods.
+struct FusedParticle {
+    int cls;
+    int nR, nT;
+    int rowOff;
+    int transRow;
+    int sgOff;
+    long long dOff;
+};
+// A class's pixel set (K pixels; Kp padded floats per row, a multiple of 64).
+struct FusedPixels {
+    const int* iCol;
+    const int* iRow;
+    int K, Kp;
+};
+int fused_items(int nR);                              // work items of one particle
+size_t fused_smem_bytes(int vdim, int ntile, int* stages);
+cudaError_t launch_fused_uniform_setup(int nP, int nR, int nT, int K, const int* cls,
+                                       FusedParticle* part, int* itemOff, cudaStream_t st);
+// D as launch_gemm_bf16x3 would write it from k_project's slices (alpha times
+// the split-bf16 cross term plus the row norm), for every particle of `part`;
+// B: hi plane of the shifted data (rowsB x KpB bf16), lo plane after it;
+// pix: host array of kMaxClasses pixel sets; counter: one device int.
+cudaError_t launch_fused_bf16x3(float4* const* volTable, int vdim, int pf, const float* mf,
+                                const FusedParticle* part, const int* itemOff, int nP,
+                                int nItems, const FusedPixels* pix, const float* sigRcp,
+                                const float* ctf, const void* B, long long rowsB, int KpB,
+                                int maxNT, float* D, float alpha, int* flag, int* counter,
+                                cudaStream_t st);
+// FP32 rotation matrices [rows][9] from quaternions or FP64 matrices.
+cudaError_t launch_rot_f32(const double* quat, const double* mat, int rows, float* mf,
+                           cudaStream_t st);
+
 bool bf16x3_available();
 cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda,
                                   const float* B, long long sB, int ldb,

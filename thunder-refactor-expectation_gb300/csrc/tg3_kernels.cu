@@ -181,9 +181,6 @@ __device__ __forceinline__ size_t brick_index(int x, int y, int z, int nxc, int 
     return (cube * 64 + brick) * 512 + v;
 }
 
-// Cube counts along x (nx = vdim / 2 + 1 stored columns) and along y and z.
-__host__ __device__ __forceinline__ int cubes_x(int vdim) { return (vdim / 2 + 1 + 31) / 32; }
-__host__ __device__ __forceinline__ int cubes_yz(int vdim) { return (vdim + 31) / 32; }
 
 // Corner-block content: the 64-byte element of voxel (z, y, x) holds, for
 // slab z then slab z + 1, V[.][y][x], V[.][y][x+1], V[.][y+1][x],
@@ -257,20 +254,11 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
     // brick_index split into per-axis terms: tx[x] + ty[y + vdim/2] +
     // tz[z + vdim/2], the y and z tables absorbing the wrap of negative rows
     extern __shared__ int tab[];
-    const int nx = vdim / 2 + 1, half = vdim / 2;
+    const int half = vdim / 2;
     int* tx = tab;
-    int* ty = tab + nx;
+    int* ty = tab + vdim / 2 + 1;
     int* tz = ty + vdim;
-    {
-        const int nxc = cubes_x(vdim), nyc = cubes_yz(vdim);
-        for (int j = threadIdx.x; j < nx; j += blockDim.x)
-            tx[j] = (j >> 5) * 32768 + ((j >> 3) & 3) * 512 + (j & 7);
-        for (int j = threadIdx.x; j < vdim; j += blockDim.x) {
-            const int w = j - half < 0 ? j + half : j - half;
-            ty[j] = (w >> 5) * nxc * 32768 + ((w >> 3) & 3) * 2048 + (w & 7) * 8;
-            tz[j] = (w >> 5) * nyc * nxc * 32768 + ((w >> 3) & 3) * 8192 + (w & 7) * 64;
-        }
-    }
+    fill_brick_tables(vdim, tx, ty, tz);
     if (threadIdx.x < 9 * nRot) m[threadIdx.x / 9][threadIdx.x % 9] = mf[9 * row0 + threadIdx.x];
     __syncthreads();
     const int nOut = ldo / 2;
@@ -1082,6 +1070,14 @@ cudaError_t launch_volume_blocks(const float2* vol, int vdim, float4* blocks, cu
 {
     size_t n = (size_t)vdim * vdim * (vdim / 2 + 1);
     k_volume_blocks<<<grid_for(n, 256), 256, 0, st>>>(vol, vdim, blocks);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rot_f32(const double* quat, const double* mat, int rows, float* mf,
+                           cudaStream_t st)
+{
+    if (rows <= 0) return cudaSuccess;
+    k_rot_f32<<<grid_for((size_t)rows, 256), 256, 0, st>>>(quat, mat, rows, mf);
     return cudaGetLastError();
 }
 

@@ -19,126 +19,17 @@
 #include <stdint.h>
 
 #include "tg3_internal.cuh"
+#include "tg3_tcgen05.cuh"
 
 namespace tg3 {
 
 namespace {
 
+using namespace tc;
+
 constexpr int TC_M = 128;          // rows of A per CTA (UMMA M)
 constexpr int TC_BK = 64;          // bf16 elements per K block (one 128-byte row)
 constexpr int TC_THREADS = 128;
-constexpr long long kWaitBudget = 4000000000LL;   // ~2 s of SM clocks
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p)
-{
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n"
-        " .reg .pred p;\n"
-        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n"
-        "}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait; false when the budget ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long budget)
-{
-    if (mbar_try_wait(bar, parity)) return true;
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > budget) return false;
-    return true;
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
-                                            int c0, int c1)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
-        : "memory");
-}
-
-// UMMA shared-memory descriptor: K-major operand, 128-byte swizzle, rows of
-// 128 bytes, 8-row groups 1024 bytes apart (SBO); LBO unused for this layout.
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr)
-{
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)1 << 16;                 // LBO (16 B; ignored for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;       // SBO
-    d |= (uint64_t)1 << 46;                 // descriptor version for tcgen05
-    d |= (uint64_t)2 << 61;                 // 128-byte swizzle
-    return d;
-}
-
-// Instruction descriptor, kind::f16: FP32 accumulate, bf16 A and B, both
-// K-major, shape M x N.
-__host__ __device__ constexpr uint32_t umma_idesc(int M, int N)
-{
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
-           ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                          uint32_t idesc, uint32_t accumulate)
-{
-    asm volatile(
-        "{\n"
-        " .reg .pred p;\n"
-        " setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
-        "}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
-__device__ __forceinline__ void umma_commit(uint64_t* bar)
-{
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            smem_u32(bar))
-        : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
-{
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32"
-        " {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
-
 struct TcParams {
     int M, N, Kd;            // rows of A per item, columns (rows of B) per item, K
     int aRowsPerItem;        // A row offset between items (0: A shared by all items)
@@ -320,46 +211,9 @@ k_gemm_bf16x3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ 
     }
 }
 
-// ------------------------------------------------------- host: tensor maps
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn()
-{
-    static EncodeTiledFn fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
-        void* f = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000,
-                                             cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiledFn>(f);
-    }
-    return fn;
-}
-
-// 2-D bf16 plane [rows][Kd], box [64 x boxRows], 128-byte swizzle.
-bool make_map(CUtensorMap* m, const void* base, long long rows, int Kd, int boxRows)
-{
-    EncodeTiledFn fn = encode_fn();
-    if (!fn) return false;
-    cuuint64_t dims[2] = {(cuuint64_t)Kd, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)Kd * 2};
-    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)boxRows};
-    cuuint32_t es[2] = {1, 1};
-    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
-                    box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS;
-}
-
 }  // namespace
 
-bool bf16x3_available() { return encode_fn() != nullptr; }
+bool bf16x3_available() { return tc::encode_fn() != nullptr; }
 
 size_t bf16x3_scratch_bytes(int, int, int, int) { return 256; }
 
@@ -408,8 +262,8 @@ cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, lo
     p.alpha = alpha;
     p.flag = flag;
     CUtensorMap mAh, mAl, mBh, mBl;
-    if (!make_map(&mAh, Ah, rowsA, Kd, TC_M) || !make_map(&mAl, Al, rowsA, Kd, TC_M) ||
-        !make_map(&mBh, Bh, rowsB, Kd, p.ntile) || !make_map(&mBl, Bl, rowsB, Kd, p.ntile))
+    if (!tc::make_map(&mAh, Ah, rowsA, Kd, TC_M) || !tc::make_map(&mAl, Al, rowsA, Kd, TC_M) ||
+        !tc::make_map(&mBh, Bh, rowsB, Kd, p.ntile) || !tc::make_map(&mBl, Bl, rowsB, Kd, p.ntile))
         return cudaErrorInvalidValue;
     const size_t smem = 1024 + (size_t)p.stages * stageBytes + 256;
     cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,

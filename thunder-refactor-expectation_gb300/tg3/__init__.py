@@ -29,9 +29,11 @@ EXPORTS = [
     "tg3_local_phase_d", "tg3_resample_d", "tg3_ctx_insert_begin", "tg3_insert_d",
     "tg3_ctx_insert_read_d", "tg3_rotmat_d", "tg3_translate_d", "tg3_ctf_d",
     "tg3_project_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
+    "tg3_ctx_set_option",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
-STAGES = ("project", "shift", "cross", "weights", "resample", "insert")
+STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
+OPT_FUSED = 0
 
 
 class TG3Error(RuntimeError):
@@ -87,6 +89,7 @@ def lib():
             "tg3_project_d": ([_P, _I, _P, _I, _P], _I),
             "tg3_local_phase": ([_P, _I, _I, _I] + [_P] * 14 + [_I], _I),
             "tg3_ctx_set_timing": ([_P, _I], _I),
+            "tg3_ctx_set_option": ([_P, _I, _I], _I),
             "tg3_ctx_stage_times": ([_P, _P, _P, _I], _I),
             "tg3_noalloc_scratch_bytes": ([], ctypes.c_size_t),
             "tg3_global_scan_d": ([_P, _I, _I, _I, _I] + [_P] * 12 + [_I], _I),
@@ -186,6 +189,9 @@ class Context:
         check(lib().tg3_local_phase(self.h, nP, nR, nT, ptr(dat), ptr(ctf), ptr(sig), ptr(quat),
                                     ptr(trans), ptr(pwR), ptr(pwT), ptr(pwC), ptr(cls), ptr(wC),
                                     ptr(wR), ptr(wT), ptr(base), ptr(dvp), precision))
+
+    def set_option(self, option: int, value: int):
+        check(lib().tg3_ctx_set_option(self.h, option, int(value)))
 
     def set_timing(self, enable: bool):
         check(lib().tg3_ctx_set_timing(self.h, int(enable)))
