@@ -178,6 +178,16 @@ int tg3_ctx_set_volume(tg3_ctx* ctx, int cls, const float* volume, int vdim,
 int tg3_ctx_set_pixels(tg3_ctx* ctx, const int* iCol, const int* iRow, int K,
                        int idim);
 
+/* Several pixel sets in one context (no counterpart in the reference): each
+ * class of a refinement may have its own cutoff, hence its own pixel list.
+ * tg3_ctx_set_pixels_slot uploads a list into slot 0..15;
+ * tg3_ctx_use_pixels(slot) makes it the context's active set for the calls
+ * that follow (-1: the set of tg3_ctx_set_pixels).  Device inputs of those
+ * calls hold K values per particle for the active set. */
+int tg3_ctx_set_pixels_slot(tg3_ctx* ctx, int slot, const int* iCol, const int* iRow, int K,
+                            int idim);
+int tg3_ctx_use_pixels(tg3_ctx* ctx, int slot);
+
 /* Batched local phase of nP particles (all device pointers, layouts
  * particle-major): dat [nP][K] complex, ctf, sigRcp [nP][K]; quat
  * [nP][nR][4], trans [nP][nT][2] (double); priors pwR [nP][nR],
@@ -223,6 +233,36 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
 enum { TG3_OPT_FUSED = 0 };
 int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);
+
+/* Uneven batches (no single counterpart in the reference: the batching of
+ * Optimiser::expectationG's particle loop, src/Optimiser.cpp:2359-2566, for
+ * particles whose rotation / translation sets differ in size after
+ * Particle::resample, src/Particle.cpp:1275-1463).  One plan covers nP
+ * particles of any classes (each class needs a volume and a pixel slot of the
+ * same index).  Host arrays cls, nR, nT give every particle's class and set
+ * sizes; every other pointer is a device array packed particle after
+ * particle: dat (complex), ctf, sigRcp with the K of the particle's class;
+ * quat [4], pwR, permR, wR, srcR, wOutR with its nR entries; trans [2], pwT,
+ * permT, wT, srcT, wOutT with its nT entries; pwC, u0R, peakR, u0T, peakT,
+ * wC, baseL, topR, topT with one entry.  A run computes for every particle
+ * what tg3_local_phase_d followed by tg3_resample_d of its rotations and of
+ * its translations (nOut = its own set size) computes for it alone.
+ * budget: bytes of projection bank per wave, 0 to autotune; use_graph: the
+ * run replays one captured CUDA graph.  Runs are asynchronous on the
+ * context stream (tg3_ctx_sync reports device-side errors). */
+typedef struct tg3_plan tg3_plan;
+int tg3_ragged_plan_create(tg3_ctx* ctx, int nP, const int* cls, const int* nR, const int* nT,
+                           const float* dat, const float* ctf, const float* sigRcp,
+                           const double* quat, const double* trans, const double* pwR,
+                           const double* pwT, const double* pwC, const int* permR,
+                           const double* u0R, const double* peakR, const int* permT,
+                           const double* u0T, const double* peakT, double* wC, double* baseL,
+                           double* wR, double* wT, int* srcR, double* wOutR, int* srcT,
+                           double* wOutT, int* topR, int* topT, int precision, size_t budget,
+                           int use_graph, tg3_plan** plan);
+int tg3_ragged_plan_run(tg3_plan* plan);
+int tg3_ragged_plan_info(const tg3_plan* plan, int* waves, size_t* budget);
+int tg3_ragged_plan_destroy(tg3_plan* plan);
 
 /* Global scan of nImg images over one shared set of nR rotations and nT
  * translations, for the context's class-`cls` volume: the scan of

@@ -136,7 +136,7 @@ static void mkb_table(double a, double alpha, double b, int n, std::vector<float
 constexpr double kMkbA = 1.9, kMkbAlpha = 15.0;
 constexpr int kMkbN = 100000;
 
-static int check_ctx(tg3_ctx* c)
+int check_ctx(tg3_ctx* c)
 {
     if (!c) return fail(TG3_ERR_ARG, "null context");
     cudaError_t e = cudaSetDevice(c->device);
@@ -305,8 +305,12 @@ extern "C" int tg3_ctx_destroy(tg3_ctx* c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto& v : c->vol) cudaFree(v.blocks);
     for (auto& b : c->ws) cudaFree(b.ptr);
-    cudaFree(c->px.iCol);
-    cudaFree(c->px.iRow);
+    cudaFree(c->pxMain.iCol);
+    cudaFree(c->pxMain.iRow);
+    for (auto& q : c->pxSlot) {
+        cudaFree(q.iCol);
+        cudaFree(q.iRow);
+    }
     cudaFree(c->ins.acc);
     cudaFree(c->ins.tab);
     cudaFree(c->d_flag);
@@ -377,11 +381,9 @@ extern "C" int tg3_ctx_set_volume(tg3_ctx* c, int cls, const float* volume, int 
     return TG3_OK;
 }
 
-extern "C" int tg3_ctx_set_pixels(tg3_ctx* c, const int* iCol, const int* iRow, int K,
-                                  int idim)
+// Upload a pixel list into an owned set (device buffers grown as needed).
+static int upload_pixels(tg3_ctx* c, Pixels& px, const int* iCol, const int* iRow, int K, int idim)
 {
-    int st = check_ctx(c);
-    if (st) return st;
     if (!iCol || !iRow || K <= 0 || idim <= 0) return fail(TG3_ERR_ARG, "bad pixel list");
     double mr = 0;
     for (int p = 0; p < K; p++) {
@@ -389,21 +391,52 @@ extern "C" int tg3_ctx_set_pixels(tg3_ctx* c, const int* iCol, const int* iRow, 
             return fail(TG3_ERR_ARG, "pixel outside the half plane of the image");
         mr = std::max(mr, std::sqrt((double)iCol[p] * iCol[p] + (double)iRow[p] * iRow[p]));
     }
-    if (c->px.K != K) {
+    if (px.K != K) {
         TG3_CUDA(cudaStreamSynchronize(c->stream));
-        cudaFree(c->px.iCol);
-        cudaFree(c->px.iRow);
-        c->px.iCol = c->px.iRow = nullptr;
-        TG3_CUDA(cudaMalloc(&c->px.iCol, sizeof(int) * K));
-        TG3_CUDA(cudaMalloc(&c->px.iRow, sizeof(int) * K));
+        cudaFree(px.iCol);
+        cudaFree(px.iRow);
+        px.iCol = px.iRow = nullptr;
+        px.K = 0;
+        TG3_CUDA(cudaMalloc(&px.iCol, sizeof(int) * K));
+        TG3_CUDA(cudaMalloc(&px.iRow, sizeof(int) * K));
     }
-    TG3_CUDA(cudaMemcpyAsync(c->px.iCol, iCol, sizeof(int) * K, cudaMemcpyHostToDevice, c->stream));
-    TG3_CUDA(cudaMemcpyAsync(c->px.iRow, iRow, sizeof(int) * K, cudaMemcpyHostToDevice, c->stream));
+    TG3_CUDA(cudaMemcpyAsync(px.iCol, iCol, sizeof(int) * K, cudaMemcpyHostToDevice, c->stream));
+    TG3_CUDA(cudaMemcpyAsync(px.iRow, iRow, sizeof(int) * K, cudaMemcpyHostToDevice, c->stream));
     TG3_CUDA(cudaStreamSynchronize(c->stream));
-    c->px.K = K;
-    c->px.Kp = (int)round_up(2 * (size_t)K, 64);
-    c->px.idim = idim;
-    c->px.maxRadius = mr;
+    px.K = K;
+    px.Kp = (int)round_up(2 * (size_t)K, 64);
+    px.idim = idim;
+    px.maxRadius = mr;
+    return TG3_OK;
+}
+
+extern "C" int tg3_ctx_set_pixels(tg3_ctx* c, const int* iCol, const int* iRow, int K,
+                                  int idim)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if ((st = upload_pixels(c, c->pxMain, iCol, iRow, K, idim))) return st;
+    c->px = c->pxMain;
+    return TG3_OK;
+}
+
+extern "C" int tg3_ctx_set_pixels_slot(tg3_ctx* c, int slot, const int* iCol, const int* iRow,
+                                       int K, int idim)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (slot < 0 || slot >= kMaxClasses) return fail(TG3_ERR_ARG, "pixel slot out of range");
+    return upload_pixels(c, c->pxSlot[slot], iCol, iRow, K, idim);
+}
+
+extern "C" int tg3_ctx_use_pixels(tg3_ctx* c, int slot)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (slot < -1 || slot >= kMaxClasses) return fail(TG3_ERR_ARG, "pixel slot out of range");
+    const Pixels& src = slot < 0 ? c->pxMain : c->pxSlot[slot];
+    if (!src.iCol) return fail(TG3_ERR_STATE, "pixel set not uploaded");
+    c->px = src;
     return TG3_OK;
 }
 

@@ -120,7 +120,9 @@ struct tg3_ctx {
     cudaStream_t stream = nullptr;
     tg3::Volume vol[tg3::kMaxClasses];
     float4** d_volTable = nullptr;   // device copy of the class -> blocks table
-    tg3::Pixels px;
+    tg3::Pixels px;                          // the active pixel set (a view)
+    tg3::Pixels pxMain;                      // owned: tg3_ctx_set_pixels
+    tg3::Pixels pxSlot[tg3::kMaxClasses];    // owned: tg3_ctx_set_pixels_slot
     tg3::InsertAcc ins;
     tg3::Buffer ws[tg3::WS_COUNT];
     int* d_flag = nullptr;           // device error word
@@ -211,7 +213,8 @@ cudaError_t launch_resample(int nP, int n, const double* u, const double* w,
                             const int* perm, const double* u0,
                             const double* peak, int nOut, int* src,
                             double* wOut, int* top, int* flag,
-                            cudaStream_t st);
+                            cudaStream_t st,
+                            const int* nPer = nullptr);
 // One CTA per draw; draw d uses image d / drawsPerImage.
 cudaError_t launch_insert(float4* acc, int vdim, int kernel, const float* tab,
                           int tabNz, float tabInvStep, int nDraws,
@@ -283,4 +286,9 @@ cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, lo
                                const float* nrm, long long sN, float alpha, int* flag,
                                cudaStream_t st, int cGroup = 0, long long cGroupStride = 0);
 
+}  // namespace tg3
+
+namespace tg3 {
+// Makes the context's device current; TG3_ERR_ARG for a null context.
+int check_ctx(tg3_ctx* c);
 }  // namespace tg3

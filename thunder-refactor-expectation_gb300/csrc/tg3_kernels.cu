@@ -571,6 +571,7 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
     extern __shared__ float wsm[];
     float* wTs = wsm;                // [nT]
     float* pTs = wTs + nT;           // [nT]
+    float* wTw = pTs + nT;           // [warps][nT] when TS > 0: per-warp sums, added in order
     __shared__ float redf[32];
     __shared__ double red[32];
     const int blk = blockIdx.x;
@@ -678,11 +679,19 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
 #pragma unroll
         for (int j = 0; j < (TS > 0 ? TS : 1); j++) {
             const int t = lane + 32 * j;
-            if (t < nT) atomicAdd(wTs + t, tacc[j]);
+            if (t < nT) wTw[wid * nT + t] = tacc[j];
         }
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < nT; t += blockDim.x) wT[(size_t)blk * nT + t] = (double)wTs[t] * pc;
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
+        float v = wTs[t];
+        if (TS > 0) {
+            // the warps' sums in warp order: the same bits on every run
+            v = 0.f;
+            for (int w = 0; w < nw; w++) v += wTw[w * nT + t];
+        }
+        wT[(size_t)blk * nT + t] = (double)v * pc;
+    }
     // every lane holds the same cacc per warp: count lane 0's only
     const double c = block_sum_d(lane == 0 ? (double)cacc : 0.0, red);
     if (threadIdx.x == 0) {
@@ -748,24 +757,30 @@ __global__ void k_merge_class(int nK, int kIdx, int nR, int nT,
 // the draws use a binary search, which finds the same first index with
 // cdf >= u_j as the reference's forward scan.
 __global__ void __launch_bounds__(256)
-k_resample(int n, const double* __restrict__ uIn, const double* __restrict__ wIn,
+k_resample(int ld, const double* __restrict__ uIn, const double* __restrict__ wIn,
            const int* __restrict__ perm, const double* __restrict__ u0s,
-           const double* __restrict__ peaks, int nOut, int* __restrict__ src,
-           double* __restrict__ wOut, int* __restrict__ top, int* __restrict__ flag)
+           const double* __restrict__ peaks, int ldo, const int* __restrict__ nPer,
+           int* __restrict__ src, double* __restrict__ wOut, int* __restrict__ top,
+           int* __restrict__ flag)
 {
+    // ld / ldo: pitches of the inputs / outputs of a particle; its own set has
+    // n = nPer[b] entries (all ld without nPer) and it draws nOut = n of them
+    // (ldo without nPer)
     extern __shared__ double sm[];
-    double* u = sm;                 // [n]
-    double* w = u + n;              // [n]
-    double* cdf = w + n;            // [max(n, nOut)]
-    int* idx = reinterpret_cast<int*>(cdf + (n > nOut ? n : nOut));   // [n]
+    double* u = sm;                 // [ld]
+    double* w = u + ld;             // [ld]
+    double* cdf = w + ld;           // [max(ld, ldo)]
+    int* idx = reinterpret_cast<int*>(cdf + (ld > ldo ? ld : ldo));   // [ld]
     __shared__ double sval[32];
     __shared__ int sidx[32];
     __shared__ double sh;
     __shared__ int bad;
     const int b = blockIdx.x;
-    const double* ub = uIn + (size_t)b * n;
-    const double* wb = wIn + (size_t)b * n;
-    const int* pb = perm + (size_t)b * n;
+    const int n = nPer ? nPer[b] : ld;
+    const int nOut = nPer ? n : ldo;
+    const double* ub = uIn + (size_t)b * ld;
+    const double* wb = wIn + (size_t)b * ld;
+    const int* pb = perm + (size_t)b * ld;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if (threadIdx.x == 0) bad = 0;
     // maximum of u (exact in any order)
@@ -869,7 +884,7 @@ k_resample(int n, const double* __restrict__ uIn, const double* __restrict__ wIn
     for (int i = threadIdx.x; i < n; i += blockDim.x) cdf[i] = __ddiv_rn(cdf[i], last);
     __syncthreads();
     const double u0 = u0s[b];
-    int* so = src + (size_t)b * nOut;
+    int* so = src + (size_t)b * ldo;
     for (int j = threadIdx.x; j < nOut; j += blockDim.x) {
         const double uj = __dadd_rn(u0, __ddiv_rn((double)j, (double)nOut));
         int lo = 0, hi = n - 1;       // first i with cdf[i] >= uj
@@ -879,11 +894,11 @@ k_resample(int n, const double* __restrict__ uIn, const double* __restrict__ wIn
         }
         so[j] = idx[lo];
         // new prior 1 / u of the source (PARTICLE_PRIOR_ONE)
-        wOut[(size_t)b * nOut + j] = __ddiv_rn(1.0, u[lo]);
+        wOut[(size_t)b * ldo + j] = __ddiv_rn(1.0, u[lo]);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        const double* wb2 = wOut + (size_t)b * nOut;
+        const double* wb2 = wOut + (size_t)b * ldo;
         double s = wb2[0];
         for (int j = 1; j < nOut; j++) s = __dadd_rn(s, wb2[j]);
         sh = s;
@@ -891,7 +906,7 @@ k_resample(int n, const double* __restrict__ uIn, const double* __restrict__ wIn
     __syncthreads();
     const double s2 = sh;
     for (int j = threadIdx.x; j < nOut; j += blockDim.x)
-        wOut[(size_t)b * nOut + j] = __ddiv_rn(wOut[(size_t)b * nOut + j], s2);
+        wOut[(size_t)b * ldo + j] = __ddiv_rn(wOut[(size_t)b * ldo + j], s2);
 }
 
 // ------------------------------------------------------------------------
@@ -1159,7 +1174,7 @@ cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR, int nT
                            double* wC, double* wR, double* wT, double* base, float* dvp,
                            cudaStream_t st)
 {
-    const size_t smem = sizeof(float) * 2 * (size_t)nT;
+    const size_t smem = sizeof(float) * (2 + (nT <= 256 ? WEIGHTS_THREADS / 32 : 0)) * (size_t)nT;
     if (smem > 48 * 1024) return cudaErrorInvalidValue;
 #define TG3_WEIGHTS(TS)                                                                        \
     k_weights<TS><<<nBlocks, WEIGHTS_THREADS, smem, st>>>(D, sD, ldc, nR, nT, G, nrmG, nrmRS, x0, pwR, \
@@ -1184,14 +1199,14 @@ cudaError_t launch_merge_class(int nImg, int nK, int kIdx, int nR, int nT, const
 
 cudaError_t launch_resample(int nP, int n, const double* u, const double* w, const int* perm,
                             const double* u0, const double* peak, int nOut, int* src,
-                            double* wOut, int* top, int* flag, cudaStream_t st)
+                            double* wOut, int* top, int* flag, cudaStream_t st, const int* nPer)
 {
     size_t smem = sizeof(double) * (2 * (size_t)n + (size_t)(n > nOut ? n : nOut))
                 + sizeof(int) * (size_t)n;
     cudaError_t e = cudaFuncSetAttribute(k_resample, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    k_resample<<<nP, 256, smem, st>>>(n, u, w, perm, u0, peak, nOut, src, wOut, top, flag);
+    k_resample<<<nP, 256, smem, st>>>(n, u, w, perm, u0, peak, nOut, nPer, src, wOut, top, flag);
     return cudaGetLastError();
 }
 

@@ -29,7 +29,9 @@ EXPORTS = [
     "tg3_local_phase_d", "tg3_resample_d", "tg3_ctx_insert_begin", "tg3_insert_d",
     "tg3_ctx_insert_read_d", "tg3_rotmat_d", "tg3_translate_d", "tg3_ctf_d",
     "tg3_project_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
-    "tg3_ctx_set_option",
+    "tg3_ctx_set_option", "tg3_ctx_set_pixels_slot", "tg3_ctx_use_pixels",
+    "tg3_ragged_plan_create", "tg3_ragged_plan_run", "tg3_ragged_plan_info",
+    "tg3_ragged_plan_destroy",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
@@ -90,6 +92,12 @@ def lib():
             "tg3_local_phase": ([_P, _I, _I, _I] + [_P] * 14 + [_I], _I),
             "tg3_ctx_set_timing": ([_P, _I], _I),
             "tg3_ctx_set_option": ([_P, _I, _I], _I),
+            "tg3_ctx_set_pixels_slot": ([_P, _I, _P, _P, _I, _I], _I),
+            "tg3_ctx_use_pixels": ([_P, _I], _I),
+            "tg3_ragged_plan_create": ([_P, _I] + [_P] * 27 + [_I, ctypes.c_size_t, _I, _P], _I),
+            "tg3_ragged_plan_run": ([_P], _I),
+            "tg3_ragged_plan_info": ([_P, _P, _P], _I),
+            "tg3_ragged_plan_destroy": ([_P], _I),
             "tg3_ctx_stage_times": ([_P, _P, _P, _I], _I),
             "tg3_noalloc_scratch_bytes": ([], ctypes.c_size_t),
             "tg3_global_scan_d": ([_P, _I, _I, _I, _I] + [_P] * 12 + [_I], _I),
@@ -193,6 +201,14 @@ class Context:
     def set_option(self, option: int, value: int):
         check(lib().tg3_ctx_set_option(self.h, option, int(value)))
 
+    def set_pixels_slot(self, slot: int, iCol, iRow, idim: int):
+        iCol = np.ascontiguousarray(iCol, dtype=np.int32)
+        iRow = np.ascontiguousarray(iRow, dtype=np.int32)
+        check(lib().tg3_ctx_set_pixels_slot(self.h, slot, ptr(iCol), ptr(iRow), len(iCol), idim))
+
+    def use_pixels(self, slot: int):
+        check(lib().tg3_ctx_use_pixels(self.h, slot))
+
     def set_timing(self, enable: bool):
         check(lib().tg3_ctx_set_timing(self.h, int(enable)))
 
@@ -234,3 +250,50 @@ class Context:
 
 def version() -> str:
     return lib().tg3_version().decode()
+
+
+RAGGED_INPUTS = ("dat", "ctf", "sig", "quat", "trans", "pwR", "pwT", "pwC", "permR", "u0R",
+                 "peakR", "permT", "u0T", "peakT")
+RAGGED_OUTPUTS = ("wC", "base", "wR", "wT", "srcR", "wOutR", "srcT", "wOutT", "topR", "topT")
+
+
+class RaggedPlan:
+    """tg3_ragged_plan: a batch of particles with uneven hypothesis sets.
+
+    cls, nR, nT: host int arrays (one entry per particle); inp / out: dicts
+    of device tensors packed particle after particle (RAGGED_INPUTS /
+    RAGGED_OUTPUTS, layouts as in thunder_gb300.h).  budget 0 autotunes."""
+
+    def __init__(self, ctx: Context, cls, nR, nT, inp: dict, out: dict,
+                 precision: int = SCORE_FP32, budget: int = 0, graph: bool = True):
+        self.ctx = ctx
+        self._keep = [inp, out]
+        self.cls = np.ascontiguousarray(cls, dtype=np.int32)
+        self.nR = np.ascontiguousarray(nR, dtype=np.int32)
+        self.nT = np.ascontiguousarray(nT, dtype=np.int32)
+        h = ctypes.c_void_p()
+        args = [ptr(inp[k]) for k in RAGGED_INPUTS] + [ptr(out[k]) for k in RAGGED_OUTPUTS]
+        check(lib().tg3_ragged_plan_create(ctx.h, len(self.cls), ptr(self.cls), ptr(self.nR),
+                                           ptr(self.nT), *args, precision, int(budget),
+                                           int(graph), ctypes.byref(h)))
+        self.h = h
+
+    def run(self):
+        check(lib().tg3_ragged_plan_run(self.h))
+
+    def info(self):
+        w = ctypes.c_int()
+        b = ctypes.c_size_t()
+        check(lib().tg3_ragged_plan_info(self.h, ctypes.byref(w), ctypes.byref(b)))
+        return w.value, b.value
+
+    def close(self):
+        if self.h:
+            lib().tg3_ragged_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
