@@ -509,6 +509,157 @@ def run_global(args, rank, world, local_rank):
     return res
 
 
+UNEVEN = dict(box=192, pixel_size=1.3, n_blobs=150, sigma_a=(1.5, 3.0), radius_px=60.0,
+              cutoffs=(40, 56, 72, 96), pf=2, shift=8.0, snr=0.03, kappa=200.0,
+              nR=(200, 8000), nT=(9, 81))
+
+
+def run_uneven(args, rank, world, local_rank):
+    """Uneven batches: 192^3 maps, 1.3 A/px, 4 classes of 150-blob maps with
+    cutoffs 40 / 56 / 72 / 96 (K = 2,452 / 4,844 / 8,026 / 14,324); every
+    particle keeps log-uniform [200, 8,000] rotations x [9, 81] translations,
+    as after narrowing.  A step is one ragged plan over the batch (waves of
+    similar particles, replayed as one captured CUDA graph, autotuned wave
+    budget); the same particles scored one at a time (three calls each) are
+    timed beside it on a bounded sample."""
+    import torch
+    import tg3
+    from tg3 import synth
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    U = UNEVEN
+    nP = args.batch_uneven
+    rng = np.random.default_rng(3000 + 97 * rank)
+    box, px, pf = U["box"], U["pixel_size"], U["pf"]
+    nC = len(U["cutoffs"])
+    maps = [synth.blob_map(rng, U["n_blobs"], U["sigma_a"], px, U["radius_px"]) for _ in range(nC)]
+    ctx = tg3.Context(local_rank)
+    for c, bm in enumerate(maps):
+        ctx.set_volume(c, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
+    rL = synth.config_rL(box, px)
+    cls = np.arange(nP) % nC
+    lo_r, hi_r = U["nR"]
+    lo_t, hi_t = U["nT"]
+    nR = np.round(np.exp(rng.uniform(np.log(lo_r), np.log(hi_r), nP))).astype(np.int32)
+    nT = np.round(np.exp(rng.uniform(np.log(lo_t), np.log(hi_t), nP))).astype(np.int32)
+    stacks, Ks = [], []
+    for c, rU in enumerate(U["cutoffs"]):
+        n_c = int(np.sum(cls == c))
+        st = synth.make_stack(3100 + c + 97 * rank, [maps[c]], box, px, pf, rU, rL, n_c,
+                              U["shift"], U["snr"], device=dev)
+        ctx.set_pixels_slot(c, st.iCol, st.iRow, box)
+        stacks.append(st)
+        Ks.append(st.K)
+    # particle l is particle l // nC of its class's stack
+    row = np.arange(nP) // nC
+    qtrue = np.stack([stacks[cls[l]].quat_true[row[l]] for l in range(nP)])
+    ttrue = np.stack([stacks[cls[l]].trans_true[row[l]] for l in range(nP)])
+    qc, tc = synth.perturb_poses(rng, qtrue, ttrue, 3.0, 1.0)
+    quat = synth.vmf_quaternions_many(rng, qc, U["kappa"], nR)
+    trans = np.repeat(tc, nT, axis=0) + 2.0 * rng.standard_normal((int(nT.sum()), 2))
+    cat = lambda f: np.concatenate([f(l) for l in range(nP)])
+    host = dict(
+        dat=cat(lambda l: stacks[cls[l]].dat[row[l]]).astype(np.complex64),
+        ctf=cat(lambda l: stacks[cls[l]].ctf[row[l]]).astype(np.float32),
+        sig=cat(lambda l: stacks[cls[l]].sigRcp[row[l]]).astype(np.float32),
+        quat=quat, trans=trans,
+        pwR=np.repeat(1.0 / nR, nR), pwT=np.repeat(1.0 / nT, nT), pwC=np.ones(nP),
+        permR=cat(lambda l: rng.permutation(int(nR[l]))).astype(np.int32),
+        u0R=rng.random(nP) / nR, peakR=np.full(nP, np.nan),
+        permT=cat(lambda l: rng.permutation(int(nT[l]))).astype(np.int32),
+        u0T=rng.random(nP) / nT, peakT=np.zeros(nP))
+    inp = {k: torch.as_tensor(np.ascontiguousarray(v)).to(dev) for k, v in host.items()}
+    R, T = int(nR.sum()), int(nT.sum())
+    f64 = dict(dtype=torch.float64, device=dev)
+    i32 = dict(dtype=torch.int32, device=dev)
+    out = dict(wC=torch.empty(nP, **f64), base=torch.empty(nP, **f64), wR=torch.empty(R, **f64),
+               wT=torch.empty(T, **f64), srcR=torch.empty(R, **i32), wOutR=torch.empty(R, **f64),
+               srcT=torch.empty(T, **i32), wOutT=torch.empty(T, **f64),
+               topR=torch.empty(nP, **i32), topT=torch.empty(nP, **i32))
+    prec = tg3.SCORE_BF16X3 if args.precision == "bf16x3" else tg3.SCORE_FP32
+    t0 = time.perf_counter()
+    plan = tg3.RaggedPlan(ctx, cls, nR, nT, inp, out, prec, budget=0, graph=True)
+    plan_s = time.perf_counter() - t0
+    waves, budget = plan.info()
+    for _ in range(args.warmup):
+        plan.run()
+    ctx.sync()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    torch.cuda.synchronize()
+    clk = ClockSampler(local_rank)
+    clk.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.run()
+    e1.record(stream)
+    e1.synchronize()
+    clocks = clk.stop()
+    ctx.sync()
+    ms = e0.elapsed_time(e1) / args.steps
+    # the same particles one at a time (local phase + two resamplings each)
+    ns = min(nP, args.per_particle_sample)
+    pref = dict(po=np.concatenate([[0], np.cumsum([Ks[c] for c in cls])]),
+                ro=np.concatenate([[0], np.cumsum(nR)]), to=np.concatenate([[0], np.cumsum(nT)]))
+    cl1 = [torch.tensor([c], dtype=torch.int32, device=dev) for c in range(nC)]
+    tmp = {k: torch.empty_like(v) for k, v in out.items()}
+
+    def one(l):
+        K, r, t = Ks[cls[l]], int(nR[l]), int(nT[l])
+        po, ro, to = int(pref["po"][l]), int(pref["ro"][l]), int(pref["to"][l])
+        ctx.use_pixels(int(cls[l]))
+        ctx.local_phase(1, r, t, inp["dat"][po:po + K], inp["ctf"][po:po + K],
+                        inp["sig"][po:po + K], inp["quat"][ro:ro + r], inp["trans"][to:to + t],
+                        inp["pwR"][ro:ro + r], inp["pwT"][to:to + t], inp["pwC"][l:l + 1],
+                        cl1[cls[l]], tmp["wC"][l:l + 1], tmp["wR"][ro:ro + r],
+                        tmp["wT"][to:to + t], tmp["base"][l:l + 1], None, prec)
+        ctx.resample(1, r, tmp["wR"][ro:ro + r], inp["pwR"][ro:ro + r], inp["permR"][ro:ro + r],
+                     inp["u0R"][l:l + 1], inp["peakR"][l:l + 1], r, tmp["srcR"][ro:ro + r],
+                     tmp["wOutR"][ro:ro + r], tmp["topR"][l:l + 1])
+        ctx.resample(1, t, tmp["wT"][to:to + t], inp["pwT"][to:to + t], inp["permT"][to:to + t],
+                     inp["u0T"][l:l + 1], inp["peakT"][l:l + 1], t, tmp["srcT"][to:to + t],
+                     tmp["wOutT"][to:to + t], tmp["topT"][l:l + 1])
+
+    for l in range(min(ns, 8)):
+        one(l)
+    ctx.sync()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    for l in range(ns):
+        one(l)
+    e3.record(stream)
+    e3.synchronize()
+    ctx.sync()
+    pp_ms = e2.elapsed_time(e3)
+    # per-particle work of the sample, to scale its time to the whole batch
+    work = lambda idx: float(np.sum(nR[idx].astype(np.float64) * np.array(Ks)[cls[idx]]))
+    pp_batch_ms = pp_ms * work(np.arange(nP)) / work(np.arange(ns))
+    samples = work(np.arange(nP))
+    hyps = float(np.sum(nR.astype(np.float64) * nT))
+    flop = 4.0 * float(np.sum(nR.astype(np.float64) * nT * np.array(Ks)[cls]))
+    res = {"metric": "uneven-batch E-step particles/s, box 192, 4 classes, ragged hypothesis sets",
+           "value": round(nP / (ms * 1e-3), 1), "unit": UNIT, "ms_per_step": round(ms, 3),
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+           "precision": args.precision, "clocks": clocks,
+           "config": {"workload": "ragged plan: 4 classes, cutoffs 40/56/72/96 (K = "
+                                  + "/".join(str(k) for k in Ks) + "), rotations log-uniform "
+                                  "[200, 8000] x translations log-uniform [9, 81] per particle",
+                      "particles_per_step": nP, "rotations_total": R, "translations_total": T,
+                      "plan_waves": waves, "wave_budget_bytes": budget,
+                      "plan_create_s": round(plan_s, 2)},
+           "hypotheses_per_s": round(hyps / (ms * 1e-3), 1),
+           "samples_per_s": round(samples / (ms * 1e-3), 1),
+           "cross_term_tflops": round(flop / (ms * 1e-3) / 1e12, 1),
+           "per_particle_launches": {
+               "value": round(nP / (pp_batch_ms * 1e-3), 1), "unit": UNIT,
+               "sample": f"first {ns} particles one at a time (local phase + 2 resamplings "
+                         f"each, {pp_ms:.1f} ms), scaled to the batch by rotations x pixels"},
+           "speedup_vs_per_particle": round(pp_batch_ms / ms, 2)}
+    plan.close()
+    ctx.close()
+    return res
+
+
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per particle of a
 # launch, box 256 local workload: one 1-pass ncu capture of a 64-particle
 # launch (k_project 13.36 GB read + 5.09 GB written; k_gemm_bf16x3 5.62 GB +
@@ -702,7 +853,11 @@ def main():
                     help="split-bf16 path through the fused projection + tcgen05 kernel")
     ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
     ap.add_argument("--workload", default="local256",
-                    choices=["local256", "local256c3", "global64"])
+                    choices=["local256", "local256c3", "global64", "uneven192"])
+    ap.add_argument("--batch-uneven", type=int, default=4096,
+                    help="particles per ragged plan (uneven192)")
+    ap.add_argument("--per-particle-sample", type=int, default=256,
+                    help="particles timed one at a time beside the plan (uneven192)")
     ap.add_argument("--global-particles", type=int, default=2000)
     args = ap.parse_args()
     rank, world, local = init_dist()
@@ -710,6 +865,8 @@ def main():
         res = run_reference(args, rank, world)
     elif args.workload == "global64":
         res = run_global(args, rank, world, local)
+    elif args.workload == "uneven192":
+        res = run_uneven(args, rank, world, local)
     else:
         res = run_tg3(args, rank, world, local)
     if rank == 0 and res is not None:

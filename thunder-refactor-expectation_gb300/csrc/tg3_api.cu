@@ -144,12 +144,14 @@ int check_ctx(tg3_ctx* c)
     return TG3_OK;
 }
 
-static int check_geometry(tg3_ctx* c, int vdim, int pf)
+// Every rotated pixel must stay inside the stored half volume, |R v| = |v|:
+// margin 1 keeps a trilinear sample's corner block (its x0 + 1 <= vdim / 2
+// is stored; its y0, z0 stay in [-vdim / 2, vdim / 2)), margin 2 also the
+// MKB insertion support.
+static int check_geometry(tg3_ctx* c, int vdim, int pf, double margin = 1.0)
 {
     if (c->px.K <= 0) return fail(TG3_ERR_STATE, "pixel list not set");
-    // every rotated pixel must stay strictly inside the stored half volume:
-    // |R v| = |v| < vdim / 2 - 1 keeps all eight corners (and the MKB support)
-    if (c->px.maxRadius * pf + 2.0 > vdim / 2)
+    if (c->px.maxRadius * pf + margin > vdim / 2)
         return fail(TG3_ERR_ARG, "pixel radius " + std::to_string(c->px.maxRadius) +
                                      " x pf does not fit the volume edge " + std::to_string(vdim));
     return TG3_OK;
@@ -658,7 +660,7 @@ static int insert_draws(tg3_ctx* c, int nDraws, int drawsPerImage, const float* 
     if (!c->ins.acc) return fail(TG3_ERR_STATE, "insertion volume not begun");
     if (kernel != TG3_KERNEL_MKB && kernel != TG3_KERNEL_TRILINEAR)
         return fail(TG3_ERR_ARG, "unknown insertion kernel");
-    int st = check_geometry(c, c->ins.vdim, c->ins.pf);
+    int st = check_geometry(c, c->ins.vdim, c->ins.pf, 2.0);
     if (st) return st;
     StageTimer tm(c, TG3_STAGE_INSERT);
     TG3_CUDA(launch_insert(c->ins.acc, c->ins.vdim, kernel, c->ins.tab, c->ins.tabNz,

@@ -19,7 +19,9 @@ constexpr int kMaxClasses = 16;
 constexpr int kProjU = 4;
 constexpr int kProjChunk = 128 * kProjU;
 constexpr int kProjG = 8;
-constexpr int kMaxResampleN = 4096;   // particle-set size held in shared memory
+// particle-set size held in shared memory by the resampler: 3 doubles and one
+// int per entry (8,192 entries = 224 KB of the 227 KB a CTA may hold)
+constexpr int kMaxResampleN = 8192;
 
 // ---------------------------------------------------------------- errors --
 void set_error(const std::string& msg);

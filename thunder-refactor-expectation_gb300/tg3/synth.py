@@ -381,6 +381,36 @@ def global_translations(half: int = 3, step: float = 1.0) -> np.ndarray:
     return np.stack([tx.ravel(), ty.ravel()], 1)
 
 
+def vmf_quaternions_many(rng: np.random.Generator, means: np.ndarray, kappa: float,
+                         counts) -> np.ndarray:
+    """counts[i] vMF samples about means[i] (one concentration for all), as
+    vmf_quaternions draws them, packed particle after particle:
+    (sum(counts), 4)."""
+    counts = np.asarray(counts, dtype=np.int64)
+    n = int(counts.sum())
+    p = 4
+    b = (-2 * kappa + math.sqrt(4 * kappa * kappa + (p - 1) ** 2)) / (p - 1)
+    x0 = (1 - b) / (1 + b)
+    c = kappa * x0 + (p - 1) * math.log(1 - x0 * x0)
+    w = np.empty(n)
+    filled = 0
+    while filled < n:
+        m = (n - filled) * 2 + 8
+        z = rng.beta((p - 1) / 2, (p - 1) / 2, m)
+        u = rng.random(m)
+        ww = (1 - (1 + b) * z) / (1 - (1 - b) * z)
+        ok = kappa * ww + (p - 1) * np.log(1 - x0 * ww) - c >= np.log(u)
+        take = ww[ok][: n - filled]
+        w[filled:filled + len(take)] = take
+        filled += len(take)
+    v = rng.standard_normal((n, p - 1))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    samp = np.concatenate([w[:, None], np.sqrt(1 - w * w)[:, None] * v], 1)
+    out = quat_mul(np.repeat(means, counts, axis=0), samp)
+    out /= np.linalg.norm(out, axis=1, keepdims=True)
+    return out
+
+
 def local_hypotheses(rng: np.random.Generator, q_centre: np.ndarray,
                      t_centre: np.ndarray, nR: int, nT: int, kappa: float,
                      trans_sd: float):
