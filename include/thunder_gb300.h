@@ -169,7 +169,8 @@ size_t tg3_ctx_workspace_bytes(tg3_ctx* ctx);
 
 /* Projection volume for class `cls` (0-based, < 16): device or host complex
  * half-FT volume of edge vdim, padding factor pf.  Copied into the
- * context's paired-corner layout. */
+ * context's layout: 64-byte blocks of a voxel's eight trilinear corners,
+ * placed in 32^3-voxel cubes (about 8x the bytes of the volume). */
 int tg3_ctx_set_volume(tg3_ctx* ctx, int cls, const float* volume, int vdim,
                        int pf, int volume_on_device);
 
