@@ -265,6 +265,31 @@ int tg3_ragged_plan_run(tg3_plan* plan);
 int tg3_ragged_plan_info(const tg3_plan* plan, int* waves, size_t* budget);
 int tg3_ragged_plan_destroy(tg3_plan* plan);
 
+/* Pose-proposal network (no counterpart in the reference: a learned seed for
+ * the particle filter's rotation and translation samples, rescored by the
+ * exact likelihood).  Input: images [n][64][64] float (device).  Output
+ * [n][68]: 8 components x (6-D rotation a1 a2, raw concentration, logit),
+ * shift mean (2), shift log-variance (2).  All kernels are the library's
+ * own; weights are used in bf16 (FP32 master copies), accumulation FP32.
+ * tg3_cnn_loss: mean negative log-likelihood of the true poses Rstar
+ * [n][9] (row-major) and tstar [n][2] (device); with accumulate_grads its
+ * gradient is added to the network's gradient buffer, which tg3_cnn_adam
+ * applies (learning rate lr) and tg3_cnn_zero_grads clears.
+ * tg3_cnn_params copies the parameters to (set = 0) or from (set = 1) the
+ * host; tg3_cnn_set_bf16(net, 0) keeps weights in FP32 (gradient checks). */
+typedef struct tg3_cnn tg3_cnn;
+int tg3_cnn_create(tg3_cnn** net, int device, unsigned long long seed);
+int tg3_cnn_destroy(tg3_cnn* net);
+size_t tg3_cnn_param_count(const tg3_cnn* net);
+int tg3_cnn_params(tg3_cnn* net, float* host, int set);
+int tg3_cnn_grads(tg3_cnn* net, float* host);
+int tg3_cnn_set_bf16(tg3_cnn* net, int enable);
+int tg3_cnn_forward(tg3_cnn* net, const float* img, int n, float* out);
+int tg3_cnn_loss(tg3_cnn* net, const float* img, int n, const double* Rstar,
+                 const double* tstar, int accumulate_grads, double* loss);
+int tg3_cnn_zero_grads(tg3_cnn* net);
+int tg3_cnn_adam(tg3_cnn* net, float lr);
+
 /* Global scan of nImg images over one shared set of nR rotations and nT
  * translations, for the context's class-`cls` volume: the scan of
  * Optimiser::doGlobalSearch (src/Optimiser.cpp:759-899), the work of

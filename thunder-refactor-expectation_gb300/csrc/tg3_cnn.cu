@@ -1,0 +1,696 @@
+// tg3_cnn.cu -- the pose-proposal network: forward, backward and Adam, all
+// hand-written kernels (no library calls).
+//
+// Input: a 64 x 64 particle image (real space, normalised).  Layers:
+//   conv1  1 -> 32, 3x3, stride 1   64 x 64
+//   conv2 32 -> 32, 3x3, stride 2   32 x 32
+//   conv3 32 -> 64, stride 1        32 x 32
+//   conv4 64 -> 64, stride 2        16 x 16
+//   conv5 64 -> 128, stride 1       16 x 16
+//   conv6 128 -> 128, stride 2       8 x  8     (every conv: pad 1, bias, ReLU)
+//   fc1  8192 -> 256, ReLU;  fc2  256 -> 68.
+// Output per image: 8 mixture components x (6-D rotation, raw concentration,
+// logit) = 64 values, then the shift mean (2) and its log-variance (2).
+// The weights are used in bf16 (rounded from FP32 master copies on every
+// load), activations and accumulation are FP32.
+//
+// Loss per image (the negative log-likelihood of the true pose):
+//   R_k = GramSchmidt(a_k, b_k),  c_k = (tr(R_k^T R*) - 1) / 2 = cos(angle),
+//   kappa_k = softplus(raw_k) + 1e-3,
+//   -log sum_k softmax(logit)_k kappa_k^{3/2} exp(kappa_k (c_k - 1))
+//   + 0.5 sum_d ((t*_d - mu_d)^2 exp(-lv_d) + lv_d).
+// (A concentrated rotation density in the angle: kappa^{3/2} exp(-kappa
+// angle^2 / 2) for small angles, up to constants.)
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <cstring>
+#include <vector>
+
+#include "tg3_internal.cuh"
+
+namespace tg3 {
+
+namespace {
+
+constexpr int kLayers = 8;   // 6 conv + 2 fc
+
+inline int cnn_grid(size_t n, int block)
+{
+    const size_t g = (n + block - 1) / block;
+    return (int)(g < 4096 ? (g ? g : 1) : 4096);
+}
+constexpr int kOut = 68;
+constexpr int kComp = 8;
+
+struct LayerShape {
+    int cin, cout, hin, hout, stride;   // fc: hin = hout = 1, stride 0
+};
+
+constexpr LayerShape kShape[kLayers] = {
+    {1, 32, 64, 64, 1},   {32, 32, 64, 32, 2},  {32, 64, 32, 32, 1},  {64, 64, 32, 16, 2},
+    {64, 128, 16, 16, 1}, {128, 128, 16, 8, 2}, {8192, 256, 1, 1, 0}, {256, kOut, 1, 1, 0}};
+
+__host__ __device__ inline size_t weight_count(const LayerShape& s)
+{
+    return s.stride ? (size_t)s.cout * s.cin * 9 : (size_t)s.cout * s.cin;
+}
+
+// weights as the forward and backward passes use them: rounded to bf16, or
+// kept in FP32 (gradient checks by finite differences need a smooth loss)
+__device__ __forceinline__ float bf(float w, int round = 1)
+{
+    return round ? __bfloat162float(__float2bfloat16_rn(w)) : w;
+}
+
+// ---------------------------------------------------------------- conv ---
+// y[n][co][oy][ox] = relu(b[co] + sum_ci,ky,kx W[co][ci][ky][kx] x[n][ci][oy s + ky - 1][ox s + kx - 1])
+// CTA: 16 output channels x 256 output pixels of one image; weights of a
+// 16-channel input slice staged in shared memory.
+__global__ void __launch_bounds__(256)
+k_conv_fwd(const float* __restrict__ x, const float* __restrict__ W, const float* __restrict__ b,
+           float* __restrict__ y, int cin, int cout, int hin, int hout, int stride, int relu,
+           int roundW)
+{
+    __shared__ float ws[16][16][9];
+    const int n = blockIdx.z, co0 = blockIdx.y * 16;
+    const int pix = blockIdx.x * 256 + threadIdx.x;
+    const int oy = pix / hout, ox = pix % hout;
+    const bool valid = pix < hout * hout;
+    float acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++) acc[c] = 0.f;
+    const float* xn = x + (size_t)n * cin * hin * hin;
+    for (int ci0 = 0; ci0 < cin; ci0 += 16) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 16 * 16 * 9; i += 256) {
+            const int c = i / 144, cc = (i / 9) % 16, k = i % 9;
+            ws[c][cc][k] = (co0 + c < cout && ci0 + cc < cin)
+                               ? bf(W[((size_t)(co0 + c) * cin + ci0 + cc) * 9 + k], roundW)
+                               : 0.f;
+        }
+        __syncthreads();
+        if (!valid) continue;
+        const int ncc = min(16, cin - ci0);
+        for (int cc = 0; cc < ncc; cc++) {
+            const float* xc = xn + (size_t)(ci0 + cc) * hin * hin;
+            float v[9];
+#pragma unroll
+            for (int ky = 0; ky < 3; ky++)
+#pragma unroll
+                for (int kx = 0; kx < 3; kx++) {
+                    const int iy = oy * stride + ky - 1, ix = ox * stride + kx - 1;
+                    v[ky * 3 + kx] = (iy >= 0 && iy < hin && ix >= 0 && ix < hin) ? xc[iy * hin + ix] : 0.f;
+                }
+#pragma unroll
+            for (int c = 0; c < 16; c++)
+#pragma unroll
+                for (int k = 0; k < 9; k++) acc[c] = fmaf(ws[c][cc][k], v[k], acc[c]);
+        }
+    }
+    if (!valid) return;
+    for (int c = 0; c < 16 && co0 + c < cout; c++) {
+        float o = acc[c] + b[co0 + c];
+        if (relu) o = fmaxf(o, 0.f);
+        y[(((size_t)n * cout + co0 + c) * hout + oy) * hout + ox] = o;
+    }
+}
+
+// dx[n][ci][iy][ix] = sum_co,ky,kx W[co][ci][ky][kx] dy[n][co][oy][ox] with
+// iy = oy s + ky - 1 (the taps that reached the input pixel).  CTA: 16 input
+// channels x 256 input pixels of one image.
+__global__ void __launch_bounds__(256)
+k_conv_bwd_data(const float* __restrict__ dy, const float* __restrict__ W, float* __restrict__ dx,
+                int cin, int cout, int hin, int hout, int stride, int roundW)
+{
+    __shared__ float ws[16][16][9];   // [co slice][ci][k]
+    const int n = blockIdx.z, ci0 = blockIdx.y * 16;
+    const int pix = blockIdx.x * 256 + threadIdx.x;
+    const int iy = pix / hin, ix = pix % hin;
+    const bool valid = pix < hin * hin;
+    float acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++) acc[c] = 0.f;
+    const float* dyn = dy + (size_t)n * cout * hout * hout;
+    for (int co0 = 0; co0 < cout; co0 += 16) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 16 * 16 * 9; i += 256) {
+            const int c = i / 144, cc = (i / 9) % 16, k = i % 9;
+            ws[c][cc][k] = (co0 + c < cout && ci0 + cc < cin)
+                               ? bf(W[((size_t)(co0 + c) * cin + ci0 + cc) * 9 + k], roundW)
+                               : 0.f;
+        }
+        __syncthreads();
+        if (!valid) continue;
+        const int nc = min(16, cout - co0);
+        for (int c = 0; c < nc; c++) {
+            const float* dc = dyn + (size_t)(co0 + c) * hout * hout;
+#pragma unroll
+            for (int ky = 0; ky < 3; ky++) {
+                const int ty = iy + 1 - ky;
+                if (ty < 0 || ty % stride) continue;
+                const int oy = ty / stride;
+                if (oy >= hout) continue;
+#pragma unroll
+                for (int kx = 0; kx < 3; kx++) {
+                    const int tx = ix + 1 - kx;
+                    if (tx < 0 || tx % stride) continue;
+                    const int ox = tx / stride;
+                    if (ox >= hout) continue;
+                    const float g = dc[oy * hout + ox];
+#pragma unroll
+                    for (int cc = 0; cc < 16; cc++) acc[cc] = fmaf(ws[c][cc][ky * 3 + kx], g, acc[cc]);
+                }
+            }
+        }
+    }
+    if (!valid) return;
+    for (int cc = 0; cc < 16 && ci0 + cc < cin; cc++)
+        dx[(((size_t)n * cin + ci0 + cc) * hin + iy) * hin + ix] = acc[cc];
+}
+
+// dW[co][ci][k] += sum_n,oy,ox dy[n][co][oy][ox] x[n][ci][tap k], db[co] +=
+// sum dy.  CTA: one output channel, 8 input channels, one slice of images;
+// the CTA's partial sums go to the gradient with one atomic add each.
+__global__ void __launch_bounds__(256)
+k_conv_bwd_weight(const float* __restrict__ x, const float* __restrict__ dy, float* __restrict__ dW,
+                  float* __restrict__ db, int N, int cin, int cout, int hin, int hout, int stride,
+                  int imgPerCta)
+{
+    __shared__ float red[72 + 1][8];
+    const int co = blockIdx.x, ci0 = blockIdx.y * 8, n0 = blockIdx.z * imgPerCta;
+    const int nci = min(8, cin - ci0);
+    float acc[8][9];
+    float accb = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+#pragma unroll
+        for (int k = 0; k < 9; k++) acc[c][k] = 0.f;
+    const int P = hout * hout;
+    const int total = min(imgPerCta, N - n0) * P;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int n = n0 + e / P, pix = e % P;
+        const int oy = pix / hout, ox = pix % hout;
+        const float g = dy[(((size_t)n * cout + co) * hout + oy) * hout + ox];
+        if (g == 0.f) continue;
+        accb += g;
+        for (int c = 0; c < nci; c++) {
+            const float* xc = x + ((size_t)n * cin + ci0 + c) * hin * hin;
+#pragma unroll
+            for (int ky = 0; ky < 3; ky++)
+#pragma unroll
+                for (int kx = 0; kx < 3; kx++) {
+                    const int iy = oy * stride + ky - 1, ix = ox * stride + kx - 1;
+                    if (iy >= 0 && iy < hin && ix >= 0 && ix < hin)
+                        acc[c][ky * 3 + kx] = fmaf(g, xc[iy * hin + ix], acc[c][ky * 3 + kx]);
+                }
+        }
+    }
+    // block reduction: warp sums, then the 8 warps' sums in order
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            float v = acc[c][k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) red[c * 9 + k][wid] = v;
+        }
+    for (int o = 16; o > 0; o >>= 1) accb += __shfl_xor_sync(0xffffffffu, accb, o);
+    if (lane == 0) red[72][wid] = accb;
+    __syncthreads();
+    if (threadIdx.x < 73) {
+        float s = 0.f;
+        for (int w = 0; w < 8; w++) s += red[threadIdx.x][w];
+        if (threadIdx.x == 72) {
+            if (blockIdx.y == 0) atomicAdd(db + co, s);
+        } else {
+            const int c = threadIdx.x / 9, k = threadIdx.x % 9;
+            if (c < nci) atomicAdd(dW + ((size_t)co * cin + ci0 + c) * 9 + k, s);
+        }
+    }
+}
+
+// ------------------------------------------------------------ dense ---
+// C[m][n] (+)= sum_k A(m, k) B(k, n); A(m, k) = A[m lda + k] or A[k lda + m]
+// (transA), B(k, n) = B[k ldb + n] or B[n ldb + k] (transB).  Optional bias
+// per column, ReLU, bf16 rounding of B (weights).  16 x 16 tiles.
+__global__ void k_dense(const float* __restrict__ A, const float* __restrict__ B, float* __restrict__ C,
+                        int M, int N, int K, int lda, int ldb, int ldc, int transA, int transB,
+                        const float* __restrict__ bias, int relu, int accumulate, int bfB)
+{
+    __shared__ float As[16][17], Bs[16][17];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int m = blockIdx.y * 16 + ty, n = blockIdx.x * 16 + tx;
+    float acc = 0.f;
+    for (int k0 = 0; k0 < K; k0 += 16) {
+        {
+            const int mm = blockIdx.y * 16 + ty, kk = k0 + tx;
+            float v = 0.f;
+            if (mm < M && kk < K) v = transA ? A[(size_t)kk * lda + mm] : A[(size_t)mm * lda + kk];
+            As[ty][tx] = v;
+        }
+        {
+            const int kk = k0 + ty, nn = blockIdx.x * 16 + tx;
+            float v = 0.f;
+            if (kk < K && nn < N) v = transB ? B[(size_t)nn * ldb + kk] : B[(size_t)kk * ldb + nn];
+            Bs[ty][tx] = bf(v, bfB);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 16; k++) acc = fmaf(As[ty][k], Bs[k][tx], acc);
+        __syncthreads();
+    }
+    if (m < M && n < N) {
+        float* c = C + (size_t)m * ldc + n;
+        float v = acc + (bias ? bias[n] : 0.f);
+        if (relu) v = fmaxf(v, 0.f);
+        *c = accumulate ? *c + v : v;
+    }
+}
+
+// g *= (y > 0): the gradient through a ReLU whose output is y
+__global__ void k_relu_bwd(float* __restrict__ g, const float* __restrict__ y, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        if (!(y[i] > 0.f)) g[i] = 0.f;
+}
+
+// db[n] += sum_m g[m][n]
+__global__ void k_col_sum(const float* __restrict__ g, float* __restrict__ db, int M, int N)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    float s = 0.f;
+    for (int m = 0; m < M; m++) s += g[(size_t)m * N + n];
+    db[n] += s;
+}
+
+// --------------------------------------------------------------- head ---
+struct V3 {
+    double x, y, z;
+};
+__device__ inline V3 v3(double a, double b, double c) { return {a, b, c}; }
+__device__ inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ inline V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ inline V3 mul(V3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ inline V3 cross(V3 a, V3 b)
+{
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+// One thread per image: loss and its gradient with respect to the 68 outputs.
+// Rstar: the true rotation, columns r1, r2, r3 (row-major 3x3); tstar: shift.
+__global__ void k_head_loss(const float* __restrict__ out, const double* __restrict__ Rstar,
+                            const double* __restrict__ tstar, float* __restrict__ gout,
+                            double* __restrict__ loss, int N, float scale)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    const float* o = out + (size_t)n * kOut;
+    const double* Rs = Rstar + (size_t)n * 9;
+    const V3 r1 = v3(Rs[0], Rs[3], Rs[6]), r2 = v3(Rs[1], Rs[4], Rs[7]), r3 = v3(Rs[2], Rs[5], Rs[8]);
+    double lp[kComp], c[kComp], kap[kComp], maxlp = -1e300;
+    V3 b1s[kComp], b2s[kComp], a1s[kComp], a2s[kComp];
+    double n1s[kComp], n2s[kComp];
+    // log-softmax of the logits
+    double lmax = -1e300;
+    for (int k = 0; k < kComp; k++) lmax = fmax(lmax, (double)o[k * 8 + 7]);
+    double lsum = 0;
+    for (int k = 0; k < kComp; k++) lsum += exp((double)o[k * 8 + 7] - lmax);
+    const double llse = lmax + log(lsum);
+    for (int k = 0; k < kComp; k++) {
+        const float* q = o + k * 8;
+        const V3 a1 = v3(q[0], q[1], q[2]), a2 = v3(q[3], q[4], q[5]);
+        const double n1 = sqrt(dot(a1, a1)) + 1e-12;
+        const V3 b1 = mul(a1, 1.0 / n1);
+        const V3 u2 = sub(a2, mul(b1, dot(b1, a2)));
+        const double n2 = sqrt(dot(u2, u2)) + 1e-12;
+        const V3 b2 = mul(u2, 1.0 / n2);
+        const V3 b3 = cross(b1, b2);
+        c[k] = 0.5 * (dot(b1, r1) + dot(b2, r2) + dot(b3, r3) - 1.0);
+        const double raw = q[6];
+        kap[k] = (raw > 20 ? raw : log1p(exp(raw))) + 1e-3;
+        lp[k] = (double)q[7] - llse + 1.5 * log(kap[k]) + kap[k] * (c[k] - 1.0);
+        maxlp = fmax(maxlp, lp[k]);
+        b1s[k] = b1;
+        b2s[k] = b2;
+        a1s[k] = a1;
+        a2s[k] = a2;
+        n1s[k] = n1;
+        n2s[k] = n2;
+    }
+    double s = 0;
+    for (int k = 0; k < kComp; k++) s += exp(lp[k] - maxlp);
+    const double lse = maxlp + log(s);
+    double L = -lse;
+    float* g = gout + (size_t)n * kOut;
+    // responsibilities
+    double resp[kComp];
+    for (int k = 0; k < kComp; k++) resp[k] = exp(lp[k] - lse);
+    for (int k = 0; k < kComp; k++) {
+        const float* q = o + k * 8;
+        // d(-lse)/d lp_k = -resp_k; d lp_k / d logit_j = delta_kj - softmax_j
+        // summed: dL/dlogit_j = -resp_j + softmax_j
+        const double sm = exp((double)q[7] - llse);
+        g[k * 8 + 7] = (float)(scale * (sm - resp[k]));
+        // kappa: d lp / d kappa = 1.5 / kappa + (c - 1); d kappa / d raw = sigmoid(raw)
+        const double raw = q[6];
+        const double sig = raw > 20 ? 1.0 : 1.0 / (1.0 + exp(-raw));
+        g[k * 8 + 6] = (float)(scale * (-resp[k]) * (1.5 / kap[k] + c[k] - 1.0) * sig);
+        // rotation: d lp / d c = kappa; dc/db1 = (r1 + b2 x r3) / 2, dc/db2 = (r2 + r3 x b1) / 2
+        const double w = -resp[k] * kap[k] * scale;
+        const V3 b1 = b1s[k], b2 = b2s[k], a2 = a2s[k];
+        V3 gb1 = mul(add(r1, cross(b2, r3)), 0.5 * w);
+        const V3 gb2 = mul(add(r2, cross(r3, b1)), 0.5 * w);
+        // b2 = u2 / |u2|
+        const V3 gu2 = mul(sub(gb2, mul(b2, dot(b2, gb2))), 1.0 / n2s[k]);
+        // u2 = a2 - (b1 . a2) b1
+        const V3 ga2 = sub(gu2, mul(b1, dot(b1, gu2)));
+        gb1 = sub(gb1, add(mul(gu2, dot(b1, a2)), mul(a2, dot(b1, gu2))));
+        // b1 = a1 / |a1|
+        const V3 ga1 = mul(sub(gb1, mul(b1, dot(b1, gb1))), 1.0 / n1s[k]);
+        g[k * 8 + 0] = (float)ga1.x;
+        g[k * 8 + 1] = (float)ga1.y;
+        g[k * 8 + 2] = (float)ga1.z;
+        g[k * 8 + 3] = (float)ga2.x;
+        g[k * 8 + 4] = (float)ga2.y;
+        g[k * 8 + 5] = (float)ga2.z;
+    }
+    // shift: 0.5 sum ((t - mu)^2 exp(-lv) + lv)
+    for (int d = 0; d < 2; d++) {
+        const double mu = o[64 + d], lv = o[66 + d];
+        const double diff = tstar[(size_t)n * 2 + d] - mu;
+        const double e = exp(-lv);
+        L += 0.5 * (diff * diff * e + lv);
+        g[64 + d] = (float)(scale * (-diff * e));
+        g[66 + d] = (float)(scale * 0.5 * (1.0 - diff * diff * e));
+    }
+    loss[n] = L;
+}
+
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, size_t n, float lr, float b1, float b2, float c1,
+                       float c2, float eps)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+}  // namespace
+}  // namespace tg3
+
+using namespace tg3;
+
+struct tg3_cnn {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    size_t nParams = 0;
+    size_t off[kLayers][2];     // weight / bias offsets in the parameter vector
+    float* params = nullptr;    // FP32 master weights and biases
+    float* grads = nullptr;
+    float* m = nullptr;
+    float* v = nullptr;
+    long long step = 0;
+    int roundW = 1;             // weights used in bf16 (0: FP32, for gradient checks)
+    int cap = 0;                // images the activation buffers hold
+    float* act[kLayers + 1] = {};   // act[0] input copy .. act[8] outputs
+    float* gact[kLayers + 1] = {};
+    double* Rstar = nullptr;
+    double* loss = nullptr;
+};
+
+namespace {
+
+size_t act_size(int l)
+{
+    if (l == 0) return 64 * 64;
+    const LayerShape& s = kShape[l - 1];
+    return s.stride ? (size_t)s.cout * s.hout * s.hout : (size_t)s.cout;
+}
+
+int ensure_capacity(tg3_cnn* net, int n)
+{
+    if (n <= net->cap) return TG3_OK;
+    TG3_CUDA(cudaStreamSynchronize(net->stream));
+    for (int l = 0; l <= kLayers; l++) {
+        cudaFree(net->act[l]);
+        cudaFree(net->gact[l]);
+        net->act[l] = net->gact[l] = nullptr;
+    }
+    cudaFree(net->Rstar);
+    cudaFree(net->loss);
+    for (int l = 0; l <= kLayers; l++) {
+        TG3_CUDA(cudaMalloc(&net->act[l], sizeof(float) * act_size(l) * n));
+        TG3_CUDA(cudaMalloc(&net->gact[l], sizeof(float) * act_size(l) * n));
+    }
+    TG3_CUDA(cudaMalloc(&net->Rstar, sizeof(double) * 9 * n));
+    TG3_CUDA(cudaMalloc(&net->loss, sizeof(double) * n));
+    net->cap = n;
+    return TG3_OK;
+}
+
+int forward(tg3_cnn* net, int n)
+{
+    cudaStream_t s = net->stream;
+    for (int l = 0; l < kLayers; l++) {
+        const LayerShape& sh = kShape[l];
+        const float* W = net->params + net->off[l][0];
+        const float* b = net->params + net->off[l][1];
+        if (sh.stride) {
+            dim3 grid((sh.hout * sh.hout + 255) / 256, (sh.cout + 15) / 16, n);
+            k_conv_fwd<<<grid, 256, 0, s>>>(net->act[l], W, b, net->act[l + 1], sh.cin, sh.cout,
+                                             sh.hin, sh.hout, sh.stride, 1, net->roundW);
+        } else {
+            dim3 grid((sh.cout + 15) / 16, (n + 15) / 16);
+            k_dense<<<grid, dim3(16, 16), 0, s>>>(net->act[l], W, net->act[l + 1], n, sh.cout,
+                                                  sh.cin, sh.cin, sh.cin, sh.cout, 0, 1, b,
+                                                  l < kLayers - 1, 0, net->roundW);
+        }
+        TG3_LAUNCH_CHECK("network forward");
+    }
+    return TG3_OK;
+}
+
+// gact[kLayers] holds dL/d outputs; fills grads (accumulating)
+int backward(tg3_cnn* net, int n)
+{
+    cudaStream_t s = net->stream;
+    for (int l = kLayers - 1; l >= 0; l--) {
+        const LayerShape& sh = kShape[l];
+        const float* W = net->params + net->off[l][0];
+        float* dW = net->grads + net->off[l][0];
+        float* db = net->grads + net->off[l][1];
+        float* gy = net->gact[l + 1];
+        // through this layer's ReLU (all but the last)
+        if (l < kLayers - 1) {
+            const size_t cnt = act_size(l + 1) * n;
+            k_relu_bwd<<<cnn_grid(cnt, 256), 256, 0, s>>>(gy, net->act[l + 1], cnt);
+        }
+        if (sh.stride) {
+            const int imgPerCta = 8;
+            dim3 gw(sh.cout, (sh.cin + 7) / 8, (n + imgPerCta - 1) / imgPerCta);
+            k_conv_bwd_weight<<<gw, 256, 0, s>>>(net->act[l], gy, dW, db, n, sh.cin, sh.cout,
+                                                  sh.hin, sh.hout, sh.stride, imgPerCta);
+            if (l > 0) {
+                dim3 gd((sh.hin * sh.hin + 255) / 256, (sh.cin + 15) / 16, n);
+                k_conv_bwd_data<<<gd, 256, 0, s>>>(gy, W, net->gact[l], sh.cin, sh.cout, sh.hin,
+                                                    sh.hout, sh.stride, net->roundW);
+            }
+        } else {
+            // dW[o][i] += sum_n gy[n][o] x[n][i]; db[o] += sum_n gy[n][o]; dx = gy W
+            dim3 g1((sh.cin + 15) / 16, (sh.cout + 15) / 16);
+            k_dense<<<g1, dim3(16, 16), 0, s>>>(gy, net->act[l], dW, sh.cout, sh.cin, n, sh.cout,
+                                                sh.cin, sh.cin, 1, 0, nullptr, 0, 1, 0);
+            k_col_sum<<<(sh.cout + 255) / 256, 256, 0, s>>>(gy, db, n, sh.cout);
+            dim3 g2((sh.cin + 15) / 16, (n + 15) / 16);
+            k_dense<<<g2, dim3(16, 16), 0, s>>>(gy, W, net->gact[l], n, sh.cin, sh.cout, sh.cout,
+                                                sh.cin, sh.cin, 0, 0, nullptr, 0, 0, net->roundW);
+        }
+        TG3_LAUNCH_CHECK("network backward");
+    }
+    return TG3_OK;
+}
+
+// He-normal weights from a counter-based generator (splitmix64 + Box-Muller),
+// zero biases.
+void init_params(std::vector<float>& h, const tg3_cnn* net, uint64_t seed)
+{
+    uint64_t st = seed ? seed : 0x9E3779B97F4A7C15ull;
+    auto next = [&]() {
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    auto unif = [&]() { return ((next() >> 11) + 0.5) * (1.0 / 9007199254740992.0); };
+    for (int l = 0; l < kLayers; l++) {
+        const LayerShape& s = kShape[l];
+        const size_t nw = weight_count(s);
+        const double fan = s.stride ? s.cin * 9.0 : (double)s.cin;
+        const double sd = sqrt(2.0 / fan) * (l == kLayers - 1 ? 0.1 : 1.0);
+        for (size_t i = 0; i < nw; i++) {
+            const double u1 = unif(), u2 = unif();
+            h[net->off[l][0] + i] = (float)(sd * sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" int tg3_cnn_create(tg3_cnn** out, int device, unsigned long long seed)
+{
+    if (!out) return fail(TG3_ERR_ARG, "null output");
+    TG3_CUDA(cudaSetDevice(device));
+    tg3_cnn* net = new tg3_cnn();
+    net->device = device;
+    size_t o = 0;
+    for (int l = 0; l < kLayers; l++) {
+        net->off[l][0] = o;
+        o += weight_count(kShape[l]);
+        net->off[l][1] = o;
+        o += kShape[l].cout;
+    }
+    net->nParams = o;
+    if (cudaStreamCreateWithFlags(&net->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&net->params, sizeof(float) * o) != cudaSuccess ||
+        cudaMalloc(&net->grads, sizeof(float) * o) != cudaSuccess ||
+        cudaMalloc(&net->m, sizeof(float) * o) != cudaSuccess ||
+        cudaMalloc(&net->v, sizeof(float) * o) != cudaSuccess) {
+        tg3_cnn_destroy(net);
+        return fail(TG3_ERR_ALLOC, "network allocation");
+    }
+    std::vector<float> h(o, 0.f);
+    init_params(h, net, seed);
+    cudaMemcpy(net->params, h.data(), sizeof(float) * o, cudaMemcpyHostToDevice);
+    cudaMemset(net->grads, 0, sizeof(float) * o);
+    cudaMemset(net->m, 0, sizeof(float) * o);
+    cudaMemset(net->v, 0, sizeof(float) * o);
+    *out = net;
+    return TG3_OK;
+}
+
+extern "C" int tg3_cnn_destroy(tg3_cnn* net)
+{
+    if (!net) return TG3_OK;
+    cudaSetDevice(net->device);
+    if (net->stream) cudaStreamSynchronize(net->stream);
+    for (int l = 0; l <= kLayers; l++) {
+        cudaFree(net->act[l]);
+        cudaFree(net->gact[l]);
+    }
+    cudaFree(net->Rstar);
+    cudaFree(net->loss);
+    cudaFree(net->params);
+    cudaFree(net->grads);
+    cudaFree(net->m);
+    cudaFree(net->v);
+    if (net->stream) cudaStreamDestroy(net->stream);
+    delete net;
+    return TG3_OK;
+}
+
+extern "C" size_t tg3_cnn_param_count(const tg3_cnn* net) { return net ? net->nParams : 0; }
+
+extern "C" int tg3_cnn_params(tg3_cnn* net, float* host, int set)
+{
+    if (!net || !host) return fail(TG3_ERR_ARG, "null argument");
+    TG3_CUDA(cudaSetDevice(net->device));
+    TG3_CUDA(cudaStreamSynchronize(net->stream));
+    TG3_CUDA(cudaMemcpy(set ? (void*)net->params : (void*)host, set ? (const void*)host : net->params,
+                        sizeof(float) * net->nParams,
+                        set ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost));
+    return TG3_OK;
+}
+
+extern "C" int tg3_cnn_grads(tg3_cnn* net, float* host)
+{
+    if (!net || !host) return fail(TG3_ERR_ARG, "null argument");
+    TG3_CUDA(cudaSetDevice(net->device));
+    TG3_CUDA(cudaStreamSynchronize(net->stream));
+    TG3_CUDA(cudaMemcpy(host, net->grads, sizeof(float) * net->nParams, cudaMemcpyDeviceToHost));
+    return TG3_OK;
+}
+
+// outputs [n][68] (device) for images [n][64][64] (device)
+extern "C" int tg3_cnn_forward(tg3_cnn* net, const float* img, int n, float* out)
+{
+    if (!net || !img || !out || n <= 0) return fail(TG3_ERR_ARG, "bad forward arguments");
+    TG3_CUDA(cudaSetDevice(net->device));
+    int st = ensure_capacity(net, n);
+    if (st) return st;
+    TG3_CUDA(cudaMemcpyAsync(net->act[0], img, sizeof(float) * 64 * 64 * n,
+                             cudaMemcpyDeviceToDevice, net->stream));
+    if ((st = forward(net, n))) return st;
+    TG3_CUDA(cudaMemcpyAsync(out, net->act[kLayers], sizeof(float) * kOut * n,
+                             cudaMemcpyDeviceToDevice, net->stream));
+    TG3_CUDA(cudaStreamSynchronize(net->stream));
+    return TG3_OK;
+}
+
+// Loss of a batch (mean over images, returned on the host) and, with
+// `accumulate_grads`, the gradient of that mean added to the network's
+// gradient buffer.  Rstar [n][9] row-major true rotations, tstar [n][2].
+extern "C" int tg3_cnn_loss(tg3_cnn* net, const float* img, int n, const double* Rstar,
+                            const double* tstar, int accumulate_grads, double* lossOut)
+{
+    if (!net || !img || !Rstar || !tstar || n <= 0) return fail(TG3_ERR_ARG, "bad loss arguments");
+    TG3_CUDA(cudaSetDevice(net->device));
+    int st = ensure_capacity(net, n);
+    if (st) return st;
+    cudaStream_t s = net->stream;
+    TG3_CUDA(cudaMemcpyAsync(net->act[0], img, sizeof(float) * 64 * 64 * n,
+                             cudaMemcpyDeviceToDevice, s));
+    if ((st = forward(net, n))) return st;
+    k_head_loss<<<(n + 127) / 128, 128, 0, s>>>(net->act[kLayers], Rstar, tstar,
+                                                 net->gact[kLayers], net->loss, n, 1.0f / n);
+    TG3_LAUNCH_CHECK("network loss");
+    if (accumulate_grads && (st = backward(net, n))) return st;
+    std::vector<double> h(n);
+    TG3_CUDA(cudaMemcpyAsync(h.data(), net->loss, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaStreamSynchronize(s));
+    double sum = 0;
+    for (double x : h) sum += x;
+    if (lossOut) *lossOut = sum / n;
+    return TG3_OK;
+}
+
+extern "C" int tg3_cnn_zero_grads(tg3_cnn* net)
+{
+    if (!net) return fail(TG3_ERR_ARG, "null network");
+    TG3_CUDA(cudaSetDevice(net->device));
+    TG3_CUDA(cudaMemsetAsync(net->grads, 0, sizeof(float) * net->nParams, net->stream));
+    return TG3_OK;
+}
+
+extern "C" int tg3_cnn_adam(tg3_cnn* net, float lr)
+{
+    if (!net) return fail(TG3_ERR_ARG, "null network");
+    TG3_CUDA(cudaSetDevice(net->device));
+    net->step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)net->step), c2 = 1.f - powf(b2, (float)net->step);
+    k_adam<<<cnn_grid(net->nParams, 256), 256, 0, net->stream>>>(net->params, net->grads, net->m,
+                                                                  net->v, net->nParams, lr, b1, b2,
+                                                                  c1, c2, 1e-8f);
+    TG3_LAUNCH_CHECK("adam");
+    return TG3_OK;
+}
+
+extern "C" int tg3_cnn_set_bf16(tg3_cnn* net, int enable)
+{
+    if (!net) return fail(TG3_ERR_ARG, "null network");
+    net->roundW = enable != 0;
+    return TG3_OK;
+}

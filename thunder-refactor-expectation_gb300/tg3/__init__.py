@@ -31,7 +31,9 @@ EXPORTS = [
     "tg3_project_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
     "tg3_ctx_set_option", "tg3_ctx_set_pixels_slot", "tg3_ctx_use_pixels",
     "tg3_ragged_plan_create", "tg3_ragged_plan_run", "tg3_ragged_plan_info",
-    "tg3_ragged_plan_destroy",
+    "tg3_ragged_plan_destroy", "tg3_cnn_create", "tg3_cnn_destroy", "tg3_cnn_param_count",
+    "tg3_cnn_params", "tg3_cnn_grads", "tg3_cnn_set_bf16", "tg3_cnn_forward", "tg3_cnn_loss",
+    "tg3_cnn_zero_grads", "tg3_cnn_adam",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
@@ -98,6 +100,16 @@ def lib():
             "tg3_ragged_plan_run": ([_P], _I),
             "tg3_ragged_plan_info": ([_P, _P, _P], _I),
             "tg3_ragged_plan_destroy": ([_P], _I),
+            "tg3_cnn_create": ([_P, _I, ctypes.c_ulonglong], _I),
+            "tg3_cnn_destroy": ([_P], _I),
+            "tg3_cnn_param_count": ([_P], ctypes.c_size_t),
+            "tg3_cnn_params": ([_P, _P, _I], _I),
+            "tg3_cnn_grads": ([_P, _P], _I),
+            "tg3_cnn_set_bf16": ([_P, _I], _I),
+            "tg3_cnn_forward": ([_P, _P, _I, _P], _I),
+            "tg3_cnn_loss": ([_P, _P, _I, _P, _P, _I, _P], _I),
+            "tg3_cnn_zero_grads": ([_P], _I),
+            "tg3_cnn_adam": ([_P, ctypes.c_float], _I),
             "tg3_ctx_stage_times": ([_P, _P, _P, _I], _I),
             "tg3_noalloc_scratch_bytes": ([], ctypes.c_size_t),
             "tg3_global_scan_d": ([_P, _I, _I, _I, _I] + [_P] * 12 + [_I], _I),
@@ -290,6 +302,65 @@ class RaggedPlan:
     def close(self):
         if self.h:
             lib().tg3_ragged_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Cnn:
+    """tg3_cnn: the pose-proposal network (64 x 64 images -> 68 outputs)."""
+
+    N_OUT = 68
+
+    def __init__(self, device: int = 0, seed: int = 1):
+        h = ctypes.c_void_p()
+        check(lib().tg3_cnn_create(ctypes.byref(h), device, seed))
+        self.h = h
+
+    @property
+    def n_params(self) -> int:
+        return lib().tg3_cnn_param_count(self.h)
+
+    def params(self) -> np.ndarray:
+        a = np.empty(self.n_params, np.float32)
+        check(lib().tg3_cnn_params(self.h, ptr(a), 0))
+        return a
+
+    def set_params(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        check(lib().tg3_cnn_params(self.h, ptr(a), 1))
+
+    def grads(self) -> np.ndarray:
+        a = np.empty(self.n_params, np.float32)
+        check(lib().tg3_cnn_grads(self.h, ptr(a)))
+        return a
+
+    def set_bf16(self, enable: bool):
+        check(lib().tg3_cnn_set_bf16(self.h, int(enable)))
+
+    def forward(self, img, out):
+        """img: device float32 [n][64][64]; out: device float32 [n][68]."""
+        check(lib().tg3_cnn_forward(self.h, ptr(img), img.shape[0], ptr(out)))
+
+    def loss(self, img, Rstar, tstar, grads: bool = True) -> float:
+        v = ctypes.c_double()
+        check(lib().tg3_cnn_loss(self.h, ptr(img), img.shape[0], ptr(Rstar), ptr(tstar),
+                                 int(grads), ctypes.byref(v)))
+        return v.value
+
+    def zero_grads(self):
+        check(lib().tg3_cnn_zero_grads(self.h))
+
+    def adam(self, lr: float):
+        check(lib().tg3_cnn_adam(self.h, lr))
+
+    def close(self):
+        if self.h:
+            lib().tg3_cnn_destroy(self.h)
             self.h = None
 
     def __del__(self):
