@@ -660,6 +660,199 @@ def run_uneven(args, rank, world, local_rank):
     return res
 
 
+LEARNED = dict(box=128, pixel_size=1.4, n_blobs=120, sigma_a=(1.5, 3.0), radius_px=40.0,
+               n_maps=16, n_train_maps=12, rU=32, pf=2, shift=3.0, snr=0.05,
+               n_rot=256, n_trans=25)
+
+
+def run_learned(args, rank, world, local_rank):
+    """Learned proposal: 16 random 128^3 blob maps (120 blobs, 1.4 A/px), 12 for
+    training pairs and 4 held out.  The pose network trains on the GPU (its own
+    kernels) on (image, true pose) pairs of the 12 training maps, then seeds
+    256 rotations x 25 translations per particle, every one rescored by the
+    exact likelihood (split-bf16 local phase).  Compared with the plain
+    global search (6,912 x 49 hypotheses) on held-out particles of the
+    training maps and on particles of the 4 held-out maps.  Cutoff 32
+    (K = 1,563: the global scan's scaling, r = box / 4)."""
+    import torch
+    import tg3
+    from tg3 import learned, synth
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    L = LEARNED
+    box, px, pf, rU = L["box"], L["pixel_size"], L["pf"], L["rU"]
+    rng = np.random.default_rng(4000 + 97 * rank)
+    maps = [synth.blob_map(rng, L["n_blobs"], L["sigma_a"], px, L["radius_px"])
+            for _ in range(L["n_maps"])]
+    rL = synth.config_rL(box, px)
+    prec = tg3.SCORE_BF16X3 if args.precision == "bf16x3" else tg3.SCORE_FP32
+    nTr = L["n_train_maps"]
+    t0 = time.perf_counter()
+    # training pairs, generated in chunks (images stay on the device)
+    imgs, Rs, ts = [], [], []
+    chunk = 10000
+    for s0 in range(0, args.train_particles, chunk):
+        m = min(chunk, args.train_particles - s0)
+        ps = synth.particle_set(4100 + s0, maps[:nTr], np.arange(m) % nTr, box, px, rU, rL,
+                                L["shift"], args.learned_snr, device=dev)
+        imgs.append(ps.images)
+        Rs.append(synth.quat_to_mat(ps.quat_true).reshape(m, 9))
+        ts.append(ps.trans_true)
+    images = torch.cat(imgs)
+    Rstar = torch.as_tensor(np.concatenate(Rs)).to(dev)
+    tstar = torch.as_tensor(np.concatenate(ts)).to(dev)
+    gen_s = time.perf_counter() - t0
+    net = tg3.Cnn(local_rank, seed=4242)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    losses = learned.train(net, images, Rstar, tstar, args.epochs, 256, args.learned_lr, seed=7)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+    del images, Rstar, tstar
+    # the exact likelihood: one context with every map as a class
+    ctx = tg3.Context(local_rank)
+    for c, bm in enumerate(maps):
+        ctx.set_volume(c, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
+    quats_g = synth.global_rotations(4, 36)
+    mats_g = torch.as_tensor(synth.quat_to_mat(quats_g).reshape(-1, 9)).to(dev)
+    trans_g = torch.as_tensor(synth.global_translations(3, 1.0)).to(dev)
+    nRg, nTg = len(quats_g), int(trans_g.shape[0])
+
+    def evaluate(ps, name):
+        n = len(ps.cls)
+        ctx.set_pixels(ps.iCol, ps.iRow, box)
+        d = dict(dat=torch.as_tensor(ps.dat).to(dev), ctf=torch.as_tensor(ps.ctf).to(dev),
+                 sig=torch.as_tensor(ps.sigRcp).to(dev))
+        f64 = dict(dtype=torch.float64, device=dev)
+        stream = torch.cuda.ExternalStream(ctx.stream)
+        ev = lambda: torch.cuda.Event(enable_timing=True)
+        # -- plain global search, per map
+        og = dict(wC=torch.empty(n, **f64), wR=torch.empty((n, nRg), **f64),
+                  wT=torch.empty((n, nTg), **f64), base=torch.empty(n, **f64))
+        pR = torch.full((nRg,), 1.0 / nRg, **f64)
+        pT = torch.full((nTg,), 1.0 / nTg, **f64)
+        groups = [np.nonzero(ps.cls == c)[0] for c in np.unique(ps.cls)]
+        sub = {}
+        for g in groups:
+            idx = torch.as_tensor(g, device=dev)
+            sub[int(ps.cls[g[0]])] = (idx, {k: v[idx].contiguous() for k, v in d.items()},
+                                      {k: v[idx].contiguous() for k, v in og.items()})
+
+        def global_all():
+            # the plain method: FP32 global search
+            for c, (idx, dd, oo) in sub.items():
+                ctx.global_scan(c, len(idx), nRg, nTg, dd["dat"], dd["ctf"], dd["sig"], mats_g,
+                                trans_g, pR, pT, oo["wC"], oo["wR"], oo["wT"], oo["base"], None,
+                                tg3.SCORE_FP32)
+
+        global_all()
+        ctx.sync()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        global_all()
+        e1.record(stream)
+        e1.synchronize()
+        ctx.sync()
+        tg_ms = e0.elapsed_time(e1)
+        bestg, baseg = np.empty(n, np.int64), np.empty(n)
+        for c, (idx, dd, oo) in sub.items():
+            g = idx.cpu().numpy()
+            bestg[g] = oo["wR"].argmax(1).cpu().numpy()
+            baseg[g] = oo["base"].cpu().numpy()
+        err_g = learned.angle_deg(quats_g[bestg], ps.quat_true)
+        # -- learned proposal: network, proposals, exact rescoring
+        nR, nT = L["n_rot"], L["n_trans"]
+        out = torch.empty((n, tg3.Cnn.N_OUT), dtype=torch.float32, device=dev)
+        cls_d = torch.as_tensor(ps.cls.astype(np.int32)).to(dev)
+        ol = dict(wC=torch.empty(n, **f64), wR=torch.empty((n, nR), **f64),
+                  wT=torch.empty((n, nT), **f64), base=torch.empty(n, **f64),
+                  dvp=torch.empty((n, nR, nT), dtype=torch.float32, device=dev))
+
+        qd = torch.empty((n, nR, 4), **f64)
+        td = torch.empty((n, nT, 2), **f64)
+
+        def learned_all():
+            # network, proposals and exact rescoring, all on the device
+            net.forward(ps.images, out)
+            tg3.Cnn.propose(out, nR, nT, 99, qd, td, ctx.stream)
+            ctx.local_phase(n, nR, nT, d["dat"], d["ctf"], d["sig"], qd, td,
+                            torch.full((n, nR), 1.0 / nR, **f64), torch.full((n, nT), 1.0 / nT, **f64),
+                            torch.ones(n, **f64), cls_d, ol["wC"], ol["wR"], ol["wT"], ol["base"],
+                            ol["dvp"], prec)
+            ctx.sync()
+            return qd.cpu().numpy()
+
+        learned_all()
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        q = learned_all()
+        torch.cuda.synchronize()
+        tl_ms = (time.perf_counter() - ta) * 1e3
+        bestl = ol["wR"].argmax(1).cpu().numpy()
+        err_l = learned.angle_deg(q[np.arange(n), bestl], ps.quat_true)
+        basel = ol["base"].cpu().numpy()
+        dv = ol["dvp"].reshape(n, -1).cpu().numpy().astype(np.float64)
+        med = np.median(dv, 1)
+        mad = np.median(np.abs(dv - med[:, None]), 1) + 1e-12
+        peak = (dv.max(1) - med) / (1.4826 * mad)
+        return dict(n=n, tg_ms=tg_ms, tl_ms=tl_ms, err_g=err_g, err_l=err_l, peak=peak,
+                    better=basel >= baseg)
+
+    nSeen = args.eval_particles_seen
+    nUn = args.eval_particles_unseen
+    seen = synth.particle_set(5001, maps[:nTr], np.arange(nSeen) % nTr, box, px, rU, rL,
+                              L["shift"], args.learned_snr, device=dev)
+    unseen = synth.particle_set(5002, maps[nTr:], np.arange(nUn) % (L["n_maps"] - nTr), box, px,
+                                rU, rL, L["shift"], args.learned_snr, device=dev)
+    unseen.cls = unseen.cls + nTr
+    rs = evaluate(seen, "seen")
+    ru = evaluate(unseen, "unseen")
+    # fallback rule: the proposal's peak score (best minus median of its rescored
+    # hypotheses, in robust deviations) below a threshold calibrated on the
+    # held-out particles of the training maps: 95 % of proposals within 10
+    # degrees of the truth pass
+    good = rs["err_l"] < 10.0
+    tau = float(np.quantile(rs["peak"][good], 0.05)) if good.any() else float("inf")
+
+    def report(r):
+        fb = r["peak"] < tau
+        err_c = np.where(fb, r["err_g"], r["err_l"])
+        t_c = r["tl_ms"] + fb.mean() * r["tg_ms"]
+        return {"particles": r["n"],
+                "plain_fp32_global_search": {"particles_per_s": round(r["n"] / (r["tg_ms"] * 1e-3), 1),
+                                  "median_error_deg": round(float(np.median(r["err_g"])), 3)},
+                "proposal_only": {"particles_per_s": round(r["n"] / (r["tl_ms"] * 1e-3), 1),
+                                  "median_error_deg": round(float(np.median(r["err_l"])), 3),
+                                  "within_10deg": round(float(np.mean(r["err_l"] < 10)), 4)},
+                "proposal_with_fallback": {
+                    "particles_per_s": round(r["n"] / (t_c * 1e-3), 1),
+                    "median_error_deg": round(float(np.median(err_c)), 3),
+                    "fallback_fraction": round(float(fb.mean()), 4)},
+                "proposal_at_least_as_likely_as_global": round(float(r["better"].mean()), 4),
+                "speedup_with_fallback": round(r["tg_ms"] / t_c, 2)}
+
+    res = {"metric": "learned proposal + split-bf16 rescoring vs plain FP32 global search, box 128",
+           "value": report(ru)["proposal_with_fallback"]["particles_per_s"], "unit": UNIT,
+           "higher_is_better": True, "precision": args.precision,
+           "config": {"workload": "16 blob maps 128^3 (120 blobs, 1.4 A/px): 12 training maps, "
+                                  "4 held out; proposal 256 rotations x 25 translations rescored "
+                                  "exactly, fallback 6,912 x 49 global search; cutoff 32, K = "
+                                  + str(len(seen.iCol)),
+                      "train_particles": args.train_particles, "epochs": args.epochs,
+                      "snr": args.learned_snr, "learning_rate": args.learned_lr,
+                      "eval_particles": {"seen_maps": nSeen, "held_out_maps": nUn},
+                      "labels": "true poses of the synthetic particles"},
+           "training": {"generate_s": round(gen_s, 1), "train_s": round(train_s, 1),
+                        "loss_per_epoch": [round(x, 4) for x in losses],
+                        "images_per_s": round(args.train_particles * args.epochs / train_s, 1)},
+           "fallback_threshold_peak": round(tau, 3),
+           "held_out_particles_of_training_maps": report(rs),
+           "held_out_maps": report(ru)}
+    net.close()
+    ctx.close()
+    return res
+
+
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per particle of a
 # launch, box 256 local workload: one 1-pass ncu capture of a 64-particle
 # launch (k_project 13.36 GB read + 5.09 GB written; k_gemm_bf16x3 5.62 GB +
@@ -853,7 +1046,14 @@ def main():
                     help="split-bf16 path through the fused projection + tcgen05 kernel")
     ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
     ap.add_argument("--workload", default="local256",
-                    choices=["local256", "local256c3", "global64", "uneven192"])
+                    choices=["local256", "local256c3", "global64", "uneven192", "learned128"])
+    ap.add_argument("--train-particles", type=int, default=150000)
+    ap.add_argument("--epochs", type=int, default=6)
+    ap.add_argument("--learned-snr", type=float, default=1.0,
+                    help="noise level of the learned-proposal particles (signal / noise power)")
+    ap.add_argument("--learned-lr", type=float, default=2e-3)
+    ap.add_argument("--eval-particles-seen", type=int, default=1200)
+    ap.add_argument("--eval-particles-unseen", type=int, default=2000)
     ap.add_argument("--batch-uneven", type=int, default=4096,
                     help="particles per ragged plan (uneven192)")
     ap.add_argument("--per-particle-sample", type=int, default=256,
@@ -867,6 +1067,8 @@ def main():
         res = run_global(args, rank, world, local)
     elif args.workload == "uneven192":
         res = run_uneven(args, rank, world, local)
+    elif args.workload == "learned128":
+        res = run_learned(args, rank, world, local)
     else:
         res = run_tg3(args, rank, world, local)
     if rank == 0 and res is not None:

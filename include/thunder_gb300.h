@@ -289,6 +289,14 @@ int tg3_cnn_loss(tg3_cnn* net, const float* img, int n, const double* Rstar,
                  const double* tstar, int accumulate_grads, double* loss);
 int tg3_cnn_zero_grads(tg3_cnn* net);
 int tg3_cnn_adam(tg3_cnn* net, float lr);
+/* Hypotheses from network outputs out [n][68] (device): quat [n][nRot][4]
+ * (the 8 component rotations, then rotations drawn by the mixture weights,
+ * each turned by a rotation vector ~ N(0, I / kappa)) and trans [n][nTrans][2]
+ * ~ N(mu, exp(log-variance)), the first the mean; counter-based random
+ * numbers from `seed`.  8 <= nRot <= 512, nTrans <= 512; asynchronous on
+ * `stream` (a cudaStream_t, NULL for the default stream). */
+int tg3_cnn_propose(const float* out, int n, int nRot, int nTrans, unsigned long long seed,
+                    double* quat, double* trans, void* stream);
 
 /* Global scan of nImg images over one shared set of nR rotations and nT
  * translations, for the context's class-`cls` volume: the scan of

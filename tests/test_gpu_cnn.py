@@ -79,3 +79,24 @@ def test_adam_lowers_the_loss(net):
         net.adam(1e-3)
     last = net.loss(im, Rd, td, grads=False)
     assert last < 0.8 * first, (first, last)
+
+
+def test_proposals_follow_the_outputs():
+    from tg3 import learned
+    rng = np.random.default_rng(5)
+    n, nR, nT = 6, 64, 9
+    out = rng.standard_normal((n, tg3.Cnn.N_OUT)).astype(np.float32)
+    od = torch.as_tensor(out).to(DEV)
+    q = torch.empty((n, nR, 4), dtype=torch.float64, device=DEV)
+    t = torch.empty((n, nT, 2), dtype=torch.float64, device=DEV)
+    tg3.Cnn.propose(od, nR, nT, 11, q, t)
+    torch.cuda.synchronize()
+    q, t = q.cpu().numpy(), t.cpu().numpy()
+    R, kap, w, mu, sd = learned.decode(out)
+    centres = learned.mat_to_quat(R)
+    assert np.allclose(np.abs((q[:, :8] * centres).sum(-1)), 1.0, atol=1e-9)
+    assert np.allclose(np.linalg.norm(q, axis=-1), 1.0) and (q[..., 0] >= 0).all()
+    assert np.allclose(t[:, 0], mu)
+    # drawn rotations stay near their components (within a few 1/sqrt(kappa))
+    ang = np.radians(learned.angle_deg(q[:, 8:, None, :], centres[:, None, :, :])).min(-1)
+    assert (ang <= 6.0 / np.sqrt(kap.min(1))[:, None] + 1e-9).all()

@@ -393,6 +393,118 @@ __global__ void k_head_loss(const float* __restrict__ out, const double* __restr
     loss[n] = L;
 }
 
+// ------------------------------------------------------------- proposals ---
+__device__ inline uint64_t mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+// uniform in (0, 1) from a counter
+__device__ inline double u01(uint64_t seed, uint64_t a, uint64_t b)
+{
+    const uint64_t z = mix64(seed ^ mix64(a * 0x9E3779B97F4A7C15ull + b));
+    return ((z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+__device__ inline double normal(uint64_t seed, uint64_t a, uint64_t b)
+{
+    const double u1 = u01(seed, a, 2 * b), u2 = u01(seed, a, 2 * b + 1);
+    return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+// One CTA per particle: decode its 8 components, draw nRot rotations
+// (the 8 centres, then components by the mixture weights, each turned by a
+// rotation vector ~ N(0, I / kappa)) as quaternions (w >= 0), and nTrans
+// translations ~ N(mu, exp(lv)) (the first one the mean).
+__global__ void k_propose(const float* __restrict__ out, int nRot, int nTrans, uint64_t seed,
+                          double* __restrict__ quat, double* __restrict__ trans)
+{
+    __shared__ double Rk[kComp][9];
+    __shared__ double kap[kComp];
+    __shared__ double cdf[kComp];
+    const int l = blockIdx.x;
+    const float* o = out + (size_t)l * kOut;
+    if (threadIdx.x < kComp) {
+        const int k = threadIdx.x;
+        const float* q = o + k * 8;
+        const V3 a1 = v3(q[0], q[1], q[2]), a2 = v3(q[3], q[4], q[5]);
+        const V3 b1 = mul(a1, 1.0 / (sqrt(dot(a1, a1)) + 1e-12));
+        const V3 u2 = sub(a2, mul(b1, dot(b1, a2)));
+        const V3 b2 = mul(u2, 1.0 / (sqrt(dot(u2, u2)) + 1e-12));
+        const V3 b3 = cross(b1, b2);
+        // columns b1 b2 b3, row-major
+        const double m[9] = {b1.x, b2.x, b3.x, b1.y, b2.y, b3.y, b1.z, b2.z, b3.z};
+        for (int i = 0; i < 9; i++) Rk[k][i] = m[i];
+        const double raw = q[6];
+        kap[k] = (raw > 20 ? raw : log1p(exp(raw))) + 1e-3;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double mx = -1e300;
+        for (int k = 0; k < kComp; k++) mx = fmax(mx, (double)o[k * 8 + 7]);
+        double acc = 0;
+        for (int k = 0; k < kComp; k++) {
+            acc += exp((double)o[k * 8 + 7] - mx);
+            cdf[k] = acc;
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nRot; j += blockDim.x) {
+        int k = j;
+        double v[3] = {0, 0, 0};
+        if (j >= kComp) {
+            const double u = u01(seed, (uint64_t)l * 1024 + j, 7) * cdf[kComp - 1];
+            k = 0;
+            while (k < kComp - 1 && u > cdf[k]) k++;
+            const double s = 1.0 / sqrt(kap[k]);
+            for (int d = 0; d < 3; d++) v[d] = s * normal(seed, (uint64_t)l * 1024 + j, d);
+        }
+        // R = R_k exp([v]x) (Rodrigues)
+        const double th = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        double E[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        if (th > 0) {
+            const double kx = v[0] / th, ky = v[1] / th, kz = v[2] / th;
+            const double sn = sin(th), cs = 1 - cos(th);
+            const double K[9] = {0, -kz, ky, kz, 0, -kx, -ky, kx, 0};
+            double K2[9];
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 3; b++) {
+                    double t = 0;
+                    for (int c = 0; c < 3; c++) t += K[a * 3 + c] * K[c * 3 + b];
+                    K2[a * 3 + b] = t;
+                }
+            for (int i = 0; i < 9; i++) E[i] += sn * K[i] + cs * K2[i];
+        }
+        double M[9];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                double t = 0;
+                for (int c = 0; c < 3; c++) t += Rk[k][a * 3 + c] * E[c * 3 + b];
+                M[a * 3 + b] = t;
+            }
+        // matrix -> quaternion (w, x, y, z), w >= 0
+        const double tr = M[0] + M[4] + M[8];
+        double w = sqrt(fmax(0.0, 1 + tr)) / 2, x = sqrt(fmax(0.0, 1 + M[0] - M[4] - M[8])) / 2,
+               y = sqrt(fmax(0.0, 1 - M[0] + M[4] - M[8])) / 2,
+               z = sqrt(fmax(0.0, 1 - M[0] - M[4] + M[8])) / 2;
+        x = copysign(x, M[7] - M[5]);
+        y = copysign(y, M[2] - M[6]);
+        z = copysign(z, M[3] - M[1]);
+        const double nq = sqrt(w * w + x * x + y * y + z * z);
+        double* qo = quat + ((size_t)l * nRot + j) * 4;
+        qo[0] = w / nq;
+        qo[1] = x / nq;
+        qo[2] = y / nq;
+        qo[3] = z / nq;
+    }
+    for (int j = threadIdx.x; j < nTrans; j += blockDim.x)
+        for (int d = 0; d < 2; d++) {
+            const double mu = o[64 + d], sd = exp(0.5 * (double)o[66 + d]);
+            trans[((size_t)l * nTrans + j) * 2 + d] =
+                j == 0 ? mu : mu + sd * normal(seed, (uint64_t)l * 1024 + 512 + j, d);
+        }
+}
+
 __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ v, size_t n, float lr, float b1, float b2, float c1,
                        float c2, float eps)
@@ -692,5 +804,17 @@ extern "C" int tg3_cnn_set_bf16(tg3_cnn* net, int enable)
 {
     if (!net) return fail(TG3_ERR_ARG, "null network");
     net->roundW = enable != 0;
+    return TG3_OK;
+}
+
+extern "C" int tg3_cnn_propose(const float* out, int n, int nRot, int nTrans,
+                               unsigned long long seed, double* quat, double* trans, void* stream)
+{
+    if (!out || !quat || !trans || n <= 0 || nRot < kComp || nRot > 512 || nTrans <= 0 ||
+        nTrans > 512)
+        return fail(TG3_ERR_ARG, "bad proposal arguments (8 <= nRot <= 512, nTrans <= 512)");
+    k_propose<<<n, 256, 0, static_cast<cudaStream_t>(stream)>>>(out, nRot, nTrans, seed, quat,
+                                                                 trans);
+    TG3_LAUNCH_CHECK("proposals");
     return TG3_OK;
 }

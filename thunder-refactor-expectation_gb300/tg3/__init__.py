@@ -33,7 +33,7 @@ EXPORTS = [
     "tg3_ragged_plan_create", "tg3_ragged_plan_run", "tg3_ragged_plan_info",
     "tg3_ragged_plan_destroy", "tg3_cnn_create", "tg3_cnn_destroy", "tg3_cnn_param_count",
     "tg3_cnn_params", "tg3_cnn_grads", "tg3_cnn_set_bf16", "tg3_cnn_forward", "tg3_cnn_loss",
-    "tg3_cnn_zero_grads", "tg3_cnn_adam",
+    "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
@@ -110,6 +110,7 @@ def lib():
             "tg3_cnn_loss": ([_P, _P, _I, _P, _P, _I, _P], _I),
             "tg3_cnn_zero_grads": ([_P], _I),
             "tg3_cnn_adam": ([_P, ctypes.c_float], _I),
+            "tg3_cnn_propose": ([_P, _I, _I, _I, ctypes.c_ulonglong, _P, _P, _P], _I),
             "tg3_ctx_stage_times": ([_P, _P, _P, _I], _I),
             "tg3_noalloc_scratch_bytes": ([], ctypes.c_size_t),
             "tg3_global_scan_d": ([_P, _I, _I, _I, _I] + [_P] * 12 + [_I], _I),
@@ -354,6 +355,13 @@ class Cnn:
 
     def zero_grads(self):
         check(lib().tg3_cnn_zero_grads(self.h))
+
+    @staticmethod
+    def propose(out, n_rot, n_trans, seed, quat, trans, stream=None):
+        """Hypotheses from outputs (device tensors; quat [n][n_rot][4], trans
+        [n][n_trans][2] float64), asynchronous on `stream` (an int handle)."""
+        check(lib().tg3_cnn_propose(ptr(out), out.shape[0], n_rot, n_trans, seed, ptr(quat),
+                                    ptr(trans), stream))
 
     def adam(self, lr: float):
         check(lib().tg3_cnn_adam(self.h, lr))

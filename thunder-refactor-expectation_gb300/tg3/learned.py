@@ -1,0 +1,122 @@
+"""Learned proposal: training the pose network and drawing hypotheses from it.
+
+The network (tg3.Cnn, all kernels the library's own) maps a particle's
+64 x 64 image to a mixture of 8 rotations (6-D representation, concentration,
+weight) and a Gaussian shift.  Its proposals seed the particle filter in
+place of the uniform global initialisation: every proposed hypothesis is
+rescored by the exact likelihood (tg3_local_phase_d), and the plain global
+search remains the fallback.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import synth
+
+N_COMP = 8
+
+
+def _softplus(x):
+    return np.where(x > 20, x, np.log1p(np.exp(np.minimum(x, 20))))
+
+
+def decode(out: np.ndarray):
+    """Network outputs [n][68] -> rotations [n][8][3][3], concentrations
+    [n][8], weights [n][8], shift mean [n][2], shift deviation [n][2]."""
+    n = out.shape[0]
+    comp = out[:, :64].astype(np.float64).reshape(n, N_COMP, 8)
+    a1, a2 = comp[..., 0:3], comp[..., 3:6]
+    b1 = a1 / (np.linalg.norm(a1, axis=-1, keepdims=True) + 1e-12)
+    u2 = a2 - (b1 * a2).sum(-1, keepdims=True) * b1
+    b2 = u2 / (np.linalg.norm(u2, axis=-1, keepdims=True) + 1e-12)
+    R = np.stack([b1, b2, np.cross(b1, b2)], -1)      # columns b1 b2 b3
+    kap = _softplus(comp[..., 6]) + 1e-3
+    lg = comp[..., 7]
+    w = np.exp(lg - lg.max(1, keepdims=True))
+    w /= w.sum(1, keepdims=True)
+    mu = out[:, 64:66].astype(np.float64)
+    sd = np.exp(0.5 * out[:, 66:68].astype(np.float64))
+    return R, kap, w, mu, sd
+
+
+def mat_to_quat(R: np.ndarray) -> np.ndarray:
+    """Rotation matrices [..., 3, 3] -> unit quaternions (w, x, y, z), w >= 0."""
+    m = R.reshape(-1, 3, 3)
+    tr = m[:, 0, 0] + m[:, 1, 1] + m[:, 2, 2]
+    q = np.empty((len(m), 4))
+    q[:, 0] = np.sqrt(np.maximum(0.0, 1 + tr)) / 2
+    q[:, 1] = np.sqrt(np.maximum(0.0, 1 + m[:, 0, 0] - m[:, 1, 1] - m[:, 2, 2])) / 2
+    q[:, 2] = np.sqrt(np.maximum(0.0, 1 - m[:, 0, 0] + m[:, 1, 1] - m[:, 2, 2])) / 2
+    q[:, 3] = np.sqrt(np.maximum(0.0, 1 - m[:, 0, 0] - m[:, 1, 1] + m[:, 2, 2])) / 2
+    q[:, 1] = np.copysign(q[:, 1], m[:, 2, 1] - m[:, 1, 2])
+    q[:, 2] = np.copysign(q[:, 2], m[:, 0, 2] - m[:, 2, 0])
+    q[:, 3] = np.copysign(q[:, 3], m[:, 1, 0] - m[:, 0, 1])
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    return q.reshape(R.shape[:-2] + (4,))
+
+
+def _axis_angle(v: np.ndarray) -> np.ndarray:
+    """Rotation vectors [..., 3] -> matrices [..., 3, 3] (Rodrigues)."""
+    th = np.linalg.norm(v, axis=-1, keepdims=True)
+    k = v / np.maximum(th, 1e-12)
+    K = np.zeros(v.shape[:-1] + (3, 3))
+    K[..., 0, 1], K[..., 0, 2], K[..., 1, 2] = -k[..., 2], k[..., 1], -k[..., 0]
+    K[..., 1, 0], K[..., 2, 0], K[..., 2, 1] = k[..., 2], -k[..., 1], k[..., 0]
+    th = th[..., None]
+    return np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * (K @ K)
+
+
+def propose(out: np.ndarray, n_rot: int, n_trans: int, rng: np.random.Generator):
+    """Hypotheses drawn from the network's outputs: quaternions [n][n_rot][4]
+    (component counts from the mixture weights, each sample the component's
+    rotation turned by a rotation vector ~ N(0, I / kappa)) and translations
+    [n][n_trans][2] ~ N(mu, sd^2).  The component centres are always kept."""
+    R, kap, w, mu, sd = decode(out)
+    n = len(out)
+    # component of every extra sample by inverse CDF of the mixture weights
+    cdf = np.cumsum(w, 1)
+    u = rng.random((n, n_rot - N_COMP)) * cdf[:, -1:]
+    c = np.minimum((u[:, :, None] > cdf[:, None, :]).sum(-1), N_COMP - 1)
+    comp = np.concatenate([np.broadcast_to(np.arange(N_COMP), (n, N_COMP)), c], 1)
+    Rc = R[np.arange(n)[:, None], comp]                      # [n][n_rot][3][3]
+    v = rng.standard_normal((n, n_rot, 3)) / np.sqrt(kap[np.arange(n)[:, None], comp])[..., None]
+    v[:, :N_COMP] = 0.0
+    Rs = Rc @ _axis_angle(v)
+    quat = mat_to_quat(Rs)
+    trans = mu[:, None, :] + sd[:, None, :] * rng.standard_normal((n, n_trans, 2))
+    trans[:, 0] = mu
+    return np.ascontiguousarray(quat), np.ascontiguousarray(trans)
+
+
+def angle_deg(q1: np.ndarray, q2: np.ndarray) -> np.ndarray:
+    d = np.abs((q1 * q2).sum(-1)).clip(0.0, 1.0)
+    return np.degrees(2.0 * np.arccos(d))
+
+
+def train(net, images, Rstar, tstar, epochs: int, batch: int, lr: float, seed: int = 0,
+          log=None):
+    """Minibatch Adam on (image, true pose) pairs: images [n][64][64],
+    Rstar [n][9], tstar [n][2] (device tensors).  Cosine-decayed learning
+    rate; returns the mean loss of every epoch."""
+    import torch
+    n = images.shape[0]
+    rng = np.random.default_rng(seed)
+    steps = epochs * (n // batch)
+    k = 0
+    losses = []
+    for e in range(epochs):
+        order = torch.as_tensor(rng.permutation(n), device=images.device)
+        tot = 0.0
+        for s in range(n // batch):
+            idx = order[s * batch:(s + 1) * batch]
+            net.zero_grads()
+            tot += net.loss(images[idx].contiguous(), Rstar[idx].contiguous(),
+                            tstar[idx].contiguous(), grads=True)
+            net.adam(lr * 0.5 * (1 + math.cos(math.pi * k / max(steps, 1))))
+            k += 1
+        losses.append(tot / max(n // batch, 1))
+        if log:
+            log(f"epoch {e}: loss {losses[-1]:.4f}")
+    return losses

@@ -374,6 +374,72 @@ def make_stack(seed: int, maps, box: int, pixel_size: float, pf: int,
 # --------------------------------------------------------------------------
 # named workloads
 # --------------------------------------------------------------------------
+@dataclass
+class ParticleSet:
+    images: torch.Tensor       # (n, img, img) float32, per-image normalised (device)
+    dat: np.ndarray            # (n, K) complex64: the same data at the cutoff's pixels
+    ctf: np.ndarray            # (n, K) float32
+    sigRcp: np.ndarray         # (n, K) float32
+    iCol: np.ndarray
+    iRow: np.ndarray
+    quat_true: np.ndarray      # (n, 4)
+    trans_true: np.ndarray     # (n, 2) pixels at the full box
+    cls: np.ndarray            # (n,) map of every particle
+
+
+def particle_set(seed: int, maps, cls, box: int, pixel_size: float, rU: float, rL: float,
+                 shift_range: float, snr: float, img: int = 64, device="cpu",
+                 chunk: int = 512) -> ParticleSet:
+    """Particles of several maps (particle l shows maps[cls[l]]) at Haar-uniform
+    poses and U(-shift_range, shift_range) shifts, with CTF and white noise at
+    `snr` (signal / noise power over the band-limited grid).
+
+    The data of a particle is its transform on the rfft grid of an img x img
+    image at the full box's frequencies (|k| <= img / 2, i.e. the box
+    band-limited and downsampled by box / img).  Its real-space image (the
+    network's input, centred, normalised to zero mean and unit deviation) and
+    its values at the pixels of cutoff rU (the likelihood's input) come from
+    that one noisy transform, so both see the same particle."""
+    rng = np.random.default_rng(seed)
+    cls = np.asarray(cls)
+    n = len(cls)
+    q = haar_quaternions(rng, n)
+    t = rng.uniform(-shift_range, shift_range, (n, 2))
+    attr = ctf_attrs(rng, n)
+    h = img // 2
+    jj = np.concatenate([np.arange(0, h), np.arange(-h, 0)])     # FFT row order
+    ii = np.arange(0, h + 1)
+    J, I = np.meshgrid(jj, ii, indexing="ij")
+    gi, gj = I.ravel(), J.ravel()                                  # (img (h + 1),)
+    ctf_g = ctf_values(attr, pixel_size, box, gi, gj)              # (n, G)
+    R = quat_to_mat(q)
+    k2 = np.stack([gi, gj, np.zeros_like(gi)], 0).astype(np.float32) / box
+    sig = np.empty((n, len(gi)), np.complex64)
+    for c in range(len(maps)):
+        sel = np.nonzero(cls == c)[0]
+        for s in range(0, len(sel), chunk):
+            ids = sel[s:s + chunk]
+            f = torch.as_tensor(np.einsum("nij,jk->nki", R[ids].astype(np.float32), k2), device=device)
+            sig[ids] = blob_ft(maps[c], f).cpu().numpy()
+    sig *= ctf_g.astype(np.float32)
+    sig *= np.exp(-2j * math.pi * (np.outer(t[:, 0] / box, gi) + np.outer(t[:, 1] / box, gj))).astype(np.complex64)
+    p_sig = float(np.mean(np.abs(sig) ** 2))
+    s2 = p_sig / snr / 2.0
+    noise = (rng.standard_normal(sig.shape) + 1j * rng.standard_normal(sig.shape)) * math.sqrt(s2)
+    data = (sig + noise.astype(np.complex64)).astype(np.complex64)
+    grid = torch.as_tensor(data.reshape(n, img, h + 1), device=device)
+    ims = torch.fft.irfft2(grid, s=(img, img))
+    ims = torch.fft.fftshift(ims, dim=(-2, -1))
+    ims = ims - ims.mean(dim=(-2, -1), keepdim=True)
+    ims = ims / ims.std(dim=(-2, -1), keepdim=True)
+    iCol, iRow, _, _ = pixel_index(box, rU, rL)
+    col = (np.where(iRow >= 0, iRow, iRow + img)) * (h + 1) + iCol   # grid index of each pixel
+    return ParticleSet(images=ims.float().contiguous(), dat=np.ascontiguousarray(data[:, col]),
+                       ctf=np.ascontiguousarray(ctf_g[:, col].astype(np.float32)),
+                       sigRcp=np.full((n, len(iCol)), -1.0 / (2.0 * s2), np.float32),
+                       iCol=iCol, iRow=iRow, quat_true=q, trans_true=t, cls=cls)
+
+
 def global_translations(half: int = 3, step: float = 1.0) -> np.ndarray:
     """(2 half + 1)^2 grid of shifts, `step` pixels apart (7 x 7 = 49)."""
     g = np.arange(-half, half + 1) * step
