@@ -189,7 +189,7 @@ def run_tg3(args, rank, world, local_rank):
     dev = f"cuda:{local_rank}"
     nP = args.batch
     W0 = WORKLOAD_C3 if args.workload == "local256c3" else WORKLOAD
-    W, vols, st, batches = make_workload(torch, dev, nP, args.batches, 1000 + 1 + 97 * rank,
+    W, vols, st, batches = make_workload(torch, dev, nP, args.batches, rank_seed(1001, rank),
                                          box=args.box, W0=W0)
     nR, nT, K = W["nR"], W["nT"], st.K
     ctx = tg3.Context(local_rank)
@@ -390,7 +390,7 @@ def run_tg3(args, rank, world, local_rank):
     launches_per_step = 8 if fused else 9
     ins_ms = ins_stage[0] / max(ins_stage[1], 1)
     ins_bytes = 705.5 * K * nP             # 16 B in + 28.7 voxel updates x 24 B per pixel
-    value = nP * args.steps * world / (ms * 1e-3)
+    value = job_rate(nP * args.steps, ms, world)
     res = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
@@ -408,7 +408,7 @@ def run_tg3(args, rank, world, local_rank):
                    "l2": "inputs larger than L2: the projection bank alone is "
                          f"{nP * nR * ctx_kp(K) * 4 / 1e9:.1f} GB per step"},
         "clocks": clocks,
-        "e2e": {"value": round(nP * args.e2e_steps * world / e2e_s, 2), "unit": UNIT,
+        "e2e": {"value": round(job_rate(nP * args.e2e_steps, e2e_s * 1e3, world), 2), "unit": UNIT,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "wall_s": round(e2e_s, 3)},
         "gpu_launches": launches_per_step * args.steps,
@@ -427,7 +427,7 @@ def run_tg3(args, rank, world, local_rank):
     }
     if plain is not None:
         ms_p, stages_p, clocks_p = plain
-        v_p = nP * args.steps * world / (ms_p * 1e-3)
+        v_p = job_rate(nP * args.steps, ms_p, world)
         res["plain_fp32"] = {"value": round(v_p, 2), "ms_per_step": round(ms_p / args.steps, 4),
                              "stages": {k: round(v[0] / max(v[1], 1), 4)
                                         for k, v in stages_p.items() if v[1]},
@@ -450,10 +450,10 @@ def run_global(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = f"cuda:{local_rank}"
     box, px, pf, rU, n = 64, 1.5, 2, 16, args.global_particles
-    rng = np.random.default_rng(1000 + 97 * rank)
+    rng = np.random.default_rng(rank_seed(1000, rank))
     bm = synth.blob_map(rng, 40, (2.0, 4.0), px, 20.0)
     vol = synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32)
-    st = synth.make_stack(1001 + 97 * rank, [bm], box, px, pf, rU, synth.config_rL(box, px), n,
+    st = synth.make_stack(rank_seed(1001, rank), [bm], box, px, pf, rU, synth.config_rL(box, px), n,
                           3.0, 0.05, device=dev)
     quats = synth.global_rotations(4, 36)
     mats = torch.as_tensor(synth.quat_to_mat(quats).reshape(-1, 9)).to(dev)
@@ -486,21 +486,24 @@ def run_global(args, rank, world, local_rank):
     ctx.stage_times(reset=True)
     stream = torch.cuda.ExternalStream(ctx.stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
     e1.synchronize()
+    barrier(world)
     clocks = clk.stop()
     stages = ctx.stage_times(reset=True)
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = reduce_max(world, e0.elapsed_time(e1)) / args.steps
     cross = stages["cross"][0] / max(stages["cross"][1], 1)
     flop = 4.0 * K * nR * nT * n
     hbm, bf16, kind = peaks()
     res = {"metric": "global scan particles/s, box 64, 6912 rotations x 49 translations, K=375",
-           "value": round(n / (ms * 1e-3), 1), "unit": UNIT, "ms_per_step": round(ms, 3),
+           "value": round(job_rate(n, ms, world), 1), "unit": UNIT, "ms_per_step": round(ms, 3),
+           "n_gpus": world, "scaling": "weak",
            "particles": n, "precision": args.precision, "clocks": clocks,
-           "hypotheses_per_s": round(n * nR * nT / (ms * 1e-3), 1),
+           "hypotheses_per_s": round(job_rate(n * nR * nT, ms, world), 1),
            "stages": {k: round(v[0] / max(v[1], 1), 4) for k, v in stages.items() if v[1]},
            "cross_term": {"achieved_tflops": round(flop / (cross * 1e-3) / 1e12, 1),
                           "note": "algorithmic 4 K FLOP per hypothesis; the stage also "
@@ -529,7 +532,7 @@ def run_uneven(args, rank, world, local_rank):
     dev = f"cuda:{local_rank}"
     U = UNEVEN
     nP = args.batch_uneven
-    rng = np.random.default_rng(3000 + 97 * rank)
+    rng = np.random.default_rng(rank_seed(3000, rank))
     box, px, pf = U["box"], U["pixel_size"], U["pf"]
     nC = len(U["cutoffs"])
     maps = [synth.blob_map(rng, U["n_blobs"], U["sigma_a"], px, U["radius_px"]) for _ in range(nC)]
@@ -545,7 +548,7 @@ def run_uneven(args, rank, world, local_rank):
     stacks, Ks = [], []
     for c, rU in enumerate(U["cutoffs"]):
         n_c = int(np.sum(cls == c))
-        st = synth.make_stack(3100 + c + 97 * rank, [maps[c]], box, px, pf, rU, rL, n_c,
+        st = synth.make_stack(rank_seed(3100 + c, rank), [maps[c]], box, px, pf, rU, rL, n_c,
                               U["shift"], U["snr"], device=dev)
         ctx.set_pixels_slot(c, st.iCol, st.iRow, box)
         stacks.append(st)
@@ -589,14 +592,16 @@ def run_uneven(args, rank, world, local_rank):
     clk = ClockSampler(local_rank)
     clk.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
     e0.record(stream)
     for _ in range(args.steps):
         plan.run()
     e1.record(stream)
     e1.synchronize()
+    barrier(world)
     clocks = clk.stop()
     ctx.sync()
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = reduce_max(world, e0.elapsed_time(e1)) / args.steps
     # the same particles one at a time (local phase + two resamplings each)
     ns = min(nP, args.per_particle_sample)
     pref = dict(po=np.concatenate([[0], np.cumsum([Ks[c] for c in cls])]),
@@ -638,7 +643,8 @@ def run_uneven(args, rank, world, local_rank):
     hyps = float(np.sum(nR.astype(np.float64) * nT))
     flop = 4.0 * float(np.sum(nR.astype(np.float64) * nT * np.array(Ks)[cls]))
     res = {"metric": "uneven-batch E-step particles/s, box 192, 4 classes, ragged hypothesis sets",
-           "value": round(nP / (ms * 1e-3), 1), "unit": UNIT, "ms_per_step": round(ms, 3),
+           "value": round(job_rate(nP, ms, world), 1), "unit": UNIT, "ms_per_step": round(ms, 3),
+           "n_gpus": world, "scaling": "weak",
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
            "precision": args.precision, "clocks": clocks,
            "config": {"workload": "ragged plan: 4 classes, cutoffs 40/56/72/96 (K = "
@@ -647,9 +653,9 @@ def run_uneven(args, rank, world, local_rank):
                       "particles_per_step": nP, "rotations_total": R, "translations_total": T,
                       "plan_waves": waves, "wave_budget_bytes": budget,
                       "plan_create_s": round(plan_s, 2)},
-           "hypotheses_per_s": round(hyps / (ms * 1e-3), 1),
-           "samples_per_s": round(samples / (ms * 1e-3), 1),
-           "cross_term_tflops": round(flop / (ms * 1e-3) / 1e12, 1),
+           "hypotheses_per_s": round(job_rate(hyps, ms, world), 1),
+           "samples_per_s": round(job_rate(samples, ms, world), 1),
+           "cross_term_tflops": round(job_rate(flop, ms, world) / 1e12, 1),
            "per_particle_launches": {
                "value": round(nP / (pp_batch_ms * 1e-3), 1), "unit": UNIT,
                "sample": f"first {ns} particles one at a time (local phase + 2 resamplings "
@@ -681,7 +687,7 @@ def run_learned(args, rank, world, local_rank):
     dev = f"cuda:{local_rank}"
     L = LEARNED
     box, px, pf, rU = L["box"], L["pixel_size"], L["pf"], L["rU"]
-    rng = np.random.default_rng(4000 + 97 * rank)
+    rng = np.random.default_rng(4000)
     maps = [synth.blob_map(rng, L["n_blobs"], L["sigma_a"], px, L["radius_px"])
             for _ in range(L["n_maps"])]
     rL = synth.config_rL(box, px)
@@ -753,7 +759,7 @@ def run_learned(args, rank, world, local_rank):
         e1.record(stream)
         e1.synchronize()
         ctx.sync()
-        tg_ms = e0.elapsed_time(e1)
+        tg_ms = reduce_max(world, e0.elapsed_time(e1))
         bestg, baseg = np.empty(n, np.int64), np.empty(n)
         for c, (idx, dd, oo) in sub.items():
             g = idx.cpu().numpy()
@@ -787,7 +793,7 @@ def run_learned(args, rank, world, local_rank):
         ta = time.perf_counter()
         q = learned_all()
         torch.cuda.synchronize()
-        tl_ms = (time.perf_counter() - ta) * 1e3
+        tl_ms = reduce_max(world, (time.perf_counter() - ta) * 1e3)
         bestl = ol["wR"].argmax(1).cpu().numpy()
         err_l = learned.angle_deg(q[np.arange(n), bestl], ps.quat_true)
         basel = ol["base"].cpu().numpy()
@@ -800,9 +806,9 @@ def run_learned(args, rank, world, local_rank):
 
     nSeen = args.eval_particles_seen
     nUn = args.eval_particles_unseen
-    seen = synth.particle_set(5001, maps[:nTr], np.arange(nSeen) % nTr, box, px, rU, rL,
+    seen = synth.particle_set(rank_seed(5001, rank), maps[:nTr], np.arange(nSeen) % nTr, box, px, rU, rL,
                               L["shift"], args.learned_snr, device=dev)
-    unseen = synth.particle_set(5002, maps[nTr:], np.arange(nUn) % (L["n_maps"] - nTr), box, px,
+    unseen = synth.particle_set(rank_seed(5002, rank), maps[nTr:], np.arange(nUn) % (L["n_maps"] - nTr), box, px,
                                 rU, rL, L["shift"], args.learned_snr, device=dev)
     unseen.cls = unseen.cls + nTr
     rs = evaluate(seen, "seen")
@@ -819,13 +825,13 @@ def run_learned(args, rank, world, local_rank):
         err_c = np.where(fb, r["err_g"], r["err_l"])
         t_c = r["tl_ms"] + fb.mean() * r["tg_ms"]
         return {"particles": r["n"],
-                "plain_fp32_global_search": {"particles_per_s": round(r["n"] / (r["tg_ms"] * 1e-3), 1),
+                "plain_fp32_global_search": {"particles_per_s": round(job_rate(r["n"], r["tg_ms"], world), 1),
                                   "median_error_deg": round(float(np.median(r["err_g"])), 3)},
-                "proposal_only": {"particles_per_s": round(r["n"] / (r["tl_ms"] * 1e-3), 1),
+                "proposal_only": {"particles_per_s": round(job_rate(r["n"], r["tl_ms"], world), 1),
                                   "median_error_deg": round(float(np.median(r["err_l"])), 3),
                                   "within_10deg": round(float(np.mean(r["err_l"] < 10)), 4)},
                 "proposal_with_fallback": {
-                    "particles_per_s": round(r["n"] / (t_c * 1e-3), 1),
+                    "particles_per_s": round(job_rate(r["n"], t_c, world), 1),
                     "median_error_deg": round(float(np.median(err_c)), 3),
                     "fallback_fraction": round(float(fb.mean()), 4)},
                 "proposal_at_least_as_likely_as_global": round(float(r["better"].mean()), 4),
@@ -833,6 +839,7 @@ def run_learned(args, rank, world, local_rank):
 
     res = {"metric": "learned proposal + split-bf16 rescoring vs plain FP32 global search, box 128",
            "value": report(ru)["proposal_with_fallback"]["particles_per_s"], "unit": UNIT,
+           "n_gpus": world, "scaling": "weak",
            "higher_is_better": True, "precision": args.precision,
            "config": {"workload": "16 blob maps 128^3 (120 blobs, 1.4 A/px): 12 training maps, "
                                   "4 held out; proposal 256 rotations x 25 translations rescored "
@@ -1024,6 +1031,18 @@ def reduce_max(world, x: float) -> float:
         _pg.all_reduce(t, op=_pg.ReduceOp.MAX)
         return float(t.item())
     return float(x)
+
+
+def rank_seed(base: int, rank: int) -> int:
+    """Seed of one rank's particles: every rank scores its own particles (the
+    E-step shards over particles with no exchange), so the sets differ."""
+    return base + 97 * rank
+
+
+def job_rate(units_per_rank: float, ms: float, world: int) -> float:
+    """Whole-job throughput (units/s): the units all ranks processed over the
+    slowest rank's time; `ms` is already the max over ranks."""
+    return units_per_rank * world / (ms * 1e-3)
 
 
 def main():
