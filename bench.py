@@ -280,18 +280,27 @@ def run_tg3(args, rank, world, local_rank):
     zero2 = torch.zeros((nP, 2), dtype=torch.float64, device=dev)
     ins_q = [b["quat"][:, 0, :].contiguous() for b in dbat]
     ins_t = [b["trans"][:, 0, :].contiguous() for b in dbat]
-    for i in range(2):
-        ctx.insert(nP, dbat[i % len(dbat)]["dat"], dbat[i % len(dbat)]["ctf"],
-                   ins_q[i % len(dbat)], ins_t[i % len(dbat)], zero2, ins_w, tg3.KERNEL_MKB)
-    ctx.sync()
-    ctx.set_timing(True)
-    ctx.stage_times(reset=True)
-    for i in range(args.steps):
-        ctx.insert(nP, dbat[i % len(dbat)]["dat"], dbat[i % len(dbat)]["ctf"],
-                   ins_q[i % len(dbat)], ins_t[i % len(dbat)], zero2, ins_w, tg3.KERNEL_MKB)
-    ins_stage = ctx.stage_times(reset=True)["insert"]
-    ctx.set_timing(False)
-    ctx.sync()
+
+    def time_insert(gather):
+        # pixel-order scatter form (the default) or the voxel gather form
+        ctx.set_option(tg3.OPT_INSERT_GATHER, gather)
+        for i in range(2):
+            ctx.insert(nP, dbat[i % len(dbat)]["dat"], dbat[i % len(dbat)]["ctf"],
+                       ins_q[i % len(dbat)], ins_t[i % len(dbat)], zero2, ins_w, tg3.KERNEL_MKB)
+        ctx.sync()
+        ctx.set_timing(True)
+        ctx.stage_times(reset=True)
+        for i in range(args.steps):
+            ctx.insert(nP, dbat[i % len(dbat)]["dat"], dbat[i % len(dbat)]["ctf"],
+                       ins_q[i % len(dbat)], ins_t[i % len(dbat)], zero2, ins_w, tg3.KERNEL_MKB)
+        stage = ctx.stage_times(reset=True)["insert"]
+        ctx.set_timing(False)
+        ctx.sync()
+        ctx.set_option(tg3.OPT_INSERT_GATHER, 0)
+        return stage
+
+    ins_stage = time_insert(0)
+    ins_gather = time_insert(1)
 
     # ---- end to end: host buffers, copies inside the timed region
     hbat = [pin(torch, b) for b in batches]
@@ -389,6 +398,7 @@ def run_tg3(args, rank, world, local_rank):
     # fused: descriptors + the fused kernel; else: projection, norm sum, cross term
     launches_per_step = 8 if fused else 9
     ins_ms = ins_stage[0] / max(ins_stage[1], 1)
+    ins_ga_ms = ins_gather[0] / max(ins_gather[1], 1)
     ins_bytes = 705.5 * K * nP             # 16 B in + 28.7 voxel updates x 24 B per pixel
     value = job_rate(nP * args.steps, ms, world)
     res = {
@@ -417,11 +427,17 @@ def run_tg3(args, rank, world, local_rank):
         "roofline_projection": None if fused else proj_roof(stages),
         "stages": {k: {"ms_per_launch": round(v[0] / max(v[1], 1), 4), "launches": v[1]}
                    for k, v in stages.items() if v[1]},
-        "insertion": {"kernel": "k_insert (MKB, a = 1.9, alpha = 15)", "particles": nP,
+        "insertion": {"kernel": "k_insert (MKB, a = 1.9, alpha = 15)",
+                      "particles": nP,
                       "ms_per_launch": round(ins_ms, 4),
                       "particles_per_s": round(nP / (ins_ms * 1e-3), 1),
                       "achieved_gbs": round(ins_bytes / (ins_ms * 1e-3) / 1e9, 1),
-                      "peak_gbs": hbm, "frac": round(ins_bytes / (ins_ms * 1e-3) / 1e9 / hbm, 4)},
+                      "peak_gbs": hbm, "frac": round(ins_bytes / (ins_ms * 1e-3) / 1e9 / hbm, 4),
+                      "algorithmic_bytes": "705.5 B per inserted pixel (16 B in + 28.73 "
+                                           "voxel updates x 24 B)",
+                      "gather_form": {"kernel": "k_insert_stage + k_insert_gather",
+                                      "ms_per_launch": round(ins_ga_ms, 4),
+                                      "particles_per_s": round(nP / (ins_ga_ms * 1e-3), 1)}},
         "hypotheses_per_s": round(value * nR * nT, 1),
         "pose": pose,
     }

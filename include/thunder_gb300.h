@@ -230,8 +230,14 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  *   slice straight into the tensor-core operand of one persistent kernel
  *   (projection + cross term fused, no slice bank in HBM); 0 keeps the
  *   two-kernel form (k_project writing the slice bank, then the GEMM), which
- *   is the faster of the two on GB300. */
-enum { TG3_OPT_FUSED = 0 };
+ *   is the faster of the two on GB300.
+ * TG3_OPT_INSERT_GATHER (default 0): 1 makes MKB insertion gather each voxel
+ *   of a slice's slab from its pixels and add it once (one atomic per voxel);
+ *   0 scatters every pixel's support voxels with one atomic each (the
+ *   reference's loop order), which is the faster of the two on GB300.  Both
+ *   give the same sums up to FP32 rounding order; a pixel list holding a pixel
+ *   twice always scatters. */
+enum { TG3_OPT_FUSED = 0, TG3_OPT_INSERT_GATHER = 1 };
 int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);
 

@@ -246,8 +246,10 @@ def test_resample_rejects_bad_permutation():
     assert st == tg3.ERR_ARG
 
 
-@pytest.mark.parametrize("kernel", [tg3.KERNEL_MKB, tg3.KERNEL_TRILINEAR])
-def test_insert(small, kernel):
+@pytest.mark.parametrize("kernel,gather", [(tg3.KERNEL_MKB, 0), (tg3.KERNEL_MKB, 1),
+                                           (tg3.KERNEL_TRILINEAR, 0)],
+                         ids=["mkb-scatter", "mkb-gather", "trilinear"])
+def test_insert(small, kernel, gather):
     rng = np.random.default_rng(23)
     st = small["st"]
     K, pf, box = st.K, small["pf"], small["box"]
@@ -262,6 +264,7 @@ def test_insert(small, kernel):
     c = tg3.Context(0)
     try:
         c.set_pixels(small["iCol"], small["iRow"], box)
+        c.set_option(tg3.OPT_INSERT_GATHER, gather)
         c.insert_begin(vdim, pf)
         O3D = torch.zeros(3, dtype=torch.float64, device=DEV)
         cnt = torch.zeros(1, dtype=torch.int32, device=DEV)

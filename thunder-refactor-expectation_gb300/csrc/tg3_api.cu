@@ -309,9 +309,11 @@ extern "C" int tg3_ctx_destroy(tg3_ctx* c)
     for (auto& b : c->ws) cudaFree(b.ptr);
     cudaFree(c->pxMain.iCol);
     cudaFree(c->pxMain.iRow);
+    cudaFree(c->pxMain.cellPix);
     for (auto& q : c->pxSlot) {
         cudaFree(q.iCol);
         cudaFree(q.iRow);
+        cudaFree(q.cellPix);
     }
     cudaFree(c->ins.acc);
     cudaFree(c->ins.tab);
@@ -388,10 +390,21 @@ static int upload_pixels(tg3_ctx* c, Pixels& px, const int* iCol, const int* iRo
 {
     if (!iCol || !iRow || K <= 0 || idim <= 0) return fail(TG3_ERR_ARG, "bad pixel list");
     double mr = 0;
+    int ma = 0;
     for (int p = 0; p < K; p++) {
         if (iCol[p] < 0 || std::abs(iCol[p]) > idim / 2 || std::abs(iRow[p]) > idim / 2)
             return fail(TG3_ERR_ARG, "pixel outside the half plane of the image");
         mr = std::max(mr, std::sqrt((double)iCol[p] * iCol[p] + (double)iRow[p] * iRow[p]));
+        ma = std::max(ma, std::max(iCol[p], std::abs(iRow[p])));
+    }
+    // the insertion gather's cell map; a pixel listed twice cannot share a cell
+    const size_t cells = (size_t)(ma + 1) * (2 * ma + 1);
+    std::vector<int> cell(cells, -1);
+    bool unique = true;
+    for (int p = 0; p < K && unique; p++) {
+        int& s = cell[(size_t)(iRow[p] + ma) * (ma + 1) + iCol[p]];
+        unique = s < 0;
+        s = p;
     }
     if (px.K != K) {
         TG3_CUDA(cudaStreamSynchronize(c->stream));
@@ -404,11 +417,25 @@ static int upload_pixels(tg3_ctx* c, Pixels& px, const int* iCol, const int* iRo
     }
     TG3_CUDA(cudaMemcpyAsync(px.iCol, iCol, sizeof(int) * K, cudaMemcpyHostToDevice, c->stream));
     TG3_CUDA(cudaMemcpyAsync(px.iRow, iRow, sizeof(int) * K, cudaMemcpyHostToDevice, c->stream));
+    if (unique) {
+        if (px.cells != cells) {
+            TG3_CUDA(cudaStreamSynchronize(c->stream));
+            cudaFree(px.cellPix);
+            px.cellPix = nullptr;
+            px.cells = 0;
+            TG3_CUDA(cudaMalloc(&px.cellPix, sizeof(int) * cells));
+            px.cells = cells;
+        }
+        TG3_CUDA(cudaMemcpyAsync(px.cellPix, cell.data(), sizeof(int) * cells,
+                                 cudaMemcpyHostToDevice, c->stream));
+    }
     TG3_CUDA(cudaStreamSynchronize(c->stream));
     px.K = K;
     px.Kp = (int)round_up(2 * (size_t)K, 64);
     px.idim = idim;
     px.maxRadius = mr;
+    px.maxAbs = ma;
+    px.unique = unique;
     return TG3_OK;
 }
 
@@ -663,11 +690,29 @@ static int insert_draws(tg3_ctx* c, int nDraws, int drawsPerImage, const float* 
     int st = check_geometry(c, c->ins.vdim, c->ins.pf, 2.0);
     if (st) return st;
     StageTimer tm(c, TG3_STAGE_INSERT);
+    if (kernel == TG3_KERNEL_MKB && c->insertGather && c->px.unique && c->px.cellPix) {
+        const size_t per = insert_draw_bytes(c->px.maxAbs);
+        const size_t bytes = std::max(per, std::min((size_t)nDraws * per, (size_t)96 << 20));
+        void* scratch = ws_get(c, WS_INSERT, bytes, &st);
+        if (st) return st;
+        TG3_CUDA(launch_insert_gather(c->ins.acc, c->ins.vdim, c->ins.tab, c->ins.tabNz,
+                                      c->ins.tabInvStep, nDraws, drawsPerImage,
+                                      reinterpret_cast<const float2*>(dat), ctf, quat, trans,
+                                      offset, w, c->px.cellPix, c->px.iCol, c->px.iRow,
+                                      c->px.K, c->ins.pf,
+                                      c->px.idim, c->px.maxAbs,
+                                      (float)(c->px.maxRadius * c->ins.pf), O3D, counter,
+                                      scratch, bytes, c->stream));
+        return TG3_OK;
+    }
+    float* params = static_cast<float*>(
+        ws_get(c, WS_INSERT, (size_t)nDraws * 16 * sizeof(float), &st));
+    if (st) return st;
     TG3_CUDA(launch_insert(c->ins.acc, c->ins.vdim, kernel, c->ins.tab, c->ins.tabNz,
                            c->ins.tabInvStep, nDraws, drawsPerImage,
                            reinterpret_cast<const float2*>(dat), ctf, quat, trans, offset, w,
                            c->px.iCol, c->px.iRow, c->px.K, c->ins.pf, c->px.idim, O3D,
-                           counter, c->stream));
+                           counter, params, c->stream));
     return TG3_OK;
 }
 
@@ -1141,8 +1186,9 @@ extern "C" int tg3_ctx_set_option(tg3_ctx* c, int option, int value)
 {
     int st = check_ctx(c);
     if (st) return st;
-    if (option != TG3_OPT_FUSED) return fail(TG3_ERR_ARG, "unknown option");
-    c->fused = value != 0;
+    if (option == TG3_OPT_FUSED) c->fused = value != 0;
+    else if (option == TG3_OPT_INSERT_GATHER) c->insertGather = value != 0;
+    else return fail(TG3_ERR_ARG, "unknown option");
     return TG3_OK;
 }
 

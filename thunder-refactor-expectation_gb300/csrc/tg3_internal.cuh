@@ -81,6 +81,7 @@ enum WsSlot {
     WS_D2H,
     WS_BF16,         // split-bf16 operand planes
     WS_MISC,
+    WS_INSERT,       // insertion: per-draw pixel grids and rotations
     WS_COUNT
 };
 
@@ -103,6 +104,12 @@ struct Pixels {
     int Kp = 0;        // floats per padded complex row (multiple of 64)
     int idim = 0;
     double maxRadius = 0;
+    int maxAbs = 0;    // max |iCol|, |iRow|
+    bool unique = true;
+    // pixel of each cell of the half plane [2 maxAbs + 1][maxAbs + 1]
+    // (row iRow + maxAbs, column iCol), -1 where none; set when unique
+    int* cellPix = nullptr;
+    size_t cells = 0;
 };
 
 struct InsertAcc {
@@ -130,6 +137,7 @@ struct tg3_ctx {
     int* d_flag = nullptr;           // device error word
     // tg3_ctx_set_option
     bool fused = false;
+    bool insertGather = false;    // TG3_OPT_INSERT_GATHER
     // per-stage event timing (tg3_ctx_set_timing)
     bool timing = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[TG3_STAGE_COUNT];
@@ -217,7 +225,9 @@ cudaError_t launch_resample(int nP, int n, const double* u, const double* w,
                             double* wOut, int* top, int* flag,
                             cudaStream_t st,
                             const int* nPer = nullptr);
-// One CTA per draw; draw d uses image d / drawsPerImage.
+// k_insert_draws (one thread per draw: parameters into params, 16 floats
+// per draw, and the O3D / counter bookkeeping), then k_insert: CTA (share
+// of the pixels, draw); draw d uses image d / drawsPerImage.
 cudaError_t launch_insert(float4* acc, int vdim, int kernel, const float* tab,
                           int tabNz, float tabInvStep, int nDraws,
                           int drawsPerImage, const float2* dat,
@@ -225,7 +235,19 @@ cudaError_t launch_insert(float4* acc, int vdim, int kernel, const float* tab,
                           const double* trans, const double* offset,
                           const float* w, const int* iCol, const int* iRow,
                           int K, int pf, int idim, double* O3D, int* counter,
-                          cudaStream_t st);
+                          float* params, cudaStream_t st);
+// MKB insertion by gather: per chunk of draws, k_insert_stage (tiles x
+// draws) fills the draws' dense pixel grids from the cell map cellPix,
+// k_insert_gather (tiles x draws) adds each slab voxel once.  scratch holds
+// insert_draw_bytes(Rg) per draw of a chunk; pixels must be unique.
+size_t insert_draw_bytes(int Rg);
+cudaError_t launch_insert_gather(float4* acc, int vdim, const float* tab, int tabNz,
+                                 float tabInvStep, int nDraws, int drawsPerImage,
+                                 const float2* dat, const float* ctf, const double* quat,
+                                 const double* trans, const double* offset, const float* w,
+                                 const int* cellPix, const int* iCol, const int* iRow, int K,
+                                 int pf, int idim, int Rg, float Rp, double* O3D, int* counter,
+                                 void* scratch, size_t scratchBytes, cudaStream_t st);
 cudaError_t launch_acc_read(const float4* acc, size_t n, float2* F, float* T,
                             int accumulate, cudaStream_t st);
 cudaError_t launch_merge_class(int nImg, int nK, int kIdx, int nR, int nT,

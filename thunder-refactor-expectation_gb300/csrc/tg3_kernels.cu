@@ -13,6 +13,8 @@
 //                        per-particle constant sum sigRcp |X|^2;
 //   insertion volume   : float4 [vdim][vdim][nx] of (F.re, F.im, T, 0), one
 //                        16-byte atomic per voxel update.
+#include <algorithm>
+
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
@@ -931,44 +933,76 @@ __device__ __forceinline__ void red_voxel(float4* acc, int vdim, int nx, int i, 
     atomicAdd(p, make_float4(fr, fi, t, 0.f));
 }
 
+// Per-draw parameters of the insertion, one thread per draw: the FP32
+// rotation (quat_to_mat in FP64, rounded), the shift t - offset and the
+// image weight, 16 floats per draw; and the bookkeeping: O3D -= R (t -
+// offset, 0) (insertDir, src/Optimiser.cpp:7180-7186), summed per block
+// before one atomic per component, and the draw counter.
 __global__ void __launch_bounds__(256)
-k_insert(float4* __restrict__ acc, int vdim, int kernel, const float* __restrict__ tab,
-         int tabNz, float tabInvStep, const float2* __restrict__ dat,
-         const float* __restrict__ ctf, const double* __restrict__ quat,
-         const double* __restrict__ trans, const double* __restrict__ offset,
-         const float* __restrict__ wgt, const int* __restrict__ iCol,
-         const int* __restrict__ iRow, int K, int pf, int idim, int drawsPerImage,
-         double* __restrict__ O3D, int* __restrict__ counter)
+k_insert_draws(int nDraws, int drawsPerImage, const double* __restrict__ quat,
+               const double* __restrict__ trans, const double* __restrict__ offset,
+               const float* __restrict__ wgt, float* __restrict__ params,
+               double* __restrict__ O3D, int* __restrict__ counter)
 {
-    __shared__ float m[9];
-    __shared__ float sh[3];
-    const int d = blockIdx.x;                 // draw
-    const int l = d / drawsPerImage;          // image
-    if (threadIdx.x == 0) {
+    __shared__ double part[3][8];
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    double o[3] = {0.0, 0.0, 0.0};
+    if (d < nDraws) {
+        const int l = d / drawsPerImage;
         double q[4] = {quat[4 * (size_t)d], quat[4 * (size_t)d + 1], quat[4 * (size_t)d + 2],
                        quat[4 * (size_t)d + 3]};
         double md[9];
         quat_to_mat(q, md);
-        for (int i = 0; i < 9; i++) m[i] = (float)md[i];
         const double tx = trans[2 * (size_t)d] - (offset ? offset[2 * (size_t)l] : 0.0);
         const double ty = trans[2 * (size_t)d + 1] - (offset ? offset[2 * (size_t)l + 1] : 0.0);
-        sh[0] = (float)tx;
-        sh[1] = (float)ty;
-        sh[2] = wgt[l];
-        if (O3D) {
-            // insertDir(-R (t - offset, 0)), src/Optimiser.cpp:7180-7186
-            atomicAdd(O3D + 0, -(md[0] * tx + md[1] * ty));
-            atomicAdd(O3D + 1, -(md[3] * tx + md[4] * ty));
-            atomicAdd(O3D + 2, -(md[6] * tx + md[7] * ty));
-        }
-        if (counter) atomicAdd(counter, 1);
+        float* pd = params + 16 * (size_t)d;
+        for (int i = 0; i < 9; i++) pd[i] = (float)md[i];
+        pd[9] = (float)tx;
+        pd[10] = (float)ty;
+        pd[11] = wgt[l];
+        o[0] = -(md[0] * tx + md[1] * ty);
+        o[1] = -(md[3] * tx + md[4] * ty);
+        o[2] = -(md[6] * tx + md[7] * ty);
     }
-    __syncthreads();
+    if (O3D) {
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        for (int k = 0; k < 3; k++) {
+            double v = o[k];
+            for (int sft = 16; sft; sft >>= 1) v += __shfl_xor_sync(0xffffffffu, v, sft);
+            if (lane == 0) part[k][wid] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            double v = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += part[threadIdx.x][w];
+            atomicAdd(O3D + threadIdx.x, v);
+        }
+    }
+    if (counter && threadIdx.x == 0) {
+        const int n = min((int)blockDim.x, nDraws - (int)(blockIdx.x * blockDim.x));
+        if (n > 0) atomicAdd(counter, n);
+    }
+}
+
+// CTA (share of the pixels, draw); parameters from k_insert_draws.
+__global__ void __launch_bounds__(256)
+k_insert(float4* __restrict__ acc, int vdim, int kernel, const float* __restrict__ tab,
+         int tabNz, float tabInvStep, float rs2, const float2* __restrict__ dat,
+         const float* __restrict__ ctf, const float* __restrict__ params,
+         const int* __restrict__ iCol, const int* __restrict__ iRow, int K, int pf, int idim,
+         int d0, int drawsPerImage)
+{
+    const int d = d0 + blockIdx.y;            // draw; blockIdx.x: share of its pixels
+    const int l = d / drawsPerImage;          // image
+    const float* pd = params + 16 * (size_t)d;
+    float m[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) m[i] = __ldg(pd + i);
     const int nx = vdim / 2 + 1, half = vdim / 2;
-    const float tx = sh[0], ty = sh[1], w = sh[2];
+    const float tx = __ldg(pd + 9), ty = __ldg(pd + 10), w = __ldg(pd + 11);
     const float invN = 1.0f / (float)idim;
     const float fpf = (float)pf;
-    for (int p = threadIdx.x; p < K; p += blockDim.x) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K; p += gridDim.x * blockDim.x) {
         const size_t di = (size_t)l * K + p;
         const float c = ctf[di];
         const float2 X = dat[di];
@@ -984,23 +1018,41 @@ k_insert(float4* __restrict__ acc, int vdim, int kernel, const float* __restrict
         float y = m[3] * a + m[4] * b;
         float z = m[6] * a + m[7] * b;
         if (kernel == TG3_KERNEL_MKB) {
-            const float rad = 2.0f;   // covers the table's support r^2 <= 3.6101
-            const int k0 = max(-half, (int)floorf(z - rad)), k1 = min(half - 1, (int)ceilf(z + rad));
-            const int j0 = max(-half, (int)floorf(y - rad)), j1 = min(half - 1, (int)ceilf(y + rad));
-            const int i0 = max(-half, (int)floorf(x - rad)), i1 = min(half, (int)ceilf(x + rad));
+            // every voxel with rint(r^2 n / b) <= tabNz has r^2 < rs2: per
+            // axis, only the lattice points inside that sphere are visited
+            const float rs = sqrtf(rs2);
+            const int k0 = max(-half, (int)ceilf(z - rs)), k1 = min(half - 1, (int)floorf(z + rs));
             for (int kk = k0; kk <= k1; kk++) {
                 const float dz = z - (float)kk;
+                const float sz = rs2 - dz * dz;
+                if (sz < 0.f) continue;
+                const float ry = sqrtf(sz);
+                const int j0 = max(-half, (int)ceilf(y - ry));
+                const int j1 = min(half - 1, (int)floorf(y + ry));
                 for (int jj = j0; jj <= j1; jj++) {
                     const float dy = y - (float)jj;
                     const float dyz = dy * dy + dz * dz;
-                    for (int ii = i0; ii <= i1; ii++) {
-                        const float dx = x - (float)ii;
-                        const float r2 = dx * dx + dyz;
-                        const int ti = __float2int_rn(r2 * tabInvStep);
-                        if (ti > tabNz) continue;
-                        const float kv = __ldg(tab + ti);
-                        red_voxel(acc, vdim, nx, ii, jj, kk, vr * kv, vi * kv, vt * kv);
+                    const float sx = rs2 - dyz;
+                    if (sx < 0.f) continue;
+                    const float rx = sqrtf(sx);
+                    const int i0 = max(-half, (int)ceilf(x - rx));
+                    const int i1 = min(half, (int)floorf(x + rx));
+                    // at most 4 lattice points (2 rx < 4, checked by the
+                    // launcher): the row's table loads are issued together
+                    int tv[4];
+                    float kv[4];
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const float dx = x - (float)(i0 + v);
+                        const int ti = __float2int_rn((dx * dx + dyz) * tabInvStep);
+                        tv[v] = (i0 + v <= i1 && ti <= tabNz) ? ti : -1;
+                        kv[v] = tv[v] >= 0 ? __ldg(tab + tv[v]) : 0.f;
                     }
+#pragma unroll
+                    for (int v = 0; v < 4; v++)
+                        if (tv[v] >= 0)
+                            red_voxel(acc, vdim, nx, i0 + v, jj, kk, vr * kv[v], vi * kv[v],
+                                      vt * kv[v]);
                 }
             }
         } else {
@@ -1023,6 +1075,150 @@ k_insert(float4* __restrict__ acc, int vdim, int kernel, const float* __restrict
                         atomicAdd(acc + ((size_t)zz * vdim + yy) * nx + (x0 + i),
                                   make_float4(vr * ww, fi * ww, vt * ww, 0.f));
                     }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------
+// MKB insertion as a gather (same sums as k_insert, one atomic per voxel).
+//
+// Stage: CTA (tile, draw) writes cells of the draw's dense half-plane grid
+// [2 Rg + 1 rows][Rg + 1 columns] of float4: the shifted, weighted value
+// (c w X e^{2 pi i k.t/N}, c^2 w) of the cell's pixel, zero where no pixel
+// lies (cellPix < 0).  CTA (0, draw) also writes the draw's FP32 rotation
+// and does its bookkeeping (O3D, counter) exactly as k_insert.
+__global__ void __launch_bounds__(256)
+k_insert_stage(float4* __restrict__ grid, int cells, float* __restrict__ rot,
+               const int* __restrict__ cellPix, const int* __restrict__ iCol,
+               const int* __restrict__ iRow, const float2* __restrict__ dat,
+               const float* __restrict__ ctf, const double* __restrict__ quat,
+               const double* __restrict__ trans, const double* __restrict__ offset,
+               const float* __restrict__ wgt, int K, int idim, int d0, int drawsPerImage,
+               double* __restrict__ O3D, int* __restrict__ counter)
+{
+    const int dl = blockIdx.y;                // draw within the chunk
+    const int d = d0 + dl;
+    const int l = d / drawsPerImage;
+    const double txd = trans[2 * (size_t)d] - (offset ? offset[2 * (size_t)l] : 0.0);
+    const double tyd = trans[2 * (size_t)d + 1] - (offset ? offset[2 * (size_t)l + 1] : 0.0);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        double q[4] = {quat[4 * (size_t)d], quat[4 * (size_t)d + 1], quat[4 * (size_t)d + 2],
+                       quat[4 * (size_t)d + 3]};
+        double md[9];
+        quat_to_mat(q, md);
+        for (int i = 0; i < 9; i++) rot[16 * (size_t)dl + i] = (float)md[i];
+        if (O3D) {
+            atomicAdd(O3D + 0, -(md[0] * txd + md[1] * tyd));
+            atomicAdd(O3D + 1, -(md[3] * txd + md[4] * tyd));
+            atomicAdd(O3D + 2, -(md[6] * txd + md[7] * tyd));
+        }
+        if (counter) atomicAdd(counter, 1);
+    }
+    const float tx = (float)txd, ty = (float)tyd, w = wgt[l];
+    const float invN = 1.0f / (float)idim;
+    float4* g = grid + (size_t)dl * cells;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cells; i += gridDim.x * blockDim.x) {
+        const int p = cellPix[i];
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (p >= 0) {
+            const size_t di = (size_t)l * K + p;
+            const float c = ctf[di];
+            const float2 X = dat[di];
+            float f = ((float)iCol[p] * tx + (float)iRow[p] * ty) * invN;
+            float sn, co;
+            sincospif(2.0f * f, &sn, &co);
+            const float cw = c * w;
+            v = make_float4((X.x * co - X.y * sn) * cw, (X.x * sn + X.y * co) * cw, c * c * w,
+                            0.f);
+        }
+        g[i] = v;
+    }
+}
+
+// Gather: CTA (tile, draw); each thread takes rows (x-runs of fixed y, z) of
+// the stored half volume that cross the draw's slab |h| <= hs, h = e3 . v,
+// inside the cylinder of in-plane radius Rp + hs.  Each voxel v = (x, y, z)
+// takes its plane coordinates (a, b, h) = R^T v and sums the MKB-weighted
+// values of the grid cells within the support: a pixel (c, r) at
+// (pf c, pf r, 0) directly, and, for x > 0, the Friedel mate of pixel (c, r)
+// at (-pf c, -pf r, 0), conjugated.  This is the set of writes k_insert
+// makes to v (direct writes to x >= 0, mirrored writes from x < 0 to x > 0).
+__global__ void __launch_bounds__(256, 4)
+k_insert_gather(float4* __restrict__ acc, int vdim, const float4* __restrict__ grid, int gw,
+                int Rg, const float* __restrict__ rot, const float* __restrict__ tab, int tabNz,
+                float tabInvStep, int pf, float Rp, float hs)
+{
+    const int dl = blockIdx.y;
+    const float* mr = rot + 16 * (size_t)dl;
+    const float e1x = __ldg(mr + 0), e1y = __ldg(mr + 3), e1z = __ldg(mr + 6);
+    const float e2x = __ldg(mr + 1), e2y = __ldg(mr + 4), e2z = __ldg(mr + 7);
+    const float e3x = __ldg(mr + 2), e3y = __ldg(mr + 5), e3z = __ldg(mr + 8);
+    const float4* g = grid + (size_t)dl * gw * (2 * Rg + 1);
+    const int half = vdim / 2, nx = half + 1;
+    const float Rc = Rp + hs;                           // cylinder radius
+    const float R2 = Rc * Rc + hs * hs;                 // |v|^2 bound
+    const int Y = min(half - 1, (int)ceilf(Rc * sqrtf(fmaxf(0.f, 1.f - e3y * e3y)) +
+                                           hs * fabsf(e3y)));
+    const int Z = min(half - 1, (int)ceilf(Rc * sqrtf(fmaxf(0.f, 1.f - e3z * e3z)) +
+                                           hs * fabsf(e3z)));
+    const int ny = 2 * Y + 1;
+    const int nRows = ny * (2 * Z + 1);
+    const float fpf = (float)pf, inv_pf = 1.0f / fpf;
+
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nRows;
+         row += gridDim.x * blockDim.x) {
+        const int y = row % ny - Y, z = row / ny - Z;
+        const float fy = (float)y, fz = (float)z;
+        const float rem = R2 - fy * fy - fz * fz;
+        if (rem < 0.f) continue;
+        const float hyz = e3y * fy + e3z * fz;
+        float lo = 0.f, hi = fminf(sqrtf(rem), (float)(half - 1));
+        if (fabsf(e3x) > 1e-6f) {
+            const float ta = (-hs - hyz) / e3x, tb = (hs - hyz) / e3x;
+            lo = fmaxf(lo, fminf(ta, tb));
+            hi = fminf(hi, fmaxf(ta, tb));
+        } else if (fabsf(hyz) > hs) {
+            continue;
+        }
+        if (hi < lo) continue;
+        const int xa = max((int)ceilf(lo - 1e-3f), 0);
+        const int xb = min((int)floorf(hi + 1e-3f), half - 1);
+        const float ayz = e1y * fy + e1z * fz, byz = e2y * fy + e2z * fz;
+        float4* line = acc + ((size_t)(z < 0 ? z + vdim : z) * vdim + (y < 0 ? y + vdim : y)) * nx;
+        for (int x = xa; x <= xb; x++) {
+            const float fx = (float)x;
+            const float a = fmaf(e1x, fx, ayz);
+            const float b = fmaf(e2x, fx, byz);
+            const float h = fmaf(e3x, fx, hyz);
+            const float h2 = h * h;
+            const int c0 = (int)ceilf((a - hs) * inv_pf), c1 = (int)floorf((a + hs) * inv_pf);
+            const int q0 = max((int)ceilf((b - hs) * inv_pf), -Rg);
+            const int q1 = min((int)floorf((b + hs) * inv_pf), Rg);
+            float sr = 0.f, si = 0.f, st = 0.f;
+            for (int c = c0; c <= c1; c++) {
+                const float dx = a - fpf * (float)c;
+                const float dx2h = fmaf(dx, dx, h2);
+                for (int r = q0; r <= q1; r++) {
+                    const float dy = b - fpf * (float)r;
+                    const int ti = __float2int_rn(fmaf(dy, dy, dx2h) * tabInvStep);
+                    if (ti > tabNz) continue;
+                    const float kv = __ldg(tab + ti);
+                    if (c >= 0 && c <= Rg) {
+                        const float4 v = __ldg(g + (r + Rg) * gw + c);
+                        sr = fmaf(kv, v.x, sr);
+                        si = fmaf(kv, v.y, si);
+                        st = fmaf(kv, v.z, st);
+                    }
+                    if (x > 0 && c <= 0 && -c <= Rg) {
+                        const float4 v = __ldg(g + (Rg - r) * gw - c);
+                        sr = fmaf(kv, v.x, sr);
+                        si = fmaf(-kv, v.y, si);
+                        st = fmaf(kv, v.z, st);
+                    }
+                }
+            }
+            if (sr != 0.f || si != 0.f || st != 0.f)
+                atomicAdd(line + x, make_float4(sr, si, st, 0.f));
         }
     }
 }
@@ -1215,12 +1411,60 @@ cudaError_t launch_insert(float4* acc, int vdim, int kernel, const float* tab, i
                           const float* ctf, const double* quat, const double* trans,
                           const double* offset, const float* w, const int* iCol,
                           const int* iRow, int K, int pf, int idim, double* O3D, int* counter,
-                          cudaStream_t st)
+                          float* params, cudaStream_t st)
 {
     if (nDraws <= 0) return cudaSuccess;
-    k_insert<<<nDraws, 256, 0, st>>>(acc, vdim, kernel, tab, tabNz, tabInvStep, dat, ctf, quat,
-                                      trans, offset, w, iCol, iRow, K, pf, idim, drawsPerImage,
-                                      O3D, counter);
+    // r^2 bound of the table's support: rint(r^2 n / b) <= tabNz  =>  r^2 < (tabNz + 1/2) b / n
+    const float rs2 = (((float)tabNz + 0.5f) / tabInvStep) * (1.0f + 1e-4f);
+    if (kernel == TG3_KERNEL_MKB && 2.0f * sqrtf(rs2) >= 4.0f) return cudaErrorInvalidValue;
+    k_insert_draws<<<(nDraws + 255) / 256, 256, 0, st>>>(nDraws, drawsPerImage, quat, trans,
+                                                         offset, w, params, O3D, counter);
+    // one pixel per thread: the draw's pixels spread over ceil(K / 256) CTAs
+    const int tiles = std::max(1, std::min(1024, (K + 255) / 256));
+    for (int d0 = 0; d0 < nDraws; d0 += 65535) {
+        const int n = std::min(65535, nDraws - d0);
+        k_insert<<<dim3(tiles, n), 256, 0, st>>>(acc, vdim, kernel, tab, tabNz, tabInvStep, rs2,
+                                                 dat, ctf, params, iCol, iRow, K, pf, idim, d0,
+                                                 drawsPerImage);
+    }
+    return cudaGetLastError();
+}
+
+size_t insert_draw_bytes(int Rg)
+{
+    return (size_t)(Rg + 1) * (2 * Rg + 1) * sizeof(float4) + 16 * sizeof(float);
+}
+
+cudaError_t launch_insert_gather(float4* acc, int vdim, const float* tab, int tabNz,
+                                 float tabInvStep, int nDraws, int drawsPerImage,
+                                 const float2* dat, const float* ctf, const double* quat,
+                                 const double* trans, const double* offset, const float* w,
+                                 const int* cellPix, const int* iCol, const int* iRow, int K,
+                                 int pf, int idim, int Rg, float Rp, double* O3D, int* counter,
+                                 void* scratch, size_t scratchBytes, cudaStream_t st)
+{
+    if (nDraws <= 0) return cudaSuccess;
+    const int gw = Rg + 1, cells = gw * (2 * Rg + 1);
+    const size_t gridBytes = (size_t)cells * sizeof(float4);
+    const size_t chunkMax = scratchBytes / insert_draw_bytes(Rg);
+    if (chunkMax < 1) return cudaErrorInvalidValue;
+    const int chunk = (int)std::min<size_t>(std::min<size_t>((size_t)nDraws, chunkMax), 65535);
+    float4* grid = static_cast<float4*>(scratch);
+    float* rot = reinterpret_cast<float*>(static_cast<char*>(scratch) + gridBytes * chunk);
+    // slab half thickness: rint(r^2 n / b) <= tabNz  <=>  r^2 < (tabNz + 1/2) b / n
+    const float hs = sqrtf(((float)tabNz + 0.5f) / tabInvStep) + 1e-3f;
+    const int stageTiles = std::max(1, std::min(64, (cells + 1023) / 1024));
+    for (int d0 = 0; d0 < nDraws; d0 += chunk) {
+        const int n = std::min(chunk, nDraws - d0);
+        k_insert_stage<<<dim3(stageTiles, n), 256, 0, st>>>(grid, cells, rot, cellPix, iCol, iRow,
+                                                            dat, ctf, quat, trans, offset, w, K,
+                                                            idim, d0, drawsPerImage, O3D,
+                                                            counter);
+        // about two waves of resident CTAs (152 SMs x 8 CTAs of 256 threads)
+        const int tiles = std::max(1, std::min(128, (2 * 152 * 8 + n - 1) / n));
+        k_insert_gather<<<dim3(tiles, n), 256, 0, st>>>(acc, vdim, grid, gw, Rg, rot, tab, tabNz,
+                                                        tabInvStep, pf, Rp, hs);
+    }
     return cudaGetLastError();
 }
 

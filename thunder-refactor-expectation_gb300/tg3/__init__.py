@@ -38,6 +38,7 @@ EXPORTS = [
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
 OPT_FUSED = 0
+OPT_INSERT_GATHER = 1
 
 
 class TG3Error(RuntimeError):
