@@ -338,6 +338,18 @@ int tg3_insert_d(tg3_ctx* ctx, int nP, const float* dat, const float* ctf,
  * arrays of [vdim][vdim][vdim/2+1] entries, adding to their contents
  * when accumulate != 0. */
 int tg3_ctx_insert_read_d(tg3_ctx* ctx, float* F, float* T, int accumulate);
+/* The inserted slices' average V = F / T (complex, [vdim][vdim][vdim/2+1])
+ * where T > floor, 0 elsewhere.  The normalisation that precedes the
+ * reference's reconstruction (Reconstructor, src/Reconstructor.cpp:1056-2713)
+ * without its W balancing or gridding correction. */
+int tg3_ctx_insert_ratio_d(tg3_ctx* ctx, float* V, float floor);
+
+/* Fourier shell correlation of two complex half volumes A, B
+ * [vdim][vdim][vdim/2+1] (device): fsc[u] for shells u = rint(|k|) <
+ * nShell, 0 for an empty shell (FSC, src/Functions/Spectrum.cpp:302-329).
+ * scratch: device double[3 nShell]; nShell <= 8533. */
+int tg3_fsc_d(const float* A, const float* B, int vdim, int nShell, double* fsc,
+              double* scratch, void* stream);
 
 /* ------------------------------------------------------------------------
  * Allocation-free local scoring.  No counterpart in the reference.

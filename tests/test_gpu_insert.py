@@ -122,3 +122,51 @@ def test_both_forms_match_the_oracle_at_box_256():
         assert f[1:].min() >= 0.999, f
         assert abs(int((Tg != 0).sum()) - nzr) <= 1e-5 * nzr
         del Fg, Tg
+
+
+def test_fsc_matches_the_oracle():
+    rng = np.random.default_rng(47)
+    vdim, n_shell = 48, 24
+    shape = (vdim, vdim, vdim // 2 + 1)
+    A = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    B = (A + 0.7 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape))).astype(
+        np.complex64)
+    B[..., 3] = 0                 # shells with data in one volume only
+    got = tg3.fsc(torch.as_tensor(A).to(DEV), torch.as_tensor(B).to(DEV), n_shell).cpu().numpy()
+    ref = O.fsc(A.astype(np.complex128), B.astype(np.complex128), n_shell)
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-14)
+    # identical volumes correlate fully in every shell that holds data
+    one = tg3.fsc(torch.as_tensor(A).to(DEV), torch.as_tensor(A).to(DEV), n_shell).cpu().numpy()
+    np.testing.assert_allclose(one, 1.0, rtol=0, atol=1e-12)
+
+
+def test_insert_ratio_is_F_over_T():
+    rng = np.random.default_rng(53)
+    box, pf, px = 24, 2, 1.5
+    iCol, iRow = synth.pixel_index(box, 9, synth.config_rL(box, px))[:2]
+    K, nP = len(iCol), 7
+    vdim = pf * box
+    d = lambda x: torch.as_tensor(np.ascontiguousarray(x)).to(DEV)
+    q = synth.haar_quaternions(rng, nP)
+    dat = (rng.standard_normal((nP, K)) + 1j * rng.standard_normal((nP, K))).astype(np.complex64)
+    ctf = rng.uniform(-1, 1, (nP, K)).astype(np.float32)
+    c = tg3.Context(0)
+    try:
+        c.set_pixels(iCol, iRow, box)
+        c.insert_begin(vdim, pf)
+        c.insert(nP, d(dat), d(ctf), d(q), d(np.zeros((nP, 2))), None,
+                 d(np.ones(nP, np.float32)), tg3.KERNEL_MKB)
+        F = torch.empty((vdim, vdim, vdim // 2 + 1, 2), dtype=torch.float32, device=DEV)
+        T = torch.empty((vdim, vdim, vdim // 2 + 1), dtype=torch.float32, device=DEV)
+        V = torch.empty((vdim, vdim, vdim // 2 + 1), dtype=torch.complex64, device=DEV)
+        c.insert_read(F, T)
+        floor = 1e-3 * float(T.max())
+        c.insert_ratio(V, floor)
+        c.sync()
+    finally:
+        c.close()
+    F, T, V = F.cpu().numpy(), T.cpu().numpy(), V.cpu().numpy()
+    keep = T > floor
+    ref = np.where(keep, (F[..., 0] + 1j * F[..., 1]) / np.where(keep, T, 1.0), 0)
+    np.testing.assert_allclose(V, ref.astype(np.complex64), rtol=1e-6, atol=0)
+    assert keep.sum() > 1000 and np.all(V[~keep] == 0)

@@ -738,6 +738,28 @@ extern "C" int tg3_ctx_insert_read_d(tg3_ctx* c, float* F, float* T, int accumul
     return TG3_OK;
 }
 
+extern "C" int tg3_ctx_insert_ratio_d(tg3_ctx* c, float* V, float floor_)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (!c->ins.acc) return fail(TG3_ERR_STATE, "insertion volume not begun");
+    if (!V || !(floor_ >= 0.f)) return fail(TG3_ERR_ARG, "bad ratio args");
+    const size_t n = (size_t)c->ins.vdim * c->ins.vdim * (c->ins.vdim / 2 + 1);
+    TG3_CUDA(launch_acc_ratio(c->ins.acc, n, floor_, reinterpret_cast<float2*>(V), c->stream));
+    return TG3_OK;
+}
+
+extern "C" int tg3_fsc_d(const float* A, const float* B, int vdim, int nShell, double* fsc,
+                         double* scratch, void* stream)
+{
+    if (!A || !B || !fsc || !scratch || vdim < 2 || (vdim & 1) || nShell < 1 ||
+        (size_t)nShell * 3 * sizeof(double) > 200 * 1024)
+        return fail(TG3_ERR_ARG, "bad fsc args");
+    TG3_CUDA(launch_fsc(reinterpret_cast<const float2*>(A), reinterpret_cast<const float2*>(B),
+                        vdim, nShell, scratch, fsc, (cudaStream_t)stream));
+    return TG3_OK;
+}
+
 // ======================================================= kernel-level calls
 extern "C" int tg3_rotmat_d(const double* quat, int n, double* mat, void* stream)
 {

@@ -248,6 +248,11 @@ cudaError_t launch_insert_gather(float4* acc, int vdim, const float* tab, int ta
                                  const int* cellPix, const int* iCol, const int* iRow, int K,
                                  int pf, int idim, int Rg, float Rp, double* O3D, int* counter,
                                  void* scratch, size_t scratchBytes, cudaStream_t st);
+// Shell correlation of two half volumes; sums holds 3 nShell doubles.
+cudaError_t launch_fsc(const float2* A, const float2* B, int vdim, int nShell,
+                       double* sums, double* fsc, cudaStream_t st);
+cudaError_t launch_acc_ratio(const float4* acc, size_t n, float floor_, float2* V,
+                             cudaStream_t st);
 cudaError_t launch_acc_read(const float4* acc, size_t n, float2* F, float* T,
                             int accumulate, cudaStream_t st);
 cudaError_t launch_merge_class(int nImg, int nK, int kIdx, int nR, int nT,

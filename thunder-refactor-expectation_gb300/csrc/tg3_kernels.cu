@@ -1223,6 +1223,58 @@ k_insert_gather(float4* __restrict__ acc, int vdim, const float4* __restrict__ g
     }
 }
 
+// Fourier shell correlation of two half volumes [vdim][vdim][vdim/2+1] of
+// complex values (FSC(vec&, const Volume&, const Volume&),
+// src/Functions/Spectrum.cpp:302-329): shell u = rint(|k|) in voxel units,
+// for u < nShell, of sum Re(A conj B), sum |A|^2, sum |B|^2 in FP64.  Each
+// CTA sums its voxels per shell in shared memory, then adds its shells once.
+__global__ void __launch_bounds__(256)
+k_fsc_shells(const float2* __restrict__ A, const float2* __restrict__ B, int vdim, int nShell,
+             double* __restrict__ sums)
+{
+    extern __shared__ double sacc[];             // [3][nShell]
+    for (int i = threadIdx.x; i < 3 * nShell; i += blockDim.x) sacc[i] = 0.0;
+    __syncthreads();
+    const int nx = vdim / 2 + 1, half = vdim / 2;
+    const size_t n = (size_t)vdim * vdim * nx;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(i % nx);
+        const size_t zy = i / nx;
+        const int y = (int)(zy % vdim), z = (int)(zy / vdim);
+        const int fy = y < half ? y : y - vdim, fz = z < half ? z : z - vdim;
+        const int u = __double2int_rn(sqrt((double)x * x + (double)fy * fy + (double)fz * fz));
+        if (u >= nShell) continue;
+        const float2 a = A[i], b = B[i];
+        atomicAdd(sacc + u, (double)a.x * b.x + (double)a.y * b.y);
+        atomicAdd(sacc + nShell + u, (double)a.x * a.x + (double)a.y * a.y);
+        atomicAdd(sacc + 2 * nShell + u, (double)b.x * b.x + (double)b.y * b.y);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * nShell; i += blockDim.x)
+        if (sacc[i] != 0.0) atomicAdd(sums + i, sacc[i]);
+}
+
+__global__ void k_fsc_finish(const double* __restrict__ sums, int nShell, double* __restrict__ fsc)
+{
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nShell) return;
+    const double xy = sums[u], xx = sums[nShell + u], yy = sums[2 * nShell + u];
+    fsc[u] = (xx * yy == 0.0) ? 0.0 : xy / sqrt(xx * yy);
+}
+
+// V = F / T where T > floor, else 0: the inserted slices' average at every
+// voxel of the accumulator.
+__global__ void k_acc_ratio(const float4* __restrict__ acc, size_t n, float floor_,
+                            float2* __restrict__ V)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float4 a = acc[i];
+        V[i] = a.z > floor_ ? make_float2(a.x / a.z, a.y / a.z) : make_float2(0.f, 0.f);
+    }
+}
+
 __global__ void k_acc_read(const float4* __restrict__ acc, size_t n, float2* __restrict__ F,
                            float* __restrict__ T, int accumulate)
 {
@@ -1465,6 +1517,26 @@ cudaError_t launch_insert_gather(float4* acc, int vdim, const float* tab, int ta
         k_insert_gather<<<dim3(tiles, n), 256, 0, st>>>(acc, vdim, grid, gw, Rg, rot, tab, tabNz,
                                                         tabInvStep, pf, Rp, hs);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fsc(const float2* A, const float2* B, int vdim, int nShell, double* sums,
+                       double* fsc, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(sums, 0, sizeof(double) * 3 * (size_t)nShell, st);
+    if (e != cudaSuccess) return e;
+    const size_t smem = sizeof(double) * 3 * (size_t)nShell;
+    e = cudaFuncSetAttribute(k_fsc_shells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const size_t n = (size_t)vdim * vdim * (vdim / 2 + 1);
+    k_fsc_shells<<<grid_for(n, 256, 152 * 4), 256, smem, st>>>(A, B, vdim, nShell, sums);
+    k_fsc_finish<<<(nShell + 127) / 128, 128, 0, st>>>(sums, nShell, fsc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_acc_ratio(const float4* acc, size_t n, float floor_, float2* V, cudaStream_t st)
+{
+    k_acc_ratio<<<grid_for(n, 256), 256, 0, st>>>(acc, n, floor_, V);
     return cudaGetLastError();
 }
 

@@ -27,7 +27,7 @@ EXPORTS = [
     "tg3_ctx_create", "tg3_ctx_destroy", "tg3_ctx_stream", "tg3_ctx_sync",
     "tg3_ctx_workspace_bytes", "tg3_ctx_set_volume", "tg3_ctx_set_pixels",
     "tg3_local_phase_d", "tg3_resample_d", "tg3_ctx_insert_begin", "tg3_insert_d",
-    "tg3_ctx_insert_read_d", "tg3_rotmat_d", "tg3_translate_d", "tg3_ctf_d",
+    "tg3_ctx_insert_read_d", "tg3_ctx_insert_ratio_d", "tg3_fsc_d", "tg3_rotmat_d", "tg3_translate_d", "tg3_ctf_d",
     "tg3_project_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
     "tg3_ctx_set_option", "tg3_ctx_set_pixels_slot", "tg3_ctx_use_pixels",
     "tg3_ragged_plan_create", "tg3_ragged_plan_run", "tg3_ragged_plan_info",
@@ -88,6 +88,8 @@ def lib():
             "tg3_ctx_insert_begin": ([_P, _I, _I], _I),
             "tg3_insert_d": ([_P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _P], _I),
             "tg3_ctx_insert_read_d": ([_P, _P, _P, _I], _I),
+            "tg3_ctx_insert_ratio_d": ([_P, _P, _F], _I),
+            "tg3_fsc_d": ([_P, _P, _I, _I, _P, _P, _P], _I),
             "tg3_rotmat_d": ([_P, _I, _P, _P], _I),
             "tg3_translate_d": ([_P, _I, _I, _P, _P, _I, _P, _P], _I),
             "tg3_ctf_d": ([_P, _I, _F, _I, _P, _P, _I, _P, _P], _I),
@@ -146,6 +148,20 @@ def ptr(x) -> int | None:
         return x.data_ptr()
     raise TypeError(type(x))
 
+
+
+def fsc(A, B, n_shell: int, stream=None):
+    """Fourier shell correlation of two complex half volumes on the device
+    ([vdim][vdim][vdim/2+1], complex64 or float32 pairs): a float64 tensor of
+    n_shell values, shells rint(|k|) in voxel units."""
+    import torch
+    vdim = A.shape[0]
+    out = torch.empty(n_shell, dtype=torch.float64, device=A.device)
+    scratch = torch.empty(3 * n_shell, dtype=torch.float64, device=A.device)
+    check(lib().tg3_fsc_d(ptr(A), ptr(B), vdim, n_shell, ptr(out), ptr(scratch), stream))
+    if stream is None:
+        torch.cuda.synchronize(A.device)
+    return out
 
 class Context:
     """A tg3_ctx: stream, volumes, pixel list, workspace on one device.
@@ -256,6 +272,11 @@ class Context:
     def insert_read(self, F, T, accumulate=False):
         self._hold(F, T)
         check(lib().tg3_ctx_insert_read_d(self.h, ptr(F), ptr(T), int(accumulate)))
+
+    def insert_ratio(self, V, floor=0.0):
+        """V (complex64 half volume, device) = F / T where T > floor, else 0."""
+        self._hold(V)
+        check(lib().tg3_ctx_insert_ratio_d(self.h, ptr(V), float(floor)))
 
     def project(self, cls, rotmat, nR, out):
         self._hold(rotmat, out)
