@@ -730,10 +730,13 @@ def synth_padded(bm, box, pf, dev):
 
 def run_learned(args, rank, world, local_rank):
     """Learned proposal: 16 random 128^3 blob maps (120 blobs, 1.4 A/px), 12 for
-    training pairs and 4 held out.  The pose network trains on the GPU (its own
-    kernels) on (image, true pose) pairs of the 12 training maps, then seeds
-    256 rotations x 25 translations per particle, every one rescored by the
-    exact likelihood (split-bf16 local phase).  Compared with the plain
+    training pairs and 4 held out.  The network trains on the GPU (its own
+    kernels) on pairs of the 12 training maps: in matching mode (the default)
+    particle images against clean reference projections at their true poses,
+    in regression mode (image, true pose).  It then seeds 256 rotations x 25
+    translations per particle (matching: the best-matching of the map's 6,912
+    references), every one rescored by the exact likelihood (split-bf16
+    local phase).  Compared with the plain
     global search (6,912 x 49 hypotheses) on held-out particles of the
     training maps and on particles of the 4 held-out maps.  Cutoff 32
     (K = 1,563: the global scan's scaling, r = box / 4)."""
@@ -752,7 +755,7 @@ def run_learned(args, rank, world, local_rank):
     nTr = L["n_train_maps"]
     t0 = time.perf_counter()
     # training pairs, generated in chunks (images stay on the device)
-    imgs, Rs, ts = [], [], []
+    imgs, Rs, ts, qtrue, ctr = [], [], [], [], []
     chunk = 10000
     for s0 in range(0, args.train_particles, chunk):
         m = min(chunk, args.train_particles - s0)
@@ -761,28 +764,63 @@ def run_learned(args, rank, world, local_rank):
         imgs.append(ps.images)
         Rs.append(synth.quat_to_mat(ps.quat_true).reshape(m, 9))
         ts.append(ps.trans_true)
+        qtrue.append(ps.quat_true)
+        ctr.append(ps.cls)
     images = torch.cat(imgs)
     Rstar = torch.as_tensor(np.concatenate(Rs)).to(dev)
     tstar = torch.as_tensor(np.concatenate(ts)).to(dev)
+    # the exact likelihood and the reference projections: one context with
+    # every map as a class
+    ctx = tg3.Context(local_rank)
+    for c, bm in enumerate(maps):
+        ctx.set_volume(c, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
+    match = args.learned_mode == "match"
+    if match:
+        # clean references at the training particles' true rotations
+        qtr = np.concatenate(qtrue)
+        ctr = np.concatenate(ctr)
+        refs = torch.empty_like(images)
+        for c in range(nTr):
+            sel = np.nonzero(ctr == c)[0]
+            refs[torch.as_tensor(sel, device=dev)] = learned.render_references(ctx, c, qtr[sel], box)
     gen_s = time.perf_counter() - t0
     net = tg3.Cnn(local_rank, seed=4242)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    losses = learned.train(net, images, Rstar, tstar, args.epochs, 256, args.learned_lr, seed=7)
+    if match:
+        losses = learned.train_match(net, images, refs, tstar, ctr, args.epochs, 256,
+                                     args.learned_lr, tau=args.learned_tau, seed=7)
+        del refs
+    else:
+        losses = learned.train(net, images, Rstar, tstar, args.epochs, 256, args.learned_lr,
+                               seed=7)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t1
     del images, Rstar, tstar
-    # the exact likelihood: one context with every map as a class
-    ctx = tg3.Context(local_rank)
-    for c, bm in enumerate(maps):
-        ctx.set_volume(c, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
     quats_g = synth.global_rotations(4, 36)
     mats_g = torch.as_tensor(synth.quat_to_mat(quats_g).reshape(-1, 9)).to(dev)
     trans_g = torch.as_tensor(synth.global_translations(3, 1.0)).to(dev)
     nRg, nTg = len(quats_g), int(trans_g.shape[0])
 
+    quats_g_dev = torch.as_tensor(quats_g).to(dev)
+    ref_emb, ref_ms = {}, []
+
+    def embeddings_of(c):
+        # the map's references at the global rotations, embedded (timed)
+        if c not in ref_emb:
+            torch.cuda.synchronize()
+            ta = time.perf_counter()
+            ref_emb[c] = learned.reference_embeddings(
+                net, learned.render_references(ctx, c, quats_g, box))
+            torch.cuda.synchronize()
+            ref_ms.append((time.perf_counter() - ta) * 1e3)
+        return ref_emb[c]
+
     def evaluate(ps, name):
         n = len(ps.cls)
+        if match:
+            for c in np.unique(ps.cls):
+                embeddings_of(int(c))
         ctx.set_pixels(ps.iCol, ps.iRow, box)
         d = dict(dat=torch.as_tensor(ps.dat).to(dev), ctf=torch.as_tensor(ps.ctf).to(dev),
                  sig=torch.as_tensor(ps.sigRcp).to(dev))
@@ -836,10 +874,24 @@ def run_learned(args, rank, world, local_rank):
         qd = torch.empty((n, nR, 4), **f64)
         td = torch.empty((n, nT, 2), **f64)
 
+        grp = [(int(c), torch.as_tensor(np.nonzero(ps.cls == c)[0], device=dev))
+               for c in np.unique(ps.cls)]
+
         def learned_all():
             # network, proposals and exact rescoring, all on the device
             net.forward(ps.images, out)
-            tg3.Cnn.propose(out, nR, nT, 99, qd, td, ctx.stream)
+            if match:
+                # per map: the best-matching references of that map's embeddings
+                for c, idx in grp:
+                    og_ = out[idx].contiguous()
+                    qg_ = torch.empty((len(idx), nR, 4), **f64)
+                    tg_ = torch.empty((len(idx), nT, 2), **f64)
+                    tg3.Cnn.match_propose(og_, ref_emb[c], quats_g_dev, nR, nT, 99, qg_, tg_)
+                    qd[idx] = qg_
+                    td[idx] = tg_
+                torch.cuda.synchronize()
+            else:
+                tg3.Cnn.propose(out, nR, nT, 99, qd, td, ctx.stream)
             ctx.local_phase(n, nR, nT, d["dat"], d["ctf"], d["sig"], qd, td,
                             torch.full((n, nR), 1.0 / nR, **f64), torch.full((n, nT), 1.0 / nT, **f64),
                             torch.ones(n, **f64), cls_d, ol["wC"], ol["wR"], ol["wT"], ol["base"],
@@ -882,14 +934,20 @@ def run_learned(args, rank, world, local_rank):
     good = rs["err_l"] < 10.0
     tau = float(np.quantile(rs["peak"][good], 0.05)) if good.any() else float("inf")
 
+    # matching mode: a map's reference embeddings are made once per map and
+    # serve all its particles; charged per particle over the 50,000 particles
+    # of a held-out map
+    ref_pp_ms = float(np.mean(ref_ms)) / 50000.0 if match and ref_ms else 0.0
+
     def report(r):
         fb = r["peak"] < tau
         err_c = np.where(fb, r["err_g"], r["err_l"])
-        t_c = r["tl_ms"] + fb.mean() * r["tg_ms"]
+        t_l = r["tl_ms"] + r["n"] * ref_pp_ms
+        t_c = t_l + fb.mean() * r["tg_ms"]
         return {"particles": r["n"],
                 "plain_fp32_global_search": {"particles_per_s": round(job_rate(r["n"], r["tg_ms"], world), 1),
                                   "median_error_deg": round(float(np.median(r["err_g"])), 3)},
-                "proposal_only": {"particles_per_s": round(job_rate(r["n"], r["tl_ms"], world), 1),
+                "proposal_only": {"particles_per_s": round(job_rate(r["n"], t_l, world), 1),
                                   "median_error_deg": round(float(np.median(r["err_l"])), 3),
                                   "within_10deg": round(float(np.mean(r["err_l"] < 10)), 4)},
                 "proposal_with_fallback": {
@@ -926,6 +984,13 @@ def run_learned(args, rank, world, local_rank):
                         "loss_per_epoch": [round(x, 4) for x in losses],
                         "images_per_s": round(args.train_particles * args.epochs / train_s, 1)},
            "fallback_threshold_peak": round(tau, 3),
+           "mode": args.learned_mode,
+           "reference_embedding": ({"ms_per_map": round(float(np.mean(ref_ms)), 2),
+                                    "maps": len(ref_ms),
+                                    "charged_per_particle_over": 50000,
+                                    "note": "6,912 references rendered by the library's "
+                                            "projector and embedded, once per map"}
+                                   if match else None),
            "fsc_0143_resolution_A": {
                k: v for k, v in fsc_res.items()},
            "fsc_note": ("held-out maps: every map reconstructed from its particles at the "
@@ -1150,6 +1215,11 @@ def main():
     ap.add_argument("--learned-snr", type=float, default=1.0,
                     help="noise level of the learned-proposal particles (signal / noise power)")
     ap.add_argument("--learned-lr", type=float, default=2e-3)
+    ap.add_argument("--learned-mode", default="match", choices=["match", "regress"],
+                    help="learned proposal: embedding match against the map's reference "
+                         "projections, or pose regression")
+    ap.add_argument("--learned-tau", type=float, default=0.1,
+                    help="temperature of the matching loss")
     ap.add_argument("--eval-particles-seen", type=int, default=1200)
     ap.add_argument("--eval-particles-unseen", type=int, default=2000)
     ap.add_argument("--batch-uneven", type=int, default=4096,

@@ -304,6 +304,31 @@ int tg3_cnn_adam(tg3_cnn* net, float lr);
 int tg3_cnn_propose(const float* out, int n, int nRot, int nTrans, unsigned long long seed,
                     double* quat, double* trans, void* stream);
 
+/* Matching mode of the same network: outputs 0..63 are an embedding,
+ * compared by cosine with the embeddings of reference projections of the
+ * particle's map; outputs 64..67 stay the shift mean and log-variance.
+ * tg3_cnn_backward adds to the gradient buffer the gradient of a loss whose
+ * derivative with respect to the outputs for images img is dOut [n][68]
+ * (device).
+ * tg3_cnn_contrastive: symmetric InfoNCE of n particles against their n
+ * reference projections (particle i's positive is reference i) on cosine /
+ * tau, plus the Gaussian shift loss against tstar [n][2]; writes dL/d
+ * outputs for both (dOutP, dOutR) and the mean loss.  1 < n <= 1024.
+ * tg3_cnn_embed: normalised embeddings z [n][64] of outputs [n][68].
+ * tg3_cnn_match_propose: per particle, the nRot references of highest cosine
+ * score (ref [nRef][64] normalised, refQuat [nRef][4]; ties to the lower
+ * index) and nTrans translations drawn as tg3_cnn_propose draws them.
+ * nRot <= nRef <= 16384, nTrans <= 512; asynchronous on `stream`. */
+int tg3_cnn_backward(tg3_cnn* net, const float* img, int n, const float* dOut);
+int tg3_cnn_contrastive(tg3_cnn* net, const float* outP, const float* outR, int n,
+                        const double* tstar, float tau, float* dOutP, float* dOutR,
+                        double* loss);
+int tg3_cnn_embed(const float* out, int n, float* z, void* stream);
+int tg3_cnn_match_propose(const float* out, int n, const float* ref, int nRef,
+                          const double* refQuat, int nRot, int nTrans,
+                          unsigned long long seed, double* quat, double* trans,
+                          void* stream);
+
 /* Global scan of nImg images over one shared set of nR rotations and nT
  * translations, for the context's class-`cls` volume: the scan of
  * Optimiser::doGlobalSearch (src/Optimiser.cpp:759-899), the work of

@@ -7,9 +7,9 @@ analytic gradient of that loss with respect to every parameter.  The
 parameter vector holds, layer after layer, the weights (conv [co][ci][3][3],
 dense [out][in]) and then the biases, as the library does.
 
-The tests check this oracle's gradient against central finite differences
-(on a reduced network), and the library's GPU forward and gradient against
-this oracle.  There is no reference counterpart: the network is an addition
+The tests check this oracle's gradients (the pose loss and the matching
+loss) against central finite differences (on a reduced network), and the
+library's GPU forward, gradients and losses against this oracle.  There is no reference counterpart: the network is an addition
 to the E-step (a learned seed for the particle filter's samples).
 """
 import numpy as np
@@ -139,12 +139,62 @@ def forward(params, img, shapes=SHAPES, round_bf16=True):
 
 def loss_and_grad(params, img, Rstar, tstar, shapes=SHAPES, round_bf16=True):
     """Mean loss over the batch and its gradient (the parameter layout)."""
-    lay, total = layout(shapes)
     acts = forward(params, img, shapes, round_bf16)
-    n = len(img)
     loss, g = head_loss(acts[-1], Rstar, tstar)
+    return float(loss.mean()), grad_from_output(params, img, g / len(img), shapes, round_bf16,
+                                                acts)
+
+
+def contrastive(out_p, out_r, tstar, tau):
+    """Matching loss of n particles' outputs against their n references'
+    outputs and its gradient with respect to both: symmetric InfoNCE on the
+    cosine similarities / tau of the normalised embeddings (outputs 0..63;
+    particle i's positive is reference i) plus the Gaussian shift loss of the
+    particles' outputs 64..67 against tstar.  Returns (mean loss, g_p, g_r)."""
+    P = np.asarray(out_p, dtype=np.float64)
+    Rr = np.asarray(out_r, dtype=np.float64)
+    n = len(P)
+    u, v = P[:, :64], Rr[:, :64]
+    fu = 1.0 / np.sqrt((u * u).sum(1, keepdims=True) + 1e-12)
+    fv = 1.0 / np.sqrt((v * v).sum(1, keepdims=True) + 1e-12)
+    zp, zr = u * fu, v * fv
+    S = zp @ zr.T / tau
+    rm = S.max(1, keepdims=True)
+    rowL = rm[:, 0] + np.log(np.exp(S - rm).sum(1))
+    cm = S.max(0, keepdims=True)
+    colL = cm[0] + np.log(np.exp(S - cm).sum(0))
+    d = np.diag(S)
+    mu, lv = P[:, 64:66], P[:, 66:68]
+    diff = tstar - mu
+    e = np.exp(-lv)
+    loss = 0.5 * (rowL - d) + 0.5 * (colL - d) + 0.5 * (diff * diff * e + lv).sum(1)
+    eye = np.eye(n)
+    G = (0.5 / n) * ((np.exp(S - rowL[:, None]) - eye) + (np.exp(S - colL[None, :]) - eye))
+    dzp = G @ zr / tau
+    dzr = G.T @ zp / tau
+
+    def through_norm(x, f, dz):
+        # z = x f, f = (|x|^2 + eps)^-1/2:  dL/dx = f dz - f^3 x (x . dz)
+        return f * dz - f ** 3 * x * (x * dz).sum(1, keepdims=True)
+
+    g_p = np.zeros_like(P)
+    g_r = np.zeros_like(Rr)
+    g_p[:, :64] = through_norm(u, fu, dzp)
+    g_r[:, :64] = through_norm(v, fv, dzr)
+    g_p[:, 64:66] = -diff * e / n
+    g_p[:, 66:68] = 0.5 * (1.0 - diff * diff * e) / n
+    return float(loss.mean()), g_p, g_r
+
+
+def grad_from_output(params, img, gout, shapes=SHAPES, round_bf16=True, acts=None):
+    """Gradient (the parameter layout) of a loss whose derivative with
+    respect to the outputs is gout [n][68]."""
+    lay, total = layout(shapes)
+    if acts is None:
+        acts = forward(params, img, shapes, round_bf16)
+    n = len(img)
     grad = np.zeros(total)
-    gy = g / n
+    gy = np.asarray(gout, dtype=np.float64)
     for li in range(len(shapes) - 1, -1, -1):
         (wo, ws, bo, co), (cin, cout, hin, hout, s) = lay[li], shapes[li]
         W = np.asarray(params[wo:wo + int(np.prod(ws))], dtype=np.float32)
@@ -161,4 +211,4 @@ def loss_and_grad(params, img, Rstar, tstar, shapes=SHAPES, round_bf16=True):
         grad[wo:wo + gW.size] = gW.ravel()
         grad[bo:bo + co] = gb
         gy = gx
-    return float(loss.mean()), grad
+    return grad

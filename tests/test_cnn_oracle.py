@@ -59,3 +59,47 @@ def test_bf16_rounding():
     assert r[0] == 1.0 and r[1] == 1.0
     assert r[2] == np.float32(1.0078125)
     assert abs(r[3] - (-3.140625)) < 1e-7 and r[4] == 0.0
+
+
+def test_contrastive_gradient_matches_finite_differences():
+    rng = np.random.default_rng(17)
+    n, tau = 6, 0.2
+    P = rng.standard_normal((n, 68))
+    Rr = rng.standard_normal((n, 68))
+    t = rng.standard_normal((n, 2))
+    loss, gp, gr = C.contrastive(P, Rr, t, tau)
+    h = 1e-6
+    for X, g in ((P, gp), (Rr, gr)):
+        for (i, j) in [(0, 0), (2, 17), (5, 63), (1, 64), (3, 67), (4, 65)]:
+            Xp, Xm = X.copy(), X.copy()
+            Xp[i, j] += h
+            Xm[i, j] -= h
+            args_p = (Xp, Rr) if X is P else (P, Xp)
+            args_m = (Xm, Rr) if X is P else (P, Xm)
+            fd = (C.contrastive(*args_p, t, tau)[0] - C.contrastive(*args_m, t, tau)[0]) / (2 * h)
+            assert abs(fd - g[i, j]) < 1e-6 * max(1.0, abs(fd)), (i, j, fd, g[i, j])
+
+
+def test_contrastive_prefers_matching_pairs():
+    rng = np.random.default_rng(19)
+    n = 8
+    Z = rng.standard_normal((n, 68))
+    t = np.zeros((n, 2))
+    Z[:, 64:] = 0.0
+    matched = C.contrastive(Z, Z, t, 0.1)[0]
+    shuffled = C.contrastive(Z, Z[::-1].copy(), t, 0.1)[0]
+    assert matched < shuffled
+
+
+def test_output_gradient_backprop_matches_the_pose_loss_path():
+    rng = np.random.default_rng(23)
+    _, total = C.layout(TINY)
+    params = rng.standard_normal(total) * 0.1
+    img = rng.standard_normal((3, TINY[0][2], TINY[0][2]))
+    R = _rot(rng, 3)
+    t = rng.standard_normal((3, 2))
+    loss, grad = C.loss_and_grad(params, img, R, t, TINY, round_bf16=False)
+    acts = C.forward(params, img, TINY, round_bf16=False)
+    _, g = C.head_loss(acts[-1], R, t)
+    np.testing.assert_allclose(C.grad_from_output(params, img, g / 3, TINY, round_bf16=False),
+                               grad, rtol=1e-12, atol=1e-14)

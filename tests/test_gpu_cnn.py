@@ -100,3 +100,77 @@ def test_proposals_follow_the_outputs():
     # drawn rotations stay near their components (within a few 1/sqrt(kappa))
     ang = np.radians(learned.angle_deg(q[:, 8:, None, :], centres[:, None, :, :])).min(-1)
     assert (ang <= 6.0 / np.sqrt(kap.min(1))[:, None] + 1e-9).all()
+
+
+def test_contrastive_loss_matches_oracle(net):
+    rng = np.random.default_rng(31)
+    n, tau = 40, 0.1
+    P = rng.standard_normal((n, tg3.Cnn.N_OUT)).astype(np.float32)
+    Rr = rng.standard_normal((n, tg3.Cnn.N_OUT)).astype(np.float32)
+    t = rng.standard_normal((n, 2))
+    dP = torch.empty((n, tg3.Cnn.N_OUT), dtype=torch.float32, device=DEV)
+    dR = torch.empty_like(dP)
+    loss = net.contrastive(torch.as_tensor(P).to(DEV), torch.as_tensor(Rr).to(DEV),
+                           torch.as_tensor(t).to(DEV), tau, dP, dR)
+    ref_loss, gp, gr = C.contrastive(P, Rr, t, tau)
+    assert abs(loss - ref_loss) < 1e-5 * max(1.0, abs(ref_loss)), (loss, ref_loss)
+    for got, ref in ((dP.cpu().numpy(), gp), (dR.cpu().numpy(), gr)):
+        assert np.abs(got - ref).max() < 1e-4 * np.abs(ref).max()
+
+
+def test_backward_from_outputs_matches_oracle(net):
+    img, _, _ = _batch(3, 37)
+    rng = np.random.default_rng(41)
+    g_out = (rng.standard_normal((3, tg3.Cnn.N_OUT)) * 0.1).astype(np.float32)
+    net.set_bf16(False)
+    net.zero_grads()
+    net.backward(torch.as_tensor(img).to(DEV), torch.as_tensor(g_out).to(DEV))
+    g = net.grads().astype(np.float64)
+    net.set_bf16(True)
+    ref = C.grad_from_output(net.params(), img, g_out, round_bf16=False)
+    lay, _ = C.layout()
+    for li, (wo, ws, bo, co) in enumerate(lay):
+        nw = int(np.prod(ws))
+        for name, a, b in (("w", wo, wo + nw), ("b", bo, bo + co)):
+            d = np.linalg.norm(g[a:b] - ref[a:b])
+            r = np.linalg.norm(ref[a:b])
+            assert d <= 2e-3 * r + 1e-7, (li, name, d, r)
+    net.zero_grads()
+
+
+def test_match_proposals_are_the_best_references():
+    rng = np.random.default_rng(43)
+    n, n_ref, n_rot, n_trans = 5, 300, 40, 9
+    out = rng.standard_normal((n, tg3.Cnn.N_OUT)).astype(np.float32)
+    ref = rng.standard_normal((n_ref, 64)).astype(np.float32)
+    ref[7] = ref[3]                        # a tie: the lower index comes first
+    ref /= np.linalg.norm(ref, axis=1, keepdims=True)
+    rq = rng.standard_normal((n_ref, 4))
+    rq /= np.linalg.norm(rq, axis=1, keepdims=True)
+    od = torch.as_tensor(out).to(DEV)
+    q = torch.empty((n, n_rot, 4), dtype=torch.float64, device=DEV)
+    t = torch.empty((n, n_trans, 2), dtype=torch.float64, device=DEV)
+    tg3.Cnn.match_propose(od, torch.as_tensor(ref).to(DEV), torch.as_tensor(rq).to(DEV), n_rot,
+                          n_trans, 11, q, t)
+    q2 = torch.empty((n, tg3.Cnn.N_OUT // 8 * 8, 4), dtype=torch.float64, device=DEV)
+    t2 = torch.empty_like(t)
+    tg3.Cnn.propose(od, q2.shape[1], n_trans, 11, q2, t2)
+    z = torch.empty((n, 64), dtype=torch.float32, device=DEV)
+    tg3.Cnn.embed(od, z)
+    torch.cuda.synchronize()
+    zp = z.cpu().numpy()
+    np.testing.assert_allclose(zp, out[:, :64] / np.linalg.norm(out[:, :64], axis=1,
+                                                                keepdims=True), rtol=1e-5)
+    score = zp.astype(np.float64) @ ref.T.astype(np.float64)
+    q = q.cpu().numpy()
+    for l in range(n):
+        sel = np.array([int(np.argmin(np.abs(rq - q[l, j]).sum(1))) for j in range(n_rot)])
+        np.testing.assert_array_equal(rq[sel], q[l])
+        # the selected set is the top n_rot by score (float32 scores: allow a
+        # near-tie at the boundary), in descending order
+        order = np.argsort(-score[l], kind="stable")
+        assert len(set(sel) ^ set(order[:n_rot])) <= 2
+        assert np.all(np.diff(score[l, sel]) <= 1e-5)
+        if 3 in sel and 7 in sel:
+            assert list(sel).index(3) < list(sel).index(7)
+    np.testing.assert_array_equal(t.cpu().numpy(), t2.cpu().numpy())

@@ -315,7 +315,7 @@ __global__ void k_head_loss(const float* __restrict__ out, const double* __restr
     const double* Rs = Rstar + (size_t)n * 9;
     const V3 r1 = v3(Rs[0], Rs[3], Rs[6]), r2 = v3(Rs[1], Rs[4], Rs[7]), r3 = v3(Rs[2], Rs[5], Rs[8]);
     double lp[kComp], c[kComp], kap[kComp], maxlp = -1e300;
-    V3 b1s[kComp], b2s[kComp], a1s[kComp], a2s[kComp];
+    V3 b1s[kComp], b2s[kComp], a2s[kComp];
     double n1s[kComp], n2s[kComp];
     // log-softmax of the logits
     double lmax = -1e300;
@@ -339,7 +339,6 @@ __global__ void k_head_loss(const float* __restrict__ out, const double* __restr
         maxlp = fmax(maxlp, lp[k]);
         b1s[k] = b1;
         b2s[k] = b2;
-        a1s[k] = a1;
         a2s[k] = a2;
         n1s[k] = n1;
         n2s[k] = n2;
@@ -410,6 +409,19 @@ __device__ inline double normal(uint64_t seed, uint64_t a, uint64_t b)
 {
     const double u1 = u01(seed, a, 2 * b), u2 = u01(seed, a, 2 * b + 1);
     return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+// nTrans translations ~ N(mu, exp(lv)) from outputs 64..67, the first one
+// the mean (counter-based draws, the same for every proposal kernel).
+__device__ void propose_trans(const float* o, int l, int nTrans, uint64_t seed,
+                              double* __restrict__ trans)
+{
+    for (int j = threadIdx.x; j < nTrans; j += blockDim.x)
+        for (int d = 0; d < 2; d++) {
+            const double mu = o[64 + d], sd = exp(0.5 * (double)o[66 + d]);
+            trans[((size_t)l * nTrans + j) * 2 + d] =
+                j == 0 ? mu : mu + sd * normal(seed, (uint64_t)l * 1024 + 512 + j, d);
+        }
 }
 
 // One CTA per particle: decode its 8 components, draw nRot rotations
@@ -497,12 +509,192 @@ __global__ void k_propose(const float* __restrict__ out, int nRot, int nTrans, u
         qo[2] = y / nq;
         qo[3] = z / nq;
     }
-    for (int j = threadIdx.x; j < nTrans; j += blockDim.x)
-        for (int d = 0; d < 2; d++) {
-            const double mu = o[64 + d], sd = exp(0.5 * (double)o[66 + d]);
-            trans[((size_t)l * nTrans + j) * 2 + d] =
-                j == 0 ? mu : mu + sd * normal(seed, (uint64_t)l * 1024 + 512 + j, d);
+    propose_trans(o, l, nTrans, seed, trans);
+}
+
+// ------------------------------------------------------------------------
+// Matching mode: outputs 0..63 are an embedding, compared by cosine with
+// the embeddings of reference projections of the particle's map.
+constexpr int kEmb = 64;
+
+// z = u / sqrt(|u|^2 + 1e-12) for u = out[row][0..63]; inv[row] = the factor.
+__global__ void k_emb_norm(const float* __restrict__ out, int n, float* __restrict__ z,
+                           float* __restrict__ inv)
+{
+    const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const float* u = out + (size_t)row * kOut;
+    const float a = u[lane], b = u[lane + 32];
+    float s = a * a + b * b;
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const float f = 1.0f / sqrtf(s + 1e-12f);
+    z[(size_t)row * kEmb + lane] = a * f;
+    z[(size_t)row * kEmb + lane + 32] = b * f;
+    if (lane == 0 && inv) inv[row] = f;
+}
+
+// S[i][j] = zp[i] . zr[j] / tau
+__global__ void k_emb_sim(const float* __restrict__ zp, const float* __restrict__ zr, int n,
+                          float invTau, float* __restrict__ S)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (j >= n) return;
+    const float* a = zp + (size_t)i * kEmb;
+    const float* b = zr + (size_t)j * kEmb;
+    float acc = 0.f;
+#pragma unroll 16
+    for (int d = 0; d < kEmb; d++) acc = fmaf(a[d], b[d], acc);
+    S[(size_t)i * n + j] = acc * invTau;
+}
+
+// log-sum-exp of every row (blockIdx.y = 0) and column (1) of S
+__global__ void k_emb_lse(const float* __restrict__ S, int n, float* __restrict__ rowL,
+                          float* __restrict__ colL)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bool rows = blockIdx.y == 0;
+    const size_t st = rows ? 1 : (size_t)n, base = rows ? (size_t)i * n : (size_t)i;
+    float m = -INFINITY;
+    for (int k = 0; k < n; k++) m = fmaxf(m, S[base + k * st]);
+    double acc = 0.0;
+    for (int k = 0; k < n; k++) acc += exp((double)(S[base + k * st] - m));
+    (rows ? rowL : colL)[i] = m + (float)log(acc);
+}
+
+// G = dL/dS for L = (1/n) sum_i 0.5 (rowL_i - S_ii) + 0.5 (colL_i - S_ii)
+__global__ void k_emb_dS(const float* __restrict__ S, const float* __restrict__ rowL,
+                         const float* __restrict__ colL, int n, float* __restrict__ G)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (j >= n) return;
+    const float sij = S[(size_t)i * n + j];
+    const float d = i == j ? 1.f : 0.f;
+    G[(size_t)i * n + j] = (0.5f / n) * ((expf(sij - rowL[i]) - d) + (expf(sij - colL[j]) - d));
+}
+
+// dOut rows: blockIdx.y = 0 particles (embedding part from G zr, shift part
+// from the Gaussian shift loss), 1 references (embedding part from G^T zp,
+// zero shift part).  One CTA of 64 threads per row.
+__global__ void k_emb_grad(const float* __restrict__ G, const float* __restrict__ zp,
+                           const float* __restrict__ zr, const float* __restrict__ invP,
+                           const float* __restrict__ invR, const float* __restrict__ outP,
+                           const double* __restrict__ tstar, int n, float invTau,
+                           const float* __restrict__ S, const float* __restrict__ rowL,
+                           const float* __restrict__ colL, float* __restrict__ dP,
+                           float* __restrict__ dR, double* __restrict__ loss)
+{
+    __shared__ float red[2];
+    const int i = blockIdx.x, d = threadIdx.x;
+    const bool part = blockIdx.y == 0;
+    const float* zo = part ? zr : zp;            // the other side
+    const float* zs = part ? zp : zr;            // this side
+    float acc = 0.f;
+    for (int k = 0; k < n; k++) {
+        const float g = part ? G[(size_t)i * n + k] : G[(size_t)k * n + i];
+        acc = fmaf(g, zo[(size_t)k * kEmb + d], acc);
+    }
+    const float dz = acc * invTau;
+    const float zi = zs[(size_t)i * kEmb + d];
+    float c = zi * dz;
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((d & 31) == 0) red[d >> 5] = c;
+    __syncthreads();
+    const float zdz = red[0] + red[1];
+    const float f = part ? invP[i] : invR[i];
+    float* dOut = (part ? dP : dR) + (size_t)i * kOut;
+    dOut[d] = f * (dz - zi * zdz);
+    if (d < 4) {
+        if (!part) {
+            dOut[kEmb + d] = 0.f;
+        } else if (d < 2) {
+            const float* o = outP + (size_t)i * kOut;
+            const double mu = o[64 + d], lv = o[66 + d];
+            const double diff = tstar[2 * (size_t)i + d] - mu, e = exp(-lv);
+            dOut[64 + d] = (float)(-diff * e / n);
+            dOut[66 + d] = (float)(0.5 * (1.0 - diff * diff * e) / n);
         }
+    }
+    if (part && d == 0) {
+        const float* o = outP + (size_t)i * kOut;
+        double sh = 0.0;
+        for (int k = 0; k < 2; k++) {
+            const double mu = o[64 + k], lv = o[66 + k];
+            const double diff = tstar[2 * (size_t)i + k] - mu;
+            sh += 0.5 * (diff * diff * exp(-lv) + lv);
+        }
+        const double sii = S[(size_t)i * n + i];
+        loss[i] = 0.5 * ((double)rowL[i] - sii) + 0.5 * ((double)colL[i] - sii) + sh;
+    }
+}
+
+// One CTA per particle: cosine scores of its embedding against nRef
+// normalised reference embeddings, the nRot best references (descending
+// score, ties to the lower index: a bitonic sort of 64-bit keys in shared
+// memory) as the rotation proposals, and nTrans translations as k_propose.
+__global__ void __launch_bounds__(256)
+k_match_propose(const float* __restrict__ out, const float* __restrict__ ref, int nRef,
+                int nPow2, const double* __restrict__ refQuat, int nRot, int nTrans,
+                uint64_t seed, double* __restrict__ quat, double* __restrict__ trans)
+{
+    extern __shared__ unsigned long long key[];          // [nPow2]
+    __shared__ float zp[kEmb];
+    __shared__ float red[8];
+    const int l = blockIdx.x;
+    const float* o = out + (size_t)l * kOut;
+    if (threadIdx.x < kEmb) {
+        const float a = o[threadIdx.x];
+        float s = a * a;
+        for (int k = 16; k; k >>= 1) s += __shfl_xor_sync(0xffffffffu, s, k);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < kEmb) zp[threadIdx.x] = o[threadIdx.x] / sqrtf(red[0] + red[1] + 1e-12f);
+    __syncthreads();
+    for (int j = threadIdx.x; j < nPow2; j += blockDim.x) {
+        unsigned long long k = 0;                        // padding sorts last
+        if (j < nRef) {
+            const float4* r = reinterpret_cast<const float4*>(ref + (size_t)j * kEmb);
+            float acc = 0.f;
+#pragma unroll
+            for (int q = 0; q < kEmb / 4; q++) {
+                const float4 v = __ldg(r + q);
+                acc = fmaf(zp[4 * q], v.x, acc);
+                acc = fmaf(zp[4 * q + 1], v.y, acc);
+                acc = fmaf(zp[4 * q + 2], v.z, acc);
+                acc = fmaf(zp[4 * q + 3], v.w, acc);
+            }
+            // order-preserving map of the float score, then the inverted index
+            const unsigned int b = __float_as_uint(acc);
+            const unsigned int ob = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+            k = ((unsigned long long)ob << 32) | (0xFFFFFFFFu - (unsigned int)j);
+        }
+        key[j] = k;
+    }
+    __syncthreads();
+    // bitonic sort, descending
+    for (int size = 2; size <= nPow2; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < nPow2 / 2; t += blockDim.x) {
+                const int lo = 2 * t - (t & (stride - 1));
+                const int hi = lo + stride;
+                const bool desc = (lo & size) == 0;
+                const unsigned long long a = key[lo], b = key[hi];
+                if ((a < b) == desc) {
+                    key[lo] = b;
+                    key[hi] = a;
+                }
+            }
+            __syncthreads();
+        }
+    for (int j = threadIdx.x; j < nRot; j += blockDim.x) {
+        const int idx = (int)(0xFFFFFFFFu - (unsigned int)(key[j] & 0xFFFFFFFFu));
+        const double* src = refQuat + 4 * (size_t)idx;
+        double* qo = quat + ((size_t)l * nRot + j) * 4;
+        for (int c = 0; c < 4; c++) qo[c] = src[c];
+    }
+    propose_trans(o, l, nTrans, seed, trans);
 }
 
 __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
@@ -541,6 +733,10 @@ struct tg3_cnn {
     float* gact[kLayers + 1] = {};
     double* Rstar = nullptr;
     double* loss = nullptr;
+    // contrastive scratch (matching mode), grown as needed
+    int embCap = 0;
+    float* emb = nullptr;       // zp, zr [n][64]; invP, invR [n]; rowL, colL [n]; S, G [n][n]
+    double* embLoss = nullptr;
 };
 
 namespace {
@@ -704,6 +900,8 @@ extern "C" int tg3_cnn_destroy(tg3_cnn* net)
     }
     cudaFree(net->Rstar);
     cudaFree(net->loss);
+    cudaFree(net->emb);
+    cudaFree(net->embLoss);
     cudaFree(net->params);
     cudaFree(net->grads);
     cudaFree(net->m);
@@ -816,5 +1014,107 @@ extern "C" int tg3_cnn_propose(const float* out, int n, int nRot, int nTrans,
     k_propose<<<n, 256, 0, static_cast<cudaStream_t>(stream)>>>(out, nRot, nTrans, seed, quat,
                                                                  trans);
     TG3_LAUNCH_CHECK("proposals");
+    return TG3_OK;
+}
+
+// Add to the gradient buffer the gradient of a loss whose derivative with
+// respect to the outputs for images img [n][64][64] is dOut [n][68]
+// (device; the forward pass is run again to rebuild the activations).
+extern "C" int tg3_cnn_backward(tg3_cnn* net, const float* img, int n, const float* dOut)
+{
+    if (!net || !img || !dOut || n <= 0) return fail(TG3_ERR_ARG, "bad backward arguments");
+    TG3_CUDA(cudaSetDevice(net->device));
+    int st = ensure_capacity(net, n);
+    if (st) return st;
+    cudaStream_t s = net->stream;
+    TG3_CUDA(cudaMemcpyAsync(net->act[0], img, sizeof(float) * 64 * 64 * n,
+                             cudaMemcpyDeviceToDevice, s));
+    if ((st = forward(net, n))) return st;
+    TG3_CUDA(cudaMemcpyAsync(net->gact[kLayers], dOut, sizeof(float) * kOut * n,
+                             cudaMemcpyDeviceToDevice, s));
+    return backward(net, n);
+}
+
+// Matching loss of a batch of n particles and their n reference
+// projections (outputs outP, outR [n][68], device): symmetric InfoNCE on the
+// cosine similarities / tau of the normalised embeddings (outputs 0..63),
+// particle i's positive being reference i, plus the Gaussian shift loss of
+// the particles' outputs 64..67 against tstar [n][2].  Writes dL/d outputs
+// (dOutP, dOutR) and the mean loss (host).  n <= 1024.
+extern "C" int tg3_cnn_contrastive(tg3_cnn* net, const float* outP, const float* outR, int n,
+                                   const double* tstar, float tau, float* dOutP, float* dOutR,
+                                   double* lossOut)
+{
+    if (!net || !outP || !outR || !tstar || !dOutP || !dOutR || n <= 1 || n > 1024 ||
+        !(tau > 0.f))
+        return fail(TG3_ERR_ARG, "bad contrastive arguments (1 < n <= 1024, tau > 0)");
+    TG3_CUDA(cudaSetDevice(net->device));
+    cudaStream_t s = net->stream;
+    if (n > net->embCap) {
+        TG3_CUDA(cudaStreamSynchronize(s));
+        cudaFree(net->emb);
+        cudaFree(net->embLoss);
+        net->emb = nullptr;
+        net->embLoss = nullptr;
+        net->embCap = 0;
+        TG3_CUDA(cudaMalloc(&net->emb, sizeof(float) * ((size_t)2 * kEmb * n + 4 * n +
+                                                        2 * (size_t)n * n)));
+        TG3_CUDA(cudaMalloc(&net->embLoss, sizeof(double) * n));
+        net->embCap = n;
+    }
+    float* zp = net->emb;
+    float* zr = zp + (size_t)kEmb * n;
+    float* invP = zr + (size_t)kEmb * n;
+    float* invR = invP + n;
+    float* rowL = invR + n;
+    float* colL = rowL + n;
+    float* S = colL + n;
+    float* G = S + (size_t)n * n;
+    const float invTau = 1.0f / tau;
+    k_emb_norm<<<(n + 7) / 8, 256, 0, s>>>(outP, n, zp, invP);
+    k_emb_norm<<<(n + 7) / 8, 256, 0, s>>>(outR, n, zr, invR);
+    k_emb_sim<<<dim3((n + 127) / 128, n), 128, 0, s>>>(zp, zr, n, invTau, S);
+    k_emb_lse<<<dim3((n + 127) / 128, 2), 128, 0, s>>>(S, n, rowL, colL);
+    k_emb_dS<<<dim3((n + 127) / 128, n), 128, 0, s>>>(S, rowL, colL, n, G);
+    k_emb_grad<<<dim3(n, 2), kEmb, 0, s>>>(G, zp, zr, invP, invR, outP, tstar, n, invTau, S, rowL,
+                                           colL, dOutP, dOutR, net->embLoss);
+    TG3_LAUNCH_CHECK("contrastive loss");
+    std::vector<double> h(n);
+    TG3_CUDA(cudaMemcpyAsync(h.data(), net->embLoss, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaStreamSynchronize(s));
+    double sum = 0;
+    for (double x : h) sum += x;
+    if (lossOut) *lossOut = sum / n;
+    return TG3_OK;
+}
+
+// Normalised embeddings z [n][64] of outputs out [n][68] (device).
+extern "C" int tg3_cnn_embed(const float* out, int n, float* z, void* stream)
+{
+    if (!out || !z || n <= 0) return fail(TG3_ERR_ARG, "bad embed arguments");
+    k_emb_norm<<<(n + 7) / 8, 256, 0, static_cast<cudaStream_t>(stream)>>>(out, n, z, nullptr);
+    TG3_LAUNCH_CHECK("embeddings");
+    return TG3_OK;
+}
+
+// Rotation proposals by matching: for every particle (outputs out [n][68]),
+// the nRot references of highest cosine score (ref [nRef][64] normalised,
+// refQuat [nRef][4]), and nTrans translations from the shift outputs.
+extern "C" int tg3_cnn_match_propose(const float* out, int n, const float* ref, int nRef,
+                                     const double* refQuat, int nRot, int nTrans,
+                                     unsigned long long seed, double* quat, double* trans,
+                                     void* stream)
+{
+    if (!out || !ref || !refQuat || !quat || !trans || n <= 0 || nRef <= 0 || nRef > 16384 ||
+        nRot <= 0 || nRot > nRef || nTrans <= 0 || nTrans > 512)
+        return fail(TG3_ERR_ARG, "bad match arguments (nRot <= nRef <= 16384, nTrans <= 512)");
+    int p2 = 1;
+    while (p2 < nRef) p2 <<= 1;
+    const size_t smem = sizeof(unsigned long long) * p2;
+    TG3_CUDA(cudaFuncSetAttribute(k_match_propose, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    k_match_propose<<<n, 256, smem, static_cast<cudaStream_t>(stream)>>>(
+        out, ref, nRef, p2, refQuat, nRot, nTrans, seed, quat, trans);
+    TG3_LAUNCH_CHECK("match proposals");
     return TG3_OK;
 }

@@ -33,7 +33,8 @@ EXPORTS = [
     "tg3_ragged_plan_create", "tg3_ragged_plan_run", "tg3_ragged_plan_info",
     "tg3_ragged_plan_destroy", "tg3_cnn_create", "tg3_cnn_destroy", "tg3_cnn_param_count",
     "tg3_cnn_params", "tg3_cnn_grads", "tg3_cnn_set_bf16", "tg3_cnn_forward", "tg3_cnn_loss",
-    "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose",
+    "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose", "tg3_cnn_backward",
+    "tg3_cnn_contrastive", "tg3_cnn_embed", "tg3_cnn_match_propose",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
@@ -114,6 +115,11 @@ def lib():
             "tg3_cnn_zero_grads": ([_P], _I),
             "tg3_cnn_adam": ([_P, ctypes.c_float], _I),
             "tg3_cnn_propose": ([_P, _I, _I, _I, ctypes.c_ulonglong, _P, _P, _P], _I),
+            "tg3_cnn_backward": ([_P, _P, _I, _P], _I),
+            "tg3_cnn_contrastive": ([_P, _P, _P, _I, _P, _F, _P, _P, _P], _I),
+            "tg3_cnn_embed": ([_P, _I, _P, _P], _I),
+            "tg3_cnn_match_propose": ([_P, _I, _P, _I, _P, _I, _I, ctypes.c_ulonglong, _P, _P,
+                                       _P], _I),
             "tg3_ctx_stage_times": ([_P, _P, _P, _I], _I),
             "tg3_noalloc_scratch_bytes": ([], ctypes.c_size_t),
             "tg3_global_scan_d": ([_P, _I, _I, _I, _I] + [_P] * 12 + [_I], _I),
@@ -387,6 +393,31 @@ class Cnn:
 
     def adam(self, lr: float):
         check(lib().tg3_cnn_adam(self.h, lr))
+
+    def backward(self, img, d_out):
+        """Add the gradient of a loss with d loss / d outputs = d_out [n][68]."""
+        check(lib().tg3_cnn_backward(self.h, ptr(img), img.shape[0], ptr(d_out)))
+
+    def contrastive(self, out_p, out_r, tstar, tau, d_p, d_r) -> float:
+        """Matching loss of particles against their references (device
+        tensors); fills d_p, d_r with d loss / d outputs; returns the loss."""
+        v = ctypes.c_double()
+        check(lib().tg3_cnn_contrastive(self.h, ptr(out_p), ptr(out_r), out_p.shape[0],
+                                        ptr(tstar), float(tau), ptr(d_p), ptr(d_r),
+                                        ctypes.byref(v)))
+        return v.value
+
+    @staticmethod
+    def embed(out, z, stream=None):
+        check(lib().tg3_cnn_embed(ptr(out), out.shape[0], ptr(z), stream))
+
+    @staticmethod
+    def match_propose(out, ref, ref_quat, n_rot, n_trans, seed, quat, trans, stream=None):
+        """Rotations: the n_rot references of highest score; translations as
+        propose (device tensors; ref [nRef][64] normalised, ref_quat [nRef][4])."""
+        check(lib().tg3_cnn_match_propose(ptr(out), out.shape[0], ptr(ref), ref.shape[0],
+                                          ptr(ref_quat), n_rot, n_trans, seed, ptr(quat),
+                                          ptr(trans), stream))
 
     def close(self):
         if self.h:

@@ -1,11 +1,16 @@
 """Learned proposal: training the pose network and drawing hypotheses from it.
 
-The network (tg3.Cnn, all kernels the library's own) maps a particle's
-64 x 64 image to a mixture of 8 rotations (6-D representation, concentration,
-weight) and a Gaussian shift.  Its proposals seed the particle filter in
-place of the uniform global initialisation: every proposed hypothesis is
-rescored by the exact likelihood (tg3_local_phase_d), and the plain global
-search remains the fallback.
+The network (tg3.Cnn, all kernels the library's own) runs in one of two
+modes on a particle's 64 x 64 image:
+- regression: outputs a mixture of 8 rotations (6-D representation,
+  concentration, weight) and a Gaussian shift; proposals are drawn from it;
+- matching: outputs an embedding (compared by cosine with the embeddings of
+  clean reference projections of the particle's map) and the same Gaussian
+  shift; proposals are the best-matching reference rotations.
+Either way the proposals seed the particle filter in place of the uniform
+global initialisation: every proposed hypothesis is rescored by the exact
+likelihood (tg3_local_phase_d), and the plain global search remains the
+fallback.
 """
 from __future__ import annotations
 
@@ -117,6 +122,106 @@ def train(net, images, Rstar, tstar, epochs: int, batch: int, lr: float, seed: i
             net.adam(lr * 0.5 * (1 + math.cos(math.pi * k / max(steps, 1))))
             k += 1
         losses.append(tot / max(n // batch, 1))
+        if log:
+            log(f"epoch {e}: loss {losses[-1]:.4f}")
+    return losses
+
+
+# --------------------------------------------------------------------------
+# Matching mode: the same network embeds particle images and clean reference
+# projections of the particle's map (outputs 0..63, compared by cosine), so
+# its proposals follow the map it is given, not the maps it was trained on.
+# --------------------------------------------------------------------------
+def image_grid(img: int = 64):
+    """(iCol, iRow) of the img x img image's rfft grid, rows in FFT order
+    (the order of the particle images' transforms)."""
+    h = img // 2
+    jj = np.concatenate([np.arange(0, h), np.arange(-h, 0)])
+    ii = np.arange(0, h + 1)
+    J, I = np.meshgrid(jj, ii, indexing="ij")
+    return I.ravel().astype(np.int32), J.ravel().astype(np.int32)
+
+
+def render_references(ctx, cls: int, quats: np.ndarray, box: int, img: int = 64,
+                      chunk: int = 4096):
+    """Clean projections of the context's class-`cls` volume at `quats` (the
+    library's projector over the img x img rfft grid at the box's
+    frequencies), as the network sees particles: to real space, centred, zero
+    mean and unit deviation.  Returns a device float32 tensor [n][img][img].
+    Leaves the context's pixel set at that grid."""
+    import torch
+    iCol, iRow = image_grid(img)
+    ctx.set_pixels(iCol, iRow, box)
+    dev = f"cuda:{torch.cuda.current_device()}"
+    n = len(quats)
+    h = img // 2
+    out = torch.empty((n, img, img), dtype=torch.float32, device=dev)
+    for s in range(0, n, chunk):
+        m = min(chunk, n - s)
+        R = torch.as_tensor(synth.quat_to_mat(quats[s:s + m]).reshape(m, 9)).to(dev)
+        P = torch.empty((m, len(iCol)), dtype=torch.complex64, device=dev)
+        ctx.project(cls, R, m, P)
+        ctx.sync()
+        ims = torch.fft.irfft2(P.view(m, img, h + 1), s=(img, img))
+        ims = torch.fft.fftshift(ims, dim=(-2, -1))
+        ims = ims - ims.mean(dim=(-2, -1), keepdim=True)
+        out[s:s + m] = ims / ims.std(dim=(-2, -1), keepdim=True)
+    return out
+
+
+def reference_embeddings(net, refs, chunk: int = 4096):
+    """Normalised embeddings [n][64] of reference images [n][64][64]."""
+    import torch
+    n = refs.shape[0]
+    z = torch.empty((n, 64), dtype=torch.float32, device=refs.device)
+    out = torch.empty((min(chunk, n), net.N_OUT), dtype=torch.float32, device=refs.device)
+    for s in range(0, n, chunk):
+        m = min(chunk, n - s)
+        net.forward(refs[s:s + m].contiguous(), out[:m])
+        net.embed(out[:m], z[s:s + m])
+    torch.cuda.synchronize()
+    return z
+
+
+def train_match(net, images, refs, tstar, cls, epochs: int, batch: int, lr: float,
+                tau: float = 0.1, seed: int = 0, log=None):
+    """Minibatch Adam on the matching loss: particle images [n][64][64] and
+    the clean references at their true rotations [n][64][64], shifts tstar
+    [n][2] (device tensors); every batch holds particles of one map
+    (cls [n]), so its negatives are other poses of that map.  Cosine-decayed
+    learning rate; returns the mean loss of every epoch."""
+    import torch
+    rng = np.random.default_rng(seed)
+    cls = np.asarray(cls)
+    groups = [np.nonzero(cls == c)[0] for c in np.unique(cls)]
+    per_epoch = sum(len(g) // batch for g in groups)
+    steps = epochs * per_epoch
+    dev = images.device
+    outP = torch.empty((batch, net.N_OUT), dtype=torch.float32, device=dev)
+    outR = torch.empty_like(outP)
+    dP = torch.empty_like(outP)
+    dR = torch.empty_like(outP)
+    k = 0
+    losses = []
+    for e in range(epochs):
+        batches = []
+        for g in groups:
+            p = rng.permutation(g)
+            batches += [p[b * batch:(b + 1) * batch] for b in range(len(g) // batch)]
+        order = rng.permutation(len(batches))
+        tot = 0.0
+        for bi in order:
+            idx = torch.as_tensor(batches[bi], device=dev)
+            ip, ir = images[idx].contiguous(), refs[idx].contiguous()
+            net.forward(ip, outP)
+            net.forward(ir, outR)
+            net.zero_grads()
+            tot += net.contrastive(outP, outR, tstar[idx].contiguous(), tau, dP, dR)
+            net.backward(ip, dP)
+            net.backward(ir, dR)
+            net.adam(lr * 0.5 * (1 + math.cos(math.pi * k / max(steps, 1))))
+            k += 1
+        losses.append(tot / max(per_epoch, 1))
         if log:
             log(f"epoch {e}: loss {losses[-1]:.4f}")
     return losses
