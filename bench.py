@@ -816,12 +816,23 @@ def run_learned(args, rank, world, local_rank):
             ref_ms.append((time.perf_counter() - ta) * 1e3)
         return ref_emb[c]
 
+    bank_ms = {}
+
     def evaluate(ps, name):
         n = len(ps.cls)
         if match:
             for c in np.unique(ps.cls):
                 embeddings_of(int(c))
         ctx.set_pixels(ps.iCol, ps.iRow, box)
+        if match:
+            # each map's projections at the 6,912 references, made once and
+            # gathered by the proposals' indices (timed with the embeddings)
+            for c in np.unique(ps.cls):
+                torch.cuda.synchronize()
+                ta = time.perf_counter()
+                ctx.set_bank(int(c), quats_g_dev, nRg)
+                ctx.sync()
+                bank_ms[int(c)] = (time.perf_counter() - ta) * 1e3
         d = dict(dat=torch.as_tensor(ps.dat).to(dev), ctf=torch.as_tensor(ps.ctf).to(dev),
                  sig=torch.as_tensor(ps.sigRcp).to(dev))
         f64 = dict(dtype=torch.float64, device=dev)
@@ -873,38 +884,65 @@ def run_learned(args, rank, world, local_rank):
 
         qd = torch.empty((n, nR, 4), **f64)
         td = torch.empty((n, nT, 2), **f64)
+        bidx = torch.empty((n, nR), dtype=torch.int32, device=dev)
+        pRl = torch.full((n, nR), 1.0 / nR, **f64)
+        pTl = torch.full((n, nT), 1.0 / nT, **f64)
+        pCl = torch.ones(n, **f64)
 
         grp = [(int(c), torch.as_tensor(np.nonzero(ps.cls == c)[0], device=dev))
                for c in np.unique(ps.cls)]
 
+        marks = []
+
         def learned_all():
             # network, proposals and exact rescoring, all on the device
+            marks.clear()
+            marks.append(time.perf_counter())
             net.forward(ps.images, out)
+            marks.append(time.perf_counter())
             if match:
                 # per map: the best-matching references of that map's embeddings
                 for c, idx in grp:
                     og_ = out[idx].contiguous()
                     qg_ = torch.empty((len(idx), nR, 4), **f64)
                     tg_ = torch.empty((len(idx), nT, 2), **f64)
-                    tg3.Cnn.match_propose(og_, ref_emb[c], quats_g_dev, nR, nT, 99, qg_, tg_)
+                    ig_ = torch.empty((len(idx), nR), dtype=torch.int32, device=dev)
+                    tg3.Cnn.match_propose(og_, ref_emb[c], quats_g_dev, nR, nT, 99, qg_, tg_,
+                                          ig_)
                     qd[idx] = qg_
                     td[idx] = tg_
+                    bidx[idx] = ig_
                 torch.cuda.synchronize()
             else:
                 tg3.Cnn.propose(out, nR, nT, 99, qd, td, ctx.stream)
-            ctx.local_phase(n, nR, nT, d["dat"], d["ctf"], d["sig"], qd, td,
-                            torch.full((n, nR), 1.0 / nR, **f64), torch.full((n, nT), 1.0 / nT, **f64),
-                            torch.ones(n, **f64), cls_d, ol["wC"], ol["wR"], ol["wT"], ol["base"],
-                            ol["dvp"], prec)
+                ctx.sync()
+            marks.append(time.perf_counter())
+            if match:
+                ctx.local_phase_bank(n, nR, nT, d["dat"], d["ctf"], d["sig"], bidx, td, pRl, pTl,
+                                     pCl, cls_d, ol["wC"], ol["wR"], ol["wT"], ol["base"],
+                                     ol["dvp"], prec)
+            else:
+                ctx.local_phase(n, nR, nT, d["dat"], d["ctf"], d["sig"], qd, td, pRl, pTl, pCl,
+                                cls_d, ol["wC"], ol["wR"], ol["wT"], ol["base"], ol["dvp"], prec)
             ctx.sync()
-            return qd.cpu().numpy()
+            marks.append(time.perf_counter())
+            q_host = qd.cpu().numpy()
+            marks.append(time.perf_counter())
+            return q_host
 
         learned_all()
         torch.cuda.synchronize()
+        ctx.set_timing(True)
+        ctx.stage_times(reset=True)
         ta = time.perf_counter()
         q = learned_all()
         torch.cuda.synchronize()
         tl_ms = reduce_max(world, (time.perf_counter() - ta) * 1e3)
+        st_l = ctx.stage_times(reset=True)
+        ctx.set_timing(False)
+        split = {k: round((marks[i + 1] - marks[i]) * 1e3, 3) for i, k in
+                 enumerate(("network_forward", "proposals", "rescoring", "copy_out"))}
+        split["rescoring_stages"] = {k: round(v[0], 3) for k, v in st_l.items() if v[1]}
         bestl = ol["wR"].argmax(1).cpu().numpy()
         besttl = ol["wT"].argmax(1).cpu().numpy()
         err_l = learned.angle_deg(q[np.arange(n), bestl], ps.quat_true)
@@ -913,7 +951,8 @@ def run_learned(args, rank, world, local_rank):
         med = np.median(dv, 1)
         mad = np.median(np.abs(dv - med[:, None]), 1) + 1e-12
         peak = (dv.max(1) - med) / (1.4826 * mad)
-        return dict(n=n, tg_ms=tg_ms, tl_ms=tl_ms, err_g=err_g, err_l=err_l, peak=peak,
+        return dict(n=n, tg_ms=tg_ms, tl_ms=tl_ms, split_ms=split, err_g=err_g, err_l=err_l,
+                    peak=peak,
                     better=basel >= baseg,
                     pose_g=(quats_g[bestg], trans_g.cpu().numpy()[besttg]),
                     pose_l=(q[np.arange(n), bestl], td.cpu().numpy()[np.arange(n), besttl]))
@@ -937,7 +976,9 @@ def run_learned(args, rank, world, local_rank):
     # matching mode: a map's reference embeddings are made once per map and
     # serve all its particles; charged per particle over the 50,000 particles
     # of a held-out map
-    ref_pp_ms = float(np.mean(ref_ms)) / 50000.0 if match and ref_ms else 0.0
+    map_ms = (float(np.mean(ref_ms)) + (float(np.mean(list(bank_ms.values()))) if bank_ms else 0.0)
+              if match and ref_ms else 0.0)
+    ref_pp_ms = map_ms / 50000.0
 
     def report(r):
         fb = r["peak"] < tau
@@ -955,6 +996,7 @@ def run_learned(args, rank, world, local_rank):
                     "median_error_deg": round(float(np.median(err_c)), 3),
                     "fallback_fraction": round(float(fb.mean()), 4)},
                 "proposal_at_least_as_likely_as_global": round(float(r["better"].mean()), 4),
+                "proposal_path_ms": r["split_ms"],
                 "speedup_with_fallback": round(r["tg_ms"] / t_c, 2)}
 
     # reconstructions of the held-out maps from each method's poses (MKB
@@ -985,11 +1027,15 @@ def run_learned(args, rank, world, local_rank):
                         "images_per_s": round(args.train_particles * args.epochs / train_s, 1)},
            "fallback_threshold_peak": round(tau, 3),
            "mode": args.learned_mode,
-           "reference_embedding": ({"ms_per_map": round(float(np.mean(ref_ms)), 2),
+           "reference_embedding": ({"ms_per_map": round(map_ms, 2),
+                                    "embedding_ms_per_map": round(float(np.mean(ref_ms)), 2),
+                                    "bank_ms_per_map": round(float(np.mean(list(
+                                        bank_ms.values()))), 2) if bank_ms else None,
                                     "maps": len(ref_ms),
                                     "charged_per_particle_over": 50000,
                                     "note": "6,912 references rendered by the library's "
-                                            "projector and embedded, once per map"}
+                                            "projector and embedded, and the map's projection "
+                                            "bank at the same rotations, once per map"}
                                    if match else None),
            "fsc_0143_resolution_A": {
                k: v for k, v in fsc_res.items()},

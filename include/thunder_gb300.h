@@ -317,7 +317,9 @@ int tg3_cnn_propose(const float* out, int n, int nRot, int nTrans, unsigned long
  * tg3_cnn_embed: normalised embeddings z [n][64] of outputs [n][68].
  * tg3_cnn_match_propose: per particle, the nRot references of highest cosine
  * score (ref [nRef][64] normalised, refQuat [nRef][4]; ties to the lower
- * index) and nTrans translations drawn as tg3_cnn_propose draws them.
+ * index) as quaternions and, when idx is not NULL, as indices idx [n][nRot]
+ * (rows of a bank made at refQuat), and nTrans translations drawn as
+ * tg3_cnn_propose draws them.
  * nRot <= nRef <= 16384, nTrans <= 512; asynchronous on `stream`. */
 int tg3_cnn_backward(tg3_cnn* net, const float* img, int n, const float* dOut);
 int tg3_cnn_contrastive(tg3_cnn* net, const float* outP, const float* outR, int n,
@@ -326,7 +328,7 @@ int tg3_cnn_contrastive(tg3_cnn* net, const float* outP, const float* outR, int 
 int tg3_cnn_embed(const float* out, int n, float* z, void* stream);
 int tg3_cnn_match_propose(const float* out, int n, const float* ref, int nRef,
                           const double* refQuat, int nRot, int nTrans,
-                          unsigned long long seed, double* quat, double* trans,
+                          unsigned long long seed, double* quat, double* trans, int* idx,
                           void* stream);
 
 /* Global scan of nImg images over one shared set of nR rotations and nT
@@ -343,6 +345,23 @@ int tg3_global_scan_d(tg3_ctx* ctx, int cls, int nImg, int nR, int nT,
                       const double* pR, const double* pT, double* wC,
                       double* wR, double* wT, double* baseL, float* dvp,
                       int precision);
+
+/* Projection banks (no single counterpart in the reference: the global
+ * search's projections, ExpectProject, src/Optimiser.cpp:759-785, kept for
+ * reuse).  tg3_ctx_set_bank projects the class-`cls` volume at nB rotations
+ * quat [nB][4] (device, double) over the active pixel set, once.
+ * tg3_local_phase_bank_d is tg3_local_phase_d with every particle's nR
+ * rotations given as rows bankIdx [nP][nR] (device int) of its class's bank
+ * instead of quaternions: the same likelihoods, weights and outputs, without
+ * projecting.  A bank serves while its pixel set is the active one; an index
+ * outside its class's bank, or into a bank built on another pixel set, is
+ * reported at the next synchronising call. */
+int tg3_ctx_set_bank(tg3_ctx* ctx, int cls, const double* quat, int nB);
+int tg3_local_phase_bank_d(tg3_ctx* ctx, int nP, int nR, int nT, const float* dat,
+                           const float* ctf, const float* sigRcp, const int* bankIdx,
+                           const double* trans, const double* pwR, const double* pwT,
+                           const double* pwC, const int* cls, double* wC, double* wR,
+                           double* wT, double* baseL, float* dvp, int precision);
 
 /* Device form of tg3_resample (all pointers device memory, stream of ctx). */
 int tg3_resample_d(tg3_ctx* ctx, int nP, int n, const double* u,

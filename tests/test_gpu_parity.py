@@ -454,3 +454,66 @@ def test_fused_matches_two_kernel_form(small, ctx, shape):
     assert rel.max() < 1e-5, rel.max()
     assert np.all(np.argmax(f["dvp"].reshape(nP, -1), 1) == np.argmax(u["dvp"].reshape(nP, -1), 1))
     assert np.allclose(f["base"], u["base"], rtol=1e-6)
+
+
+@pytest.mark.parametrize("precision", [tg3.SCORE_FP32, tg3.SCORE_BF16X3])
+def test_local_phase_from_bank(small, precision):
+    """Rotations given as rows of a projection bank score as the same
+    rotations projected directly (the bank rows are the same projections; the
+    row norms are summed in another order)."""
+    nP, nR, nT, nB = 4, 48, 21, 150
+    rng = np.random.default_rng(61)
+    d = _local_inputs(small, nP, nR, nT, 5)
+    bq = synth.haar_quaternions(rng, nB)
+    bq[:nP] = small["st"].quat_true[:nP]
+    idx = rng.integers(0, nB, (nP, nR)).astype(np.int32)
+    idx[:, 0] = np.arange(nP)                  # each particle's true pose among them
+    c = tg3.Context(0)
+    try:
+        c.set_volume(0, torch.as_tensor(small["vol32"]).to(DEV), small["pf"])
+        c.set_pixels(small["iCol"], small["iRow"], small["box"])
+        c.set_bank(0, dev(bq), nB)
+        res = []
+        for use_bank in (True, False):
+            o = dict(wC=torch.empty(nP, dtype=torch.float64, device=DEV),
+                     wR=torch.empty((nP, nR), dtype=torch.float64, device=DEV),
+                     wT=torch.empty((nP, nT), dtype=torch.float64, device=DEV),
+                     base=torch.empty(nP, dtype=torch.float64, device=DEV),
+                     dvp=torch.empty((nP, nR, nT), dtype=torch.float32, device=DEV))
+            args = (dev(d["dat"]), dev(d["ctf"]), dev(d["sig"]))
+            rest = (dev(d["ts"]), dev(d["pwR"]), dev(d["pwT"]), dev(d["pwC"]), None,
+                    o["wC"], o["wR"], o["wT"], o["base"], o["dvp"], precision)
+            if use_bank:
+                c.local_phase_bank(nP, nR, nT, *args, dev(idx), *rest)
+            else:
+                c.local_phase(nP, nR, nT, *args, dev(np.ascontiguousarray(bq[idx])), *rest)
+            c.sync()
+            res.append({k: v.cpu().numpy() for k, v in o.items()})
+        a, b = res
+        np.testing.assert_allclose(a["dvp"], b["dvp"], rtol=2e-5)
+        np.testing.assert_allclose(a["base"], b["base"], rtol=1e-6)
+        for k in ("wR", "wT"):
+            np.testing.assert_allclose(a[k] / a[k].sum(1, keepdims=True),
+                                       b[k] / b[k].sum(1, keepdims=True), atol=1e-4)
+        assert np.array_equal(a["wR"].argmax(1), b["wR"].argmax(1))
+        # an index outside the bank is reported, and the context stays usable
+        bad = idx.copy()
+        bad[1, 3] = nB
+        o = res[0]
+        outs = [torch.empty(x.shape, dtype=torch.float64 if x.dtype == np.float64 else
+                            torch.float32, device=DEV) for x in (o["wC"], o["wR"], o["wT"],
+                                                                  o["base"], o["dvp"])]
+        c.local_phase_bank(nP, nR, nT, dev(d["dat"]), dev(d["ctf"]), dev(d["sig"]), dev(bad),
+                           dev(d["ts"]), dev(d["pwR"]), dev(d["pwT"]), dev(d["pwC"]), None,
+                           *outs, precision)
+        with pytest.raises(tg3.TG3Error):
+            c.sync()
+        c.sync()
+        # a bank built on another pixel set is refused
+        c.set_pixels(small["iCol"][:-5], small["iRow"][:-5], small["box"])
+        with pytest.raises(tg3.TG3Error):
+            c.local_phase_bank(nP, nR, nT, dev(d["dat"]), dev(d["ctf"]), dev(d["sig"]),
+                               dev(idx), dev(d["ts"]), dev(d["pwR"]), dev(d["pwT"]),
+                               dev(d["pwC"]), None, *outs, precision)
+    finally:
+        c.close()

@@ -176,6 +176,9 @@ static int sync_and_check(tg3_ctx* c)
         if (flag & 2) return fail(TG3_ERR_NUMERIC, "resampling weights sum to zero");
         if (flag & 4) return fail(TG3_ERR_TIMEOUT, "device wait expired");
         if (flag & 8) return fail(TG3_ERR_STATE, "a particle's class has no volume set");
+        if (flag & (1 << 16))
+            return fail(TG3_ERR_ARG, "bank index out of range (or its class has no bank on the "
+                                     "active pixel set)");
         return fail(TG3_ERR_CUDA, "device error flag " + std::to_string(flag));
     }
     return TG3_OK;
@@ -317,6 +320,12 @@ extern "C" int tg3_ctx_destroy(tg3_ctx* c)
     }
     cudaFree(c->ins.acc);
     cudaFree(c->ins.tab);
+    for (auto& b : c->bank) {
+        cudaFree(b.f32);
+        cudaFree(b.hi);
+        cudaFree(b.abs2);
+    }
+    cudaFree(c->d_bankTable);
     cudaFree(c->d_flag);
     cudaFree(c->d_volTable);
     for (auto& v : c->pending)
@@ -436,6 +445,7 @@ static int upload_pixels(tg3_ctx* c, Pixels& px, const int* iCol, const int* iRo
     px.maxRadius = mr;
     px.maxAbs = ma;
     px.unique = unique;
+    px.gen = ++c->pixGen;
     return TG3_OK;
 }
 
@@ -473,7 +483,7 @@ extern "C" int tg3_ctx_use_pixels(tg3_ctx* c, int slot)
 // Sequence per batch: project (+ per-row norm) -> shifted data bank -> cross
 // term GEMM (FP32 CUDA cores or split-bf16 tensor cores) with the norm folded
 // into its epilogue -> marginal weights.
-static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
+static int local_phase(tg3_ctx* c, const int* bankIdx, int nP, int nR, int nT, const float* dat,
                        const float* ctf, const float* sigRcp, const double* quat,
                        const double* trans, const double* pwR, const double* pwT,
                        const double* pwC, const int* cls, double* wC, double* wR,
@@ -489,7 +499,7 @@ static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
             return fail(TG3_ERR_ARG, "all class volumes must share one edge and pf");
     if ((st = check_geometry(c, v0.vdim, v0.pf))) return st;
     if ((st = check_weights_shape(nR, nT))) return st;
-    const bool fusedPath = precision == TG3_SCORE_BF16X3 && c->fused;
+    const bool fusedPath = precision == TG3_SCORE_BF16X3 && c->fused && !bankIdx;
     float* P = fusedPath ? nullptr
                          : (float*)ws_get(c, WS_P, sizeof(float) * (size_t)nP * nR * Kp, &st);
     if (!fusedPath && !P) return st;
@@ -514,7 +524,7 @@ static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
     // split-bf16: the same buffers hold a hi plane followed by a lo plane
     const long long splitP = split ? (long long)nP * nR * Kp : 0;
     const long long splitA = split ? (long long)nP * nT * Kp : 0;
-    if (split && c->fused) {
+    if (fusedPath) {
         // projection + cross term in one kernel; the slices stay on chip
         const size_t partBytes = round_up(sizeof(FusedParticle) * (size_t)nP, 256);
         const size_t offBytes = round_up(sizeof(int) * ((size_t)nP + 1), 256);
@@ -548,7 +558,11 @@ static int local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
         }
         return TG3_OK;
     }
-    {
+    if (bankIdx) {
+        StageTimer tm(c, TG3_STAGE_PROJECT);
+        TG3_CUDA(launch_bank_gather(c->d_bankTable, cls, bankIdx, nP, nR, K, Kp, sigRcp, ctf, P,
+                                    splitP, nrm, c->d_flag, s));
+    } else {
         StageTimer tm(c, TG3_STAGE_PROJECT);
         TG3_CUDA(launch_project(c->d_volTable, cls, nullptr, v0.vdim, v0.pf, quat, nullptr,
                                 nP * nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, sigRcp, ctf, nrm,
@@ -591,8 +605,90 @@ extern "C" int tg3_local_phase_d(tg3_ctx* c, int nP, int nR, int nT, const float
     if (nP <= 0 || nR <= 0 || nT <= 0 || nT > 2048) return fail(TG3_ERR_ARG, "bad batch shape (nT <= 2048)");
     if (!dat || !ctf || !sigRcp || !quat || !trans || !pwR || !pwT || !wC || !wR || !wT || !baseL)
         return fail(TG3_ERR_ARG, "null device pointer");
-    return local_phase(c, nP, nR, nT, dat, ctf, sigRcp, quat, trans, pwR, pwT, pwC, cls, wC, wR,
+    return local_phase(c, nullptr, nP, nR, nT, dat, ctf, sigRcp, quat, trans, pwR, pwT, pwC, cls, wC, wR,
                        wT, baseL, dvp, precision);
+}
+
+// ================================================================= banks
+// Upload the device views of the banks; a bank built on another pixel set
+// than the active one shows no rows, so an index into it is flagged.
+static int upload_bank_table(tg3_ctx* c, bool* anyValid)
+{
+    if (!c->d_bankTable) TG3_CUDA(cudaMalloc(&c->d_bankTable, sizeof(BankView) * kMaxClasses));
+    BankView view[kMaxClasses];
+    bool any = false;
+    for (int k = 0; k < kMaxClasses; k++) {
+        const Bank& q = c->bank[k];
+        const bool ok = q.nB > 0 && q.gen == c->px.gen && q.K == c->px.K;
+        const size_t rf = (size_t)q.nB * q.Kp;
+        view[k] = {q.f32, q.hi, q.hi ? q.hi + rf : nullptr, q.abs2, ok ? q.nB : 0};
+        any = any || ok;
+    }
+    TG3_CUDA(cudaMemcpyAsync(c->d_bankTable, view, sizeof(view), cudaMemcpyHostToDevice,
+                             c->stream));
+    if (anyValid) *anyValid = any;
+    return TG3_OK;
+}
+
+extern "C" int tg3_ctx_set_bank(tg3_ctx* c, int cls, const double* quat, int nB)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].blocks)
+        return fail(TG3_ERR_STATE, "volume of the bank's class not set");
+    if (!quat || nB <= 0) return fail(TG3_ERR_ARG, "bad bank arguments");
+    const Volume& v = c->vol[cls];
+    if ((st = check_geometry(c, v.vdim, v.pf))) return st;
+    const int K = c->px.K, Kp = c->px.Kp;
+    Bank& b = c->bank[cls];
+    const size_t rowF = (size_t)nB * Kp;
+    const size_t need = rowF * sizeof(float) + 2 * rowF * sizeof(__nv_bfloat16) +
+                        (size_t)nB * K * sizeof(float);
+    if (b.bytes < need) {
+        TG3_CUDA(cudaStreamSynchronize(c->stream));
+        cudaFree(b.f32);
+        cudaFree(b.hi);
+        cudaFree(b.abs2);
+        b = Bank();
+        TG3_CUDA(cudaMalloc(&b.f32, rowF * sizeof(float)));
+        TG3_CUDA(cudaMalloc(&b.hi, 2 * rowF * sizeof(__nv_bfloat16)));
+        TG3_CUDA(cudaMalloc(&b.abs2, (size_t)nB * K * sizeof(float)));
+        b.bytes = need;
+    }
+    float* pscr = (float*)ws_get(c, WS_PROJ, sizeof(float) * project_scratch_floats(nB, Kp), &st);
+    if (!pscr) return st;
+    TG3_CUDA(launch_project(nullptr, nullptr, v.blocks, v.vdim, v.pf, quat, nullptr, nB, nB,
+                            c->px.iCol, c->px.iRow, K, b.f32, Kp, nullptr, nullptr, nullptr, pscr,
+                            c->d_flag, 0, c->stream));
+    TG3_CUDA(launch_bank_planes(b.f32, nB, K, Kp, b.hi, b.hi + rowF, b.abs2, c->stream));
+    b.nB = nB;
+    b.K = K;
+    b.Kp = Kp;
+    b.gen = c->px.gen;
+    if ((st = upload_bank_table(c, nullptr))) return st;
+    TG3_CUDA(cudaStreamSynchronize(c->stream));
+    return TG3_OK;
+}
+
+extern "C" int tg3_local_phase_bank_d(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
+                                      const float* ctf, const float* sigRcp, const int* bankIdx,
+                                      const double* trans, const double* pwR, const double* pwT,
+                                      const double* pwC, const int* cls, double* wC, double* wR,
+                                      double* wT, double* baseL, float* dvp, int precision)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (nP <= 0 || nR <= 0 || nT <= 0 || nT > 2048) return fail(TG3_ERR_ARG, "bad batch shape (nT <= 2048)");
+    if (!dat || !ctf || !sigRcp || !bankIdx || !trans || !pwR || !pwT || !wC || !wR || !wT ||
+        !baseL)
+        return fail(TG3_ERR_ARG, "null device pointer");
+    // the classes are device data: banks built on another pixel set show no
+    // rows, and a particle that names one is flagged
+    bool any = false;
+    if ((st = upload_bank_table(c, &any))) return st;
+    if (!any) return fail(TG3_ERR_STATE, "no projection bank built on the active pixel set");
+    return local_phase(c, bankIdx, nP, nR, nT, dat, ctf, sigRcp, nullptr, trans, pwR, pwT, pwC,
+                       cls, wC, wR, wT, baseL, dvp, precision);
 }
 
 // ================================================================ resample
@@ -1135,7 +1231,7 @@ extern "C" int tg3_ExpectLocal3D(tg3_volume* h, const float* dat, const float* c
     TG3_CUDA(cudaMemcpyAsync(b + opr, oldR, 8 * (size_t)nR, cudaMemcpyHostToDevice, s));
     TG3_CUDA(cudaMemcpyAsync(b + opt, oldT, 8 * (size_t)nT, cudaMemcpyHostToDevice, s));
     TG3_CUDA(cudaMemcpyAsync(b + opc, &oldC, 8, cudaMemcpyHostToDevice, s));
-    st = local_phase(c, 1, nR, nT, (float*)(b + od), (float*)(b + oc), (float*)(b + os),
+    st = local_phase(c, nullptr, 1, nR, nT, (float*)(b + od), (float*)(b + oc), (float*)(b + os),
                      (double*)(b + oq), (double*)(b + ot), (double*)(b + opr), (double*)(b + opt),
                      (double*)(b + opc), nullptr, (double*)(b + owc), (double*)(b + owr),
                      (double*)(b + owt), (double*)(b + obl), dvp ? (float*)(b + odv) : nullptr,
@@ -1189,7 +1285,7 @@ extern "C" int tg3_local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* 
     TG3_CUDA(cudaMemcpyAsync(b + opt, pwT, 8 * P_ * T_, cudaMemcpyHostToDevice, s));
     if (pwC) TG3_CUDA(cudaMemcpyAsync(b + opc, pwC, 8 * P_, cudaMemcpyHostToDevice, s));
     if (cls) TG3_CUDA(cudaMemcpyAsync(b + ocl, cls, 4 * P_, cudaMemcpyHostToDevice, s));
-    st = local_phase(c, nP, nR, nT, (float*)(b + od), (float*)(b + oc), (float*)(b + os),
+    st = local_phase(c, nullptr, nP, nR, nT, (float*)(b + od), (float*)(b + oc), (float*)(b + os),
                      (double*)(b + oq), (double*)(b + ot), (double*)(b + opr), (double*)(b + opt),
                      pwC ? (double*)(b + opc) : nullptr, cls ? (int*)(b + ocl) : nullptr,
                      (double*)(b + owc), (double*)(b + owr), (double*)(b + owt),

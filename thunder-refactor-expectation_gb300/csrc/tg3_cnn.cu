@@ -636,7 +636,8 @@ __global__ void k_emb_grad(const float* __restrict__ G, const float* __restrict_
 __global__ void __launch_bounds__(256)
 k_match_propose(const float* __restrict__ out, const float* __restrict__ ref, int nRef,
                 int nPow2, const double* __restrict__ refQuat, int nRot, int nTrans,
-                uint64_t seed, double* __restrict__ quat, double* __restrict__ trans)
+                uint64_t seed, double* __restrict__ quat, double* __restrict__ trans,
+                int* __restrict__ idxOut)
 {
     extern __shared__ unsigned long long key[];          // [nPow2]
     __shared__ float zp[kEmb];
@@ -690,6 +691,7 @@ k_match_propose(const float* __restrict__ out, const float* __restrict__ ref, in
         }
     for (int j = threadIdx.x; j < nRot; j += blockDim.x) {
         const int idx = (int)(0xFFFFFFFFu - (unsigned int)(key[j] & 0xFFFFFFFFu));
+        if (idxOut) idxOut[(size_t)l * nRot + j] = idx;
         const double* src = refQuat + 4 * (size_t)idx;
         double* qo = quat + ((size_t)l * nRot + j) * 4;
         for (int c = 0; c < 4; c++) qo[c] = src[c];
@@ -1099,11 +1101,12 @@ extern "C" int tg3_cnn_embed(const float* out, int n, float* z, void* stream)
 
 // Rotation proposals by matching: for every particle (outputs out [n][68]),
 // the nRot references of highest cosine score (ref [nRef][64] normalised,
-// refQuat [nRef][4]), and nTrans translations from the shift outputs.
+// refQuat [nRef][4]) with their indices (idx [n][nRot], may be NULL), and
+// nTrans translations from the shift outputs.
 extern "C" int tg3_cnn_match_propose(const float* out, int n, const float* ref, int nRef,
                                      const double* refQuat, int nRot, int nTrans,
                                      unsigned long long seed, double* quat, double* trans,
-                                     void* stream)
+                                     int* idx, void* stream)
 {
     if (!out || !ref || !refQuat || !quat || !trans || n <= 0 || nRef <= 0 || nRef > 16384 ||
         nRot <= 0 || nRot > nRef || nTrans <= 0 || nTrans > 512)
@@ -1114,7 +1117,7 @@ extern "C" int tg3_cnn_match_propose(const float* out, int n, const float* ref, 
     TG3_CUDA(cudaFuncSetAttribute(k_match_propose, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
     k_match_propose<<<n, 256, smem, static_cast<cudaStream_t>(stream)>>>(
-        out, ref, nRef, p2, refQuat, nRot, nTrans, seed, quat, trans);
+        out, ref, nRef, p2, refQuat, nRot, nTrans, seed, quat, trans, idx);
     TG3_LAUNCH_CHECK("match proposals");
     return TG3_OK;
 }

@@ -1,6 +1,7 @@
 // tg3_internal.cuh -- shared declarations of the GB300 E-step library.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
@@ -110,6 +111,27 @@ struct Pixels {
     // (row iRow + maxAbs, column iCol), -1 where none; set when unique
     int* cellPix = nullptr;
     size_t cells = 0;
+    unsigned gen = 0;  // upload generation (a bank records the set it was built on)
+};
+
+// Projections of one class at a fixed rotation set, made once and gathered
+// by index (tg3_ctx_set_bank): FP32 rows [nB][Kp] (complex interleaved,
+// zero padded), split-bf16 planes hi, lo [nB][Kp], |P|^2 rows [nB][K].
+struct Bank {
+    float* f32 = nullptr;
+    __nv_bfloat16* hi = nullptr;
+    float* abs2 = nullptr;
+    int nB = 0, K = 0, Kp = 0;
+    unsigned gen = 0;
+    size_t bytes = 0;
+};
+// The device view the gather reads, one per class.
+struct BankView {
+    const float* f32;
+    const __nv_bfloat16* hi;
+    const __nv_bfloat16* lo;
+    const float* abs2;
+    int nB;
 };
 
 struct InsertAcc {
@@ -133,6 +155,9 @@ struct tg3_ctx {
     tg3::Pixels pxMain;                      // owned: tg3_ctx_set_pixels
     tg3::Pixels pxSlot[tg3::kMaxClasses];    // owned: tg3_ctx_set_pixels_slot
     tg3::InsertAcc ins;
+    tg3::Bank bank[tg3::kMaxClasses];        // tg3_ctx_set_bank
+    tg3::BankView* d_bankTable = nullptr;    // device copy of the views
+    unsigned pixGen = 0;                     // pixel uploads so far
     tg3::Buffer ws[tg3::WS_COUNT];
     int* d_flag = nullptr;           // device error word
     // tg3_ctx_set_option
@@ -248,6 +273,17 @@ cudaError_t launch_insert_gather(float4* acc, int vdim, const float* tab, int ta
                                  const int* cellPix, const int* iCol, const int* iRow, int K,
                                  int pf, int idim, int Rg, float Rp, double* O3D, int* counter,
                                  void* scratch, size_t scratchBytes, cudaStream_t st);
+// Bank of projections: split planes and |P|^2 rows from the FP32 rows.
+cudaError_t launch_bank_planes(const float* f32, int nB, int K, int Kp, __nv_bfloat16* hi,
+                               __nv_bfloat16* lo, float* abs2, cudaStream_t st);
+// P rows [nP * nR][Kp] (FP32, or hi / lo planes when splitLo != 0) gathered
+// from the banks of the particles' classes at idx [nP][nR], and the rows'
+// norms sum sigRcp ctf^2 |P|^2.  An index outside the bank sets flag bit 16
+// and yields a zero row.
+cudaError_t launch_bank_gather(const BankView* table, const int* cls, const int* idx, int nP,
+                               int nR, int K, int Kp, const float* sigRcp, const float* ctf,
+                               float* P, long long splitLo, float* nrm, int* flag,
+                               cudaStream_t st);
 // Shell correlation of two half volumes; sums holds 3 nShell doubles.
 cudaError_t launch_fsc(const float2* A, const float2* B, int vdim, int nShell,
                        double* sums, double* fsc, cudaStream_t st);

@@ -1223,6 +1223,92 @@ k_insert_gather(float4* __restrict__ acc, int vdim, const float4* __restrict__ g
     }
 }
 
+// ------------------------------------------------------------------------
+// Projection banks: one class's projections at a fixed rotation set, made
+// once (k_project) and gathered by index for every particle that uses them.
+// Planes: hi = bf16(x), lo = bf16(x - hi), the rounding of the split store.
+__global__ void k_bank_planes(const float* __restrict__ f32, int nB, int K, int Kp,
+                              __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                              float* __restrict__ abs2)
+{
+    const size_t pairs = (size_t)nB * (Kp / 2);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < pairs;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = i / (Kp / 2);
+        const int p = (int)(i % (Kp / 2));
+        const float2 v = reinterpret_cast<const float2*>(f32 + row * Kp)[p];
+        __nv_bfloat162 h = __floats2bfloat162_rn(v.x, v.y);
+        const float2 hf = __bfloat1622float2(h);
+        reinterpret_cast<__nv_bfloat162*>(hi + row * Kp)[p] = h;
+        reinterpret_cast<__nv_bfloat162*>(lo + row * Kp)[p] =
+            __floats2bfloat162_rn(v.x - hf.x, v.y - hf.y);
+        if (p < K) abs2[row * K + p] = v.x * v.x + v.y * v.y;
+    }
+}
+
+// CTA (particle, group of 16 rows): w = sigRcp ctf^2 of the particle in
+// shared memory, then per row a 16-byte copy of the bank row and the norm
+// as a block reduction.
+constexpr int kBankRows = 16;
+
+__global__ void __launch_bounds__(256)
+k_bank_gather(const BankView* __restrict__ table, const int* __restrict__ cls,
+              const int* __restrict__ idx, int nR, int K, int Kp,
+              const float* __restrict__ sigRcp, const float* __restrict__ ctf,
+              float* __restrict__ P, long long splitLo, float* __restrict__ nrm,
+              int* __restrict__ flag)
+{
+    extern __shared__ float w[];                 // [K]
+    __shared__ float red[8];
+    const int l = blockIdx.x;
+    const BankView b = table[cls ? cls[l] : 0];
+    for (int p = threadIdx.x; p < K; p += blockDim.x) {
+        const float c = ctf[(size_t)l * K + p];
+        w[p] = sigRcp[(size_t)l * K + p] * c * c;
+    }
+    __syncthreads();
+    const int j0 = blockIdx.y * kBankRows;
+    const int j1 = min(nR, j0 + kBankRows);
+    const int n16 = Kp / 4;                      // 16-byte units of a row (4 floats / 8 bf16)
+    for (int j = j0; j < j1; j++) {
+        const size_t row = (size_t)l * nR + j;
+        int r = idx[row];
+        const bool ok = r >= 0 && r < b.nB;
+        if (!ok && threadIdx.x == 0) atomicOr(flag, 1 << 16);
+        if (splitLo == 0) {
+            const float4* src = reinterpret_cast<const float4*>(b.f32 + (size_t)(ok ? r : 0) * Kp);
+            float4* dst = reinterpret_cast<float4*>(P + row * Kp);
+            for (int u = threadIdx.x; u < n16; u += blockDim.x)
+                dst[u] = ok ? __ldg(src + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            __nv_bfloat16* hp = reinterpret_cast<__nv_bfloat16*>(P);
+            const uint4* sh = reinterpret_cast<const uint4*>(b.hi + (size_t)(ok ? r : 0) * Kp);
+            const uint4* sl = reinterpret_cast<const uint4*>(b.lo + (size_t)(ok ? r : 0) * Kp);
+            uint4* dh = reinterpret_cast<uint4*>(hp + row * Kp);
+            uint4* dl = reinterpret_cast<uint4*>(hp + splitLo + row * Kp);
+            const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+            for (int u = threadIdx.x; u < n16 / 2; u += blockDim.x) {
+                dh[u] = ok ? __ldg(sh + u) : z;
+                dl[u] = ok ? __ldg(sl + u) : z;
+            }
+        }
+        float acc = 0.f;
+        if (ok) {
+            const float* a2 = b.abs2 + (size_t)r * K;
+            for (int p = threadIdx.x; p < K; p += blockDim.x) acc = fmaf(w[p], __ldg(a2 + p), acc);
+        }
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float s = 0.f;
+            for (int k = 0; k < 8; k++) s += red[k];
+            nrm[row] = s;
+        }
+        __syncthreads();
+    }
+}
+
 // Fourier shell correlation of two half volumes [vdim][vdim][vdim/2+1] of
 // complex values (FSC(vec&, const Volume&, const Volume&),
 // src/Functions/Spectrum.cpp:302-329): shell u = rint(|k|) in voxel units,
@@ -1517,6 +1603,33 @@ cudaError_t launch_insert_gather(float4* acc, int vdim, const float* tab, int ta
         k_insert_gather<<<dim3(tiles, n), 256, 0, st>>>(acc, vdim, grid, gw, Rg, rot, tab, tabNz,
                                                         tabInvStep, pf, Rp, hs);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bank_planes(const float* f32, int nB, int K, int Kp, __nv_bfloat16* hi,
+                               __nv_bfloat16* lo, float* abs2, cudaStream_t st)
+{
+    k_bank_planes<<<grid_for((size_t)nB * (Kp / 2), 256), 256, 0, st>>>(f32, nB, K, Kp, hi, lo,
+                                                                       abs2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bank_gather(const BankView* table, const int* cls, const int* idx, int nP,
+                               int nR, int K, int Kp, const float* sigRcp, const float* ctf,
+                               float* P, long long splitLo, float* nrm, int* flag,
+                               cudaStream_t st)
+{
+    if (Kp % 8) return cudaErrorInvalidValue;
+    const size_t smem = sizeof(float) * (size_t)K;
+    if (smem > 48 * 1024) {
+        if (smem > 200 * 1024) return cudaErrorInvalidValue;
+        cudaError_t e = cudaFuncSetAttribute(k_bank_gather,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    dim3 grid(nP, (nR + kBankRows - 1) / kBankRows);
+    k_bank_gather<<<grid, 256, smem, st>>>(table, cls, idx, nR, K, Kp, sigRcp, ctf, P, splitLo,
+                                           nrm, flag);
     return cudaGetLastError();
 }
 

@@ -34,7 +34,8 @@ EXPORTS = [
     "tg3_ragged_plan_destroy", "tg3_cnn_create", "tg3_cnn_destroy", "tg3_cnn_param_count",
     "tg3_cnn_params", "tg3_cnn_grads", "tg3_cnn_set_bf16", "tg3_cnn_forward", "tg3_cnn_loss",
     "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose", "tg3_cnn_backward",
-    "tg3_cnn_contrastive", "tg3_cnn_embed", "tg3_cnn_match_propose",
+    "tg3_cnn_contrastive", "tg3_cnn_embed", "tg3_cnn_match_propose", "tg3_ctx_set_bank",
+    "tg3_local_phase_bank_d",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
@@ -119,7 +120,9 @@ def lib():
             "tg3_cnn_contrastive": ([_P, _P, _P, _I, _P, _F, _P, _P, _P], _I),
             "tg3_cnn_embed": ([_P, _I, _P, _P], _I),
             "tg3_cnn_match_propose": ([_P, _I, _P, _I, _P, _I, _I, ctypes.c_ulonglong, _P, _P,
-                                       _P], _I),
+                                       _P, _P], _I),
+            "tg3_ctx_set_bank": ([_P, _I, _P, _I], _I),
+            "tg3_local_phase_bank_d": ([_P, _I, _I, _I] + [_P] * 14 + [_I], _I),
             "tg3_ctx_stage_times": ([_P, _P, _P, _I], _I),
             "tg3_noalloc_scratch_bytes": ([], ctypes.c_size_t),
             "tg3_global_scan_d": ([_P, _I, _I, _I, _I] + [_P] * 12 + [_I], _I),
@@ -225,6 +228,22 @@ class Context:
                                       ptr(quat), ptr(trans), ptr(pwR), ptr(pwT), ptr(pwC),
                                       ptr(cls), ptr(wC), ptr(wR), ptr(wT), ptr(base), ptr(dvp),
                                       precision))
+
+    def set_bank(self, cls: int, quat, nB: int):
+        """Project class `cls` at nB rotations (quat [nB][4] float64, device)
+        once, over the active pixel set."""
+        self._hold(quat)
+        check(lib().tg3_ctx_set_bank(self.h, cls, ptr(quat), nB))
+
+    def local_phase_bank(self, nP, nR, nT, dat, ctf, sig, bank_idx, trans, pwR, pwT, pwC, cls,
+                         wC, wR, wT, base, dvp=None, precision=SCORE_FP32):
+        """local_phase with the rotations given as rows bank_idx [nP][nR] (int32)
+        of the classes' banks."""
+        self._hold(dat, ctf, sig, bank_idx, trans, pwR, pwT, pwC, cls, wC, wR, wT, base, dvp)
+        check(lib().tg3_local_phase_bank_d(self.h, nP, nR, nT, ptr(dat), ptr(ctf), ptr(sig),
+                                           ptr(bank_idx), ptr(trans), ptr(pwR), ptr(pwT),
+                                           ptr(pwC), ptr(cls), ptr(wC), ptr(wR), ptr(wT),
+                                           ptr(base), ptr(dvp), precision))
 
     def local_phase_host(self, nP, nR, nT, dat, ctf, sig, quat, trans, pwR, pwT, pwC, cls,
                          wC, wR, wT, base, dvp=None, precision=SCORE_FP32):
@@ -412,12 +431,14 @@ class Cnn:
         check(lib().tg3_cnn_embed(ptr(out), out.shape[0], ptr(z), stream))
 
     @staticmethod
-    def match_propose(out, ref, ref_quat, n_rot, n_trans, seed, quat, trans, stream=None):
-        """Rotations: the n_rot references of highest score; translations as
-        propose (device tensors; ref [nRef][64] normalised, ref_quat [nRef][4])."""
+    def match_propose(out, ref, ref_quat, n_rot, n_trans, seed, quat, trans, idx=None,
+                      stream=None):
+        """Rotations: the n_rot references of highest score (and their indices
+        into idx [n][n_rot] int32 when given); translations as propose
+        (device tensors; ref [nRef][64] normalised, ref_quat [nRef][4])."""
         check(lib().tg3_cnn_match_propose(ptr(out), out.shape[0], ptr(ref), ref.shape[0],
                                           ptr(ref_quat), n_rot, n_trans, seed, ptr(quat),
-                                          ptr(trans), stream))
+                                          ptr(trans), ptr(idx), stream))
 
     def close(self):
         if self.h:
