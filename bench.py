@@ -898,7 +898,7 @@ def run_learned(args, rank, world, local_rank):
             # network, proposals and exact rescoring, all on the device
             marks.clear()
             marks.append(time.perf_counter())
-            net.forward(ps.images, out)
+            net.infer(ps.images, out)
             marks.append(time.perf_counter())
             if match:
                 # per map: the best-matching references of that map's embeddings

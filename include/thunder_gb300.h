@@ -322,6 +322,10 @@ int tg3_cnn_propose(const float* out, int n, int nRot, int nTrans, unsigned long
  * tg3_cnn_propose draws them.
  * nRot <= nRef <= 16384, nTrans <= 512; asynchronous on `stream`. */
 int tg3_cnn_backward(tg3_cnn* net, const float* img, int n, const float* dOut);
+/* Inference forward for proposals: the same network with bf16 activations
+ * (bf16 weights, FP32 accumulation), the wide layers as implicit GEMMs on
+ * the tensor cores; outputs [n][68] (device) for images [n][64][64]. */
+int tg3_cnn_infer(tg3_cnn* net, const float* img, int n, float* out);
 int tg3_cnn_contrastive(tg3_cnn* net, const float* outP, const float* outR, int n,
                         const double* tstar, float tau, float* dOutP, float* dOutR,
                         double* loss);

@@ -118,10 +118,14 @@ def head_loss(out, Rstar, tstar):
     return loss, g
 
 
-def forward(params, img, shapes=SHAPES, round_bf16=True):
-    """Activations of every layer (post-ReLU, the last without)."""
+def forward(params, img, shapes=SHAPES, round_bf16=True, round_act=False):
+    """Activations of every layer (post-ReLU, the last without).  round_act:
+    the image and every hidden layer's output rounded to bf16, as the
+    inference forward stores them (tg3_cnn_infer)."""
     lay, _ = layout(shapes)
     x = np.asarray(img, dtype=np.float64).reshape(len(img), 1, shapes[0][2], shapes[0][2])
+    if round_act:
+        x = bf16(x).astype(np.float64)
     acts = [x]
     for li, ((wo, ws, bo, co), (cin, cout, hin, hout, s)) in enumerate(zip(lay, shapes)):
         W = np.asarray(params[wo:wo + int(np.prod(ws))], dtype=np.float32)
@@ -133,6 +137,8 @@ def forward(params, img, shapes=SHAPES, round_bf16=True):
             y = acts[-1].reshape(len(img), -1) @ W.T + b
         if li < len(shapes) - 1:
             y = np.maximum(y, 0.0)
+            if round_act:
+                y = bf16(y).astype(np.float64)
         acts.append(y)
     return acts
 

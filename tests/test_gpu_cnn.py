@@ -174,3 +174,26 @@ def test_match_proposals_are_the_best_references():
         if 3 in sel and 7 in sel:
             assert list(sel).index(3) < list(sel).index(7)
     np.testing.assert_array_equal(t.cpu().numpy(), t2.cpu().numpy())
+
+
+def test_tensor_core_inference_matches_oracle(net):
+    """tg3_cnn_infer (bf16 activations, implicit-GEMM convolutions on the
+    tensor cores) against the float64 network with the same bf16 roundings;
+    the accumulation order differs, so a hidden value near a bf16 rounding
+    boundary may round the other way."""
+    img, _, _ = _batch(37, 47)                  # not a multiple of the 128-pixel tile
+    net.set_bf16(True)
+    out = torch.empty((37, tg3.Cnn.N_OUT), dtype=torch.float32, device=DEV)
+    net.infer(torch.as_tensor(img).to(DEV), out)
+    got = out.cpu().numpy().astype(np.float64)
+    ref = C.forward(net.params(), img, round_bf16=True, round_act=True)[-1]
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    assert err < 2e-2, err
+    cos = (got[:, :64] * ref[:, :64]).sum(1) / (np.linalg.norm(got[:, :64], axis=1) *
+                                                np.linalg.norm(ref[:, :64], axis=1))
+    assert cos.min() > 0.999, cos.min()
+    # and close to the FP32-activation forward
+    f32 = torch.empty_like(out)
+    net.forward(torch.as_tensor(img).to(DEV), f32)
+    ref32 = f32.cpu().numpy()
+    assert np.abs(got - ref32).max() < 5e-2 * np.abs(ref32).max()

@@ -26,6 +26,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -735,6 +736,12 @@ struct tg3_cnn {
     float* gact[kLayers + 1] = {};
     double* Rstar = nullptr;
     double* loss = nullptr;
+    // tensor-core inference: repacked bf16 weights, bf16 NHWC activations
+    __nv_bfloat16* tcW = nullptr;
+    size_t tcOff[kLayers] = {};
+    int tcCap = 0;
+    __nv_bfloat16* tcAct[kLayers] = {};     // outputs of layers 0 .. 6
+    int* tcFlag = nullptr;
     // contrastive scratch (matching mode), grown as needed
     int embCap = 0;
     float* emb = nullptr;       // zp, zr [n][64]; invP, invR [n]; rowL, colL [n]; S, G [n][n]
@@ -904,6 +911,9 @@ extern "C" int tg3_cnn_destroy(tg3_cnn* net)
     cudaFree(net->loss);
     cudaFree(net->emb);
     cudaFree(net->embLoss);
+    cudaFree(net->tcW);
+    cudaFree(net->tcFlag);
+    for (int l = 0; l < kLayers; l++) cudaFree(net->tcAct[l]);
     cudaFree(net->params);
     cudaFree(net->grads);
     cudaFree(net->m);
@@ -1119,5 +1129,154 @@ extern "C" int tg3_cnn_match_propose(const float* out, int n, const float* ref, 
     k_match_propose<<<n, 256, smem, static_cast<cudaStream_t>(stream)>>>(
         out, ref, nRef, p2, refQuat, nRot, nTrans, seed, quat, trans, idx);
     TG3_LAUNCH_CHECK("match proposals");
+    return TG3_OK;
+}
+
+namespace tg3 {
+namespace {
+
+// Rows and K (padded) of every layer's repacked weights for the inference
+// path: conv 0 [32][9]; convs 1..5 [cout][9 cin] (tap-major K); dense 6
+// [256][8192] with K in NHWC order (y, x, c); dense 7 [68][256].
+void tc_dims(int l, int* rows, int* kpad)
+{
+    const LayerShape& s = kShape[l];
+    if (l == 0) {
+        *rows = s.cout;
+        *kpad = 9;
+    } else if (s.stride) {
+        *rows = s.cout;
+        *kpad = 9 * s.cin;
+    } else {
+        *rows = s.cout;
+        *kpad = s.cin;
+    }
+}
+
+__global__ void k_tc_repack(const float* __restrict__ W, int l, int rows, int kpad, int cin,
+                            int hin, __nv_bfloat16* __restrict__ out)
+{
+    const size_t total = (size_t)rows * kpad;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int o = (int)(i / kpad), k = (int)(i % kpad);
+        size_t src;
+        if (l == 0) {
+            src = (size_t)o * 9 + k;                                  // [o][0][ky][kx]
+        } else if (l <= 5) {
+            const int tap = k / cin, ci = k % cin;                    // k = tap cin + ci
+            src = ((size_t)o * cin + ci) * 9 + tap;
+        } else if (l == 6) {
+            const int c = k % 128, yx = k / 128;                      // k = (y 8 + x) 128 + c
+            src = (size_t)o * kpad + (size_t)c * 64 + yx;
+        } else {
+            src = (size_t)o * kpad + k;
+        }
+        out[i] = __float2bfloat16_rn(W[src]);
+    }
+    (void)hin;
+}
+
+constexpr int kInferChunk = 2048;
+
+int tc_prepare(tg3_cnn* net, int n)
+{
+    cudaStream_t s = net->stream;
+    if (!net->tcW) {
+        size_t o = 0;
+        for (int l = 0; l < kLayers; l++) {
+            int rows, kpad;
+            tc_dims(l, &rows, &kpad);
+            net->tcOff[l] = o;
+            o += (size_t)rows * kpad;
+            o = (o + 63) & ~(size_t)63;
+        }
+        TG3_CUDA(cudaMalloc(&net->tcW, sizeof(__nv_bfloat16) * o));
+        TG3_CUDA(cudaMalloc(&net->tcFlag, sizeof(int)));
+        TG3_CUDA(cudaMemset(net->tcFlag, 0, sizeof(int)));
+    }
+    for (int l = 0; l < kLayers; l++) {
+        int rows, kpad;
+        tc_dims(l, &rows, &kpad);
+        k_tc_repack<<<cnn_grid((size_t)rows * kpad, 256), 256, 0, s>>>(
+            net->params + net->off[l][0], l, rows, kpad, kShape[l].cin, kShape[l].hin,
+            net->tcW + net->tcOff[l]);
+    }
+    TG3_LAUNCH_CHECK("weights repack");
+    const int cap = std::min(n, kInferChunk);
+    if (cap > net->tcCap) {
+        TG3_CUDA(cudaStreamSynchronize(s));
+        for (int l = 0; l < kLayers; l++) {
+            cudaFree(net->tcAct[l]);
+            net->tcAct[l] = nullptr;
+        }
+        net->tcCap = 0;
+        for (int l = 0; l < kLayers - 1; l++)
+            TG3_CUDA(cudaMalloc(&net->tcAct[l], sizeof(__nv_bfloat16) * act_size(l + 1) * cap));
+        net->tcCap = cap;
+    }
+    return TG3_OK;
+}
+
+}  // namespace
+}  // namespace tg3
+
+// Inference forward with bf16 activations (tensor cores for the wide
+// layers): outputs [n][68] (device) for images [n][64][64] (device).
+extern "C" int tg3_cnn_infer(tg3_cnn* net, const float* img, int n, float* out)
+{
+    if (!net || !img || !out || n <= 0) return fail(TG3_ERR_ARG, "bad inference arguments");
+    TG3_CUDA(cudaSetDevice(net->device));
+    int st = tc_prepare(net, n);
+    if (st) return st;
+    cudaStream_t s = net->stream;
+    for (int i0 = 0; i0 < n; i0 += kInferChunk) {
+        const int m = std::min(kInferChunk, n - i0);
+        const float* b0 = net->params + net->off[0][1];
+        TG3_CUDA(launch_conv1_nhwc(img + (size_t)i0 * 64 * 64, net->tcW + net->tcOff[0], b0, m,
+                                   64, net->tcAct[0], s));
+        for (int l = 1; l <= 6; l++) {
+            const LayerShape& sh = kShape[l];
+            int rows, kpad;
+            tc_dims(l, &rows, &kpad);
+            ConvTcArgs a;
+            a.in = net->tcAct[l - 1];
+            a.w = net->tcW + net->tcOff[l];
+            a.bias = net->params + net->off[l][1];
+            a.out = net->tcAct[l];
+            a.n = m;
+            if (sh.stride) {
+                a.H = a.W = sh.hin;
+                a.Ho = a.Wo = sh.hout;
+                a.Cin = sh.cin;
+                a.ks = 3;
+                a.stride = sh.stride;
+                a.pad = 1;
+            } else {
+                a.H = a.W = a.Ho = a.Wo = 1;
+                a.Cin = sh.cin;
+                a.ks = 1;
+                a.stride = 1;
+                a.pad = 0;
+            }
+            a.Cout = sh.cout;
+            a.coutPad = sh.cout;
+            a.Kpad = kpad;
+            a.tmemCols = sh.cout < 32 ? 32 : sh.cout;
+            a.relu = 1;
+            a.flag = net->tcFlag;
+            TG3_CUDA(launch_conv_tc(a, s));
+        }
+        TG3_CUDA(launch_fc_out(net->tcAct[6], net->tcW + net->tcOff[7],
+                               net->params + net->off[7][1], m, kShape[7].cin, kOut,
+                               out + (size_t)i0 * kOut, s));
+    }
+    TG3_CUDA(cudaStreamSynchronize(s));
+    int flag = 0;
+    TG3_CUDA(cudaMemcpy(&flag, net->tcFlag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+        cudaMemset(net->tcFlag, 0, sizeof(int));
+        return fail(TG3_ERR_TIMEOUT, "tensor-core wait expired in the network");
+    }
     return TG3_OK;
 }

@@ -284,6 +284,26 @@ cudaError_t launch_bank_gather(const BankView* table, const int* cls, const int*
                                int nR, int K, int Kp, const float* sigRcp, const float* ctf,
                                float* P, long long splitLo, float* nrm, int* flag,
                                cudaStream_t st);
+// Pose network inference on the tensor cores (tg3_conv_tc.cu).  One layer
+// as an implicit GEMM: in NHWC bf16 [n][H][W][Cin] (Cin a multiple of 32),
+// w [coutPad][Kpad] bf16 with K = tap * Cin + ci (tap = ky * ks + kx),
+// out NHWC bf16 [n][Ho][Wo][Cout] after bias (FP32) and optional ReLU.
+struct ConvTcArgs {
+    const __nv_bfloat16* in;
+    const __nv_bfloat16* w;
+    const float* bias;
+    __nv_bfloat16* out;
+    int n, H, W, Cin, Ho, Wo, Cout, coutPad, ks, stride, pad, Kpad, tmemCols, relu;
+    int* flag;
+};
+size_t conv_tc_smem(int coutPad);
+cudaError_t launch_conv_tc(const ConvTcArgs& a, cudaStream_t st);
+// first layer: FP32 images [n][H][H], w [32][9] bf16, out NHWC bf16 [n][H][H][32]
+cudaError_t launch_conv1_nhwc(const float* img, const __nv_bfloat16* w, const float* bias, int n,
+                              int H, __nv_bfloat16* out, cudaStream_t st);
+// output layer: out [n][N] = act [n][K] (bf16) W^T (bf16 [N][K]) + bias
+cudaError_t launch_fc_out(const __nv_bfloat16* act, const __nv_bfloat16* w, const float* bias,
+                          int n, int K, int N, float* out, cudaStream_t st);
 // Shell correlation of two half volumes; sums holds 3 nShell doubles.
 cudaError_t launch_fsc(const float2* A, const float2* B, int vdim, int nShell,
                        double* sums, double* fsc, cudaStream_t st);

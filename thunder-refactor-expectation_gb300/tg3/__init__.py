@@ -33,7 +33,7 @@ EXPORTS = [
     "tg3_ragged_plan_create", "tg3_ragged_plan_run", "tg3_ragged_plan_info",
     "tg3_ragged_plan_destroy", "tg3_cnn_create", "tg3_cnn_destroy", "tg3_cnn_param_count",
     "tg3_cnn_params", "tg3_cnn_grads", "tg3_cnn_set_bf16", "tg3_cnn_forward", "tg3_cnn_loss",
-    "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose", "tg3_cnn_backward",
+    "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose", "tg3_cnn_backward", "tg3_cnn_infer",
     "tg3_cnn_contrastive", "tg3_cnn_embed", "tg3_cnn_match_propose", "tg3_ctx_set_bank",
     "tg3_local_phase_bank_d",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
@@ -117,6 +117,7 @@ def lib():
             "tg3_cnn_adam": ([_P, ctypes.c_float], _I),
             "tg3_cnn_propose": ([_P, _I, _I, _I, ctypes.c_ulonglong, _P, _P, _P], _I),
             "tg3_cnn_backward": ([_P, _P, _I, _P], _I),
+            "tg3_cnn_infer": ([_P, _P, _I, _P], _I),
             "tg3_cnn_contrastive": ([_P, _P, _P, _I, _P, _F, _P, _P, _P], _I),
             "tg3_cnn_embed": ([_P, _I, _P, _P], _I),
             "tg3_cnn_match_propose": ([_P, _I, _P, _I, _P, _I, _I, ctypes.c_ulonglong, _P, _P,
@@ -393,6 +394,10 @@ class Cnn:
     def forward(self, img, out):
         """img: device float32 [n][64][64]; out: device float32 [n][68]."""
         check(lib().tg3_cnn_forward(self.h, ptr(img), img.shape[0], ptr(out)))
+
+    def infer(self, img, out):
+        """Inference forward (bf16 activations, tensor cores): as forward."""
+        check(lib().tg3_cnn_infer(self.h, ptr(img), img.shape[0], ptr(out)))
 
     def loss(self, img, Rstar, tstar, grads: bool = True) -> float:
         v = ctypes.c_double()

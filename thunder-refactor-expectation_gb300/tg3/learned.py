@@ -170,14 +170,15 @@ def render_references(ctx, cls: int, quats: np.ndarray, box: int, img: int = 64,
 
 
 def reference_embeddings(net, refs, chunk: int = 4096):
-    """Normalised embeddings [n][64] of reference images [n][64][64]."""
+    """Normalised embeddings [n][64] of reference images [n][64][64] (the
+    inference forward: bf16 activations on the tensor cores)."""
     import torch
     n = refs.shape[0]
     z = torch.empty((n, 64), dtype=torch.float32, device=refs.device)
     out = torch.empty((min(chunk, n), net.N_OUT), dtype=torch.float32, device=refs.device)
     for s in range(0, n, chunk):
         m = min(chunk, n - s)
-        net.forward(refs[s:s + m].contiguous(), out[:m])
+        net.infer(refs[s:s + m].contiguous(), out[:m])
         net.embed(out[:m], z[s:s + m])
     torch.cuda.synchronize()
     return z
