@@ -630,68 +630,142 @@ __global__ void k_emb_grad(const float* __restrict__ G, const float* __restrict_
     }
 }
 
-// One CTA per particle: cosine scores of its embedding against nRef
-// normalised reference embeddings, the nRot best references (descending
-// score, ties to the lower index: a bitonic sort of 64-bit keys in shared
-// memory) as the rotation proposals, and nTrans translations as k_propose.
+// Inclusive scan of v over the CTA's 256 threads (eight warps); ws: 8 words.
+__device__ __forceinline__ unsigned block_scan256(unsigned v, unsigned* ws, unsigned* total)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) ws[w] = v;
+    __syncthreads();
+    unsigned before = 0, all = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        before += k < w ? ws[k] : 0u;
+        all += ws[k];
+    }
+    __syncthreads();
+    *total = all;
+    return before + v;
+}
+
+// One CTA (256 threads) per particle: cosine scores of its embedding
+// against nRef normalised reference embeddings, and the nRot best
+// references (descending score, ties to the lower index) as the rotation
+// proposals.  The nRot-th largest score key is found by four 8-bit radix
+// passes over order-preserving keys in shared memory; the keys above it and
+// the lowest-index keys equal to it are compacted in index order, then
+// sorted (bitonic, nSort = nRot rounded up to a power of two).
 __global__ void __launch_bounds__(256)
 k_match_propose(const float* __restrict__ out, const float* __restrict__ ref, int nRef,
-                int nPow2, const double* __restrict__ refQuat, int nRot, int nTrans,
+                int nSort, const double* __restrict__ refQuat, int nRot, int nTrans,
                 uint64_t seed, double* __restrict__ quat, double* __restrict__ trans,
                 int* __restrict__ idxOut)
 {
-    extern __shared__ unsigned long long key[];          // [nPow2]
+    extern __shared__ unsigned long long smx[];
+    unsigned long long* sel = smx;                                   // [nSort]
+    uint32_t* skey = reinterpret_cast<uint32_t*>(smx + nSort);       // [nRef]
     __shared__ float zp[kEmb];
     __shared__ float red[8];
-    const int l = blockIdx.x;
+    __shared__ unsigned hist[256];
+    __shared__ unsigned ws[8];
+    __shared__ unsigned sPrefix, sMask, sK;
+    const int l = blockIdx.x, tid = threadIdx.x;
     const float* o = out + (size_t)l * kOut;
-    if (threadIdx.x < kEmb) {
-        const float a = o[threadIdx.x];
-        float s = a * a;
-        for (int k = 16; k; k >>= 1) s += __shfl_xor_sync(0xffffffffu, s, k);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    if (tid < kEmb) {
+        const float a = o[tid];
+        float q = a * a;
+        for (int k = 16; k; k >>= 1) q += __shfl_xor_sync(0xffffffffu, q, k);
+        if ((tid & 31) == 0) red[tid >> 5] = q;
     }
     __syncthreads();
-    if (threadIdx.x < kEmb) zp[threadIdx.x] = o[threadIdx.x] / sqrtf(red[0] + red[1] + 1e-12f);
+    if (tid < kEmb) zp[tid] = o[tid] / sqrtf(red[0] + red[1] + 1e-12f);
+    if (tid == 0) {
+        sPrefix = 0u;
+        sMask = 0u;
+        sK = (unsigned)nRot;
+    }
     __syncthreads();
-    for (int j = threadIdx.x; j < nPow2; j += blockDim.x) {
-        unsigned long long k = 0;                        // padding sorts last
-        if (j < nRef) {
-            const float4* r = reinterpret_cast<const float4*>(ref + (size_t)j * kEmb);
-            float acc = 0.f;
+    for (int j = tid; j < nRef; j += blockDim.x) {
+        const float4* r = reinterpret_cast<const float4*>(ref + (size_t)j * kEmb);
+        float acc = 0.f;
 #pragma unroll
-            for (int q = 0; q < kEmb / 4; q++) {
-                const float4 v = __ldg(r + q);
-                acc = fmaf(zp[4 * q], v.x, acc);
-                acc = fmaf(zp[4 * q + 1], v.y, acc);
-                acc = fmaf(zp[4 * q + 2], v.z, acc);
-                acc = fmaf(zp[4 * q + 3], v.w, acc);
-            }
-            // order-preserving map of the float score, then the inverted index
-            const unsigned int b = __float_as_uint(acc);
-            const unsigned int ob = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-            k = ((unsigned long long)ob << 32) | (0xFFFFFFFFu - (unsigned int)j);
+        for (int q = 0; q < kEmb / 4; q++) {
+            const float4 v = __ldg(r + q);
+            acc = fmaf(zp[4 * q], v.x, acc);
+            acc = fmaf(zp[4 * q + 1], v.y, acc);
+            acc = fmaf(zp[4 * q + 2], v.z, acc);
+            acc = fmaf(zp[4 * q + 3], v.w, acc);
         }
-        key[j] = k;
+        const unsigned b = __float_as_uint(acc);
+        skey[j] = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
     }
+    // the nRot-th largest key
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        hist[tid] = 0u;
+        __syncthreads();
+        const unsigned prefix = sPrefix, mask = sMask;
+        for (int j = tid; j < nRef; j += blockDim.x) {
+            const unsigned k = skey[j];
+            if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            unsigned kth = sK, acc = 0u;
+            int d = 255;
+            for (; d > 0; d--) {
+                if (acc + hist[d] >= kth) break;
+                acc += hist[d];
+            }
+            sK = kth - acc;
+            sPrefix = prefix | ((unsigned)d << shift);
+            sMask = mask | (255u << shift);
+        }
+        __syncthreads();
+    }
+    const unsigned T = sPrefix, kEq = sK;
+    // compaction in index order: thread t holds indices [t per, (t + 1) per)
+    const int per = (nRef + blockDim.x - 1) / blockDim.x;
+    const int j0 = min(nRef, tid * per), j1 = min(nRef, j0 + per);
+    unsigned cg = 0u, ce = 0u;
+    for (int j = j0; j < j1; j++) {
+        cg += skey[j] > T;
+        ce += skey[j] == T;
+    }
+    unsigned totG, totE;
+    unsigned pg = block_scan256(cg, ws, &totG) - cg;
+    unsigned pe = block_scan256(ce, ws, &totE) - ce;
+    for (int j = j0; j < j1; j++) {
+        const unsigned k = skey[j];
+        const unsigned long long key = ((unsigned long long)k << 32) | (0xFFFFFFFFu - (unsigned)j);
+        if (k > T) {
+            sel[pg++] = key;
+        } else if (k == T) {
+            if (pe < kEq) sel[totG + pe] = key;
+            pe++;
+        }
+    }
+    for (int j = nRot + tid; j < nSort; j += blockDim.x) sel[j] = 0ull;
     __syncthreads();
-    // bitonic sort, descending
-    for (int size = 2; size <= nPow2; size <<= 1)
+    for (int size = 2; size <= nSort; size <<= 1)
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int t = threadIdx.x; t < nPow2 / 2; t += blockDim.x) {
+            for (int t = tid; t < nSort / 2; t += blockDim.x) {
                 const int lo = 2 * t - (t & (stride - 1));
                 const int hi = lo + stride;
                 const bool desc = (lo & size) == 0;
-                const unsigned long long a = key[lo], b = key[hi];
+                const unsigned long long a = sel[lo], b = sel[hi];
                 if ((a < b) == desc) {
-                    key[lo] = b;
-                    key[hi] = a;
+                    sel[lo] = b;
+                    sel[hi] = a;
                 }
             }
             __syncthreads();
         }
-    for (int j = threadIdx.x; j < nRot; j += blockDim.x) {
-        const int idx = (int)(0xFFFFFFFFu - (unsigned int)(key[j] & 0xFFFFFFFFu));
+    for (int j = tid; j < nRot; j += blockDim.x) {
+        const int idx = (int)(0xFFFFFFFFu - (unsigned int)(sel[j] & 0xFFFFFFFFu));
         if (idxOut) idxOut[(size_t)l * nRot + j] = idx;
         const double* src = refQuat + 4 * (size_t)idx;
         double* qo = quat + ((size_t)l * nRot + j) * 4;
@@ -1122,8 +1196,9 @@ extern "C" int tg3_cnn_match_propose(const float* out, int n, const float* ref, 
         nRot <= 0 || nRot > nRef || nTrans <= 0 || nTrans > 512)
         return fail(TG3_ERR_ARG, "bad match arguments (nRot <= nRef <= 16384, nTrans <= 512)");
     int p2 = 1;
-    while (p2 < nRef) p2 <<= 1;
-    const size_t smem = sizeof(unsigned long long) * p2;
+    while (p2 < nRot) p2 <<= 1;
+    const size_t smem = sizeof(unsigned long long) * p2 + sizeof(uint32_t) * (size_t)nRef;
+    if (smem > 200 * 1024) return fail(TG3_ERR_ARG, "match sizes need too much shared memory");
     TG3_CUDA(cudaFuncSetAttribute(k_match_propose, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
     k_match_propose<<<n, 256, smem, static_cast<cudaStream_t>(stream)>>>(
