@@ -1283,7 +1283,7 @@ def main():
     ap.add_argument("--workload", default="local256",
                     choices=["local256", "local256c3", "global64", "uneven192", "learned128"])
     ap.add_argument("--train-particles", type=int, default=150000)
-    ap.add_argument("--epochs", type=int, default=6)
+    ap.add_argument("--epochs", type=int, default=3)
     ap.add_argument("--learned-snr", type=float, default=1.0,
                     help="noise level of the learned-proposal particles (signal / noise power)")
     ap.add_argument("--learned-lr", type=float, default=2e-3)

@@ -1246,10 +1246,10 @@ __global__ void k_bank_planes(const float* __restrict__ f32, int nB, int K, int 
     }
 }
 
-// CTA (particle, group of 16 rows): w = sigRcp ctf^2 of the particle in
-// shared memory, then per row a 16-byte copy of the bank row and the norm
-// as a block reduction.
-constexpr int kBankRows = 16;
+// CTA (particle, group of 64 rows): w = sigRcp ctf^2 of the particle in
+// shared memory; a warp per row copies the bank row in 16-byte units and
+// sums its norm with shuffles.
+constexpr int kBankRows = 64;
 
 __global__ void __launch_bounds__(256)
 k_bank_gather(const BankView* __restrict__ table, const int* __restrict__ cls,
@@ -1259,7 +1259,6 @@ k_bank_gather(const BankView* __restrict__ table, const int* __restrict__ cls,
               int* __restrict__ flag)
 {
     extern __shared__ float w[];                 // [K]
-    __shared__ float red[8];
     const int l = blockIdx.x;
     const BankView b = table[cls ? cls[l] : 0];
     for (int p = threadIdx.x; p < K; p += blockDim.x) {
@@ -1267,45 +1266,39 @@ k_bank_gather(const BankView* __restrict__ table, const int* __restrict__ cls,
         w[p] = sigRcp[(size_t)l * K + p] * c * c;
     }
     __syncthreads();
-    const int j0 = blockIdx.y * kBankRows;
-    const int j1 = min(nR, j0 + kBankRows);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j1 = min(nR, (blockIdx.y + 1) * kBankRows);
     const int n16 = Kp / 4;                      // 16-byte units of a row (4 floats / 8 bf16)
-    for (int j = j0; j < j1; j++) {
+    for (int j = blockIdx.y * kBankRows + warp; j < j1; j += 8) {
         const size_t row = (size_t)l * nR + j;
-        int r = idx[row];
+        const int r = idx[row];
         const bool ok = r >= 0 && r < b.nB;
-        if (!ok && threadIdx.x == 0) atomicOr(flag, 1 << 16);
+        if (!ok && lane == 0) atomicOr(flag, 1 << 16);
+        const size_t rs = (size_t)(ok ? r : 0);
         if (splitLo == 0) {
-            const float4* src = reinterpret_cast<const float4*>(b.f32 + (size_t)(ok ? r : 0) * Kp);
+            const float4* src = reinterpret_cast<const float4*>(b.f32 + rs * Kp);
             float4* dst = reinterpret_cast<float4*>(P + row * Kp);
-            for (int u = threadIdx.x; u < n16; u += blockDim.x)
+            for (int u = lane; u < n16; u += 32)
                 dst[u] = ok ? __ldg(src + u) : make_float4(0.f, 0.f, 0.f, 0.f);
         } else {
             __nv_bfloat16* hp = reinterpret_cast<__nv_bfloat16*>(P);
-            const uint4* sh = reinterpret_cast<const uint4*>(b.hi + (size_t)(ok ? r : 0) * Kp);
-            const uint4* sl = reinterpret_cast<const uint4*>(b.lo + (size_t)(ok ? r : 0) * Kp);
+            const uint4* sh = reinterpret_cast<const uint4*>(b.hi + rs * Kp);
+            const uint4* sl = reinterpret_cast<const uint4*>(b.lo + rs * Kp);
             uint4* dh = reinterpret_cast<uint4*>(hp + row * Kp);
             uint4* dl = reinterpret_cast<uint4*>(hp + splitLo + row * Kp);
             const uint4 z = make_uint4(0u, 0u, 0u, 0u);
-            for (int u = threadIdx.x; u < n16 / 2; u += blockDim.x) {
+            for (int u = lane; u < n16 / 2; u += 32) {
                 dh[u] = ok ? __ldg(sh + u) : z;
                 dl[u] = ok ? __ldg(sl + u) : z;
             }
         }
         float acc = 0.f;
         if (ok) {
-            const float* a2 = b.abs2 + (size_t)r * K;
-            for (int p = threadIdx.x; p < K; p += blockDim.x) acc = fmaf(w[p], __ldg(a2 + p), acc);
+            const float* a2 = b.abs2 + rs * K;
+            for (int p = lane; p < K; p += 32) acc = fmaf(w[p], __ldg(a2 + p), acc);
         }
         for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            float s = 0.f;
-            for (int k = 0; k < 8; k++) s += red[k];
-            nrm[row] = s;
-        }
-        __syncthreads();
+        if (lane == 0) nrm[row] = acc;
     }
 }
 
