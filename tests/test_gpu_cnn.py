@@ -197,3 +197,19 @@ def test_tensor_core_inference_matches_oracle(net):
     net.forward(torch.as_tensor(img).to(DEV), f32)
     ref32 = f32.cpu().numpy()
     assert np.abs(got - ref32).max() < 5e-2 * np.abs(ref32).max()
+
+
+def test_inference_does_not_depend_on_the_batch(net):
+    """2,100 images (two inference chunks of 2,048 and partial pixel tiles):
+    every image's outputs are bit-identical to those of the same image in a
+    batch of its own or of 5."""
+    rng = np.random.default_rng(53)
+    n = 2100
+    img = torch.as_tensor(rng.standard_normal((n, 64, 64)).astype(np.float32)).to(DEV)
+    net.set_bf16(True)
+    out = torch.empty((n, tg3.Cnn.N_OUT), dtype=torch.float32, device=DEV)
+    net.infer(img, out)
+    for i0, m in ((0, 1), (2047, 5), (2099, 1)):
+        o2 = torch.empty((m, tg3.Cnn.N_OUT), dtype=torch.float32, device=DEV)
+        net.infer(img[i0:i0 + m].contiguous(), o2)
+        assert torch.equal(o2, out[i0:i0 + m])

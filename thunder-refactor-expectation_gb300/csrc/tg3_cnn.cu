@@ -816,6 +816,7 @@ struct tg3_cnn {
     int tcCap = 0;
     __nv_bfloat16* tcAct[kLayers] = {};     // outputs of layers 0 .. 6
     int* tcFlag = nullptr;
+    float* tcPartial = nullptr;             // split-K sums of the dense layer
     // contrastive scratch (matching mode), grown as needed
     int embCap = 0;
     float* emb = nullptr;       // zp, zr [n][64]; invP, invR [n]; rowL, colL [n]; S, G [n][n]
@@ -987,6 +988,7 @@ extern "C" int tg3_cnn_destroy(tg3_cnn* net)
     cudaFree(net->embLoss);
     cudaFree(net->tcW);
     cudaFree(net->tcFlag);
+    cudaFree(net->tcPartial);
     for (int l = 0; l < kLayers; l++) cudaFree(net->tcAct[l]);
     cudaFree(net->params);
     cudaFree(net->grads);
@@ -1253,6 +1255,7 @@ __global__ void k_tc_repack(const float* __restrict__ W, int l, int rows, int kp
 }
 
 constexpr int kInferChunk = 2048;
+constexpr int kDenseSplit = 16;
 
 int tc_prepare(tg3_cnn* net, int n)
 {
@@ -1286,8 +1289,12 @@ int tc_prepare(tg3_cnn* net, int n)
             net->tcAct[l] = nullptr;
         }
         net->tcCap = 0;
+        cudaFree(net->tcPartial);
+        net->tcPartial = nullptr;
         for (int l = 0; l < kLayers - 1; l++)
             TG3_CUDA(cudaMalloc(&net->tcAct[l], sizeof(__nv_bfloat16) * act_size(l + 1) * cap));
+        TG3_CUDA(cudaMalloc(&net->tcPartial,
+                            sizeof(float) * kDenseSplit * (size_t)cap * kShape[6].cout));
         net->tcCap = cap;
     }
     return TG3_OK;
@@ -1340,6 +1347,9 @@ extern "C" int tg3_cnn_infer(tg3_cnn* net, const float* img, int n, float* out)
             a.tmemCols = sh.cout < 32 ? 32 : sh.cout;
             a.relu = 1;
             a.flag = net->tcFlag;
+            // the dense layer: few rows of 128 images, 256 K blocks -> 16 K slices
+            a.kSplit = sh.stride ? 1 : kDenseSplit;
+            a.partial = sh.stride ? nullptr : net->tcPartial;
             TG3_CUDA(launch_conv_tc(a, s));
         }
         TG3_CUDA(launch_fc_out(net->tcAct[6], net->tcW + net->tcOff[7],

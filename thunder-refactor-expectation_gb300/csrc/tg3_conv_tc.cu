@@ -4,6 +4,10 @@
 // GEMM on the 5th-generation tensor cores; the first convolution (one input
 // channel) and the 256 -> 68 output layer on CUDA cores.
 //
+// A split-K launch (the dense layer: few output rows, a long K) gives each
+// CTA of grid row y a slice of the K blocks and writes FP32 partial sums,
+// added in slice order by k_splitk_reduce with the bias and ReLU.
+//
 // Implicit GEMM: M = output pixels (images x rows x columns, NHWC order),
 // N = output channels, K = taps x input channels (tap-major).  A CTA takes
 // 128 output pixels and all N channels; per K block of 32 bf16 (one tap,
@@ -38,7 +42,7 @@ __device__ __forceinline__ uint32_t swz64(int r, int b)
                       ((((b >> 4) ^ ((r >> 1) & 3)) << 4) | (b & 15)));
 }
 
-__global__ void __launch_bounds__(CT_THREADS)
+__global__ void __launch_bounds__(CT_THREADS, 4)
 k_conv_tc(ConvTcArgs a)
 {
     extern __shared__ uint8_t smem_raw[];
@@ -88,22 +92,21 @@ k_conv_tc(ConvTcArgs a)
         ox = rem % a.Wo;
     }
     const int taps = a.ks * a.ks;
-    const int nkb = a.Kpad / CT_BK;
+    // this CTA's K blocks: all, or its slice of a split-K launch
+    const int nkbAll = a.Kpad / CT_BK;
+    const int per = (nkbAll + a.kSplit - 1) / a.kSplit;
+    const int kbBeg = blockIdx.y * per;
+    const int nkb = min(nkbAll, kbBeg + per) - kbBeg;
     const uint32_t idesc = umma_idesc(CT_M, a.coutPad);
     bool issued = false;
-    for (int kb = 0; kb < nkb; kb++) {
-        const int s = kb & 1;
-        uint8_t* st = smem + s * stageBytes;
-        // the MMAs of block kb - 2 read this stage
-        if (kb >= 2 && tid == 0 && !mbar_wait(empty + s, ((kb - 2) >> 1) & 1, kWaitBudget))
-            *abortp = 1;
-        __syncthreads();
-        if (*abortp) break;
-        // A: 16 channels of one tap for this row
-        const int k0 = kb * CT_BK;
+    // the next block's A and B pieces, loaded a block ahead into registers
+    uint4 v0, v1, wb[4];
+    auto load_block = [&](int kb) {
+        const int k0 = (kbBeg + kb) * CT_BK;
         const int tap = k0 / a.Cin;
         const int ci = k0 - tap * a.Cin + 16 * hh;
-        uint4 v0 = make_uint4(0u, 0u, 0u, 0u), v1 = v0;
+        v0 = make_uint4(0u, 0u, 0u, 0u);
+        v1 = v0;
         if (rowOk && tap < taps) {
             const int ky = tap / a.ks, kx = tap - (tap / a.ks) * a.ks;
             const int iy = oy * a.stride + ky - a.pad, ix = ox * a.stride + kx - a.pad;
@@ -114,14 +117,34 @@ k_conv_tc(ConvTcArgs a)
                 v1 = __ldg(src + 1);
             }
         }
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int u = tid + i * CT_THREADS;
+            if (u < a.coutPad * 4)
+                wb[i] = __ldg(reinterpret_cast<const uint4*>(a.w + (size_t)(u >> 2) * a.Kpad + k0) +
+                              (u & 3));
+        }
+    };
+    if (nkb > 0) load_block(0);
+    for (int kb = 0; kb < nkb; kb++) {
+        const int s = kb & 1;
+        uint8_t* st = smem + s * stageBytes;
+        // the MMAs of block kb - 2 read this stage
+        if (kb >= 2 && tid == 0 && !mbar_wait(empty + s, ((kb - 2) >> 1) & 1, kWaitBudget))
+            *abortp = 1;
+        __syncthreads();
+        if (*abortp) break;
+        // A: 16 channels of one tap for this row; B: the block's 32 K columns
+        // of every output channel
         *reinterpret_cast<uint4*>(st + swz64(r, 32 * hh)) = v0;
         *reinterpret_cast<uint4*>(st + swz64(r, 32 * hh + 16)) = v1;
-        // B: the block's 32 K columns of every output channel
-        for (int u = tid; u < a.coutPad * 4; u += CT_THREADS) {
-            const int row = u >> 2, q = u & 3;
-            const uint4 w = __ldg(reinterpret_cast<const uint4*>(a.w + (size_t)row * a.Kpad + k0) + q);
-            *reinterpret_cast<uint4*>(st + CT_ABYTES + swz64(row, 16 * q)) = w;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int u = tid + i * CT_THREADS;
+            if (u < a.coutPad * 4)
+                *reinterpret_cast<uint4*>(st + CT_ABYTES + swz64(u >> 2, 16 * (u & 3))) = wb[i];
         }
+        if (kb + 1 < nkb) load_block(kb + 1);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
@@ -136,7 +159,7 @@ k_conv_tc(ConvTcArgs a)
         }
         issued = true;
     }
-    if (tid == 0 && !*abortp && !mbar_wait(accum, 0, kWaitBudget)) *abortp = 1;
+    if (tid == 0 && !*abortp && nkb > 0 && !mbar_wait(accum, 0, kWaitBudget)) *abortp = 1;
     __syncthreads();
     const bool ok = !*abortp;
     if (ok) {
@@ -146,8 +169,20 @@ k_conv_tc(ConvTcArgs a)
         const long long mo = m0 + row;
         for (int c0 = 16 * colHalf; c0 < a.coutPad; c0 += 32) {
             float v[16];
-            tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)c0, v);
-            if (mo < M && c0 < a.Cout) {
+            if (nkb > 0) {
+                tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)c0, v);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 16; i++) v[i] = 0.f;
+            }
+            if (a.partial && mo < M && c0 < a.Cout) {
+                // split-K: this slice's sums, reduced by k_splitk_reduce
+                float4* dst = reinterpret_cast<float4*>(
+                    a.partial + ((size_t)blockIdx.y * M + mo) * a.Cout + c0);
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+                    dst[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+            } else if (mo < M && c0 < a.Cout) {
                 uint32_t pk[8];
 #pragma unroll
                 for (int i = 0; i < 8; i++) {
@@ -229,19 +264,54 @@ k_conv1_nhwc(const float* __restrict__ img, const __nv_bfloat16* __restrict__ w,
 }
 
 // Output layer: out[i][o] = bias[o] + sum_k W[o][k] act[i][k] (FP32 out).
-__global__ void k_fc_out(const __nv_bfloat16* __restrict__ act, const __nv_bfloat16* __restrict__ w,
-                         const float* __restrict__ bias, int n, int K, int N,
-                         float* __restrict__ out)
+// A CTA takes 8 images (their inputs in shared memory); a warp per output
+// row of W, lanes along k (coalesced), one shuffle reduction per image.
+constexpr int kFcImages = 8;
+
+__global__ void __launch_bounds__(256)
+k_fc_out(const __nv_bfloat16* __restrict__ act, const __nv_bfloat16* __restrict__ w,
+         const float* __restrict__ bias, int n, int K, int N, float* __restrict__ out)
 {
-    const int i = blockIdx.x;
-    extern __shared__ float xs[];
-    for (int k = threadIdx.x; k < K; k += blockDim.x)
-        xs[k] = __bfloat162float(act[(size_t)i * K + k]);
+    extern __shared__ float xs[];                      // [kFcImages][K]
+    const int i0 = blockIdx.x * kFcImages;
+    const int ni = min(kFcImages, n - i0);
+    for (int t = threadIdx.x; t < ni * K; t += blockDim.x)
+        xs[t] = __bfloat162float(act[(size_t)i0 * K + t]);
     __syncthreads();
-    for (int o = threadIdx.x; o < N; o += blockDim.x) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int o = warp; o < N; o += blockDim.x >> 5) {
+        float acc[kFcImages];
+#pragma unroll
+        for (int i = 0; i < kFcImages; i++) acc[i] = 0.f;
+        for (int k = lane; k < K; k += 32) {
+            const float wk = __bfloat162float(w[(size_t)o * K + k]);
+#pragma unroll
+            for (int i = 0; i < kFcImages; i++)
+                if (i < ni) acc[i] = fmaf(wk, xs[i * K + k], acc[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < kFcImages; i++) {
+            float v = acc[i];
+            for (int sft = 16; sft; sft >>= 1) v += __shfl_xor_sync(0xffffffffu, v, sft);
+            if (lane == 0 && i < ni) out[(size_t)(i0 + i) * N + o] = v + bias[o];
+        }
+    }
+}
+
+// out[m][c] = bf16(act(sum over the slices of partial[s][m][c] + bias[c])),
+// the slices in order.
+__global__ void k_splitk_reduce(const float* __restrict__ partial, int kSplit, long long M,
+                                int Cout, const float* __restrict__ bias, int relu,
+                                __nv_bfloat16* __restrict__ out)
+{
+    const size_t n = (size_t)M * Cout;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
         float acc = 0.f;
-        for (int k = 0; k < K; k++) acc = fmaf(__bfloat162float(w[(size_t)o * K + k]), xs[k], acc);
-        out[(size_t)i * N + o] = acc + bias[o];
+        for (int s = 0; s < kSplit; s++) acc += partial[(size_t)s * n + i];
+        acc += bias[i % Cout];
+        if (relu) acc = fmaxf(acc, 0.f);
+        out[i] = __float2bfloat16_rn(acc);
     }
 }
 
@@ -262,10 +332,17 @@ cudaError_t launch_conv_tc(const ConvTcArgs& a, cudaStream_t st)
     cudaError_t e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
+    if (a.kSplit < 1 || a.kSplit > 65535 || (a.kSplit > 1 && !a.partial))
+        return cudaErrorInvalidValue;
     const long long M = (long long)a.n * a.Ho * a.Wo;
     const long long grid = (M + CT_M - 1) / CT_M;
     if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    k_conv_tc<<<(unsigned)grid, CT_THREADS, smem, st>>>(a);
+    k_conv_tc<<<dim3((unsigned)grid, (unsigned)a.kSplit), CT_THREADS, smem, st>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || !a.partial) return e;
+    const size_t n = (size_t)M * a.Cout;
+    k_splitk_reduce<<<(unsigned)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, st>>>(
+        a.partial, a.kSplit, M, a.Cout, a.bias, a.relu, a.out);
     return cudaGetLastError();
 }
 
@@ -281,7 +358,9 @@ cudaError_t launch_conv1_nhwc(const float* img, const __nv_bfloat16* w, const fl
 cudaError_t launch_fc_out(const __nv_bfloat16* act, const __nv_bfloat16* w, const float* bias,
                           int n, int K, int N, float* out, cudaStream_t st)
 {
-    k_fc_out<<<n, 128, sizeof(float) * K, st>>>(act, w, bias, n, K, N, out);
+    const size_t smem = sizeof(float) * kFcImages * (size_t)K;
+    if (smem > 48 * 1024) return cudaErrorInvalidValue;
+    k_fc_out<<<(n + kFcImages - 1) / kFcImages, 256, smem, st>>>(act, w, bias, n, K, N, out);
     return cudaGetLastError();
 }
 

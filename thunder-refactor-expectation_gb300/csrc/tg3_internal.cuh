@@ -294,6 +294,8 @@ struct ConvTcArgs {
     const float* bias;
     __nv_bfloat16* out;
     int n, H, W, Cin, Ho, Wo, Cout, coutPad, ks, stride, pad, Kpad, tmemCols, relu;
+    int kSplit;          // K slices (1: no split); > 1 needs partial
+    float* partial;      // [kSplit][M][Cout] FP32 sums of the slices
     int* flag;
 };
 size_t conv_tc_smem(int coutPad);
