@@ -682,6 +682,13 @@ def run_uneven(args, rank, world, local_rank):
     return res
 
 
+# the same comparison at box 256: maps, cutoff and noise model of the
+# production configuration (256^3, 1.1 A/px, 200 blobs; cutoff 80, K = 9,930;
+# SNR 0.03 over the likelihood's pixels), shifts within the global search's
+# 7 x 7 translation grid
+LEARNED256 = dict(box=256, pixel_size=1.1, n_blobs=200, sigma_a=(1.5, 3.0), radius_px=80.0,
+                  n_maps=16, n_train_maps=12, rU=80, pf=2, shift=3.0, snr_lik=0.03,
+                  n_rot=256, n_trans=25)
 LEARNED = dict(box=128, pixel_size=1.4, n_blobs=120, sigma_a=(1.5, 3.0), radius_px=40.0,
                n_maps=16, n_train_maps=12, rU=32, pf=2, shift=3.0, snr=0.05,
                n_rot=256, n_trans=25)
@@ -718,14 +725,22 @@ def reconstruction_resolution(tg3, torch, ctx, ps, maps, quat, trans, box, pf, p
                 u = (k - 1) + (f[k - 1] - 0.143) / max(f[k - 1] - f[k], 1e-12)
                 break
         out.append(pf * box * px / u)
-        del F, T, V, truth
+        del F, T, V
     return round(float(np.mean(out)), 3)
 
 
+_TRUTH = {}
+
+
 def synth_padded(bm, box, pf, dev):
+    """The map's exact padded transform (kept: every pose source is compared
+    with the same maps)."""
     import torch
     from tg3 import synth
-    return synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32)
+    key = (id(bm), box, pf)
+    if key not in _TRUTH:
+        _TRUTH[key] = synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32)
+    return _TRUTH[key]
 
 
 def run_learned(args, rank, world, local_rank):
@@ -745,7 +760,7 @@ def run_learned(args, rank, world, local_rank):
     from tg3 import learned, synth
     torch.cuda.set_device(local_rank)
     dev = f"cuda:{local_rank}"
-    L = LEARNED
+    L = LEARNED256 if args.workload == "learned256" else LEARNED
     box, px, pf, rU = L["box"], L["pixel_size"], L["pf"], L["rU"]
     rng = np.random.default_rng(4000)
     maps = [synth.blob_map(rng, L["n_blobs"], L["sigma_a"], px, L["radius_px"])
@@ -754,13 +769,22 @@ def run_learned(args, rank, world, local_rank):
     prec = tg3.SCORE_BF16X3 if args.precision == "bf16x3" else tg3.SCORE_FP32
     nTr = L["n_train_maps"]
     t0 = time.perf_counter()
+    # noise: SNR over the image grid, or (box 256) over the likelihood's pixels
+    if "snr_lik" in L:
+        noise = dict(noise_var=synth.signal_power(maps[:nTr], box, px, rU, rL, device=dev)
+                     / L["snr_lik"] / 2.0)
+        snr_note = f"{L['snr_lik']} over the likelihood's pixels (cutoff {rU})"
+    else:
+        noise = {}
+        snr_note = f"{args.learned_snr} over the image grid"
     # training pairs, generated in chunks (images stay on the device)
     imgs, Rs, ts, qtrue, ctr = [], [], [], [], []
     chunk = 10000
     for s0 in range(0, args.train_particles, chunk):
         m = min(chunk, args.train_particles - s0)
         ps = synth.particle_set(4100 + s0, maps[:nTr], np.arange(m) % nTr, box, px, rU, rL,
-                                L["shift"], args.learned_snr, device=dev)
+                                L["shift"], args.learned_snr, device=dev, with_data=False,
+                                **noise)
         imgs.append(ps.images)
         Rs.append(synth.quat_to_mat(ps.quat_true).reshape(m, 9))
         ts.append(ps.trans_true)
@@ -972,9 +996,9 @@ def run_learned(args, rank, world, local_rank):
     nSeen = args.eval_particles_seen
     nUn = args.eval_particles_unseen
     seen = synth.particle_set(rank_seed(5001, rank), maps[:nTr], np.arange(nSeen) % nTr, box, px, rU, rL,
-                              L["shift"], args.learned_snr, device=dev)
+                              L["shift"], args.learned_snr, device=dev, **noise)
     unseen = synth.particle_set(rank_seed(5002, rank), maps[nTr:], np.arange(nUn) % (L["n_maps"] - nTr), box, px,
-                                rU, rL, L["shift"], args.learned_snr, device=dev)
+                                rU, rL, L["shift"], args.learned_snr, device=dev, **noise)
     unseen.cls = unseen.cls + nTr
     rs = evaluate(seen, "seen")
     ru = evaluate(unseen, "unseen")
@@ -1035,17 +1059,18 @@ def run_learned(args, rank, world, local_rank):
                                             rU, dev)
                for k, (q, t) in poses.items()}
     res = {"metric": "learned proposal + split-bf16 E-step (rescoring and fallback global search) "
-                     "vs plain FP32 global search, box 128, held-out maps",
+                     f"vs plain FP32 global search, box {box}, held-out maps",
            "value": report(ru)["proposal_with_split_bf16_fallback"]["particles_per_s"],
            "unit": UNIT,
            "n_gpus": world, "scaling": "weak",
            "higher_is_better": True, "precision": args.precision,
-           "config": {"workload": "16 blob maps 128^3 (120 blobs, 1.4 A/px): 12 training maps, "
-                                  "4 held out; proposal 256 rotations x 25 translations rescored "
-                                  "exactly, fallback 6,912 x 49 global search; cutoff 32, K = "
-                                  + str(len(seen.iCol)),
+           "config": {"workload": f"16 blob maps {box}^3 ({L['n_blobs']} blobs, {px} A/px): 12 "
+                                  "training maps, 4 held out; proposal 256 rotations x 25 "
+                                  "translations rescored exactly, fallback 6,912 x 49 global "
+                                  f"search; cutoff {rU}, K = " + str(len(seen.iCol)),
                       "train_particles": args.train_particles, "epochs": args.epochs,
-                      "snr": args.learned_snr, "learning_rate": args.learned_lr,
+                      "snr": snr_note, "shift_px": L["shift"],
+                      "learning_rate": args.learned_lr,
                       "eval_particles": {"seen_maps": nSeen, "held_out_maps": nUn},
                       "labels": "true poses of the synthetic particles"},
            "training": {"generate_s": round(gen_s, 1), "train_s": round(train_s, 1),
@@ -1281,7 +1306,8 @@ def main():
                     help="split-bf16 path through the fused projection + tcgen05 kernel")
     ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
     ap.add_argument("--workload", default="local256",
-                    choices=["local256", "local256c3", "global64", "uneven192", "learned128"])
+                    choices=["local256", "local256c3", "global64", "uneven192", "learned128",
+                             "learned256"])
     ap.add_argument("--train-particles", type=int, default=150000)
     ap.add_argument("--epochs", type=int, default=3)
     ap.add_argument("--learned-snr", type=float, default=1.0,
@@ -1307,7 +1333,7 @@ def main():
         res = run_global(args, rank, world, local)
     elif args.workload == "uneven192":
         res = run_uneven(args, rank, world, local)
-    elif args.workload == "learned128":
+    elif args.workload in ("learned128", "learned256"):
         res = run_learned(args, rank, world, local)
     else:
         res = run_tg3(args, rank, world, local)

@@ -389,17 +389,21 @@ class ParticleSet:
 
 def particle_set(seed: int, maps, cls, box: int, pixel_size: float, rU: float, rL: float,
                  shift_range: float, snr: float, img: int = 64, device="cpu",
-                 chunk: int = 512) -> ParticleSet:
+                 chunk: int = 512, noise_var: float | None = None,
+                 with_data: bool = True) -> ParticleSet:
     """Particles of several maps (particle l shows maps[cls[l]]) at Haar-uniform
     poses and U(-shift_range, shift_range) shifts, with CTF and white noise at
-    `snr` (signal / noise power over the band-limited grid).
+    `snr` (signal / noise power over the band-limited image grid), or of
+    variance `noise_var` per real and imaginary part when given.
 
-    The data of a particle is its transform on the rfft grid of an img x img
-    image at the full box's frequencies (|k| <= img / 2, i.e. the box
-    band-limited and downsampled by box / img).  Its real-space image (the
-    network's input, centred, normalised to zero mean and unit deviation) and
-    its values at the pixels of cutoff rU (the likelihood's input) come from
-    that one noisy transform, so both see the same particle."""
+    The data of a particle is one noisy transform on the union of two pixel
+    sets at the full box's frequencies: the rfft grid of an img x img image
+    (|k| <= img / 2, i.e. the box band-limited and downsampled by box / img)
+    and the pixels of cutoff rU (the likelihood's input).  Its real-space image
+    (the network's input, centred, normalised to zero mean and unit
+    deviation) and its values at the likelihood's pixels come from that one
+    transform, so both see the same particle.  with_data=False computes the
+    image only (dat, ctf and sigRcp are then empty)."""
     rng = np.random.default_rng(seed)
     cls = np.asarray(cls)
     n = len(cls)
@@ -410,34 +414,76 @@ def particle_set(seed: int, maps, cls, box: int, pixel_size: float, rU: float, r
     jj = np.concatenate([np.arange(0, h), np.arange(-h, 0)])     # FFT row order
     ii = np.arange(0, h + 1)
     J, I = np.meshgrid(jj, ii, indexing="ij")
-    gi, gj = I.ravel(), J.ravel()                                  # (img (h + 1),)
-    ctf_g = ctf_values(attr, pixel_size, box, gi, gj)              # (n, G)
+    gi, gj = I.ravel(), J.ravel()                                  # image grid (img (h + 1),)
+    iCol, iRow, _, _ = pixel_index(box, rU, rL)
+    if with_data:
+        # union of the image grid and the likelihood's pixels, image grid first
+        key_img = gj.astype(np.int64) * (box + 1) + gi
+        key_lik = iRow.astype(np.int64) * (box + 1) + iCol
+        img_pos = {int(k): i for i, k in enumerate(key_img)}
+        inside = np.isin(key_lik, key_img)
+        ui = np.concatenate([gi, iCol[~inside]])
+        uj = np.concatenate([gj, iRow[~inside]])
+        lik = np.empty(len(iCol), np.int64)
+        lik[inside] = [img_pos[int(k)] for k in key_lik[inside]]
+        lik[~inside] = len(gi) + np.arange(int((~inside).sum()))
+    else:
+        ui, uj, lik = gi, gj, None
+    G = len(gi)
+    ctf_u = ctf_values(attr, pixel_size, box, ui, uj)              # (n, U)
     R = quat_to_mat(q)
-    k2 = np.stack([gi, gj, np.zeros_like(gi)], 0).astype(np.float32) / box
-    sig = np.empty((n, len(gi)), np.complex64)
+    k2 = np.stack([ui, uj, np.zeros_like(ui)], 0).astype(np.float32) / box
+    sig = np.empty((n, len(ui)), np.complex64)
     for c in range(len(maps)):
-        sel = np.nonzero(cls == c)[0]
-        for s in range(0, len(sel), chunk):
-            ids = sel[s:s + chunk]
+        sel_c = np.nonzero(cls == c)[0]
+        for s0 in range(0, len(sel_c), chunk):
+            ids = sel_c[s0:s0 + chunk]
             f = torch.as_tensor(np.einsum("nij,jk->nki", R[ids].astype(np.float32), k2), device=device)
             sig[ids] = blob_ft(maps[c], f).cpu().numpy()
-    sig *= ctf_g.astype(np.float32)
-    sig *= np.exp(-2j * math.pi * (np.outer(t[:, 0] / box, gi) + np.outer(t[:, 1] / box, gj))).astype(np.complex64)
-    p_sig = float(np.mean(np.abs(sig) ** 2))
-    s2 = p_sig / snr / 2.0
+    sig *= ctf_u.astype(np.float32)
+    sig *= np.exp(-2j * math.pi * (np.outer(t[:, 0] / box, ui) + np.outer(t[:, 1] / box, uj))).astype(np.complex64)
+    if noise_var is None:
+        p_sig = float(np.mean(np.abs(sig[:, :G]) ** 2))
+        s2 = p_sig / snr / 2.0
+    else:
+        s2 = float(noise_var)
     noise = (rng.standard_normal(sig.shape) + 1j * rng.standard_normal(sig.shape)) * math.sqrt(s2)
     data = (sig + noise.astype(np.complex64)).astype(np.complex64)
-    grid = torch.as_tensor(data.reshape(n, img, h + 1), device=device)
+    grid = torch.as_tensor(np.ascontiguousarray(data[:, :G]).reshape(n, img, h + 1), device=device)
     ims = torch.fft.irfft2(grid, s=(img, img))
     ims = torch.fft.fftshift(ims, dim=(-2, -1))
     ims = ims - ims.mean(dim=(-2, -1), keepdim=True)
     ims = ims / ims.std(dim=(-2, -1), keepdim=True)
-    iCol, iRow, _, _ = pixel_index(box, rU, rL)
-    col = (np.where(iRow >= 0, iRow, iRow + img)) * (h + 1) + iCol   # grid index of each pixel
-    return ParticleSet(images=ims.float().contiguous(), dat=np.ascontiguousarray(data[:, col]),
-                       ctf=np.ascontiguousarray(ctf_g[:, col].astype(np.float32)),
-                       sigRcp=np.full((n, len(iCol)), -1.0 / (2.0 * s2), np.float32),
+    if with_data:
+        dat = np.ascontiguousarray(data[:, lik])
+        ctf_k = np.ascontiguousarray(ctf_u[:, lik].astype(np.float32))
+        sigr = np.full((n, len(iCol)), -1.0 / (2.0 * s2), np.float32)
+    else:
+        dat = np.zeros((n, 0), np.complex64)
+        ctf_k = np.zeros((n, 0), np.float32)
+        sigr = np.zeros((n, 0), np.float32)
+    return ParticleSet(images=ims.float().contiguous(), dat=dat, ctf=ctf_k, sigRcp=sigr,
                        iCol=iCol, iRow=iRow, quat_true=q, trans_true=t, cls=cls)
+
+
+def signal_power(maps, box: int, pixel_size: float, rU: float, rL: float, n: int = 64,
+                 seed: int = 0, device="cpu") -> float:
+    """Mean |signal|^2 (CTF applied) over the pixels of cutoff rU of n
+    particles of every map: the noise variance of an SNR defined over the
+    likelihood's pixels is this / snr / 2 per real and imaginary part."""
+    rng = np.random.default_rng(seed)
+    iCol, iRow, _, _ = pixel_index(box, rU, rL)
+    k2 = np.stack([iCol, iRow, np.zeros_like(iCol)], 0).astype(np.float32) / box
+    tot = 0.0
+    for bm in maps:
+        q = haar_quaternions(rng, n)
+        attr = ctf_attrs(rng, n)
+        ctf_k = ctf_values(attr, pixel_size, box, iCol, iRow)
+        f = torch.as_tensor(np.einsum("nij,jk->nki", quat_to_mat(q).astype(np.float32), k2),
+                            device=device)
+        s = blob_ft(bm, f).cpu().numpy() * ctf_k
+        tot += float(np.mean(np.abs(s) ** 2))
+    return tot / len(maps)
 
 
 def global_translations(half: int = 3, step: float = 1.0) -> np.ndarray:
