@@ -350,6 +350,23 @@ int tg3_global_scan_d(tg3_ctx* ctx, int cls, int nImg, int nR, int nT,
                       double* wR, double* wT, double* baseL, float* dvp,
                       int precision);
 
+/* Local phase with a defocus search (Optimiser::updateSP with
+ * SEARCH_TYPE_CTF, src/Optimiser.cpp:1139-1436; the GPU path of
+ * ExpectLocalPreI3D / ExpectLocalM with cSearch, gpu/interface/Interface.h
+ * :107-140): every particle's nR rotations x nT translations x nD defocus
+ * hypotheses, hypothesis d scored with the CTF ctfD [nP][nD][K] (device;
+ * the particle's CTF at defocus scaled by its d-th factor, e.g. from
+ * tg3_ctf_d with defocusU, V x d).  pwD [nP][nD] are the defocus weights of
+ * the particles; outputs as tg3_local_phase_d plus wD [nP][nD], all relative
+ * to each particle's best hypothesis; dvp (may be NULL) [nP][nD][nR][nT].
+ * 1 <= nD <= 16; the split-bf16 path needs nD nT <= 256. */
+int tg3_local_phase_ctf_d(tg3_ctx* ctx, int nP, int nR, int nT, int nD, const float* dat,
+                          const float* ctfD, const float* sigRcp, const double* quat,
+                          const double* trans, const double* pwR, const double* pwT,
+                          const double* pwD, const double* pwC, const int* cls, double* wC,
+                          double* wR, double* wT, double* wD, double* baseL, float* dvp,
+                          int precision);
+
 /* Projection banks (no single counterpart in the reference: the global
  * search's projections, ExpectProject, src/Optimiser.cpp:759-785, kept for
  * reuse).  tg3_ctx_set_bank projects the class-`cls` volume at nB rotations

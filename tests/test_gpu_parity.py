@@ -517,3 +517,59 @@ def test_local_phase_from_bank(small, precision):
                                dev(d["pwC"]), None, *outs, precision)
     finally:
         c.close()
+
+
+@pytest.mark.parametrize("precision", [tg3.SCORE_FP32, tg3.SCORE_BF16X3])
+def test_local_phase_defocus_search(small, precision):
+    """The defocus search of Optimiser::updateSP (SEARCH_TYPE_CTF): every
+    (rotation, translation, defocus) hypothesis scored with the CTF at the
+    particle's defocus scaled by that hypothesis' factor.  The oracle scores
+    each defocus with score_local and merges the results to the particle's
+    best hypothesis, as the running baseline does."""
+    nP, nR, nT, nD = 3, 40, 9, 3
+    d = _local_inputs(small, nP, nR, nT, 9)
+    rng = np.random.default_rng(67)
+    attr = synth.ctf_attrs(rng, nP)
+    factors = np.array([[0.96, 1.0, 1.04], [0.9, 1.0, 1.1], [1.0, 1.02, 0.98]])
+    ctfD = np.empty((nP, nD, d["K"]), np.float32)
+    for k in range(nD):
+        a = attr.copy()
+        a[:, 1] *= factors[:, k]
+        a[:, 2] *= factors[:, k]
+        ctfD[:, k] = synth.ctf_values(a, small["px"], small["box"], small["iCol"],
+                                      small["iRow"]).astype(np.float32)
+    pwD = rng.random((nP, nD)) + 0.5
+    c = tg3.Context(0)
+    try:
+        c.set_volume(0, torch.as_tensor(small["vol32"]).to(DEV), small["pf"])
+        c.set_pixels(small["iCol"], small["iRow"], small["box"])
+        o = dict(wC=torch.empty(nP, dtype=torch.float64, device=DEV),
+                 wR=torch.empty((nP, nR), dtype=torch.float64, device=DEV),
+                 wT=torch.empty((nP, nT), dtype=torch.float64, device=DEV),
+                 wD=torch.empty((nP, nD), dtype=torch.float64, device=DEV),
+                 base=torch.empty(nP, dtype=torch.float64, device=DEV),
+                 dvp=torch.empty((nP, nD, nR, nT), dtype=torch.float32, device=DEV))
+        c.local_phase_ctf(nP, nR, nT, nD, dev(d["dat"]), dev(ctfD), dev(d["sig"]), dev(d["qs"]),
+                          dev(d["ts"]), dev(d["pwR"]), dev(d["pwT"]), dev(pwD), dev(d["pwC"]),
+                          None, o["wC"], o["wR"], o["wT"], o["wD"], o["base"], o["dvp"],
+                          precision)
+        c.sync()
+        g = {k: v.cpu().numpy() for k, v in o.items()}
+    finally:
+        c.close()
+    for l in range(nP):
+        rs = [O.score_local(small["vol"], small["pf"], small["iCol"], small["iRow"], small["box"],
+                            f32(d["dat"][l]), f32(ctfD[l, k]), f32(d["sig"][l]), f32(d["qs"][l]),
+                            f32(d["ts"][l]), d["pwR"][l], d["pwT"][l], 1.0) for k in range(nD)]
+        for k in range(nD):
+            rel = np.abs(g["dvp"][l, k] - rs[k]["dvp"]) / np.abs(rs[k]["dvp"])
+            assert rel.max() < 1e-4, (k, rel.max())
+        base = max(r["base"] for r in rs)
+        assert abs(g["base"][l] - base) / abs(base) < 1e-4
+        e = np.array([np.exp(r["base"] - base) for r in rs])
+        wD = e * np.array([r["wC"] for r in rs])
+        wR = sum(pwD[l, k] * e[k] * rs[k]["wR"] for k in range(nD))
+        wT = sum(pwD[l, k] * e[k] * rs[k]["wT"] for k in range(nD))
+        for got, ref in ((g["wD"][l], wD), (g["wR"][l], wR), (g["wT"][l], wT)):
+            assert np.abs(got / got.sum() - ref / ref.sum()).max() < 2e-3
+        assert np.argmax(g["wD"][l]) == np.argmax(wD)

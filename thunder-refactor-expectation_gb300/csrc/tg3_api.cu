@@ -609,6 +609,107 @@ extern "C" int tg3_local_phase_d(tg3_ctx* c, int nP, int nR, int nT, const float
                        wT, baseL, dvp, precision);
 }
 
+// ========================================================== defocus search
+// The local phase with a defocus axis (Optimiser::updateSP,
+// src/Optimiser.cpp:1139-1436, SEARCH_TYPE_CTF): every (rotation,
+// translation, defocus) hypothesis scored with the particle's CTF for that
+// defocus.  The weights kernel takes (particle, defocus) blocks, each with
+// its own maximum; k_merge_defocus rescales them to the particle's maximum.
+extern "C" int tg3_local_phase_ctf_d(tg3_ctx* c, int nP, int nR, int nT, int nD,
+                                     const float* dat, const float* ctfD, const float* sigRcp,
+                                     const double* quat, const double* trans, const double* pwR,
+                                     const double* pwT, const double* pwD, const double* pwC,
+                                     const int* cls, double* wC, double* wR, double* wT,
+                                     double* wD, double* baseL, float* dvp, int precision)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (nP <= 0 || nR <= 0 || nT <= 0 || nD < 1 || nD > 16)
+        return fail(TG3_ERR_ARG, "bad batch shape (1 <= nD <= 16)");
+    if (!dat || !ctfD || !sigRcp || !quat || !trans || !pwR || !pwT || !pwD || !wC || !wR ||
+        !wT || !wD || !baseL)
+        return fail(TG3_ERR_ARG, "null device pointer");
+    if (precision != TG3_SCORE_FP32 && precision != TG3_SCORE_BF16X3)
+        return fail(TG3_ERR_ARG, "unknown precision");
+    const bool split = precision == TG3_SCORE_BF16X3;
+    if (split && !bf16x3_available())
+        return fail(TG3_ERR_UNSUPPORTED, "split-bf16 tensor-core path unavailable (no TMA encoder)");
+    if (split && nD * nT > 256)
+        return fail(TG3_ERR_UNSUPPORTED, "split-bf16 path needs nD nT <= 256");
+    const int K = c->px.K, Kp = c->px.Kp;
+    const Volume& v0 = c->vol[0];
+    if (!v0.blocks) return fail(TG3_ERR_STATE, "volume of class 0 not set");
+    if ((st = check_geometry(c, v0.vdim, v0.pf))) return st;
+    if ((st = check_weights_shape(nR, nT))) return st;
+    const int nTD = nD * nT;
+    float* P = (float*)ws_get(c, WS_P, sizeof(float) * (size_t)nP * nR * Kp, &st);
+    if (!P) return st;
+    float* A = (float*)ws_get(c, WS_A, sizeof(float) * (size_t)nP * nTD * Kp, &st);
+    if (!A) return st;
+    float* D = (float*)ws_get(c, WS_D, sizeof(float) * (size_t)nP * nR * nTD, &st);
+    if (!D) return st;
+    float* nrm = (float*)ws_get(c, WS_NRM, sizeof(float) * (size_t)nP * nR * nD, &st);
+    if (!nrm) return st;
+    float* pscr = (float*)ws_get(
+        c, WS_PROJ, sizeof(float) * project_scratch_floats(nP * nR, (int)Kp), &st);
+    if (!pscr) return st;
+    double* x0 = (double*)ws_get(c, WS_X0, sizeof(double) * (size_t)nP, &st);
+    if (!x0) return st;
+    // per-block priors, x0 and weights: blocks (l, d)
+    const size_t nB = (size_t)nP * nD;
+    const size_t dbl = nB * ((size_t)nR + nT + 2) * 2 + 2 * nB;
+    double* dw = (double*)ws_get(c, WS_DEFOCUS, sizeof(double) * dbl, &st);
+    if (!dw) return st;
+    double* pRb = dw;
+    double* pTb = pRb + nB * nR;
+    double* pCb = pTb + nB * nT;
+    double* x0b = pCb + nB;
+    double* wRb = x0b + nB;
+    double* wTb = wRb + nB * nR;
+    double* wCb = wTb + nB * nT;
+    double* bb = wCb + nB;
+    cudaStream_t s = c->stream;
+    const long long splitP = split ? (long long)nP * nR * Kp : 0;
+    const long long splitA = split ? (long long)nP * nTD * Kp : 0;
+    {
+        StageTimer tm(c, TG3_STAGE_PROJECT);
+        TG3_CUDA(launch_project(c->d_volTable, cls, nullptr, v0.vdim, v0.pf, quat, nullptr,
+                                nP * nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, nullptr, nullptr,
+                                nullptr, pscr, c->d_flag, splitP, s));
+        TG3_CUDA(launch_norm_defocus(P, splitP, nP, nR, nD, K, Kp, sigRcp, ctfD, nrm, s));
+    }
+    {
+        StageTimer tm(c, TG3_STAGE_SHIFT);
+        TG3_CUDA(launch_shift_bank(reinterpret_cast<const float2*>(dat), ctfD, sigRcp, trans,
+                                   nullptr, nP, nT, c->px.idim, c->px.iCol, c->px.iRow, K, A, Kp,
+                                   splitA, s, nD));
+        TG3_CUDA(launch_x0(reinterpret_cast<const float2*>(dat), sigRcp, nP, K, x0, s));
+    }
+    {
+        StageTimer tm(c, TG3_STAGE_CROSS);
+        if (split)
+            TG3_CUDA(launch_gemm_nt_bf16x3(P, (long long)nR * Kp, Kp, A, (long long)nTD * Kp, Kp,
+                                           nR, nTD, Kp, nP, D, (long long)nR * nTD, nTD, nullptr,
+                                           nR, -2.0f, nullptr, 0, c->d_flag, s));
+        else
+            TG3_CUDA(launch_gemm_nt_fp32(P, (long long)nR * Kp, Kp, A, (long long)nTD * Kp, Kp,
+                                         nR, nTD, Kp, nP, D, (long long)nR * nTD, nTD, nullptr,
+                                         nR, -2.0f, s));
+    }
+    {
+        StageTimer tm(c, TG3_STAGE_WEIGHTS);
+        TG3_CUDA(launch_repeat_rows(pwR, nP, nR, nD, pRb, s));
+        TG3_CUDA(launch_repeat_rows(pwT, nP, nT, nD, pTb, s));
+        TG3_CUDA(launch_repeat_rows(pwC, nP, 1, nD, pCb, s));
+        TG3_CUDA(launch_repeat_rows(x0, nP, 1, nD, x0b, s));
+        TG3_CUDA(launch_weights(D, (long long)nR * nTD, nTD, nR, nT, nD, (int)nB, nrm,
+                                (int)nB, x0b, pRb, nR, pTb, nT, pCb, wCb, wRb, wTb, bb, dvp, s));
+        TG3_CUDA(launch_merge_defocus(nP, nD, nR, nT, wCb, wRb, wTb, bb, pwD, wC, wR, wT, wD,
+                                      baseL, s));
+    }
+    return TG3_OK;
+}
+
 // ================================================================= banks
 // Upload the device views of the banks; a bank built on another pixel set
 // than the active one shows no rows, so an index into it is flagged.

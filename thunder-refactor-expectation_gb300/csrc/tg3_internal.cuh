@@ -83,6 +83,7 @@ enum WsSlot {
     WS_BF16,         // split-bf16 operand planes
     WS_MISC,
     WS_INSERT,       // insertion: per-draw pixel grids and rotations
+    WS_DEFOCUS,      // defocus search: block priors, block weights
     WS_COUNT
 };
 
@@ -219,12 +220,25 @@ cudaError_t launch_project(float4* const* volTable, const int* cls,
 // Either trans [nP][nT][2] or a shared phase bank [nT][K] complex.
 // splitLo != 0: write bf16 hi/lo planes (lo plane splitLo elements after
 // the hi plane at `out`) instead of floats; the same for launch_project.
+// rows (l nD + d) nT + t; ctf [nP][nD][K] (nD = 1: one CTF per particle)
 cudaError_t launch_shift_bank(const float2* dat, const float* ctf,
                               const float* sigRcp, const double* trans,
                               const float2* bank,
                               int nP, int nT, int idim, const int* iCol,
                               const int* iRow, int K, float* out, int ldo,
-                              long long splitLo, cudaStream_t st);
+                              long long splitLo, cudaStream_t st, int nD = 1);
+// Defocus search: norms nrm[r][l][d] of the projected rows for each CTF
+// (ctf [nP][nD][K], nD <= 16), per-block copies of a particle's priors, and
+// the merge of the (particle, defocus) blocks' weights.
+cudaError_t launch_norm_defocus(const float* P, long long splitLo, int nP, int nR, int nD, int K,
+                                int Kp, const float* sigRcp, const float* ctf, float* nrm,
+                                cudaStream_t st);
+cudaError_t launch_repeat_rows(const double* src, int rows, int len, int nRep, double* dst,
+                               cudaStream_t st);
+cudaError_t launch_merge_defocus(int nP, int nD, int nR, int nT, const double* wCb,
+                                 const double* wRb, const double* wTb, const double* baseb,
+                                 const double* pwD, double* wC, double* wR, double* wT,
+                                 double* wD, double* base, cudaStream_t st);
 cudaError_t launch_x0(const float2* dat, const float* sigRcp, int nP, int K,
                       double* x0, cudaStream_t st);
 // C[b][i][j] = alpha * sum_k A[b][i][k] B[b][j][k] + nrm[b][i]   (FP32).

@@ -395,31 +395,35 @@ __global__ void k_norm_reduce(const float* __restrict__ nrmPart, int rows, int n
     }
 }
 
-// Shifted, weighted data A''[l][t][p] = sigRcp ctf X exp(+2 pi i (iCol tx +
-// iRow ty) / N), the conjugate of sigRcp ctf conj(X) S_t, so that
-// Re sum_p sigRcp ctf conj(X) S_t P = sum over the 2K floats of A'' . P.
+// Shifted, weighted data A''[l][d][t][p] = sigRcp ctf_d X exp(+2 pi i (iCol tx
+// + iRow ty) / N), the conjugate of sigRcp ctf_d conj(X) S_t, so that
+// Re sum_p sigRcp ctf_d conj(X) S_t P = sum over the 2K floats of A'' . P.
+// nD CTFs per particle (ctf [nP][nD][K]; one without a defocus search).
 __global__ void k_shift_bank(const float2* __restrict__ dat, const float* __restrict__ ctf,
                              const float* __restrict__ sigRcp,
                              const double* __restrict__ trans, const float2* __restrict__ bank,
-                             int nT, int idim,
+                             int nT, int nD, int idim,
                              const int* __restrict__ iCol, const int* __restrict__ iRow,
                              int K, float* __restrict__ out, int ldo, long long splitLo)
 {
-    const int lt = blockIdx.x;            // l * nT + t
-    const int l = lt / nT;
-    const float tx = bank ? 0.f : (float)trans[2 * (size_t)lt];
-    const float ty = bank ? 0.f : (float)trans[2 * (size_t)lt + 1];
+    const int row = blockIdx.x;           // (l nD + d) nT + t
+    const int t = row % nT;
+    const int ld = row / nT;              // l nD + d
+    const int l = ld / nD;
+    const size_t lt = (size_t)l * nT + t;
+    const float tx = bank ? 0.f : (float)trans[2 * lt];
+    const float ty = bank ? 0.f : (float)trans[2 * lt + 1];
     const float invN = 1.0f / (float)idim;
     for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x) {
         float2 v = make_float2(0.f, 0.f);
         if (p < K) {
             const size_t i = (size_t)l * K + p;
-            const float sc = sigRcp[i] * ctf[i];
+            const float sc = sigRcp[i] * ctf[(size_t)ld * K + p];
             const float2 X = dat[i];
             float s, c;
             if (bank) {
                 // shared phase bank S[t][p] = (cos, -sin): use conj(S)
-                const float2 S = bank[(size_t)(lt % nT) * K + p];
+                const float2 S = bank[(size_t)t * K + p];
                 c = S.x;
                 s = -S.y;
             } else {
@@ -428,7 +432,110 @@ __global__ void k_shift_bank(const float2* __restrict__ dat, const float* __rest
             }
             v = make_float2(sc * (X.x * c - X.y * s), sc * (X.x * s + X.y * c));
         }
-        store_pair(out, splitLo, lt, ldo, p, v.x, v.y);
+        store_pair(out, splitLo, row, ldo, p, v.x, v.y);
+    }
+}
+
+// Defocus search: the norm sum_p sigRcp ctf_d^2 |P|^2 of every projected row
+// for each of the particle's nD CTFs, nrm[r][l][d] (the layout the weights
+// kernel reads per (row, block)).  CTA: (particle, 8 rows), a warp per row,
+// |P|^2 from the FP32 row or from the split planes (hi + lo).
+constexpr int kMaxDefocus = 16;
+
+__global__ void __launch_bounds__(256)
+k_norm_defocus(const float* __restrict__ P, long long splitLo, int nP, int nR, int nD, int K,
+               int Kp, const float* __restrict__ sigRcp, const float* __restrict__ ctf,
+               float* __restrict__ nrm)
+{
+    const int l = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blockIdx.y * 8 + warp;
+    if (r >= nR) return;
+    const size_t row = (size_t)l * nR + r;
+    float acc[kMaxDefocus];
+#pragma unroll
+    for (int d = 0; d < kMaxDefocus; d++) acc[d] = 0.f;
+    const __nv_bfloat162* hi = reinterpret_cast<const __nv_bfloat162*>(P);
+    for (int p = lane; p < K; p += 32) {
+        float re, im;
+        if (splitLo == 0) {
+            const float2 v = reinterpret_cast<const float2*>(P + row * Kp)[p];
+            re = v.x;
+            im = v.y;
+        } else {
+            const float2 h = __bfloat1622float2(hi[(row * Kp) / 2 + p]);
+            const float2 o = __bfloat1622float2(hi[(splitLo + row * Kp) / 2 + p]);
+            re = h.x + o.x;
+            im = h.y + o.y;
+        }
+        const float a2 = sigRcp[(size_t)l * K + p] * (re * re + im * im);
+#pragma unroll
+        for (int d = 0; d < kMaxDefocus; d++) {
+            if (d < nD) {
+                const float c = ctf[((size_t)l * nD + d) * K + p];
+                acc[d] = fmaf(a2, c * c, acc[d]);
+            }
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < kMaxDefocus; d++) {
+        if (d >= nD) break;
+        float v = acc[d];
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) nrm[((size_t)r * nP + l) * nD + d] = v;
+    }
+}
+
+// dst[(row nRep + k) len + j] = src[row len + j] (per-block copies of a
+// particle's priors for the weights kernel's (particle, defocus) blocks)
+__global__ void k_repeat_rows(const double* __restrict__ src, int rows, int len, int nRep,
+                              double* __restrict__ dst)
+{
+    const size_t n = (size_t)rows * nRep * len;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t j = i % len, rk = i / len;
+        dst[i] = src ? src[(rk / nRep) * len + j] : 1.0;
+    }
+}
+
+// Merge of a particle's nD (particle, defocus) blocks, each relative to its
+// own maximum, into the particle's weights relative to the overall maximum
+// (the running baseline of Optimiser::updateSP, src/Optimiser.cpp:1326-1347,
+// with its defocus axis): wD[d] = e_d wC_d, wC = sum_d pD[d] e_d wC_d,
+// wR / wT = sum_d pD[d] e_d wR_d / wT_d, e_d = exp(base_d - base).
+__global__ void k_merge_defocus(int nD, int nR, int nT, const double* __restrict__ wCb,
+                                const double* __restrict__ wRb, const double* __restrict__ wTb,
+                                const double* __restrict__ baseb, const double* __restrict__ pwD,
+                                double* __restrict__ wC, double* __restrict__ wR,
+                                double* __restrict__ wT, double* __restrict__ wD,
+                                double* __restrict__ base)
+{
+    __shared__ double e[kMaxDefocus], pd[kMaxDefocus];
+    const int l = blockIdx.x;
+    if (threadIdx.x == 0) {
+        double m = baseb[(size_t)l * nD];
+        for (int d = 1; d < nD; d++) m = fmax(m, baseb[(size_t)l * nD + d]);
+        double c = 0.0;
+        for (int d = 0; d < nD; d++) {
+            e[d] = exp(baseb[(size_t)l * nD + d] - m);
+            pd[d] = pwD[(size_t)l * nD + d];
+            wD[(size_t)l * nD + d] = e[d] * wCb[(size_t)l * nD + d];
+            c += pd[d] * wD[(size_t)l * nD + d];
+        }
+        wC[l] = c;
+        base[l] = m;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < nR; r += blockDim.x) {
+        double s = 0.0;
+        for (int d = 0; d < nD; d++) s += pd[d] * e[d] * wRb[((size_t)l * nD + d) * nR + r];
+        wR[(size_t)l * nR + r] = s;
+    }
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
+        double s = 0.0;
+        for (int d = 0; d < nD; d++) s += pd[d] * e[d] * wTb[((size_t)l * nD + d) * nT + t];
+        wT[(size_t)l * nT + t] = s;
     }
 }
 
@@ -1467,11 +1574,41 @@ cudaError_t launch_project(float4* const* volTable, const int* cls, const float4
 cudaError_t launch_shift_bank(const float2* dat, const float* ctf, const float* sigRcp,
                               const double* trans, const float2* bank, int nP, int nT,
                               int idim, const int* iCol, const int* iRow, int K, float* out,
-                              int ldo, long long splitLo, cudaStream_t st)
+                              int ldo, long long splitLo, cudaStream_t st, int nD)
 {
-    dim3 grid(nP * nT);
-    k_shift_bank<<<grid, 256, 0, st>>>(dat, ctf, sigRcp, trans, bank, nT, idim, iCol, iRow,
+    if (nD < 1) return cudaErrorInvalidValue;
+    dim3 grid(nP * nD * nT);
+    k_shift_bank<<<grid, 256, 0, st>>>(dat, ctf, sigRcp, trans, bank, nT, nD, idim, iCol, iRow,
                                         K, out, ldo, splitLo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_norm_defocus(const float* P, long long splitLo, int nP, int nR, int nD, int K,
+                                int Kp, const float* sigRcp, const float* ctf, float* nrm,
+                                cudaStream_t st)
+{
+    if (nD < 1 || nD > kMaxDefocus) return cudaErrorInvalidValue;
+    k_norm_defocus<<<dim3(nP, (nR + 7) / 8), 256, 0, st>>>(P, splitLo, nP, nR, nD, K, Kp, sigRcp,
+                                                           ctf, nrm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_repeat_rows(const double* src, int rows, int len, int nRep, double* dst,
+                               cudaStream_t st)
+{
+    k_repeat_rows<<<grid_for((size_t)rows * nRep * len, 256), 256, 0, st>>>(src, rows, len, nRep,
+                                                                          dst);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_merge_defocus(int nP, int nD, int nR, int nT, const double* wCb,
+                                 const double* wRb, const double* wTb, const double* baseb,
+                                 const double* pwD, double* wC, double* wR, double* wT,
+                                 double* wD, double* base, cudaStream_t st)
+{
+    if (nD < 1 || nD > kMaxDefocus) return cudaErrorInvalidValue;
+    k_merge_defocus<<<nP, 256, 0, st>>>(nD, nR, nT, wCb, wRb, wTb, baseb, pwD, wC, wR, wT, wD,
+                                        base);
     return cudaGetLastError();
 }
 

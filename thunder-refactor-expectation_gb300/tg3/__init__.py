@@ -35,7 +35,7 @@ EXPORTS = [
     "tg3_cnn_params", "tg3_cnn_grads", "tg3_cnn_set_bf16", "tg3_cnn_forward", "tg3_cnn_loss",
     "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose", "tg3_cnn_backward", "tg3_cnn_infer",
     "tg3_cnn_contrastive", "tg3_cnn_embed", "tg3_cnn_match_propose", "tg3_ctx_set_bank",
-    "tg3_local_phase_bank_d",
+    "tg3_local_phase_bank_d", "tg3_local_phase_ctf_d",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
@@ -123,6 +123,7 @@ def lib():
             "tg3_cnn_match_propose": ([_P, _I, _P, _I, _P, _I, _I, ctypes.c_ulonglong, _P, _P,
                                        _P, _P], _I),
             "tg3_ctx_set_bank": ([_P, _I, _P, _I], _I),
+            "tg3_local_phase_ctf_d": ([_P, _I, _I, _I, _I] + [_P] * 16 + [_I], _I),
             "tg3_local_phase_bank_d": ([_P, _I, _I, _I] + [_P] * 14 + [_I], _I),
             "tg3_ctx_stage_times": ([_P, _P, _P, _I], _I),
             "tg3_noalloc_scratch_bytes": ([], ctypes.c_size_t),
@@ -229,6 +230,15 @@ class Context:
                                       ptr(quat), ptr(trans), ptr(pwR), ptr(pwT), ptr(pwC),
                                       ptr(cls), ptr(wC), ptr(wR), ptr(wT), ptr(base), ptr(dvp),
                                       precision))
+
+    def local_phase_ctf(self, nP, nR, nT, nD, dat, ctfD, sig, quat, trans, pwR, pwT, pwD, pwC,
+                        cls, wC, wR, wT, wD, base, dvp=None, precision=SCORE_FP32):
+        """Local phase with nD defocus hypotheses per particle (ctfD [nP][nD][K])."""
+        self._hold(dat, ctfD, sig, quat, trans, pwR, pwT, pwD, pwC, cls, wC, wR, wT, wD, base, dvp)
+        check(lib().tg3_local_phase_ctf_d(self.h, nP, nR, nT, nD, ptr(dat), ptr(ctfD), ptr(sig),
+                                          ptr(quat), ptr(trans), ptr(pwR), ptr(pwT), ptr(pwD),
+                                          ptr(pwC), ptr(cls), ptr(wC), ptr(wR), ptr(wT), ptr(wD),
+                                          ptr(base), ptr(dvp), precision))
 
     def set_bank(self, cls: int, quat, nB: int):
         """Project class `cls` at nB rotations (quat [nB][4] float64, device)
