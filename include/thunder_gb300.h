@@ -138,6 +138,21 @@ int tg3_ExpectLocal3D(tg3_volume* vol, const float* dat, const float* ctf,
                       const double* trans, int nT, const double* oldR,
                       const double* oldT, double oldC, float* wC, float* wR,
                       float* wT, float* dvp, float* baseL);
+/* The same with the defocus search (cSearch; ExpectLocalP / RTD / PreI3D /
+ * M of gpu/interface/Interface.h:50-139 with k1 != 0): the particle's CTF
+ * for each of its nD defocus factors dpara is made on the device from its
+ * per-pixel defocus defO and frequency freQ, k1, k2, phaseShift and the
+ * amplitude contrast conT (kernel_CalCTFL, gpu/src/Kernel.cu:481-512);
+ * oldD are the particle's defocus weights; wD [nD] the marginal defocus
+ * weights; dvp (may be NULL) [nD][nR][nT].  1 <= nD <= 16. */
+int tg3_ExpectLocal3D_ctf(tg3_volume* vol, const float* dat, const float* defO,
+                          const float* freQ, float k1, float k2, float phaseShift,
+                          float conT, const float* sigRcp, const int* iCol,
+                          const int* iRow, int npxl, int idim, const double* rot,
+                          int nR, const double* trans, int nT, const double* dpara,
+                          int nD, const double* oldR, const double* oldT,
+                          const double* oldD, double oldC, float* wC, float* wR,
+                          float* wT, float* wD, float* dvp, float* baseL);
 
 /* Particle-filter narrowing + systematic resampling of one axis of nP
  * particles, Particle::keepHalfHeightPeak + Particle::resample(n, pt)

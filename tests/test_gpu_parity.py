@@ -573,3 +573,67 @@ def test_local_phase_defocus_search(small, precision):
         for got, ref in ((g["wD"][l], wD), (g["wR"][l], wR), (g["wT"][l], wT)):
             assert np.abs(got / got.sum() - ref / ref.sum()).max() < 2e-3
         assert np.argmax(g["wD"][l]) == np.argmax(wD)
+
+
+def test_expect_local3d_defocus_host(small):
+    """The reference-shaped defocus search (ExpectLocalP / RTD / PreI3D / M
+    with k1 != 0): CTFs made on the device from the per-pixel defocus and
+    frequency (kernel_CalCTFL's formula) for each defocus factor."""
+    st = small["st"]
+    nR, nT, nD = 48, 9, 3
+    d = _local_inputs(small, 1, nR, nT, 37)
+    rng = np.random.default_rng(71)
+    attr = synth.ctf_attrs(rng, 1)[0]
+    V, dU, dV, th, Cs, A, ps = attr
+    lam = 12.2643247 / np.sqrt(V * (1 + V * 0.978466e-6))
+    k1, k2 = np.pi * lam, (np.pi / 2) * Cs * lam ** 3
+    iCol, iRow = small["iCol"], small["iRow"]
+    freq = np.hypot(iCol, iRow) / (small["px"] * small["box"])
+    ang = np.arctan2(iRow, iCol) - th
+    defO = -(dU + dV + (dU - dV) * np.cos(2 * ang)) / 2
+    dpara = np.array([0.95, 1.0, 1.05])
+    pwD = np.array([0.2, 0.5, 0.3])
+    vol = np.ascontiguousarray(small["vol32"])
+    h = tg3.ctypes.c_void_p()
+    tg3.check(tg3.lib().tg3_volume_create(tg3.ctypes.byref(h), tg3.ptr(vol), vol.shape[0],
+                                          small["pf"]))
+    try:
+        wC = np.zeros(1, np.float32)
+        wR = np.zeros(nR, np.float32)
+        wT = np.zeros(nT, np.float32)
+        wD = np.zeros(nD, np.float32)
+        dvp = np.zeros((nD, nR, nT), np.float32)
+        bl = np.zeros(1, np.float32)
+        # every array the call reads is held here: a temporary passed by
+        # address would be freed before the call
+        c = lambda x, dt: np.ascontiguousarray(x, dtype=dt)
+        q, t = c(d["qs"][0], np.float64), c(d["ts"][0], np.float64)
+        dat, sig = c(d["dat"][0], np.complex64), c(d["sig"][0], np.float32)
+        dO, fq = c(defO, np.float32), c(freq, np.float32)
+        ic, ir = c(iCol, np.int32), c(iRow, np.int32)
+        dp, pr, pt, pd = (c(dpara, np.float64), c(d["pwR"][0], np.float64),
+                          c(d["pwT"][0], np.float64), c(pwD, np.float64))
+        tg3.check(tg3.lib().tg3_ExpectLocal3D_ctf(
+            h, tg3.ptr(dat), tg3.ptr(dO), tg3.ptr(fq), k1, k2, ps, A, tg3.ptr(sig), tg3.ptr(ic),
+            tg3.ptr(ir), st.K, small["box"], tg3.ptr(q), nR, tg3.ptr(t), nT, tg3.ptr(dp), nD,
+            tg3.ptr(pr), tg3.ptr(pt), tg3.ptr(pd), 1.0, tg3.ptr(wC), tg3.ptr(wR), tg3.ptr(wT),
+            tg3.ptr(wD), tg3.ptr(dvp), tg3.ptr(bl)))
+    finally:
+        tg3.lib().tg3_volume_destroy(h)
+    rs = []
+    for k in range(nD):
+        a = attr.copy()
+        a[1] *= dpara[k]
+        a[2] *= dpara[k]
+        ctf_k = synth.ctf_values(a[None], small["px"], small["box"], iCol, iRow)[0]
+        rs.append(O.score_local(small["vol"], small["pf"], iCol, iRow, small["box"],
+                                f32(d["dat"][0]), f32(ctf_k), f32(d["sig"][0]), f32(q), f32(t),
+                                d["pwR"][0], d["pwT"][0], 1.0))
+    for k in range(nD):
+        assert (np.abs(dvp[k] - rs[k]["dvp"]) / np.abs(rs[k]["dvp"])).max() < 1e-4
+    base = max(r["base"] for r in rs)
+    e = np.array([np.exp(r["base"] - base) for r in rs])
+    wD_ref = e * np.array([r["wC"] for r in rs])
+    wR_ref = sum(pwD[k] * e[k] * rs[k]["wR"] for k in range(nD))
+    np.testing.assert_allclose(wD / wD.sum(), wD_ref / wD_ref.sum(), atol=2e-3)
+    np.testing.assert_allclose(wR / wR.sum(), wR_ref / wR_ref.sum(), atol=2e-3)

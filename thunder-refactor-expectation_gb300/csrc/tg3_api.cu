@@ -615,15 +615,14 @@ extern "C" int tg3_local_phase_d(tg3_ctx* c, int nP, int nR, int nT, const float
 // translation, defocus) hypothesis scored with the particle's CTF for that
 // defocus.  The weights kernel takes (particle, defocus) blocks, each with
 // its own maximum; k_merge_defocus rescales them to the particle's maximum.
-extern "C" int tg3_local_phase_ctf_d(tg3_ctx* c, int nP, int nR, int nT, int nD,
-                                     const float* dat, const float* ctfD, const float* sigRcp,
-                                     const double* quat, const double* trans, const double* pwR,
-                                     const double* pwT, const double* pwD, const double* pwC,
-                                     const int* cls, double* wC, double* wR, double* wT,
-                                     double* wD, double* baseL, float* dvp, int precision)
+static int local_phase_ctf(tg3_ctx* c, int nP, int nR, int nT, int nD, const float* dat,
+                           const float* ctfD, const float* sigRcp, const double* quat,
+                           const double* trans, const double* pwR, const double* pwT,
+                           const double* pwD, const double* pwC, const int* cls, double* wC,
+                           double* wR, double* wT, double* wD, double* baseL, float* dvp,
+                           int precision)
 {
-    int st = check_ctx(c);
-    if (st) return st;
+    int st = TG3_OK;
     if (nP <= 0 || nR <= 0 || nT <= 0 || nD < 1 || nD > 16)
         return fail(TG3_ERR_ARG, "bad batch shape (1 <= nD <= 16)");
     if (!dat || !ctfD || !sigRcp || !quat || !trans || !pwR || !pwT || !pwD || !wC || !wR ||
@@ -708,6 +707,19 @@ extern "C" int tg3_local_phase_ctf_d(tg3_ctx* c, int nP, int nR, int nT, int nD,
                                       baseL, s));
     }
     return TG3_OK;
+}
+
+extern "C" int tg3_local_phase_ctf_d(tg3_ctx* c, int nP, int nR, int nT, int nD,
+                                     const float* dat, const float* ctfD, const float* sigRcp,
+                                     const double* quat, const double* trans, const double* pwR,
+                                     const double* pwT, const double* pwD, const double* pwC,
+                                     const int* cls, double* wC, double* wR, double* wT,
+                                     double* wD, double* baseL, float* dvp, int precision)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    return local_phase_ctf(c, nP, nR, nT, nD, dat, ctfD, sigRcp, quat, trans, pwR, pwT, pwD, pwC,
+                           cls, wC, wR, wT, wD, baseL, dvp, precision);
 }
 
 // ================================================================= banks
@@ -1348,6 +1360,77 @@ extern "C" int tg3_ExpectLocal3D(tg3_volume* h, const float* dat, const float* c
     if ((st = sync_and_check(c))) return st;
     for (int r = 0; r < nR; r++) wR[r] = (float)hwr[r];
     for (int t = 0; t < nT; t++) wT[t] = (float)hwt[t];
+    *wC = (float)hwc;
+    *baseL = (float)hbl;
+    return TG3_OK;
+}
+
+// The defocus-search form of tg3_ExpectLocal3D: the particle's CTF for each
+// defocus factor dpara[d] from its per-pixel defocus defO and frequency freQ
+// (kernel_CalCTFL), then the local phase over rotation x translation x
+// defocus; wD[d] as wR / wT.
+extern "C" int tg3_ExpectLocal3D_ctf(tg3_volume* h, const float* dat, const float* defO,
+                                     const float* freQ, float k1, float k2, float phaseShift,
+                                     float conT, const float* sigRcp, const int* iCol,
+                                     const int* iRow, int npxl, int idim, const double* rot,
+                                     int nR, const double* trans, int nT, const double* dpara,
+                                     int nD, const double* oldR, const double* oldT,
+                                     const double* oldD, double oldC, float* wC, float* wR,
+                                     float* wT, float* wD, float* dvp, float* baseL)
+{
+    if (!h || !h->ctx) return fail(TG3_ERR_ARG, "null volume handle");
+    if (!dat || !defO || !freQ || !sigRcp || !iCol || !iRow || !rot || !trans || !dpara ||
+        !oldR || !oldT || !oldD || !wC || !wR || !wT || !wD || !baseL || npxl <= 0 || nR <= 0 ||
+        nT <= 0 || nD < 1 || nD > 16)
+        return fail(TG3_ERR_ARG, "bad ExpectLocal3D_ctf args");
+    tg3_ctx* c = h->ctx;
+    int st = check_ctx(c);
+    if (st) return st;
+    if (c->px.K != npxl || c->px.idim != idim) {
+        if ((st = tg3_ctx_set_pixels(c, iCol, iRow, npxl, idim))) return st;
+    }
+    cudaStream_t s = c->stream;
+    const size_t K = npxl, R_ = nR, T_ = nT, D_ = nD;
+    Arena ar(c, WS_H2D);
+    size_t od = ar.add(8 * K), odo = ar.add(4 * K), ofq = ar.add(4 * K), os = ar.add(4 * K),
+           octf = ar.add(4 * K * D_), oq = ar.add(32 * R_), ot = ar.add(16 * T_),
+           odp = ar.add(8 * D_), opr = ar.add(8 * R_), opt = ar.add(8 * T_), opd = ar.add(8 * D_),
+           opc = ar.add(8), owc = ar.add(8), owr = ar.add(8 * R_), owt = ar.add(8 * T_),
+           owd = ar.add(8 * D_), obl = ar.add(8), odv = ar.add(dvp ? 4 * D_ * R_ * T_ : 0);
+    char* b = (char*)ws_get(c, WS_H2D, ar.used, &st);
+    if (!b) return st;
+    TG3_CUDA(cudaMemcpyAsync(b + od, dat, 8 * K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + odo, defO, 4 * K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + ofq, freQ, 4 * K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + os, sigRcp, 4 * K, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + oq, rot, 32 * R_, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + ot, trans, 16 * T_, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + odp, dpara, 8 * D_, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opr, oldR, 8 * R_, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opt, oldT, 8 * T_, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opd, oldD, 8 * D_, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opc, &oldC, 8, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(launch_ctf_defocus((float*)(b + odo), (float*)(b + ofq), (double*)(b + odp), nD,
+                                npxl, k1, k2, phaseShift, conT, (float*)(b + octf), s));
+    st = local_phase_ctf(c, 1, nR, nT, nD, (float*)(b + od), (float*)(b + octf), (float*)(b + os),
+                         (double*)(b + oq), (double*)(b + ot), (double*)(b + opr),
+                         (double*)(b + opt), (double*)(b + opd), (double*)(b + opc), nullptr,
+                         (double*)(b + owc), (double*)(b + owr), (double*)(b + owt),
+                         (double*)(b + owd), (double*)(b + obl), dvp ? (float*)(b + odv) : nullptr,
+                         TG3_SCORE_FP32);
+    if (st) return st;
+    std::vector<double> hwr(R_), hwt(T_), hwd(D_);
+    double hwc = 0, hbl = 0;
+    TG3_CUDA(cudaMemcpyAsync(hwr.data(), b + owr, 8 * R_, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(hwt.data(), b + owt, 8 * T_, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(hwd.data(), b + owd, 8 * D_, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(&hwc, b + owc, 8, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(&hbl, b + obl, 8, cudaMemcpyDeviceToHost, s));
+    if (dvp) TG3_CUDA(cudaMemcpyAsync(dvp, b + odv, 4 * D_ * R_ * T_, cudaMemcpyDeviceToHost, s));
+    if ((st = sync_and_check(c))) return st;
+    for (int r = 0; r < nR; r++) wR[r] = (float)hwr[r];
+    for (int t = 0; t < nT; t++) wT[t] = (float)hwt[t];
+    for (int d = 0; d < nD; d++) wD[d] = (float)hwd[d];
     *wC = (float)hwc;
     *baseL = (float)hbl;
     return TG3_OK;

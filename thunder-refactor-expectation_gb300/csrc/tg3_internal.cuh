@@ -235,6 +235,11 @@ cudaError_t launch_norm_defocus(const float* P, long long splitLo, int nP, int n
                                 cudaStream_t st);
 cudaError_t launch_repeat_rows(const double* src, int rows, int len, int nRep, double* dst,
                                cudaStream_t st);
+// one particle's CTFs at defocus factors dpara [nD] from per-pixel defocus
+// defO and frequency freQ: ctf [nD][K]
+cudaError_t launch_ctf_defocus(const float* defO, const float* freQ, const double* dpara, int nD,
+                               int K, double k1, double k2, double phaseShift, double conT,
+                               float* ctf, cudaStream_t st);
 cudaError_t launch_merge_defocus(int nP, int nD, int nR, int nT, const double* wCb,
                                  const double* wRb, const double* wTb, const double* baseb,
                                  const double* pwD, double* wC, double* wR, double* wT,

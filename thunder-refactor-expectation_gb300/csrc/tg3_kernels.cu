@@ -486,6 +486,23 @@ k_norm_defocus(const float* __restrict__ P, long long splitLo, int nP, int nR, i
     }
 }
 
+// CTF of one particle for each defocus factor d (kernel_CalCTFL of the
+// reference GPU path; the CTF of Optimiser::updateSP, src/Optimiser.cpp:
+// 1196-1214): ki = k1 defO[p] d f[p]^2 + k2 f[p]^4 - phaseShift,
+// ctf = -sqrt(1 - conT^2) sin ki + conT cos ki, in FP64; ctf [nD][K].
+__global__ void k_ctf_defocus(const float* __restrict__ defO, const float* __restrict__ freQ,
+                              const double* __restrict__ dpara, int K, double k1, double k2,
+                              double phaseShift, double conT, float* __restrict__ ctf)
+{
+    const int d = blockIdx.y;
+    const double w1 = sqrt(1.0 - conT * conT);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K; p += gridDim.x * blockDim.x) {
+        const double f2 = (double)freQ[p] * freQ[p];
+        const double ki = k1 * defO[p] * dpara[d] * f2 + k2 * f2 * f2 - phaseShift;
+        ctf[(size_t)d * K + p] = (float)(-w1 * sin(ki) + conT * cos(ki));
+    }
+}
+
 // dst[(row nRep + k) len + j] = src[row len + j] (per-block copies of a
 // particle's priors for the weights kernel's (particle, defocus) blocks)
 __global__ void k_repeat_rows(const double* __restrict__ src, int rows, int len, int nRep,
@@ -1590,6 +1607,15 @@ cudaError_t launch_norm_defocus(const float* P, long long splitLo, int nP, int n
     if (nD < 1 || nD > kMaxDefocus) return cudaErrorInvalidValue;
     k_norm_defocus<<<dim3(nP, (nR + 7) / 8), 256, 0, st>>>(P, splitLo, nP, nR, nD, K, Kp, sigRcp,
                                                            ctf, nrm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ctf_defocus(const float* defO, const float* freQ, const double* dpara, int nD,
+                               int K, double k1, double k2, double phaseShift, double conT,
+                               float* ctf, cudaStream_t st)
+{
+    k_ctf_defocus<<<dim3((K + 255) / 256, nD), 256, 0, st>>>(defO, freQ, dpara, K, k1, k2,
+                                                            phaseShift, conT, ctf);
     return cudaGetLastError();
 }
 

@@ -71,12 +71,15 @@ std::map<ManagedArrayTexture*, VolState> g_vols;
 
 // ExpectLocalRTD / PreI3D: the hypothesis set behind a ManagedCalPoint.
 struct CalState {
-    std::vector<double> rot, trans, oldR, oldT;
-    int nR = 0, nT = 0;
+    std::vector<double> rot, trans, oldR, oldT, dpara, oldD;
+    int nR = 0, nT = 0, nD = 0;
     ManagedArrayTexture* mgr = nullptr;
     int idim = 0, npxl = 0;
     const int* iCol = nullptr;
     const int* iRow = nullptr;
+    // defocus search (ExpectLocalPreI3D with k1 != 0)
+    float k1 = 0, k2 = 0, phaseShift = 0, conT = 0;
+    const RFLOAT* freQ = nullptr;
 };
 std::map<ManagedCalPoint*, CalState> g_cal;
 
@@ -205,17 +208,23 @@ void ExpectLocalRTD(int gpuIdx, ManagedCalPoint* mcp, double* oldR, double* oldT
                     double* trans, double* rot, double* dpara)
 {
     (void)gpuIdx;
-    (void)oldD;
-    (void)dpara;
     std::lock_guard<std::mutex> lk(g_mu);
     CalState& c = g_cal[mcp];
-    // the hypothesis counts are those of ManagedCalPoint::Init (getNR/getNT)
+    // the hypothesis counts are those of ManagedCalPoint::Init (getNR/getNT/getMD)
     c.nR = mcp->getNR();
     c.nT = mcp->getNT();
+    c.nD = mcp->getMD();
     c.rot.assign(rot, rot + 4 * c.nR);
     c.trans.assign(trans, trans + 2 * c.nT);
     c.oldR.assign(oldR, oldR + c.nR);
     c.oldT.assign(oldT, oldT + c.nT);
+    if (c.nD > 0 && dpara && oldD) {
+        c.dpara.assign(dpara, dpara + c.nD);
+        c.oldD.assign(oldD, oldD + c.nD);
+    } else {
+        c.dpara.clear();
+        c.oldD.clear();
+    }
 }
 
 // gpu/interface/Interface.h:107-123: bind the volume and geometry; the
@@ -227,11 +236,7 @@ void ExpectLocalPreI3D(int gpuIdx, int datShift, ManagedArrayTexture* mgr, Manag
 {
     (void)gpuIdx;
     (void)datShift;
-    (void)devdefO;
-    (void)devfreQ;
-    (void)phaseShift;
-    (void)conT;
-    if (k1 != 0 || k2 != 0) die("ExpectLocalPreI3D: defocus search", TG3_ERR_UNSUPPORTED);
+    (void)devdefO;    // the slot's defocus offsets are read in ExpectLocalM
     if (interp != 1) die("ExpectLocalPreI3D: interpolation", TG3_ERR_UNSUPPORTED);
     const PixelList* px = pixels_of(deviCol);
     (void)deviRow;
@@ -251,6 +256,12 @@ void ExpectLocalPreI3D(int gpuIdx, int datShift, ManagedArrayTexture* mgr, Manag
     c.npxl = npxl;
     c.iCol = px->iCol.data();
     c.iRow = px->iRow.data();
+    // k1 = k2 = 0 outside the defocus search (src/Optimiser.cpp:2511-2550)
+    c.k1 = k1;
+    c.k2 = k2;
+    c.phaseShift = phaseShift;
+    c.conT = conT;
+    c.freQ = devfreQ;     // ExpectPrefre's copy of the frequencies
 }
 
 // gpu/interface/Interface.h:125-139: project, shift, score and return the
@@ -273,6 +284,18 @@ void ExpectLocalM(int gpuIdx, int datShift, ManagedCalPoint* mcp, Complex* devda
     if (!h || c.npxl != npxl) die("ExpectLocalM: call order", TG3_ERR_STATE);
     const size_t off = (size_t)datShift * npxl;
     float baseL = 0;
+    if (c.k1 != 0 || c.k2 != 0) {
+        // defocus search: the slot holds the particle's defocus offsets
+        if (c.nD < 1 || (int)c.dpara.size() != c.nD || !c.freQ || s->def.empty())
+            die("ExpectLocalM: defocus search state", TG3_ERR_STATE);
+        ok("ExpectLocalM",
+           tg3_ExpectLocal3D_ctf(h, reinterpret_cast<const float*>(&s->dat[off]), &s->def[off],
+                                 c.freQ, c.k1, c.k2, c.phaseShift, c.conT, &s->sig[off], c.iCol,
+                                 c.iRow, npxl, c.idim, c.rot.data(), c.nR, c.trans.data(), c.nT,
+                                 c.dpara.data(), c.nD, c.oldR.data(), c.oldT.data(),
+                                 c.oldD.data(), oldC, wC, wR, wT, wD, nullptr, &baseL));
+        return;
+    }
     ok("ExpectLocalM",
        tg3_ExpectLocal3D(h, reinterpret_cast<const float*>(&s->dat[off]), &s->ctf[off],
                          &s->sig[off], c.iCol, c.iRow, npxl, c.idim, c.rot.data(), c.nR,
