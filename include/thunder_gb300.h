@@ -111,8 +111,11 @@ int tg3_ExpectGlobal3D(const float* rotP, const float* traP, const float* datP,
  * accumulated into (not cleared).  Note: dimSize here is the volume edge;
  * the reference's InsertFT passes the voxel count in its dimSize and the
  * edge (F3D.nSlcFT()) to its back end.
- * ctfaData, nD and cSearch are accepted for signature parity; cSearch must
- * be false.  kernel is TG3_KERNEL_*. */
+ * With cSearch the CTF of every draw is made on the device from the
+ * image's CTFAttr (ctfaData [imgNum][7] floats, CTFAttr field order) with
+ * defocusU, V scaled by the draw's factor nD [imgNum][mReco] at pixelSize
+ * (kernel_CalculateCTF, gpu/src/Kernel.cu:2132-2198) and ctfP is not read;
+ * without it ctfP [imgNum][npxl] is.  kernel is TG3_KERNEL_*. */
 int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter,
                  const float* datP, const float* ctfP, const float* sigRcpP,
                  const float* ctfaData, const double* offS, const float* w,

@@ -637,3 +637,54 @@ def test_expect_local3d_defocus_host(small):
     wR_ref = sum(pwD[k] * e[k] * rs[k]["wR"] for k in range(nD))
     np.testing.assert_allclose(wD / wD.sum(), wD_ref / wD_ref.sum(), atol=2e-3)
     np.testing.assert_allclose(wR / wR.sum(), wR_ref / wR_ref.sum(), atol=2e-3)
+
+
+@pytest.mark.parametrize("kernel", [tg3.KERNEL_MKB, tg3.KERNEL_TRILINEAR])
+def test_insertft_defocus_host(small, kernel):
+    """InsertFT with the defocus search: every draw's CTF from its image's
+    attributes with the draw's defocus factor (kernel_CalculateCTF); ctfP
+    is not read."""
+    rng = np.random.default_rng(73)
+    st = small["st"]
+    K, pf, box = st.K, small["pf"], small["box"]
+    vdim = pf * box
+    nImg, mReco = 4, 3
+    quats = synth.haar_quaternions(rng, nImg * mReco)
+    trans = rng.uniform(-2, 2, (nImg * mReco, 2))
+    offS = rng.uniform(-0.5, 0.5, (nImg, 2))
+    w = (np.ones(nImg) / mReco).astype(np.float32)
+    attr = synth.ctf_attrs(rng, nImg)
+    attr32 = np.ascontiguousarray(attr.astype(np.float32))
+    nD = rng.uniform(0.9, 1.1, nImg * mReco)
+    F = np.zeros((vdim, vdim, vdim // 2 + 1), np.complex64)
+    T = np.zeros((vdim, vdim, vdim // 2 + 1), np.float32)
+    O3D = np.zeros(3)
+    counter = np.zeros(1, np.int32)
+    dat = np.ascontiguousarray(st.dat[:nImg].astype(np.complex64))
+    sig = np.ascontiguousarray(st.sigRcp[:nImg].astype(np.float32))
+    iColPad = np.ascontiguousarray(small["iCol"] * pf, np.int32)
+    iRowPad = np.ascontiguousarray(small["iRow"] * pf, np.int32)
+    tg3.check(tg3.lib().tg3_InsertFT(
+        tg3.ptr(F), tg3.ptr(T), tg3.ptr(O3D), tg3.ptr(counter), tg3.ptr(dat), None,
+        tg3.ptr(sig), tg3.ptr(attr32), tg3.ptr(offS), tg3.ptr(w), tg3.ptr(quats), tg3.ptr(trans),
+        tg3.ptr(nD), tg3.ptr(iColPad), tg3.ptr(iRowPad),
+        small["px"], 1, pf, K, mReco, box, vdim, nImg, kernel))
+    assert counter[0] == nImg * mReco
+    Fr = np.zeros(F.shape, np.complex128)
+    Tr = np.zeros(T.shape)
+    b = (pf * 1.9) ** 2
+    tab = O.mkb_table(1.9, 15.0, b, 100000)
+    mats = O.rotmat(quats)
+    for l in range(nImg):
+        for m in range(mReco):
+            d = l * mReco + m
+            a = attr32[l].astype(np.float64)
+            a[1] *= nD[d]
+            a[2] *= nD[d]
+            ctf_d = synth.ctf_values(a[None], small["px"], box, small["iCol"], small["iRow"])[0]
+            tt = f32(trans[d]) - f32(offS[l])
+            img = O.translate_image(f32(dat[l]), -tt[0], -tt[1], box, small["iCol"], small["iRow"])
+            O.insert(Fr, Tr, img, f32(ctf_d), mats[d], float(w[l]), small["iCol"] * pf,
+                     small["iRow"] * pf, kernel, pf * 1.9, tab, b)
+    assert np.abs(F - Fr).max() < 2e-4 * np.abs(Fr).max()
+    assert np.abs(T - Tr).max() < 2e-4 * np.abs(Tr).max()

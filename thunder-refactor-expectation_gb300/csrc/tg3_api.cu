@@ -888,10 +888,12 @@ extern "C" int tg3_ctx_insert_begin(tg3_ctx* c, int vdim, int pf)
     return TG3_OK;
 }
 
+// ctfRows == nDraws: one CTF row per draw (the defocus search), else one
+// per image
 static int insert_draws(tg3_ctx* c, int nDraws, int drawsPerImage, const float* dat,
                         const float* ctf, const double* quat, const double* trans,
                         const double* offset, const float* w, int kernel, double* O3D,
-                        int* counter)
+                        int* counter, int ctfRows = 0)
 {
     if (!c->ins.acc) return fail(TG3_ERR_STATE, "insertion volume not begun");
     if (kernel != TG3_KERNEL_MKB && kernel != TG3_KERNEL_TRILINEAR)
@@ -911,7 +913,7 @@ static int insert_draws(tg3_ctx* c, int nDraws, int drawsPerImage, const float* 
                                       c->px.K, c->ins.pf,
                                       c->px.idim, c->px.maxAbs,
                                       (float)(c->px.maxRadius * c->ins.pf), O3D, counter,
-                                      scratch, bytes, c->stream));
+                                      scratch, bytes, c->stream, ctfRows));
         return TG3_OK;
     }
     float* params = static_cast<float*>(
@@ -921,7 +923,7 @@ static int insert_draws(tg3_ctx* c, int nDraws, int drawsPerImage, const float* 
                            c->ins.tabInvStep, nDraws, drawsPerImage,
                            reinterpret_cast<const float2*>(dat), ctf, quat, trans, offset, w,
                            c->px.iCol, c->px.iRow, c->px.K, c->ins.pf, c->px.idim, O3D,
-                           counter, params, c->stream));
+                           counter, params, c->stream, ctfRows));
     return TG3_OK;
 }
 
@@ -1215,11 +1217,12 @@ extern "C" int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter, c
                             float pixelSize, int cSearch, int opf, int npxl, int mReco, int idim,
                             int dimSize, int imgNum, int kernel)
 {
-    (void)sigRcpP; (void)ctfaData; (void)nD; (void)pixelSize;
-    if (cSearch) return fail(TG3_ERR_UNSUPPORTED, "defocus search insertion (cSearch) not supported");
-    if (!F3D || !T3D || !O3D || !counter || !datP || !ctfP || !offS || !w || !nR || !nT || !iCol ||
-        !iRow)
+    (void)sigRcpP;
+    if (!F3D || !T3D || !O3D || !counter || !datP || (!ctfP && !cSearch) || !offS || !w || !nR ||
+        !nT || !iCol || !iRow)
         return fail(TG3_ERR_ARG, "null pointer");
+    if (cSearch && (!ctfaData || !nD || !(pixelSize > 0)))
+        return fail(TG3_ERR_ARG, "defocus search insertion needs ctfaData, nD and pixelSize");
     if (opf < 1 || npxl <= 0 || mReco <= 0 || idim <= 0 || imgNum <= 0 || dimSize != opf * idim)
         return fail(TG3_ERR_ARG, "bad InsertFT sizes (dimSize must equal opf * idim)");
     int st = TG3_OK;
@@ -1241,10 +1244,16 @@ extern "C" int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter, c
     Arena ar(c, WS_H2D);
     const int IB = 4096;
     const int nb = std::min(imgNum, IB);
-    size_t od = ar.add(sizeof(float) * 2 * (size_t)nb * K), oc = ar.add(sizeof(float) * (size_t)nb * K),
+    // the defocus search: one CTF row per draw, made on the device from the
+    // image's attributes with the draw's defocus factor (kernel_CalculateCTF)
+    const size_t ctfRowsB = cSearch ? (size_t)nb * mReco : (size_t)nb;
+    size_t od = ar.add(sizeof(float) * 2 * (size_t)nb * K), oc = ar.add(sizeof(float) * ctfRowsB * K),
            oq = ar.add(sizeof(double) * 4 * (size_t)nb * mReco), ot = ar.add(sizeof(double) * 2 * (size_t)nb * mReco),
            oo = ar.add(sizeof(double) * 2 * (size_t)nb), ow = ar.add(sizeof(float) * (size_t)nb),
-           oO = ar.add(sizeof(double) * 3), on = ar.add(sizeof(int));
+           oO = ar.add(sizeof(double) * 3), on = ar.add(sizeof(int)),
+           oa = ar.add(cSearch ? sizeof(float) * 7 * (size_t)nb : 0),
+           oda = ar.add(cSearch ? sizeof(float) * 7 * (size_t)nb * mReco : 0),
+           ond = ar.add(cSearch ? sizeof(double) * (size_t)nb * mReco : 0);
     char* b = (char*)ws_get(c, WS_H2D, ar.used, &st);
     if (!b) return st;
     TG3_CUDA(cudaMemcpyAsync(b + oO, O3D, sizeof(double) * 3, cudaMemcpyHostToDevice, s));
@@ -1253,8 +1262,19 @@ extern "C" int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter, c
         const int n = std::min(IB, imgNum - l0);
         TG3_CUDA(cudaMemcpyAsync(b + od, datP + 2 * (size_t)l0 * K, sizeof(float) * 2 * (size_t)n * K,
                                  cudaMemcpyHostToDevice, s));
-        TG3_CUDA(cudaMemcpyAsync(b + oc, ctfP + (size_t)l0 * K, sizeof(float) * (size_t)n * K,
-                                 cudaMemcpyHostToDevice, s));
+        if (cSearch) {
+            TG3_CUDA(cudaMemcpyAsync(b + oa, ctfaData + 7 * (size_t)l0, sizeof(float) * 7 * (size_t)n,
+                                     cudaMemcpyHostToDevice, s));
+            TG3_CUDA(cudaMemcpyAsync(b + ond, nD + (size_t)l0 * mReco,
+                                     sizeof(double) * (size_t)n * mReco, cudaMemcpyHostToDevice, s));
+            TG3_CUDA(launch_draw_attr((const float*)(b + oa), (const double*)(b + ond), n * mReco,
+                                      mReco, (float*)(b + oda), s));
+            TG3_CUDA(launch_ctf((const float*)(b + oda), n * mReco, pixelSize, idim, c->px.iCol,
+                                c->px.iRow, K, (float*)(b + oc), s));
+        } else {
+            TG3_CUDA(cudaMemcpyAsync(b + oc, ctfP + (size_t)l0 * K, sizeof(float) * (size_t)n * K,
+                                     cudaMemcpyHostToDevice, s));
+        }
         TG3_CUDA(cudaMemcpyAsync(b + oq, nR + 4 * (size_t)l0 * mReco, sizeof(double) * 4 * (size_t)n * mReco,
                                  cudaMemcpyHostToDevice, s));
         TG3_CUDA(cudaMemcpyAsync(b + ot, nT + 2 * (size_t)l0 * mReco, sizeof(double) * 2 * (size_t)n * mReco,
@@ -1265,7 +1285,7 @@ extern "C" int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter, c
         if ((st = insert_draws(c, n * mReco, mReco, (const float*)(b + od), (const float*)(b + oc),
                                (const double*)(b + oq), (const double*)(b + ot),
                                (const double*)(b + oo), (const float*)(b + ow), kernel,
-                               (double*)(b + oO), (int*)(b + on))))
+                               (double*)(b + oO), (int*)(b + on), cSearch ? n * mReco : 0)))
             return st;
         // the staging buffer is reused by the next pass
         TG3_CUDA(cudaStreamSynchronize(s));

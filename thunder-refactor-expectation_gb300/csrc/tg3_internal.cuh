@@ -235,6 +235,9 @@ cudaError_t launch_norm_defocus(const float* P, long long splitLo, int nP, int n
                                 cudaStream_t st);
 cudaError_t launch_repeat_rows(const double* src, int rows, int len, int nRep, double* dst,
                                cudaStream_t st);
+// CTF attributes [nDraws][7] of insertion draws: the image's, defocus x nD[d]
+cudaError_t launch_draw_attr(const float* attr, const double* nD, int nDraws, int drawsPerImage,
+                             float* out, cudaStream_t st);
 // one particle's CTFs at defocus factors dpara [nD] from per-pixel defocus
 // defO and frequency freQ: ctf [nD][K]
 cudaError_t launch_ctf_defocus(const float* defO, const float* freQ, const double* dpara, int nD,
@@ -279,7 +282,7 @@ cudaError_t launch_insert(float4* acc, int vdim, int kernel, const float* tab,
                           const double* trans, const double* offset,
                           const float* w, const int* iCol, const int* iRow,
                           int K, int pf, int idim, double* O3D, int* counter,
-                          float* params, cudaStream_t st);
+                          float* params, cudaStream_t st, int ctfRows = 0);
 // MKB insertion by gather: per chunk of draws, k_insert_stage (tiles x
 // draws) fills the draws' dense pixel grids from the cell map cellPix,
 // k_insert_gather (tiles x draws) adds each slab voxel once.  scratch holds
@@ -291,7 +294,8 @@ cudaError_t launch_insert_gather(float4* acc, int vdim, const float* tab, int ta
                                  const double* trans, const double* offset, const float* w,
                                  const int* cellPix, const int* iCol, const int* iRow, int K,
                                  int pf, int idim, int Rg, float Rp, double* O3D, int* counter,
-                                 void* scratch, size_t scratchBytes, cudaStream_t st);
+                                 void* scratch, size_t scratchBytes, cudaStream_t st,
+                                 int ctfRows = 0);
 // Bank of projections: split planes and |P|^2 rows from the FP32 rows.
 cudaError_t launch_bank_planes(const float* f32, int nB, int K, int Kp, __nv_bfloat16* hi,
                                __nv_bfloat16* lo, float* abs2, cudaStream_t st);

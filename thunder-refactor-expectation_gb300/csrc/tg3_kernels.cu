@@ -503,6 +503,21 @@ __global__ void k_ctf_defocus(const float* __restrict__ defO, const float* __res
     }
 }
 
+// CTF attributes of every insertion draw with the defocus search: the
+// image's attributes with defocusU, V scaled by the draw's factor nD (the
+// defocus kernel_CalculateCTF uses, gpu/src/Kernel.cu:2132-2198).
+__global__ void k_draw_attr(const float* __restrict__ attr, const double* __restrict__ nD,
+                            int nDraws, int drawsPerImage, float* __restrict__ out)
+{
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= nDraws) return;
+    const float* a = attr + 7 * (size_t)(d / drawsPerImage);
+    float* o = out + 7 * (size_t)d;
+    for (int k = 0; k < 7; k++) o[k] = a[k];
+    o[1] = (float)((double)a[1] * nD[d]);
+    o[2] = (float)((double)a[2] * nD[d]);
+}
+
 // dst[(row nRep + k) len + j] = src[row len + j] (per-block copies of a
 // particle's priors for the weights kernel's (particle, defocus) blocks)
 __global__ void k_repeat_rows(const double* __restrict__ src, int rows, int len, int nRep,
@@ -1114,7 +1129,7 @@ k_insert(float4* __restrict__ acc, int vdim, int kernel, const float* __restrict
          int tabNz, float tabInvStep, float rs2, const float2* __restrict__ dat,
          const float* __restrict__ ctf, const float* __restrict__ params,
          const int* __restrict__ iCol, const int* __restrict__ iRow, int K, int pf, int idim,
-         int d0, int drawsPerImage)
+         int d0, int drawsPerImage, int ctfPerDraw)
 {
     const int d = d0 + blockIdx.y;            // draw; blockIdx.x: share of its pixels
     const int l = d / drawsPerImage;          // image
@@ -1128,7 +1143,7 @@ k_insert(float4* __restrict__ acc, int vdim, int kernel, const float* __restrict
     const float fpf = (float)pf;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K; p += gridDim.x * blockDim.x) {
         const size_t di = (size_t)l * K + p;
-        const float c = ctf[di];
+        const float c = ctf[(ctfPerDraw ? (size_t)d : (size_t)l) * K + p];
         const float2 X = dat[di];
         // shift by -(t - offset): multiply by exp(+2 pi i k.t / N)
         float f = ((float)iCol[p] * tx + (float)iRow[p] * ty) * invN;
@@ -1218,7 +1233,7 @@ k_insert_stage(float4* __restrict__ grid, int cells, float* __restrict__ rot,
                const float* __restrict__ ctf, const double* __restrict__ quat,
                const double* __restrict__ trans, const double* __restrict__ offset,
                const float* __restrict__ wgt, int K, int idim, int d0, int drawsPerImage,
-               double* __restrict__ O3D, int* __restrict__ counter)
+               int ctfPerDraw, double* __restrict__ O3D, int* __restrict__ counter)
 {
     const int dl = blockIdx.y;                // draw within the chunk
     const int d = d0 + dl;
@@ -1246,7 +1261,7 @@ k_insert_stage(float4* __restrict__ grid, int cells, float* __restrict__ rot,
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
         if (p >= 0) {
             const size_t di = (size_t)l * K + p;
-            const float c = ctf[di];
+            const float c = ctf[(ctfPerDraw ? (size_t)d : (size_t)l) * K + p];
             const float2 X = dat[di];
             float f = ((float)iCol[p] * tx + (float)iRow[p] * ty) * invN;
             float sn, co;
@@ -1610,6 +1625,13 @@ cudaError_t launch_norm_defocus(const float* P, long long splitLo, int nP, int n
     return cudaGetLastError();
 }
 
+cudaError_t launch_draw_attr(const float* attr, const double* nD, int nDraws, int drawsPerImage,
+                             float* out, cudaStream_t st)
+{
+    k_draw_attr<<<(nDraws + 255) / 256, 256, 0, st>>>(attr, nD, nDraws, drawsPerImage, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_ctf_defocus(const float* defO, const float* freQ, const double* dpara, int nD,
                                int K, double k1, double k2, double phaseShift, double conT,
                                float* ctf, cudaStream_t st)
@@ -1705,7 +1727,7 @@ cudaError_t launch_insert(float4* acc, int vdim, int kernel, const float* tab, i
                           const float* ctf, const double* quat, const double* trans,
                           const double* offset, const float* w, const int* iCol,
                           const int* iRow, int K, int pf, int idim, double* O3D, int* counter,
-                          float* params, cudaStream_t st)
+                          float* params, cudaStream_t st, int ctfRows)
 {
     if (nDraws <= 0) return cudaSuccess;
     // r^2 bound of the table's support: rint(r^2 n / b) <= tabNz  =>  r^2 < (tabNz + 1/2) b / n
@@ -1713,13 +1735,14 @@ cudaError_t launch_insert(float4* acc, int vdim, int kernel, const float* tab, i
     if (kernel == TG3_KERNEL_MKB && 2.0f * sqrtf(rs2) >= 4.0f) return cudaErrorInvalidValue;
     k_insert_draws<<<(nDraws + 255) / 256, 256, 0, st>>>(nDraws, drawsPerImage, quat, trans,
                                                          offset, w, params, O3D, counter);
+    const int ctfPerDraw = ctfRows == nDraws && drawsPerImage > 1;
     // one pixel per thread: the draw's pixels spread over ceil(K / 256) CTAs
     const int tiles = std::max(1, std::min(1024, (K + 255) / 256));
     for (int d0 = 0; d0 < nDraws; d0 += 65535) {
         const int n = std::min(65535, nDraws - d0);
         k_insert<<<dim3(tiles, n), 256, 0, st>>>(acc, vdim, kernel, tab, tabNz, tabInvStep, rs2,
                                                  dat, ctf, params, iCol, iRow, K, pf, idim, d0,
-                                                 drawsPerImage);
+                                                 drawsPerImage, ctfPerDraw);
     }
     return cudaGetLastError();
 }
@@ -1735,9 +1758,10 @@ cudaError_t launch_insert_gather(float4* acc, int vdim, const float* tab, int ta
                                  const double* trans, const double* offset, const float* w,
                                  const int* cellPix, const int* iCol, const int* iRow, int K,
                                  int pf, int idim, int Rg, float Rp, double* O3D, int* counter,
-                                 void* scratch, size_t scratchBytes, cudaStream_t st)
+                                 void* scratch, size_t scratchBytes, cudaStream_t st, int ctfRows)
 {
     if (nDraws <= 0) return cudaSuccess;
+    const int ctfPerDraw = ctfRows == nDraws && drawsPerImage > 1;
     const int gw = Rg + 1, cells = gw * (2 * Rg + 1);
     const size_t gridBytes = (size_t)cells * sizeof(float4);
     const size_t chunkMax = scratchBytes / insert_draw_bytes(Rg);
@@ -1752,8 +1776,8 @@ cudaError_t launch_insert_gather(float4* acc, int vdim, const float* tab, int ta
         const int n = std::min(chunk, nDraws - d0);
         k_insert_stage<<<dim3(stageTiles, n), 256, 0, st>>>(grid, cells, rot, cellPix, iCol, iRow,
                                                             dat, ctf, quat, trans, offset, w, K,
-                                                            idim, d0, drawsPerImage, O3D,
-                                                            counter);
+                                                            idim, d0, drawsPerImage, ctfPerDraw,
+                                                            O3D, counter);
         // about two waves of resident CTAs (152 SMs x 8 CTAs of 256 threads)
         const int tiles = std::max(1, std::min(128, (2 * 152 * 8 + n - 1) / n));
         k_insert_gather<<<dim3(tiles, n), 256, 0, st>>>(acc, vdim, grid, gw, Rg, rot, tab, tabNz,

@@ -409,6 +409,9 @@ void InsertFT(Volume& F3D, Volume& T3D, double* O3D, int* counter, MPI_Comm& hem
     for (size_t i = 0; i < n; i++) T[i] = REAL(T3D[i]);
     const int vdim = F3D.nSlcFT();
     (void)dimSize;
+    // CTFAttr (include/Database.h:108-122) is seven RFLOATs in the order the
+    // library reads
+    static_assert(sizeof(CTFAttr) == 7 * sizeof(RFLOAT), "CTFAttr layout");
     ok("InsertFT",
        tg3_InsertFT(reinterpret_cast<float*>(&F3D[0]), T.data(), O3D, counter,
                     reinterpret_cast<const float*>(datP), ctfP, sigRcpP,
