@@ -157,6 +157,38 @@ int tg3_ExpectLocal3D_ctf(tg3_volume* vol, const float* dat, const float* defO,
                           const double* oldD, double oldC, float* wC, float* wR,
                           float* wT, float* wD, float* dvp, float* baseL);
 
+/* 2-D classification's global search, ExpectGlobal2D
+ * (gpu/interface/Interface.h:176-197): imgNum images (datP [imgNum][npxl]
+ * complex, ctfP, sigRcpP [imgNum][npxl]) against nK class images vol
+ * [nK][vdim][vdim/2 + 1] complex (2-D half transforms, rows in FFT order) at
+ * nR in-plane rotations rot [nR][2] = (cos, sin) and nT translations trans
+ * [nT][2], priors pR [nR], pT [nT].  Outputs wC [imgNum][nK], wR
+ * [imgNum][nK][nR], wT [imgNum][nK][nT], relative to each image's best
+ * hypothesis over all classes.  iCol / iRow are the image's pixels (the
+ * projection samples (iCol pf, iRow pf) rotated); interp must be 1 (linear).
+ * Host pointers; FP32 scoring. */
+int tg3_ExpectGlobal2D(const float* vol, const float* datP, const float* ctfP,
+                       const float* sigRcpP, const double* trans, float* wC, float* wR,
+                       float* wT, const double* pR, const double* pT, const double* rot,
+                       const int* iCol, const int* iRow, int nK, int nR, int nT, int pf,
+                       int interp, int idim, int vdim, int npxl, int imgNum);
+
+/* 2-D classification's insertion, InsertI2D (gpu/interface/Interface.h:
+ * 239-266, without its communicators): draw d = l mReco + m of image l goes
+ * into class nC[d] at in-plane rotation nR[d] = (cos, sin) and shift nT[d]
+ * (minus offS[l]) with weight w[l]: F2D (complex) and T2D (real), both
+ * [nk][vdim][vdim/2 + 1], accumulated into by bilinear interpolation;
+ * O2D [nk][2] and counter [nk] added to.  iCol / iRow are the padded
+ * indices (i opf); vdim = opf idim.  cSearch: each draw's CTF from its
+ * image's CTFAttr (ctfaData [imgNum][7]) with defocus x nD[d], ctfP unread.
+ * Host pointers. */
+int tg3_InsertI2D(float* F2D, float* T2D, double* O2D, int* counter, const float* datP,
+                  const float* ctfP, const float* sigRcpP, const float* w, const double* offS,
+                  const int* nC, const double* nR, const double* nT, const double* nD,
+                  const float* ctfaData, const int* iCol, const int* iRow, float pixelSize,
+                  int cSearch, int nk, int opf, int npxl, int mReco, int idim, int vdim,
+                  int imgNum);
+
 /* Particle-filter narrowing + systematic resampling of one axis of nP
  * particles, Particle::keepHalfHeightPeak + Particle::resample(n, pt)
  * (src/Particle.cpp:1935-1973, 1275-1463) with the shuffle permutation and
@@ -352,6 +384,15 @@ int tg3_cnn_match_propose(const float* out, int n, const float* ref, int nRef,
                           const double* refQuat, int nRot, int nTrans,
                           unsigned long long seed, double* quat, double* trans, int* idx,
                           void* stream);
+
+/* The global scan of one 2-D class image img [vdim][vdim/2 + 1] complex
+ * (device) at in-plane rotations rot [nR][2] = (cos, sin): otherwise as
+ * tg3_global_scan_d. */
+int tg3_global_scan2d_d(tg3_ctx* ctx, const float* img, int vdim, int pf, int nImg, int nR,
+                        int nT, const float* dat, const float* ctf, const float* sigRcp,
+                        const double* rot, const double* trans, const double* pR,
+                        const double* pT, double* wC, double* wR, double* wT, double* baseL,
+                        float* dvp, int precision);
 
 /* Global scan of nImg images over one shared set of nR rotations and nT
  * translations, for the context's class-`cls` volume: the scan of

@@ -62,6 +62,8 @@ def lib():
         L.or_pixel_index.restype = _c
         L.or_rotmat.argtypes = [_f64p, _c, _f64p]
         L.or_project.argtypes = [_c128p, _c, _f64p, _c, _i32p, _i32p, _c, _c, _c128p]
+        L.or_project2d.argtypes = [_c128p, _c, _f64p, _c, _i32p, _i32p, _c, _c, _c128p]
+        L.or_insert2d.argtypes = [_c128p, _f64p, _c, _c128p, _f64p, _d, _d, _d, _i32p, _i32p, _c]
         L.or_translate.argtypes = [_f64p, _c, _c, _i32p, _i32p, _c, _c128p]
         L.or_translate_image.argtypes = [_c128p, _d, _d, _c, _i32p, _i32p, _c, _c128p]
         L.or_ctf.argtypes = [_f64p, _d, _c, _i32p, _i32p, _c, _f64p]
@@ -98,6 +100,8 @@ def ref():
         R = ctypes.CDLL(str(path), mode=os.RTLD_LAZY)
         R.ref_rotmat.argtypes = [_f64p, _c, _f64p]
         R.ref_project.argtypes = [_c128p, _c, _f64p, _c, _i32p, _i32p, _c, _c, _c128p]
+        R.ref_project2d.argtypes = [_c128p, _c, _f64p, _c, _i32p, _i32p, _c, _c, _c128p]
+        R.ref_insert2d.argtypes = [_c128p, _f64p, _c, _c128p, _f64p, _d, _d, _d, _i32p, _i32p, _c]
         R.ref_translate.argtypes = [_f64p, _c, _c, _i32p, _i32p, _c, _c128p]
         R.ref_translate_image.argtypes = [_c128p, _d, _d, _c, _i32p, _i32p, _c, _c128p]
         R.ref_ctf.argtypes = [_f64p, _d, _c, _i32p, _i32p, _c, _f64p]
@@ -142,6 +146,24 @@ def project(vol, mat, iCol, iRow, pf):
     out = np.zeros((len(mat), len(iCol)), np.complex128)
     lib().or_project(vol, vol.shape[0], mat, len(mat), iCol, iRow, len(iCol), pf, out)
     return out
+
+
+def project2d(img, rot, iCol, iRow, pf):
+    """2-D projections of a half transform img [vdim][vdim/2 + 1] at in-plane
+    rotations rot [nR][2] = (cos, sin); [nR][K] complex."""
+    img = _a(img, np.complex128)
+    rot = _a(rot, np.float64).reshape(-1, 2)
+    iCol, iRow = _a(iCol, np.int32), _a(iRow, np.int32)
+    out = np.zeros((len(rot), len(iCol)), np.complex128)
+    lib().or_project2d(img, img.shape[0], rot, len(rot), iCol, iRow, len(iCol), pf, out)
+    return out
+
+
+def insert2d(F, T, img, c, rot, w, iColPad, iRowPad):
+    """Add one slice into a 2-D F (complex) and T (real) in place."""
+    lib().or_insert2d(F, T, F.shape[0], _a(img, np.complex128), _a(c, np.float64),
+                      float(rot[0]), float(rot[1]), float(w), _a(iColPad, np.int32),
+                      _a(iRowPad, np.int32), len(iColPad))
 
 
 def translate(trans, N, iCol, iRow):

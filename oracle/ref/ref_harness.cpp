@@ -102,6 +102,46 @@ void ref_project(const double* vol, int vdim, const double* mat, int nR,
     }
 }
 
+/* Image::getByInterpolationFT(iCol, iRow, LINEAR_INTERP),
+ * src/Image/Image.cpp:345-368, on a 2-D half transform set directly in
+ * Fourier space, at the in-plane rotation (c, s) of the reference's 2-D
+ * projector (gpu/src/Kernel.cu:786-819). */
+void ref_project2d(const double* img, int vdim, const double* rot, int nR, const int* iCol,
+                   const int* iRow, int K, int pf, double* out)
+{
+    Image I(vdim, vdim, FT_SPACE);
+    memcpy(&I[0], img, sizeof(Complex) * I.sizeFT());
+    for (int r = 0; r < nR; r++) {
+        const double c = rot[2 * r], s = rot[2 * r + 1];
+        for (int p = 0; p < K; p++) {
+            const double i = (double)(iCol[p] * pf), j = (double)(iRow[p] * pf);
+            const Complex v = I.getByInterpolationFT(i * c - j * s, i * s + j * c, LINEAR_INTERP);
+            out[2 * ((size_t)r * K + p)] = REAL(v);
+            out[2 * ((size_t)r * K + p) + 1] = IMAG(v);
+        }
+    }
+}
+
+/* One 2-D insertion through Image::addFT(Complex / RFLOAT, iCol, iRow),
+ * src/Image/Image.cpp:370-402: img times ctf times w into F, ctf^2 w into T,
+ * at the in-plane rotation (c, s) of the padded pixel (iColPad, iRowPad). */
+void ref_insert2d(double* F, double* T, int vdim, const double* img, const double* ctf, double c,
+                  double s, double w, const int* iColPad, const int* iRowPad, int K)
+{
+    Image IF(vdim, vdim, FT_SPACE), IT(vdim, vdim, FT_SPACE);
+    memcpy(&IF[0], F, sizeof(Complex) * IF.sizeFT());
+    for (size_t i = 0; i < IT.sizeFT(); i++) IT[i] = COMPLEX(T[i], 0);
+    for (int p = 0; p < K; p++) {
+        const double a = iColPad[p], b = iRowPad[p];
+        const double x = c * a - s * b, y = s * a + c * b;
+        const Complex v = COMPLEX(img[2 * p] * ctf[p] * w, img[2 * p + 1] * ctf[p] * w);
+        IF.addFT(v, x, y);
+        IT.addFT(ctf[p] * ctf[p] * w, x, y);
+    }
+    memcpy(F, &IF[0], sizeof(Complex) * IF.sizeFT());
+    for (size_t i = 0; i < IT.sizeFT(); i++) T[i] = REAL(IT[i]);
+}
+
 /* translate(Complex*, nTransCol, nTransRow, nCol, nRow, iCol, iRow, nPxl,
  * nThread), src/Image/ImageFunctions.cpp:233-252 */
 void ref_translate(const double* trans, int nT, int N, const int* iCol,

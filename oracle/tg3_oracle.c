@@ -149,6 +149,80 @@ OR_EXPORT void or_project(const double* vol, int vdim, const double* mat,
 }
 
 /* ---------------------------------------------------------------------------
+ * 2-D: bilinear sample of a half transform [vdim][vdim/2 + 1] (rows in FFT
+ * order) at (x, y), Image::getByInterpolationFT(iCol, iRow, LINEAR_INTERP),
+ * src/Image/Image.cpp:345-368: x < 0 is read at (-x, -y) and conjugated
+ * (conjHalf); WG_BI_INTERP_LINEAR weights; getFTHalf wraps negative rows.
+ * ------------------------------------------------------------------------- */
+static void sample_bilinear(const double* img, int vdim, double x, double y, double out[2])
+{
+    int conj = 0;
+    if (x < 0) { x = -x; y = -y; conj = 1; }
+    const int nx = vdim / 2 + 1;
+    const int x0 = (int)floor(x), y0 = (int)floor(y);
+    const double fx = x - x0, fy = y - y0;
+    const double wx[2] = {1 - fx, fx}, wy[2] = {1 - fy, fy};
+    double re = 0, im = 0;
+    for (int j = 0; j < 2; j++)
+        for (int i = 0; i < 2; i++) {
+            int yy = y0 + j;
+            if (yy < 0) yy += vdim;
+            const size_t idx = (size_t)yy * nx + (x0 + i);
+            re += img[2 * idx] * wx[i] * wy[j];
+            im += img[2 * idx + 1] * wx[i] * wy[j];
+        }
+    out[0] = re;
+    out[1] = conj ? -im : im;
+}
+
+/* 2-D projection: in-plane rotation (c, s) of the pixel (iCol pf, iRow pf),
+ * the form of the reference's 2-D projector (kernel_Project2D,
+ * gpu/src/Kernel.cu:786-819: x = i c - j s, y = i s + j c).  rot is
+ * [nR][2] (c, s); out [nR][K] complex. */
+OR_EXPORT void or_project2d(const double* img, int vdim, const double* rot, int nR,
+                            const int* iCol, const int* iRow, int K, int pf, double* out)
+{
+    for (int r = 0; r < nR; r++) {
+        const double c = rot[2 * r], s = rot[2 * r + 1];
+        for (int p = 0; p < K; p++) {
+            const double i = (double)(iCol[p] * pf), j = (double)(iRow[p] * pf);
+            sample_bilinear(img, vdim, i * c - j * s, i * s + j * c,
+                            out + 2 * ((size_t)r * K + p));
+        }
+    }
+}
+
+/* 2-D insertion of one slice: Image::addFT(value, iCol, iRow),
+ * src/Image/Image.cpp:370-386 (bilinear, x < 0 at (-x, -y) conjugated) at the
+ * in-plane rotation (c, s) of the padded pixel (iColPad, iRowPad):
+ * F += w ctf img, T += w ctf^2, both [vdim][vdim/2 + 1]. */
+OR_EXPORT void or_insert2d(double* F, double* T, int vdim, const double* img, const double* ctf,
+                           double c, double s, double w, const int* iColPad,
+                           const int* iRowPad, int K)
+{
+    const int nx = vdim / 2 + 1;
+    for (int p = 0; p < K; p++) {
+        const double a = iColPad[p], b = iRowPad[p];
+        double x = c * a - s * b, y = s * a + c * b;
+        double vr = img[2 * p] * ctf[p] * w, vi = img[2 * p + 1] * ctf[p] * w;
+        const double vt = ctf[p] * ctf[p] * w;
+        if (x < 0) { x = -x; y = -y; vi = -vi; }
+        const int x0 = (int)floor(x), y0 = (int)floor(y);
+        const double fx = x - x0, fy = y - y0;
+        for (int j = 0; j < 2; j++)
+            for (int i = 0; i < 2; i++) {
+                const double ww = (i ? fx : 1 - fx) * (j ? fy : 1 - fy);
+                int yy = y0 + j;
+                if (yy < 0) yy += vdim;
+                const size_t idx = (size_t)yy * nx + x0 + i;
+                F[2 * idx] += vr * ww;
+                F[2 * idx + 1] += vi * ww;
+                T[idx] += vt * ww;
+            }
+    }
+}
+
+/* ---------------------------------------------------------------------------
  * Phase-shift bank.  translate(Complex*, nTransCol, nTransRow, nCol, nRow,
  * iCol, iRow, nPxl), src/Image/ImageFunctions.cpp:233-252:
  * S[p] = exp(-2 pi i (iCol tx / N + iRow ty / N)).  trans is [nT][2].

@@ -688,3 +688,170 @@ def test_insertft_defocus_host(small, kernel):
                      small["iRow"] * pf, kernel, pf * 1.9, tab, b)
     assert np.abs(F - Fr).max() < 2e-4 * np.abs(Fr).max()
     assert np.abs(T - Tr).max() < 2e-4 * np.abs(Tr).max()
+
+
+def test_expect_global2d_host():
+    """2-D classification's global search (ExpectGlobal2D) against the
+    oracle: the 2-D projection of every class (or_project2d, pinned to the
+    reference's Image::getByInterpolationFT) scored by the multi-class global
+    scan with its running baseline over classes."""
+    rng = np.random.default_rng(83)
+    box, pf, px = 24, 2, 1.5
+    vdim = box * pf
+    iCol, iRow = synth.pixel_index(box, 10, synth.config_rL(box, px))[:2]
+    K = len(iCol)
+    nK, nR, nImg = 2, 36, 6
+    imgs = (rng.standard_normal((nK, vdim, vdim // 2 + 1)) +
+            1j * rng.standard_normal((nK, vdim, vdim // 2 + 1))).astype(np.complex64)
+    ang = np.arange(nR) * (2 * np.pi / nR)
+    rot = np.ascontiguousarray(np.stack([np.cos(ang), np.sin(ang)], 1))
+    trans = np.ascontiguousarray(synth.global_translations(1, 1.0))
+    nT = len(trans)
+    attr = synth.ctf_attrs(rng, nImg)
+    ctf = np.ascontiguousarray(synth.ctf_values(attr, px, box, iCol, iRow).astype(np.float32))
+    sig = np.full((nImg, K), -0.5, np.float32)
+    traP = O.translate(trans, box, iCol, iRow)
+    rotP = [O.project2d(imgs[k].astype(np.complex128), rot, iCol, iRow, pf) for k in range(nK)]
+    kt, rt, tt = rng.integers(0, nK, nImg), rng.integers(0, nR, nImg), rng.integers(0, nT, nImg)
+    dat = np.stack([ctf[l] * rotP[kt[l]][rt[l]] * traP[tt[l]] for l in range(nImg)])
+    dat = np.ascontiguousarray((dat + 0.3 * (rng.standard_normal(dat.shape) +
+                                             1j * rng.standard_normal(dat.shape))).astype(np.complex64))
+    pR = np.full(nR, 1.0 / nR)
+    pT = np.full(nT, 1.0 / nT)
+    wC = np.zeros(nImg * nK, np.float32)
+    wR = np.zeros(nImg * nK * nR, np.float32)
+    wT = np.zeros(nImg * nK * nT, np.float32)
+    vol = np.ascontiguousarray(imgs)
+    ic, ir = np.ascontiguousarray(iCol, np.int32), np.ascontiguousarray(iRow, np.int32)
+    tg3.check(tg3.lib().tg3_ExpectGlobal2D(
+        tg3.ptr(vol), tg3.ptr(dat), tg3.ptr(ctf), tg3.ptr(sig), tg3.ptr(trans), tg3.ptr(wC),
+        tg3.ptr(wR), tg3.ptr(wT), tg3.ptr(pR), tg3.ptr(pT), tg3.ptr(rot), tg3.ptr(ic),
+        tg3.ptr(ir), nK, nR, nT, pf, 1, box, vdim, K, nImg))
+    state = None
+    for k in range(nK):
+        res = O.score_global(rotP[k], traP, f32(dat), f32(ctf), f32(sig), pR, pT, kIdx=k, nK=nK,
+                             state=state, want_dvp=False)
+        state = (res["wC"], res["wR"], res["wT"], res["baseL"])
+    rC, rR = state[0].reshape(nImg, nK), state[1].reshape(nImg, nK, nR)
+    gC, gR = wC.reshape(nImg, nK), wR.reshape(nImg, nK, nR)
+    np.testing.assert_allclose(gC / gC.sum(1, keepdims=True), rC / rC.sum(1, keepdims=True),
+                               atol=2e-3)
+    for l in range(nImg):
+        k = int(np.argmax(rC[l]))
+        assert int(np.argmax(gC[l])) == k == kt[l]
+        assert int(np.argmax(gR[l, k])) == int(np.argmax(rR[l, k])) == rt[l]
+        np.testing.assert_allclose(gR[l, k] / gR[l, k].sum(), rR[l, k] / rR[l, k].sum(),
+                                   atol=2e-3)
+
+
+def test_global_scan2d_device_split(small):
+    """The device 2-D scan in both precisions gives the same best rotation and
+    log-likelihoods within the split path's bound."""
+    rng = np.random.default_rng(89)
+    box, pf = small["box"], small["pf"]
+    vdim = box * pf
+    img = (rng.standard_normal((vdim, vdim // 2 + 1)) +
+           1j * rng.standard_normal((vdim, vdim // 2 + 1))).astype(np.complex64)
+    nR, nImg = 24, 4
+    ang = rng.uniform(0, 2 * np.pi, nR)
+    rot = np.stack([np.cos(ang), np.sin(ang)], 1)
+    trans = synth.global_translations(1, 1.0)
+    nT = len(trans)
+    st = small["st"]
+    out = {}
+    c = tg3.Context(0)
+    try:
+        c.set_pixels(small["iCol"], small["iRow"], box)
+        # device inputs held here: a temporary passed by address would be freed
+        ins = [dev(x) for x in (img, st.dat[:nImg].astype(np.complex64),
+                                st.ctf[:nImg].astype(np.float32),
+                                st.sigRcp[:nImg].astype(np.float32), rot, trans,
+                                np.full(nR, 1.0 / nR), np.full(nT, 1.0 / nT))]
+        for prec in (tg3.SCORE_FP32, tg3.SCORE_BF16X3):
+            o = [torch.empty(s, dtype=torch.float64, device=DEV)
+                 for s in (nImg, (nImg, nR), (nImg, nT), nImg)]
+            dvp = torch.empty((nImg, nR, nT), dtype=torch.float32, device=DEV)
+            tg3.check(tg3.lib().tg3_global_scan2d_d(
+                c.h, tg3.ptr(ins[0]), vdim, pf, nImg, nR, nT, tg3.ptr(ins[1]), tg3.ptr(ins[2]),
+                tg3.ptr(ins[3]), tg3.ptr(ins[4]), tg3.ptr(ins[5]), tg3.ptr(ins[6]),
+                tg3.ptr(ins[7]), tg3.ptr(o[0]), tg3.ptr(o[1]), tg3.ptr(o[2]), tg3.ptr(o[3]),
+                tg3.ptr(dvp), prec))
+            c.sync()
+            out[prec] = dvp.cpu().numpy()
+    finally:
+        c.close()
+    a, b = out[tg3.SCORE_FP32], out[tg3.SCORE_BF16X3]
+    assert np.abs(a - b).max() / np.abs(a).max() < 1e-4
+    assert np.array_equal(a.reshape(nImg, -1).argmax(1), b.reshape(nImg, -1).argmax(1))
+
+
+@pytest.mark.parametrize("csearch", [0, 1])
+def test_insert_i2d_host(csearch):
+    """2-D classification's insertion (InsertI2D) against the oracle: each
+    draw's shifted image, times its CTF and its image's weight, added
+    bilinearly at the draw's in-plane rotation into its class (or_insert2d,
+    pinned to the reference's Image::addFT); O2D and counter per class.
+    With the defocus search every draw's CTF comes from its image's
+    attributes and the draw's defocus factor."""
+    rng = np.random.default_rng(97)
+    box, pf, px = 24, 2, 1.5
+    vdim = box * pf
+    nx = vdim // 2 + 1
+    iCol, iRow = synth.pixel_index(box, 10, synth.config_rL(box, px))[:2]
+    K = len(iCol)
+    nK, nImg, mReco = 3, 7, 2
+    nd = nImg * mReco
+    dat = np.ascontiguousarray((rng.standard_normal((nImg, K)) +
+                                1j * rng.standard_normal((nImg, K))).astype(np.complex64))
+    attr = synth.ctf_attrs(rng, nImg)
+    attr32 = np.ascontiguousarray(attr.astype(np.float32))
+    ctf = np.ascontiguousarray(synth.ctf_values(attr, px, box, iCol, iRow).astype(np.float32))
+    sig = np.full((nImg, K), 1.0, np.float32)
+    w = rng.uniform(0.2, 1.0, nImg).astype(np.float32)
+    offS = rng.uniform(-0.5, 0.5, (nImg, 2))
+    nC = np.ascontiguousarray(rng.integers(0, nK, nd), np.int32)
+    ang = rng.uniform(0, 2 * np.pi, nd)
+    nR = np.ascontiguousarray(np.stack([np.cos(ang), np.sin(ang)], 1))
+    nT = rng.uniform(-2, 2, (nd, 2))
+    nD = rng.uniform(0.9, 1.1, nd)
+    F = np.zeros((nK, vdim, nx), np.complex64)
+    F[1, 2, 3] = 1 - 1j       # accumulated into, not overwritten
+    T = np.zeros((nK, vdim, nx), np.float32)
+    O2D = np.zeros((nK, 2))
+    O2D[0] = (0.5, -0.25)
+    counter = np.zeros(nK, np.int32)
+    counter[2] = 4
+    iColPad = np.ascontiguousarray(iCol * pf, np.int32)
+    iRowPad = np.ascontiguousarray(iRow * pf, np.int32)
+    tg3.check(tg3.lib().tg3_InsertI2D(
+        tg3.ptr(F), tg3.ptr(T), tg3.ptr(O2D), tg3.ptr(counter), tg3.ptr(dat),
+        None if csearch else tg3.ptr(ctf), tg3.ptr(sig), tg3.ptr(w), tg3.ptr(offS), tg3.ptr(nC),
+        tg3.ptr(nR), tg3.ptr(nT), tg3.ptr(nD) if csearch else None,
+        tg3.ptr(attr32) if csearch else None, tg3.ptr(iColPad), tg3.ptr(iRowPad), px, csearch,
+        nK, pf, K, mReco, box, vdim, nImg))
+    Fr = np.zeros(F.shape, np.complex128)
+    Fr[1, 2, 3] = 1 - 1j
+    Tr = np.zeros(T.shape)
+    Or = np.array([[0.5, -0.25], [0, 0], [0, 0]])
+    cr = np.array([0, 0, 4])
+    for l in range(nImg):
+        for m in range(mReco):
+            d = l * mReco + m
+            if csearch:
+                a = attr32[l].astype(np.float64)
+                a[1] *= nD[d]
+                a[2] *= nD[d]
+                c = synth.ctf_values(a[None], px, box, iCol, iRow)[0]
+            else:
+                c = ctf[l]
+            tt = nT[d] - offS[l]
+            img = O.translate_image(f32(dat[l]), -tt[0], -tt[1], box, iCol, iRow)
+            k = nC[d]
+            O.insert2d(Fr[k], Tr[k], img, f32(c), nR[d], float(w[l]), iColPad, iRowPad)
+            c_, s_ = nR[d]
+            Or[k] -= (c_ * tt[0] - s_ * tt[1], s_ * tt[0] + c_ * tt[1])
+            cr[k] += 1
+    np.testing.assert_array_equal(counter, cr)
+    np.testing.assert_allclose(O2D, Or, rtol=0, atol=1e-9)
+    assert np.abs(F - Fr).max() < 2e-4 * np.abs(Fr).max()
+    assert np.abs(T - Tr).max() < 2e-4 * np.abs(Tr).max()

@@ -69,3 +69,43 @@ def test_resample(n, n_out, mode):
     src1, w1, _ = O.resample(u, w, perm.astype(np.int32), u0, pfac, n_out)
     assert np.array_equal(src1, src2)
     assert np.array_equal(w1, w2)
+
+
+def test_project2d():
+    """The 2-D projection (bilinear in a half transform, Friedel mirror,
+    wrapped rows) against the reference's Image::getByInterpolationFT."""
+    rng = np.random.default_rng(17)
+    box, pf = 24, 2
+    vdim = box * pf
+    iCol, iRow, _, _ = synth.pixel_index(box, 10, 1)
+    img = np.ascontiguousarray(rng.standard_normal((vdim, vdim // 2 + 1)) +
+                               1j * rng.standard_normal((vdim, vdim // 2 + 1)))
+    ang = rng.uniform(0, 2 * np.pi, 40)
+    rot = np.ascontiguousarray(np.stack([np.cos(ang), np.sin(ang)], 1))
+    P2 = np.zeros((40, len(iCol)), np.complex128)
+    R.ref_project2d(img, vdim, rot, 40, iCol, iRow, len(iCol), pf, P2)
+    P1 = O.project2d(img, rot, iCol, iRow, pf)
+    np.testing.assert_allclose(P1, P2, rtol=0, atol=1e-12)
+
+
+def test_insert2d():
+    """The 2-D insertion (bilinear into a half transform, Friedel mirror,
+    wrapped rows) against the reference's Image::addFT, complex and real."""
+    rng = np.random.default_rng(19)
+    box, pf = 24, 2
+    vdim = box * pf
+    iCol, iRow, _, _ = synth.pixel_index(box, 10, 1)
+    K = len(iCol)
+    ic, ir = np.ascontiguousarray(iCol * pf, np.int32), np.ascontiguousarray(iRow * pf, np.int32)
+    F1 = np.zeros((vdim, vdim // 2 + 1), np.complex128)
+    T1 = np.zeros((vdim, vdim // 2 + 1))
+    F2, T2 = F1.copy(), T1.copy()
+    for ang in rng.uniform(0, 2 * np.pi, 6):
+        img = rng.standard_normal(K) + 1j * rng.standard_normal(K)
+        c = rng.uniform(-1, 1, K)
+        w = float(rng.uniform(0.1, 1))
+        O.insert2d(F1, T1, img, c, (np.cos(ang), np.sin(ang)), w, ic, ir)
+        R.ref_insert2d(F2, T2, vdim, np.ascontiguousarray(img), np.ascontiguousarray(c),
+                       np.cos(ang), np.sin(ang), w, ic, ir, K)
+    np.testing.assert_allclose(F1, F2, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(T1, T2, rtol=0, atol=1e-12)

@@ -1456,6 +1456,198 @@ extern "C" int tg3_ExpectLocal3D_ctf(tg3_volume* h, const float* dat, const floa
     return TG3_OK;
 }
 
+static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim, int pf,
+                       int nImg, int nR, int nT, const float* dat, const float* ctf,
+                       const float* sigRcp, const double* rotMat, const double* trans,
+                       const double* pR, const double* pT, double* wC, double* wR, double* wT,
+                       double* baseL, float* dvp, int precision);
+
+// 2-D classification's global search (ExpectGlobal2D,
+// gpu/interface/Interface.h:176-197; expectGlobal2D, gpu/src/cuthunder.cu:
+// 889-): every image against nK class images at nR in-plane rotations x nT
+// translations, the classes merged to each image's best hypothesis as the
+// reference's running baseline does.  FP32, the reference's plain path.
+extern "C" int tg3_ExpectGlobal2D(const float* vol, const float* datP, const float* ctfP,
+                                  const float* sigRcpP, const double* trans, float* wC, float* wR,
+                                  float* wT, const double* pR, const double* pT, const double* rot,
+                                  const int* iCol, const int* iRow, int nK, int nR, int nT,
+                                  int pf, int interp, int idim, int vdim, int npxl, int imgNum)
+{
+    if (!vol || !datP || !ctfP || !sigRcpP || !trans || !wC || !wR || !wT || !pR || !pT || !rot ||
+        !iCol || !iRow)
+        return fail(TG3_ERR_ARG, "null pointer");
+    if (nK <= 0 || nK > kMaxClasses || nR <= 0 || nT <= 0 || npxl <= 0 || imgNum <= 0 ||
+        pf < 1 || vdim < 4 || (vdim & 1) || nT > 2048)
+        return fail(TG3_ERR_ARG, "bad ExpectGlobal2D sizes");
+    if (interp != 1) return fail(TG3_ERR_UNSUPPORTED, "only linear interpolation");
+    int st = TG3_OK;
+    tg3_ctx* c = default_ctx(&st);
+    if (!c) return st;
+    if ((st = tg3_ctx_set_pixels(c, iCol, iRow, npxl, idim))) return st;
+    cudaStream_t s = c->stream;
+    const int K = npxl;
+    const size_t img = (size_t)vdim * (vdim / 2 + 1);
+    const int IB = 1024;
+    const int nb = std::min(imgNum, IB);
+    Arena ar(c, WS_H2D);
+    size_t oim = ar.add(sizeof(float) * 2 * img * nK), orot = ar.add(sizeof(double) * 2 * nR),
+           otr = ar.add(sizeof(double) * 2 * nT), opr = ar.add(sizeof(double) * nR),
+           opt = ar.add(sizeof(double) * nT), od = ar.add(sizeof(float) * 2 * (size_t)nb * K),
+           oc = ar.add(sizeof(float) * (size_t)nb * K), os = ar.add(sizeof(float) * (size_t)nb * K),
+           owc = ar.add(sizeof(double) * nb), owr = ar.add(sizeof(double) * (size_t)nb * nR),
+           owt = ar.add(sizeof(double) * (size_t)nb * nT), obs = ar.add(sizeof(double) * nb),
+           oWC = ar.add(sizeof(float) * (size_t)nb * nK),
+           oWR = ar.add(sizeof(float) * (size_t)nb * nK * nR),
+           oWT = ar.add(sizeof(float) * (size_t)nb * nK * nT), oBL = ar.add(sizeof(float) * nb);
+    char* b = (char*)ws_get(c, WS_H2D, ar.used, &st);
+    if (!b) return st;
+    TG3_CUDA(cudaMemcpyAsync(b + oim, vol, sizeof(float) * 2 * img * nK, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + orot, rot, sizeof(double) * 2 * nR, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + otr, trans, sizeof(double) * 2 * nT, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opr, pR, sizeof(double) * nR, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + opt, pT, sizeof(double) * nT, cudaMemcpyHostToDevice, s));
+    for (int l0 = 0; l0 < imgNum; l0 += IB) {
+        const int n = std::min(IB, imgNum - l0);
+        TG3_CUDA(cudaMemcpyAsync(b + od, datP + 2 * (size_t)l0 * K, sizeof(float) * 2 * (size_t)n * K,
+                                 cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + oc, ctfP + (size_t)l0 * K, sizeof(float) * (size_t)n * K,
+                                 cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + os, sigRcpP + (size_t)l0 * K, sizeof(float) * (size_t)n * K,
+                                 cudaMemcpyHostToDevice, s));
+        for (int k = 0; k < nK; k++) {
+            st = global_scan(c, nullptr, (const float2*)(b + oim) + img * k, vdim, pf, n, nR, nT,
+                             (const float*)(b + od), (const float*)(b + oc), (const float*)(b + os),
+                             (const double*)(b + orot), (const double*)(b + otr),
+                             (const double*)(b + opr), (const double*)(b + opt), (double*)(b + owc),
+                             (double*)(b + owr), (double*)(b + owt), (double*)(b + obs), nullptr,
+                             TG3_SCORE_FP32);
+            if (st) return st;
+            TG3_CUDA(launch_merge_class(n, nK, k, nR, nT, (const double*)(b + owc),
+                                        (const double*)(b + owr), (const double*)(b + owt),
+                                        (const double*)(b + obs), (float*)(b + oWC),
+                                        (float*)(b + oWR), (float*)(b + oWT), (float*)(b + oBL),
+                                        s));
+        }
+        TG3_CUDA(cudaMemcpyAsync(wC + (size_t)l0 * nK, b + oWC, sizeof(float) * (size_t)n * nK,
+                                 cudaMemcpyDeviceToHost, s));
+        TG3_CUDA(cudaMemcpyAsync(wR + (size_t)l0 * nK * nR, b + oWR,
+                                 sizeof(float) * (size_t)n * nK * nR, cudaMemcpyDeviceToHost, s));
+        TG3_CUDA(cudaMemcpyAsync(wT + (size_t)l0 * nK * nT, b + oWT,
+                                 sizeof(float) * (size_t)n * nK * nT, cudaMemcpyDeviceToHost, s));
+        // the staging buffer is reused by the next pass
+        if ((st = sync_and_check(c))) return st;
+    }
+    return TG3_OK;
+}
+
+// 2-D classification's insertion, InsertI2D (gpu/interface/Interface.h:
+// 239-266, without its communicators): every draw into the accumulator of
+// its class; F2D / T2D [nk][vdim][vdim/2 + 1] accumulated into, O2D [nk][2]
+// and counter [nk] added to.  iCol / iRow are the reconstructor's padded
+// indices (i opf).  With cSearch each draw's CTF is made from its image's
+// CTFAttr and the draw's defocus factor nD, as in tg3_InsertFT.
+extern "C" int tg3_InsertI2D(float* F2D, float* T2D, double* O2D, int* counter,
+                             const float* datP, const float* ctfP, const float* sigRcpP,
+                             const float* w, const double* offS, const int* nC, const double* nR,
+                             const double* nT, const double* nD, const float* ctfaData,
+                             const int* iCol, const int* iRow, float pixelSize, int cSearch,
+                             int nk, int opf, int npxl, int mReco, int idim, int vdim,
+                             int imgNum)
+{
+    (void)sigRcpP;
+    if (!F2D || !T2D || !O2D || !counter || !datP || (!ctfP && !cSearch) || !w || !offS ||
+        !nC || !nR || !nT || !iCol || !iRow)
+        return fail(TG3_ERR_ARG, "null pointer");
+    if (cSearch && (!ctfaData || !nD || !(pixelSize > 0)))
+        return fail(TG3_ERR_ARG, "defocus search insertion needs ctfaData, nD and pixelSize");
+    if (nk <= 0 || opf < 1 || npxl <= 0 || mReco <= 0 || idim <= 0 || imgNum <= 0 ||
+        vdim != opf * idim)
+        return fail(TG3_ERR_ARG, "bad InsertI2D sizes (vdim must equal opf * idim)");
+    for (int d = 0; d < imgNum * mReco; d++)
+        if (nC[d] < 0 || nC[d] >= nk) return fail(TG3_ERR_ARG, "class index out of range");
+    int st = TG3_OK;
+    tg3_ctx* c = default_ctx(&st);
+    if (!c) return st;
+    std::vector<int> ic(npxl), ir(npxl);
+    for (int p = 0; p < npxl; p++) {
+        if (iCol[p] % opf || iRow[p] % opf)
+            return fail(TG3_ERR_ARG, "InsertI2D pixel indices must be multiples of opf");
+        ic[p] = iCol[p] / opf;
+        ir[p] = iRow[p] / opf;
+    }
+    if ((st = tg3_ctx_set_pixels(c, ic.data(), ir.data(), npxl, idim))) return st;
+    if ((st = check_geometry(c, vdim, opf, 1.0))) return st;
+    cudaStream_t s = c->stream;
+    const size_t nvox = (size_t)vdim * (vdim / 2 + 1);
+    const int K = npxl;
+    const int IB = 4096;
+    const int nb = std::min(imgNum, IB);
+    const size_t ctfRowsB = cSearch ? (size_t)nb * mReco : (size_t)nb;
+    Arena ar(c, WS_H2D);
+    size_t oacc = ar.add(sizeof(float4) * nvox * nk), od = ar.add(sizeof(float) * 2 * (size_t)nb * K),
+           oc = ar.add(sizeof(float) * ctfRowsB * K), ow = ar.add(sizeof(float) * nb),
+           oo = ar.add(sizeof(double) * 2 * nb), onc = ar.add(sizeof(int) * (size_t)nb * mReco),
+           onr = ar.add(sizeof(double) * 2 * (size_t)nb * mReco),
+           ont = ar.add(sizeof(double) * 2 * (size_t)nb * mReco), oO = ar.add(sizeof(double) * 2 * nk),
+           ocn = ar.add(sizeof(int) * nk), oa = ar.add(cSearch ? sizeof(float) * 7 * (size_t)nb : 0),
+           oda = ar.add(cSearch ? sizeof(float) * 7 * (size_t)nb * mReco : 0),
+           ond = ar.add(cSearch ? sizeof(double) * (size_t)nb * mReco : 0),
+           oF = ar.add(sizeof(float) * 2 * nvox), oT = ar.add(sizeof(float) * nvox);
+    char* b = (char*)ws_get(c, WS_H2D, ar.used, &st);
+    if (!b) return st;
+    float4* acc = (float4*)(b + oacc);
+    TG3_CUDA(cudaMemsetAsync(acc, 0, sizeof(float4) * nvox * nk, s));
+    TG3_CUDA(cudaMemcpyAsync(b + oO, O2D, sizeof(double) * 2 * nk, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + ocn, counter, sizeof(int) * nk, cudaMemcpyHostToDevice, s));
+    for (int l0 = 0; l0 < imgNum; l0 += IB) {
+        const int n = std::min(IB, imgNum - l0);
+        const size_t nd = (size_t)n * mReco, d0 = (size_t)l0 * mReco;
+        TG3_CUDA(cudaMemcpyAsync(b + od, datP + 2 * (size_t)l0 * K, sizeof(float) * 2 * (size_t)n * K,
+                                 cudaMemcpyHostToDevice, s));
+        if (cSearch) {
+            TG3_CUDA(cudaMemcpyAsync(b + oa, ctfaData + 7 * (size_t)l0, sizeof(float) * 7 * (size_t)n,
+                                     cudaMemcpyHostToDevice, s));
+            TG3_CUDA(cudaMemcpyAsync(b + ond, nD + d0, sizeof(double) * nd, cudaMemcpyHostToDevice, s));
+            TG3_CUDA(launch_draw_attr((const float*)(b + oa), (const double*)(b + ond), (int)nd,
+                                      mReco, (float*)(b + oda), s));
+            TG3_CUDA(launch_ctf((const float*)(b + oda), (int)nd, pixelSize, idim, c->px.iCol,
+                                c->px.iRow, K, (float*)(b + oc), s));
+        } else {
+            TG3_CUDA(cudaMemcpyAsync(b + oc, ctfP + (size_t)l0 * K, sizeof(float) * (size_t)n * K,
+                                     cudaMemcpyHostToDevice, s));
+        }
+        TG3_CUDA(cudaMemcpyAsync(b + ow, w + l0, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + oo, offS + 2 * (size_t)l0, sizeof(double) * 2 * n,
+                                 cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + onc, nC + d0, sizeof(int) * nd, cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + onr, nR + 2 * d0, sizeof(double) * 2 * nd, cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + ont, nT + 2 * d0, sizeof(double) * 2 * nd, cudaMemcpyHostToDevice, s));
+        TG3_CUDA(launch_insert2d(acc, vdim, (const float2*)(b + od), (const float*)(b + oc),
+                                 cSearch ? 1 : 0, (const float*)(b + ow), (const double*)(b + oo),
+                                 (const int*)(b + onc), (const double*)(b + onr),
+                                 (const double*)(b + ont), c->px.iCol, c->px.iRow, K, opf, idim,
+                                 (int)nd, mReco, (double*)(b + oO), (int*)(b + ocn), s));
+        // the staging buffers are reused by the next pass
+        TG3_CUDA(cudaStreamSynchronize(s));
+    }
+    // add every class's accumulator to the caller's volumes
+    for (int k = 0; k < nk; k++) {
+        TG3_CUDA(cudaMemcpyAsync(b + oF, F2D + 2 * nvox * k, sizeof(float) * 2 * nvox,
+                                 cudaMemcpyHostToDevice, s));
+        TG3_CUDA(cudaMemcpyAsync(b + oT, T2D + nvox * k, sizeof(float) * nvox, cudaMemcpyHostToDevice,
+                                 s));
+        TG3_CUDA(launch_acc_read(acc + nvox * k, nvox, (float2*)(b + oF), (float*)(b + oT), 1, s));
+        TG3_CUDA(cudaMemcpyAsync(F2D + 2 * nvox * k, b + oF, sizeof(float) * 2 * nvox,
+                                 cudaMemcpyDeviceToHost, s));
+        TG3_CUDA(cudaMemcpyAsync(T2D + nvox * k, b + oT, sizeof(float) * nvox, cudaMemcpyDeviceToHost,
+                                 s));
+        TG3_CUDA(cudaStreamSynchronize(s));
+    }
+    TG3_CUDA(cudaMemcpyAsync(O2D, b + oO, sizeof(double) * 2 * nk, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(counter, b + ocn, sizeof(int) * nk, cudaMemcpyDeviceToHost, s));
+    return sync_and_check(c);
+}
+
 // ====================================================== host batched phase
 extern "C" int tg3_local_phase(tg3_ctx* c, int nP, int nR, int nT, const float* dat,
                                const float* ctf, const float* sigRcp, const double* quat,
@@ -1571,16 +1763,16 @@ __global__ void k_abs2_from(const float* __restrict__ P, long long loOff, int K,
 }
 }  // namespace tg3
 
-extern "C" int tg3_global_scan_d(tg3_ctx* c, int cls, int nImg, int nR, int nT, const float* dat,
-                                 const float* ctf, const float* sigRcp, const double* rotMat,
-                                 const double* trans, const double* pR, const double* pT,
-                                 double* wC, double* wR, double* wT, double* baseL, float* dvp,
-                                 int precision)
+// The global scan of one class.  The projections come from the class's 3-D
+// volume v at rotation matrices rot [nR][9], or (img2 != nullptr) from a 2-D
+// class image img2 [vdim][vdim/2 + 1] at in-plane rotations rot [nR][2].
+static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim, int pf,
+                       int nImg, int nR, int nT, const float* dat, const float* ctf,
+                       const float* sigRcp, const double* rotMat, const double* trans,
+                       const double* pR, const double* pT, double* wC, double* wR, double* wT,
+                       double* baseL, float* dvp, int precision)
 {
-    int st = check_ctx(c);
-    if (st) return st;
-    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].blocks)
-        return fail(TG3_ERR_STATE, "volume of the class not set");
+    int st = TG3_OK;
     if (nImg <= 0 || nR <= 0 || nT <= 0 || nT > 2048) return fail(TG3_ERR_ARG, "bad scan shape");
     if (!dat || !ctf || !sigRcp || !rotMat || !trans || !pR || !pT || !wC || !wR || !wT || !baseL)
         return fail(TG3_ERR_ARG, "null device pointer");
@@ -1588,8 +1780,7 @@ extern "C" int tg3_global_scan_d(tg3_ctx* c, int cls, int nImg, int nR, int nT, 
         return fail(TG3_ERR_ARG, "unknown precision");
     const bool split = precision == TG3_SCORE_BF16X3;
     if (split && !bf16x3_available()) return fail(TG3_ERR_UNSUPPORTED, "no TMA encoder");
-    const Volume& v = c->vol[cls];
-    if ((st = check_geometry(c, v.vdim, v.pf))) return st;
+    if ((st = check_geometry(c, vdim, pf))) return st;
     if ((st = check_weights_shape(nR, nT))) return st;
     const int K = c->px.K, Kp = c->px.Kp, Kq = (int)round_up(K, 64);
     // images per pass: keep the likelihood block within 4 GiB
@@ -1620,9 +1811,13 @@ extern "C" int tg3_global_scan_d(tg3_ctx* c, int cls, int nImg, int nR, int nT, 
     const long long splitP = split ? (long long)nR * Kp : 0;
     {
         StageTimer tm(c, TG3_STAGE_PROJECT);
-        TG3_CUDA(launch_project(nullptr, nullptr, v.blocks, v.vdim, v.pf, nullptr, rotMat, nR, nR,
-                                c->px.iCol, c->px.iRow, K, P, Kp, nullptr, nullptr, nullptr,
-                                pscr, c->d_flag, splitP, s));
+        if (img2)
+            TG3_CUDA(launch_project2d(img2, vdim, pf, rotMat, nR, c->px.iCol, c->px.iRow, K, P, Kp,
+                                      splitP, s));
+        else
+            TG3_CUDA(launch_project(nullptr, nullptr, v->blocks, v->vdim, v->pf, nullptr, rotMat,
+                                    nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, nullptr, nullptr,
+                                    nullptr, pscr, c->d_flag, splitP, s));
         k_abs2_from<<<nR, 256, 0, s>>>(P, splitP, K, Kp, abs2, Kq);
         TG3_LAUNCH_CHECK("projection norms");
     }
@@ -1667,4 +1862,32 @@ extern "C" int tg3_global_scan_d(tg3_ctx* c, int cls, int nImg, int nR, int nT, 
         }
     }
     return TG3_OK;
+}
+
+extern "C" int tg3_global_scan_d(tg3_ctx* c, int cls, int nImg, int nR, int nT, const float* dat,
+                                 const float* ctf, const float* sigRcp, const double* rotMat,
+                                 const double* trans, const double* pR, const double* pT,
+                                 double* wC, double* wR, double* wT, double* baseL, float* dvp,
+                                 int precision)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].blocks)
+        return fail(TG3_ERR_STATE, "volume of the class not set");
+    const Volume& v = c->vol[cls];
+    return global_scan(c, &v, nullptr, v.vdim, v.pf, nImg, nR, nT, dat, ctf, sigRcp, rotMat,
+                       trans, pR, pT, wC, wR, wT, baseL, dvp, precision);
+}
+
+extern "C" int tg3_global_scan2d_d(tg3_ctx* c, const float* img, int vdim, int pf, int nImg,
+                                   int nR, int nT, const float* dat, const float* ctf,
+                                   const float* sigRcp, const double* rot, const double* trans,
+                                   const double* pR, const double* pT, double* wC, double* wR,
+                                   double* wT, double* baseL, float* dvp, int precision)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (!img || vdim < 4 || (vdim & 1) || pf < 1) return fail(TG3_ERR_ARG, "bad class image");
+    return global_scan(c, nullptr, reinterpret_cast<const float2*>(img), vdim, pf, nImg, nR, nT,
+                       dat, ctf, sigRcp, rot, trans, pR, pT, wC, wR, wT, baseL, dvp, precision);
 }

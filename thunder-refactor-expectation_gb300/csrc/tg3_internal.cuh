@@ -235,6 +235,18 @@ cudaError_t launch_norm_defocus(const float* P, long long splitLo, int nP, int n
                                 cudaStream_t st);
 cudaError_t launch_repeat_rows(const double* src, int rows, int len, int nRep, double* dst,
                                cudaStream_t st);
+// 2-D insertion of nDraws draws into per-class accumulators acc
+// [nK][vdim][vdim/2 + 1] (F.re, F.im, T, 0); nR, nT [nDraws][2]; nC [nDraws]
+cudaError_t launch_insert2d(float4* acc, int vdim, const float2* dat, const float* ctf,
+                            int ctfPerDraw, const float* w, const double* offS, const int* nC,
+                            const double* nR, const double* nT, const int* iCol, const int* iRow,
+                            int K, int pf, int idim, int nDraws, int drawsPerImage, double* O2D,
+                            int* counter, cudaStream_t st);
+// 2-D projections of a class image [vdim][vdim/2 + 1] at in-plane rotations
+// rot [nR][2] (cos, sin): rows out [nR][ldo] (FP32, or split planes)
+cudaError_t launch_project2d(const float2* img, int vdim, int pf, const double* rot, int nR,
+                             const int* iCol, const int* iRow, int K, float* out, int ldo,
+                             long long splitLo, cudaStream_t st);
 // CTF attributes [nDraws][7] of insertion draws: the image's, defocus x nD[d]
 cudaError_t launch_draw_attr(const float* attr, const double* nD, int nDraws, int drawsPerImage,
                              float* out, cudaStream_t st);

@@ -503,6 +503,118 @@ __global__ void k_ctf_defocus(const float* __restrict__ defO, const float* __res
     }
 }
 
+// 2-D projection (2-D classification): the bilinear sample of a class's
+// half transform img [vdim][vdim/2 + 1] at the in-plane rotation (c, s) of
+// every pixel (iCol pf, iRow pf): x = i c - j s, y = i s + j c (the
+// reference's kernel_Project2D, gpu/src/Kernel.cu:786-819, reading as
+// Image::getByInterpolationFT, src/Image/Image.cpp:345-368: x < 0 at (-x, -y)
+// conjugated, rows wrapped).  Rows out [nR][ldo] as k_project writes them
+// (FP32 pairs, or split planes when splitLo != 0), zero beyond K.
+__global__ void k_project2d(const float2* __restrict__ img, int vdim, int pf,
+                            const double* __restrict__ rot, const int* __restrict__ iCol,
+                            const int* __restrict__ iRow, int K, float* __restrict__ out,
+                            int ldo, long long splitLo)
+{
+    const int r = blockIdx.y;
+    const float c = (float)rot[2 * (size_t)r], s = (float)rot[2 * (size_t)r + 1];
+    const int nx = vdim / 2 + 1;
+    const float fpf = (float)pf;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ldo / 2;
+         p += gridDim.x * blockDim.x) {
+        float re = 0.f, im = 0.f;
+        if (p < K) {
+            const float i = (float)iCol[p] * fpf, j = (float)iRow[p] * fpf;
+            float x = i * c - j * s, y = i * s + j * c;
+            const bool conj = x < 0.f;
+            if (conj) {
+                x = -x;
+                y = -y;
+            }
+            const float xf = floorf(x), yf = floorf(y);
+            const int x0 = (int)xf, y0 = (int)yf;
+            const float fx = x - xf, fy = y - yf;
+#pragma unroll
+            for (int b = 0; b < 2; b++) {
+                int yy = y0 + b;
+                yy = yy < 0 ? yy + vdim : yy;
+                const float wy = b ? fy : 1.f - fy;
+                const float2 v0 = __ldg(img + (size_t)yy * nx + x0);
+                const float2 v1 = __ldg(img + (size_t)yy * nx + x0 + 1);
+                re += wy * ((1.f - fx) * v0.x + fx * v1.x);
+                im += wy * ((1.f - fx) * v0.y + fx * v1.y);
+            }
+            if (conj) im = -im;
+        }
+        store_pair(out, splitLo, r, ldo, p, re, im);
+    }
+}
+
+// 2-D insertion (2-D classification; Reconstructor::insertP's 2-D form,
+// Image::addFT(value, iCol, iRow), src/Image/Image.cpp:370-386; the
+// reference's kernel_InsertF2D / T2D / O2D, gpu/src/Kernel.cu:2276-2470):
+// draw d (image d / drawsPerImage, class nC[d], in-plane rotation nR[d] =
+// (c, s), shift nT[d]) adds w ctf X shifted by -(t - offS) and w ctf^2
+// bilinearly at (c a - s b, s a + c b), (a, b) = (iCol pf, iRow pf), into its
+// class's (F.re, F.im, T, 0) accumulator [vdim][vdim/2 + 1] (x < 0: at
+// (-x, -y), conjugated); O2D[class] gets -R (t - offS), counter[class] + 1.
+// CTA (share of the pixels, draw).
+__global__ void __launch_bounds__(256)
+k_insert2d(float4* __restrict__ acc, int vdim, const float2* __restrict__ dat,
+           const float* __restrict__ ctf, int ctfPerDraw, const float* __restrict__ wgt,
+           const double* __restrict__ offS, const int* __restrict__ nC,
+           const double* __restrict__ nR, const double* __restrict__ nT,
+           const int* __restrict__ iCol, const int* __restrict__ iRow, int K, int pf, int idim,
+           int d0, int drawsPerImage, double* __restrict__ O2D, int* __restrict__ counter)
+{
+    const int d = d0 + blockIdx.y;
+    const int l = d / drawsPerImage;
+    const int k = nC[d];
+    const double cd = nR[2 * (size_t)d], sd = nR[2 * (size_t)d + 1];
+    const double dx = nT[2 * (size_t)d] - offS[2 * (size_t)l];
+    const double dy = nT[2 * (size_t)d + 1] - offS[2 * (size_t)l + 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (O2D) {
+            atomicAdd(O2D + 2 * k, -(cd * dx - sd * dy));
+            atomicAdd(O2D + 2 * k + 1, -(sd * dx + cd * dy));
+        }
+        if (counter) atomicAdd(counter + k, 1);
+    }
+    const int nx = vdim / 2 + 1;
+    float4* a4 = acc + (size_t)k * vdim * nx;
+    const float c = (float)cd, s = (float)sd, tx = (float)dx, ty = (float)dy, w = wgt[l];
+    const float invN = 1.0f / (float)idim, fpf = (float)pf;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K; p += gridDim.x * blockDim.x) {
+        const float2 X = dat[(size_t)l * K + p];
+        const float cv = ctf[(ctfPerDraw ? (size_t)d : (size_t)l) * K + p];
+        float sn, co;
+        sincospif(2.0f * (((float)iCol[p] * tx + (float)iRow[p] * ty) * invN), &sn, &co);
+        const float cw = cv * w;
+        float vr = (X.x * co - X.y * sn) * cw, vi = (X.x * sn + X.y * co) * cw;
+        const float vt = cv * cv * w;
+        const float a = (float)iCol[p] * fpf, b = (float)iRow[p] * fpf;
+        float x = c * a - s * b, y = s * a + c * b;
+        if (x < 0.f) {
+            x = -x;
+            y = -y;
+            vi = -vi;
+        }
+        const float xf = floorf(x), yf = floorf(y);
+        const int x0 = (int)xf, y0 = (int)yf;
+        const float fx = x - xf, fy = y - yf;
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            int yy = y0 + j;
+            yy = yy < 0 ? yy + vdim : yy;
+            const float wy = j ? fy : 1.f - fy;
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const float ww = (i ? fx : 1.f - fx) * wy;
+                atomicAdd(a4 + (size_t)yy * nx + x0 + i, make_float4(vr * ww, vi * ww, vt * ww, 0.f));
+            }
+        }
+    }
+}
+
 // CTF attributes of every insertion draw with the defocus search: the
 // image's attributes with defocusU, V scaled by the draw's factor nD (the
 // defocus kernel_CalculateCTF uses, gpu/src/Kernel.cu:2132-2198).
@@ -1622,6 +1734,32 @@ cudaError_t launch_norm_defocus(const float* P, long long splitLo, int nP, int n
     if (nD < 1 || nD > kMaxDefocus) return cudaErrorInvalidValue;
     k_norm_defocus<<<dim3(nP, (nR + 7) / 8), 256, 0, st>>>(P, splitLo, nP, nR, nD, K, Kp, sigRcp,
                                                            ctf, nrm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_project2d(const float2* img, int vdim, int pf, const double* rot, int nR,
+                             const int* iCol, const int* iRow, int K, float* out, int ldo,
+                             long long splitLo, cudaStream_t st)
+{
+    if (nR <= 0 || nR > 65535) return cudaErrorInvalidValue;
+    k_project2d<<<dim3((ldo / 2 + 255) / 256, nR), 256, 0, st>>>(img, vdim, pf, rot, iCol, iRow,
+                                                                K, out, ldo, splitLo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_insert2d(float4* acc, int vdim, const float2* dat, const float* ctf,
+                            int ctfPerDraw, const float* w, const double* offS, const int* nC,
+                            const double* nR, const double* nT, const int* iCol, const int* iRow,
+                            int K, int pf, int idim, int nDraws, int drawsPerImage, double* O2D,
+                            int* counter, cudaStream_t st)
+{
+    const int tiles = std::max(1, std::min(1024, (K + 255) / 256));
+    for (int d0 = 0; d0 < nDraws; d0 += 65535) {
+        const int n = std::min(65535, nDraws - d0);
+        k_insert2d<<<dim3(tiles, n), 256, 0, st>>>(acc, vdim, dat, ctf, ctfPerDraw, w, offS, nC, nR,
+                                                   nT, iCol, iRow, K, pf, idim, d0,
+                                                   drawsPerImage, O2D, counter);
+    }
     return cudaGetLastError();
 }
 

@@ -393,6 +393,36 @@ void ExpectGlobal3D(Complex* rotP, Complex* traP, Complex* datP, RFLOAT* ctfP, R
                           baseL, kIdx, nK, nR, nT, npxl, imgNum));
 }
 
+// gpu/interface/Interface.h:176-197.  vol holds the nK class images
+// [vdim][vdim/2 + 1] one after another.
+void ExpectGlobal2D(Complex* vol, Complex* datP, RFLOAT* ctfP, RFLOAT* sigRcpP, double* trans,
+                    RFLOAT* wC, RFLOAT* wR, RFLOAT* wT, double* pR, double* pT, double* rot,
+                    const int* iCol, const int* iRow, int nK, int nR, int nT, int pf, int interp,
+                    int idim, int vdim, int npxl, int imgNum)
+{
+    ok("ExpectGlobal2D",
+       tg3_ExpectGlobal2D(reinterpret_cast<const float*>(vol), reinterpret_cast<const float*>(datP),
+                          ctfP, sigRcpP, trans, wC, wR, wT, pR, pT, rot, iCol, iRow, nK, nR, nT,
+                          pf, interp, idim, vdim, npxl, imgNum));
+}
+
+// gpu/interface/Interface.h:239-266.  F2D / T2D hold the nk class
+// accumulators [vdim][vdim/2 + 1] one after another.
+void InsertI2D(Complex* F2D, RFLOAT* T2D, double* O2D, int* counter, MPI_Comm& hemi,
+               MPI_Comm& slav, Complex* datP, RFLOAT* ctfP, RFLOAT* sigRcpP, RFLOAT* w,
+               double* offS, int* nC, double* nR, double* nT, double* nD, CTFAttr* ctfaData,
+               const int* iCol, const int* iRow, RFLOAT pixelSize, bool cSearch, int nk, int opf,
+               int npxl, int mReco, int idim, int vdim, int imgNum)
+{
+    (void)hemi;
+    (void)slav;
+    ok("InsertI2D",
+       tg3_InsertI2D(reinterpret_cast<float*>(F2D), T2D, O2D, counter,
+                     reinterpret_cast<const float*>(datP), ctfP, sigRcpP, w, offS, nC, nR, nT, nD,
+                     reinterpret_cast<const float*>(ctfaData), iCol, iRow, pixelSize,
+                     cSearch ? 1 : 0, nk, opf, npxl, mReco, idim, vdim, imgNum));
+}
+
 // gpu/interface/Interface.h:294-318 (single-class form).  F3D is complex and
 // T3D is a complex Volume whose real parts hold T (Interface.cpp of the
 // reference converts it the same way around the call).

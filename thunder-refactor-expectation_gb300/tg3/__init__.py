@@ -36,6 +36,7 @@ EXPORTS = [
     "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose", "tg3_cnn_backward", "tg3_cnn_infer",
     "tg3_cnn_contrastive", "tg3_cnn_embed", "tg3_cnn_match_propose", "tg3_ctx_set_bank",
     "tg3_local_phase_bank_d", "tg3_local_phase_ctf_d", "tg3_ExpectLocal3D_ctf",
+    "tg3_ExpectGlobal2D", "tg3_global_scan2d_d", "tg3_InsertI2D",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
@@ -124,6 +125,9 @@ def lib():
                                        _P, _P], _I),
             "tg3_ctx_set_bank": ([_P, _I, _P, _I], _I),
             "tg3_local_phase_ctf_d": ([_P, _I, _I, _I, _I] + [_P] * 16 + [_I], _I),
+            "tg3_ExpectGlobal2D": ([_P] * 13 + [_I] * 9, _I),
+            "tg3_InsertI2D": ([_P] * 16 + [_F] + [_I] * 8, _I),
+            "tg3_global_scan2d_d": ([_P, _P, _I, _I, _I, _I, _I] + [_P] * 12 + [_I], _I),
             "tg3_ExpectLocal3D_ctf": ([_P, _P, _P, _P, _F, _F, _F, _F, _P, _P, _P, _I, _I, _P, _I,
                                        _P, _I, _P, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P],
                                       _I),
