@@ -528,6 +528,171 @@ def run_global(args, rank, world, local_rank):
     return res
 
 
+CLASS2D = dict(box=128, pixel_size=1.4, pf=2, rU=24, n_classes=16, n_blobs=80,
+               sigma_a=(1.5, 3.0), radius_px=40.0, nR=72, half_t=3, snr=0.1)
+
+
+def run_class2d(args, rank, world, local_rank):
+    """2-D classification's global search (ExpectGlobal2D, Optimiser's 2-D
+    expectation): 16 class images (box 128, padded 2x, central sections of
+    blob maps), 2,000 particles per step, 72 in-plane rotations (5 degrees)
+    x 49 translations (7 x 7, 1 px), cutoff 24 px; all classes scored in one
+    pass and merged, each particle's class read from the merged weights."""
+    import torch
+    import tg3
+    from tg3 import synth
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    W = CLASS2D
+    box, px, pf, n, nK, nR = W["box"], W["pixel_size"], W["pf"], args.global_particles, \
+        W["n_classes"], W["nR"]
+    rng = np.random.default_rng(rank_seed(3000, rank))
+    maps = [synth.blob_map(rng, W["n_blobs"], W["sigma_a"], px, W["radius_px"]) for _ in range(nK)]
+    imgs = synth.class_images_2d(maps, box, pf, device=dev)
+    iCol, iRow = synth.pixel_index(box, W["rU"], synth.config_rL(box, px))[:2]
+    K = len(iCol)
+    ang = np.arange(nR) * (2 * np.pi / nR)
+    rot_np = np.ascontiguousarray(np.stack([np.cos(ang), np.sin(ang)], 1))
+    trans_np = np.ascontiguousarray(synth.global_translations(W["half_t"], 1.0))
+    nT = len(trans_np)
+    rot, trans = torch.as_tensor(rot_np).to(dev), torch.as_tensor(trans_np).to(dev)
+    # particles: class, rotation and translation drawn from the grids, CTF, noise
+    kt = torch.as_tensor(rng.integers(0, nK, n)).to(dev)
+    rt, tt = rng.integers(0, nR, n), rng.integers(0, nT, n)
+    attr = synth.ctf_attrs(rng, n)
+    ctf_np = synth.ctf_values(attr, px, box, iCol, iRow).astype(np.float32)
+    clean = synth.sample_2d(imgs, kt, rot[torch.as_tensor(rt).to(dev)], iCol, iRow, pf)
+    clean = clean * torch.as_tensor(synth.phase_shift(trans_np[tt], box, iCol, iRow)).to(dev) \
+        .to(torch.complex64) * torch.as_tensor(ctf_np).to(dev)
+    s2 = float((clean.abs() ** 2).mean()) / W["snr"] / 2
+    gen = torch.Generator(device=dev).manual_seed(rank_seed(3001, rank))
+    noise = torch.complex(torch.randn(clean.shape, generator=gen, device=dev),
+                          torch.randn(clean.shape, generator=gen, device=dev)) * math.sqrt(s2)
+    dat = (clean + noise).contiguous()
+    ctf = torch.as_tensor(ctf_np).to(dev)
+    sig = torch.full((n, K), -1.0 / (2 * s2), dtype=torch.float32, device=dev)
+    pR = torch.full((nR,), 1.0 / nR, dtype=torch.float64, device=dev)
+    pT = torch.full((nT,), 1.0 / nT, dtype=torch.float64, device=dev)
+    o = dict(wC=torch.empty((n, nK), dtype=torch.float32, device=dev),
+             wR=torch.empty((n, nK, nR), dtype=torch.float32, device=dev),
+             wT=torch.empty((n, nK, nT), dtype=torch.float32, device=dev),
+             base=torch.empty(n, dtype=torch.float32, device=dev))
+    ctx = tg3.Context(local_rank)
+    ctx.set_pixels(iCol, iRow, box)
+    prec = tg3.SCORE_BF16X3 if args.precision == "bf16x3" else tg3.SCORE_FP32
+
+    def step(p=prec):
+        # every class in one pass, merged over the classes (ExpectGlobal2D's outputs)
+        ctx.global_scan2d_classes(imgs, pf, n, nR, nT, dat, ctf, sig, rot, trans, pR, pT,
+                                  o["wC"], o["wR"], o["wT"], o["base"], p)
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def timed(fn, steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier(world)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        barrier(world)
+        return reduce_max(world, e0.elapsed_time(e1)) / steps
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    clk = ClockSampler(local_rank)
+    clk.start()
+    ctx.set_timing(True)
+    ctx.stage_times(reset=True)
+    ms = timed(step, args.steps)
+    stages = ctx.stage_times(reset=True)
+    ctx.set_timing(False)
+    clocks = clk.stop()
+    # each particle's class: the one with the largest merged class weight
+    best = o["wC"].argmax(1)
+    recovered = float((best == kt).float().mean())
+    ms_fp32 = None
+    if prec != tg3.SCORE_FP32 and not args.no_compare:
+        step(tg3.SCORE_FP32)
+        ctx.sync()
+        ms_fp32 = timed(lambda: step(tg3.SCORE_FP32), max(3, args.steps // 4))
+    # end to end through the reference-shaped entry (ExpectGlobal2D; FP32
+    # scoring, host buffers, all classes in one pass per batch of 1,024):
+    # class images, particles and weights cross the host link every call
+    host = dict(vol=imgs.cpu().numpy(), dat=dat.cpu().numpy(), ctf=ctf_np,
+                sig=sig.cpu().numpy())
+    host = {k: np.ascontiguousarray(v) for k, v in host.items()}
+    wCh = np.zeros(n * nK, np.float32)
+    wRh = np.zeros(n * nK * nR, np.float32)
+    wTh = np.zeros(n * nK * nT, np.float32)
+    pRh, pTh = np.full(nR, 1.0 / nR), np.full(nT, 1.0 / nT)
+    ic, ir = np.ascontiguousarray(iCol, np.int32), np.ascontiguousarray(iRow, np.int32)
+
+    def e2e():
+        tg3.check(tg3.lib().tg3_ExpectGlobal2D(
+            tg3.ptr(host["vol"]), tg3.ptr(host["dat"]), tg3.ptr(host["ctf"]), tg3.ptr(host["sig"]),
+            tg3.ptr(trans_np), tg3.ptr(wCh), tg3.ptr(wRh), tg3.ptr(wTh), tg3.ptr(pRh),
+            tg3.ptr(pTh), tg3.ptr(rot_np), tg3.ptr(ic), tg3.ptr(ir), nK, nR, nT, pf, 1, box,
+            pf * box, K, n))
+
+    e2e()
+    barrier(world)
+    t0 = time.perf_counter()
+    e2e_steps = max(1, args.e2e_steps // 2)
+    for _ in range(e2e_steps):
+        e2e()
+    e2e_ms = reduce_max(world, (time.perf_counter() - t0) * 1e3) / e2e_steps
+    e2e_rec = float((wCh.reshape(n, nK).argmax(1) == kt.cpu().numpy()).mean())
+    # roofline of the scoring GEMM (the "cross" stage: 4 K FLOP per hypothesis)
+    cross = stages["cross"][0] / max(stages["cross"][1], 1)
+    flop = 4.0 * K * nK * nR * nT * n
+    hbm, bf16, kind = peaks()
+    achieved = flop / (cross * 1e-3) / 1e12
+    res = {"metric": "2-D classification global search particles/s, box 128, 16 classes x "
+                     "72 rotations x 49 translations, K=%d" % K,
+           "value": round(job_rate(n, ms, world), 1), "unit": UNIT, "ms_per_step": round(ms, 3),
+           "n_gpus": world, "scaling": "weak", "steps": args.steps, "warmup": args.warmup,
+           "higher_is_better": True, "dtype": "f32" if prec == tg3.SCORE_FP32 else "bf16x3",
+           "data": "synthetic: central sections of blob maps, CTF, Gaussian noise",
+           "config": {"workload": "class2d128", "particles": n, "classes": nK, "nR": nR,
+                      "nT": nT, "K": K, "l2": "inputs stay resident (scored once per class)"},
+           "precision": args.precision, "clocks": clocks,
+           "class_recovered": round(recovered, 4),
+           "hypotheses_per_s": round(job_rate(n * nK * nR * nT, ms, world), 1),
+           "fp32_value": None if ms_fp32 is None else round(job_rate(n, ms_fp32, world), 1),
+           "stages": {k: round(v[0] / max(v[1], 1), 4) for k, v in stages.items() if v[1]},
+           "roofline": {"bound": "tensor", "kernel": "cross-term GEMM",
+                        "achieved": round(achieved, 1), "peak": bf16, "unit": "TFLOP/s",
+                        "frac": round(achieved / bf16, 4), "peak_kind": kind, "traffic": None},
+           "e2e": {"value": round(job_rate(n, e2e_ms, world), 1), "unit": UNIT,
+                   "path": "tg3_ExpectGlobal2D, FP32 scoring, host buffers",
+                   "h2d_bytes_per_step": int(host["vol"].nbytes + host["dat"].nbytes +
+                                             host["ctf"].nbytes + host["sig"].nbytes),
+                   "d2h_bytes_per_step": int(wCh.nbytes + wRh.nbytes + wTh.nbytes),
+                   "class_recovered": round(e2e_rec, 4)}}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        m = 16
+        sel = np.arange(m)
+        rotP = O.project2d(host["vol"][0].astype(np.complex128), rot_np, iCol, iRow, pf)
+        traP = O.translate(trans_np, box, iCol, iRow)
+        t0 = time.perf_counter()
+        O.score_global(rotP, traP, host["dat"][sel].astype(np.complex128),
+                       host["ctf"][sel].astype(np.float64), host["sig"][sel].astype(np.float64),
+                       pRh, pTh, want_dvp=False)
+        secs = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": round(m / (secs * nK), 3), "unit": UNIT, "cores": 1,
+                               "kind": "port",
+                               "sample": f"{m} particles x 1 of {nK} classes (projection and "
+                                         f"shift banks precomputed), scaled to {nK} classes "
+                                         f"({secs:.2f} s measured); double-precision oracle, "
+                                         "one core"}
+    ctx.close()
+    return res
+
+
 UNEVEN = dict(box=192, pixel_size=1.3, n_blobs=150, sigma_a=(1.5, 3.0), radius_px=60.0,
               cutoffs=(40, 56, 72, 96), pf=2, shift=8.0, snr=0.03, kappa=200.0,
               nR=(200, 8000), nT=(9, 81))
@@ -1307,7 +1472,7 @@ def main():
     ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
     ap.add_argument("--workload", default="local256",
                     choices=["local256", "local256c3", "global64", "uneven192", "learned128",
-                             "learned256"])
+                             "learned256", "class2d128"])
     ap.add_argument("--train-particles", type=int, default=150000)
     ap.add_argument("--epochs", type=int, default=3)
     ap.add_argument("--learned-snr", type=float, default=1.0,
@@ -1333,6 +1498,8 @@ def main():
         res = run_global(args, rank, world, local)
     elif args.workload == "uneven192":
         res = run_uneven(args, rank, world, local)
+    elif args.workload == "class2d128":
+        res = run_class2d(args, rank, world, local)
     elif args.workload in ("learned128", "learned256"):
         res = run_learned(args, rank, world, local)
     else:

@@ -394,6 +394,19 @@ int tg3_global_scan2d_d(tg3_ctx* ctx, const float* img, int vdim, int pf, int nI
                         const double* pT, double* wC, double* wR, double* wT, double* baseL,
                         float* dvp, int precision);
 
+/* 2-D classification's global scan of nImg images against nK class images
+ * imgs (device, complex [nK][vdim][vdim/2 + 1]) at nR in-plane rotations
+ * rot [nR][2] = (cos, sin) x nT translations, every class in one pass (one
+ * shifted-data bank, one cross-term GEMM over all classes' rotations), the
+ * classes merged in order with the reference's running baseline, as
+ * ExpectGlobal2D returns them: wC [nImg][nK], wR [nImg][nK][nR],
+ * wT [nImg][nK][nT], baseL [nImg] (float, device). */
+int tg3_global_scan2d_classes_d(tg3_ctx* ctx, const float* imgs, int nK, int vdim, int pf,
+                                int nImg, int nR, int nT, const float* dat, const float* ctf,
+                                const float* sigRcp, const double* rot, const double* trans,
+                                const double* pR, const double* pT, float* wC, float* wR,
+                                float* wT, float* baseL, int precision);
+
 /* Global scan of nImg images over one shared set of nR rotations and nT
  * translations, for the context's class-`cls` volume: the scan of
  * Optimiser::doGlobalSearch (src/Optimiser.cpp:759-899), the work of

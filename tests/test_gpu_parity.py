@@ -855,3 +855,65 @@ def test_insert_i2d_host(csearch):
     np.testing.assert_allclose(O2D, Or, rtol=0, atol=1e-9)
     assert np.abs(F - Fr).max() < 2e-4 * np.abs(Fr).max()
     assert np.abs(T - Tr).max() < 2e-4 * np.abs(Tr).max()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16x3"])
+def test_global_scan2d_classes_device(precision):
+    """The multi-class device scan (every class's rotations as rows of one
+    projection matrix, one cross-term GEMM) against the oracle's class-by-class
+    scan with the running baseline: merged class weights and, for the best
+    class, its rotation weights; the best class and rotation exactly."""
+    rng = np.random.default_rng(101)
+    box, pf, px = 24, 2, 1.5
+    vdim = box * pf
+    iCol, iRow = synth.pixel_index(box, 10, synth.config_rL(box, px))[:2]
+    K = len(iCol)
+    nK, nR, nImg = 5, 36, 9
+    imgs = (rng.standard_normal((nK, vdim, vdim // 2 + 1)) +
+            1j * rng.standard_normal((nK, vdim, vdim // 2 + 1))).astype(np.complex64)
+    ang = np.arange(nR) * (2 * np.pi / nR)
+    rot = np.ascontiguousarray(np.stack([np.cos(ang), np.sin(ang)], 1))
+    trans = np.ascontiguousarray(synth.global_translations(1, 1.0))
+    nT = len(trans)
+    attr = synth.ctf_attrs(rng, nImg)
+    ctf = np.ascontiguousarray(synth.ctf_values(attr, px, box, iCol, iRow).astype(np.float32))
+    sig = np.full((nImg, K), -0.5, np.float32)
+    traP = O.translate(trans, box, iCol, iRow)
+    rotP = [O.project2d(imgs[k].astype(np.complex128), rot, iCol, iRow, pf) for k in range(nK)]
+    kt, rt, tt = rng.integers(0, nK, nImg), rng.integers(0, nR, nImg), rng.integers(0, nT, nImg)
+    dat = np.stack([ctf[l] * rotP[kt[l]][rt[l]] * traP[tt[l]] for l in range(nImg)])
+    dat = np.ascontiguousarray((dat + 0.3 * (rng.standard_normal(dat.shape) +
+                                             1j * rng.standard_normal(dat.shape))).astype(np.complex64))
+    pR = np.full(nR, 1.0 / nR)
+    pT = np.full(nT, 1.0 / nT)
+    dev = "cuda:0"
+    td = lambda x: torch.as_tensor(np.ascontiguousarray(x)).to(dev)
+    wC = torch.empty((nImg, nK), dtype=torch.float32, device=dev)
+    wR = torch.empty((nImg, nK, nR), dtype=torch.float32, device=dev)
+    wT = torch.empty((nImg, nK, nT), dtype=torch.float32, device=dev)
+    base = torch.empty(nImg, dtype=torch.float32, device=dev)
+    ctx = tg3.Context(0)
+    try:
+        ctx.set_pixels(iCol, iRow, box)
+        prec = tg3.SCORE_BF16X3 if precision == "bf16x3" else tg3.SCORE_FP32
+        ctx.global_scan2d_classes(td(imgs), pf, nImg, nR, nT, td(dat), td(ctf), td(sig), td(rot),
+                                  td(trans), td(pR), td(pT), wC, wR, wT, base, prec)
+        ctx.sync()
+    finally:
+        ctx.close()
+    state = None
+    for k in range(nK):
+        res = O.score_global(rotP[k], traP, f32(dat), f32(ctf), f32(sig), pR, pT, kIdx=k, nK=nK,
+                             state=state, want_dvp=False)
+        state = (res["wC"], res["wR"], res["wT"], res["baseL"])
+    rC, rR = state[0].reshape(nImg, nK), state[1].reshape(nImg, nK, nR)
+    gC, gR = wC.cpu().numpy(), wR.cpu().numpy()
+    np.testing.assert_allclose(base.cpu().numpy(), state[3], rtol=1e-3)
+    np.testing.assert_allclose(gC / gC.sum(1, keepdims=True), rC / rC.sum(1, keepdims=True),
+                               atol=2e-3)
+    for l in range(nImg):
+        k = int(np.argmax(rC[l]))
+        assert int(np.argmax(gC[l])) == k == kt[l]
+        assert int(np.argmax(gR[l, k])) == int(np.argmax(rR[l, k])) == rt[l]
+        np.testing.assert_allclose(gR[l, k] / gR[l, k].sum(), rR[l, k] / rR[l, k].sum(),
+                                   atol=2e-3)

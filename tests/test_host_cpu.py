@@ -98,6 +98,25 @@ def test_ctf_vectorised_matches_oracle():
                                O.ctf(attr, 1.5, 64, iCol, iRow), atol=1e-12)
 
 
+def test_2d_particle_generator_matches_oracle_projection():
+    """The benchmark's torch generator of 2-D particles samples the class
+    images as the oracle's 2-D projection does (bilinear, Friedel mirror,
+    wrapped rows)."""
+    import torch
+    rng = np.random.default_rng(5)
+    box, pf, px = 24, 2, 1.5
+    maps = [synth.blob_map(rng, 12, (1.5, 3.0), px, 8.0) for _ in range(2)]
+    imgs = synth.class_images_2d(maps, box, pf)
+    iCol, iRow = synth.pixel_index(box, 10, synth.config_rL(box, px))[:2]
+    ang = rng.uniform(0, 2 * np.pi, 5)
+    rot = np.stack([np.cos(ang), np.sin(ang)], 1)
+    k = np.array([0, 1, 1, 0, 1])
+    got = synth.sample_2d(imgs, torch.as_tensor(k), torch.as_tensor(rot), iCol, iRow, pf).numpy()
+    for r in range(5):
+        ref = O.project2d(imgs[k[r]].numpy().astype(np.complex128), rot[r:r + 1], iCol, iRow, pf)[0]
+        np.testing.assert_allclose(got[r], ref, rtol=0, atol=2e-5 * np.abs(ref).max())
+
+
 def test_blob_volume_is_hermitian_on_x0_plane():
     rng = np.random.default_rng(3)
     bm = synth.blob_map(rng, 5, (2.0, 4.0), 1.5, 5.0)

@@ -1460,7 +1460,11 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
                        int nImg, int nR, int nT, const float* dat, const float* ctf,
                        const float* sigRcp, const double* rotMat, const double* trans,
                        const double* pR, const double* pT, double* wC, double* wR, double* wT,
-                       double* baseL, float* dvp, int precision);
+                       double* baseL, float* dvp, int precision, int nK = 1,
+                       size_t imgStride = 0);
+static int merge_classes(tg3_ctx* c, int n, int nK, int nR, int nT, const double* wCd,
+                         const double* wRd, const double* wTd, const double* bd, float* wC,
+                         float* wR, float* wT, float* baseL);
 
 // 2-D classification's global search (ExpectGlobal2D,
 // gpu/interface/Interface.h:176-197; expectGlobal2D, gpu/src/cuthunder.cu:
@@ -1476,8 +1480,8 @@ extern "C" int tg3_ExpectGlobal2D(const float* vol, const float* datP, const flo
     if (!vol || !datP || !ctfP || !sigRcpP || !trans || !wC || !wR || !wT || !pR || !pT || !rot ||
         !iCol || !iRow)
         return fail(TG3_ERR_ARG, "null pointer");
-    if (nK <= 0 || nK > kMaxClasses || nR <= 0 || nT <= 0 || npxl <= 0 || imgNum <= 0 ||
-        pf < 1 || vdim < 4 || (vdim & 1) || nT > 2048)
+    if (nK <= 0 || nK > 6144 || nR <= 0 || nT <= 0 || npxl <= 0 || imgNum <= 0 || pf < 1 ||
+        vdim < 4 || (vdim & 1) || nT > 2048)
         return fail(TG3_ERR_ARG, "bad ExpectGlobal2D sizes");
     if (interp != 1) return fail(TG3_ERR_UNSUPPORTED, "only linear interpolation");
     int st = TG3_OK;
@@ -1494,8 +1498,10 @@ extern "C" int tg3_ExpectGlobal2D(const float* vol, const float* datP, const flo
            otr = ar.add(sizeof(double) * 2 * nT), opr = ar.add(sizeof(double) * nR),
            opt = ar.add(sizeof(double) * nT), od = ar.add(sizeof(float) * 2 * (size_t)nb * K),
            oc = ar.add(sizeof(float) * (size_t)nb * K), os = ar.add(sizeof(float) * (size_t)nb * K),
-           owc = ar.add(sizeof(double) * nb), owr = ar.add(sizeof(double) * (size_t)nb * nR),
-           owt = ar.add(sizeof(double) * (size_t)nb * nT), obs = ar.add(sizeof(double) * nb),
+           owc = ar.add(sizeof(double) * (size_t)nb * nK),
+           owr = ar.add(sizeof(double) * (size_t)nb * nK * nR),
+           owt = ar.add(sizeof(double) * (size_t)nb * nK * nT),
+           obs = ar.add(sizeof(double) * (size_t)nb * nK),
            oWC = ar.add(sizeof(float) * (size_t)nb * nK),
            oWR = ar.add(sizeof(float) * (size_t)nb * nK * nR),
            oWT = ar.add(sizeof(float) * (size_t)nb * nK * nT), oBL = ar.add(sizeof(float) * nb);
@@ -1514,20 +1520,19 @@ extern "C" int tg3_ExpectGlobal2D(const float* vol, const float* datP, const flo
                                  cudaMemcpyHostToDevice, s));
         TG3_CUDA(cudaMemcpyAsync(b + os, sigRcpP + (size_t)l0 * K, sizeof(float) * (size_t)n * K,
                                  cudaMemcpyHostToDevice, s));
-        for (int k = 0; k < nK; k++) {
-            st = global_scan(c, nullptr, (const float2*)(b + oim) + img * k, vdim, pf, n, nR, nT,
-                             (const float*)(b + od), (const float*)(b + oc), (const float*)(b + os),
-                             (const double*)(b + orot), (const double*)(b + otr),
-                             (const double*)(b + opr), (const double*)(b + opt), (double*)(b + owc),
-                             (double*)(b + owr), (double*)(b + owt), (double*)(b + obs), nullptr,
-                             TG3_SCORE_FP32);
-            if (st) return st;
-            TG3_CUDA(launch_merge_class(n, nK, k, nR, nT, (const double*)(b + owc),
-                                        (const double*)(b + owr), (const double*)(b + owt),
-                                        (const double*)(b + obs), (float*)(b + oWC),
-                                        (float*)(b + oWR), (float*)(b + oWT), (float*)(b + oBL),
-                                        s));
-        }
+        // every class in one scan: one shifted-data bank, one cross-term GEMM
+        st = global_scan(c, nullptr, (const float2*)(b + oim), vdim, pf, n, nR, nT,
+                         (const float*)(b + od), (const float*)(b + oc), (const float*)(b + os),
+                         (const double*)(b + orot), (const double*)(b + otr),
+                         (const double*)(b + opr), (const double*)(b + opt), (double*)(b + owc),
+                         (double*)(b + owr), (double*)(b + owt), (double*)(b + obs), nullptr,
+                         TG3_SCORE_FP32, nK, img);
+        if (st) return st;
+        if ((st = merge_classes(c, n, nK, nR, nT, (const double*)(b + owc),
+                                (const double*)(b + owr), (const double*)(b + owt),
+                                (const double*)(b + obs), (float*)(b + oWC), (float*)(b + oWR),
+                                (float*)(b + oWT), (float*)(b + oBL))))
+            return st;
         TG3_CUDA(cudaMemcpyAsync(wC + (size_t)l0 * nK, b + oWC, sizeof(float) * (size_t)n * nK,
                                  cudaMemcpyDeviceToHost, s));
         TG3_CUDA(cudaMemcpyAsync(wR + (size_t)l0 * nK * nR, b + oWR,
@@ -1766,14 +1771,24 @@ __global__ void k_abs2_from(const float* __restrict__ P, long long loOff, int K,
 // The global scan of one class.  The projections come from the class's 3-D
 // volume v at rotation matrices rot [nR][9], or (img2 != nullptr) from a 2-D
 // class image img2 [vdim][vdim/2 + 1] at in-plane rotations rot [nR][2].
+// The global scan of nImg images over nR rotations x nT translations.  With
+// nK > 1 (2-D classes only: img2 holds nK class images imgStride complex
+// values apart) every class's rotations are rows of one projection matrix,
+// so the shifted-data bank is built once and one cross-term GEMM serves all
+// classes; the weights are then per (image, class) block, each relative to
+// its own best hypothesis: wC / baseL [nImg][nK], wR [nImg][nK][nR],
+// wT [nImg][nK][nT], dvp [nImg][nK][nR][nT].
 static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim, int pf,
                        int nImg, int nR, int nT, const float* dat, const float* ctf,
                        const float* sigRcp, const double* rotMat, const double* trans,
                        const double* pR, const double* pT, double* wC, double* wR, double* wT,
-                       double* baseL, float* dvp, int precision)
+                       double* baseL, float* dvp, int precision, int nK, size_t imgStride)
 {
     int st = TG3_OK;
     if (nImg <= 0 || nR <= 0 || nT <= 0 || nT > 2048) return fail(TG3_ERR_ARG, "bad scan shape");
+    if (nK < 1 || (nK > 1 && !img2) || (long long)nK * nR > (1LL << 20))
+        return fail(TG3_ERR_ARG, "bad class count");
+    const int nRt = nK * nR;     // projected rows
     if (!dat || !ctf || !sigRcp || !rotMat || !trans || !pR || !pT || !wC || !wR || !wT || !baseL)
         return fail(TG3_ERR_ARG, "null device pointer");
     if (precision != TG3_SCORE_FP32 && precision != TG3_SCORE_BF16X3)
@@ -1784,41 +1799,54 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
     if ((st = check_weights_shape(nR, nT))) return st;
     const int K = c->px.K, Kp = c->px.Kp, Kq = (int)round_up(K, 64);
     // images per pass: keep the likelihood block within 4 GiB
-    long long ib = (4LL << 30) / (4LL * nR * nT);
+    long long ib = (4LL << 30) / (4LL * nRt * nT);
     const int IB = (int)std::max(1LL, std::min(std::min((long long)nImg, ib), 65535LL));
     // workspace
-    float* P = (float*)ws_get(c, WS_P, 4 * (size_t)nR * Kp, &st);
+    float* P = (float*)ws_get(c, WS_P, 4 * (size_t)nRt * Kp, &st);
     if (!P) return st;
     float* A = (float*)ws_get(c, WS_A, 4 * (size_t)IB * nT * Kp, &st);
     if (!A) return st;
-    float* D = (float*)ws_get(c, WS_D, 4 * (size_t)IB * nR * nT, &st);
+    float* D = (float*)ws_get(c, WS_D, 4 * (size_t)IB * nRt * nT, &st);
     if (!D) return st;
-    float* nrmG = (float*)ws_get(c, WS_NRM, 4 * (size_t)nR * IB, &st);
+    float* nrmG = (float*)ws_get(c, WS_NRM, 4 * (size_t)nRt * IB, &st);
     if (!nrmG) return st;
     double* x0 = (double*)ws_get(c, WS_X0, 8 * (size_t)nImg, &st);
     if (!x0) return st;
     Arena ar(c, WS_MISC);
-    const size_t oAbs = ar.add(4 * (size_t)nR * Kq), oBank = ar.add(8 * (size_t)nT * K),
-                 oSc = ar.add(4 * (size_t)IB * Kq);
+    const size_t oAbs = ar.add(4 * (size_t)nRt * Kq), oBank = ar.add(8 * (size_t)nT * K),
+                 oSc = ar.add(4 * (size_t)IB * Kq),
+                 oNc = ar.add(nK > 1 ? 4 * (size_t)nRt * IB : 0),
+                 oX0 = ar.add(nK > 1 ? 8 * (size_t)IB * nK : 0);
     char* m = (char*)ws_get(c, WS_MISC, ar.used, &st);
     if (!m) return st;
     float* abs2 = (float*)(m + oAbs);
     float2* bank = (float2*)(m + oBank);
     float* sc2 = (float*)(m + oSc);
-    float* pscr = (float*)ws_get(c, WS_PROJ, sizeof(float) * project_scratch_floats(nR, Kp), &st);
-    if (!pscr) return st;
+    float* nrmC = (float*)(m + oNc);
+    double* x0r = (double*)(m + oX0);
+    float* pscr = img2 ? nullptr
+                       : (float*)ws_get(c, WS_PROJ, sizeof(float) * project_scratch_floats(nR, Kp),
+                                        &st);
+    if (!img2 && !pscr) return st;
     cudaStream_t s = c->stream;
-    const long long splitP = split ? (long long)nR * Kp : 0;
+    const long long splitP = split ? (long long)nRt * Kp : 0;
     {
         StageTimer tm(c, TG3_STAGE_PROJECT);
-        if (img2)
-            TG3_CUDA(launch_project2d(img2, vdim, pf, rotMat, nR, c->px.iCol, c->px.iRow, K, P, Kp,
-                                      splitP, s));
-        else
+        if (img2) {
+            for (int k = 0; k < nK; k++) {
+                // class k's rows start k nR rows in (bf16 rows in the split layout)
+                const size_t off = (size_t)k * nR * Kp;
+                float* Pk = split ? reinterpret_cast<float*>(reinterpret_cast<__nv_bfloat16*>(P) + off)
+                                  : P + off;
+                TG3_CUDA(launch_project2d(img2 + (size_t)k * imgStride, vdim, pf, rotMat, nR,
+                                          c->px.iCol, c->px.iRow, K, Pk, Kp, splitP, s));
+            }
+        } else {
             TG3_CUDA(launch_project(nullptr, nullptr, v->blocks, v->vdim, v->pf, nullptr, rotMat,
                                     nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, nullptr, nullptr,
                                     nullptr, pscr, c->d_flag, splitP, s));
-        k_abs2_from<<<nR, 256, 0, s>>>(P, splitP, K, Kp, abs2, Kq);
+        }
+        k_abs2_from<<<nRt, 256, 0, s>>>(P, splitP, K, Kp, abs2, Kq);
         TG3_LAUNCH_CHECK("projection norms");
     }
     TG3_CUDA(launch_translate(trans, nT, c->px.idim, c->px.iCol, c->px.iRow, K, bank, K, s));
@@ -1839,26 +1867,40 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
         {
             StageTimer tm(c, TG3_STAGE_CROSS);
             // per-(rotation, image) norm, then the cross term
-            TG3_CUDA(launch_gemm_nt_fp32(abs2, 0, Kq, sc2, 0, Kq, nR, n, Kq, 1, nrmG, 0, n, nullptr,
-                                         0, 1.0f, s));
+            TG3_CUDA(launch_gemm_nt_fp32(abs2, 0, Kq, sc2, 0, Kq, nRt, n, Kq, 1, nrmG, 0, n,
+                                         nullptr, 0, 1.0f, s));
             // the cross term is written image-major: D[l][r][t]
             const int cols = n * nT;
             if (split) {
                 const int Nt = std::min(256, (cols + 15) / 16 * 16);
                 const int items = (cols + Nt - 1) / Nt;
-                TG3_CUDA(launch_gemm_bf16x3(P, nR, A, (long long)cols, nR, Nt, Kp, items, 0, Nt,
+                TG3_CUDA(launch_gemm_bf16x3(P, nRt, A, (long long)cols, nRt, Nt, Kp, items, 0, Nt,
                                             cols, D, 0, nT, nullptr, 0, -2.0f, c->d_flag, s, nT,
-                                            (long long)nR * nT));
+                                            (long long)nRt * nT));
             } else {
-                TG3_CUDA(launch_gemm_nt_fp32(P, 0, Kp, A, 0, Kp, nR, cols, Kp, 1, D, 0, nT, nullptr,
-                                             0, -2.0f, s, nT, (long long)nR * nT));
+                TG3_CUDA(launch_gemm_nt_fp32(P, 0, Kp, A, 0, Kp, nRt, cols, Kp, 1, D, 0, nT,
+                                             nullptr, 0, -2.0f, s, nT, (long long)nRt * nT));
             }
         }
         {
             StageTimer tm(c, TG3_STAGE_WEIGHTS);
-            TG3_CUDA(launch_weights(D, (long long)nR * nT, nT, nR, nT, 1, n, nrmG, n, x0 + l0, pR, 0, pT, 0,
-                                    nullptr, wC + l0, wR + (size_t)l0 * nR, wT + (size_t)l0 * nT,
-                                    baseL + l0, dvp ? dvp + (size_t)l0 * nR * nT : nullptr, s));
+            if (nK == 1) {
+                TG3_CUDA(launch_weights(D, (long long)nR * nT, nT, nR, nT, 1, n, nrmG, n, x0 + l0,
+                                        pR, 0, pT, 0, nullptr, wC + l0, wR + (size_t)l0 * nR,
+                                        wT + (size_t)l0 * nT, baseL + l0,
+                                        dvp ? dvp + (size_t)l0 * nR * nT : nullptr, s));
+            } else {
+                // one block per (image, class): D[l][k nR + r][t] is block l nK + k
+                const size_t b0 = (size_t)l0 * nK;
+                TG3_CUDA(launch_nrm_classes(nrmG, nK, nR, n, nrmC, s));
+                TG3_CUDA(launch_repeat_rows(x0 + l0, n, 1, nK, x0r, s));
+                // many small blocks: 4 warps each when a class has few rotations
+                TG3_CUDA(launch_weights(D, (long long)nR * nT, nT, nR, nT, 1, n * nK, nrmC, n * nK,
+                                        x0r, pR, 0, pT, 0, nullptr, wC + b0, wR + b0 * nR,
+                                        wT + b0 * nT, baseL + b0,
+                                        dvp ? dvp + b0 * nR * nT : nullptr, s,
+                                        nR < 128 ? 128 : (nR < 256 ? 256 : 512)));
+            }
         }
     }
     return TG3_OK;
@@ -1890,4 +1932,45 @@ extern "C" int tg3_global_scan2d_d(tg3_ctx* c, const float* img, int vdim, int p
     if (!img || vdim < 4 || (vdim & 1) || pf < 1) return fail(TG3_ERR_ARG, "bad class image");
     return global_scan(c, nullptr, reinterpret_cast<const float2*>(img), vdim, pf, nImg, nR, nT,
                        dat, ctf, sigRcp, rot, trans, pR, pT, wC, wR, wT, baseL, dvp, precision);
+}
+
+// Per-(image, class) weights of a multi-class scan merged over the classes
+// to the value the reference's running baseline (kernel_setBaseLine /
+// kernel_UpdateW) reaches; the outputs in the ExpectGlobal2D layout.
+static int merge_classes(tg3_ctx* c, int n, int nK, int nR, int nT, const double* wCd,
+                         const double* wRd, const double* wTd, const double* bd, float* wC,
+                         float* wR, float* wT, float* baseL)
+{
+    TG3_CUDA(launch_merge_classes(n, nK, nR, nT, wCd, wRd, wTd, bd, wC, wR, wT, baseL,
+                                  c->stream));
+    return TG3_OK;
+}
+
+extern "C" int tg3_global_scan2d_classes_d(tg3_ctx* c, const float* imgs, int nK, int vdim,
+                                           int pf, int nImg, int nR, int nT, const float* dat,
+                                           const float* ctf, const float* sigRcp,
+                                           const double* rot, const double* trans,
+                                           const double* pR, const double* pT, float* wC,
+                                           float* wR, float* wT, float* baseL, int precision)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (!imgs || nK < 1 || nK > 6144 || vdim < 4 || (vdim & 1) || pf < 1)
+        return fail(TG3_ERR_ARG, "bad class images");
+    if (!wC || !wR || !wT || !baseL) return fail(TG3_ERR_ARG, "null device pointer");
+    if (nImg <= 0 || nR <= 0 || nT <= 0) return fail(TG3_ERR_ARG, "bad scan shape");
+    const size_t blocks = (size_t)nImg * nK;
+    Arena ar(c, WS_CLASSES);
+    const size_t oC = ar.add(8 * blocks), oR = ar.add(8 * blocks * nR),
+                 oT = ar.add(8 * blocks * nT), oB = ar.add(8 * blocks);
+    char* b = (char*)ws_get(c, WS_CLASSES, ar.used, &st);
+    if (!b) return st;
+    double *wCd = (double*)(b + oC), *wRd = (double*)(b + oR), *wTd = (double*)(b + oT),
+           *bd = (double*)(b + oB);
+    const size_t img = (size_t)vdim * (vdim / 2 + 1);
+    st = global_scan(c, nullptr, reinterpret_cast<const float2*>(imgs), vdim, pf, nImg, nR, nT,
+                     dat, ctf, sigRcp, rot, trans, pR, pT, wCd, wRd, wTd, bd, nullptr, precision,
+                     nK, img);
+    if (st) return st;
+    return merge_classes(c, nImg, nK, nR, nT, wCd, wRd, wTd, bd, wC, wR, wT, baseL);
 }

@@ -84,6 +84,7 @@ enum WsSlot {
     WS_MISC,
     WS_INSERT,       // insertion: per-draw pixel grids and rotations
     WS_DEFOCUS,      // defocus search: block priors, block weights
+    WS_CLASSES,      // multi-class 2-D scan: per-(image, class) weights
     WS_COUNT
 };
 
@@ -277,7 +278,7 @@ cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR,
                            const double* pwR, long long sR, const double* pwT,
                            long long sT, const double* pwC, double* wC,
                            double* wR, double* wT, double* base, float* dvp,
-                           cudaStream_t st);
+                           cudaStream_t st, int threads = 512);
 cudaError_t launch_resample(int nP, int n, const double* u, const double* w,
                             const int* perm, const double* u0,
                             const double* peak, int nOut, int* src,
@@ -352,6 +353,16 @@ cudaError_t launch_merge_class(int nImg, int nK, int kIdx, int nR, int nT,
                                const double* wCn, const double* wRn,
                                const double* wTn, const double* basen,
                                float* wC, float* wR, float* wT, float* baseL,
+                               cudaStream_t st, int inStride = 1);
+// Per-(image, class) weights wCn / basen [nImg][nK], wRn [nImg][nK][nR],
+// wTn [nImg][nK][nT] merged over the classes into ExpectGlobal2D's float
+// outputs relative to each image's best class (nK <= 6144)
+cudaError_t launch_merge_classes(int nImg, int nK, int nR, int nT, const double* wCn,
+                                 const double* wRn, const double* wTn, const double* basen,
+                                 float* wC, float* wR, float* wT, float* baseL, cudaStream_t st);
+// Row norms of a multi-class scan regrouped per (image, class) block:
+// out[r][l nK + k] = nrm[(k nR + r) n + l]
+cudaError_t launch_nrm_classes(const float* nrm, int nK, int nR, int n, float* out,
                                cudaStream_t st);
 
 // Split-bf16 tensor-core cross term (tcgen05), when available.

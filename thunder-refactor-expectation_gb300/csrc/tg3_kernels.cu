@@ -399,6 +399,10 @@ __global__ void k_norm_reduce(const float* __restrict__ nrmPart, int rows, int n
 // + iRow ty) / N), the conjugate of sigRcp ctf_d conj(X) S_t, so that
 // Re sum_p sigRcp ctf_d conj(X) S_t P = sum over the 2K floats of A'' . P.
 // nD CTFs per particle (ctf [nP][nD][K]; one without a defocus search).
+// CTA: (particle l, CTF d) x SHIFT_T translations; a thread loads its
+// pixels' data, sigRcp and CTF once and writes them for every translation.
+constexpr int SHIFT_T = 8;
+
 __global__ void k_shift_bank(const float2* __restrict__ dat, const float* __restrict__ ctf,
                              const float* __restrict__ sigRcp,
                              const double* __restrict__ trans, const float2* __restrict__ bank,
@@ -406,33 +410,44 @@ __global__ void k_shift_bank(const float2* __restrict__ dat, const float* __rest
                              const int* __restrict__ iCol, const int* __restrict__ iRow,
                              int K, float* __restrict__ out, int ldo, long long splitLo)
 {
-    const int row = blockIdx.x;           // (l nD + d) nT + t
-    const int t = row % nT;
-    const int ld = row / nT;              // l nD + d
+    const int ld = blockIdx.x;            // l nD + d
     const int l = ld / nD;
-    const size_t lt = (size_t)l * nT + t;
-    const float tx = bank ? 0.f : (float)trans[2 * lt];
-    const float ty = bank ? 0.f : (float)trans[2 * lt + 1];
+    const int t0 = blockIdx.y * SHIFT_T;
+    const int t1 = min(nT, t0 + SHIFT_T);
     const float invN = 1.0f / (float)idim;
     for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x) {
-        float2 v = make_float2(0.f, 0.f);
+        float sc = 0.f;
+        float2 X = make_float2(0.f, 0.f);
+        float fc = 0.f, fr = 0.f;
         if (p < K) {
             const size_t i = (size_t)l * K + p;
-            const float sc = sigRcp[i] * ctf[(size_t)ld * K + p];
-            const float2 X = dat[i];
-            float s, c;
-            if (bank) {
-                // shared phase bank S[t][p] = (cos, -sin): use conj(S)
-                const float2 S = bank[(size_t)t * K + p];
-                c = S.x;
-                s = -S.y;
-            } else {
-                float f = ((float)iCol[p] * tx + (float)iRow[p] * ty) * invN;
-                sincospif(2.0f * f, &s, &c);
+            sc = sigRcp[i] * ctf[(size_t)ld * K + p];
+            X = dat[i];
+            if (!bank) {
+                fc = (float)iCol[p];
+                fr = (float)iRow[p];
             }
-            v = make_float2(sc * (X.x * c - X.y * s), sc * (X.x * s + X.y * c));
         }
-        store_pair(out, splitLo, row, ldo, p, v.x, v.y);
+        for (int t = t0; t < t1; t++) {
+            const size_t row = (size_t)ld * nT + t;     // (l nD + d) nT + t
+            float2 v = make_float2(0.f, 0.f);
+            if (p < K) {
+                float s, c;
+                if (bank) {
+                    // shared phase bank S[t][p] = (cos, -sin): use conj(S)
+                    const float2 S = bank[(size_t)t * K + p];
+                    c = S.x;
+                    s = -S.y;
+                } else {
+                    const size_t lt = (size_t)l * nT + t;
+                    const float tx = (float)trans[2 * lt], ty = (float)trans[2 * lt + 1];
+                    float f = (fc * tx + fr * ty) * invN;
+                    sincospif(2.0f * f, &s, &c);
+                }
+                v = make_float2(sc * (X.x * c - X.y * s), sc * (X.x * s + X.y * c));
+            }
+            store_pair(out, splitLo, row, ldo, p, v.x, v.y);
+        }
     }
 }
 
@@ -810,6 +825,9 @@ k_gemm_nt_fp32(const float* __restrict__ A, long long sA, int lda,
 // with shuffles, and keeps its share of wT in registers (TS slots of 32
 // translations; TS == 0: shared-memory atomics for long rows).  FP32
 // accumulation, as in the reference GPU path; totals are combined in FP64.
+// Callers with many small blocks (the multi-class scan) may launch fewer
+// warps, so that the per-warp fixed work -- reductions, loop set-up -- is
+// spread over more rows; the warp count sets the order of the wT sums.
 constexpr int WEIGHTS_THREADS = 512;
 
 template <int TS>
@@ -957,14 +975,18 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
 // layout: wC [img][nK], wR [img][nK][nR], wT [img][nK][nT] relative to baseL
 // (kernel_setBaseLine / kernel_UpdateW of the reference GPU path, with the
 // CPU scan's rescale rule, src/Optimiser.cpp:835-898).
+// The class's inputs of image l are wCn[l s], wRn[l s nR + r], wTn[l s nT + t],
+// basen[l s], s = inStride (1: one class's arrays; nK: a class's column of
+// per-(image, class) arrays).
 __global__ void k_merge_class(int nK, int kIdx, int nR, int nT,
                               const double* __restrict__ wCn, const double* __restrict__ wRn,
                               const double* __restrict__ wTn, const double* __restrict__ basen,
                               float* __restrict__ wC, float* __restrict__ wR,
-                              float* __restrict__ wT, float* __restrict__ baseL)
+                              float* __restrict__ wT, float* __restrict__ baseL, int inStride)
 {
     const int l = blockIdx.x;
-    const double bn = basen[l];
+    const size_t li = (size_t)l * inStride;
+    const double bn = basen[li];
     double scaleOld = 0.0, scaleNew = 1.0, newBase = bn;
     if (kIdx > 0) {
         const double bo = baseL[l];
@@ -984,11 +1006,11 @@ __global__ void k_merge_class(int nK, int kIdx, int nR, int nT,
             continue;
         }
         if (cur) {
-            if (threadIdx.x == 0) wC[(size_t)l * nK + k] = (float)(wCn[l] * scaleNew);
+            if (threadIdx.x == 0) wC[(size_t)l * nK + k] = (float)(wCn[li] * scaleNew);
             for (int r = threadIdx.x; r < nR; r += blockDim.x)
-                wR[((size_t)l * nK + k) * nR + r] = (float)(wRn[(size_t)l * nR + r] * scaleNew);
+                wR[((size_t)l * nK + k) * nR + r] = (float)(wRn[li * nR + r] * scaleNew);
             for (int t = threadIdx.x; t < nT; t += blockDim.x)
-                wT[((size_t)l * nK + k) * nT + t] = (float)(wTn[(size_t)l * nT + t] * scaleNew);
+                wT[((size_t)l * nK + k) * nT + t] = (float)(wTn[li * nT + t] * scaleNew);
         } else if (scaleOld != 1.0) {
             if (threadIdx.x == 0) wC[(size_t)l * nK + k] = (float)(wC[(size_t)l * nK + k] * scaleOld);
             for (int r = threadIdx.x; r < nR; r += blockDim.x)
@@ -1720,8 +1742,8 @@ cudaError_t launch_shift_bank(const float2* dat, const float* ctf, const float* 
                               int idim, const int* iCol, const int* iRow, int K, float* out,
                               int ldo, long long splitLo, cudaStream_t st, int nD)
 {
-    if (nD < 1) return cudaErrorInvalidValue;
-    dim3 grid(nP * nD * nT);
+    if (nD < 1 || nT < 1) return cudaErrorInvalidValue;
+    dim3 grid((unsigned)nP * nD, (nT + SHIFT_T - 1) / SHIFT_T);
     k_shift_bank<<<grid, 256, 0, st>>>(dat, ctf, sigRcp, trans, bank, nT, nD, idim, iCol, iRow,
                                         K, out, ldo, splitLo);
     return cudaGetLastError();
@@ -1822,13 +1844,15 @@ cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR, int nT
                            const double* pwR,
                            long long sR, const double* pwT, long long sT, const double* pwC,
                            double* wC, double* wR, double* wT, double* base, float* dvp,
-                           cudaStream_t st)
+                           cudaStream_t st, int threads)
 {
-    const size_t smem = sizeof(float) * (2 + (nT <= 256 ? WEIGHTS_THREADS / 32 : 0)) * (size_t)nT;
+    if (threads != 128 && threads != 256 && threads != WEIGHTS_THREADS)
+        return cudaErrorInvalidValue;
+    const size_t smem = sizeof(float) * (2 + (nT <= 256 ? threads / 32 : 0)) * (size_t)nT;
     if (smem > 48 * 1024) return cudaErrorInvalidValue;
 #define TG3_WEIGHTS(TS)                                                                        \
-    k_weights<TS><<<nBlocks, WEIGHTS_THREADS, smem, st>>>(D, sD, ldc, nR, nT, G, nrmG, nrmRS, x0, pwR, \
-                                                          sR, pwT, sT, pwC, wC, wR, wT, base, dvp)
+    k_weights<TS><<<nBlocks, threads, smem, st>>>(D, sD, ldc, nR, nT, G, nrmG, nrmRS, x0, pwR, \
+                                                  sR, pwT, sT, pwC, wC, wR, wT, base, dvp)
     if (nT <= 32) TG3_WEIGHTS(1);
     else if (nT <= 64) TG3_WEIGHTS(2);
     else if (nT <= 128) TG3_WEIGHTS(4);
@@ -1840,10 +1864,77 @@ cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR, int nT
 
 cudaError_t launch_merge_class(int nImg, int nK, int kIdx, int nR, int nT, const double* wCn,
                                const double* wRn, const double* wTn, const double* basen,
-                               float* wC, float* wR, float* wT, float* baseL, cudaStream_t st)
+                               float* wC, float* wR, float* wT, float* baseL, cudaStream_t st,
+                               int inStride)
 {
     k_merge_class<<<nImg, 256, 0, st>>>(nK, kIdx, nR, nT, wCn, wRn, wTn, basen, wC, wR, wT,
-                                         baseL);
+                                         baseL, inStride);
+    return cudaGetLastError();
+}
+
+// All nK per-(image, class) weight blocks of a multi-class scan folded into
+// ExpectGlobal2D's outputs in one pass: relative to the image's best class,
+// class k scaled by exp(base_k - max_k base_k) -- the value the running
+// baseline of kernel_setBaseLine / kernel_UpdateW reaches class by class.
+// One CTA per image; smem: nK doubles.
+__global__ void k_merge_classes(int nK, int nR, int nT, const double* __restrict__ wCn,
+                                const double* __restrict__ wRn, const double* __restrict__ wTn,
+                                const double* __restrict__ basen, float* __restrict__ wC,
+                                float* __restrict__ wR, float* __restrict__ wT,
+                                float* __restrict__ baseL)
+{
+    extern __shared__ double esc[];
+    __shared__ double Bm;
+    const size_t l = blockIdx.x;
+    const double* bl = basen + l * nK;
+    if (threadIdx.x == 0) {
+        double m = bl[0];
+        for (int k = 1; k < nK; k++) m = fmax(m, bl[k]);
+        Bm = m;
+        baseL[l] = (float)m;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nK; k += blockDim.x) {
+        esc[k] = exp(bl[k] - Bm);
+        wC[l * nK + k] = (float)(wCn[l * nK + k] * esc[k]);
+    }
+    __syncthreads();
+    const size_t oR = l * nK * nR, oT = l * nK * nT;
+    for (int i = threadIdx.x; i < nK * nR; i += blockDim.x)
+        wR[oR + i] = (float)(wRn[oR + i] * esc[i / nR]);
+    for (int i = threadIdx.x; i < nK * nT; i += blockDim.x)
+        wT[oT + i] = (float)(wTn[oT + i] * esc[i / nT]);
+}
+
+cudaError_t launch_merge_classes(int nImg, int nK, int nR, int nT, const double* wCn,
+                                 const double* wRn, const double* wTn, const double* basen,
+                                 float* wC, float* wR, float* wT, float* baseL, cudaStream_t st)
+{
+    const size_t smem = sizeof(double) * (size_t)nK;
+    if (smem > 48 * 1024) return cudaErrorInvalidValue;
+    k_merge_classes<<<nImg, 256, smem, st>>>(nK, nR, nT, wCn, wRn, wTn, basen, wC, wR, wT, baseL);
+    return cudaGetLastError();
+}
+
+__global__ void k_nrm_classes(const float* __restrict__ nrm, int nK, int nR, int n,
+                              float* __restrict__ out)
+{
+    const size_t total = (size_t)nK * nR * n;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+        // i walks the output: i = r (n nK) + l nK + k
+        const int k = (int)(i % nK);
+        const size_t rl = i / nK;
+        const int l = (int)(rl % n);
+        const int r = (int)(rl / n);
+        out[i] = nrm[((size_t)k * nR + r) * n + l];
+    }
+}
+
+cudaError_t launch_nrm_classes(const float* nrm, int nK, int nR, int n, float* out,
+                               cudaStream_t st)
+{
+    k_nrm_classes<<<grid_for((size_t)nK * nR * n, 256), 256, 0, st>>>(nrm, nK, nR, n, out);
     return cudaGetLastError();
 }
 

@@ -36,7 +36,7 @@ EXPORTS = [
     "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose", "tg3_cnn_backward", "tg3_cnn_infer",
     "tg3_cnn_contrastive", "tg3_cnn_embed", "tg3_cnn_match_propose", "tg3_ctx_set_bank",
     "tg3_local_phase_bank_d", "tg3_local_phase_ctf_d", "tg3_ExpectLocal3D_ctf",
-    "tg3_ExpectGlobal2D", "tg3_global_scan2d_d", "tg3_InsertI2D",
+    "tg3_ExpectGlobal2D", "tg3_global_scan2d_d", "tg3_InsertI2D", "tg3_global_scan2d_classes_d",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
@@ -127,6 +127,7 @@ def lib():
             "tg3_local_phase_ctf_d": ([_P, _I, _I, _I, _I] + [_P] * 16 + [_I], _I),
             "tg3_ExpectGlobal2D": ([_P] * 13 + [_I] * 9, _I),
             "tg3_InsertI2D": ([_P] * 16 + [_F] + [_I] * 8, _I),
+            "tg3_global_scan2d_classes_d": ([_P, _P] + [_I] * 6 + [_P] * 11 + [_I], _I),
             "tg3_global_scan2d_d": ([_P, _P, _I, _I, _I, _I, _I] + [_P] * 12 + [_I], _I),
             "tg3_ExpectLocal3D_ctf": ([_P, _P, _P, _P, _F, _F, _F, _F, _P, _P, _P, _I, _I, _P, _I,
                                        _P, _I, _P, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P],
@@ -298,6 +299,27 @@ class Context:
         check(lib().tg3_global_scan_d(self.h, cls, nImg, nR, nT, ptr(dat), ptr(ctf), ptr(sig),
                                       ptr(rotmat), ptr(trans), ptr(pR), ptr(pT), ptr(wC),
                                       ptr(wR), ptr(wT), ptr(base), ptr(dvp), precision))
+
+    def global_scan2d(self, img, pf, nImg, nR, nT, dat, ctf, sig, rot, trans, pR, pT,
+                      wC, wR, wT, base, dvp=None, precision=SCORE_FP32):
+        """Global scan against one 2-D class image img (device, complex
+        [vdim][vdim/2 + 1]) at in-plane rotations rot [nR][2] = (cos, sin)."""
+        self._hold(img, dat, ctf, sig, rot, trans, pR, pT, wC, wR, wT, base, dvp)
+        check(lib().tg3_global_scan2d_d(self.h, ptr(img), img.shape[-2], pf, nImg, nR, nT,
+                                        ptr(dat), ptr(ctf), ptr(sig), ptr(rot), ptr(trans),
+                                        ptr(pR), ptr(pT), ptr(wC), ptr(wR), ptr(wT), ptr(base),
+                                        ptr(dvp), precision))
+
+    def global_scan2d_classes(self, imgs, pf, nImg, nR, nT, dat, ctf, sig, rot, trans, pR, pT,
+                              wC, wR, wT, base, precision=SCORE_FP32):
+        """Global scan against every 2-D class image imgs (device, complex
+        [nK][vdim][vdim/2 + 1]) in one pass, merged over the classes: wC
+        [nImg][nK], wR [nImg][nK][nR], wT [nImg][nK][nT], base [nImg] (float32)."""
+        self._hold(imgs, dat, ctf, sig, rot, trans, pR, pT, wC, wR, wT, base)
+        check(lib().tg3_global_scan2d_classes_d(self.h, ptr(imgs), imgs.shape[0], imgs.shape[-2],
+                                                pf, nImg, nR, nT, ptr(dat), ptr(ctf), ptr(sig),
+                                                ptr(rot), ptr(trans), ptr(pR), ptr(pT), ptr(wC),
+                                                ptr(wR), ptr(wT), ptr(base), precision))
 
     def resample(self, nP, n, u, w, perm, u0, peak, nOut, src, wOut, top):
         self._hold(u, w, perm, u0, peak, src, wOut, top)

@@ -263,6 +263,48 @@ def padded_volume(bm: BlobMap, box: int, pf: int, device="cpu",
     return out
 
 
+def class_images_2d(maps, box: int, pf: int, device="cpu") -> torch.Tensor:
+    """2-D class images: the transform of each map's projection along z (its
+    central section) on the padded half grid, complex64 (nK, vdim, vdim//2 + 1),
+    indexed [k, y, x]."""
+    vdim = pf * box
+    nx = vdim // 2 + 1
+    y = torch.arange(vdim, device=device)
+    y = torch.where(y < vdim // 2, y, y - vdim).to(torch.float64)
+    x = torch.arange(nx, device=device, dtype=torch.float64)
+    f = torch.stack([x[None, :].expand(vdim, nx), y[:, None].expand(vdim, nx),
+                     torch.zeros(vdim, nx, dtype=torch.float64, device=device)], -1) / vdim
+    return torch.stack([blob_ft(bm, f) for bm in maps]).to(torch.complex64)
+
+
+def sample_2d(imgs: torch.Tensor, k: torch.Tensor, rot: torch.Tensor, iCol, iRow, pf: int):
+    """Bilinear samples of class images imgs (nK, vdim, nx) at the in-plane
+    rotations rot (n, 2) = (cos, sin) of the padded pixels (iCol pf, iRow pf),
+    class k (n,) per row; a point with x < 0 reads (-x, -y) conjugated and
+    rows wrap: (n, K) complex64."""
+    nK, vdim, nx = imgs.shape
+    dev = imgs.device
+    a = torch.as_tensor(np.asarray(iCol) * pf, dtype=torch.float32, device=dev)[None, :]
+    b = torch.as_tensor(np.asarray(iRow) * pf, dtype=torch.float32, device=dev)[None, :]
+    c, s = rot[:, 0:1].float(), rot[:, 1:2].float()
+    x, y = c * a - s * b, s * a + c * b
+    neg = x < 0
+    x, y = torch.where(neg, -x, x), torch.where(neg, -y, y)
+    x0, y0 = torch.floor(x), torch.floor(y)
+    fx, fy = x - x0, y - y0
+    x0, y0 = x0.long(), y0.long()
+    flat = imgs.reshape(nK, -1)
+    out = torch.zeros(x.shape, dtype=torch.complex64, device=dev)
+    for j in (0, 1):
+        yy = torch.remainder(y0 + j, vdim)
+        wy = fy if j else 1 - fy
+        for i in (0, 1):
+            wx = fx if i else 1 - fx
+            v = flat[k[:, None], yy * nx + x0 + i]
+            out = out + v * (wx * wy)
+    return torch.where(neg, out.conj(), out)
+
+
 # --------------------------------------------------------------------------
 # CTF
 # --------------------------------------------------------------------------
