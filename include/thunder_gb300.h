@@ -394,6 +394,44 @@ int tg3_global_scan2d_d(tg3_ctx* ctx, const float* img, int vdim, int pf, int nI
                         const double* pT, double* wC, double* wR, double* wT, double* baseL,
                         float* dvp, int precision);
 
+/* ----------------------------------------------------------- input data --
+ * Image preprocessing (Optimiser::initImg, src/Optimiser.cpp:4600-4760, and
+ * allocPreCal, :7995-8030): nImg real-space images img [nImg][N][N]
+ * (device, file order, x fastest) to the complex pixel data dat [nImg][K]
+ * of the context's pixel set (made for idim = N).  Per image: background
+ * (i^2 + j^2 > r^2 about pixel (N/2, N/2), r = maskRadiusPx) mean and
+ * standard deviation subtracted and divided; with mask, the raised-cosine
+ * soft mask of edge 6 pixels to 0 (zeroMask); scaled by 1 / stdN (stdN > 0
+ * given, else the batch mean of the normalised background deviations);
+ * unnormalised forward transform with the centre at index 0; the pixels
+ * gathered.  stats (device, may be NULL): [nImg][3] float background mean,
+ * deviation, and normalised deviation. */
+int tg3_prepare_images_d(tg3_ctx* ctx, const float* img, int nImg, int N, float maskRadiusPx,
+                         int mask, float stdN, float* dat, float* stats);
+
+/* MRC stacks (src/Image/ImageFile.cpp): header fields, and sections
+ * [first, first + count) as float32 in file order (modes 0, 1, 2, 6).
+ * pixelSize (may be NULL) = cella[0] / mx.  Writing: float32 (mode 2) with
+ * the header of ImageFile::fillMRCHeader; volume != 0 scales the z cell by
+ * the pixel size.  Host pointers. */
+int tg3_mrc_info(const char* path, int* nx, int* ny, int* nz, int* mode, float* pixelSize);
+int tg3_mrc_read(const char* path, int first, int count, float* out);
+int tg3_mrc_write(const char* path, const float* data, int nx, int ny, int nz, float pixelSize,
+                  int volume);
+
+/* .thu particle databases (src/Database.cpp; include/Database.h columns
+ * THU_VOLTAGE = 0 ... THU_SCORE = 26): tg3_thu_count gives the particle
+ * (non-blank line) count; tg3_thu_read fills cols [n][27] (double; the two
+ * path columns 7 and 8 hold NaN) and the particle and micrograph paths as n
+ * NUL-terminated strings of `stride` bytes (either may be NULL).
+ * tg3_thu_write writes Optimiser::saveDatabase's format (src/Optimiser.cpp:
+ * 8221-8262): %18.9f reals, %6d group and class ids. */
+int tg3_thu_count(const char* path, int* n);
+int tg3_thu_read(const char* path, int n, double* cols, char* paths, char* micrographs,
+                 int stride);
+int tg3_thu_write(const char* path, int n, const double* cols, const char* paths,
+                  const char* micrographs, int stride);
+
 /* 2-D classification's global scan of nImg images against nK class images
  * imgs (device, complex [nK][vdim][vdim/2 + 1]) at nR in-plane rotations
  * rot [nR][2] = (cos, sin) x nT translations, every class in one pass (one

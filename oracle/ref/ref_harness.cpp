@@ -12,7 +12,9 @@
 
 #include <boost/bind.hpp>
 
+#include "ImageFile.h"
 #include "Logging.h"
+#include "Mask.h"
 #include "Precision.h"
 #include "Functions.h"
 #include "TabFunction.h"
@@ -140,6 +142,41 @@ void ref_insert2d(double* F, double* T, int vdim, const double* img, const doubl
     }
     memcpy(F, &IF[0], sizeof(Complex) * IF.sizeFT());
     for (size_t i = 0; i < IT.sizeFT(); i++) T[i] = REAL(IT[i]);
+}
+
+/* ImageFile::readMetaData + readImage(dst, iSlc), src/Image/ImageFile.cpp:
+ * 209-290: section iSlc of an MRC stack in the reference's in-memory layout
+ * (the file's centre pixel at index 0).  Returns non-zero on a size mismatch. */
+int ref_read_mrc(const char* path, int iSlc, int N, double* out)
+{
+    ImageFile imf(path, "rb");
+    imf.readMetaData();
+    Image img;
+    imf.readImage(img, iSlc);
+    if (img.nColRL() != N || img.nRowRL() != N) return 1;
+    for (size_t i = 0; i < img.sizeRL(); i++) out[i] = img.iGetRL(i);
+    return 0;
+}
+
+/* One image through Optimiser::substractBgImg (bgMeanStddev), statImg's
+ * bgStddev about 0 and maskImg with zeroMask (softMask to 0, edge
+ * EDGE_WIDTH_RL), src/Optimiser.cpp:4796-4985; in / out in the in-memory
+ * layout; stats = (background mean, deviation, normalised deviation). */
+void ref_prep_image(const double* in, int N, double r, int mask, double* out, double* stats)
+{
+    Image img(N, N, RL_SPACE);
+    for (size_t i = 0; i < img.sizeRL(); i++) img(i) = in[i];
+    RFLOAT m, s;
+    bgMeanStddev(m, s, img, r);
+    for (size_t i = 0; i < img.sizeRL(); i++) {
+        img(i) -= m;
+        img(i) /= s;
+    }
+    stats[0] = m;
+    stats[1] = s;
+    stats[2] = bgStddev(0, img, r);
+    if (mask) softMask(img, img, (RFLOAT)r, (RFLOAT)EDGE_WIDTH_RL, (RFLOAT)0, 1u);
+    for (size_t i = 0; i < img.sizeRL(); i++) out[i] = img(i);
 }
 
 /* translate(Complex*, nTransCol, nTransRow, nCol, nRow, iCol, iRow, nPxl,

@@ -1,0 +1,66 @@
+"""Image preprocessing on the GPU (tg3_prepare_images_d) against the oracle's
+restatement of the reference's chain (oracle/preprocess.py, pinned to the
+compiled reference on the CPU): background normalisation, zero soft mask,
+1 / stdN, transform of the centred image, pixel gather.  Inputs are read
+from an MRC stack written and read by the library."""
+import numpy as np
+import pytest
+import torch
+
+import tg3
+from oracle import preprocess as PP
+from tg3 import io, synth
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+def _stack(rng, n, N):
+    c = np.arange(N) - N // 2
+    i, j = np.meshgrid(c, c)
+    out = []
+    for _ in range(n):
+        img = 2.0 + 0.5 * rng.standard_normal((N, N))
+        for _ in range(6):
+            x0, y0 = rng.uniform(-N / 6, N / 6, 2)
+            img += rng.uniform(1, 3) * np.exp(-((i - x0) ** 2 + (j - y0) ** 2) /
+                                              (2 * rng.uniform(2, 4) ** 2))
+        out.append(img)
+    return np.stack(out).astype(np.float32)
+
+
+@pytest.mark.parametrize("mask,std_n", [(1, 0.0), (0, 0.0), (1, 1.3)])
+def test_prepare_images_matches_oracle(tmp_path, mask, std_n):
+    rng = np.random.default_rng(40 + mask)
+    N, n, r = 64, 37, 24.5
+    io.write_mrc(tmp_path / "p.mrcs", _stack(rng, n, N), pixel_size=1.5)
+    imgs = io.read_mrc(tmp_path / "p.mrcs")
+    iCol, iRow = synth.pixel_index(N, 20, synth.config_rL(N, 1.5))[:2]
+    K = len(iCol)
+    ctx = tg3.Context(0)
+    try:
+        ctx.set_pixels(iCol, iRow, N)
+        dat = torch.empty((n, K), dtype=torch.complex64, device=DEV)
+        stats = torch.empty((n, 3), dtype=torch.float32, device=DEV)
+        ctx.prepare_images(torch.as_tensor(imgs).to(DEV), r, dat, mask=bool(mask), std_n=std_n,
+                           stats=stats)
+        ctx.sync()
+    finally:
+        ctx.close()
+    ref, st, _ = PP.preprocess(imgs, r, iCol, iRow, mask=bool(mask), std_n=std_n or None)
+    got = dat.cpu().numpy()
+    assert np.abs(got - ref).max() < 2e-5 * np.abs(ref).max()
+    np.testing.assert_allclose(stats.cpu().numpy(), st, rtol=2e-6)
+
+
+def test_prepare_images_rejects_mismatched_pixel_set():
+    ctx = tg3.Context(0)
+    try:
+        iCol, iRow = synth.pixel_index(32, 10, 1)[:2]
+        ctx.set_pixels(iCol, iRow, 32)
+        img = torch.zeros((2, 64, 64), dtype=torch.float32, device=DEV)
+        dat = torch.empty((2, len(iCol)), dtype=torch.complex64, device=DEV)
+        with pytest.raises(tg3.TG3Error):
+            ctx.prepare_images(img, 20.0, dat)
+    finally:
+        ctx.close()

@@ -308,6 +308,7 @@ extern "C" int tg3_ctx_destroy(tg3_ctx* c)
     if (!c) return TG3_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    prep_release(c);
     for (auto& v : c->vol) cudaFree(v.blocks);
     for (auto& b : c->ws) cudaFree(b.ptr);
     cudaFree(c->pxMain.iCol);

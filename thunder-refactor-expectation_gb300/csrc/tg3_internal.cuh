@@ -85,6 +85,7 @@ enum WsSlot {
     WS_INSERT,       // insertion: per-draw pixel grids and rotations
     WS_DEFOCUS,      // defocus search: block priors, block weights
     WS_CLASSES,      // multi-class 2-D scan: per-(image, class) weights
+    WS_PREP,         // image preprocessing: statistics, real and transformed images
     WS_COUNT
 };
 
@@ -424,4 +425,6 @@ cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, lo
 namespace tg3 {
 // Makes the context's device current; TG3_ERR_ARG for a null context.
 int check_ctx(tg3_ctx* c);
+// releases the context's preprocessing FFT plans
+void prep_release(tg3_ctx* c);
 }  // namespace tg3

@@ -1,0 +1,245 @@
+// Image preprocessing ahead of the expectation: real-space particle images
+// to the complex pixel data the scoring kernels read (Optimiser::initImg,
+// src/Optimiser.cpp:4600-4760, and allocPreCal, src/Optimiser.cpp:7995-8030).
+// With r = maskRadius / pixelSize and centred coordinates (i, j), i, j in
+// [-N/2, N/2) about the file's pixel (N/2, N/2):
+//   substractBgImg (:4917): the mean m and standard deviation s (n - 1) of
+//     the pixels with i^2 + j^2 > r^2 (bgMeanStddev, src/Image/
+//     ImageFunctions.cpp:607-620); y = (x - m) / s;
+//   statImg (:4796): stdN = the mean over the images of the same region's
+//     standard deviation of y about 0 (bgStddev, ImageFunctions.cpp:585-596);
+//   maskImg (:4953, zeroMask): y (u < r), y (1 - w) for r <= u <= r + 6 with
+//     w = 0.5 - 0.5 cos((u - r) / 6 pi), 0 beyond (softMask, src/Functions/
+//     Mask.cpp:363-385; EDGE_WIDTH_RL = 6); u = sqrt(i^2 + j^2);
+//   normaliseImg (:4987): y / stdN;
+//   fwImg (:5003): unnormalised forward r2c transform of the image with its
+//     centre at index 0 (ImageFile's MESH_IMAGE_INDEX layout);
+//   allocPreCal: dat[l][p] = FT at (iCol[p], iRow[p] mod N).
+// The unmasked form (the reference's _imgOri) skips the mask.  The noise-
+// filled mask of the non-zeroMask option draws from the reference's GSL
+// random stream and is not offered.
+#include <cufft.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "tg3_internal.cuh"
+
+namespace tg3 {
+namespace {
+
+__device__ double prep_block_sum(double v, double* scratch)
+{
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) scratch[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double r = lane < nw ? scratch[lane] : 0.0;
+        for (int o = 16; o; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+        if (lane == 0) scratch[0] = r;
+    }
+    __syncthreads();
+    return scratch[0];
+}
+
+// Per-image background statistics, FP64 sums: stats[l] = (m, s, sN) with sN
+// the background standard deviation of (x - m) / s about 0.  CTA per image.
+__global__ void __launch_bounds__(256)
+k_bg_stats(const float* __restrict__ img, int N, double r2, double* __restrict__ st)
+{
+    __shared__ double red[32];
+    const size_t l = blockIdx.x;
+    const float* im = img + l * N * N;
+    const int half = N / 2;
+    double s = 0.0, cnt = 0.0;
+    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+        const int i = q % N - half, j = q / N - half;
+        if ((double)(i * i + j * j) > r2) {
+            s += im[q];
+            cnt += 1.0;
+        }
+    }
+    s = prep_block_sum(s, red);
+    cnt = prep_block_sum(cnt, red);
+    const double m = s / cnt;
+    double ss = 0.0;
+    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+        const int i = q % N - half, j = q / N - half;
+        if ((double)(i * i + j * j) > r2) {
+            const double d = im[q] - m;
+            ss += d * d;
+        }
+    }
+    ss = prep_block_sum(ss, red);
+    const double sd = sqrt(ss / (cnt - 1.0));
+    // the normalised background's deviation about 0, from the same values
+    double sn = 0.0;
+    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+        const int i = q % N - half, j = q / N - half;
+        if ((double)(i * i + j * j) > r2) {
+            const double y = (im[q] - m) / sd;
+            sn += y * y;
+        }
+    }
+    sn = prep_block_sum(sn, red);
+    if (threadIdx.x == 0) {
+        st[3 * l] = m;
+        st[3 * l + 1] = sd;
+        st[3 * l + 2] = sqrt(sn / (cnt - 1.0));
+    }
+}
+
+__global__ void k_stats_f32(const double* __restrict__ st, int n, float* __restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * n; i += gridDim.x * blockDim.x)
+        out[i] = (float)st[i];
+}
+
+// stdN: the given value, or the mean of the images' sN.
+__global__ void k_stdn(const double* __restrict__ st, int n, float given, double* __restrict__ out)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int l = threadIdx.x; l < n; l += blockDim.x) s += st[3 * (size_t)l + 2];
+    s = prep_block_sum(s, red);
+    if (threadIdx.x == 0) out[0] = given > 0.f ? (double)given : s / n;
+}
+
+// Normalise, mask and scale one image, written with its centre at index 0.
+__global__ void k_prep_image(const float* __restrict__ img, int N, float r, float ew, int mask,
+                             const double* __restrict__ st, const double* __restrict__ stdN,
+                             float* __restrict__ out)
+{
+    const size_t l = blockIdx.y;
+    const float m = (float)st[3 * l], sd = (float)st[3 * l + 1];
+    const float scale = (float)(1.0 / stdN[0]);
+    const int half = N / 2;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N * N; q += gridDim.x * blockDim.x) {
+        const int x = q % N, y = q / N;
+        const int i = x - half, j = y - half;
+        float v = (img[l * N * N + q] - m) / sd;
+        if (mask) {
+            const float u = sqrtf((float)(i * i + j * j));
+            if (u > r + ew)
+                v = 0.f;
+            else if (u >= r) {
+                const float w = 0.5f - 0.5f * cospif((u - r) / ew);
+                v = v * (1.f - w);
+            }
+        }
+        const int ci = i < 0 ? i + N : i, cj = j < 0 ? j + N : j;
+        out[l * N * N + (size_t)cj * N + ci] = v * scale;
+    }
+}
+
+// dat[l][p] = FT[l][iRow mod N][iCol]
+__global__ void k_gather_pixels(const float2* __restrict__ ft, int N, const int* __restrict__ iCol,
+                                const int* __restrict__ iRow, int K, float2* __restrict__ dat)
+{
+    const size_t l = blockIdx.y;
+    const int nx = N / 2 + 1;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K; p += gridDim.x * blockDim.x) {
+        const int row = iRow[p] < 0 ? iRow[p] + N : iRow[p];
+        dat[l * K + p] = ft[(l * N + row) * nx + iCol[p]];
+    }
+}
+
+// batched r2c plans, one per (context, size, batch), kept until the context goes
+struct Plan {
+    tg3_ctx* c;
+    int N, batch;
+    cufftHandle h;
+};
+std::vector<Plan> g_plans;
+std::mutex g_planLock;
+
+int get_plan(tg3_ctx* c, int N, int batch, cufftHandle* out)
+{
+    std::lock_guard<std::mutex> g(g_planLock);
+    for (auto& p : g_plans)
+        if (p.c == c && p.N == N && p.batch == batch) {
+            *out = p.h;
+            return TG3_OK;
+        }
+    cufftHandle h;
+    int n[2] = {N, N};
+    if (cufftPlanMany(&h, 2, n, nullptr, 1, N * N, nullptr, 1, N * (N / 2 + 1), CUFFT_R2C,
+                      batch) != CUFFT_SUCCESS)
+        return fail(TG3_ERR_CUDA, "cuFFT plan creation failed");
+    g_plans.push_back({c, N, batch, h});
+    *out = h;
+    return TG3_OK;
+}
+
+}  // namespace
+
+void prep_release(tg3_ctx* c)
+{
+    std::lock_guard<std::mutex> g(g_planLock);
+    for (size_t i = 0; i < g_plans.size();) {
+        if (g_plans[i].c == c) {
+            cufftDestroy(g_plans[i].h);
+            g_plans.erase(g_plans.begin() + i);
+        } else {
+            i++;
+        }
+    }
+}
+
+}  // namespace tg3
+
+using namespace tg3;
+
+extern "C" int tg3_prepare_images_d(tg3_ctx* c, const float* img, int nImg, int N,
+                                    float maskRadiusPx, int mask, float stdN, float* dat,
+                                    float* stats)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (!img || !dat || nImg <= 0 || N < 4 || (N & 1) || !(maskRadiusPx > 0))
+        return fail(TG3_ERR_ARG, "bad preprocessing arguments");
+    if (!c->px.iCol || c->px.idim != N)
+        return fail(TG3_ERR_STATE, "the active pixel set was not made for this image size");
+    if (maskRadiusPx >= N / 2 * 1.4142135f)
+        return fail(TG3_ERR_ARG, "mask radius leaves no background pixels");
+    const int K = c->px.K;
+    const int IB = std::min(nImg, 2048);
+    const size_t img2 = (size_t)N * N, ft2 = (size_t)N * (N / 2 + 1);
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t oSt = 0, oN = up(sizeof(double) * 3 * (size_t)nImg), oR = oN + 256,
+                 oF = up(oR + sizeof(float) * img2 * IB), total = oF + sizeof(float2) * ft2 * IB;
+    char* b = (char*)ws_get(c, WS_PREP, total, &st);
+    if (!b) return st;
+    double* stv = (double*)(b + oSt);
+    double* sN = (double*)(b + oN);
+    float* real = (float*)(b + oR);
+    cufftComplex* ft = (cufftComplex*)(b + oF);
+    cudaStream_t s = c->stream;
+    const float r = maskRadiusPx;
+    k_bg_stats<<<nImg, 256, 0, s>>>(img, N, (double)r * (double)r, stv);
+    TG3_LAUNCH_CHECK("background statistics");
+    k_stdn<<<1, 256, 0, s>>>(stv, nImg, stdN, sN);
+    TG3_LAUNCH_CHECK("noise level");
+    for (int l0 = 0; l0 < nImg; l0 += IB) {
+        const int n = std::min(IB, nImg - l0);
+        k_prep_image<<<dim3((unsigned)std::min<size_t>(64, (img2 + 255) / 256), n), 256, 0, s>>>(
+            img + (size_t)l0 * img2, N, r, 6.0f, mask, stv + 3 * (size_t)l0, sN, real);
+        TG3_LAUNCH_CHECK("normalise and mask");
+        cufftHandle h;
+        if ((st = get_plan(c, N, n, &h))) return st;
+        if (cufftSetStream(h, s) != CUFFT_SUCCESS || cufftExecR2C(h, real, ft) != CUFFT_SUCCESS)
+            return fail(TG3_ERR_CUDA, "cuFFT forward transform failed");
+        k_gather_pixels<<<dim3((K + 255) / 256, n), 256, 0, s>>>(
+            reinterpret_cast<const float2*>(ft), N, c->px.iCol, c->px.iRow, K,
+            reinterpret_cast<float2*>(dat) + (size_t)l0 * K);
+        TG3_LAUNCH_CHECK("pixel gather");
+    }
+    if (stats) {
+        k_stats_f32<<<(3 * nImg + 255) / 256, 256, 0, s>>>(stv, nImg, stats);
+        TG3_LAUNCH_CHECK("statistics");
+    }
+    return TG3_OK;
+}

@@ -37,6 +37,8 @@ EXPORTS = [
     "tg3_cnn_contrastive", "tg3_cnn_embed", "tg3_cnn_match_propose", "tg3_ctx_set_bank",
     "tg3_local_phase_bank_d", "tg3_local_phase_ctf_d", "tg3_ExpectLocal3D_ctf",
     "tg3_ExpectGlobal2D", "tg3_global_scan2d_d", "tg3_InsertI2D", "tg3_global_scan2d_classes_d",
+    "tg3_prepare_images_d", "tg3_mrc_info", "tg3_mrc_read", "tg3_mrc_write", "tg3_thu_count",
+    "tg3_thu_read", "tg3_thu_write",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
@@ -128,6 +130,13 @@ def lib():
             "tg3_ExpectGlobal2D": ([_P] * 13 + [_I] * 9, _I),
             "tg3_InsertI2D": ([_P] * 16 + [_F] + [_I] * 8, _I),
             "tg3_global_scan2d_classes_d": ([_P, _P] + [_I] * 6 + [_P] * 11 + [_I], _I),
+            "tg3_prepare_images_d": ([_P, _P, _I, _I, _F, _I, _F, _P, _P], _I),
+            "tg3_mrc_info": ([ctypes.c_char_p] + [_P] * 5, _I),
+            "tg3_mrc_read": ([ctypes.c_char_p, _I, _I, _P], _I),
+            "tg3_mrc_write": ([ctypes.c_char_p, _P, _I, _I, _I, _F, _I], _I),
+            "tg3_thu_count": ([ctypes.c_char_p, _P], _I),
+            "tg3_thu_read": ([ctypes.c_char_p, _I, _P, _P, _P, _I], _I),
+            "tg3_thu_write": ([ctypes.c_char_p, _I, _P, _P, _P, _I], _I),
             "tg3_global_scan2d_d": ([_P, _P, _I, _I, _I, _I, _I] + [_P] * 12 + [_I], _I),
             "tg3_ExpectLocal3D_ctf": ([_P, _P, _P, _P, _F, _F, _F, _F, _P, _P, _P, _I, _I, _P, _I,
                                        _P, _I, _P, _I, _P, _P, _P, _D, _P, _P, _P, _P, _P, _P],
@@ -320,6 +329,14 @@ class Context:
                                                 pf, nImg, nR, nT, ptr(dat), ptr(ctf), ptr(sig),
                                                 ptr(rot), ptr(trans), ptr(pR), ptr(pT), ptr(wC),
                                                 ptr(wR), ptr(wT), ptr(base), precision))
+
+    def prepare_images(self, img, mask_radius_px, dat, mask=True, std_n=0.0, stats=None):
+        """Real-space images img (device float32 (n, N, N), file order) to the
+        pixel data dat (device complex64 (n, K)) of the active pixel set."""
+        n, N = img.shape[0], img.shape[-1]
+        self._hold(img, dat, stats)
+        check(lib().tg3_prepare_images_d(self.h, ptr(img), n, N, float(mask_radius_px),
+                                         int(bool(mask)), float(std_n), ptr(dat), ptr(stats)))
 
     def resample(self, nP, n, u, w, perm, u0, peak, nOut, src, wOut, top):
         self._hold(u, w, perm, u0, peak, src, wOut, top)

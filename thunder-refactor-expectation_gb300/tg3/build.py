@@ -19,7 +19,7 @@ OUT_DIR = PKG / "_build"
 LIB = PKG / "libtg3.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["tg3_kernels.cu", "tg3_api.cu", "tg3_tc.cu", "tg3_fused.cu", "tg3_ragged.cu",
-           "tg3_cnn.cu", "tg3_conv_tc.cu", "tg3_noalloc.cu"]
+           "tg3_cnn.cu", "tg3_conv_tc.cu", "tg3_noalloc.cu", "tg3_io.cpp", "tg3_prep.cu"]
 
 
 def nvcc() -> str:
@@ -66,7 +66,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         list(ex.map(run, jobs))
     objs = [str(OUT_DIR / (Path(s).stem + ".o")) for s in SOURCES]
     if force or jobs or not LIB.exists():
-        run([cc, *ARCH, "-shared", "-o", str(LIB), *objs, "-lcudart"])
+        run([cc, *ARCH, "-shared", "-o", str(LIB), *objs, "-lcudart", "-lcufft"])
     return LIB
 
 
