@@ -693,6 +693,112 @@ def run_class2d(args, rank, world, local_rank):
     return res
 
 
+def run_prep(args, rank, world, local_rank):
+    """Input preprocessing of box-256 particle images (Optimiser::initImg and
+    allocPreCal): 4,096 real-space images per step to the pixel data of the
+    production cutoff (K = 9,930): background normalisation, zero soft mask
+    (radius 100 px), transform, gather.  e2e: the MRC stack read from a file
+    by the library, copied in, preprocessed and the pixel data copied out."""
+    import tempfile
+    import torch
+    import tg3
+    from tg3 import io, synth
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    N, n, r, px = 256, 4096, 100.0, 1.1
+    rng = np.random.default_rng(rank_seed(4000, rank))
+    c = np.arange(N) - N // 2
+    ii, jj = np.meshgrid(c, c)
+    gen = torch.Generator(device=dev).manual_seed(rank_seed(4001, rank))
+    imgs = 2.0 + torch.randn((n, N, N), generator=gen, device=dev)
+    blob = torch.as_tensor(np.exp(-(ii ** 2 + jj ** 2) / (2 * 30.0 ** 2)), dtype=torch.float32,
+                           device=dev)
+    imgs += 3.0 * blob
+    iCol, iRow = synth.pixel_index(N, 80, synth.config_rL(N, px))[:2]
+    K = len(iCol)
+    ctx = tg3.Context(local_rank)
+    ctx.set_pixels(iCol, iRow, N)
+    dat = torch.empty((n, K), dtype=torch.complex64, device=dev)
+
+    def step():
+        ctx.prepare_images(imgs, r, dat, mask=True)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    clk = ClockSampler(local_rank)
+    clk.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    barrier(world)
+    clocks = clk.stop()
+    ms = reduce_max(world, e0.elapsed_time(e1)) / args.steps
+    # algorithmic bytes: every image read once, its pixel data written once
+    alg = n * (N * N * 4 + K * 8)
+    hbm, bf16, kind = peaks()
+    achieved = alg / (ms * 1e-3) / 1e9
+    # end to end: an MRC stack of 512 images on local disk through the library
+    m = 512
+    host = imgs[:m].cpu().numpy()
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "particles.mrcs")
+        io.write_mrc(path, host, pixel_size=px)
+        pin = torch.empty((m, N, N), dtype=torch.float32).pin_memory()
+        out = torch.empty((m, K), dtype=torch.complex64).pin_memory()
+        dimg = torch.empty((m, N, N), dtype=torch.float32, device=dev)
+        ddat = torch.empty((m, K), dtype=torch.complex64, device=dev)
+
+        def e2e():
+            # copies on torch's stream (its pinned-memory allocator keeps
+            # events on the stream a copy ran on), the preprocessing on the
+            # library's
+            tg3.check(tg3.lib().tg3_mrc_read(path.encode(), 0, m, pin.data_ptr()))
+            dimg.copy_(pin, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+            ctx.prepare_images(dimg, r, ddat, mask=True)
+            ctx.sync()
+            out.copy_(ddat, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+
+        e2e()
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.e2e_steps)):
+            e2e()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.e2e_steps)
+    res = {"metric": "image preprocessing images/s, box 256, K=%d" % K,
+           "value": round(job_rate(n, ms, world), 1), "unit": "images/s",
+           "ms_per_step": round(ms, 3), "n_gpus": world, "scaling": "weak",
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic: a Gaussian blob on unit-variance noise",
+           "config": {"workload": "prep256", "images": n, "box": N, "mask_radius_px": r, "K": K,
+                      "l2": "inputs (1.07 GB) larger than L2"},
+           "clocks": clocks,
+           "roofline": {"bound": "hbm", "kernel": "whole preprocessing step",
+                        "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                        "frac": round(achieved / hbm, 4), "peak_kind": kind,
+                        "algorithmic_bytes_per_image": N * N * 4 + K * 8, "traffic": None},
+           "e2e": {"value": round(m / (e2e_ms * 1e-3) * world, 1), "unit": "images/s",
+                   "path": "tg3_mrc_read from a local file, pinned copies, tg3_prepare_images_d",
+                   "h2d_bytes_per_step": m * N * N * 4, "d2h_bytes_per_step": m * K * 8}}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import preprocess as PP
+        k = 32
+        t0 = time.perf_counter()
+        PP.preprocess(host[:k], r, iCol, iRow, mask=True)
+        secs = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": round(k / secs, 1), "unit": "images/s", "cores": 1,
+                               "kind": "port",
+                               "sample": f"{k} images through the numpy oracle ({secs:.2f} s)"}
+    ctx.close()
+    return res
+
+
 UNEVEN = dict(box=192, pixel_size=1.3, n_blobs=150, sigma_a=(1.5, 3.0), radius_px=60.0,
               cutoffs=(40, 56, 72, 96), pf=2, shift=8.0, snr=0.03, kappa=200.0,
               nR=(200, 8000), nT=(9, 81))
@@ -1472,7 +1578,7 @@ def main():
     ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
     ap.add_argument("--workload", default="local256",
                     choices=["local256", "local256c3", "global64", "uneven192", "learned128",
-                             "learned256", "class2d128"])
+                             "learned256", "class2d128", "prep256"])
     ap.add_argument("--train-particles", type=int, default=150000)
     ap.add_argument("--epochs", type=int, default=3)
     ap.add_argument("--learned-snr", type=float, default=1.0,
@@ -1500,6 +1606,8 @@ def main():
         res = run_uneven(args, rank, world, local)
     elif args.workload == "class2d128":
         res = run_class2d(args, rank, world, local)
+    elif args.workload == "prep256":
+        res = run_prep(args, rank, world, local)
     elif args.workload in ("learned128", "learned256"):
         res = run_learned(args, rank, world, local)
     else:

@@ -45,50 +45,51 @@ __device__ double prep_block_sum(double v, double* scratch)
     return scratch[0];
 }
 
-// Per-image background statistics, FP64 sums: stats[l] = (m, s, sN) with sN
-// the background standard deviation of (x - m) / s about 0.  CTA per image.
+// Per-image background statistics: stats[l] = (m, s, sN), sN the background
+// standard deviation of (x - m) / s about 0.  One pass: a warp per row, lanes
+// over columns; each lane sums its pixels of a row about a pivot (the
+// corner pixel, always background) in FP32 and adds the row's partial sums
+// to FP64 totals.  Background: i^2 + j^2 > r^2, i.e. > floor(r^2) in
+// integers.  CTA per image.
 __global__ void __launch_bounds__(256)
-k_bg_stats(const float* __restrict__ img, int N, double r2, double* __restrict__ st)
+k_bg_stats(const float* __restrict__ img, int N, long long bgAbove, double* __restrict__ st)
 {
     __shared__ double red[32];
     const size_t l = blockIdx.x;
     const float* im = img + l * N * N;
     const int half = N / 2;
-    double s = 0.0, cnt = 0.0;
-    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
-        const int i = q % N - half, j = q / N - half;
-        if ((double)(i * i + j * j) > r2) {
-            s += im[q];
-            cnt += 1.0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const float pivot = im[0];
+    double s1 = 0.0, s2 = 0.0, cnt = 0.0;
+    for (int y = warp; y < N; y += nw) {
+        const int j = y - half;
+        const float* row = im + (size_t)y * N;
+        float a1 = 0.f, a2 = 0.f;
+        int c = 0;
+        for (int x = lane; x < N; x += 32) {
+            const int i = x - half;
+            if ((long long)(i * i + j * j) > bgAbove) {
+                const float d = row[x] - pivot;
+                a1 += d;
+                a2 = fmaf(d, d, a2);
+                c++;
+            }
         }
+        s1 += a1;
+        s2 += a2;
+        cnt += c;
     }
-    s = prep_block_sum(s, red);
+    s1 = prep_block_sum(s1, red);
+    s2 = prep_block_sum(s2, red);
     cnt = prep_block_sum(cnt, red);
-    const double m = s / cnt;
-    double ss = 0.0;
-    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
-        const int i = q % N - half, j = q / N - half;
-        if ((double)(i * i + j * j) > r2) {
-            const double d = im[q] - m;
-            ss += d * d;
-        }
-    }
-    ss = prep_block_sum(ss, red);
-    const double sd = sqrt(ss / (cnt - 1.0));
-    // the normalised background's deviation about 0, from the same values
-    double sn = 0.0;
-    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
-        const int i = q % N - half, j = q / N - half;
-        if ((double)(i * i + j * j) > r2) {
-            const double y = (im[q] - m) / sd;
-            sn += y * y;
-        }
-    }
-    sn = prep_block_sum(sn, red);
     if (threadIdx.x == 0) {
-        st[3 * l] = m;
+        const double mu = s1 / cnt;                 // mean about the pivot
+        const double ss = fmax(s2 - s1 * mu, 0.0);  // sum of (x - m)^2
+        const double sd = sqrt(ss / (cnt - 1.0));
+        st[3 * l] = pivot + mu;
         st[3 * l + 1] = sd;
-        st[3 * l + 2] = sqrt(sn / (cnt - 1.0));
+        // sum of ((x - m) / sd)^2 over the background, over (n - 1)
+        st[3 * l + 2] = sqrt(ss / (sd * sd) / (cnt - 1.0));
     }
 }
 
@@ -98,27 +99,36 @@ __global__ void k_stats_f32(const double* __restrict__ st, int n, float* __restr
         out[i] = (float)st[i];
 }
 
-// stdN: the given value, or the mean of the images' sN.
+// stdN: the given value, or the mean of the images' sN; out = (stdN, 1 / stdN).
 __global__ void k_stdn(const double* __restrict__ st, int n, float given, double* __restrict__ out)
 {
     __shared__ double red[32];
     double s = 0.0;
     for (int l = threadIdx.x; l < n; l += blockDim.x) s += st[3 * (size_t)l + 2];
     s = prep_block_sum(s, red);
-    if (threadIdx.x == 0) out[0] = given > 0.f ? (double)given : s / n;
+    if (threadIdx.x == 0) {
+        out[0] = given > 0.f ? (double)given : s / n;
+        out[1] = 1.0 / out[0];
+    }
 }
 
-// Normalise, mask and scale one image, written with its centre at index 0.
+constexpr int kPrepRows = 4;   // image rows per CTA of k_prep_image
+
+// Normalise, mask and scale one image row, written with the image's centre
+// at index 0.
 __global__ void k_prep_image(const float* __restrict__ img, int N, float r, float ew, int mask,
                              const double* __restrict__ st, const double* __restrict__ stdN,
                              float* __restrict__ out)
 {
     const size_t l = blockIdx.y;
     const float m = (float)st[3 * l], sd = (float)st[3 * l + 1];
-    const float scale = (float)(1.0 / stdN[0]);
+    const float scale = (float)stdN[1];
     const int half = N / 2;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < N * N; q += gridDim.x * blockDim.x) {
-        const int x = q % N, y = q / N;
+    // CTA (kPrepRows rows, image l); threads over the rows' columns
+    const int y1 = min(N, (int)(blockIdx.x + 1) * kPrepRows);
+    for (int y = blockIdx.x * kPrepRows; y < y1; y++)
+    for (int x = threadIdx.x; x < N; x += blockDim.x) {
+        const int q = y * N + x;
         const int i = x - half, j = y - half;
         float v = (img[l * N * N + q] - m) / sd;
         if (mask) {
@@ -209,7 +219,7 @@ extern "C" int tg3_prepare_images_d(tg3_ctx* c, const float* img, int nImg, int 
     const int IB = std::min(nImg, 2048);
     const size_t img2 = (size_t)N * N, ft2 = (size_t)N * (N / 2 + 1);
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
-    const size_t oSt = 0, oN = up(sizeof(double) * 3 * (size_t)nImg), oR = oN + 256,
+    const size_t oSt = 0, oN = up(sizeof(double) * 3 * (size_t)nImg), oR = oN + 256,   // oN: 2 doubles
                  oF = up(oR + sizeof(float) * img2 * IB), total = oF + sizeof(float2) * ft2 * IB;
     char* b = (char*)ws_get(c, WS_PREP, total, &st);
     if (!b) return st;
@@ -219,13 +229,13 @@ extern "C" int tg3_prepare_images_d(tg3_ctx* c, const float* img, int nImg, int 
     cufftComplex* ft = (cufftComplex*)(b + oF);
     cudaStream_t s = c->stream;
     const float r = maskRadiusPx;
-    k_bg_stats<<<nImg, 256, 0, s>>>(img, N, (double)r * (double)r, stv);
+    k_bg_stats<<<nImg, 256, 0, s>>>(img, N, (long long)std::floor((double)r * (double)r), stv);
     TG3_LAUNCH_CHECK("background statistics");
     k_stdn<<<1, 256, 0, s>>>(stv, nImg, stdN, sN);
     TG3_LAUNCH_CHECK("noise level");
     for (int l0 = 0; l0 < nImg; l0 += IB) {
         const int n = std::min(IB, nImg - l0);
-        k_prep_image<<<dim3((unsigned)std::min<size_t>(64, (img2 + 255) / 256), n), 256, 0, s>>>(
+        k_prep_image<<<dim3((N + kPrepRows - 1) / kPrepRows, n), std::min(N, 256), 0, s>>>(
             img + (size_t)l0 * img2, N, r, 6.0f, mask, stv + 3 * (size_t)l0, sN, real);
         TG3_LAUNCH_CHECK("normalise and mask");
         cufftHandle h;
