@@ -409,6 +409,22 @@ int tg3_global_scan2d_d(tg3_ctx* ctx, const float* img, int vdim, int pf, int nI
 int tg3_prepare_images_d(tg3_ctx* ctx, const float* img, int nImg, int N, float maskRadiusPx,
                          int mask, float stdN, float* dat, float* stats);
 
+/* Noise spectrum sigma^2 from the images at their best poses
+ * (Optimiser::allReduceSigma, src/Optimiser.cpp:6355-6630): the active pixel
+ * set must hold the shells u = rint(|k|) < rSig of the half transform (i in
+ * [0, N/2], every row; powerSpectrum, src/Functions/Spectrum.cpp:161-190).
+ * Per image (device arrays): masked and unmasked data datM / datN [nImg][K]
+ * complex, ctf [nImg][K], rotMat [nImg][9], trans [nImg][2], offset
+ * [nImg][2] (may be NULL), group [nImg] (1-based; read when byGroup).  The
+ * class-`cls` volume gives the model.  Out (device, double): sig and
+ * sigRcp = -0.5 / sig, [nGroup][rSig]; without byGroup every group gets the
+ * pooled spectrum.  maskRadius and pixelSize in Angstrom set alpha =
+ * sqrt(pi (maskRadius / (N pixelSize))^2). */
+int tg3_sigma_d(tg3_ctx* ctx, int cls, int nImg, const float* datM, const float* datN,
+                const float* ctf, const double* rotMat, const double* trans, const double* offset,
+                const int* group, int nGroup, int byGroup, int rSig, float maskRadius,
+                float pixelSize, double* sig, double* sigRcp);
+
 /* MRC stacks (src/Image/ImageFile.cpp): header fields, and sections
  * [first, first + count) as float32 in file order (modes 0, 1, 2, 6).
  * pixelSize (may be NULL) = cella[0] / mx.  Writing: float32 (mode 2) with

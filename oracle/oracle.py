@@ -105,6 +105,7 @@ def ref():
         R.ref_read_mrc.argtypes = [ctypes.c_char_p, _c, _c, _f64p]
         R.ref_read_mrc.restype = _c
         R.ref_prep_image.argtypes = [_f64p, _c, _d, _c, _f64p, _f64p]
+        R.ref_power_spectrum.argtypes = [_c128p, _c, _c, _f64p]
         R.ref_translate.argtypes = [_f64p, _c, _c, _i32p, _i32p, _c, _c128p]
         R.ref_translate_image.argtypes = [_c128p, _d, _d, _c, _i32p, _i32p, _c, _c128p]
         R.ref_ctf.argtypes = [_f64p, _d, _c, _i32p, _i32p, _c, _f64p]

@@ -63,3 +63,49 @@ def preprocess(imgs, r, iCol, iRow, mask=True, std_n=None):
     rows = np.asarray(iRow) % N
     dat = F[:, rows, np.asarray(iCol)]
     return dat, st, corner
+
+
+def power_spectrum(F, r):
+    """Shell means of |F|^2 over a half transform F (N, N/2 + 1), rows j in
+    wrapped order: shells u = rint(|k|) < r among pixels with i^2 + j^2 < r^2
+    (powerSpectrum, src/Functions/Spectrum.cpp:161-190)."""
+    N = F.shape[0]
+    j, i = np.meshgrid(np.arange(-N // 2, N // 2), np.arange(N // 2 + 1), indexing="ij")
+    q = i * i + j * j
+    u = np.rint(np.sqrt(q)).astype(int)
+    keep = (q < r * r) & (u < r)
+    vals = np.abs(F[j[keep] % N, i[keep]]) ** 2
+    s = np.bincount(u[keep], weights=vals, minlength=r)[:r]
+    c = np.bincount(u[keep], minlength=r)[:r]
+    return s / c
+
+
+def sigma(models, datM, datN, offsets, iCol, iRow, N, r, groups, n_group, by_group, mask_radius,
+          pixel_size):
+    """Optimiser::allReduceSigma (src/Optimiser.cpp:6355-6630, rank-1 pose,
+    whole frequency range) over pixel data at the pixels (iCol, iRow) of the
+    shells below r: models [n][K] = ctf P(R) S(t) of each image's best pose;
+    the unmasked model is that times S(-offset).  Returns sig, sigRcp
+    [n_group][r]."""
+    iCol, iRow = np.asarray(iCol), np.asarray(iRow)
+    u = np.rint(np.sqrt(iCol * iCol + iRow * iRow)).astype(int)
+    cnt = np.bincount(u, minlength=r)[:r]
+    shell = lambda v: np.bincount(u, weights=v, minlength=r)[:r] / cnt
+    acc = np.zeros((n_group, 3 * r + 1))
+    for l in range(len(models)):
+        M = models[l]
+        ox, oy = (offsets[l] if offsets is not None else (0.0, 0.0))
+        Nm = M * np.exp(2j * np.pi * (iCol * ox + iRow * oy) / N)
+        g = groups[l] - 1 if by_group else 0
+        acc[g, :r] += shell(np.abs(datM[l] - M) ** 2) / 2
+        acc[g, r:2 * r] += shell(np.abs(datN[l] - Nm) ** 2) / 2
+        acc[g, 2 * r:3 * r] += np.sqrt(shell(np.abs(M) ** 2) / shell(np.abs(datM[l]) ** 2))
+        acc[g, 3 * r] += 1
+    if not by_group:
+        acc[:] = acc[0]
+    w = acc[:, 3 * r:3 * r + 1]
+    sM, sN, svd = acc[:, :r] / w, acc[:, r:2 * r] / w, acc[:, 2 * r:3 * r] / w
+    alpha = np.sqrt(np.pi * (mask_radius / (N * pixel_size)) ** 2)
+    ratio = np.minimum(1.0, svd)
+    sig = ratio * sM + (1 - ratio) * alpha * sN
+    return sig, -0.5 / sig

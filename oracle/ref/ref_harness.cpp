@@ -15,6 +15,7 @@
 #include "ImageFile.h"
 #include "Logging.h"
 #include "Mask.h"
+#include "Spectrum.h"
 #include "Precision.h"
 #include "Functions.h"
 #include "TabFunction.h"
@@ -177,6 +178,17 @@ void ref_prep_image(const double* in, int N, double r, int mask, double* out, do
     stats[2] = bgStddev(0, img, r);
     if (mask) softMask(img, img, (RFLOAT)r, (RFLOAT)EDGE_WIDTH_RL, (RFLOAT)0, 1u);
     for (size_t i = 0; i < img.sizeRL(); i++) out[i] = img(i);
+}
+
+/* powerSpectrum(vec&, const Image&, r, nThread), src/Functions/Spectrum.cpp:
+ * 161-190, of a half transform ft [N][N/2 + 1] complex; out [r]. */
+void ref_power_spectrum(const double* ft, int N, int r, double* out)
+{
+    Image img(N, N, FT_SPACE);
+    memcpy(&img[0], ft, sizeof(Complex) * img.sizeFT());
+    vec ps(r);
+    powerSpectrum(ps, img, r, 1);
+    for (int i = 0; i < r; i++) out[i] = ps(i);
 }
 
 /* translate(Complex*, nTransCol, nTransRow, nCol, nRow, iCol, iRow, nPxl,

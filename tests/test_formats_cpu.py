@@ -169,3 +169,28 @@ def test_thu_round_trip_and_errors(tmp_path):
         io.read_thu(bad)
     with pytest.raises(tg3.TG3Error):
         io.write_thu(tmp_path / "x.thu", v, ["has space"] * 5, mics)
+
+
+@needs_ref
+def test_power_spectrum_matches_reference():
+    """Shell means of the oracle against the compiled reference's
+    powerSpectrum (rint shells, i^2 + j^2 < r^2, the x = 0 column counted on
+    both sides)."""
+    rng = np.random.default_rng(21)
+    N, r = 32, 15
+    F = rng.standard_normal((N, N // 2 + 1)) + 1j * rng.standard_normal((N, N // 2 + 1))
+    ref = np.zeros(r)
+    R.ref_power_spectrum(np.ascontiguousarray(F), N, r, ref)
+    np.testing.assert_allclose(PP.power_spectrum(F, r), ref, rtol=1e-13)
+
+
+def test_spectrum_pixels_are_the_power_spectrum_support():
+    rng = np.random.default_rng(22)
+    N, r = 32, 15
+    F = rng.standard_normal((N, N // 2 + 1)) + 1j * rng.standard_normal((N, N // 2 + 1))
+    iCol, iRow = io.spectrum_pixels(N, r)
+    u = np.rint(np.sqrt(iCol.astype(float) ** 2 + iRow ** 2)).astype(int)
+    assert u.max() == r - 1 and np.all(np.bincount(u) > 0)
+    v = np.abs(F[iRow % N, iCol]) ** 2
+    np.testing.assert_allclose(np.bincount(u, weights=v) / np.bincount(u),
+                               PP.power_spectrum(F, r), rtol=1e-13)

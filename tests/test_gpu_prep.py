@@ -64,3 +64,46 @@ def test_prepare_images_rejects_mismatched_pixel_set():
             ctx.prepare_images(img, 20.0, dat)
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("by_group", [True, False])
+def test_sigma_matches_oracle(by_group):
+    """Noise spectrum from the images at their best poses (allReduceSigma)
+    against the oracle's restatement over the same pixel data."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(50 + by_group)
+    N, pf, px, r = 32, 2, 1.5, 15
+    bm = synth.blob_map(rng, 16, (2.0, 4.0), px, 8.0)
+    vol = synth.padded_volume(bm, N, pf).numpy().astype(np.complex64)
+    iCol, iRow = io.spectrum_pixels(N, r)
+    K = len(iCol)
+    n, n_group = 40, 3
+    quats = synth.haar_quaternions(rng, n)
+    mats = synth.quat_to_mat(quats).reshape(n, 9)
+    trans = rng.uniform(-2, 2, (n, 2))
+    offset = rng.uniform(-0.5, 0.5, (n, 2))
+    groups = rng.integers(1, n_group + 1, n).astype(np.int32)
+    ctf = synth.ctf_values(synth.ctf_attrs(rng, n), px, N, iCol, iRow).astype(np.float32)
+    P = O.project(vol.astype(np.complex128), mats, iCol, iRow, pf)
+    models = np.stack([ctf[l] * P[l] * synth.phase_shift(trans[l], N, iCol, iRow)[0]
+                       for l in range(n)])
+    noise = lambda: 0.4 * (rng.standard_normal((n, K)) + 1j * rng.standard_normal((n, K)))
+    datM = (models + noise()).astype(np.complex64)
+    datN = (models * np.exp(2j * np.pi * (np.outer(offset[:, 0], iCol) + np.outer(offset[:, 1], iRow)) / N)
+            + noise()).astype(np.complex64)
+    d = lambda x: torch.as_tensor(np.ascontiguousarray(x)).to(DEV)
+    sig = torch.empty((n_group, r), dtype=torch.float64, device=DEV)
+    rcp = torch.empty_like(sig)
+    ctx = tg3.Context(0)
+    try:
+        ctx.set_volume(0, d(vol), pf)
+        ctx.set_pixels(iCol, iRow, N)
+        ctx.sigma(0, d(datM), d(datN), d(ctf), d(mats), d(trans), d(offset), d(groups), n_group, r,
+                  60.0, px, sig, rcp, by_group=by_group)
+        ctx.sync()
+    finally:
+        ctx.close()
+    rs, rr = PP.sigma(models, datM.astype(np.complex128), datN.astype(np.complex128), offset, iCol,
+                      iRow, N, r, groups, n_group, by_group, 60.0, px)
+    np.testing.assert_allclose(sig.cpu().numpy(), rs, rtol=2e-4)
+    np.testing.assert_allclose(rcp.cpu().numpy(), rr, rtol=2e-4)

@@ -148,7 +148,7 @@ int check_ctx(tg3_ctx* c)
 // margin 1 keeps a trilinear sample's corner block (its x0 + 1 <= vdim / 2
 // is stored; its y0, z0 stay in [-vdim / 2, vdim / 2)), margin 2 also the
 // MKB insertion support.
-static int check_geometry(tg3_ctx* c, int vdim, int pf, double margin = 1.0)
+int check_geometry(tg3_ctx* c, int vdim, int pf, double margin)
 {
     if (c->px.K <= 0) return fail(TG3_ERR_STATE, "pixel list not set");
     if (c->px.maxRadius * pf + margin > vdim / 2)

@@ -425,6 +425,8 @@ cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, lo
 namespace tg3 {
 // Makes the context's device current; TG3_ERR_ARG for a null context.
 int check_ctx(tg3_ctx* c);
+// the active pixel set, scaled by pf, fits a volume of vdim with `margin` to spare
+int check_geometry(tg3_ctx* c, int vdim, int pf, double margin = 1.0);
 // releases the context's preprocessing FFT plans
 void prep_release(tg3_ctx* c);
 }  // namespace tg3

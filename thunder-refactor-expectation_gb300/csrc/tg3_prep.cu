@@ -157,6 +157,88 @@ __global__ void k_gather_pixels(const float2* __restrict__ ft, int N, const int*
     }
 }
 
+// ------------------------------------------------------------ sigma^2 --
+// Noise spectrum of the images against their best poses (Optimiser::
+// allReduceSigma, src/Optimiser.cpp:6355-6630, with OPTIMISER_SIGMA_RANK1ST
+// and OPTIMISER_SIGMA_WHOLE_FREQUENCY).  Per image l, with its model
+// M = ctf P(R) S(t) and the unmasked model N = ctf P(R) S(t - offset) over the
+// pixels of shells u = rint(|k|) < rSig (powerSpectrum, src/Functions/
+// Spectrum.cpp:161-190, shell means):
+//   vSigM[u] = <|datM - M|^2>, vSigN[u] = <|datN - N|^2>,
+//   svd[u] = sqrt(<|M|^2> / <|datM|^2>);
+// its group accumulates vSigM / 2, vSigN / 2, svd and a count.  CTA per
+// image; shell sums in shared memory (FP32), group sums in FP64.
+__global__ void __launch_bounds__(256)
+k_sigma_image(const float2* __restrict__ P, int ldp, const float2* __restrict__ datM,
+              const float2* __restrict__ datN, const float* __restrict__ ctf,
+              const double* __restrict__ trans, const double* __restrict__ offset,
+              const int* __restrict__ group, int byGroup, const int* __restrict__ iCol,
+              const int* __restrict__ iRow, int K, int N, int rSig, double* __restrict__ acc)
+{
+    extern __shared__ float sh[];
+    float* pM = sh;               // [rSig] each
+    float* pN = pM + rSig;
+    float* pS = pN + rSig;
+    float* pD = pS + rSig;
+    int* cnt = reinterpret_cast<int*>(pD + rSig);
+    const size_t l = blockIdx.x;
+    for (int u = threadIdx.x; u < rSig; u += blockDim.x) {
+        pM[u] = pN[u] = pS[u] = pD[u] = 0.f;
+        cnt[u] = 0;
+    }
+    __syncthreads();
+    const float invN = 1.0f / (float)N;
+    const float tx = (float)trans[2 * l], ty = (float)trans[2 * l + 1];
+    const float ox = offset ? (float)offset[2 * l] : 0.f, oy = offset ? (float)offset[2 * l + 1] : 0.f;
+    for (int p = threadIdx.x; p < K; p += blockDim.x) {
+        const int i = iCol[p], j = iRow[p];
+        const int u = (int)rintf(sqrtf((float)(i * i + j * j)));
+        if (u >= rSig || i * i + j * j >= rSig * rSig) continue;
+        const float2 pr = P[l * ldp + p];
+        const float c = ctf[l * K + p];
+        float sn, cs;
+        // S(t) = exp(-2 pi i (i tx + j ty) / N)
+        sincospif(-2.0f * ((float)i * tx + (float)j * ty) * invN, &sn, &cs);
+        const float mr = c * (pr.x * cs - pr.y * sn), mi = c * (pr.x * sn + pr.y * cs);
+        float so, co;
+        sincospif(2.0f * ((float)i * ox + (float)j * oy) * invN, &so, &co);
+        const float nr = mr * co - mi * so, ni = mr * so + mi * co;   // S(t - offset)
+        const float2 a = datM[l * K + p], b = datN[l * K + p];
+        atomicAdd(pM + u, (a.x - mr) * (a.x - mr) + (a.y - mi) * (a.y - mi));
+        atomicAdd(pN + u, (b.x - nr) * (b.x - nr) + (b.y - ni) * (b.y - ni));
+        atomicAdd(pS + u, mr * mr + mi * mi);
+        atomicAdd(pD + u, a.x * a.x + a.y * a.y);
+        atomicAdd(cnt + u, 1);
+    }
+    __syncthreads();
+    const int g = byGroup ? group[l] - 1 : 0;
+    double* ag = acc + (size_t)g * (3 * rSig + 1);
+    for (int u = threadIdx.x; u < rSig; u += blockDim.x) {
+        const double n = (double)cnt[u];
+        atomicAdd(ag + u, 0.5 * pM[u] / n);
+        atomicAdd(ag + rSig + u, 0.5 * pN[u] / n);
+        atomicAdd(ag + 2 * rSig + u, sqrt((double)pS[u] / (double)pD[u]));
+    }
+    if (threadIdx.x == 0) atomicAdd(ag + 3 * rSig, 1.0);
+}
+
+// sig = ratio sigM + (1 - ratio) alpha sigN, ratio = min(1, svd); all groups
+// copy group 0 when the images were pooled.  One thread per (group, shell).
+__global__ void k_sigma_finish(const double* __restrict__ acc, int nGroup, int rSig, int byGroup,
+                               double alpha, double* __restrict__ sig, double* __restrict__ sigRcp)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nGroup * rSig) return;
+    const int g = idx / rSig, u = idx % rSig;
+    const double* ag = acc + (size_t)(byGroup ? g : 0) * (3 * rSig + 1);
+    const double w = ag[3 * rSig];
+    const double sM = ag[u] / w, sN = ag[rSig + u] / w, svd = ag[2 * rSig + u] / w;
+    const double ratio = fmin(1.0, svd);
+    const double s = ratio * sM + (1.0 - ratio) * alpha * sN;
+    sig[idx] = s;
+    sigRcp[idx] = -0.5 / s;
+}
+
 // batched r2c plans, one per (context, size, batch), kept until the context goes
 struct Plan {
     tg3_ctx* c;
@@ -202,6 +284,58 @@ void prep_release(tg3_ctx* c)
 }  // namespace tg3
 
 using namespace tg3;
+
+extern "C" int tg3_sigma_d(tg3_ctx* c, int cls, int nImg, const float* datM, const float* datN,
+                           const float* ctf, const double* rotMat, const double* trans,
+                           const double* offset, const int* group, int nGroup, int byGroup,
+                           int rSig, float maskRadius, float pixelSize, double* sig,
+                           double* sigRcp)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].blocks)
+        return fail(TG3_ERR_STATE, "volume of the class not set");
+    if (!datM || !datN || !ctf || !rotMat || !trans || !sig || !sigRcp || (byGroup && !group))
+        return fail(TG3_ERR_ARG, "null device pointer");
+    if (nImg <= 0 || nGroup <= 0 || rSig <= 0 || rSig > 2048 || !(pixelSize > 0))
+        return fail(TG3_ERR_ARG, "bad sigma arguments");
+    const Volume& v = c->vol[cls];
+    if ((st = check_geometry(c, v.vdim, v.pf))) return st;
+    const int K = c->px.K, N = c->px.idim;
+    if (rSig > N / 2) return fail(TG3_ERR_ARG, "rSig beyond the image's Nyquist shell");
+    const int IB = std::min(nImg, 2048);
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t accN = (size_t)nGroup * (3 * rSig + 1);
+    const size_t oA = 0, oP = up(sizeof(double) * accN), total = oP + sizeof(float2) * (size_t)K * IB;
+    char* b = (char*)ws_get(c, WS_PREP, total, &st);
+    if (!b) return st;
+    double* acc = (double*)(b + oA);
+    float* P = (float*)(b + oP);
+    float* pscr = (float*)ws_get(c, WS_PROJ, sizeof(float) * project_scratch_floats(IB, 2 * K), &st);
+    if (!pscr) return st;
+    cudaStream_t s = c->stream;
+    TG3_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * accN, s));
+    const size_t smem = (4 * sizeof(float) + sizeof(int)) * (size_t)rSig;
+    for (int l0 = 0; l0 < nImg; l0 += IB) {
+        const int n = std::min(IB, nImg - l0);
+        TG3_CUDA(launch_project(nullptr, nullptr, v.blocks, v.vdim, v.pf, nullptr,
+                                rotMat + 9 * (size_t)l0, n, n, c->px.iCol, c->px.iRow, K, P, 2 * K,
+                                nullptr, nullptr, nullptr, pscr, c->d_flag, 0, s));
+        const size_t o = (size_t)l0 * K;
+        k_sigma_image<<<n, 256, smem, s>>>(
+            reinterpret_cast<const float2*>(P), K, reinterpret_cast<const float2*>(datM) + o,
+            reinterpret_cast<const float2*>(datN) + o, ctf + o, trans + 2 * (size_t)l0,
+            offset ? offset + 2 * (size_t)l0 : nullptr, byGroup ? group + l0 : nullptr, byGroup,
+            c->px.iCol, c->px.iRow, K, N, rSig, acc);
+        TG3_LAUNCH_CHECK("sigma per image");
+    }
+    const double rm = (double)maskRadius / ((double)N * (double)pixelSize);
+    const double alpha = sqrt(M_PI * rm * rm);
+    k_sigma_finish<<<(nGroup * rSig + 255) / 256, 256, 0, s>>>(acc, nGroup, rSig, byGroup, alpha,
+                                                                sig, sigRcp);
+    TG3_LAUNCH_CHECK("sigma finish");
+    return TG3_OK;
+}
 
 extern "C" int tg3_prepare_images_d(tg3_ctx* c, const float* img, int nImg, int N,
                                     float maskRadiusPx, int mask, float stdN, float* dat,

@@ -37,7 +37,7 @@ EXPORTS = [
     "tg3_cnn_contrastive", "tg3_cnn_embed", "tg3_cnn_match_propose", "tg3_ctx_set_bank",
     "tg3_local_phase_bank_d", "tg3_local_phase_ctf_d", "tg3_ExpectLocal3D_ctf",
     "tg3_ExpectGlobal2D", "tg3_global_scan2d_d", "tg3_InsertI2D", "tg3_global_scan2d_classes_d",
-    "tg3_prepare_images_d", "tg3_mrc_info", "tg3_mrc_read", "tg3_mrc_write", "tg3_thu_count",
+    "tg3_prepare_images_d", "tg3_sigma_d", "tg3_mrc_info", "tg3_mrc_read", "tg3_mrc_write", "tg3_thu_count",
     "tg3_thu_read", "tg3_thu_write",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
@@ -131,6 +131,7 @@ def lib():
             "tg3_InsertI2D": ([_P] * 16 + [_F] + [_I] * 8, _I),
             "tg3_global_scan2d_classes_d": ([_P, _P] + [_I] * 6 + [_P] * 11 + [_I], _I),
             "tg3_prepare_images_d": ([_P, _P, _I, _I, _F, _I, _F, _P, _P], _I),
+            "tg3_sigma_d": ([_P, _I, _I] + [_P] * 7 + [_I, _I, _I, _F, _F, _P, _P], _I),
             "tg3_mrc_info": ([ctypes.c_char_p] + [_P] * 5, _I),
             "tg3_mrc_read": ([ctypes.c_char_p, _I, _I, _P], _I),
             "tg3_mrc_write": ([ctypes.c_char_p, _P, _I, _I, _I, _F, _I], _I),
@@ -337,6 +338,18 @@ class Context:
         self._hold(img, dat, stats)
         check(lib().tg3_prepare_images_d(self.h, ptr(img), n, N, float(mask_radius_px),
                                          int(bool(mask)), float(std_n), ptr(dat), ptr(stats)))
+
+    def sigma(self, cls, datM, datN, ctf, rotmat, trans, offset, group, n_group, r_sig,
+              mask_radius, pixel_size, sig, sig_rcp, by_group=True):
+        """Noise spectrum of the images at their best poses: sig / sig_rcp
+        (device float64 (n_group, r_sig)); the active pixel set must be the
+        shells below r_sig (tg3.io.spectrum_pixels)."""
+        n = datM.shape[0]
+        self._hold(datM, datN, ctf, rotmat, trans, offset, group, sig, sig_rcp)
+        check(lib().tg3_sigma_d(self.h, cls, n, ptr(datM), ptr(datN), ptr(ctf), ptr(rotmat),
+                                ptr(trans), ptr(offset), ptr(group), n_group, int(by_group),
+                                r_sig, float(mask_radius), float(pixel_size), ptr(sig),
+                                ptr(sig_rcp)))
 
     def resample(self, nP, n, u, w, perm, u0, peak, nOut, src, wOut, top):
         self._hold(u, w, perm, u0, peak, src, wOut, top)

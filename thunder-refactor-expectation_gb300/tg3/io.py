@@ -17,6 +17,17 @@ THU_FIELDS = ("voltage", "defocusU", "defocusV", "defocusTheta", "Cs", "amplitud
               "defocusFactor", "stdDefocusFactor", "score")
 
 
+def spectrum_pixels(N, r):
+    """The half-transform pixels of shells rint(|k|) < r, in the order of the
+    reference's powerSpectrum loop (rows j in [-N/2, N/2), columns i in
+    [0, N/2]): iCol, iRow (int32)."""
+    j, i = np.meshgrid(np.arange(-N // 2, N // 2), np.arange(N // 2 + 1), indexing="ij")
+    i, j = i.ravel(), j.ravel()
+    q = i * i + j * j
+    keep = (q < r * r) & (np.rint(np.sqrt(q)) < r)
+    return i[keep].astype(np.int32), j[keep].astype(np.int32)
+
+
 def mrc_info(path):
     """(nx, ny, nz, mode, pixel size) of an MRC file."""
     v = [ctypes.c_int() for _ in range(4)]
