@@ -799,6 +799,79 @@ def run_prep(args, rank, world, local_rank):
     return res
 
 
+def run_reco(args, rank, world, local_rank):
+    """Reconstruction of a box-256 map from its insertion accumulators
+    (Reconstructor::reconstruct): padded grid 512^3 (pf 2), Wiener filter from
+    an FSC curve, grid correction by balancing against the MKB kernel, the
+    inverse transform and gridding correction.  F: the padded transform of a
+    200-blob map; T: a smooth radial weight.  One step = one map."""
+    import torch
+    import tg3
+    from tg3 import synth
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    N, pf, px, maxR = 256, 2, 1.1, 120
+    vdim = N * pf
+    rng = np.random.default_rng(rank_seed(5000, rank))
+    bm = synth.blob_map(rng, 200, (1.5, 3.0), px, 80.0)
+    F = synth.padded_volume(bm, N, pf, device=dev, dtype=torch.float32)
+    q = torch.fft.fftfreq(vdim, 1.0 / vdim, device=dev)
+    kz, ky, kx = torch.meshgrid(q, q, torch.arange(vdim // 2 + 1, device=dev, dtype=q.dtype),
+                                indexing="ij")
+    T = (50.0 * torch.exp(-torch.sqrt(kx * kx + ky * ky + kz * kz) / (0.4 * vdim)) + 0.5).float()
+    F = (F * T).contiguous()
+    del kx, ky, kz
+    fsc = torch.as_tensor(np.clip(1.05 - np.arange(N // 2 + 1) / (N / 2), 0, 1)).to(dev)
+    ctx = tg3.Context(local_rank)
+    ctx.insert_begin(vdim, pf)
+    vol = torch.empty((N, N, N), dtype=torch.float32, device=dev)
+
+    def step():
+        ctx.insert_load(F, T)
+        return ctx.reconstruct(vol, maxR, fsc=fsc, join_half=True, grid_corr=True,
+                               kernel=tg3.KERNEL_MKB)
+
+    for _ in range(args.warmup):
+        rounds = step()
+    ctx.sync()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    clk = ClockSampler(local_rank)
+    clk.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(1, min(args.steps, 10))
+    barrier(world)
+    e0.record(stream)
+    for _ in range(steps):
+        rounds = step()
+    e1.record(stream)
+    e1.synchronize()
+    barrier(world)
+    clocks = clk.stop()
+    ms = reduce_max(world, e0.elapsed_time(e1)) / steps
+    nh = vdim * vdim * (vdim // 2 + 1)
+    nr = vdim ** 3
+    # algorithmic bytes of one balancing round: T, W read and C written
+    # (C = T W), C read and the real map written (inverse), the map read and
+    # written (kernel product), read and C written (forward), C read and W
+    # read and written (update) -- each array once per pass
+    per_round = 4 * nh * 2 + 8 * nh + 8 * nh + 4 * nr + 8 * nr + 4 * nr + 8 * nh + 8 * nh + 8 * nh
+    alg = rounds * per_round + 16 * nh + 8 * nh + 4 * nr + 4 * N ** 3
+    hbm, bf16, kind = peaks()
+    achieved = alg / (ms * 1e-3) / 1e9
+    ctx.close()
+    return {"metric": "reconstruction maps/s, box 256 (512^3 padded), grid correction",
+            "value": round(job_rate(1, ms, world), 3), "unit": "maps/s", "ms_per_step": round(ms, 3),
+            "n_gpus": world, "scaling": "weak", "steps": steps, "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic: padded transform of a 200-blob map, radial T",
+            "config": {"workload": "reco256", "box": N, "pf": pf, "max_radius": maxR,
+                       "balancing_rounds": rounds, "l2": "arrays (2.7 GB) larger than L2"},
+            "clocks": clocks,
+            "roofline": {"bound": "hbm", "kernel": "whole reconstruction (cuFFT-dominated)",
+                         "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(achieved / hbm, 4), "peak_kind": kind, "traffic": None}}
+
+
 UNEVEN = dict(box=192, pixel_size=1.3, n_blobs=150, sigma_a=(1.5, 3.0), radius_px=60.0,
               cutoffs=(40, 56, 72, 96), pf=2, shift=8.0, snr=0.03, kappa=200.0,
               nR=(200, 8000), nT=(9, 81))
@@ -1578,7 +1651,7 @@ def main():
     ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
     ap.add_argument("--workload", default="local256",
                     choices=["local256", "local256c3", "global64", "uneven192", "learned128",
-                             "learned256", "class2d128", "prep256"])
+                             "learned256", "class2d128", "prep256", "reco256"])
     ap.add_argument("--train-particles", type=int, default=150000)
     ap.add_argument("--epochs", type=int, default=3)
     ap.add_argument("--learned-snr", type=float, default=1.0,
@@ -1608,6 +1681,8 @@ def main():
         res = run_class2d(args, rank, world, local)
     elif args.workload == "prep256":
         res = run_prep(args, rank, world, local)
+    elif args.workload == "reco256":
+        res = run_reco(args, rank, world, local)
     elif args.workload in ("learned128", "learned256"):
         res = run_learned(args, rank, world, local)
     else:

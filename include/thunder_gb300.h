@@ -409,6 +409,24 @@ int tg3_global_scan2d_d(tg3_ctx* ctx, const float* img, int vdim, int pf, int nI
 int tg3_prepare_images_d(tg3_ctx* ctx, const float* img, int nImg, int N, float maskRadiusPx,
                          int mask, float stdN, float* dat, float* stats);
 
+/* The insertion accumulator set to F (complex) and T (real), device arrays
+ * [vdim][vdim][vdim/2 + 1] -- e.g. the sums over ranks or half maps that
+ * the reference all-reduces before reconstructing (allReduceF / T). */
+int tg3_ctx_insert_load_d(tg3_ctx* ctx, const float* F, const float* T);
+
+/* Reconstruction of the map from the context's insertion accumulators
+ * (Reconstructor::reconstruct, src/Reconstructor.cpp:1129-1790; 3-D, no
+ * symmetry): Wiener filter of T from the FSC per unpadded shell (fsc [nFsc];
+ * NULL: none), joined half maps when joinHalf; with gridCorr the balancing of
+ * W against the MKB kernel (a, alpha) for up to 30 rounds (rounds returns
+ * how many ran; may be NULL), else W = 1 / T; the inverse transform of F W
+ * inside maxRadius (unpadded pixels); the central N^3 (N = vdim / pf),
+ * divided by the insertion kernel's real-space transform (kernel
+ * TG3_KERNEL_TRILINEAR or TG3_KERNEL_MKB).  vol: device float [N][N][N],
+ * centred (coordinate i at index i + N/2). */
+int tg3_ctx_reconstruct_d(tg3_ctx* ctx, const double* fsc, int nFsc, int joinHalf, int maxRadius,
+                          int gridCorr, int kernel, float a, float alpha, float* vol, int* rounds);
+
 /* Noise spectrum sigma^2 from the images at their best poses
  * (Optimiser::allReduceSigma, src/Optimiser.cpp:6355-6630): the active pixel
  * set must hold the shells u = rint(|k|) < rSig of the half transform (i in

@@ -194,3 +194,26 @@ def test_spectrum_pixels_are_the_power_spectrum_support():
     v = np.abs(F[iRow % N, iCol]) ** 2
     np.testing.assert_allclose(np.bincount(u, weights=v) / np.bincount(u),
                                PP.power_spectrum(F, r), rtol=1e-13)
+
+
+@needs_ref
+def test_mkb_real_space_form_is_the_transform_of_the_reference_window():
+    """The oracle's MKB_RL (closed form) against the 3-D Fourier transform
+    of the reference's own Fourier-space window MKB_FT (compiled, sampled as
+    its TabFunction), integrated radially: 4 pi int_0^a MKB_FT(k) sinc(2 k r)
+    k^2 dk, compared as ratios to r = 0."""
+    from scipy import integrate
+    from oracle import reconstruct as RC
+    a, alpha, n = 1.9, 15.0, 200000
+    tab = np.zeros(n + 1)
+    R.ref_mkb_table(a, alpha, a * a, n, tab)       # MKB_FT as a function of k^2
+    ft = lambda k: np.interp(k * k, np.linspace(0, a * a, n + 1), tab)
+
+    def rl(r):
+        f = lambda k: ft(k) * np.sinc(2 * k * r) * k * k
+        return 4 * np.pi * integrate.quad(f, 0, a, limit=400, epsabs=1e-13)[0]
+
+    rs = np.array([0.0, 0.02, 0.05, 0.1, 0.2, 0.3])
+    num = np.array([rl(r) for r in rs])
+    np.testing.assert_allclose(RC.mkb_rl(rs, a, alpha) / RC.mkb_rl(0.0, a, alpha), num / num[0],
+                               rtol=2e-4, atol=1e-7)

@@ -1,0 +1,57 @@
+"""Reconstruction on the GPU (tg3_ctx_reconstruct_d) against the oracle's
+restatement of Reconstructor::reconstruct (oracle/reconstruct.py): Wiener
+filter from the FSC, W by balancing against the MKB kernel or 1 / T, the
+inverse transform of F W, the central N^3 and the gridding correction.  F
+and T are Hermitian-consistent (F the transform of a real map, T radial), as
+sums over whole slices are in the limit: an inverse real transform of a
+half grid is otherwise implementation-defined."""
+import numpy as np
+import pytest
+import torch
+
+import tg3
+from oracle import reconstruct as RC
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+def _inputs(rng, N, pf):
+    vdim = N * pf
+    c = np.arange(vdim) - vdim // 2
+    z, y, x = np.meshgrid(c, c, c, indexing="ij")
+    m = np.zeros((vdim, vdim, vdim))
+    for _ in range(8):
+        p = rng.uniform(-N / 5, N / 5, 3)
+        m += np.exp(-((x - p[0]) ** 2 + (y - p[1]) ** 2 + (z - p[2]) ** 2) / (2 * rng.uniform(1.5, 3) ** 2))
+    q = np.fft.fftfreq(vdim, 1.0 / vdim)
+    kz, ky, kx = np.meshgrid(q, q, np.arange(vdim // 2 + 1), indexing="ij")
+    k = np.sqrt(kx * kx + ky * ky + kz * kz)
+    T = 50.0 * np.exp(-k / (0.4 * vdim)) + 0.5
+    F = np.fft.rfftn(np.fft.ifftshift(m)) * T / 40.0
+    return F, T
+
+
+@pytest.mark.parametrize("grid_corr,kernel", [(True, tg3.KERNEL_TRILINEAR), (False, tg3.KERNEL_MKB),
+                                              (True, tg3.KERNEL_MKB)])
+def test_reconstruct_matches_oracle(grid_corr, kernel):
+    rng = np.random.default_rng(7 + kernel)
+    N, pf, maxR = 32, 2, 14
+    F, T = _inputs(rng, N, pf)
+    fsc = np.clip(1.05 - np.arange(N // 2 + 1) / (N / 2), 0, 1)
+    ctx = tg3.Context(0)
+    try:
+        ctx.insert_begin(N * pf, pf)
+        ctx.insert_load(torch.as_tensor(F.astype(np.complex64)).to(DEV),
+                        torch.as_tensor(T.astype(np.float32)).to(DEV))
+        vol = torch.empty((N, N, N), dtype=torch.float32, device=DEV)
+        rounds = ctx.reconstruct(vol, maxR, fsc=torch.as_tensor(fsc).to(DEV), join_half=True,
+                                 grid_corr=grid_corr, kernel=kernel)
+        ctx.sync()
+    finally:
+        ctx.close()
+    ref, ref_rounds = RC.reconstruct(F, T, pf, maxR, fsc=fsc, join_half=True, grid_corr=grid_corr,
+                                     kernel="mkb" if kernel == tg3.KERNEL_MKB else "trilinear")
+    got = vol.cpu().numpy()
+    assert rounds == ref_rounds
+    assert np.abs(got - ref).max() < 1e-3 * np.abs(ref).max()

@@ -309,6 +309,7 @@ extern "C" int tg3_ctx_destroy(tg3_ctx* c)
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     prep_release(c);
+    reco_release(c);
     for (auto& v : c->vol) cudaFree(v.blocks);
     for (auto& b : c->ws) cudaFree(b.ptr);
     cudaFree(c->pxMain.iCol);

@@ -86,6 +86,7 @@ enum WsSlot {
     WS_DEFOCUS,      // defocus search: block priors, block weights
     WS_CLASSES,      // multi-class 2-D scan: per-(image, class) weights
     WS_PREP,         // image preprocessing: statistics, real and transformed images
+    WS_RECO,         // reconstruction: T, W, C and the real-space map on the padded grid
     WS_COUNT
 };
 
@@ -427,6 +428,7 @@ namespace tg3 {
 int check_ctx(tg3_ctx* c);
 // the active pixel set, scaled by pf, fits a volume of vdim with `margin` to spare
 int check_geometry(tg3_ctx* c, int vdim, int pf, double margin = 1.0);
-// releases the context's preprocessing FFT plans
+// releases the context's preprocessing and reconstruction FFT plans
 void prep_release(tg3_ctx* c);
+void reco_release(tg3_ctx* c);
 }  // namespace tg3

@@ -1,0 +1,370 @@
+// Reconstruction of a map from the insertion accumulators (Reconstructor::
+// reconstruct, src/Reconstructor.cpp:1129-1790, 3-D, no symmetry), on the
+// padded half grid vdim = N pf, coordinates (x, y, z) with x in [0, vdim/2]
+// and y, z wrapped:
+//   Wiener filter from the FSC (RECONSTRUCTOR_WIENER_FILTER_FSC, :1236-1262):
+//     for (5 pf)^2 <= |k|^2 < (maxR pf)^2, u = rint(|k|): f = FSC[u / pf]
+//     (0 past its end), clamped to [1e-3, 1 - 1e-3], f = sqrt(2 f / (1 + f))
+//     when the half maps are joined; T /= f;
+//   T = max(T, 1e-25); W = 1 inside maxR pf, 0 outside (:1268-1300);
+//   grid correction (:1318-1460): up to 30 rounds of C = T W,
+//     C = FT(iFT(C) kRL(r^2) / nf) (convoluteC, :2593-2660; kRL the MKB
+//     kernel's real-space form at r = |x| / (N pf), nf = kRL(0)),
+//     W /= max(|C|, 1e-6) inside maxR pf, stopping when max ||C| - 1| < 1e-2
+//     or, after 10 rounds, when it failed twice in a row to fall below 0.95 x
+//     the previous (checkC with RECONSTRUCTOR_CHECK_C_MAX, :2520-2590);
+//     without it W = 1 / max(|T|, 1e-6) (:1463-1490);
+//   V = F W inside maxR pf; the inverse transform (1 / vdim^3); the central
+//   N^3 kept (VOL_EXTRACT_RL); divided by the kernel's real-space transform
+//   at |x| / (pf N): j0(pi r)^2 for the trilinear kernel (TIK_RL), MKB_RL(r,
+//   a pf, alpha) / MKB_RL(0, a pf, alpha) for MKB (:1700-1790).
+// MKB_RL (src/Functions/Functions.cpp:128-160, order 0): with u = 2 pi a r and
+// v = sqrt(|alpha^2 - u^2|), (2 pi)^1.5 a^3 / I0(alpha) I_1.5(v) / v^1.5 for
+// u <= alpha, J_1.5(v) / v^1.5 beyond; the half-integer Bessel functions in
+// their closed forms.
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "tg3_internal.cuh"
+
+namespace tg3 {
+namespace {
+
+// I_1.5(v) / v^1.5 and J_1.5(v) / v^1.5 (closed forms; series near 0)
+__host__ __device__ double i15_over(double v)
+{
+    if (v < 1e-3) return (1.0 + v * v / 10.0) / (3.0 * sqrt(M_PI / 2.0));
+    return sqrt(2.0 / M_PI) * (cosh(v) - sinh(v) / v) / (v * v);
+}
+
+__host__ __device__ double j15_over(double v)
+{
+    if (v < 1e-3) return (1.0 - v * v / 10.0) / (3.0 * sqrt(M_PI / 2.0));
+    return sqrt(2.0 / M_PI) * (sin(v) / v - cos(v)) / (v * v);
+}
+
+// the modified Bessel function I0 by its power series (alpha is O(10))
+__host__ __device__ double bessel_i0(double x)
+{
+    double s = 1.0, t = 1.0;
+    const double q = x * x / 4.0;
+    for (int k = 1; k < 200; k++) {
+        t *= q / ((double)k * k);
+        s += t;
+        if (t < 1e-17 * s) break;
+    }
+    return s;
+}
+
+__host__ __device__ double mkb_rl(double r, double a, double alpha, double i0a)
+{
+    const double u = 2.0 * M_PI * a * r;
+    const double w = pow(2.0 * M_PI, 1.5) * a * a * a / i0a;
+    if (u <= alpha) return w * i15_over(sqrt(alpha * alpha - u * u));
+    return w * j15_over(sqrt(u * u - alpha * alpha));
+}
+
+__device__ double tik_rl(double r)
+{
+    const double x = M_PI * r;
+    const double j0 = x < 1e-8 ? 1.0 : sin(x) / x;
+    return j0 * j0;
+}
+
+__device__ __forceinline__ int wrapc(int i, int n) { return i < n / 2 ? i : i - n; }
+
+// Wiener-filtered, floored T and the initial W (1 inside the radius)
+__global__ void k_reco_init(const float4* __restrict__ acc, int vdim, int pf, const double* __restrict__ fsc,
+                            int nFsc, int joinHalf, long long r2max, float* __restrict__ T,
+                            float* __restrict__ W)
+{
+    const int nx = vdim / 2 + 1;
+    const size_t n = (size_t)vdim * vdim * nx;
+    const long long r2min = 25LL * pf * pf;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(idx % nx);
+        const int y = wrapc((int)((idx / nx) % vdim), vdim);
+        const int z = wrapc((int)(idx / ((size_t)nx * vdim)), vdim);
+        const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
+        double t = acc[idx].z;
+        if (fsc && q >= r2min && q < r2max) {
+            const int u = (int)rint(sqrt((double)q));
+            double f = (u / pf >= nFsc) ? 0.0 : fsc[u / pf];
+            f = fmax(1e-3, fmin(1.0 - 1e-3, f));
+            if (joinHalf) f = sqrt(2.0 * f / (1.0 + f));
+            t /= f;
+        }
+        T[idx] = (float)fmax(t, 1e-25);
+        W[idx] = q < r2max ? 1.f : 0.f;
+    }
+}
+
+// C = T W (real, as a complex half grid)
+__global__ void k_reco_tw(const float* __restrict__ T, const float* __restrict__ W, size_t n,
+                          float2* __restrict__ C)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        C[i] = make_float2(T[i] * W[i], 0.f);
+}
+
+// A radial function of the integer squared radius q, tabulated once per call
+// (the kernels depend on x^2 + y^2 + z^2 only): tab[q] = scale k(sqrt(q) / s)
+// with k the MKB real-space form (mkb) or j0(pi r)^2.
+__global__ void k_radial_table(float* __restrict__ tab, int nq, double s, int mkb, double a,
+                               double alpha, double i0a, double scale)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const double r = sqrt((double)q) / s;
+        tab[q] = (float)(scale * (mkb ? mkb_rl(r, a, alpha, i0a) : tik_rl(r)));
+    }
+}
+
+// real-space C (after the unnormalised inverse) times kRL(r^2) / nf / vdim^3
+// (the table holds kRL / nf / vdim^3)
+__global__ void k_reco_kernel_rl(float* __restrict__ c, int vdim, const float* __restrict__ tab)
+{
+    const size_t n = (size_t)vdim * vdim * vdim;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int x = wrapc((int)(idx % vdim), vdim);
+        const int y = wrapc((int)((idx / vdim) % vdim), vdim);
+        const int z = wrapc((int)(idx / ((size_t)vdim * vdim)), vdim);
+        c[idx] *= tab[x * x + y * y + z * z];
+    }
+}
+
+// W /= max(|C|, 1e-6) inside the radius; diff = max ||C| - 1| there (float
+// bits compared as ints: the values are non-negative)
+__global__ void k_reco_update(const float2* __restrict__ C, int vdim, long long r2max,
+                              float* __restrict__ W, unsigned* __restrict__ diffBits)
+{
+    const int nx = vdim / 2 + 1;
+    const size_t n = (size_t)vdim * vdim * nx;
+    float dmax = 0.f;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(idx % nx);
+        const int y = wrapc((int)((idx / nx) % vdim), vdim);
+        const int z = wrapc((int)(idx / ((size_t)nx * vdim)), vdim);
+        const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
+        if (q < r2max) {
+            const float m = sqrtf(C[idx].x * C[idx].x + C[idx].y * C[idx].y);
+            W[idx] = W[idx] / fmaxf(m, 1e-6f);
+            dmax = fmaxf(dmax, fabsf(m - 1.f));
+        }
+    }
+    for (int o = 16; o; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(diffBits, __float_as_uint(dmax));
+}
+
+// without grid correction: W = 1 / max(|T|, 1e-6) inside the radius
+__global__ void k_reco_w_from_t(const float* __restrict__ T, int vdim, long long r2max,
+                                float* __restrict__ W)
+{
+    const int nx = vdim / 2 + 1;
+    const size_t n = (size_t)vdim * vdim * nx;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(idx % nx);
+        const int y = wrapc((int)((idx / nx) % vdim), vdim);
+        const int z = wrapc((int)(idx / ((size_t)nx * vdim)), vdim);
+        const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
+        if (q < r2max) W[idx] = 1.f / fmaxf(fabsf(T[idx]), 1e-6f);
+    }
+}
+
+// V = F W inside the radius, 0 outside
+__global__ void k_reco_fw(const float4* __restrict__ acc, const float* __restrict__ W, int vdim,
+                          long long r2max, float2* __restrict__ V)
+{
+    const int nx = vdim / 2 + 1;
+    const size_t n = (size_t)vdim * vdim * nx;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(idx % nx);
+        const int y = wrapc((int)((idx / nx) % vdim), vdim);
+        const int z = wrapc((int)(idx / ((size_t)nx * vdim)), vdim);
+        const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
+        const float4 a = acc[idx];
+        V[idx] = q < r2max ? make_float2(a.x * W[idx], a.y * W[idx]) : make_float2(0.f, 0.f);
+    }
+}
+
+// the central N^3 of the padded real-space map, in centred order (index i +
+// N/2 for coordinate i), divided by the kernel's real-space transform
+// (the table holds the kernel's real-space transform times vdim^3)
+__global__ void k_reco_extract(const float* __restrict__ pad, int vdim, int N,
+                               const float* __restrict__ tab, float* __restrict__ out)
+{
+    const size_t n = (size_t)N * N * N;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(idx % N) - N / 2;
+        const int y = (int)((idx / N) % N) - N / 2;
+        const int z = (int)(idx / ((size_t)N * N)) - N / 2;
+        const int px = x < 0 ? x + vdim : x, py = y < 0 ? y + vdim : y, pz = z < 0 ? z + vdim : z;
+        out[idx] = pad[((size_t)pz * vdim + py) * vdim + px] / tab[x * x + y * y + z * z];
+    }
+}
+
+// accumulator <- (F, T): the sums of several contexts or ranks loaded back
+__global__ void k_acc_load(const float2* __restrict__ F, const float* __restrict__ T, size_t n,
+                           float4* __restrict__ acc)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        acc[i] = make_float4(F[i].x, F[i].y, T[i], 0.f);
+}
+
+struct Plan3 {
+    tg3_ctx* c;
+    int vdim, type;
+    cufftHandle h;
+};
+std::vector<Plan3> g_plans3;
+
+int plan3(tg3_ctx* c, int vdim, cufftType type, cufftHandle* out)
+{
+    for (auto& p : g_plans3)
+        if (p.c == c && p.vdim == vdim && p.type == (int)type) {
+            *out = p.h;
+            return TG3_OK;
+        }
+    cufftHandle h;
+    if (cufftPlan3d(&h, vdim, vdim, vdim, type) != CUFFT_SUCCESS)
+        return fail(TG3_ERR_CUDA, "cuFFT 3-D plan creation failed");
+    g_plans3.push_back({c, vdim, (int)type, h});
+    *out = h;
+    return TG3_OK;
+}
+
+}  // namespace
+
+void reco_release(tg3_ctx* c)
+{
+    for (size_t i = 0; i < g_plans3.size();) {
+        if (g_plans3[i].c == c) {
+            cufftDestroy(g_plans3[i].h);
+            g_plans3.erase(g_plans3.begin() + i);
+        } else {
+            i++;
+        }
+    }
+}
+
+}  // namespace tg3
+
+using namespace tg3;
+
+extern "C" int tg3_ctx_insert_load_d(tg3_ctx* c, const float* F, const float* T)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (!c->ins.acc) return fail(TG3_ERR_STATE, "no insertion accumulator (tg3_ctx_insert_begin)");
+    if (!F || !T) return fail(TG3_ERR_ARG, "null device pointer");
+    const int vdim = c->ins.vdim;
+    const size_t n = (size_t)vdim * vdim * (vdim / 2 + 1);
+    k_acc_load<<<152 * 8, 256, 0, c->stream>>>(reinterpret_cast<const float2*>(F), T, n, c->ins.acc);
+    TG3_LAUNCH_CHECK("accumulator load");
+    return TG3_OK;
+}
+
+extern "C" int tg3_ctx_reconstruct_d(tg3_ctx* c, const double* fsc, int nFsc, int joinHalf,
+                                     int maxRadius, int gridCorr, int kernel, float a,
+                                     float alpha, float* vol, int* rounds)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (!c->ins.acc) return fail(TG3_ERR_STATE, "no insertion accumulator (tg3_ctx_insert_begin)");
+    if (!vol || maxRadius <= 0 || (fsc && nFsc <= 0) ||
+        (kernel != TG3_KERNEL_MKB && kernel != TG3_KERNEL_TRILINEAR))
+        return fail(TG3_ERR_ARG, "bad reconstruction arguments");
+    if ((gridCorr || kernel == TG3_KERNEL_MKB) && !(a > 0 && alpha > 0))
+        return fail(TG3_ERR_ARG, "MKB parameters a and alpha must be positive");
+    const int vdim = c->ins.vdim, pf = c->ins.pf, N = vdim / pf;
+    if (maxRadius * pf > vdim / 2) return fail(TG3_ERR_ARG, "maxRadius beyond the padded grid");
+    const size_t nh = (size_t)vdim * vdim * (vdim / 2 + 1), nr = (size_t)vdim * vdim * vdim;
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    const int nqPad = 3 * (vdim / 2) * (vdim / 2) + 1, nqBox = 3 * (N / 2) * (N / 2) + 1;
+    const size_t oT = 0, oW = up(4 * nh), oC = oW + up(4 * nh), oR = oC + up(8 * nh),
+                 oD = oR + up(4 * nr), oK = oD + 256, oE = oK + up(4 * (size_t)nqPad),
+                 total = oE + up(4 * (size_t)nqBox);
+    char* b = (char*)ws_get(c, WS_RECO, total, &st);
+    if (!b) return st;
+    float* T = (float*)(b + oT);
+    float* W = (float*)(b + oW);
+    float2* C = (float2*)(b + oC);
+    float* R = (float*)(b + oR);
+    unsigned* dBits = (unsigned*)(b + oD);
+    float* tabK = (float*)(b + oK);
+    float* tabE = (float*)(b + oE);
+    cudaStream_t s = c->stream;
+    const long long r2max = (long long)maxRadius * pf * maxRadius * pf;
+    const int G = 152 * 8;
+    k_reco_init<<<G, 256, 0, s>>>(c->ins.acc, vdim, pf, fsc, nFsc, joinHalf, r2max, T, W);
+    TG3_LAUNCH_CHECK("reconstruction set-up");
+    const double i0a = bessel_i0(alpha);
+    int m = 0;
+    if (gridCorr) {
+        cufftHandle inv, fwd;
+        if ((st = plan3(c, vdim, CUFFT_C2R, &inv)) || (st = plan3(c, vdim, CUFFT_R2C, &fwd)))
+            return st;
+        if (cufftSetStream(inv, s) != CUFFT_SUCCESS || cufftSetStream(fwd, s) != CUFFT_SUCCESS)
+            return fail(TG3_ERR_CUDA, "cuFFT stream");
+        const double invNf = 1.0 / mkb_rl(0.0, a, alpha, i0a);
+        k_radial_table<<<(nqPad + 255) / 256, 256, 0, s>>>(
+            tabK, nqPad, (double)N * pf, 1, a, alpha, i0a,
+            invNf / ((double)vdim * vdim * vdim));
+        TG3_LAUNCH_CHECK("balancing kernel table");
+        float diff = 3.4e38f, prev;
+        int noDecrease = 0;
+        for (m = 0; m < 30; m++) {
+            k_reco_tw<<<G, 256, 0, s>>>(T, W, nh, C);
+            TG3_LAUNCH_CHECK("balancing C = T W");
+            if (cufftExecC2R(inv, reinterpret_cast<cufftComplex*>(C), R) != CUFFT_SUCCESS)
+                return fail(TG3_ERR_CUDA, "cuFFT inverse transform failed");
+            k_reco_kernel_rl<<<G, 256, 0, s>>>(R, vdim, tabK);
+            TG3_LAUNCH_CHECK("balancing kernel product");
+            if (cufftExecR2C(fwd, R, reinterpret_cast<cufftComplex*>(C)) != CUFFT_SUCCESS)
+                return fail(TG3_ERR_CUDA, "cuFFT forward transform failed");
+            TG3_CUDA(cudaMemsetAsync(dBits, 0, sizeof(unsigned), s));
+            k_reco_update<<<G, 256, 0, s>>>(C, vdim, r2max, W, dBits);
+            TG3_LAUNCH_CHECK("balancing update");
+            unsigned bits = 0;
+            TG3_CUDA(cudaMemcpyAsync(&bits, dBits, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+            TG3_CUDA(cudaStreamSynchronize(s));
+            prev = diff;
+            std::memcpy(&diff, &bits, sizeof(float));
+            noDecrease = diff > prev * 0.95f ? noDecrease + 1 : 0;
+            if (diff < 1e-2f || (m >= 10 && noDecrease == 2)) break;
+        }
+    } else {
+        k_reco_w_from_t<<<G, 256, 0, s>>>(T, vdim, r2max, W);
+        TG3_LAUNCH_CHECK("W from T");
+    }
+    if (rounds) *rounds = gridCorr ? std::min(m + 1, 30) : 0;
+    cufftHandle inv;
+    if ((st = plan3(c, vdim, CUFFT_C2R, &inv))) return st;
+    if (cufftSetStream(inv, s) != CUFFT_SUCCESS) return fail(TG3_ERR_CUDA, "cuFFT stream");
+    k_reco_fw<<<G, 256, 0, s>>>(c->ins.acc, W, vdim, r2max, C);
+    TG3_LAUNCH_CHECK("F W");
+    if (cufftExecC2R(inv, reinterpret_cast<cufftComplex*>(C), R) != CUFFT_SUCCESS)
+        return fail(TG3_ERR_CUDA, "cuFFT inverse transform failed");
+    const int mkb = kernel == TG3_KERNEL_MKB;
+    const double nf = mkb ? mkb_rl(0.0, (double)a * pf, alpha, i0a) : 1.0;
+    // gridding correction: the map (times vdim^3 after the unnormalised
+    // inverse) over the kernel's real-space transform at |x| / (pf N)
+    k_radial_table<<<(nqBox + 255) / 256, 256, 0, s>>>(
+        tabE, nqBox, (double)pf * N, mkb, (double)a * pf, alpha, i0a,
+        (double)vdim * vdim * vdim / nf);
+    TG3_LAUNCH_CHECK("gridding correction table");
+    k_reco_extract<<<G, 256, 0, s>>>(R, vdim, N, tabE, vol);
+    TG3_LAUNCH_CHECK("extract and gridding correction");
+    return TG3_OK;
+}

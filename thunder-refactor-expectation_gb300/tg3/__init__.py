@@ -37,7 +37,8 @@ EXPORTS = [
     "tg3_cnn_contrastive", "tg3_cnn_embed", "tg3_cnn_match_propose", "tg3_ctx_set_bank",
     "tg3_local_phase_bank_d", "tg3_local_phase_ctf_d", "tg3_ExpectLocal3D_ctf",
     "tg3_ExpectGlobal2D", "tg3_global_scan2d_d", "tg3_InsertI2D", "tg3_global_scan2d_classes_d",
-    "tg3_prepare_images_d", "tg3_sigma_d", "tg3_mrc_info", "tg3_mrc_read", "tg3_mrc_write", "tg3_thu_count",
+    "tg3_prepare_images_d", "tg3_sigma_d", "tg3_ctx_reconstruct_d", "tg3_ctx_insert_load_d",
+    "tg3_mrc_info", "tg3_mrc_read", "tg3_mrc_write", "tg3_thu_count",
     "tg3_thu_read", "tg3_thu_write",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
 ]
@@ -132,6 +133,8 @@ def lib():
             "tg3_global_scan2d_classes_d": ([_P, _P] + [_I] * 6 + [_P] * 11 + [_I], _I),
             "tg3_prepare_images_d": ([_P, _P, _I, _I, _F, _I, _F, _P, _P], _I),
             "tg3_sigma_d": ([_P, _I, _I] + [_P] * 7 + [_I, _I, _I, _F, _F, _P, _P], _I),
+            "tg3_ctx_reconstruct_d": ([_P, _P, _I, _I, _I, _I, _I, _F, _F, _P, _P], _I),
+            "tg3_ctx_insert_load_d": ([_P, _P, _P], _I),
             "tg3_mrc_info": ([ctypes.c_char_p] + [_P] * 5, _I),
             "tg3_mrc_read": ([ctypes.c_char_p, _I, _I, _P], _I),
             "tg3_mrc_write": ([ctypes.c_char_p, _P, _I, _I, _I, _F, _I], _I),
@@ -350,6 +353,23 @@ class Context:
                                 ptr(trans), ptr(offset), ptr(group), n_group, int(by_group),
                                 r_sig, float(mask_radius), float(pixel_size), ptr(sig),
                                 ptr(sig_rcp)))
+
+    def insert_load(self, F, T):
+        """Accumulator <- F (complex64) and T (float32), device half grids."""
+        self._hold(F, T)
+        check(lib().tg3_ctx_insert_load_d(self.h, ptr(F), ptr(T)))
+
+    def reconstruct(self, vol, max_radius, fsc=None, join_half=False, grid_corr=True,
+                    kernel=None, a=1.9, alpha=15.0):
+        """The map from the insertion accumulators into vol (device float32
+        (N, N, N), centred); returns the number of balancing rounds."""
+        kernel = KERNEL_TRILINEAR if kernel is None else kernel
+        self._hold(vol, fsc)
+        rounds = ctypes.c_int(0)
+        check(lib().tg3_ctx_reconstruct_d(self.h, ptr(fsc), 0 if fsc is None else len(fsc),
+                                          int(join_half), max_radius, int(grid_corr), kernel,
+                                          float(a), float(alpha), ptr(vol), ctypes.byref(rounds)))
+        return rounds.value
 
     def resample(self, nP, n, u, w, perm, u0, peak, nOut, src, wOut, top):
         self._hold(u, w, perm, u0, peak, src, wOut, top)
