@@ -87,13 +87,16 @@ __global__ void k_reco_init(const float4* __restrict__ acc, int vdim, int pf, co
     const long long r2min = 25LL * pf * pf;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
-        const int x = (int)(idx % nx);
-        const int y = wrapc((int)((idx / nx) % vdim), vdim);
-        const int z = wrapc((int)(idx / ((size_t)nx * vdim)), vdim);
+        const unsigned u32 = (unsigned)idx, row = u32 / (unsigned)nx;
+        const int x = (int)(u32 - row * (unsigned)nx);
+        const int y = wrapc((int)(row % (unsigned)vdim), vdim);
+        const int z = wrapc((int)(row / (unsigned)vdim), vdim);
         const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
         double t = acc[idx].z;
         if (fsc && q >= r2min && q < r2max) {
-            const int u = (int)rint(sqrt((double)q));
+            // rint(sqrt(q)) in FP32 is exact here: no integer q lies within
+            // FP32 rounding of a half-integer radius below 2^11
+            const int u = (int)rintf(sqrtf((float)q));
             double f = (u / pf >= nFsc) ? 0.0 : fsc[u / pf];
             f = fmax(1e-3, fmin(1.0 - 1e-3, f));
             if (joinHalf) f = sqrt(2.0 * f / (1.0 + f));
@@ -132,9 +135,10 @@ __global__ void k_reco_kernel_rl(float* __restrict__ c, int vdim, const float* _
     const size_t n = (size_t)vdim * vdim * vdim;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
-        const int x = wrapc((int)(idx % vdim), vdim);
-        const int y = wrapc((int)((idx / vdim) % vdim), vdim);
-        const int z = wrapc((int)(idx / ((size_t)vdim * vdim)), vdim);
+        const unsigned u32 = (unsigned)idx, row = u32 / (unsigned)vdim;
+        const int x = wrapc((int)(u32 - row * (unsigned)vdim), vdim);
+        const int y = wrapc((int)(row % (unsigned)vdim), vdim);
+        const int z = wrapc((int)(row / (unsigned)vdim), vdim);
         c[idx] *= tab[x * x + y * y + z * z];
     }
 }
@@ -149,9 +153,10 @@ __global__ void k_reco_update(const float2* __restrict__ C, int vdim, long long 
     float dmax = 0.f;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
-        const int x = (int)(idx % nx);
-        const int y = wrapc((int)((idx / nx) % vdim), vdim);
-        const int z = wrapc((int)(idx / ((size_t)nx * vdim)), vdim);
+        const unsigned u32 = (unsigned)idx, row = u32 / (unsigned)nx;
+        const int x = (int)(u32 - row * (unsigned)nx);
+        const int y = wrapc((int)(row % (unsigned)vdim), vdim);
+        const int z = wrapc((int)(row / (unsigned)vdim), vdim);
         const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
         if (q < r2max) {
             const float m = sqrtf(C[idx].x * C[idx].x + C[idx].y * C[idx].y);
@@ -171,9 +176,10 @@ __global__ void k_reco_w_from_t(const float* __restrict__ T, int vdim, long long
     const size_t n = (size_t)vdim * vdim * nx;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
-        const int x = (int)(idx % nx);
-        const int y = wrapc((int)((idx / nx) % vdim), vdim);
-        const int z = wrapc((int)(idx / ((size_t)nx * vdim)), vdim);
+        const unsigned u32 = (unsigned)idx, row = u32 / (unsigned)nx;
+        const int x = (int)(u32 - row * (unsigned)nx);
+        const int y = wrapc((int)(row % (unsigned)vdim), vdim);
+        const int z = wrapc((int)(row / (unsigned)vdim), vdim);
         const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
         if (q < r2max) W[idx] = 1.f / fmaxf(fabsf(T[idx]), 1e-6f);
     }
@@ -187,9 +193,10 @@ __global__ void k_reco_fw(const float4* __restrict__ acc, const float* __restric
     const size_t n = (size_t)vdim * vdim * nx;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
-        const int x = (int)(idx % nx);
-        const int y = wrapc((int)((idx / nx) % vdim), vdim);
-        const int z = wrapc((int)(idx / ((size_t)nx * vdim)), vdim);
+        const unsigned u32 = (unsigned)idx, row = u32 / (unsigned)nx;
+        const int x = (int)(u32 - row * (unsigned)nx);
+        const int y = wrapc((int)(row % (unsigned)vdim), vdim);
+        const int z = wrapc((int)(row / (unsigned)vdim), vdim);
         const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
         const float4 a = acc[idx];
         V[idx] = q < r2max ? make_float2(a.x * W[idx], a.y * W[idx]) : make_float2(0.f, 0.f);
@@ -289,6 +296,8 @@ extern "C" int tg3_ctx_reconstruct_d(tg3_ctx* c, const double* fsc, int nFsc, in
         return fail(TG3_ERR_ARG, "MKB parameters a and alpha must be positive");
     const int vdim = c->ins.vdim, pf = c->ins.pf, N = vdim / pf;
     if (maxRadius * pf > vdim / 2) return fail(TG3_ERR_ARG, "maxRadius beyond the padded grid");
+    // 32-bit voxel indices in the kernels
+    if ((size_t)vdim * vdim * vdim >= (1ull << 31)) return fail(TG3_ERR_UNSUPPORTED, "padded grid above 1290^3");
     const size_t nh = (size_t)vdim * vdim * (vdim / 2 + 1), nr = (size_t)vdim * vdim * vdim;
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
     const int nqPad = 3 * (vdim / 2) * (vdim / 2) + 1, nqBox = 3 * (N / 2) * (N / 2) + 1;
