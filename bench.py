@@ -645,6 +645,35 @@ def run_class2d(args, rank, world, local_rank):
         e2e()
     e2e_ms = reduce_max(world, (time.perf_counter() - t0) * 1e3) / e2e_steps
     e2e_rec = float((wCh.reshape(n, nK).argmax(1) == kt.cpu().numpy()).mean())
+    # 2-D insertion through the reference-shaped entry (InsertI2D): every
+    # particle's best (class, rotation, translation) into its class's
+    # accumulators, host volumes in and out, as the reference's call
+    best_k = wCh.reshape(n, nK).argmax(1).astype(np.int32)
+    wRb = wRh.reshape(n, nK, nR)[np.arange(n), best_k]
+    wTb = wTh.reshape(n, nK, nT)[np.arange(n), best_k]
+    nRd = np.ascontiguousarray(rot_np[wRb.argmax(1)])
+    nTd = np.ascontiguousarray(trans_np[wTb.argmax(1)])
+    vdim = pf * box
+    F2 = np.zeros((nK, vdim, vdim // 2 + 1), np.complex64)
+    T2 = np.zeros((nK, vdim, vdim // 2 + 1), np.float32)
+    O2 = np.zeros((nK, 2))
+    cnt = np.zeros(nK, np.int32)
+    wl = np.ones(n, np.float32)
+    offS = np.zeros((n, 2))
+    icp, irp = np.ascontiguousarray(ic * pf), np.ascontiguousarray(ir * pf)
+
+    def insert2d():
+        tg3.check(tg3.lib().tg3_InsertI2D(
+            tg3.ptr(F2), tg3.ptr(T2), tg3.ptr(O2), tg3.ptr(cnt), tg3.ptr(host["dat"]),
+            tg3.ptr(host["ctf"]), tg3.ptr(host["sig"]), tg3.ptr(wl), tg3.ptr(offS),
+            tg3.ptr(best_k), tg3.ptr(nRd), tg3.ptr(nTd), None, None, tg3.ptr(icp), tg3.ptr(irp),
+            px, 0, nK, pf, K, 1, box, vdim, n))
+
+    insert2d()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        insert2d()
+    ins_ms = (time.perf_counter() - t0) * 1e3 / 3
     # roofline of the scoring GEMM (the "cross" stage: 4 K FLOP per hypothesis)
     cross = stages["cross"][0] / max(stages["cross"][1], 1)
     flop = 4.0 * K * nK * nR * nT * n
@@ -671,7 +700,10 @@ def run_class2d(args, rank, world, local_rank):
                    "h2d_bytes_per_step": int(host["vol"].nbytes + host["dat"].nbytes +
                                              host["ctf"].nbytes + host["sig"].nbytes),
                    "d2h_bytes_per_step": int(wCh.nbytes + wRh.nbytes + wTh.nbytes),
-                   "class_recovered": round(e2e_rec, 4)}}
+                   "class_recovered": round(e2e_rec, 4)},
+           "insert2d": {"path": "tg3_InsertI2D, host volumes in and out, 16 classes",
+                        "images_per_s": round(n / (ins_ms * 1e-3), 1),
+                        "ms_per_call": round(ins_ms, 3)}}
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle as O
         m = 16
