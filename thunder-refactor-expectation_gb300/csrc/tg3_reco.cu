@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "tg3_internal.cuh"
@@ -235,9 +236,11 @@ struct Plan3 {
     cufftHandle h;
 };
 std::vector<Plan3> g_plans3;
+std::mutex g_plans3Lock;
 
 int plan3(tg3_ctx* c, int vdim, cufftType type, cufftHandle* out)
 {
+    std::lock_guard<std::mutex> g(g_plans3Lock);
     for (auto& p : g_plans3)
         if (p.c == c && p.vdim == vdim && p.type == (int)type) {
             *out = p.h;
@@ -255,6 +258,7 @@ int plan3(tg3_ctx* c, int vdim, cufftType type, cufftHandle* out)
 
 void reco_release(tg3_ctx* c)
 {
+    std::lock_guard<std::mutex> g(g_plans3Lock);
     for (size_t i = 0; i < g_plans3.size();) {
         if (g_plans3[i].c == c) {
             cufftDestroy(g_plans3[i].h);
