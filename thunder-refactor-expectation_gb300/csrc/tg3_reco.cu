@@ -145,9 +145,11 @@ __global__ void k_reco_kernel_rl(float* __restrict__ c, int vdim, const float* _
 }
 
 // W /= max(|C|, 1e-6) inside the radius; diff = max ||C| - 1| there (float
-// bits compared as ints: the values are non-negative)
-__global__ void k_reco_update(const float2* __restrict__ C, int vdim, long long r2max,
-                              float* __restrict__ W, unsigned* __restrict__ diffBits)
+// bits compared as ints: the values are non-negative); then C <- T W for the
+// next round (the inverse transform consumes C)
+__global__ void k_reco_update(float2* __restrict__ C, const float* __restrict__ T, int vdim,
+                              long long r2max, float* __restrict__ W,
+                              unsigned* __restrict__ diffBits)
 {
     const int nx = vdim / 2 + 1;
     const size_t n = (size_t)vdim * vdim * nx;
@@ -159,11 +161,14 @@ __global__ void k_reco_update(const float2* __restrict__ C, int vdim, long long 
         const int y = wrapc((int)(row % (unsigned)vdim), vdim);
         const int z = wrapc((int)(row / (unsigned)vdim), vdim);
         const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
+        float w = W[idx];
         if (q < r2max) {
             const float m = sqrtf(C[idx].x * C[idx].x + C[idx].y * C[idx].y);
-            W[idx] = W[idx] / fmaxf(m, 1e-6f);
+            w = w / fmaxf(m, 1e-6f);
+            W[idx] = w;
             dmax = fmaxf(dmax, fabsf(m - 1.f));
         }
+        C[idx] = make_float2(T[idx] * w, 0.f);
     }
     for (int o = 16; o; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
     if ((threadIdx.x & 31) == 0) atomicMax(diffBits, __float_as_uint(dmax));
@@ -337,9 +342,9 @@ extern "C" int tg3_ctx_reconstruct_d(tg3_ctx* c, const double* fsc, int nFsc, in
         TG3_LAUNCH_CHECK("balancing kernel table");
         float diff = 3.4e38f, prev;
         int noDecrease = 0;
+        k_reco_tw<<<G, 256, 0, s>>>(T, W, nh, C);
+        TG3_LAUNCH_CHECK("balancing C = T W");
         for (m = 0; m < 30; m++) {
-            k_reco_tw<<<G, 256, 0, s>>>(T, W, nh, C);
-            TG3_LAUNCH_CHECK("balancing C = T W");
             if (cufftExecC2R(inv, reinterpret_cast<cufftComplex*>(C), R) != CUFFT_SUCCESS)
                 return fail(TG3_ERR_CUDA, "cuFFT inverse transform failed");
             k_reco_kernel_rl<<<G, 256, 0, s>>>(R, vdim, tabK);
@@ -347,7 +352,7 @@ extern "C" int tg3_ctx_reconstruct_d(tg3_ctx* c, const double* fsc, int nFsc, in
             if (cufftExecR2C(fwd, R, reinterpret_cast<cufftComplex*>(C)) != CUFFT_SUCCESS)
                 return fail(TG3_ERR_CUDA, "cuFFT forward transform failed");
             TG3_CUDA(cudaMemsetAsync(dBits, 0, sizeof(unsigned), s));
-            k_reco_update<<<G, 256, 0, s>>>(C, vdim, r2max, W, dBits);
+            k_reco_update<<<G, 256, 0, s>>>(C, T, vdim, r2max, W, dBits);
             TG3_LAUNCH_CHECK("balancing update");
             unsigned bits = 0;
             TG3_CUDA(cudaMemcpyAsync(&bits, dBits, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
