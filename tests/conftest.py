@@ -19,3 +19,11 @@ def pytest_configure(config):
 def golden():
     import numpy as np
     return dict(np.load(ROOT / "tests" / "golden" / "ref_golden.npz"))
+
+
+@pytest.fixture(scope="session")
+def golden_formats():
+    """Outputs of the reference's 2-D, preprocessing, spectrum and MRC
+    routines (tests/golden/make_golden.py)."""
+    import numpy as np
+    return dict(np.load(ROOT / "tests" / "golden" / "ref_golden_formats.npz"))

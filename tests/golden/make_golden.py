@@ -2,7 +2,8 @@
 own compiled routines (oracle/_ref/libthunder_ref.so, built by
 oracle/ref/Makefile from the THUNDER sources) on small seeded cases.
 
-Run in a checkout that has the THUNDER tree:
+Also writes tests/golden/ref_golden_formats.npz (the 2-D, preprocessing,
+spectrum and MRC routines).  Run in a checkout that has the THUNDER tree:
     python tests/golden/make_golden.py
 The fixture pins the oracle (tests/test_oracle_golden.py) on machines that
 do not have the reference sources."""
@@ -124,5 +125,71 @@ def main():
     print(f"wrote {out} ({out.stat().st_size} bytes)")
 
 
+def main_formats():
+    """ref_golden_formats.npz: the 2-D projection and insertion
+    (Image::getByInterpolationFT, Image::addFT), image preprocessing
+    (bgMeanStddev, bgStddev, softMask), powerSpectrum and the MRC reader."""
+    import tempfile
+    from tg3 import io
+    R = O.ref()
+    if R is None:
+        raise SystemExit("reference cross-check library unavailable")
+    rng = np.random.default_rng(20261204)
+    g = {}
+    box, pf = 16, 2
+    vdim = box * pf
+    iCol, iRow = synth.pixel_index(box, 6, 1)[:2]
+    K = len(iCol)
+    g["iCol"], g["iRow"], g["box"], g["pf"] = iCol, iRow, box, pf
+    img = np.ascontiguousarray(rng.standard_normal((vdim, vdim // 2 + 1)) +
+                               1j * rng.standard_normal((vdim, vdim // 2 + 1)))
+    ang = rng.uniform(0, 2 * np.pi, 6)
+    rot = np.ascontiguousarray(np.stack([np.cos(ang), np.sin(ang)], 1))
+    p2 = np.zeros((6, K), np.complex128)
+    R.ref_project2d(img, vdim, rot, 6, iCol, iRow, K, pf, p2)
+    g["p2_img"], g["p2_rot"], g["p2"] = img, rot, p2
+    F = np.zeros((vdim, vdim // 2 + 1), np.complex128)
+    T = np.zeros((vdim, vdim // 2 + 1))
+    ic, ir = np.ascontiguousarray(iCol * pf, np.int32), np.ascontiguousarray(iRow * pf, np.int32)
+    ins_img = rng.standard_normal((3, K)) + 1j * rng.standard_normal((3, K))
+    ins_ctf = rng.uniform(-1, 1, (3, K))
+    ins_w = rng.uniform(0.2, 1.0, 3)
+    for s in range(3):
+        R.ref_insert2d(F, T, vdim, np.ascontiguousarray(ins_img[s]), np.ascontiguousarray(ins_ctf[s]),
+                       rot[s, 0], rot[s, 1], float(ins_w[s]), ic, ir, K)
+    g["i2_img"], g["i2_ctf"], g["i2_w"], g["i2_F"], g["i2_T"] = ins_img, ins_ctf, ins_w, F, T
+    N, r = 32, 11.3
+    c = np.arange(N) - N // 2
+    xx, yy = np.meshgrid(c, c)
+    imgs = 2.0 + 0.6 * rng.standard_normal((2, N, N)) + 3.0 * np.exp(-(xx ** 2 + yy ** 2) / 40.0)
+    outs, stats = [], []
+    for m in (1, 0):
+        for l in range(2):
+            o, st = np.zeros(N * N), np.zeros(3)
+            R.ref_prep_image(np.ascontiguousarray(io.centred(imgs[l])).ravel(), N, r, m, o, st)
+            outs.append(o.reshape(N, N))
+            stats.append(st)
+    g["pp_imgs"], g["pp_r"], g["pp_out"], g["pp_stats"] = imgs, np.array([r]), np.stack(outs), np.stack(stats)
+    Fh = rng.standard_normal((N, N // 2 + 1)) + 1j * rng.standard_normal((N, N // 2 + 1))
+    ps = np.zeros(15)
+    R.ref_power_spectrum(np.ascontiguousarray(Fh), N, 15, ps)
+    g["ps_F"], g["ps"] = Fh, ps
+    stack = rng.standard_normal((2, 12, 12)).astype(np.float32)
+    with tempfile.TemporaryDirectory() as td:
+        path = str(Path(td) / "s.mrcs")
+        io.write_mrc(path, stack)
+        reads = []
+        for s in range(2):
+            o = np.zeros(144)
+            if R.ref_read_mrc(path.encode(), s, 12, o):
+                raise SystemExit("reference MRC read failed")
+            reads.append(o.reshape(12, 12))
+    g["mrc_stack"], g["mrc_ref"] = stack, np.stack(reads)
+    out = Path(__file__).resolve().parent / "ref_golden_formats.npz"
+    np.savez_compressed(out, **g)
+    print(f"wrote {out} ({out.stat().st_size} bytes)")
+
+
 if __name__ == "__main__":
     main()
+    main_formats()
