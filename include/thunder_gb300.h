@@ -581,10 +581,12 @@ int tg3_fsc_d(const float* A, const float* B, int vdim, int nShell, double* fsc,
  * Limit: 256 + 4 ((nR + nT) Kp + nR nT + nR) + 512 bytes (rounded up to
  * 256-byte pieces) must fit the scratch, Kp = 2K rounded up to 64; larger
  * sets are rejected with TG3_ERR_ARG.  The call returns after the work has
- * finished on `stream` (cudaStream_t, NULL for the legacy stream).
- * The first call on a device looks up the scratch array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  Every call shares the one array: calls that
+ * finished on `stream` (cudaStream_t, NULL for the legacy stream): it reads
+ * its error word back with a copy on that stream and synchronises that
+ * stream only.  The first call on a device looks up the scratch array's
+ * device address (cudaGetSymbolAddress) with that device current, and so
+ * does the first call after the device's context is re-created (after
+ * cudaDeviceReset); make that first call before any stream capture.  Every call shares the one array: calls that
  * may overlap on the GPU (other streams, unsynchronised host threads) race
  * and must not be issued.  Each call writes all the scratch it reads, so no
  * clearing is needed between calls. */

@@ -33,6 +33,23 @@ def _case(seed, box=32, pf=2, px=1.5, rU=12, nR=80, nT=15):
                 pwR=rng.random(nR) + 0.5, pwT=rng.random(nT) + 0.5, nR=nR, nT=nT)
 
 
+def _edge_case(seed=404, box=32, nR=40, nT=9):
+    """Padding 1 with every pixel within radius 15 of a box-32 image: the
+    pixel (0, 15) at the identity rotation samples row y0 = 15 = vdim / 2 - 1,
+    whose upper corner is the stored Nyquist row; both entry points must take it."""
+    import dataclasses
+    c = _case(seed, box=box, pf=1, rU=16, nR=nR, nT=nT)
+    st = c["st"]
+    keep = np.nonzero(st.iCol.astype(np.int64) ** 2 + st.iRow.astype(np.int64) ** 2 <= 225)[0]
+    assert np.any((st.iCol[keep] == 0) & (st.iRow[keep] == 15))
+    c["st"] = dataclasses.replace(st, iCol=st.iCol[keep], iRow=st.iRow[keep], iSig=st.iSig[keep],
+                                  ctf=st.ctf[:, keep], dat=st.dat[:, keep],
+                                  sigRcp=st.sigRcp[:, keep])
+    c["q"] = c["q"].copy()
+    c["q"][0] = (1.0, 0.0, 0.0, 0.0)
+    return c
+
+
 def _dev(x):
     return torch.as_tensor(np.ascontiguousarray(x)).to(DEV)
 
@@ -73,7 +90,8 @@ def _noalloc(c):
     torch.cuda.synchronize()
     p = tg3.ptr
     tg3.check(tg3.lib().tg3_local_phase_noalloc(
-        p(ins["vol"]), c["vol"].shape[0], c["pf"], p(ins["iCol"]), p(ins["iRow"]), st.K, c["box"],
+        p(ins["vol"]), c["vol"].shape[0], c["pf"], p(ins["iCol"]), p(ins["iRow"]), len(st.iCol),
+        c["box"],
         p(ins["dat"]), p(ins["ctf"]), p(ins["sig"]), p(ins["q"]), c["nR"], p(ins["t"]), c["nT"],
         p(ins["pwR"]), p(ins["pwT"]), None, p(o["wC"]), p(o["wR"]), p(o["wT"]), p(o["base"]),
         p(o["dvp"]), None))
@@ -95,6 +113,11 @@ def test_noalloc_matches_regular_entry_twice():
     second = _case(202, nR=120, nT=9)      # a different shape reuses the scratch
     _agree(_noalloc(first), _regular(first))
     _agree(_noalloc(second), _regular(second))
+
+
+def test_noalloc_samples_the_nyquist_row():
+    c = _edge_case()
+    _agree(_noalloc(c), _regular(c))
 
 
 def test_noalloc_rejects_oversized_sets():

@@ -19,6 +19,7 @@
 //     rows and their zero padding, the shifted data, the likelihoods, the
 //     norms and the error word), so no stale content from an earlier call is
 //     used.
+#include <cuda.h>   // CUcontext / CUresult types only; the driver is reached through cudart
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
@@ -75,7 +76,7 @@ k_project_plain(const float2* __restrict__ vol, int vdim, int pf, const double* 
         if (conj) { x = -x; y = -y; z = -z; }
         const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
         const int x0 = (int)xf, y0 = (int)yf, z0 = (int)zf;
-        if (x0 + 1 > half || y0 < -half || y0 + 1 >= half || z0 < -half || z0 + 1 >= half) {
+        if (x0 + 1 > half || y0 < -half || y0 + 1 > half || z0 < -half || z0 + 1 > half) {
             atomicOr(flag, 1 << 16);
             orow[p] = make_float2(0.f, 0.f);
             continue;
@@ -111,23 +112,72 @@ k_project_plain(const float2* __restrict__ vol, int vdim, int pf, const double* 
     }
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array, looked up once per device and
+// context.  The context's 64-bit id (cuCtxGetId, unique for the process's
+// life) is kept with the address: after cudaDeviceReset the runtime makes a
+// new primary context, reloads the library's module, and the array may sit
+// at another address, so a changed id repeats the lookup.
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+struct ScratchSlot {
+    unsigned long long ctx_id = 0;
+    void* addr = nullptr;
+};
+
 std::mutex g_mu;
-void* g_scratch_addr[64] = {};
+ScratchSlot g_slot[64];
+std::once_flag g_driver_once;
+PfnCtxGetCurrent g_ctx_get_current = nullptr;
+PfnCtxGetId g_ctx_get_id = nullptr;
+
+int current_context_id(int dev, unsigned long long* id)
+{
+    std::call_once(g_driver_once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess && q == cudaDriverEntryPointSuccess)
+            g_ctx_get_current = reinterpret_cast<PfnCtxGetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            g_ctx_get_id = reinterpret_cast<PfnCtxGetId>(f);
+    });
+    if (!g_ctx_get_current || !g_ctx_get_id)
+        return fail(TG3_ERR_CUDA, "driver entry points cuCtxGetCurrent / cuCtxGetId not found");
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS)
+        return fail(TG3_ERR_CUDA, "cuCtxGetCurrent failed");
+    if (!ctx) {
+        // no context current on this thread yet: make the device's primary
+        // context current (cudaSetDevice initialises it)
+        TG3_CUDA(cudaSetDevice(dev));
+        if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx)
+            return fail(TG3_ERR_CUDA, "no CUDA context current after cudaSetDevice");
+    }
+    if (g_ctx_get_id(ctx, id) != CUDA_SUCCESS) return fail(TG3_ERR_CUDA, "cuCtxGetId failed");
+    return TG3_OK;
+}
 
 int scratch_for_current_device(void** out)
 {
     int dev = 0;
     TG3_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return fail(TG3_ERR_ARG, "device ordinal out of range");
+    unsigned long long id = 0;
+    int st = current_context_id(dev, &id);
+    if (st) return st;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_addr[dev]) {
+    ScratchSlot& s = g_slot[dev];
+    if (!s.addr || s.ctx_id != id) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
-        g_scratch_addr[dev] = p;
+        s.addr = p;
+        s.ctx_id = id;
     }
-    *out = g_scratch_addr[dev];
+    *out = s.addr;
     return TG3_OK;
 }
 
@@ -189,9 +239,11 @@ extern "C" int tg3_local_phase_noalloc(const float* volume, int vdim, int pf, co
                                  -2.0f, cs));
     TG3_CUDA(launch_weights(D, 0, nT, nR, nT, 1, 1, nullptr, 0, x0, pwR, 0, pwT, 0, pwC, wC, wR, wT,
                             baseL, dvp, cs));
-    TG3_CUDA(cudaStreamSynchronize(cs));
+    // the error word comes back on the call's own stream: a copy on the
+    // legacy stream would also wait for every other blocking stream
     int h = 0;
-    TG3_CUDA(cudaMemcpy(&h, flag, sizeof(int), cudaMemcpyDeviceToHost));
+    TG3_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, cs));
+    TG3_CUDA(cudaStreamSynchronize(cs));
     if (h & (1 << 16))
         return fail(TG3_ERR_ARG, "a rotated pixel falls outside the volume (pf x radius too large)");
     return TG3_OK;
