@@ -1066,7 +1066,7 @@ LEARNED256 = dict(box=256, pixel_size=1.1, n_blobs=200, sigma_a=(1.5, 3.0), radi
                   n_maps=16, n_train_maps=12, rU=80, pf=2, shift=3.0, snr_lik=0.03,
                   n_rot=256, n_trans=25)
 LEARNED = dict(box=128, pixel_size=1.4, n_blobs=120, sigma_a=(1.5, 3.0), radius_px=40.0,
-               n_maps=16, n_train_maps=12, rU=32, pf=2, shift=3.0, snr=0.05,
+               n_maps=16, n_train_maps=12, rU=32, pf=2, shift=3.0, snr_lik=0.05,
                n_rot=256, n_trans=25)
 
 
@@ -1080,11 +1080,15 @@ def reconstruction_resolution(tg3, torch, ctx, ps, maps, quat, trans, box, pf, p
     out = []
     for c in np.unique(ps.cls):
         g = np.nonzero(ps.cls == c)[0]
-        d = lambda x: torch.as_tensor(np.ascontiguousarray(x)).to(dev)
+
+        def d(x):
+            if torch.is_tensor(x):
+                return x[torch.as_tensor(g, device=x.device)].contiguous()
+            return torch.as_tensor(np.ascontiguousarray(np.asarray(x)[g])).to(dev)
         ctx.insert_begin(vdim, pf)
-        ctx.insert(len(g), d(ps.dat[g]), d(ps.ctf[g]), d(np.asarray(quat, np.float64)[g]),
-                   d(np.asarray(trans, np.float64)[g]), None,
-                   d(np.ones(len(g), np.float32)), tg3.KERNEL_MKB)
+        ctx.insert(len(g), d(ps.dat), d(ps.ctf), d(np.asarray(quat, np.float64)),
+                   d(np.asarray(trans, np.float64)), None,
+                   torch.ones(len(g), dtype=torch.float32, device=dev), tg3.KERNEL_MKB)
         F = torch.empty(shape + (2,), dtype=torch.float32, device=dev)
         T = torch.empty(shape, dtype=torch.float32, device=dev)
         V = torch.empty(shape, dtype=torch.complex64, device=dev)
@@ -1120,17 +1124,21 @@ def synth_padded(bm, box, pf, dev):
 
 
 def run_learned(args, rank, world, local_rank):
-    """Learned proposal: 16 random 128^3 blob maps (120 blobs, 1.4 A/px), 12 for
-    training pairs and 4 held out.  The network trains on the GPU (its own
-    kernels) on pairs of the 12 training maps: in matching mode (the default)
-    particle images against clean reference projections at their true poses,
-    in regression mode (image, true pose).  It then seeds 256 rotations x 25
-    translations per particle (matching: the best-matching of the map's 6,912
-    references), every one rescored by the exact likelihood (split-bf16
-    local phase).  Compared with the plain
-    global search (6,912 x 49 hypotheses) on held-out particles of the
-    training maps and on particles of the 4 held-out maps.  Cutoff 32
-    (K = 1,563: the global scan's scaling, r = box / 4)."""
+    """The headline: the learned E-step (pose-network proposals rescored by
+    the exact split-bf16 likelihood, global search as the fallback) against
+    the plain FP32 global search, at box 256 (learned256) or 128 (learned128).
+
+    16 blob maps; 12 give the training particles, 4 are held out.  The
+    training labels are the plain method's converged poses (FP32 global
+    search over 6,912 rotations x 49 translations, then three narrowing local
+    phases of 1,000 x 100).  The network (matching mode, trained on the GPU by
+    the library's kernels) proposes 256 rotations x 25 translations per
+    particle; the fallback threshold is calibrated on held-out particles of
+    the training maps against the plain method's poses.  The timed step is
+    one E-step over the particles of the 4 held-out maps; after it both
+    methods' poses are refined by one local phase of 1,000 x 100 and compared
+    (median error against the true pose, FSC-0.143 of the maps
+    reconstructed from them)."""
     import torch
     import tg3
     from tg3 import learned, synth
@@ -1138,343 +1146,574 @@ def run_learned(args, rank, world, local_rank):
     dev = f"cuda:{local_rank}"
     L = LEARNED256 if args.workload == "learned256" else LEARNED
     box, px, pf, rU = L["box"], L["pixel_size"], L["pf"], L["rU"]
+    nTr, nMaps = L["n_train_maps"], L["n_maps"]
+    nRot, nTrans = L["n_rot"], L["n_trans"]
+    prec = tg3.SCORE_BF16X3 if args.precision == "bf16x3" else tg3.SCORE_FP32
+    lab_prec = tg3.SCORE_FP32 if args.label_precision == "fp32" else tg3.SCORE_BF16X3
+    f64 = dict(dtype=torch.float64, device=dev)
     rng = np.random.default_rng(4000)
     maps = [synth.blob_map(rng, L["n_blobs"], L["sigma_a"], px, L["radius_px"])
-            for _ in range(L["n_maps"])]
+            for _ in range(nMaps)]
     rL = synth.config_rL(box, px)
-    prec = tg3.SCORE_BF16X3 if args.precision == "bf16x3" else tg3.SCORE_FP32
-    nTr = L["n_train_maps"]
-    t0 = time.perf_counter()
-    # noise: SNR over the image grid, or (box 256) over the likelihood's pixels
-    if "snr_lik" in L:
-        noise = dict(noise_var=synth.signal_power(maps[:nTr], box, px, rU, rL, device=dev)
-                     / L["snr_lik"] / 2.0)
-        snr_note = f"{L['snr_lik']} over the likelihood's pixels (cutoff {rU})"
-    else:
-        noise = {}
-        snr_note = f"{args.learned_snr} over the image grid"
-    # training pairs, generated in chunks (images stay on the device)
-    imgs, Rs, ts, qtrue, ctr = [], [], [], [], []
-    chunk = 10000
-    for s0 in range(0, args.train_particles, chunk):
-        m = min(chunk, args.train_particles - s0)
-        ps = synth.particle_set(4100 + s0, maps[:nTr], np.arange(m) % nTr, box, px, rU, rL,
-                                L["shift"], args.learned_snr, device=dev, with_data=False,
-                                **noise)
-        imgs.append(ps.images)
-        Rs.append(synth.quat_to_mat(ps.quat_true).reshape(m, 9))
-        ts.append(ps.trans_true)
-        qtrue.append(ps.quat_true)
-        ctr.append(ps.cls)
-    images = torch.cat(imgs)
-    Rstar = torch.as_tensor(np.concatenate(Rs)).to(dev)
-    tstar = torch.as_tensor(np.concatenate(ts)).to(dev)
-    # the exact likelihood and the reference projections: one context with
-    # every map as a class
+    iCol, iRow, _, _ = synth.pixel_index(box, rU, rL)
+    K = len(iCol)
+    noise_var = synth.signal_power(maps[:nTr], box, px, rU, rL, device=dev) / L["snr_lik"] / 2.0
     ctx = tg3.Context(local_rank)
     for c, bm in enumerate(maps):
         ctx.set_volume(c, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
-    match = args.learned_mode == "match"
-    if match:
-        # clean references at the training particles' true rotations
-        qtr = np.concatenate(qtrue)
-        ctr = np.concatenate(ctr)
-        refs = torch.empty_like(images)
-        for c in range(nTr):
-            sel = np.nonzero(ctr == c)[0]
-            refs[torch.as_tensor(sel, device=dev)] = learned.render_references(ctx, c, qtr[sel], box)
-    gen_s = time.perf_counter() - t0
+    ctx.set_pixels(iCol, iRow, box)
+    quats_g = synth.global_rotations(4, 36)
+    nRg = len(quats_g)
+    quats_g_dev = torch.as_tensor(quats_g, **f64)
+    mats_g = torch.as_tensor(synth.quat_to_mat(quats_g).reshape(-1, 9), **f64)
+    trans_g = torch.as_tensor(synth.global_translations(3, 1.0), **f64)
+    nTg = int(trans_g.shape[0])
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(rank_seed(7100, rank))
+    log = (lambda m: print(m, file=sys.stderr, flush=True)) if args.verbose else (lambda m: None)
+
+    # ---- 1. training particles of the 12 training maps, labelled with the
+    # plain method's converged poses
+    t0 = time.perf_counter()
+    imgs, q_lab, t_lab, q_tru, cls_tr, moves = [], [], [], [], [], []
+    chunk = 10000
+    for s0 in range(0, args.train_particles, chunk):
+        m = min(chunk, args.train_particles - s0)
+        ps = synth.particle_set_dev(4100 + s0, maps, (s0 + np.arange(m)) % nTr, box, px, rU, rL,
+                                    L["shift"], noise_var, device=dev)
+        ql, tl, mv = learned.plain_method_poses(ctx, ps, quats_g, mats_g, trans_g, lab_prec, gen)
+        imgs.append(ps.images)
+        q_lab.append(ql)
+        t_lab.append(tl)
+        q_tru.append(ps.quat_true)
+        cls_tr.append(ps.cls)
+        moves.append(mv)
+        del ps
+        log(f"labels {s0 + m}/{args.train_particles}: phase moves {mv}")
+    images = torch.cat(imgs)
+    del imgs
+    q_lab, t_lab = np.concatenate(q_lab), np.concatenate(t_lab)
+    q_tru, cls_tr = np.concatenate(q_tru), np.concatenate(cls_tr)
+    torch.cuda.synchronize()
+    label_s = time.perf_counter() - t0
+    label_err = learned.angle_deg(q_lab, q_tru)
+
+    # ---- 2. training (matching mode): references at the label rotations
+    refs = torch.empty_like(images)
+    for c in range(nTr):
+        sel = np.nonzero(cls_tr == c)[0]
+        refs[torch.as_tensor(sel, device=dev)] = learned.render_references(ctx, c, q_lab[sel], box)
     net = tg3.Cnn(local_rank, seed=4242)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    if match:
-        losses = learned.train_match(net, images, refs, tstar, ctr, args.epochs, 256,
-                                     args.learned_lr, tau=args.learned_tau, seed=7)
-        del refs
-    else:
-        losses = learned.train(net, images, Rstar, tstar, args.epochs, 256, args.learned_lr,
-                               seed=7)
+    losses = learned.train_match(net, images, refs, torch.as_tensor(t_lab, **f64), cls_tr,
+                                 args.epochs, 256, args.learned_lr, tau=args.learned_tau, seed=7)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t1
-    del images, Rstar, tstar
-    quats_g = synth.global_rotations(4, 36)
-    mats_g = torch.as_tensor(synth.quat_to_mat(quats_g).reshape(-1, 9)).to(dev)
-    trans_g = torch.as_tensor(synth.global_translations(3, 1.0)).to(dev)
-    nRg, nTg = len(quats_g), int(trans_g.shape[0])
+    del refs, images
+    log(f"trained: losses {losses}")
 
-    quats_g_dev = torch.as_tensor(quats_g).to(dev)
-    ref_emb, ref_ms = {}, []
+    # ---- 3. evaluation particles: held-out particles of the training maps
+    # (calibration) and particles of the 4 held-out maps (the timed batch)
+    nSeen, nUn = args.eval_particles_seen, args.eval_particles_unseen
+    seen = synth.particle_set_dev(rank_seed(5001, rank), maps, np.arange(nSeen) % nTr, box, px,
+                                  rU, rL, L["shift"], noise_var, device=dev)
+    unseen = synth.particle_set_dev(rank_seed(5002, rank), maps,
+                                    nTr + np.arange(nUn) % (nMaps - nTr), box, px, rU, rL,
+                                    L["shift"], noise_var, device=dev)
 
-    def embeddings_of(c):
-        # the map's references at the global rotations, embedded (timed)
-        if c not in ref_emb:
-            torch.cuda.synchronize()
-            ta = time.perf_counter()
-            ref_emb[c] = learned.reference_embeddings(
-                net, learned.render_references(ctx, c, quats_g, box))
-            torch.cuda.synchronize()
-            ref_ms.append((time.perf_counter() - ta) * 1e3)
-        return ref_emb[c]
-
-    bank_ms = {}
-
-    def evaluate(ps, name):
-        n = len(ps.cls)
-        if match:
-            for c in np.unique(ps.cls):
-                embeddings_of(int(c))
-        ctx.set_pixels(ps.iCol, ps.iRow, box)
-        if match:
-            # each map's projections at the 6,912 references, made once and
-            # gathered by the proposals' indices (timed with the embeddings)
-            for c in np.unique(ps.cls):
-                torch.cuda.synchronize()
-                ta = time.perf_counter()
-                ctx.set_bank(int(c), quats_g_dev, nRg)
-                ctx.sync()
-                bank_ms[int(c)] = (time.perf_counter() - ta) * 1e3
-        d = dict(dat=torch.as_tensor(ps.dat).to(dev), ctf=torch.as_tensor(ps.ctf).to(dev),
-                 sig=torch.as_tensor(ps.sigRcp).to(dev))
-        f64 = dict(dtype=torch.float64, device=dev)
-        stream = torch.cuda.ExternalStream(ctx.stream)
-        ev = lambda: torch.cuda.Event(enable_timing=True)
-        # -- plain global search, per map
-        og = dict(wC=torch.empty(n, **f64), wR=torch.empty((n, nRg), **f64),
-                  wT=torch.empty((n, nTg), **f64), base=torch.empty(n, **f64))
-        pR = torch.full((nRg,), 1.0 / nRg, **f64)
-        pT = torch.full((nTg,), 1.0 / nTg, **f64)
-        groups = [np.nonzero(ps.cls == c)[0] for c in np.unique(ps.cls)]
-        sub = {}
-        for g in groups:
-            idx = torch.as_tensor(g, device=dev)
-            sub[int(ps.cls[g[0]])] = (idx, {k: v[idx].contiguous() for k, v in d.items()},
-                                      {k: v[idx].contiguous() for k, v in og.items()},
-                                      {k: v[idx].contiguous() for k, v in og.items()})
-
-        def global_all(split=False):
-            # the plain method: FP32 global search; split: the same search in
-            # split-bf16 (the learned E-step's own fallback)
-            for c, (idx, dd, oo, o2) in sub.items():
-                oo = o2 if split else oo
-                ctx.global_scan(c, len(idx), nRg, nTg, dd["dat"], dd["ctf"], dd["sig"], mats_g,
-                                trans_g, pR, pT, oo["wC"], oo["wR"], oo["wT"], oo["base"], None,
-                                prec if split else tg3.SCORE_FP32)
-
-        def timed_global(split):
-            global_all(split)
-            ctx.sync()
-            e0, e1 = ev(), ev()
-            e0.record(stream)
-            global_all(split)
-            e1.record(stream)
-            e1.synchronize()
-            ctx.sync()
-            return reduce_max(world, e0.elapsed_time(e1))
-
-        tg_ms = timed_global(False)
-        tgs_ms = timed_global(True)
-        bestg, baseg = np.empty(n, np.int64), np.empty(n)
-        besttg = np.empty(n, np.int64)
-        bestgs, besttgs = np.empty(n, np.int64), np.empty(n, np.int64)
-        for c, (idx, dd, oo, o2) in sub.items():
-            g = idx.cpu().numpy()
-            bestg[g] = oo["wR"].argmax(1).cpu().numpy()
-            besttg[g] = oo["wT"].argmax(1).cpu().numpy()
-            baseg[g] = oo["base"].cpu().numpy()
-            bestgs[g] = o2["wR"].argmax(1).cpu().numpy()
-            besttgs[g] = o2["wT"].argmax(1).cpu().numpy()
-        err_g = learned.angle_deg(quats_g[bestg], ps.quat_true)
-        err_gs = learned.angle_deg(quats_g[bestgs], ps.quat_true)
-        # -- learned proposal: network, proposals, exact rescoring
-        nR, nT = L["n_rot"], L["n_trans"]
-        out = torch.empty((n, tg3.Cnn.N_OUT), dtype=torch.float32, device=dev)
-        cls_d = torch.as_tensor(ps.cls.astype(np.int32)).to(dev)
-        ol = dict(wC=torch.empty(n, **f64), wR=torch.empty((n, nR), **f64),
-                  wT=torch.empty((n, nT), **f64), base=torch.empty(n, **f64),
-                  dvp=torch.empty((n, nR, nT), dtype=torch.float32, device=dev))
-
-        qd = torch.empty((n, nR, 4), **f64)
-        td = torch.empty((n, nT, 2), **f64)
-        bidx = torch.empty((n, nR), dtype=torch.int32, device=dev)
-        pRl = torch.full((n, nR), 1.0 / nR, **f64)
-        pTl = torch.full((n, nT), 1.0 / nT, **f64)
-        pCl = torch.ones(n, **f64)
-
-        grp = [(int(c), torch.as_tensor(np.nonzero(ps.cls == c)[0], device=dev))
-               for c in np.unique(ps.cls)]
-
-        marks = []
-
-        def learned_all():
-            # network, proposals and exact rescoring, all on the device
-            marks.clear()
-            marks.append(time.perf_counter())
-            net.infer(ps.images, out)
-            marks.append(time.perf_counter())
-            if match:
-                # per map: the best-matching references of that map's embeddings
-                for c, idx in grp:
-                    og_ = out[idx].contiguous()
-                    qg_ = torch.empty((len(idx), nR, 4), **f64)
-                    tg_ = torch.empty((len(idx), nT, 2), **f64)
-                    ig_ = torch.empty((len(idx), nR), dtype=torch.int32, device=dev)
-                    tg3.Cnn.match_propose(og_, ref_emb[c], quats_g_dev, nR, nT, 99, qg_, tg_,
-                                          ig_)
-                    qd[idx] = qg_
-                    td[idx] = tg_
-                    bidx[idx] = ig_
-                torch.cuda.synchronize()
-            else:
-                tg3.Cnn.propose(out, nR, nT, 99, qd, td, ctx.stream)
-                ctx.sync()
-            marks.append(time.perf_counter())
-            if match:
-                ctx.local_phase_bank(n, nR, nT, d["dat"], d["ctf"], d["sig"], bidx, td, pRl, pTl,
-                                     pCl, cls_d, ol["wC"], ol["wR"], ol["wT"], ol["base"],
-                                     ol["dvp"], prec)
-            else:
-                ctx.local_phase(n, nR, nT, d["dat"], d["ctf"], d["sig"], qd, td, pRl, pTl, pCl,
-                                cls_d, ol["wC"], ol["wR"], ol["wT"], ol["base"], ol["dvp"], prec)
-            ctx.sync()
-            marks.append(time.perf_counter())
-            q_host = qd.cpu().numpy()
-            marks.append(time.perf_counter())
-            return q_host
-
-        learned_all()
+    # ---- 4. per map, once: the 6,912 references rendered and embedded, the
+    # projection bank at the same rotations, the references attached to it
+    classes = sorted(set(int(c) for c in seen.cls) | set(int(c) for c in unseen.cls))
+    emb, embed_ms, bank_ms = {}, {}, {}
+    for c in classes:
         torch.cuda.synchronize()
-        ctx.set_timing(True)
-        ctx.stage_times(reset=True)
         ta = time.perf_counter()
-        q = learned_all()
+        emb[c] = learned.reference_embeddings(net, learned.render_references(ctx, c, quats_g, box))
         torch.cuda.synchronize()
-        tl_ms = reduce_max(world, (time.perf_counter() - ta) * 1e3)
-        st_l = ctx.stage_times(reset=True)
-        ctx.set_timing(False)
-        split = {k: round((marks[i + 1] - marks[i]) * 1e3, 3) for i, k in
-                 enumerate(("network_forward", "proposals", "rescoring", "copy_out"))}
-        split["rescoring_stages"] = {k: round(v[0], 3) for k, v in st_l.items() if v[1]}
-        bestl = ol["wR"].argmax(1).cpu().numpy()
-        besttl = ol["wT"].argmax(1).cpu().numpy()
-        err_l = learned.angle_deg(q[np.arange(n), bestl], ps.quat_true)
-        basel = ol["base"].cpu().numpy()
-        dv = ol["dvp"].reshape(n, -1).cpu().numpy().astype(np.float64)
-        med = np.median(dv, 1)
-        mad = np.median(np.abs(dv - med[:, None]), 1) + 1e-12
-        peak = (dv.max(1) - med) / (1.4826 * mad)
-        return dict(n=n, tg_ms=tg_ms, tgs_ms=tgs_ms, tl_ms=tl_ms, split_ms=split, err_g=err_g,
-                    err_gs=err_gs, err_l=err_l, peak=peak,
-                    pose_gs=(quats_g[bestgs], trans_g.cpu().numpy()[besttgs]),
-                    better=basel >= baseg,
-                    pose_g=(quats_g[bestg], trans_g.cpu().numpy()[besttg]),
-                    pose_l=(q[np.arange(n), bestl], td.cpu().numpy()[np.arange(n), besttl]))
+        embed_ms[c] = (time.perf_counter() - ta) * 1e3
+    ctx.set_pixels(iCol, iRow, box)          # the renders used the image grid
+    for c in classes:
+        ctx.sync()
+        ta = time.perf_counter()
+        ctx.set_bank(c, quats_g_dev, nRg)
+        ctx.set_references(c, emb[c])
+        ctx.sync()
+        bank_ms[c] = (time.perf_counter() - ta) * 1e3
+    held = [c for c in classes if c >= nTr]
+    map_ms = float(np.mean([embed_ms[c] + bank_ms[c] for c in held]))
+    per_map_particles = 50000
+    map_ms_pp = map_ms / per_map_particles
 
-    nSeen = args.eval_particles_seen
-    nUn = args.eval_particles_unseen
-    seen = synth.particle_set(rank_seed(5001, rank), maps[:nTr], np.arange(nSeen) % nTr, box, px, rU, rL,
-                              L["shift"], args.learned_snr, device=dev, **noise)
-    unseen = synth.particle_set(rank_seed(5002, rank), maps[nTr:], np.arange(nUn) % (L["n_maps"] - nTr), box, px,
-                                rU, rL, L["shift"], args.learned_snr, device=dev, **noise)
-    unseen.cls = unseen.cls + nTr
-    rs = evaluate(seen, "seen")
-    ru = evaluate(unseen, "unseen")
-    # fallback rule: the proposal's peak score (best minus median of its rescored
-    # hypotheses, in robust deviations) below a threshold calibrated on the
-    # held-out particles of the training maps: 95 % of proposals within 10
-    # degrees of the truth pass
-    good = rs["err_l"] < 10.0
-    tau = float(np.quantile(rs["peak"][good], 0.05)) if good.any() else float("inf")
+    # ---- 5. the plain method run to convergence on the evaluation particles:
+    # the judge of the proposals (and the poses the calibration trusts)
+    judge_seen, _, _ = learned.plain_method_poses(ctx, seen, quats_g, mats_g, trans_g,
+                                                  tg3.SCORE_FP32, gen)
+    judge_un, judge_un_t, _ = learned.plain_method_poses(ctx, unseen, quats_g, mats_g, trans_g,
+                                                         tg3.SCORE_FP32, gen)
 
-    # matching mode: a map's reference embeddings are made once per map and
-    # serve all its particles; charged per particle over the 50,000 particles
-    # of a held-out map
-    map_ms = (float(np.mean(ref_ms)) + (float(np.mean(list(bank_ms.values()))) if bank_ms else 0.0)
-              if match and ref_ms else 0.0)
-    ref_pp_ms = map_ms / 50000.0
+    def outputs(n, full=True):
+        o = dict(bestQuat=torch.empty((n, 4), **f64), bestTrans=torch.empty((n, 2), **f64),
+                 baseL=torch.empty(n, **f64),
+                 peak=torch.empty(n, dtype=torch.float32, device=dev),
+                 fellBack=torch.empty(n, dtype=torch.int32, device=dev))
+        if full:
+            o.update(propIdx=torch.empty((n, nRot), dtype=torch.int32, device=dev),
+                     propQuat=torch.empty((n, nRot, 4), **f64),
+                     propTrans=torch.empty((n, nTrans, 2), **f64),
+                     propWR=torch.empty((n, nRot), **f64), propWT=torch.empty((n, nTrans), **f64),
+                     propBase=torch.empty(n, **f64),
+                     propDvp=torch.empty((n, nRot, nTrans), dtype=torch.float32, device=dev))
+        return o
 
-    def report(r):
-        fb = r["peak"] < tau
-        err_c = np.where(fb, r["err_g"], r["err_l"])
-        t_l = r["tl_ms"] + r["n"] * ref_pp_ms
-        t_c = t_l + fb.mean() * r["tg_ms"]
-        t_s = t_l + fb.mean() * r["tgs_ms"]
-        err_s = np.where(fb, r["err_gs"], r["err_l"])
-        return {"particles": r["n"],
-                "plain_fp32_global_search": {"particles_per_s": round(job_rate(r["n"], r["tg_ms"], world), 1),
-                                  "median_error_deg": round(float(np.median(r["err_g"])), 3)},
-                "proposal_only": {"particles_per_s": round(job_rate(r["n"], t_l, world), 1),
-                                  "median_error_deg": round(float(np.median(r["err_l"])), 3),
-                                  "within_10deg": round(float(np.mean(r["err_l"] < 10)), 4)},
-                "proposal_with_fallback": {
-                    "particles_per_s": round(job_rate(r["n"], t_c, world), 1),
-                    "median_error_deg": round(float(np.median(err_c)), 3),
-                    "fallback_fraction": round(float(fb.mean()), 4)},
-                "proposal_with_split_bf16_fallback": {
-                    "particles_per_s": round(job_rate(r["n"], t_s, world), 1),
-                    "median_error_deg": round(float(np.median(err_s)), 3),
-                    "fallback_fraction": round(float(fb.mean()), 4),
-                    "fallback_global_search_particles_per_s":
-                        round(job_rate(r["n"], r["tgs_ms"], world), 1)},
-                "speedup_with_split_bf16_fallback": round(r["tg_ms"] / t_s, 2),
-                "proposal_at_least_as_likely_as_global": round(float(r["better"].mean()), 4),
-                "proposal_path_ms": r["split_ms"],
-                "speedup_with_fallback": round(r["tg_ms"] / t_c, 2)}
+    def expect(ps, peak_min, out, precision=prec):
+        ctx.learned_expect(net, ps.images, ps.dat, ps.ctf, ps.sigRcp,
+                           torch.as_tensor(ps.cls.astype(np.int32), device=dev), nRot, nTrans, 99,
+                           trans_g, peak_min, precision, out)
 
-    # reconstructions of the held-out maps from each method's poses (MKB
-    # insertion, V = F / T), FSC against the map's exact transform
-    fb = ru["peak"] < tau
-    poses = {"true_poses": (unseen.quat_true, unseen.trans_true),
-             "plain_fp32_global_search": ru["pose_g"],
-             "proposal_only": ru["pose_l"],
-             "proposal_with_fallback": (np.where(fb[:, None], ru["pose_g"][0], ru["pose_l"][0]),
-                                        np.where(fb[:, None], ru["pose_g"][1], ru["pose_l"][1])),
-             "proposal_with_split_bf16_fallback": (
-                 np.where(fb[:, None], ru["pose_gs"][0], ru["pose_l"][0]),
-                 np.where(fb[:, None], ru["pose_gs"][1], ru["pose_l"][1]))}
-    fsc_res = {k: reconstruction_resolution(tg3, torch, ctx, unseen, maps, q, t, box, pf, px,
-                                            rU, dev)
+    # ---- 6. fallback threshold: 95 % of the held-out particles of the
+    # training maps whose proposal lies within 10 degrees of the plain
+    # method's converged pose pass it
+    o_seen = outputs(nSeen, full=False)
+    expect(seen, float("-inf"), o_seen)
+    err_seen = learned.angle_deg(o_seen["bestQuat"].cpu().numpy(), judge_seen)
+    pk_seen = o_seen["peak"].cpu().numpy()
+    good = err_seen < 10.0
+    tau = float(np.quantile(pk_seen[good], 0.05)) if good.any() else float("inf")
+    del o_seen
+
+    # ---- 7. the timed E-steps over the particles of the held-out maps
+    n = nUn
+    cls_un = torch.as_tensor(unseen.cls.astype(np.int32), device=dev)
+    out = outputs(n)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def learned_step():
+        ctx.learned_expect(net, unseen.images, unseen.dat, unseen.ctf, unseen.sigRcp, cls_un,
+                           nRot, nTrans, 99, trans_g, tau, prec, out)
+
+    for _ in range(args.warmup):
+        learned_step()
+    barrier(world)
+    torch.cuda.synchronize()
+    ctx.set_timing(True)
+    ctx.stage_times(reset=True)
+    clk = ClockSampler(local_rank)
+    clk.start()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(args.steps):
+        learned_step()
+    e1.record(stream)
+    e1.synchronize()
+    clocks = clk.stop()
+    torch.cuda.synchronize()
+    barrier(world)
+    tl_ms = reduce_max(world, e0.elapsed_time(e1))
+    st_l = ctx.stage_times(reset=True)
+    ctx.set_timing(False)
+    fb = out["fellBack"].cpu().numpy().astype(bool)
+    q_l = out["bestQuat"].cpu().numpy()
+    t_l = out["bestTrans"].cpu().numpy()
+    base_l = out["baseL"].cpu().numpy()
+    prop_q = out["propQuat"].cpu().numpy()
+    prop_base = out["propBase"].cpu().numpy()
+    peak_un = out["peak"].cpu().numpy()
+    idx_un = out["propIdx"].cpu().numpy()
+    ptr_un = out["propTrans"].cpu().numpy()
+    dvp_un = out["propDvp"].cpu().numpy()
+    q_prop_best = prop_q[np.arange(n), out["propWR"].argmax(1).cpu().numpy()]
+
+    # the plain FP32 global search on the same particles (per map)
+    groups = [(int(c), torch.as_tensor(np.nonzero(unseen.cls == c)[0], device=dev))
+              for c in np.unique(unseen.cls)]
+    sub = []
+    for c, idx in groups:
+        m = len(idx)
+        sub.append((c, m, unseen.dat[idx].contiguous(), unseen.ctf[idx].contiguous(),
+                    unseen.sigRcp[idx].contiguous(),
+                    dict(wC=torch.empty(m, **f64), wR=torch.empty((m, nRg), **f64),
+                         wT=torch.empty((m, nTg), **f64), base=torch.empty(m, **f64))))
+    pRg = torch.full((nRg,), 1.0 / nRg, **f64)
+    pTg = torch.full((nTg,), 1.0 / nTg, **f64)
+
+    def plain_step(precision=tg3.SCORE_FP32):
+        for c, m, dd, cc, ss, o in sub:
+            ctx.global_scan(c, m, nRg, nTg, dd, cc, ss, mats_g, trans_g, pRg, pTg, o["wC"],
+                            o["wR"], o["wT"], o["base"], None, precision)
+        ctx.sync()
+
+    plain_step()
+    plain_steps = max(1, min(args.steps, args.plain_steps))
+    clk_p = ClockSampler(local_rank)
+    clk_p.start()
+    barrier(world)
+    e0.record(stream)
+    for _ in range(plain_steps):
+        plain_step()
+    e1.record(stream)
+    e1.synchronize()
+    clocks_p = clk_p.stop()
+    tp_ms = reduce_max(world, e0.elapsed_time(e1))
+    q_p = np.empty((n, 4))
+    t_p = np.empty((n, 2))
+    base_p = np.empty(n)
+    for (c, idx), (_, m, _, _, _, o) in zip(groups, sub):
+        g = idx.cpu().numpy()
+        q_p[g] = quats_g[o["wR"].argmax(1).cpu().numpy()]
+        t_p[g] = trans_g.cpu().numpy()[o["wT"].argmax(1).cpu().numpy()]
+        base_p[g] = o["base"].cpu().numpy()
+
+    # ---- 8. end to end through the host-buffer C ABI (page-locked inputs
+    # copied in, poses copied out, inside the timed calls)
+    hin = dict(images=unseen.images.cpu().pin_memory(), dat=unseen.dat.cpu().pin_memory(),
+               ctf=unseen.ctf.cpu().pin_memory(), sig=unseen.sigRcp.cpu().pin_memory(),
+               cls=cls_un.cpu().pin_memory(), gt=trans_g.cpu().pin_memory())
+    hout = dict(q=torch.empty((n, 4), dtype=torch.float64).pin_memory(),
+                t=torch.empty((n, 2), dtype=torch.float64).pin_memory(),
+                b=torch.empty(n, dtype=torch.float64).pin_memory(),
+                pk=torch.empty(n, dtype=torch.float32).pin_memory(),
+                fb=torch.empty(n, dtype=torch.int32).pin_memory())
+
+    def e2e_step():
+        ctx.learned_expect_host(net, hin["images"], hin["dat"], hin["ctf"], hin["sig"],
+                                hin["cls"], nRot, nTrans, 99, hin["gt"], tau, prec, hout["q"],
+                                hout["t"], hout["b"], hout["pk"], hout["fb"])
+
+    e2e_step()
+    barrier(world)
+    te = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e2e_s = reduce_max(world, time.perf_counter() - te)
+    e2e_same = bool(np.array_equal(hout["q"].numpy(), q_l))
+    h2d = sum(int(v.numel() * v.element_size()) for v in hin.values())
+    d2h = sum(int(v.numel() * v.element_size()) for v in hout.values())
+
+    # ---- 9. the benchmark spec's own fallback rule, measured beside the
+    # threshold: the global search on every particle, its pose taken where
+    # its best likelihood beats the proposal's
+    o_all = outputs(n, full=False)
+    expect(unseen, float("inf"), o_all)          # every particle through the global search
+    torch.cuda.synchronize()
+    tb = time.perf_counter()
+    expect(unseen, float("inf"), o_all)
+    t_all_ms = reduce_max(world, (time.perf_counter() - tb) * 1e3)
+    base_gs = o_all["baseL"].cpu().numpy()
+    q_gs = o_all["bestQuat"].cpu().numpy()
+    t_gs = o_all["bestTrans"].cpu().numpy()
+    ruleB = base_gs > prop_base
+    t_prop_best = ptr_un[np.arange(n), out["propWT"].argmax(1).cpu().numpy()]
+    q_B = np.where(ruleB[:, None], q_gs, q_prop_best)
+    t_B = np.where(ruleB[:, None], t_gs, t_prop_best)
+    del o_all
+
+    # ---- 10. one local refinement phase about each method's pose
+    # (1,000 vMF rotations, kappa 200, x 100 translations, deviation 2 px)
+    def refine(q, t, precision):
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        qn, tn, _ = learned.local_refine(ctx, unseen, torch.as_tensor(q, **f64),
+                                         torch.as_tensor(t, **f64), 200.0, 2.0, precision, gen)
+        torch.cuda.synchronize()
+        return qn.cpu().numpy(), tn.cpu().numpy(), (time.perf_counter() - ta) * 1e3
+
+    q_p_r, t_p_r, tr_p_ms = refine(q_p, t_p, tg3.SCORE_FP32)
+    q_l_r, t_l_r, tr_l_ms = refine(q_l, t_l, prec)
+    q_B_r, t_B_r, _ = refine(q_B, t_B, prec)
+    qt = unseen.quat_true
+    err = lambda q: learned.angle_deg(q, qt)
+    med = lambda x: round(float(np.median(x)), 3)
+
+    # ---- 11. FSC-0.143 of the held-out maps reconstructed from each method's
+    # refined poses (and from the true poses)
+    poses = {"true_poses": (qt, unseen.trans_true),
+             "plain_fp32_refined": (q_p_r, t_p_r),
+             "learned_refined": (q_l_r, t_l_r),
+             "plain_fp32_e_step": (q_p, t_p),
+             "learned_e_step": (q_l, t_l)}
+    fsc_res = {k: reconstruction_resolution(tg3, torch, ctx, unseen, maps, q, t, box, pf, px, rU,
+                                            dev)
                for k, (q, t) in poses.items()}
-    res = {"metric": "learned proposal + split-bf16 E-step (rescoring and fallback global search) "
-                     f"vs plain FP32 global search, box {box}, held-out maps",
-           "value": report(ru)["proposal_with_split_bf16_fallback"]["particles_per_s"],
-           "unit": UNIT,
-           "n_gpus": world, "scaling": "weak",
-           "higher_is_better": True, "precision": args.precision,
-           "config": {"workload": f"16 blob maps {box}^3 ({L['n_blobs']} blobs, {px} A/px): 12 "
-                                  "training maps, 4 held out; proposal 256 rotations x 25 "
-                                  "translations rescored exactly, fallback 6,912 x 49 global "
-                                  f"search; cutoff {rU}, K = " + str(len(seen.iCol)),
-                      "train_particles": args.train_particles, "epochs": args.epochs,
-                      "snr": snr_note, "shift_px": L["shift"],
-                      "learning_rate": args.learned_lr,
-                      "eval_particles": {"seen_maps": nSeen, "held_out_maps": nUn},
-                      "labels": "true poses of the synthetic particles"},
-           "training": {"generate_s": round(gen_s, 1), "train_s": round(train_s, 1),
-                        "loss_per_epoch": [round(x, 4) for x in losses],
-                        "images_per_s": round(args.train_particles * args.epochs / train_s, 1)},
-           "fallback_threshold_peak": round(tau, 3),
-           "mode": args.learned_mode,
-           "reference_embedding": ({"ms_per_map": round(map_ms, 2),
-                                    "embedding_ms_per_map": round(float(np.mean(ref_ms)), 2),
-                                    "bank_ms_per_map": round(float(np.mean(list(
-                                        bank_ms.values()))), 2) if bank_ms else None,
-                                    "maps": len(ref_ms),
-                                    "charged_per_particle_over": 50000,
-                                    "note": "6,912 references rendered by the library's "
-                                            "projector and embedded, and the map's projection "
-                                            "bank at the same rotations, once per map"}
-                                   if match else None),
-           "fsc_0143_resolution_A": {
-               k: v for k, v in fsc_res.items()},
-           "fsc_note": ("held-out maps: every map reconstructed from its particles at the "
-                        "method's best poses (MKB insertion, F / T where T > 1 % of its mean), "
-                        "FSC against the map's exact transform, resolution where it falls "
-                        "below 0.143 (linear between shells; the mean over the 4 maps)"),
-           "held_out_particles_of_training_maps": report(rs),
-           "held_out_maps": report(ru)}
+
+    # ---- 12. the FP64 oracle on the proposals of >= 1,000 held-out
+    # particles: the same argmax among the proposals, and the error of the
+    # log-likelihood differences L - max L
+    parity = None
+    if args.check_particles > 0 and rank == 0:
+        parity = proposal_parity_fp64(ctx, maps, unseen, idx_un, ptr_un, dvp_un, quats_g, box, pf,
+                                      args.check_particles, dev)
+
+    # ---- 13. rates, roofline, baselines
+    stages = {k: {"ms_per_step": round(v[0] / args.steps, 4), "launches": v[1]}
+              for k, v in st_l.items() if v[1]}
+    ms_step = tl_ms / args.steps
+    v_l = job_rate(n, ms_step + n * map_ms_pp, world)
+    v_p = job_rate(n, tp_ms / plain_steps, world)
+    # dominant kernel of the learned step
+    dom = max((k for k in st_l if st_l[k][1]), key=lambda k: st_l[k][0])
+    roof = learned_roofline(dom, st_l, args.steps, n, nRot, nTrans, K, ctx_kp(K), fb)
+    res = {
+        "metric": METRIC, "value": round(v_l, 1), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16x3 (split-bf16 cross term, FP32 accumulate)" if prec == tg3.SCORE_BF16X3
+                 else "fp32",
+        "data": "synthetic (seeded blob maps and particles; no dataset is named)",
+        "config": {"workload": f"learned E-step, box {box}: 16 blob maps {box}^3 "
+                               f"({L['n_blobs']} blobs, {px} A/px), 12 for training, 4 held out; "
+                               f"{n} particles of the held-out maps per step; proposals "
+                               f"{nRot} rotations x {nTrans} translations rescored exactly, "
+                               f"fallback {nRg} x {nTg} global search; cutoff {rU}, K = {K}",
+                   "snr": f"{L['snr_lik']} over the likelihood's pixels",
+                   "train_particles": args.train_particles, "epochs": args.epochs,
+                   "labels": "the plain method's converged poses: FP32 global search, then "
+                             "three local phases of 1,000 x 100 (kappa 200 / 1,000 / 5,000, "
+                             "translation deviation 2 / 0.7 / 0.3 px)"
+                             + ("" if lab_prec == tg3.SCORE_FP32 else " (scored in split-bf16)"),
+                   "l2": "inputs larger than L2 (pixel data 159 MB, banks 0.55 GB per map)",
+                   "per_map_work": f"references and bank once per map ({map_ms:.1f} ms), "
+                                   f"charged over {per_map_particles} particles per map"},
+        "clocks": clocks,
+        "e2e": {"value": round(job_rate(n * args.e2e_steps, e2e_s * 1e3 + n * args.e2e_steps
+                                        * map_ms_pp, world), 1),
+                "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "wall_s": round(e2e_s, 3), "entry": "tg3_ExpectLearned3D (host buffers)",
+                "same_poses_as_device_entry": e2e_same},
+        "gpu_launches": learned_launches(st_l, fb, unseen.cls) * args.steps,
+        "roofline": roof,
+        "stages": stages,
+        "plain_fp32": {"value": round(v_p, 1), "ms_per_step": round(tp_ms / plain_steps, 3),
+                       "steps": plain_steps, "clocks": clocks_p,
+                       "what": f"FP32 global search, {nRg} x {nTg} hypotheses per particle"},
+        "speedup_vs_plain_fp32": round(v_l / v_p, 2),
+        "hypotheses_per_s": round(v_l * (nRot * nTrans + fb.mean() * nRg * nTg), 1),
+        "pose": {
+            "median_error_deg": {"plain_fp32_e_step": med(err(q_p)),
+                                 "learned_e_step": med(err(q_l)),
+                                 "plain_fp32_refined": med(err(q_p_r)),
+                                 "learned_refined": med(err(q_l_r)),
+                                 "north_star_rule_refined": med(err(q_B_r)),
+                                 "plain_method_converged": med(err(judge_un))},
+            "refined_gap_deg": round(float(np.median(err(q_l_r)) - np.median(err(q_p_r))), 3),
+            "within_5deg_of_plain_converged": round(float(np.mean(
+                learned.angle_deg(q_l_r, judge_un) < 5.0)), 4),
+            "note": "error = angle between the method's best rotation and the true one; "
+                    "refined = after one local phase of 1,000 x 100 about the method's pose "
+                    "(plain in FP32, learned in its own precision)"},
+        "fsc_0143_resolution_A": fsc_res,
+        "fsc_gap_refined_A": round(fsc_res["learned_refined"] - fsc_res["plain_fp32_refined"], 3),
+        "fallback": {
+            "rule": "peak score (best - median) / (1.4826 MAD) of the rescored proposals below "
+                    "a threshold; threshold = 5 % quantile of the peaks of the held-out "
+                    "particles of the training maps whose proposal is within 10 degrees of "
+                    "the plain method's converged pose",
+            "threshold": round(tau, 4), "fraction": round(float(fb.mean()), 4),
+            "north_star_rule": {
+                "rule": "global search on every particle; its pose where its best likelihood "
+                        "beats the proposal's",
+                "fraction": round(float(ruleB.mean()), 4),
+                "particles_per_s": round(job_rate(n, t_all_ms + n * map_ms_pp, world), 1),
+                "median_error_refined_deg": med(err(q_B_r))}},
+        "with_refinement": {
+            "plain_fp32_particles_per_s": round(job_rate(n, tp_ms / plain_steps + tr_p_ms,
+                                                         world), 1),
+            "learned_particles_per_s": round(job_rate(n, ms_step + n * map_ms_pp + tr_l_ms,
+                                                      world), 1),
+            "refine_ms": {"plain_fp32": round(tr_p_ms, 2), "learned": round(tr_l_ms, 2)}},
+        "training": {"label_s": round(label_s, 1), "train_s": round(train_s, 1),
+                     "label_median_error_deg": med(label_err),
+                     "label_phase_moves_deg": [round(float(x), 3) for x in
+                                               np.median(np.asarray(moves), 0)],
+                     "loss_per_epoch": [round(x, 4) for x in losses]},
+        "reference_maps": {"embed_ms_per_map": round(float(np.mean([embed_ms[c] for c in held])), 2),
+                           "bank_ms_per_map": round(float(np.mean([bank_ms[c] for c in held])), 2)},
+    }
+    if parity is not None:
+        res["parity_vs_fp64"] = parity
+    if rank == 0 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_baseline_global(ctx, maps[nTr], unseen, quats_g, box, pf,
+                                                  args.cpu_sample_global, 1)
     net.close()
     ctx.close()
     return res
+
+
+def learned_roofline(dom, st, steps, n, nRot, nTrans, K, Kp, fb):
+    """Roofline of the learned step's dominant stage.  The bank gather (the
+    'project' stage of the rescoring) moves, per proposed rotation, its hi
+    and lo bf16 rows (4 Kp bytes) and |P|^2 row (4 K) in and the operand rows
+    (4 Kp) out; the cross term does 4 K FLOP per hypothesis (3x in bf16)."""
+    hbm, bf16, src = peaks()
+    ms = st[dom][0] / max(st[dom][1], 1)
+    if dom == "project":
+        algo = float(n) * nRot * (8.0 * Kp + 4.0 * K + 4.0)
+        ach = algo / (ms * 1e-3) / 1e9
+        return {"kernel": "k_bank_gather (rescoring slices from the banks)", "bound": "hbm",
+                "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(ach / hbm, 4), "peak_source": f"hbm_gbs, {src} (MEASURED_PEAKS.json)",
+                "traffic": None, "algorithmic_bytes_per_launch": algo,
+                "ms_per_launch": round(ms, 4)}
+    if dom == "cross":
+        flop = 4.0 * K * float(n) * nRot * nTrans
+        ach = flop / (ms * 1e-3) / 1e12
+        return {"kernel": "k_gemm_bf16x3 (rescoring cross term)", "bound": "tensor",
+                "achieved": round(ach, 2), "peak": bf16, "unit": "TFLOP/s",
+                "frac": round(ach / bf16, 4), "peak_source": f"bf16_tflops, {src}",
+                "traffic": None, "algorithmic_flop_per_launch": flop,
+                "ms_per_launch": round(ms, 4)}
+    return {"kernel": dom, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s",
+            "frac": None, "traffic": None, "ms_per_launch": round(ms, 4),
+            "note": "dominant stage has no single-kernel byte count"}
+
+
+def learned_launches(st, fb, cls):
+    """Kernels of one learned E-step (this library's own): network 16 (8
+    weight repacks, the first convolution, 6 tensor-core layers, the output
+    layer), matching 1, priors 3, rescoring 5 (gather, shift bank, |X|^2,
+    cross term, weights), confidence and best pose 2; per class with
+    fallback particles 13 (3 gathers, priors, |P|^2, translations, shift
+    bank, |X|^2, norm operand, norm GEMM, cross term, weights, best pose)
+    and 1 for the translation priors."""
+    k = len(np.unique(np.asarray(cls)[np.asarray(fb, bool)]))
+    return 16 + 1 + 3 + 5 + 2 + (13 * k + 1 if k else 0)
+
+
+def _fp64_bank_rows(job):
+    """Worker: FP64 oracle projections of rows [r0, r1) of one map's bank,
+    written into the shared output file."""
+    import sys as _s
+    for p in job["paths"]:
+        if p not in _s.path:
+            _s.path.insert(0, p)
+    from oracle import oracle as O
+    vol = np.load(job["vol"], mmap_mode="r")
+    out = np.load(job["out"], mmap_mode="r+")
+    out[job["r0"]:job["r1"]] = O.project(np.asarray(vol), job["mats"], job["iCol"], job["iRow"],
+                                         job["pf"])
+    out.flush()
+    return job["r1"] - job["r0"]
+
+
+def proposal_parity_fp64(ctx, maps, ps, idx, trans, dvp, quats_g, box, pf, n_check, dev):
+    """The FP64 oracle's log-likelihoods of the proposals of n_check
+    particles (the first of every held-out map in turn): projections of the
+    bank rotations by the oracle (a spawn pool over the host's cores),
+    L(r, t) = sum_p sigRcp |X - c S_t P_r|^2 expanded as
+    x0 + sum sigRcp c^2 |P_r|^2 - 2 Re sum sigRcp c conj(X) S_t P_r, checked
+    against the oracle's logDataVSPrior on a sample.  Reports the fraction of
+    particles whose best proposal (argmax over rotation x translation) is
+    the oracle's, and the largest error of L - max L."""
+    import multiprocessing as mp
+    import tempfile
+    import torch
+    from tg3 import synth
+    from oracle import oracle as O
+    n = len(ps.cls)
+    order = []
+    per = {int(c): list(np.nonzero(ps.cls == c)[0]) for c in np.unique(ps.cls)}
+    while len(order) < min(n_check, n):
+        for c in per:
+            if per[c] and len(order) < n_check:
+                order.append(per[c].pop(0))
+    order = np.asarray(order)
+    iCol, iRow = ps.iCol, ps.iRow
+    mats = synth.quat_to_mat(quats_g).reshape(-1, 9)
+    workers = max(1, min(16, os.cpu_count() or 1))
+    tmp = tempfile.mkdtemp()
+    dat = ps.dat[torch.as_tensor(order, device=dev)].cpu().numpy().astype(np.complex128)
+    ctf = ps.ctf[torch.as_tensor(order, device=dev)].cpu().numpy().astype(np.float64)
+    sig = ps.sigRcp[torch.as_tensor(order, device=dev)].cpu().numpy().astype(np.float64)
+    t0 = time.perf_counter()
+    same, max_err, max_err_near, checked = 0, 0.0, 0.0, 0
+    spot = []
+    ctxp = mp.get_context("spawn")
+    with ctxp.Pool(workers) as pool:
+        for c in sorted(set(int(x) for x in ps.cls[order])):
+            vol = synth.padded_volume(maps[c], box, pf, device=dev,
+                                      dtype=torch.float64).cpu().numpy()
+            vpath = os.path.join(tmp, "vol.npy")
+            opath = os.path.join(tmp, "bank.npy")
+            np.save(vpath, vol)
+            del vol
+            bank = np.lib.format.open_memmap(opath, mode="w+", dtype=np.complex128,
+                                             shape=(len(mats), len(iCol)))
+            del bank
+            step = (len(mats) + workers - 1) // workers
+            jobs = [dict(vol=vpath, out=opath, r0=r0, r1=min(len(mats), r0 + step),
+                         mats=mats[r0:r0 + step], iCol=iCol, iRow=iRow, pf=pf,
+                         paths=[str(ROOT), str(PKG)]) for r0 in range(0, len(mats), step)]
+            pool.map(_fp64_bank_rows, jobs)
+            bank = np.load(opath, mmap_mode="r")
+            for j in np.nonzero(ps.cls[order] == c)[0]:
+                l = order[j]
+                P = np.asarray(bank[idx[l]])                       # [nRot][K]
+                S = O.translate(trans[l], box, iCol, iRow)         # [nTrans][K]
+                X, cc, ss = dat[j], ctf[j], sig[j]
+                x0 = float(np.sum(ss * np.abs(X) ** 2))
+                nrm = (np.abs(P) ** 2) @ (ss * cc * cc)
+                A = (ss * cc * np.conj(X))[None, :] * S
+                cross = np.real(A @ P.T)                          # [nTrans][nRot]
+                L64 = x0 + nrm[:, None] - 2.0 * cross.T           # [nRot][nTrans]
+                if len(spot) < 8:
+                    r, t = len(spot) % L64.shape[0], len(spot) % L64.shape[1]
+                    ref = O.logdvp(X, S[t] * P[r], cc, ss)
+                    spot.append(abs(ref - L64[r, t]) / abs(ref))
+                d64 = L64 - L64.max()
+                g = dvp[l].astype(np.float64)
+                dg = g - g.max()
+                same += int(np.argmax(L64) == np.argmax(g))
+                e = np.abs(dg - d64)
+                max_err = max(max_err, float(e.max()))
+                near = d64 > -30.0
+                max_err_near = max(max_err_near, float(e[near].max()))
+                checked += 1
+            del bank
+            os.unlink(opath)
+            os.unlink(vpath)
+    os.rmdir(tmp)
+    return {"particles": checked, "same_argmax": round(same / max(checked, 1), 5),
+            "max_abs_err_dL": round(max_err, 5),
+            "max_abs_err_dL_within_30": round(max_err_near, 5),
+            "expansion_check_rel": float(max(spot)) if spot else None,
+            "oracle_s": round(time.perf_counter() - t0, 1),
+            "what": "the learned step's rescored proposals (split-bf16) against the FP64 "
+                    "oracle: argmax over rotation x translation, and |(L - max L) - "
+                    "(L64 - max L64)| over all hypotheses and over those within 30 of the "
+                    "best (the ones with weight)"}
+
+
+def cpu_baseline_global(ctx, bm, ps, quats_g, box, pf, n_rot, workers):
+    """The oracle port of the reference's CPU global search (doGlobalSearch:
+    projections of the rotations, then every image against every rotation x
+    translation) on a bounded sample: one particle x n_rot of the 6,912
+    rotations x 49 translations, scaled to a full particle (the projections
+    are shared by all particles of an E-step and not charged)."""
+    import torch
+    from tg3 import synth
+    from oracle import oracle as O
+    vol = synth.padded_volume(bm, box, pf, device=ps.dat.device,
+                              dtype=torch.float32).cpu().numpy().astype(np.complex128)
+    sel = np.linspace(0, len(quats_g) - 1, n_rot).astype(int)
+    mats = synth.quat_to_mat(quats_g[sel]).reshape(-1, 9)
+    P = O.project(vol, mats, ps.iCol, ps.iRow, pf)
+    trans = synth.global_translations(3, 1.0)
+    S = O.translate(trans, box, ps.iCol, ps.iRow)
+    l = int(np.nonzero(ps.cls == ps.cls[0])[0][0])
+    X = ps.dat[l:l + 1].cpu().numpy().astype(np.complex128)
+    c = ps.ctf[l:l + 1].cpu().numpy().astype(np.float64)
+    s = ps.sigRcp[l:l + 1].cpu().numpy().astype(np.float64)
+    t0 = time.perf_counter()
+    O.score_global(P, S, X, c, s, np.full(n_rot, 1.0 / n_rot), np.full(len(trans), 1.0 / len(trans)),
+                   want_dvp=False)
+    secs = time.perf_counter() - t0
+    per_particle = secs * len(quats_g) / n_rot
+    return {"value": round(1.0 / per_particle, 6), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"1 particle x {n_rot} of the {len(quats_g)} global rotations x "
+                      f"{len(trans)} translations, K={len(ps.iCol)}, scaled to a full particle "
+                      f"({secs:.2f} s measured); double-precision oracle port of the "
+                      "reference's CPU global search (doGlobalSearch), one core"}
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per particle of a
@@ -1572,8 +1811,92 @@ def cpu_baseline(st, host, W, sample_rot):
                       "double-precision oracle port, one core"}
 
 
+def _cpu_global_worker(job):
+    """Score one particle against the shared projections (oracle port)."""
+    import sys as _s
+    for p in job["paths"]:
+        if p not in _s.path:
+            _s.path.insert(0, p)
+    from oracle import oracle as O
+    O.score_global(job["P"], job["S"], job["X"], job["c"], job["s"], job["pR"], job["pT"],
+                   want_dvp=False)
+    return 0
+
+
+def run_reference_learned(args, rank, world):
+    """The reference's CPU E-step that the learned E-step replaces: the
+    global search (doGlobalSearch, src/Optimiser.cpp:633-1136) of the
+    held-out maps' particles over 6,912 rotations x 49 translations, as the
+    oracle port on every host core (one particle per core), each step a
+    bounded sample of the rotations scaled to full particles."""
+    if rank != 0:
+        return None
+    import multiprocessing as mp
+    import torch
+    from tg3 import synth
+    from oracle import oracle as O
+    L = LEARNED256 if args.workload == "learned256" else LEARNED
+    box, px, pf, rU = L["box"], L["pixel_size"], L["pf"], L["rU"]
+    rng = np.random.default_rng(4000)
+    maps = [synth.blob_map(rng, L["n_blobs"], L["sigma_a"], px, L["radius_px"])
+            for _ in range(L["n_maps"])]
+    rL = synth.config_rL(box, px)
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    cores = os.cpu_count() or 1
+    nTr = L["n_train_maps"]
+    noise_var = synth.signal_power(maps[:nTr], box, px, rU, rL, device=dev) / L["snr_lik"] / 2.0
+    ps = synth.particle_set_dev(rank_seed(5002, rank), maps, np.full(cores, nTr), box, px, rU,
+                                rL, L["shift"], noise_var, device=dev)
+    vol = synth.padded_volume(maps[nTr], box, pf, device=dev,
+                              dtype=torch.float32).cpu().numpy().astype(np.complex128)
+    quats_g = synth.global_rotations(4, 36)
+    n_rot = args.cpu_sample_global
+    sel = np.linspace(0, len(quats_g) - 1, n_rot).astype(int)
+    P = O.project(vol, synth.quat_to_mat(quats_g[sel]).reshape(-1, 9), ps.iCol, ps.iRow, pf)
+    trans = synth.global_translations(3, 1.0)
+    S = O.translate(trans, box, ps.iCol, ps.iRow)
+    del vol
+    X = ps.dat.cpu().numpy().astype(np.complex128)
+    c = ps.ctf.cpu().numpy().astype(np.float64)
+    s = ps.sigRcp.cpu().numpy().astype(np.float64)
+    jobs = [dict(P=P, S=S, X=X[i:i + 1], c=c[i:i + 1], s=s[i:i + 1],
+                 pR=np.full(n_rot, 1.0 / n_rot), pT=np.full(len(trans), 1.0 / len(trans)),
+                 paths=[str(ROOT), str(PKG)]) for i in range(cores)]
+    times = []
+    with mp.get_context("spawn").Pool(cores) as pool:
+        pool.map(_cpu_global_worker, jobs)                  # start-up and page-in
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            pool.map(_cpu_global_worker, jobs)
+            if i >= args.warmup:
+                times.append(time.perf_counter() - t0)
+    per_step = float(np.mean(times))
+    value = cores * (n_rot / len(quats_g)) / per_step
+    sample = (f"{cores} particles of a held-out map (one per core) x {n_rot} of the "
+              f"{len(quats_g)} global rotations x {len(trans)} translations per step, K = "
+              f"{len(ps.iCol)}, scaled to full particles (the projections, shared by every "
+              "particle of an E-step, are made once and not timed); double-precision oracle "
+              "port of doGlobalSearch (the reference's sources are not on this machine)")
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(per_step * 1e3, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+            "data": "synthetic", "config": {"workload": f"E-step of the held-out maps' "
+                                            f"particles, box {box}: global search "
+                                            f"{len(quats_g)} x {len(trans)}, cutoff {rU}, "
+                                            f"K = {len(ps.iCol)}",
+                                            "sample_rotations": n_rot,
+                                            "particles_per_step": cores},
+            "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": cores,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
 def run_reference(args, rank, world):
     """The CPU implementation of the path on all host cores (rank 0 only)."""
+    if args.workload in ("learned128", "learned256"):
+        return run_reference_learned(args, rank, world)
     if rank != 0:
         return None
     import torch
@@ -1665,8 +1988,7 @@ def job_rate(units_per_rank: float, ms: float, world: int) -> float:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    # about 2 s of timed work at the default batch: enough clock samples
-    ap.add_argument("--steps", type=int, default=150)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="tg3", choices=["tg3", "reference"])
     ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16x3"])
@@ -1681,7 +2003,7 @@ def main():
     ap.add_argument("--fused", action="store_true",
                     help="split-bf16 path through the fused projection + tcgen05 kernel")
     ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
-    ap.add_argument("--workload", default="local256",
+    ap.add_argument("--workload", default="learned256",
                     choices=["local256", "local256c3", "global64", "uneven192", "learned128",
                              "learned256", "class2d128", "prep256", "reco256"])
     ap.add_argument("--train-particles", type=int, default=150000)
@@ -1701,6 +2023,17 @@ def main():
     ap.add_argument("--per-particle-sample", type=int, default=256,
                     help="particles timed one at a time beside the plan (uneven192)")
     ap.add_argument("--global-particles", type=int, default=2000)
+    ap.add_argument("--label-precision", default="fp32", choices=["fp32", "bf16x3"],
+                    help="precision of the plain method that labels the training particles")
+    ap.add_argument("--plain-steps", type=int, default=20,
+                    help="timed steps of the plain FP32 global search beside the learned step")
+    ap.add_argument("--check-particles", type=int, default=1000,
+                    help="particles whose proposals are checked against the FP64 oracle")
+    ap.add_argument("--cpu-sample-global", type=int, default=96,
+                    help="rotations per particle in the CPU global-search sample")
+    ap.add_argument("--no-local", action="store_true",
+                    help="learned workloads: skip the local-phase measurement beside them")
+    ap.add_argument("--verbose", action="store_true")
     args = ap.parse_args()
     rank, world, local = init_dist()
     if args.impl == "reference":
@@ -1717,6 +2050,16 @@ def main():
         res = run_reco(args, rank, world, local)
     elif args.workload in ("learned128", "learned256"):
         res = run_learned(args, rank, world, local)
+        if args.workload == "learned256" and not args.no_local:
+            # the local particle-filter phase at box 256 (1,000 x 100 per
+            # particle), split-bf16 beside plain FP32, kept beside the headline
+            import torch
+            torch.cuda.empty_cache()
+            loc = run_tg3(args, rank, world, local)
+            if res is not None and loc is not None:
+                res["local_phase_box256"] = {k: v for k, v in loc.items()
+                                             if k not in ("metric", "n_gpus", "higher_is_better",
+                                                          "scaling", "vs_baseline", "data")}
     else:
         res = run_tg3(args, rank, world, local)
     if rank == 0 and res is not None:

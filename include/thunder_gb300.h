@@ -124,6 +124,20 @@ int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter,
                  int cSearch, int opf, int npxl, int mReco, int idim,
                  int dimSize, int imgNum, int kernel);
 
+/* Replaces the multi-class InsertFT, gpu/interface/Interface.h:267-292
+ * (gpu/src/cuthunder.cu:4099): as tg3_InsertFT for the volume of one
+ * class, with nC [imgNum] the number of image l's draws that belong to it:
+ * draw m of image l is inserted, and counted in O3D and counter, only when
+ * m < nC[l] (0 <= nC[l] <= mReco; Optimiser::reconstructRef draws each
+ * image's classes and passes their counts, src/Optimiser.cpp:6808-6900). */
+int tg3_InsertFT_classes(float* F3D, float* T3D, double* O3D, int* counter,
+                         const float* datP, const float* ctfP, const float* sigRcpP,
+                         const float* ctfaData, const double* offS, const float* w,
+                         const double* nR, const double* nT, const double* nD,
+                         const int* nC, const int* iCol, const int* iRow, float pixelSize,
+                         int cSearch, int opf, int npxl, int mReco, int idim, int dimSize,
+                         int imgNum, int kernel);
+
 /* Local particle-filter scoring of one particle, the combined work of
  * ExpectLocalRTD + ExpectLocalPreI3D + ExpectLocalM,
  * gpu/interface/Interface.h:80-139 (no defocus search): project the nR
@@ -271,7 +285,9 @@ enum {
     TG3_STAGE_PROJECT = 0, TG3_STAGE_SHIFT = 1, TG3_STAGE_CROSS = 2,
     TG3_STAGE_WEIGHTS = 3, TG3_STAGE_RESAMPLE = 4, TG3_STAGE_INSERT = 5,
     TG3_STAGE_FUSED = 6,   /* projection + split-bf16 cross term in one kernel */
-    TG3_STAGE_COUNT = 7
+    TG3_STAGE_NETWORK = 7, /* learned E-step: network, matching, proposal confidence */
+    TG3_STAGE_FALLBACK = 8,/* learned E-step: global search of the fallback particles */
+    TG3_STAGE_COUNT = 9
 };
 int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
 
@@ -286,8 +302,14 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  *   0 scatters every pixel's support voxels with one atomic each (the
  *   reference's loop order), which is the faster of the two on GB300.  Both
  *   give the same sums up to FP32 rounding order; a pixel list holding a pixel
- *   twice always scatters. */
-enum { TG3_OPT_FUSED = 0, TG3_OPT_INSERT_GATHER = 1 };
+ *   twice always scatters.
+ * TG3_OPT_BANK_GATHER (default 0): 1 makes the split-bf16 bank-row local
+ *   phase (tg3_local_phase_bank_d, the learned E-step's rescoring) copy the
+ *   proposed rows into a slice buffer and sum their norms from the bank's
+ *   |P|^2 rows before the GEMM; 0 loads the GEMM's operand tiles straight
+ *   from the bank rows (TMA gather) and sums the norms from those tiles, in
+ *   compensated FP32. */
+enum { TG3_OPT_FUSED = 0, TG3_OPT_INSERT_GATHER = 1, TG3_OPT_BANK_GATHER = 2 };
 int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);
 
@@ -384,6 +406,74 @@ int tg3_cnn_match_propose(const float* out, int n, const float* ref, int nRef,
                           const double* refQuat, int nRot, int nTrans,
                           unsigned long long seed, double* quat, double* trans, int* idx,
                           void* stream);
+
+/* ------------------------------------------------------ learned E-step --
+ * The first expectation of a refinement with the pose network's proposals
+ * in place of the uniform global search.  It replaces the global search of
+ * ExpectGlobal3D (gpu/interface/Interface.h:221; CPU
+ * Optimiser::doGlobalSearch, src/Optimiser.cpp:633-1136), which stays the
+ * fallback; the network itself has no counterpart in the reference.
+ *
+ * Set-up per class k (its volume set, the active pixel set made):
+ *   tg3_ctx_set_bank(ctx, k, quat, nB)       projections at nB rotations;
+ *   tg3_ctx_set_references(ctx, k, emb, nB)  the network's normalised
+ *     embeddings [nB][64] (device) of clean references at the same
+ *     rotations (tg3_cnn_infer + tg3_cnn_embed of the rendered references).
+ *
+ * tg3_learned_expect_d, per particle l of class cls[l] (device inputs:
+ * images [nP][64][64] the network's input, dat [nP][K] complex, ctf,
+ * sigRcp [nP][K], cls [nP], gTrans [nTg][2] the fallback's translation grid):
+ *   1. the network's embedding of the image;
+ *   2. proposals: the nRot references of class cls[l] of highest cosine
+ *      score (ties to the lower index) x nTrans shifts drawn from the
+ *      network's shift output (counter-based, from `seed`);
+ *   3. every proposal scored by the exact likelihood (as tg3_local_phase_d,
+ *      uniform priors), slices read from the class's bank;
+ *   4. confidence peak[l] = (max - median) / (1.4826 (MAD + 1e-12)) of the
+ *      nRot x nTrans log-likelihoods;
+ *   5. particles with peak[l] < peakMin (or not a number) fall back to the
+ *      global search over the bank's nB rotations x gTrans (uniform priors),
+ *      reusing the bank's projections.
+ * Required outputs (device): bestQuat [nP][4] and bestTrans [nP][2], the
+ * argmax of the rotation and of the translation marginals of the method
+ * the particle used, and baseL [nP] its largest log-likelihood.  Optional
+ * (NULL to skip): peak, fellBack [nP]; the proposals' bank rows propIdx
+ * [nP][nRot], rotations propQuat [nP][nRot][4], translations propTrans
+ * [nP][nTrans][2], marginals propWR [nP][nRot], propWT [nP][nTrans], best
+ * log-likelihood propBase [nP] and log-likelihoods propDvp
+ * [nP][nRot][nTrans] (less the per-particle constant, as dvp of
+ * tg3_local_phase_d).  nTrans, nTg <= 256, nRot x nTrans <= 16384, nRot at
+ * most every used class's reference count.  Returns after the work has
+ * finished (the fallback's sizes are read on the host).
+ *
+ * tg3_ExpectLearned3D: the same with every array in host memory (copied in
+ * and out on the context's stream; page-locked buffers copy fastest). */
+typedef struct tg3_learned_out {
+    double* bestQuat;
+    double* bestTrans;
+    double* baseL;
+    float* peak;
+    int* fellBack;
+    int* propIdx;
+    double* propQuat;
+    double* propTrans;
+    double* propWR;
+    double* propWT;
+    double* propBase;
+    float* propDvp;
+} tg3_learned_out;
+int tg3_ctx_set_references(tg3_ctx* ctx, int cls, const float* emb, int n);
+int tg3_learned_expect_d(tg3_ctx* ctx, tg3_cnn* net, int nP, const float* images,
+                         const float* dat, const float* ctf, const float* sigRcp,
+                         const int* cls, int nRot, int nTrans, unsigned long long seed,
+                         const double* gTrans, int nTg, float peakMin, int precision,
+                         const tg3_learned_out* out);
+int tg3_ExpectLearned3D(tg3_ctx* ctx, tg3_cnn* net, int nP, const float* images,
+                        const float* dat, const float* ctf, const float* sigRcp,
+                        const int* cls, int nRot, int nTrans, unsigned long long seed,
+                        const double* gTrans, int nTg, float peakMin, int precision,
+                        double* bestQuat, double* bestTrans, double* baseL, float* peak,
+                        int* fellBack);
 
 /* The global scan of one 2-D class image img [vdim][vdim/2 + 1] complex
  * (device) at in-plane rotations rot [nR][2] = (cos, sin): otherwise as

@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import re
 import subprocess
 from pathlib import Path
 
@@ -21,7 +22,18 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libthunder_ref.so"
-REF_TREE = Path(os.environ.get("THUNDER_REF", "/root/reference"))
+
+
+def _default_ref_tree() -> str:
+    """The THUNDER tree the cross-check library is built from: THUNDER_REF,
+    else the default of the build recipe (oracle/ref/Makefile's REF)."""
+    if os.environ.get("THUNDER_REF"):
+        return os.environ["THUNDER_REF"]
+    m = re.search(r"^REF \?= (\S+)$", (HERE / "ref" / "Makefile").read_text(), flags=re.M)
+    return m.group(1) if m else ""
+
+
+REF_TREE = Path(_default_ref_tree())
 
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")

@@ -1,6 +1,7 @@
 /* Single-process stand-in for <mpi.h>, used only to compile the reference's
- * sources for the oracle's cross-check library (oracle/_ref).  It declares the
- * MPI names those sources mention; nothing in the cross-check calls them. */
+ * sources for the oracle's cross-check library (oracle/_ref) and the drop-in
+ * adaptor in the compile test.  It declares the MPI names those sources
+ * mention; nothing in the cross-check calls them. */
 #ifndef TG3_REF_MPI_SHIM_H
 #define TG3_REF_MPI_SHIM_H
 typedef int MPI_Comm;
@@ -10,6 +11,7 @@ typedef int MPI_Group;
 typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
 #define MPI_COMM_WORLD 0
 #define MPI_COMM_NULL (-1)
+#define MPI_SUCCESS 0
 #define MPI_SUM 1
 #define MPI_IN_PLACE ((void*)1)
 #define MPI_INT 1

@@ -74,7 +74,7 @@ static cudaEvent_t take_event(tg3_ctx* c)
 
 StageTimer::StageTimer(tg3_ctx* c_, int s) : c(c_), stage(s)
 {
-    if (!c->timing) return;
+    if (!c->timing || c->stageMute) return;
     a = take_event(c);
     b = take_event(c);
     if (a) cudaEventRecord(a, c->stream);
@@ -222,20 +222,6 @@ static int upload(tg3_ctx* c, WsSlot slot, size_t offset_bytes, const T* host, s
     return TG3_OK;
 }
 
-// Bump allocator over one workspace slot (host-staged arrays of one call).
-struct Arena {
-    tg3_ctx* c;
-    WsSlot slot;
-    size_t used = 0;
-    std::vector<std::pair<size_t, size_t>> items;
-    Arena(tg3_ctx* c_, WsSlot s) : c(c_), slot(s) {}
-    size_t add(size_t bytes)
-    {
-        size_t off = round_up(used, 256);
-        used = off + bytes;
-        return off;
-    }
-};
 
 }  // namespace tg3
 
@@ -326,8 +312,11 @@ extern "C" int tg3_ctx_destroy(tg3_ctx* c)
         cudaFree(b.f32);
         cudaFree(b.hi);
         cudaFree(b.abs2);
+        cudaFree(b.quat);
+        cudaFree(b.emb);
     }
     cudaFree(c->d_bankTable);
+    cudaFree(c->d_refTable);
     cudaFree(c->d_flag);
     cudaFree(c->d_volTable);
     for (auto& v : c->pending)
@@ -560,6 +549,28 @@ static int local_phase(tg3_ctx* c, const int* bankIdx, int nP, int nR, int nT, c
         }
         return TG3_OK;
     }
+    if (bankIdx && split && !c->bankGather) {
+        // the cross term reads the proposed rows straight from the banks and
+        // sums their norms itself: no slice copy, no |P|^2 rows
+        {
+            StageTimer tm(c, TG3_STAGE_SHIFT);
+            TG3_CUDA(launch_shift_bank(reinterpret_cast<const float2*>(dat), ctf, sigRcp, trans,
+                                       nullptr, nP, nT, c->px.idim, c->px.iCol, c->px.iRow, K,
+                                       A, Kp, splitA, s));
+            TG3_CUDA(launch_x0(reinterpret_cast<const float2*>(dat), sigRcp, nP, K, x0, s));
+        }
+        {
+            StageTimer tm(c, TG3_STAGE_CROSS);
+            TG3_CUDA(launch_gemm_bank_bf16x3(c->bank, c->px.gen, bankIdx, cls, nP, nR, A, nT, Kp,
+                                             K, sigRcp, ctf, D, -2.0f, c->d_flag, s));
+        }
+        {
+            StageTimer tm(c, TG3_STAGE_WEIGHTS);
+            TG3_CUDA(launch_weights(D, (long long)nR * nT, nT, nR, nT, 1, nP, nullptr, 0, x0, pwR,
+                                    nR, pwT, nT, pwC, wC, wR, wT, baseL, dvp, s));
+        }
+        return TG3_OK;
+    }
     if (bankIdx) {
         StageTimer tm(c, TG3_STAGE_PROJECT);
         TG3_CUDA(launch_bank_gather(c->d_bankTable, cls, bankIdx, nP, nR, K, Kp, sigRcp, ctf, P,
@@ -725,24 +736,39 @@ extern "C" int tg3_local_phase_ctf_d(tg3_ctx* c, int nP, int nR, int nT, int nD,
 }
 
 // ================================================================= banks
-// Upload the device views of the banks; a bank built on another pixel set
-// than the active one shows no rows, so an index into it is flagged.
-static int upload_bank_table(tg3_ctx* c, bool* anyValid)
+// Upload the device views of the banks and of the references; a bank built
+// on another pixel set than the active one shows no rows, so an index into
+// it is flagged, and its references are not offered.
+int tg3::upload_bank_views(tg3_ctx* c, bool* anyBank, bool* anyRef)
 {
     if (!c->d_bankTable) TG3_CUDA(cudaMalloc(&c->d_bankTable, sizeof(BankView) * kMaxClasses));
+    if (!c->d_refTable) TG3_CUDA(cudaMalloc(&c->d_refTable, sizeof(RefView) * kMaxClasses));
     BankView view[kMaxClasses];
-    bool any = false;
+    RefView ref[kMaxClasses];
+    bool any = false, anyR = false;
     for (int k = 0; k < kMaxClasses; k++) {
         const Bank& q = c->bank[k];
         const bool ok = q.nB > 0 && q.gen == c->px.gen && q.K == c->px.K;
         const size_t rf = (size_t)q.nB * q.Kp;
         view[k] = {q.f32, q.hi, q.hi ? q.hi + rf : nullptr, q.abs2, ok ? q.nB : 0};
+        const bool okR = ok && q.emb && q.nEmb == q.nB;
+        ref[k] = {q.emb, q.quat, okR ? q.nEmb : 0};
         any = any || ok;
+        anyR = anyR || okR;
     }
     TG3_CUDA(cudaMemcpyAsync(c->d_bankTable, view, sizeof(view), cudaMemcpyHostToDevice,
                              c->stream));
-    if (anyValid) *anyValid = any;
+    TG3_CUDA(cudaMemcpyAsync(c->d_refTable, ref, sizeof(ref), cudaMemcpyHostToDevice,
+                             c->stream));
+    if (anyBank) *anyBank = any;
+    if (anyRef) *anyRef = anyR;
+    // (copies from pageable memory return once the source has been staged)
     return TG3_OK;
+}
+
+static int upload_bank_table(tg3_ctx* c, bool* anyValid)
+{
+    return upload_bank_views(c, anyValid, nullptr);
 }
 
 extern "C" int tg3_ctx_set_bank(tg3_ctx* c, int cls, const double* quat, int nB)
@@ -759,12 +785,17 @@ extern "C" int tg3_ctx_set_bank(tg3_ctx* c, int cls, const double* quat, int nB)
     const size_t rowF = (size_t)nB * Kp;
     const size_t need = rowF * sizeof(float) + 2 * rowF * sizeof(__nv_bfloat16) +
                         (size_t)nB * K * sizeof(float);
-    if (b.bytes < need) {
+    // the references belong to the previous rotation set
+    b.nEmb = 0;
+    if (b.bytes < need || b.nB != nB) {
         TG3_CUDA(cudaStreamSynchronize(c->stream));
         cudaFree(b.f32);
         cudaFree(b.hi);
         cudaFree(b.abs2);
+        cudaFree(b.quat);
+        cudaFree(b.emb);
         b = Bank();
+        TG3_CUDA(cudaMalloc(&b.quat, (size_t)nB * 4 * sizeof(double)));
         TG3_CUDA(cudaMalloc(&b.f32, rowF * sizeof(float)));
         TG3_CUDA(cudaMalloc(&b.hi, 2 * rowF * sizeof(__nv_bfloat16)));
         TG3_CUDA(cudaMalloc(&b.abs2, (size_t)nB * K * sizeof(float)));
@@ -776,6 +807,8 @@ extern "C" int tg3_ctx_set_bank(tg3_ctx* c, int cls, const double* quat, int nB)
                             c->px.iCol, c->px.iRow, K, b.f32, Kp, nullptr, nullptr, nullptr, pscr,
                             c->d_flag, 0, c->stream));
     TG3_CUDA(launch_bank_planes(b.f32, nB, K, Kp, b.hi, b.hi + rowF, b.abs2, c->stream));
+    TG3_CUDA(cudaMemcpyAsync(b.quat, quat, (size_t)nB * 4 * sizeof(double),
+                             cudaMemcpyDeviceToDevice, c->stream));
     b.nB = nB;
     b.K = K;
     b.Kp = Kp;
@@ -892,10 +925,12 @@ extern "C" int tg3_ctx_insert_begin(tg3_ctx* c, int vdim, int pf)
 
 // ctfRows == nDraws: one CTF row per draw (the defocus search), else one
 // per image
+// nC (device, per image; NULL: every draw): draw m of image l is inserted
+// only when m < nC[l] (the multi-class InsertFT); it takes the scatter form.
 static int insert_draws(tg3_ctx* c, int nDraws, int drawsPerImage, const float* dat,
                         const float* ctf, const double* quat, const double* trans,
                         const double* offset, const float* w, int kernel, double* O3D,
-                        int* counter, int ctfRows = 0)
+                        int* counter, int ctfRows = 0, const int* nC = nullptr)
 {
     if (!c->ins.acc) return fail(TG3_ERR_STATE, "insertion volume not begun");
     if (kernel != TG3_KERNEL_MKB && kernel != TG3_KERNEL_TRILINEAR)
@@ -903,7 +938,7 @@ static int insert_draws(tg3_ctx* c, int nDraws, int drawsPerImage, const float* 
     int st = check_geometry(c, c->ins.vdim, c->ins.pf, 2.0);
     if (st) return st;
     StageTimer tm(c, TG3_STAGE_INSERT);
-    if (kernel == TG3_KERNEL_MKB && c->insertGather && c->px.unique && c->px.cellPix) {
+    if (kernel == TG3_KERNEL_MKB && c->insertGather && c->px.unique && c->px.cellPix && !nC) {
         const size_t per = insert_draw_bytes(c->px.maxAbs);
         const size_t bytes = std::max(per, std::min((size_t)nDraws * per, (size_t)96 << 20));
         void* scratch = ws_get(c, WS_INSERT, bytes, &st);
@@ -925,7 +960,7 @@ static int insert_draws(tg3_ctx* c, int nDraws, int drawsPerImage, const float* 
                            c->ins.tabInvStep, nDraws, drawsPerImage,
                            reinterpret_cast<const float2*>(dat), ctf, quat, trans, offset, w,
                            c->px.iCol, c->px.iRow, c->px.K, c->ins.pf, c->px.idim, O3D,
-                           counter, params, c->stream, ctfRows));
+                           counter, params, c->stream, ctfRows, nC));
     return TG3_OK;
 }
 
@@ -1212,14 +1247,13 @@ extern "C" int tg3_ExpectGlobal3D(const float* rotP, const float* traP, const fl
     return TG3_OK;
 }
 
-extern "C" int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter, const float* datP,
-                            const float* ctfP, const float* sigRcpP, const float* ctfaData,
-                            const double* offS, const float* w, const double* nR,
-                            const double* nT, const double* nD, const int* iCol, const int* iRow,
-                            float pixelSize, int cSearch, int opf, int npxl, int mReco, int idim,
-                            int dimSize, int imgNum, int kernel)
+static int insert_ft(float* F3D, float* T3D, double* O3D, int* counter, const float* datP,
+                     const float* ctfP, const float* ctfaData, const double* offS,
+                     const float* w, const double* nR, const double* nT, const double* nD,
+                     const int* nC, const int* iCol, const int* iRow, float pixelSize,
+                     int cSearch, int opf, int npxl, int mReco, int idim, int dimSize,
+                     int imgNum, int kernel)
 {
-    (void)sigRcpP;
     if (!F3D || !T3D || !O3D || !counter || !datP || (!ctfP && !cSearch) || !offS || !w || !nR ||
         !nT || !iCol || !iRow)
         return fail(TG3_ERR_ARG, "null pointer");
@@ -1255,7 +1289,8 @@ extern "C" int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter, c
            oO = ar.add(sizeof(double) * 3), on = ar.add(sizeof(int)),
            oa = ar.add(cSearch ? sizeof(float) * 7 * (size_t)nb : 0),
            oda = ar.add(cSearch ? sizeof(float) * 7 * (size_t)nb * mReco : 0),
-           ond = ar.add(cSearch ? sizeof(double) * (size_t)nb * mReco : 0);
+           ond = ar.add(cSearch ? sizeof(double) * (size_t)nb * mReco : 0),
+           onc = ar.add(nC ? sizeof(int) * (size_t)nb : 0);
     char* b = (char*)ws_get(c, WS_H2D, ar.used, &st);
     if (!b) return st;
     TG3_CUDA(cudaMemcpyAsync(b + oO, O3D, sizeof(double) * 3, cudaMemcpyHostToDevice, s));
@@ -1284,10 +1319,14 @@ extern "C" int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter, c
         TG3_CUDA(cudaMemcpyAsync(b + oo, offS + 2 * (size_t)l0, sizeof(double) * 2 * (size_t)n,
                                  cudaMemcpyHostToDevice, s));
         TG3_CUDA(cudaMemcpyAsync(b + ow, w + l0, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, s));
+        if (nC)
+            TG3_CUDA(cudaMemcpyAsync(b + onc, nC + l0, sizeof(int) * (size_t)n,
+                                     cudaMemcpyHostToDevice, s));
         if ((st = insert_draws(c, n * mReco, mReco, (const float*)(b + od), (const float*)(b + oc),
                                (const double*)(b + oq), (const double*)(b + ot),
                                (const double*)(b + oo), (const float*)(b + ow), kernel,
-                               (double*)(b + oO), (int*)(b + on), cSearch ? n * mReco : 0)))
+                               (double*)(b + oO), (int*)(b + on), cSearch ? n * mReco : 0,
+                               nC ? (const int*)(b + onc) : nullptr)))
             return st;
         // the staging buffer is reused by the next pass
         TG3_CUDA(cudaStreamSynchronize(s));
@@ -1304,6 +1343,37 @@ extern "C" int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter, c
     TG3_CUDA(cudaMemcpyAsync(O3D, b + oO, sizeof(double) * 3, cudaMemcpyDeviceToHost, s));
     TG3_CUDA(cudaMemcpyAsync(counter, b + on, sizeof(int), cudaMemcpyDeviceToHost, s));
     return sync_and_check(c);
+}
+
+extern "C" int tg3_InsertFT(float* F3D, float* T3D, double* O3D, int* counter, const float* datP,
+                            const float* ctfP, const float* sigRcpP, const float* ctfaData,
+                            const double* offS, const float* w, const double* nR,
+                            const double* nT, const double* nD, const int* iCol, const int* iRow,
+                            float pixelSize, int cSearch, int opf, int npxl, int mReco, int idim,
+                            int dimSize, int imgNum, int kernel)
+{
+    (void)sigRcpP;
+    return insert_ft(F3D, T3D, O3D, counter, datP, ctfP, ctfaData, offS, w, nR, nT, nD, nullptr,
+                     iCol, iRow, pixelSize, cSearch, opf, npxl, mReco, idim, dimSize, imgNum,
+                     kernel);
+}
+
+extern "C" int tg3_InsertFT_classes(float* F3D, float* T3D, double* O3D, int* counter,
+                                    const float* datP, const float* ctfP, const float* sigRcpP,
+                                    const float* ctfaData, const double* offS, const float* w,
+                                    const double* nR, const double* nT, const double* nD,
+                                    const int* nC, const int* iCol, const int* iRow,
+                                    float pixelSize, int cSearch, int opf, int npxl, int mReco,
+                                    int idim, int dimSize, int imgNum, int kernel)
+{
+    (void)sigRcpP;
+    if (!nC) return fail(TG3_ERR_ARG, "null nC");
+    for (int l = 0; l < imgNum; l++)
+        if (nC[l] < 0 || nC[l] > mReco)
+            return fail(TG3_ERR_ARG, "nC[l] must lie in [0, mReco]");
+    return insert_ft(F3D, T3D, O3D, counter, datP, ctfP, ctfaData, offS, w, nR, nT, nD, nC,
+                     iCol, iRow, pixelSize, cSearch, opf, npxl, mReco, idim, dimSize, imgNum,
+                     kernel);
 }
 
 // ====================================================== volume handle + local
@@ -1463,7 +1533,7 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
                        const float* sigRcp, const double* rotMat, const double* trans,
                        const double* pR, const double* pT, double* wC, double* wR, double* wT,
                        double* baseL, float* dvp, int precision, int nK = 1,
-                       size_t imgStride = 0);
+                       size_t imgStride = 0, const Bank* pbank = nullptr);
 static int merge_classes(tg3_ctx* c, int n, int nK, int nR, int nT, const double* wCd,
                          const double* wRd, const double* wTd, const double* bd, float* wC,
                          float* wR, float* wT, float* baseL);
@@ -1709,6 +1779,7 @@ extern "C" int tg3_ctx_set_option(tg3_ctx* c, int option, int value)
     if (st) return st;
     if (option == TG3_OPT_FUSED) c->fused = value != 0;
     else if (option == TG3_OPT_INSERT_GATHER) c->insertGather = value != 0;
+    else if (option == TG3_OPT_BANK_GATHER) c->bankGather = value != 0;
     else return fail(TG3_ERR_ARG, "unknown option");
     return TG3_OK;
 }
@@ -1784,9 +1855,19 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
                        int nImg, int nR, int nT, const float* dat, const float* ctf,
                        const float* sigRcp, const double* rotMat, const double* trans,
                        const double* pR, const double* pT, double* wC, double* wR, double* wT,
-                       double* baseL, float* dvp, int precision, int nK, size_t imgStride)
+                       double* baseL, float* dvp, int precision, int nK, size_t imgStride,
+                       const Bank* pbank)
 {
     int st = TG3_OK;
+    if (pbank) {
+        // the rotations are the bank's, already projected on the active pixels
+        if (pbank->nB <= 0 || pbank->gen != c->px.gen || pbank->K != c->px.K)
+            return fail(TG3_ERR_STATE, "no projection bank of the class on the active pixel set");
+        nR = pbank->nB;
+        nK = 1;
+        img2 = nullptr;
+        rotMat = pbank->quat;   // checked as non-null only
+    }
     if (nImg <= 0 || nR <= 0 || nT <= 0 || nT > 2048) return fail(TG3_ERR_ARG, "bad scan shape");
     if (nK < 1 || (nK > 1 && !img2) || (long long)nK * nR > (1LL << 20))
         return fail(TG3_ERR_ARG, "bad class count");
@@ -1804,7 +1885,8 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
     long long ib = (4LL << 30) / (4LL * nRt * nT);
     const int IB = (int)std::max(1LL, std::min(std::min((long long)nImg, ib), 65535LL));
     // workspace
-    float* P = (float*)ws_get(c, WS_P, 4 * (size_t)nRt * Kp, &st);
+    float* P = pbank ? (split ? reinterpret_cast<float*>(pbank->hi) : pbank->f32)
+                    : (float*)ws_get(c, WS_P, 4 * (size_t)nRt * Kp, &st);
     if (!P) return st;
     float* A = (float*)ws_get(c, WS_A, 4 * (size_t)IB * nT * Kp, &st);
     if (!A) return st;
@@ -1826,15 +1908,18 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
     float* sc2 = (float*)(m + oSc);
     float* nrmC = (float*)(m + oNc);
     double* x0r = (double*)(m + oX0);
-    float* pscr = img2 ? nullptr
-                       : (float*)ws_get(c, WS_PROJ, sizeof(float) * project_scratch_floats(nR, Kp),
-                                        &st);
-    if (!img2 && !pscr) return st;
+    float* pscr = (img2 || pbank)
+                      ? nullptr
+                      : (float*)ws_get(c, WS_PROJ, sizeof(float) * project_scratch_floats(nR, Kp),
+                                       &st);
+    if (!img2 && !pbank && !pscr) return st;
     cudaStream_t s = c->stream;
     const long long splitP = split ? (long long)nRt * Kp : 0;
     {
         StageTimer tm(c, TG3_STAGE_PROJECT);
-        if (img2) {
+        if (pbank) {
+            // the bank's planes are the projections (hi then lo: nB Kp apart)
+        } else if (img2) {
             for (int k = 0; k < nK; k++) {
                 // class k's rows start k nR rows in (bf16 rows in the split layout)
                 const size_t off = (size_t)k * nR * Kp;
@@ -1906,6 +1991,18 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
         }
     }
     return TG3_OK;
+}
+
+int tg3::global_scan_bank(tg3_ctx* c, int cls, int nImg, int nT, const float* dat,
+                          const float* ctf, const float* sigRcp, const double* trans,
+                          const double* pR, const double* pT, double* wC, double* wR,
+                          double* wT, double* baseL, float* dvp, int precision)
+{
+    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].blocks)
+        return fail(TG3_ERR_STATE, "volume of the class not set");
+    const Volume& v = c->vol[cls];
+    return global_scan(c, &v, nullptr, v.vdim, v.pf, nImg, 0, nT, dat, ctf, sigRcp, nullptr,
+                       trans, pR, pT, wC, wR, wT, baseL, dvp, precision, 1, 0, &c->bank[cls]);
 }
 
 extern "C" int tg3_global_scan_d(tg3_ctx* c, int cls, int nImg, int nR, int nT, const float* dat,

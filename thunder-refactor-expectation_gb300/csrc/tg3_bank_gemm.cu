@@ -1,0 +1,376 @@
+// tg3_bank_gemm.cu -- the rescoring cross term with the proposals' slices
+// read straight from the projection banks.
+//
+// The learned E-step scores nR proposed rotations x nT translations of every
+// particle.  The rotations are rows of its class's projection bank (the
+// class projected once at a fixed rotation set), so the slices need no
+// projection -- and no copy either: this kernel loads each 128-row A tile of
+// the cross-term GEMM from the bank rows the particle proposed, with TMA
+// tile::gather4 loads (four rows of one K block per instruction, box one row
+// high, 128-byte swizzle), and computes the rows' norms sum_p sigRcp ctf^2
+// |P|^2 from the same staged tiles.  Against the gather-then-GEMM form it
+// saves, per proposed row, the copy written and read back (8 Kp bytes) and
+// the |P|^2 row read for the norm (4 K bytes).
+//
+// C[l][r][t] = alpha sum_k Ph[l,r][k] (Bh + Bl)[l,t][k] + Pl Bh + nrm[l][r],
+// the split-bf16 product of tg3_tc.cu (hi x hi + hi x lo + lo x hi, FP32
+// accumulation in tensor memory).  One CTA per (128-row tile, particle),
+// 192 threads, warp-specialised:
+//   warp 4      : TMA producer (lane 0: the B tiles and the stage's byte
+//                 count; every lane: two gather4 loads of the A planes);
+//   warp 5      : tensor-memory allocation; lane 0 issues the tcgen05.mma
+//                 and commits each stage to its empty barrier;
+//   warps 0 - 3 : thread t sums row t's norm in compensated (Kahan) FP32 as
+//                 each stage lands, then releases the stage; afterwards the
+//                 epilogue (tcgen05.ld 32x32b, + norm, coalesced stores).
+// A stage is free when the MMAs that read it have completed and the four
+// norm warps have read it (empty barrier count 5).  Every wait is bounded
+// (clock budget); on expiry the CTA records TG3 flag bit 4, stops issuing,
+// waits (bounded) for its own copies and MMAs, frees its tensor memory and
+// returns.  A bank row index outside the particle's bank sets flag bit 16
+// and row 0 is read in its place.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tg3_internal.cuh"
+#include "tg3_tcgen05.cuh"
+
+namespace tg3 {
+
+namespace {
+
+using namespace tc;
+
+constexpr int BG_M = 128;          // rows of A per CTA (UMMA M)
+constexpr int BG_BK = 64;          // bf16 elements per K block (one 128-byte row)
+constexpr int BG_THREADS = 192;
+
+struct BankMaps {
+    CUtensorMap hi[kMaxClasses];
+    CUtensorMap lo[kMaxClasses];
+    int nB[kMaxClasses];           // rows of each class's bank (0: none)
+};
+
+struct BgParams {
+    int nR, nT, Kd, K;             // rows / columns per particle, K (bf16 elements), pixels
+    int ntile, tmemCols, stages;
+    const int* idx;                // [nP][nR] bank rows
+    const int* cls;                // [nP] (null: class 0)
+    const float* sigRcp;           // [nP][K]
+    const float* ctf;              // [nP][K]
+    float* C;                      // [nP][nR][nT]
+    float alpha;
+    int* flag;
+};
+
+__device__ __forceinline__ void tma_gather4(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int col, int r0, int r1, int r2, int r3)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(col), "r"(r0), "r"(r1), "r"(r2), "r"(r3),
+        "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Kahan summation step: s + v with the lost low part kept in c.
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v)
+{
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+__global__ void __launch_bounds__(BG_THREADS, 1)
+k_gemm_bank_bf16x3(const __grid_constant__ BankMaps maps, const __grid_constant__ CUtensorMap tmBh,
+                   const __grid_constant__ CUtensorMap tmBl, const BgParams p)
+{
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const int aBytes = BG_M * BG_BK * 2;                  // 16 KB per plane
+    const int bBytes = p.ntile * BG_BK * 2;
+    const int stageBytes = 2 * aBytes + 2 * bBytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + p.stages * stageBytes);
+    uint64_t* empty = full + p.stages;
+    uint64_t* accum = empty + p.stages;
+    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(accum + 1);
+    int* abortFlag = reinterpret_cast<int*>(tmemSlot + 1);
+    int* rows = abortFlag + 1;                            // [BG_M] bank rows of the tile
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mtile = blockIdx.x, item = blockIdx.y;
+    const int cl = p.cls ? p.cls[item] : 0;
+    const bool clOk = cl >= 0 && cl < kMaxClasses && maps.nB[cl] > 0;
+    const int k = clOk ? cl : 0;
+    const int nB = clOk ? maps.nB[k] : 0;
+    const int nkb = p.Kd / BG_BK;
+    const int bRow0 = item * p.nT;
+
+    if (threadIdx.x < BG_M) {
+        const int r = mtile * BG_M + threadIdx.x;
+        int b = 0;
+        if (r < p.nR) {
+            b = p.idx[(size_t)item * p.nR + r];
+            if (b < 0 || b >= nB) {
+                atomicOr(p.flag, 1 << 16);
+                b = 0;
+            }
+        }
+        rows[threadIdx.x] = b;
+    }
+    if (threadIdx.x == BG_M) {
+        for (int s = 0; s < p.stages; s++) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 5);
+        }
+        mbar_init(accum, 1);
+        *abortFlag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 5) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmemSlot)),
+                     "r"(p.tmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmemSlot;
+
+    int issuedTma = 0;      // K blocks whose copies were issued (producer lane 0)
+    int issuedMma = 0;      // K blocks whose MMAs were issued (issuer)
+    float nrmS = 0.f, nrmC = 0.f;
+    if (warp == 4) {
+        // ---------------- TMA producer
+        const CUtensorMap* mh = &maps.hi[k];
+        const CUtensorMap* ml = &maps.lo[k];
+        const int r0 = rows[4 * lane], r1 = rows[4 * lane + 1], r2 = rows[4 * lane + 2],
+                  r3 = rows[4 * lane + 3];
+        for (int kb = 0; kb < nkb; kb++) {
+            const int s = kb % p.stages;
+            const int round = kb / p.stages;
+            int go = 1;
+            uint8_t* st = smem + s * stageBytes;
+            if (lane == 0) {
+                if (round > 0 && !mbar_wait(empty + s, (round - 1) & 1, kWaitBudget)) {
+                    atomicOr(p.flag, 4);
+                    *(volatile int*)abortFlag = 1;
+                    go = 0;
+                } else if (*(volatile int*)abortFlag) {
+                    go = 0;
+                } else {
+                    mbar_expect_tx(full + s, stageBytes);
+                    tma_load_2d(st + 2 * aBytes, &tmBh, full + s, kb * BG_BK, bRow0);
+                    tma_load_2d(st + 2 * aBytes + bBytes, &tmBl, full + s, kb * BG_BK, bRow0);
+                    issuedTma = kb + 1;
+                }
+            }
+            go = __shfl_sync(0xffffffffu, go, 0);
+            if (!go) break;
+            // rows 4 lane .. 4 lane + 3 of both planes: 512 bytes each
+            tma_gather4(st + lane * 512, mh, full + s, kb * BG_BK, r0, r1, r2, r3);
+            tma_gather4(st + aBytes + lane * 512, ml, full + s, kb * BG_BK, r0, r1, r2, r3);
+        }
+    } else if (warp == 5) {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = umma_idesc(BG_M, p.ntile);
+            for (int kb = 0; kb < nkb; kb++) {
+                const int s = kb % p.stages;
+                const int round = kb / p.stages;
+                if (!mbar_wait(full + s, round & 1, kWaitBudget)) {
+                    atomicOr(p.flag, 4);
+                    *(volatile int*)abortFlag = 1;
+                    break;
+                }
+                if (*(volatile int*)abortFlag) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                uint8_t* st = smem + s * stageBytes;
+                const uint32_t ah = smem_u32(st), al = smem_u32(st + aBytes);
+                const uint32_t bh = smem_u32(st + 2 * aBytes),
+                               bl = smem_u32(st + 2 * aBytes + bBytes);
+#pragma unroll
+                for (int kk = 0; kk < BG_BK / 16; kk++) {
+                    const uint32_t off = kk * 32;
+                    umma_bf16(tmem, umma_desc(ah + off), umma_desc(bh + off), idesc,
+                              (kb | kk) != 0);
+                    umma_bf16(tmem, umma_desc(ah + off), umma_desc(bl + off), idesc, 1);
+                    umma_bf16(tmem, umma_desc(al + off), umma_desc(bh + off), idesc, 1);
+                }
+                umma_commit(empty + s);
+                issuedMma = kb + 1;
+            }
+            umma_commit(accum);
+        }
+    } else {
+        // ---------------- norm of row t = threadIdx.x, stage by stage
+        const int t = threadIdx.x;
+        const float* sg = p.sigRcp + (size_t)item * p.K;
+        const float* cf = p.ctf + (size_t)item * p.K;
+        for (int kb = 0; kb < nkb; kb++) {
+            const int s = kb % p.stages;
+            const int round = kb / p.stages;
+            if (!mbar_wait(full + s, round & 1, kWaitBudget)) {
+                atomicOr(p.flag, 4);
+                *(volatile int*)abortFlag = 1;
+                break;
+            }
+            const uint8_t* st = smem + s * stageBytes;
+            const uint8_t* rh = st + t * 128;
+            const uint8_t* rl = st + aBytes + t * 128;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                // logical 16-byte chunk j of the row sits at chunk j ^ (row % 8)
+                const int ph = ((j ^ (t & 7)) << 4);
+                const uint4 h = *reinterpret_cast<const uint4*>(rh + ph);
+                const uint4 lo = *reinterpret_cast<const uint4*>(rl + ph);
+                const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {lo.x, lo.y, lo.z, lo.w};
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int px = kb * (BG_BK / 2) + j * 4 + q;
+                    if (px < p.K) {
+                        const float2 hf = __bfloat1622float2(
+                            *reinterpret_cast<const __nv_bfloat162*>(&hw[q]));
+                        const float2 lf = __bfloat1622float2(
+                            *reinterpret_cast<const __nv_bfloat162*>(&lw[q]));
+                        const float re = hf.x + lf.x, im = hf.y + lf.y;
+                        const float c = __ldg(cf + px);
+                        kahan_add(nrmS, nrmC, __ldg(sg + px) * c * c * (re * re + im * im));
+                    }
+                }
+            }
+            // generic reads of this stage done before the producer's next
+            // asynchronous copy into it
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(empty + s);
+        }
+    }
+    __syncthreads();
+    // ---------------- epilogue (warps 0 - 3)
+    bool ok = *(volatile int*)abortFlag == 0;
+    if (warp < 4) ok = ok && mbar_wait(accum, 0, kWaitBudget);
+    ok = __syncthreads_and(ok) != 0;
+    if (!ok && threadIdx.x == 0) {
+        atomicOr(p.flag, 4);
+        *(volatile int*)abortFlag = 1;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool aborted = !ok;
+    if (!aborted && warp < 4) {
+        const int pitch = p.ntile + 1;
+        float* stage = reinterpret_cast<float*>(smem) + (size_t)warp * 32 * pitch;
+        const int rowBase = mtile * BG_M + warp * 32;
+        const float add = nrmS - nrmC;
+        for (int c0 = 0; c0 < p.ntile; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; i++) stage[lane * pitch + c0 + i] = fmaf(p.alpha, v[i], add);
+        }
+        __syncwarp();
+        float* cbase = p.C + (size_t)item * p.nR * p.nT;
+        for (int rr = 0; rr < 32; rr++) {
+            const int r = rowBase + rr;
+            if (r >= p.nR) break;
+            for (int j = lane; j < p.nT; j += 32) cbase[(size_t)r * p.nT + j] = stage[rr * pitch + j];
+        }
+    }
+    // on an abort, the copies and MMAs this CTA issued are waited for (bounded)
+    if (aborted && warp == 4 && lane == 0) {
+        for (int kb = 0; kb < issuedTma; kb++) {
+            const int s = kb % p.stages;
+            mbar_wait(full + s, (kb / p.stages) & 1, kWaitBudget / 4);
+        }
+    }
+    if (aborted && warp == 5 && lane == 0 && issuedMma > 0) mbar_wait(accum, 0, kWaitBudget / 4);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 5) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(p.tmemCols)
+                     : "memory");
+    }
+}
+
+}  // namespace
+
+// A: the classes' banks (bank[k].hi holds the hi plane, then the lo plane
+// nB Kd elements later); B: the shifted data, hi plane [nP nT][Kd] then the
+// lo plane.  C [nP][nR][nT] = alpha (split product) + the rows' norms.
+cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const int* idx,
+                                    const int* cls, int nP, int nR, const void* B, int nT,
+                                    int Kd, int K, const float* sigRcp, const float* ctf,
+                                    float* C, float alpha, int* flag, cudaStream_t st)
+{
+    if (nP <= 0 || nR <= 0 || nT <= 0 || nT > 256 || Kd <= 0 || Kd % BG_BK || nP > 65535)
+        return cudaErrorInvalidValue;
+    BankMaps maps;
+    int first = -1;
+    for (int k = 0; k < kMaxClasses; k++) {
+        const Bank& b = banks[k];
+        const bool ok = b.nB > 0 && b.gen == pixGen && b.Kp == Kd;
+        maps.nB[k] = ok ? b.nB : 0;
+        if (ok && first < 0) first = k;
+    }
+    if (first < 0) return cudaErrorInvalidValue;
+    for (int k = 0; k < kMaxClasses; k++) {
+        const Bank& b = banks[maps.nB[k] ? k : first];
+        const __nv_bfloat16* hi = b.hi;
+        const __nv_bfloat16* lo = b.hi + (size_t)b.nB * b.Kp;
+        // one-row boxes: the rows of a tile are gathered four at a time
+        if (!tc::make_map(&maps.hi[k], hi, b.nB, Kd, 1) || !tc::make_map(&maps.lo[k], lo, b.nB, Kd, 1))
+            return cudaErrorInvalidValue;
+    }
+    BgParams p;
+    p.nR = nR;
+    p.nT = nT;
+    p.Kd = Kd;
+    p.K = K;
+    p.ntile = (nT + 15) / 16 * 16;
+    p.tmemCols = 32;
+    while (p.tmemCols < p.ntile) p.tmemCols <<= 1;
+    const int stageBytes = 2 * BG_M * BG_BK * 2 + 2 * p.ntile * BG_BK * 2;
+    p.stages = (200 * 1024) / stageBytes;
+    if (p.stages > 4) p.stages = 4;
+    if (p.stages < 2) return cudaErrorInvalidValue;
+    if ((size_t)BG_M * (p.ntile + 1) * 4 > (size_t)p.stages * stageBytes)
+        return cudaErrorInvalidValue;
+    p.idx = idx;
+    p.cls = cls;
+    p.sigRcp = sigRcp;
+    p.ctf = ctf;
+    p.C = C;
+    p.alpha = alpha;
+    p.flag = flag;
+    const __nv_bfloat16* Bh = reinterpret_cast<const __nv_bfloat16*>(B);
+    const __nv_bfloat16* Bl = Bh + (size_t)nP * nT * Kd;
+    CUtensorMap mBh, mBl;
+    if (!tc::make_map(&mBh, Bh, (long long)nP * nT, Kd, p.ntile) ||
+        !tc::make_map(&mBl, Bl, (long long)nP * nT, Kd, p.ntile))
+        return cudaErrorInvalidValue;
+    // stages, then barriers (2 stages + 1, 8 bytes each), the TMEM slot, the
+    // abort word and the tile's row list
+    const size_t smem = 1024 + (size_t)p.stages * stageBytes + 256 + sizeof(int) * BG_M;
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_bank_bf16x3,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((nR + BG_M - 1) / BG_M, nP);
+    k_gemm_bank_bf16x3<<<grid, BG_THREADS, smem, st>>>(maps, mBh, mBl, p);
+    return cudaGetLastError();
+}
+
+}  // namespace tg3

@@ -659,11 +659,17 @@ __device__ __forceinline__ unsigned block_scan256(unsigned v, unsigned* ws, unsi
 // passes over order-preserving keys in shared memory; the keys above it and
 // the lowest-index keys equal to it are compacted in index order, then
 // sorted (bitonic, nSort = nRot rounded up to a power of two).
+//
+// With table != null, particle l matches the references of its class:
+// table[cls[l]] (embeddings, rotations, count) replaces ref / refQuat /
+// nRef.  A class without nRot references gets index -1 proposals, which
+// the rescoring gather reports as out of range.
 __global__ void __launch_bounds__(256)
 k_match_propose(const float* __restrict__ out, const float* __restrict__ ref, int nRef,
                 int nSort, const double* __restrict__ refQuat, int nRot, int nTrans,
                 uint64_t seed, double* __restrict__ quat, double* __restrict__ trans,
-                int* __restrict__ idxOut)
+                int* __restrict__ idxOut, const RefView* __restrict__ table,
+                const int* __restrict__ cls)
 {
     extern __shared__ unsigned long long smx[];
     unsigned long long* sel = smx;                                   // [nSort]
@@ -675,6 +681,23 @@ k_match_propose(const float* __restrict__ out, const float* __restrict__ ref, in
     __shared__ unsigned sPrefix, sMask, sK;
     const int l = blockIdx.x, tid = threadIdx.x;
     const float* o = out + (size_t)l * kOut;
+    if (table) {
+        const int k = cls[l];
+        const RefView v = (k >= 0 && k < kMaxClasses) ? table[k] : RefView{nullptr, nullptr, 0};
+        if (!v.emb || !v.quat || v.n < nRot) {
+            for (int j = tid; j < nRot; j += blockDim.x) {
+                if (idxOut) idxOut[(size_t)l * nRot + j] = -1;
+                double* qo = quat + ((size_t)l * nRot + j) * 4;
+                qo[0] = 1.0;
+                qo[1] = qo[2] = qo[3] = 0.0;
+            }
+            propose_trans(o, l, nTrans, seed, trans);
+            return;
+        }
+        ref = v.emb;
+        refQuat = v.quat;
+        nRef = v.n;
+    }
     if (tid < kEmb) {
         const float a = o[tid];
         float q = a * a;
@@ -1204,9 +1227,30 @@ extern "C" int tg3_cnn_match_propose(const float* out, int n, const float* ref, 
     TG3_CUDA(cudaFuncSetAttribute(k_match_propose, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
     k_match_propose<<<n, 256, smem, static_cast<cudaStream_t>(stream)>>>(
-        out, ref, nRef, p2, refQuat, nRot, nTrans, seed, quat, trans, idx);
+        out, ref, nRef, p2, refQuat, nRot, nTrans, seed, quat, trans, idx, nullptr, nullptr);
     TG3_LAUNCH_CHECK("match proposals");
     return TG3_OK;
+}
+
+// Every particle against the references of its own class (RefView table).
+cudaError_t tg3::launch_match_propose_classes(const float* out, int n, const RefView* table,
+                                              const int* cls, int maxRef, int nRot, int nTrans,
+                                              unsigned long long seed, double* quat,
+                                              double* trans, int* idx, cudaStream_t st)
+{
+    if (!out || !table || !cls || !quat || !trans || n <= 0 || maxRef <= 0 || maxRef > 16384 ||
+        nRot <= 0 || nRot > maxRef || nTrans <= 0 || nTrans > 512)
+        return cudaErrorInvalidValue;
+    int p2 = 1;
+    while (p2 < nRot) p2 <<= 1;
+    const size_t smem = sizeof(unsigned long long) * p2 + sizeof(uint32_t) * (size_t)maxRef;
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_match_propose,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_match_propose<<<n, 256, smem, st>>>(out, nullptr, maxRef, p2, nullptr, nRot, nTrans, seed,
+                                          quat, trans, idx, table, cls);
+    return cudaGetLastError();
 }
 
 namespace tg3 {

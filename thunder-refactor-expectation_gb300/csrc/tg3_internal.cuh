@@ -87,6 +87,8 @@ enum WsSlot {
     WS_CLASSES,      // multi-class 2-D scan: per-(image, class) weights
     WS_PREP,         // image preprocessing: statistics, real and transformed images
     WS_RECO,         // reconstruction: T, W, C and the real-space map on the padded grid
+    WS_LEARN,        // learned E-step: network outputs, proposals, their weights, fallback lists
+    WS_LEARN_IO,     // learned E-step, host-buffer form: staged inputs and outputs
     WS_COUNT
 };
 
@@ -125,9 +127,21 @@ struct Bank {
     float* f32 = nullptr;
     __nv_bfloat16* hi = nullptr;
     float* abs2 = nullptr;
+    double* quat = nullptr;   // the bank's rotations [nB][4]
     int nB = 0, K = 0, Kp = 0;
     unsigned gen = 0;
     size_t bytes = 0;
+    // the pose network's embeddings of the clean references at the bank's
+    // rotations [nEmb][64], normalised (tg3_ctx_set_references)
+    float* emb = nullptr;
+    int nEmb = 0;
+};
+// The device view of one class's references: embeddings [n][64] and their
+// rotations [n][4] (the bank's), for the matching proposals.
+struct RefView {
+    const float* emb;
+    const double* quat;
+    int n;
 };
 // The device view the gather reads, one per class.
 struct BankView {
@@ -161,14 +175,17 @@ struct tg3_ctx {
     tg3::InsertAcc ins;
     tg3::Bank bank[tg3::kMaxClasses];        // tg3_ctx_set_bank
     tg3::BankView* d_bankTable = nullptr;    // device copy of the views
+    tg3::RefView* d_refTable = nullptr;      // device copy of the reference views
     unsigned pixGen = 0;                     // pixel uploads so far
     tg3::Buffer ws[tg3::WS_COUNT];
     int* d_flag = nullptr;           // device error word
     // tg3_ctx_set_option
     bool fused = false;
     bool insertGather = false;    // TG3_OPT_INSERT_GATHER
+    bool bankGather = true;       // TG3_OPT_BANK_GATHER
     // per-stage event timing (tg3_ctx_set_timing)
     bool timing = false;
+    bool stageMute = false;       // inner stages not recorded (a bracketing stage is)
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[TG3_STAGE_COUNT];
     std::vector<cudaEvent_t> eventPool;
     double stageMs[TG3_STAGE_COUNT] = {};
@@ -193,6 +210,21 @@ struct tg3_volume {
 namespace tg3 {
 
 void* ws_get(tg3_ctx* c, WsSlot s, size_t bytes, int* status);
+
+// Bump allocator over one workspace slot (the arrays of one call): add()
+// returns 256-byte aligned offsets; ws_get(c, slot, used) then holds them all.
+struct Arena {
+    tg3_ctx* c;
+    WsSlot slot;
+    size_t used = 0;
+    Arena(tg3_ctx* c_, WsSlot s) : c(c_), slot(s) {}
+    size_t add(size_t bytes)
+    {
+        size_t off = round_up(used, 256);
+        used = off + bytes;
+        return off;
+    }
+};
 
 // ---------------------------------------------------------- kernel calls --
 // All launchers return cudaError_t of the launch (no synchronisation).
@@ -297,7 +329,8 @@ cudaError_t launch_insert(float4* acc, int vdim, int kernel, const float* tab,
                           const double* trans, const double* offset,
                           const float* w, const int* iCol, const int* iRow,
                           int K, int pf, int idim, double* O3D, int* counter,
-                          float* params, cudaStream_t st, int ctfRows = 0);
+                          float* params, cudaStream_t st, int ctfRows = 0,
+                          const int* nC = nullptr);
 // MKB insertion by gather: per chunk of draws, k_insert_stage (tiles x
 // draws) fills the draws' dense pixel grids from the cell map cellPix,
 // k_insert_gather (tiles x draws) adds each slab voxel once.  scratch holds
@@ -405,6 +438,14 @@ cudaError_t launch_rot_f32(const double* quat, const double* mat, int rows, floa
                            cudaStream_t st);
 
 bool bf16x3_available();
+// The bank-row cross term (tg3_bank_gemm.cu): C [nP][nR][nT] = alpha x the
+// split product of the rows idx [nP][nR] of the particles' class banks with
+// the shifted data B (hi plane [nP nT][Kd], then the lo plane), plus the
+// rows' norms sum_p sigRcp ctf^2 |P|^2 (compensated FP32).
+cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const int* idx,
+                                    const int* cls, int nP, int nR, const void* B, int nT,
+                                    int Kd, int K, const float* sigRcp, const float* ctf,
+                                    float* C, float alpha, int* flag, cudaStream_t st);
 cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda,
                                   const float* B, long long sB, int ldb,
                                   int M, int N, int Kd, int batch, float* C,
@@ -431,4 +472,21 @@ int check_geometry(tg3_ctx* c, int vdim, int pf, double margin = 1.0);
 // releases the context's preprocessing and reconstruction FFT plans
 void prep_release(tg3_ctx* c);
 void reco_release(tg3_ctx* c);
+// The global scan of nImg images against class `cls`'s projection bank (its
+// nB rotations, already projected on the active pixel set) x nT
+// translations; outputs as tg3_global_scan_d with nR = nB.
+int global_scan_bank(tg3_ctx* c, int cls, int nImg, int nT, const float* dat, const float* ctf,
+                     const float* sigRcp, const double* trans, const double* pR,
+                     const double* pT, double* wC, double* wR, double* wT, double* baseL,
+                     float* dvp, int precision);
+// Uploads the device views of the banks (BankView) and of the references
+// (RefView); anyBank / anyRef report whether any class has one on the
+// active pixel set.
+int upload_bank_views(tg3_ctx* c, bool* anyBank, bool* anyRef);
+// Matching proposals (tg3_cnn.cu): particle l matches the references of its
+// class cls[l] (table[cls[l]]); maxRef bounds every class's reference count.
+cudaError_t launch_match_propose_classes(const float* out, int n, const RefView* table,
+                                         const int* cls, int maxRef, int nRot, int nTrans,
+                                         unsigned long long seed, double* quat, double* trans,
+                                         int* idx, cudaStream_t st);
 }  // namespace tg3

@@ -1211,16 +1211,25 @@ __device__ __forceinline__ void red_voxel(float4* acc, int vdim, int nx, int i, 
 // image weight, 16 floats per draw; and the bookkeeping: O3D -= R (t -
 // offset, 0) (insertDir, src/Optimiser.cpp:7180-7186), summed per block
 // before one atomic per component, and the draw counter.
+// With nC (the multi-class InsertFT), draw m of image l is inserted only
+// when m < nC[l] (kernel_getRandomR / kernel_InsertF, gpu/src/Kernel.cu:
+// 1847-1899, 2552-2600): a skipped draw gets weight 0, which k_insert
+// skips, and adds nothing to O3D or the counter.
 __global__ void __launch_bounds__(256)
 k_insert_draws(int nDraws, int drawsPerImage, const double* __restrict__ quat,
                const double* __restrict__ trans, const double* __restrict__ offset,
                const float* __restrict__ wgt, float* __restrict__ params,
-               double* __restrict__ O3D, int* __restrict__ counter)
+               double* __restrict__ O3D, int* __restrict__ counter, const int* __restrict__ nC)
 {
     __shared__ double part[3][8];
     const int d = blockIdx.x * blockDim.x + threadIdx.x;
     double o[3] = {0.0, 0.0, 0.0};
-    if (d < nDraws) {
+    const bool active = d < nDraws && (!nC || d % drawsPerImage < nC[d / drawsPerImage]);
+    if (d < nDraws && !active) {
+        float* pd = params + 16 * (size_t)d;
+        for (int i = 0; i < 12; i++) pd[i] = 0.f;
+    }
+    if (active) {
         const int l = d / drawsPerImage;
         double q[4] = {quat[4 * (size_t)d], quat[4 * (size_t)d + 1], quat[4 * (size_t)d + 2],
                        quat[4 * (size_t)d + 3]};
@@ -1251,9 +1260,9 @@ k_insert_draws(int nDraws, int drawsPerImage, const double* __restrict__ quat,
             atomicAdd(O3D + threadIdx.x, v);
         }
     }
-    if (counter && threadIdx.x == 0) {
-        const int n = min((int)blockDim.x, nDraws - (int)(blockIdx.x * blockDim.x));
-        if (n > 0) atomicAdd(counter, n);
+    if (counter) {
+        const int n = __syncthreads_count(active);
+        if (threadIdx.x == 0 && n > 0) atomicAdd(counter, n);
     }
 }
 
@@ -1273,6 +1282,7 @@ k_insert(float4* __restrict__ acc, int vdim, int kernel, const float* __restrict
     for (int i = 0; i < 9; i++) m[i] = __ldg(pd + i);
     const int nx = vdim / 2 + 1, half = vdim / 2;
     const float tx = __ldg(pd + 9), ty = __ldg(pd + 10), w = __ldg(pd + 11);
+    if (w == 0.f) return;                     // a skipped draw (or one of weight 0)
     const float invN = 1.0f / (float)idim;
     const float fpf = (float)pf;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K; p += gridDim.x * blockDim.x) {
@@ -1956,14 +1966,14 @@ cudaError_t launch_insert(float4* acc, int vdim, int kernel, const float* tab, i
                           const float* ctf, const double* quat, const double* trans,
                           const double* offset, const float* w, const int* iCol,
                           const int* iRow, int K, int pf, int idim, double* O3D, int* counter,
-                          float* params, cudaStream_t st, int ctfRows)
+                          float* params, cudaStream_t st, int ctfRows, const int* nC)
 {
     if (nDraws <= 0) return cudaSuccess;
     // r^2 bound of the table's support: rint(r^2 n / b) <= tabNz  =>  r^2 < (tabNz + 1/2) b / n
     const float rs2 = (((float)tabNz + 0.5f) / tabInvStep) * (1.0f + 1e-4f);
     if (kernel == TG3_KERNEL_MKB && 2.0f * sqrtf(rs2) >= 4.0f) return cudaErrorInvalidValue;
     k_insert_draws<<<(nDraws + 255) / 256, 256, 0, st>>>(nDraws, drawsPerImage, quat, trans,
-                                                         offset, w, params, O3D, counter);
+                                                         offset, w, params, O3D, counter, nC);
     const int ctfPerDraw = ctfRows == nDraws && drawsPerImage > 1;
     // one pixel per thread: the draw's pixels spread over ceil(K / 256) CTAs
     const int tiles = std::max(1, std::min(1024, (K + 255) / 256));

@@ -4,9 +4,17 @@
  *
  * The signatures are those of gpu/interface/Interface.h (cited per function);
  * this file replaces the corresponding definitions of the reference's
- * gpu/interface/Interface.cpp.  Entry points outside this path (2-D
- * classification, PrepareTF and the reconstruction Expose* family, the
- * multi-class InsertFT) keep their reference definitions.
+ * gpu/interface/Interface.cpp.  Entry points outside this path (PrepareTF and
+ * the reconstruction Expose* family) keep their reference definitions.
+ *
+ * Insertion sums over the hemisphere's ranks inside the call, as the
+ * reference's does (ncclAllReduce of F and T over the ranks of `hemi`,
+ * gpu/src/cuthunder.cu:4956-5000): every rank inserts its own images on its
+ * GPU, then F and T are summed over `hemi` on the host with MPI.  O3D and
+ * the counter stay per rank (the reference sums them over the process's own
+ * GPUs only).  The kernel follows the reference's build switch:
+ * RECONSTRUCTOR_MKB_KERNEL (include/Config.h:95) selects the MKB kernel,
+ * otherwise the trilinear one of the reference's GPU insertion.
  *
  * Behaviour kept from the reference: functions return void and a failure
  * prints the library's message and exits the process (the reference's
@@ -44,6 +52,26 @@ std::mutex g_mu;
 inline void ok(const char* where, int status)
 {
     if (status != TG3_OK) die(where, status);
+}
+
+#ifdef RECONSTRUCTOR_MKB_KERNEL
+constexpr int kInsertKernel = TG3_KERNEL_MKB;
+#else
+constexpr int kInsertKernel = TG3_KERNEL_TRILINEAR;
+#endif
+
+// Sum n floats over the ranks of comm in place, in pieces whose counts fit
+// an int (MPI_Allreduce_Large does the same, include/Parallel.h:266).
+void allreduce_sum(float* buf, size_t n, MPI_Comm& comm, const char* where)
+{
+    const size_t piece = (size_t)1 << 30;
+    for (size_t o = 0; o < n; o += piece) {
+        const int cnt = (int)(n - o < piece ? n - o : piece);
+        if (MPI_Allreduce(MPI_IN_PLACE, buf + o, cnt, MPI_FLOAT, MPI_SUM, comm) != MPI_SUCCESS) {
+            std::fprintf(stderr, "%s: MPI_Allreduce over the hemisphere failed\n", where);
+            std::exit(1);
+        }
+    }
 }
 
 // ExpectPreidx: the pixel list, returned to the caller as opaque handles.
@@ -414,39 +442,79 @@ void InsertI2D(Complex* F2D, RFLOAT* T2D, double* O2D, int* counter, MPI_Comm& h
                const int* iCol, const int* iRow, RFLOAT pixelSize, bool cSearch, int nk, int opf,
                int npxl, int mReco, int idim, int vdim, int imgNum)
 {
-    (void)hemi;
     (void)slav;
     ok("InsertI2D",
        tg3_InsertI2D(reinterpret_cast<float*>(F2D), T2D, O2D, counter,
                      reinterpret_cast<const float*>(datP), ctfP, sigRcpP, w, offS, nC, nR, nT, nD,
                      reinterpret_cast<const float*>(ctfaData), iCol, iRow, pixelSize,
                      cSearch ? 1 : 0, nk, opf, npxl, mReco, idim, vdim, imgNum));
+    // the class accumulators summed over the hemisphere (gpu/src/cuthunder.cu:3913-4017)
+    const size_t n = (size_t)nk * vdim * (vdim / 2 + 1);
+    allreduce_sum(reinterpret_cast<float*>(F2D), 2 * n, hemi, "InsertI2D");
+    allreduce_sum(T2D, n, hemi, "InsertI2D");
 }
 
+namespace {
+
+// Both InsertFT forms: the library call on T as a real array (the
+// reference converts its complex T Volume the same way around the call),
+// then the sums over the hemisphere.
+void insert_ft(const char* where, Volume& F3D, Volume& T3D, double* O3D, int* counter,
+               MPI_Comm& hemi, Complex* datP, RFLOAT* ctfP, RFLOAT* sigRcpP,
+               CTFAttr* ctfaData, double* offS, RFLOAT* w, double* nR, double* nT, double* nD,
+               const int* nC, const int* iCol, const int* iRow, RFLOAT pixelSize, bool cSearch,
+               int opf, int npxl, int mReco, int idim, int imgNum)
+{
+    const size_t n = F3D.sizeFT();
+    std::vector<RFLOAT> T(n);
+    for (size_t i = 0; i < n; i++) T[i] = REAL(T3D[i]);
+    const int vdim = F3D.nSlcFT();
+    // CTFAttr (include/Database.h:108-122) is seven RFLOATs in the order the
+    // library reads
+    static_assert(sizeof(CTFAttr) == 7 * sizeof(RFLOAT), "CTFAttr layout");
+    const float* dat = reinterpret_cast<const float*>(datP);
+    const float* attr = reinterpret_cast<const float*>(ctfaData);
+    float* F = reinterpret_cast<float*>(&F3D[0]);
+    if (nC)
+        ok(where, tg3_InsertFT_classes(F, T.data(), O3D, counter, dat, ctfP, sigRcpP, attr, offS,
+                                       w, nR, nT, nD, nC, iCol, iRow, pixelSize, cSearch ? 1 : 0,
+                                       opf, npxl, mReco, idim, vdim, imgNum, kInsertKernel));
+    else
+        ok(where, tg3_InsertFT(F, T.data(), O3D, counter, dat, ctfP, sigRcpP, attr, offS, w, nR,
+                               nT, nD, iCol, iRow, pixelSize, cSearch ? 1 : 0, opf, npxl, mReco,
+                               idim, vdim, imgNum, kInsertKernel));
+    allreduce_sum(F, 2 * n, hemi, where);
+    allreduce_sum(T.data(), n, hemi, where);
+    for (size_t i = 0; i < n; i++) T3D[i] = COMPLEX(T[i], 0);
+}
+
+}  // namespace
+
 // gpu/interface/Interface.h:294-318 (single-class form).  F3D is complex and
-// T3D is a complex Volume whose real parts hold T (Interface.cpp of the
-// reference converts it the same way around the call).
+// T3D is a complex Volume whose real parts hold T.
 void InsertFT(Volume& F3D, Volume& T3D, double* O3D, int* counter, MPI_Comm& hemi,
               MPI_Comm& slav, Complex* datP, RFLOAT* ctfP, RFLOAT* sigRcpP,
               CTFAttr* ctfaData, double* offS, RFLOAT* w, double* nR, double* nT, double* nD,
               const int* iCol, const int* iRow, RFLOAT pixelSize, bool cSearch, int opf,
               int npxl, int mReco, int idim, int dimSize, int imgNum)
 {
-    (void)hemi;
     (void)slav;
-    const size_t n = F3D.sizeFT();
-    std::vector<RFLOAT> T(n);
-    for (size_t i = 0; i < n; i++) T[i] = REAL(T3D[i]);
-    const int vdim = F3D.nSlcFT();
     (void)dimSize;
-    // CTFAttr (include/Database.h:108-122) is seven RFLOATs in the order the
-    // library reads
-    static_assert(sizeof(CTFAttr) == 7 * sizeof(RFLOAT), "CTFAttr layout");
-    ok("InsertFT",
-       tg3_InsertFT(reinterpret_cast<float*>(&F3D[0]), T.data(), O3D, counter,
-                    reinterpret_cast<const float*>(datP), ctfP, sigRcpP,
-                    reinterpret_cast<const float*>(ctfaData), offS, w, nR, nT, nD, iCol, iRow,
-                    pixelSize, cSearch ? 1 : 0, opf, npxl, mReco, idim, vdim, imgNum,
-                    TG3_KERNEL_TRILINEAR));
-    for (size_t i = 0; i < n; i++) T3D[i] = COMPLEX(T[i], 0);
+    insert_ft("InsertFT", F3D, T3D, O3D, counter, hemi, datP, ctfP, sigRcpP, ctfaData, offS, w,
+              nR, nT, nD, nullptr, iCol, iRow, pixelSize, cSearch, opf, npxl, mReco, idim,
+              imgNum);
+}
+
+// gpu/interface/Interface.h:267-292 (multi-class form): the volume of one
+// class; nC [imgNum] counts the draws of each image that belong to it.
+void InsertFT(Volume& F3D, Volume& T3D, double* O3D, int* counter, MPI_Comm& hemi,
+              MPI_Comm& slav, Complex* datP, RFLOAT* ctfP, RFLOAT* sigRcpP,
+              CTFAttr* ctfaData, double* offS, RFLOAT* w, double* nR, double* nT, double* nD,
+              int* nC, const int* iCol, const int* iRow, RFLOAT pixelSize, bool cSearch,
+              int opf, int npxl, int mReco, int idim, int dimSize, int imgNum)
+{
+    (void)slav;
+    (void)dimSize;
+    insert_ft("InsertFT", F3D, T3D, O3D, counter, hemi, datP, ctfP, sigRcpP, ctfaData, offS, w,
+              nR, nT, nD, nC, iCol, iRow, pixelSize, cSearch, opf, npxl, mReco, idim, imgNum);
 }

@@ -41,16 +41,27 @@ EXPORTS = [
     "tg3_mrc_info", "tg3_mrc_read", "tg3_mrc_write", "tg3_thu_count",
     "tg3_thu_read", "tg3_thu_write",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
+    "tg3_ctx_set_references", "tg3_learned_expect_d", "tg3_ExpectLearned3D",
+    "tg3_InsertFT_classes",
 ]
-STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused")
+STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused", "network",
+          "fallback")
 OPT_FUSED = 0
 OPT_INSERT_GATHER = 1
+OPT_BANK_GATHER = 2
 
 
 class TG3Error(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"tg3 status {status}: {msg}")
         self.status = status
+
+
+class LearnedOut(ctypes.Structure):
+    """tg3_learned_out: device pointers of the learned E-step's outputs."""
+    _fields_ = [(k, ctypes.c_void_p) for k in (
+        "bestQuat", "bestTrans", "baseL", "peak", "fellBack", "propIdx", "propQuat",
+        "propTrans", "propWR", "propWT", "propBase", "propDvp")]
 
 
 _lib = None
@@ -77,6 +88,7 @@ def lib():
             "tg3_ExpectProject": ([_P, _P, _P, _P, _P, _I, _I, _I, _I, _I], _I),
             "tg3_ExpectGlobal3D": ([_P] * 11 + [_I] * 6, _I),
             "tg3_InsertFT": ([_P] * 15 + [_F, _I, _I, _I, _I, _I, _I, _I, _I], _I),
+            "tg3_InsertFT_classes": ([_P] * 16 + [_F, _I, _I, _I, _I, _I, _I, _I, _I], _I),
             "tg3_volume_create": ([_P, _P, _I, _I], _I),
             "tg3_volume_destroy": ([_P], _I),
             "tg3_ExpectLocal3D": ([_P, _P, _P, _P, _P, _P, _I, _I, _P, _I, _P, _I, _P, _P, _D,
@@ -151,6 +163,12 @@ def lib():
             "tg3_global_scan_d": ([_P, _I, _I, _I, _I] + [_P] * 12 + [_I], _I),
             "tg3_local_phase_noalloc": ([_P, _I, _I, _P, _P, _I, _I, _P, _P, _P, _P, _I, _P, _I,
                                          _P, _P, _P, _P, _P, _P, _P, _P, _P], _I),
+            "tg3_ctx_set_references": ([_P, _I, _P, _I], _I),
+            "tg3_learned_expect_d": ([_P, _P, _I, _P, _P, _P, _P, _P, _I, _I,
+                                      ctypes.c_ulonglong, _P, _I, _F, _I,
+                                      ctypes.POINTER(LearnedOut)], _I),
+            "tg3_ExpectLearned3D": ([_P, _P, _I, _P, _P, _P, _P, _P, _I, _I, ctypes.c_ulonglong,
+                                     _P, _I, _F, _I, _P, _P, _P, _P, _P], _I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -276,6 +294,34 @@ class Context:
                                            ptr(bank_idx), ptr(trans), ptr(pwR), ptr(pwT),
                                            ptr(pwC), ptr(cls), ptr(wC), ptr(wR), ptr(wT),
                                            ptr(base), ptr(dvp), precision))
+
+    def set_references(self, cls: int, emb):
+        """The network's normalised embeddings emb [nB][64] (device float32) of
+        clean references at the rotations of class `cls`'s bank."""
+        check(lib().tg3_ctx_set_references(self.h, cls, ptr(emb), emb.shape[0]))
+
+    def learned_expect(self, net, images, dat, ctf, sig, cls, n_rot, n_trans, seed, g_trans,
+                       peak_min, precision, out: dict):
+        """The learned E-step (tg3_learned_expect_d) on device tensors; `out`
+        maps LearnedOut field names to device tensors (bestQuat, bestTrans and
+        baseL required).  Returns after the work has finished."""
+        o = LearnedOut(**{k: ptr(v) for k, v in out.items() if v is not None})
+        check(lib().tg3_learned_expect_d(self.h, net.h, images.shape[0], ptr(images), ptr(dat),
+                                         ptr(ctf), ptr(sig), ptr(cls), n_rot, n_trans, seed,
+                                         ptr(g_trans), g_trans.shape[0], float(peak_min),
+                                         precision, ctypes.byref(o)))
+        self._keep = []
+
+    def learned_expect_host(self, net, images, dat, ctf, sig, cls, n_rot, n_trans, seed,
+                            g_trans, peak_min, precision, best_quat, best_trans, base,
+                            peak=None, fell_back=None):
+        """tg3_ExpectLearned3D: the same with host arrays or tensors (inputs
+        copied in, outputs copied out inside the call)."""
+        check(lib().tg3_ExpectLearned3D(self.h, net.h, images.shape[0], ptr(images), ptr(dat),
+                                        ptr(ctf), ptr(sig), ptr(cls), n_rot, n_trans, seed,
+                                        ptr(g_trans), g_trans.shape[0], float(peak_min),
+                                        precision, ptr(best_quat), ptr(best_trans), ptr(base),
+                                        ptr(peak), ptr(fell_back)))
 
     def local_phase_host(self, nP, nR, nT, dat, ctf, sig, quat, trans, pwR, pwT, pwC, cls,
                          wC, wR, wT, base, dvp=None, precision=SCORE_FP32):

@@ -226,3 +226,106 @@ def train_match(net, images, refs, tstar, cls, epochs: int, batch: int, lr: floa
         if log:
             log(f"epoch {e}: loss {losses[-1]:.4f}")
     return losses
+
+
+# --------------------------------------------------------------------------
+# The plain method's converged poses (training labels and the judge of the
+# proposals): the global search, then local particle-filter phases that
+# narrow around the current best pose.
+# --------------------------------------------------------------------------
+# (concentration of the rotations' vMF, deviation of the translations in
+# pixels) of the local phases after the global search: the particle
+# filter's narrowing as the poses converge
+CONVERGE_SCHEDULE = ((200.0, 2.0), (1000.0, 0.7), (5000.0, 0.3))
+
+
+def global_best(ctx, ps, quats_g, mats_g, trans_g, precision, batch: int = 2048):
+    """Best rotation (quaternion) and translation of every particle of ps
+    (a synth.ParticleSetDev; the context holds every class's volume and the
+    likelihood's pixel set) by the global search over quats_g x trans_g with
+    uniform priors: argmax of the rotation and translation marginals.
+    Returns float64 device tensors [n][4], [n][2] and the best
+    log-likelihoods [n]."""
+    import torch
+    dev = ps.dat.device
+    n = len(ps.cls)
+    nRg, nTg = len(quats_g), int(trans_g.shape[0])
+    f64 = dict(dtype=torch.float64, device=dev)
+    qg = torch.as_tensor(quats_g, **f64)
+    pR = torch.full((nRg,), 1.0 / nRg, **f64)
+    pT = torch.full((nTg,), 1.0 / nTg, **f64)
+    q_best = torch.empty((n, 4), **f64)
+    t_best = torch.empty((n, 2), **f64)
+    base = torch.empty(n, **f64)
+    for c in np.unique(ps.cls):
+        sel = np.nonzero(ps.cls == c)[0]
+        for s in range(0, len(sel), batch):
+            idx = torch.as_tensor(sel[s:s + batch], device=dev)
+            m = len(idx)
+            wC = torch.empty(m, **f64)
+            wR = torch.empty((m, nRg), **f64)
+            wT = torch.empty((m, nTg), **f64)
+            b = torch.empty(m, **f64)
+            ctx.global_scan(int(c), m, nRg, nTg, ps.dat[idx].contiguous(),
+                            ps.ctf[idx].contiguous(), ps.sigRcp[idx].contiguous(), mats_g,
+                            trans_g, pR, pT, wC, wR, wT, b, None, precision)
+            ctx.sync()
+            q_best[idx] = qg[wR.argmax(1)]
+            t_best[idx] = trans_g[wT.argmax(1)]
+            base[idx] = b
+    return q_best, t_best, base
+
+
+def local_refine(ctx, ps, q_c, t_c, kappa, trans_sd, precision, gen, nR: int = 1000,
+                 nT: int = 100, batch: int = 256, sel=None):
+    """One local phase about the poses q_c [n][4], t_c [n][2] (device float64):
+    nR vMF rotations (concentration kappa) x nT Gaussian translations
+    (deviation trans_sd) per particle, scored with uniform priors; the best
+    rotation and translation (argmax of the marginals) and the best
+    log-likelihood.  `sel` (optional index array) restricts it to those
+    particles of ps (q_c, t_c then have one row per selected particle)."""
+    import torch
+    dev = ps.dat.device
+    rows = np.arange(len(ps.cls)) if sel is None else np.asarray(sel)
+    n = len(rows)
+    f64 = dict(dtype=torch.float64, device=dev)
+    q_new = torch.empty((n, 4), **f64)
+    t_new = torch.empty((n, 2), **f64)
+    base = torch.empty(n, **f64)
+    cls_all = torch.as_tensor(ps.cls.astype(np.int32), device=dev)
+    for s in range(0, n, batch):
+        e = min(n, s + batch)
+        m = e - s
+        idx = torch.as_tensor(rows[s:e], device=dev)
+        qs, ts = synth.local_hypotheses_dev(gen, q_c[s:e], t_c[s:e], nR, nT, kappa, trans_sd)
+        pwR = torch.full((m, nR), 1.0 / nR, **f64)
+        pwT = torch.full((m, nT), 1.0 / nT, **f64)
+        pwC = torch.ones(m, **f64)
+        wC = torch.empty(m, **f64)
+        wR = torch.empty((m, nR), **f64)
+        wT = torch.empty((m, nT), **f64)
+        b = torch.empty(m, **f64)
+        ctx.local_phase(m, nR, nT, ps.dat[idx].contiguous(), ps.ctf[idx].contiguous(),
+                        ps.sigRcp[idx].contiguous(), qs.contiguous(), ts.contiguous(), pwR, pwT,
+                        pwC, cls_all[idx].contiguous(), wC, wR, wT, b, None, precision)
+        ctx.sync()
+        ar = torch.arange(m, device=dev)
+        q_new[s:e] = qs[ar, wR.argmax(1)]
+        t_new[s:e] = ts[ar, wT.argmax(1)]
+        base[s:e] = b
+    return q_new, t_new, base
+
+
+def plain_method_poses(ctx, ps, quats_g, mats_g, trans_g, precision, gen,
+                       schedule=CONVERGE_SCHEDULE):
+    """The plain method run to convergence on ps: the global search, then
+    one local phase per (kappa, trans_sd) of `schedule`, each about the
+    previous phase's best pose.  Returns host arrays quat [n][4], trans
+    [n][2] and the median rotation change (degrees) of every local phase."""
+    q, t, _ = global_best(ctx, ps, quats_g, mats_g, trans_g, precision)
+    moves = []
+    for kappa, tsd in schedule:
+        qn, tn, _ = local_refine(ctx, ps, q, t, kappa, tsd, precision, gen)
+        moves.append(float(np.median(angle_deg(qn.cpu().numpy(), q.cpu().numpy()))))
+        q, t = qn, tn
+    return q.cpu().numpy(), t.cpu().numpy(), moves

@@ -608,3 +608,163 @@ def config_rL(box: int, pixel_size: float, ignore_res: float = 200.0) -> float:
     rL = floor(resA2P(1 / ignoreRes, size, pixelSize)) (src/Optimiser.cpp:243,
     resA2P src/Functions/Spectrum.cpp:26-31); ignoreRes 200 Angstrom."""
     return float(math.floor(box * pixel_size / ignore_res))
+
+
+# --------------------------------------------------------------------------
+# device-side generators (large particle sets: training sets at box 256)
+# --------------------------------------------------------------------------
+def quat_mul_t(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """Hamilton product of quaternion tensors (..., 4)."""
+    aw, ax, ay, az = a.unbind(-1)
+    bw, bx, by, bz = b.unbind(-1)
+    return torch.stack([aw * bw - ax * bx - ay * by - az * bz,
+                        aw * bx + ax * bw + ay * bz - az * by,
+                        aw * by - ax * bz + ay * bw + az * bx,
+                        aw * bz + ax * by - ay * bx + az * bw], dim=-1)
+
+
+def vmf_quaternions_dev(gen: torch.Generator, means: torch.Tensor, kappa: float,
+                        n: int) -> torch.Tensor:
+    """n von Mises-Fisher samples about each of means [m][4] (float64,
+    device) with concentration kappa: [m][n][4] float64.  Wood's (1994)
+    rejection sampler, as vmf_quaternions; its Beta((p-1)/2, (p-1)/2) proposal
+    for p = 4 is drawn as (1 + g0 / |g|) / 2 with g a standard 4-D Gaussian
+    (the first coordinate of a uniform point of S^3), and the samples are
+    drawn with the device generator `gen`."""
+    dev = means.device
+    m = means.shape[0]
+    p = 4
+    b = (-2 * kappa + math.sqrt(4 * kappa * kappa + (p - 1) ** 2)) / (p - 1)
+    x0 = (1 - b) / (1 + b)
+    c = kappa * x0 + (p - 1) * math.log(1 - x0 * x0)
+    total = m * n
+    w = torch.empty(total, dtype=torch.float64, device=dev)
+    filled = 0
+    while filled < total:
+        k = int((total - filled) * 1.3) + 64
+        g = torch.randn((k, 4), generator=gen, dtype=torch.float64, device=dev)
+        z = 0.5 * (1.0 + g[:, 0] / g.norm(dim=1))
+        u = torch.rand(k, generator=gen, dtype=torch.float64, device=dev)
+        ww = (1 - (1 + b) * z) / (1 - (1 - b) * z)
+        ok = kappa * ww + (p - 1) * torch.log(1 - x0 * ww) - c >= torch.log(u)
+        take = ww[ok][: total - filled]
+        w[filled:filled + take.numel()] = take
+        filled += take.numel()
+    v = torch.randn((total, 3), generator=gen, dtype=torch.float64, device=dev)
+    v = v / v.norm(dim=1, keepdim=True)
+    samp = torch.cat([w[:, None], torch.sqrt(torch.clamp(1 - w * w, min=0.0))[:, None] * v], 1)
+    out = quat_mul_t(means.to(torch.float64).repeat_interleave(n, 0), samp)
+    out = out / out.norm(dim=1, keepdim=True)
+    return out.view(m, n, 4)
+
+
+def local_hypotheses_dev(gen: torch.Generator, q_centre: torch.Tensor, t_centre: torch.Tensor,
+                         nR: int, nT: int, kappa: float, trans_sd: float):
+    """local_hypotheses on the device: nR vMF rotations about each q_centre
+    [m][4] and nT Gaussian translations (deviation trans_sd) about each
+    t_centre [m][2]; float64 tensors [m][nR][4] and [m][nT][2]."""
+    qs = vmf_quaternions_dev(gen, q_centre, kappa, nR)
+    ts = t_centre.to(torch.float64)[:, None, :] + trans_sd * torch.randn(
+        (q_centre.shape[0], nT, 2), generator=gen, dtype=torch.float64, device=q_centre.device)
+    return qs, ts
+
+
+def ctf_values_t(attr: torch.Tensor, pixel_size: float, N: int, iCol: torch.Tensor,
+                 iRow: torch.Tensor) -> torch.Tensor:
+    """ctf_values on tensors (float64): attr [n][7], pixels iCol / iRow [K]."""
+    V, dU, dV, th, Cs, A, ps = [attr[:, k:k + 1] for k in range(7)]
+    lam = 12.2643247 / torch.sqrt(V * (1 + V * 0.978466e-6))
+    K1 = math.pi * lam
+    K2 = (math.pi / 2) * Cs * lam ** 3
+    fc = iCol.to(torch.float64) / (pixel_size * N)
+    fr = iRow.to(torch.float64) / (pixel_size * N)
+    u = torch.hypot(fc, fr)[None, :]
+    ang = torch.atan2(iRow.to(torch.float64), iCol.to(torch.float64))[None, :] - th
+    dfc = -(dU + dV + (dU - dV) * torch.cos(2 * ang)) / 2
+    ki = K1 * dfc * u ** 2 + K2 * u ** 4 - ps
+    return -torch.sqrt(1 - A * A) * torch.sin(ki) + A * torch.cos(ki)
+
+
+@dataclass
+class ParticleSetDev:
+    images: torch.Tensor       # (n, img, img) float32, per-image normalised
+    dat: torch.Tensor          # (n, K) complex64 at the likelihood's pixels
+    ctf: torch.Tensor          # (n, K) float32
+    sigRcp: torch.Tensor       # (n, K) float32
+    iCol: np.ndarray
+    iRow: np.ndarray
+    quat_true: np.ndarray      # (n, 4)
+    trans_true: np.ndarray     # (n, 2)
+    cls: np.ndarray            # (n,)
+
+
+def particle_set_dev(seed: int, maps, cls, box: int, pixel_size: float, rU: float, rL: float,
+                     shift_range: float, noise_var: float, img: int = 64, device="cuda",
+                     chunk: int = 2048) -> ParticleSetDev:
+    """particle_set with every per-pixel array made and kept on the device:
+    the same model (one noisy transform on the union of the img x img image
+    grid and the likelihood's pixels, CTF, phase shift, white noise of
+    variance noise_var per part) with poses and CTF parameters from a numpy
+    generator seeded `seed` and the noise from a device generator seeded
+    `seed`."""
+    rng = np.random.default_rng(seed)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed))
+    cls = np.asarray(cls)
+    n = len(cls)
+    q = haar_quaternions(rng, n)
+    t = rng.uniform(-shift_range, shift_range, (n, 2))
+    attr = ctf_attrs(rng, n)
+    h = img // 2
+    jj = np.concatenate([np.arange(0, h), np.arange(-h, 0)])
+    ii = np.arange(0, h + 1)
+    J, I = np.meshgrid(jj, ii, indexing="ij")
+    gi, gj = I.ravel(), J.ravel()
+    iCol, iRow, _, _ = pixel_index(box, rU, rL)
+    key_img = gj.astype(np.int64) * (box + 1) + gi
+    key_lik = iRow.astype(np.int64) * (box + 1) + iCol
+    img_pos = {int(k): i for i, k in enumerate(key_img)}
+    inside = np.isin(key_lik, key_img)
+    ui = np.concatenate([gi, iCol[~inside]])
+    uj = np.concatenate([gj, iRow[~inside]])
+    lik = np.empty(len(iCol), np.int64)
+    lik[inside] = [img_pos[int(k)] for k in key_lik[inside]]
+    lik[~inside] = len(gi) + np.arange(int((~inside).sum()))
+    G, K = len(gi), len(iCol)
+    ui_t = torch.as_tensor(ui, device=device)
+    uj_t = torch.as_tensor(uj, device=device)
+    lik_t = torch.as_tensor(lik, device=device)
+    k2 = torch.stack([ui_t, uj_t, torch.zeros_like(ui_t)], 0).to(torch.float32) / box
+    R = torch.as_tensor(quat_to_mat(q).astype(np.float32), device=device)
+    attr_t = torch.as_tensor(attr, device=device)
+    tt = torch.as_tensor(t, device=device)
+    images = torch.empty((n, img, img), dtype=torch.float32, device=device)
+    dat = torch.empty((n, K), dtype=torch.complex64, device=device)
+    ctf_k = torch.empty((n, K), dtype=torch.float32, device=device)
+    sd = math.sqrt(noise_var)
+    for s0 in range(0, n, chunk):
+        s1 = min(n, s0 + chunk)
+        idx = np.arange(s0, s1)
+        sig = torch.empty((s1 - s0, len(ui)), dtype=torch.complex64, device=device)
+        for c in np.unique(cls[idx]):
+            sel = np.nonzero(cls[idx] == c)[0]
+            sel_t = torch.as_tensor(sel, device=device)
+            f = torch.einsum("nij,jk->nki", R[s0 + sel_t], k2)
+            sig[sel_t] = blob_ft(maps[int(c)], f)
+        ctf_u = ctf_values_t(attr_t[s0:s1], pixel_size, box, ui_t, uj_t)
+        ph = -2 * math.pi * (tt[s0:s1, 0:1] / box * ui_t[None, :].to(torch.float64)
+                             + tt[s0:s1, 1:2] / box * uj_t[None, :].to(torch.float64))
+        sig = sig * (ctf_u * torch.exp(1j * ph)).to(torch.complex64)
+        noise = torch.complex(torch.randn(sig.shape, generator=gen, device=device),
+                              torch.randn(sig.shape, generator=gen, device=device)) * sd
+        data = sig + noise
+        grid = data[:, :G].reshape(s1 - s0, img, h + 1)
+        ims = torch.fft.irfft2(grid, s=(img, img))
+        ims = torch.fft.fftshift(ims, dim=(-2, -1))
+        ims = ims - ims.mean(dim=(-2, -1), keepdim=True)
+        images[s0:s1] = (ims / ims.std(dim=(-2, -1), keepdim=True)).float()
+        dat[s0:s1] = data[:, lik_t]
+        ctf_k[s0:s1] = ctf_u[:, lik_t].float()
+    sigRcp = torch.full((n, K), -1.0 / (2.0 * noise_var), dtype=torch.float32, device=device)
+    return ParticleSetDev(images=images, dat=dat, ctf=ctf_k, sigRcp=sigRcp, iCol=iCol,
+                          iRow=iRow, quat_true=q, trans_true=t, cls=cls)
