@@ -831,6 +831,118 @@ def run_prep(args, rank, world, local_rank):
     return res
 
 
+def run_bank(args, rank, world, local_rank):
+    """The learned E-step's rescoring on its own: one box-256 class (200-blob
+    map, cutoff 80, K = 9,930), its projection bank at the 6,912 global
+    rotations, and args.batch particles with 256 proposed bank rows x 25
+    translations each (rows drawn near each particle's true rotation: the
+    512 nearest bank rotations, 256 of them at random).  One step = the
+    split-bf16 bank-row phase (shift bank, cross term, weights) over the
+    batch; timed with the cross term reading the proposed rows from the bank
+    and with the rows copied out first (TG3_OPT_BANK_GATHER).  A small,
+    self-contained case for profiling the rescoring kernels."""
+    import torch
+    import tg3
+    from tg3 import learned, synth
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    # --box: a smaller map for profiling captures (cutoff scaled with it)
+    box = args.box or 256
+    px, pf, rU = 1.1, 2, 80 * box // 256
+    nP, nR, nT = args.batch, 256, 25
+    f64 = dict(dtype=torch.float64, device=dev)
+    rng = np.random.default_rng(rank_seed(6000, rank))
+    bm = synth.blob_map(rng, 200, (1.5, 3.0), px, 80.0)
+    rL = synth.config_rL(box, px)
+    nv = synth.signal_power([bm], box, px, rU, rL, device=dev) / 0.03 / 2.0
+    ps = synth.particle_set_dev(rank_seed(6001, rank), [bm], np.zeros(nP, np.int64), box, px,
+                                rU, rL, 3.0, nv, device=dev)
+    ctx = tg3.Context(local_rank)
+    ctx.set_volume(0, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
+    ctx.set_pixels(ps.iCol, ps.iRow, box)
+    qg = synth.global_rotations(4, 36)
+    ctx.set_bank(0, torch.as_tensor(qg, **f64), len(qg))
+    # proposals: 256 of the 512 bank rotations nearest each particle's own
+    near = np.argsort(-np.abs(ps.quat_true @ qg.T), axis=1)[:, :512]
+    idx = np.stack([rng.choice(near[l], nR, replace=False) for l in range(nP)]).astype(np.int32)
+    idx_d = torch.as_tensor(idx, device=dev)
+    trans = torch.as_tensor(ps.trans_true[:, None, :] + rng.normal(0, 1.0, (nP, nT, 2)), **f64)
+    cls = torch.zeros(nP, dtype=torch.int32, device=dev)
+    o = dict(wC=torch.empty(nP, **f64), wR=torch.empty((nP, nR), **f64),
+             wT=torch.empty((nP, nT), **f64), base=torch.empty(nP, **f64))
+    pR = torch.full((nP, nR), 1.0 / nR, **f64)
+    pT = torch.full((nP, nT), 1.0 / nT, **f64)
+    pC = torch.ones(nP, **f64)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def step():
+        ctx.local_phase_bank(nP, nR, nT, ps.dat, ps.ctf, ps.sigRcp, idx_d, trans, pR, pT, pC,
+                             cls, o["wC"], o["wR"], o["wT"], o["base"], None, tg3.SCORE_BF16X3)
+
+    def timed(form):
+        ctx.set_option(tg3.OPT_BANK_GATHER, int(form))
+        for _ in range(args.warmup):
+            step()
+        ctx.sync()
+        ctx.set_timing(True)
+        ctx.stage_times(reset=True)
+        clk = ClockSampler(local_rank)
+        clk.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier(world)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+        clocks = clk.stop()
+        st = ctx.stage_times(reset=True)
+        ctx.set_timing(False)
+        ctx.sync()
+        best = o["wR"].argmax(1).cpu().numpy()
+        return reduce_max(world, e0.elapsed_time(e1)) / args.steps, st, clocks, best
+
+    ms_g, st_g, _, best_g = timed(1)          # rows copied out, then the GEMM
+    ms_t, st_t, _, best_t = timed(2)          # in-GEMM rows, TMA gathers
+    ms, st, clocks, best = timed(0)           # in-GEMM rows, the warps' own loads
+    K, Kp = len(ps.iCol), ctx_kp(len(ps.iCol))
+    hbm, bf16, kind = peaks()
+    cross_ms = st["cross"][0] / max(st["cross"][1], 1)
+    algo = float(nP) * (nR * 4.0 * Kp + nT * 4.0 * Kp + nR * nT * 4.0)
+    ach = algo / (cross_ms * 1e-3) / 1e9
+    err = learned.angle_deg(qg[idx[np.arange(nP), best]], ps.quat_true)
+    res = {"metric": "rescoring particles/s (learned E-step, bank-row local phase), box 256",
+           "value": round(job_rate(nP, ms, world), 1), "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "bf16x3", "data": "synthetic",
+           "config": {"workload": f"{nP} particles x {nR} bank rows x {nT} translations, one "
+                                  f"box-{box} class, bank of {len(qg)} rotations, K = {K}",
+                      "l2": "inputs larger than L2 (bank 0.55 GB)"},
+           "clocks": clocks,
+           "roofline": {"kernel": "k_gemm_bank_bf16x3", "bound": "hbm", "achieved": round(ach, 1),
+                        "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4),
+                        "peak_source": f"hbm_gbs, {kind} (MEASURED_PEAKS.json)",
+                        "traffic": None, "algorithmic_bytes_per_launch": algo,
+                        "ms_per_launch": round(cross_ms, 4),
+                        "tflops_algorithmic": round(4.0 * K * nP * nR * nT / (cross_ms * 1e-3)
+                                                    / 1e12, 2)},
+           "stages": {k: round(v[0] / max(v[1], 1), 4) for k, v in st.items() if v[1]},
+           "gather_form": {"ms_per_step": round(ms_g, 4),
+                           "stages": {k: round(v[0] / max(v[1], 1), 4) for k, v in st_g.items()
+                                      if v[1]},
+                           "same_best_rotation": round(float(np.mean(best == best_g)), 4)},
+           "tma_gather_form": {"ms_per_step": round(ms_t, 4),
+                               "stages": {k: round(v[0] / max(v[1], 1), 4)
+                                          for k, v in st_t.items() if v[1]},
+                               "same_best_rotation": round(float(np.mean(best == best_t)), 4)},
+           "speedup_vs_gather_form": round(ms_g / ms, 3),
+           "median_error_best_deg": round(float(np.median(err)), 3),
+           "gpu_launches": 4 * args.steps}
+    ctx.close()
+    return res
+
+
 def run_reco(args, rank, world, local_rank):
     """Reconstruction of a box-256 map from its insertion accumulators
     (Reconstructor::reconstruct): padded grid 512^3 (pf 2), Wiener filter from
@@ -1159,6 +1271,7 @@ def run_learned(args, rank, world, local_rank):
     K = len(iCol)
     noise_var = synth.signal_power(maps[:nTr], box, px, rU, rL, device=dev) / L["snr_lik"] / 2.0
     ctx = tg3.Context(local_rank)
+    ctx.set_option(tg3.OPT_BANK_GATHER, 1 if args.bank_gather else 0)
     for c, bm in enumerate(maps):
         ctx.set_volume(c, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
     ctx.set_pixels(iCol, iRow, box)
@@ -1177,7 +1290,8 @@ def run_learned(args, rank, world, local_rank):
     t0 = time.perf_counter()
     imgs, q_lab, t_lab, q_tru, cls_tr, moves = [], [], [], [], [], []
     chunk = 10000
-    for s0 in range(0, args.train_particles, chunk):
+    n_train = 0 if args.load_net else args.train_particles
+    for s0 in range(0, n_train, chunk):
         m = min(chunk, args.train_particles - s0)
         ps = synth.particle_set_dev(4100 + s0, maps, (s0 + np.arange(m)) % nTr, box, px, rU, rL,
                                     L["shift"], noise_var, device=dev)
@@ -1190,28 +1304,38 @@ def run_learned(args, rank, world, local_rank):
         moves.append(mv)
         del ps
         log(f"labels {s0 + m}/{args.train_particles}: phase moves {mv}")
-    images = torch.cat(imgs)
-    del imgs
-    q_lab, t_lab = np.concatenate(q_lab), np.concatenate(t_lab)
-    q_tru, cls_tr = np.concatenate(q_tru), np.concatenate(cls_tr)
-    torch.cuda.synchronize()
-    label_s = time.perf_counter() - t0
-    label_err = learned.angle_deg(q_lab, q_tru)
-
-    # ---- 2. training (matching mode): references at the label rotations
-    refs = torch.empty_like(images)
-    for c in range(nTr):
-        sel = np.nonzero(cls_tr == c)[0]
-        refs[torch.as_tensor(sel, device=dev)] = learned.render_references(ctx, c, q_lab[sel], box)
     net = tg3.Cnn(local_rank, seed=4242)
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    losses = learned.train_match(net, images, refs, torch.as_tensor(t_lab, **f64), cls_tr,
-                                 args.epochs, 256, args.learned_lr, tau=args.learned_tau, seed=7)
-    torch.cuda.synchronize()
-    train_s = time.perf_counter() - t1
-    del refs, images
-    log(f"trained: losses {losses}")
+    if args.load_net:
+        # a network trained by an earlier run of this workload (profiling runs)
+        net.set_params(np.load(args.load_net)["params"])
+        label_s = train_s = 0.0
+        label_err, moves, losses = np.zeros(1), [[0.0, 0.0, 0.0]], []
+    else:
+        images = torch.cat(imgs)
+        del imgs
+        q_lab, t_lab = np.concatenate(q_lab), np.concatenate(t_lab)
+        q_tru, cls_tr = np.concatenate(q_tru), np.concatenate(cls_tr)
+        torch.cuda.synchronize()
+        label_s = time.perf_counter() - t0
+        label_err = learned.angle_deg(q_lab, q_tru)
+
+        # ---- 2. training (matching mode): references at the label rotations
+        refs = torch.empty_like(images)
+        for c in range(nTr):
+            sel = np.nonzero(cls_tr == c)[0]
+            refs[torch.as_tensor(sel, device=dev)] = learned.render_references(ctx, c, q_lab[sel],
+                                                                               box)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        losses = learned.train_match(net, images, refs, torch.as_tensor(t_lab, **f64), cls_tr,
+                                     args.epochs, 256, args.learned_lr, tau=args.learned_tau,
+                                     seed=7)
+        torch.cuda.synchronize()
+        train_s = time.perf_counter() - t1
+        del refs, images
+        log(f"trained: losses {losses}")
+        if args.save_net:
+            np.savez(args.save_net, params=net.params())
 
     # ---- 3. evaluation particles: held-out particles of the training maps
     # (calibration) and particles of the 4 held-out maps (the timed batch)
@@ -1313,6 +1437,23 @@ def run_learned(args, rank, world, local_rank):
     tl_ms = reduce_max(world, e0.elapsed_time(e1))
     st_l = ctx.stage_times(reset=True)
     ctx.set_timing(False)
+    # the other rescoring form on the same step, stage-timed (not the headline)
+    ab = None
+    if not args.bank_gather:
+        ctx.set_option(tg3.OPT_BANK_GATHER, 1)
+        learned_step()
+        ctx.set_timing(True)
+        ctx.stage_times(reset=True)
+        for _ in range(2):
+            learned_step()
+        st_g = ctx.stage_times(reset=True)
+        ctx.set_timing(False)
+        ctx.set_option(tg3.OPT_BANK_GATHER, 0)
+        ab = {"gather_then_gemm_ms_per_step": round((st_g["project"][0] + st_g["cross"][0]) / 2, 4),
+              "bank_rows_in_gemm_ms_per_step": round(st_l["cross"][0] / args.steps, 4),
+              "note": "rescoring of the same step: slices copied out of the banks then the "
+                      "cross term (TG3_OPT_BANK_GATHER) against the cross term reading the "
+                      "proposed bank rows itself"}
     fb = out["fellBack"].cpu().numpy().astype(bool)
     q_l = out["bestQuat"].cpu().numpy()
     t_l = out["bestTrans"].cpu().numpy()
@@ -1451,9 +1592,11 @@ def run_learned(args, rank, world, local_rank):
     ms_step = tl_ms / args.steps
     v_l = job_rate(n, ms_step + n * map_ms_pp, world)
     v_p = job_rate(n, tp_ms / plain_steps, world)
-    # dominant kernel of the learned step
-    dom = max((k for k in st_l if st_l[k][1]), key=lambda k: st_l[k][0])
-    roof = learned_roofline(dom, st_l, args.steps, n, nRot, nTrans, K, ctx_kp(K), fb)
+    # the learned step's kernels against their rooflines; the dominant one
+    # is the line's roofline
+    dom, roofs = learned_rooflines(st_l, args.steps, n, nRot, nTrans, K, ctx_kp(K),
+                                   int(fb.sum()), nRg, nTg, not args.bank_gather, ms_step)
+    roof = dict(roofs[dom]) if dom else {"kernel": None, "note": "no stage timed"}
     res = {
         "metric": METRIC, "value": round(v_l, 1), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
@@ -1467,7 +1610,9 @@ def run_learned(args, rank, world, local_rank):
                                f"{nRot} rotations x {nTrans} translations rescored exactly, "
                                f"fallback {nRg} x {nTg} global search; cutoff {rU}, K = {K}",
                    "snr": f"{L['snr_lik']} over the likelihood's pixels",
-                   "train_particles": args.train_particles, "epochs": args.epochs,
+                   "train_particles": 0 if args.load_net else args.train_particles,
+                   "epochs": args.epochs, "network": ("loaded: " + args.load_net) if args.load_net
+                   else "trained in this run",
                    "labels": "the plain method's converged poses: FP32 global search, then "
                              "three local phases of 1,000 x 100 (kappa 200 / 1,000 / 5,000, "
                              "translation deviation 2 / 0.7 / 0.3 px)"
@@ -1481,8 +1626,10 @@ def run_learned(args, rank, world, local_rank):
                 "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "wall_s": round(e2e_s, 3), "entry": "tg3_ExpectLearned3D (host buffers)",
                 "same_poses_as_device_entry": e2e_same},
-        "gpu_launches": learned_launches(st_l, fb, unseen.cls) * args.steps,
+        "gpu_launches": learned_launches(fb, unseen.cls, not args.bank_gather) * args.steps,
         "roofline": roof,
+        "roofline_kernels": roofs,
+        "rescoring_forms": ab,
         "stages": stages,
         "plain_fp32": {"value": round(v_p, 1), "ms_per_step": round(tp_ms / plain_steps, 3),
                        "steps": plain_steps, "clocks": clocks_p,
@@ -1540,44 +1687,79 @@ def run_learned(args, rank, world, local_rank):
     return res
 
 
-def learned_roofline(dom, st, steps, n, nRot, nTrans, K, Kp, fb):
-    """Roofline of the learned step's dominant stage.  The bank gather (the
-    'project' stage of the rescoring) moves, per proposed rotation, its hi
-    and lo bf16 rows (4 Kp bytes) and |P|^2 row (4 K) in and the operand rows
-    (4 Kp) out; the cross term does 4 K FLOP per hypothesis (3x in bf16)."""
+def learned_rooflines(st, steps, n, nRot, nTrans, K, Kp, nfb, nRg, nTg, bank_gemm, step_ms):
+    """Rooflines of the learned step's kernels, from the stage times of the
+    timed steps (CUDA events on the library's stream), and the dominant one.
+    - rescoring slice gather (TG3_OPT_BANK_GATHER form): per proposed row its
+      hi and lo bf16 rows (4 Kp bytes) and |P|^2 row (4 K) in, the operand
+      rows (4 Kp) out;
+    - rescoring cross term: with the bank-row kernel, per launch the proposed
+      rows' planes (4 Kp bytes a row), the shifted data (4 Kp a translation)
+      and the log-likelihoods (4 bytes a hypothesis): HBM-bound; otherwise
+      4 K FLOP per hypothesis (split: 3x that in bf16);
+    - fallback cross term (the global search of the fallback particles):
+      4 K FLOP per hypothesis, nRg x nTg per fallback particle."""
     hbm, bf16, src = peaks()
-    ms = st[dom][0] / max(st[dom][1], 1)
-    if dom == "project":
-        algo = float(n) * nRot * (8.0 * Kp + 4.0 * K + 4.0)
-        ach = algo / (ms * 1e-3) / 1e9
-        return {"kernel": "k_bank_gather (rescoring slices from the banks)", "bound": "hbm",
-                "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(ach / hbm, 4), "peak_source": f"hbm_gbs, {src} (MEASURED_PEAKS.json)",
-                "traffic": None, "algorithmic_bytes_per_launch": algo,
-                "ms_per_launch": round(ms, 4)}
-    if dom == "cross":
-        flop = 4.0 * K * float(n) * nRot * nTrans
-        ach = flop / (ms * 1e-3) / 1e12
-        return {"kernel": "k_gemm_bf16x3 (rescoring cross term)", "bound": "tensor",
+    out = {}
+    tot = lambda k: st[k][0] if st.get(k, (0, 0))[1] else 0.0
+    if tot("project") > 0:
+        algo = float(n) * nRot * (8.0 * Kp + 4.0 * K + 4.0) * steps
+        ach = algo / (tot("project") * 1e-3) / 1e9
+        out["rescoring_gather"] = {
+            "kernel": "k_bank_gather (rescoring slices copied from the banks)", "bound": "hbm",
+            "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4),
+            "traffic": None, "algorithmic_bytes_per_launch": algo / steps}
+    if tot("cross") > 0:
+        if bank_gemm:
+            algo = (float(n) * nRot * 4.0 * Kp + float(n) * nTrans * 4.0 * Kp
+                    + float(n) * nRot * nTrans * 4.0) * steps
+            ach = algo / (tot("cross") * 1e-3) / 1e9
+            out["rescoring_cross"] = {
+                "kernel": "k_gemm_bank_bf16x3 (rescoring cross term, proposed rows gathered "
+                          "from the banks by TMA)", "bound": "hbm", "achieved": round(ach, 1),
+                "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": None,
+                "algorithmic_bytes_per_launch": algo / steps,
+                "tflops_algorithmic": round(4.0 * K * n * nRot * nTrans * steps
+                                            / (tot("cross") * 1e-3) / 1e12, 2)}
+        else:
+            flop = 4.0 * K * n * nRot * nTrans * steps
+            ach = flop / (tot("cross") * 1e-3) / 1e12
+            out["rescoring_cross"] = {
+                "kernel": "k_gemm_bf16x3 (rescoring cross term)", "bound": "tensor",
                 "achieved": round(ach, 2), "peak": bf16, "unit": "TFLOP/s",
-                "frac": round(ach / bf16, 4), "peak_source": f"bf16_tflops, {src}",
-                "traffic": None, "algorithmic_flop_per_launch": flop,
-                "ms_per_launch": round(ms, 4)}
-    return {"kernel": dom, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s",
-            "frac": None, "traffic": None, "ms_per_launch": round(ms, 4),
-            "note": "dominant stage has no single-kernel byte count"}
+                "frac": round(ach / bf16, 4), "traffic": None,
+                "algorithmic_flop_per_launch": flop / steps}
+    if tot("fallback_cross") > 0 and nfb > 0:
+        flop = 4.0 * K * nfb * nRg * nTg * steps
+        ach = flop / (tot("fallback_cross") * 1e-3) / 1e12
+        out["fallback_cross"] = {
+            "kernel": "k_gemm_bf16x3 (global search of the fallback particles)",
+            "bound": "tensor", "achieved": round(ach, 2), "peak": bf16, "unit": "TFLOP/s",
+            "frac": round(ach / bf16, 4), "traffic": None,
+            "algorithmic_flop_per_step": flop / steps,
+            "executed_bf16_flop_per_step": 3 * flop / steps}
+    for k, v in out.items():
+        stage = {"rescoring_gather": "project", "rescoring_cross": "cross",
+                 "fallback_cross": "fallback_cross"}[k]
+        v["ms_per_step"] = round(tot(stage) / steps, 4)
+        v["share_of_step"] = round(tot(stage) / steps / step_ms, 4)
+        v["peak_source"] = f"{'hbm_gbs' if v['bound'] == 'hbm' else 'bf16_tflops'}, {src} " \
+                           "(MEASURED_PEAKS.json)"
+    dom = max(out, key=lambda k: out[k]["ms_per_step"]) if out else None
+    return dom, out
 
 
-def learned_launches(st, fb, cls):
-    """Kernels of one learned E-step (this library's own): network 16 (8
-    weight repacks, the first convolution, 6 tensor-core layers, the output
-    layer), matching 1, priors 3, rescoring 5 (gather, shift bank, |X|^2,
-    cross term, weights), confidence and best pose 2; per class with
-    fallback particles 13 (3 gathers, priors, |P|^2, translations, shift
-    bank, |X|^2, norm operand, norm GEMM, cross term, weights, best pose)
-    and 1 for the translation priors."""
+def learned_launches(fb, cls, bank_gemm):
+    """Kernels of one learned E-step (this library's own): network 17 (8
+    weight repacks, the first convolution, 6 tensor-core layers, the split-K
+    sum, the output layer), matching 1, priors 3, rescoring 4 with the
+    bank-row cross term (shift bank, |X|^2, cross term, weights; 5 with the
+    slice gather), confidence and best pose 2; per class with fallback
+    particles 13 (3 gathers, priors, |P|^2, translations, shift bank, |X|^2,
+    norm operand, norm GEMM, cross term, weights, best pose) and 1 for the
+    translation priors."""
     k = len(np.unique(np.asarray(cls)[np.asarray(fb, bool)]))
-    return 16 + 1 + 3 + 5 + 2 + (13 * k + 1 if k else 0)
+    return 17 + 1 + 3 + (4 if bank_gemm else 5) + 2 + (13 * k + 1 if k else 0)
 
 
 def _fp64_bank_rows(job):
@@ -2005,7 +2187,7 @@ def main():
     ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
     ap.add_argument("--workload", default="learned256",
                     choices=["local256", "local256c3", "global64", "uneven192", "learned128",
-                             "learned256", "class2d128", "prep256", "reco256"])
+                             "learned256", "class2d128", "prep256", "reco256", "bank256"])
     ap.add_argument("--train-particles", type=int, default=150000)
     ap.add_argument("--epochs", type=int, default=3)
     ap.add_argument("--learned-snr", type=float, default=1.0,
@@ -2031,8 +2213,16 @@ def main():
                     help="particles whose proposals are checked against the FP64 oracle")
     ap.add_argument("--cpu-sample-global", type=int, default=96,
                     help="rotations per particle in the CPU global-search sample")
+    ap.add_argument("--bank-gather", action="store_true",
+                    help="learned workloads: rescoring slices copied out of the banks before "
+                         "the cross term (TG3_OPT_BANK_GATHER) instead of read by it")
     ap.add_argument("--no-local", action="store_true",
                     help="learned workloads: skip the local-phase measurement beside them")
+    ap.add_argument("--save-net", default=None,
+                    help="learned workloads: save the trained network's parameters (.npz)")
+    ap.add_argument("--load-net", default=None,
+                    help="learned workloads: use saved parameters instead of labelling and "
+                         "training (profiling runs)")
     ap.add_argument("--verbose", action="store_true")
     args = ap.parse_args()
     rank, world, local = init_dist()
@@ -2048,6 +2238,8 @@ def main():
         res = run_prep(args, rank, world, local)
     elif args.workload == "reco256":
         res = run_reco(args, rank, world, local)
+    elif args.workload == "bank256":
+        res = run_bank(args, rank, world, local)
     elif args.workload in ("learned128", "learned256"):
         res = run_learned(args, rank, world, local)
         if args.workload == "learned256" and not args.no_local:

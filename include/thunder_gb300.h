@@ -287,7 +287,8 @@ enum {
     TG3_STAGE_FUSED = 6,   /* projection + split-bf16 cross term in one kernel */
     TG3_STAGE_NETWORK = 7, /* learned E-step: network, matching, proposal confidence */
     TG3_STAGE_FALLBACK = 8,/* learned E-step: global search of the fallback particles */
-    TG3_STAGE_COUNT = 9
+    TG3_STAGE_FALLBACK_CROSS = 9, /* ... of which its cross-term GEMMs */
+    TG3_STAGE_COUNT = 10
 };
 int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
 
@@ -303,12 +304,12 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  *   reference's loop order), which is the faster of the two on GB300.  Both
  *   give the same sums up to FP32 rounding order; a pixel list holding a pixel
  *   twice always scatters.
- * TG3_OPT_BANK_GATHER (default 0): 1 makes the split-bf16 bank-row local
- *   phase (tg3_local_phase_bank_d, the learned E-step's rescoring) copy the
- *   proposed rows into a slice buffer and sum their norms from the bank's
- *   |P|^2 rows before the GEMM; 0 loads the GEMM's operand tiles straight
- *   from the bank rows (TMA gather) and sums the norms from those tiles, in
- *   compensated FP32. */
+ * TG3_OPT_BANK_GATHER (default 1): how the split-bf16 bank-row local phase
+ *   (tg3_local_phase_bank_d, the learned E-step's rescoring) reads the
+ *   proposed rows.  1: copied into a slice buffer, their norms summed from
+ *   the bank's |P|^2 rows, then the GEMM.  0: the GEMM's own warps load its
+ *   operand tiles from the bank rows and sum the rows' norms from them
+ *   (compensated FP32).  2: as 0 with the tiles loaded by TMA gathers. */
 enum { TG3_OPT_FUSED = 0, TG3_OPT_INSERT_GATHER = 1, TG3_OPT_BANK_GATHER = 2 };
 int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);
@@ -498,6 +499,42 @@ int tg3_global_scan2d_d(tg3_ctx* ctx, const float* img, int vdim, int pf, int nI
  * deviation, and normalised deviation. */
 int tg3_prepare_images_d(tg3_ctx* ctx, const float* img, int nImg, int N, float maskRadiusPx,
                          int mask, float stdN, float* dat, float* stats);
+
+/* Re-masking of the particle images (Optimiser::reMaskImg,
+ * src/Optimiser.cpp:6053-6111; on the GPU reMask, gpu/src/cuthunder.cu:
+ * 9384-9560): every image's half transform [N][N/2 + 1] (complex, its centre
+ * at index 0) to real space by the normalised inverse transform, times the
+ * soft mask of radius maskRadiusPx and edge edgeWidth pixels about the
+ * centre (1 inside, 0.5 + 0.5 cos((u - r) / ew pi) on the edge, 0 beyond),
+ * back by the unnormalised forward transform.
+ * tg3_remask_d: imgFT and out [nImg][N][N/2 + 1] on the device (out may be
+ * imgFT); asynchronous on the context's stream.
+ * tg3_ReMask replaces ReMask (gpu/interface/Interface.h:517-522): the
+ * images are nImg host arrays of idim (idim/2 + 1) complex values,
+ * re-masked in place with radius maskRadius / pixelSize (the reference's
+ * EDGE_WIDTH_RL is 6); returns when they are written back. */
+int tg3_remask_d(tg3_ctx* ctx, const float* imgFT, int nImg, int N, float maskRadiusPx,
+                 float edgeWidth, float* out);
+int tg3_ReMask(float* const* images, int nImg, int idim, float maskRadius, float pixelSize,
+               float ew);
+
+/* The accumulators prepared for reconstruction, as PrepareTF does on the GPU
+ * (gpu/src/cuthunder.cu:6160-6400; the CPU path's prepareTF with the
+ * normalisation in allReduceT, src/Reconstructor.cpp:1056-1090,
+ * 2453-2480): with normalise, F and T scaled by 1 / T at the origin; then
+ * both symmetrised -- the volume plus, for every symmetry element R, the
+ * volume sampled trilinearly at R v (Friedel mates conjugated) for
+ * |R v| < maxRadius pf + 1 (SYMMETRIZE_FT, include/Geometry/
+ * Transformation.h:170-196) -- and T floored at 1e-25.  symMat [nSym][9]
+ * row-major, the elements other than the identity (nSym <= 64; 0: no
+ * symmetrisation).  Asynchronous on the context's stream.
+ * tg3_PrepareTF replaces PrepareTF (gpu/interface/Interface.h:320-326) on
+ * host arrays: F3D complex and T3D real [vdim][vdim][vdim/2 + 1], replaced
+ * in place (normalised and symmetrised); returns when they are written. */
+int tg3_ctx_prepare_tf_d(tg3_ctx* ctx, const double* symMat, int nSym, int maxRadius,
+                         int normalise);
+int tg3_PrepareTF(float* F3D, float* T3D, int vdim, const double* symMat, int nSym,
+                  int maxRadius, int pf);
 
 /* The insertion accumulator set to F (complex) and T (real), device arrays
  * [vdim][vdim][vdim/2 + 1] -- e.g. the sums over ranks or half maps that

@@ -98,6 +98,7 @@ def lib():
         L.or_insert.argtypes = [_c128p, _f64p, _c, _c128p, _f64p, _f64p, _d,
                                 _i32p, _i32p, _c, _c, _d, _f64p, _d, _c]
         L.or_fsc.argtypes = [_c128p, _c128p, _c, _c, _f64p]
+        L.or_symmetrize.argtypes = [_c128p, _c, _f64p, _c, _d]
         _lib = L
     return _lib
 
@@ -130,6 +131,7 @@ def ref():
         R.ref_resample.argtypes = [_c, _f64p, _f64p, _u64p, _d, _c, _c, _i32p, _f64p]
         R.ref_resample.restype = _d
         R.ref_sort_descend.argtypes = [_f64p, _c, _u64p]
+        R.ref_symmetrize.argtypes = [_c128p, _c, _f64p, _c, _d]
         _ref = R
     return _ref
 
@@ -312,3 +314,24 @@ def fsc(A, B, n_shell):
     out = np.zeros(n_shell)
     lib().or_fsc(A, B, A.shape[0], n_shell, out)
     return out
+
+
+def symmetrize(vol, mats, r):
+    """SYMMETRIZE_FT of a half transform vol [vdim][vdim][vdim/2 + 1]
+    (complex; a real T as its real part) over the symmetry elements mats
+    [nSym][3][3] within radius r; returns a new array."""
+    v = np.array(vol, dtype=np.complex128, order="C")
+    m = _a(mats, np.float64).reshape(-1, 9)
+    lib().or_symmetrize(v, v.shape[0], m, len(m), float(r))
+    return v
+
+
+def ref_symmetrize(vol, mats, r):
+    """The same through the compiled reference (None if unavailable)."""
+    R = ref()
+    if R is None:
+        return None
+    v = np.array(vol, dtype=np.complex128, order="C")
+    m = _a(mats, np.float64).reshape(-1, 9)
+    R.ref_symmetrize(v, v.shape[0], m, len(m), float(r))
+    return v

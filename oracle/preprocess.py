@@ -109,3 +109,17 @@ def sigma(models, datM, datN, offsets, iCol, iRow, N, r, groups, n_group, by_gro
     ratio = np.minimum(1.0, svd)
     sig = ratio * sM + (1 - ratio) * alpha * sN
     return sig, -0.5 / sig
+
+
+def remask(F, r, ew=EDGE_WIDTH_RL):
+    """Optimiser::reMaskImg (src/Optimiser.cpp:6053-6111; on the GPU reMask,
+    gpu/src/cuthunder.cu:9384-9560): every half transform F [n][N][N/2 + 1]
+    (the image's centre at index 0) taken to real space by the normalised
+    inverse transform (FFT::bw, src/FFT.cpp:143-167), multiplied by the soft
+    mask of radius r and edge ew about the centre, and transformed back by
+    the unnormalised forward transform."""
+    F = np.asarray(F, np.complex128)
+    N = F.shape[-2]
+    real = np.fft.irfft2(F, s=(N, N))
+    masked = np.stack([np.fft.ifftshift(soft_mask(np.fft.fftshift(x), r, ew)) for x in real])
+    return np.fft.rfft2(masked)

@@ -25,6 +25,7 @@
 #include "Volume.h"
 #include "Projector.h"
 #include "Particle.h"
+#include "Transformation.h"
 
 INITIALIZE_EASYLOGGINGPP
 
@@ -337,6 +338,33 @@ double ref_resample(int n, const double* u, const double* w, const size_t* perm,
 
 /* d_index_sort_descend (gsl_sort_largest_index),
  * src/Functions/Functions.cpp:72-79 */
+/* SYMMETRIZE_FT (include/Geometry/Transformation.h:170-196) with the
+ * elements given as matrices: the volume plus, for every R,
+ * VOL_TRANSFORM_MAT_FT(se, src, R, r, LINEAR_INTERP) of the original.  vol
+ * complex [vdim][vdim][vdim/2 + 1], in place; mats [nSym][9] row-major. */
+void ref_symmetrize(double* vol, int vdim, const double* mats, int nSym, double r)
+{
+    Volume src(vdim, vdim, vdim, FT_SPACE);
+    const size_t n = src.sizeFT();
+    for (size_t i = 0; i < n; i++) {
+        src[i].dat[0] = vol[2 * i];
+        src[i].dat[1] = vol[2 * i + 1];
+    }
+    Volume result = src.copyVolume();
+    Volume se(vdim, vdim, vdim, FT_SPACE);
+    for (int s = 0; s < nSym; s++) {
+        dmat33 R;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) R(a, b) = mats[9 * s + 3 * a + b];
+        VOL_TRANSFORM_MAT_FT(se, src, R, r, LINEAR_INTERP, 1);
+        ADD_FT(result, se);
+    }
+    for (size_t i = 0; i < n; i++) {
+        vol[2 * i] = result[i].dat[0];
+        vol[2 * i + 1] = result[i].dat[1];
+    }
+}
+
 void ref_sort_descend(const double* v, int n, size_t* idx)
 {
     dvec d(n);

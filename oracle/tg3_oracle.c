@@ -640,3 +640,43 @@ OR_EXPORT void or_fsc(const double* A, const double* B, int vdim, int nShell,
         fsc[u] = (xx[u] * yy[u] == 0) ? 0.0 : xy[u] / sqrt(xx[u] * yy[u]);
     free(xy); free(xx); free(yy);
 }
+
+
+/* ---------------------------------------------------------------------------
+ * Symmetrisation of a half transform.  SYMMETRIZE_FT (include/Geometry/
+ * Transformation.h:170-196): the result is the volume plus, for every
+ * symmetry element R, the volume transformed by R -- VOL_TRANSFORM_MAT_FT
+ * (:104-125), whose voxel v = (i, j, k) of the half grid (i >= 0) holds the
+ * original sampled trilinearly at R v (getByInterpolationFT, LINEAR_INTERP:
+ * the Friedel mate conjugated for a negative x) when |R v|^2 < r^2, else 0.
+ * vol complex [vdim][vdim][vdim/2 + 1], in place; mats [nSym][9] row-major.
+ */
+void or_symmetrize(double* vol, int vdim, const double* mats, int nSym, double r)
+{
+    const int nx = vdim / 2 + 1, half = vdim / 2;
+    const size_t n = (size_t)vdim * vdim * nx;
+    double* src = (double*)malloc(sizeof(double) * 2 * n);
+    memcpy(src, vol, sizeof(double) * 2 * n);
+    for (int s = 0; s < nSym; s++) {
+        const double* m = mats + 9 * s;
+        for (int z = 0; z < vdim; z++) {
+            const int k = z < half ? z : z - vdim;
+            for (int y = 0; y < vdim; y++) {
+                const int j = y < half ? y : y - vdim;
+                for (int i = 0; i < nx; i++) {
+                    const double a = m[0] * i + m[1] * j + m[2] * k;
+                    const double b = m[3] * i + m[4] * j + m[5] * k;
+                    const double c = m[6] * i + m[7] * j + m[8] * k;
+                    if (a * a + b * b + c * c < r * r) {
+                        double out[2];
+                        sample_trilinear(src, vdim, a, b, c, out);
+                        const size_t idx = ((size_t)z * vdim + y) * nx + i;
+                        vol[2 * idx] += out[0];
+                        vol[2 * idx + 1] += out[1];
+                    }
+                }
+            }
+        }
+    }
+    free(src);
+}

@@ -7,7 +7,8 @@
  * The layouts are the reference's single-precision ones: Complex is two
  * RFLOATs (include/Precision.h:77-99), CTFAttr seven RFLOATs
  * (include/Database.h:108-122), a Volume holds the half transform
- * [nSlc][nSlc][nSlc / 2 + 1] of Complex (include/Image/Volume.h); the
+ * [nSlc][nSlc][nSlc / 2 + 1] of Complex (include/Image/Volume.h) and an
+ * Image the half transform [n][n / 2 + 1] (include/Image/Image.h); the
  * handles carry only what the adaptor reads (ManagedCalPoint's hypothesis
  * counts, gpu/include/ManagedCalPoint.h:15-51).  The function declarations
  * repeat the reference's signatures, which the adaptor defines.
@@ -41,6 +42,15 @@ public:
 
 private:
     int n_;
+    std::vector<Complex> d_;
+};
+
+class Image {
+public:
+    explicit Image(int n) : d_((size_t)n * (n / 2 + 1), Complex{{0, 0}}) {}
+    Complex& operator[](size_t i) { return d_[i]; }
+
+private:
     std::vector<Complex> d_;
 };
 
@@ -93,6 +103,10 @@ void ExpectLocalHostF(int gpuIdx, RFLOAT** wC, RFLOAT** wR, RFLOAT** wT, RFLOAT*
 void ExpectLocalFin(int gpuIdx, Complex** devdatP, RFLOAT** devctfP, RFLOAT** devdefO,
                     RFLOAT** devfreQ, RFLOAT** devsigP, int cSearch);
 void ExpectFreeIdx(int gpuIdx, int** deviCol, int** deviRow);
+void ReMask(std::vector<Image>& img, RFLOAT maskRadius, RFLOAT pixelSize, RFLOAT ew, int idim,
+            int imgNum);
+void PrepareTF(int gpuIdx, Volume& F3D, Volume& T3D, double* symMat, int nSymmetryElement,
+               int maxRadius, int pf);
 void InsertFT(Volume& F3D, Volume& T3D, double* O3D, int* counter, MPI_Comm& hemi,
               MPI_Comm& slav, Complex* datP, RFLOAT* ctfP, RFLOAT* sigRcpP,
               CTFAttr* ctfaData, double* offS, RFLOAT* w, double* nR, double* nT, double* nD,

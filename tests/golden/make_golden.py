@@ -3,7 +3,8 @@ own compiled routines (oracle/_ref/libthunder_ref.so, built by
 oracle/ref/Makefile from the THUNDER sources) on small seeded cases.
 
 Also writes tests/golden/ref_golden_formats.npz (the 2-D, preprocessing,
-spectrum and MRC routines).  Run in a checkout that has the THUNDER tree:
+spectrum and MRC routines) and tests/golden/ref_golden_recon.npz (the
+symmetrisation of half transforms).  Run in a checkout that has the THUNDER tree:
     python tests/golden/make_golden.py
 The fixture pins the oracle (tests/test_oracle_golden.py) on machines that
 do not have the reference sources."""
@@ -125,6 +126,38 @@ def main():
     print(f"wrote {out} ({out.stat().st_size} bytes)")
 
 
+def symmetry_elements():
+    """Non-identity elements of C4 about z and of D2 (rotations by 180 degrees
+    about x, y and z): the symmetry sets of the pins."""
+    def rz(a):
+        c, s = np.cos(a), np.sin(a)
+        return np.array([[c, -s, 0], [s, c, 0], [0, 0, 1.0]])
+    c4 = np.stack([rz(np.pi / 2 * k) for k in (1, 2, 3)])
+    d2 = np.stack([np.diag([1.0, -1, -1]), np.diag([-1.0, 1, -1]), np.diag([-1.0, -1, 1])])
+    return c4, d2
+
+
+def main_recon():
+    """ref_golden_recon.npz: the reference's symmetrisation of half
+    transforms (SYMMETRIZE_FT through VOL_TRANSFORM_MAT_FT)."""
+    R = O.ref()
+    if R is None:
+        raise SystemExit("reference cross-check library unavailable")
+    rng = np.random.default_rng(20261204)
+    g = {}
+    vdim = 16
+    vol = (rng.standard_normal((vdim, vdim, vdim // 2 + 1))
+           + 1j * rng.standard_normal((vdim, vdim, vdim // 2 + 1)))
+    g["sym_vol"] = vol
+    for name, mats in zip(("c4", "d2"), symmetry_elements()):
+        g[f"sym_mats_{name}"] = mats
+        g[f"sym_out_{name}"] = O.ref_symmetrize(vol, mats, 6.5)
+    g["sym_r"] = 6.5
+    out = ROOT / "tests" / "golden" / "ref_golden_recon.npz"
+    np.savez_compressed(out, **g)
+    print("wrote", out)
+
+
 def main_formats():
     """ref_golden_formats.npz: the 2-D projection and insertion
     (Image::getByInterpolationFT, Image::addFT), image preprocessing
@@ -193,3 +226,4 @@ def main_formats():
 if __name__ == "__main__":
     main()
     main_formats()
+    main_recon()

@@ -183,11 +183,13 @@ def test_host_form_matches_device_form(case):
     np.testing.assert_array_equal(h["fb"], r["fellBack"])
 
 
+@pytest.mark.parametrize("form", [0, 2])
 @pytest.mark.parametrize("nR", [32, 160])
-def test_bank_rows_straight_into_the_cross_term(case, nR):
+def test_bank_rows_straight_into_the_cross_term(case, nR, form):
     """The split-bf16 bank-row local phase with the operand tiles loaded
     straight from the banks (TMA gather, norms from the staged tiles)
-    against the form that first copies the rows out (TG3_OPT_BANK_GATHER),
+    against the form that first copies the rows out (TG3_OPT_BANK_GATHER 1;
+    form 0 loads the tiles with the warps' own loads, form 2 by TMA gathers),
     and against the oracle: log-likelihoods within 1e-4 relative, the same
     best hypothesis, marginals within 2e-3 as distributions.  nR = 160
     leaves a partial second row tile."""
@@ -197,8 +199,8 @@ def test_bank_rows_straight_into_the_cross_term(case, nR):
     idx = torch.as_tensor(rng.integers(0, len(case["qg"]), (n, nR)).astype(np.int32), device=DEV)
     trans = torch.as_tensor(rng.uniform(-2, 2, (n, nT, 2)), **F64)
 
-    def run(gather):
-        ctx.set_option(tg3.OPT_BANK_GATHER, int(gather))
+    def run(opt):
+        ctx.set_option(tg3.OPT_BANK_GATHER, int(opt))
         o = dict(wC=torch.empty(n, **F64), wR=torch.empty((n, nR), **F64),
                  wT=torch.empty((n, nT), **F64), base=torch.empty(n, **F64),
                  dvp=torch.empty((n, nR, nT), dtype=torch.float32, device=DEV))
@@ -211,9 +213,9 @@ def test_bank_rows_straight_into_the_cross_term(case, nR):
         return {k: v.cpu().numpy() for k, v in o.items()}
 
     try:
-        a, b = run(False), run(True)
+        a, b = run(form), run(1)
     finally:
-        ctx.set_option(tg3.OPT_BANK_GATHER, 0)
+        ctx.set_option(tg3.OPT_BANK_GATHER, 1)
     assert np.max(np.abs(a["dvp"] - b["dvp"]) / np.abs(b["dvp"])) < 1e-5
     for l in range(n):
         assert np.argmax(a["dvp"][l]) == np.argmax(b["dvp"][l])

@@ -10,6 +10,7 @@ import pytest
 import torch
 
 import tg3
+from oracle import oracle as O
 from oracle import reconstruct as RC
 
 pytestmark = pytest.mark.gpu
@@ -55,3 +56,48 @@ def test_reconstruct_matches_oracle(grid_corr, kernel):
     got = vol.cpu().numpy()
     assert rounds == ref_rounds
     assert np.abs(got - ref).max() < 1e-3 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("which", ["c4", "d2"])
+def test_prepare_tf_matches_oracle(which):
+    """PrepareTF on the accumulators: F and T scaled by 1 / T at the origin,
+    then symmetrised over the elements of C4 or D2 within maxRadius pf + 1,
+    T floored -- against the oracle's SYMMETRIZE_FT (pinned bit for bit to
+    the reference's), within 1e-5 of the peak; and the reference-shaped host
+    form against the device form."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from make_golden import symmetry_elements
+    mats = dict(zip(("c4", "d2"), symmetry_elements()))[which]
+    rng = np.random.default_rng(83)
+    box, pf, maxR = 24, 2, 10
+    vd = box * pf
+    shape = (vd, vd, vd // 2 + 1)
+    F = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    T = (rng.random(shape) + 0.5).astype(np.float32)
+    ctx = tg3.Context(0)
+    try:
+        ctx.insert_begin(vd, pf)
+        ctx.insert_load(torch.as_tensor(F).to(DEV), torch.as_tensor(T).to(DEV))
+        ctx.prepare_tf(mats, maxR)
+        Fo = torch.empty(shape + (2,), dtype=torch.float32, device=DEV)
+        To = torch.empty(shape, dtype=torch.float32, device=DEV)
+        ctx.insert_read(Fo, To)
+        ctx.sync()
+        Fg = Fo.cpu().numpy().view(np.complex64)[..., 0]
+        Tg = To.cpu().numpy()
+    finally:
+        ctx.close()
+    sf = 1.0 / float(T[0, 0, 0])
+    r = maxR * pf + 1.0
+    Fr = O.symmetrize(F.astype(np.complex128) * sf, mats, r)
+    Tr = np.maximum(O.symmetrize(T.astype(np.float64) * sf, mats, r).real, 1e-25)
+    assert np.abs(Fg - Fr).max() < 1e-5 * np.abs(Fr).max()
+    assert np.abs(Tg - Tr).max() < 1e-5 * np.abs(Tr).max()
+    Fh, Th = F.copy(), T.copy()
+    tg3.check(tg3.lib().tg3_PrepareTF(tg3.ptr(Fh), tg3.ptr(Th), vd,
+                                      tg3.ptr(np.ascontiguousarray(mats.reshape(-1, 9))),
+                                      len(mats), maxR, pf))
+    np.testing.assert_array_equal(Fh, Fg)
+    np.testing.assert_array_equal(Th, Tg)

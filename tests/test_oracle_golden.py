@@ -2,6 +2,7 @@
 tests/golden/ref_golden.npz by tests/golden/make_golden.py (which ran the
 reference's compiled sources).  CPU only."""
 import numpy as np
+import pytest
 
 from oracle import oracle as O
 
@@ -145,3 +146,13 @@ def test_mrc_reader_golden(golden_formats, tmp_path):
     got = io.read_mrc(p)
     for s in range(len(got)):
         np.testing.assert_array_equal(io.centred(got[s]), g["mrc_ref"][s])
+
+
+@pytest.mark.parametrize("which", ["c4", "d2"])
+def test_symmetrize_matches_reference_fixture(which):
+    """The oracle's SYMMETRIZE_FT against the reference's output recorded in
+    tests/golden/ref_golden_recon.npz (tests/golden/make_golden.py)."""
+    from pathlib import Path
+    g = np.load(Path(__file__).resolve().parent / "golden" / "ref_golden_recon.npz")
+    out = O.symmetrize(g["sym_vol"], g[f"sym_mats_{which}"], float(g["sym_r"]))
+    np.testing.assert_array_equal(out, g[f"sym_out_{which}"])

@@ -109,3 +109,19 @@ def test_insert2d():
                        np.cos(ang), np.sin(ang), w, ic, ir, K)
     np.testing.assert_allclose(F1, F2, rtol=0, atol=1e-12)
     np.testing.assert_allclose(T1, T2, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("which", ["c4", "d2"])
+def test_symmetrize(which):
+    """SYMMETRIZE_FT: the oracle's restatement equals the reference's
+    VOL_TRANSFORM_MAT_FT sums bit for bit."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from make_golden import symmetry_elements
+    mats = dict(zip(("c4", "d2"), symmetry_elements()))[which]
+    rng = np.random.default_rng(71)
+    vdim = 20
+    vol = (rng.standard_normal((vdim, vdim, vdim // 2 + 1))
+           + 1j * rng.standard_normal((vdim, vdim, vdim // 2 + 1)))
+    np.testing.assert_array_equal(O.symmetrize(vol, mats, 7.5), O.ref_symmetrize(vol, mats, 7.5))

@@ -74,7 +74,11 @@ static cudaEvent_t take_event(tg3_ctx* c)
 
 StageTimer::StageTimer(tg3_ctx* c_, int s) : c(c_), stage(s)
 {
-    if (!c->timing || c->stageMute) return;
+    if (!c->timing) return;
+    if (c->fallbackScope) {
+        if (s != TG3_STAGE_CROSS) return;
+        stage = TG3_STAGE_FALLBACK_CROSS;
+    }
     a = take_event(c);
     b = take_event(c);
     if (a) cudaEventRecord(a, c->stream);
@@ -549,7 +553,7 @@ static int local_phase(tg3_ctx* c, const int* bankIdx, int nP, int nR, int nT, c
         }
         return TG3_OK;
     }
-    if (bankIdx && split && !c->bankGather) {
+    if (bankIdx && split && c->bankGather != 1) {
         // the cross term reads the proposed rows straight from the banks and
         // sums their norms itself: no slice copy, no |P|^2 rows
         {
@@ -562,7 +566,8 @@ static int local_phase(tg3_ctx* c, const int* bankIdx, int nP, int nR, int nT, c
         {
             StageTimer tm(c, TG3_STAGE_CROSS);
             TG3_CUDA(launch_gemm_bank_bf16x3(c->bank, c->px.gen, bankIdx, cls, nP, nR, A, nT, Kp,
-                                             K, sigRcp, ctf, D, -2.0f, c->d_flag, s));
+                                             K, sigRcp, ctf, D, -2.0f, c->d_flag, s,
+                                             c->bankGather == 2));
         }
         {
             StageTimer tm(c, TG3_STAGE_WEIGHTS);
@@ -1779,7 +1784,10 @@ extern "C" int tg3_ctx_set_option(tg3_ctx* c, int option, int value)
     if (st) return st;
     if (option == TG3_OPT_FUSED) c->fused = value != 0;
     else if (option == TG3_OPT_INSERT_GATHER) c->insertGather = value != 0;
-    else if (option == TG3_OPT_BANK_GATHER) c->bankGather = value != 0;
+    else if (option == TG3_OPT_BANK_GATHER) {
+        if (value < 0 || value > 2) return fail(TG3_ERR_ARG, "TG3_OPT_BANK_GATHER takes 0, 1 or 2");
+        c->bankGather = value;
+    }
     else return fail(TG3_ERR_ARG, "unknown option");
     return TG3_OK;
 }

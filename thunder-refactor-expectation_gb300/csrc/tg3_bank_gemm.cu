@@ -306,6 +306,276 @@ k_gemm_bank_bf16x3(const __grid_constant__ BankMaps maps, const __grid_constant_
     }
 }
 
+
+// The same product with the A tiles loaded by the four norm warps
+// themselves: per K block every thread loads 16 bytes of each plane of 8
+// rows (8 lanes cover a row's 128-byte chunk, so a warp instruction reads 4
+// whole rows' chunks), stores them at their swizzled places, and adds the
+// rows' |P|^2 weighted by sigRcp ctf^2 to its partial norms in compensated
+// FP32; the 8 lanes' partials are summed at the end.  The next K block's
+// loads are issued before the current one is stored (two register sets).
+// A stage is full when the four warps have stored their share (one arrival
+// each) and the B tiles' bytes have landed (TMA, warp 4 lane 0); it is free
+// when the MMAs that read it have completed.
+struct LdgRows {
+    const __nv_bfloat16* hi[kMaxClasses];
+    const __nv_bfloat16* lo[kMaxClasses];
+    int nB[kMaxClasses];
+};
+
+__global__ void __launch_bounds__(BG_THREADS, 1)
+k_gemm_bank_ldg(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
+                const __grid_constant__ CUtensorMap tmBl, const BgParams p)
+{
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const int aBytes = BG_M * BG_BK * 2;
+    const int bBytes = p.ntile * BG_BK * 2;
+    const int stageBytes = 2 * aBytes + 2 * bBytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + p.stages * stageBytes);
+    uint64_t* empty = full + p.stages;
+    uint64_t* accum = empty + p.stages;
+    uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(accum + 1);
+    int* abortFlag = reinterpret_cast<int*>(tmemSlot + 1);
+    int* rows = abortFlag + 1;                            // [BG_M]
+    float* nrmRow = reinterpret_cast<float*>(rows + BG_M);  // [BG_M]
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mtile = blockIdx.x, item = blockIdx.y;
+    const int cl = p.cls ? p.cls[item] : 0;
+    const bool clOk = cl >= 0 && cl < kMaxClasses && banks.nB[cl] > 0;
+    const int k = clOk ? cl : 0;
+    const int nB = clOk ? banks.nB[k] : 0;
+    const int nkb = p.Kd / BG_BK;
+    const int bRow0 = item * p.nT;
+
+    if (threadIdx.x < BG_M) {
+        const int r = mtile * BG_M + threadIdx.x;
+        int b = 0;
+        if (r < p.nR) {
+            b = p.idx[(size_t)item * p.nR + r];
+            if (b < 0 || b >= nB) {
+                atomicOr(p.flag, 1 << 16);
+                b = 0;
+            }
+        }
+        rows[threadIdx.x] = b;
+    }
+    if (threadIdx.x == BG_M) {
+        for (int s = 0; s < p.stages; s++) {
+            mbar_init(full + s, 5);
+            mbar_init(empty + s, 1);
+        }
+        mbar_init(accum, 1);
+        *abortFlag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 5) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmemSlot)),
+                     "r"(p.tmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmemSlot;
+
+    int issuedTma = 0, issuedMma = 0;
+    if (warp < 4) {
+        // ---------------- A tiles and the rows' norms
+        const int t = threadIdx.x;
+        const int g = t >> 3, q = t & 7;                   // row group, 16-byte chunk
+        const __nv_bfloat16* bh = banks.hi[k];
+        const __nv_bfloat16* bl = banks.lo[k];
+        const __nv_bfloat16* srcH[8];
+        const __nv_bfloat16* srcL[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const size_t off = (size_t)rows[g + 16 * i] * p.Kd + q * 8;
+            srcH[i] = bh + off;
+            srcL[i] = bl + off;
+        }
+        const float* sg = p.sigRcp + (size_t)item * p.K;
+        const float* cf = p.ctf + (size_t)item * p.K;
+        float nS[8], nC[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) nS[i] = nC[i] = 0.f;
+        uint4 cur[16], nxt[16];
+        // K block 0
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            cur[2 * i] = __ldg(reinterpret_cast<const uint4*>(srcH[i]));
+            cur[2 * i + 1] = __ldg(reinterpret_cast<const uint4*>(srcL[i]));
+        }
+        for (int kb = 0; kb < nkb; kb++) {
+            const int s = kb % p.stages;
+            const int round = kb / p.stages;
+            // the next K block's loads go out before this one is stored
+            if (kb + 1 < nkb) {
+                const size_t o = (size_t)(kb + 1) * BG_BK;
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    nxt[2 * i] = __ldg(reinterpret_cast<const uint4*>(srcH[i] + o));
+                    nxt[2 * i + 1] = __ldg(reinterpret_cast<const uint4*>(srcL[i] + o));
+                }
+            }
+            if (round > 0) {
+                bool ok = lane != 0 || mbar_wait(empty + s, (round - 1) & 1, kWaitBudget);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok || *(volatile int*)abortFlag) {
+                    if (lane == 0) {
+                        atomicOr(p.flag, 4);
+                        *(volatile int*)abortFlag = 1;
+                    }
+                    break;
+                }
+            }
+            uint8_t* st = smem + s * stageBytes;
+            // the weights sigRcp ctf^2 of this lane's 4 pixels
+            const int px0 = kb * (BG_BK / 2) + q * 4;
+            float w[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const int px = px0 + c;
+                const float cc = px < p.K ? __ldg(cf + px) : 0.f;
+                w[c] = px < p.K ? __ldg(sg + px) * cc * cc : 0.f;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const int r = g + 16 * i;
+                const int phys = r * 128 + ((q ^ (r & 7)) << 4);
+                *reinterpret_cast<uint4*>(st + phys) = cur[2 * i];
+                *reinterpret_cast<uint4*>(st + aBytes + phys) = cur[2 * i + 1];
+                const uint32_t hw[4] = {cur[2 * i].x, cur[2 * i].y, cur[2 * i].z, cur[2 * i].w};
+                const uint32_t lw[4] = {cur[2 * i + 1].x, cur[2 * i + 1].y, cur[2 * i + 1].z,
+                                        cur[2 * i + 1].w};
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const float2 hf = __bfloat1622float2(
+                        *reinterpret_cast<const __nv_bfloat162*>(&hw[c]));
+                    const float2 lf = __bfloat1622float2(
+                        *reinterpret_cast<const __nv_bfloat162*>(&lw[c]));
+                    const float re = hf.x + lf.x, im = hf.y + lf.y;
+                    kahan_add(nS[i], nC[i], w[c] * (re * re + im * im));
+                }
+            }
+            // generic stores visible to the tensor cores' reads, then arrive
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(full + s);
+#pragma unroll
+            for (int j = 0; j < 16; j++) cur[j] = nxt[j];
+        }
+        // the rows' norms: the 8 lanes of a row group hold partials
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            float v = nS[i] - nC[i];
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            v += __shfl_xor_sync(0xffffffffu, v, 2);
+            v += __shfl_xor_sync(0xffffffffu, v, 4);
+            if (q == 0) nrmRow[g + 16 * i] = v;
+        }
+    } else if (warp == 4) {
+        // ---------------- B tiles (TMA)
+        if (lane == 0) {
+            for (int kb = 0; kb < nkb; kb++) {
+                const int s = kb % p.stages;
+                const int round = kb / p.stages;
+                if (round > 0 && !mbar_wait(empty + s, (round - 1) & 1, kWaitBudget)) {
+                    atomicOr(p.flag, 4);
+                    *(volatile int*)abortFlag = 1;
+                    break;
+                }
+                if (*(volatile int*)abortFlag) break;
+                uint8_t* st = smem + s * stageBytes;
+                mbar_expect_tx(full + s, 2 * bBytes);
+                tma_load_2d(st + 2 * aBytes, &tmBh, full + s, kb * BG_BK, bRow0);
+                tma_load_2d(st + 2 * aBytes + bBytes, &tmBl, full + s, kb * BG_BK, bRow0);
+                issuedTma = kb + 1;
+            }
+        }
+    } else {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = umma_idesc(BG_M, p.ntile);
+            for (int kb = 0; kb < nkb; kb++) {
+                const int s = kb % p.stages;
+                const int round = kb / p.stages;
+                if (!mbar_wait(full + s, round & 1, kWaitBudget)) {
+                    atomicOr(p.flag, 4);
+                    *(volatile int*)abortFlag = 1;
+                    break;
+                }
+                if (*(volatile int*)abortFlag) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                uint8_t* st = smem + s * stageBytes;
+                const uint32_t ah = smem_u32(st), al = smem_u32(st + aBytes);
+                const uint32_t bh = smem_u32(st + 2 * aBytes),
+                               bl = smem_u32(st + 2 * aBytes + bBytes);
+#pragma unroll
+                for (int kk = 0; kk < BG_BK / 16; kk++) {
+                    const uint32_t off = kk * 32;
+                    umma_bf16(tmem, umma_desc(ah + off), umma_desc(bh + off), idesc,
+                              (kb | kk) != 0);
+                    umma_bf16(tmem, umma_desc(ah + off), umma_desc(bl + off), idesc, 1);
+                    umma_bf16(tmem, umma_desc(al + off), umma_desc(bh + off), idesc, 1);
+                }
+                umma_commit(empty + s);
+                issuedMma = kb + 1;
+            }
+            umma_commit(accum);
+        }
+    }
+    __syncthreads();
+    // ---------------- epilogue (warps 0 - 3)
+    bool ok = *(volatile int*)abortFlag == 0;
+    if (warp < 4) ok = ok && mbar_wait(accum, 0, kWaitBudget);
+    ok = __syncthreads_and(ok) != 0;
+    if (!ok && threadIdx.x == 0) {
+        atomicOr(p.flag, 4);
+        *(volatile int*)abortFlag = 1;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool aborted = !ok;
+    if (!aborted && warp < 4) {
+        const int pitch = p.ntile + 1;
+        float* stage = reinterpret_cast<float*>(smem) + (size_t)warp * 32 * pitch;
+        const int rowBase = mtile * BG_M + warp * 32;
+        const float add = nrmRow[warp * 32 + lane];
+        for (int c0 = 0; c0 < p.ntile; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; i++) stage[lane * pitch + c0 + i] = fmaf(p.alpha, v[i], add);
+        }
+        __syncwarp();
+        float* cbase = p.C + (size_t)item * p.nR * p.nT;
+        for (int rr = 0; rr < 32; rr++) {
+            const int r = rowBase + rr;
+            if (r >= p.nR) break;
+            for (int j = lane; j < p.nT; j += 32) cbase[(size_t)r * p.nT + j] = stage[rr * pitch + j];
+        }
+    }
+    if (aborted && warp == 4 && lane == 0) {
+        for (int kb = 0; kb < issuedTma; kb++) {
+            const int s = kb % p.stages;
+            mbar_wait(full + s, (kb / p.stages) & 1, kWaitBudget / 4);
+        }
+    }
+    if (aborted && warp == 5 && lane == 0 && issuedMma > 0) mbar_wait(accum, 0, kWaitBudget / 4);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 5) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(p.tmemCols)
+                     : "memory");
+    }
+}
+
 }  // namespace
 
 // A: the classes' banks (bank[k].hi holds the hi plane, then the lo plane
@@ -314,7 +584,8 @@ k_gemm_bank_bf16x3(const __grid_constant__ BankMaps maps, const __grid_constant_
 cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const int* idx,
                                     const int* cls, int nP, int nR, const void* B, int nT,
                                     int Kd, int K, const float* sigRcp, const float* ctf,
-                                    float* C, float alpha, int* flag, cudaStream_t st)
+                                    float* C, float alpha, int* flag, cudaStream_t st,
+                                    bool tmaGather)
 {
     if (nP <= 0 || nR <= 0 || nT <= 0 || nT > 256 || Kd <= 0 || Kd % BG_BK || nP > 65535)
         return cudaErrorInvalidValue;
@@ -364,12 +635,27 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
         return cudaErrorInvalidValue;
     // stages, then barriers (2 stages + 1, 8 bytes each), the TMEM slot, the
     // abort word and the tile's row list
-    const size_t smem = 1024 + (size_t)p.stages * stageBytes + 256 + sizeof(int) * BG_M;
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_bank_bf16x3,
+    const size_t smem = 1024 + (size_t)p.stages * stageBytes + 256 + 2 * sizeof(int) * BG_M;
+    dim3 grid((nR + BG_M - 1) / BG_M, nP);
+    if (tmaGather) {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_bank_bf16x3,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        k_gemm_bank_bf16x3<<<grid, BG_THREADS, smem, st>>>(maps, mBh, mBl, p);
+        return cudaGetLastError();
+    }
+    LdgRows rowsOf;
+    for (int k = 0; k < kMaxClasses; k++) {
+        const Bank& b = banks[maps.nB[k] ? k : first];
+        rowsOf.hi[k] = b.hi;
+        rowsOf.lo[k] = b.hi + (size_t)b.nB * b.Kp;
+        rowsOf.nB[k] = maps.nB[k];
+    }
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_bank_ldg,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    dim3 grid((nR + BG_M - 1) / BG_M, nP);
-    k_gemm_bank_bf16x3<<<grid, BG_THREADS, smem, st>>>(maps, mBh, mBl, p);
+    k_gemm_bank_ldg<<<grid, BG_THREADS, smem, st>>>(rowsOf, mBh, mBl, p);
     return cudaGetLastError();
 }
 

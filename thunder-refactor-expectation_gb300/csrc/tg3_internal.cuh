@@ -182,10 +182,13 @@ struct tg3_ctx {
     // tg3_ctx_set_option
     bool fused = false;
     bool insertGather = false;    // TG3_OPT_INSERT_GATHER
-    bool bankGather = true;       // TG3_OPT_BANK_GATHER
+    int bankGather = 1;           // TG3_OPT_BANK_GATHER (0, 1 or 2)
     // per-stage event timing (tg3_ctx_set_timing)
     bool timing = false;
-    bool stageMute = false;       // inner stages not recorded (a bracketing stage is)
+    // inside the learned E-step's fallback: its cross-term launches are
+    // recorded as TG3_STAGE_FALLBACK_CROSS and its other inner stages not
+    // at all (the bracketing TG3_STAGE_FALLBACK covers them)
+    bool fallbackScope = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[TG3_STAGE_COUNT];
     std::vector<cudaEvent_t> eventPool;
     double stageMs[TG3_STAGE_COUNT] = {};
@@ -445,7 +448,8 @@ bool bf16x3_available();
 cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const int* idx,
                                     const int* cls, int nP, int nR, const void* B, int nT,
                                     int Kd, int K, const float* sigRcp, const float* ctf,
-                                    float* C, float alpha, int* flag, cudaStream_t st);
+                                    float* C, float alpha, int* flag, cudaStream_t st,
+                                    bool tmaGather = false);
 cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda,
                                   const float* B, long long sB, int ldb,
                                   int M, int N, int Kd, int batch, float* C,

@@ -345,7 +345,7 @@ extern "C" int tg3_learned_expect_d(tg3_ctx* c, tg3_cnn* net, int nP, const floa
             return fail(TG3_ERR_ARG, "a particle's class is out of range");
     if (!hList.empty()) {
         StageTimer tm(c, TG3_STAGE_FALLBACK);
-        c->stageMute = true;
+        c->fallbackScope = true;
         TG3_CUDA(cudaMemcpyAsync(list, hList.data(), sizeof(int) * hList.size(),
                                  cudaMemcpyHostToDevice, s));
         k_fill_f64<<<1, 256, 0, s>>>(gpT, nTg, 1.0 / nTg);
@@ -353,7 +353,7 @@ extern "C" int tg3_learned_expect_d(tg3_ctx* c, tg3_cnn* net, int nP, const floa
             const int k = g.first, start = g.second.first, m = g.second.second;
             const Bank& b = c->bank[k];
             if (b.nB <= 0 || b.gen != c->px.gen || b.K != K) {
-                c->stageMute = false;
+                c->fallbackScope = false;
                 return fail(TG3_ERR_STATE, "a fallback particle's class has no bank");
             }
             const int* li = list + start;
@@ -366,7 +366,7 @@ extern "C" int tg3_learned_expect_d(tg3_ctx* c, tg3_cnn* net, int nP, const floa
             st = global_scan_bank(c, k, m, nTg, gdat, gctf, gsig, gTrans, gpR, gpT, gwC, gwR, gwT,
                                   gbase, nullptr, precision);
             if (st) {
-                c->stageMute = false;
+                c->fallbackScope = false;
                 return st;
             }
             k_best_global<<<(m + 7) / 8, 256, 0, s>>>(gwR, gwT, gbase, li, m, b.nB, nTg, b.quat,
@@ -374,7 +374,7 @@ extern "C" int tg3_learned_expect_d(tg3_ctx* c, tg3_cnn* net, int nP, const floa
                                                       out->baseL);
             TG3_LAUNCH_CHECK("fallback best pose");
         }
-        c->stageMute = false;
+        c->fallbackScope = false;
     }
     // ---- optional outputs
     if ((st = copy_out(out->peak, peak, nP, s))) return st;

@@ -248,22 +248,46 @@ struct Plan {
 std::vector<Plan> g_plans;
 std::mutex g_planLock;
 
-int get_plan(tg3_ctx* c, int N, int batch, cufftHandle* out)
+// Batched 2-D plans of a context, forward (real to complex) or inverse.
+int get_plan(tg3_ctx* c, int N, int batch, cufftHandle* out, bool inverse = false)
 {
     std::lock_guard<std::mutex> g(g_planLock);
+    const int key = inverse ? -batch : batch;
     for (auto& p : g_plans)
-        if (p.c == c && p.N == N && p.batch == batch) {
+        if (p.c == c && p.N == N && p.batch == key) {
             *out = p.h;
             return TG3_OK;
         }
     cufftHandle h;
     int n[2] = {N, N};
-    if (cufftPlanMany(&h, 2, n, nullptr, 1, N * N, nullptr, 1, N * (N / 2 + 1), CUFFT_R2C,
-                      batch) != CUFFT_SUCCESS)
-        return fail(TG3_ERR_CUDA, "cuFFT plan creation failed");
-    g_plans.push_back({c, N, batch, h});
+    const cufftResult r =
+        inverse ? cufftPlanMany(&h, 2, n, nullptr, 1, N * (N / 2 + 1), nullptr, 1, N * N,
+                                CUFFT_C2R, batch)
+                : cufftPlanMany(&h, 2, n, nullptr, 1, N * N, nullptr, 1, N * (N / 2 + 1),
+                                CUFFT_R2C, batch);
+    if (r != CUFFT_SUCCESS) return fail(TG3_ERR_CUDA, "cuFFT plan creation failed");
+    g_plans.push_back({c, N, key, h});
     *out = h;
     return TG3_OK;
+}
+
+// ReMask's real-space step: x / N^2 (the normalisation of the inverse
+// transform, FFT::bw) times the soft mask of radius r and edge ew about the
+// centre at index 0 (kernel_SoftMask / kernel_MulMask, gpu/src/Kernel.cu:
+// 5249-5316): 1 inside r, 0.5 + 0.5 cos((u - r) / ew pi) on the edge, 0
+// beyond r + ew, u from the wrapped indices.
+__global__ void k_remask_real(float* __restrict__ real, int N, float r, float ew, size_t n)
+{
+    const float inv = 1.0f / ((float)N * (float)N);
+    const size_t per = (size_t)N * N;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n * per;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(q % N), y = (int)((q / N) % N);
+        const int i = x < N / 2 ? x : x - N, j = y < N / 2 ? y : y - N;
+        const float u = sqrtf((float)(i * i + j * j));
+        const float m = u > r + ew ? 0.f : (u >= r ? 0.5f + 0.5f * cospif((u - r) / ew) : 1.f);
+        real[q] = real[q] * inv * m;
+    }
 }
 
 }  // namespace
@@ -384,6 +408,81 @@ extern "C" int tg3_prepare_images_d(tg3_ctx* c, const float* img, int nImg, int 
     if (stats) {
         k_stats_f32<<<(3 * nImg + 255) / 256, 256, 0, s>>>(stv, nImg, stats);
         TG3_LAUNCH_CHECK("statistics");
+    }
+    return TG3_OK;
+}
+
+extern "C" int tg3_remask_d(tg3_ctx* c, const float* imgFT, int nImg, int N, float maskRadiusPx,
+                            float edgeWidth, float* out)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (!imgFT || !out || nImg <= 0 || N < 4 || (N & 1) || !(maskRadiusPx > 0) ||
+        !(edgeWidth > 0))
+        return fail(TG3_ERR_ARG, "bad re-mask arguments");
+    const int IB = std::min(nImg, 2048);
+    const size_t img2 = (size_t)N * N, ft2 = (size_t)N * (N / 2 + 1);
+    // the inverse transform overwrites its input: it reads a copy
+    const size_t oR = 0, oF = (sizeof(float) * img2 * IB + 255) / 256 * 256,
+                 total = oF + sizeof(float2) * ft2 * IB;
+    char* b = (char*)ws_get(c, WS_PREP, total, &st);
+    if (!b) return st;
+    float* real = (float*)(b + oR);
+    cufftComplex* ft = (cufftComplex*)(b + oF);
+    cudaStream_t s = c->stream;
+    for (int l0 = 0; l0 < nImg; l0 += IB) {
+        const int n = std::min(IB, nImg - l0);
+        TG3_CUDA(cudaMemcpyAsync(ft, imgFT + 2 * ft2 * (size_t)l0, sizeof(float2) * ft2 * n,
+                                 cudaMemcpyDeviceToDevice, s));
+        cufftHandle hi, hf;
+        if ((st = get_plan(c, N, n, &hi, true))) return st;
+        if ((st = get_plan(c, N, n, &hf, false))) return st;
+        if (cufftSetStream(hi, s) != CUFFT_SUCCESS || cufftExecC2R(hi, ft, real) != CUFFT_SUCCESS)
+            return fail(TG3_ERR_CUDA, "cuFFT inverse transform failed");
+        const size_t cnt = img2 * n;
+        k_remask_real<<<(unsigned)std::min<size_t>((cnt + 255) / 256, 152 * 32), 256, 0, s>>>(
+            real, N, maskRadiusPx, edgeWidth, n);
+        TG3_LAUNCH_CHECK("re-mask");
+        if (cufftSetStream(hf, s) != CUFFT_SUCCESS ||
+            cufftExecR2C(hf, real, reinterpret_cast<cufftComplex*>(out) + ft2 * (size_t)l0) !=
+                CUFFT_SUCCESS)
+            return fail(TG3_ERR_CUDA, "cuFFT forward transform failed");
+    }
+    return TG3_OK;
+}
+
+extern "C" int tg3_ReMask(float* const* images, int nImg, int idim, float maskRadius,
+                          float pixelSize, float ew)
+{
+    if (!images || nImg <= 0 || idim <= 0 || !(pixelSize > 0))
+        return fail(TG3_ERR_ARG, "bad ReMask arguments");
+    int st = TG3_OK;
+    tg3_ctx* c = nullptr;
+    {
+        int dev = 0;
+        TG3_CUDA(cudaGetDevice(&dev));
+        static std::mutex mu;
+        static tg3_ctx* ctxs[64] = {};
+        if (dev < 0 || dev >= 64) return fail(TG3_ERR_ARG, "device ordinal out of range");
+        std::lock_guard<std::mutex> lk(mu);
+        if (!ctxs[dev] && (st = tg3_ctx_create(&ctxs[dev], dev))) return st;
+        c = ctxs[dev];
+    }
+    const size_t ft2 = (size_t)idim * (idim / 2 + 1);
+    const int IB = std::min(nImg, 1024);
+    float* d = (float*)ws_get(c, WS_H2D, sizeof(float2) * ft2 * IB, &st);
+    if (!d) return st;
+    cudaStream_t s = c->stream;
+    for (int l0 = 0; l0 < nImg; l0 += IB) {
+        const int n = std::min(IB, nImg - l0);
+        for (int i = 0; i < n; i++)
+            TG3_CUDA(cudaMemcpyAsync(d + 2 * ft2 * i, images[l0 + i], sizeof(float2) * ft2,
+                                     cudaMemcpyHostToDevice, s));
+        if ((st = tg3_remask_d(c, d, n, idim, maskRadius / pixelSize, ew, d))) return st;
+        for (int i = 0; i < n; i++)
+            TG3_CUDA(cudaMemcpyAsync(images[l0 + i], d + 2 * ft2 * i, sizeof(float2) * ft2,
+                                     cudaMemcpyDeviceToHost, s));
+        TG3_CUDA(cudaStreamSynchronize(s));
     }
     return TG3_OK;
 }

@@ -259,6 +259,98 @@ int plan3(tg3_ctx* c, int vdim, cufftType type, cufftHandle* out)
     return TG3_OK;
 }
 
+// ---- PrepareTF: normalisation and symmetrisation of the accumulators
+constexpr int kMaxSym = 64;     // symmetry elements (the icosahedral group has 59 besides E)
+
+struct SymMats {
+    float m[kMaxSym * 9];
+};
+
+// src = acc, scaled by 1 / T at the origin when normalising (allReduceT's
+// RECONSTRUCTOR_NORMALISE_T_F, src/Reconstructor.cpp:2453-2480).
+__global__ void k_acc_scaled_copy(const float4* __restrict__ acc, size_t n, int normalise,
+                                  float4* __restrict__ src)
+{
+    const float sf = normalise ? 1.0f / acc[0].z : 1.0f;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float4 v = acc[i];
+        src[i] = make_float4(v.x * sf, v.y * sf, v.z * sf, 0.f);
+    }
+}
+
+// Trilinear sample of the (F, T) half grid at (x, y, z), the Friedel mate
+// conjugated for x < 0 (Volume::getByInterpolationFT, LINEAR_INTERP).
+__device__ __forceinline__ float3 sample_ft(const float4* __restrict__ v, int vdim, float x,
+                                            float y, float z)
+{
+    float sgn = 1.f;
+    if (x < 0.f) {
+        x = -x;
+        y = -y;
+        z = -z;
+        sgn = -1.f;
+    }
+    const int nx = vdim / 2 + 1;
+    const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+    const int x0 = (int)xf, y0 = (int)yf, z0 = (int)zf;
+    const float fx = x - xf, fy = y - yf, fz = z - zf;
+    const float wx[2] = {1.f - fx, fx}, wy[2] = {1.f - fy, fy}, wz[2] = {1.f - fz, fz};
+    float3 o = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const int zz = z0 + k < 0 ? z0 + k + vdim : z0 + k;
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int yy = y0 + j < 0 ? y0 + j + vdim : y0 + j;
+            const float4* row = v + ((size_t)zz * vdim + yy) * nx + x0;
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const float w = wx[i] * wy[j] * wz[k];
+                const float4 c = __ldg(row + i);
+                o.x += c.x * w;
+                o.y += c.y * w;
+                o.z += c.z * w;
+            }
+        }
+    }
+    o.y *= sgn;
+    return o;
+}
+
+// acc = src + sum over the symmetry elements R of src sampled at R v for
+// |R v|^2 < r2 (SYMMETRIZE_FT, include/Geometry/Transformation.h:170-196),
+// T floored at 1e-25 (PrepareTF's symmetrizeT).
+__global__ void k_symmetrize(float4* __restrict__ acc, const float4* __restrict__ src, int vdim,
+                             const SymMats mats, int nSym, float r2)
+{
+    const int nx = vdim / 2 + 1, half = vdim / 2;
+    const size_t n = (size_t)vdim * vdim * nx;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nx);
+        const int y = (int)((q / nx) % vdim), z = (int)(q / ((size_t)nx * vdim));
+        const int j = y < half ? y : y - vdim, k = z < half ? z : z - vdim;
+        float4 v = src[q];
+        if ((float)(i * i + j * j + k * k) < r2) {
+            for (int s = 0; s < nSym; s++) {
+                const float* m = mats.m + 9 * s;
+                const float a = m[0] * i + m[1] * j + m[2] * k;
+                const float b = m[3] * i + m[4] * j + m[5] * k;
+                const float c = m[6] * i + m[7] * j + m[8] * k;
+                if (a * a + b * b + c * c < r2) {
+                    const float3 w = sample_ft(src, vdim, a, b, c);
+                    v.x += w.x;
+                    v.y += w.y;
+                    v.z += w.z;
+                }
+            }
+        }
+        v.z = fmaxf(v.z, 1e-25f);
+        acc[q] = v;
+    }
+}
+
 }  // namespace
 
 void reco_release(tg3_ctx* c)
@@ -384,5 +476,63 @@ extern "C" int tg3_ctx_reconstruct_d(tg3_ctx* c, const double* fsc, int nFsc, in
     TG3_LAUNCH_CHECK("gridding correction table");
     k_reco_extract<<<G, 256, 0, s>>>(R, vdim, N, tabE, vol);
     TG3_LAUNCH_CHECK("extract and gridding correction");
+    return TG3_OK;
+}
+
+extern "C" int tg3_ctx_prepare_tf_d(tg3_ctx* c, const double* symMat, int nSym, int maxRadius,
+                                    int normalise)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (!c->ins.acc) return fail(TG3_ERR_STATE, "no insertion accumulator (tg3_ctx_insert_begin)");
+    if (nSym < 0 || nSym > kMaxSym || (nSym > 0 && !symMat))
+        return fail(TG3_ERR_ARG, "symmetry elements: 0 to 64 matrices");
+    const int vdim = c->ins.vdim, pf = c->ins.pf;
+    const double r = (double)maxRadius * pf + 1.0;
+    if (maxRadius <= 0 || r + 1.0 > vdim / 2)
+        return fail(TG3_ERR_ARG, "maxRadius x pf + 2 must not exceed vdim / 2");
+    SymMats mats;
+    for (int i = 0; i < 9 * nSym; i++) mats.m[i] = (float)symMat[i];
+    const size_t n = (size_t)vdim * vdim * (vdim / 2 + 1);
+    float4* src = (float4*)ws_get(c, WS_RECO, sizeof(float4) * n, &st);
+    if (!src) return st;
+    cudaStream_t s = c->stream;
+    k_acc_scaled_copy<<<152 * 8, 256, 0, s>>>(c->ins.acc, n, normalise, src);
+    TG3_LAUNCH_CHECK("accumulator copy");
+    k_symmetrize<<<152 * 16, 256, 0, s>>>(c->ins.acc, src, vdim, mats, nSym, (float)(r * r));
+    TG3_LAUNCH_CHECK("symmetrisation");
+    return TG3_OK;
+}
+
+extern "C" int tg3_PrepareTF(float* F3D, float* T3D, int vdim, const double* symMat, int nSym,
+                             int maxRadius, int pf)
+{
+    if (!F3D || !T3D || vdim < 4 || (vdim & 1) || pf < 1)
+        return fail(TG3_ERR_ARG, "bad PrepareTF arguments");
+    int dev = 0;
+    TG3_CUDA(cudaGetDevice(&dev));
+    static std::mutex mu;
+    static tg3_ctx* ctxs[64] = {};
+    if (dev < 0 || dev >= 64) return fail(TG3_ERR_ARG, "device ordinal out of range");
+    tg3_ctx* c = nullptr;
+    int st = TG3_OK;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!ctxs[dev] && (st = tg3_ctx_create(&ctxs[dev], dev))) return st;
+        c = ctxs[dev];
+    }
+    if ((st = tg3_ctx_insert_begin(c, vdim, pf))) return st;
+    const size_t n = (size_t)vdim * vdim * (vdim / 2 + 1);
+    float* d = (float*)ws_get(c, WS_D2H, sizeof(float) * 3 * n, &st);
+    if (!d) return st;
+    cudaStream_t s = c->stream;
+    TG3_CUDA(cudaMemcpyAsync(d, F3D, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(d + 2 * n, T3D, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    if ((st = tg3_ctx_insert_load_d(c, d, d + 2 * n))) return st;
+    if ((st = tg3_ctx_prepare_tf_d(c, symMat, nSym, maxRadius, 1))) return st;
+    if ((st = tg3_ctx_insert_read_d(c, d, d + 2 * n, 0))) return st;
+    TG3_CUDA(cudaMemcpyAsync(F3D, d, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaMemcpyAsync(T3D, d + 2 * n, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    TG3_CUDA(cudaStreamSynchronize(s));
     return TG3_OK;
 }

@@ -4,8 +4,10 @@
  *
  * The signatures are those of gpu/interface/Interface.h (cited per function);
  * this file replaces the corresponding definitions of the reference's
- * gpu/interface/Interface.cpp.  Entry points outside this path (PrepareTF and
- * the reconstruction Expose* family) keep their reference definitions.
+ * gpu/interface/Interface.cpp.  Entry points outside this path (the
+ * reconstruction's Expose* family) keep their reference definitions; ReMask
+ * (the images' re-masking ahead of an expectation) and PrepareTF (the
+ * accumulators' normalisation and symmetrisation) are defined here.
  *
  * Insertion sums over the hemisphere's ranks inside the call, as the
  * reference's does (ncclAllReduce of F and T over the ranks of `hemi`,
@@ -452,6 +454,35 @@ void InsertI2D(Complex* F2D, RFLOAT* T2D, double* O2D, int* counter, MPI_Comm& h
     const size_t n = (size_t)nk * vdim * (vdim / 2 + 1);
     allreduce_sum(reinterpret_cast<float*>(F2D), 2 * n, hemi, "InsertI2D");
     allreduce_sum(T2D, n, hemi, "InsertI2D");
+}
+
+// gpu/interface/Interface.h:517-522: every image's transform re-masked in place
+void ReMask(std::vector<Image>& img, RFLOAT maskRadius, RFLOAT pixelSize, RFLOAT ew, int idim,
+            int imgNum)
+{
+    std::vector<float*> p((size_t)imgNum);
+    for (int i = 0; i < imgNum; i++) p[(size_t)i] = reinterpret_cast<float*>(&img[(size_t)i][0]);
+    ok("ReMask", tg3_ReMask(p.data(), imgNum, idim, maskRadius, pixelSize, ew));
+}
+
+// gpu/interface/Interface.h:320-326: T3D is a complex Volume whose real
+// parts hold T; the symmetry matrices come as Eigen dmat33 (column-major,
+// Reconstructor::prepareTFG, src/Reconstructor.cpp:1020-1052) and are passed
+// on row-major.
+void PrepareTF(int gpuIdx, Volume& F3D, Volume& T3D, double* symMat, int nSymmetryElement,
+               int maxRadius, int pf)
+{
+    (void)gpuIdx;
+    const size_t n = F3D.sizeFT();
+    std::vector<RFLOAT> T(n);
+    for (size_t i = 0; i < n; i++) T[i] = REAL(T3D[i]);
+    std::vector<double> rowMajor((size_t)9 * (nSymmetryElement > 0 ? nSymmetryElement : 0));
+    for (int e = 0; e < nSymmetryElement; e++)
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) rowMajor[9 * e + 3 * a + b] = symMat[9 * e + 3 * b + a];
+    ok("PrepareTF", tg3_PrepareTF(reinterpret_cast<float*>(&F3D[0]), T.data(), F3D.nSlcFT(),
+                                  rowMajor.data(), nSymmetryElement, maxRadius, pf));
+    for (size_t i = 0; i < n; i++) T3D[i] = COMPLEX(T[i], 0);
 }
 
 namespace {

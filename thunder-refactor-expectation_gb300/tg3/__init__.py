@@ -42,10 +42,11 @@ EXPORTS = [
     "tg3_thu_read", "tg3_thu_write",
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
     "tg3_ctx_set_references", "tg3_learned_expect_d", "tg3_ExpectLearned3D",
-    "tg3_InsertFT_classes",
+    "tg3_InsertFT_classes", "tg3_remask_d", "tg3_ReMask", "tg3_ctx_prepare_tf_d",
+    "tg3_PrepareTF",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused", "network",
-          "fallback")
+          "fallback", "fallback_cross")
 OPT_FUSED = 0
 OPT_INSERT_GATHER = 1
 OPT_BANK_GATHER = 2
@@ -89,6 +90,10 @@ def lib():
             "tg3_ExpectGlobal3D": ([_P] * 11 + [_I] * 6, _I),
             "tg3_InsertFT": ([_P] * 15 + [_F, _I, _I, _I, _I, _I, _I, _I, _I], _I),
             "tg3_InsertFT_classes": ([_P] * 16 + [_F, _I, _I, _I, _I, _I, _I, _I, _I], _I),
+            "tg3_remask_d": ([_P, _P, _I, _I, _F, _F, _P], _I),
+            "tg3_ReMask": ([_P, _I, _I, _F, _F, _F], _I),
+            "tg3_ctx_prepare_tf_d": ([_P, _P, _I, _I, _I], _I),
+            "tg3_PrepareTF": ([_P, _P, _I, _P, _I, _I, _I], _I),
             "tg3_volume_create": ([_P, _P, _I, _I], _I),
             "tg3_volume_destroy": ([_P], _I),
             "tg3_ExpectLocal3D": ([_P, _P, _P, _P, _P, _P, _I, _I, _P, _I, _P, _I, _P, _P, _D,
@@ -399,6 +404,27 @@ class Context:
                                 ptr(trans), ptr(offset), ptr(group), n_group, int(by_group),
                                 r_sig, float(mask_radius), float(pixel_size), ptr(sig),
                                 ptr(sig_rcp)))
+
+    def remask(self, img_ft, mask_radius_px, out=None, edge_width=6.0):
+        """Re-mask image transforms img_ft (device complex64 (n, N, N/2 + 1),
+        centre at index 0) into out (a new tensor unless given)."""
+        if out is None:
+            import torch
+            out = torch.empty_like(img_ft)
+        self._hold(img_ft, out)
+        check(lib().tg3_remask_d(self.h, ptr(img_ft), img_ft.shape[0], img_ft.shape[-2],
+                                 float(mask_radius_px), float(edge_width), ptr(out)))
+        return out
+
+    def prepare_tf(self, sym_mats, max_radius, normalise=True):
+        """Normalise (1 / T at the origin) and symmetrise the insertion
+        accumulators in place; sym_mats: (nSym, 3, 3) rotations besides the
+        identity (host), or None."""
+        m = np.ascontiguousarray(np.zeros((0, 9)) if sym_mats is None else sym_mats,
+                                 dtype=np.float64).reshape(-1, 9)
+        check(lib().tg3_ctx_prepare_tf_d(self.h, ptr(m) if len(m) else None, len(m),
+                                         int(max_radius), int(bool(normalise))))
+        self.sync()
 
     def insert_load(self, F, T):
         """Accumulator <- F (complex64) and T (float32), device half grids."""
