@@ -831,6 +831,12 @@ def run_prep(args, rank, world, local_rank):
     return res
 
 
+# the rescoring cross term's kernel under each TG3_OPT_BANK_GATHER value
+BANK_KERNELS = {0: "k_gemm_bank_cp (bank rows gathered by cp.async)",
+                1: "k_gemm_bf16x3 (rows copied out of the banks first)",
+                2: "k_gemm_bank_bf16x3 (bank rows gathered by TMA)"}
+
+
 def run_bank(args, rank, world, local_rank):
     """The learned E-step's rescoring on its own: one box-256 class (200-blob
     map, cutoff 80, K = 9,930), its projection bank at the 6,912 global
@@ -879,8 +885,9 @@ def run_bank(args, rank, world, local_rank):
         ctx.local_phase_bank(nP, nR, nT, ps.dat, ps.ctf, ps.sigRcp, idx_d, trans, pR, pT, pC,
                              cls, o["wC"], o["wR"], o["wT"], o["base"], None, tg3.SCORE_BF16X3)
 
-    def timed(form):
+    def timed(form, order):
         ctx.set_option(tg3.OPT_BANK_GATHER, int(form))
+        ctx.set_option(tg3.OPT_BANK_ORDER, int(order))
         for _ in range(args.warmup):
             step()
         ctx.sync()
@@ -902,9 +909,13 @@ def run_bank(args, rank, world, local_rank):
         best = o["wR"].argmax(1).cpu().numpy()
         return reduce_max(world, e0.elapsed_time(e1)) / args.steps, st, clocks, best
 
-    ms_g, st_g, _, best_g = timed(1)          # rows copied out, then the GEMM
-    ms_t, st_t, _, best_t = timed(2)          # in-GEMM rows, TMA gathers
-    ms, st, clocks, best = timed(0)           # in-GEMM rows, the warps' own loads
+    # every form, the headline one (--bank-form, --bank-order) last
+    main = (args.bank_form, args.bank_order)
+    others = {}
+    for form, order in ((1, 0), (2, 0), (2, 1), (0, 0), (0, 1)):
+        if (form, order) != main:
+            others[(form, order)] = timed(form, order)
+    ms, st, clocks, best = timed(*main)
     K, Kp = len(ps.iCol), ctx_kp(len(ps.iCol))
     hbm, bf16, kind = peaks()
     cross_ms = st["cross"][0] / max(st["cross"][1], 1)
@@ -920,7 +931,8 @@ def run_bank(args, rank, world, local_rank):
                                   f"box-{box} class, bank of {len(qg)} rotations, K = {K}",
                       "l2": "inputs larger than L2 (bank 0.55 GB)"},
            "clocks": clocks,
-           "roofline": {"kernel": "k_gemm_bank_bf16x3", "bound": "hbm", "achieved": round(ach, 1),
+           "roofline": {"kernel": BANK_KERNELS[main[0]], "bound": "hbm",
+                        "achieved": round(ach, 1),
                         "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4),
                         "peak_source": f"hbm_gbs, {kind} (MEASURED_PEAKS.json)",
                         "traffic": None, "algorithmic_bytes_per_launch": algo,
@@ -928,17 +940,19 @@ def run_bank(args, rank, world, local_rank):
                         "tflops_algorithmic": round(4.0 * K * nP * nR * nT / (cross_ms * 1e-3)
                                                     / 1e12, 2)},
            "stages": {k: round(v[0] / max(v[1], 1), 4) for k, v in st.items() if v[1]},
-           "gather_form": {"ms_per_step": round(ms_g, 4),
-                           "stages": {k: round(v[0] / max(v[1], 1), 4) for k, v in st_g.items()
-                                      if v[1]},
-                           "same_best_rotation": round(float(np.mean(best == best_g)), 4)},
-           "tma_gather_form": {"ms_per_step": round(ms_t, 4),
-                               "stages": {k: round(v[0] / max(v[1], 1), 4)
-                                          for k, v in st_t.items() if v[1]},
-                               "same_best_rotation": round(float(np.mean(best == best_t)), 4)},
-           "speedup_vs_gather_form": round(ms_g / ms, 3),
+           "bank_form": {"form": main[0], "order": main[1],
+                         "what": "TG3_OPT_BANK_GATHER (0: cp.async gathers in the cross term, "
+                                 "1: rows copied out then the GEMM, 2: TMA gathers in the cross "
+                                 "term) and TG3_OPT_BANK_ORDER (particles sorted by first "
+                                 "proposed row)"},
+           "other_forms": {f"form{f}_order{r}": {
+               "ms_per_step": round(v[0], 4),
+               "stages": {k: round(x[0] / max(x[1], 1), 4) for k, x in v[1].items() if x[1]},
+               "same_best_rotation": round(float(np.mean(best == v[3])), 4)}
+               for (f, r), v in others.items()},
+           "speedup_vs_copy_form": round(others[(1, 0)][0] / ms, 3) if (1, 0) in others else 1.0,
            "median_error_best_deg": round(float(np.median(err)), 3),
-           "gpu_launches": 4 * args.steps}
+           "gpu_launches": (5 if main[0] == 1 else 4 + main[1]) * args.steps}
     ctx.close()
     return res
 
@@ -1271,7 +1285,8 @@ def run_learned(args, rank, world, local_rank):
     K = len(iCol)
     noise_var = synth.signal_power(maps[:nTr], box, px, rU, rL, device=dev) / L["snr_lik"] / 2.0
     ctx = tg3.Context(local_rank)
-    ctx.set_option(tg3.OPT_BANK_GATHER, 1 if args.bank_gather else 0)
+    ctx.set_option(tg3.OPT_BANK_GATHER, args.bank_form)
+    ctx.set_option(tg3.OPT_BANK_ORDER, args.bank_order)
     for c, bm in enumerate(maps):
         ctx.set_volume(c, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
     ctx.set_pixels(iCol, iRow, box)
@@ -1356,7 +1371,7 @@ def run_learned(args, rank, world, local_rank):
         emb[c] = learned.reference_embeddings(net, learned.render_references(ctx, c, quats_g, box))
         torch.cuda.synchronize()
         embed_ms[c] = (time.perf_counter() - ta) * 1e3
-    ctx.set_pixels(iCol, iRow, box)          # the renders used the image grid
+    ctx.set_pixels(iCol, iRow, box)          # the particles' pixel set, for the banks
     for c in classes:
         ctx.sync()
         ta = time.perf_counter()
@@ -1426,11 +1441,15 @@ def run_learned(args, rank, world, local_rank):
     clk = ClockSampler(local_rank)
     clk.start()
     e0, e1 = ev(), ev()
+    # an NVTX range around the timed steps: profilers select its kernels
+    # (ncu --nvtx --nvtx-include "learned_step/")
+    torch.cuda.nvtx.range_push("learned_step")
     e0.record(stream)
     for _ in range(args.steps):
         learned_step()
     e1.record(stream)
     e1.synchronize()
+    torch.cuda.nvtx.range_pop()
     clocks = clk.stop()
     torch.cuda.synchronize()
     barrier(world)
@@ -1438,9 +1457,18 @@ def run_learned(args, rank, world, local_rank):
     st_l = ctx.stage_times(reset=True)
     ctx.set_timing(False)
     # the other rescoring form on the same step, stage-timed (not the headline)
-    ab = None
-    if not args.bank_gather:
-        ctx.set_option(tg3.OPT_BANK_GATHER, 1)
+    ab = {"timed_form": {"bank_form": args.bank_form, "bank_order": args.bank_order,
+                         "ms_per_step": round((st_l["project"][0] if "project" in st_l else 0.0)
+                                              / args.steps + st_l["cross"][0] / args.steps, 4)},
+          "note": "rescoring of the same step, slices copied out of the banks then the cross "
+                  "term (TG3_OPT_BANK_GATHER 1) and the cross term reading the proposed bank "
+                  "rows itself (0: cp.async gathers, 2: TMA gathers; TG3_OPT_BANK_ORDER: "
+                  "particles sorted by first proposed row); project + cross stages"}
+    for form, order in ((1, 0), (0, 0), (0, 1), (2, 1)):
+        if (form, order) == (args.bank_form, args.bank_order):
+            continue
+        ctx.set_option(tg3.OPT_BANK_GATHER, form)
+        ctx.set_option(tg3.OPT_BANK_ORDER, order)
         learned_step()
         ctx.set_timing(True)
         ctx.stage_times(reset=True)
@@ -1448,12 +1476,10 @@ def run_learned(args, rank, world, local_rank):
             learned_step()
         st_g = ctx.stage_times(reset=True)
         ctx.set_timing(False)
-        ctx.set_option(tg3.OPT_BANK_GATHER, 0)
-        ab = {"gather_then_gemm_ms_per_step": round((st_g["project"][0] + st_g["cross"][0]) / 2, 4),
-              "bank_rows_in_gemm_ms_per_step": round(st_l["cross"][0] / args.steps, 4),
-              "note": "rescoring of the same step: slices copied out of the banks then the "
-                      "cross term (TG3_OPT_BANK_GATHER) against the cross term reading the "
-                      "proposed bank rows itself"}
+        ab[f"form{form}_order{order}_ms_per_step"] = round(
+            ((st_g["project"][0] if "project" in st_g else 0.0) + st_g["cross"][0]) / 2, 4)
+    ctx.set_option(tg3.OPT_BANK_GATHER, args.bank_form)
+    ctx.set_option(tg3.OPT_BANK_ORDER, args.bank_order)
     fb = out["fellBack"].cpu().numpy().astype(bool)
     q_l = out["bestQuat"].cpu().numpy()
     t_l = out["bestTrans"].cpu().numpy()
@@ -1490,11 +1516,13 @@ def run_learned(args, rank, world, local_rank):
     clk_p = ClockSampler(local_rank)
     clk_p.start()
     barrier(world)
+    torch.cuda.nvtx.range_push("plain_step")
     e0.record(stream)
     for _ in range(plain_steps):
         plain_step()
     e1.record(stream)
     e1.synchronize()
+    torch.cuda.nvtx.range_pop()
     clocks_p = clk_p.stop()
     tp_ms = reduce_max(world, e0.elapsed_time(e1))
     q_p = np.empty((n, 4))
@@ -1595,7 +1623,7 @@ def run_learned(args, rank, world, local_rank):
     # the learned step's kernels against their rooflines; the dominant one
     # is the line's roofline
     dom, roofs = learned_rooflines(st_l, args.steps, n, nRot, nTrans, K, ctx_kp(K),
-                                   int(fb.sum()), nRg, nTg, not args.bank_gather, ms_step)
+                                   int(fb.sum()), nRg, nTg, args.bank_form, ms_step)
     roof = dict(roofs[dom]) if dom else {"kernel": None, "note": "no stage timed"}
     res = {
         "metric": METRIC, "value": round(v_l, 1), "unit": UNIT, "n_gpus": world,
@@ -1626,7 +1654,8 @@ def run_learned(args, rank, world, local_rank):
                 "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "wall_s": round(e2e_s, 3), "entry": "tg3_ExpectLearned3D (host buffers)",
                 "same_poses_as_device_entry": e2e_same},
-        "gpu_launches": learned_launches(fb, unseen.cls, not args.bank_gather) * args.steps,
+        "gpu_launches": learned_launches(fb, unseen.cls, args.bank_form != 1,
+                                         args.bank_order and args.bank_form != 1) * args.steps,
         "roofline": roof,
         "roofline_kernels": roofs,
         "rescoring_forms": ab,
@@ -1687,16 +1716,16 @@ def run_learned(args, rank, world, local_rank):
     return res
 
 
-def learned_rooflines(st, steps, n, nRot, nTrans, K, Kp, nfb, nRg, nTg, bank_gemm, step_ms):
+def learned_rooflines(st, steps, n, nRot, nTrans, K, Kp, nfb, nRg, nTg, bank_form, step_ms):
     """Rooflines of the learned step's kernels, from the stage times of the
     timed steps (CUDA events on the library's stream), and the dominant one.
     - rescoring slice gather (TG3_OPT_BANK_GATHER form): per proposed row its
       hi and lo bf16 rows (4 Kp bytes) and |P|^2 row (4 K) in, the operand
       rows (4 Kp) out;
-    - rescoring cross term: with the bank-row kernel, per launch the proposed
-      rows' planes (4 Kp bytes a row), the shifted data (4 Kp a translation)
-      and the log-likelihoods (4 bytes a hypothesis): HBM-bound; otherwise
-      4 K FLOP per hypothesis (split: 3x that in bf16);
+    - rescoring cross term (every form): per launch the proposed rows' planes
+      (4 Kp bytes a row), the shifted data (4 Kp a translation) and the
+      log-likelihoods (4 bytes a hypothesis): HBM-bound (4 K FLOP per
+      hypothesis, 3x that in bf16, is far below the tensor cores' rate);
     - fallback cross term (the global search of the fallback particles):
       4 K FLOP per hypothesis, nRg x nTg per fallback particle."""
     hbm, bf16, src = peaks()
@@ -1710,25 +1739,16 @@ def learned_rooflines(st, steps, n, nRot, nTrans, K, Kp, nfb, nRg, nTg, bank_gem
             "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4),
             "traffic": None, "algorithmic_bytes_per_launch": algo / steps}
     if tot("cross") > 0:
-        if bank_gemm:
-            algo = (float(n) * nRot * 4.0 * Kp + float(n) * nTrans * 4.0 * Kp
-                    + float(n) * nRot * nTrans * 4.0) * steps
-            ach = algo / (tot("cross") * 1e-3) / 1e9
-            out["rescoring_cross"] = {
-                "kernel": "k_gemm_bank_bf16x3 (rescoring cross term, proposed rows gathered "
-                          "from the banks by TMA)", "bound": "hbm", "achieved": round(ach, 1),
-                "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": None,
-                "algorithmic_bytes_per_launch": algo / steps,
-                "tflops_algorithmic": round(4.0 * K * n * nRot * nTrans * steps
-                                            / (tot("cross") * 1e-3) / 1e12, 2)}
-        else:
-            flop = 4.0 * K * n * nRot * nTrans * steps
-            ach = flop / (tot("cross") * 1e-3) / 1e12
-            out["rescoring_cross"] = {
-                "kernel": "k_gemm_bf16x3 (rescoring cross term)", "bound": "tensor",
-                "achieved": round(ach, 2), "peak": bf16, "unit": "TFLOP/s",
-                "frac": round(ach / bf16, 4), "traffic": None,
-                "algorithmic_flop_per_launch": flop / steps}
+        # every form streams the proposed rows' planes: HBM-bound
+        algo = (float(n) * nRot * 4.0 * Kp + float(n) * nTrans * 4.0 * Kp
+                + float(n) * nRot * nTrans * 4.0) * steps
+        ach = algo / (tot("cross") * 1e-3) / 1e9
+        out["rescoring_cross"] = {
+            "kernel": BANK_KERNELS[bank_form], "bound": "hbm", "achieved": round(ach, 1),
+            "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": None,
+            "algorithmic_bytes_per_launch": algo / steps,
+            "tflops_algorithmic": round(4.0 * K * n * nRot * nTrans * steps
+                                        / (tot("cross") * 1e-3) / 1e12, 2)}
     if tot("fallback_cross") > 0 and nfb > 0:
         flop = 4.0 * K * nfb * nRg * nTg * steps
         ach = flop / (tot("fallback_cross") * 1e-3) / 1e12
@@ -1749,17 +1769,18 @@ def learned_rooflines(st, steps, n, nRot, nTrans, K, Kp, nfb, nRg, nTg, bank_gem
     return dom, out
 
 
-def learned_launches(fb, cls, bank_gemm):
+def learned_launches(fb, cls, bank_gemm, order=False):
     """Kernels of one learned E-step (this library's own): network 17 (8
     weight repacks, the first convolution, 6 tensor-core layers, the split-K
     sum, the output layer), matching 1, priors 3, rescoring 4 with the
     bank-row cross term (shift bank, |X|^2, cross term, weights; 5 with the
-    slice gather), confidence and best pose 2; per class with fallback
+    slice gather or with the particles' visiting order sorted first),
+    confidence and best pose 2; per class with fallback
     particles 13 (3 gathers, priors, |P|^2, translations, shift bank, |X|^2,
     norm operand, norm GEMM, cross term, weights, best pose) and 1 for the
     translation priors."""
     k = len(np.unique(np.asarray(cls)[np.asarray(fb, bool)]))
-    return 17 + 1 + 3 + (4 if bank_gemm else 5) + 2 + (13 * k + 1 if k else 0)
+    return 17 + 1 + 3 + (4 + int(bool(order)) if bank_gemm else 5) + 2 + (13 * k + 1 if k else 0)
 
 
 def _fp64_bank_rows(job):
@@ -2213,9 +2234,11 @@ def main():
                     help="particles whose proposals are checked against the FP64 oracle")
     ap.add_argument("--cpu-sample-global", type=int, default=96,
                     help="rotations per particle in the CPU global-search sample")
-    ap.add_argument("--bank-gather", action="store_true",
-                    help="learned workloads: rescoring slices copied out of the banks before "
-                         "the cross term (TG3_OPT_BANK_GATHER) instead of read by it")
+    ap.add_argument("--bank-form", type=int, default=0, choices=[0, 1, 2],
+                    help="rescoring form (TG3_OPT_BANK_GATHER): 0 cross term gathers the bank "
+                         "rows with cp.async, 1 rows copied out first, 2 TMA gathers")
+    ap.add_argument("--bank-order", type=int, default=1, choices=[0, 1],
+                    help="TG3_OPT_BANK_ORDER: particles visited sorted by first proposed row")
     ap.add_argument("--no-local", action="store_true",
                     help="learned workloads: skip the local-phase measurement beside them")
     ap.add_argument("--save-net", default=None,

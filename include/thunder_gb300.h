@@ -155,6 +155,23 @@ int tg3_ExpectLocal3D(tg3_volume* vol, const float* dat, const float* ctf,
                       const double* trans, int nT, const double* oldR,
                       const double* oldT, double oldC, float* wC, float* wR,
                       float* wT, float* dvp, float* baseL);
+
+/* The same for 2-D classification's local phase, the combined work of
+ * ExpectLocalV2D + ExpectLocalRTD + ExpectLocalPreI2D + ExpectLocalM
+ * (gpu/interface/Interface.h:40-43, 80-105, 125-139): the nR in-plane
+ * rotations rot [nR][2] = (cos, sin) of a class image (sampled bilinearly
+ * at (c i pf - s j pf, s i pf + c j pf), kernel_Project2DL,
+ * gpu/src/Kernel.cu:750-778), otherwise as tg3_ExpectLocal3D.  The class
+ * image handle holds img [vdim][vdim/2 + 1] (complex, host at creation),
+ * padded by pf. */
+typedef struct tg3_image tg3_image;
+int tg3_image_create(tg3_image** img, const float* data, int vdim, int pf);
+int tg3_image_destroy(tg3_image* img);
+int tg3_ExpectLocal2D(tg3_image* img, const float* dat, const float* ctf,
+                      const float* sigRcp, const int* iCol, const int* iRow, int npxl,
+                      int idim, const double* rot, int nR, const double* trans, int nT,
+                      const double* oldR, const double* oldT, double oldC, float* wC,
+                      float* wR, float* wT, float* dvp, float* baseL);
 /* The same with the defocus search (cSearch; ExpectLocalP / RTD / PreI3D /
  * M of gpu/interface/Interface.h:50-139 with k1 != 0): the particle's CTF
  * for each of its nD defocus factors dpara is made on the device from its
@@ -309,8 +326,18 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  *   proposed rows.  1: copied into a slice buffer, their norms summed from
  *   the bank's |P|^2 rows, then the GEMM.  0: the GEMM's own warps load its
  *   operand tiles from the bank rows and sum the rows' norms from them
- *   (compensated FP32).  2: as 0 with the tiles loaded by TMA gathers. */
-enum { TG3_OPT_FUSED = 0, TG3_OPT_INSERT_GATHER = 1, TG3_OPT_BANK_GATHER = 2 };
+ *   (compensated FP32).  2: as 0 with the tiles loaded by TMA gathers.
+ * TG3_OPT_BANK_ORDER (default 0): 1 makes forms 0 and 2 above visit the
+ *   particles in the order of their first proposed row (class, then bank
+ *   row), so that the particles in flight together share bank rows in L2;
+ *   batches of more than 8,192 particles keep their own order.  The results
+ *   do not depend on it. */
+enum {
+    TG3_OPT_FUSED = 0,
+    TG3_OPT_INSERT_GATHER = 1,
+    TG3_OPT_BANK_GATHER = 2,
+    TG3_OPT_BANK_ORDER = 3
+};
 int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);
 
@@ -743,6 +770,16 @@ int tg3_ctf_d(const float* attr, int nImg, float pixelSize, int idim,
  * rotMat [nR][9] (double). */
 int tg3_project_d(tg3_ctx* ctx, int cls, const double* rotMat, int nR,
                   float* out);
+/* The learned E-step's reference images (no counterpart in the reference):
+ * out [n][img][img] float, the class-`cls` volume projected at rotMat [n][9]
+ * (double) over the img x img rfft grid of the volume's own frequencies
+ * (columns 0 .. img/2, rows -img/2 .. img/2 - 1, times pf), taken to real
+ * space (cuFFT C2R), centred (index 0 in the middle), minus its mean and
+ * over its unbiased standard deviation -- the particle images' form at the
+ * network's input.  img even, >= 8; the grid must lie inside the volume.
+ * Leaves the context's pixel set alone. */
+int tg3_ctx_render_references_d(tg3_ctx* ctx, int cls, const double* rotMat,
+                                int n, int img, float* out);
 
 #ifdef __cplusplus
 }

@@ -60,7 +60,7 @@ class ManagedCalPoint {
 public:
     void Init(int mode, int cSearch, int gpuIdx, int nR, int nT, int mD, int npxl)
     {
-        (void)mode;
+        mode_ = mode;
         (void)cSearch;
         (void)gpuIdx;
         (void)npxl;
@@ -71,9 +71,10 @@ public:
     int getNR() { return nR_; }
     int getNT() { return nT_; }
     int getMD() { return mD_; }
+    int getMode() { return mode_; }
 
 private:
-    int nR_ = 0, nT_ = 0, mD_ = 0;
+    int nR_ = 0, nT_ = 0, mD_ = 0, mode_ = 1;
 };
 
 void getAviDevice(std::vector<int>& gpus);
@@ -81,6 +82,7 @@ void ExpectPreidx(int gpuIdx, int** deviCol, int** deviRow, int* iCol, int* iRow
 void ExpectPrefre(int gpuIdx, RFLOAT** devfreQ, RFLOAT* freQ, int npxl);
 void ExpectLocalIn(int gpuIdx, Complex** devdatP, RFLOAT** devctfP, RFLOAT** devdefO,
                    RFLOAT** devsigP, int nPxl, int cpyNumL, int searchType);
+void ExpectLocalV2D(int gpuIdx, ManagedArrayTexture* mgr, Complex* volume, int dimSize);
 void ExpectLocalV3D(int gpuIdx, ManagedArrayTexture* mgr, Complex* volume, int vdim);
 void ExpectLocalP(int gpuIdx, Complex* devdatP, RFLOAT* devctfP, RFLOAT* devdefO,
                   RFLOAT* devsigP, Complex* datP, RFLOAT* ctfP, RFLOAT* defO, RFLOAT* sigP,
@@ -90,6 +92,10 @@ void ExpectLocalHostA(int gpuIdx, RFLOAT** wC, RFLOAT** wR, RFLOAT** wT, RFLOAT*
                       double** rot, double** dpara, int mR, int mT, int mD, int cSearch);
 void ExpectLocalRTD(int gpuIdx, ManagedCalPoint* mcp, double* oldR, double* oldT, double* oldD,
                     double* trans, double* rot, double* dpara);
+void ExpectLocalPreI2D(int gpuIdx, int datShift, ManagedArrayTexture* mgr, ManagedCalPoint* mcp,
+                       RFLOAT* devdefO, RFLOAT* devfreQ, int* deviCol, int* deviRow,
+                       RFLOAT phaseShift, RFLOAT conT, RFLOAT k1, RFLOAT k2, int pf, int idim,
+                       int vdim, int npxl, int interp);
 void ExpectLocalPreI3D(int gpuIdx, int datShift, ManagedArrayTexture* mgr, ManagedCalPoint* mcp,
                        RFLOAT* devdefO, RFLOAT* devfreQ, int* deviCol, int* deviRow,
                        RFLOAT phaseShift, RFLOAT conT, RFLOAT k1, RFLOAT k2, int pf, int idim,

@@ -9,7 +9,8 @@
  * (src/Optimiser.cpp:2212-2566): ExpectPreidx, ExpectLocalIn, ExpectLocalV3D
  * once; per image ExpectLocalP into a slot, ExpectLocalHostA,
  * ManagedCalPoint::Init, ExpectLocalRTD, ExpectLocalPreI3D, ExpectLocalM,
- * ExpectLocalHostF; then ExpectLocalFin and ExpectFreeIdx.  Insertion as
+ * ExpectLocalHostF; then ExpectLocalFin and ExpectFreeIdx.  Then the same in
+ * 2-D mode (ExpectLocalV2D, ExpectLocalPreI2D, in-plane rotations).  Insertion as
  * Reconstructor::insertI (src/Reconstructor.cpp:867-1000): the single-class
  * InsertFT, then the multi-class one with per-image draw counts, each into
  * zeroed volumes with O3D and the counter starting at zero.
@@ -126,6 +127,50 @@ int main(int argc, char** argv)
     save(dir, "out_wC.bin", outC.data(), outC.size());
     save(dir, "out_wR.bin", outR.data(), outR.size());
     save(dir, "out_wT.bin", outT.data(), outT.size());
+
+    // ------------------------------------------- 2-D local expectation
+    // (ExpectLocalV2D, then per image the same sequence with PreI2D and a
+    // ManagedCalPoint of mode 0, the rotations as (cos, sin) pairs)
+    {
+        const size_t n2 = (size_t)vdim * (vdim / 2 + 1);
+        auto img2 = load<Complex>(dir, "vol2d.bin", n2);
+        auto rot2 = load<double>(dir, "rot2d.bin", (size_t)nP * nR * 2);
+        ExpectPreidx(gpu, &deviCol, &deviRow, iCol.data(), iRow.data(), npxl);
+        ExpectLocalIn(gpu, &devdatP, &devctfP, &devdefO, &devsigP, npxl, slots, 0);
+        ManagedArrayTexture mgr2;
+        ExpectLocalV2D(gpu, &mgr2, img2.data(), (int)n2);
+        for (int l = 0; l < nP; l++) {
+            const int slot = l % slots;
+            ExpectLocalP(gpu, devdatP, devctfP, devdefO, devsigP, dat.data(), ctf.data(),
+                         nullptr, sig.data(), slot, l, npxl, 0);
+            RFLOAT *wC, *wR, *wT, *wD;
+            double *oldR, *oldT, *oldD, *trans, *rotq, *dpara;
+            ExpectLocalHostA(gpu, &wC, &wR, &wT, &wD, &oldR, &oldT, &oldD, &trans, &rotq, &dpara,
+                             nR, nT, 1, 0);
+            ManagedCalPoint mcp;
+            mcp.Init(0, 0, gpu, nR, nT, 1, npxl);
+            std::memcpy(rotq, &rot2[(size_t)l * nR * 2], sizeof(double) * nR * 2);
+            std::memcpy(trans, &trs[(size_t)l * nT * 2], sizeof(double) * nT * 2);
+            std::memcpy(oldR, &oR[(size_t)l * nR], sizeof(double) * nR);
+            std::memcpy(oldT, &oT[(size_t)l * nT], sizeof(double) * nT);
+            oldD[0] = 1;
+            dpara[0] = 1;
+            ExpectLocalRTD(gpu, &mcp, oldR, oldT, oldD, trans, rotq, dpara);
+            ExpectLocalPreI2D(gpu, slot, &mgr2, &mcp, devdefO, devfreQ, deviCol, deviRow, 0, 0, 0,
+                              0, pf, box, vdim, npxl, 1);
+            ExpectLocalM(gpu, slot, &mcp, devdatP, devctfP, devsigP, wC, wR, wT, wD, 1.0, npxl);
+            outC[l] = wC[0];
+            std::memcpy(&outR[(size_t)l * nR], wR, sizeof(RFLOAT) * nR);
+            std::memcpy(&outT[(size_t)l * nT], wT, sizeof(RFLOAT) * nT);
+            ExpectLocalHostF(gpu, &wC, &wR, &wT, &wD, &oldR, &oldT, &oldD, &trans, &rotq, &dpara,
+                             0);
+        }
+        ExpectLocalFin(gpu, &devdatP, &devctfP, &devdefO, &devfreQ, &devsigP, 0);
+        ExpectFreeIdx(gpu, &deviCol, &deviRow);
+        save(dir, "out2_wC.bin", outC.data(), outC.size());
+        save(dir, "out2_wR.bin", outR.data(), outR.size());
+        save(dir, "out2_wT.bin", outT.data(), outT.size());
+    }
 
     // ------------------------------------------------------------ insertion
     auto nr = load<double>(dir, "ins_rot.bin", (size_t)nP * mReco * 4);

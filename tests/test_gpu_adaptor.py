@@ -3,7 +3,8 @@ with a C++ driver (tests/adaptor/driver.cpp) against libtg3.so and called
 through the reference's own call sequences -- the local expectation
 (ExpectPreidx, ExpectLocalIn, ExpectLocalV3D, then per image ExpectLocalP,
 ExpectLocalHostA, ExpectLocalRTD, ExpectLocalPreI3D, ExpectLocalM,
-ExpectLocalHostF; ExpectLocalFin, ExpectFreeIdx) and both InsertFT forms
+ExpectLocalHostF; ExpectLocalFin, ExpectFreeIdx), the same in 2-D mode
+(ExpectLocalV2D, ExpectLocalPreI2D) and both InsertFT forms
 (single class; multi-class with per-image draw counts nC).  What the caller
 receives is compared with the oracle:
 - the marginal weights wR, wT as distributions within 2e-3 and the same best
@@ -65,7 +66,10 @@ def run(tmp_path_factory):
              ins_rot=synth.haar_quaternions(rng, nP * mReco).reshape(nP, mReco, 4),
              ins_trans=rng.uniform(-2, 2, (nP, mReco, 2)), offs=rng.uniform(-0.5, 0.5, (nP, 2)),
              w=(rng.random(nP) + 0.5).astype(np.float32),
-             nc=np.array([3, 0, 1, 2, 3, 1], np.int32))
+             nc=np.array([3, 0, 1, 2, 3, 1], np.int32),
+             img2d=synth.class_images_2d([bm], box, pf)[0].cpu().numpy().astype(np.complex64))
+    ang = rng.uniform(0, 2 * np.pi, (nP, nR))
+    c["rot2d"] = np.stack([np.cos(ang), np.sin(ang)], -1)
     (d / "meta.txt").write_text(f"{box} {pf} {st.K} {nP} {nR} {nT} {mReco}\n")
     for name, a, dt in (("vol", vol, np.complex64), ("icol", st.iCol, np.int32),
                         ("irow", st.iRow, np.int32), ("dat", c["dat"], np.complex64),
@@ -75,7 +79,8 @@ def run(tmp_path_factory):
                         ("ins_rot", c["ins_rot"], np.float64),
                         ("ins_trans", c["ins_trans"], np.float64),
                         ("offs", c["offs"], np.float64), ("w", c["w"], np.float32),
-                        ("nc", c["nc"], np.int32)):
+                        ("nc", c["nc"], np.int32), ("vol2d", c["img2d"], np.complex64),
+                        ("rot2d", c["rot2d"], np.float64)):
         np.ascontiguousarray(a, dt).tofile(d / f"{name}.bin")
     outs = {}
     for ranks in (1, 2):
@@ -85,6 +90,8 @@ def run(tmp_path_factory):
         vd = box * pf
         shape = (vd, vd, vd // 2 + 1)
         o = {k: np.fromfile(d / f"out_{k}.bin", np.float32) for k in ("wC", "wR", "wT")}
+        o.update({"2" + k: np.fromfile(d / f"out2_{k}.bin", np.float32)
+                  for k in ("wC", "wR", "wT")})
         for form in (1, 2):
             o[f"F{form}"] = np.fromfile(d / f"out_F{form}.bin", np.complex64).reshape(shape)
             o[f"T{form}"] = np.fromfile(d / f"out_T{form}.bin", np.float32).reshape(shape)
@@ -109,6 +116,28 @@ def test_local_sequence_matches_the_oracle(run):
         assert np.abs(wT[l] / wT[l].sum() - ref["wT"] / ref["wT"].sum()).max() < 2e-3
         assert np.argmax(wR[l]) == np.argmax(ref["wR"])
         assert np.argmax(wT[l]) == np.argmax(ref["wT"])
+
+
+def test_local_sequence_2d_matches_the_oracle(run):
+    """The 2-D local sequence (ExpectLocalV2D, ExpectLocalPreI2D, in-plane
+    rotations) against the oracle's bilinear projection and likelihood."""
+    c, outs = run
+    o, st = outs[1], c["st"]
+    nP, nR, nT = c["nP"], c["nR"], c["nT"]
+    wR = o["2wR"].reshape(nP, nR).astype(np.float64)
+    wT = o["2wT"].reshape(nP, nT).astype(np.float64)
+    img = f32(c["img2d"])
+    for l in range(nP):
+        P = O.project2d(img, c["rot2d"][l], st.iCol, st.iRow, c["pf"])
+        S = O.translate(f32(c["trans"][l]), c["box"], st.iCol, st.iRow)
+        X, cc, ss = f32(c["dat"][l]), f32(c["ctf"][l]), f32(c["sig"][l])
+        L = np.array([[O.logdvp(X, S[t] * P[r], cc, ss) for t in range(nT)] for r in range(nR)])
+        w = np.exp(L - L.max()) * c["oldR"][l][:, None] * c["oldT"][l][None, :]
+        rR, rT = w.sum(1), w.sum(0)
+        assert np.abs(wR[l] / wR[l].sum() - rR / rR.sum()).max() < 2e-3
+        assert np.abs(wT[l] / wT[l].sum() - rT / rT.sum()).max() < 2e-3
+        assert np.argmax(wR[l]) == np.argmax(rR)
+        assert np.argmax(wT[l]) == np.argmax(rT)
 
 
 def _oracle_insert(c, counts):

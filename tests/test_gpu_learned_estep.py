@@ -183,16 +183,19 @@ def test_host_form_matches_device_form(case):
     np.testing.assert_array_equal(h["fb"], r["fellBack"])
 
 
+@pytest.mark.parametrize("order", [0, 1])
 @pytest.mark.parametrize("form", [0, 2])
 @pytest.mark.parametrize("nR", [32, 160])
-def test_bank_rows_straight_into_the_cross_term(case, nR, form):
+def test_bank_rows_straight_into_the_cross_term(case, nR, form, order):
     """The split-bf16 bank-row local phase with the operand tiles loaded
-    straight from the banks (TMA gather, norms from the staged tiles)
-    against the form that first copies the rows out (TG3_OPT_BANK_GATHER 1;
-    form 0 loads the tiles with the warps' own loads, form 2 by TMA gathers),
-    and against the oracle: log-likelihoods within 1e-4 relative, the same
-    best hypothesis, marginals within 2e-3 as distributions.  nR = 160
-    leaves a partial second row tile."""
+    straight from the banks (norms from the staged tiles) against the form
+    that first copies the rows out (TG3_OPT_BANK_GATHER 1; form 0 gathers
+    the tiles with the warps' own cp.async copies, form 2 with TMA gathers),
+    with the particles visited in their own order and sorted by first
+    proposed row (TG3_OPT_BANK_ORDER), and against the oracle:
+    log-likelihoods within 1e-4 relative, the same best hypothesis,
+    marginals within 2e-3 as distributions.  nR = 160 leaves a partial
+    second row tile."""
     ps, ctx, n = case["ps"], case["ctx"], len(case["ps"].cls)
     nT = 9
     rng = np.random.default_rng(nR)
@@ -213,9 +216,11 @@ def test_bank_rows_straight_into_the_cross_term(case, nR, form):
         return {k: v.cpu().numpy() for k, v in o.items()}
 
     try:
+        ctx.set_option(tg3.OPT_BANK_ORDER, order)
         a, b = run(form), run(1)
     finally:
         ctx.set_option(tg3.OPT_BANK_GATHER, 1)
+        ctx.set_option(tg3.OPT_BANK_ORDER, 0)
     assert np.max(np.abs(a["dvp"] - b["dvp"]) / np.abs(b["dvp"])) < 1e-5
     for l in range(n):
         assert np.argmax(a["dvp"][l]) == np.argmax(b["dvp"][l])
@@ -233,3 +238,32 @@ def test_bank_rows_straight_into_the_cross_term(case, nR, form):
         assert np.argmax(a["dvp"][l]) == np.argmax(ref["dvp"])
         for k in ("wR", "wT"):
             assert np.abs(a[k][l] / a[k][l].sum() - ref[k] / ref[k].sum()).max() < 2e-3
+
+
+def test_reference_rendering_matches_the_torch_form():
+    """tg3_ctx_render_references_d (projection over the image's rfft grid,
+    cuFFT C2R, centring, normalisation, all in the library) against the
+    same steps written with the context's projection and torch.fft: equal
+    to float32 rounding, and the context's pixel set untouched."""
+    rng = np.random.default_rng(12)
+    box, px, pf, img = 128, 1.4, 2, 64
+    bm = synth.blob_map(rng, 60, (1.5, 3.0), px, 40.0)
+    ctx = tg3.Context(0)
+    try:
+        ctx.set_volume(0, synth.padded_volume(bm, box, pf, device=DEV, dtype=torch.float32), pf)
+        q = synth.haar_quaternions(rng, 37)
+        got = learned.render_references(ctx, 0, q, box, img)
+        iCol, iRow = learned.image_grid(img)
+        ctx.set_pixels(iCol, iRow, box)
+        R = torch.as_tensor(synth.quat_to_mat(q).reshape(len(q), 9)).to(DEV)
+        P = torch.empty((len(q), len(iCol)), dtype=torch.complex64, device=DEV)
+        ctx.project(0, R, len(q), P)
+        ctx.sync()
+        ims = torch.fft.irfft2(P.view(len(q), img, img // 2 + 1), s=(img, img))
+        ims = torch.fft.fftshift(ims, dim=(-2, -1))
+        ims = ims - ims.mean(dim=(-2, -1), keepdim=True)
+        want = ims / ims.std(dim=(-2, -1), keepdim=True)
+        assert torch.isfinite(got).all()
+        assert (got - want).abs().max().item() < 1e-4
+    finally:
+        ctx.close()

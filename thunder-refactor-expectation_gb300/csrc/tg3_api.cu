@@ -565,9 +565,15 @@ static int local_phase(tg3_ctx* c, const int* bankIdx, int nP, int nR, int nT, c
         }
         {
             StageTimer tm(c, TG3_STAGE_CROSS);
+            int* order = nullptr;
+            if (c->bankOrder && nP <= 8192) {
+                int ost = TG3_OK;
+                order = (int*)ws_get(c, WS_ORDER, sizeof(int) * (size_t)nP, &ost);
+                if (!order) return ost;
+            }
             TG3_CUDA(launch_gemm_bank_bf16x3(c->bank, c->px.gen, bankIdx, cls, nP, nR, A, nT, Kp,
                                              K, sigRcp, ctf, D, -2.0f, c->d_flag, s,
-                                             c->bankGather == 2));
+                                             c->bankGather == 2, order));
         }
         {
             StageTimer tm(c, TG3_STAGE_WEIGHTS);
@@ -1788,6 +1794,7 @@ extern "C" int tg3_ctx_set_option(tg3_ctx* c, int option, int value)
         if (value < 0 || value > 2) return fail(TG3_ERR_ARG, "TG3_OPT_BANK_GATHER takes 0, 1 or 2");
         c->bankGather = value;
     }
+    else if (option == TG3_OPT_BANK_ORDER) c->bankOrder = value != 0;
     else return fail(TG3_ERR_ARG, "unknown option");
     return TG3_OK;
 }

@@ -58,6 +58,7 @@ struct BgParams {
     int ntile, tmemCols, stages;
     const int* idx;                // [nP][nR] bank rows
     const int* cls;                // [nP] (null: class 0)
+    const int* order;              // [nP] particle of each grid row (null: identity)
     const float* sigRcp;           // [nP][K]
     const float* ctf;              // [nP][K]
     float* C;                      // [nP][nR][nT]
@@ -108,7 +109,7 @@ k_gemm_bank_bf16x3(const __grid_constant__ BankMaps maps, const __grid_constant_
     int* rows = abortFlag + 1;                            // [BG_M] bank rows of the tile
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int mtile = blockIdx.x, item = blockIdx.y;
+    const int mtile = blockIdx.x, item = p.order ? p.order[blockIdx.y] : blockIdx.y;
     const int cl = p.cls ? p.cls[item] : 0;
     const bool clOk = cl >= 0 && cl < kMaxClasses && maps.nB[cl] > 0;
     const int k = clOk ? cl : 0;
@@ -307,25 +308,34 @@ k_gemm_bank_bf16x3(const __grid_constant__ BankMaps maps, const __grid_constant_
 }
 
 
-// The same product with the A tiles loaded by the four norm warps
-// themselves: per K block every thread loads 16 bytes of each plane of 8
-// rows (8 lanes cover a row's 128-byte chunk, so a warp instruction reads 4
-// whole rows' chunks), stores them at their swizzled places, and adds the
-// rows' |P|^2 weighted by sigRcp ctf^2 to its partial norms in compensated
-// FP32; the 8 lanes' partials are summed at the end.  The next K block's
-// loads are issued before the current one is stored (two register sets).
-// A stage is full when the four warps have stored their share (one arrival
-// each) and the B tiles' bytes have landed (TMA, warp 4 lane 0); it is free
-// when the MMAs that read it have completed.
+// The same product with the A tiles gathered by the four norm warps
+// themselves with cp.async: per K block every thread copies 16 bytes of each
+// plane of 8 rows straight to their swizzled places in shared memory (8
+// lanes cover a row's 128-byte chunk, so a warp instruction reads 4 whole
+// rows' chunks), with no register staging, so that all S stages' copies can
+// be in flight at once.  Once the thread's own copies of a K block have
+// landed (cp.async.wait_group S-1) it adds their |P|^2, weighted by sigRcp
+// ctf^2, to its partial norms in compensated FP32 (the 8 lanes' partials are
+// summed at the end), makes them visible to the tensor cores (proxy fence)
+// and arrives.  A stage is full when the four warps have arrived and the B
+// tiles' bytes have landed (TMA, warp 4 lane 0); it is free when the MMAs
+// that read it have completed.
 struct LdgRows {
     const __nv_bfloat16* hi[kMaxClasses];
     const __nv_bfloat16* lo[kMaxClasses];
     int nB[kMaxClasses];
 };
 
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src)
+                 : "memory");
+}
+
+template <int S>
 __global__ void __launch_bounds__(BG_THREADS, 1)
-k_gemm_bank_ldg(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
-                const __grid_constant__ CUtensorMap tmBl, const BgParams p)
+k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
+               const __grid_constant__ CUtensorMap tmBl, const BgParams p)
 {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>(
@@ -333,16 +343,16 @@ k_gemm_bank_ldg(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
     const int aBytes = BG_M * BG_BK * 2;
     const int bBytes = p.ntile * BG_BK * 2;
     const int stageBytes = 2 * aBytes + 2 * bBytes;
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + p.stages * stageBytes);
-    uint64_t* empty = full + p.stages;
-    uint64_t* accum = empty + p.stages;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * stageBytes);
+    uint64_t* empty = full + S;
+    uint64_t* accum = empty + S;
     uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(accum + 1);
     int* abortFlag = reinterpret_cast<int*>(tmemSlot + 1);
     int* rows = abortFlag + 1;                            // [BG_M]
     float* nrmRow = reinterpret_cast<float*>(rows + BG_M);  // [BG_M]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int mtile = blockIdx.x, item = blockIdx.y;
+    const int mtile = blockIdx.x, item = p.order ? p.order[blockIdx.y] : blockIdx.y;
     const int cl = p.cls ? p.cls[item] : 0;
     const bool clOk = cl >= 0 && cl < kMaxClasses && banks.nB[cl] > 0;
     const int k = clOk ? cl : 0;
@@ -363,7 +373,7 @@ k_gemm_bank_ldg(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
         rows[threadIdx.x] = b;
     }
     if (threadIdx.x == BG_M) {
-        for (int s = 0; s < p.stages; s++) {
+        for (int s = 0; s < S; s++) {
             mbar_init(full + s, 5);
             mbar_init(empty + s, 1);
         }
@@ -392,50 +402,50 @@ k_gemm_bank_ldg(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
         const __nv_bfloat16* bl = banks.lo[k];
         const __nv_bfloat16* srcH[8];
         const __nv_bfloat16* srcL[8];
+        int phys[8];
 #pragma unroll
         for (int i = 0; i < 8; i++) {
-            const size_t off = (size_t)rows[g + 16 * i] * p.Kd + q * 8;
+            const int r = g + 16 * i;
+            const size_t off = (size_t)rows[r] * p.Kd + q * 8;
             srcH[i] = bh + off;
             srcL[i] = bl + off;
+            phys[i] = r * 128 + ((q ^ (r & 7)) << 4);
         }
         const float* sg = p.sigRcp + (size_t)item * p.K;
         const float* cf = p.ctf + (size_t)item * p.K;
         float nS[8], nC[8];
 #pragma unroll
         for (int i = 0; i < 8; i++) nS[i] = nC[i] = 0.f;
-        uint4 cur[16], nxt[16];
-        // K block 0
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            cur[2 * i] = __ldg(reinterpret_cast<const uint4*>(srcH[i]));
-            cur[2 * i + 1] = __ldg(reinterpret_cast<const uint4*>(srcL[i]));
-        }
-        for (int kb = 0; kb < nkb; kb++) {
-            const int s = kb % p.stages;
-            const int round = kb / p.stages;
-            // the next K block's loads go out before this one is stored
-            if (kb + 1 < nkb) {
-                const size_t o = (size_t)(kb + 1) * BG_BK;
+        for (int kb = 0; kb < nkb + S - 1; kb++) {
+            if (kb < nkb) {
+                const int s = kb % S;
+                const int round = kb / S;
+                if (round > 0) {
+                    bool ok = lane != 0 || mbar_wait(empty + s, (round - 1) & 1, kWaitBudget);
+                    ok = __all_sync(0xffffffffu, ok);
+                    if (!ok || *(volatile int*)abortFlag) {
+                        if (lane == 0) {
+                            atomicOr(p.flag, 4);
+                            *(volatile int*)abortFlag = 1;
+                        }
+                        break;
+                    }
+                }
+                uint8_t* st = smem + s * stageBytes;
+                const size_t o = (size_t)kb * BG_BK;
 #pragma unroll
                 for (int i = 0; i < 8; i++) {
-                    nxt[2 * i] = __ldg(reinterpret_cast<const uint4*>(srcH[i] + o));
-                    nxt[2 * i + 1] = __ldg(reinterpret_cast<const uint4*>(srcL[i] + o));
+                    cp_async16(st + phys[i], srcH[i] + o);
+                    cp_async16(st + aBytes + phys[i], srcL[i] + o);
                 }
             }
-            if (round > 0) {
-                bool ok = lane != 0 || mbar_wait(empty + s, (round - 1) & 1, kWaitBudget);
-                ok = __all_sync(0xffffffffu, ok);
-                if (!ok || *(volatile int*)abortFlag) {
-                    if (lane == 0) {
-                        atomicOr(p.flag, 4);
-                        *(volatile int*)abortFlag = 1;
-                    }
-                    break;
-                }
-            }
-            uint8_t* st = smem + s * stageBytes;
-            // the weights sigRcp ctf^2 of this lane's 4 pixels
-            const int px0 = kb * (BG_BK / 2) + q * 4;
+            // one group per iteration (empty at the tail), so that
+            // "S - 1 groups pending" always means K block kb - S + 1 landed
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            const int kd = kb - (S - 1);
+            if (kd < 0) continue;
+            // the weights sigRcp ctf^2 of this lane's 4 pixels of K block kd
+            const int px0 = kd * (BG_BK / 2) + q * 4;
             float w[4];
 #pragma unroll
             for (int c = 0; c < 4; c++) {
@@ -443,15 +453,13 @@ k_gemm_bank_ldg(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                 const float cc = px < p.K ? __ldg(cf + px) : 0.f;
                 w[c] = px < p.K ? __ldg(sg + px) * cc * cc : 0.f;
             }
+            asm volatile("cp.async.wait_group %0;" ::"n"(S - 1) : "memory");
+            const uint8_t* st = smem + (kd % S) * stageBytes;
 #pragma unroll
             for (int i = 0; i < 8; i++) {
-                const int r = g + 16 * i;
-                const int phys = r * 128 + ((q ^ (r & 7)) << 4);
-                *reinterpret_cast<uint4*>(st + phys) = cur[2 * i];
-                *reinterpret_cast<uint4*>(st + aBytes + phys) = cur[2 * i + 1];
-                const uint32_t hw[4] = {cur[2 * i].x, cur[2 * i].y, cur[2 * i].z, cur[2 * i].w};
-                const uint32_t lw[4] = {cur[2 * i + 1].x, cur[2 * i + 1].y, cur[2 * i + 1].z,
-                                        cur[2 * i + 1].w};
+                const uint4 h = *reinterpret_cast<const uint4*>(st + phys[i]);
+                const uint4 lo = *reinterpret_cast<const uint4*>(st + aBytes + phys[i]);
+                const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {lo.x, lo.y, lo.z, lo.w};
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
                     const float2 hf = __bfloat1622float2(
@@ -462,13 +470,13 @@ k_gemm_bank_ldg(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                     kahan_add(nS[i], nC[i], w[c] * (re * re + im * im));
                 }
             }
-            // generic stores visible to the tensor cores' reads, then arrive
+            // the copies (generic proxy) visible to the tensor cores' reads
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
-            if (lane == 0) mbar_arrive(full + s);
-#pragma unroll
-            for (int j = 0; j < 16; j++) cur[j] = nxt[j];
+            if (lane == 0) mbar_arrive(full + kd % S);
         }
+        // copies still in flight after an abort land before the CTA leaves
+        asm volatile("cp.async.wait_all;" ::: "memory");
         // the rows' norms: the 8 lanes of a row group hold partials
 #pragma unroll
         for (int i = 0; i < 8; i++) {
@@ -482,8 +490,8 @@ k_gemm_bank_ldg(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
         // ---------------- B tiles (TMA)
         if (lane == 0) {
             for (int kb = 0; kb < nkb; kb++) {
-                const int s = kb % p.stages;
-                const int round = kb / p.stages;
+                const int s = kb % S;
+                const int round = kb / S;
                 if (round > 0 && !mbar_wait(empty + s, (round - 1) & 1, kWaitBudget)) {
                     atomicOr(p.flag, 4);
                     *(volatile int*)abortFlag = 1;
@@ -502,8 +510,8 @@ k_gemm_bank_ldg(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
         if (lane == 0) {
             const uint32_t idesc = umma_idesc(BG_M, p.ntile);
             for (int kb = 0; kb < nkb; kb++) {
-                const int s = kb % p.stages;
-                const int round = kb / p.stages;
+                const int s = kb % S;
+                const int round = kb / S;
                 if (!mbar_wait(full + s, round & 1, kWaitBudget)) {
                     atomicOr(p.flag, 4);
                     *(volatile int*)abortFlag = 1;
@@ -561,8 +569,8 @@ k_gemm_bank_ldg(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
     }
     if (aborted && warp == 4 && lane == 0) {
         for (int kb = 0; kb < issuedTma; kb++) {
-            const int s = kb % p.stages;
-            mbar_wait(full + s, (kb / p.stages) & 1, kWaitBudget / 4);
+            const int s = kb % S;
+            mbar_wait(full + s, (kb / S) & 1, kWaitBudget / 4);
         }
     }
     if (aborted && warp == 5 && lane == 0 && issuedMma > 0) mbar_wait(accum, 0, kWaitBudget / 4);
@@ -576,6 +584,41 @@ k_gemm_bank_ldg(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
     }
 }
 
+// The visiting order of the particles: sorted by (class, first proposed bank
+// row), ties by particle index; one CTA, bitonic sort of n <= 8192 keys in
+// shared memory.  A row outside [0, 2^24) or a class outside [0, 2^7) only
+// moves its particle.
+__global__ void k_bank_order(const int* __restrict__ idx, const int* __restrict__ cls, int nP,
+                             int nR, int nPow2, int* __restrict__ order)
+{
+    extern __shared__ unsigned long long key[];
+    for (int l = threadIdx.x; l < nPow2; l += blockDim.x) {
+        unsigned long long v = ~0ull;
+        if (l < nP) {
+            const unsigned r = (unsigned)idx[(size_t)l * nR] & 0xffffffu;
+            const unsigned c = cls ? (unsigned)cls[l] & 0x7fu : 0u;
+            v = ((unsigned long long)((c << 24) | r) << 32) | (unsigned)l;
+        }
+        key[l] = v;
+    }
+    __syncthreads();
+    for (int size = 2; size <= nPow2; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < nPow2 / 2; t += blockDim.x) {
+                const int lo = 2 * t - (t & (stride - 1));
+                const int hi = lo + stride;
+                const bool asc = (lo & size) == 0;
+                const unsigned long long a = key[lo], b = key[hi];
+                if ((a > b) == asc) {
+                    key[lo] = b;
+                    key[hi] = a;
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < nP; i += blockDim.x) order[i] = (int)(key[i] & 0xffffffffu);
+}
+
 }  // namespace
 
 // A: the classes' banks (bank[k].hi holds the hi plane, then the lo plane
@@ -585,7 +628,7 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
                                     const int* cls, int nP, int nR, const void* B, int nT,
                                     int Kd, int K, const float* sigRcp, const float* ctf,
                                     float* C, float alpha, int* flag, cudaStream_t st,
-                                    bool tmaGather)
+                                    bool tmaGather, int* order)
 {
     if (nP <= 0 || nR <= 0 || nT <= 0 || nT > 256 || Kd <= 0 || Kd % BG_BK || nP > 65535)
         return cudaErrorInvalidValue;
@@ -622,6 +665,22 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
         return cudaErrorInvalidValue;
     p.idx = idx;
     p.cls = cls;
+    p.order = nullptr;
+    if (order && nP <= 8192) {
+        int n2 = 1;
+        while (n2 < nP) n2 <<= 1;
+        const size_t sm = sizeof(unsigned long long) * n2;
+        if (sm > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(k_bank_order,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)sm);
+            if (e != cudaSuccess) return e;
+        }
+        k_bank_order<<<1, 1024, sm, st>>>(idx, cls, nP, nR, n2, order);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        p.order = order;
+    }
     p.sigRcp = sigRcp;
     p.ctf = ctf;
     p.C = C;
@@ -652,10 +711,20 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
         rowsOf.lo[k] = b.hi + (size_t)b.nB * b.Kp;
         rowsOf.nB[k] = maps.nB[k];
     }
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_bank_ldg,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the cp.async form keeps every stage in flight: as many as fit (<= 5)
+    int S = (int)((227 * 1024 - 1024 - 256 - 2 * sizeof(int) * BG_M) / stageBytes);
+    if (S > 5) S = 5;
+    if (S < 2 || (size_t)BG_M * (p.ntile + 1) * 4 > (size_t)S * stageBytes)
+        return cudaErrorInvalidValue;
+    p.stages = S;
+    const size_t smemCp = 1024 + (size_t)S * stageBytes + 256 + 2 * sizeof(int) * BG_M;
+    void (*kern)(const LdgRows, const CUtensorMap, const CUtensorMap, const BgParams) =
+        S == 5 ? k_gemm_bank_cp<5> : S == 4 ? k_gemm_bank_cp<4> : S == 3 ? k_gemm_bank_cp<3>
+                                                                         : k_gemm_bank_cp<2>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smemCp);
     if (e != cudaSuccess) return e;
-    k_gemm_bank_ldg<<<grid, BG_THREADS, smem, st>>>(rowsOf, mBh, mBl, p);
+    kern<<<grid, BG_THREADS, smemCp, st>>>(rowsOf, mBh, mBl, p);
     return cudaGetLastError();
 }
 

@@ -89,6 +89,8 @@ enum WsSlot {
     WS_RECO,         // reconstruction: T, W, C and the real-space map on the padded grid
     WS_LEARN,        // learned E-step: network outputs, proposals, their weights, fallback lists
     WS_LEARN_IO,     // learned E-step, host-buffer form: staged inputs and outputs
+    WS_ORDER,        // bank-row cross term: the particles' visiting order
+    WS_RENDER,       // reference rendering: image grid, projections, real images
     WS_COUNT
 };
 
@@ -183,6 +185,7 @@ struct tg3_ctx {
     bool fused = false;
     bool insertGather = false;    // TG3_OPT_INSERT_GATHER
     int bankGather = 1;           // TG3_OPT_BANK_GATHER (0, 1 or 2)
+    int bankOrder = 0;            // TG3_OPT_BANK_ORDER
     // per-stage event timing (tg3_ctx_set_timing)
     bool timing = false;
     // inside the learned E-step's fallback: its cross-term launches are
@@ -449,7 +452,7 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
                                     const int* cls, int nP, int nR, const void* B, int nT,
                                     int Kd, int K, const float* sigRcp, const float* ctf,
                                     float* C, float alpha, int* flag, cudaStream_t st,
-                                    bool tmaGather = false);
+                                    bool tmaGather = false, int* order = nullptr);
 cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda,
                                   const float* B, long long sB, int ldb,
                                   int M, int N, int Kd, int batch, float* C,

@@ -290,7 +290,111 @@ __global__ void k_remask_real(float* __restrict__ real, int N, float r, float ew
     }
 }
 
+// The img x img rfft grid in the particle transforms' order: pixel
+// p = r (img/2 + 1) + i holds column i and row j = r (r < img/2), r - img.
+__global__ void k_image_grid(int img, int* __restrict__ iCol, int* __restrict__ iRow)
+{
+    const int h = img / 2, n = img * (h + 1);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const int r = p / (h + 1), i = p % (h + 1);
+        iCol[p] = i;
+        iRow[p] = r < h ? r : r - img;
+    }
+}
+
+// One CTA per image: the centred image (index 0 moved to the middle, as an
+// fftshift), minus its mean, over its unbiased standard deviation; the sums
+// in FP64.
+__global__ void k_centre_normalise(const float* __restrict__ real, int img,
+                                   float* __restrict__ out)
+{
+    __shared__ double s1[32], s2[32];
+    const int n = img * img, h = img / 2;
+    const float* src = real + (size_t)blockIdx.x * n;
+    float* dst = out + (size_t)blockIdx.x * n;
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double v = src[i];
+        a += v;
+        b += v * v;
+    }
+    for (int o = 16; o; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s1[threadIdx.x >> 5] = a;
+        s2[threadIdx.x >> 5] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            ta += s1[w];
+            tb += s2[w];
+        }
+        const double mean = ta / n;
+        const double var = fmax((tb - ta * mean) / (n - 1), 0.0);
+        s1[0] = mean;
+        s2[0] = var > 0.0 ? 1.0 / sqrt(var) : 0.0;
+    }
+    __syncthreads();
+    const double mean = s1[0], rs = s2[0];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int y = i / img, x = i % img;
+        const int ys = y + h < img ? y + h : y + h - img, xs = x + h < img ? x + h : x + h - img;
+        dst[(size_t)y * img + x] = (float)(((double)src[(size_t)ys * img + xs] - mean) * rs);
+    }
+}
+
 }  // namespace
+
+extern "C" int tg3_ctx_render_references_d(tg3_ctx* c, int cls, const double* rotMat, int n,
+                                           int img, float* out)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (cls < 0 || cls >= kMaxClasses || !c->vol[cls].blocks)
+        return fail(TG3_ERR_STATE, "volume not set");
+    if (!rotMat || !out || n <= 0 || img < 8 || (img & 1))
+        return fail(TG3_ERR_ARG, "bad reference rendering arguments");
+    const Volume& v = c->vol[cls];
+    const int h = img / 2, K = img * (h + 1);
+    // the grid's farthest pixel, (h, h) pf voxels out, with its trilinear
+    // corners, must lie inside the stored half grid
+    if ((int)ceil(1.41422 * h * v.pf) + 2 > v.vdim / 2)
+        return fail(TG3_ERR_ARG, "reference image grid reaches past the volume");
+    const int IB = std::min(n, 4096);
+    const size_t oCol = 0, oRow = (sizeof(int) * K + 255) / 256 * 256,
+                 oP = oRow + (sizeof(int) * K + 255) / 256 * 256,
+                 oR = oP + (sizeof(float2) * (size_t)K * IB + 255) / 256 * 256,
+                 total = oR + sizeof(float) * (size_t)img * img * IB;
+    char* b = (char*)ws_get(c, WS_RENDER, total, &st);
+    if (!b) return st;
+    float* pscr = (float*)ws_get(c, WS_PROJ, sizeof(float) * project_scratch_floats(IB, 2 * K), &st);
+    if (!pscr) return st;
+    int* gCol = (int*)(b + oCol);
+    int* gRow = (int*)(b + oRow);
+    float* P = (float*)(b + oP);
+    float* R = (float*)(b + oR);
+    cudaStream_t s = c->stream;
+    k_image_grid<<<(K + 255) / 256, 256, 0, s>>>(img, gCol, gRow);
+    TG3_LAUNCH_CHECK("image grid");
+    cufftHandle plan;
+    for (int r0 = 0; r0 < n; r0 += IB) {
+        const int m = std::min(IB, n - r0);
+        TG3_CUDA(launch_project(nullptr, nullptr, v.blocks, v.vdim, v.pf, nullptr,
+                                rotMat + 9 * (size_t)r0, m, m, gCol, gRow, K, P, 2 * K, nullptr,
+                                nullptr, nullptr, pscr, c->d_flag, 0, s));
+        if ((st = get_plan(c, img, m, &plan, true))) return st;
+        if (cufftSetStream(plan, s) != CUFFT_SUCCESS ||
+            cufftExecC2R(plan, reinterpret_cast<cufftComplex*>(P), R) != CUFFT_SUCCESS)
+            return fail(TG3_ERR_CUDA, "cuFFT inverse transform failed");
+        k_centre_normalise<<<m, 256, 0, s>>>(R, img, out + (size_t)r0 * img * img);
+        TG3_LAUNCH_CHECK("reference centring");
+    }
+    return TG3_OK;
+}
 
 void prep_release(tg3_ctx* c)
 {

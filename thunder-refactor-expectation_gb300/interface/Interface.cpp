@@ -90,19 +90,32 @@ struct Slots {
 };
 std::map<Complex*, Slots*> g_slots;
 
-// ExpectLocalV3D: the volume behind a ManagedArrayTexture.
+// ExpectLocalV3D / V2D: the volume (or 2-D class image) behind a
+// ManagedArrayTexture.
 struct VolState {
     const Complex* host = nullptr;
     int vdim = 0;
     int pf = 0;
     tg3_volume* h = nullptr;
+    bool twoD = false;          // bound by ExpectLocalV2D
+    int dimSize = 0;            // the class image's element count (2-D)
+    tg3_image* img = nullptr;
 };
+
+void release(VolState& v)
+{
+    if (v.h) tg3_volume_destroy(v.h);
+    if (v.img) tg3_image_destroy(v.img);
+    v.h = nullptr;
+    v.img = nullptr;
+}
 std::map<ManagedArrayTexture*, VolState> g_vols;
 
 // ExpectLocalRTD / PreI3D: the hypothesis set behind a ManagedCalPoint.
 struct CalState {
     std::vector<double> rot, trans, oldR, oldT, dpara, oldD;
     int nR = 0, nT = 0, nD = 0;
+    int mode = 1;               // ManagedCalPoint mode: 1 for 3-D, 0 for 2-D
     ManagedArrayTexture* mgr = nullptr;
     int idim = 0, npxl = 0;
     const int* iCol = nullptr;
@@ -189,11 +202,26 @@ void ExpectLocalV3D(int gpuIdx, ManagedArrayTexture* mgr, Complex* volume, int v
     (void)gpuIdx;
     std::lock_guard<std::mutex> lk(g_mu);
     VolState& v = g_vols[mgr];
-    if (v.h) tg3_volume_destroy(v.h);
-    v.h = nullptr;
+    release(v);
     v.host = volume;
     v.vdim = vdim;
     v.pf = 0;
+    v.twoD = false;
+}
+
+// gpu/interface/Interface.h:40-43: a class image of dimSize complex values
+// (its edge arrives with ExpectLocalPreI2D)
+void ExpectLocalV2D(int gpuIdx, ManagedArrayTexture* mgr, Complex* volume, int dimSize)
+{
+    (void)gpuIdx;
+    std::lock_guard<std::mutex> lk(g_mu);
+    VolState& v = g_vols[mgr];
+    release(v);
+    v.host = volume;
+    v.vdim = 0;
+    v.pf = 0;
+    v.twoD = true;
+    v.dimSize = dimSize;
 }
 
 // gpu/interface/Interface.h:50-62: copy image imgId into slot threadId
@@ -240,11 +268,13 @@ void ExpectLocalRTD(int gpuIdx, ManagedCalPoint* mcp, double* oldR, double* oldT
     (void)gpuIdx;
     std::lock_guard<std::mutex> lk(g_mu);
     CalState& c = g_cal[mcp];
-    // the hypothesis counts are those of ManagedCalPoint::Init (getNR/getNT/getMD)
+    // the hypothesis counts are those of ManagedCalPoint::Init (getNR/getNT/getMD);
+    // 2-D rotations are (cos, sin) pairs (expectLocalRTD, gpu/src/cuthunder.cu:2683-2697)
     c.nR = mcp->getNR();
     c.nT = mcp->getNT();
     c.nD = mcp->getMD();
-    c.rot.assign(rot, rot + 4 * c.nR);
+    c.mode = mcp->getMode();
+    c.rot.assign(rot, rot + (c.mode == 1 ? 4 : 2) * c.nR);
     c.trans.assign(trans, trans + 2 * c.nT);
     c.oldR.assign(oldR, oldR + c.nR);
     c.oldT.assign(oldT, oldT + c.nT);
@@ -272,10 +302,9 @@ void ExpectLocalPreI3D(int gpuIdx, int datShift, ManagedArrayTexture* mgr, Manag
     (void)deviRow;
     std::lock_guard<std::mutex> lk(g_mu);
     VolState& v = g_vols[mgr];
-    if (!v.host || v.vdim != vdim) die("ExpectLocalPreI3D: volume not set", TG3_ERR_STATE);
+    if (!v.host || v.twoD || v.vdim != vdim) die("ExpectLocalPreI3D: volume not set", TG3_ERR_STATE);
     if (!v.h || v.pf != pf) {
-        if (v.h) tg3_volume_destroy(v.h);
-        v.h = nullptr;
+        release(v);
         ok("ExpectLocalPreI3D", tg3_volume_create(&v.h, reinterpret_cast<const float*>(v.host),
                                                   vdim, pf));
         v.pf = pf;
@@ -294,6 +323,42 @@ void ExpectLocalPreI3D(int gpuIdx, int datShift, ManagedArrayTexture* mgr, Manag
     c.freQ = devfreQ;     // ExpectPrefre's copy of the frequencies
 }
 
+// gpu/interface/Interface.h:89-105: the 2-D form (no defocus search)
+void ExpectLocalPreI2D(int gpuIdx, int datShift, ManagedArrayTexture* mgr, ManagedCalPoint* mcp,
+                       RFLOAT* devdefO, RFLOAT* devfreQ, int* deviCol, int* deviRow,
+                       RFLOAT phaseShift, RFLOAT conT, RFLOAT k1, RFLOAT k2, int pf, int idim,
+                       int vdim, int npxl, int interp)
+{
+    (void)gpuIdx;
+    (void)datShift;
+    (void)devdefO;
+    (void)devfreQ;
+    (void)phaseShift;
+    (void)conT;
+    if (interp != 1) die("ExpectLocalPreI2D: interpolation", TG3_ERR_UNSUPPORTED);
+    if (k1 != 0 || k2 != 0) die("ExpectLocalPreI2D: 2-D defocus search", TG3_ERR_UNSUPPORTED);
+    const PixelList* px = pixels_of(deviCol);
+    (void)deviRow;
+    std::lock_guard<std::mutex> lk(g_mu);
+    VolState& v = g_vols[mgr];
+    if (!v.host || !v.twoD || v.dimSize != vdim * (vdim / 2 + 1))
+        die("ExpectLocalPreI2D: class image not set", TG3_ERR_STATE);
+    if (!v.img || v.pf != pf || v.vdim != vdim) {
+        release(v);
+        ok("ExpectLocalPreI2D", tg3_image_create(&v.img, reinterpret_cast<const float*>(v.host),
+                                                 vdim, pf));
+        v.pf = pf;
+        v.vdim = vdim;
+    }
+    CalState& c = g_cal[mcp];
+    c.mgr = mgr;
+    c.idim = idim;
+    c.npxl = npxl;
+    c.iCol = px->iCol.data();
+    c.iRow = px->iRow.data();
+    c.k1 = c.k2 = 0;
+}
+
 // gpu/interface/Interface.h:125-139: project, shift, score and return the
 // marginal weights of the particle in slot datShift
 void ExpectLocalM(int gpuIdx, int datShift, ManagedCalPoint* mcp, Complex* devdatP,
@@ -306,14 +371,26 @@ void ExpectLocalM(int gpuIdx, int datShift, ManagedCalPoint* mcp, Complex* devda
     Slots* s = slots_of(devdatP);
     CalState c;
     tg3_volume* h = nullptr;
+    tg3_image* img = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_mu);
         c = g_cal[mcp];
         h = g_vols[c.mgr].h;
+        img = g_vols[c.mgr].twoD ? g_vols[c.mgr].img : nullptr;
     }
-    if (!h || c.npxl != npxl) die("ExpectLocalM: call order", TG3_ERR_STATE);
     const size_t off = (size_t)datShift * npxl;
     float baseL = 0;
+    if (img) {
+        if (c.npxl != npxl || c.mode != 0) die("ExpectLocalM: call order", TG3_ERR_STATE);
+        ok("ExpectLocalM",
+           tg3_ExpectLocal2D(img, reinterpret_cast<const float*>(&s->dat[off]), &s->ctf[off],
+                             &s->sig[off], c.iCol, c.iRow, npxl, c.idim, c.rot.data(), c.nR,
+                             c.trans.data(), c.nT, c.oldR.data(), c.oldT.data(), oldC, wC, wR,
+                             wT, nullptr, &baseL));
+        wD[0] = 1;
+        return;
+    }
+    if (!h || c.npxl != npxl) die("ExpectLocalM: call order", TG3_ERR_STATE);
     if (c.k1 != 0 || c.k2 != 0) {
         // defocus search: the slot holds the particle's defocus offsets
         if (c.nD < 1 || (int)c.dpara.size() != c.nD || !c.freQ || s->def.empty())
@@ -372,11 +449,7 @@ void ExpectLocalFin(int gpuIdx, Complex** devdatP, RFLOAT** devctfP, RFLOAT** de
         delete[] *devfreQ;
         *devfreQ = nullptr;
     }
-    for (auto& kv : g_vols)
-        if (kv.second.h) {
-            tg3_volume_destroy(kv.second.h);
-            kv.second.h = nullptr;
-        }
+    for (auto& kv : g_vols) release(kv.second);
     g_vols.clear();
     g_cal.clear();
 }

@@ -28,7 +28,7 @@ EXPORTS = [
     "tg3_ctx_workspace_bytes", "tg3_ctx_set_volume", "tg3_ctx_set_pixels",
     "tg3_local_phase_d", "tg3_resample_d", "tg3_ctx_insert_begin", "tg3_insert_d",
     "tg3_ctx_insert_read_d", "tg3_ctx_insert_ratio_d", "tg3_fsc_d", "tg3_rotmat_d", "tg3_translate_d", "tg3_ctf_d",
-    "tg3_project_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
+    "tg3_project_d", "tg3_ctx_render_references_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
     "tg3_ctx_set_option", "tg3_ctx_set_pixels_slot", "tg3_ctx_use_pixels",
     "tg3_ragged_plan_create", "tg3_ragged_plan_run", "tg3_ragged_plan_info",
     "tg3_ragged_plan_destroy", "tg3_cnn_create", "tg3_cnn_destroy", "tg3_cnn_param_count",
@@ -43,13 +43,14 @@ EXPORTS = [
     "tg3_noalloc_scratch_bytes", "tg3_local_phase_noalloc", "tg3_global_scan_d",
     "tg3_ctx_set_references", "tg3_learned_expect_d", "tg3_ExpectLearned3D",
     "tg3_InsertFT_classes", "tg3_remask_d", "tg3_ReMask", "tg3_ctx_prepare_tf_d",
-    "tg3_PrepareTF",
+    "tg3_PrepareTF", "tg3_image_create", "tg3_image_destroy", "tg3_ExpectLocal2D",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused", "network",
           "fallback", "fallback_cross")
 OPT_FUSED = 0
 OPT_INSERT_GATHER = 1
 OPT_BANK_GATHER = 2
+OPT_BANK_ORDER = 3
 
 
 class TG3Error(RuntimeError):
@@ -94,6 +95,10 @@ def lib():
             "tg3_ReMask": ([_P, _I, _I, _F, _F, _F], _I),
             "tg3_ctx_prepare_tf_d": ([_P, _P, _I, _I, _I], _I),
             "tg3_PrepareTF": ([_P, _P, _I, _P, _I, _I, _I], _I),
+            "tg3_image_create": ([_P, _P, _I, _I], _I),
+            "tg3_image_destroy": ([_P], _I),
+            "tg3_ExpectLocal2D": ([_P, _P, _P, _P, _P, _P, _I, _I, _P, _I, _P, _I, _P, _P, _D,
+                                   _P, _P, _P, _P, _P], _I),
             "tg3_volume_create": ([_P, _P, _I, _I], _I),
             "tg3_volume_destroy": ([_P], _I),
             "tg3_ExpectLocal3D": ([_P, _P, _P, _P, _P, _P, _I, _I, _P, _I, _P, _I, _P, _P, _D,
@@ -117,6 +122,7 @@ def lib():
             "tg3_translate_d": ([_P, _I, _I, _P, _P, _I, _P, _P], _I),
             "tg3_ctf_d": ([_P, _I, _F, _I, _P, _P, _I, _P, _P], _I),
             "tg3_project_d": ([_P, _I, _P, _I, _P], _I),
+            "tg3_ctx_render_references_d": ([_P, _I, _P, _I, _I, _P], _I),
             "tg3_local_phase": ([_P, _I, _I, _I] + [_P] * 14 + [_I], _I),
             "tg3_ctx_set_timing": ([_P, _I], _I),
             "tg3_ctx_set_option": ([_P, _I, _I], _I),
@@ -468,6 +474,11 @@ class Context:
     def project(self, cls, rotmat, nR, out):
         self._hold(rotmat, out)
         check(lib().tg3_project_d(self.h, cls, ptr(rotmat), nR, ptr(out)))
+
+    def render_references(self, cls, rotmat, n, img, out):
+        """tg3_ctx_render_references_d: out [n][img][img] float32 (device)."""
+        self._hold(rotmat, out)
+        check(lib().tg3_ctx_render_references_d(self.h, cls, ptr(rotmat), n, img, ptr(out)))
 
 
 def version() -> str:

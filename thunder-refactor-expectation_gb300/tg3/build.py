@@ -20,7 +20,7 @@ LIB = PKG / "libtg3.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["tg3_kernels.cu", "tg3_api.cu", "tg3_tc.cu", "tg3_fused.cu", "tg3_ragged.cu",
            "tg3_cnn.cu", "tg3_conv_tc.cu", "tg3_noalloc.cu", "tg3_io.cpp", "tg3_prep.cu", "tg3_reco.cu",
-           "tg3_learned.cu", "tg3_bank_gemm.cu"]
+           "tg3_learned.cu", "tg3_bank_gemm.cu", "tg3_local2d.cu"]
 
 
 def nvcc() -> str:

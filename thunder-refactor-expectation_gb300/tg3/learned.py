@@ -144,28 +144,22 @@ def image_grid(img: int = 64):
 
 def render_references(ctx, cls: int, quats: np.ndarray, box: int, img: int = 64,
                       chunk: int = 4096):
-    """Clean projections of the context's class-`cls` volume at `quats` (the
-    library's projector over the img x img rfft grid at the box's
-    frequencies), as the network sees particles: to real space, centred, zero
-    mean and unit deviation.  Returns a device float32 tensor [n][img][img].
-    Leaves the context's pixel set at that grid."""
+    """Clean projections of the context's class-`cls` volume at `quats` over
+    the img x img rfft grid at the box's frequencies, as the network sees
+    particles: to real space, centred, zero mean and unit deviation
+    (tg3_ctx_render_references_d, all on the device: projection, cuFFT
+    C2R, centring and normalisation).  Returns a device float32 tensor
+    [n][img][img]; the context's pixel set is left alone."""
     import torch
-    iCol, iRow = image_grid(img)
-    ctx.set_pixels(iCol, iRow, box)
+    del box  # the grid is in the volume's own frequencies
     dev = f"cuda:{torch.cuda.current_device()}"
     n = len(quats)
-    h = img // 2
     out = torch.empty((n, img, img), dtype=torch.float32, device=dev)
+    R = torch.as_tensor(synth.quat_to_mat(quats).reshape(n, 9)).to(dev).contiguous()
     for s in range(0, n, chunk):
         m = min(chunk, n - s)
-        R = torch.as_tensor(synth.quat_to_mat(quats[s:s + m]).reshape(m, 9)).to(dev)
-        P = torch.empty((m, len(iCol)), dtype=torch.complex64, device=dev)
-        ctx.project(cls, R, m, P)
-        ctx.sync()
-        ims = torch.fft.irfft2(P.view(m, img, h + 1), s=(img, img))
-        ims = torch.fft.fftshift(ims, dim=(-2, -1))
-        ims = ims - ims.mean(dim=(-2, -1), keepdim=True)
-        out[s:s + m] = ims / ims.std(dim=(-2, -1), keepdim=True)
+        ctx.render_references(cls, R[s:s + m], m, img, out[s:s + m])
+    ctx.sync()
     return out
 
 
