@@ -47,7 +47,10 @@ def build(force: bool = False) -> Path:
     """Compile tg3_oracle.c into liboracle.so (gcc, -O2, portable flags)."""
     src = HERE / "tg3_oracle.c"
     if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
-        subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-fno-fast-math",
+        # no contraction into fused multiply-adds: the same double rounding on
+        # every machine (gcc contracts by default where the target has FMA),
+        # as the reference's x86 build without FMA computes
+        subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-fno-fast-math", "-ffp-contract=off",
                         "-o", str(LIB), str(src), "-lm"], check=True)
     return LIB
 

@@ -132,8 +132,11 @@ def test_local_sequence_2d_matches_the_oracle(run):
         S = O.translate(f32(c["trans"][l]), c["box"], st.iCol, st.iRow)
         X, cc, ss = f32(c["dat"][l]), f32(c["ctf"][l]), f32(c["sig"][l])
         L = np.array([[O.logdvp(X, S[t] * P[r], cc, ss) for t in range(nT)] for r in range(nR)])
-        w = np.exp(L - L.max()) * c["oldR"][l][:, None] * c["oldT"][l][None, :]
-        rR, rT = w.sum(1), w.sum(0)
+        e = np.exp(L - L.max())
+        # the marginals of updateSP (or_score_local): wR[r] sums over t with
+        # the translation priors, wT[t] over r with the rotation priors
+        rR = (e * c["oldT"][l][None, :]).sum(1)
+        rT = (e * c["oldR"][l][:, None]).sum(0)
         assert np.abs(wR[l] / wR[l].sum() - rR / rR.sum()).max() < 2e-3
         assert np.abs(wT[l] / wT[l].sum() - rT / rT.sum()).max() < 2e-3
         assert np.argmax(wR[l]) == np.argmax(rR)

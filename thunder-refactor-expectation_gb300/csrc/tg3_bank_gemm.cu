@@ -312,14 +312,18 @@ k_gemm_bank_bf16x3(const __grid_constant__ BankMaps maps, const __grid_constant_
 // themselves with cp.async: per K block every thread copies 16 bytes of each
 // plane of 8 rows straight to their swizzled places in shared memory (8
 // lanes cover a row's 128-byte chunk, so a warp instruction reads 4 whole
-// rows' chunks), with no register staging, so that all S stages' copies can
-// be in flight at once.  Once the thread's own copies of a K block have
-// landed (cp.async.wait_group S-1) it adds their |P|^2, weighted by sigRcp
-// ctf^2, to its partial norms in compensated FP32 (the 8 lanes' partials are
-// summed at the end), makes them visible to the tensor cores (proxy fence)
-// and arrives.  A stage is full when the four warps have arrived and the B
-// tiles' bytes have landed (TMA, warp 4 lane 0); it is free when the MMAs
-// that read it have completed.
+// rows' chunks), with no register staging.  The wait for a K block's copies
+// lags their issue by LAG = S - 3 blocks (cp.async.wait_group LAG): the
+// copies of LAG + 1 blocks are in flight, and the MMAs of a block have two
+// blocks' time to finish before the producers need its stage again (with a
+// lag of S - 1 the producers stalled every block on the MMA round trip).
+// Once the thread's own copies of a K block have landed it adds their
+// |P|^2, weighted by sigRcp ctf^2, to its partial norms (a plain FP32 sum
+// of each row's four pixels, added to the running sum in compensated FP32;
+// the 8 lanes' partials are summed at the end), makes them visible to the
+// tensor cores (proxy fence) and arrives.  A stage is full when the four
+// warps have arrived and the B tiles' bytes have landed (TMA, warp 4 lane
+// 0); it is free when the MMAs that read it have completed.
 struct LdgRows {
     const __nv_bfloat16* hi[kMaxClasses];
     const __nv_bfloat16* lo[kMaxClasses];
@@ -416,7 +420,8 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
         float nS[8], nC[8];
 #pragma unroll
         for (int i = 0; i < 8; i++) nS[i] = nC[i] = 0.f;
-        for (int kb = 0; kb < nkb + S - 1; kb++) {
+        constexpr int LAG = S > 3 ? S - 3 : 0;
+        for (int kb = 0; kb < nkb + LAG; kb++) {
             if (kb < nkb) {
                 const int s = kb % S;
                 const int round = kb / S;
@@ -440,9 +445,9 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                 }
             }
             // one group per iteration (empty at the tail), so that
-            // "S - 1 groups pending" always means K block kb - S + 1 landed
+            // "LAG groups pending" always means K block kb - LAG landed
             asm volatile("cp.async.commit_group;" ::: "memory");
-            const int kd = kb - (S - 1);
+            const int kd = kb - LAG;
             if (kd < 0) continue;
             // the weights sigRcp ctf^2 of this lane's 4 pixels of K block kd
             const int px0 = kd * (BG_BK / 2) + q * 4;
@@ -453,13 +458,14 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                 const float cc = px < p.K ? __ldg(cf + px) : 0.f;
                 w[c] = px < p.K ? __ldg(sg + px) * cc * cc : 0.f;
             }
-            asm volatile("cp.async.wait_group %0;" ::"n"(S - 1) : "memory");
+            asm volatile("cp.async.wait_group %0;" ::"n"(LAG) : "memory");
             const uint8_t* st = smem + (kd % S) * stageBytes;
 #pragma unroll
             for (int i = 0; i < 8; i++) {
                 const uint4 h = *reinterpret_cast<const uint4*>(st + phys[i]);
                 const uint4 lo = *reinterpret_cast<const uint4*>(st + aBytes + phys[i]);
                 const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {lo.x, lo.y, lo.z, lo.w};
+                float part = 0.f;
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
                     const float2 hf = __bfloat1622float2(
@@ -467,8 +473,9 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                     const float2 lf = __bfloat1622float2(
                         *reinterpret_cast<const __nv_bfloat162*>(&lw[c]));
                     const float re = hf.x + lf.x, im = hf.y + lf.y;
-                    kahan_add(nS[i], nC[i], w[c] * (re * re + im * im));
+                    part = fmaf(w[c], re * re + im * im, part);
                 }
+                kahan_add(nS[i], nC[i], part);
             }
             // the copies (generic proxy) visible to the tensor cores' reads
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

@@ -263,7 +263,7 @@ int plan3(tg3_ctx* c, int vdim, cufftType type, cufftHandle* out)
 constexpr int kMaxSym = 64;     // symmetry elements (the icosahedral group has 59 besides E)
 
 struct SymMats {
-    float m[kMaxSym * 9];
+    double m[kMaxSym * 9];
 };
 
 // src = acc, scaled by 1 / T at the origin when normalising (allReduceT's
@@ -320,9 +320,18 @@ __device__ __forceinline__ float3 sample_ft(const float4* __restrict__ v, int vd
 
 // acc = src + sum over the symmetry elements R of src sampled at R v for
 // |R v|^2 < r2 (SYMMETRIZE_FT, include/Geometry/Transformation.h:170-196),
-// T floored at 1e-25 (PrepareTF's symmetrizeT).
+// T floored at 1e-25 (PrepareTF's symmetrizeT).  R v and its squared norm are
+// formed in FP64 in the reference's order, ((m0 i + m1 j) + m2 k) and
+// (a^2 + b^2) + c^2, with every product and sum rounded on its own (no fused
+// multiply-add): a voxel whose rotated image lies on the sphere |u| = r up to
+// rounding is then kept or dropped as the reference keeps or drops it.
+__device__ __forceinline__ double dot3_rn(const double* m, double i, double j, double k)
+{
+    return __dadd_rn(__dadd_rn(__dmul_rn(m[0], i), __dmul_rn(m[1], j)), __dmul_rn(m[2], k));
+}
+
 __global__ void k_symmetrize(float4* __restrict__ acc, const float4* __restrict__ src, int vdim,
-                             const SymMats mats, int nSym, float r2)
+                             const SymMats mats, int nSym, double r2)
 {
     const int nx = vdim / 2 + 1, half = vdim / 2;
     const size_t n = (size_t)vdim * vdim * nx;
@@ -332,14 +341,16 @@ __global__ void k_symmetrize(float4* __restrict__ acc, const float4* __restrict_
         const int y = (int)((q / nx) % vdim), z = (int)(q / ((size_t)nx * vdim));
         const int j = y < half ? y : y - vdim, k = z < half ? z : z - vdim;
         float4 v = src[q];
-        if ((float)(i * i + j * j + k * k) < r2) {
+        // a rotation keeps |v|: voxels well outside the sphere have nothing to add
+        if ((double)(i * i + j * j + k * k) <= r2 + 1.0) {
             for (int s = 0; s < nSym; s++) {
-                const float* m = mats.m + 9 * s;
-                const float a = m[0] * i + m[1] * j + m[2] * k;
-                const float b = m[3] * i + m[4] * j + m[5] * k;
-                const float c = m[6] * i + m[7] * j + m[8] * k;
-                if (a * a + b * b + c * c < r2) {
-                    const float3 w = sample_ft(src, vdim, a, b, c);
+                const double* m = mats.m + 9 * s;
+                const double a = dot3_rn(m, i, j, k), b = dot3_rn(m + 3, i, j, k),
+                             c = dot3_rn(m + 6, i, j, k);
+                const double nn = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)),
+                                            __dmul_rn(c, c));
+                if (nn < r2) {
+                    const float3 w = sample_ft(src, vdim, (float)a, (float)b, (float)c);
                     v.x += w.x;
                     v.y += w.y;
                     v.z += w.z;
@@ -492,14 +503,14 @@ extern "C" int tg3_ctx_prepare_tf_d(tg3_ctx* c, const double* symMat, int nSym, 
     if (maxRadius <= 0 || r + 1.0 > vdim / 2)
         return fail(TG3_ERR_ARG, "maxRadius x pf + 2 must not exceed vdim / 2");
     SymMats mats;
-    for (int i = 0; i < 9 * nSym; i++) mats.m[i] = (float)symMat[i];
+    for (int i = 0; i < 9 * nSym; i++) mats.m[i] = symMat[i];
     const size_t n = (size_t)vdim * vdim * (vdim / 2 + 1);
     float4* src = (float4*)ws_get(c, WS_RECO, sizeof(float4) * n, &st);
     if (!src) return st;
     cudaStream_t s = c->stream;
     k_acc_scaled_copy<<<152 * 8, 256, 0, s>>>(c->ins.acc, n, normalise, src);
     TG3_LAUNCH_CHECK("accumulator copy");
-    k_symmetrize<<<152 * 16, 256, 0, s>>>(c->ins.acc, src, vdim, mats, nSym, (float)(r * r));
+    k_symmetrize<<<152 * 16, 256, 0, s>>>(c->ins.acc, src, vdim, mats, nSym, r * r);
     TG3_LAUNCH_CHECK("symmetrisation");
     return TG3_OK;
 }
