@@ -336,8 +336,14 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src)
                  : "memory");
 }
 
+// Eight gather warps (0 - 7), then the B-tile TMA warp (8) and the MMA warp
+// (9, which also holds the tensor memory); warps 0 - 3 run the epilogue.
+constexpr int CP_PW = 8;
+constexpr int CP_THREADS = (CP_PW + 2) * 32;
+constexpr int CP_RPT = BG_M * 8 / (CP_PW * 32);   // rows per gather thread (4)
+
 template <int S>
-__global__ void __launch_bounds__(BG_THREADS, 1)
+__global__ void __launch_bounds__(CP_THREADS, 1)
 k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                const __grid_constant__ CUtensorMap tmBl, const BgParams p)
 {
@@ -378,14 +384,14 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
     }
     if (threadIdx.x == BG_M) {
         for (int s = 0; s < S; s++) {
-            mbar_init(full + s, 5);
+            mbar_init(full + s, CP_PW + 1);
             mbar_init(empty + s, 1);
         }
         mbar_init(accum, 1);
         *abortFlag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 5) {
+    if (warp == CP_PW + 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(tmemSlot)),
                      "r"(p.tmemCols)
@@ -398,18 +404,18 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
     const uint32_t tmem = *tmemSlot;
 
     int issuedTma = 0, issuedMma = 0;
-    if (warp < 4) {
+    if (warp < CP_PW) {
         // ---------------- A tiles and the rows' norms
         const int t = threadIdx.x;
         const int g = t >> 3, q = t & 7;                   // row group, 16-byte chunk
         const __nv_bfloat16* bh = banks.hi[k];
         const __nv_bfloat16* bl = banks.lo[k];
-        const __nv_bfloat16* srcH[8];
-        const __nv_bfloat16* srcL[8];
-        int phys[8];
+        const __nv_bfloat16* srcH[CP_RPT];
+        const __nv_bfloat16* srcL[CP_RPT];
+        int phys[CP_RPT];
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const int r = g + 16 * i;
+        for (int i = 0; i < CP_RPT; i++) {
+            const int r = g + (CP_PW * 4) * i;
             const size_t off = (size_t)rows[r] * p.Kd + q * 8;
             srcH[i] = bh + off;
             srcL[i] = bl + off;
@@ -417,9 +423,21 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
         }
         const float* sg = p.sigRcp + (size_t)item * p.K;
         const float* cf = p.ctf + (size_t)item * p.K;
-        float nS[8], nC[8];
+        float nS[CP_RPT], nC[CP_RPT];
 #pragma unroll
-        for (int i = 0; i < 8; i++) nS[i] = nC[i] = 0.f;
+        for (int i = 0; i < CP_RPT; i++) nS[i] = nC[i] = 0.f;
+        // the weights sigRcp ctf^2 of this lane's 4 pixels, one K block ahead
+        auto weights = [&](int kd, float* w) {
+            const int px0 = kd * (BG_BK / 2) + q * 4;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const int px = px0 + c;
+                const float cc = px < p.K ? __ldg(cf + px) : 0.f;
+                w[c] = px < p.K ? __ldg(sg + px) * cc * cc : 0.f;
+            }
+        };
+        float wCur[4], wNext[4];
+        weights(0, wCur);
         constexpr int LAG = S > 3 ? S - 3 : 0;
         for (int kb = 0; kb < nkb + LAG; kb++) {
             if (kb < nkb) {
@@ -439,7 +457,7 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                 uint8_t* st = smem + s * stageBytes;
                 const size_t o = (size_t)kb * BG_BK;
 #pragma unroll
-                for (int i = 0; i < 8; i++) {
+                for (int i = 0; i < CP_RPT; i++) {
                     cp_async16(st + phys[i], srcH[i] + o);
                     cp_async16(st + aBytes + phys[i], srcL[i] + o);
                 }
@@ -449,19 +467,11 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
             asm volatile("cp.async.commit_group;" ::: "memory");
             const int kd = kb - LAG;
             if (kd < 0) continue;
-            // the weights sigRcp ctf^2 of this lane's 4 pixels of K block kd
-            const int px0 = kd * (BG_BK / 2) + q * 4;
-            float w[4];
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-                const int px = px0 + c;
-                const float cc = px < p.K ? __ldg(cf + px) : 0.f;
-                w[c] = px < p.K ? __ldg(sg + px) * cc * cc : 0.f;
-            }
+            if (kd + 1 < nkb) weights(kd + 1, wNext);
             asm volatile("cp.async.wait_group %0;" ::"n"(LAG) : "memory");
             const uint8_t* st = smem + (kd % S) * stageBytes;
 #pragma unroll
-            for (int i = 0; i < 8; i++) {
+            for (int i = 0; i < CP_RPT; i++) {
                 const uint4 h = *reinterpret_cast<const uint4*>(st + phys[i]);
                 const uint4 lo = *reinterpret_cast<const uint4*>(st + aBytes + phys[i]);
                 const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {lo.x, lo.y, lo.z, lo.w};
@@ -473,7 +483,7 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                     const float2 lf = __bfloat1622float2(
                         *reinterpret_cast<const __nv_bfloat162*>(&lw[c]));
                     const float re = hf.x + lf.x, im = hf.y + lf.y;
-                    part = fmaf(w[c], re * re + im * im, part);
+                    part = fmaf(wCur[c], re * re + im * im, part);
                 }
                 kahan_add(nS[i], nC[i], part);
             }
@@ -481,19 +491,21 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(full + kd % S);
+#pragma unroll
+            for (int c = 0; c < 4; c++) wCur[c] = wNext[c];
         }
         // copies still in flight after an abort land before the CTA leaves
         asm volatile("cp.async.wait_all;" ::: "memory");
         // the rows' norms: the 8 lanes of a row group hold partials
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
+        for (int i = 0; i < CP_RPT; i++) {
             float v = nS[i] - nC[i];
             v += __shfl_xor_sync(0xffffffffu, v, 1);
             v += __shfl_xor_sync(0xffffffffu, v, 2);
             v += __shfl_xor_sync(0xffffffffu, v, 4);
-            if (q == 0) nrmRow[g + 16 * i] = v;
+            if (q == 0) nrmRow[g + (CP_PW * 4) * i] = v;
         }
-    } else if (warp == 4) {
+    } else if (warp == CP_PW) {
         // ---------------- B tiles (TMA)
         if (lane == 0) {
             for (int kb = 0; kb < nkb; kb++) {
@@ -574,16 +586,17 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
             for (int j = lane; j < p.nT; j += 32) cbase[(size_t)r * p.nT + j] = stage[rr * pitch + j];
         }
     }
-    if (aborted && warp == 4 && lane == 0) {
+    if (aborted && warp == CP_PW && lane == 0) {
         for (int kb = 0; kb < issuedTma; kb++) {
             const int s = kb % S;
             mbar_wait(full + s, (kb / S) & 1, kWaitBudget / 4);
         }
     }
-    if (aborted && warp == 5 && lane == 0 && issuedMma > 0) mbar_wait(accum, 0, kWaitBudget / 4);
+    if (aborted && warp == CP_PW + 1 && lane == 0 && issuedMma > 0)
+        mbar_wait(accum, 0, kWaitBudget / 4);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 5) {
+    if (warp == CP_PW + 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                      "r"(p.tmemCols)
@@ -731,7 +744,7 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smemCp);
     if (e != cudaSuccess) return e;
-    kern<<<grid, BG_THREADS, smemCp, st>>>(rowsOf, mBh, mBl, p);
+    kern<<<grid, CP_THREADS, smemCp, st>>>(rowsOf, mBh, mBl, p);
     return cudaGetLastError();
 }
 

@@ -408,24 +408,54 @@ __global__ void k_shift_bank(const float2* __restrict__ dat, const float* __rest
                              const double* __restrict__ trans, const float2* __restrict__ bank,
                              int nT, int nD, int idim,
                              const int* __restrict__ iCol, const int* __restrict__ iRow,
-                             int K, float* __restrict__ out, int ldo, long long splitLo)
+                             int K, float* __restrict__ out, int ldo, long long splitLo,
+                             int useTab)
 {
+    // per-particle translations with useTab: the phase e^{2 pi i (iCol tx + iRow ty) / N}
+    // is the product of a column factor and a row factor, tabulated once per
+    // CTA for its translations (tabX [SHIFT_T][h + 1] over iCol = 0 .. h, tabY
+    // [SHIFT_T][2h + 1] over iRow = -h .. h), so a pixel costs two shared
+    // loads and a complex product instead of a sine and a cosine
+    extern __shared__ float2 tabX[];
     const int ld = blockIdx.x;            // l nD + d
     const int l = ld / nD;
     const int t0 = blockIdx.y * SHIFT_T;
     const int t1 = min(nT, t0 + SHIFT_T);
     const float invN = 1.0f / (float)idim;
+    const int h = idim / 2, nc = h + 1, nr = 2 * h + 1;
+    float2* tabY = tabX + SHIFT_T * nc;
+    if (useTab && !bank) {
+        for (int e = threadIdx.x; e < (t1 - t0) * (nc + nr); e += blockDim.x) {
+            const int tt = e / (nc + nr), j = e % (nc + nr);
+            const size_t lt = (size_t)l * nT + t0 + tt;
+            float sn, cs;
+            if (j < nc) {
+                sincospif(2.0f * ((float)j * (float)trans[2 * lt]) * invN, &sn, &cs);
+                tabX[tt * nc + j] = make_float2(cs, sn);
+            } else {
+                const int r = j - nc - h;
+                sincospif(2.0f * ((float)r * (float)trans[2 * lt + 1]) * invN, &sn, &cs);
+                tabY[tt * nr + (j - nc)] = make_float2(cs, sn);
+            }
+        }
+        __syncthreads();
+    }
     for (int p = threadIdx.x; p < ldo / 2; p += blockDim.x) {
         float sc = 0.f;
         float2 X = make_float2(0.f, 0.f);
         float fc = 0.f, fr = 0.f;
+        int ic = 0, ir = 0;
+        bool tabOk = false;
         if (p < K) {
             const size_t i = (size_t)l * K + p;
             sc = sigRcp[i] * ctf[(size_t)ld * K + p];
             X = dat[i];
             if (!bank) {
-                fc = (float)iCol[p];
-                fr = (float)iRow[p];
+                ic = iCol[p];
+                ir = iRow[p];
+                fc = (float)ic;
+                fr = (float)ir;
+                tabOk = useTab && ic >= 0 && ic <= h && ir >= -h && ir <= h;
             }
         }
         for (int t = t0; t < t1; t++) {
@@ -438,6 +468,10 @@ __global__ void k_shift_bank(const float2* __restrict__ dat, const float* __rest
                     const float2 S = bank[(size_t)t * K + p];
                     c = S.x;
                     s = -S.y;
+                } else if (tabOk) {
+                    const float2 ex = tabX[(t - t0) * nc + ic], ey = tabY[(t - t0) * nr + ir + h];
+                    c = ex.x * ey.x - ex.y * ey.y;
+                    s = ex.y * ey.x + ex.x * ey.y;
                 } else {
                     const size_t lt = (size_t)l * nT + t;
                     const float tx = (float)trans[2 * lt], ty = (float)trans[2 * lt + 1];
@@ -1754,8 +1788,11 @@ cudaError_t launch_shift_bank(const float2* dat, const float* ctf, const float* 
 {
     if (nD < 1 || nT < 1) return cudaErrorInvalidValue;
     dim3 grid((unsigned)nP * nD, (nT + SHIFT_T - 1) / SHIFT_T);
-    k_shift_bank<<<grid, 256, 0, st>>>(dat, ctf, sigRcp, trans, bank, nT, nD, idim, iCol, iRow,
-                                        K, out, ldo, splitLo);
+    // the separable phase tables when they fit the default shared memory
+    const size_t tab = bank ? 0 : sizeof(float2) * SHIFT_T * (size_t)(3 * (idim / 2) + 2);
+    const int useTab = (!bank && idim >= 2 && tab <= 48 * 1024) ? 1 : 0;
+    k_shift_bank<<<grid, 256, useTab ? tab : 0, st>>>(dat, ctf, sigRcp, trans, bank, nT, nD, idim,
+                                                      iCol, iRow, K, out, ldo, splitLo, useTab);
     return cudaGetLastError();
 }
 
