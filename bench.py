@@ -1255,9 +1255,11 @@ def run_learned(args, rank, world, local_rank):
     the plain FP32 global search, at box 256 (learned256) or 128 (learned128).
 
     16 blob maps; 12 give the training particles, 4 are held out.  The
-    training labels are the plain method's converged poses (FP32 global
+    training labels are the plain method's converged poses (the global
     search over 6,912 rotations x 49 translations, then three narrowing local
-    phases of 1,000 x 100).  The network (matching mode, trained on the GPU by
+    phases of 1,000 x 100; scored in split-bf16 by default, whose argmax
+    equals the FP64 oracle's on the population tests, so that the whole
+    line, training included, finishes in under five minutes).  The network (matching mode, trained on the GPU by
     the library's kernels) proposes 256 rotations x 25 translations per
     particle; the fallback threshold is calibrated on held-out particles of
     the training maps against the plain method's poses.  The timed step is
@@ -1287,6 +1289,7 @@ def run_learned(args, rank, world, local_rank):
     ctx = tg3.Context(local_rank)
     ctx.set_option(tg3.OPT_BANK_GATHER, args.bank_form)
     ctx.set_option(tg3.OPT_BANK_ORDER, args.bank_order)
+    ctx.set_option(tg3.OPT_SCAN_PAIR, args.scan_pair)
     for c, bm in enumerate(maps):
         ctx.set_volume(c, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
     ctx.set_pixels(iCol, iRow, box)
@@ -1641,10 +1644,10 @@ def run_learned(args, rank, world, local_rank):
                    "train_particles": 0 if args.load_net else args.train_particles,
                    "epochs": args.epochs, "network": ("loaded: " + args.load_net) if args.load_net
                    else "trained in this run",
-                   "labels": "the plain method's converged poses: FP32 global search, then "
+                   "labels": "the plain method's converged poses: the global search, then "
                              "three local phases of 1,000 x 100 (kappa 200 / 1,000 / 5,000, "
-                             "translation deviation 2 / 0.7 / 0.3 px)"
-                             + ("" if lab_prec == tg3.SCORE_FP32 else " (scored in split-bf16)"),
+                             "translation deviation 2 / 0.7 / 0.3 px), scored in "
+                             + ("FP32" if lab_prec == tg3.SCORE_FP32 else "split-bf16"),
                    "l2": "inputs larger than L2 (pixel data 159 MB, banks 0.55 GB per map)",
                    "per_map_work": f"references and bank once per map ({map_ms:.1f} ms), "
                                    f"charged over {per_map_particles} particles per map"},
@@ -2226,7 +2229,7 @@ def main():
     ap.add_argument("--per-particle-sample", type=int, default=256,
                     help="particles timed one at a time beside the plan (uneven192)")
     ap.add_argument("--global-particles", type=int, default=2000)
-    ap.add_argument("--label-precision", default="fp32", choices=["fp32", "bf16x3"],
+    ap.add_argument("--label-precision", default="bf16x3", choices=["fp32", "bf16x3"],
                     help="precision of the plain method that labels the training particles")
     ap.add_argument("--plain-steps", type=int, default=20,
                     help="timed steps of the plain FP32 global search beside the learned step")
@@ -2237,6 +2240,9 @@ def main():
     ap.add_argument("--bank-form", type=int, default=0, choices=[0, 1, 2],
                     help="rescoring form (TG3_OPT_BANK_GATHER): 0 cross term gathers the bank "
                          "rows with cp.async, 1 rows copied out first, 2 TMA gathers")
+    ap.add_argument("--scan-pair", type=int, default=0, choices=[0, 1],
+                    help="TG3_OPT_SCAN_PAIR: the global search's cross term on CTA pairs that "
+                         "share each column tile by TMA multicast")
     ap.add_argument("--bank-order", type=int, default=1, choices=[0, 1],
                     help="TG3_OPT_BANK_ORDER: particles visited sorted by first proposed row")
     ap.add_argument("--no-local", action="store_true",

@@ -331,12 +331,22 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  *   particles in the order of their first proposed row (class, then bank
  *   row), so that the particles in flight together share bank rows in L2;
  *   batches of more than 8,192 particles keep their own order.  The results
- *   do not depend on it. */
+ *   do not depend on it.
+ * TG3_OPT_SCAN_TILE_N (default 0 = 256): the column tile (UMMA N, a multiple
+ *   of 16 up to 256) of the split-bf16 global scan's cross term; a narrower
+ *   tile leaves room for more pipeline stages.  The results do not depend on
+ *   it.
+ * TG3_OPT_SCAN_PAIR (default 0): 1 runs that cross term on pairs of CTAs
+ *   (a thread-block cluster of two on neighbouring row tiles) that share
+ *   each column tile: each CTA loads half of it, multicast to both, halving
+ *   the bytes the column operand takes from L2.  Same results. */
 enum {
     TG3_OPT_FUSED = 0,
     TG3_OPT_INSERT_GATHER = 1,
     TG3_OPT_BANK_GATHER = 2,
-    TG3_OPT_BANK_ORDER = 3
+    TG3_OPT_BANK_ORDER = 3,
+    TG3_OPT_SCAN_TILE_N = 4,
+    TG3_OPT_SCAN_PAIR = 5
 };
 int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);

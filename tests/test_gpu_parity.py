@@ -428,6 +428,53 @@ def test_global_scan(small, ctx, precision):
         np.testing.assert_allclose(a, b / b.sum(), atol=2e-3)
 
 
+@pytest.mark.parametrize("form", [(0, 1), (128, 0), (128, 1), (64, 1)])
+def test_global_scan_tile_forms(small, ctx, form):
+    """The split-bf16 global scan's cross term with a narrower column tile
+    (TG3_OPT_SCAN_TILE_N) and on CTA pairs that share each column tile by TMA
+    multicast (TG3_OPT_SCAN_PAIR; 300 rotations = 3 row tiles, so one pair
+    holds a tile past the last row) against the default form on the same
+    inputs.  The pair form issues the same MMAs in the same order: the same
+    log-likelihoods to the last bit.  A narrower tile changes the MMA shape,
+    so its sums may round differently: log-likelihoods within 1e-6 relative,
+    weights within 1e-4."""
+    rng = np.random.default_rng(43)
+    st = small["st"]
+    nImg, nR, nT = 30, 300, 9
+    q = synth.haar_quaternions(rng, nR)
+    mat = np.ascontiguousarray(O.rotmat(q).reshape(-1, 9))
+    trans = synth.global_translations(1, 1.0)
+    pR = rng.random(nR) + 0.5
+    pT = rng.random(nT) + 0.5
+    args = [dev(st.dat[:nImg].astype(np.complex64)), dev(st.ctf[:nImg].astype(np.float32)),
+            dev(st.sigRcp[:nImg].astype(np.float32)), dev(mat), dev(trans), dev(pR), dev(pT)]
+
+    def run(tile_n, pair):
+        ctx.set_option(tg3.OPT_SCAN_TILE_N, tile_n)
+        ctx.set_option(tg3.OPT_SCAN_PAIR, pair)
+        o = dict(wC=torch.empty(nImg, dtype=torch.float64, device=DEV),
+                 wR=torch.empty((nImg, nR), dtype=torch.float64, device=DEV),
+                 wT=torch.empty((nImg, nT), dtype=torch.float64, device=DEV),
+                 base=torch.empty(nImg, dtype=torch.float64, device=DEV),
+                 dvp=torch.empty((nImg, nR, nT), dtype=torch.float32, device=DEV))
+        ctx.global_scan(0, nImg, nR, nT, *args, o["wC"], o["wR"], o["wT"], o["base"], o["dvp"],
+                        tg3.SCORE_BF16X3)
+        ctx.sync()
+        return {k: v.cpu().numpy() for k, v in o.items()}
+
+    try:
+        a, b = run(*form), run(0, 0)
+    finally:
+        ctx.set_option(tg3.OPT_SCAN_TILE_N, 0)
+        ctx.set_option(tg3.OPT_SCAN_PAIR, 0)
+    for k in ("dvp", "wC", "wR", "wT", "base"):
+        if form[0] == 0:
+            np.testing.assert_array_equal(a[k], b[k])
+        else:
+            np.testing.assert_allclose(a[k], b[k], rtol=1e-6 if k in ("dvp", "base") else 1e-4,
+                                       atol=0)
+
+
 @pytest.mark.parametrize("shape", [(4, 96, 21), (3, 300, 100), (2, 129, 7)])
 def test_fused_matches_two_kernel_form(small, ctx, shape):
     """The fused projection + split-bf16 kernel (slices gathered straight into

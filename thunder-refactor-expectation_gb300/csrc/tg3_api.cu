@@ -316,6 +316,7 @@ extern "C" int tg3_ctx_destroy(tg3_ctx* c)
         cudaFree(b.f32);
         cudaFree(b.hi);
         cudaFree(b.abs2);
+        cudaFree(b.abs2q);
         cudaFree(b.quat);
         cudaFree(b.emb);
     }
@@ -796,13 +797,15 @@ extern "C" int tg3_ctx_set_bank(tg3_ctx* c, int cls, const double* quat, int nB)
     const size_t rowF = (size_t)nB * Kp;
     const size_t need = rowF * sizeof(float) + 2 * rowF * sizeof(__nv_bfloat16) +
                         (size_t)nB * K * sizeof(float);
-    // the references belong to the previous rotation set
+    // the references and the |P|^2 rows belong to the previous rotation set
     b.nEmb = 0;
+    b.abs2qSplit = -1;
     if (b.bytes < need || b.nB != nB) {
         TG3_CUDA(cudaStreamSynchronize(c->stream));
         cudaFree(b.f32);
         cudaFree(b.hi);
         cudaFree(b.abs2);
+        cudaFree(b.abs2q);
         cudaFree(b.quat);
         cudaFree(b.emb);
         b = Bank();
@@ -1544,7 +1547,7 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
                        const float* sigRcp, const double* rotMat, const double* trans,
                        const double* pR, const double* pT, double* wC, double* wR, double* wT,
                        double* baseL, float* dvp, int precision, int nK = 1,
-                       size_t imgStride = 0, const Bank* pbank = nullptr);
+                       size_t imgStride = 0, Bank* pbank = nullptr);
 static int merge_classes(tg3_ctx* c, int n, int nK, int nR, int nT, const double* wCd,
                          const double* wRd, const double* wTd, const double* bd, float* wC,
                          float* wR, float* wT, float* baseL);
@@ -1795,6 +1798,12 @@ extern "C" int tg3_ctx_set_option(tg3_ctx* c, int option, int value)
         c->bankGather = value;
     }
     else if (option == TG3_OPT_BANK_ORDER) c->bankOrder = value != 0;
+    else if (option == TG3_OPT_SCAN_TILE_N) {
+        if (value != 0 && (value < 16 || value > 256 || value % 16))
+            return fail(TG3_ERR_ARG, "TG3_OPT_SCAN_TILE_N takes 0 or a multiple of 16 up to 256");
+        c->scanTileN = value;
+    }
+    else if (option == TG3_OPT_SCAN_PAIR) c->scanPair = value != 0;
     else return fail(TG3_ERR_ARG, "unknown option");
     return TG3_OK;
 }
@@ -1866,12 +1875,46 @@ __global__ void k_abs2_from(const float* __restrict__ P, long long loOff, int K,
 // classes; the weights are then per (image, class) block, each relative to
 // its own best hypothesis: wC / baseL [nImg][nK], wR [nImg][nK][nR],
 // wT [nImg][nK][nT], dvp [nImg][nK][nR][nT].
+// nrmG [M][n] = sum_k abs2 [M][k] sc2 [n][k] over Kq columns: the FP32 GEMM,
+// split along K into S chunks when its M x n tiles alone would not fill the
+// GPU (the global search of a few fallback particles has n of about 70), the
+// chunks' partial sums added in chunk order.
+static int norm_gemm(tg3_ctx* c, const float* abs2, const float* sc2, int M, int n, int Kq,
+                     float* nrmG, cudaStream_t s)
+{
+    const int tiles = ((M + 127) / 128) * ((n + 127) / 128);
+    int S = 1;
+    const int blocks64 = Kq / 64;
+    if (tiles < 2 * 152 && Kq % 64 == 0) {
+        const int want = std::min(16, (2 * 152 + tiles - 1) / tiles);
+        for (int d = want; d >= 2; d--)
+            if (blocks64 % d == 0) {
+                S = d;
+                break;
+            }
+    }
+    if (S == 1) {
+        TG3_CUDA(launch_gemm_nt_fp32(abs2, 0, Kq, sc2, 0, Kq, M, n, Kq, 1, nrmG, 0, n, nullptr, 0,
+                                     1.0f, s));
+        return TG3_OK;
+    }
+    int st = TG3_OK;
+    const size_t cnt = (size_t)M * n;
+    float* part = (float*)ws_get(c, WS_SPLITK, sizeof(float) * cnt * S, &st);
+    if (!part) return st;
+    const int kc = Kq / S;
+    TG3_CUDA(launch_gemm_nt_fp32(abs2, kc, Kq, sc2, kc, Kq, M, n, kc, S, part, (long long)cnt, n,
+                                 nullptr, 0, 1.0f, s));
+    TG3_CUDA(launch_sum_parts(part, S, cnt, nrmG, s));
+    return TG3_OK;
+}
+
 static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim, int pf,
                        int nImg, int nR, int nT, const float* dat, const float* ctf,
                        const float* sigRcp, const double* rotMat, const double* trans,
                        const double* pR, const double* pT, double* wC, double* wR, double* wT,
                        double* baseL, float* dvp, int precision, int nK, size_t imgStride,
-                       const Bank* pbank)
+                       Bank* pbank)
 {
     int st = TG3_OK;
     if (pbank) {
@@ -1912,13 +1955,13 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
     double* x0 = (double*)ws_get(c, WS_X0, 8 * (size_t)nImg, &st);
     if (!x0) return st;
     Arena ar(c, WS_MISC);
-    const size_t oAbs = ar.add(4 * (size_t)nRt * Kq), oBank = ar.add(8 * (size_t)nT * K),
+    const size_t oAbs = ar.add(pbank ? 0 : 4 * (size_t)nRt * Kq), oBank = ar.add(8 * (size_t)nT * K),
                  oSc = ar.add(4 * (size_t)IB * Kq),
                  oNc = ar.add(nK > 1 ? 4 * (size_t)nRt * IB : 0),
                  oX0 = ar.add(nK > 1 ? 8 * (size_t)IB * nK : 0);
     char* m = (char*)ws_get(c, WS_MISC, ar.used, &st);
     if (!m) return st;
-    float* abs2 = (float*)(m + oAbs);
+    float* abs2 = pbank ? nullptr : (float*)(m + oAbs);
     float2* bank = (float2*)(m + oBank);
     float* sc2 = (float*)(m + oSc);
     float* nrmC = (float*)(m + oNc);
@@ -1948,8 +1991,20 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
                                     nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, nullptr, nullptr,
                                     nullptr, pscr, c->d_flag, splitP, s));
         }
-        k_abs2_from<<<nRt, 256, 0, s>>>(P, splitP, K, Kp, abs2, Kq);
-        TG3_LAUNCH_CHECK("projection norms");
+        if (pbank) {
+            // the bank's |P|^2 rows, made once per bank and precision
+            if (!pbank->abs2q)
+                TG3_CUDA(cudaMalloc(&pbank->abs2q, sizeof(float) * (size_t)pbank->nB * Kq));
+            if (pbank->abs2qSplit != (split ? 1 : 0)) {
+                k_abs2_from<<<nRt, 256, 0, s>>>(P, splitP, K, Kp, pbank->abs2q, Kq);
+                TG3_LAUNCH_CHECK("projection norms");
+                pbank->abs2qSplit = split ? 1 : 0;
+            }
+            abs2 = pbank->abs2q;
+        } else {
+            k_abs2_from<<<nRt, 256, 0, s>>>(P, splitP, K, Kp, abs2, Kq);
+            TG3_LAUNCH_CHECK("projection norms");
+        }
     }
     TG3_CUDA(launch_translate(trans, nT, c->px.idim, c->px.iCol, c->px.iRow, K, bank, K, s));
     for (int l0 = 0; l0 < nImg; l0 += IB) {
@@ -1969,16 +2024,16 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
         {
             StageTimer tm(c, TG3_STAGE_CROSS);
             // per-(rotation, image) norm, then the cross term
-            TG3_CUDA(launch_gemm_nt_fp32(abs2, 0, Kq, sc2, 0, Kq, nRt, n, Kq, 1, nrmG, 0, n,
-                                         nullptr, 0, 1.0f, s));
+            if ((st = norm_gemm(c, abs2, sc2, nRt, n, Kq, nrmG, s))) return st;
             // the cross term is written image-major: D[l][r][t]
             const int cols = n * nT;
             if (split) {
-                const int Nt = std::min(256, (cols + 15) / 16 * 16);
+                const int Nt = std::min(c->scanTileN > 0 ? c->scanTileN : 256,
+                                        (cols + 15) / 16 * 16);
                 const int items = (cols + Nt - 1) / Nt;
                 TG3_CUDA(launch_gemm_bf16x3(P, nRt, A, (long long)cols, nRt, Nt, Kp, items, 0, Nt,
                                             cols, D, 0, nT, nullptr, 0, -2.0f, c->d_flag, s, nT,
-                                            (long long)nRt * nT));
+                                            (long long)nRt * nT, c->scanPair != 0));
             } else {
                 TG3_CUDA(launch_gemm_nt_fp32(P, 0, Kp, A, 0, Kp, nRt, cols, Kp, 1, D, 0, nT,
                                              nullptr, 0, -2.0f, s, nT, (long long)nRt * nT));

@@ -91,6 +91,7 @@ enum WsSlot {
     WS_LEARN_IO,     // learned E-step, host-buffer form: staged inputs and outputs
     WS_ORDER,        // bank-row cross term: the particles' visiting order
     WS_RENDER,       // reference rendering: image grid, projections, real images
+    WS_SPLITK,       // split-K partial sums of the global search's norm term
     WS_COUNT
 };
 
@@ -137,6 +138,11 @@ struct Bank {
     // rotations [nEmb][64], normalised (tg3_ctx_set_references)
     float* emb = nullptr;
     int nEmb = 0;
+    // |P|^2 rows [nB][Kq] (zero padded) for the global search's norm term,
+    // made on first use from the planes the search reads (abs2qSplit: from
+    // hi + lo, else from the FP32 rows; -1: not made)
+    float* abs2q = nullptr;
+    int abs2qSplit = -1;
 };
 // The device view of one class's references: embeddings [n][64] and their
 // rotations [n][4] (the bank's), for the matching proposals.
@@ -186,6 +192,8 @@ struct tg3_ctx {
     bool insertGather = false;    // TG3_OPT_INSERT_GATHER
     int bankGather = 1;           // TG3_OPT_BANK_GATHER (0, 1 or 2)
     int bankOrder = 0;            // TG3_OPT_BANK_ORDER
+    int scanTileN = 0;            // TG3_OPT_SCAN_TILE_N (0: 256)
+    int scanPair = 0;             // TG3_OPT_SCAN_PAIR
     // per-stage event timing (tg3_ctx_set_timing)
     bool timing = false;
     // inside the learned E-step's fallback: its cross-term launches are
@@ -312,6 +320,8 @@ cudaError_t launch_gemm_nt_fp32(const float* A, long long sA, int lda,
                                 long long sN, float alpha, cudaStream_t st,
                                 int cGroup = 0, long long cGroupStride = 0);
 // nrmG (optional) adds a per-(rotation, block) term nrmG[r nrmRS + blk].
+// out[i] = sum_b part[b cnt + i], b = 0 .. S-1 in order.
+cudaError_t launch_sum_parts(const float* part, int S, size_t cnt, float* out, cudaStream_t st);
 cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR,
                            int nT, int G, int nBlocks, const float* nrmG,
                            int nrmRS, const double* x0,
@@ -467,7 +477,8 @@ cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, lo
                                int M, int N, int Kd, int items, int aRowsPerItem,
                                int bRowsPerItem, int nTotal, float* C, long long sC, int ldc,
                                const float* nrm, long long sN, float alpha, int* flag,
-                               cudaStream_t st, int cGroup = 0, long long cGroupStride = 0);
+                               cudaStream_t st, int cGroup = 0, long long cGroupStride = 0,
+                               bool pair = false);
 
 }  // namespace tg3
 

@@ -1886,6 +1886,27 @@ cudaError_t launch_gemm_nt_fp32(const float* A, long long sA, int lda, const flo
     return cudaGetLastError();
 }
 
+// out[i] = sum over the S partial results part[b][i], b = 0 .. S-1 in order
+// (the split-K chunks of a GEMM).
+__global__ void k_sum_parts(const float* __restrict__ part, int S, size_t cnt,
+                            float* __restrict__ out)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < cnt;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float v = part[i];
+        for (int b = 1; b < S; b++) v += part[(size_t)b * cnt + i];
+        out[i] = v;
+    }
+}
+
+cudaError_t launch_sum_parts(const float* part, int S, size_t cnt, float* out, cudaStream_t st)
+{
+    if (S < 1) return cudaErrorInvalidValue;
+    const unsigned blocks = (unsigned)std::min<size_t>((cnt + 255) / 256, 152 * 16);
+    k_sum_parts<<<blocks, 256, 0, st>>>(part, S, cnt, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR, int nT, int G,
                            int nBlocks, const float* nrmG, int nrmRS, const double* x0,
                            const double* pwR,

@@ -51,6 +51,8 @@ OPT_FUSED = 0
 OPT_INSERT_GATHER = 1
 OPT_BANK_GATHER = 2
 OPT_BANK_ORDER = 3
+OPT_SCAN_TILE_N = 4
+OPT_SCAN_PAIR = 5
 
 
 class TG3Error(RuntimeError):
