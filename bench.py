@@ -1290,6 +1290,7 @@ def run_learned(args, rank, world, local_rank):
     ctx.set_option(tg3.OPT_BANK_GATHER, args.bank_form)
     ctx.set_option(tg3.OPT_BANK_ORDER, args.bank_order)
     ctx.set_option(tg3.OPT_SCAN_PAIR, args.scan_pair)
+    ctx.set_option(tg3.OPT_SCAN_BK, args.scan_bk)
     for c, bm in enumerate(maps):
         ctx.set_volume(c, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
     ctx.set_pixels(iCol, iRow, box)
@@ -2243,6 +2244,8 @@ def main():
     ap.add_argument("--scan-pair", type=int, default=0, choices=[0, 1],
                     help="TG3_OPT_SCAN_PAIR: the global search's cross term on CTA pairs that "
                          "share each column tile by TMA multicast")
+    ap.add_argument("--scan-bk", type=int, default=32, choices=[32, 64],
+                    help="TG3_OPT_SCAN_BK: K block of the global search's cross-term stages")
     ap.add_argument("--bank-order", type=int, default=1, choices=[0, 1],
                     help="TG3_OPT_BANK_ORDER: particles visited sorted by first proposed row")
     ap.add_argument("--no-local", action="store_true",

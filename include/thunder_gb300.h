@@ -339,14 +339,19 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  * TG3_OPT_SCAN_PAIR (default 0): 1 runs that cross term on pairs of CTAs
  *   (a thread-block cluster of two on neighbouring row tiles) that share
  *   each column tile: each CTA loads half of it, multicast to both, halving
- *   the bytes the column operand takes from L2.  Same results. */
+ *   the bytes the column operand takes from L2.  Same results.
+ * TG3_OPT_SCAN_BK (default 32): the K block of that cross term's pipeline
+ *   stages, 64 bf16 (128-byte rows, 128-byte swizzle) or 32 (64-byte rows,
+ *   64-byte swizzle: half the bytes a stage, twice the stages in flight).
+ *   Same products in the same order. */
 enum {
     TG3_OPT_FUSED = 0,
     TG3_OPT_INSERT_GATHER = 1,
     TG3_OPT_BANK_GATHER = 2,
     TG3_OPT_BANK_ORDER = 3,
     TG3_OPT_SCAN_TILE_N = 4,
-    TG3_OPT_SCAN_PAIR = 5
+    TG3_OPT_SCAN_PAIR = 5,
+    TG3_OPT_SCAN_BK = 6
 };
 int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);

@@ -390,12 +390,17 @@ def test_bad_geometry_rejected(small):
 
 
 @pytest.mark.parametrize("precision", [tg3.SCORE_FP32, tg3.SCORE_BF16X3])
-def test_global_scan(small, ctx, precision):
+@pytest.mark.parametrize("shape", [(40, 70), (5, 1024)])
+def test_global_scan(small, ctx, precision, shape):
     """Device global scan (shared rotations x translations for many images)
-    against the oracle's doGlobalSearch restatement."""
+    against the oracle's doGlobalSearch restatement.  40 images x 70
+    rotations: 360 columns, two split-bf16 column tiles; 5 images x 1,024
+    rotations: so few images that each image's rotations are weighed by
+    several CTAs and folded (k_merge_chunks)."""
     rng = np.random.default_rng(41)
     st = small["st"]
-    nImg, nR, nT = 40, 70, 9     # 360 columns: two split-bf16 column tiles
+    nImg, nR = shape
+    nT = 9
     q = synth.haar_quaternions(rng, nR)
     mat = np.ascontiguousarray(O.rotmat(q).reshape(-1, 9))
     trans = synth.global_translations(1, 1.0)
@@ -428,16 +433,18 @@ def test_global_scan(small, ctx, precision):
         np.testing.assert_allclose(a, b / b.sum(), atol=2e-3)
 
 
-@pytest.mark.parametrize("form", [(0, 1), (128, 0), (128, 1), (64, 1)])
+@pytest.mark.parametrize("form", [(0, 1, 64), (128, 0, 64), (128, 1, 64), (64, 1, 64),
+                                  (0, 0, 32), (0, 1, 32)])
 def test_global_scan_tile_forms(small, ctx, form):
     """The split-bf16 global scan's cross term with a narrower column tile
-    (TG3_OPT_SCAN_TILE_N) and on CTA pairs that share each column tile by TMA
+    (TG3_OPT_SCAN_TILE_N), on CTA pairs that share each column tile by TMA
     multicast (TG3_OPT_SCAN_PAIR; 300 rotations = 3 row tiles, so one pair
-    holds a tile past the last row) against the default form on the same
-    inputs.  The pair form issues the same MMAs in the same order: the same
-    log-likelihoods to the last bit.  A narrower tile changes the MMA shape,
-    so its sums may round differently: log-likelihoods within 1e-6 relative,
-    weights within 1e-4."""
+    holds a tile past the last row) and with 32-wide K blocks in 64-byte
+    swizzled stages (TG3_OPT_SCAN_BK) against the default form on the same
+    inputs.  The pair and K-block forms issue the same MMAs in the same
+    order: the same log-likelihoods to the last bit.  A narrower tile changes
+    the MMA shape, so its sums may round differently: log-likelihoods within
+    1e-6 relative, weights within 1e-4."""
     rng = np.random.default_rng(43)
     st = small["st"]
     nImg, nR, nT = 30, 300, 9
@@ -449,9 +456,10 @@ def test_global_scan_tile_forms(small, ctx, form):
     args = [dev(st.dat[:nImg].astype(np.complex64)), dev(st.ctf[:nImg].astype(np.float32)),
             dev(st.sigRcp[:nImg].astype(np.float32)), dev(mat), dev(trans), dev(pR), dev(pT)]
 
-    def run(tile_n, pair):
+    def run(tile_n, pair, bk):
         ctx.set_option(tg3.OPT_SCAN_TILE_N, tile_n)
         ctx.set_option(tg3.OPT_SCAN_PAIR, pair)
+        ctx.set_option(tg3.OPT_SCAN_BK, bk)
         o = dict(wC=torch.empty(nImg, dtype=torch.float64, device=DEV),
                  wR=torch.empty((nImg, nR), dtype=torch.float64, device=DEV),
                  wT=torch.empty((nImg, nT), dtype=torch.float64, device=DEV),
@@ -463,10 +471,11 @@ def test_global_scan_tile_forms(small, ctx, form):
         return {k: v.cpu().numpy() for k, v in o.items()}
 
     try:
-        a, b = run(*form), run(0, 0)
+        a, b = run(*form), run(0, 0, 64)
     finally:
         ctx.set_option(tg3.OPT_SCAN_TILE_N, 0)
         ctx.set_option(tg3.OPT_SCAN_PAIR, 0)
+        ctx.set_option(tg3.OPT_SCAN_BK, 32)
     for k in ("dvp", "wC", "wR", "wT", "base"):
         if form[0] == 0:
             np.testing.assert_array_equal(a[k], b[k])

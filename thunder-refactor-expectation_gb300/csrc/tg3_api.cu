@@ -1804,6 +1804,10 @@ extern "C" int tg3_ctx_set_option(tg3_ctx* c, int option, int value)
         c->scanTileN = value;
     }
     else if (option == TG3_OPT_SCAN_PAIR) c->scanPair = value != 0;
+    else if (option == TG3_OPT_SCAN_BK) {
+        if (value != 32 && value != 64) return fail(TG3_ERR_ARG, "TG3_OPT_SCAN_BK takes 32 or 64");
+        c->scanBK = value;
+    }
     else return fail(TG3_ERR_ARG, "unknown option");
     return TG3_OK;
 }
@@ -2033,7 +2037,8 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
                 const int items = (cols + Nt - 1) / Nt;
                 TG3_CUDA(launch_gemm_bf16x3(P, nRt, A, (long long)cols, nRt, Nt, Kp, items, 0, Nt,
                                             cols, D, 0, nT, nullptr, 0, -2.0f, c->d_flag, s, nT,
-                                            (long long)nRt * nT, c->scanPair != 0));
+                                            (long long)nRt * nT, c->scanPair != 0,
+                                            Kp % c->scanBK == 0 ? c->scanBK : 64));
             } else {
                 TG3_CUDA(launch_gemm_nt_fp32(P, 0, Kp, A, 0, Kp, nRt, cols, Kp, 1, D, 0, nT,
                                              nullptr, 0, -2.0f, s, nT, (long long)nRt * nT));
@@ -2042,10 +2047,22 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
         {
             StageTimer tm(c, TG3_STAGE_WEIGHTS);
             if (nK == 1) {
+                // few images (the fallback particles of one class): each
+                // image's rotations over several CTAs, so the GPU fills
+                int nc = 1;
+                if (n < 2 * 152 && nR >= 512)
+                    nc = std::min(std::min(16, nR / 256), (2 * 152 + n - 1) / n);
+                double* tmp = nullptr;
+                if (nc > 1) {
+                    tmp = (double*)ws_get(c, WS_WCHUNK,
+                                          sizeof(double) * weights_chunk_doubles(n, nc, nT), &st);
+                    if (!tmp) return st;
+                }
                 TG3_CUDA(launch_weights(D, (long long)nR * nT, nT, nR, nT, 1, n, nrmG, n, x0 + l0,
                                         pR, 0, pT, 0, nullptr, wC + l0, wR + (size_t)l0 * nR,
                                         wT + (size_t)l0 * nT, baseL + l0,
-                                        dvp ? dvp + (size_t)l0 * nR * nT : nullptr, s));
+                                        dvp ? dvp + (size_t)l0 * nR * nT : nullptr, s, 512, nc,
+                                        tmp));
             } else {
                 // one block per (image, class): D[l][k nR + r][t] is block l nK + k
                 const size_t b0 = (size_t)l0 * nK;

@@ -92,6 +92,7 @@ enum WsSlot {
     WS_ORDER,        // bank-row cross term: the particles' visiting order
     WS_RENDER,       // reference rendering: image grid, projections, real images
     WS_SPLITK,       // split-K partial sums of the global search's norm term
+    WS_WCHUNK,       // per-chunk weights of a row-split weights launch
     WS_COUNT
 };
 
@@ -194,6 +195,7 @@ struct tg3_ctx {
     int bankOrder = 0;            // TG3_OPT_BANK_ORDER
     int scanTileN = 0;            // TG3_OPT_SCAN_TILE_N (0: 256)
     int scanPair = 0;             // TG3_OPT_SCAN_PAIR
+    int scanBK = 32;              // TG3_OPT_SCAN_BK
     // per-stage event timing (tg3_ctx_set_timing)
     bool timing = false;
     // inside the learned E-step's fallback: its cross-term launches are
@@ -328,7 +330,13 @@ cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR,
                            const double* pwR, long long sR, const double* pwT,
                            long long sT, const double* pwC, double* wC,
                            double* wR, double* wT, double* base, float* dvp,
-                           cudaStream_t st, int threads = 512);
+                           cudaStream_t st, int threads = 512, int nc = 1,
+                           double* chunkTmp = nullptr);
+// doubles of chunkTmp launch_weights needs for nBlocks items of nc chunks
+inline size_t weights_chunk_doubles(int nBlocks, int nc, int nT)
+{
+    return (size_t)nBlocks * nc * (2 + (size_t)nT);
+}
 cudaError_t launch_resample(int nP, int n, const double* u, const double* w,
                             const int* perm, const double* u0,
                             const double* peak, int nOut, int* src,
@@ -478,7 +486,7 @@ cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, lo
                                int bRowsPerItem, int nTotal, float* C, long long sC, int ldc,
                                const float* nrm, long long sN, float alpha, int* flag,
                                cudaStream_t st, int cGroup = 0, long long cGroupStride = 0,
-                               bool pair = false);
+                               bool pair = false, int bk = 64);
 
 }  // namespace tg3
 

@@ -871,7 +871,7 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
           const double* __restrict__ pwR, long long sR,
           const double* __restrict__ pwT, long long sT, const double* __restrict__ pwC,
           double* __restrict__ wC, double* __restrict__ wR, double* __restrict__ wT,
-          double* __restrict__ base, float* __restrict__ dvp)
+          double* __restrict__ base, float* __restrict__ dvp, int nc)
 {
     extern __shared__ float wsm[];
     float* wTs = wsm;                // [nT]
@@ -879,12 +879,22 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
     float* wTw = pTs + nT;           // [warps][nT] when TS > 0: per-warp sums, added in order
     __shared__ float redf[32];
     __shared__ double red[32];
+    // nc > 1: the rows of item blk / nc are cut into nc chunks, one per CTA;
+    // wC, wT, base are then per chunk (relative to the chunk's maximum) and
+    // k_merge_chunks folds them; wR and dvp rows go straight to the item's
     const int blk = blockIdx.x;
-    const int b = blk / G, g = blk % G;
-    const float* Db = D + b * sD + (size_t)g * nT;
-    const double* pr = pwR + blk * sR;
-    const double* pt = pwT + blk * sT;
-    const double pc = pwC ? pwC[blk] : 1.0;
+    const int item = blk / nc, chunk = blk % nc;
+    const int rpb = (nR + nc - 1) / nc;
+    const int r0c = min(nR, chunk * rpb);
+    const int nRc = min(nR, r0c + rpb) - r0c;
+    const int b = item / G, g = item % G;
+    const float* Db = D + b * sD + (size_t)g * nT + (size_t)r0c * ldc;
+    const double* pr = pwR + item * sR + r0c;
+    const double* pt = pwT + item * sT;
+    const double pc = pwC ? pwC[item] : 1.0;
+    const float* nrmB = nrmG ? nrmG + (size_t)r0c * nrmRS : nullptr;
+    const int nRall = nR;
+    nR = nRc;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int t = threadIdx.x; t < nT; t += blockDim.x) {
         wTs[t] = 0.f;
@@ -897,7 +907,7 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const int r = r0 + q * nw;
-            const float ad = (r < nR && nrmG) ? nrmG[(size_t)r * nrmRS + blk] : 0.f;
+            const float ad = (r < nR && nrmB) ? nrmB[(size_t)r * nrmRS + item] : 0.f;
             const float* row = Db + (size_t)(r < nR ? r : 0) * ldc;
 #pragma unroll
             for (int j = 0; j < (TS > 0 ? TS : 1); j++) {
@@ -922,7 +932,7 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
     }
     __syncthreads();
     const float M = redf[0];
-    const double x0b = x0 ? x0[blk] : 0.0;
+    const double x0b = x0 ? x0[item] : 0.0;
     // pass 2: marginals
     float tacc[TS > 0 ? TS : 1], ptv[TS > 0 ? TS : 1];
 #pragma unroll
@@ -940,7 +950,7 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
             const int r = r0 + q * nw;
             const bool rok = r < nR;
             prr[q] = rok ? (float)pr[r] : 0.f;
-            ad[q] = (rok && nrmG) ? nrmG[(size_t)r * nrmRS + blk] : 0.f;
+            ad[q] = (rok && nrmB) ? nrmB[(size_t)r * nrmRS + item] : 0.f;
             const float* row = Db + (size_t)(rok ? r : 0) * ldc;
 #pragma unroll
             for (int j = 0; j < (TS > 0 ? TS : 1); j++) {
@@ -963,7 +973,9 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
                         const float sv = __expf(d - M);
                         racc = fmaf(sv, ptv[j], racc);
                         tacc[j] = fmaf(sv, prr[q], tacc[j]);
-                        if (dvp) dvp[((size_t)blk * nR + r) * nT + t] = (float)(x0b + (double)d);
+                        if (dvp)
+                            dvp[((size_t)item * nRall + r0c + r) * nT + t] =
+                                (float)(x0b + (double)d);
                     }
                 }
             } else {
@@ -972,12 +984,14 @@ k_weights(const float* __restrict__ D, long long sD, int ldc, int nR, int nT, in
                     const float sv = __expf(d - M);
                     racc = fmaf(sv, pTs[t], racc);
                     atomicAdd(wTs + t, sv * prr[q]);
-                    if (dvp) dvp[((size_t)blk * nR + r) * nT + t] = (float)(x0b + (double)d);
+                    if (dvp)
+                        dvp[((size_t)item * nRall + r0c + r) * nT + t] =
+                            (float)(x0b + (double)d);
                 }
             }
             racc = warp_sum(racc);
             cacc = fmaf(racc, prr[q], cacc);   // sum_t s pT[t] pR[r], once per row
-            if (lane == 0) wR[(size_t)blk * nR + r] = (double)racc * pc;
+            if (lane == 0) wR[(size_t)item * nRall + r0c + r] = (double)racc * pc;
         }
     }
     if (TS > 0) {
@@ -1907,26 +1921,68 @@ cudaError_t launch_sum_parts(const float* part, int S, size_t cnt, float* out, c
     return cudaGetLastError();
 }
 
+// Fold the row chunks of k_weights (nc per item): M = max_c base_c, every
+// chunk scaled by exp(base_c - M): wC, wT summed over the chunks in order, the
+// chunk's wR rows rescaled in place, base = M.  One CTA per item.
+__global__ void k_merge_chunks(int nc, int nR, int nT, const double* __restrict__ wCc,
+                               const double* __restrict__ wTc, const double* __restrict__ basec,
+                               double* __restrict__ wC, double* __restrict__ wR,
+                               double* __restrict__ wT, double* __restrict__ base)
+{
+    extern __shared__ double sc[];   // [nc]
+    const int l = blockIdx.x;
+    const double* bc = basec + (size_t)l * nc;
+    double M = bc[0];
+    for (int c = 1; c < nc; c++) M = fmax(M, bc[c]);
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) sc[c] = exp(bc[c] - M);
+    __syncthreads();
+    const int rpb = (nR + nc - 1) / nc;
+    for (int r = threadIdx.x; r < nR; r += blockDim.x) wR[(size_t)l * nR + r] *= sc[r / rpb];
+    for (int t = threadIdx.x; t < nT; t += blockDim.x) {
+        double v = 0.0;
+        for (int c = 0; c < nc; c++) v += wTc[((size_t)l * nc + c) * nT + t] * sc[c];
+        wT[(size_t)l * nT + t] = v;
+    }
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        for (int c = 0; c < nc; c++) v += wCc[(size_t)l * nc + c] * sc[c];
+        wC[l] = v;
+        base[l] = M;
+    }
+}
+
 cudaError_t launch_weights(const float* D, long long sD, int ldc, int nR, int nT, int G,
                            int nBlocks, const float* nrmG, int nrmRS, const double* x0,
                            const double* pwR,
                            long long sR, const double* pwT, long long sT, const double* pwC,
                            double* wC, double* wR, double* wT, double* base, float* dvp,
-                           cudaStream_t st, int threads)
+                           cudaStream_t st, int threads, int nc, double* chunkTmp)
 {
+    if (nc < 1 || (nc > 1 && (G != 1 || !chunkTmp))) return cudaErrorInvalidValue;
     if (threads != 128 && threads != 256 && threads != WEIGHTS_THREADS)
         return cudaErrorInvalidValue;
     const size_t smem = sizeof(float) * (2 + (nT <= 256 ? threads / 32 : 0)) * (size_t)nT;
     if (smem > 48 * 1024) return cudaErrorInvalidValue;
+    // nc > 1: per-chunk wC, wT, base in chunkTmp, folded afterwards
+    double* cC = nc > 1 ? chunkTmp : wC;
+    double* cB = nc > 1 ? chunkTmp + (size_t)nBlocks * nc : base;
+    double* cT = nc > 1 ? chunkTmp + 2 * (size_t)nBlocks * nc : wT;
 #define TG3_WEIGHTS(TS)                                                                        \
-    k_weights<TS><<<nBlocks, threads, smem, st>>>(D, sD, ldc, nR, nT, G, nrmG, nrmRS, x0, pwR, \
-                                                  sR, pwT, sT, pwC, wC, wR, wT, base, dvp)
+    k_weights<TS><<<nBlocks * nc, threads, smem, st>>>(D, sD, ldc, nR, nT, G, nrmG, nrmRS, x0, \
+                                                       pwR, sR, pwT, sT, pwC, cC, wR, cT, cB,  \
+                                                       dvp, nc)
     if (nT <= 32) TG3_WEIGHTS(1);
     else if (nT <= 64) TG3_WEIGHTS(2);
     else if (nT <= 128) TG3_WEIGHTS(4);
     else if (nT <= 256) TG3_WEIGHTS(8);
     else TG3_WEIGHTS(0);
 #undef TG3_WEIGHTS
+    if (nc > 1) {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        k_merge_chunks<<<nBlocks, 128, sizeof(double) * nc, st>>>(nc, nR, nT, cC, cT, cB, wC, wR,
+                                                                  wT, base);
+    }
     return cudaGetLastError();
 }
 

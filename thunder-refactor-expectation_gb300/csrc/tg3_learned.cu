@@ -67,9 +67,43 @@ __device__ __forceinline__ double sorted_median(const float* v, int n)
     return (n & 1) ? (double)v[n / 2] : 0.5 * ((double)v[n / 2 - 1] + (double)v[n / 2]);
 }
 
+// The deviations |v - med| of the sorted values v[0 .. n) (rounded to float)
+// form two ascending runs: med - v[s - 1 - j] over the s values below med,
+// and v[s + j] - med over the rest.  dev_kth returns the k-th smallest
+// (0-based) of their union by a binary search over how many come from the
+// left run -- the same value a sort of all n deviations would put at k.
+__device__ __forceinline__ float dev_left(const float* v, int s, double med, int j)
+{
+    return (float)fabs((double)v[s - 1 - j] - med);
+}
+
+__device__ __forceinline__ float dev_right(const float* v, int s, double med, int j)
+{
+    return (float)fabs((double)v[s + j] - med);
+}
+
+__device__ float dev_kth(const float* v, int n, int s, double med, int k)
+{
+    const int a = s, b = n - s;
+    int lo = max(0, k + 1 - b), hi = min(k + 1, a);   // values taken from the left run
+    while (lo < hi) {
+        const int i = (lo + hi) >> 1, j = k + 1 - i;
+        if (i < a && j > 0 && dev_left(v, s, med, i) < dev_right(v, s, med, j - 1))
+            lo = i + 1;
+        else
+            hi = i;
+    }
+    const int i = lo, j = k + 1 - lo;
+    float x = -CUDART_INF_F;
+    if (i > 0) x = dev_left(v, s, med, i - 1);
+    if (j > 0) x = fmaxf(x, dev_right(v, s, med, j - 1));
+    return x;
+}
+
 // One CTA per particle: the confidence of its n rescored hypotheses,
 // (max - median) / (1.4826 (MAD + 1e-12)), MAD the median absolute
 // deviation from the median.  nPow2 >= n is a power of two (shared floats).
+// One sort: the deviations' median comes from the sorted values (dev_kth).
 __global__ void __launch_bounds__(512)
 k_peak_score(const float* __restrict__ dvp, int n, int nPow2, float* __restrict__ peak)
 {
@@ -78,20 +112,25 @@ k_peak_score(const float* __restrict__ dvp, int n, int nPow2, float* __restrict_
     for (int i = threadIdx.x; i < nPow2; i += blockDim.x) v[i] = i < n ? d[i] : CUDART_INF_F;
     __syncthreads();
     bitonic_sort_asc(v, nPow2);
-    __shared__ double sMed, sMax;
     if (threadIdx.x == 0) {
-        sMed = sorted_median(v, n);
-        sMax = v[n - 1];
-    }
-    __syncthreads();
-    const double med = sMed;
-    for (int i = threadIdx.x; i < nPow2; i += blockDim.x)
-        v[i] = i < n ? (float)fabs((double)v[i] - med) : CUDART_INF_F;
-    __syncthreads();
-    bitonic_sort_asc(v, nPow2);
-    if (threadIdx.x == 0) {
-        const double mad = sorted_median(v, n) + 1e-12;
-        peak[blockIdx.x] = (float)((sMax - med) / (1.4826 * mad));
+        const double med = sorted_median(v, n);
+        const double mx = v[n - 1];
+        float out = CUDART_NAN_F;
+        if (!isnan(med) && !isnan(mx)) {
+            // s: the first value not below the median
+            int lo = 0, hi = n;
+            while (lo < hi) {
+                const int m = (lo + hi) >> 1;
+                if ((double)v[m] < med) lo = m + 1;
+                else hi = m;
+            }
+            const int s = lo;
+            const double madv = (n & 1) ? (double)dev_kth(v, n, s, med, n / 2)
+                                        : 0.5 * ((double)dev_kth(v, n, s, med, n / 2 - 1) +
+                                                 (double)dev_kth(v, n, s, med, n / 2));
+            out = (float)((mx - med) / (1.4826 * (madv + 1e-12)));
+        }
+        peak[blockIdx.x] = out;
     }
 }
 

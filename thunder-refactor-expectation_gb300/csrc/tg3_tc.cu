@@ -50,6 +50,16 @@ struct TcParams {
     int* flag;
 };
 
+// K-major operand descriptors: 128-byte rows with the 128-byte swizzle
+// (K blocks of 64 bf16) or 64-byte rows with the 64-byte swizzle (K blocks
+// of 32, half the stage bytes and so twice the stages in flight).
+template <int BK>
+__device__ __forceinline__ uint64_t desc(uint32_t saddr)
+{
+    return BK == 64 ? umma_desc(saddr) : umma_desc_sw64(saddr);
+}
+
+template <int BK>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_bf16x3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
               const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
@@ -59,8 +69,8 @@ k_gemm_bf16x3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ 
     // 1024-byte aligned stage buffers
     uint8_t* smem = reinterpret_cast<uint8_t*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    const int aBytes = TC_M * TC_BK * 2;                  // 16 KB
-    const int bBytes = p.ntile * TC_BK * 2;               // ntile * 128 B
+    const int aBytes = TC_M * BK * 2;                  // 16 KB (BK 64) or 8 KB (32)
+    const int bBytes = p.ntile * BK * 2;               // ntile rows of 2 BK bytes
     const int stageBytes = 2 * aBytes + 2 * bBytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + p.stages * stageBytes);
     uint64_t* empty = full + p.stages;
@@ -73,7 +83,7 @@ k_gemm_bf16x3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ 
     const int aRow0 = item * p.aRowsPerItem + mtile * TC_M;
     const int bRow0 = item * p.bRowsPerItem;
     const int nValid = p.nTotal > 0 ? min(p.N, p.nTotal - item * p.N) : p.N;
-    const int nkb = p.Kd / TC_BK;
+    const int nkb = p.Kd / BK;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < p.stages; s++) {
@@ -111,10 +121,10 @@ k_gemm_bf16x3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ 
             if (*(volatile int*)abortFlag) break;
             uint8_t* st = smem + s * stageBytes;
             mbar_expect_tx(full + s, stageBytes);
-            tma_load_2d(st, &tmAh, full + s, kb * TC_BK, aRow0);
-            tma_load_2d(st + aBytes, &tmAl, full + s, kb * TC_BK, aRow0);
-            tma_load_2d(st + 2 * aBytes, &tmBh, full + s, kb * TC_BK, bRow0);
-            tma_load_2d(st + 2 * aBytes + bBytes, &tmBl, full + s, kb * TC_BK, bRow0);
+            tma_load_2d(st, &tmAh, full + s, kb * BK, aRow0);
+            tma_load_2d(st + aBytes, &tmAl, full + s, kb * BK, aRow0);
+            tma_load_2d(st + 2 * aBytes, &tmBh, full + s, kb * BK, bRow0);
+            tma_load_2d(st + 2 * aBytes + bBytes, &tmBl, full + s, kb * BK, bRow0);
             issuedTma = kb + 1;
         }
     } else if (warp == 1 && lane == 0) {
@@ -134,12 +144,12 @@ k_gemm_bf16x3(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ 
             const uint32_t ah = smem_u32(st), al = smem_u32(st + aBytes);
             const uint32_t bh = smem_u32(st + 2 * aBytes), bl = smem_u32(st + 2 * aBytes + bBytes);
 #pragma unroll
-            for (int kk = 0; kk < TC_BK / 16; kk++) {
+            for (int kk = 0; kk < BK / 16; kk++) {
                 const uint32_t off = kk * 32;      // 16 bf16 = 32 bytes along K
-                umma_bf16(tmem, umma_desc(ah + off), umma_desc(bh + off), idesc,
+                umma_bf16(tmem, desc<BK>(ah + off), desc<BK>(bh + off), idesc,
                           (kb | kk) != 0);
-                umma_bf16(tmem, umma_desc(ah + off), umma_desc(bl + off), idesc, 1);
-                umma_bf16(tmem, umma_desc(al + off), umma_desc(bh + off), idesc, 1);
+                umma_bf16(tmem, desc<BK>(ah + off), desc<BK>(bl + off), idesc, 1);
+                umma_bf16(tmem, desc<BK>(al + off), desc<BK>(bh + off), idesc, 1);
             }
             umma_commit(empty + s);        // stage free once these MMAs have read it
             issuedMma = kb + 1;
@@ -258,6 +268,7 @@ __device__ __forceinline__ void umma_commit_mc(uint64_t* bar, uint16_t mask)
         : "memory");
 }
 
+template <int BK>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_bf16x3_pair(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                    const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
@@ -266,8 +277,8 @@ k_gemm_bf16x3_pair(const __grid_constant__ CUtensorMap tmAh, const __grid_consta
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    const int aBytes = TC_M * TC_BK * 2;
-    const int bBytes = p.ntile * TC_BK * 2;
+    const int aBytes = TC_M * BK * 2;
+    const int bBytes = p.ntile * BK * 2;
     const int halfRows = p.ntile / 2;                     // B rows each CTA loads
     const int stageBytes = 2 * aBytes + 2 * bBytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + p.stages * stageBytes);
@@ -283,7 +294,7 @@ k_gemm_bf16x3_pair(const __grid_constant__ CUtensorMap tmAh, const __grid_consta
     const int aRow0 = item * p.aRowsPerItem + mtile * TC_M;
     const int bRow0 = item * p.bRowsPerItem + (int)rank * halfRows;
     const int nValid = p.nTotal > 0 ? min(p.N, p.nTotal - item * p.N) : p.N;
-    const int nkb = p.Kd / TC_BK;
+    const int nkb = p.Kd / BK;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < p.stages; s++) {
@@ -321,11 +332,11 @@ k_gemm_bf16x3_pair(const __grid_constant__ CUtensorMap tmAh, const __grid_consta
             if (*(volatile int*)abortFlag) break;
             uint8_t* st = smem + s * stageBytes;
             mbar_expect_tx(full + s, stageBytes);
-            tma_load_2d(st, &tmAh, full + s, kb * TC_BK, aRow0);
-            tma_load_2d(st + aBytes, &tmAl, full + s, kb * TC_BK, aRow0);
-            uint8_t* bh = st + 2 * aBytes + (size_t)rank * halfRows * 128;
-            tma_load_2d_mc(bh, &tmBh, full + s, kb * TC_BK, bRow0, both);
-            tma_load_2d_mc(bh + bBytes, &tmBl, full + s, kb * TC_BK, bRow0, both);
+            tma_load_2d(st, &tmAh, full + s, kb * BK, aRow0);
+            tma_load_2d(st + aBytes, &tmAl, full + s, kb * BK, aRow0);
+            uint8_t* bh = st + 2 * aBytes + (size_t)rank * halfRows * BK * 2;
+            tma_load_2d_mc(bh, &tmBh, full + s, kb * BK, bRow0, both);
+            tma_load_2d_mc(bh + bBytes, &tmBl, full + s, kb * BK, bRow0, both);
             issuedTma = kb + 1;
         }
     } else if (warp == 1 && lane == 0) {
@@ -344,12 +355,12 @@ k_gemm_bf16x3_pair(const __grid_constant__ CUtensorMap tmAh, const __grid_consta
             const uint32_t ah = smem_u32(st), al = smem_u32(st + aBytes);
             const uint32_t bh = smem_u32(st + 2 * aBytes), bl = smem_u32(st + 2 * aBytes + bBytes);
 #pragma unroll
-            for (int kk = 0; kk < TC_BK / 16; kk++) {
+            for (int kk = 0; kk < BK / 16; kk++) {
                 const uint32_t off = kk * 32;
-                umma_bf16(tmem, umma_desc(ah + off), umma_desc(bh + off), idesc,
+                umma_bf16(tmem, desc<BK>(ah + off), desc<BK>(bh + off), idesc,
                           (kb | kk) != 0);
-                umma_bf16(tmem, umma_desc(ah + off), umma_desc(bl + off), idesc, 1);
-                umma_bf16(tmem, umma_desc(al + off), umma_desc(bh + off), idesc, 1);
+                umma_bf16(tmem, desc<BK>(ah + off), desc<BK>(bl + off), idesc, 1);
+                umma_bf16(tmem, desc<BK>(al + off), desc<BK>(bh + off), idesc, 1);
             }
             umma_commit_mc(empty + s, both);     // frees the stage in both CTAs' count
             issuedMma = kb + 1;
@@ -432,9 +443,11 @@ cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, lo
                                int M, int N, int Kd, int items, int aRowsPerItem,
                                int bRowsPerItem, int nTotal, float* C, long long sC, int ldc,
                                const float* nrm, long long sN, float alpha, int* flag,
-                               cudaStream_t st, int cGroup, long long cGroupStride, bool pair)
+                               cudaStream_t st, int cGroup, long long cGroupStride, bool pair,
+                               int bk)
 {
-    if (N <= 0 || N > 256 || M <= 0 || items <= 0 || Kd <= 0 || Kd % TC_BK)
+    if (bk != 64 && bk != 32) return cudaErrorInvalidValue;
+    if (N <= 0 || N > 256 || M <= 0 || items <= 0 || Kd <= 0 || Kd % bk)
         return cudaErrorInvalidValue;
     const __nv_bfloat16* Ah = reinterpret_cast<const __nv_bfloat16*>(A);
     const __nv_bfloat16* Al = Ah + rowsA * Kd;
@@ -453,9 +466,10 @@ cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, lo
     p.ntile = (N + 15) / 16 * 16;
     p.tmemCols = 32;
     while (p.tmemCols < p.ntile) p.tmemCols <<= 1;
-    const int stageBytes = 2 * TC_M * TC_BK * 2 + 2 * p.ntile * TC_BK * 2;
+    const int stageBytes = 2 * TC_M * bk * 2 + 2 * p.ntile * bk * 2;
     p.stages = (200 * 1024) / stageBytes;
-    if (p.stages > 4) p.stages = 4;
+    const int maxStages = bk == 64 ? 4 : 6;
+    if (p.stages > maxStages) p.stages = maxStages;
     if (p.stages < 2) return cudaErrorInvalidValue;
     // the epilogue stages 128 rows of ntile + 1 floats in the pipeline buffers
     if ((size_t)TC_M * (p.ntile + 1) * 4 > (size_t)p.stages * stageBytes) return cudaErrorInvalidValue;
@@ -466,9 +480,12 @@ cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, lo
     p.sN = sN;
     p.alpha = alpha;
     p.flag = flag;
+    const bool sw64 = bk == 32;
     CUtensorMap mAh, mAl, mBh, mBl;
-    if (!tc::make_map(&mAh, Ah, rowsA, Kd, TC_M) || !tc::make_map(&mAl, Al, rowsA, Kd, TC_M) ||
-        !tc::make_map(&mBh, Bh, rowsB, Kd, p.ntile) || !tc::make_map(&mBl, Bl, rowsB, Kd, p.ntile))
+    if (!tc::make_map(&mAh, Ah, rowsA, Kd, TC_M, bk, sw64) ||
+        !tc::make_map(&mAl, Al, rowsA, Kd, TC_M, bk, sw64) ||
+        !tc::make_map(&mBh, Bh, rowsB, Kd, p.ntile, bk, sw64) ||
+        !tc::make_map(&mBl, Bl, rowsB, Kd, p.ntile, bk, sw64))
         return cudaErrorInvalidValue;
     const size_t smem = 1024 + (size_t)p.stages * stageBytes + 256;
     const int mTiles = (M + TC_M - 1) / TC_M;
@@ -477,11 +494,13 @@ cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, lo
         // rows past M, zero-filled by TMA and not stored); each loads half of
         // the B rows, multicast to both
         CUtensorMap hBh, hBl;
-        if (!tc::make_map(&hBh, Bh, rowsB, Kd, p.ntile / 2) ||
-            !tc::make_map(&hBl, Bl, rowsB, Kd, p.ntile / 2))
+        if (!tc::make_map(&hBh, Bh, rowsB, Kd, p.ntile / 2, bk, sw64) ||
+            !tc::make_map(&hBl, Bl, rowsB, Kd, p.ntile / 2, bk, sw64))
             return cudaErrorInvalidValue;
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16x3_pair,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        void (*kern)(const CUtensorMap, const CUtensorMap, const CUtensorMap, const CUtensorMap,
+                     const TcParams) = bk == 64 ? k_gemm_bf16x3_pair<64> : k_gemm_bf16x3_pair<32>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
         if (e != cudaSuccess) return e;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)((mTiles + 1) / 2 * 2), (unsigned)items);
@@ -495,13 +514,15 @@ cudaError_t launch_gemm_bf16x3(const void* A, long long rowsA, const void* B, lo
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, k_gemm_bf16x3_pair, mAh, mAl, hBh, hBl, p);
+        return cudaLaunchKernelEx(&cfg, kern, mAh, mAl, hBh, hBl, p);
     }
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    void (*kern)(const CUtensorMap, const CUtensorMap, const CUtensorMap, const CUtensorMap,
+                 const TcParams) = bk == 64 ? k_gemm_bf16x3<64> : k_gemm_bf16x3<32>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid(mTiles, items);
-    k_gemm_bf16x3<<<grid, TC_THREADS, smem, st>>>(mAh, mAl, mBh, mBl, p);
+    kern<<<grid, TC_THREADS, smem, st>>>(mAh, mAl, mBh, mBl, p);
     return cudaGetLastError();
 }
 

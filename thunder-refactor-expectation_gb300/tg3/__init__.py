@@ -53,6 +53,7 @@ OPT_BANK_GATHER = 2
 OPT_BANK_ORDER = 3
 OPT_SCAN_TILE_N = 4
 OPT_SCAN_PAIR = 5
+OPT_SCAN_BK = 6
 
 
 class TG3Error(RuntimeError):
