@@ -957,6 +957,93 @@ def run_bank(args, rank, world, local_rank):
     return res
 
 
+def run_fallback(args, rank, world, local_rank):
+    """The learned E-step's fallback search on its own: the global search of a
+    few particles of one class (args.batch, default 70, about one class's
+    share of the fallback particles of a 2,000-particle step) over the
+    class's bank of 6,912 rotations x 49 translations, split-bf16, at box 256
+    (cutoff 80, K = 9,930; --box for a smaller profiling case).  One step =
+    one search of the batch; stages timed by the library (the norm term, the
+    cross term, the weights)."""
+    import torch
+    import tg3
+    from tg3 import synth
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    box = args.box or 256
+    px, pf, rU = 1.1, 2, 80 * box // 256
+    nP = args.batch if args.batch != 128 else 70
+    f64 = dict(dtype=torch.float64, device=dev)
+    rng = np.random.default_rng(rank_seed(7000, rank))
+    bm = synth.blob_map(rng, 200, (1.5, 3.0), px, 80.0)
+    rL = synth.config_rL(box, px)
+    nv = synth.signal_power([bm], box, px, rU, rL, device=dev) / 0.03 / 2.0
+    ps = synth.particle_set_dev(rank_seed(7001, rank), [bm], np.zeros(nP, np.int64), box, px,
+                                rU, rL, 3.0, nv, device=dev)
+    ctx = tg3.Context(local_rank)
+    ctx.set_option(tg3.OPT_SCAN_PAIR, args.scan_pair)
+    ctx.set_option(tg3.OPT_SCAN_BK, args.scan_bk)
+    ctx.set_volume(0, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
+    ctx.set_pixels(ps.iCol, ps.iRow, box)
+    qg = synth.global_rotations(4, 36)
+    R = torch.as_tensor(synth.quat_to_mat(qg).reshape(-1, 9)).to(dev).contiguous()
+    tr = torch.as_tensor(synth.global_translations(3, 1.0), **f64).contiguous()
+    nR, nT = len(qg), len(tr)
+    pR = torch.full((nR,), 1.0 / nR, **f64)
+    pT = torch.full((nT,), 1.0 / nT, **f64)
+    o = dict(wC=torch.empty(nP, **f64), wR=torch.empty((nP, nR), **f64),
+             wT=torch.empty((nP, nT), **f64), base=torch.empty(nP, **f64))
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def step():
+        ctx.global_scan(0, nP, nR, nT, ps.dat, ps.ctf, ps.sigRcp, R, tr, pR, pT, o["wC"], o["wR"],
+                        o["wT"], o["base"], None, tg3.SCORE_BF16X3)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    ctx.set_timing(True)
+    ctx.stage_times(reset=True)
+    clk = ClockSampler(local_rank)
+    clk.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    clocks = clk.stop()
+    st = ctx.stage_times(reset=True)
+    ctx.set_timing(False)
+    ms = reduce_max(world, e0.elapsed_time(e1)) / args.steps
+    K = len(ps.iCol)
+    hbm, bf16, kind = peaks()
+    cross_ms = st["cross"][0] / max(st["cross"][1], 1)
+    flop = 4.0 * K * nP * nR * nT
+    res = {"metric": "fallback global search particles/s (learned E-step), box 256",
+           "value": round(job_rate(nP, ms, world), 1), "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "bf16x3", "data": "synthetic",
+           "config": {"workload": f"{nP} particles of one box-{box} class x {nR} rotations x "
+                                  f"{nT} translations, K = {K}",
+                      "scan_pair": args.scan_pair, "scan_bk": args.scan_bk},
+           "clocks": clocks,
+           "roofline": {"kernel": "k_gemm_bf16x3 (cross term; the norm term is stage norm)",
+                        "bound": "tensor",
+                        "achieved": round(flop / (cross_ms * 1e-3) / 1e12, 2), "peak": bf16,
+                        "unit": "TFLOP/s",
+                        "frac": round(flop / (cross_ms * 1e-3) / 1e12 / bf16, 4),
+                        "executed_bf16_tflops": round(3 * flop / (cross_ms * 1e-3) / 1e12, 1),
+                        "peak_source": f"bf16_tflops, {kind} (MEASURED_PEAKS.json)",
+                        "traffic": None, "ms_per_launch": round(cross_ms, 4)},
+           "stages": {k: round(v[0] / max(v[1], 1), 4) for k, v in st.items() if v[1]},
+           "gpu_launches": 13 * args.steps}
+    ctx.close()
+    return res
+
+
 def run_reco(args, rank, world, local_rank):
     """Reconstruction of a box-256 map from its insertion accumulators
     (Reconstructor::reconstruct): padded grid 512^3 (pf 2), Wiener filter from
@@ -1328,6 +1415,7 @@ def run_learned(args, rank, world, local_rank):
         # a network trained by an earlier run of this workload (profiling runs)
         net.set_params(np.load(args.load_net)["params"])
         label_s = train_s = 0.0
+        restarts = 0
         label_err, moves, losses = np.zeros(1), [[0.0, 0.0, 0.0]], []
     else:
         images = torch.cat(imgs)
@@ -1346,9 +1434,21 @@ def run_learned(args, rank, world, local_rank):
                                                                                box)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        losses = learned.train_match(net, images, refs, torch.as_tensor(t_lab, **f64), cls_tr,
-                                     args.epochs, 256, args.learned_lr, tau=args.learned_tau,
-                                     seed=7)
+        # a run that stays on the loss's starting plateau through its first
+        # epoch starts again from another initialisation (at most twice)
+        restarts = 0
+        while True:
+            try:
+                losses = learned.train_match(net, images, refs, torch.as_tensor(t_lab, **f64),
+                                             cls_tr, args.epochs, 256, args.learned_lr,
+                                             tau=args.learned_tau, seed=7 + restarts,
+                                             stall_check=restarts < 2)
+                break
+            except learned.TrainingStalled as ex:
+                log(f"training stalled ({ex}); new initialisation")
+                restarts += 1
+                net.close()
+                net = tg3.Cnn(local_rank, seed=4242 + restarts)
         torch.cuda.synchronize()
         train_s = time.perf_counter() - t1
         del refs, images
@@ -1703,6 +1803,7 @@ def run_learned(args, rank, world, local_rank):
                                                       world), 1),
             "refine_ms": {"plain_fp32": round(tr_p_ms, 2), "learned": round(tr_l_ms, 2)}},
         "training": {"label_s": round(label_s, 1), "train_s": round(train_s, 1),
+                     "restarts": restarts,
                      "label_median_error_deg": med(label_err),
                      "label_phase_moves_deg": [round(float(x), 3) for x in
                                                np.median(np.asarray(moves), 0)],
@@ -2212,7 +2313,8 @@ def main():
     ap.add_argument("--box", type=int, default=None, help="reduced box (profiling only)")
     ap.add_argument("--workload", default="learned256",
                     choices=["local256", "local256c3", "global64", "uneven192", "learned128",
-                             "learned256", "class2d128", "prep256", "reco256", "bank256"])
+                             "learned256", "class2d128", "prep256", "reco256", "bank256",
+                             "fallback256"])
     ap.add_argument("--train-particles", type=int, default=150000)
     ap.add_argument("--epochs", type=int, default=3)
     ap.add_argument("--learned-snr", type=float, default=1.0,
@@ -2272,6 +2374,8 @@ def main():
         res = run_reco(args, rank, world, local)
     elif args.workload == "bank256":
         res = run_bank(args, rank, world, local)
+    elif args.workload == "fallback256":
+        res = run_fallback(args, rank, world, local)
     elif args.workload in ("learned128", "learned256"):
         res = run_learned(args, rank, world, local)
         if args.workload == "learned256" and not args.no_local:

@@ -305,7 +305,9 @@ enum {
     TG3_STAGE_NETWORK = 7, /* learned E-step: network, matching, proposal confidence */
     TG3_STAGE_FALLBACK = 8,/* learned E-step: global search of the fallback particles */
     TG3_STAGE_FALLBACK_CROSS = 9, /* ... of which its cross-term GEMMs */
-    TG3_STAGE_COUNT = 10
+    TG3_STAGE_NORM = 10,   /* global search: the norm term sum sigRcp ctf^2 |P|^2 per
+                              (rotation, image), in and out of the fallback */
+    TG3_STAGE_COUNT = 11
 };
 int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
 

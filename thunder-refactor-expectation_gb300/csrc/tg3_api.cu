@@ -76,8 +76,8 @@ StageTimer::StageTimer(tg3_ctx* c_, int s) : c(c_), stage(s)
 {
     if (!c->timing) return;
     if (c->fallbackScope) {
-        if (s != TG3_STAGE_CROSS) return;
-        stage = TG3_STAGE_FALLBACK_CROSS;
+        if (s != TG3_STAGE_CROSS && s != TG3_STAGE_NORM) return;
+        if (s == TG3_STAGE_CROSS) stage = TG3_STAGE_FALLBACK_CROSS;
     }
     a = take_event(c);
     b = take_event(c);
@@ -2026,9 +2026,12 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
             TG3_LAUNCH_CHECK("norm operand");
         }
         {
-            StageTimer tm(c, TG3_STAGE_CROSS);
-            // per-(rotation, image) norm, then the cross term
+            // per-(rotation, image) norm
+            StageTimer tm(c, TG3_STAGE_NORM);
             if ((st = norm_gemm(c, abs2, sc2, nRt, n, Kq, nrmG, s))) return st;
+        }
+        {
+            StageTimer tm(c, TG3_STAGE_CROSS);
             // the cross term is written image-major: D[l][r][t]
             const int cols = n * nT;
             if (split) {

@@ -46,7 +46,7 @@ EXPORTS = [
     "tg3_PrepareTF", "tg3_image_create", "tg3_image_destroy", "tg3_ExpectLocal2D",
 ]
 STAGES = ("project", "shift", "cross", "weights", "resample", "insert", "fused", "network",
-          "fallback", "fallback_cross")
+          "fallback", "fallback_cross", "norm")
 OPT_FUSED = 0
 OPT_INSERT_GATHER = 1
 OPT_BANK_GATHER = 2

@@ -178,13 +178,26 @@ def reference_embeddings(net, refs, chunk: int = 4096):
     return z
 
 
+class TrainingStalled(RuntimeError):
+    """The matching loss did not leave its starting plateau in the first
+    epoch (stall_check): the embeddings stayed uninformative."""
+
+
 def train_match(net, images, refs, tstar, cls, epochs: int, batch: int, lr: float,
-                tau: float = 0.1, seed: int = 0, log=None):
+                tau: float = 0.1, seed: int = 0, log=None, warmup: float = 0.02,
+                stall_check: bool = False):
     """Minibatch Adam on the matching loss: particle images [n][64][64] and
     the clean references at their true rotations [n][64][64], shifts tstar
     [n][2] (device tensors); every batch holds particles of one map
-    (cls [n]), so its negatives are other poses of that map.  Cosine-decayed
-    learning rate; returns the mean loss of every epoch."""
+    (cls [n]), so its negatives are other poses of that map.  Learning rate
+    ramped up linearly over the first `warmup` fraction of the steps, then
+    cosine-decayed; returns the mean loss of every epoch.
+
+    The gradient sums use atomics, so runs differ in the last bits, and a run
+    can stay on the loss's starting plateau.  With stall_check, the first
+    epoch ends in TrainingStalled when the mean loss of its last tenth of
+    batches is above 0.95 of that of its first twentieth (the caller starts
+    again from another initialisation)."""
     import torch
     rng = np.random.default_rng(seed)
     cls = np.asarray(cls)
@@ -198,6 +211,7 @@ def train_match(net, images, refs, tstar, cls, epochs: int, batch: int, lr: floa
     dR = torch.empty_like(outP)
     k = 0
     losses = []
+    warm = max(1, int(warmup * steps))
     for e in range(epochs):
         batches = []
         for g in groups:
@@ -205,20 +219,29 @@ def train_match(net, images, refs, tstar, cls, epochs: int, batch: int, lr: floa
             batches += [p[b * batch:(b + 1) * batch] for b in range(len(g) // batch)]
         order = rng.permutation(len(batches))
         tot = 0.0
+        hist = []
         for bi in order:
             idx = torch.as_tensor(batches[bi], device=dev)
             ip, ir = images[idx].contiguous(), refs[idx].contiguous()
             net.forward(ip, outP)
             net.forward(ir, outR)
             net.zero_grads()
-            tot += net.contrastive(outP, outR, tstar[idx].contiguous(), tau, dP, dR)
+            v = net.contrastive(outP, outR, tstar[idx].contiguous(), tau, dP, dR)
+            tot += v
+            hist.append(v)
             net.backward(ip, dP)
             net.backward(ir, dR)
-            net.adam(lr * 0.5 * (1 + math.cos(math.pi * k / max(steps, 1))))
+            net.adam(lr * min(1.0, (k + 1) / warm)
+                     * 0.5 * (1 + math.cos(math.pi * k / max(steps, 1))))
             k += 1
         losses.append(tot / max(per_epoch, 1))
         if log:
             log(f"epoch {e}: loss {losses[-1]:.4f}")
+        if stall_check and e == 0 and len(hist) >= 40:
+            first = float(np.mean(hist[:max(1, len(hist) // 20)]))
+            last = float(np.mean(hist[-max(1, len(hist) // 10):]))
+            if last > 0.95 * first:
+                raise TrainingStalled(f"first-epoch loss {first:.3f} -> {last:.3f}")
     return losses
 
 
