@@ -1840,9 +1840,11 @@ extern "C" int tg3_ctx_stage_times(tg3_ctx* c, double* ms, int* launches, int re
 // ======================================================= global scan (device)
 namespace tg3 {
 // |P|^2 of padded projection rows (floats, or split bf16 planes with the lo
-// plane loOff elements after the hi plane) into rows of ldq floats.
+// plane loOff elements after the hi plane) into rows of ldq floats, or with
+// outLo != 0 into split bf16 planes (hi = bf16(v), lo = bf16(v - hi), the lo
+// plane outLo elements after the hi plane) for the tensor-core norm term.
 __global__ void k_abs2_from(const float* __restrict__ P, long long loOff, int K, int Kp,
-                            float* __restrict__ out, int ldq)
+                            float* __restrict__ out, int ldq, long long outLo = 0)
 {
     const int r = blockIdx.x;
     for (int p = threadIdx.x; p < ldq; p += blockDim.x) {
@@ -1864,7 +1866,32 @@ __global__ void k_abs2_from(const float* __restrict__ P, long long loOff, int K,
             }
             v = re * re + im * im;
         }
-        out[(size_t)r * ldq + p] = v;
+        if (outLo == 0) {
+            out[(size_t)r * ldq + p] = v;
+        } else {
+            __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(out);
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            hi[(size_t)r * ldq + p] = h;
+            hi[outLo + (size_t)r * ldq + p] = __float2bfloat16_rn(v - __bfloat162float(h));
+        }
+    }
+}
+
+// sigRcp ctf^2 of every image's pixels as split bf16 planes [n][ldq] (hi,
+// then lo outLo elements later), zero beyond K: the norm term's B operand.
+__global__ void k_sc2_split(const float* __restrict__ sig, const float* __restrict__ ctf, int K,
+                            __nv_bfloat16* __restrict__ hi, long long outLo, int ldq)
+{
+    const int r = blockIdx.y;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ldq; p += gridDim.x * blockDim.x) {
+        float v = 0.f;
+        if (p < K) {
+            const float c = ctf[(size_t)r * K + p];
+            v = sig[(size_t)r * K + p] * c * c;
+        }
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[(size_t)r * ldq + p] = h;
+        hi[outLo + (size_t)r * ldq + p] = __float2bfloat16_rn(v - __bfloat162float(h));
     }
 }
 }  // namespace tg3
@@ -1995,18 +2022,21 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
                                     nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, nullptr, nullptr,
                                     nullptr, pscr, c->d_flag, splitP, s));
         }
+        // |P|^2 rows: FP32 for the FP32 search, split bf16 planes (the same
+        // bytes) for the split search's tensor-core norm term
+        const long long outLo = split ? (long long)nRt * Kq : 0;
         if (pbank) {
-            // the bank's |P|^2 rows, made once per bank and precision
+            // the bank's, made once per bank and precision
             if (!pbank->abs2q)
                 TG3_CUDA(cudaMalloc(&pbank->abs2q, sizeof(float) * (size_t)pbank->nB * Kq));
             if (pbank->abs2qSplit != (split ? 1 : 0)) {
-                k_abs2_from<<<nRt, 256, 0, s>>>(P, splitP, K, Kp, pbank->abs2q, Kq);
+                k_abs2_from<<<nRt, 256, 0, s>>>(P, splitP, K, Kp, pbank->abs2q, Kq, outLo);
                 TG3_LAUNCH_CHECK("projection norms");
                 pbank->abs2qSplit = split ? 1 : 0;
             }
             abs2 = pbank->abs2q;
         } else {
-            k_abs2_from<<<nRt, 256, 0, s>>>(P, splitP, K, Kp, abs2, Kq);
+            k_abs2_from<<<nRt, 256, 0, s>>>(P, splitP, K, Kp, abs2, Kq, outLo);
             TG3_LAUNCH_CHECK("projection norms");
         }
     }
@@ -2022,13 +2052,27 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
             TG3_CUDA(launch_shift_bank(dd, cc, ss, nullptr, bank, n, nT, 1, nullptr, nullptr, K, A,
                                        Kp, splitA, s));
             TG3_CUDA(launch_x0(dd, ss, n, K, x0 + l0, s));
-            k_sc2_rows<<<dim3((Kq + 255) / 256, n), 256, 0, s>>>(ss, cc, K, sc2, Kq);
+            if (split)
+                k_sc2_split<<<dim3((Kq + 255) / 256, n), 256, 0, s>>>(
+                    ss, cc, K, reinterpret_cast<__nv_bfloat16*>(sc2), (long long)n * Kq, Kq);
+            else
+                k_sc2_rows<<<dim3((Kq + 255) / 256, n), 256, 0, s>>>(ss, cc, K, sc2, Kq);
             TG3_LAUNCH_CHECK("norm operand");
         }
         {
-            // per-(rotation, image) norm
+            // per-(rotation, image) norm: FP32 for the FP32 search; for the
+            // split search the same three-product split-bf16 GEMM as the cross
+            // term (|P|^2 and sigRcp ctf^2 are both split; FP32 accumulation)
             StageTimer tm(c, TG3_STAGE_NORM);
-            if ((st = norm_gemm(c, abs2, sc2, nRt, n, Kq, nrmG, s))) return st;
+            if (split) {
+                const int Nn = std::min(256, (n + 15) / 16 * 16);
+                const int itemsN = (n + Nn - 1) / Nn;
+                TG3_CUDA(launch_gemm_bf16x3(abs2, nRt, sc2, n, nRt, Nn, Kq, itemsN, 0, Nn, n, nrmG,
+                                            Nn, n, nullptr, 0, 1.0f, c->d_flag, s, 0, 0, false,
+                                            Kq % c->scanBK == 0 ? c->scanBK : 64));
+            } else if ((st = norm_gemm(c, abs2, sc2, nRt, n, Kq, nrmG, s))) {
+                return st;
+            }
         }
         {
             StageTimer tm(c, TG3_STAGE_CROSS);
