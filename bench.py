@@ -193,6 +193,7 @@ def run_tg3(args, rank, world, local_rank):
                                          box=args.box, W0=W0)
     nR, nT, K = W["nR"], W["nT"], st.K
     ctx = tg3.Context(local_rank)
+    ctx.set_option(tg3.OPT_LOCAL_BK, args.local_bk)
     if args.fused:
         ctx.set_option(tg3.OPT_FUSED, 1)
     for c, v in enumerate(vols):
@@ -1189,6 +1190,7 @@ def run_uneven(args, rank, world, local_rank):
     plan = tg3.RaggedPlan(ctx, cls, nR, nT, inp, out, prec, budget=0, graph=True)
     plan_s = time.perf_counter() - t0
     waves, budget = plan.info()
+    kblock = plan.kblock()
     for _ in range(args.warmup):
         plan.run()
     ctx.sync()
@@ -1257,6 +1259,7 @@ def run_uneven(args, rank, world, local_rank):
                                   "[200, 8000] x translations log-uniform [9, 81] per particle",
                       "particles_per_step": nP, "rotations_total": R, "translations_total": T,
                       "plan_waves": waves, "wave_budget_bytes": budget,
+                      "cross_term_k_block": kblock,
                       "plan_create_s": round(plan_s, 2)},
            "hypotheses_per_s": round(job_rate(hyps, ms, world), 1),
            "samples_per_s": round(job_rate(samples, ms, world), 1),
@@ -2346,6 +2349,8 @@ def main():
     ap.add_argument("--scan-pair", type=int, default=0, choices=[0, 1],
                     help="TG3_OPT_SCAN_PAIR: the global search's cross term on CTA pairs that "
                          "share each column tile by TMA multicast")
+    ap.add_argument("--local-bk", type=int, default=64, choices=[32, 64],
+                    help="TG3_OPT_LOCAL_BK: K block of the local phase's split cross term")
     ap.add_argument("--scan-bk", type=int, default=32, choices=[32, 64],
                     help="TG3_OPT_SCAN_BK: K block of the global search's cross-term stages")
     ap.add_argument("--bank-order", type=int, default=1, choices=[0, 1],

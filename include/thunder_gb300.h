@@ -345,7 +345,11 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  * TG3_OPT_SCAN_BK (default 32): the K block of that cross term's pipeline
  *   stages, 64 bf16 (128-byte rows, 128-byte swizzle) or 32 (64-byte rows,
  *   64-byte swizzle: half the bytes a stage, twice the stages in flight).
- *   Same products in the same order. */
+ *   Same products in the same order.
+ * TG3_OPT_LOCAL_BK (default 64): the same choice for the split-bf16 local
+ *   phase's cross term (tg3_local_phase_d); an uneven-batch plan created
+ *   with an autotuned budget tries both and keeps the faster for its
+ *   waves. */
 enum {
     TG3_OPT_FUSED = 0,
     TG3_OPT_INSERT_GATHER = 1,
@@ -353,7 +357,8 @@ enum {
     TG3_OPT_BANK_ORDER = 3,
     TG3_OPT_SCAN_TILE_N = 4,
     TG3_OPT_SCAN_PAIR = 5,
-    TG3_OPT_SCAN_BK = 6
+    TG3_OPT_SCAN_BK = 6,
+    TG3_OPT_LOCAL_BK = 7
 };
 int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);
@@ -386,6 +391,10 @@ int tg3_ragged_plan_create(tg3_ctx* ctx, int nP, const int* cls, const int* nR, 
                            int use_graph, tg3_plan** plan);
 int tg3_ragged_plan_run(tg3_plan* plan);
 int tg3_ragged_plan_info(const tg3_plan* plan, int* waves, size_t* budget);
+/* The K block of the plan's split-bf16 cross term (64 or 32: TG3_OPT_LOCAL_BK
+ * as the autotuner chose it for this batch, or the context's when the plan
+ * was given a budget). */
+int tg3_ragged_plan_kblock(const tg3_plan* plan, int* bk);
 int tg3_ragged_plan_destroy(tg3_plan* plan);
 
 /* Pose-proposal network (no counterpart in the reference: a learned seed for

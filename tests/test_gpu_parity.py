@@ -484,6 +484,34 @@ def test_global_scan_tile_forms(small, ctx, form):
                                        atol=0)
 
 
+def test_local_phase_k_block_forms(small, ctx):
+    """The split-bf16 local phase's cross term with 32-wide K blocks in
+    64-byte swizzled stages (TG3_OPT_LOCAL_BK 32, a choice of the uneven-batch
+    autotuner) against the default 64-wide blocks: the same MMAs in the same
+    order, so the same log-likelihoods and weights to the last bit."""
+    nP, nR, nT = 3, 300, 100
+    d = _local_inputs(small, nP, nR, nT, 11)
+    res = {}
+    try:
+        for bk in (32, 64):
+            ctx.set_option(tg3.OPT_LOCAL_BK, bk)
+            o = dict(wC=torch.empty(nP, dtype=torch.float64, device=DEV),
+                     wR=torch.empty((nP, nR), dtype=torch.float64, device=DEV),
+                     wT=torch.empty((nP, nT), dtype=torch.float64, device=DEV),
+                     base=torch.empty(nP, dtype=torch.float64, device=DEV),
+                     dvp=torch.empty((nP, nR, nT), dtype=torch.float32, device=DEV))
+            ctx.local_phase(nP, nR, nT, dev(d["dat"]), dev(d["ctf"]), dev(d["sig"]),
+                            dev(d["qs"]), dev(d["ts"]), dev(d["pwR"]), dev(d["pwT"]),
+                            dev(d["pwC"]), None, o["wC"], o["wR"], o["wT"], o["base"], o["dvp"],
+                            tg3.SCORE_BF16X3)
+            ctx.sync()
+            res[bk] = {k: v.cpu().numpy() for k, v in o.items()}
+    finally:
+        ctx.set_option(tg3.OPT_LOCAL_BK, 64)
+    for k in ("dvp", "wC", "wR", "wT", "base"):
+        np.testing.assert_array_equal(res[32][k], res[64][k])
+
+
 @pytest.mark.parametrize("shape", [(4, 96, 21), (3, 300, 100), (2, 129, 7)])
 def test_fused_matches_two_kernel_form(small, ctx, shape):
     """The fused projection + split-bf16 kernel (slices gathered straight into

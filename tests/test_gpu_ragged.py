@@ -113,3 +113,24 @@ def test_ragged_plan_equals_particles_alone(setup, precision):
     exp = {k: v.cpu().numpy() for k, v in ref.items()}
     for k in tg3.RAGGED_OUTPUTS:
         assert np.array_equal(got[k], exp[k]), k
+
+
+def test_autotuned_plan_matches_a_fixed_plan(setup):
+    """A plan whose budget and cross-term K block the autotuner chose
+    (tg3_ragged_plan_kblock reports the block) gives the same outputs as a
+    plan with a fixed budget: waves and K blocks change the launches, not the
+    arithmetic."""
+    ctx, cls, nR, nT, d = setup["ctx"], setup["cls"], setup["nR"], setup["nT"], setup["dev"]
+    nP = len(cls)
+    res = []
+    for budget in (0, 96 << 10):
+        out = _outputs(nP, nR, nT)
+        plan = tg3.RaggedPlan(ctx, cls, nR, nT, d, out, tg3.SCORE_BF16X3, budget=budget,
+                              graph=True)
+        assert plan.kblock() in (32, 64)
+        plan.run()
+        ctx.sync()
+        res.append({k: v.cpu().numpy() for k, v in out.items()})
+        plan.close()
+    for k in res[0]:
+        np.testing.assert_array_equal(res[0][k], res[1][k])

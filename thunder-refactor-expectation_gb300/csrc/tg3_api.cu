@@ -605,7 +605,7 @@ static int local_phase(tg3_ctx* c, const int* bankIdx, int nP, int nR, int nT, c
         if (split)
             TG3_CUDA(launch_gemm_nt_bf16x3(P, (long long)nR * Kp, Kp, A, (long long)nT * Kp, Kp,
                                            nR, nT, Kp, nP, D, (long long)nR * nT, nT, nrm, nR,
-                                           -2.0f, nullptr, 0, c->d_flag, s));
+                                           -2.0f, nullptr, 0, c->d_flag, s, c->localBK));
         else
             TG3_CUDA(launch_gemm_nt_fp32(P, (long long)nR * Kp, Kp, A, (long long)nT * Kp, Kp, nR,
                                          nT, Kp, nP, D, (long long)nR * nT, nT, nrm, nR, -2.0f,
@@ -1807,6 +1807,10 @@ extern "C" int tg3_ctx_set_option(tg3_ctx* c, int option, int value)
     else if (option == TG3_OPT_SCAN_BK) {
         if (value != 32 && value != 64) return fail(TG3_ERR_ARG, "TG3_OPT_SCAN_BK takes 32 or 64");
         c->scanBK = value;
+    }
+    else if (option == TG3_OPT_LOCAL_BK) {
+        if (value != 32 && value != 64) return fail(TG3_ERR_ARG, "TG3_OPT_LOCAL_BK takes 32 or 64");
+        c->localBK = value;
     }
     else return fail(TG3_ERR_ARG, "unknown option");
     return TG3_OK;

@@ -196,6 +196,7 @@ struct tg3_ctx {
     int scanTileN = 0;            // TG3_OPT_SCAN_TILE_N (0: 256)
     int scanPair = 0;             // TG3_OPT_SCAN_PAIR
     int scanBK = 32;              // TG3_OPT_SCAN_BK
+    int localBK = 64;             // TG3_OPT_LOCAL_BK
     // per-stage event timing (tg3_ctx_set_timing)
     bool timing = false;
     // inside the learned E-step's fallback: its cross-term launches are
@@ -477,7 +478,7 @@ cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda,
                                   long long sC, int ldc, const float* nrm,
                                   long long sN, float alpha, void* scratch,
                                   size_t scratchBytes, int* flag,
-                                  cudaStream_t st);
+                                  cudaStream_t st, int bk = 64);
 size_t bf16x3_scratch_bytes(int M, int N, int Kd, int batch);
 // General split-bf16 GEMM over `items` (see tg3_tc.cu): A/B point at hi
 // planes followed by lo planes of rowsA / rowsB rows of Kd bf16 elements.

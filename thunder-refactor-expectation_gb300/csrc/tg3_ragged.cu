@@ -178,6 +178,7 @@ struct tg3_plan {
     tg3_ctx* c = nullptr;
     int nP = 0, precision = 0;
     size_t budget = 0;
+    int bk = 64;                 // the local phase's K block (TG3_OPT_LOCAL_BK) for this plan
     RaggedIn in;
     RaggedOut out;
     std::vector<int> clsH, nRH, nTH;
@@ -299,7 +300,19 @@ int plan_waves(tg3_plan* p, size_t budget)
 }
 
 // The launches of every wave, in order, on the context stream.
+int plan_issue_waves(tg3_plan* p);
+
+// The plan's waves with its K block set on the context for their duration.
 int plan_issue(tg3_plan* p)
+{
+    const int saved = p->c->localBK;
+    p->c->localBK = p->bk;
+    const int st = plan_issue_waves(p);
+    p->c->localBK = saved;
+    return st;
+}
+
+int plan_issue_waves(tg3_plan* p)
 {
     tg3_ctx* c = p->c;
     cudaStream_t s = c->stream;
@@ -410,24 +423,35 @@ extern "C" int tg3_ragged_plan_create(
         return fail_free(fail(TG3_ERR_CUDA, "plan upload"));
     const bool timing = c->timing;
     c->timing = false;
+    p->bk = c->localBK;
     if (budget == 0) {
-        // autotune: time every candidate budget on this batch (the first run
-        // of a candidate also sizes the workspaces), keep the fastest
+        // autotune: time every candidate (wave budget, and for the split
+        // precision the cross term's K block: 128-byte stages of 64 bf16 or
+        // 64-byte stages of 32) on this batch -- the first run of a candidate
+        // also sizes the workspaces -- and keep the fastest
         const size_t cand[3] = {(size_t)2 << 30, (size_t)6 << 30, (size_t)16 << 30};
+        const int bks[2] = {64, 32};
+        const int nbk = precision == TG3_SCORE_BF16X3 ? 2 : 1;
         float best = 1e30f;
         size_t bestB = cand[0];
-        for (size_t b : cand) {
-            float ms = 0;
-            if ((st = plan_waves(p, b)) || (st = plan_time(p, &ms)) || (st = plan_time(p, &ms))) {
-                c->timing = timing;
-                return fail_free(st);
+        int bestK = 64;
+        for (size_t b : cand)
+            for (int ik = 0; ik < nbk; ik++) {
+                float ms = 0;
+                p->bk = bks[ik];
+                if ((st = plan_waves(p, b)) || (st = plan_time(p, &ms)) ||
+                    (st = plan_time(p, &ms))) {
+                    c->timing = timing;
+                    return fail_free(st);
+                }
+                if (ms < best) {
+                    best = ms;
+                    bestB = b;
+                    bestK = bks[ik];
+                }
             }
-            if (ms < best) {
-                best = ms;
-                bestB = b;
-            }
-        }
         budget = bestB;
+        p->bk = bestK;
     }
     float warmMs = 0;
     if ((st = plan_waves(p, budget)) || (st = plan_time(p, &warmMs))) {
@@ -477,6 +501,13 @@ extern "C" int tg3_ragged_plan_info(const tg3_plan* p, int* waves, size_t* budge
     if (!p) return fail(TG3_ERR_ARG, "null plan");
     if (waves) *waves = (int)p->waves.size();
     if (budget) *budget = p->budget;
+    return TG3_OK;
+}
+
+extern "C" int tg3_ragged_plan_kblock(const tg3_plan* p, int* bk)
+{
+    if (!p || !bk) return fail(TG3_ERR_ARG, "null plan or output");
+    *bk = p->bk;
     return TG3_OK;
 }
 

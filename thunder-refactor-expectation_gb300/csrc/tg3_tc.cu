@@ -532,12 +532,13 @@ cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda, const f
                                   long long sB, int ldb, int M, int N, int Kd, int batch,
                                   float* C, long long sC, int ldc, const float* nrm,
                                   long long sN, float alpha, void*, size_t, int* flag,
-                                  cudaStream_t st)
+                                  cudaStream_t st, int bk)
 {
     if (lda != Kd || ldb != Kd || sA != (long long)M * Kd || sB != (long long)N * Kd)
         return cudaErrorInvalidValue;
     return launch_gemm_bf16x3(A, (long long)batch * M, B, (long long)batch * N, M, N, Kd, batch, M,
-                              N, 0, C, sC, ldc, nrm, sN, alpha, flag, st, 0, 0);
+                              N, 0, C, sC, ldc, nrm, sN, alpha, flag, st, 0, 0, false,
+                              Kd % bk == 0 ? bk : 64);
 }
 
 }  // namespace tg3

@@ -31,6 +31,7 @@ EXPORTS = [
     "tg3_project_d", "tg3_ctx_render_references_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
     "tg3_ctx_set_option", "tg3_ctx_set_pixels_slot", "tg3_ctx_use_pixels",
     "tg3_ragged_plan_create", "tg3_ragged_plan_run", "tg3_ragged_plan_info",
+    "tg3_ragged_plan_kblock",
     "tg3_ragged_plan_destroy", "tg3_cnn_create", "tg3_cnn_destroy", "tg3_cnn_param_count",
     "tg3_cnn_params", "tg3_cnn_grads", "tg3_cnn_set_bf16", "tg3_cnn_forward", "tg3_cnn_loss",
     "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose", "tg3_cnn_backward", "tg3_cnn_infer",
@@ -54,6 +55,7 @@ OPT_BANK_ORDER = 3
 OPT_SCAN_TILE_N = 4
 OPT_SCAN_PAIR = 5
 OPT_SCAN_BK = 6
+OPT_LOCAL_BK = 7
 
 
 class TG3Error(RuntimeError):
@@ -134,6 +136,7 @@ def lib():
             "tg3_ragged_plan_create": ([_P, _I] + [_P] * 27 + [_I, ctypes.c_size_t, _I, _P], _I),
             "tg3_ragged_plan_run": ([_P], _I),
             "tg3_ragged_plan_info": ([_P, _P, _P], _I),
+            "tg3_ragged_plan_kblock": ([_P, _P], _I),
             "tg3_ragged_plan_destroy": ([_P], _I),
             "tg3_cnn_create": ([_P, _I, ctypes.c_ulonglong], _I),
             "tg3_cnn_destroy": ([_P], _I),
@@ -522,6 +525,12 @@ class RaggedPlan:
         b = ctypes.c_size_t()
         check(lib().tg3_ragged_plan_info(self.h, ctypes.byref(w), ctypes.byref(b)))
         return w.value, b.value
+
+    def kblock(self) -> int:
+        """The K block of the plan's split-bf16 cross term (64 or 32)."""
+        k = ctypes.c_int()
+        check(lib().tg3_ragged_plan_kblock(self.h, ctypes.byref(k)))
+        return k.value
 
     def close(self):
         if self.h:
