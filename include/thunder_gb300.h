@@ -606,6 +606,17 @@ int tg3_ctx_insert_load_d(tg3_ctx* ctx, const float* F, const float* T);
  * centred (coordinate i at index i + N/2). */
 int tg3_ctx_reconstruct_d(tg3_ctx* ctx, const double* fsc, int nFsc, int joinHalf, int maxRadius,
                           int gridCorr, int kernel, float a, float alpha, float* vol, int* rounds);
+/* 2-D reconstruction (Reconstructor::reconstruct(Image&) in MODE_2D,
+ * src/Reconstructor.cpp:1093-1103 and its _T2D / _W2D / _C2D branches): the
+ * same chain as tg3_ctx_reconstruct_d on one class's 2-D accumulators,
+ * host buffers: F2D complex and T2D real [vdim][vdim/2 + 1] (the summed
+ * InsertI2D accumulators), img [N][N] out (N = vdim / pf, centred:
+ * coordinate i at index i + N/2).  The inverse transform's normalisation
+ * is 1 / vdim^2. */
+int tg3_Reconstruct2D(const float* F2D, const float* T2D, int vdim, int pf,
+                      const double* fsc, int nFsc, int joinHalf, int maxRadius,
+                      int gridCorr, int kernel, float a, float alpha, float* img,
+                      int* rounds);
 
 /* Noise spectrum sigma^2 from the images at their best poses
  * (Optimiser::allReduceSigma, src/Optimiser.cpp:6355-6630): the active pixel

@@ -1,6 +1,9 @@
 """Oracle (test infrastructure only): Reconstructor::reconstruct
-(src/Reconstructor.cpp:1129-1790; 3-D, no symmetry) in numpy float64 -- the
-checker for tg3_ctx_reconstruct_d, never on the product path.  The kernel
+(src/Reconstructor.cpp:1129-1790; 3-D and 2-D, no symmetry) in numpy float64
+-- the checker for tg3_ctx_reconstruct_d and tg3_Reconstruct2D, never on the
+product path.  The 2-D mode is the same chain on the padded 2-D half grid
+(the reference's _T2D / _W2D / _C2D branches, with the same MKB_RL and TIK_RL
+forms at |x| / (pf N)).  The kernel
 functions use scipy's Bessel functions (MKB_RL, TIK_RL of
 src/Functions/Functions.cpp:128-220) and are pinned to the compiled
 reference (tests/test_formats_cpu.py); the transforms are numpy's
@@ -29,20 +32,22 @@ def tik_rl(r):
     return np.sinc(np.asarray(r, np.float64)) ** 2
 
 
-def _coords(vdim):
+def _coords(vdim, dim=3):
     c = np.fft.fftfreq(vdim, 1.0 / vdim)
-    z, y, x = np.meshgrid(c, c, np.arange(vdim // 2 + 1), indexing="ij")
-    return x * x + y * y + z * z
+    g = np.meshgrid(*([c] * (dim - 1) + [np.arange(vdim // 2 + 1)]), indexing="ij")
+    return sum(v * v for v in g)
 
 
 def reconstruct(F, T, pf, max_radius, fsc=None, join_half=False, grid_corr=True, kernel="trilinear",
                 a=1.9, alpha=15.0):
-    """F (complex), T (real) on the padded half grid (vdim, vdim, vdim/2 + 1)
-    -> the map (N, N, N) centred (coordinate i at index i + N/2) and the
-    number of balancing rounds."""
+    """F (complex), T (real) on the padded half grid (vdim, vdim, vdim/2 + 1),
+    or (vdim, vdim/2 + 1) in 2-D -> the map (N, N, N) or image (N, N)
+    centred (coordinate i at index i + N/2) and the number of balancing
+    rounds."""
+    dim = F.ndim
     vdim = F.shape[0]
     N = vdim // pf
-    q = _coords(vdim)
+    q = _coords(vdim, dim)
     r2max = (max_radius * pf) ** 2
     inside = q < r2max
     T = np.asarray(T, np.float64).copy()
@@ -59,12 +64,13 @@ def reconstruct(F, T, pf, max_radius, fsc=None, join_half=False, grid_corr=True,
     rounds = 0
     if grid_corr:
         c = np.fft.fftfreq(vdim, 1.0 / vdim)
-        zz, yy, xx = np.meshgrid(c, c, c, indexing="ij")
-        rr = np.sqrt(xx * xx + yy * yy + zz * zz) / (N * pf)
+        g = np.meshgrid(*([c] * dim), indexing="ij")
+        rr = np.sqrt(sum(v * v for v in g)) / (N * pf)
         krl = mkb_rl(rr, a, alpha) / mkb_rl(0.0, a, alpha)
         diff, no_dec = np.inf, 0
+        axes = tuple(range(dim))
         for m in range(30):
-            C = np.fft.rfftn(np.fft.irfftn(T * W, s=(vdim,) * 3, axes=(0, 1, 2)) * krl)
+            C = np.fft.rfftn(np.fft.irfftn(T * W, s=(vdim,) * dim, axes=axes) * krl, axes=axes)
             mag = np.abs(C)
             W[inside] /= np.maximum(mag[inside], 1e-6)
             prev, diff = diff, np.abs(mag[inside] - 1).max()
@@ -75,11 +81,11 @@ def reconstruct(F, T, pf, max_radius, fsc=None, join_half=False, grid_corr=True,
     else:
         W[inside] = 1.0 / np.maximum(np.abs(T[inside]), 1e-6)
     V = np.where(inside, F * W, 0)
-    pad = np.fft.irfftn(V, s=(vdim,) * 3, axes=(0, 1, 2))
+    pad = np.fft.irfftn(V, s=(vdim,) * dim, axes=tuple(range(dim)))
     idx = np.arange(N) - N // 2
-    vol = pad[np.ix_(idx % vdim, idx % vdim, idx % vdim)]
-    zz, yy, xx = np.meshgrid(idx, idx, idx, indexing="ij")
-    r = np.sqrt(xx * xx + yy * yy + zz * zz) / (pf * N)
+    vol = pad[np.ix_(*([idx % vdim] * dim))]
+    g = np.meshgrid(*([idx] * dim), indexing="ij")
+    r = np.sqrt(sum(v * v for v in g)) / (pf * N)
     if kernel == "mkb":
         k = mkb_rl(r, a * pf, alpha) / mkb_rl(0.0, a * pf, alpha)
     else:

@@ -58,6 +58,44 @@ def test_reconstruct_matches_oracle(grid_corr, kernel):
     assert np.abs(got - ref).max() < 1e-3 * np.abs(ref).max()
 
 
+def _inputs2d(rng, N, pf):
+    vdim = N * pf
+    c = np.arange(vdim) - vdim // 2
+    y, x = np.meshgrid(c, c, indexing="ij")
+    m = np.zeros((vdim, vdim))
+    for _ in range(6):
+        p = rng.uniform(-N / 5, N / 5, 2)
+        m += np.exp(-((x - p[0]) ** 2 + (y - p[1]) ** 2) / (2 * rng.uniform(1.5, 3) ** 2))
+    q = np.fft.fftfreq(vdim, 1.0 / vdim)
+    ky, kx = np.meshgrid(q, np.arange(vdim // 2 + 1), indexing="ij")
+    k = np.sqrt(kx * kx + ky * ky)
+    T = 50.0 * np.exp(-k / (0.4 * vdim)) + 0.5
+    F = np.fft.rfft2(np.fft.ifftshift(m)) * T / 40.0
+    return F, T
+
+
+@pytest.mark.parametrize("grid_corr,kernel", [(True, tg3.KERNEL_TRILINEAR), (False, tg3.KERNEL_MKB),
+                                              (True, tg3.KERNEL_MKB)])
+def test_reconstruct_2d_matches_oracle(grid_corr, kernel):
+    """tg3_Reconstruct2D (MODE_2D: the 2-D accumulators of one class, host
+    buffers) against the oracle's 2-D chain: the same number of balancing
+    rounds and the image within 1e-3 of its peak."""
+    rng = np.random.default_rng(17 + kernel)
+    N, pf, maxR = 64, 2, 28
+    F, T = _inputs2d(rng, N, pf)
+    fsc = np.clip(1.05 - np.arange(N // 2 + 1) / (N / 2), 0, 1)
+    img = np.zeros((N, N), np.float32)
+    rounds = np.zeros(1, np.int32)
+    tg3.check(tg3.lib().tg3_Reconstruct2D(
+        tg3.ptr(np.ascontiguousarray(F.astype(np.complex64))),
+        tg3.ptr(np.ascontiguousarray(T.astype(np.float32))), N * pf, pf, tg3.ptr(fsc), len(fsc), 1,
+        maxR, int(grid_corr), kernel, 1.9, 15.0, tg3.ptr(img), tg3.ptr(rounds)))
+    ref, ref_rounds = RC.reconstruct(F, T, pf, maxR, fsc=fsc, join_half=True, grid_corr=grid_corr,
+                                     kernel="mkb" if kernel == tg3.KERNEL_MKB else "trilinear")
+    assert int(rounds[0]) == ref_rounds
+    assert np.abs(img - ref).max() < 1e-3 * np.abs(ref).max()
+
+
 @pytest.mark.parametrize("which", ["c4", "d2"])
 def test_prepare_tf_matches_oracle(which):
     """PrepareTF on the accumulators: F and T scaled by 1 / T at the origin,

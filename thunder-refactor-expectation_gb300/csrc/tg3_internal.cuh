@@ -93,6 +93,7 @@ enum WsSlot {
     WS_RENDER,       // reference rendering: image grid, projections, real images
     WS_SPLITK,       // split-K partial sums of the global search's norm term
     WS_WCHUNK,       // per-chunk weights of a row-split weights launch
+    WS_RECO2D,       // 2-D reconstruction: accumulator, staged F / T, image
     WS_COUNT
 };
 

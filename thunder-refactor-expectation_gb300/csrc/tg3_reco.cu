@@ -79,19 +79,19 @@ __device__ double tik_rl(double r)
 __device__ __forceinline__ int wrapc(int i, int n) { return i < n / 2 ? i : i - n; }
 
 // Wiener-filtered, floored T and the initial W (1 inside the radius)
-__global__ void k_reco_init(const float4* __restrict__ acc, int vdim, int pf, const double* __restrict__ fsc,
-                            int nFsc, int joinHalf, long long r2max, float* __restrict__ T,
-                            float* __restrict__ W)
+__global__ void k_reco_init(const float4* __restrict__ acc, int vdim, int nz, int pf,
+                            const double* __restrict__ fsc, int nFsc, int joinHalf,
+                            long long r2max, float* __restrict__ T, float* __restrict__ W)
 {
     const int nx = vdim / 2 + 1;
-    const size_t n = (size_t)vdim * vdim * nx;
+    const size_t n = (size_t)nz * vdim * nx;
     const long long r2min = 25LL * pf * pf;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
         const unsigned u32 = (unsigned)idx, row = u32 / (unsigned)nx;
         const int x = (int)(u32 - row * (unsigned)nx);
         const int y = wrapc((int)(row % (unsigned)vdim), vdim);
-        const int z = wrapc((int)(row / (unsigned)vdim), vdim);
+        const int z = nz > 1 ? wrapc((int)(row / (unsigned)vdim), vdim) : 0;
         const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
         double t = acc[idx].z;
         if (fsc && q >= r2min && q < r2max) {
@@ -131,15 +131,16 @@ __global__ void k_radial_table(float* __restrict__ tab, int nq, double s, int mk
 
 // real-space C (after the unnormalised inverse) times kRL(r^2) / nf / vdim^3
 // (the table holds kRL / nf / vdim^3)
-__global__ void k_reco_kernel_rl(float* __restrict__ c, int vdim, const float* __restrict__ tab)
+__global__ void k_reco_kernel_rl(float* __restrict__ c, int vdim, int nz,
+                                 const float* __restrict__ tab)
 {
-    const size_t n = (size_t)vdim * vdim * vdim;
+    const size_t n = (size_t)nz * vdim * vdim;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
         const unsigned u32 = (unsigned)idx, row = u32 / (unsigned)vdim;
         const int x = wrapc((int)(u32 - row * (unsigned)vdim), vdim);
         const int y = wrapc((int)(row % (unsigned)vdim), vdim);
-        const int z = wrapc((int)(row / (unsigned)vdim), vdim);
+        const int z = nz > 1 ? wrapc((int)(row / (unsigned)vdim), vdim) : 0;
         c[idx] *= tab[x * x + y * y + z * z];
     }
 }
@@ -148,18 +149,18 @@ __global__ void k_reco_kernel_rl(float* __restrict__ c, int vdim, const float* _
 // bits compared as ints: the values are non-negative); then C <- T W for the
 // next round (the inverse transform consumes C)
 __global__ void k_reco_update(float2* __restrict__ C, const float* __restrict__ T, int vdim,
-                              long long r2max, float* __restrict__ W,
+                              int nz, long long r2max, float* __restrict__ W,
                               unsigned* __restrict__ diffBits)
 {
     const int nx = vdim / 2 + 1;
-    const size_t n = (size_t)vdim * vdim * nx;
+    const size_t n = (size_t)nz * vdim * nx;
     float dmax = 0.f;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
         const unsigned u32 = (unsigned)idx, row = u32 / (unsigned)nx;
         const int x = (int)(u32 - row * (unsigned)nx);
         const int y = wrapc((int)(row % (unsigned)vdim), vdim);
-        const int z = wrapc((int)(row / (unsigned)vdim), vdim);
+        const int z = nz > 1 ? wrapc((int)(row / (unsigned)vdim), vdim) : 0;
         const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
         float w = W[idx];
         if (q < r2max) {
@@ -175,17 +176,17 @@ __global__ void k_reco_update(float2* __restrict__ C, const float* __restrict__ 
 }
 
 // without grid correction: W = 1 / max(|T|, 1e-6) inside the radius
-__global__ void k_reco_w_from_t(const float* __restrict__ T, int vdim, long long r2max,
+__global__ void k_reco_w_from_t(const float* __restrict__ T, int vdim, int nz, long long r2max,
                                 float* __restrict__ W)
 {
     const int nx = vdim / 2 + 1;
-    const size_t n = (size_t)vdim * vdim * nx;
+    const size_t n = (size_t)nz * vdim * nx;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
         const unsigned u32 = (unsigned)idx, row = u32 / (unsigned)nx;
         const int x = (int)(u32 - row * (unsigned)nx);
         const int y = wrapc((int)(row % (unsigned)vdim), vdim);
-        const int z = wrapc((int)(row / (unsigned)vdim), vdim);
+        const int z = nz > 1 ? wrapc((int)(row / (unsigned)vdim), vdim) : 0;
         const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
         if (q < r2max) W[idx] = 1.f / fmaxf(fabsf(T[idx]), 1e-6f);
     }
@@ -193,16 +194,16 @@ __global__ void k_reco_w_from_t(const float* __restrict__ T, int vdim, long long
 
 // V = F W inside the radius, 0 outside
 __global__ void k_reco_fw(const float4* __restrict__ acc, const float* __restrict__ W, int vdim,
-                          long long r2max, float2* __restrict__ V)
+                          int nz, long long r2max, float2* __restrict__ V)
 {
     const int nx = vdim / 2 + 1;
-    const size_t n = (size_t)vdim * vdim * nx;
+    const size_t n = (size_t)nz * vdim * nx;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
         const unsigned u32 = (unsigned)idx, row = u32 / (unsigned)nx;
         const int x = (int)(u32 - row * (unsigned)nx);
         const int y = wrapc((int)(row % (unsigned)vdim), vdim);
-        const int z = wrapc((int)(row / (unsigned)vdim), vdim);
+        const int z = nz > 1 ? wrapc((int)(row / (unsigned)vdim), vdim) : 0;
         const long long q = (long long)x * x + (long long)y * y + (long long)z * z;
         const float4 a = acc[idx];
         V[idx] = q < r2max ? make_float2(a.x * W[idx], a.y * W[idx]) : make_float2(0.f, 0.f);
@@ -212,15 +213,15 @@ __global__ void k_reco_fw(const float4* __restrict__ acc, const float* __restric
 // the central N^3 of the padded real-space map, in centred order (index i +
 // N/2 for coordinate i), divided by the kernel's real-space transform
 // (the table holds the kernel's real-space transform times vdim^3)
-__global__ void k_reco_extract(const float* __restrict__ pad, int vdim, int N,
+__global__ void k_reco_extract(const float* __restrict__ pad, int vdim, int nz, int N,
                                const float* __restrict__ tab, float* __restrict__ out)
 {
-    const size_t n = (size_t)N * N * N;
+    const size_t n = (size_t)(nz > 1 ? N : 1) * N * N;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(idx % N) - N / 2;
         const int y = (int)((idx / N) % N) - N / 2;
-        const int z = (int)(idx / ((size_t)N * N)) - N / 2;
+        const int z = nz > 1 ? (int)(idx / ((size_t)N * N)) - N / 2 : 0;
         const int px = x < 0 ? x + vdim : x, py = y < 0 ? y + vdim : y, pz = z < 0 ? z + vdim : z;
         out[idx] = pad[((size_t)pz * vdim + py) * vdim + px] / tab[x * x + y * y + z * z];
     }
@@ -237,24 +238,26 @@ __global__ void k_acc_load(const float2* __restrict__ F, const float* __restrict
 
 struct Plan3 {
     tg3_ctx* c;
-    int vdim, type;
+    int vdim, nz, type;
     cufftHandle h;
 };
 std::vector<Plan3> g_plans3;
 std::mutex g_plans3Lock;
 
-int plan3(tg3_ctx* c, int vdim, cufftType type, cufftHandle* out)
+// cuFFT plan of the padded grid: vdim^3 (nz = vdim) or vdim^2 (nz = 1)
+int plan3(tg3_ctx* c, int vdim, int nz, cufftType type, cufftHandle* out)
 {
     std::lock_guard<std::mutex> g(g_plans3Lock);
     for (auto& p : g_plans3)
-        if (p.c == c && p.vdim == vdim && p.type == (int)type) {
+        if (p.c == c && p.vdim == vdim && p.nz == nz && p.type == (int)type) {
             *out = p.h;
             return TG3_OK;
         }
     cufftHandle h;
-    if (cufftPlan3d(&h, vdim, vdim, vdim, type) != CUFFT_SUCCESS)
-        return fail(TG3_ERR_CUDA, "cuFFT 3-D plan creation failed");
-    g_plans3.push_back({c, vdim, (int)type, h});
+    const cufftResult r = nz > 1 ? cufftPlan3d(&h, vdim, vdim, vdim, type)
+                                 : cufftPlan2d(&h, vdim, vdim, type);
+    if (r != CUFFT_SUCCESS) return fail(TG3_ERR_CUDA, "cuFFT plan creation failed");
+    g_plans3.push_back({c, vdim, nz, (int)type, h});
     *out = h;
     return TG3_OK;
 }
@@ -394,23 +397,19 @@ extern "C" int tg3_ctx_insert_load_d(tg3_ctx* c, const float* F, const float* T)
     return TG3_OK;
 }
 
-extern "C" int tg3_ctx_reconstruct_d(tg3_ctx* c, const double* fsc, int nFsc, int joinHalf,
-                                     int maxRadius, int gridCorr, int kernel, float a,
-                                     float alpha, float* vol, int* rounds)
+namespace {
+
+// The reconstruction chain on an accumulator acc of vdim x vdim x (vdim/2+1)
+// cells (nz = vdim, 3-D) or vdim x (vdim/2+1) (nz = 1, 2-D), into out: the
+// central N^3 or N^2 of the padded real-space result, N = vdim / pf.
+int reconstruct_core(tg3_ctx* c, const float4* acc, int vdim, int nz, int pf, const double* fsc,
+                     int nFsc, int joinHalf, int maxRadius, int gridCorr, int kernel, float a,
+                     float alpha, float* vol, int* rounds)
 {
-    int st = check_ctx(c);
-    if (st) return st;
-    if (!c->ins.acc) return fail(TG3_ERR_STATE, "no insertion accumulator (tg3_ctx_insert_begin)");
-    if (!vol || maxRadius <= 0 || (fsc && nFsc <= 0) ||
-        (kernel != TG3_KERNEL_MKB && kernel != TG3_KERNEL_TRILINEAR))
-        return fail(TG3_ERR_ARG, "bad reconstruction arguments");
-    if ((gridCorr || kernel == TG3_KERNEL_MKB) && !(a > 0 && alpha > 0))
-        return fail(TG3_ERR_ARG, "MKB parameters a and alpha must be positive");
-    const int vdim = c->ins.vdim, pf = c->ins.pf, N = vdim / pf;
-    if (maxRadius * pf > vdim / 2) return fail(TG3_ERR_ARG, "maxRadius beyond the padded grid");
-    // 32-bit voxel indices in the kernels
-    if ((size_t)vdim * vdim * vdim >= (1ull << 31)) return fail(TG3_ERR_UNSUPPORTED, "padded grid above 1290^3");
-    const size_t nh = (size_t)vdim * vdim * (vdim / 2 + 1), nr = (size_t)vdim * vdim * vdim;
+    int st = TG3_OK;
+    const int N = vdim / pf;
+    const double cells = nz > 1 ? (double)vdim * vdim * vdim : (double)vdim * vdim;
+    const size_t nh = (size_t)nz * vdim * (vdim / 2 + 1), nr = (size_t)nz * vdim * vdim;
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
     const int nqPad = 3 * (vdim / 2) * (vdim / 2) + 1, nqBox = 3 * (N / 2) * (N / 2) + 1;
     const size_t oT = 0, oW = up(4 * nh), oC = oW + up(4 * nh), oR = oC + up(8 * nh),
@@ -428,20 +427,19 @@ extern "C" int tg3_ctx_reconstruct_d(tg3_ctx* c, const double* fsc, int nFsc, in
     cudaStream_t s = c->stream;
     const long long r2max = (long long)maxRadius * pf * maxRadius * pf;
     const int G = 152 * 8;
-    k_reco_init<<<G, 256, 0, s>>>(c->ins.acc, vdim, pf, fsc, nFsc, joinHalf, r2max, T, W);
+    k_reco_init<<<G, 256, 0, s>>>(acc, vdim, nz, pf, fsc, nFsc, joinHalf, r2max, T, W);
     TG3_LAUNCH_CHECK("reconstruction set-up");
     const double i0a = bessel_i0(alpha);
     int m = 0;
     if (gridCorr) {
         cufftHandle inv, fwd;
-        if ((st = plan3(c, vdim, CUFFT_C2R, &inv)) || (st = plan3(c, vdim, CUFFT_R2C, &fwd)))
+        if ((st = plan3(c, vdim, nz, CUFFT_C2R, &inv)) || (st = plan3(c, vdim, nz, CUFFT_R2C, &fwd)))
             return st;
         if (cufftSetStream(inv, s) != CUFFT_SUCCESS || cufftSetStream(fwd, s) != CUFFT_SUCCESS)
             return fail(TG3_ERR_CUDA, "cuFFT stream");
         const double invNf = 1.0 / mkb_rl(0.0, a, alpha, i0a);
-        k_radial_table<<<(nqPad + 255) / 256, 256, 0, s>>>(
-            tabK, nqPad, (double)N * pf, 1, a, alpha, i0a,
-            invNf / ((double)vdim * vdim * vdim));
+        k_radial_table<<<(nqPad + 255) / 256, 256, 0, s>>>(tabK, nqPad, (double)N * pf, 1, a, alpha,
+                                                            i0a, invNf / cells);
         TG3_LAUNCH_CHECK("balancing kernel table");
         float diff = 3.4e38f, prev;
         int noDecrease = 0;
@@ -450,12 +448,12 @@ extern "C" int tg3_ctx_reconstruct_d(tg3_ctx* c, const double* fsc, int nFsc, in
         for (m = 0; m < 30; m++) {
             if (cufftExecC2R(inv, reinterpret_cast<cufftComplex*>(C), R) != CUFFT_SUCCESS)
                 return fail(TG3_ERR_CUDA, "cuFFT inverse transform failed");
-            k_reco_kernel_rl<<<G, 256, 0, s>>>(R, vdim, tabK);
+            k_reco_kernel_rl<<<G, 256, 0, s>>>(R, vdim, nz, tabK);
             TG3_LAUNCH_CHECK("balancing kernel product");
             if (cufftExecR2C(fwd, R, reinterpret_cast<cufftComplex*>(C)) != CUFFT_SUCCESS)
                 return fail(TG3_ERR_CUDA, "cuFFT forward transform failed");
             TG3_CUDA(cudaMemsetAsync(dBits, 0, sizeof(unsigned), s));
-            k_reco_update<<<G, 256, 0, s>>>(C, T, vdim, r2max, W, dBits);
+            k_reco_update<<<G, 256, 0, s>>>(C, T, vdim, nz, r2max, W, dBits);
             TG3_LAUNCH_CHECK("balancing update");
             unsigned bits = 0;
             TG3_CUDA(cudaMemcpyAsync(&bits, dBits, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
@@ -466,28 +464,103 @@ extern "C" int tg3_ctx_reconstruct_d(tg3_ctx* c, const double* fsc, int nFsc, in
             if (diff < 1e-2f || (m >= 10 && noDecrease == 2)) break;
         }
     } else {
-        k_reco_w_from_t<<<G, 256, 0, s>>>(T, vdim, r2max, W);
+        k_reco_w_from_t<<<G, 256, 0, s>>>(T, vdim, nz, r2max, W);
         TG3_LAUNCH_CHECK("W from T");
     }
     if (rounds) *rounds = gridCorr ? std::min(m + 1, 30) : 0;
     cufftHandle inv;
-    if ((st = plan3(c, vdim, CUFFT_C2R, &inv))) return st;
+    if ((st = plan3(c, vdim, nz, CUFFT_C2R, &inv))) return st;
     if (cufftSetStream(inv, s) != CUFFT_SUCCESS) return fail(TG3_ERR_CUDA, "cuFFT stream");
-    k_reco_fw<<<G, 256, 0, s>>>(c->ins.acc, W, vdim, r2max, C);
+    k_reco_fw<<<G, 256, 0, s>>>(acc, W, vdim, nz, r2max, C);
     TG3_LAUNCH_CHECK("F W");
     if (cufftExecC2R(inv, reinterpret_cast<cufftComplex*>(C), R) != CUFFT_SUCCESS)
         return fail(TG3_ERR_CUDA, "cuFFT inverse transform failed");
     const int mkb = kernel == TG3_KERNEL_MKB;
     const double nf = mkb ? mkb_rl(0.0, (double)a * pf, alpha, i0a) : 1.0;
-    // gridding correction: the map (times vdim^3 after the unnormalised
-    // inverse) over the kernel's real-space transform at |x| / (pf N)
-    k_radial_table<<<(nqBox + 255) / 256, 256, 0, s>>>(
-        tabE, nqBox, (double)pf * N, mkb, (double)a * pf, alpha, i0a,
-        (double)vdim * vdim * vdim / nf);
+    // gridding correction: the map (times the cell count after the
+    // unnormalised inverse) over the kernel's real-space transform at
+    // |x| / (pf N)
+    k_radial_table<<<(nqBox + 255) / 256, 256, 0, s>>>(tabE, nqBox, (double)pf * N, mkb,
+                                                        (double)a * pf, alpha, i0a, cells / nf);
     TG3_LAUNCH_CHECK("gridding correction table");
-    k_reco_extract<<<G, 256, 0, s>>>(R, vdim, N, tabE, vol);
+    k_reco_extract<<<G, 256, 0, s>>>(R, vdim, nz, N, tabE, vol);
     TG3_LAUNCH_CHECK("extract and gridding correction");
     return TG3_OK;
+}
+
+}  // namespace
+
+extern "C" int tg3_ctx_reconstruct_d(tg3_ctx* c, const double* fsc, int nFsc, int joinHalf,
+                                     int maxRadius, int gridCorr, int kernel, float a,
+                                     float alpha, float* vol, int* rounds)
+{
+    int st = check_ctx(c);
+    if (st) return st;
+    if (!c->ins.acc) return fail(TG3_ERR_STATE, "no insertion accumulator (tg3_ctx_insert_begin)");
+    if (!vol || maxRadius <= 0 || (fsc && nFsc <= 0) ||
+        (kernel != TG3_KERNEL_MKB && kernel != TG3_KERNEL_TRILINEAR))
+        return fail(TG3_ERR_ARG, "bad reconstruction arguments");
+    if ((gridCorr || kernel == TG3_KERNEL_MKB) && !(a > 0 && alpha > 0))
+        return fail(TG3_ERR_ARG, "MKB parameters a and alpha must be positive");
+    const int vdim = c->ins.vdim, pf = c->ins.pf;
+    if (maxRadius * pf > vdim / 2) return fail(TG3_ERR_ARG, "maxRadius beyond the padded grid");
+    // 32-bit voxel indices in the kernels
+    if ((size_t)vdim * vdim * vdim >= (1ull << 31)) return fail(TG3_ERR_UNSUPPORTED, "padded grid above 1290^3");
+    return reconstruct_core(c, c->ins.acc, vdim, vdim, pf, fsc, nFsc, joinHalf, maxRadius,
+                            gridCorr, kernel, a, alpha, vol, rounds);
+}
+
+// 2-D reconstruction (Reconstructor::reconstruct(Image&), MODE_2D): the same
+// chain on one class's 2-D accumulators, host buffers in and out.
+extern "C" int tg3_Reconstruct2D(const float* F2D, const float* T2D, int vdim, int pf,
+                                 const double* fsc, int nFsc, int joinHalf, int maxRadius,
+                                 int gridCorr, int kernel, float a, float alpha, float* img,
+                                 int* rounds)
+{
+    if (!F2D || !T2D || !img || vdim < 4 || (vdim & 1) || pf < 1 || vdim % pf ||
+        maxRadius <= 0 || maxRadius * pf > vdim / 2 || (fsc && nFsc <= 0) ||
+        (kernel != TG3_KERNEL_MKB && kernel != TG3_KERNEL_TRILINEAR))
+        return fail(TG3_ERR_ARG, "bad 2-D reconstruction arguments");
+    if ((gridCorr || kernel == TG3_KERNEL_MKB) && !(a > 0 && alpha > 0))
+        return fail(TG3_ERR_ARG, "MKB parameters a and alpha must be positive");
+    int dev = 0;
+    TG3_CUDA(cudaGetDevice(&dev));
+    static std::mutex mu;
+    static tg3_ctx* ctxs[64] = {};
+    if (dev < 0 || dev >= 64) return fail(TG3_ERR_ARG, "device ordinal out of range");
+    int st = TG3_OK;
+    tg3_ctx* c = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!ctxs[dev] && (st = tg3_ctx_create(&ctxs[dev], dev))) return st;
+        c = ctxs[dev];
+    }
+    const size_t nh = (size_t)vdim * (vdim / 2 + 1);
+    const int N = vdim / pf;
+    const size_t oA = 0, oF = (sizeof(float4) * nh + 255) / 256 * 256,
+                 oT = oF + (sizeof(float2) * nh + 255) / 256 * 256,
+                 oO = oT + (sizeof(float) * nh + 255) / 256 * 256,
+                 total = oO + sizeof(float) * (size_t)N * N;
+    char* b = (char*)ws_get(c, WS_RECO2D, total, &st);
+    if (!b) return st;
+    cudaStream_t s = c->stream;
+    double* dFsc = nullptr;
+    if (fsc) {
+        dFsc = (double*)ws_get(c, WS_MISC, sizeof(double) * nFsc, &st);
+        if (!dFsc) return st;
+        TG3_CUDA(cudaMemcpyAsync(dFsc, fsc, sizeof(double) * nFsc, cudaMemcpyHostToDevice, s));
+    }
+    TG3_CUDA(cudaMemcpyAsync(b + oF, F2D, sizeof(float2) * nh, cudaMemcpyHostToDevice, s));
+    TG3_CUDA(cudaMemcpyAsync(b + oT, T2D, sizeof(float) * nh, cudaMemcpyHostToDevice, s));
+    float4* acc = (float4*)(b + oA);
+    k_acc_load<<<152 * 2, 256, 0, s>>>((const float2*)(b + oF), (const float*)(b + oT), nh, acc);
+    TG3_LAUNCH_CHECK("2-D accumulator load");
+    if ((st = reconstruct_core(c, acc, vdim, 1, pf, dFsc, nFsc, joinHalf, maxRadius, gridCorr,
+                               kernel, a, alpha, (float*)(b + oO), rounds)))
+        return st;
+    TG3_CUDA(cudaMemcpyAsync(img, b + oO, sizeof(float) * (size_t)N * N, cudaMemcpyDeviceToHost,
+                             s));
+    return tg3_ctx_sync(c);
 }
 
 extern "C" int tg3_ctx_prepare_tf_d(tg3_ctx* c, const double* symMat, int nSym, int maxRadius,
