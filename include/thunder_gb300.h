@@ -617,6 +617,12 @@ int tg3_Reconstruct2D(const float* F2D, const float* T2D, int vdim, int pf,
                       const double* fsc, int nFsc, int joinHalf, int maxRadius,
                       int gridCorr, int kernel, float a, float alpha, float* img,
                       int* rounds);
+/* Reconstructor::symmetrizeO (src/Reconstructor.cpp, prepareO under
+ * RECONSTRUCTOR_SYMMETRIZE_DURING_RECONSTRUCT): O3D += sum over the symmetry
+ * elements symMat [nSym][9] (row-major, the identity excluded) of R O3D,
+ * counter *= 1 + nSym -- the offsets' share of the symmetrisation whose F and
+ * T share is tg3_PrepareTF.  Host arithmetic, no device. */
+int tg3_SymmetrizeO(double* O3D, int* counter, const double* symMat, int nSym);
 
 /* Noise spectrum sigma^2 from the images at their best poses
  * (Optimiser::allReduceSigma, src/Optimiser.cpp:6355-6630): the active pixel

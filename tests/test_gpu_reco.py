@@ -86,10 +86,12 @@ def test_reconstruct_2d_matches_oracle(grid_corr, kernel):
     fsc = np.clip(1.05 - np.arange(N // 2 + 1) / (N / 2), 0, 1)
     img = np.zeros((N, N), np.float32)
     rounds = np.zeros(1, np.int32)
-    tg3.check(tg3.lib().tg3_Reconstruct2D(
-        tg3.ptr(np.ascontiguousarray(F.astype(np.complex64))),
-        tg3.ptr(np.ascontiguousarray(T.astype(np.float32))), N * pf, pf, tg3.ptr(fsc), len(fsc), 1,
-        maxR, int(grid_corr), kernel, 1.9, 15.0, tg3.ptr(img), tg3.ptr(rounds)))
+    # named arrays: the addresses passed must stay alive through the call
+    F32 = np.ascontiguousarray(F.astype(np.complex64))
+    T32 = np.ascontiguousarray(T.astype(np.float32))
+    tg3.check(tg3.lib().tg3_Reconstruct2D(tg3.ptr(F32), tg3.ptr(T32), N * pf, pf, tg3.ptr(fsc),
+                                          len(fsc), 1, maxR, int(grid_corr), kernel, 1.9, 15.0,
+                                          tg3.ptr(img), tg3.ptr(rounds)))
     ref, ref_rounds = RC.reconstruct(F, T, pf, maxR, fsc=fsc, join_half=True, grid_corr=grid_corr,
                                      kernel="mkb" if kernel == tg3.KERNEL_MKB else "trilinear")
     assert int(rounds[0]) == ref_rounds

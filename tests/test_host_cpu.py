@@ -168,3 +168,26 @@ def test_binding_signatures_match_header():
         name, params = m.group(1), m.group(2).strip()
         n = 0 if params in ("", "void") else params.count(",") + 1
         assert len(getattr(L, name).argtypes) == n, (name, n, len(getattr(L, name).argtypes))
+
+
+def test_symmetrize_offsets_is_host_arithmetic():
+    """tg3_SymmetrizeO (Reconstructor::symmetrizeO): O + sum_s R_s O over the
+    elements besides the identity, counter times 1 + nSym -- host arithmetic,
+    so it runs without a device; against numpy for C4 about z."""
+    import ctypes
+    import tg3
+    sys_path = Path(__file__).resolve().parent / "golden"
+    import sys
+    sys.path.insert(0, str(sys_path))
+    from make_golden import symmetry_elements
+    c4, _ = symmetry_elements()
+    o = np.array([1.5, -0.25, 2.0])
+    got = o.copy()
+    cnt = np.array([7], np.int32)
+    tg3.check(tg3.lib().tg3_SymmetrizeO(tg3.ptr(got), tg3.ptr(cnt),
+                                        tg3.ptr(np.ascontiguousarray(c4.reshape(-1, 9))), len(c4)))
+    want = o + sum(m @ o for m in c4)
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-12)
+    assert cnt[0] == 7 * 4
+    # C4 about z: the x, y parts cancel, z adds up four times
+    np.testing.assert_allclose(got, [0.0, 0.0, 8.0], atol=1e-12)

@@ -510,6 +510,27 @@ extern "C" int tg3_ctx_reconstruct_d(tg3_ctx* c, const double* fsc, int nFsc, in
                             gridCorr, kernel, a, alpha, vol, rounds);
 }
 
+// The offsets' symmetrisation of Reconstructor::symmetrizeO (src/Reconstructor.cpp,
+// under RECONSTRUCTOR_SYMMETRIZE_DURING_RECONSTRUCT): O += sum_s R_s O over
+// the symmetry elements besides the identity (each R_s applied to the
+// unsymmetrised O), counter *= 1 + nSym.  Host arithmetic.
+extern "C" int tg3_SymmetrizeO(double* O3D, int* counter, const double* symMat, int nSym)
+{
+    if (!O3D || !counter || nSym < 0 || (nSym > 0 && !symMat))
+        return fail(TG3_ERR_ARG, "bad symmetrizeO arguments");
+    const double o[3] = {O3D[0], O3D[1], O3D[2]};
+    double r[3] = {o[0], o[1], o[2]};
+    for (int e = 0; e < nSym; e++) {
+        const double* m = symMat + 9 * e;
+        for (int i = 0; i < 3; i++) r[i] += m[3 * i] * o[0] + m[3 * i + 1] * o[1] + m[3 * i + 2] * o[2];
+    }
+    O3D[0] = r[0];
+    O3D[1] = r[1];
+    O3D[2] = r[2];
+    *counter *= 1 + nSym;
+    return TG3_OK;
+}
+
 // 2-D reconstruction (Reconstructor::reconstruct(Image&), MODE_2D): the same
 // chain on one class's 2-D accumulators, host buffers in and out.
 extern "C" int tg3_Reconstruct2D(const float* F2D, const float* T2D, int vdim, int pf,

@@ -31,7 +31,7 @@ EXPORTS = [
     "tg3_project_d", "tg3_ctx_render_references_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
     "tg3_ctx_set_option", "tg3_ctx_set_pixels_slot", "tg3_ctx_use_pixels",
     "tg3_ragged_plan_create", "tg3_ragged_plan_run", "tg3_ragged_plan_info",
-    "tg3_ragged_plan_kblock", "tg3_Reconstruct2D",
+    "tg3_ragged_plan_kblock", "tg3_Reconstruct2D", "tg3_SymmetrizeO",
     "tg3_ragged_plan_destroy", "tg3_cnn_create", "tg3_cnn_destroy", "tg3_cnn_param_count",
     "tg3_cnn_params", "tg3_cnn_grads", "tg3_cnn_set_bf16", "tg3_cnn_forward", "tg3_cnn_loss",
     "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose", "tg3_cnn_backward", "tg3_cnn_infer",
@@ -139,6 +139,7 @@ def lib():
             "tg3_ragged_plan_kblock": ([_P, _P], _I),
             "tg3_Reconstruct2D": ([_P, _P, _I, _I, _P, _I, _I, _I, _I, _I, ctypes.c_float,
                                    ctypes.c_float, _P, _P], _I),
+            "tg3_SymmetrizeO": ([_P, _P, _P, _I], _I),
             "tg3_ragged_plan_destroy": ([_P], _I),
             "tg3_cnn_create": ([_P, _I, ctypes.c_ulonglong], _I),
             "tg3_cnn_destroy": ([_P], _I),
