@@ -323,13 +323,14 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  *   reference's loop order), which is the faster of the two on GB300.  Both
  *   give the same sums up to FP32 rounding order; a pixel list holding a pixel
  *   twice always scatters.
- * TG3_OPT_BANK_GATHER (default 1): how the split-bf16 bank-row local phase
+ * TG3_OPT_BANK_GATHER (default 0): how the split-bf16 bank-row local phase
  *   (tg3_local_phase_bank_d, the learned E-step's rescoring) reads the
- *   proposed rows.  1: copied into a slice buffer, their norms summed from
- *   the bank's |P|^2 rows, then the GEMM.  0: the GEMM's own warps load its
- *   operand tiles from the bank rows and sum the rows' norms from them
- *   (compensated FP32).  2: as 0 with the tiles loaded by TMA gathers.
- * TG3_OPT_BANK_ORDER (default 0): 1 makes forms 0 and 2 above visit the
+ *   proposed rows.  0: the GEMM's own warps gather its operand tiles from
+ *   the bank rows with cp.async and sum the rows' norms from them
+ *   (compensated FP32) -- the fastest.  1: copied into a slice buffer, their
+ *   norms summed from the bank's |P|^2 rows, then the GEMM.  2: as 0 with the
+ *   tiles loaded by TMA gathers.
+ * TG3_OPT_BANK_ORDER (default 1): 1 makes forms 0 and 2 above visit the
  *   particles in the order of their first proposed row (class, then bank
  *   row), so that the particles in flight together share bank rows in L2;
  *   batches of more than 8,192 particles keep their own order.  The results

@@ -219,8 +219,9 @@ def test_bank_rows_straight_into_the_cross_term(case, nR, form, order):
         ctx.set_option(tg3.OPT_BANK_ORDER, order)
         a, b = run(form), run(1)
     finally:
-        ctx.set_option(tg3.OPT_BANK_GATHER, 1)
-        ctx.set_option(tg3.OPT_BANK_ORDER, 0)
+        # the library's defaults
+        ctx.set_option(tg3.OPT_BANK_GATHER, 0)
+        ctx.set_option(tg3.OPT_BANK_ORDER, 1)
     assert np.max(np.abs(a["dvp"] - b["dvp"]) / np.abs(b["dvp"])) < 1e-5
     for l in range(n):
         assert np.argmax(a["dvp"][l]) == np.argmax(b["dvp"][l])

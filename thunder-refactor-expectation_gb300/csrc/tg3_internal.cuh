@@ -192,8 +192,8 @@ struct tg3_ctx {
     // tg3_ctx_set_option
     bool fused = false;
     bool insertGather = false;    // TG3_OPT_INSERT_GATHER
-    int bankGather = 1;           // TG3_OPT_BANK_GATHER (0, 1 or 2)
-    int bankOrder = 0;            // TG3_OPT_BANK_ORDER
+    int bankGather = 0;           // TG3_OPT_BANK_GATHER (0, 1 or 2)
+    int bankOrder = 1;            // TG3_OPT_BANK_ORDER
     int scanTileN = 0;            // TG3_OPT_SCAN_TILE_N (0: 256)
     int scanPair = 0;             // TG3_OPT_SCAN_PAIR
     int scanBK = 32;              // TG3_OPT_SCAN_BK
