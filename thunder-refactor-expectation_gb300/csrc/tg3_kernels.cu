@@ -409,7 +409,7 @@ __global__ void k_shift_bank(const float2* __restrict__ dat, const float* __rest
                              int nT, int nD, int idim,
                              const int* __restrict__ iCol, const int* __restrict__ iRow,
                              int K, float* __restrict__ out, int ldo, long long splitLo,
-                             int useTab)
+                             int useTab, int tPer)
 {
     // per-particle translations with useTab: the phase e^{2 pi i (iCol tx + iRow ty) / N}
     // is the product of a column factor and a row factor, tabulated once per
@@ -419,8 +419,9 @@ __global__ void k_shift_bank(const float2* __restrict__ dat, const float* __rest
     extern __shared__ float2 tabX[];
     const int ld = blockIdx.x;            // l nD + d
     const int l = ld / nD;
-    const int t0 = blockIdx.y * SHIFT_T;
-    const int t1 = min(nT, t0 + SHIFT_T);
+    // tPer (<= SHIFT_T) translations per CTA, spread evenly over the groups
+    const int t0 = blockIdx.y * tPer;
+    const int t1 = min(nT, t0 + tPer);
     const float invN = 1.0f / (float)idim;
     const int h = idim / 2, nc = h + 1, nr = 2 * h + 1;
     float2* tabY = tabX + SHIFT_T * nc;
@@ -739,8 +740,10 @@ __global__ void k_x0(const float2* __restrict__ dat, const float* __restrict__ s
     const int l = blockIdx.x;
     double acc = 0;
     for (int p = threadIdx.x; p < K; p += blockDim.x) {
+        // FP32 terms, FP64 sum: one double add a pixel (the GPU's FP64
+        // rate is a small fraction of its FP32 rate)
         const float2 X = dat[(size_t)l * K + p];
-        acc += (double)sigRcp[(size_t)l * K + p] * ((double)X.x * X.x + (double)X.y * X.y);
+        acc += (double)(sigRcp[(size_t)l * K + p] * fmaf(X.x, X.x, X.y * X.y));
     }
     double s = block_sum_d(acc, red);
     if (threadIdx.x == 0) x0[l] = s;
@@ -1801,12 +1804,17 @@ cudaError_t launch_shift_bank(const float2* dat, const float* ctf, const float* 
                               int ldo, long long splitLo, cudaStream_t st, int nD)
 {
     if (nD < 1 || nT < 1) return cudaErrorInvalidValue;
-    dim3 grid((unsigned)nP * nD, (nT + SHIFT_T - 1) / SHIFT_T);
+    // groups of at most SHIFT_T translations, as even as possible (25 as
+    // 7 + 7 + 7 + 4, not 8 + 8 + 8 + 1: every CTA reloads its pixels)
+    const int groups = (nT + SHIFT_T - 1) / SHIFT_T;
+    const int tPer = (nT + groups - 1) / groups;
+    dim3 grid((unsigned)nP * nD, (nT + tPer - 1) / tPer);
     // the separable phase tables when they fit the default shared memory
     const size_t tab = bank ? 0 : sizeof(float2) * SHIFT_T * (size_t)(3 * (idim / 2) + 2);
     const int useTab = (!bank && idim >= 2 && tab <= 48 * 1024) ? 1 : 0;
     k_shift_bank<<<grid, 256, useTab ? tab : 0, st>>>(dat, ctf, sigRcp, trans, bank, nT, nD, idim,
-                                                      iCol, iRow, K, out, ldo, splitLo, useTab);
+                                                      iCol, iRow, K, out, ldo, splitLo, useTab,
+                                                      tPer);
     return cudaGetLastError();
 }
 
