@@ -2134,6 +2134,21 @@ def _cpu_global_worker(job):
     return 0
 
 
+# a pool worker's copy of the reference arm's inputs, sent once at start-up
+_CPU_JOBS = None
+
+
+def _cpu_init(jobs):
+    global _CPU_JOBS
+    _CPU_JOBS = jobs
+
+
+def _cpu_global_task(i):
+    """Particle i of the inputs the worker received at start-up: only the
+    index crosses the process boundary inside the timed steps."""
+    return _cpu_global_worker(_CPU_JOBS[i])
+
+
 def run_reference_learned(args, rank, world):
     """The reference's CPU E-step that the learned E-step replaces: the
     global search (doGlobalSearch, src/Optimiser.cpp:633-1136) of the
@@ -2174,11 +2189,13 @@ def run_reference_learned(args, rank, world):
                  pR=np.full(n_rot, 1.0 / n_rot), pT=np.full(len(trans), 1.0 / len(trans)),
                  paths=[str(ROOT), str(PKG)]) for i in range(cores)]
     times = []
-    with mp.get_context("spawn").Pool(cores) as pool:
-        pool.map(_cpu_global_worker, jobs)                  # start-up and page-in
+    # the inputs go to every worker once, at start-up (untimed); a step sends
+    # each worker one particle index
+    with mp.get_context("spawn").Pool(cores, initializer=_cpu_init, initargs=(jobs,)) as pool:
+        pool.map(_cpu_global_task, range(cores), chunksize=1)   # start-up and page-in
         for i in range(args.warmup + args.steps):
             t0 = time.perf_counter()
-            pool.map(_cpu_global_worker, jobs)
+            pool.map(_cpu_global_task, range(cores), chunksize=1)
             if i >= args.warmup:
                 times.append(time.perf_counter() - t0)
     per_step = float(np.mean(times))
