@@ -13,7 +13,6 @@ from __future__ import annotations
 
 import ctypes
 import os
-import re
 import subprocess
 from pathlib import Path
 
@@ -26,11 +25,11 @@ REF_LIB = HERE / "_ref" / "libthunder_ref.so"
 
 def _default_ref_tree() -> str:
     """The THUNDER tree the cross-check library is built from: THUNDER_REF,
-    else the default of the build recipe (oracle/ref/Makefile's REF)."""
+    else a tree named `reference` beside the repository's folder (the build
+    recipe's default too)."""
     if os.environ.get("THUNDER_REF"):
         return os.environ["THUNDER_REF"]
-    m = re.search(r"^REF \?= (\S+)$", (HERE / "ref" / "Makefile").read_text(), flags=re.M)
-    return m.group(1) if m else ""
+    return str(HERE.parent.parent / "reference")
 
 
 REF_TREE = Path(_default_ref_tree())
@@ -135,6 +134,9 @@ def ref():
         R.ref_resample.restype = _d
         R.ref_sort_descend.argtypes = [_f64p, _c, _u64p]
         R.ref_symmetrize.argtypes = [_c128p, _c, _f64p, _c, _d]
+        R.ref_reconstruct.argtypes = [_c, _c, _c, _d, _d, _c, _c128p, _f64p, _f64p, _c,
+                                      _c, _c, _c, _f64p]
+        R.ref_reconstruct.restype = _c
         _ref = R
     return _ref
 
@@ -338,3 +340,26 @@ def ref_symmetrize(vol, mats, r):
     m = _a(mats, np.float64).reshape(-1, 9)
     R.ref_symmetrize(v, v.shape[0], m, len(m), float(r))
     return v
+
+
+def ref_reconstruct(F, T, pf, max_radius, fsc, join_half=False, grid_corr=True, a=1.9,
+                    alpha=15.0, n_thread=1):
+    """Reconstructor::reconstruct through the compiled reference (None if
+    unavailable): F complex, T real on the padded half grid ((vdim,) * (d - 1)
+    + (vdim/2 + 1,)), d = 2 or 3 -> the N^d map, coordinate i at index
+    i + N/2.  The reference's build configures the trilinear real-space
+    correction."""
+    R = ref()
+    if R is None:
+        return None
+    F = _a(F, np.complex128)
+    T = _a(T, np.float64)
+    dim, vdim = F.ndim, F.shape[0]
+    N = vdim // pf
+    f = _a(np.zeros(1) if fsc is None else fsc, np.float64)
+    out = np.zeros((N,) * dim)
+    rc = R.ref_reconstruct(dim, N, pf, float(a), float(alpha), int(max_radius), F, T, f,
+                           len(f), int(join_half), int(grid_corr), int(n_thread), out.reshape(-1))
+    if rc != 0:
+        raise ValueError("reference reconstruct: accumulator size mismatch")
+    return out

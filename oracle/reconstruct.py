@@ -3,12 +3,14 @@
 -- the checker for tg3_ctx_reconstruct_d and tg3_Reconstruct2D, never on the
 product path.  The 2-D mode is the same chain on the padded 2-D half grid
 (the reference's _T2D / _W2D / _C2D branches, with the same MKB_RL and TIK_RL
-forms at |x| / (pf N)).  The kernel
-functions use scipy's Bessel functions (MKB_RL, TIK_RL of
-src/Functions/Functions.cpp:128-220) and are pinned to the compiled
-reference (tests/test_formats_cpu.py); the transforms are numpy's
-(unnormalised forward, 1/n inverse, as the reference's FFTW wrappers), so
-the whole chain is parity-unpinned beyond those functions."""
+forms at |x| / (pf N)).  The kernel functions use scipy's Bessel functions
+(MKB_RL, TIK_RL of src/Functions/Functions.cpp:128-220); the balancing kernel
+is looked up at r^2 rounded to the reference's table step.  The transforms
+are numpy's (unnormalised forward, 1/n inverse, as the reference's FFTW
+wrappers, src/FFT.cpp).  Pinned: the whole chain matches the compiled
+reference (with the vendored FFTW) to 1e-12 of the map's peak, live in
+tests/test_oracle_pin.py and by the fixtures of tests/golden/ref_golden_recon.npz
+in tests/test_oracle_golden.py."""
 from __future__ import annotations
 
 import numpy as np
@@ -39,11 +41,15 @@ def _coords(vdim, dim=3):
 
 
 def reconstruct(F, T, pf, max_radius, fsc=None, join_half=False, grid_corr=True, kernel="trilinear",
-                a=1.9, alpha=15.0):
+                a=1.9, alpha=15.0, kernel_step=1.0 / 100000):
     """F (complex), T (real) on the padded half grid (vdim, vdim, vdim/2 + 1),
     or (vdim, vdim/2 + 1) in 2-D -> the map (N, N, N) or image (N, N)
     centred (coordinate i at index i + N/2) and the number of balancing
-    rounds."""
+    rounds.  The balancing kernel is taken at r^2 rounded to the nearest
+    multiple of kernel_step, as the reference's table of it
+    (Reconstructor::_kernelRL, a TabFunction of r^2 over [0, 1] in 1e5 steps,
+    src/Reconstructor.cpp:76-85, looked up by src/TabFunction.cpp:42-45);
+    kernel_step = 0 evaluates it exactly."""
     dim = F.ndim
     vdim = F.shape[0]
     N = vdim // pf
@@ -65,8 +71,10 @@ def reconstruct(F, T, pf, max_radius, fsc=None, join_half=False, grid_corr=True,
     if grid_corr:
         c = np.fft.fftfreq(vdim, 1.0 / vdim)
         g = np.meshgrid(*([c] * dim), indexing="ij")
-        rr = np.sqrt(sum(v * v for v in g)) / (N * pf)
-        krl = mkb_rl(rr, a, alpha) / mkb_rl(0.0, a, alpha)
+        r2 = sum(v * v for v in g) / float(N * pf) ** 2
+        if kernel_step > 0:
+            r2 = np.rint(r2 / kernel_step) * kernel_step
+        krl = mkb_rl(np.sqrt(r2), a, alpha) / mkb_rl(0.0, a, alpha)
         diff, no_dec = np.inf, 0
         axes = tuple(range(dim))
         for m in range(30):

@@ -27,7 +27,30 @@
 #include "Particle.h"
 #include "Transformation.h"
 
+/* The reconstruction entry loads the accumulators the reference keeps as
+ * private members (_F3D, _T3D); the class is opened for this file only. */
+#define private public
+#define protected public
+#include "Reconstructor.h"
+#undef private
+#undef protected
+
 INITIALIZE_EASYLOGGINGPP
+
+/* The loggers the reconstruction writes to, registered and silenced. */
+static struct RefLoggers {
+    RefLoggers()
+    {
+        static el::Configurations conf;
+        conf.setToDefault();
+        conf.set(el::Level::All, el::ConfigurationType::Enabled, "false");
+        conf.set(el::Level::All, el::ConfigurationType::ToFile, "false");
+        conf.set(el::Level::All, el::ConfigurationType::ToStandardOutput, "false");
+        el::Loggers::setDefaultConfigurations(conf, true);
+        const char* names[] = {"LOGGER_SYS", "LOGGER_RECO", "LOGGER_MPI", "LOGGER_FFT"};
+        for (const char* n : names) el::Loggers::getLogger(n);
+    }
+} g_ref_loggers;
 
 /* Defined in src/Optimiser.cpp (non-static, no header declaration). */
 RFLOAT logDataVSPrior_m_huabin(const Complex* dat, const Complex* pri,
@@ -38,15 +61,6 @@ RFLOAT* logDataVSPrior_m_n_huabin(const Complex* dat, const Complex* pri,
                                   const int n, const int m, RFLOAT* result);
 
 /* ---- stand-ins for the external calls the compared routines make -------- */
-
-/* FFTW's allocator, used by ImageBase through TSFFTW_malloc. */
-extern "C" void* fftw_malloc(size_t n)
-{
-    void* p = NULL;
-    if (posix_memalign(&p, 64, n ? n : 64) != 0) return NULL;
-    return p;
-}
-extern "C" void fftw_free(void* p) { free(p); }
 
 /* Particle::resample / Particle::shuffle draw their randomness through these
  * two GSL calls; the harness injects the permutation and u0 instead. */
@@ -363,6 +377,57 @@ void ref_symmetrize(double* vol, int vdim, const double* mats, int nSym, double 
         vol[2 * i] = result[i].dat[0];
         vol[2 * i + 1] = result[i].dat[1];
     }
+}
+
+/* Reconstructor::reconstruct(Volume&, nThread), src/Reconstructor.cpp:1129-1790,
+ * on accumulators set directly: F complex and T real on the padded half grid
+ * ([vdim][vdim][vdim/2 + 1] in 3-D, [vdim][vdim/2 + 1] in 2-D, vdim = N pf),
+ * with the MAP Wiener step from fsc (nFsc shells), W balancing against the
+ * MKB kernel (gridCorr != 0) or W = 1/T, and the real-space correction the
+ * build configures (include/Config.h: trilinear).  The reconstructing rank
+ * is a non-master rank (the master returns at once).  out: the N^d map,
+ * coordinate i at index i + N/2, slowest axis first.  Returns 0. */
+int ref_reconstruct(int dim, int N, int pf, double a, double alpha, int maxRadius,
+                    const double* F, const double* T, const double* fsc, int nFsc,
+                    int joinHalf, int gridCorr, int nThread, double* out)
+{
+    Reconstructor R;
+    R.setCommRank(1);
+    R.setCommSize(2);
+    R.init(dim == 2 ? MODE_2D : MODE_3D, N, N, pf, NULL, a, alpha);
+    R.allocSpace(nThread);
+    R.setMaxRadius(maxRadius);
+    R.setMAP(true);
+    R.setGridCorr(gridCorr != 0);
+    R.setJoinHalf(joinHalf != 0);
+    vec v(nFsc);
+    for (int i = 0; i < nFsc; i++) v(i) = fsc[i];
+    R.setFSC(v);
+    const int vdim = N * pf;
+    Complex* pF = dim == 2 ? &R._F2D[0] : &R._F3D[0];
+    Complex* pT = dim == 2 ? &R._T2D[0] : &R._T3D[0];
+    const size_t n = dim == 2 ? R._F2D.sizeFT() : R._F3D.sizeFT();
+    if (n != (size_t)(dim == 2 ? 1 : vdim) * vdim * (vdim / 2 + 1)) return 1;
+    for (size_t i = 0; i < n; i++) {
+        pF[i].dat[0] = F[2 * i];
+        pF[i].dat[1] = F[2 * i + 1];
+        pT[i].dat[0] = T[i];
+        pT[i].dat[1] = 0;
+    }
+    Volume dst;
+    R.reconstruct(dst, nThread);
+    const int h = N / 2;
+    if (dim == 2) {
+        for (int j = -h; j < N - h; j++)
+            for (int i = -h; i < N - h; i++)
+                out[(size_t)(j + h) * N + (i + h)] = dst.getRL(i, j, 0);
+    } else {
+        for (int k = -h; k < N - h; k++)
+            for (int j = -h; j < N - h; j++)
+                for (int i = -h; i < N - h; i++)
+                    out[((size_t)(k + h) * N + (j + h)) * N + (i + h)] = dst.getRL(i, j, k);
+    }
+    return 0;
 }
 
 void ref_sort_descend(const double* v, int n, size_t* idx)

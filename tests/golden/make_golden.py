@@ -4,7 +4,7 @@ oracle/ref/Makefile from the THUNDER sources) on small seeded cases.
 
 Also writes tests/golden/ref_golden_formats.npz (the 2-D, preprocessing,
 spectrum and MRC routines) and tests/golden/ref_golden_recon.npz (the
-symmetrisation of half transforms).  Run in a checkout that has the THUNDER tree:
+symmetrisation of half transforms and the reconstruction chain).  Run in a checkout that has the THUNDER tree:
     python tests/golden/make_golden.py
 The fixture pins the oracle (tests/test_oracle_golden.py) on machines that
 do not have the reference sources."""
@@ -139,7 +139,8 @@ def symmetry_elements():
 
 def main_recon():
     """ref_golden_recon.npz: the reference's symmetrisation of half
-    transforms (SYMMETRIZE_FT through VOL_TRANSFORM_MAT_FT)."""
+    transforms (SYMMETRIZE_FT through VOL_TRANSFORM_MAT_FT) and its
+    reconstruction (Reconstructor::reconstruct, with the vendored FFTW)."""
     R = O.ref()
     if R is None:
         raise SystemExit("reference cross-check library unavailable")
@@ -153,6 +154,27 @@ def main_recon():
         g[f"sym_mats_{name}"] = mats
         g[f"sym_out_{name}"] = O.ref_symmetrize(vol, mats, 6.5)
     g["sym_r"] = 6.5
+    # Reconstructor::reconstruct on Hermitian-consistent accumulators (F the
+    # half transform of a real volume, T = |half transform|^2 + 0.5, real and
+    # even), stored at float32 precision (exact as float64) to keep the file
+    # small; 3-D with W balancing, with joinHalf and with W = 1/T on one pair
+    # of accumulators, and 2-D with W balancing
+    rng = np.random.default_rng(20261205)
+    pf = 2
+    for dim, N, flags in ((3, 12, ((True, False), (True, True), (False, False))),
+                          (2, 32, ((True, False),))):
+        shape = (N * pf,) * dim
+        F = np.fft.rfftn(rng.standard_normal(shape)).astype(np.complex64)
+        T = (np.abs(np.fft.rfftn(rng.standard_normal(shape))) ** 2 / np.prod(shape)
+             + 0.5).astype(np.float32)
+        fsc = np.linspace(0.999, 0.2, N // 2 + 2)
+        maxR = N // 2
+        g[f"reco{dim}_F"], g[f"reco{dim}_T"], g[f"reco{dim}_fsc"] = F, T, fsc
+        g[f"reco{dim}_args"] = np.array([pf, maxR])
+        g[f"reco{dim}_flags"] = np.array(flags, dtype=np.int32)
+        g[f"reco{dim}_out"] = np.stack([
+            O.ref_reconstruct(F, T, pf, maxR, fsc, join_half=join, grid_corr=gc)
+            for gc, join in flags])
     out = ROOT / "tests" / "golden" / "ref_golden_recon.npz"
     np.savez_compressed(out, **g)
     print("wrote", out)

@@ -98,6 +98,61 @@ def test_reconstruct_2d_matches_oracle(grid_corr, kernel):
     assert np.abs(img - ref).max() < 1e-3 * np.abs(ref).max()
 
 
+def _golden_recon():
+    from pathlib import Path
+    return np.load(Path(__file__).resolve().parent / "golden" / "ref_golden_recon.npz")
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_reconstruct_matches_reference_fixture(case):
+    """tg3_ctx_reconstruct_d against the reference's own
+    Reconstructor::reconstruct (compiled with the vendored FFTW; outputs in
+    tests/golden/ref_golden_recon.npz): W balancing, joinHalf, W = 1/T; the
+    build's trilinear correction.  The map within 1e-3 of its peak, with the
+    balancing rounds of the oracle (which matches the fixture to 1e-14)."""
+    g = _golden_recon()
+    pf, maxR = (int(v) for v in g["reco3_args"])
+    gc, join = (bool(v) for v in g["reco3_flags"][case])
+    F, T, fsc = g["reco3_F"], g["reco3_T"], g["reco3_fsc"]
+    N = F.shape[0] // pf
+    ctx = tg3.Context(0)
+    try:
+        ctx.insert_begin(N * pf, pf)
+        ctx.insert_load(torch.as_tensor(F).to(DEV), torch.as_tensor(T).to(DEV))
+        vol = torch.empty((N, N, N), dtype=torch.float32, device=DEV)
+        rounds = ctx.reconstruct(vol, maxR, fsc=torch.as_tensor(fsc).to(DEV), join_half=join,
+                                 grid_corr=gc, kernel=tg3.KERNEL_TRILINEAR)
+        ctx.sync()
+    finally:
+        ctx.close()
+    ref = g["reco3_out"][case]
+    _, ref_rounds = RC.reconstruct(F, T, pf, maxR, fsc=fsc, join_half=join, grid_corr=gc)
+    assert rounds == ref_rounds
+    assert np.abs(vol.cpu().numpy() - ref).max() < 1e-3 * np.abs(ref).max()
+
+
+def test_reconstruct_2d_matches_reference_fixture():
+    """tg3_Reconstruct2D against the reference's MODE_2D reconstruct
+    (tests/golden/ref_golden_recon.npz), W balancing, trilinear correction."""
+    g = _golden_recon()
+    pf, maxR = (int(v) for v in g["reco2_args"])
+    gc, join = (bool(v) for v in g["reco2_flags"][0])
+    F = np.ascontiguousarray(g["reco2_F"])
+    T = np.ascontiguousarray(g["reco2_T"])
+    fsc = np.ascontiguousarray(g["reco2_fsc"])
+    N = F.shape[0] // pf
+    img = np.zeros((N, N), np.float32)
+    rounds = np.zeros(1, np.int32)
+    tg3.check(tg3.lib().tg3_Reconstruct2D(tg3.ptr(F), tg3.ptr(T), N * pf, pf, tg3.ptr(fsc),
+                                          len(fsc), int(join), maxR, int(gc),
+                                          tg3.KERNEL_TRILINEAR, 1.9, 15.0, tg3.ptr(img),
+                                          tg3.ptr(rounds)))
+    ref = g["reco2_out"][0]
+    _, ref_rounds = RC.reconstruct(F, T, pf, maxR, fsc=fsc, join_half=join, grid_corr=gc)
+    assert int(rounds[0]) == ref_rounds
+    assert np.abs(img - ref).max() < 1e-3 * np.abs(ref).max()
+
+
 @pytest.mark.parametrize("which", ["c4", "d2"])
 def test_prepare_tf_matches_oracle(which):
     """PrepareTF on the accumulators: F and T scaled by 1 / T at the origin,

@@ -119,12 +119,17 @@ __global__ void k_reco_tw(const float* __restrict__ T, const float* __restrict__
 
 // A radial function of the integer squared radius q, tabulated once per call
 // (the kernels depend on x^2 + y^2 + z^2 only): tab[q] = scale k(sqrt(q) / s)
-// with k the MKB real-space form (mkb) or j0(pi r)^2.
+// with k the MKB real-space form (mkb) or j0(pi r)^2.  r2step > 0 takes the
+// kernel at r^2 rounded to the nearest multiple of r2step, as a TabFunction
+// of r^2 looks it up (src/TabFunction.cpp:42-45; the balancing kernel
+// Reconstructor::_kernelRL is one over [0, 1] in 1e5 steps,
+// src/Reconstructor.cpp:76-85).
 __global__ void k_radial_table(float* __restrict__ tab, int nq, double s, int mkb, double a,
-                               double alpha, double i0a, double scale)
+                               double alpha, double i0a, double scale, double r2step)
 {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
-        const double r = sqrt((double)q) / s;
+        double r = sqrt((double)q) / s;
+        if (r2step > 0) r = sqrt(rint((double)q / (s * s) / r2step) * r2step);
         tab[q] = (float)(scale * (mkb ? mkb_rl(r, a, alpha, i0a) : tik_rl(r)));
     }
 }
@@ -439,7 +444,7 @@ int reconstruct_core(tg3_ctx* c, const float4* acc, int vdim, int nz, int pf, co
             return fail(TG3_ERR_CUDA, "cuFFT stream");
         const double invNf = 1.0 / mkb_rl(0.0, a, alpha, i0a);
         k_radial_table<<<(nqPad + 255) / 256, 256, 0, s>>>(tabK, nqPad, (double)N * pf, 1, a, alpha,
-                                                            i0a, invNf / cells);
+                                                            i0a, invNf / cells, 1.0 / 100000);
         TG3_LAUNCH_CHECK("balancing kernel table");
         float diff = 3.4e38f, prev;
         int noDecrease = 0;
@@ -481,7 +486,7 @@ int reconstruct_core(tg3_ctx* c, const float4* acc, int vdim, int nz, int pf, co
     // unnormalised inverse) over the kernel's real-space transform at
     // |x| / (pf N)
     k_radial_table<<<(nqBox + 255) / 256, 256, 0, s>>>(tabE, nqBox, (double)pf * N, mkb,
-                                                        (double)a * pf, alpha, i0a, cells / nf);
+                                                        (double)a * pf, alpha, i0a, cells / nf, 0.0);
     TG3_LAUNCH_CHECK("gridding correction table");
     k_reco_extract<<<G, 256, 0, s>>>(R, vdim, nz, N, tabE, vol);
     TG3_LAUNCH_CHECK("extract and gridding correction");
