@@ -194,6 +194,7 @@ def run_tg3(args, rank, world, local_rank):
     nR, nT, K = W["nR"], W["nT"], st.K
     ctx = tg3.Context(local_rank)
     ctx.set_option(tg3.OPT_LOCAL_BK, args.local_bk)
+    ctx.set_option(tg3.OPT_PROJECT_FORM, args.project_form)
     if args.fused:
         ctx.set_option(tg3.OPT_FUSED, 1)
     for c, v in enumerate(vols):
@@ -415,7 +416,7 @@ def run_tg3(args, rank, world, local_rank):
                                   "split evenly" if W["n_classes"] > 1 else ""),
                    "box": W["box"], "pf": W["pf"], "K": K, "nR": nR, "nT": nT,
                    "classes": W["n_classes"], "particles_per_step": nP,
-                   "precision": args.precision,
+                   "precision": args.precision, "projection_form": args.project_form,
                    "l2": "inputs larger than L2: the projection bank alone is "
                          f"{nP * nR * ctx_kp(K) * 4 / 1e9:.1f} GB per step"},
         "clocks": clocks,
@@ -984,6 +985,7 @@ def run_fallback(args, rank, world, local_rank):
     ctx = tg3.Context(local_rank)
     ctx.set_option(tg3.OPT_SCAN_PAIR, args.scan_pair)
     ctx.set_option(tg3.OPT_SCAN_BK, args.scan_bk)
+    ctx.set_option(tg3.OPT_PROJECT_FORM, args.project_form)
     ctx.set_volume(0, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
     ctx.set_pixels(ps.iCol, ps.iRow, box)
     qg = synth.global_rotations(4, 36)
@@ -1381,6 +1383,7 @@ def run_learned(args, rank, world, local_rank):
     ctx.set_option(tg3.OPT_BANK_ORDER, args.bank_order)
     ctx.set_option(tg3.OPT_SCAN_PAIR, args.scan_pair)
     ctx.set_option(tg3.OPT_SCAN_BK, args.scan_bk)
+    ctx.set_option(tg3.OPT_PROJECT_FORM, args.project_form)
     for c, bm in enumerate(maps):
         ctx.set_volume(c, synth.padded_volume(bm, box, pf, device=dev, dtype=torch.float32), pf)
     ctx.set_pixels(iCol, iRow, box)
@@ -2368,6 +2371,10 @@ def main():
                          "share each column tile by TMA multicast")
     ap.add_argument("--local-bk", type=int, default=64, choices=[32, 64],
                     help="TG3_OPT_LOCAL_BK: K block of the local phase's split cross term")
+    ap.add_argument("--project-form", type=int, default=4, choices=[0, 1, 2, 3, 4],
+                    help="TG3_OPT_PROJECT_FORM: 0 a lane pair per pixel, 1 one lane per pixel, "
+                         "2 one lane per pixel with the block index computed, 3/4 lane pairs "
+                         "sharing whole-block loads (index looked up / computed)")
     ap.add_argument("--scan-bk", type=int, default=32, choices=[32, 64],
                     help="TG3_OPT_SCAN_BK: K block of the global search's cross-term stages")
     ap.add_argument("--bank-order", type=int, default=1, choices=[0, 1],

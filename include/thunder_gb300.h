@@ -350,7 +350,13 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  * TG3_OPT_LOCAL_BK (default 64): the same choice for the split-bf16 local
  *   phase's cross term (tg3_local_phase_d); an uneven-batch plan created
  *   with an autotuned budget tries both and keeps the faster for its
- *   waves. */
+ *   waves.
+ * TG3_OPT_PROJECT_FORM (default 4): how the projection extracts samples,
+ *   0 with a lane pair per pixel (each lane one slab of the corner block,
+ *   joined by a shuffle), 1 with one lane per pixel, 2 with one lane per
+ *   pixel and the block index computed instead of looked up, 3 and 4 with
+ *   every lane finding its own pixel's block and a lane pair loading both
+ *   pixels' blocks together (index looked up, computed).  Same samples. */
 enum {
     TG3_OPT_FUSED = 0,
     TG3_OPT_INSERT_GATHER = 1,
@@ -359,7 +365,8 @@ enum {
     TG3_OPT_SCAN_TILE_N = 4,
     TG3_OPT_SCAN_PAIR = 5,
     TG3_OPT_SCAN_BK = 6,
-    TG3_OPT_LOCAL_BK = 7
+    TG3_OPT_LOCAL_BK = 7,
+    TG3_OPT_PROJECT_FORM = 8
 };
 int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);

@@ -103,6 +103,67 @@ def test_project(small, ctx):
     assert np.max(np.abs(P - ref) / scale) < 1e-5
 
 
+def test_project_forms(small, ctx):
+    """The projection forms (TG3_OPT_PROJECT_FORM: 0 lane pair, 1 one lane per
+    pixel, 2 the same with a computed block index, 3 / 4 lane pairs sharing
+    whole-block loads) against the oracle, and against each other: the same
+    corner sums in the same order, so the samples agree to within one
+    rounding of a sum's contraction, and forms differing only in how the
+    block index is found (1 and 2, 3 and 4) exactly."""
+    rng = small["rng"]
+    q = synth.haar_quaternions(rng, 40)
+    mat = O.rotmat(q).reshape(-1, 9)
+    K = len(small["iCol"])
+    res = {}
+    try:
+        for form in (0, 1, 2, 3, 4):
+            ctx.set_option(tg3.OPT_PROJECT_FORM, form)
+            out = torch.empty((40, K, 2), dtype=torch.float32, device=DEV)
+            ctx.project(0, dev(mat), 40, out)
+            ctx.sync()
+            P = out.cpu().numpy().astype(np.float64)
+            res[form] = P[..., 0] + 1j * P[..., 1]
+    finally:
+        ctx.set_option(tg3.OPT_PROJECT_FORM, 4)
+    ref = O.project(small["vol"], mat, small["iCol"], small["iRow"], small["pf"])
+    scale = np.abs(ref).max(axis=1, keepdims=True)
+    for form in (0, 1, 2, 3, 4):
+        assert np.max(np.abs(res[form] - ref) / scale) < 1e-5
+    assert np.max(np.abs(res[0] - res[1]) / scale) < 1e-6
+    assert np.max(np.abs(res[0] - res[3]) / scale) < 1e-6
+    np.testing.assert_array_equal(res[1], res[2])
+    np.testing.assert_array_equal(res[3], res[4])
+
+
+def test_local_phase_project_forms(small, ctx):
+    """The split-bf16 local phase with either projection form: likelihoods
+    within 1e-6 relative of each other (the bf16 split of equal samples is
+    equal; the norms' pixel sums run in another order)."""
+    nP, nR, nT = 3, 200, 30
+    d = _local_inputs(small, nP, nR, nT, 13)
+    res = {}
+    try:
+        for form in (0, 2, 4):
+            ctx.set_option(tg3.OPT_PROJECT_FORM, form)
+            o = dict(wC=torch.empty(nP, dtype=torch.float64, device=DEV),
+                     wR=torch.empty((nP, nR), dtype=torch.float64, device=DEV),
+                     wT=torch.empty((nP, nT), dtype=torch.float64, device=DEV),
+                     base=torch.empty(nP, dtype=torch.float64, device=DEV),
+                     dvp=torch.empty((nP, nR, nT), dtype=torch.float32, device=DEV))
+            ctx.local_phase(nP, nR, nT, dev(d["dat"]), dev(d["ctf"]), dev(d["sig"]),
+                            dev(d["qs"]), dev(d["ts"]), dev(d["pwR"]), dev(d["pwT"]),
+                            dev(d["pwC"]), None, o["wC"], o["wR"], o["wT"], o["base"], o["dvp"],
+                            tg3.SCORE_BF16X3)
+            ctx.sync()
+            res[form] = {k: v.cpu().numpy() for k, v in o.items()}
+    finally:
+        ctx.set_option(tg3.OPT_PROJECT_FORM, 4)
+    a = res[0]["dvp"].astype(np.float64)
+    for form in (2, 4):
+        b = res[form]["dvp"].astype(np.float64)
+        assert np.max(np.abs(a - b)) < 1e-6 * np.abs(a).max()
+
+
 def test_expect_project_host(small):
     rng = small["rng"]
     q = synth.haar_quaternions(rng, 10)

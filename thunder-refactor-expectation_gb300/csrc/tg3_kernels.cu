@@ -366,6 +366,358 @@ k_project(float4* const* __restrict__ volTable, const int* __restrict__ cls,
     }
 }
 
+// The same extraction with one lane per pixel (form 1).  A lane reads both
+// slabs of its pixel's corner block (two 256-bit loads) and forms the sample
+// alone, so the coordinates, the block address and the fractions are
+// computed once per sample instead of once per lane of a pair, and no
+// shuffle joins the halves.  The slab sums are formed in the pair form's
+// order (slab z0's four corners, slab z0 + 1's, then their sum).  Pixels:
+// p = chunk kProjChunk + u blockDim + threadIdx, u < kProjChunk / blockDim.
+// A warp's 32 pixels are consecutive, so its hi and lo (or FP32) stores are
+// 128-byte (256-byte) runs.
+// kArith forms the block index from the coordinates with integer
+// arithmetic instead of the per-axis shared-memory tables: lanes of a warp
+// look up scattered table entries, and those lookups share the L1 data pipe
+// with the corner-block loads.
+constexpr int kLaneU = kProjChunk / 256;
+template <bool kArith>
+__global__ void __launch_bounds__(256, 4)
+k_project_lane(float4* const* __restrict__ volTable, const int* __restrict__ cls,
+               const float4* __restrict__ vol0, int vdim, int pf, const float* __restrict__ mf,
+               int rowsPerParticle, int nGroups, int nChunks, const int* __restrict__ iCol,
+               const int* __restrict__ iRow, int K, float* __restrict__ out, int ldo,
+               const float* __restrict__ sigRcp, const float* __restrict__ ctf,
+               float* __restrict__ nrmPart, int* __restrict__ flag, long long splitLo)
+{
+    __shared__ float m[kProjG][9];
+    __shared__ float red[kProjG][8];
+    const int g = blockIdx.x % nGroups;
+    const int chunk = (blockIdx.x / nGroups) % nChunks;
+    const int l = blockIdx.x / (nGroups * nChunks);
+    const int r0 = g * kProjG;
+    const int nRot = min(kProjG, rowsPerParticle - r0);
+    const size_t row0 = (size_t)l * rowsPerParticle + r0;
+    extern __shared__ int tab[];
+    const int half = vdim / 2;
+    const int nxc = cubes_x(vdim), nyc = cubes_yz(vdim);
+    int* tx = tab;
+    int* ty = tab + vdim / 2 + 1;
+    int* tz = ty + vdim;
+    if (!kArith) fill_brick_tables(vdim, tx, ty, tz);
+    if (threadIdx.x < 9 * nRot) m[threadIdx.x / 9][threadIdx.x % 9] = mf[9 * row0 + threadIdx.x];
+    __syncthreads();
+    const int nOut = ldo / 2;
+    const int pBase = chunk * kProjChunk + threadIdx.x;
+    __nv_bfloat162* hiPlane = reinterpret_cast<__nv_bfloat162*>(out);
+    __nv_bfloat162* loPlane = reinterpret_cast<__nv_bfloat162*>(
+        reinterpret_cast<__nv_bfloat16*>(out) + splitLo);
+    auto store = [&](size_t row, int p, float re, float im) {
+        if (splitLo == 0) {
+            reinterpret_cast<float2*>(out + row * ldo)[p] = make_float2(re, im);
+        } else {
+            const __nv_bfloat162 v = __floats2bfloat162_rn(re, im);
+            const float2 hf = __bfloat1622float2(v);
+            hiPlane[row * nOut + p] = v;
+            loPlane[row * nOut + p] = __floats2bfloat162_rn(re - hf.x, im - hf.y);
+        }
+    };
+    const float4* __restrict__ vol = vol0;
+    if (volTable) {
+        const int k = cls ? cls[l] : 0;
+        vol = (k >= 0 && k < kMaxClasses) ? volTable[k] : nullptr;
+        if (!vol) {
+            // unknown class: record it, leave the rows' chunk zero and skip sampling
+            if (threadIdx.x == 0 && flag) atomicOr(flag, 8);
+            for (int i = 0; i < nRot; i++)
+#pragma unroll
+                for (int u = 0; u < kLaneU; u++) {
+                    const int p = pBase + u * 256;
+                    if (p < nOut) store(row0 + i, p, 0.f, 0.f);
+                }
+            if (nrmPart && threadIdx.x < nRot) nrmPart[(row0 + threadIdx.x) * nChunks + chunk] = 0.f;
+            return;
+        }
+    }
+    const float fpf = (float)pf;
+    const float* sg = sigRcp ? sigRcp + (size_t)l * K : nullptr;
+    const float* cf = ctf ? ctf + (size_t)l * K : nullptr;
+    float pa[kLaneU], pb[kLaneU], w2[kLaneU];
+#pragma unroll
+    for (int u = 0; u < kLaneU; u++) {
+        const int p = pBase + u * 256;
+        const int q = p < K ? p : 0;
+        pa[u] = (float)iCol[q] * fpf;
+        pb[u] = (float)iRow[q] * fpf;
+        w2[u] = (nrmPart && p < K) ? sg[q] * cf[q] * cf[q] : 0.f;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll 1
+    for (int i = 0; i < nRot; i++) {   // nRot is uniform across the CTA
+        const float* mm = m[i];
+        float acc = 0.f;
+        float fw[kLaneU][3];
+        bool cj[kLaneU];
+        const float4* e[kLaneU];
+#pragma unroll
+        for (int u = 0; u < kLaneU; u++) {
+            float x = mm[0] * pa[u] + mm[1] * pb[u];
+            float y = mm[3] * pa[u] + mm[4] * pb[u];
+            float z = mm[6] * pa[u] + mm[7] * pb[u];
+            cj[u] = x < 0.f;
+            if (cj[u]) { x = -x; y = -y; z = -z; }
+            const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+            const int x0 = (int)xf, y0 = (int)yf, z0 = (int)zf;
+            fw[u][0] = x - xf;
+            fw[u][1] = y - yf;
+            fw[u][2] = z - zf;
+            unsigned blk;
+            if (kArith) {
+                // brick_index with the rows' and slabs' wrap of negative indices
+                const int yy = y0 < 0 ? y0 + vdim : y0;
+                const int zz = z0 < 0 ? z0 + vdim : z0;
+                blk = (unsigned)((((zz >> 5) * nyc + (yy >> 5)) * nxc + (x0 >> 5)) * 32768
+                                 + ((((zz >> 3) & 3) * 4 + ((yy >> 3) & 3)) * 4 + ((x0 >> 3) & 3)) * 512
+                                 + ((zz & 7) * 8 + (yy & 7)) * 8 + (x0 & 7));
+            } else {
+                blk = (unsigned)(tx[x0] + ty[y0 + half] + tz[z0 + half]);
+            }
+            e[u] = vol + 4 * (size_t)blk;
+        }
+        float4 c[kLaneU][4];
+#pragma unroll
+        for (int u = 0; u < kLaneU; u++)
+#pragma unroll
+            for (int k = 0; k < 2; k++)
+                asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                    : "=f"(c[u][2 * k].x), "=f"(c[u][2 * k].y), "=f"(c[u][2 * k].z),
+                      "=f"(c[u][2 * k].w), "=f"(c[u][2 * k + 1].x), "=f"(c[u][2 * k + 1].y),
+                      "=f"(c[u][2 * k + 1].z), "=f"(c[u][2 * k + 1].w)
+                    : "l"(e[u] + 2 * k));
+#pragma unroll
+        for (int u = 0; u < kLaneU; u++) {
+            const float fx = fw[u][0], fy = fw[u][1], fz = fw[u][2];
+            const float wx0 = 1.f - fx, wx1 = fx;
+            float sr[2], si[2];
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const float wz = k ? fz : 1.f - fz;
+                const float wy0 = (1.f - fy) * wz, wy1 = fy * wz;
+                const float4 a = c[u][2 * k], b = c[u][2 * k + 1];
+                float re = a.x * (wx0 * wy0) + a.z * (wx1 * wy0);
+                float im = a.y * (wx0 * wy0) + a.w * (wx1 * wy0);
+                re += b.x * (wx0 * wy1) + b.z * (wx1 * wy1);
+                im += b.y * (wx0 * wy1) + b.w * (wx1 * wy1);
+                sr[k] = re;
+                si[k] = im;
+            }
+            float re = sr[0] + sr[1];
+            float im = si[0] + si[1];
+            const int p = pBase + u * 256;
+            if (p < nOut) {
+                if (p < K) {
+                    if (cj[u]) im = -im;
+                    store(row0 + i, p, re, im);
+                    acc = fmaf(w2[u], re * re + im * im, acc);
+                } else {
+                    store(row0 + i, p, 0.f, 0.f);
+                }
+            }
+        }
+        if (nrmPart) {
+            acc = warp_sum(acc);
+            if (lane == 0) red[i][wid] = acc;
+        }
+    }
+    if (nrmPart) {
+        __syncthreads();
+        if (threadIdx.x < nRot) {
+            float s = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[threadIdx.x][w];
+            nrmPart[(row0 + threadIdx.x) * nChunks + chunk] = s;
+        }
+    }
+}
+
+// Lane pairs that share loads but not the coordinate work (forms 3 and 4).
+// Every lane finds the block index and fractions of its own pixel (as in the
+// one-lane form: once per sample), then a pair swaps them by one shuffle
+// each.  The pair's two loads read pixel A's block (lane 0 slab z0, lane 1
+// slab z0 + 1) and then pixel B's, so every load instruction takes whole
+// 64-byte blocks, one L1 wavefront per pixel as in the lane-pair form.
+// Each lane forms its slab's share of both pixels; lane 0 keeps A and lane 1
+// B, the other share arriving by shuffle (slab z0's share plus slab z0 + 1's,
+// the pair form's sum).  (Recomputing the partner's fractions from its
+// coordinates instead of receiving them by three shuffles measured slower:
+// 8.99 against 8.56 ms per 128 particles at box 256.)
+template <bool kArith>
+__global__ void __launch_bounds__(256, 4)
+k_project_xchg(float4* const* __restrict__ volTable, const int* __restrict__ cls,
+               const float4* __restrict__ vol0, int vdim, int pf, const float* __restrict__ mf,
+               int rowsPerParticle, int nGroups, int nChunks, const int* __restrict__ iCol,
+               const int* __restrict__ iRow, int K, float* __restrict__ out, int ldo,
+               const float* __restrict__ sigRcp, const float* __restrict__ ctf,
+               float* __restrict__ nrmPart, int* __restrict__ flag, long long splitLo)
+{
+    __shared__ float m[kProjG][9];
+    __shared__ float red[kProjG][8];
+    const int g = blockIdx.x % nGroups;
+    const int chunk = (blockIdx.x / nGroups) % nChunks;
+    const int l = blockIdx.x / (nGroups * nChunks);
+    const int r0 = g * kProjG;
+    const int nRot = min(kProjG, rowsPerParticle - r0);
+    const size_t row0 = (size_t)l * rowsPerParticle + r0;
+    extern __shared__ int tab[];
+    const int half = vdim / 2;
+    const int nxc = cubes_x(vdim), nyc = cubes_yz(vdim);
+    int* tx = tab;
+    int* ty = tab + vdim / 2 + 1;
+    int* tz = ty + vdim;
+    if (!kArith) fill_brick_tables(vdim, tx, ty, tz);
+    if (threadIdx.x < 9 * nRot) m[threadIdx.x / 9][threadIdx.x % 9] = mf[9 * row0 + threadIdx.x];
+    __syncthreads();
+    const int nOut = ldo / 2;
+    const int h = threadIdx.x & 1;
+    const int pBase = chunk * kProjChunk + threadIdx.x;
+    __nv_bfloat162* hiPlane = reinterpret_cast<__nv_bfloat162*>(out);
+    __nv_bfloat162* loPlane = reinterpret_cast<__nv_bfloat162*>(
+        reinterpret_cast<__nv_bfloat16*>(out) + splitLo);
+    auto store = [&](size_t row, int p, float re, float im) {
+        if (splitLo == 0) {
+            reinterpret_cast<float2*>(out + row * ldo)[p] = make_float2(re, im);
+        } else {
+            const __nv_bfloat162 v = __floats2bfloat162_rn(re, im);
+            const float2 hf = __bfloat1622float2(v);
+            hiPlane[row * nOut + p] = v;
+            loPlane[row * nOut + p] = __floats2bfloat162_rn(re - hf.x, im - hf.y);
+        }
+    };
+    const float4* __restrict__ vol = vol0;
+    if (volTable) {
+        const int k = cls ? cls[l] : 0;
+        vol = (k >= 0 && k < kMaxClasses) ? volTable[k] : nullptr;
+        if (!vol) {
+            // unknown class: record it, leave the rows' chunk zero and skip sampling
+            if (threadIdx.x == 0 && flag) atomicOr(flag, 8);
+            for (int i = 0; i < nRot; i++)
+#pragma unroll
+                for (int u = 0; u < kLaneU; u++) {
+                    const int p = pBase + u * 256;
+                    if (p < nOut) store(row0 + i, p, 0.f, 0.f);
+                }
+            if (nrmPart && threadIdx.x < nRot) nrmPart[(row0 + threadIdx.x) * nChunks + chunk] = 0.f;
+            return;
+        }
+    }
+    const float fpf = (float)pf;
+    const float* sg = sigRcp ? sigRcp + (size_t)l * K : nullptr;
+    const float* cf = ctf ? ctf + (size_t)l * K : nullptr;
+    float pa[kLaneU], pb[kLaneU], w2[kLaneU];
+#pragma unroll
+    for (int u = 0; u < kLaneU; u++) {
+        const int p = pBase + u * 256;
+        const int q = p < K ? p : 0;
+        pa[u] = (float)iCol[q] * fpf;
+        pb[u] = (float)iRow[q] * fpf;
+        w2[u] = (nrmPart && p < K) ? sg[q] * cf[q] * cf[q] : 0.f;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll 1
+    for (int i = 0; i < nRot; i++) {   // nRot is uniform across the CTA
+        const float* mm = m[i];
+        float acc = 0.f;
+        float fo[kLaneU][3], fp[kLaneU][3];   // own and partner fractions
+        bool cj[kLaneU];
+        unsigned bo[kLaneU], bp[kLaneU];      // own and partner block index
+#pragma unroll
+        for (int u = 0; u < kLaneU; u++) {
+            float x = mm[0] * pa[u] + mm[1] * pb[u];
+            float y = mm[3] * pa[u] + mm[4] * pb[u];
+            float z = mm[6] * pa[u] + mm[7] * pb[u];
+            cj[u] = x < 0.f;
+            if (cj[u]) { x = -x; y = -y; z = -z; }
+            const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+            const int x0 = (int)xf, y0 = (int)yf, z0 = (int)zf;
+            fo[u][0] = x - xf;
+            fo[u][1] = y - yf;
+            fo[u][2] = z - zf;
+            if (kArith) {
+                const int yy = y0 < 0 ? y0 + vdim : y0;
+                const int zz = z0 < 0 ? z0 + vdim : z0;
+                bo[u] = (unsigned)((((zz >> 5) * nyc + (yy >> 5)) * nxc + (x0 >> 5)) * 32768
+                                   + ((((zz >> 3) & 3) * 4 + ((yy >> 3) & 3)) * 4 + ((x0 >> 3) & 3)) * 512
+                                   + ((zz & 7) * 8 + (yy & 7)) * 8 + (x0 & 7));
+            } else {
+                bo[u] = (unsigned)(tx[x0] + ty[y0 + half] + tz[z0 + half]);
+            }
+            bp[u] = __shfl_xor_sync(0xffffffffu, bo[u], 1);
+#pragma unroll
+            for (int k = 0; k < 3; k++) fp[u][k] = __shfl_xor_sync(0xffffffffu, fo[u][k], 1);
+        }
+        // slab h of pixel A (the even lane's) then of pixel B (the odd lane's)
+        float4 c[kLaneU][4];
+#pragma unroll
+        for (int u = 0; u < kLaneU; u++)
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const unsigned b = (k == 0) == (h == 0) ? bo[u] : bp[u];
+                const float4* e = vol + 4 * (size_t)b + 2 * h;
+                asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                    : "=f"(c[u][2 * k].x), "=f"(c[u][2 * k].y), "=f"(c[u][2 * k].z),
+                      "=f"(c[u][2 * k].w), "=f"(c[u][2 * k + 1].x), "=f"(c[u][2 * k + 1].y),
+                      "=f"(c[u][2 * k + 1].z), "=f"(c[u][2 * k + 1].w)
+                    : "l"(e));
+            }
+#pragma unroll
+        for (int u = 0; u < kLaneU; u++) {
+            float sr[2], si[2];
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const bool own = (k == 0) == (h == 0);
+                const float fx = own ? fo[u][0] : fp[u][0];
+                const float fy = own ? fo[u][1] : fp[u][1];
+                const float fz = own ? fo[u][2] : fp[u][2];
+                const float wz = h ? fz : 1.f - fz;
+                const float wx0 = 1.f - fx, wx1 = fx;
+                const float wy0 = (1.f - fy) * wz, wy1 = fy * wz;
+                const float4 a = c[u][2 * k], b = c[u][2 * k + 1];
+                float re = a.x * (wx0 * wy0) + a.z * (wx1 * wy0);
+                float im = a.y * (wx0 * wy0) + a.w * (wx1 * wy0);
+                re += b.x * (wx0 * wy1) + b.z * (wx1 * wy1);
+                im += b.y * (wx0 * wy1) + b.w * (wx1 * wy1);
+                sr[k] = re;
+                si[k] = im;
+            }
+            // lane 0 keeps A (k = 0) and sends its share of B; lane 1 keeps B
+            const float keepR = h ? sr[1] : sr[0], keepI = h ? si[1] : si[0];
+            const float sendR = h ? sr[0] : sr[1], sendI = h ? si[0] : si[1];
+            float re = keepR + __shfl_xor_sync(0xffffffffu, sendR, 1);
+            float im = keepI + __shfl_xor_sync(0xffffffffu, sendI, 1);
+            const int p = pBase + u * 256;
+            if (p < nOut) {
+                if (p < K) {
+                    if (cj[u]) im = -im;
+                    store(row0 + i, p, re, im);
+                    acc = fmaf(w2[u], re * re + im * im, acc);
+                } else {
+                    store(row0 + i, p, 0.f, 0.f);
+                }
+            }
+        }
+        if (nrmPart) {
+            acc = warp_sum(acc);
+            if (lane == 0) red[i][wid] = acc;
+        }
+    }
+    if (nrmPart) {
+        __syncthreads();
+        if (threadIdx.x < nRot) {
+            float s = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[threadIdx.x][w];
+            nrmPart[(row0 + threadIdx.x) * nChunks + chunk] = s;
+        }
+    }
+}
+
 // FP32 rotation matrix of each projected row, from its quaternion
 // (quat_to_mat in FP64, then rounded) or from an FP64 matrix.
 __global__ void k_rot_f32(const double* __restrict__ quat, const double* __restrict__ mat,
@@ -1769,10 +2121,11 @@ cudaError_t launch_project(float4* const* volTable, const int* cls, const float4
                            int rows, int rowsPerParticle, const int* iCol,
                            const int* iRow, int K, float* out, int ldo,
                            const float* sigRcp, const float* ctf, float* nrm, float* scratch,
-                           int* flag, long long splitLo, cudaStream_t st)
+                           int* flag, long long splitLo, cudaStream_t st, int form)
 {
     if (rows <= 0) return cudaSuccess;
     if (!scratch || rows % rowsPerParticle) return cudaErrorInvalidValue;
+    static_assert(kProjChunk % 256 == 0, "one lane per pixel takes whole 256-pixel passes");
     const int nP = rows / rowsPerParticle;
     const int nGroups = (rowsPerParticle + kProjG - 1) / kProjG;
     const int nChunks = project_chunks(ldo);
@@ -1784,14 +2137,18 @@ cudaError_t launch_project(float4* const* volTable, const int* cls, const float4
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const size_t tabBytes = sizeof(int) * ((size_t)vdim / 2 + 1 + 2 * (size_t)vdim);
+    auto kern = form == 4   ? k_project_xchg<true>
+                : form == 3 ? k_project_xchg<false>
+                : form == 2 ? k_project_lane<true>
+                : form == 1 ? k_project_lane<false>
+                            : k_project;
     if (tabBytes > 48 * 1024) {
-        e = cudaFuncSetAttribute(k_project, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tabBytes);
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tabBytes);
         if (e != cudaSuccess) return e;
     }
-    k_project<<<(unsigned)grid, 256, tabBytes, st>>>(volTable, cls, vol, vdim, pf, mf, rowsPerParticle,
-                                               nGroups, nChunks, iCol, iRow, K, out, ldo, sigRcp,
-                                               ctf, nrm ? nrmPart : nullptr, flag, splitLo);
+    kern<<<(unsigned)grid, 256, tabBytes, st>>>(volTable, cls, vol, vdim, pf, mf, rowsPerParticle,
+                                                nGroups, nChunks, iCol, iRow, K, out, ldo, sigRcp,
+                                                ctf, nrm ? nrmPart : nullptr, flag, splitLo);
     e = cudaGetLastError();
     if (e != cudaSuccess || !nrm) return e;
     k_norm_reduce<<<grid_for((size_t)rows, 256), 256, 0, st>>>(nrmPart, rows, nChunks, nrm);

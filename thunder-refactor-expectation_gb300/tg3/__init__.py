@@ -56,6 +56,7 @@ OPT_SCAN_TILE_N = 4
 OPT_SCAN_PAIR = 5
 OPT_SCAN_BK = 6
 OPT_LOCAL_BK = 7
+OPT_PROJECT_FORM = 8
 
 
 class TG3Error(RuntimeError):
