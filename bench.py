@@ -887,6 +887,8 @@ def run_bank(args, rank, world, local_rank):
         ctx.local_phase_bank(nP, nR, nT, ps.dat, ps.ctf, ps.sigRcp, idx_d, trans, pR, pT, pC,
                              cls, o["wC"], o["wR"], o["wT"], o["base"], None, tg3.SCORE_BF16X3)
 
+    ctx.set_option(tg3.OPT_BANK_SHAPE, args.bank_shape)
+
     def timed(form, order):
         ctx.set_option(tg3.OPT_BANK_GATHER, int(form))
         ctx.set_option(tg3.OPT_BANK_ORDER, int(order))
@@ -942,7 +944,7 @@ def run_bank(args, rank, world, local_rank):
                         "tflops_algorithmic": round(4.0 * K * nP * nR * nT / (cross_ms * 1e-3)
                                                     / 1e12, 2)},
            "stages": {k: round(v[0] / max(v[1], 1), 4) for k, v in st.items() if v[1]},
-           "bank_form": {"form": main[0], "order": main[1],
+           "bank_form": {"form": main[0], "order": main[1], "shape": args.bank_shape,
                          "what": "TG3_OPT_BANK_GATHER (0: cp.async gathers in the cross term, "
                                  "1: rows copied out then the GEMM, 2: TMA gathers in the cross "
                                  "term) and TG3_OPT_BANK_ORDER (particles sorted by first "
@@ -1380,6 +1382,7 @@ def run_learned(args, rank, world, local_rank):
     noise_var = synth.signal_power(maps[:nTr], box, px, rU, rL, device=dev) / L["snr_lik"] / 2.0
     ctx = tg3.Context(local_rank)
     ctx.set_option(tg3.OPT_BANK_GATHER, args.bank_form)
+    ctx.set_option(tg3.OPT_BANK_SHAPE, args.bank_shape)
     ctx.set_option(tg3.OPT_BANK_ORDER, args.bank_order)
     ctx.set_option(tg3.OPT_SCAN_PAIR, args.scan_pair)
     ctx.set_option(tg3.OPT_SCAN_BK, args.scan_bk)
@@ -1589,6 +1592,7 @@ def run_learned(args, rank, world, local_rank):
         ab[f"form{form}_order{order}_ms_per_step"] = round(
             ((st_g["project"][0] if "project" in st_g else 0.0) + st_g["cross"][0]) / 2, 4)
     ctx.set_option(tg3.OPT_BANK_GATHER, args.bank_form)
+    ctx.set_option(tg3.OPT_BANK_SHAPE, args.bank_shape)
     ctx.set_option(tg3.OPT_BANK_ORDER, args.bank_order)
     fb = out["fellBack"].cpu().numpy().astype(bool)
     q_l = out["bestQuat"].cpu().numpy()
@@ -2371,6 +2375,9 @@ def main():
                          "share each column tile by TMA multicast")
     ap.add_argument("--local-bk", type=int, default=64, choices=[32, 64],
                     help="TG3_OPT_LOCAL_BK: K block of the local phase's split cross term")
+    ap.add_argument("--bank-shape", type=int, default=0, choices=[0, 1, 2],
+                    help="TG3_OPT_BANK_SHAPE: the cp.async bank cross term's K block and "
+                         "CTAs per SM (0: 64, one; 1: 32, twice the stages; 2: 32, two)")
     ap.add_argument("--project-form", type=int, default=4, choices=[0, 1, 2, 3, 4],
                     help="TG3_OPT_PROJECT_FORM: 0 a lane pair per pixel, 1 one lane per pixel, "
                          "2 one lane per pixel with the block index computed, 3/4 lane pairs "

@@ -356,7 +356,12 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  *   joined by a shuffle), 1 with one lane per pixel, 2 with one lane per
  *   pixel and the block index computed instead of looked up, 3 and 4 with
  *   every lane finding its own pixel's block and a lane pair loading both
- *   pixels' blocks together (index looked up, computed).  Same samples. */
+ *   pixels' blocks together (index looked up, computed).  Same samples.
+ * TG3_OPT_BANK_SHAPE (default 0): the pipeline of the bank-row cross term's
+ *   cp.async form (TG3_OPT_BANK_GATHER 0): 0 K blocks of 64 bf16 (128-byte
+ *   rows) and one CTA an SM, 1 K blocks of 32 (64-byte rows) with twice the
+ *   stages, 2 K blocks of 32 with two CTAs an SM.  Same products in the
+ *   same order. */
 enum {
     TG3_OPT_FUSED = 0,
     TG3_OPT_INSERT_GATHER = 1,
@@ -366,7 +371,8 @@ enum {
     TG3_OPT_SCAN_PAIR = 5,
     TG3_OPT_SCAN_BK = 6,
     TG3_OPT_LOCAL_BK = 7,
-    TG3_OPT_PROJECT_FORM = 8
+    TG3_OPT_PROJECT_FORM = 8,
+    TG3_OPT_BANK_SHAPE = 9
 };
 int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);

@@ -268,3 +268,38 @@ def test_reference_rendering_matches_the_torch_form():
         assert (got - want).abs().max().item() < 1e-4
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("shape", [1, 2])
+@pytest.mark.parametrize("nR", [32, 160])
+def test_bank_pipeline_shapes(case, nR, shape):
+    """The cp.async bank-row cross term with K blocks of 32 bf16 (64-byte
+    swizzled rows): twice the stages (TG3_OPT_BANK_SHAPE 1) or two CTAs an SM
+    (2), against the default K blocks of 64: the same MMAs in the same order
+    and the norms summed over other lane partitions, so log-likelihoods
+    within 1e-6 relative and the same best hypothesis."""
+    ps, ctx, n = case["ps"], case["ctx"], len(case["ps"].cls)
+    nT = 9
+    rng = np.random.default_rng(nR + 7)
+    idx = torch.as_tensor(rng.integers(0, len(case["qg"]), (n, nR)).astype(np.int32), device=DEV)
+    trans = torch.as_tensor(rng.uniform(-2, 2, (n, nT, 2)), **F64)
+
+    def run(sh):
+        ctx.set_option(tg3.OPT_BANK_SHAPE, sh)
+        dvp = torch.empty((n, nR, nT), dtype=torch.float32, device=DEV)
+        o = [torch.empty(n, **F64), torch.empty((n, nR), **F64), torch.empty((n, nT), **F64),
+             torch.empty(n, **F64)]
+        ctx.local_phase_bank(n, nR, nT, ps.dat, ps.ctf, ps.sigRcp, idx, trans,
+                             torch.full((n, nR), 1.0 / nR, **F64),
+                             torch.full((n, nT), 1.0 / nT, **F64), torch.ones(n, **F64),
+                             case["cls"], *o, dvp, tg3.SCORE_BF16X3)
+        ctx.sync()
+        return dvp.cpu().numpy().astype(np.float64)
+
+    try:
+        a, b = run(shape), run(0)
+    finally:
+        ctx.set_option(tg3.OPT_BANK_SHAPE, 0)
+    assert np.max(np.abs(a - b) / np.abs(b)) < 1e-6
+    for l in range(n):
+        assert np.argmax(a[l]) == np.argmax(b[l])

@@ -574,7 +574,7 @@ static int local_phase(tg3_ctx* c, const int* bankIdx, int nP, int nR, int nT, c
             }
             TG3_CUDA(launch_gemm_bank_bf16x3(c->bank, c->px.gen, bankIdx, cls, nP, nR, A, nT, Kp,
                                              K, sigRcp, ctf, D, -2.0f, c->d_flag, s,
-                                             c->bankGather == 2, order));
+                                             c->bankGather == 2, order, c->bankShape));
         }
         {
             StageTimer tm(c, TG3_STAGE_WEIGHTS);
@@ -1811,6 +1811,10 @@ extern "C" int tg3_ctx_set_option(tg3_ctx* c, int option, int value)
     else if (option == TG3_OPT_LOCAL_BK) {
         if (value != 32 && value != 64) return fail(TG3_ERR_ARG, "TG3_OPT_LOCAL_BK takes 32 or 64");
         c->localBK = value;
+    }
+    else if (option == TG3_OPT_BANK_SHAPE) {
+        if (value < 0 || value > 2) return fail(TG3_ERR_ARG, "TG3_OPT_BANK_SHAPE takes 0, 1 or 2");
+        c->bankShape = value;
     }
     else if (option == TG3_OPT_PROJECT_FORM) {
         if (value < 0 || value > 4) return fail(TG3_ERR_ARG, "TG3_OPT_PROJECT_FORM takes 0 to 4");

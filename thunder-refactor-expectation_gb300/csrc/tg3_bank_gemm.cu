@@ -338,20 +338,43 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src)
 
 // Eight gather warps (0 - 7), then the B-tile TMA warp (8) and the MMA warp
 // (9, which also holds the tensor memory); warps 0 - 3 run the epilogue.
+//
+// BK is the K block: 64 bf16 (128-byte rows, 128-byte swizzle) or 32
+// (64-byte rows, 64-byte swizzle: half the bytes a stage, so more stages, or
+// two CTAs an SM with MINB = 2).  A row's chunk of a K block is BK / 8
+// 16-byte pieces, one per lane of a row group; a thread copies CP_RPT rows.
 constexpr int CP_PW = 8;
 constexpr int CP_THREADS = (CP_PW + 2) * 32;
-constexpr int CP_RPT = BG_M * 8 / (CP_PW * 32);   // rows per gather thread (4)
 
-template <int S>
-__global__ void __launch_bounds__(CP_THREADS, 1)
+template <int BK>
+__device__ __forceinline__ uint64_t bank_desc(uint32_t saddr)
+{
+    return BK == 64 ? umma_desc(saddr) : umma_desc_sw64(saddr);
+}
+
+// Byte offset of 16-byte chunk q of row r of an A plane: 128-byte rows with
+// the 128-byte swizzle (chunk XOR row mod 8) or 64-byte rows with the
+// 64-byte swizzle (8-row groups of 512 bytes, chunk XOR (row / 2) mod 4).
+template <int BK>
+__device__ __forceinline__ int bank_phys(int r, int q)
+{
+    return BK == 64 ? r * 128 + ((q ^ (r & 7)) << 4)
+                    : (r >> 3) * 512 + (r & 7) * 64 + ((q ^ ((r >> 1) & 3)) << 4);
+}
+
+template <int S, int BK, int MINB>
+__global__ void __launch_bounds__(CP_THREADS, MINB)
 k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                const __grid_constant__ CUtensorMap tmBl, const BgParams p)
 {
+    constexpr int QPR = BK / 8;                          // 16-byte chunks per row
+    constexpr int CP_RPT = BG_M * QPR / (CP_PW * 32);     // rows per gather thread
+    constexpr int RSTRIDE = CP_PW * 32 / QPR;             // rows between a thread's rows
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    const int aBytes = BG_M * BG_BK * 2;
-    const int bBytes = p.ntile * BG_BK * 2;
+    const int aBytes = BG_M * BK * 2;
+    const int bBytes = p.ntile * BK * 2;
     const int stageBytes = 2 * aBytes + 2 * bBytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * stageBytes);
     uint64_t* empty = full + S;
@@ -367,7 +390,7 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
     const bool clOk = cl >= 0 && cl < kMaxClasses && banks.nB[cl] > 0;
     const int k = clOk ? cl : 0;
     const int nB = clOk ? banks.nB[k] : 0;
-    const int nkb = p.Kd / BG_BK;
+    const int nkb = p.Kd / BK;
     const int bRow0 = item * p.nT;
 
     if (threadIdx.x < BG_M) {
@@ -407,7 +430,7 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
     if (warp < CP_PW) {
         // ---------------- A tiles and the rows' norms
         const int t = threadIdx.x;
-        const int g = t >> 3, q = t & 7;                   // row group, 16-byte chunk
+        const int g = t / QPR, q = t % QPR;                // row group, 16-byte chunk
         const __nv_bfloat16* bh = banks.hi[k];
         const __nv_bfloat16* bl = banks.lo[k];
         const __nv_bfloat16* srcH[CP_RPT];
@@ -415,11 +438,11 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
         int phys[CP_RPT];
 #pragma unroll
         for (int i = 0; i < CP_RPT; i++) {
-            const int r = g + (CP_PW * 4) * i;
+            const int r = g + RSTRIDE * i;
             const size_t off = (size_t)rows[r] * p.Kd + q * 8;
             srcH[i] = bh + off;
             srcL[i] = bl + off;
-            phys[i] = r * 128 + ((q ^ (r & 7)) << 4);
+            phys[i] = bank_phys<BK>(r, q);
         }
         const float* sg = p.sigRcp + (size_t)item * p.K;
         const float* cf = p.ctf + (size_t)item * p.K;
@@ -428,7 +451,7 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
         for (int i = 0; i < CP_RPT; i++) nS[i] = nC[i] = 0.f;
         // the weights sigRcp ctf^2 of this lane's 4 pixels, one K block ahead
         auto weights = [&](int kd, float* w) {
-            const int px0 = kd * (BG_BK / 2) + q * 4;
+            const int px0 = kd * (BK / 2) + q * 4;
 #pragma unroll
             for (int c = 0; c < 4; c++) {
                 const int px = px0 + c;
@@ -455,7 +478,7 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                     }
                 }
                 uint8_t* st = smem + s * stageBytes;
-                const size_t o = (size_t)kb * BG_BK;
+                const size_t o = (size_t)kb * BK;
 #pragma unroll
                 for (int i = 0; i < CP_RPT; i++) {
                     cp_async16(st + phys[i], srcH[i] + o);
@@ -496,14 +519,13 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
         }
         // copies still in flight after an abort land before the CTA leaves
         asm volatile("cp.async.wait_all;" ::: "memory");
-        // the rows' norms: the 8 lanes of a row group hold partials
+        // the rows' norms: the QPR lanes of a row group hold partials
 #pragma unroll
         for (int i = 0; i < CP_RPT; i++) {
             float v = nS[i] - nC[i];
-            v += __shfl_xor_sync(0xffffffffu, v, 1);
-            v += __shfl_xor_sync(0xffffffffu, v, 2);
-            v += __shfl_xor_sync(0xffffffffu, v, 4);
-            if (q == 0) nrmRow[g + (CP_PW * 4) * i] = v;
+#pragma unroll
+            for (int o = 1; o < QPR; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (q == 0) nrmRow[g + RSTRIDE * i] = v;
         }
     } else if (warp == CP_PW) {
         // ---------------- B tiles (TMA)
@@ -519,8 +541,8 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                 if (*(volatile int*)abortFlag) break;
                 uint8_t* st = smem + s * stageBytes;
                 mbar_expect_tx(full + s, 2 * bBytes);
-                tma_load_2d(st + 2 * aBytes, &tmBh, full + s, kb * BG_BK, bRow0);
-                tma_load_2d(st + 2 * aBytes + bBytes, &tmBl, full + s, kb * BG_BK, bRow0);
+                tma_load_2d(st + 2 * aBytes, &tmBh, full + s, kb * BK, bRow0);
+                tma_load_2d(st + 2 * aBytes + bBytes, &tmBl, full + s, kb * BK, bRow0);
                 issuedTma = kb + 1;
             }
         }
@@ -543,12 +565,12 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                 const uint32_t bh = smem_u32(st + 2 * aBytes),
                                bl = smem_u32(st + 2 * aBytes + bBytes);
 #pragma unroll
-                for (int kk = 0; kk < BG_BK / 16; kk++) {
+                for (int kk = 0; kk < BK / 16; kk++) {
                     const uint32_t off = kk * 32;
-                    umma_bf16(tmem, umma_desc(ah + off), umma_desc(bh + off), idesc,
+                    umma_bf16(tmem, bank_desc<BK>(ah + off), bank_desc<BK>(bh + off), idesc,
                               (kb | kk) != 0);
-                    umma_bf16(tmem, umma_desc(ah + off), umma_desc(bl + off), idesc, 1);
-                    umma_bf16(tmem, umma_desc(al + off), umma_desc(bh + off), idesc, 1);
+                    umma_bf16(tmem, bank_desc<BK>(ah + off), bank_desc<BK>(bl + off), idesc, 1);
+                    umma_bf16(tmem, bank_desc<BK>(al + off), bank_desc<BK>(bh + off), idesc, 1);
                 }
                 umma_commit(empty + s);
                 issuedMma = kb + 1;
@@ -648,8 +670,9 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
                                     const int* cls, int nP, int nR, const void* B, int nT,
                                     int Kd, int K, const float* sigRcp, const float* ctf,
                                     float* C, float alpha, int* flag, cudaStream_t st,
-                                    bool tmaGather, int* order)
+                                    bool tmaGather, int* order, int shape)
 {
+    if (shape < 0 || shape > 2) return cudaErrorInvalidValue;
     if (nP <= 0 || nR <= 0 || nT <= 0 || nT > 256 || Kd <= 0 || Kd % BG_BK || nP > 65535)
         return cudaErrorInvalidValue;
     BankMaps maps;
@@ -731,20 +754,41 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
         rowsOf.lo[k] = b.hi + (size_t)b.nB * b.Kp;
         rowsOf.nB[k] = maps.nB[k];
     }
-    // the cp.async form keeps every stage in flight: as many as fit (<= 5)
-    int S = (int)((227 * 1024 - 1024 - 256 - 2 * sizeof(int) * BG_M) / stageBytes);
-    if (S > 5) S = 5;
-    if (S < 2 || (size_t)BG_M * (p.ntile + 1) * 4 > (size_t)S * stageBytes)
+    // the cp.async form keeps every stage in flight: as many as fit in one
+    // CTA's (shape 0: K blocks of 64, <= 5 stages; shape 1: of 32, <= 9) or
+    // in half an SM's shared memory (shape 2: K blocks of 32, two CTAs an SM)
+    using KernFn = void (*)(const LdgRows, const CUtensorMap, const CUtensorMap, const BgParams);
+    const int bk = shape == 0 ? 64 : 32;
+    const int stageCp = 2 * BG_M * bk * 2 + 2 * p.ntile * bk * 2;
+    const size_t fixed = 1024 + 256 + 2 * sizeof(int) * BG_M;
+    const size_t budget = shape == 2 ? 113 * 1024 : 227 * 1024;
+    int S = (int)((budget - fixed) / stageCp);
+    const int maxS = shape == 0 ? 5 : shape == 1 ? 9 : 4;
+    if (S > maxS) S = maxS;
+    if (S < 2 || (size_t)BG_M * (p.ntile + 1) * 4 > (size_t)S * stageCp)
         return cudaErrorInvalidValue;
+    KernFn kern = nullptr;
+    if (shape == 0)
+        kern = S == 5 ? k_gemm_bank_cp<5, 64, 1> : S == 4 ? k_gemm_bank_cp<4, 64, 1>
+             : S == 3 ? k_gemm_bank_cp<3, 64, 1> : k_gemm_bank_cp<2, 64, 1>;
+    else if (shape == 1) {
+        S = S >= 9 ? 9 : S >= 8 ? 8 : S >= 6 ? 6 : S >= 4 ? 4 : 2;   // the instantiated depths
+        kern = S == 9 ? k_gemm_bank_cp<9, 32, 1> : S == 8 ? k_gemm_bank_cp<8, 32, 1>
+             : S == 6 ? k_gemm_bank_cp<6, 32, 1> : S == 4 ? k_gemm_bank_cp<4, 32, 1>
+                                                : k_gemm_bank_cp<2, 32, 1>;
+    } else
+        kern = S == 4 ? k_gemm_bank_cp<4, 32, 2> : S == 3 ? k_gemm_bank_cp<3, 32, 2>
+                                                         : k_gemm_bank_cp<2, 32, 2>;
     p.stages = S;
-    const size_t smemCp = 1024 + (size_t)S * stageBytes + 256 + 2 * sizeof(int) * BG_M;
-    void (*kern)(const LdgRows, const CUtensorMap, const CUtensorMap, const BgParams) =
-        S == 5 ? k_gemm_bank_cp<5> : S == 4 ? k_gemm_bank_cp<4> : S == 3 ? k_gemm_bank_cp<3>
-                                                                         : k_gemm_bank_cp<2>;
+    CUtensorMap cBh = mBh, cBl = mBl;
+    if (bk == 32 && (!tc::make_map(&cBh, Bh, (long long)nP * nT, Kd, p.ntile, 32, true) ||
+                     !tc::make_map(&cBl, Bl, (long long)nP * nT, Kd, p.ntile, 32, true)))
+        return cudaErrorInvalidValue;
+    const size_t smemCp = fixed + (size_t)S * stageCp;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smemCp);
     if (e != cudaSuccess) return e;
-    kern<<<grid, CP_THREADS, smemCp, st>>>(rowsOf, mBh, mBl, p);
+    kern<<<grid, CP_THREADS, smemCp, st>>>(rowsOf, cBh, cBl, p);
     return cudaGetLastError();
 }
 

@@ -57,6 +57,7 @@ OPT_SCAN_PAIR = 5
 OPT_SCAN_BK = 6
 OPT_LOCAL_BK = 7
 OPT_PROJECT_FORM = 8
+OPT_BANK_SHAPE = 9
 
 
 class TG3Error(RuntimeError):
