@@ -320,6 +320,11 @@ extern "C" int tg3_ctx_destroy(tg3_ctx* c)
         cudaFree(b.quat);
         cudaFree(b.emb);
     }
+    if (c->copyStream) {
+        cudaStreamSynchronize(c->copyStream);
+        cudaStreamDestroy(c->copyStream);
+    }
+    if (c->copyDone) cudaEventDestroy(c->copyDone);
     cudaFree(c->d_bankTable);
     cudaFree(c->d_refTable);
     cudaFree(c->d_flag);

@@ -177,6 +177,10 @@ struct InsertAcc {
 struct tg3_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // host-buffer entries: a second stream for input copies that overlap the
+    // first stages, and the event the compute stream waits on (made on first use)
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t copyDone = nullptr;
     tg3::Volume vol[tg3::kMaxClasses];
     float4** d_volTable = nullptr;   // device copy of the class -> blocks table
     tg3::Pixels px;                          // the active pixel set (a view)

@@ -244,11 +244,30 @@ extern "C" int tg3_ctx_set_references(tg3_ctx* c, int cls, const float* emb, int
     return TG3_OK;
 }
 
+// The learned E-step; with dataReady, the compute stream waits for that
+// event before the first kernel that reads dat, ctf or sigRcp (the
+// host-buffer entry copies them on its copy stream meanwhile).
+static int learned_expect(tg3_ctx* c, tg3_cnn* net, int nP, const float* images,
+                          const float* dat, const float* ctf, const float* sigRcp,
+                          const int* cls, int nRot, int nTrans, unsigned long long seed,
+                          const double* gTrans, int nTg, float peakMin, int precision,
+                          const tg3_learned_out* out, cudaEvent_t dataReady);
+
 extern "C" int tg3_learned_expect_d(tg3_ctx* c, tg3_cnn* net, int nP, const float* images,
                                     const float* dat, const float* ctf, const float* sigRcp,
                                     const int* cls, int nRot, int nTrans,
                                     unsigned long long seed, const double* gTrans, int nTg,
                                     float peakMin, int precision, const tg3_learned_out* out)
+{
+    return learned_expect(c, net, nP, images, dat, ctf, sigRcp, cls, nRot, nTrans, seed, gTrans,
+                          nTg, peakMin, precision, out, nullptr);
+}
+
+static int learned_expect(tg3_ctx* c, tg3_cnn* net, int nP, const float* images,
+                          const float* dat, const float* ctf, const float* sigRcp,
+                          const int* cls, int nRot, int nTrans, unsigned long long seed,
+                          const double* gTrans, int nTg, float peakMin, int precision,
+                          const tg3_learned_out* out, cudaEvent_t dataReady)
 {
     int st = check_ctx(c);
     if (st) return st;
@@ -345,6 +364,7 @@ extern "C" int tg3_learned_expect_d(tg3_ctx* c, tg3_cnn* net, int nP, const floa
                                                                   1.0 / nTrans);
     k_fill_f64<<<grid_for(nP, 256), 256, 0, s>>>(pwC, nP, 1.0);
     TG3_LAUNCH_CHECK("uniform priors");
+    if (dataReady) TG3_CUDA(cudaStreamWaitEvent(s, dataReady, 0));
     // ---- 3: exact rescoring from the banks
     if ((st = tg3_local_phase_bank_d(c, nP, nRot, nTrans, dat, ctf, sigRcp, idx, trans, pwR, pwT,
                                      pwC, cls, wC, wR, wT, base, dvp, precision)))
@@ -456,26 +476,40 @@ extern "C" int tg3_ExpectLearned3D(tg3_ctx* c, tg3_cnn* net, int nP, const float
                  oF = ar.add(sizeof(int) * nP);
     char* w = (char*)ws_get(c, WS_LEARN_IO, ar.used, &st);
     if (!w) return st;
-    const auto h2d = [&](size_t off, const void* src, size_t bytes) {
-        return cudaMemcpyAsync(w + off, src, bytes, cudaMemcpyHostToDevice, s);
+    const auto h2d = [&](size_t off, const void* src, size_t bytes, cudaStream_t on) {
+        return cudaMemcpyAsync(w + off, src, bytes, cudaMemcpyHostToDevice, on);
     };
-    TG3_CUDA(h2d(oIm, images, sizeof(float) * 64 * 64 * (size_t)nP));
-    TG3_CUDA(h2d(oD, dat, sizeof(float) * 2 * (size_t)nP * K));
-    TG3_CUDA(h2d(oC, ctf, sizeof(float) * (size_t)nP * K));
-    TG3_CUDA(h2d(oS, sigRcp, sizeof(float) * (size_t)nP * K));
-    TG3_CUDA(h2d(oK, cls, sizeof(int) * nP));
-    TG3_CUDA(h2d(oG, gTrans, sizeof(double) * 2 * (size_t)nTg));
+    // the images, classes and translations on the compute stream (the
+    // network needs them first); the data, CTFs and weights, nine tenths of
+    // the bytes, on the copy stream while the network and the matching run
+    if (!c->copyStream) TG3_CUDA(cudaStreamCreateWithFlags(&c->copyStream, cudaStreamNonBlocking));
+    if (!c->copyDone) TG3_CUDA(cudaEventCreateWithFlags(&c->copyDone, cudaEventDisableTiming));
+    TG3_CUDA(h2d(oIm, images, sizeof(float) * 64 * 64 * (size_t)nP, s));
+    TG3_CUDA(h2d(oK, cls, sizeof(int) * nP, s));
+    TG3_CUDA(h2d(oG, gTrans, sizeof(double) * 2 * (size_t)nTg, s));
+    // the copy stream does not overwrite the arena before the compute
+    // stream's earlier work on it is done
+    TG3_CUDA(cudaEventRecord(c->copyDone, s));
+    TG3_CUDA(cudaStreamWaitEvent(c->copyStream, c->copyDone, 0));
+    TG3_CUDA(h2d(oD, dat, sizeof(float) * 2 * (size_t)nP * K, c->copyStream));
+    TG3_CUDA(h2d(oC, ctf, sizeof(float) * (size_t)nP * K, c->copyStream));
+    TG3_CUDA(h2d(oS, sigRcp, sizeof(float) * (size_t)nP * K, c->copyStream));
+    TG3_CUDA(cudaEventRecord(c->copyDone, c->copyStream));
     tg3_learned_out o = {};
     o.bestQuat = (double*)(w + oQ);
     o.bestTrans = (double*)(w + oT);
     o.baseL = (double*)(w + oB);
     o.peak = (float*)(w + oP);
     o.fellBack = (int*)(w + oF);
-    st = tg3_learned_expect_d(c, net, nP, (const float*)(w + oIm), (const float*)(w + oD),
-                              (const float*)(w + oC), (const float*)(w + oS),
-                              (const int*)(w + oK), nRot, nTrans, seed, (const double*)(w + oG),
-                              nTg, peakMin, precision, &o);
-    if (st) return st;
+    st = learned_expect(c, net, nP, (const float*)(w + oIm), (const float*)(w + oD),
+                        (const float*)(w + oC), (const float*)(w + oS), (const int*)(w + oK), nRot,
+                        nTrans, seed, (const double*)(w + oG), nTg, peakMin, precision, &o,
+                        c->copyDone);
+    if (st) {
+        // the copies may still be landing in the arena: let them finish
+        cudaStreamSynchronize(c->copyStream);
+        return st;
+    }
     TG3_CUDA(cudaMemcpyAsync(bestQuat, o.bestQuat, sizeof(double) * 4 * nP,
                              cudaMemcpyDeviceToHost, s));
     TG3_CUDA(cudaMemcpyAsync(bestTrans, o.bestTrans, sizeof(double) * 2 * nP,
