@@ -137,6 +137,8 @@ def ref():
         R.ref_reconstruct.argtypes = [_c, _c, _c, _d, _d, _c, _c128p, _f64p, _f64p, _c,
                                       _c, _c, _c, _f64p]
         R.ref_reconstruct.restype = _c
+        R.ref_fw_image.argtypes = [_f64p, _c, _c128p]
+        R.ref_remask.argtypes = [_c128p, _c, _d, _d]
         _ref = R
     return _ref
 
@@ -363,3 +365,28 @@ def ref_reconstruct(F, T, pf, max_radius, fsc, join_half=False, grid_corr=True, 
     if rc != 0:
         raise ValueError("reference reconstruct: accumulator size mismatch")
     return out
+
+
+def ref_fw_image(img):
+    """FFT::fw of one N x N image in the Image's storage order (centre at
+    index 0) through the compiled reference and its FFTW (None if
+    unavailable) -> the half transform (N, N/2 + 1)."""
+    R = ref()
+    if R is None:
+        return None
+    img = _a(img, np.float64)
+    N = img.shape[0]
+    out = np.zeros((N, N // 2 + 1), np.complex128)
+    R.ref_fw_image(img.reshape(-1), N, out)
+    return out
+
+
+def ref_remask(F, r, ew=6.0):
+    """Optimiser::reMaskImg of one half transform F (N, N/2 + 1) through the
+    compiled reference (None if unavailable)."""
+    R = ref()
+    if R is None:
+        return None
+    F = np.array(F, dtype=np.complex128, order="C")
+    R.ref_remask(F, F.shape[0], float(r), float(ew))
+    return F

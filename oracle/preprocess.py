@@ -1,8 +1,11 @@
 """Oracle (test infrastructure only): the reference's image preprocessing in
 numpy, float64 -- the checker for tg3_prepare_images_d, never on the product
 path.  Pinned against the compiled reference's bgMeanStddev / bgStddev /
-softMask and ImageFile reader (tests/test_oracle_pin.py); the transform is
-FFTW's unnormalised forward r2c (src/FFT.cpp:118-140), here numpy's rfft2.
+softMask and ImageFile reader, and, through the reference's FFT class on the
+vendored FFTW, the whole chain with its transform and the re-mask
+(tests/test_formats_cpu.py live, tests/test_oracle_golden.py on fixtures).
+The transform is FFTW's unnormalised forward r2c (src/FFT.cpp:118-140),
+here numpy's rfft2.
 
 Steps (src/Optimiser.cpp): substractBgImg :4917 (background outside radius r
 about the file's pixel (N/2, N/2): mean and n - 1 deviation, subtracted and

@@ -195,6 +195,45 @@ void ref_prep_image(const double* in, int N, double r, int mask, double* out, do
     for (size_t i = 0; i < img.sizeRL(); i++) out[i] = img(i);
 }
 
+/* FFT::fw(Image&, nThread), src/FFT.cpp:118-140, through the vendored FFTW:
+ * the unnormalised r2c transform of an N x N image given in the Image's own
+ * storage order (its centre at index 0, as Optimiser::fwImg transforms it,
+ * src/Optimiser.cpp:5003-5013); out: the half transform [N][N/2 + 1]. */
+void ref_fw_image(const double* in, int N, double* out)
+{
+    Image img(N, N, RL_SPACE);
+    for (size_t i = 0; i < img.sizeRL(); i++) img(i) = in[i];
+    FFT fft;
+    fft.fw(img, 1);
+    for (size_t i = 0; i < img.sizeFT(); i++) {
+        out[2 * i] = img[i].dat[0];
+        out[2 * i + 1] = img[i].dat[1];
+    }
+}
+
+/* Optimiser::reMaskImg, src/Optimiser.cpp:6053-6111: the mask
+ * softMask(mask, r, ew) (src/Functions/Mask.cpp:333-350), then for the
+ * image FFT::bw (normalised), MUL_RL by the mask and FFT::fw.  ft: the half
+ * transform [N][N/2 + 1] complex, in place. */
+void ref_remask(double* ft, int N, double r, double ew)
+{
+    Image img(N, N, FT_SPACE);
+    for (size_t i = 0; i < img.sizeFT(); i++) {
+        img[i].dat[0] = ft[2 * i];
+        img[i].dat[1] = ft[2 * i + 1];
+    }
+    Image mask(N, N, RL_SPACE);
+    softMask(mask, (RFLOAT)r, (RFLOAT)ew, 1u);
+    FFT fft;
+    fft.bw(img, 1);
+    MUL_RL(img, mask);
+    fft.fw(img, 1);
+    for (size_t i = 0; i < img.sizeFT(); i++) {
+        ft[2 * i] = img[i].dat[0];
+        ft[2 * i + 1] = img[i].dat[1];
+    }
+}
+
 /* powerSpectrum(vec&, const Image&, r, nThread), src/Functions/Spectrum.cpp:
  * 161-190, of a half transform ft [N][N/2 + 1] complex; out [r]. */
 void ref_power_spectrum(const double* ft, int N, int r, double* out)

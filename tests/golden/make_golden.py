@@ -3,7 +3,7 @@ own compiled routines (oracle/_ref/libthunder_ref.so, built by
 oracle/ref/Makefile from the THUNDER sources) on small seeded cases.
 
 Also writes tests/golden/ref_golden_formats.npz (the 2-D, preprocessing,
-spectrum and MRC routines) and tests/golden/ref_golden_recon.npz (the
+transform, re-mask, spectrum and MRC routines) and tests/golden/ref_golden_recon.npz (the
 symmetrisation of half transforms and the reconstruction chain).  Run in a checkout that has the THUNDER tree:
     python tests/golden/make_golden.py
 The fixture pins the oracle (tests/test_oracle_golden.py) on machines that
@@ -240,6 +240,15 @@ def main_formats():
                 raise SystemExit("reference MRC read failed")
             reads.append(o.reshape(12, 12))
     g["mrc_stack"], g["mrc_ref"] = stack, np.stack(reads)
+    # the preprocessing's transform (FFT::fw of an image held with its centre
+    # at index 0) and the re-mask (reMaskImg: FFT::bw, soft mask, FFT::fw),
+    # through the reference's FFT class on the vendored FFTW
+    rng2 = np.random.default_rng(20261206)
+    img = rng2.standard_normal((32, 32))
+    g["fw_img"], g["fw_ref"] = img, O.ref_fw_image(img)
+    Fm = np.fft.rfft2(rng2.standard_normal((32, 32)))
+    g["remask_F"], g["remask_r"] = Fm, 9.5
+    g["remask_ref"] = O.ref_remask(Fm, 9.5)
     out = Path(__file__).resolve().parent / "ref_golden_formats.npz"
     np.savez_compressed(out, **g)
     print(f"wrote {out} ({out.stat().st_size} bytes)")

@@ -1,7 +1,8 @@
 """Input formats and preprocessing on the CPU.
 - The library's MRC reader against the reference's compiled ImageFile.
 - The oracle's preprocessing against the reference's compiled bgMeanStddev,
-  bgStddev and softMask.
+  bgStddev and softMask, and with the transform and the re-mask through the
+  reference's FFT class on the vendored FFTW.
 - .thu databases: saveDatabase-formatted lines, round trips and malformed
   input."""
 import numpy as np
@@ -97,6 +98,39 @@ def test_preprocessing_oracle_matches_reference(mask):
         R.ref_prep_image(np.ascontiguousarray(io.centred(img)).ravel(), N, r, mask, out, sref)
         np.testing.assert_allclose(io.centred(y).ravel(), out, rtol=0, atol=1e-12)
         np.testing.assert_allclose(st, sref, rtol=1e-13)
+
+
+@needs_ref
+@pytest.mark.parametrize("mask", [0, 1])
+def test_preprocessing_chain_matches_reference(mask):
+    """The oracle's whole preprocessing of an image -- normalisation, zero
+    soft mask, the transform of the image held with its centre at index 0 and
+    the pixel gather -- against the reference's own chain: bgMeanStddev /
+    softMask (ref_prep_image), then FFT::fw through the vendored FFTW
+    (ref_fw_image), gathered at (iCol, iRow mod N)."""
+    rng = np.random.default_rng(21 + mask)
+    N, r = 48, 17.3
+    img = _images(rng, 1, N)
+    iCol = rng.integers(0, N // 2 + 1, 300)
+    iRow = rng.integers(-N // 2, N // 2, 300)
+    dat, _, _ = PP.preprocess(img, r, iCol, iRow, mask=bool(mask), std_n=1.0)
+    out = np.zeros(N * N)
+    R.ref_prep_image(np.ascontiguousarray(io.centred(img[0])).ravel(), N, r, mask, out, np.zeros(3))
+    F = O.ref_fw_image(out.reshape(N, N))
+    ref = F[iRow % N, iCol]
+    assert np.abs(dat[0] - ref).max() < 1e-12 * np.abs(ref).max()
+
+
+@needs_ref
+def test_remask_matches_reference():
+    """oracle/preprocess.py remask against Optimiser::reMaskImg compiled
+    (FFT::bw, the softMask mask image, MUL_RL, FFT::fw on the vendored FFTW)."""
+    rng = np.random.default_rng(31)
+    for N, r in ((32, 9.5), (64, 21.0)):
+        F = np.fft.rfft2(rng.standard_normal((N, N)))
+        ref = O.ref_remask(F, r)
+        got = PP.remask(F[None], r)[0]
+        assert np.abs(got - ref).max() < 1e-12 * np.abs(ref).max()
 
 
 def test_preprocessed_pixels_are_the_image_transform():

@@ -171,3 +171,17 @@ def test_reconstruct_matches_reference_fixture(dim):
         out, _ = RC.reconstruct(g[f"reco{dim}_F"], g[f"reco{dim}_T"], pf, maxR,
                                 fsc=g[f"reco{dim}_fsc"], join_half=bool(join), grid_corr=bool(gc))
         assert np.abs(out - ref).max() < 1e-12 * np.abs(ref).max()
+
+
+def test_transform_and_remask_match_reference_fixture():
+    """The preprocessing's transform (numpy's rfft2 of the image held with its
+    centre at index 0) and oracle/preprocess.py remask against the reference's
+    FFT::fw and reMaskImg on the vendored FFTW, recorded in
+    tests/golden/ref_golden_formats.npz."""
+    from pathlib import Path
+    from oracle import preprocess as PP
+    g = np.load(Path(__file__).resolve().parent / "golden" / "ref_golden_formats.npz")
+    F = np.fft.rfft2(g["fw_img"])
+    assert np.abs(F - g["fw_ref"]).max() < 1e-12 * np.abs(g["fw_ref"]).max()
+    got = PP.remask(g["remask_F"][None], float(g["remask_r"]))[0]
+    assert np.abs(got - g["remask_ref"]).max() < 1e-12 * np.abs(g["remask_ref"]).max()
