@@ -195,6 +195,7 @@ def run_tg3(args, rank, world, local_rank):
     ctx = tg3.Context(local_rank)
     ctx.set_option(tg3.OPT_LOCAL_BK, args.local_bk)
     ctx.set_option(tg3.OPT_PROJECT_FORM, args.project_form)
+    ctx.set_option(tg3.OPT_PROJECT_GROUP, args.project_group)
     if args.fused:
         ctx.set_option(tg3.OPT_FUSED, 1)
     for c, v in enumerate(vols):
@@ -417,6 +418,7 @@ def run_tg3(args, rank, world, local_rank):
                    "box": W["box"], "pf": W["pf"], "K": K, "nR": nR, "nT": nT,
                    "classes": W["n_classes"], "particles_per_step": nP,
                    "precision": args.precision, "projection_form": args.project_form,
+                   "projection_group": args.project_group,
                    "l2": "inputs larger than L2: the projection bank alone is "
                          f"{nP * nR * ctx_kp(K) * 4 / 1e9:.1f} GB per step"},
         "clocks": clocks,
@@ -1195,6 +1197,7 @@ def run_uneven(args, rank, world, local_rank):
     plan_s = time.perf_counter() - t0
     waves, budget = plan.info()
     kblock = plan.kblock()
+    pgroup = plan.project_group()
     for _ in range(args.warmup):
         plan.run()
     ctx.sync()
@@ -1263,7 +1266,7 @@ def run_uneven(args, rank, world, local_rank):
                                   "[200, 8000] x translations log-uniform [9, 81] per particle",
                       "particles_per_step": nP, "rotations_total": R, "translations_total": T,
                       "plan_waves": waves, "wave_budget_bytes": budget,
-                      "cross_term_k_block": kblock,
+                      "cross_term_k_block": kblock, "projection_group": pgroup,
                       "plan_create_s": round(plan_s, 2)},
            "hypotheses_per_s": round(job_rate(hyps, ms, world), 1),
            "samples_per_s": round(job_rate(samples, ms, world), 1),
@@ -2378,6 +2381,8 @@ def main():
     ap.add_argument("--bank-shape", type=int, default=0, choices=[0, 1, 2],
                     help="TG3_OPT_BANK_SHAPE: the cp.async bank cross term's K block and "
                          "CTAs per SM (0: 64, one; 1: 32, twice the stages; 2: 32, two)")
+    ap.add_argument("--project-group", type=int, default=8, choices=[4, 8, 16],
+                    help="TG3_OPT_PROJECT_GROUP: rotations per projection CTA (forms 3, 4)")
     ap.add_argument("--project-form", type=int, default=4, choices=[0, 1, 2, 3, 4],
                     help="TG3_OPT_PROJECT_FORM: 0 a lane pair per pixel, 1 one lane per pixel, "
                          "2 one lane per pixel with the block index computed, 3/4 lane pairs "

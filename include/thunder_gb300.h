@@ -361,7 +361,10 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  *   cp.async form (TG3_OPT_BANK_GATHER 0): 0 K blocks of 64 bf16 (128-byte
  *   rows) and one CTA an SM, 1 K blocks of 32 (64-byte rows) with twice the
  *   stages, 2 K blocks of 32 with two CTAs an SM.  Same products in the
- *   same order. */
+ *   same order.
+ * TG3_OPT_PROJECT_GROUP (default 8): the rotations one CTA of projection
+ *   forms 3 and 4 takes for its 512-pixel chunk (4, 8 or 16).  Same
+ *   samples. */
 enum {
     TG3_OPT_FUSED = 0,
     TG3_OPT_INSERT_GATHER = 1,
@@ -372,7 +375,8 @@ enum {
     TG3_OPT_SCAN_BK = 6,
     TG3_OPT_LOCAL_BK = 7,
     TG3_OPT_PROJECT_FORM = 8,
-    TG3_OPT_BANK_SHAPE = 9
+    TG3_OPT_BANK_SHAPE = 9,
+    TG3_OPT_PROJECT_GROUP = 10
 };
 int tg3_ctx_set_option(tg3_ctx* ctx, int option, int value);
 int tg3_ctx_stage_times(tg3_ctx* ctx, double* ms, int* launches, int reset);
@@ -409,6 +413,10 @@ int tg3_ragged_plan_info(const tg3_plan* plan, int* waves, size_t* budget);
  * as the autotuner chose it for this batch, or the context's when the plan
  * was given a budget). */
 int tg3_ragged_plan_kblock(const tg3_plan* plan, int* bk);
+/* The projection's rotations per CTA in the plan (4, 8 or 16:
+ * TG3_OPT_PROJECT_GROUP as the autotuner chose it, or the context's when the
+ * plan was given a budget). */
+int tg3_ragged_plan_project_group(const tg3_plan* plan, int* group);
 int tg3_ragged_plan_destroy(tg3_plan* plan);
 
 /* Pose-proposal network (no counterpart in the reference: a learned seed for

@@ -135,6 +135,28 @@ def test_project_forms(small, ctx):
     np.testing.assert_array_equal(res[3], res[4])
 
 
+@pytest.mark.parametrize("group", [4, 16])
+def test_project_groups(small, ctx, group):
+    """Projection form 4 with 4 or 16 rotations a CTA (TG3_OPT_PROJECT_GROUP)
+    against the default 8: the same samples, bit for bit, 37 rotations
+    leaving partial groups."""
+    rng = small["rng"]
+    q = synth.haar_quaternions(rng, 37)
+    mat = O.rotmat(q).reshape(-1, 9)
+    K = len(small["iCol"])
+    res = {}
+    try:
+        for gr in (8, group):
+            ctx.set_option(tg3.OPT_PROJECT_GROUP, gr)
+            out = torch.empty((37, K, 2), dtype=torch.float32, device=DEV)
+            ctx.project(0, dev(mat), 37, out)
+            ctx.sync()
+            res[gr] = out.cpu().numpy()
+    finally:
+        ctx.set_option(tg3.OPT_PROJECT_GROUP, 8)
+    np.testing.assert_array_equal(res[8], res[group])
+
+
 def test_local_phase_project_forms(small, ctx):
     """The split-bf16 local phase with either projection form: likelihoods
     within 1e-6 relative of each other (the bf16 split of equal samples is

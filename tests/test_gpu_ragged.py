@@ -116,10 +116,10 @@ def test_ragged_plan_equals_particles_alone(setup, precision):
 
 
 def test_autotuned_plan_matches_a_fixed_plan(setup):
-    """A plan whose budget and cross-term K block the autotuner chose
-    (tg3_ragged_plan_kblock reports the block) gives the same outputs as a
-    plan with a fixed budget: waves and K blocks change the launches, not the
-    arithmetic."""
+    """A plan whose budget, cross-term K block and projection rotations per CTA
+    the autotuner chose (tg3_ragged_plan_kblock and _project_group report
+    them) gives the same outputs as a plan with a fixed budget: waves, K blocks
+    and projection tiles change the launches, not the arithmetic."""
     ctx, cls, nR, nT, d = setup["ctx"], setup["cls"], setup["nR"], setup["nT"], setup["dev"]
     nP = len(cls)
     res = []
@@ -128,6 +128,7 @@ def test_autotuned_plan_matches_a_fixed_plan(setup):
         plan = tg3.RaggedPlan(ctx, cls, nR, nT, d, out, tg3.SCORE_BF16X3, budget=budget,
                               graph=True)
         assert plan.kblock() in (32, 64)
+        assert plan.project_group() in (4, 8, 16)
         plan.run()
         ctx.sync()
         res.append({k: v.cpu().numpy() for k, v in out.items()})

@@ -596,7 +596,7 @@ static int local_phase(tg3_ctx* c, const int* bankIdx, int nP, int nR, int nT, c
         StageTimer tm(c, TG3_STAGE_PROJECT);
         TG3_CUDA(launch_project(c->d_volTable, cls, nullptr, v0.vdim, v0.pf, quat, nullptr,
                                 nP * nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, sigRcp, ctf, nrm,
-                                pscr, c->d_flag, splitP, s, c->projForm));
+                                pscr, c->d_flag, splitP, s, c->projForm, c->projGroup));
     }
     {
         StageTimer tm(c, TG3_STAGE_SHIFT);
@@ -704,7 +704,7 @@ static int local_phase_ctf(tg3_ctx* c, int nP, int nR, int nT, int nD, const flo
         StageTimer tm(c, TG3_STAGE_PROJECT);
         TG3_CUDA(launch_project(c->d_volTable, cls, nullptr, v0.vdim, v0.pf, quat, nullptr,
                                 nP * nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, nullptr, nullptr,
-                                nullptr, pscr, c->d_flag, splitP, s, c->projForm));
+                                nullptr, pscr, c->d_flag, splitP, s, c->projForm, c->projGroup));
         TG3_CUDA(launch_norm_defocus(P, splitP, nP, nR, nD, K, Kp, sigRcp, ctfD, nrm, s));
     }
     {
@@ -824,7 +824,7 @@ extern "C" int tg3_ctx_set_bank(tg3_ctx* c, int cls, const double* quat, int nB)
     if (!pscr) return st;
     TG3_CUDA(launch_project(nullptr, nullptr, v.blocks, v.vdim, v.pf, quat, nullptr, nB, nB,
                             c->px.iCol, c->px.iRow, K, b.f32, Kp, nullptr, nullptr, nullptr, pscr,
-                            c->d_flag, 0, c->stream, c->projForm));
+                            c->d_flag, 0, c->stream, c->projForm, c->projGroup));
     TG3_CUDA(launch_bank_planes(b.f32, nB, K, Kp, b.hi, b.hi + rowF, b.abs2, c->stream));
     TG3_CUDA(cudaMemcpyAsync(b.quat, quat, (size_t)nB * 4 * sizeof(double),
                              cudaMemcpyDeviceToDevice, c->stream));
@@ -1067,7 +1067,7 @@ extern "C" int tg3_project_d(tg3_ctx* c, int cls, const double* rotMat, int nR, 
     if (!pscr) return st;
     TG3_CUDA(launch_project(nullptr, nullptr, v.blocks, v.vdim, v.pf, nullptr, rotMat, nR, nR,
                             c->px.iCol, c->px.iRow, c->px.K, out, 2 * c->px.K, nullptr, nullptr,
-                            nullptr, pscr, c->d_flag, 0, c->stream, c->projForm));
+                            nullptr, pscr, c->d_flag, 0, c->stream, c->projForm, c->projGroup));
     return TG3_OK;
 }
 
@@ -1821,6 +1821,11 @@ extern "C" int tg3_ctx_set_option(tg3_ctx* c, int option, int value)
         if (value < 0 || value > 2) return fail(TG3_ERR_ARG, "TG3_OPT_BANK_SHAPE takes 0, 1 or 2");
         c->bankShape = value;
     }
+    else if (option == TG3_OPT_PROJECT_GROUP) {
+        if (value != 4 && value != 8 && value != 16)
+            return fail(TG3_ERR_ARG, "TG3_OPT_PROJECT_GROUP takes 4, 8 or 16");
+        c->projGroup = value;
+    }
     else if (option == TG3_OPT_PROJECT_FORM) {
         if (value < 0 || value > 4) return fail(TG3_ERR_ARG, "TG3_OPT_PROJECT_FORM takes 0 to 4");
         c->projForm = value;
@@ -2037,7 +2042,7 @@ static int global_scan(tg3_ctx* c, const Volume* v, const float2* img2, int vdim
         } else {
             TG3_CUDA(launch_project(nullptr, nullptr, v->blocks, v->vdim, v->pf, nullptr, rotMat,
                                     nR, nR, c->px.iCol, c->px.iRow, K, P, Kp, nullptr, nullptr,
-                                    nullptr, pscr, c->d_flag, splitP, s, c->projForm));
+                                    nullptr, pscr, c->d_flag, splitP, s, c->projForm, c->projGroup));
         }
         // |P|^2 rows: FP32 for the FP32 search, split bf16 planes (the same
         // bytes) for the split search's tensor-core norm term

@@ -203,6 +203,7 @@ struct tg3_ctx {
     int scanBK = 32;              // TG3_OPT_SCAN_BK
     int localBK = 64;             // TG3_OPT_LOCAL_BK
     int projForm = 4;             // TG3_OPT_PROJECT_FORM
+    int projGroup = 8;            // TG3_OPT_PROJECT_GROUP
     int bankShape = 0;            // TG3_OPT_BANK_SHAPE
     // per-stage event timing (tg3_ctx_set_timing)
     bool timing = false;
@@ -275,12 +276,14 @@ cudaError_t launch_project(float4* const* volTable, const int* cls,
                            int rowsPerParticle, const int* iCol,
                            const int* iRow, int K, float* out, int ldo,
                            const float* sigRcp, const float* ctf, float* nrm, float* scratch,
-                           int* flag, long long splitLo, cudaStream_t st, int form = 4);
+                           int* flag, long long splitLo, cudaStream_t st, int form = 4,
+                           int group = 8);
 // form: 0 a lane pair per pixel (k_project), 1 one lane per pixel
 // (k_project_lane, block index from shared tables), 2 one lane per pixel
 // with the block index from integer arithmetic, 3 and 4 lane pairs sharing
 // loads of whole blocks with the coordinates found once per pixel
-// (k_project_xchg; tables, arithmetic); the same samples.
+// (k_project_xchg; tables, arithmetic); the same samples.  group: the
+// rotations a CTA of forms 3 and 4 takes for its pixel chunk (4, 8 or 16).
 // Either trans [nP][nT][2] or a shared phase bank [nT][K] complex.
 // splitLo != 0: write bf16 hi/lo planes (lo plane splitLo elements after
 // the hi plane at `out`) instead of floats; the same for launch_project.

@@ -549,7 +549,7 @@ k_project_lane(float4* const* __restrict__ volTable, const int* __restrict__ cls
 // the pair form's sum).  (Recomputing the partner's fractions from its
 // coordinates instead of receiving them by three shuffles measured slower:
 // 8.99 against 8.56 ms per 128 particles at box 256.)
-template <bool kArith>
+template <bool kArith, int G>
 __global__ void __launch_bounds__(256, 4)
 k_project_xchg(float4* const* __restrict__ volTable, const int* __restrict__ cls,
                const float4* __restrict__ vol0, int vdim, int pf, const float* __restrict__ mf,
@@ -558,13 +558,13 @@ k_project_xchg(float4* const* __restrict__ volTable, const int* __restrict__ cls
                const float* __restrict__ sigRcp, const float* __restrict__ ctf,
                float* __restrict__ nrmPart, int* __restrict__ flag, long long splitLo)
 {
-    __shared__ float m[kProjG][9];
-    __shared__ float red[kProjG][8];
+    __shared__ float m[G][9];
+    __shared__ float red[G][8];
     const int g = blockIdx.x % nGroups;
     const int chunk = (blockIdx.x / nGroups) % nChunks;
     const int l = blockIdx.x / (nGroups * nChunks);
-    const int r0 = g * kProjG;
-    const int nRot = min(kProjG, rowsPerParticle - r0);
+    const int r0 = g * G;
+    const int nRot = min(G, rowsPerParticle - r0);
     const size_t row0 = (size_t)l * rowsPerParticle + r0;
     extern __shared__ int tab[];
     const int half = vdim / 2;
@@ -2121,13 +2121,16 @@ cudaError_t launch_project(float4* const* volTable, const int* cls, const float4
                            int rows, int rowsPerParticle, const int* iCol,
                            const int* iRow, int K, float* out, int ldo,
                            const float* sigRcp, const float* ctf, float* nrm, float* scratch,
-                           int* flag, long long splitLo, cudaStream_t st, int form)
+                           int* flag, long long splitLo, cudaStream_t st, int form, int group)
 {
     if (rows <= 0) return cudaSuccess;
     if (!scratch || rows % rowsPerParticle) return cudaErrorInvalidValue;
     static_assert(kProjChunk % 256 == 0, "one lane per pixel takes whole 256-pixel passes");
     const int nP = rows / rowsPerParticle;
-    const int nGroups = (rowsPerParticle + kProjG - 1) / kProjG;
+    if (group != 4 && group != 8 && group != 16) return cudaErrorInvalidValue;
+    // the rotation group of a CTA: kProjG for forms 0 - 2, `group` for 3 and 4
+    const int G = form >= 3 ? group : kProjG;
+    const int nGroups = (rowsPerParticle + G - 1) / G;
     const int nChunks = project_chunks(ldo);
     const long long grid = (long long)nP * nChunks * nGroups;
     if (grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
@@ -2137,8 +2140,10 @@ cudaError_t launch_project(float4* const* volTable, const int* cls, const float4
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const size_t tabBytes = sizeof(int) * ((size_t)vdim / 2 + 1 + 2 * (size_t)vdim);
-    auto kern = form == 4   ? k_project_xchg<true>
-                : form == 3 ? k_project_xchg<false>
+    auto kern = form == 4   ? (G == 4 ? k_project_xchg<true, 4> : G == 16 ? k_project_xchg<true, 16>
+                                                                   : k_project_xchg<true, 8>)
+                : form == 3 ? (G == 4 ? k_project_xchg<false, 4> : G == 16 ? k_project_xchg<false, 16>
+                                                                    : k_project_xchg<false, 8>)
                 : form == 2 ? k_project_lane<true>
                 : form == 1 ? k_project_lane<false>
                             : k_project;

@@ -17,8 +17,9 @@
 //     phase scores them (tg3_local_phase_d), the resampler draws per-particle
 //     counts, k_ragged_scatter writes the particles' own entries back;
 //   - the whole sequence is captured once in a CUDA graph and replayed.
-// The wave budget is chosen per plan by an autotuner that times candidate
-// budgets on the plan's own batch.
+// The wave budget, the split cross term's K block and the projection's
+// rotations per CTA are chosen per plan by an autotuner that times the
+// candidates on the plan's own batch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -179,6 +180,7 @@ struct tg3_plan {
     int nP = 0, precision = 0;
     size_t budget = 0;
     int bk = 64;                 // the local phase's K block (TG3_OPT_LOCAL_BK) for this plan
+    int pg = 8;                  // the projection's rotations per CTA (TG3_OPT_PROJECT_GROUP)
     RaggedIn in;
     RaggedOut out;
     std::vector<int> clsH, nRH, nTH;
@@ -302,13 +304,16 @@ int plan_waves(tg3_plan* p, size_t budget)
 // The launches of every wave, in order, on the context stream.
 int plan_issue_waves(tg3_plan* p);
 
-// The plan's waves with its K block set on the context for their duration.
+// The plan's waves with its K block and projection group set on the context
+// for their duration.
 int plan_issue(tg3_plan* p)
 {
-    const int saved = p->c->localBK;
+    const int saved = p->c->localBK, savedG = p->c->projGroup;
     p->c->localBK = p->bk;
+    p->c->projGroup = p->pg;
     const int st = plan_issue_waves(p);
     p->c->localBK = saved;
+    p->c->projGroup = savedG;
     return st;
 }
 
@@ -424,6 +429,7 @@ extern "C" int tg3_ragged_plan_create(
     const bool timing = c->timing;
     c->timing = false;
     p->bk = c->localBK;
+    p->pg = c->projGroup;
     if (budget == 0) {
         // autotune: time every candidate (wave budget, and for the split
         // precision the cross term's K block: 128-byte stages of 64 bf16 or
@@ -452,6 +458,28 @@ extern "C" int tg3_ragged_plan_create(
             }
         budget = bestB;
         p->bk = bestK;
+        // then the projection's tile: rotations per CTA for each pixel chunk
+        // (the other two of 4, 8, 16), at the chosen budget and K block
+        if ((st = plan_waves(p, budget))) {
+            c->timing = timing;
+            return fail_free(st);
+        }
+        const int pg0 = p->pg;
+        int bestG = pg0;
+        for (int g : {4, 8, 16}) {
+            if (g == pg0) continue;
+            float ms = 0;
+            p->pg = g;
+            if ((st = plan_time(p, &ms)) || (st = plan_time(p, &ms))) {
+                c->timing = timing;
+                return fail_free(st);
+            }
+            if (ms < best) {
+                best = ms;
+                bestG = g;
+            }
+        }
+        p->pg = bestG;
     }
     float warmMs = 0;
     if ((st = plan_waves(p, budget)) || (st = plan_time(p, &warmMs))) {
@@ -501,6 +529,13 @@ extern "C" int tg3_ragged_plan_info(const tg3_plan* p, int* waves, size_t* budge
     if (!p) return fail(TG3_ERR_ARG, "null plan");
     if (waves) *waves = (int)p->waves.size();
     if (budget) *budget = p->budget;
+    return TG3_OK;
+}
+
+extern "C" int tg3_ragged_plan_project_group(const tg3_plan* p, int* group)
+{
+    if (!p || !group) return fail(TG3_ERR_ARG, "null plan or output");
+    *group = p->pg;
     return TG3_OK;
 }
 

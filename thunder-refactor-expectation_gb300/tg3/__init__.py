@@ -31,7 +31,7 @@ EXPORTS = [
     "tg3_project_d", "tg3_ctx_render_references_d", "tg3_local_phase", "tg3_ctx_set_timing", "tg3_ctx_stage_times",
     "tg3_ctx_set_option", "tg3_ctx_set_pixels_slot", "tg3_ctx_use_pixels",
     "tg3_ragged_plan_create", "tg3_ragged_plan_run", "tg3_ragged_plan_info",
-    "tg3_ragged_plan_kblock", "tg3_Reconstruct2D", "tg3_SymmetrizeO",
+    "tg3_ragged_plan_kblock", "tg3_ragged_plan_project_group", "tg3_Reconstruct2D", "tg3_SymmetrizeO",
     "tg3_ragged_plan_destroy", "tg3_cnn_create", "tg3_cnn_destroy", "tg3_cnn_param_count",
     "tg3_cnn_params", "tg3_cnn_grads", "tg3_cnn_set_bf16", "tg3_cnn_forward", "tg3_cnn_loss",
     "tg3_cnn_zero_grads", "tg3_cnn_adam", "tg3_cnn_propose", "tg3_cnn_backward", "tg3_cnn_infer",
@@ -58,6 +58,7 @@ OPT_SCAN_BK = 6
 OPT_LOCAL_BK = 7
 OPT_PROJECT_FORM = 8
 OPT_BANK_SHAPE = 9
+OPT_PROJECT_GROUP = 10
 
 
 class TG3Error(RuntimeError):
@@ -139,6 +140,7 @@ def lib():
             "tg3_ragged_plan_run": ([_P], _I),
             "tg3_ragged_plan_info": ([_P, _P, _P], _I),
             "tg3_ragged_plan_kblock": ([_P, _P], _I),
+            "tg3_ragged_plan_project_group": ([_P, _P], _I),
             "tg3_Reconstruct2D": ([_P, _P, _I, _I, _P, _I, _I, _I, _I, _I, ctypes.c_float,
                                    ctypes.c_float, _P, _P], _I),
             "tg3_SymmetrizeO": ([_P, _P, _P, _I], _I),
@@ -536,6 +538,12 @@ class RaggedPlan:
         k = ctypes.c_int()
         check(lib().tg3_ragged_plan_kblock(self.h, ctypes.byref(k)))
         return k.value
+
+    def project_group(self) -> int:
+        """The projection's rotations per CTA in the plan (4, 8 or 16)."""
+        g = ctypes.c_int()
+        check(lib().tg3_ragged_plan_project_group(self.h, ctypes.byref(g)))
+        return g.value
 
     def close(self):
         if self.h:
