@@ -2378,9 +2378,10 @@ def main():
                          "share each column tile by TMA multicast")
     ap.add_argument("--local-bk", type=int, default=64, choices=[32, 64],
                     help="TG3_OPT_LOCAL_BK: K block of the local phase's split cross term")
-    ap.add_argument("--bank-shape", type=int, default=0, choices=[0, 1, 2],
+    ap.add_argument("--bank-shape", type=int, default=3, choices=[0, 1, 2, 3],
                     help="TG3_OPT_BANK_SHAPE: the cp.async bank cross term's K block and "
-                         "CTAs per SM (0: 64, one; 1: 32, twice the stages; 2: 32, two)")
+                         "CTAs per SM (0: 64, one; 1: 32, twice the stages; 2: 32, two; "
+                         "3: as 0 with 16 gather warps)")
     ap.add_argument("--project-group", type=int, default=8, choices=[4, 8, 16],
                     help="TG3_OPT_PROJECT_GROUP: rotations per projection CTA (forms 3, 4)")
     ap.add_argument("--project-form", type=int, default=4, choices=[0, 1, 2, 3, 4],

@@ -357,11 +357,11 @@ int tg3_ctx_set_timing(tg3_ctx* ctx, int enable);
  *   pixel and the block index computed instead of looked up, 3 and 4 with
  *   every lane finding its own pixel's block and a lane pair loading both
  *   pixels' blocks together (index looked up, computed).  Same samples.
- * TG3_OPT_BANK_SHAPE (default 0): the pipeline of the bank-row cross term's
+ * TG3_OPT_BANK_SHAPE (default 3): the pipeline of the bank-row cross term's
  *   cp.async form (TG3_OPT_BANK_GATHER 0): 0 K blocks of 64 bf16 (128-byte
  *   rows) and one CTA an SM, 1 K blocks of 32 (64-byte rows) with twice the
- *   stages, 2 K blocks of 32 with two CTAs an SM.  Same products in the
- *   same order.
+ *   stages, 2 K blocks of 32 with two CTAs an SM, 3 as 0 with 16 gather
+ *   warps instead of 8.  Same products in the same order.
  * TG3_OPT_PROJECT_GROUP (default 8): the rotations one CTA of projection
  *   forms 3 and 4 takes for its 512-pixel chunk (4, 8 or 16).  Same
  *   samples. */

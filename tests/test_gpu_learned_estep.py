@@ -270,14 +270,15 @@ def test_reference_rendering_matches_the_torch_form():
         ctx.close()
 
 
-@pytest.mark.parametrize("shape", [1, 2])
+@pytest.mark.parametrize("shape", [0, 1, 2])
 @pytest.mark.parametrize("nR", [32, 160])
 def test_bank_pipeline_shapes(case, nR, shape):
-    """The cp.async bank-row cross term with K blocks of 32 bf16 (64-byte
-    swizzled rows): twice the stages (TG3_OPT_BANK_SHAPE 1) or two CTAs an SM
-    (2), against the default K blocks of 64: the same MMAs in the same order
-    and the norms summed over other lane partitions, so log-likelihoods
-    within 1e-6 relative and the same best hypothesis."""
+    """The cp.async bank-row cross term's pipeline shapes (TG3_OPT_BANK_SHAPE:
+    0 eight gather warps, 1 K blocks of 32 bf16 with twice the stages, 2 K
+    blocks of 32 with two CTAs an SM) against the default (3: K blocks of 64,
+    sixteen gather warps): the same MMAs in the same order and the norms
+    summed over other lane partitions, so log-likelihoods within 1e-6
+    relative and the same best hypothesis."""
     ps, ctx, n = case["ps"], case["ctx"], len(case["ps"].cls)
     nT = 9
     rng = np.random.default_rng(nR + 7)
@@ -297,9 +298,9 @@ def test_bank_pipeline_shapes(case, nR, shape):
         return dvp.cpu().numpy().astype(np.float64)
 
     try:
-        a, b = run(shape), run(0)
+        a, b = run(shape), run(3)
     finally:
-        ctx.set_option(tg3.OPT_BANK_SHAPE, 0)
+        ctx.set_option(tg3.OPT_BANK_SHAPE, 3)
     assert np.max(np.abs(a - b) / np.abs(b)) < 1e-6
     for l in range(n):
         assert np.argmax(a[l]) == np.argmax(b[l])

@@ -1818,7 +1818,7 @@ extern "C" int tg3_ctx_set_option(tg3_ctx* c, int option, int value)
         c->localBK = value;
     }
     else if (option == TG3_OPT_BANK_SHAPE) {
-        if (value < 0 || value > 2) return fail(TG3_ERR_ARG, "TG3_OPT_BANK_SHAPE takes 0, 1 or 2");
+        if (value < 0 || value > 3) return fail(TG3_ERR_ARG, "TG3_OPT_BANK_SHAPE takes 0 to 3");
         c->bankShape = value;
     }
     else if (option == TG3_OPT_PROJECT_GROUP) {

@@ -336,15 +336,15 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src)
                  : "memory");
 }
 
-// Eight gather warps (0 - 7), then the B-tile TMA warp (8) and the MMA warp
-// (9, which also holds the tensor memory); warps 0 - 3 run the epilogue.
+// CP_PW gather warps (eight by default, 0 - 7), then the B-tile TMA warp
+// (CP_PW) and the MMA warp (CP_PW + 1, which also holds the tensor memory);
+// warps 0 - 3 run the epilogue.
 //
 // BK is the K block: 64 bf16 (128-byte rows, 128-byte swizzle) or 32
 // (64-byte rows, 64-byte swizzle: half the bytes a stage, so more stages, or
 // two CTAs an SM with MINB = 2).  A row's chunk of a K block is BK / 8
 // 16-byte pieces, one per lane of a row group; a thread copies CP_RPT rows.
-constexpr int CP_PW = 8;
-constexpr int CP_THREADS = (CP_PW + 2) * 32;
+constexpr int cp_threads(int pw) { return (pw + 2) * 32; }
 
 template <int BK>
 __device__ __forceinline__ uint64_t bank_desc(uint32_t saddr)
@@ -362,8 +362,8 @@ __device__ __forceinline__ int bank_phys(int r, int q)
                     : (r >> 3) * 512 + (r & 7) * 64 + ((q ^ ((r >> 1) & 3)) << 4);
 }
 
-template <int S, int BK, int MINB>
-__global__ void __launch_bounds__(CP_THREADS, MINB)
+template <int S, int BK, int MINB, int CP_PW = 8>
+__global__ void __launch_bounds__(cp_threads(CP_PW), MINB)
 k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                const __grid_constant__ CUtensorMap tmBl, const BgParams p)
 {
@@ -672,7 +672,7 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
                                     float* C, float alpha, int* flag, cudaStream_t st,
                                     bool tmaGather, int* order, int shape)
 {
-    if (shape < 0 || shape > 2) return cudaErrorInvalidValue;
+    if (shape < 0 || shape > 3) return cudaErrorInvalidValue;
     if (nP <= 0 || nR <= 0 || nT <= 0 || nT > 256 || Kd <= 0 || Kd % BG_BK || nP > 65535)
         return cudaErrorInvalidValue;
     BankMaps maps;
@@ -758,12 +758,12 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
     // CTA's (shape 0: K blocks of 64, <= 5 stages; shape 1: of 32, <= 9) or
     // in half an SM's shared memory (shape 2: K blocks of 32, two CTAs an SM)
     using KernFn = void (*)(const LdgRows, const CUtensorMap, const CUtensorMap, const BgParams);
-    const int bk = shape == 0 ? 64 : 32;
+    const int bk = shape == 0 || shape == 3 ? 64 : 32;
     const int stageCp = 2 * BG_M * bk * 2 + 2 * p.ntile * bk * 2;
     const size_t fixed = 1024 + 256 + 2 * sizeof(int) * BG_M;
     const size_t budget = shape == 2 ? 113 * 1024 : 227 * 1024;
     int S = (int)((budget - fixed) / stageCp);
-    const int maxS = shape == 0 ? 5 : shape == 1 ? 9 : 4;
+    const int maxS = shape == 0 || shape == 3 ? 5 : shape == 1 ? 9 : 4;
     if (S > maxS) S = maxS;
     if (S < 2 || (size_t)BG_M * (p.ntile + 1) * 4 > (size_t)S * stageCp)
         return cudaErrorInvalidValue;
@@ -771,6 +771,9 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
     if (shape == 0)
         kern = S == 5 ? k_gemm_bank_cp<5, 64, 1> : S == 4 ? k_gemm_bank_cp<4, 64, 1>
              : S == 3 ? k_gemm_bank_cp<3, 64, 1> : k_gemm_bank_cp<2, 64, 1>;
+    else if (shape == 3)
+        kern = S == 5 ? k_gemm_bank_cp<5, 64, 1, 16> : S == 4 ? k_gemm_bank_cp<4, 64, 1, 16>
+             : S == 3 ? k_gemm_bank_cp<3, 64, 1, 16> : k_gemm_bank_cp<2, 64, 1, 16>;
     else if (shape == 1) {
         S = S >= 9 ? 9 : S >= 8 ? 8 : S >= 6 ? 6 : S >= 4 ? 4 : 2;   // the instantiated depths
         kern = S == 9 ? k_gemm_bank_cp<9, 32, 1> : S == 8 ? k_gemm_bank_cp<8, 32, 1>
@@ -788,7 +791,7 @@ cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const in
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smemCp);
     if (e != cudaSuccess) return e;
-    kern<<<grid, CP_THREADS, smemCp, st>>>(rowsOf, cBh, cBl, p);
+    kern<<<grid, cp_threads(shape == 3 ? 16 : 8), smemCp, st>>>(rowsOf, cBh, cBl, p);
     return cudaGetLastError();
 }
 

@@ -204,7 +204,7 @@ struct tg3_ctx {
     int localBK = 64;             // TG3_OPT_LOCAL_BK
     int projForm = 4;             // TG3_OPT_PROJECT_FORM
     int projGroup = 8;            // TG3_OPT_PROJECT_GROUP
-    int bankShape = 0;            // TG3_OPT_BANK_SHAPE
+    int bankShape = 3;            // TG3_OPT_BANK_SHAPE
     // per-stage event timing (tg3_ctx_set_timing)
     bool timing = false;
     // inside the learned E-step's fallback: its cross-term launches are
@@ -483,12 +483,13 @@ bool bf16x3_available();
 // the shifted data B (hi plane [nP nT][Kd], then the lo plane), plus the
 // rows' norms sum_p sigRcp ctf^2 |P|^2 (compensated FP32).  shape (the
 // cp.async form): 0 K blocks of 64 bf16, one CTA an SM; 1 K blocks of 32,
-// twice the stages; 2 K blocks of 32, two CTAs an SM.
+// twice the stages; 2 K blocks of 32, two CTAs an SM; 3 as 0 with 16
+// gather warps instead of 8.
 cudaError_t launch_gemm_bank_bf16x3(const Bank* banks, unsigned pixGen, const int* idx,
                                     const int* cls, int nP, int nR, const void* B, int nT,
                                     int Kd, int K, const float* sigRcp, const float* ctf,
                                     float* C, float alpha, int* flag, cudaStream_t st,
-                                    bool tmaGather = false, int* order = nullptr, int shape = 0);
+                                    bool tmaGather = false, int* order = nullptr, int shape = 3);
 cudaError_t launch_gemm_nt_bf16x3(const float* A, long long sA, int lda,
                                   const float* B, long long sB, int ldb,
                                   int M, int N, int Kd, int batch, float* C,
