@@ -317,13 +317,13 @@ k_gemm_bank_bf16x3(const __grid_constant__ BankMaps maps, const __grid_constant_
 // copies of LAG + 1 blocks are in flight, and the MMAs of a block have two
 // blocks' time to finish before the producers need its stage again (with a
 // lag of S - 1 the producers stalled every block on the MMA round trip).
-// Once the thread's own copies of a K block have landed it adds their
+// Once the thread's own copies of a K block have landed it makes them
+// visible to the tensor cores (proxy fence), arrives, and then adds their
 // |P|^2, weighted by sigRcp ctf^2, to its partial norms (a plain FP32 sum
 // of each row's four pixels, added to the running sum in compensated FP32;
-// the 8 lanes' partials are summed at the end), makes them visible to the
-// tensor cores (proxy fence) and arrives.  A stage is full when the four
-// warps have arrived and the B tiles' bytes have landed (TMA, warp 4 lane
-// 0); it is free when the MMAs that read it have completed.
+// the lanes' partials are summed at the end).  A stage is full when the
+// gather warps have arrived and the B tiles' bytes have landed (TMA); it is
+// free when the MMAs that read it have completed.
 struct LdgRows {
     const __nv_bfloat16* hi[kMaxClasses];
     const __nv_bfloat16* lo[kMaxClasses];
@@ -492,6 +492,12 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
             if (kd < 0) continue;
             if (kd + 1 < nkb) weights(kd + 1, wNext);
             asm volatile("cp.async.wait_group %0;" ::"n"(LAG) : "memory");
+            // the copies (generic proxy) visible to the tensor cores' reads;
+            // the stage is handed over before this thread's norm reads of it
+            // (reads both, and only this thread rewrites its chunks, S blocks on)
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(full + kd % S);
             const uint8_t* st = smem + (kd % S) * stageBytes;
 #pragma unroll
             for (int i = 0; i < CP_RPT; i++) {
@@ -510,10 +516,6 @@ k_gemm_bank_cp(const LdgRows banks, const __grid_constant__ CUtensorMap tmBh,
                 }
                 kahan_add(nS[i], nC[i], part);
             }
-            // the copies (generic proxy) visible to the tensor cores' reads
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(full + kd % S);
 #pragma unroll
             for (int c = 0; c < 4; c++) wCur[c] = wNext[c];
         }
