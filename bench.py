@@ -1677,9 +1677,9 @@ def run_learned(args, rank, world, local_rank):
     h2d = sum(int(v.numel() * v.element_size()) for v in hin.values())
     d2h = sum(int(v.numel() * v.element_size()) for v in hout.values())
 
-    # ---- 9. the benchmark spec's own fallback rule, measured beside the
-    # threshold: the global search on every particle, its pose taken where
-    # its best likelihood beats the proposal's
+    # ---- 9. the fallback by likelihood, measured beside the threshold: the
+    # global search on every particle, its pose taken where its best
+    # likelihood beats the proposal's
     o_all = outputs(n, full=False)
     expect(unseen, float("inf"), o_all)          # every particle through the global search
     torch.cuda.synchronize()
@@ -1787,7 +1787,7 @@ def run_learned(args, rank, world, local_rank):
                                  "learned_e_step": med(err(q_l)),
                                  "plain_fp32_refined": med(err(q_p_r)),
                                  "learned_refined": med(err(q_l_r)),
-                                 "north_star_rule_refined": med(err(q_B_r)),
+                                 "global_wins_rule_refined": med(err(q_B_r)),
                                  "plain_method_converged": med(err(judge_un))},
             "refined_gap_deg": round(float(np.median(err(q_l_r)) - np.median(err(q_p_r))), 3),
             "within_5deg_of_plain_converged": round(float(np.mean(
@@ -1803,7 +1803,7 @@ def run_learned(args, rank, world, local_rank):
                     "particles of the training maps whose proposal is within 10 degrees of "
                     "the plain method's converged pose",
             "threshold": round(tau, 4), "fraction": round(float(fb.mean()), 4),
-            "north_star_rule": {
+            "global_wins_rule": {
                 "rule": "global search on every particle; its pose where its best likelihood "
                         "beats the proposal's",
                 "fraction": round(float(ruleB.mean()), 4),
