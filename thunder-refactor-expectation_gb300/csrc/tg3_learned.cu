@@ -490,11 +490,18 @@ extern "C" int tg3_ExpectLearned3D(tg3_ctx* c, tg3_cnn* net, int nP, const float
     // the copy stream does not overwrite the arena before the compute
     // stream's earlier work on it is done
     TG3_CUDA(cudaEventRecord(c->copyDone, s));
-    TG3_CUDA(cudaStreamWaitEvent(c->copyStream, c->copyDone, 0));
-    TG3_CUDA(h2d(oD, dat, sizeof(float) * 2 * (size_t)nP * K, c->copyStream));
-    TG3_CUDA(h2d(oC, ctf, sizeof(float) * (size_t)nP * K, c->copyStream));
-    TG3_CUDA(h2d(oS, sigRcp, sizeof(float) * (size_t)nP * K, c->copyStream));
-    TG3_CUDA(cudaEventRecord(c->copyDone, c->copyStream));
+    {
+        // a failure part-way leaves no copy still landing in the arena
+        cudaError_t e = cudaStreamWaitEvent(c->copyStream, c->copyDone, 0);
+        if (e == cudaSuccess) e = h2d(oD, dat, sizeof(float) * 2 * (size_t)nP * K, c->copyStream);
+        if (e == cudaSuccess) e = h2d(oC, ctf, sizeof(float) * (size_t)nP * K, c->copyStream);
+        if (e == cudaSuccess) e = h2d(oS, sigRcp, sizeof(float) * (size_t)nP * K, c->copyStream);
+        if (e == cudaSuccess) e = cudaEventRecord(c->copyDone, c->copyStream);
+        if (e != cudaSuccess) {
+            cudaStreamSynchronize(c->copyStream);
+            return cuda_fail(e, "learned E-step input copies");
+        }
+    }
     tg3_learned_out o = {};
     o.bestQuat = (double*)(w + oQ);
     o.bestTrans = (double*)(w + oT);
