@@ -246,9 +246,9 @@ def train_match(net, images, refs, tstar, cls, epochs: int, batch: int, lr: floa
 
 
 # --------------------------------------------------------------------------
-# The plain method's converged poses (training labels and the judge of the
-# proposals): the global search, then local particle-filter phases that
-# narrow around the current best pose.
+# The plain method's converged poses (the training labels, and the poses the
+# proposals' errors are measured against): the global search, then local
+# particle-filter phases that narrow around the current best pose.
 # --------------------------------------------------------------------------
 # (concentration of the rotations' vMF, deviation of the translations in
 # pixels) of the local phases after the global search: the particle
