@@ -1501,10 +1501,11 @@ def run_learned(args, rank, world, local_rank):
     map_ms_pp = map_ms / per_map_particles
 
     # ---- 5. the plain method run to convergence on the evaluation particles:
-    # the judge of the proposals (and the poses the calibration trusts)
-    judge_seen, _, _ = learned.plain_method_poses(ctx, seen, quats_g, mats_g, trans_g,
+    # the plain method's converged poses: what the proposals' errors are
+    # measured against (and the poses the calibration trusts)
+    conv_seen, _, _ = learned.plain_method_poses(ctx, seen, quats_g, mats_g, trans_g,
                                                   tg3.SCORE_FP32, gen)
-    judge_un, judge_un_t, _ = learned.plain_method_poses(ctx, unseen, quats_g, mats_g, trans_g,
+    conv_un, conv_un_t, _ = learned.plain_method_poses(ctx, unseen, quats_g, mats_g, trans_g,
                                                          tg3.SCORE_FP32, gen)
 
     def outputs(n, full=True):
@@ -1531,7 +1532,7 @@ def run_learned(args, rank, world, local_rank):
     # method's converged pose pass it
     o_seen = outputs(nSeen, full=False)
     expect(seen, float("-inf"), o_seen)
-    err_seen = learned.angle_deg(o_seen["bestQuat"].cpu().numpy(), judge_seen)
+    err_seen = learned.angle_deg(o_seen["bestQuat"].cpu().numpy(), conv_seen)
     pk_seen = o_seen["peak"].cpu().numpy()
     good = err_seen < 10.0
     tau = float(np.quantile(pk_seen[good], 0.05)) if good.any() else float("inf")
@@ -1788,10 +1789,10 @@ def run_learned(args, rank, world, local_rank):
                                  "plain_fp32_refined": med(err(q_p_r)),
                                  "learned_refined": med(err(q_l_r)),
                                  "global_wins_rule_refined": med(err(q_B_r)),
-                                 "plain_method_converged": med(err(judge_un))},
+                                 "plain_method_converged": med(err(conv_un))},
             "refined_gap_deg": round(float(np.median(err(q_l_r)) - np.median(err(q_p_r))), 3),
             "within_5deg_of_plain_converged": round(float(np.mean(
-                learned.angle_deg(q_l_r, judge_un) < 5.0)), 4),
+                learned.angle_deg(q_l_r, conv_un) < 5.0)), 4),
             "note": "error = angle between the method's best rotation and the true one; "
                     "refined = after one local phase of 1,000 x 100 about the method's pose "
                     "(plain in FP32, learned in its own precision)"},
